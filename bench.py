@@ -1,0 +1,360 @@
+"""Benchmark: MB-pol force + heat-current steps/s at 4096 H2O on one GB300.
+
+One step = one evaluation of the MB-pol 2B + 3B forces with the heat-current
+bookkeeping (dimer/trimer lists rebuilt on the device, forces, energy, virial,
+stress, per-atom energies, jpot and jkin) on the seeded 4096-water box
+(jittered 16^3 lattice, L = 49.70 A, 298 K).
+
+    python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+
+Our arm prints one JSON line: `value` is mixed-precision steps/s with inputs
+resident in HBM (L2 flushed between steps); `fp64` the plain FP64 path; `e2e` the
+same metric through the host-array C ABI (host<->device copies timed); `roofline`
+the dominant kernel (the 3B cluster kernel) against the FP32 pipe; `cpu_baseline`
+the reference algorithm (the oracle's restatement of the Fortran loops) timed on a
+bounded share of the same step on this host's cores.
+
+--impl reference times that CPU implementation alone (all host threads).
+Under torchrun each rank evaluates its own independent box (replicas, weak
+scaling); rank 0 prints.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(REPO, "dlpoly2-mbpol-heat_gb300")
+for _p in (PKG, os.path.join(REPO, "oracle")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "MB-pol steps/s at 4096 H2O, mixed vs FP64 on 1 GB300; served p50/p99 ms"
+WORKLOAD = "MB-pol 2B+3B forces + per-atom energies + heat current (jpot, jkin), 4096 H2O (12288 atoms + 4096 M sites), L=49.70 A"
+DATA = "synthetic: seeded 4096-H2O box, jittered 16^3 lattice, random orientations, 0.02 A noise, 298 K velocities"
+NOT_IN_STEP = ["TTM4-F polarizable electrostatics (induced dipoles, Ewald/SPME)", "DMS charges",
+               "1-body PS PES", "TT dispersion"]
+
+
+def _peaks():
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except OSError:
+        return {}
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([c.strip() for c in line.split(",")])
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        sm = [float(r[1]) for r in self.rows if len(r) > 8 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) > 8 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            if len(r) > 8:
+                for k, n in enumerate(names):
+                    if r[5 + k].lower() == "active":
+                        reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def poly_flops():
+    """Algorithmic flops of the generated polynomial value+gradient (FMA = 2)."""
+    sys.path.insert(0, os.path.join(PKG, "gen"))
+    import gen_poly_ptx as g
+    out = {}
+    for body in ("2b", "3b"):
+        _, _, monos = g.read_table(os.path.join(PKG, "tables", "poly%s.tbl" % body))
+        root = g.build_trie(monos)
+        fl = [0]
+
+        def walk(node, depth):
+            for ch in node.ch.values():
+                if not ch.ch:
+                    fl[0] += 4 if depth > 0 else 3      # two FMAs (root: FMA + add)
+                else:
+                    fl[0] += (1 if depth > 0 else 0) + (4 if depth > 0 else 3)
+                    walk(ch, depth + 1)
+        walk(root, 0)
+        out[body] = fl[0]
+    return out
+
+
+def cpu_reference(box, target_core_s=20.0, threads=None):
+    """The reference algorithm (oracle restatement of mbpol_forces) on a bounded
+    share of one step: ranks [0, T) of a size-S replicated-data split, S chosen so
+    the sample is about `target_core_s` of CPU work.  Returns (steps/s, info)."""
+    import oracle
+    o = oracle.load()
+    T = threads or os.cpu_count() or 1
+    S0 = max(T, 1 << 16)
+    t0 = time.perf_counter()
+    o.ranks(box, 0, T, S0, T)
+    dt0 = time.perf_counter() - t0
+    core_s_full = dt0 * T * (S0 / T)
+    S = int(min(max(T, core_s_full * T / target_core_s), S0))
+    S = max(S, T)
+    t0 = time.perf_counter()
+    o.ranks(box, 0, T, S, T)
+    dt = time.perf_counter() - t0
+    step_s = dt * S / T
+    return 1.0 / step_s, {"cores": T, "sample": "ranks 0..%d of a %d-rank split of mbpol_forces' pair and triple "
+                          "loops (fraction %.5f of one step), %.1f s wall" % (T - 1, S, T / S, dt),
+                          "step_seconds": step_s}
+
+
+def run_ours(args, rank, world):
+    import torch
+    from mbx import capi, systems
+
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    torch.cuda.set_device(dev)
+    box = systems.config1(seed=20241 + rank)
+    n = box.natms
+    ctx = capi.Context(dev.index)
+    stream = torch.cuda.current_stream(dev)
+    ctx.set_stream(stream.cuda_stream)
+
+    f64 = dict(dtype=torch.float64, device=dev)
+    X = [torch.tensor(np.ascontiguousarray(box.xyz[:, k]), **f64) for k in range(3)]
+    V = [torch.tensor(np.ascontiguousarray(box.vel[:, k]), **f64) for k in range(3)]
+    M = torch.tensor(box.mass, **f64)
+    F = torch.zeros((3, n), **f64)
+    AE = torch.zeros(n, **f64)
+    LST = torch.tensor(box.listttm2(), dtype=torch.int32, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)   # > 129 MB L2
+
+    def step(precision):
+        F.zero_()
+        AE.zero_()
+        return ctx.mbpol_forces_device(precision, box.imcon, box.cell, 3 * box.nw, LST.data_ptr(), n,
+                                       [x.data_ptr() for x in X], [F[k].data_ptr() for k in range(3)],
+                                       [v.data_ptr() for v in V], M.data_ptr(), AE.data_ptr())
+
+    def timed(precision, steps, warmup, profile=False):
+        ctx.set_profiling(profile)
+        for _ in range(warmup):
+            step(precision)
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        phase = np.zeros(4)
+        launches = 0
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        for s in range(steps):
+            flush.zero_()
+            ev[s][0].record(stream)
+            step(precision)
+            ev[s][1].record(stream)
+            if profile:
+                ms, cnt = ctx.last_timings()
+                phase += ms
+            launches += ctx.last_timings()[1][2] + 2   # + the two zero_ fills of the step
+        torch.cuda.synchronize()
+        tot = sum(a.elapsed_time(b) for a, b in ev) / 1e3
+        if world > 1:
+            t = torch.tensor([tot], device=dev)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            tot = float(t.item())
+        return tot, phase / steps, launches
+
+    # numerics of the mixed path against the FP64 path on this machine
+    sc64 = step(capi.FP64)
+    F64 = F.cpu().numpy().copy()
+    scm = step(capi.MIXED)
+    Fm = F.cpu().numpy()
+    err_f = float(np.sqrt(np.mean((Fm - F64) ** 2) / np.mean(F64 ** 2)))
+    j64 = sc64[12:15] + sc64[15:18]
+    jm = scm[12:15] + scm[15:18]
+    err_j = float(np.linalg.norm(jm - j64) / np.linalg.norm(j64))
+    e64 = sc64[0] + sc64[1]
+    err_e = float(abs(scm[0] + scm[1] - e64) / abs(e64))
+    _, (ndim, ntri, _) = ctx.last_timings()
+
+    clocks = ClockSampler(dev.index)
+    clocks.start()
+    t_mixed, phase_mixed, launches = timed(capi.MIXED, args.steps, args.warmup)
+    clk = clocks.stop()
+    _, phase_prof, _ = timed(capi.MIXED, max(3, args.steps // 4), 1, profile=True)
+    k64 = max(2, args.steps // 8)
+    t_fp64, _, _ = timed(capi.FP64, k64, 1)
+    _, phase64, _ = timed(capi.FP64, 2, 0, profile=True)
+
+    # e2e through the host-array C ABI from pinned host buffers
+    pin = dict(dtype=torch.float64, pin_memory=True)
+    hx = [torch.tensor(np.ascontiguousarray(box.xyz[:, k]), **pin) for k in range(3)]
+    hv = [torch.tensor(np.ascontiguousarray(box.vel[:, k]), **pin) for k in range(3)]
+    hm = torch.tensor(box.mass, **pin)
+    hf = torch.zeros((3, n), **pin)
+    hae = torch.zeros(n, **pin)
+    hl = torch.tensor(box.listttm2(), dtype=torch.int32, pin_memory=True)
+    import ctypes as C
+    D = C.POINTER(C.c_double)
+
+    def hp(t):
+        return C.cast(C.c_void_p(t.data_ptr()), D)
+
+    eng = C.c_double(0)
+    vir = C.c_double(0)
+    stress = np.zeros(9)
+    sc = np.zeros(capi.NSCALARS)
+
+    def e2e_step():
+        rc = ctx.lib.mbx_mbpol_forces(ctx.h, capi.MIXED, box.imcon, box.cell.ctypes.data_as(D), 3 * box.nw,
+                                      C.cast(C.c_void_p(hl.data_ptr()), C.POINTER(C.c_int)), n, hp(hx[0]),
+                                      hp(hx[1]), hp(hx[2]), hp(hf[0]), hp(hf[1]), hp(hf[2]), C.byref(eng),
+                                      C.byref(vir), stress.ctypes.data_as(D), hp(hv[0]), hp(hv[1]), hp(hv[2]),
+                                      hp(hm), hp(hae), sc.ctypes.data_as(D))
+        if rc:
+            raise RuntimeError("mbx_mbpol_forces failed: %d" % rc)
+
+    ctx.set_profiling(False)
+    for _ in range(args.warmup):
+        e2e_step()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        e2e_step()
+    t_e2e = time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([t_e2e], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        t_e2e = float(t.item())
+    h2d = 7 * n * 8 + 3 * box.nw * 4
+    d2h = 4 * n * 8 + capi.NSCALARS * 8
+    ctx.close()
+
+    if rank != 0:
+        return None
+    peaks = _peaks()
+    fl = poly_flops()
+    t3 = phase_prof[2] / 1e3
+    sm_max = peaks.get("sm_max_mhz", 2070.0)
+    fp32_peak = 152 * 128 * 2 * sm_max * 1e6 / 1e12   # TFLOP/s at the maximum SM clock
+    achieved = fl["3b"] * ntri / t3 / 1e12 if t3 > 0 else None
+    traffic = None
+    tfile = os.path.join(REPO, "profiles", "traffic.json")
+    if os.path.exists(tfile):
+        with open(tfile) as f:
+            tj = json.load(f)
+        per = tj.get("k_mbpol_3b_float_bytes_per_trimer")
+        if per:
+            traffic = per * ntri
+    value = world * args.steps / t_mixed
+    out = {
+        "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * t_mixed / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 per cluster, f64 accumulation",
+        "data": DATA,
+        "config": {"workload": WORKLOAD, "precision": "mixed", "parallelism": "replicas" if world > 1 else "single",
+                   "l2": "flushed between steps (256 MiB write)", "dimers": int(ndim), "trimers": int(ntri),
+                   "not_yet_in_step": NOT_IN_STEP},
+        "fp64": {"value": world * k64 / t_fp64, "unit": "steps/s", "ms_per_step": 1e3 * t_fp64 / k64,
+                 "phase_ms": {"lists": phase64[0], "2b": phase64[1], "3b": phase64[2], "jkin": phase64[3]}},
+        "mixed_over_fp64": (args.steps / t_mixed) / (k64 / t_fp64),
+        "mixed_error_vs_fp64": {"force_rms_rel": err_f, "heat_current_rel": err_j, "energy_rel": err_e},
+        "phase_ms": {"lists": phase_prof[0], "2b": phase_prof[1], "3b": phase_prof[2], "jkin": phase_prof[3]},
+        "e2e": {"value": world * args.steps / t_e2e, "unit": "steps/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "roofline": {"kernel": "k_mbpol_3b<float>", "bound": "fp32", "achieved": achieved, "peak": fp32_peak,
+                     "unit": "TFLOP/s", "frac": (achieved / fp32_peak) if achieved else None, "traffic": traffic,
+                     "flops_per_trimer": fl["3b"],
+                     "peak_source": "computed: 152 SMs x 128 FP32 lanes x 2 flop x sm_max_mhz %.0f "
+                                    "(no FP32 peak in MEASURED_PEAKS.json)" % sm_max},
+        "clocks": clk,
+        "gpu_launches": int(launches),
+    }
+    if not args.no_cpu_baseline:
+        sps, info = cpu_reference(box)
+        out["cpu_baseline"] = {"value": sps, "unit": "steps/s", "cores": info["cores"], "kind": "port",
+                               "sample": info["sample"]}
+    return out
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return None
+    from mbx import systems
+    box = systems.config1()
+    vals = []
+    info = None
+    for s in range(args.warmup + args.steps):
+        sps, info = cpu_reference(box, target_core_s=args.ref_core_s)
+        if s >= args.warmup:
+            vals.append(1.0 / sps)
+    step_s = float(np.mean(vals))
+    v = 1.0 / step_s
+    return {"metric": METRIC, "value": v, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * step_s, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": DATA, "impl": "reference",
+            "config": {"workload": WORKLOAD, "precision": "fp64", "parallelism": "host threads"},
+            "cpu_baseline": {"value": v, "unit": "steps/s", "cores": info["cores"], "kind": "port",
+                             "sample": info["sample"]},
+            "e2e": {"value": v, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=40)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ref-core-s", type=float, default=10.0)
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    rank = int(os.environ.get("RANK", 0))
+    if world > 1 and args.impl == "ours":
+        import torch
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+        torch.distributed.init_process_group("nccl")
+    out = run_reference(args, rank, world) if args.impl == "reference" else run_ours(args, rank, world)
+    if out is not None:
+        print(json.dumps(out))
+    if world > 1 and args.impl == "ours":
+        import torch
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,509 @@
+// C ABI of libmbx: contexts, host/device entry points and the per-call drop-ins.
+#include "../../include/mbx.h"
+#include "mbx_kernels.cuh"
+
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+using namespace mbx;
+
+struct mbx_context {
+    int device = 0;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+    ListBuilder lb;
+    int nw_cap = 0, natms_cap = 0;
+    double* mono = nullptr;       // 9 per water
+    int* list = nullptr;          // device copy of listttm2 (host entry point)
+    double* atoms = nullptr;      // host entry point staging: x y z vx vy vz m f(3) ae  (11 * natms)
+    double* ae_scratch = nullptr; // per-atom energy when the caller passes none
+    double* acc = nullptr;        // MBX_NSCALARS accumulators
+    int* totals = nullptr;        // device list totals
+    int* totals_h = nullptr;      // pinned
+    double* acc_h = nullptr;      // pinned
+    int2* pairs = nullptr;
+    long pairs_cap = 0;
+    int4* trip = nullptr;
+    long trip_cap = 0;
+    long npairs = 0, ntrip = 0;
+    // batch-API staging
+    double* batch = nullptr;
+    size_t batch_bytes = 0;
+    // optional per-phase timing on the context's stream (mbx_set_profiling)
+    int profiling = 0;
+    cudaEvent_t ev[8] = {nullptr};
+    float phase_ms[4] = {0, 0, 0, 0};  // lists, 2B, 3B, heat/jkin
+    long launches = 0;                 // kernel launches issued by the last evaluation
+    char err[512] = {0};
+};
+
+namespace {
+
+int fail(mbx_context* c, int code, const char* fmt, ...) {
+    if (c) {
+        va_list ap;
+        va_start(ap, fmt);
+        std::vsnprintf(c->err, sizeof c->err, fmt, ap);
+        va_end(ap);
+    }
+    return code;
+}
+
+#define CK(call)                                                                                  \
+    do {                                                                                          \
+        cudaError_t e_ = (call);                                                                  \
+        if (e_ != cudaSuccess)                                                                    \
+            return fail(ctx, MBX_ERR_CUDA, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), \
+                        __FILE__, __LINE__);                                                      \
+    } while (0)
+
+int make_cell(mbx_context* ctx, int imcon, const double* cell, Cell& cl) {
+    if (!cell) return fail(ctx, MBX_ERR_ARG, "cell is NULL");
+    if (imcon < 1 || imcon > 3) return fail(ctx, MBX_ERR_ARG, "imcon %d not supported (1, 2 or 3)", imcon);
+    cl.imcon = imcon;
+    for (int i = 0; i < 9; ++i) cl.c[i] = cell[i];
+    cl.inv[0] = 1.0 / cell[0];
+    cl.inv[1] = 1.0 / cell[4];
+    cl.inv[2] = 1.0 / cell[8];
+    // invert (SOURCE/invert.f), used for imcon 3
+    const double* a = cell;
+    double* b = cl.rc;
+    b[0] = a[4] * a[8] - a[5] * a[7];
+    b[1] = a[2] * a[7] - a[1] * a[8];
+    b[2] = a[1] * a[5] - a[2] * a[4];
+    b[3] = a[5] * a[6] - a[3] * a[8];
+    b[4] = a[0] * a[8] - a[2] * a[6];
+    b[5] = a[2] * a[3] - a[0] * a[5];
+    b[6] = a[3] * a[7] - a[4] * a[6];
+    b[7] = a[1] * a[6] - a[0] * a[7];
+    b[8] = a[0] * a[4] - a[1] * a[3];
+    const double d = a[0] * b[0] + a[3] * b[1] + a[6] * b[2];
+    const double r = std::fabs(d) > 0.0 ? 1.0 / d : 0.0;
+    for (int i = 0; i < 9; ++i) b[i] *= r;
+    if (!(cell[0] > 0.0) || !(cell[4] > 0.0) || !(cell[8] > 0.0))
+        return fail(ctx, MBX_ERR_ARG, "cell diagonal must be positive");
+    return MBX_OK;
+}
+
+int reserve_water(mbx_context* ctx, int nw, int natms) {
+    if (nw > ctx->nw_cap) {
+        if (ctx->mono) cudaFree(ctx->mono);
+        if (ctx->list) cudaFree(ctx->list);
+        ctx->mono = nullptr;
+        ctx->list = nullptr;
+        CK(cudaMalloc(&ctx->mono, 9 * (size_t)nw * sizeof(double)));
+        CK(cudaMalloc(&ctx->list, 3 * (size_t)nw * sizeof(int)));
+        ctx->nw_cap = nw;
+    }
+    if (natms > ctx->natms_cap) {
+        if (ctx->atoms) cudaFree(ctx->atoms);
+        if (ctx->ae_scratch) cudaFree(ctx->ae_scratch);
+        ctx->atoms = ctx->ae_scratch = nullptr;
+        CK(cudaMalloc(&ctx->atoms, 11 * (size_t)natms * sizeof(double)));
+        CK(cudaMalloc(&ctx->ae_scratch, (size_t)natms * sizeof(double)));
+        ctx->natms_cap = natms;
+    }
+    return MBX_OK;
+}
+
+// The whole MB-pol evaluation on device arrays.
+int run_mbpol(mbx_context* ctx, int precision, const Cell& cl, int nw, const int* list_dev, int natms,
+              const double* x, const double* y, const double* z, double* fx, double* fy, double* fz,
+              const double* vx, const double* vy, const double* vz, const double* mass, double* ae,
+              double* scalars) {
+    if (precision != MBX_FP64 && precision != MBX_MIXED)
+        return fail(ctx, MBX_ERR_ARG, "precision must be MBX_FP64 or MBX_MIXED");
+    if (nw < 0 || natms < 3 * nw) return fail(ctx, MBX_ERR_ARG, "bad sizes nw=%d natms=%d", nw, natms);
+    if (!x || !y || !z || !fx || !fy || !fz) return fail(ctx, MBX_ERR_ARG, "NULL position/force array");
+    const bool heat = vx && vy && vz;
+    int rc = reserve_water(ctx, std::max(nw, 1), std::max(natms, 1));
+    if (rc) return rc;
+    cudaStream_t s = ctx->stream;
+    CK(cudaMemsetAsync(ctx->acc, 0, MBX_NSCALARS * sizeof(double), s));
+    double* ae_use = ae;
+    if (!ae_use && heat && mass) {
+        ae_use = ctx->ae_scratch;
+        CK(cudaMemsetAsync(ae_use, 0, (size_t)natms * sizeof(double), s));
+    }
+    ctx->npairs = ctx->ntrip = 0;
+    ctx->launches = 0;
+    if (ctx->profiling) CK(cudaEventRecord(ctx->ev[0], s));
+    if (nw >= 2) {
+        // lists: count, read totals, grow capacities if needed, fill
+        for (int attempt = 0;; ++attempt) {
+            CK(ctx->lb.phase1(nw, list_dev, x, y, z, cl, ctx->mono, ctx->totals, s));
+            CK(cudaMemcpyAsync(ctx->totals_h, ctx->totals, 3 * sizeof(int), cudaMemcpyDeviceToHost, s));
+            CK(cudaStreamSynchronize(s));
+            if (!ctx->totals_h[2]) break;
+            if (attempt >= 6 || ctx->lb.cap2 >= nw + 8)
+                return fail(ctx, MBX_ERR_CAPACITY, "neighbour list capacity exceeded");
+            ctx->lb.cap2 = std::min(2 * ctx->lb.cap2, nw + 8);
+            ctx->lb.cap3 = std::min(2 * ctx->lb.cap3, nw + 8);
+        }
+        const long np = ctx->totals_h[0], nt = ctx->totals_h[1];
+        if (np > ctx->pairs_cap) {
+            if (ctx->pairs) cudaFree(ctx->pairs);
+            ctx->pairs = nullptr;
+            const long cap = np + np / 4 + 64;
+            CK(cudaMalloc(&ctx->pairs, cap * sizeof(int2)));
+            ctx->pairs_cap = cap;
+        }
+        if (nt > ctx->trip_cap) {
+            if (ctx->trip) cudaFree(ctx->trip);
+            ctx->trip = nullptr;
+            const long cap = nt + nt / 4 + 64;
+            CK(cudaMalloc(&ctx->trip, cap * sizeof(int4)));
+            ctx->trip_cap = cap;
+        }
+        CK(ctx->lb.phase2(nw, cl, ctx->mono, ctx->pairs, ctx->trip, s));
+        if (ctx->profiling) CK(cudaEventRecord(ctx->ev[1], s));
+        ctx->launches += ctx->lb.launches_last;
+        ctx->npairs = np;
+        ctx->ntrip = nt;
+        MbpolArgs a;
+        a.nw = nw;
+        a.cell = cl;
+        a.list = list_dev;
+        a.x = x; a.y = y; a.z = z;
+        a.vx = heat ? vx : nullptr;
+        a.vy = heat ? vy : nullptr;
+        a.vz = heat ? vz : nullptr;
+        a.mono = ctx->mono;
+        a.fx = fx; a.fy = fy; a.fz = fz;
+        a.ae = ae_use;
+        a.acc = ctx->acc;
+        CK(launch_2b(a, ctx->pairs, (int)np, precision, s));
+        if (ctx->profiling) CK(cudaEventRecord(ctx->ev[2], s));
+        CK(launch_3b(a, ctx->trip, (int)nt, precision, s));
+        if (ctx->profiling) CK(cudaEventRecord(ctx->ev[3], s));
+        ctx->launches += (np > 0) + (nt > 0);
+    } else if (ctx->profiling) {
+        for (int q = 1; q < 4; ++q) CK(cudaEventRecord(ctx->ev[q], s));
+    }
+    if (heat && mass) {
+        CK(launch_jkin(3 * nw, vx, vy, vz, mass, ae_use, ctx->acc, s));
+        ctx->launches += nw > 0;
+    }
+    if (ctx->profiling) CK(cudaEventRecord(ctx->ev[4], s));
+    CK(cudaMemcpyAsync(ctx->acc_h, ctx->acc, MBX_NSCALARS * sizeof(double), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (scalars) std::memcpy(scalars, ctx->acc_h, MBX_NSCALARS * sizeof(double));
+    if (ctx->profiling)
+        for (int q = 0; q < 4; ++q) CK(cudaEventElapsedTime(&ctx->phase_ms[q], ctx->ev[q], ctx->ev[q + 1]));
+    return MBX_OK;
+}
+
+int check_device(mbx_context* ctx, int device) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n <= device || device < 0)
+        return fail(ctx, MBX_ERR_NO_DEVICE, "CUDA device %d not available", device);
+    cudaDeviceProp p;
+    CK(cudaGetDeviceProperties(&p, device));
+    if (p.major != 10 || p.minor != 3)
+        return fail(ctx, MBX_ERR_NO_DEVICE, "device %d is sm_%d%d; libmbx is built for sm_103a only", device,
+                    p.major, p.minor);
+    return MBX_OK;
+}
+
+}  // namespace
+
+extern "C" int mbx_create(mbx_context** out, int device) {
+    if (!out) return MBX_ERR_ARG;
+    *out = nullptr;
+    mbx_context* ctx = new mbx_context();
+    int rc = check_device(ctx, device);
+    if (rc) {
+        std::fprintf(stderr, "mbx_create: %s\n", ctx->err);
+        delete ctx;
+        return rc;
+    }
+    ctx->device = device;
+    auto init = [&]() -> int {
+        CK(cudaSetDevice(device));
+        // the fused cluster kernels call the generated polynomial functions, whose
+        // frames need up to ~2.3 KB of stack per thread (FP64); reserve it up front
+        size_t stack = 0;
+        CK(cudaDeviceGetLimit(&stack, cudaLimitStackSize));
+        if (stack < 4096) CK(cudaDeviceSetLimit(cudaLimitStackSize, 4096));
+        CK(cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking));
+        ctx->stream = ctx->own_stream;
+        CK(cudaMalloc(&ctx->acc, MBX_NSCALARS * sizeof(double)));
+        CK(cudaMalloc(&ctx->totals, 4 * sizeof(int)));
+        CK(cudaMallocHost(&ctx->totals_h, 4 * sizeof(int)));
+        CK(cudaMallocHost(&ctx->acc_h, MBX_NSCALARS * sizeof(double)));
+        return MBX_OK;
+    };
+    rc = init();
+    if (rc) {
+        std::fprintf(stderr, "mbx_create: %s\n", ctx->err);
+        mbx_destroy(ctx);
+        return rc;
+    }
+    *out = ctx;
+    return MBX_OK;
+}
+
+extern "C" void mbx_destroy(mbx_context* ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    if (ctx->own_stream) cudaStreamSynchronize(ctx->own_stream);
+    void* dev[] = {ctx->mono, ctx->list, ctx->atoms, ctx->ae_scratch, ctx->acc, ctx->totals, ctx->pairs, ctx->trip,
+                   ctx->batch};
+    for (void* p : dev)
+        if (p) cudaFree(p);
+    if (ctx->totals_h) cudaFreeHost(ctx->totals_h);
+    if (ctx->acc_h) cudaFreeHost(ctx->acc_h);
+    ctx->lb.release();
+    for (cudaEvent_t e : ctx->ev)
+        if (e) cudaEventDestroy(e);
+    if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+    delete ctx;
+}
+
+extern "C" int mbx_set_profiling(mbx_context* ctx, int on) {
+    if (!ctx) return MBX_ERR_ARG;
+    CK(cudaSetDevice(ctx->device));
+    if (on && !ctx->ev[0])
+        for (cudaEvent_t& e : ctx->ev) CK(cudaEventCreate(&e));
+    ctx->profiling = on ? 1 : 0;
+    return MBX_OK;
+}
+
+extern "C" int mbx_last_timings(mbx_context* ctx, double* ms, long* counts) {
+    if (!ctx) return MBX_ERR_ARG;
+    if (ms)
+        for (int q = 0; q < 4; ++q) ms[q] = ctx->profiling ? ctx->phase_ms[q] : -1.0;
+    if (counts) {
+        counts[0] = ctx->npairs;
+        counts[1] = ctx->ntrip;
+        counts[2] = ctx->launches;
+    }
+    return MBX_OK;
+}
+
+extern "C" const char* mbx_error(const mbx_context* ctx) { return ctx ? ctx->err : "no context"; }
+
+extern "C" int mbx_set_stream(mbx_context* ctx, void* stream) {
+    if (!ctx) return MBX_ERR_ARG;
+    ctx->stream = stream ? (cudaStream_t)stream : ctx->own_stream;
+    return MBX_OK;
+}
+
+extern "C" int mbx_mbpol_forces_device(mbx_context* ctx, int precision, int imcon, const double* cell, int nttm2,
+                                       const int* listttm2, int natms, const double* xxx, const double* yyy,
+                                       const double* zzz, double* fxx, double* fyy, double* fzz, const double* vxx,
+                                       const double* vyy, const double* vzz, const double* weight,
+                                       double* atomic_energy, double* scalars) {
+    if (!ctx) return MBX_ERR_ARG;
+    if (nttm2 < 0 || nttm2 % 3) return fail(ctx, MBX_ERR_ARG, "nttm2 must be a multiple of 3");
+    if (nttm2 > 0 && !listttm2) return fail(ctx, MBX_ERR_ARG, "listttm2 is NULL");
+    Cell cl;
+    int rc = make_cell(ctx, imcon, cell, cl);
+    if (rc) return rc;
+    CK(cudaSetDevice(ctx->device));
+    return run_mbpol(ctx, precision, cl, nttm2 / 3, listttm2, natms, xxx, yyy, zzz, fxx, fyy, fzz, vxx, vyy, vzz,
+                     weight, atomic_energy, scalars);
+}
+
+extern "C" int mbx_mbpol_forces(mbx_context* ctx, int precision, int imcon, const double* cell, int nttm2,
+                                const int* listttm2, int natms, const double* xxx, const double* yyy,
+                                const double* zzz, double* fxx, double* fyy, double* fzz, double* engsrp,
+                                double* virsrp, double* stress, const double* vxx, const double* vyy,
+                                const double* vzz, const double* weight, double* atomic_energy, double* scalars) {
+    if (!ctx) return MBX_ERR_ARG;
+    if (nttm2 < 0 || nttm2 % 3) return fail(ctx, MBX_ERR_ARG, "nttm2 must be a multiple of 3");
+    if (!xxx || !yyy || !zzz || !fxx || !fyy || !fzz || !engsrp || !virsrp || !stress)
+        return fail(ctx, MBX_ERR_ARG, "NULL argument");
+    if (nttm2 > 0 && !listttm2) return fail(ctx, MBX_ERR_ARG, "listttm2 is NULL");
+    for (int t = 0; t < nttm2; ++t)
+        if (listttm2[t] < 1 || listttm2[t] > natms || (t % 3 && listttm2[t] != listttm2[t - t % 3] + t % 3))
+            return fail(ctx, MBX_ERR_ARG, "listttm2[%d]=%d: water atoms must be 1-based, O,H1,H2 consecutive", t,
+                        listttm2[t]);
+    Cell cl;
+    int rc = make_cell(ctx, imcon, cell, cl);
+    if (rc) return rc;
+    CK(cudaSetDevice(ctx->device));
+    const int nw = nttm2 / 3;
+    rc = reserve_water(ctx, std::max(nw, 1), std::max(natms, 1));
+    if (rc) return rc;
+    const bool heat = vxx && vyy && vzz && weight;
+    cudaStream_t s = ctx->stream;
+    const size_t nb = (size_t)natms * sizeof(double);
+    double* d = ctx->atoms;
+    double *dx = d, *dy = d + natms, *dz = d + 2 * (size_t)natms;
+    double *dvx = d + 3 * (size_t)natms, *dvy = d + 4 * (size_t)natms, *dvz = d + 5 * (size_t)natms;
+    double* dm = d + 6 * (size_t)natms;
+    double *dfx = d + 7 * (size_t)natms, *dfy = d + 8 * (size_t)natms, *dfz = d + 9 * (size_t)natms;
+    double* dae = d + 10 * (size_t)natms;
+    if (nttm2) CK(cudaMemcpyAsync(ctx->list, listttm2, nttm2 * sizeof(int), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(dx, xxx, nb, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(dy, yyy, nb, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(dz, zzz, nb, cudaMemcpyHostToDevice, s));
+    if (heat) {
+        CK(cudaMemcpyAsync(dvx, vxx, nb, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(dvy, vyy, nb, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(dvz, vzz, nb, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(dm, weight, nb, cudaMemcpyHostToDevice, s));
+    }
+    CK(cudaMemsetAsync(dfx, 0, 3 * nb, s));
+    if (atomic_energy) CK(cudaMemsetAsync(dae, 0, nb, s));
+    double sc[MBX_NSCALARS];
+    rc = run_mbpol(ctx, precision, cl, nw, ctx->list, natms, dx, dy, dz, dfx, dfy, dfz, heat ? dvx : nullptr,
+                   heat ? dvy : nullptr, heat ? dvz : nullptr, heat ? dm : nullptr, atomic_energy ? dae : nullptr,
+                   sc);
+    if (rc) return rc;
+    // bring the per-atom results back and accumulate into the caller's arrays
+    std::vector<double> h(4 * (size_t)natms);
+    CK(cudaMemcpyAsync(h.data(), dfx, 3 * nb, cudaMemcpyDeviceToHost, s));
+    if (atomic_energy) CK(cudaMemcpyAsync(h.data() + 3 * (size_t)natms, dae, nb, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    for (int i = 0; i < natms; ++i) {
+        fxx[i] += h[i];
+        fyy[i] += h[natms + i];
+        fzz[i] += h[2 * (size_t)natms + i];
+        if (atomic_energy) atomic_energy[i] += h[3 * (size_t)natms + i];
+    }
+    *engsrp += sc[MBX_S_ENG2] + sc[MBX_S_ENG3];
+    *virsrp += sc[MBX_S_VIR];
+    for (int q = 0; q < 9; ++q) stress[q] += sc[MBX_S_STRESS + q];
+    if (scalars) std::memcpy(scalars, sc, sizeof sc);
+    return MBX_OK;
+}
+
+extern "C" int mbx_last_lists(mbx_context* ctx, int* pairs, long cap_pairs, long* npairs, int* trimers,
+                              long cap_trimers, long* ntrimers) {
+    if (!ctx) return MBX_ERR_ARG;
+    if (npairs) *npairs = ctx->npairs;
+    if (ntrimers) *ntrimers = ctx->ntrip;
+    CK(cudaSetDevice(ctx->device));
+    if (pairs && ctx->npairs) {
+        const long n = std::min(cap_pairs, ctx->npairs);
+        CK(cudaMemcpy(pairs, ctx->pairs, n * sizeof(int2), cudaMemcpyDeviceToHost));
+    }
+    if (trimers && ctx->ntrip) {
+        const long n = std::min(cap_trimers, ctx->ntrip);
+        std::vector<int4> t(n);
+        CK(cudaMemcpy(t.data(), ctx->trip, n * sizeof(int4), cudaMemcpyDeviceToHost));
+        for (long q = 0; q < n; ++q) {
+            trimers[3 * q] = t[q].x;
+            trimers[3 * q + 1] = t[q].y;
+            trimers[3 * q + 2] = t[q].z;
+        }
+    }
+    return MBX_OK;
+}
+
+namespace {
+int batch_reserve(mbx_context* ctx, size_t bytes) {
+    if (bytes > ctx->batch_bytes) {
+        if (ctx->batch) cudaFree(ctx->batch);
+        ctx->batch = nullptr;
+        CK(cudaMalloc(&ctx->batch, bytes));
+        ctx->batch_bytes = bytes;
+    }
+    return MBX_OK;
+}
+}  // namespace
+
+extern "C" int mbx_2b_poly_batch(mbx_context* ctx, int precision, long n, const double* w1, const double* w2,
+                                 double* E, double* g1, double* g2) {
+    if (!ctx) return MBX_ERR_ARG;
+    if (n < 0 || n > 0x7fffffff) return fail(ctx, MBX_ERR_ARG, "bad n");
+    if (n == 0) return MBX_OK;
+    if (!w1 || !w2 || !E || !g1 || !g2) return fail(ctx, MBX_ERR_ARG, "NULL argument");
+    if (precision != MBX_FP64 && precision != MBX_MIXED) return fail(ctx, MBX_ERR_ARG, "bad precision");
+    CK(cudaSetDevice(ctx->device));
+    const size_t b9 = 9 * (size_t)n * sizeof(double);
+    int rc = batch_reserve(ctx, 4 * b9 + n * sizeof(double));
+    if (rc) return rc;
+    double *d1 = ctx->batch, *d2 = d1 + 9 * n, *dg1 = d2 + 9 * n, *dg2 = dg1 + 9 * n, *dE = dg2 + 9 * n;
+    cudaStream_t s = ctx->stream;
+    CK(cudaMemcpyAsync(d1, w1, b9, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(d2, w2, b9, cudaMemcpyHostToDevice, s));
+    CK(launch_2b_direct((int)n, d1, d2, dE, dg1, dg2, precision, s));
+    CK(cudaMemcpyAsync(E, dE, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(g1, dg1, b9, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(g2, dg2, b9, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    return MBX_OK;
+}
+
+extern "C" int mbx_3b_poly_batch(mbx_context* ctx, int precision, long n, const double* w1, const double* w2,
+                                 const double* w3, double* E, double* g1, double* g2, double* g3) {
+    if (!ctx) return MBX_ERR_ARG;
+    if (n < 0 || n > 0x7fffffff) return fail(ctx, MBX_ERR_ARG, "bad n");
+    if (n == 0) return MBX_OK;
+    if (!w1 || !w2 || !w3 || !E || !g1 || !g2 || !g3) return fail(ctx, MBX_ERR_ARG, "NULL argument");
+    if (precision != MBX_FP64 && precision != MBX_MIXED) return fail(ctx, MBX_ERR_ARG, "bad precision");
+    CK(cudaSetDevice(ctx->device));
+    const size_t b9 = 9 * (size_t)n * sizeof(double);
+    int rc = batch_reserve(ctx, 6 * b9 + n * sizeof(double));
+    if (rc) return rc;
+    double *d1 = ctx->batch, *d2 = d1 + 9 * n, *d3 = d2 + 9 * n, *dg1 = d3 + 9 * n, *dg2 = dg1 + 9 * n,
+           *dg3 = dg2 + 9 * n, *dE = dg3 + 9 * n;
+    cudaStream_t s = ctx->stream;
+    CK(cudaMemcpyAsync(d1, w1, b9, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(d2, w2, b9, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(d3, w3, b9, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(dg1, g1, b9, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(dg2, g2, b9, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(dg3, g3, b9, cudaMemcpyHostToDevice, s));
+    CK(launch_3b_direct((int)n, d1, d2, d3, dE, dg1, dg2, dg3, precision, s));
+    CK(cudaMemcpyAsync(E, dE, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(g1, dg1, b9, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(g2, dg2, b9, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(g3, dg3, b9, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    return MBX_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Per-call drop-ins: one process-wide context per device, created on first use.
+namespace {
+std::mutex g_mu;
+mbx_context* g_ctx[64] = {nullptr};
+
+mbx_context* global_ctx() {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+        std::fprintf(stderr, "libmbx: no CUDA device\n");
+        std::abort();
+    }
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (!g_ctx[dev] && mbx_create(&g_ctx[dev], dev) != MBX_OK) {
+        std::fprintf(stderr, "libmbx: cannot create a context on device %d\n", dev);
+        std::abort();
+    }
+    return g_ctx[dev];
+}
+}  // namespace
+
+extern "C" void mbpol_2b_poly_(const double* w1, const double* w2, double* E, double* g1, double* g2,
+                               double* force_matrix) {
+    (void)force_matrix;
+    mbx_context* c = global_ctx();
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (mbx_2b_poly_batch(c, MBX_FP64, 1, w1, w2, E, g1, g2) != MBX_OK) {
+        std::fprintf(stderr, "mbpol_2b_poly_: %s\n", mbx_error(c));
+        std::abort();
+    }
+}
+
+extern "C" void mbpol_3b_poly_(const double* w1, const double* w2, const double* w3, double* E, double* g1,
+                               double* g2, double* g3, double* force_matrix) {
+    (void)force_matrix;
+    mbx_context* c = global_ctx();
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (mbx_3b_poly_batch(c, MBX_FP64, 1, w1, w2, w3, E, g1, g2, g3) != MBX_OK) {
+        std::fprintf(stderr, "mbpol_3b_poly_: %s\n", mbx_error(c));
+        std::abort();
+    }
+}
+
+extern "C" void mbpol_2b_cutoff_(double* r) { *r = kR2f; }
+extern "C" void mbpol_3b_cutoff_(double* r) { *r = kR3f; }

@@ -1,0 +1,95 @@
+// Shared device helpers for the MB-pol GB300 path.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace mbx {
+
+constexpr double kEngUnit = 418.4;        // SOURCE/mbpol.f90:37, internal units per kcal/mol
+constexpr double kR2f = 6.5;              // 2B outer cutoff, SOURCE/mbpol-2b-poly.cpp:1863
+constexpr double kR2i = 4.5;              // 2B switch start, SOURCE/mbpol-2b-poly.cpp:1862
+constexpr double kR3f = 4.5;              // 3B cutoff, SOURCE/mbpol-3b-poly.cpp:1489
+constexpr int kThreads = 128;
+
+// Simulation-cell description passed by value to kernels.
+struct Cell {
+    int imcon;          // 1 cubic, 2 orthorhombic, 3 triclinic (DL_POLY keys)
+    double c[9];        // cell vectors, DL_POLY order
+    double rc[9];       // inverse (imcon 3)
+    double inv[3];      // 1/c[0], 1/c[4], 1/c[8]
+};
+
+// Unfused double arithmetic: list tests and imaging must round exactly like the
+// reference's x86-64 build (no contraction into FMA).
+__device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a, b); }
+
+// Fortran NINT on a double: round half away from zero.
+__device__ __forceinline__ double nint(double x) { return round(x); }
+
+// image_vectors (SOURCE/mbpol.f90:1305-1361) applied to one vector.
+__device__ __forceinline__ void image(const Cell& cl, double& x, double& y, double& z) {
+    if (cl.imcon == 1) {
+        x = dsub(x, dmul(cl.c[0], nint(dmul(x, cl.inv[0]))));
+        y = dsub(y, dmul(cl.c[0], nint(dmul(y, cl.inv[0]))));
+        z = dsub(z, dmul(cl.c[0], nint(dmul(z, cl.inv[0]))));
+    } else if (cl.imcon == 2) {
+        x = dsub(x, dmul(cl.c[0], nint(dmul(x, cl.inv[0]))));
+        y = dsub(y, dmul(cl.c[4], nint(dmul(y, cl.inv[1]))));
+        z = dsub(z, dmul(cl.c[8], nint(dmul(z, cl.inv[2]))));
+    } else {
+        const double* r = cl.rc;
+        const double ssx = dadd(dadd(dmul(r[0], x), dmul(r[3], y)), dmul(r[6], z));
+        const double ssy = dadd(dadd(dmul(r[1], x), dmul(r[4], y)), dmul(r[7], z));
+        const double ssz = dadd(dadd(dmul(r[2], x), dmul(r[5], y)), dmul(r[8], z));
+        const double xss = dsub(ssx, nint(ssx));
+        const double yss = dsub(ssy, nint(ssy));
+        const double zss = dsub(ssz, nint(ssz));
+        const double* c = cl.c;
+        x = dadd(dadd(dmul(c[0], xss), dmul(c[3], yss)), dmul(c[6], zss));
+        y = dadd(dadd(dmul(c[1], xss), dmul(c[4], yss)), dmul(c[7], zss));
+        z = dadd(dadd(dmul(c[2], xss), dmul(c[5], yss)), dmul(c[8], zss));
+    }
+}
+
+// |image(a - b)|^2 with the reference's association ((x^2 + y^2) + z^2).
+__device__ __forceinline__ double dist2_img(const Cell& cl, const double* a, const double* b,
+                                            double* d = nullptr) {
+    double x = dsub(a[0], b[0]), y = dsub(a[1], b[1]), z = dsub(a[2], b[2]);
+    image(cl, x, y, z);
+    if (d) { d[0] = x; d[1] = y; d[2] = z; }
+    return dadd(dadd(dmul(x, x), dmul(y, y)), dmul(z, z));
+}
+
+// Dimer test of do_dimer (SOURCE/mbpol.f90:496-503): keep iff r^2 <= r2f^2.
+__device__ __forceinline__ bool dimer_in(double r2) { return !(r2 > kR2f * kR2f); }
+// 3B pair test of do_trimer (SOURCE/mbpol.f90:839-862): the distance itself is compared.
+__device__ __forceinline__ bool tri_edge(double r2) { return !(__dsqrt_rn(r2) > kR3f); }
+
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Block-wide sum of NV doubles; thread 0 of the block adds the totals atomically.
+template <int NV>
+__device__ __forceinline__ void block_sum_atomic(double (&v)[NV], double* out) {
+    __shared__ double red[kThreads / 32][NV];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int q = 0; q < NV; ++q) {
+        double s = warp_sum(v[q]);
+        if (lane == 0) red[w][q] = s;
+    }
+    __syncthreads();
+    if (threadIdx.x < NV) {
+        double s = 0.0;
+        for (int i = 0; i < kThreads / 32; ++i) s += red[i][threadIdx.x];
+        atomicAdd(out + threadIdx.x, s);
+    }
+}
+
+}  // namespace mbx

@@ -1,0 +1,574 @@
+// Fused MB-pol 2B and 3B cluster kernels.
+//
+// One thread evaluates one dimer (or trimer) end to end:
+//   1. gather the two (three) imaged monomers and re-image them around the
+//      second one, as do_dimer / do_trimer do (SOURCE/mbpol.f90:505-509, :867-876);
+//   2. build the model's variables (2B: X sites + 31 exp / exp-over-r terms,
+//      SOURCE/mbpol-2b-poly.cpp:358-445; 3B: 36 exp terms, SOURCE/mbpol-3b-poly.cpp:148-206);
+//   3. call the generated polynomial value+gradient functions (PTX, linked in);
+//   4. chain rule back to the atoms, X-site redistribution and switching function
+//      (SOURCE/mbpol-2b-poly.cpp:447-682, SOURCE/mbpol-3b-poly.cpp:208-312);
+//   5. accumulate forces, per-atom energies (1/6, 1/9 per atom), energy, virial,
+//      stress and the cluster's exact share of the heat-current jpot term
+//      (the force-matrix rows of SOURCE/mbpol.f90:533-556 and :920-952 contracted as
+//      in SOURCE/heatcurrent.f90:703-728).
+//
+// T = double reproduces the reference's arithmetic (FP64 path).  T = float is
+// the mixed path: positions are re-imaged in FP64, shifted to the cluster's
+// frame, and everything per cluster runs in FP32; forces, energies, virial and the
+// heat current are accumulated in FP64.
+#include "mbx_kernels.cuh"
+#include "mbx_poly_gen.cuh"
+
+namespace mbx {
+
+__device__ __forceinline__ double t_exp(double v) { return exp(v); }
+__device__ __forceinline__ float t_exp(float v) { return expf(v); }
+__device__ __forceinline__ double t_sqrt(double v) { return sqrt(v); }
+__device__ __forceinline__ float t_sqrt(float v) { return sqrtf(v); }
+__device__ __forceinline__ double t_sin(double v) { return sin(v); }
+__device__ __forceinline__ float t_sin(float v) { return sinf(v); }
+__device__ __forceinline__ double t_cos(double v) { return cos(v); }
+__device__ __forceinline__ float t_cos(float v) { return cosf(v); }
+
+// ---------------------------------------------------------------------------
+// 2B model (x2b_v6x_p), constants of SOURCE/mbpol-2b-poly.cpp:1846-1866
+namespace m2b {
+constexpr double k_HH_intra = -6.480884773303821e-01;
+constexpr double k_OH_intra = 1.674518993682975e+00;
+constexpr double k_HH_coul = 1.148231864355956e+00;
+constexpr double k_OH_coul = 1.205989761123099e+00;
+constexpr double k_OO_coul = 1.395357065790959e+00;
+constexpr double k_XH_main = 7.347036852042255e-01;
+constexpr double k_XO_main = 7.998249864422826e-01;
+constexpr double k_XX_main = 7.960663960630585e-01;
+constexpr double in_plane_gamma = -9.721486914088159e-02;
+constexpr double out_of_plane_gamma = 9.859272078406150e-02;
+enum { Oa = 0, Ha1 = 3, Ha2 = 6, Ob = 9, Hb1 = 12, Hb2 = 15, Xa1 = 18, Xa2 = 21, Xb1 = 24, Xb2 = 27 };
+// variable kind (0 exp, 1 exp/r), r0, k, site1, site2 (SOURCE/mbpol-2b-poly.cpp:415-445)
+struct V { int coul; double r0, k; int s1, s2; };
+__device__ constexpr V kV[31] = {
+    {0, 1.0, k_HH_intra, Ha1, Ha2}, {0, 1.0, k_HH_intra, Hb1, Hb2}, {0, 1.0, k_OH_intra, Oa, Ha1},
+    {0, 1.0, k_OH_intra, Oa, Ha2},  {0, 1.0, k_OH_intra, Ob, Hb1},  {0, 1.0, k_OH_intra, Ob, Hb2},
+    {1, 4.0, k_HH_coul, Ha1, Hb1},  {1, 4.0, k_HH_coul, Ha1, Hb2},  {1, 4.0, k_HH_coul, Ha2, Hb1},
+    {1, 4.0, k_HH_coul, Ha2, Hb2},  {1, 4.0, k_OH_coul, Oa, Hb1},   {1, 4.0, k_OH_coul, Oa, Hb2},
+    {1, 4.0, k_OH_coul, Ob, Ha1},   {1, 4.0, k_OH_coul, Ob, Ha2},   {1, 4.0, k_OO_coul, Oa, Ob},
+    {0, 4.0, k_XH_main, Xa1, Hb1},  {0, 4.0, k_XH_main, Xa1, Hb2},  {0, 4.0, k_XH_main, Xa2, Hb1},
+    {0, 4.0, k_XH_main, Xa2, Hb2},  {0, 4.0, k_XH_main, Xb1, Ha1},  {0, 4.0, k_XH_main, Xb1, Ha2},
+    {0, 4.0, k_XH_main, Xb2, Ha1},  {0, 4.0, k_XH_main, Xb2, Ha2},  {0, 4.0, k_XO_main, Oa, Xb1},
+    {0, 4.0, k_XO_main, Oa, Xb2},   {0, 4.0, k_XO_main, Ob, Xa1},   {0, 4.0, k_XO_main, Ob, Xa2},
+    {0, 4.0, k_XX_main, Xa1, Xb1},  {0, 4.0, k_XX_main, Xa1, Xb2},  {0, 4.0, k_XX_main, Xa2, Xb1},
+    {0, 4.0, k_XX_main, Xa2, Xb2},
+};
+}  // namespace m2b
+
+// monomer::setup (SOURCE/mbpol-2b-poly.cpp:118-140)
+template <typename T>
+__device__ __forceinline__ void xsites(const T* ohh, T* oh1, T* oh2, T* x1, T* x2) {
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        oh1[i] = ohh[i + 3] - ohh[i];
+        oh2[i] = ohh[i + 6] - ohh[i];
+    }
+    const T v[3] = {oh1[1] * oh2[2] - oh1[2] * oh2[1], oh1[2] * oh2[0] - oh1[0] * oh2[2],
+                    oh1[0] * oh2[1] - oh1[1] * oh2[0]};
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        const T in_plane = ohh[i] + T(0.5) * T(m2b::in_plane_gamma) * (oh1[i] + oh2[i]);
+        const T out_of_plane = T(m2b::out_of_plane_gamma) * v[i];
+        x1[i] = in_plane + out_of_plane;
+        x2[i] = in_plane - out_of_plane;
+    }
+}
+
+// monomer::grads (SOURCE/mbpol-2b-poly.cpp:144-177)
+template <typename T>
+__device__ __forceinline__ void xsite_grads(const T* oh1, const T* oh2, const T* g1, const T* g2, T* grd) {
+    const T gm[3] = {g1[0] - g2[0], g1[1] - g2[1], g1[2] - g2[2]};
+    const T t1[3] = {oh2[1] * gm[2] - oh2[2] * gm[1], oh2[2] * gm[0] - oh2[0] * gm[2],
+                     oh2[0] * gm[1] - oh2[1] * gm[0]};
+    const T t2[3] = {oh1[1] * gm[2] - oh1[2] * gm[1], oh1[2] * gm[0] - oh1[0] * gm[2],
+                     oh1[0] * gm[1] - oh1[1] * gm[0]};
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        const T gsum = g1[i] + g2[i];
+        const T in_plane = T(0.5) * T(m2b::in_plane_gamma) * gsum;
+        const T gh1 = in_plane + T(m2b::out_of_plane_gamma) * t1[i];
+        const T gh2 = in_plane - T(m2b::out_of_plane_gamma) * t2[i];
+        grd[i + 0] += gsum - (gh1 + gh2);
+        grd[i + 3] += gh1;
+        grd[i + 6] += gh2;
+    }
+}
+
+// f_switch (SOURCE/mbpol-2b-poly.cpp:340-354 and SOURCE/mbpol-3b-poly.cpp:130-144)
+template <typename T>
+__device__ __forceinline__ T f_switch(T r, T ri, T rf, T& g) {
+    if (r > rf) {
+        g = T(0);
+        return T(0);
+    } else if (r > ri) {
+        const T t1 = T(M_PI) / (rf - ri);
+        const T x = (r - ri) * t1;
+        g = -t_sin(x) * t1 / T(2);
+        return (T(1) + t_cos(x)) / T(2);
+    }
+    g = T(0);
+    return T(1);
+}
+
+// x2b_v6x_p::operator() on coordinates already in the working frame.
+// Returns E (kcal/mol); g1/g2 assigned.
+template <typename T>
+__device__ __forceinline__ T model_2b(const T* w1, const T* w2, T* g1, T* g2) {
+    const T dOO[3] = {w1[0] - w2[0], w1[1] - w2[1], w1[2] - w2[2]};
+    const T rOO = t_sqrt(dOO[0] * dOO[0] + dOO[1] * dOO[1] + dOO[2] * dOO[2]);
+    if (rOO > T(kR2f)) {
+#pragma unroll
+        for (int i = 0; i < 9; ++i) g1[i] = g2[i] = T(0);
+        return T(0);
+    }
+    T xc[30];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) {
+        xc[i] = w1[i];
+        xc[9 + i] = w2[i];
+    }
+    T oha[2][3], ohb[2][3];
+    xsites(xc + m2b::Oa, oha[0], oha[1], xc + m2b::Xa1, xc + m2b::Xa2);
+    xsites(xc + m2b::Ob, ohb[0], ohb[1], xc + m2b::Xb1, xc + m2b::Xb2);
+    T v[31], gg[31];
+#pragma unroll
+    for (int q = 0; q < 31; ++q) {
+        const m2b::V d = m2b::kV[q];
+        const T dx = xc[d.s1] - xc[d.s2], dy = xc[d.s1 + 1] - xc[d.s2 + 1], dz = xc[d.s1 + 2] - xc[d.s2 + 2];
+        const T r = t_sqrt(dx * dx + dy * dy + dz * dz);
+        const T e = t_exp(T(d.k) * (T(d.r0) - r));
+        if (!d.coul) {
+            v[q] = e;
+            gg[q] = -T(d.k) * e / r;
+        } else {
+            const T rinv = T(1) / r;
+            v[q] = e * rinv;
+            gg[q] = -(T(d.k) + rinv) * v[q] * rinv;
+        }
+    }
+    T acc[32];
+#pragma unroll
+    for (int q = 0; q < 32; ++q) acc[q] = T(0);
+    poly2b<T>(v, acc);
+    const T E_poly = acc[0];
+    T xgrd[30];
+#pragma unroll
+    for (int q = 0; q < 30; ++q) xgrd[q] = T(0);
+#pragma unroll
+    for (int q = 0; q < 31; ++q) {
+        const m2b::V d = m2b::kV[q];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const T gv = (xc[d.s1 + c] - xc[d.s2 + c]) * gg[q];
+            const T t = acc[1 + q] * gv;
+            xgrd[d.s1 + c] += t;
+            xgrd[d.s2 + c] -= t;
+        }
+    }
+    xsite_grads(oha[0], oha[1], xgrd + m2b::Xa1, xgrd + m2b::Xa2, xgrd + m2b::Oa);
+    xsite_grads(ohb[0], ohb[1], xgrd + m2b::Xb1, xgrd + m2b::Xb2, xgrd + m2b::Ob);
+    T gsw;
+    const T sw = f_switch(rOO, T(kR2i), T(kR2f), gsw);
+#pragma unroll
+    for (int i = 0; i < 9; ++i) {
+        g1[i] = sw * xgrd[i];
+        g2[i] = sw * xgrd[i + 9];
+    }
+    gsw *= E_poly / rOO;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        const T d = gsw * dOO[i];
+        g1[i] += d;
+        g2[i] -= d;
+    }
+    return sw * E_poly;
+}
+
+// ---------------------------------------------------------------------------
+// 3B model (x3b_v2x_p), constants of SOURCE/mbpol-3b-poly.cpp:1486-1506
+namespace m3b {
+constexpr double kHH_intra = -2.254303257872797e+00;
+constexpr double kOH_intra = -2.564771901404151e-01;
+constexpr double kHH = 4.247920544074333e-01;
+constexpr double kOH = 8.128985941165371e-01;
+constexpr double kOO = 3.749457984616480e-02;
+constexpr double dHH_intra = 1.690594510379166e+00;
+constexpr double dOH_intra = -2.999999868517452e+00;
+constexpr double dHH = 3.499031358429095e+00;
+constexpr double dOH = 4.854042963514281e+00;
+constexpr double dOO = 4.816312044947604e-08;
+enum { Oa = 0, Ha1 = 3, Ha2 = 6, Ob = 9, Hb1 = 12, Hb2 = 15, Oc = 18, Hc1 = 21, Hc2 = 24 };
+struct V { double k, r0; int a1, a2; };
+// SOURCE/mbpol-3b-poly.cpp:170-206
+__device__ constexpr V kV[36] = {
+    {kHH_intra, dHH_intra, Ha1, Ha2}, {kHH_intra, dHH_intra, Hb1, Hb2}, {kHH_intra, dHH_intra, Hc1, Hc2},
+    {kOH_intra, dOH_intra, Oa, Ha1},  {kOH_intra, dOH_intra, Oa, Ha2},  {kOH_intra, dOH_intra, Ob, Hb1},
+    {kOH_intra, dOH_intra, Ob, Hb2},  {kOH_intra, dOH_intra, Oc, Hc1},  {kOH_intra, dOH_intra, Oc, Hc2},
+    {kHH, dHH, Ha1, Hb1}, {kHH, dHH, Ha1, Hb2}, {kHH, dHH, Ha1, Hc1}, {kHH, dHH, Ha1, Hc2},
+    {kHH, dHH, Ha2, Hb1}, {kHH, dHH, Ha2, Hb2}, {kHH, dHH, Ha2, Hc1}, {kHH, dHH, Ha2, Hc2},
+    {kHH, dHH, Hb1, Hc1}, {kHH, dHH, Hb1, Hc2}, {kHH, dHH, Hb2, Hc1}, {kHH, dHH, Hb2, Hc2},
+    {kOH, dOH, Oa, Hb1},  {kOH, dOH, Oa, Hb2},  {kOH, dOH, Oa, Hc1},  {kOH, dOH, Oa, Hc2},
+    {kOH, dOH, Ob, Ha1},  {kOH, dOH, Ob, Ha2},  {kOH, dOH, Ob, Hc1},  {kOH, dOH, Ob, Hc2},
+    {kOH, dOH, Oc, Ha1},  {kOH, dOH, Oc, Ha2},  {kOH, dOH, Oc, Hb1},  {kOH, dOH, Oc, Hb2},
+    {kOO, dOO, Oa, Ob},   {kOO, dOO, Oa, Oc},   {kOO, dOO, Ob, Oc},
+};
+}  // namespace m3b
+
+// x3b_v2x_p::operator() on the 27 trimer coordinates; gradients ADDED to gt.
+template <typename T>
+__device__ __forceinline__ T model_3b(const T* t, T* gt) {
+    T x[36], fk[36];
+#pragma unroll
+    for (int q = 0; q < 36; ++q) {
+        const m3b::V d = m3b::kV[q];
+        const T dx = t[d.a1] - t[d.a2], dy = t[d.a1 + 1] - t[d.a2 + 1], dz = t[d.a1 + 2] - t[d.a2 + 2];
+        const T r = t_sqrt(dx * dx + dy * dy + dz * dz);
+        const T e = t_exp(-T(d.k) * (r - T(d.r0)));
+        x[q] = e;
+        fk[q] = -T(d.k) * e / r;   // g_intra/g_main factor without the polynomial gradient
+    }
+    T acc[37];
+#pragma unroll
+    for (int q = 0; q < 37; ++q) acc[q] = T(0);
+    poly3b<T>(x, acc);
+    T retval = acc[0];
+    T rab[3], rac[3], rbc[3];
+    T drab = T(0), drac = T(0), drbc = T(0);
+#pragma unroll
+    for (int n = 0; n < 3; ++n) {
+        rab[n] = t[m3b::Oa + n] - t[m3b::Ob + n];
+        drab += rab[n] * rab[n];
+        rac[n] = t[m3b::Oa + n] - t[m3b::Oc + n];
+        drac += rac[n] * rac[n];
+        rbc[n] = t[m3b::Ob + n] - t[m3b::Oc + n];
+        drbc += rbc[n] * rbc[n];
+    }
+    drab = t_sqrt(drab);
+    drac = t_sqrt(drac);
+    drbc = t_sqrt(drbc);
+    T gab, gac, gbc;
+    const T sab = f_switch(drab, T(0), T(kR3f), gab);
+    const T sac = f_switch(drac, T(0), T(kR3f), gac);
+    const T sbc = f_switch(drbc, T(0), T(kR3f), gbc);
+    const T s = sab * sac + sab * sbc + sac * sbc;
+#pragma unroll
+    for (int q = 0; q < 36; ++q) {
+        const m3b::V d = m3b::kV[q];
+        const T gg = (acc[1 + q] * s) * fk[q];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const T dd = t[d.a1 + c] - t[d.a2 + c];
+            gt[d.a1 + c] += gg * dd;
+            gt[d.a2 + c] -= gg * dd;
+        }
+    }
+    gab *= (sac + sbc) * retval / drab;
+    gac *= (sab + sbc) * retval / drac;
+    gbc *= (sab + sac) * retval / drbc;
+    retval *= s;
+#pragma unroll
+    for (int n = 0; n < 3; ++n) {
+        gt[m3b::Oa + n] += gab * rab[n] + gac * rac[n];
+        gt[m3b::Ob + n] += gbc * rbc[n] - gab * rab[n];
+        gt[m3b::Oc + n] -= gac * rac[n] + gbc * rbc[n];
+    }
+    return retval;
+}
+
+// ---------------------------------------------------------------------------
+// Cluster bookkeeping shared by 2B and 3B: forces, per-atom energy, virial,
+// stress (do_dimer :574-667, do_trimer :967-1071) and the exact heat-current share.
+template <int NA>
+__device__ __forceinline__ void cluster_accumulate(const MbpolArgs& a, const int* at, double e_kcal,
+                                                   const double* w, const double* g_kcal, double* red) {
+    const double e = e_kcal * kEngUnit;
+    red[0] += e;
+    if (a.ae) {
+        const double ea = (1.0 / NA) * e_kcal * kEngUnit;
+#pragma unroll
+        for (int q = 0; q < NA; ++q) atomicAdd(a.ae + at[q], ea);
+    }
+    if (a.vx) {
+        double rs[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+        for (int q = 0; q < NA; ++q) {
+            rs[0] += a.x[at[q]];
+            rs[1] += a.y[at[q]];
+            rs[2] += a.z[at[q]];
+        }
+#pragma unroll
+        for (int q = 0; q < NA; ++q) {
+            const int i = at[q];
+            const double f0 = -((1.0 / NA) * g_kcal[3 * q + 0]) * kEngUnit;
+            const double f1 = -((1.0 / NA) * g_kcal[3 * q + 1]) * kEngUnit;
+            const double f2 = -((1.0 / NA) * g_kcal[3 * q + 2]) * kEngUnit;
+            const double fv = f0 * a.vx[i] + f1 * a.vy[i] + f2 * a.vz[i];
+            red[11] += fv * (NA * a.x[i] - rs[0]);
+            red[12] += fv * (NA * a.y[i] - rs[1]);
+            red[13] += fv * (NA * a.z[i] - rs[2]);
+        }
+    }
+    double sv[6] = {0, 0, 0, 0, 0, 0};
+#pragma unroll
+    for (int q = 0; q < NA; ++q) {
+        const double g0 = g_kcal[3 * q] * kEngUnit, g1 = g_kcal[3 * q + 1] * kEngUnit,
+                     g2 = g_kcal[3 * q + 2] * kEngUnit;
+        const double w0 = w[3 * q], w1 = w[3 * q + 1], w2 = w[3 * q + 2];
+        red[1] += w0 * g0 + w1 * g1 + w2 * g2;
+        sv[0] += w0 * g0;
+        sv[1] += w0 * g1;
+        sv[2] += w0 * g2;
+        sv[3] += w1 * g1;
+        sv[4] += w1 * g2;
+        sv[5] += w2 * g2;
+        atomicAdd(a.fx + at[q], -g0);
+        atomicAdd(a.fy + at[q], -g1);
+        atomicAdd(a.fz + at[q], -g2);
+    }
+    red[2] -= sv[0]; red[3] -= sv[1]; red[4] -= sv[2];
+    red[5] -= sv[1]; red[6] -= sv[3]; red[7] -= sv[4];
+    red[8] -= sv[2]; red[9] -= sv[4]; red[10] -= sv[5];
+}
+
+// Reduce red[14] = {E, vir, stress[9], jpot[3]} of the block into acc.
+__device__ __forceinline__ void flush_block(double (&red)[14], double* acc, int eslot) {
+    __shared__ double sh[kThreads / 32][14];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int q = 0; q < 14; ++q) {
+        const double s = warp_sum(red[q]);
+        if (lane == 0) sh[w][q] = s;
+    }
+    __syncthreads();
+    if (threadIdx.x < 14) {
+        double s = 0.0;
+        for (int i = 0; i < kThreads / 32; ++i) s += sh[i][threadIdx.x];
+        const int q = threadIdx.x;
+        const int slot = q == 0 ? eslot : (q == 1 ? S_VIR : (q <= 10 ? S_STRESS + (q - 2) : S_JPOT + (q - 11)));
+        if (s != 0.0) atomicAdd(acc + slot, s);
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_mbpol_2b(MbpolArgs a, const int2* __restrict__ pairs, int n) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    double red[14];
+#pragma unroll
+    for (int q = 0; q < 14; ++q) red[q] = 0.0;
+    if (t < n) {
+        const int i = pairs[t].x, j = pairs[t].y;
+        double w1[9], w2[9];
+#pragma unroll
+        for (int q = 0; q < 9; ++q) {
+            w1[q] = a.mono[9 * (size_t)i + q];
+            w2[q] = a.mono[9 * (size_t)j + q];
+        }
+        double r12[3];
+        dist2_img(a.cell, w1, w2, r12);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            w1[3 + k] = dadd(dsub(w1[3 + k], w1[k]), dadd(w2[k], r12[k]));
+            w1[6 + k] = dadd(dsub(w1[6 + k], w1[k]), dadd(w2[k], r12[k]));
+            w1[k] = dadd(w2[k], r12[k]);
+        }
+        // working frame: absolute for FP64, shifted to the second O for FP32
+        T p1[9], p2[9], g1[9], g2[9];
+        double w[18];
+#pragma unroll
+        for (int q = 0; q < 9; ++q) {
+            const double o = (sizeof(T) == 8) ? 0.0 : w2[q % 3];
+            w[q] = w1[q] - o;
+            w[9 + q] = w2[q] - o;
+            p1[q] = (T)w[q];
+            p2[q] = (T)w[9 + q];
+        }
+        const T e = model_2b<T>(p1, p2, g1, g2);
+        const int o1 = a.list[3 * i] - 1, o2 = a.list[3 * j] - 1;
+        const int at[6] = {o1, o1 + 1, o1 + 2, o2, o2 + 1, o2 + 2};
+        double g[18];
+#pragma unroll
+        for (int q = 0; q < 9; ++q) {
+            g[q] = (double)g1[q];
+            g[9 + q] = (double)g2[q];
+        }
+        cluster_accumulate<6>(a, at, (double)e, w, g, red);
+    }
+    flush_block(red, a.acc, S_E2);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_mbpol_3b(MbpolArgs a, const int4* __restrict__ trip, int n) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    double red[14];
+#pragma unroll
+    for (int q = 0; q < 14; ++q) red[q] = 0.0;
+    if (t < n) {
+        const int4 c = trip[t];
+        double w1[9], w2[9], w3[9];
+#pragma unroll
+        for (int q = 0; q < 9; ++q) {
+            w1[q] = a.mono[9 * (size_t)c.x + q];
+            w2[q] = a.mono[9 * (size_t)c.y + q];
+            w3[q] = a.mono[9 * (size_t)c.z + q];
+        }
+        double r12[3], r23[3];
+        dist2_img(a.cell, w1, w2, r12);
+        dist2_img(a.cell, w2, w3, r23);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            w1[3 + k] = dadd(dsub(w1[3 + k], w1[k]), dadd(w2[k], r12[k]));
+            w1[6 + k] = dadd(dsub(w1[6 + k], w1[k]), dadd(w2[k], r12[k]));
+            w1[k] = dadd(w2[k], r12[k]);
+            w3[3 + k] = dadd(dsub(w3[3 + k], w3[k]), dsub(w2[k], r23[k]));
+            w3[6 + k] = dadd(dsub(w3[6 + k], w3[k]), dsub(w2[k], r23[k]));
+            w3[k] = dsub(w2[k], r23[k]);
+        }
+        T p[27], gt[27];
+        double w[27];
+#pragma unroll
+        for (int q = 0; q < 9; ++q) {
+            const double o = (sizeof(T) == 8) ? 0.0 : w2[q % 3];
+            w[q] = w1[q] - o;
+            w[9 + q] = w2[q] - o;
+            w[18 + q] = w3[q] - o;
+        }
+#pragma unroll
+        for (int q = 0; q < 27; ++q) {
+            p[q] = (T)w[q];
+            gt[q] = T(0);
+        }
+        const T e = model_3b<T>(p, gt);
+        const int o1 = a.list[3 * c.x] - 1, o2 = a.list[3 * c.y] - 1, o3 = a.list[3 * c.z] - 1;
+        const int at[9] = {o1, o1 + 1, o1 + 2, o2, o2 + 1, o2 + 2, o3, o3 + 1, o3 + 2};
+        double g[27];
+#pragma unroll
+        for (int q = 0; q < 27; ++q) g[q] = (double)gt[q];
+        cluster_accumulate<9>(a, at, (double)e, w, g, red);
+    }
+    flush_block(red, a.acc, S_E3);
+}
+
+// Per-call model evaluation (drop-in for mbpol_2b_poly_/mbpol_3b_poly_ over many clusters).
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_2b_direct(int n, const double* __restrict__ w1s,
+                                                         const double* __restrict__ w2s, double* E, double* g1s,
+                                                         double* g2s) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    T p1[9], p2[9], g1[9], g2[9];
+#pragma unroll
+    for (int q = 0; q < 9; ++q) {
+        const double o = (sizeof(T) == 8) ? 0.0 : w2s[9 * (size_t)t + q % 3];
+        p1[q] = (T)(w1s[9 * (size_t)t + q] - o);
+        p2[q] = (T)(w2s[9 * (size_t)t + q] - o);
+    }
+    E[t] = (double)model_2b<T>(p1, p2, g1, g2);
+#pragma unroll
+    for (int q = 0; q < 9; ++q) {
+        g1s[9 * (size_t)t + q] = (double)g1[q];
+        g2s[9 * (size_t)t + q] = (double)g2[q];
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_3b_direct(int n, const double* __restrict__ w1s,
+                                                         const double* __restrict__ w2s,
+                                                         const double* __restrict__ w3s, double* E, double* g1s,
+                                                         double* g2s, double* g3s) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    T p[27], gt[27];
+#pragma unroll
+    for (int q = 0; q < 9; ++q) {
+        const double o = (sizeof(T) == 8) ? 0.0 : w2s[9 * (size_t)t + q % 3];
+        p[q] = (T)(w1s[9 * (size_t)t + q] - o);
+        p[9 + q] = (T)(w2s[9 * (size_t)t + q] - o);
+        p[18 + q] = (T)(w3s[9 * (size_t)t + q] - o);
+    }
+#pragma unroll
+    for (int q = 0; q < 27; ++q) gt[q] = T(0);
+    E[t] = (double)model_3b<T>(p, gt);
+#pragma unroll
+    for (int q = 0; q < 9; ++q) {  // accumulate like the reference (SOURCE/mbpol-3b-poly.cpp:39-42)
+        g1s[9 * (size_t)t + q] += (double)gt[q];
+        g2s[9 * (size_t)t + q] += (double)gt[9 + q];
+        g3s[9 * (size_t)t + q] += (double)gt[18 + q];
+    }
+}
+
+__global__ void __launch_bounds__(kThreads) k_jkin(int n, const double* __restrict__ vx,
+                                                    const double* __restrict__ vy, const double* __restrict__ vz,
+                                                    const double* __restrict__ mass, const double* __restrict__ ae,
+                                                    double* acc) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double j[3] = {0.0, 0.0, 0.0};
+    if (i < n) {
+        const double v0 = vx[i], v1 = vy[i], v2 = vz[i];
+        const double kin = 0.5 * mass[i] * (v0 * v0 + v1 * v1 + v2 * v2);
+        const double eng = kin + (ae ? ae[i] : 0.0);
+        j[0] = eng * v0;
+        j[1] = eng * v1;
+        j[2] = eng * v2;
+    }
+    __shared__ double sh[kThreads / 32][3];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+        const double s = warp_sum(j[q]);
+        if (lane == 0) sh[w][q] = s;
+    }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        double s = 0.0;
+        for (int k = 0; k < kThreads / 32; ++k) s += sh[k][threadIdx.x];
+        atomicAdd(acc + S_JKIN + threadIdx.x, s);
+    }
+}
+
+static int blocks(int n) { return (n + kThreads - 1) / kThreads; }
+
+cudaError_t launch_2b(const MbpolArgs& a, const int2* pairs, int n, int precision, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    if (precision == 0) k_mbpol_2b<double><<<blocks(n), kThreads, 0, s>>>(a, pairs, n);
+    else k_mbpol_2b<float><<<blocks(n), kThreads, 0, s>>>(a, pairs, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_3b(const MbpolArgs& a, const int4* trip, int n, int precision, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    if (precision == 0) k_mbpol_3b<double><<<blocks(n), kThreads, 0, s>>>(a, trip, n);
+    else k_mbpol_3b<float><<<blocks(n), kThreads, 0, s>>>(a, trip, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_2b_direct(int n, const double* w1, const double* w2, double* E, double* g1, double* g2,
+                             int precision, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    if (precision == 0) k_2b_direct<double><<<blocks(n), kThreads, 0, s>>>(n, w1, w2, E, g1, g2);
+    else k_2b_direct<float><<<blocks(n), kThreads, 0, s>>>(n, w1, w2, E, g1, g2);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_3b_direct(int n, const double* w1, const double* w2, const double* w3, double* E, double* g1,
+                             double* g2, double* g3, int precision, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    if (precision == 0) k_3b_direct<double><<<blocks(n), kThreads, 0, s>>>(n, w1, w2, w3, E, g1, g2, g3);
+    else k_3b_direct<float><<<blocks(n), kThreads, 0, s>>>(n, w1, w2, w3, E, g1, g2, g3);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_jkin(int n, const double* vx, const double* vy, const double* vz, const double* mass,
+                        const double* ae, double* acc, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    k_jkin<<<blocks(n), kThreads, 0, s>>>(n, vx, vy, vz, mass, ae, acc);
+    return cudaGetLastError();
+}
+
+}  // namespace mbx

@@ -1,0 +1,237 @@
+"""Generate the MB-pol polynomial kernels as PTX (value + gradient).
+
+Input: a monomial table written by extract_poly_tables.py (E(x) = sum over
+monomials of a[k] * prod x[v]).  Output: one PTX module per chunk, each with one
+relocatable device function  f(const T* x, T* acc)  that adds its share of
+[E, dE/dx_0 .. dE/dx_{nv-1}] into acc, plus a module holding the coefficient
+arrays and a C++ header declaring the functions.  The functions are linked into
+the fused per-cluster kernels (relocatable device code), so a whole cluster
+evaluation -- variables, polynomial, chain rule, accumulation -- is one launch.
+
+Evaluation scheme.  The monomials (sorted variable-index tuples) form a prefix
+tree.  Walking it depth first, a node p carries the product pi_p of the variables
+on its path (its adjoint) and returns S_p, the sum of its subtree divided by pi_p:
+
+    S_p   = a_p + sum_{child j} x_j * S_{p+j}
+    dE/dx_j += pi_p * S_{p+j}               for every edge p -> p+j
+
+so the value costs one FMA per edge and the gradient one more; leaves (S = a) need
+no product at all.  Everything lives in registers: x[], the gradient
+accumulators, and one (pi, S) pair per tree level (degree <= 4).  The root's
+children are split into chunks of similar cost so that ptxas compiles them in
+parallel and each kernel stays small.
+
+Coefficients sit in a .const array (ptxas folds them into FMA operands), so the
+code has no immediates to materialise and no spills.
+"""
+import os
+import struct
+import sys
+
+
+def read_table(path):
+    coef, monos = [], []
+    n_vars = None
+    with open(path) as f:
+        for line in f:
+            if line.startswith("# n_vars"):
+                n_vars = int(line.split()[2])
+            elif line[0] == "C":
+                _, k, a = line.split()
+                assert int(k) == len(coef)
+                coef.append(float(a))
+            elif line[0] == "M":
+                parts = line.split()
+                monos.append((int(parts[1]), tuple(int(v) for v in parts[2:])))
+    return n_vars, coef, monos
+
+
+class Node:
+    __slots__ = ("ch", "k")
+
+    def __init__(self):
+        self.ch = {}
+        self.k = None     # coefficient index of the monomial ending here
+
+
+def build_trie(monos):
+    root = Node()
+    for k, m in monos:
+        n = root
+        for v in m:
+            n = n.ch.setdefault(v, Node())
+        n.k = k
+    return root
+
+
+def cost(node):
+    c = 0
+    for ch in node.ch.values():
+        c += 2 if not ch.ch else 3 + cost(ch)
+    return c
+
+
+def split_root(root, nchunks):
+    """Greedy balance of the root's children by op count."""
+    items = sorted(((cost_child(root.ch[v]), v) for v in root.ch), reverse=True)
+    bins = [[0, []] for _ in range(nchunks)]
+    for c, v in items:
+        b = min(bins, key=lambda x: x[0])
+        b[0] += c
+        b[1].append(v)
+    return [sorted(b[1]) for b in bins if b[1]]
+
+
+def cost_child(ch):
+    return 2 if not ch.ch else 3 + cost(ch)
+
+
+def _hex(val, f64):
+    if f64:
+        return "0x%016X" % struct.unpack("<Q", struct.pack("<d", val))[0]
+    return "0x%08X" % struct.unpack("<I", struct.pack("<f", val))[0]
+
+
+def coef_symbol(body, prec):
+    return "MBX_COEF_%s_%s" % (body.upper(), prec.upper())
+
+
+def emit_coef_module(tables):
+    """One module holding every coefficient array (the .const bank is shared)."""
+    out = ["// generated by gen_poly_ptx.py -- do not edit",
+           ".version 8.8\n.target sm_103a\n.address_size 64\n"]
+    for body, coef in tables:
+        for prec in ("f64", "f32"):
+            f64 = prec == "f64"
+            vals = ",".join(_hex(c, f64) for c in coef)
+            out.append(".visible .const .align %d .b%d %s[%d] = {%s};"
+                       % (8 if f64 else 4, 64 if f64 else 32, coef_symbol(body, prec), len(coef), vals))
+    return "\n".join(out) + "\n"
+
+
+def emit_chunk(name, body_name, n_vars, coef, root, top_vars, f64):
+    """A device function  name(const T* x, T* acc):  acc[0] += E_chunk, acc[1+j] += dE_chunk/dx_j."""
+    prec = "f64" if f64 else "f32"
+    ty = prec
+    sz = 8 if f64 else 4
+    zero = "0d0000000000000000" if f64 else "0f00000000"
+    sym = coef_symbol(body_name, prec)
+    body = []
+    used = set()
+
+    def cref(k):
+        return "[%s+%d]" % (sym, sz * k)
+
+    def walk(node, pi, d):
+        S = "%%S%d" % d
+        if node.k is not None:
+            body.append("ld.const.%s %s, %s;" % (ty, S, cref(node.k)))
+        else:
+            body.append("mov.%s %s, %s;" % (ty, S, zero))
+        for j in sorted(node.ch):
+            ch = node.ch[j]
+            used.add(j)
+            if not ch.ch:
+                body.append("ld.const.%s %%c, %s;" % (ty, cref(ch.k)))
+                body.append("fma.rn.%s %s, %%x%d, %%c, %s;" % (ty, S, j, S))
+                body.append("fma.rn.%s %%g%d, %s, %%c, %%g%d;" % (ty, j, pi, j))
+            else:
+                pic = "%%P%d" % (d + 1)
+                body.append("mul.rn.%s %s, %s, %%x%d;" % (ty, pic, pi, j))
+                walk(ch, pic, d + 1)
+                body.append("fma.rn.%s %s, %%x%d, %%S%d, %s;" % (ty, S, j, d + 1, S))
+                body.append("fma.rn.%s %%g%d, %s, %%S%d, %%g%d;" % (ty, j, pi, d + 1, j))
+
+    body.append("mov.%s %%S0, %s;" % (ty, zero))
+    for j in top_vars:
+        ch = root.ch[j]
+        used.add(j)
+        if not ch.ch:
+            body.append("ld.const.%s %%c, %s;" % (ty, cref(ch.k)))
+            body.append("fma.rn.%s %%S0, %%x%d, %%c, %%S0;" % (ty, j))
+            body.append("add.rn.%s %%g%d, %%g%d, %%c;" % (ty, j, j))
+        else:
+            walk(ch, "%%x%d" % j, 1)
+            body.append("fma.rn.%s %%S0, %%x%d, %%S1, %%S0;" % (ty, j))
+            body.append("add.rn.%s %%g%d, %%g%d, %%S1;" % (ty, j, j))
+
+    out = ["// generated by gen_poly_ptx.py -- do not edit",
+           ".version 8.8\n.target sm_103a\n.address_size 64\n",
+           ".extern .const .align %d .b%d %s[%d];" % (sz, 8 * sz, sym, len(coef)),
+           ".visible .func %s(.param .b64 px, .param .b64 pacc)\n{" % name,
+           " .reg .%s %%x<%d>, %%g<%d>, %%S<6>, %%P<6>, %%c, %%t;" % (ty, n_vars, n_vars),
+           " .reg .b64 %rd<3>;",
+           " ld.param.u64 %rd1, [px];",
+           " ld.param.u64 %rd2, [pacc];"]
+    for j in sorted(used):
+        out.append(" ld.%s %%x%d, [%%rd1+%d];" % (ty, j, sz * j))
+        out.append(" mov.%s %%g%d, %s;" % (ty, j, zero))
+    out.extend(" " + l for l in body)
+    out.append(" ld.%s %%t, [%%rd2+0]; add.rn.%s %%t, %%t, %%S0; st.%s [%%rd2+0], %%t;" % (ty, ty, ty))
+    for j in sorted(used):
+        off = sz * (j + 1)
+        out.append(" ld.%s %%t, [%%rd2+%d]; add.rn.%s %%t, %%t, %%g%d; st.%s [%%rd2+%d], %%t;"
+                   % (ty, off, ty, j, ty, off))
+    out.append(" ret;\n}")
+    return "\n".join(out) + "\n"
+
+
+# chunk counts: enough to keep every ptxas job short (they run in parallel)
+CHUNKS = {"2b": {"f64": 2, "f32": 4}, "3b": {"f64": 6, "f32": 12}}
+
+
+def _write_if_changed(path, text):
+    if os.path.exists(path):
+        with open(path) as f:
+            if f.read() == text:
+                return
+    with open(path, "w") as f:
+        f.write(text)
+
+
+def generate(table_dir, out_dir):
+    """Write the PTX modules and the C++ header that declares/dispatches them.
+
+    Returns the list of PTX paths to compile."""
+    os.makedirs(out_dir, exist_ok=True)
+    made = []
+    tables = []
+    decls = ["// generated by gen_poly_ptx.py -- do not edit", "#pragma once", ""]
+    disp = []
+    for body in ("2b", "3b"):
+        n_vars, coef, monos = read_table(os.path.join(table_dir, "poly%s.tbl" % body))
+        tables.append((body, coef))
+        root = build_trie(monos)
+        for prec in ("f64", "f32"):
+            ctype = "double" if prec == "f64" else "float"
+            chunks = split_root(root, CHUNKS[body][prec])
+            names = []
+            for c, top in enumerate(chunks):
+                name = "mbx_poly%s_%s_c%d" % (body, prec, c)
+                text = emit_chunk(name, body, n_vars, coef, root, top, prec == "f64")
+                path = os.path.join(out_dir, name + ".ptx")
+                _write_if_changed(path, text)
+                made.append(path)
+                names.append(name)
+                decls.append('extern "C" __device__ void %s(const %s* x, %s* acc);' % (name, ctype, ctype))
+            disp.append("template <> __device__ __forceinline__ void poly%s<%s>(const %s* x, %s* acc) {"
+                        % (body, ctype, ctype, ctype))
+            disp.extend("    %s(x, acc);" % n for n in names)
+            disp.append("}")
+        decls.append("constexpr int kPoly%sVars = %d;" % (body.upper(), n_vars))
+    path = os.path.join(out_dir, "mbx_poly_coef.ptx")
+    _write_if_changed(path, emit_coef_module(tables))
+    made.append(path)
+    hdr = decls + ["", "template <typename T> __device__ void poly2b(const T* x, T* acc);",
+                   "template <typename T> __device__ void poly3b(const T* x, T* acc);"] + disp
+    _write_if_changed(os.path.join(out_dir, "mbx_poly_gen.cuh"), "\n".join(hdr) + "\n")
+    return made
+
+
+def chunk_counts():
+    return {b: dict(v) for b, v in CHUNKS.items()}
+
+
+if __name__ == "__main__":
+    for path in generate(sys.argv[1], sys.argv[2]):
+        print(path)

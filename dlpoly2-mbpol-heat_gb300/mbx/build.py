@@ -1,0 +1,111 @@
+"""Build libmbx.so (sm_103a) in-tree, and the CPU oracle used by the tests.
+
+Steps: generate the polynomial PTX modules from the committed monomial tables,
+compile every PTX module and CUDA source as relocatable device code in parallel,
+then device-link everything into one shared library.  Outputs go to
+``<package>/_build`` (git-ignored).  Nothing here needs a GPU.
+"""
+import os
+import shutil
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+PKG = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+REPO = os.path.dirname(PKG)
+BUILD = os.path.join(PKG, "_build")
+CSRC = os.path.join(PKG, "csrc")
+LIB = os.path.join(BUILD, "libmbx.so")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+CUDA_SOURCES = ["mbx_lists.cu", "mbx_mbpol.cu", "mbx_capi.cu"]
+HEADERS = ["mbx_common.cuh", "mbx_kernels.cuh"]
+
+
+def _nvcc():
+    for cand in (os.environ.get("NVCC"), shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and os.path.exists(cand):
+            return cand
+    raise RuntimeError("nvcc not found")
+
+
+def _newer(target, deps):
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    return any(os.path.getmtime(d) > t for d in deps if os.path.exists(d))
+
+
+def _run(cmd):
+    r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("command failed: %s\n%s" % (" ".join(cmd), r.stdout))
+    return r.stdout
+
+
+def _check_stamp():
+    """Objects from another machine (x86 here, aarch64 on the GPU hosts) are discarded."""
+    import platform
+    stamp = os.path.join(BUILD, "PLATFORM")
+    me = platform.machine() + " " + _run([_nvcc(), "--version"]).strip().splitlines()[-1]
+    if os.path.isdir(BUILD):
+        old = open(stamp).read() if os.path.exists(stamp) else ""
+        if old != me:
+            shutil.rmtree(BUILD)
+    os.makedirs(BUILD, exist_ok=True)
+    with open(stamp, "w") as f:
+        f.write(me)
+
+
+def build_lib(verbose=False, jobs=None):
+    _check_stamp()
+    sys.path.insert(0, os.path.join(PKG, "gen"))
+    import gen_poly_ptx  # noqa: E402
+
+    gen_dir = os.path.join(BUILD, "gen")
+    os.makedirs(gen_dir, exist_ok=True)
+    ptx = gen_poly_ptx.generate(os.path.join(PKG, "tables"), gen_dir)
+    nvcc = _nvcc()
+    common = ARCH + ["-Xcompiler", "-fPIC", "-rdc=true"]
+    jobs_list = []
+    for p in ptx:
+        o = p[:-4] + ".o"
+        if _newer(o, [p]):
+            jobs_list.append((o, [nvcc] + common + ["-c", p, "-o", o]))
+    hdr_deps = [os.path.join(CSRC, h) for h in HEADERS] + [os.path.join(gen_dir, "mbx_poly_gen.cuh"),
+                                                          os.path.join(REPO, "include", "mbx.h")]
+    cu_objs = []
+    for src in CUDA_SOURCES:
+        s = os.path.join(CSRC, src)
+        o = os.path.join(BUILD, src.replace(".cu", ".o"))
+        cu_objs.append(o)
+        if _newer(o, [s] + hdr_deps):
+            jobs_list.append((o, [nvcc] + common + ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr",
+                                                    "-I", CSRC, "-I", gen_dir, "-c", s, "-o", o]))
+    jobs = jobs or max(2, os.cpu_count() or 2)
+    with ThreadPoolExecutor(max_workers=jobs) as ex:
+        outs = list(ex.map(lambda j: _run(j[1]), jobs_list))
+    if verbose:
+        for o in outs:
+            if o.strip():
+                print(o)
+    objs = cu_objs + [p[:-4] + ".o" for p in ptx]
+    if _newer(LIB, objs):
+        _run([nvcc] + ARCH + ["-shared", "-rdc=true", "-Xcompiler", "-fPIC", "-o", LIB] + objs)
+    return LIB
+
+
+def build_oracle(with_reference=None):
+    """Compile the oracle (and, when the reference tree exists, its C++ polynomials)."""
+    odir = os.path.join(REPO, "oracle")
+    _run(["make", "-s", "-C", odir])
+    ref = "/root/reference/SOURCE"
+    if with_reference is None:
+        with_reference = os.path.isdir(ref)
+    if with_reference:
+        _run(["make", "-s", "-C", odir, "ref", "REFSRC=" + ref])
+    return os.path.join(odir, "liboracle.so")
+
+
+if __name__ == "__main__":
+    print(build_lib(verbose=True))
+    print(build_oracle())

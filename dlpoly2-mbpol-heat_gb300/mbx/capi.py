@@ -1,0 +1,188 @@
+"""ctypes binding of libmbx.so (include/mbx.h) -- the host-side mirror of the
+reference's mbpol_forces interface.
+
+There is no CPU fallback: if the library is missing, or no sm_103 GPU is present,
+every call raises.
+"""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+REPO = os.path.dirname(PKG)
+LIB_PATH = os.path.join(PKG, "_build", "libmbx.so")
+HEADER = os.path.join(REPO, "include", "mbx.h")
+
+FP64 = 0
+MIXED = 1
+NSCALARS = 18
+S_ENG2, S_ENG3, S_VIR, S_STRESS, S_JPOT, S_JKIN = 0, 1, 2, 3, 12, 15
+
+_D = C.POINTER(C.c_double)
+_I = C.POINTER(C.c_int)
+_L = C.POINTER(C.c_long)
+_lib = None
+
+
+class MbxError(RuntimeError):
+    pass
+
+
+def header_functions():
+    """Names of every function declared in include/mbx.h."""
+    with open(HEADER) as f:
+        text = f.read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return re.findall(r"^\s*(?:int|void|const char\*)\s+\**\s*(\w+)\s*\(", text, flags=re.M)
+
+
+def load(path=None):
+    """Load libmbx.so and declare its prototypes (no GPU needed)."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    path = path or LIB_PATH
+    if not os.path.exists(path):
+        raise MbxError("libmbx.so not built (%s); run __graft_entry__.build()" % path)
+    L = C.CDLL(path)
+    L.mbx_create.argtypes = [C.POINTER(C.c_void_p), C.c_int]
+    L.mbx_destroy.argtypes = [C.c_void_p]
+    L.mbx_destroy.restype = None
+    L.mbx_error.argtypes = [C.c_void_p]
+    L.mbx_error.restype = C.c_char_p
+    L.mbx_set_stream.argtypes = [C.c_void_p, C.c_void_p]
+    L.mbx_mbpol_forces.argtypes = [C.c_void_p, C.c_int, C.c_int, _D, C.c_int, _I, C.c_int, _D, _D, _D, _D, _D, _D,
+                                   _D, _D, _D, _D, _D, _D, _D, _D, _D]
+    L.mbx_mbpol_forces_device.argtypes = [C.c_void_p, C.c_int, C.c_int, _D, C.c_int, C.c_void_p, C.c_int,
+                                          C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                          C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, _D]
+    L.mbx_set_profiling.argtypes = [C.c_void_p, C.c_int]
+    L.mbx_last_timings.argtypes = [C.c_void_p, _D, _L]
+    L.mbx_last_lists.argtypes = [C.c_void_p, _I, C.c_long, _L, _I, C.c_long, _L]
+    L.mbx_2b_poly_batch.argtypes = [C.c_void_p, C.c_int, C.c_long, _D, _D, _D, _D, _D]
+    L.mbx_3b_poly_batch.argtypes = [C.c_void_p, C.c_int, C.c_long, _D, _D, _D, _D, _D, _D, _D]
+    L.mbpol_2b_poly_.argtypes = [_D] * 6
+    L.mbpol_2b_poly_.restype = None
+    L.mbpol_3b_poly_.argtypes = [_D] * 8
+    L.mbpol_3b_poly_.restype = None
+    L.mbpol_2b_cutoff_.argtypes = [_D]
+    L.mbpol_2b_cutoff_.restype = None
+    L.mbpol_3b_cutoff_.argtypes = [_D]
+    L.mbpol_3b_cutoff_.restype = None
+    if path == LIB_PATH:
+        _lib = L
+    return L
+
+
+def _p(a, t=_D):
+    return None if a is None else a.ctypes.data_as(t)
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+class Context:
+    """One libmbx context (own CUDA stream and device buffers)."""
+
+    def __init__(self, device=0):
+        self.lib = load()
+        h = C.c_void_p()
+        rc = self.lib.mbx_create(C.byref(h), device)
+        if rc:
+            raise MbxError("mbx_create failed with status %d" % rc)
+        self.h = h
+
+    def close(self):
+        if self.h:
+            self.lib.mbx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc, what):
+        if rc:
+            raise MbxError("%s: status %d: %s" % (what, rc, self.lib.mbx_error(self.h).decode()))
+
+    def set_stream(self, stream_ptr):
+        self._check(self.lib.mbx_set_stream(self.h, C.c_void_p(stream_ptr)), "mbx_set_stream")
+
+    def mbpol_forces(self, box, precision=FP64, heat=True, atomic_energy=True):
+        """mbpol_forces on a WaterBox (host arrays).  Returns a dict like the oracle's."""
+        n = box.natms
+        x, y, z = (_f64(box.xyz[:, k]) for k in range(3))
+        f = np.zeros((3, n))
+        eng = C.c_double(0)
+        vir = C.c_double(0)
+        stress = np.zeros(9)
+        ae = np.zeros(n) if atomic_energy else None
+        sc = np.zeros(NSCALARS)
+        v = [_f64(box.vel[:, k]) for k in range(3)] if heat else [None] * 3
+        m = _f64(box.mass) if heat else None
+        lst = np.ascontiguousarray(box.listttm2(), dtype=np.int32)
+        rc = self.lib.mbx_mbpol_forces(self.h, precision, box.imcon, _p(_f64(box.cell)), 3 * box.nw, _p(lst, _I), n,
+                                       _p(x), _p(y), _p(z), _p(f[0]), _p(f[1]), _p(f[2]), C.byref(eng),
+                                       C.byref(vir), _p(stress), _p(v[0]), _p(v[1]), _p(v[2]), _p(m), _p(ae),
+                                       _p(sc))
+        self._check(rc, "mbx_mbpol_forces")
+        out = dict(eng2=sc[S_ENG2], eng3=sc[S_ENG3], vir=sc[S_VIR], stress=sc[S_STRESS:S_STRESS + 9].copy(),
+                   forces=f.T.copy(), atomic_energy=ae, jpot=sc[S_JPOT:S_JPOT + 3].copy(),
+                   jkin=sc[S_JKIN:S_JKIN + 3].copy(), engsrp=eng.value, virsrp=vir.value, stress_acc=stress)
+        return out
+
+    def mbpol_forces_device(self, precision, imcon, cell, nttm2, list_ptr, natms, xyz_ptrs, f_ptrs, v_ptrs=None,
+                            mass_ptr=None, ae_ptr=None):
+        """Device-pointer entry point (pointers as ints); returns the scalars."""
+        sc = np.zeros(NSCALARS)
+        v_ptrs = v_ptrs or (None, None, None)
+        rc = self.lib.mbx_mbpol_forces_device(self.h, precision, imcon, _p(_f64(cell)), nttm2, list_ptr, natms,
+                                              *xyz_ptrs, *f_ptrs, *v_ptrs, mass_ptr, ae_ptr, _p(sc))
+        self._check(rc, "mbx_mbpol_forces_device")
+        return sc
+
+    def set_profiling(self, on=True):
+        self._check(self.lib.mbx_set_profiling(self.h, 1 if on else 0), "mbx_set_profiling")
+
+    def last_timings(self):
+        """(phase ms [lists, 2B, 3B, jkin], (dimers, trimers, launches))"""
+        ms = np.zeros(4)
+        cnt = (C.c_long * 3)()
+        self._check(self.lib.mbx_last_timings(self.h, _p(ms), cnt), "mbx_last_timings")
+        return ms, (cnt[0], cnt[1], cnt[2])
+
+    def last_lists(self):
+        npairs = C.c_long(0)
+        ntrip = C.c_long(0)
+        self._check(self.lib.mbx_last_lists(self.h, None, 0, C.byref(npairs), None, 0, C.byref(ntrip)),
+                    "mbx_last_lists")
+        pairs = np.zeros(2 * max(npairs.value, 1), np.int32)
+        trip = np.zeros(3 * max(ntrip.value, 1), np.int32)
+        self._check(self.lib.mbx_last_lists(self.h, _p(pairs, _I), npairs.value, C.byref(npairs), _p(trip, _I),
+                                            ntrip.value, C.byref(ntrip)), "mbx_last_lists")
+        return pairs[:2 * npairs.value].reshape(-1, 2), trip[:3 * ntrip.value].reshape(-1, 3)
+
+    def poly2b_batch(self, W1, W2, precision=FP64):
+        W1 = _f64(W1).reshape(-1, 9)
+        W2 = _f64(W2).reshape(-1, 9)
+        n = W1.shape[0]
+        E = np.zeros(n)
+        g1 = np.zeros((n, 9))
+        g2 = np.zeros((n, 9))
+        self._check(self.lib.mbx_2b_poly_batch(self.h, precision, n, _p(W1), _p(W2), _p(E), _p(g1), _p(g2)),
+                    "mbx_2b_poly_batch")
+        return E, g1, g2
+
+    def poly3b_batch(self, W1, W2, W3, precision=FP64, g=None):
+        W = [_f64(w).reshape(-1, 9) for w in (W1, W2, W3)]
+        n = W[0].shape[0]
+        E = np.zeros(n)
+        gs = [np.zeros((n, 9)) for _ in range(3)] if g is None else [_f64(a).reshape(-1, 9).copy() for a in g]
+        self._check(self.lib.mbx_3b_poly_batch(self.h, precision, n, *(_p(w) for w in W), _p(E),
+                                               *(_p(a) for a in gs)), "mbx_3b_poly_batch")
+        return (E, *gs)

@@ -1,0 +1,122 @@
+"""Seeded synthetic water boxes (the benchmark workloads).
+
+A box is built the way the benchmark configurations describe it: O atoms on a
+jittered cubic lattice (the first ``nw`` sites of an ``m**3`` lattice filling the
+box), each molecule at the rigid MB-pol-like geometry (OH 0.9572 A, HOH 104.52 deg)
+with a uniformly random orientation, then Gaussian noise (sigma 0.02 A) on every
+atom, and Maxwell-Boltzmann velocities.  The site layout is DL_POLY's for pure
+TTM/MB-pol water: atoms 0..3nw-1 are (O, H1, H2) per molecule, then the nw M
+sites (SOURCE/ttm2list.f:20-77); M sites start at the O position.
+
+Units are DL_POLY's: Angstrom, ps, amu, 10 J/mol.
+"""
+import math
+
+import numpy as np
+
+BOLTZ = 0.831451115          # SOURCE/dl_params.inc:64, 10 J/mol/K
+MASS_O = 15.9994
+MASS_H = 1.00794
+R_OH = 0.9572
+THETA_HOH = math.radians(104.52)
+LATTICE_JITTER = 0.10         # A, uniform half-width of the lattice jitter
+
+
+def _random_rotations(rng, n):
+    q = rng.normal(size=(n, 4))
+    q /= np.linalg.norm(q, axis=1, keepdims=True)
+    w, x, y, z = q.T
+    return np.stack([
+        np.stack([1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w)], -1),
+        np.stack([2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w)], -1),
+        np.stack([2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)], -1),
+    ], 1)
+
+
+class WaterBox:
+    """Positions/velocities of one periodic water box in DL_POLY site order."""
+
+    def __init__(self, nw, L, xyz, vel, seed):
+        self.nw = nw
+        self.L = float(L)
+        self.cell = np.array([L, 0, 0, 0, L, 0, 0, 0, L], dtype=np.float64)
+        self.imcon = 1
+        self.xyz = xyz          # (4*nw, 3)
+        self.vel = vel          # (4*nw, 3)
+        self.seed = seed
+
+    @property
+    def natms(self):
+        return 4 * self.nw
+
+    @property
+    def mass(self):
+        m = np.zeros(self.natms)
+        m[0:3 * self.nw:3] = MASS_O
+        m[1:3 * self.nw:3] = MASS_H
+        m[2:3 * self.nw:3] = MASS_H
+        return m
+
+    def listttm2(self):
+        """1-based atom indices of the water atoms (O,H1,H2 per molecule)."""
+        return np.arange(1, 3 * self.nw + 1, dtype=np.int32)
+
+    def monomers(self):
+        return np.ascontiguousarray(self.xyz[:3 * self.nw].reshape(self.nw, 9))
+
+
+def water_box(nw, L, seed, lattice=None, sigma=0.02, temperature=298.0, jitter=LATTICE_JITTER):
+    rng = np.random.default_rng(seed)
+    if lattice is None:
+        lattice = int(math.ceil(nw ** (1.0 / 3.0) - 1e-9))
+    a = L / lattice
+    g = np.arange(lattice)
+    sites = np.stack(np.meshgrid(g, g, g, indexing="ij"), -1).reshape(-1, 3)[:nw]
+    O = (sites + 0.5) * a + rng.uniform(-jitter, jitter, size=(nw, 3))
+    half = 0.5 * THETA_HOH
+    body = np.array([[0.0, 0.0, 0.0],
+                     [R_OH * math.sin(half), 0.0, R_OH * math.cos(half)],
+                     [-R_OH * math.sin(half), 0.0, R_OH * math.cos(half)]])
+    R = _random_rotations(rng, nw)
+    mol = O[:, None, :] + np.einsum("nij,aj->nai", R, body)
+    mol += rng.normal(scale=sigma, size=mol.shape)
+    xyz = np.zeros((4 * nw, 3))
+    xyz[:3 * nw] = mol.reshape(-1, 3)
+    xyz[3 * nw:] = mol[:, 0, :]
+    mass = np.zeros(4 * nw)
+    mass[0:3 * nw:3] = MASS_O
+    mass[1:3 * nw:3] = MASS_H
+    mass[2:3 * nw:3] = MASS_H
+    vel = np.zeros((4 * nw, 3))
+    s = np.sqrt(BOLTZ * temperature / mass[:3 * nw])
+    vel[:3 * nw] = rng.normal(size=(3 * nw, 3)) * s[:, None]
+    vel[:3 * nw] -= (mass[:3 * nw, None] * vel[:3 * nw]).sum(0) / mass[:3 * nw].sum()
+    return WaterBox(nw, L, xyz, vel, seed)
+
+
+def config0(seed=20240):
+    """256 H2O, L = 19.73 A (0.997 g/cm^3), jittered 7^3 lattice."""
+    return water_box(256, 19.73, seed, lattice=7)
+
+
+def config1(seed=20241):
+    """4096 H2O, L = 49.70 A, jittered 16^3 lattice."""
+    return water_box(4096, 49.70, seed, lattice=16)
+
+
+def box_for(nw, seed, density=0.997):
+    """A box of nw waters at the given density (g/cm^3), lattice as small as fits."""
+    mw = 18.01528
+    L = (nw * mw / (density * 0.6022140857)) ** (1.0 / 3.0)
+    return water_box(nw, L, seed)
+
+
+def beads_from(box, nbeads, sigma, seed):
+    """Path-integral-like replicas: copies of ``box`` with independent Gaussian noise."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for b in range(nbeads):
+        xyz = box.xyz.copy()
+        xyz[:3 * box.nw] += rng.normal(scale=sigma, size=(3 * box.nw, 3))
+        out.append(WaterBox(box.nw, box.L, xyz, box.vel.copy(), (box.seed, b)))
+    return out

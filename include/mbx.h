@@ -1,0 +1,128 @@
+/*
+ * libmbx -- GB300-native MB-pol force and heat-current path.
+ *
+ * C ABI: plain pointers and sizes, no C++ types, no exceptions across the
+ * boundary.  Every entry point returns an int status (MBX_OK = 0) unless it is a
+ * drop-in for a reference symbol whose signature returns void.
+ *
+ * Units and layouts follow the reference DL_POLY 2 fork: Angstrom, DL_POLY
+ * internal energy units (10 J/mol; 418.4 per kcal/mol), per-atom arrays in
+ * structure-of-arrays form (xxx, yyy, zzz), water atoms 1..3*nw in (O, H1, H2)
+ * triples located through the 1-based `listttm2` array, M sites after them.
+ *
+ * Precision modes: MBX_FP64 reproduces the reference's FP64 arithmetic;
+ * MBX_MIXED evaluates each dimer/trimer in FP32 and accumulates forces,
+ * energies, virial, stress and heat current in FP64.
+ */
+#ifndef MBX_H
+#define MBX_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MBX_FP64 0
+#define MBX_MIXED 1
+
+#define MBX_OK 0
+#define MBX_ERR_ARG 1           /* invalid argument (null pointer, bad size, bad imcon) */
+#define MBX_ERR_CUDA 2          /* a CUDA call failed; see mbx_error() */
+#define MBX_ERR_CAPACITY 3      /* a list outgrew the largest capacity the context allows */
+#define MBX_ERR_NO_DEVICE 4     /* no CUDA device, or the device is not an sm_103 part */
+
+/* Scalar outputs of one evaluation (indices into the `scalars` array). */
+#define MBX_S_ENG2 0            /* MB-pol 2B energy (internal units) */
+#define MBX_S_ENG3 1            /* MB-pol 3B energy */
+#define MBX_S_VIR 2             /* virial: sum over clusters of w . dE/dw */
+#define MBX_S_STRESS 3          /* 9 stress components, DL_POLY order (3..11) */
+#define MBX_S_JPOT 12           /* heat current, potential part jpot (12..14) */
+#define MBX_S_JKIN 15           /* heat current, kinetic+energy part jkin (15..17) */
+#define MBX_NSCALARS 18
+
+typedef struct mbx_context mbx_context;
+
+/* Create a context on CUDA device `device` (its own stream and buffers). */
+int mbx_create(mbx_context** ctx, int device);
+void mbx_destroy(mbx_context* ctx);
+/* Last error message of the context (never NULL). */
+const char* mbx_error(const mbx_context* ctx);
+/* Use the caller's CUDA stream (a cudaStream_t passed as void*; NULL = the context's own). */
+int mbx_set_stream(mbx_context* ctx, void* stream);
+
+/* Time each phase of later evaluations with CUDA events on the context's stream. */
+int mbx_set_profiling(mbx_context* ctx, int on);
+/* Phase times of the last evaluation in ms: [0] lists, [1] 2B kernel, [2] 3B kernel,
+ * [3] heat-current jkin (or -1 when profiling is off); counts: [0] dimers, [1] trimers,
+ * [2] kernel launches issued.  Either pointer may be NULL. */
+int mbx_last_timings(mbx_context* ctx, double* ms, long* counts);
+
+/*
+ * MB-pol 2B + 3B forces with the heat-current bookkeeping.
+ * Replaces mbpol_forces (SOURCE/mbpol.f90:98-449, called from SOURCE/dlpoly_cmd.f:2504)
+ * together with the HEAT_CURRENT hooks of do_dimer / do_trimer
+ * (SOURCE/mbpol.f90:515-556, :897-952) and compute_heat_flux2's jkin/jpot sums
+ * (SOURCE/heatcurrent.f90:703-728) for the MB-pol terms.
+ *
+ * HOST arrays (copied to and from the device inside the call):
+ *   imcon, cell[9]          DL_POLY boundary key (1 cubic, 2 orthorhombic, 3 parallelepiped)
+ *   nttm2, listttm2[nttm2]  water atoms (nttm2 = 3*nw), 1-based indices, O first
+ *   natms                   length of every per-atom array
+ *   xxx,yyy,zzz             positions
+ *   fxx,fyy,fzz             forces, ACCUMULATED (like mbpol_forces)
+ *   engsrp, virsrp          ACCUMULATED with eng2+eng3 and the virial
+ *   stress[9]               ACCUMULATED
+ *   vxx,vyy,vzz,weight      velocities and masses for the heat current, or all NULL
+ *   atomic_energy           per-atom MB-pol energy, ACCUMULATED, or NULL
+ *   scalars[MBX_NSCALARS]   this call's totals (see MBX_S_*), or NULL
+ */
+int mbx_mbpol_forces(mbx_context* ctx, int precision, int imcon, const double* cell, int nttm2,
+                     const int* listttm2, int natms, const double* xxx, const double* yyy, const double* zzz,
+                     double* fxx, double* fyy, double* fzz, double* engsrp, double* virsrp, double* stress,
+                     const double* vxx, const double* vyy, const double* vzz, const double* weight,
+                     double* atomic_energy, double* scalars);
+
+/*
+ * The same evaluation on DEVICE-resident arrays (no host copies of per-atom data;
+ * the call returns after the scalars are on the host).  listttm2 is a device array.
+ * fxx.. and atomic_energy are ACCUMULATED on the device.
+ */
+int mbx_mbpol_forces_device(mbx_context* ctx, int precision, int imcon, const double* cell, int nttm2,
+                            const int* listttm2, int natms, const double* xxx, const double* yyy,
+                            const double* zzz, double* fxx, double* fyy, double* fzz, const double* vxx,
+                            const double* vyy, const double* vzz, const double* weight, double* atomic_energy,
+                            double* scalars);
+
+/* Dimer and trimer lists of the last evaluation (0-based water indices, i<j<k), as
+ * index sets; the host arrays receive up to cap entries; counts are always written. */
+int mbx_last_lists(mbx_context* ctx, int* pairs, long cap_pairs, long* npairs, int* trimers, long cap_trimers,
+                   long* ntrimers);
+
+/*
+ * Batched model evaluation for explicit clusters (host arrays, 9 doubles per monomer,
+ * O H1 H2, already imaged; kcal/mol and Angstrom like the reference's C++).
+ * mbx_2b_poly_batch ASSIGNS g1/g2; mbx_3b_poly_batch ACCUMULATES into g1..g3, as
+ * x2b_v6x_p / x3b_v2x_p do (SOURCE/mbpol-2b-poly.cpp:609-612, SOURCE/mbpol-3b-poly.cpp:39-42).
+ */
+int mbx_2b_poly_batch(mbx_context* ctx, int precision, long n, const double* w1, const double* w2, double* E,
+                      double* g1, double* g2);
+int mbx_3b_poly_batch(mbx_context* ctx, int precision, long n, const double* w1, const double* w2,
+                      const double* w3, double* E, double* g1, double* g2, double* g3);
+
+/*
+ * Drop-ins for the reference's per-cluster C entry points, same signatures and
+ * meaning (SOURCE/mbpol-2b-poly.cpp:1884-1904, SOURCE/mbpol-3b-poly.cpp:1522-1542).
+ * They run one FP64 evaluation on the current CUDA device through a process-wide
+ * context.  The reference's optional `force_matrix` decomposition (used only
+ * under HEAT_STRESS) is not produced: the array is left untouched.
+ * On a CUDA error they print a message and abort (the reference has no error path).
+ */
+void mbpol_2b_poly_(const double* w1, const double* w2, double* E, double* g1, double* g2, double* force_matrix);
+void mbpol_3b_poly_(const double* w1, const double* w2, const double* w3, double* E, double* g1, double* g2,
+                    double* g3, double* force_matrix);
+void mbpol_2b_cutoff_(double* r);
+void mbpol_3b_cutoff_(double* r);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MBX_H */

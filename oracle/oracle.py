@@ -1,0 +1,152 @@
+"""ctypes binding of the CPU oracle (test infrastructure; see oracle.h).
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use this.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(HERE)
+TABLES = os.path.join(REPO, "dlpoly2-mbpol-heat_gb300", "tables")
+
+_D = C.POINTER(C.c_double)
+_I = C.POINTER(C.c_int)
+_L = C.POINTER(C.c_long)
+
+
+def _p(a, t=_D):
+    return None if a is None else a.ctypes.data_as(t)
+
+
+class Oracle:
+    def __init__(self, path=None):
+        path = path or os.path.join(HERE, "liboracle.so")
+        if not os.path.exists(path):
+            raise FileNotFoundError("oracle library missing: %s (run make -C oracle)" % path)
+        self.lib = C.CDLL(path)
+        L = self.lib
+        L.orc_load_tables.argtypes = [C.c_char_p, C.c_char_p]
+        for f in ("orc_poly2b", "orc_poly3b", "orc_poly2b_naive", "orc_poly3b_naive"):
+            getattr(L, f).argtypes = [_D, _D]
+            getattr(L, f).restype = C.c_double
+        L.orc_2b.argtypes = [_D, _D, _D, _D]
+        L.orc_2b.restype = C.c_double
+        L.orc_3b.argtypes = [_D, _D, _D, _D, _D, _D]
+        L.orc_3b.restype = C.c_double
+        L.orc_2b_vars.argtypes = [_D, _D, _D]
+        L.orc_3b_vars.argtypes = [_D, _D, _D, _D]
+        L.orc_image_monomers.argtypes = [C.c_int, _D, C.c_int, _D]
+        L.orc_mbpol_forces.argtypes = [C.c_int, _D, C.c_int, _I] + [_D] * 15 + [C.c_int, C.c_int, _I, C.c_long, _L, _I, C.c_long, _L,
+                                       C.c_int]
+        L.orc_mbpol_forces.restype = C.c_int
+        for f in ("orc_trimer_sample", "orc_dimer_sample"):
+            getattr(L, f).argtypes = [C.c_int, _D, C.c_int, _D, _I, C.c_long, C.c_int]
+            getattr(L, f).restype = C.c_double
+        L.orc_mbpol_ranks.argtypes = [C.c_int, _D, C.c_int, _I, _D, _D, _D, C.c_int, C.c_int, C.c_int, C.c_int,
+                                      C.c_int]
+        L.orc_mbpol_ranks.restype = C.c_double
+        rc = L.orc_load_tables(os.path.join(TABLES, "poly2b.tbl").encode(),
+                               os.path.join(TABLES, "poly3b.tbl").encode())
+        if rc:
+            raise RuntimeError("orc_load_tables failed: %d" % rc)
+
+    # -- polynomials / models -------------------------------------------------
+    def poly(self, body, x, naive=False):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        g = np.zeros_like(x)
+        f = getattr(self.lib, "orc_poly%s%s" % (body, "_naive" if naive else ""))
+        return f(_p(x), _p(g)), g
+
+    def model2b(self, w1, w2):
+        w1 = np.ascontiguousarray(w1, np.float64)
+        w2 = np.ascontiguousarray(w2, np.float64)
+        g1 = np.zeros(9)
+        g2 = np.zeros(9)
+        e = self.lib.orc_2b(_p(w1), _p(w2), _p(g1), _p(g2))
+        return e, g1, g2
+
+    def model3b(self, w1, w2, w3):
+        w = [np.ascontiguousarray(v, np.float64) for v in (w1, w2, w3)]
+        g = [np.zeros(9) for _ in range(3)]
+        e = self.lib.orc_3b(_p(w[0]), _p(w[1]), _p(w[2]), _p(g[0]), _p(g[1]), _p(g[2]))
+        return e, g[0], g[1], g[2]
+
+    def vars2b(self, w1, w2):
+        v = np.zeros(31)
+        self.lib.orc_2b_vars(_p(np.ascontiguousarray(w1, np.float64)), _p(np.ascontiguousarray(w2, np.float64)),
+                             _p(v))
+        return v
+
+    def vars3b(self, w1, w2, w3):
+        v = np.zeros(36)
+        w = [np.ascontiguousarray(u, np.float64) for u in (w1, w2, w3)]
+        self.lib.orc_3b_vars(_p(w[0]), _p(w[1]), _p(w[2]), _p(v))
+        return v
+
+    # -- driver ---------------------------------------------------------------
+    def mbpol_forces(self, box, dense=False, velocities=True, lists=False, nthreads=1):
+        """mbpol_forces + heat bookkeeping on a WaterBox; returns a dict."""
+        n = box.natms
+        x = np.ascontiguousarray(box.xyz[:, 0])
+        y = np.ascontiguousarray(box.xyz[:, 1])
+        z = np.ascontiguousarray(box.xyz[:, 2])
+        f = np.zeros((3, n))
+        ae = np.zeros(n)
+        e2 = C.c_double(0)
+        e3 = C.c_double(0)
+        vir = C.c_double(0)
+        stress = np.zeros(9)
+        jpot = np.zeros(3)
+        v = [np.ascontiguousarray(box.vel[:, k]) for k in range(3)] if velocities else [None] * 3
+        lst = box.listttm2()
+        nw = box.nw
+        cap_p = nw * 80 if lists else 0
+        cap_t = nw * 400 if lists else 0
+        pairs = np.zeros(2 * max(cap_p, 1), np.int32) if lists else None
+        trip = np.zeros(3 * max(cap_t, 1), np.int32) if lists else None
+        npairs = C.c_long(0)
+        ntrip = C.c_long(0)
+        rc = self.lib.orc_mbpol_forces(box.imcon, _p(box.cell), nw, _p(lst, _I), _p(x), _p(y), _p(z),
+                                       _p(f[0]), _p(f[1]), _p(f[2]), C.byref(e2), C.byref(e3), C.byref(vir),
+                                       _p(stress), _p(ae), _p(v[0]), _p(v[1]), _p(v[2]), _p(jpot),
+                                       1 if dense else 0, n, _p(pairs, _I), cap_p, C.byref(npairs),
+                                       _p(trip, _I), cap_t, C.byref(ntrip), nthreads)
+        if rc:
+            raise RuntimeError("orc_mbpol_forces: list capacity exceeded")
+        out = dict(eng2=e2.value, eng3=e3.value, vir=vir.value, stress=stress, forces=f.T.copy(),
+                   atomic_energy=ae, jpot=jpot, npairs=npairs.value, ntrip=ntrip.value)
+        if lists:
+            out["pairs"] = pairs[:2 * npairs.value].reshape(-1, 2).copy()
+            out["trimers"] = trip[:3 * ntrip.value].reshape(-1, 3).copy()
+        if velocities:
+            m = box.mass
+            vel = box.vel
+            kin = 0.5 * m * (vel * vel).sum(1)
+            eng = kin[:3 * nw] + ae[:3 * nw]
+            out["jkin"] = (eng[:, None] * vel[:3 * nw]).sum(0)
+        return out
+
+    def sample(self, body, box, monomers, lst, nthreads):
+        lst = np.ascontiguousarray(lst, dtype=np.int32)
+        f = self.lib.orc_trimer_sample if body == 3 else self.lib.orc_dimer_sample
+        n = lst.shape[0]
+        return f(box.imcon, _p(box.cell), box.nw, _p(np.ascontiguousarray(monomers, np.float64)),
+                 _p(lst, _I), n, nthreads)
+
+    def ranks(self, box, rank_begin, rank_end, size, nthreads):
+        """Energy of ranks [rank_begin, rank_end) of a `size`-rank split (CPU baseline work)."""
+        x, y, z = (np.ascontiguousarray(box.xyz[:, k]) for k in range(3))
+        lst = np.ascontiguousarray(box.listttm2(), dtype=np.int32)
+        return self.lib.orc_mbpol_ranks(box.imcon, _p(box.cell), box.nw, _p(lst, _I), _p(x), _p(y), _p(z),
+                                        box.natms, rank_begin, rank_end, size, nthreads)
+
+    def image_monomers(self, box):
+        m = box.monomers().copy()
+        self.lib.orc_image_monomers(box.imcon, _p(box.cell), box.nw, _p(m))
+        return m
+
+
+def load(path=None):
+    return Oracle(path)

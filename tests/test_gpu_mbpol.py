@@ -1,0 +1,198 @@
+"""GPU parity of libmbx against the oracle (FP64: 1e-10; mixed: the stated budgets)."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from conftest import rel_err
+from mbx import capi, systems
+
+pytestmark = pytest.mark.gpu
+
+# FP64 path tolerance (relative to the array's largest magnitude)
+TOL64 = 1e-10
+# mixed path budgets: force RMS error and heat-current error, relative
+TOL_MIXED_FORCE_RMS = 1e-5
+TOL_MIXED_HEAT = 1e-6
+
+
+def _as_set(a):
+    return set(map(tuple, np.asarray(a).tolist()))
+
+
+def _boxes():
+    return {
+        "cfg0_256": systems.config0(),
+        "small_64_allpairs": systems.box_for(64, seed=5),
+        "ortho_imcon2": _ortho(),
+        "shuffled_layout": _shuffled(),
+    }
+
+
+def _ortho():
+    b = systems.water_box(216, 19.5, seed=9, lattice=6)
+    b.xyz[:, 1] *= 1.05
+    b.xyz[:, 2] *= 0.97
+    b.cell = np.array([19.5, 0, 0, 0, 19.5 * 1.05, 0, 0, 0, 19.5 * 0.97])
+    b.imcon = 2
+    return b
+
+
+def _shuffled():
+    b = systems.box_for(128, seed=21)
+    rng = np.random.default_rng(2)
+    perm = rng.permutation(b.nw)
+    w = b.xyz[:3 * b.nw].reshape(b.nw, 3, 3)[perm].reshape(-1, 3)
+    v = b.vel[:3 * b.nw].reshape(b.nw, 3, 3)[perm].reshape(-1, 3)
+    b.xyz[:3 * b.nw] = w
+    b.vel[:3 * b.nw] = v
+    # molecules also wrapped into the box by O (atoms may straddle the boundary)
+    shift = np.floor(b.xyz[0:3 * b.nw:3] / b.L) * b.L
+    b.xyz[:3 * b.nw] -= np.repeat(shift, 3, axis=0)
+    return b
+
+
+BOXES = _boxes()
+
+
+@pytest.fixture(scope="module")
+def refs(oracle_lib):
+    return {k: oracle_lib.mbpol_forces(b, lists=True) for k, b in BOXES.items()}
+
+
+@pytest.mark.parametrize("name", list(BOXES))
+def test_fp64_matches_oracle(mbx_ctx, refs, name):
+    box = BOXES[name]
+    ref = refs[name]
+    got = mbx_ctx.mbpol_forces(box, precision=capi.FP64)
+    pairs, trip = mbx_ctx.last_lists()
+    assert _as_set(pairs) == _as_set(ref["pairs"])
+    assert _as_set(np.sort(trip, axis=1)) == _as_set(ref["trimers"])
+    assert len(trip) == len(ref["trimers"])
+    for k in ("eng2", "eng3", "vir"):
+        assert abs(got[k] - ref[k]) <= TOL64 * abs(ref[k]), k
+    assert rel_err(got["stress"], ref["stress"]) <= TOL64
+    assert rel_err(got["forces"], ref["forces"]) <= TOL64
+    assert rel_err(got["atomic_energy"], ref["atomic_energy"]) <= TOL64
+    assert rel_err(got["jpot"], ref["jpot"]) <= TOL64
+    assert rel_err(got["jkin"], ref["jkin"]) <= TOL64
+    # accumulate semantics of the mbpol_forces interface
+    assert abs(got["engsrp"] - (ref["eng2"] + ref["eng3"])) <= TOL64 * abs(ref["eng2"] + ref["eng3"])
+
+
+@pytest.mark.parametrize("name", ["cfg0_256", "shuffled_layout"])
+def test_mixed_within_budget(mbx_ctx, refs, name):
+    box = BOXES[name]
+    ref = refs[name]
+    got = mbx_ctx.mbpol_forces(box, precision=capi.MIXED)
+    f, fr = got["forces"], ref["forces"]
+    rms = np.sqrt(np.mean((f - fr) ** 2) / np.mean(fr ** 2))
+    assert rms <= TOL_MIXED_FORCE_RMS, rms
+    jt = got["jpot"] + got["jkin"]
+    jr = ref["jpot"] + ref["jkin"]
+    assert np.linalg.norm(jt - jr) <= TOL_MIXED_HEAT * np.linalg.norm(jr)
+    e, er = got["eng2"] + got["eng3"], ref["eng2"] + ref["eng3"]
+    assert abs(e - er) <= 1e-6 * abs(er)
+
+
+def test_models_fp64_and_mixed_vs_reference_golden(mbx_ctx, golden):
+    W2 = golden["W2"]
+    E, g1, g2 = mbx_ctx.poly2b_batch(W2[:, 0], W2[:, 1], precision=capi.FP64)
+    scale = np.maximum(np.abs(golden["E2"]), 1.0)
+    assert np.all(np.abs(E - golden["E2"]) <= 1e-10 * scale)
+    G = np.concatenate([g1, g2], 1)
+    GR = golden["G2"].reshape(len(W2), 18)
+    assert np.all(np.abs(G - GR).max(1) <= 1e-10 * np.maximum(np.abs(GR).max(1), 1.0))
+    W3 = golden["W3"]
+    E3, h1, h2, h3 = mbx_ctx.poly3b_batch(W3[:, 0], W3[:, 1], W3[:, 2], precision=capi.FP64)
+    assert np.all(np.abs(E3 - golden["E3"]) <= 1e-10 * np.maximum(np.abs(golden["E3"]), 1.0))
+    G3 = np.concatenate([h1, h2, h3], 1)
+    GR3 = golden["G3"].reshape(len(W3), 27)
+    assert np.all(np.abs(G3 - GR3).max(1) <= 1e-10 * np.maximum(np.abs(GR3).max(1), 1.0))
+    # mixed: FP32 per cluster
+    Em, _, _ = mbx_ctx.poly2b_batch(W2[:, 0], W2[:, 1], precision=capi.MIXED)
+    assert np.all(np.abs(Em - golden["E2"]) <= 1e-4 * scale)
+    E3m, *_ = mbx_ctx.poly3b_batch(W3[:, 0], W3[:, 1], W3[:, 2], precision=capi.MIXED)
+    assert np.all(np.abs(E3m - golden["E3"]) <= 1e-4 * np.maximum(np.abs(golden["E3"]), 1.0))
+
+
+def test_3b_batch_accumulates_into_gradients(mbx_ctx, golden):
+    W3 = golden["W3"][:8]
+    g0 = [np.full((8, 9), 0.25) for _ in range(3)]
+    E, a, b, c = mbx_ctx.poly3b_batch(W3[:, 0], W3[:, 1], W3[:, 2], g=g0)
+    assert np.allclose(np.concatenate([a, b, c], 1) - 0.25, golden["G3"][:8].reshape(8, 27), rtol=0, atol=1e-9)
+
+
+def test_dropin_symbols(golden):
+    lib = capi.load()
+    D = C.POINTER(C.c_double)
+    w1 = np.ascontiguousarray(golden["W2"][0, 0])
+    w2 = np.ascontiguousarray(golden["W2"][0, 1])
+    e = C.c_double(0)
+    g1 = np.zeros(9)
+    g2 = np.zeros(9)
+    fm = np.zeros(108)
+    lib.mbpol_2b_poly_(w1.ctypes.data_as(D), w2.ctypes.data_as(D), C.byref(e), g1.ctypes.data_as(D),
+                       g2.ctypes.data_as(D), fm.ctypes.data_as(D))
+    assert abs(e.value - golden["E2"][0]) <= 1e-10 * max(abs(golden["E2"][0]), 1.0)
+    r = C.c_double(0)
+    lib.mbpol_2b_cutoff_(C.byref(r))
+    assert r.value == 6.5
+    lib.mbpol_3b_cutoff_(C.byref(r))
+    assert r.value == 4.5
+    W = [np.ascontiguousarray(golden["W3"][0, q]) for q in range(3)]
+    g = [np.zeros(9) for _ in range(3)]
+    lib.mbpol_3b_poly_(*(w.ctypes.data_as(D) for w in W), C.byref(e), *(a.ctypes.data_as(D) for a in g),
+                       np.zeros(243).ctypes.data_as(D))
+    assert abs(e.value - golden["E3"][0]) <= 1e-10 * max(abs(golden["E3"][0]), 1.0)
+
+
+@pytest.mark.parametrize("nw", [0, 1, 2, 3])
+def test_tiny_systems(mbx_ctx, oracle_lib, nw):
+    box = systems.water_box(max(nw, 1), 12.0, seed=4, lattice=2)
+    if nw == 0:
+        box = systems.WaterBox(0, 12.0, np.zeros((0, 3)), np.zeros((0, 3)), 0)
+    got = mbx_ctx.mbpol_forces(box)
+    if nw == 0:
+        assert got["eng2"] == 0 and got["eng3"] == 0
+        return
+    ref = oracle_lib.mbpol_forces(box)
+    assert abs(got["eng2"] - ref["eng2"]) <= TOL64 * max(abs(ref["eng2"]), 1.0)
+    assert abs(got["eng3"] - ref["eng3"]) <= TOL64 * max(abs(ref["eng3"]), 1.0)
+
+
+def test_invalid_arguments_rejected(mbx_ctx):
+    box = systems.box_for(8, seed=1)
+    box.imcon = 7
+    with pytest.raises(capi.MbxError):
+        mbx_ctx.mbpol_forces(box)
+    box.imcon = 1
+    with pytest.raises(capi.MbxError):
+        mbx_ctx.mbpol_forces(box, precision=5)
+
+
+def test_repeatable_and_lists_stable(mbx_ctx):
+    box = systems.config0(seed=77)
+    a = mbx_ctx.mbpol_forces(box)
+    pa, ta = mbx_ctx.last_lists()
+    b = mbx_ctx.mbpol_forces(box)
+    pb, tb = mbx_ctx.last_lists()
+    assert np.array_equal(pa, pb) and np.array_equal(ta, tb)
+    assert abs(a["eng3"] - b["eng3"]) <= 1e-13 * abs(a["eng3"])
+
+
+def test_full_size_properties_4096(mbx_ctx):
+    """cfg1 (4096 H2O): mixed vs FP64 budgets, energy partition and momentum conservation."""
+    box = systems.config1()
+    d = mbx_ctx.mbpol_forces(box, precision=capi.FP64)
+    m = mbx_ctx.mbpol_forces(box, precision=capi.MIXED)
+    e = d["eng2"] + d["eng3"]
+    assert abs(d["atomic_energy"].sum() - e) <= 1e-10 * abs(e)
+    assert np.max(np.abs(d["forces"].sum(0))) <= 1e-8 * np.max(np.abs(d["forces"]))
+    rms = np.sqrt(np.mean((m["forces"] - d["forces"]) ** 2) / np.mean(d["forces"] ** 2))
+    assert rms <= TOL_MIXED_FORCE_RMS, rms
+    jd = d["jpot"] + d["jkin"]
+    jm = m["jpot"] + m["jkin"]
+    assert np.linalg.norm(jm - jd) <= TOL_MIXED_HEAT * np.linalg.norm(jd)
+    _, (nd, nt, _) = mbx_ctx.last_timings()
+    assert nd > 0 and nt > 0
