@@ -97,7 +97,7 @@ def build_lib(verbose=False, jobs=None):
 def build_oracle(with_reference=None):
     """Compile the oracle (and, when the reference tree exists, its C++ polynomials)."""
     odir = os.path.join(REPO, "oracle")
-    _run(["make", "-s", "-C", odir])
+    _run(["make", "-s", "-B", "-C", odir, "liboracle.so"])
     ref = "/root/reference/SOURCE"
     if with_reference is None:
         with_reference = os.path.isdir(ref)
