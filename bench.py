@@ -205,7 +205,7 @@ def run_ours(args, rank, world):
     err_j = float(np.linalg.norm(jm - j64) / np.linalg.norm(j64))
     e64 = sc64[0] + sc64[1]
     err_e = float(abs(scm[0] + scm[1] - e64) / abs(e64))
-    _, (ndim, ntri, _) = ctx.last_timings()
+    _, (ndim, ntri, _, hard2, hard3) = ctx.last_timings()
 
     clocks = ClockSampler(dev.index)
     clocks.start()
@@ -288,6 +288,7 @@ def run_ours(args, rank, world):
         "data": DATA,
         "config": {"workload": WORKLOAD, "precision": "mixed", "parallelism": "replicas" if world > 1 else "single",
                    "l2": "flushed between steps (256 MiB write)", "dimers": int(ndim), "trimers": int(ntri),
+                   "mixed_fp64_handoff": {"dimers": int(hard2), "trimers": int(hard3)},
                    "not_yet_in_step": NOT_IN_STEP},
         "fp64": {"value": world * k64 / t_fp64, "unit": "steps/s", "ms_per_step": 1e3 * t_fp64 / k64,
                  "phase_ms": {"lists": phase64[0], "2b": phase64[1], "3b": phase64[2], "jkin": phase64[3]}},

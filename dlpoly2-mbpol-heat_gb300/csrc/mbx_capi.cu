@@ -30,6 +30,11 @@ struct mbx_context {
     long pairs_cap = 0;
     int4* trip = nullptr;
     long trip_cap = 0;
+    int2* hard2 = nullptr;          // mixed path: clusters handed to the FP64 kernels
+    int4* hard3 = nullptr;
+    int* hard_count = nullptr;      // device [2]
+    float limit2 = 1.0f, limit3 = 2.0f;
+    long hard_last[2] = {0, 0};
     long npairs = 0, ntrip = 0;
     // batch-API staging
     double* batch = nullptr;
@@ -148,16 +153,22 @@ int run_mbpol(mbx_context* ctx, int precision, const Cell& cl, int nw, const int
         const long np = ctx->totals_h[0], nt = ctx->totals_h[1];
         if (np > ctx->pairs_cap) {
             if (ctx->pairs) cudaFree(ctx->pairs);
+            if (ctx->hard2) cudaFree(ctx->hard2);
             ctx->pairs = nullptr;
+            ctx->hard2 = nullptr;
             const long cap = np + np / 4 + 64;
             CK(cudaMalloc(&ctx->pairs, cap * sizeof(int2)));
+            CK(cudaMalloc(&ctx->hard2, cap * sizeof(int2)));
             ctx->pairs_cap = cap;
         }
         if (nt > ctx->trip_cap) {
             if (ctx->trip) cudaFree(ctx->trip);
+            if (ctx->hard3) cudaFree(ctx->hard3);
             ctx->trip = nullptr;
+            ctx->hard3 = nullptr;
             const long cap = nt + nt / 4 + 64;
             CK(cudaMalloc(&ctx->trip, cap * sizeof(int4)));
+            CK(cudaMalloc(&ctx->hard3, cap * sizeof(int4)));
             ctx->trip_cap = cap;
         }
         CK(ctx->lb.phase2(nw, cl, ctx->mono, ctx->pairs, ctx->trip, s));
@@ -177,11 +188,14 @@ int run_mbpol(mbx_context* ctx, int precision, const Cell& cl, int nw, const int
         a.fx = fx; a.fy = fy; a.fz = fz;
         a.ae = ae_use;
         a.acc = ctx->acc;
-        CK(launch_2b(a, ctx->pairs, (int)np, precision, s));
+        MixedPass mp{ctx->hard2, ctx->hard3, ctx->hard_count, ctx->limit2, ctx->limit3};
+        if (precision == MBX_MIXED) CK(cudaMemsetAsync(ctx->hard_count, 0, 2 * sizeof(int), s));
+        CK(launch_2b(a, ctx->pairs, (int)np, precision, mp, s));
         if (ctx->profiling) CK(cudaEventRecord(ctx->ev[2], s));
-        CK(launch_3b(a, ctx->trip, (int)nt, precision, s));
+        CK(launch_3b(a, ctx->trip, (int)nt, precision, mp, s));
         if (ctx->profiling) CK(cudaEventRecord(ctx->ev[3], s));
-        ctx->launches += (np > 0) + (nt > 0);
+        const int passes = precision == MBX_MIXED ? 2 : 1;
+        ctx->launches += passes * ((np > 0) + (nt > 0));
     } else if (ctx->profiling) {
         for (int q = 1; q < 4; ++q) CK(cudaEventRecord(ctx->ev[q], s));
     }
@@ -191,7 +205,11 @@ int run_mbpol(mbx_context* ctx, int precision, const Cell& cl, int nw, const int
     }
     if (ctx->profiling) CK(cudaEventRecord(ctx->ev[4], s));
     CK(cudaMemcpyAsync(ctx->acc_h, ctx->acc, MBX_NSCALARS * sizeof(double), cudaMemcpyDeviceToHost, s));
+    if (precision == MBX_MIXED && nw >= 2)
+        CK(cudaMemcpyAsync(ctx->totals_h + 4, ctx->hard_count, 2 * sizeof(int), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
+    ctx->hard_last[0] = (precision == MBX_MIXED && nw >= 2) ? ctx->totals_h[4] : 0;
+    ctx->hard_last[1] = (precision == MBX_MIXED && nw >= 2) ? ctx->totals_h[5] : 0;
     if (scalars) std::memcpy(scalars, ctx->acc_h, MBX_NSCALARS * sizeof(double));
     if (ctx->profiling)
         for (int q = 0; q < 4; ++q) CK(cudaEventElapsedTime(&ctx->phase_ms[q], ctx->ev[q], ctx->ev[q + 1]));
@@ -234,7 +252,8 @@ extern "C" int mbx_create(mbx_context** out, int device) {
         ctx->stream = ctx->own_stream;
         CK(cudaMalloc(&ctx->acc, MBX_NSCALARS * sizeof(double)));
         CK(cudaMalloc(&ctx->totals, 4 * sizeof(int)));
-        CK(cudaMallocHost(&ctx->totals_h, 4 * sizeof(int)));
+        CK(cudaMalloc(&ctx->hard_count, 2 * sizeof(int)));
+        CK(cudaMallocHost(&ctx->totals_h, 8 * sizeof(int)));
         CK(cudaMallocHost(&ctx->acc_h, MBX_NSCALARS * sizeof(double)));
         return MBX_OK;
     };
@@ -253,7 +272,7 @@ extern "C" void mbx_destroy(mbx_context* ctx) {
     cudaSetDevice(ctx->device);
     if (ctx->own_stream) cudaStreamSynchronize(ctx->own_stream);
     void* dev[] = {ctx->mono, ctx->list, ctx->atoms, ctx->ae_scratch, ctx->acc, ctx->totals, ctx->pairs, ctx->trip,
-                   ctx->batch};
+                   ctx->batch, ctx->hard2, ctx->hard3, ctx->hard_count};
     for (void* p : dev)
         if (p) cudaFree(p);
     if (ctx->totals_h) cudaFreeHost(ctx->totals_h);
@@ -282,7 +301,17 @@ extern "C" int mbx_last_timings(mbx_context* ctx, double* ms, long* counts) {
         counts[0] = ctx->npairs;
         counts[1] = ctx->ntrip;
         counts[2] = ctx->launches;
+        counts[3] = ctx->hard_last[0];
+        counts[4] = ctx->hard_last[1];
     }
+    return MBX_OK;
+}
+
+extern "C" int mbx_set_mixed_limits(mbx_context* ctx, double limit2b, double limit3b) {
+    if (!ctx) return MBX_ERR_ARG;
+    if (!(limit2b >= 0.0) || !(limit3b >= 0.0)) return fail(ctx, MBX_ERR_ARG, "limits must be >= 0");
+    ctx->limit2 = (float)limit2b;
+    ctx->limit3 = (float)limit3b;
     return MBX_OK;
 }
 

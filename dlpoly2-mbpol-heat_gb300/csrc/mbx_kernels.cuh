@@ -29,9 +29,21 @@ struct MbpolArgs {
     double* acc;                     // S_NSLOTS scalars, accumulated
 };
 
+// Mixed-precision pass: FP32 kernels hand ill-conditioned clusters (a shifted
+// variable further than limit2/limit3 from its centre) to an FP64 kernel through
+// these device lists; count[0] dimers, count[1] trimers (zeroed by the caller).
+struct MixedPass {
+    int2* hard2;
+    int4* hard3;
+    int* count;
+    float limit2, limit3;
+};
+
 // Fused cluster kernels (mbx_mbpol.cu).  precision: 0 FP64, 1 mixed.
-cudaError_t launch_2b(const MbpolArgs& a, const int2* pairs, int npairs, int precision, cudaStream_t s);
-cudaError_t launch_3b(const MbpolArgs& a, const int4* trip, int ntrip, int precision, cudaStream_t s);
+cudaError_t launch_2b(const MbpolArgs& a, const int2* pairs, int npairs, int precision, const MixedPass& mp,
+                      cudaStream_t s);
+cudaError_t launch_3b(const MbpolArgs& a, const int4* trip, int ntrip, int precision, const MixedPass& mp,
+                      cudaStream_t s);
 // Isolated polynomial + model evaluation for explicit clusters (the per-call ABI).
 cudaError_t launch_2b_direct(int n, const double* w1, const double* w2, double* E, double* g1, double* g2,
                              int precision, cudaStream_t s);

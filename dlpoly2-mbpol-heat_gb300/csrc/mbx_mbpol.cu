@@ -118,9 +118,12 @@ __device__ __forceinline__ T f_switch(T r, T ri, T rf, T& g) {
 }
 
 // x2b_v6x_p::operator() on coordinates already in the working frame.
-// Returns E (kcal/mol); g1/g2 assigned.
+// Returns E (kcal/mol); g1/g2 assigned.  For T = float the polynomial is evaluated
+// in the shifted variables x - kShift2B; if any of them lies further than `limit`
+// from its centre the cluster is left to the FP64 pass (*hard = true, nothing set).
 template <typename T>
-__device__ __forceinline__ T model_2b(const T* w1, const T* w2, T* g1, T* g2) {
+__device__ __forceinline__ T model_2b(const T* w1, const T* w2, T* g1, T* g2, float limit = 0.f,
+                                      bool* hard = nullptr) {
     const T dOO[3] = {w1[0] - w2[0], w1[1] - w2[1], w1[2] - w2[2]};
     const T rOO = t_sqrt(dOO[0] * dOO[0] + dOO[1] * dOO[1] + dOO[2] * dOO[2]);
     if (rOO > T(kR2f)) {
@@ -151,6 +154,18 @@ __device__ __forceinline__ T model_2b(const T* w1, const T* w2, T* g1, T* g2) {
             const T rinv = T(1) / r;
             v[q] = e * rinv;
             gg[q] = -(T(d.k) + rinv) * v[q] * rinv;
+        }
+    }
+    if constexpr (sizeof(T) == 4) {
+        float dev = 0.f;
+#pragma unroll
+        for (int q = 0; q < 31; ++q) {
+            v[q] -= kShift2B[q];
+            dev = fmaxf(dev, fabsf(v[q]));
+        }
+        if (hard && dev > limit) {
+            *hard = true;
+            return T(0);
         }
     }
     T acc[32];
@@ -222,8 +237,9 @@ __device__ constexpr V kV[36] = {
 }  // namespace m3b
 
 // x3b_v2x_p::operator() on the 27 trimer coordinates; gradients ADDED to gt.
+// T = float: shifted variables and the FP64 hand-off, as in model_2b.
 template <typename T>
-__device__ __forceinline__ T model_3b(const T* t, T* gt) {
+__device__ __forceinline__ T model_3b(const T* t, T* gt, float limit = 0.f, bool* hard = nullptr) {
     T x[36], fk[36];
 #pragma unroll
     for (int q = 0; q < 36; ++q) {
@@ -233,6 +249,18 @@ __device__ __forceinline__ T model_3b(const T* t, T* gt) {
         const T e = t_exp(-T(d.k) * (r - T(d.r0)));
         x[q] = e;
         fk[q] = -T(d.k) * e / r;   // g_intra/g_main factor without the polynomial gradient
+    }
+    if constexpr (sizeof(T) == 4) {
+        float dev = 0.f;
+#pragma unroll
+        for (int q = 0; q < 36; ++q) {
+            x[q] -= kShift3B[q];
+            dev = fmaxf(dev, fabsf(x[q]));
+        }
+        if (hard && dev > limit) {
+            *hard = true;
+            return T(0);
+        }
     }
     T acc[37];
 #pragma unroll
@@ -356,9 +384,19 @@ __device__ __forceinline__ void flush_block(double (&red)[14], double* acc, int 
     }
 }
 
+// Mixed-precision hand-off: clusters whose FP32 variables stray beyond the limit
+// are appended to `hard` and evaluated by the FP64 kernel afterwards.
+struct HardList {
+    void* items;        // int2 (dimers) or int4 (trimers)
+    int* count;
+    float limit;
+};
+
 template <typename T>
-__global__ void __launch_bounds__(kThreads) k_mbpol_2b(MbpolArgs a, const int2* __restrict__ pairs, int n) {
+__global__ void __launch_bounds__(kThreads) k_mbpol_2b(MbpolArgs a, const int2* __restrict__ pairs, int n,
+                                                        const int* __restrict__ n_dev, HardList hl) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n_dev) n = *n_dev;
     double red[14];
 #pragma unroll
     for (int q = 0; q < 14; ++q) red[q] = 0.0;
@@ -389,23 +427,30 @@ __global__ void __launch_bounds__(kThreads) k_mbpol_2b(MbpolArgs a, const int2* 
             p1[q] = (T)w[q];
             p2[q] = (T)w[9 + q];
         }
-        const T e = model_2b<T>(p1, p2, g1, g2);
-        const int o1 = a.list[3 * i] - 1, o2 = a.list[3 * j] - 1;
-        const int at[6] = {o1, o1 + 1, o1 + 2, o2, o2 + 1, o2 + 2};
-        double g[18];
+        bool hard = false;
+        const T e = model_2b<T>(p1, p2, g1, g2, hl.limit, hl.items ? &hard : nullptr);
+        if (hard) {
+            ((int2*)hl.items)[atomicAdd(hl.count, 1)] = make_int2(i, j);
+        } else {
+            const int o1 = a.list[3 * i] - 1, o2 = a.list[3 * j] - 1;
+            const int at[6] = {o1, o1 + 1, o1 + 2, o2, o2 + 1, o2 + 2};
+            double g[18];
 #pragma unroll
-        for (int q = 0; q < 9; ++q) {
-            g[q] = (double)g1[q];
-            g[9 + q] = (double)g2[q];
+            for (int q = 0; q < 9; ++q) {
+                g[q] = (double)g1[q];
+                g[9 + q] = (double)g2[q];
+            }
+            cluster_accumulate<6>(a, at, (double)e, w, g, red);
         }
-        cluster_accumulate<6>(a, at, (double)e, w, g, red);
     }
     flush_block(red, a.acc, S_E2);
 }
 
 template <typename T>
-__global__ void __launch_bounds__(kThreads) k_mbpol_3b(MbpolArgs a, const int4* __restrict__ trip, int n) {
+__global__ void __launch_bounds__(kThreads) k_mbpol_3b(MbpolArgs a, const int4* __restrict__ trip, int n,
+                                                        const int* __restrict__ n_dev, HardList hl) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n_dev) n = *n_dev;
     double red[14];
 #pragma unroll
     for (int q = 0; q < 14; ++q) red[q] = 0.0;
@@ -444,13 +489,18 @@ __global__ void __launch_bounds__(kThreads) k_mbpol_3b(MbpolArgs a, const int4* 
             p[q] = (T)w[q];
             gt[q] = T(0);
         }
-        const T e = model_3b<T>(p, gt);
-        const int o1 = a.list[3 * c.x] - 1, o2 = a.list[3 * c.y] - 1, o3 = a.list[3 * c.z] - 1;
-        const int at[9] = {o1, o1 + 1, o1 + 2, o2, o2 + 1, o2 + 2, o3, o3 + 1, o3 + 2};
-        double g[27];
+        bool hard = false;
+        const T e = model_3b<T>(p, gt, hl.limit, hl.items ? &hard : nullptr);
+        if (hard) {
+            ((int4*)hl.items)[atomicAdd(hl.count, 1)] = c;
+        } else {
+            const int o1 = a.list[3 * c.x] - 1, o2 = a.list[3 * c.y] - 1, o3 = a.list[3 * c.z] - 1;
+            const int at[9] = {o1, o1 + 1, o1 + 2, o2, o2 + 1, o2 + 2, o3, o3 + 1, o3 + 2};
+            double g[27];
 #pragma unroll
-        for (int q = 0; q < 27; ++q) g[q] = (double)gt[q];
-        cluster_accumulate<9>(a, at, (double)e, w, g, red);
+            for (int q = 0; q < 27; ++q) g[q] = (double)gt[q];
+            cluster_accumulate<9>(a, at, (double)e, w, g, red);
+        }
     }
     flush_block(red, a.acc, S_E3);
 }
@@ -534,17 +584,31 @@ __global__ void __launch_bounds__(kThreads) k_jkin(int n, const double* __restri
 
 static int blocks(int n) { return (n + kThreads - 1) / kThreads; }
 
-cudaError_t launch_2b(const MbpolArgs& a, const int2* pairs, int n, int precision, cudaStream_t s) {
+cudaError_t launch_2b(const MbpolArgs& a, const int2* pairs, int n, int precision, const MixedPass& mp,
+                      cudaStream_t s) {
     if (n <= 0) return cudaSuccess;
-    if (precision == 0) k_mbpol_2b<double><<<blocks(n), kThreads, 0, s>>>(a, pairs, n);
-    else k_mbpol_2b<float><<<blocks(n), kThreads, 0, s>>>(a, pairs, n);
+    if (precision == 0) {
+        k_mbpol_2b<double><<<blocks(n), kThreads, 0, s>>>(a, pairs, n, nullptr, HardList{nullptr, nullptr, 0.f});
+    } else {
+        k_mbpol_2b<float><<<blocks(n), kThreads, 0, s>>>(a, pairs, n, nullptr,
+                                                         HardList{mp.hard2, mp.count + 0, mp.limit2});
+        k_mbpol_2b<double><<<blocks(n), kThreads, 0, s>>>(a, mp.hard2, n, mp.count + 0,
+                                                          HardList{nullptr, nullptr, 0.f});
+    }
     return cudaGetLastError();
 }
 
-cudaError_t launch_3b(const MbpolArgs& a, const int4* trip, int n, int precision, cudaStream_t s) {
+cudaError_t launch_3b(const MbpolArgs& a, const int4* trip, int n, int precision, const MixedPass& mp,
+                      cudaStream_t s) {
     if (n <= 0) return cudaSuccess;
-    if (precision == 0) k_mbpol_3b<double><<<blocks(n), kThreads, 0, s>>>(a, trip, n);
-    else k_mbpol_3b<float><<<blocks(n), kThreads, 0, s>>>(a, trip, n);
+    if (precision == 0) {
+        k_mbpol_3b<double><<<blocks(n), kThreads, 0, s>>>(a, trip, n, nullptr, HardList{nullptr, nullptr, 0.f});
+    } else {
+        k_mbpol_3b<float><<<blocks(n), kThreads, 0, s>>>(a, trip, n, nullptr,
+                                                         HardList{mp.hard3, mp.count + 1, mp.limit3});
+        k_mbpol_3b<double><<<blocks(n), kThreads, 0, s>>>(a, mp.hard3, n, mp.count + 1,
+                                                          HardList{nullptr, nullptr, 0.f});
+    }
     return cudaGetLastError();
 }
 

@@ -21,12 +21,53 @@ accumulators, and one (pi, S) pair per tree level (degree <= 4).  The root's
 children are split into chunks of similar cost so that ptxas compiles them in
 parallel and each kernel stays small.
 
-Coefficients sit in a .const array (ptxas folds them into FMA operands), so the
-code has no immediates to materialise and no spills.
+FP64 coefficients sit in a .const array (ptxas folds them into DFMA operands).
+The FP32 kernels evaluate the polynomial re-expanded around per-class shift
+centres (see SHIFT_CLASSES), with the coefficients as FFMA immediates.
 """
+import itertools
 import os
 import struct
 import sys
+from collections import defaultdict
+from fractions import Fraction
+
+# Shift centres of the mixed-precision (FP32) polynomials, one per variable class:
+# medians of each class over seeded synthetic water boxes (the benchmark's
+# generator), rounded to float.  E(x) is re-expanded EXACTLY (rational arithmetic)
+# in d = x - centre, which removes the large cancelling terms that the raw
+# polynomial has in FP32 (e.g. the 3B O-O variables sit near 0.86 and the intra
+# O-H ones near 2.76).  Class boundaries follow the variable order of
+# SOURCE/mbpol-2b-poly.cpp:415-445 and SOURCE/mbpol-3b-poly.cpp:170-206.
+SHIFT_CLASSES = {
+    "2b": [(0, 2, 1.39557), (2, 6, 1.07224), (6, 10, 0.0393031), (10, 14, 0.0334345), (14, 15, 0.0207425),
+           (15, 23, 0.353591), (23, 27, 0.292828), (27, 31, 0.297902)],
+    "3b": [(0, 3, 0.672721), (3, 9, 2.76008), (9, 21, 0.739614), (21, 33, 1.80399), (33, 36, 0.860788)],
+}
+
+
+def shift_centres(body):
+    out = []
+    for a, b, c in SHIFT_CLASSES[body]:
+        out += [float(struct.unpack("<f", struct.pack("<f", c))[0])] * (b - a)
+    return out
+
+
+def shifted_polynomial(monos, coef, centres):
+    """Exact re-expansion of sum_k a_k prod_v x_v in d_v = x_v - centre_v.
+
+    Returns {monomial tuple: coefficient (float64)}; () is the constant term."""
+    out = defaultdict(Fraction)
+    cen = [Fraction(c) for c in centres]
+    for k, m in monos:
+        a = Fraction(coef[k])
+        for pick in itertools.product((0, 1), repeat=len(m)):
+            f = a
+            for v, keep in zip(m, pick):
+                if not keep:
+                    f *= cen[v]
+            out[tuple(v for v, keep in zip(m, pick) if keep)] += f
+    return {m: float(c) for m, c in out.items() if c != 0}
 
 
 def read_table(path):
@@ -101,16 +142,17 @@ def emit_coef_module(tables):
     out = ["// generated by gen_poly_ptx.py -- do not edit",
            ".version 8.8\n.target sm_103a\n.address_size 64\n"]
     for body, coef in tables:
-        for prec in ("f64", "f32"):
-            f64 = prec == "f64"
-            vals = ",".join(_hex(c, f64) for c in coef)
-            out.append(".visible .const .align %d .b%d %s[%d] = {%s};"
-                       % (8 if f64 else 4, 64 if f64 else 32, coef_symbol(body, prec), len(coef), vals))
+        vals = ",".join(_hex(c, True) for c in coef)
+        out.append(".visible .const .align 8 .b64 %s[%d] = {%s};" % (coef_symbol(body, "f64"), len(coef), vals))
     return "\n".join(out) + "\n"
 
 
-def emit_chunk(name, body_name, n_vars, coef, root, top_vars, f64):
-    """A device function  name(const T* x, T* acc):  acc[0] += E_chunk, acc[1+j] += dE_chunk/dx_j."""
+def emit_chunk(name, body_name, n_vars, coef, root, top_vars, f64, const_term=0.0):
+    """A device function  name(const T* x, T* acc):  acc[0] += E_chunk, acc[1+j] += dE_chunk/dx_j.
+
+    FP64 chunks read their coefficients from the shared .const array (orbit
+    coefficients, the reference's own polynomial).  FP32 chunks evaluate the shifted
+    polynomial, whose per-monomial coefficients are FFMA immediates."""
     prec = "f64" if f64 else "f32"
     ty = prec
     sz = 8 if f64 else 4
@@ -119,22 +161,25 @@ def emit_chunk(name, body_name, n_vars, coef, root, top_vars, f64):
     body = []
     used = set()
 
-    def cref(k):
-        return "[%s+%d]" % (sym, sz * k)
+    def operand(k):
+        if f64:
+            body.append("ld.const.f64 %%c, [%s+%d];" % (sym, 8 * k))
+            return "%c"
+        return "0f%08X" % struct.unpack("<I", struct.pack("<f", coef[k]))[0]
 
     def walk(node, pi, d):
         S = "%%S%d" % d
         if node.k is not None:
-            body.append("ld.const.%s %s, %s;" % (ty, S, cref(node.k)))
+            body.append("mov.%s %s, %s;" % (ty, S, operand(node.k)))
         else:
             body.append("mov.%s %s, %s;" % (ty, S, zero))
         for j in sorted(node.ch):
             ch = node.ch[j]
             used.add(j)
             if not ch.ch:
-                body.append("ld.const.%s %%c, %s;" % (ty, cref(ch.k)))
-                body.append("fma.rn.%s %s, %%x%d, %%c, %s;" % (ty, S, j, S))
-                body.append("fma.rn.%s %%g%d, %s, %%c, %%g%d;" % (ty, j, pi, j))
+                c = operand(ch.k)
+                body.append("fma.rn.%s %s, %%x%d, %s, %s;" % (ty, S, j, c, S))
+                body.append("fma.rn.%s %%g%d, %s, %s, %%g%d;" % (ty, j, pi, c, j))
             else:
                 pic = "%%P%d" % (d + 1)
                 body.append("mul.rn.%s %s, %s, %%x%d;" % (ty, pic, pi, j))
@@ -142,27 +187,31 @@ def emit_chunk(name, body_name, n_vars, coef, root, top_vars, f64):
                 body.append("fma.rn.%s %s, %%x%d, %%S%d, %s;" % (ty, S, j, d + 1, S))
                 body.append("fma.rn.%s %%g%d, %s, %%S%d, %%g%d;" % (ty, j, pi, d + 1, j))
 
-    body.append("mov.%s %%S0, %s;" % (ty, zero))
+    if f64:
+        body.append("mov.f64 %%S0, 0d%016X;" % struct.unpack("<Q", struct.pack("<d", const_term))[0])
+    else:
+        body.append("mov.f32 %%S0, 0f%08X;" % struct.unpack("<I", struct.pack("<f", const_term))[0])
     for j in top_vars:
         ch = root.ch[j]
         used.add(j)
         if not ch.ch:
-            body.append("ld.const.%s %%c, %s;" % (ty, cref(ch.k)))
-            body.append("fma.rn.%s %%S0, %%x%d, %%c, %%S0;" % (ty, j))
-            body.append("add.rn.%s %%g%d, %%g%d, %%c;" % (ty, j, j))
+            c = operand(ch.k)
+            body.append("fma.rn.%s %%S0, %%x%d, %s, %%S0;" % (ty, j, c))
+            body.append("add.rn.%s %%g%d, %%g%d, %s;" % (ty, j, j, c))
         else:
             walk(ch, "%%x%d" % j, 1)
             body.append("fma.rn.%s %%S0, %%x%d, %%S1, %%S0;" % (ty, j))
             body.append("add.rn.%s %%g%d, %%g%d, %%S1;" % (ty, j, j))
 
     out = ["// generated by gen_poly_ptx.py -- do not edit",
-           ".version 8.8\n.target sm_103a\n.address_size 64\n",
-           ".extern .const .align %d .b%d %s[%d];" % (sz, 8 * sz, sym, len(coef)),
-           ".visible .func %s(.param .b64 px, .param .b64 pacc)\n{" % name,
-           " .reg .%s %%x<%d>, %%g<%d>, %%S<6>, %%P<6>, %%c, %%t;" % (ty, n_vars, n_vars),
-           " .reg .b64 %rd<3>;",
-           " ld.param.u64 %rd1, [px];",
-           " ld.param.u64 %rd2, [pacc];"]
+           ".version 8.8\n.target sm_103a\n.address_size 64\n"]
+    if f64:
+        out.append(".extern .const .align 8 .b64 %s[%d];" % (sym, len(coef)))
+    out += [".visible .func %s(.param .b64 px, .param .b64 pacc)\n{" % name,
+            " .reg .%s %%x<%d>, %%g<%d>, %%S<6>, %%P<6>, %%c, %%t;" % (ty, n_vars, n_vars),
+            " .reg .b64 %rd<3>;",
+            " ld.param.u64 %rd1, [px];",
+            " ld.param.u64 %rd2, [pacc];"]
     for j in sorted(used):
         out.append(" ld.%s %%x%d, [%%rd1+%d];" % (ty, j, sz * j))
         out.append(" mov.%s %%g%d, %s;" % (ty, j, zero))
@@ -201,14 +250,23 @@ def generate(table_dir, out_dir):
     for body in ("2b", "3b"):
         n_vars, coef, monos = read_table(os.path.join(table_dir, "poly%s.tbl" % body))
         tables.append((body, coef))
-        root = build_trie(monos)
+        centres = shift_centres(body)
+        sp = shifted_polynomial(monos, coef, centres)
+        items = sorted(sp.items())
+        coef32 = [c for _, c in items]
+        root32 = build_trie([(i, m) for i, (m, _) in enumerate(items) if m])
+        const32 = sp.get((), 0.0)
+        root64 = build_trie(monos)
         for prec in ("f64", "f32"):
             ctype = "double" if prec == "f64" else "float"
+            root = root64 if prec == "f64" else root32
+            cf = coef if prec == "f64" else coef32
             chunks = split_root(root, CHUNKS[body][prec])
             names = []
             for c, top in enumerate(chunks):
                 name = "mbx_poly%s_%s_c%d" % (body, prec, c)
-                text = emit_chunk(name, body, n_vars, coef, root, top, prec == "f64")
+                text = emit_chunk(name, body, n_vars, cf, root, top, prec == "f64",
+                                  const_term=(const32 if (prec == "f32" and c == 0) else 0.0))
                 path = os.path.join(out_dir, name + ".ptx")
                 _write_if_changed(path, text)
                 made.append(path)
@@ -219,6 +277,9 @@ def generate(table_dir, out_dir):
             disp.extend("    %s(x, acc);" % n for n in names)
             disp.append("}")
         decls.append("constexpr int kPoly%sVars = %d;" % (body.upper(), n_vars))
+        decls.append("// FP32 polynomial variables are x - kShift%s[v]" % body.upper())
+        decls.append("__device__ constexpr float kShift%s[%d] = {%s};"
+                     % (body.upper(), n_vars, ", ".join("%.9gf" % c for c in centres)))
     path = os.path.join(out_dir, "mbx_poly_coef.ptx")
     _write_if_changed(path, emit_coef_module(tables))
     made.append(path)

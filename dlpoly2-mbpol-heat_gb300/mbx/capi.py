@@ -60,6 +60,7 @@ def load(path=None):
                                           C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, _D]
     L.mbx_set_profiling.argtypes = [C.c_void_p, C.c_int]
     L.mbx_last_timings.argtypes = [C.c_void_p, _D, _L]
+    L.mbx_set_mixed_limits.argtypes = [C.c_void_p, C.c_double, C.c_double]
     L.mbx_last_lists.argtypes = [C.c_void_p, _I, C.c_long, _L, _I, C.c_long, _L]
     L.mbx_2b_poly_batch.argtypes = [C.c_void_p, C.c_int, C.c_long, _D, _D, _D, _D, _D]
     L.mbx_3b_poly_batch.argtypes = [C.c_void_p, C.c_int, C.c_long, _D, _D, _D, _D, _D, _D, _D]
@@ -150,11 +151,14 @@ class Context:
         self._check(self.lib.mbx_set_profiling(self.h, 1 if on else 0), "mbx_set_profiling")
 
     def last_timings(self):
-        """(phase ms [lists, 2B, 3B, jkin], (dimers, trimers, launches))"""
+        """(phase ms [lists, 2B, 3B, jkin], (dimers, trimers, launches, hard dimers, hard trimers))"""
         ms = np.zeros(4)
-        cnt = (C.c_long * 3)()
+        cnt = (C.c_long * 5)()
         self._check(self.lib.mbx_last_timings(self.h, _p(ms), cnt), "mbx_last_timings")
-        return ms, (cnt[0], cnt[1], cnt[2])
+        return ms, tuple(cnt[q] for q in range(5))
+
+    def set_mixed_limits(self, limit2b, limit3b):
+        self._check(self.lib.mbx_set_mixed_limits(self.h, limit2b, limit3b), "mbx_set_mixed_limits")
 
     def last_lists(self):
         npairs = C.c_long(0)

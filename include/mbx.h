@@ -51,10 +51,16 @@ int mbx_set_stream(mbx_context* ctx, void* stream);
 
 /* Time each phase of later evaluations with CUDA events on the context's stream. */
 int mbx_set_profiling(mbx_context* ctx, int on);
-/* Phase times of the last evaluation in ms: [0] lists, [1] 2B kernel, [2] 3B kernel,
- * [3] heat-current jkin (or -1 when profiling is off); counts: [0] dimers, [1] trimers,
- * [2] kernel launches issued.  Either pointer may be NULL. */
+/* Phase times of the last evaluation in ms: [0] lists, [1] 2B kernels, [2] 3B kernels,
+ * [3] heat-current jkin (or -1 when profiling is off); counts[5]: [0] dimers, [1] trimers,
+ * [2] kernel launches issued, [3]/[4] dimers/trimers the mixed path handed to FP64.
+ * Either pointer may be NULL. */
 int mbx_last_timings(mbx_context* ctx, double* ms, long* counts);
+
+/* Mixed path: a dimer (trimer) is evaluated in FP32 only while every polynomial
+ * variable is within limit2b (limit3b) of its shift centre; the others go to the
+ * FP64 kernels in the same call.  Defaults 1.0 and 2.0; 0 sends everything to FP64. */
+int mbx_set_mixed_limits(mbx_context* ctx, double limit2b, double limit3b);
 
 /*
  * MB-pol 2B + 3B forces with the heat-current bookkeeping.

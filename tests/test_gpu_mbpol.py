@@ -194,5 +194,23 @@ def test_full_size_properties_4096(mbx_ctx):
     jd = d["jpot"] + d["jkin"]
     jm = m["jpot"] + m["jkin"]
     assert np.linalg.norm(jm - jd) <= TOL_MIXED_HEAT * np.linalg.norm(jd)
-    _, (nd, nt, _) = mbx_ctx.last_timings()
+    _, (nd, nt, _, _, _) = mbx_ctx.last_timings()
     assert nd > 0 and nt > 0
+
+
+def test_mixed_handoff_limits(mbx_ctx, refs):
+    """Limit 0 hands every cluster to the FP64 kernels: the mixed call then equals FP64."""
+    box = BOXES["small_64_allpairs"]
+    ref = refs["small_64_allpairs"]
+    try:
+        mbx_ctx.set_mixed_limits(0.0, 0.0)
+        got = mbx_ctx.mbpol_forces(box, precision=capi.MIXED)
+        _, (nd, nt, _, hd, ht) = mbx_ctx.last_timings()
+        assert hd == nd and ht == nt
+        assert rel_err(got["forces"], ref["forces"]) <= TOL64
+        mbx_ctx.set_mixed_limits(1e9, 1e9)
+        mbx_ctx.mbpol_forces(box, precision=capi.MIXED)
+        _, (_, _, _, hd, ht) = mbx_ctx.last_timings()
+        assert hd == 0 and ht == 0
+    finally:
+        mbx_ctx.set_mixed_limits(1.0, 2.0)
