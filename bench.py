@@ -312,6 +312,33 @@ def run_ours(args, rank, world):
     return out
 
 
+def run_case(args):
+    """Warmup + K device-resident steps of one precision (for profilers)."""
+    import torch
+    from mbx import capi, systems
+    box = systems.config1()
+    n = box.natms
+    ctx = capi.Context(0)
+    f64 = dict(dtype=torch.float64, device="cuda")
+    X = [torch.tensor(np.ascontiguousarray(box.xyz[:, k]), **f64) for k in range(3)]
+    V = [torch.tensor(np.ascontiguousarray(box.vel[:, k]), **f64) for k in range(3)]
+    M = torch.tensor(box.mass, **f64)
+    F = torch.zeros((3, n), **f64)
+    AE = torch.zeros(n, **f64)
+    LST = torch.tensor(box.listttm2(), dtype=torch.int32, device="cuda")
+    prec = capi.MIXED if args.case == "mixed" else capi.FP64
+    torch.cuda.synchronize()
+    for _ in range(args.warmup + args.steps):
+        F.zero_()
+        AE.zero_()
+        torch.cuda.synchronize()
+        ctx.mbpol_forces_device(prec, box.imcon, box.cell, 3 * box.nw, LST.data_ptr(), n,
+                                [x.data_ptr() for x in X], [F[k].data_ptr() for k in range(3)],
+                                [v.data_ptr() for v in V], M.data_ptr(), AE.data_ptr())
+    ctx.close()
+    print(json.dumps({"case": args.case, "steps": args.steps, "warmup": args.warmup}))
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return None
@@ -342,7 +369,11 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ref-core-s", type=float, default=10.0)
+    ap.add_argument("--case", choices=["mixed", "fp64"], default=None,
+                    help="profiling case: only warmup + K device-resident steps of one precision")
     args = ap.parse_args()
+    if args.case:
+        return run_case(args)
     world = int(os.environ.get("WORLD_SIZE", 1))
     rank = int(os.environ.get("RANK", 0))
     if world > 1 and args.impl == "ours":

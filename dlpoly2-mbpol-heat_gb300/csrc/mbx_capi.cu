@@ -33,7 +33,9 @@ struct mbx_context {
     int2* hard2 = nullptr;          // mixed path: clusters handed to the FP64 kernels
     int4* hard3 = nullptr;
     int* hard_count = nullptr;      // device [2]
-    float limit2 = 1.0f, limit3 = 2.0f;
+    // mixed-path defaults: the 2B term in FP64 (its FP32 gradient is a small difference of
+    // large partials), the 3B term entirely in shifted FP32
+    float limit2 = 0.0f, limit3 = 3.4e38f;
     long hard_last[2] = {0, 0};
     long npairs = 0, ntrip = 0;
     // batch-API staging
@@ -194,8 +196,9 @@ int run_mbpol(mbx_context* ctx, int precision, const Cell& cl, int nw, const int
         if (ctx->profiling) CK(cudaEventRecord(ctx->ev[2], s));
         CK(launch_3b(a, ctx->trip, (int)nt, precision, mp, s));
         if (ctx->profiling) CK(cudaEventRecord(ctx->ev[3], s));
-        const int passes = precision == MBX_MIXED ? 2 : 1;
-        ctx->launches += passes * ((np > 0) + (nt > 0));
+        const int p2 = (precision == MBX_MIXED && ctx->limit2 > 0.f) ? 2 : 1;
+        const int p3 = (precision == MBX_MIXED && ctx->limit3 > 0.f && ctx->limit3 < 3.0e38f) ? 2 : 1;
+        ctx->launches += p2 * (np > 0) + p3 * (nt > 0);
     } else if (ctx->profiling) {
         for (int q = 1; q < 4; ++q) CK(cudaEventRecord(ctx->ev[q], s));
     }
@@ -310,8 +313,8 @@ extern "C" int mbx_last_timings(mbx_context* ctx, double* ms, long* counts) {
 extern "C" int mbx_set_mixed_limits(mbx_context* ctx, double limit2b, double limit3b) {
     if (!ctx) return MBX_ERR_ARG;
     if (!(limit2b >= 0.0) || !(limit3b >= 0.0)) return fail(ctx, MBX_ERR_ARG, "limits must be >= 0");
-    ctx->limit2 = (float)limit2b;
-    ctx->limit3 = (float)limit3b;
+    ctx->limit2 = (float)std::min(limit2b, 3.4e38);
+    ctx->limit3 = (float)std::min(limit3b, 3.4e38);
     return MBX_OK;
 }
 

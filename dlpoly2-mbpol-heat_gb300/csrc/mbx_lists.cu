@@ -7,8 +7,8 @@
 // a cell list, so the lists are identical as sets while the work is O(N).
 //
 // Layout: monomers are 9 doubles per water (O, H1, H2; H imaged next to O), the
-// pair list is int2 (i < j) in the reference's loop order, the trimer list is
-// int4 (i < j < k, w unused) grouped by the centre water that generated it.
+// pair list is int2 (i < j) grouped by i, the trimer list is int4 (i < j < k, w
+// unused) grouped by the centre water that generated it.
 #include "mbx_kernels.cuh"
 
 #include <cub/device/device_radix_sort.cuh>
@@ -72,19 +72,10 @@ __global__ void k_cell_bounds(int nw, int ncell, const unsigned* __restrict__ sk
     if (i == nw - 1 || skey[i + 1] != c) end[c] = i + 1;
 }
 
-// Insertion of j into the ascending list l[0..n) (n < cap).
-__device__ __forceinline__ void sorted_insert(int* l, int n, int j) {
-    int p = n;
-    while (p > 0 && l[p - 1] > j) {
-        l[p] = l[p - 1];
-        --p;
-    }
-    l[p] = j;
-}
-
 // Per water i: dimer partners j > i (2B test) and 3B neighbours j != i (3B edge test),
-// both ascending.  Candidates come from the 27 surrounding cells, or from every water
-// when the grid is too coarse (all_pairs).
+// in candidate order (deterministic: cells in a fixed order, waters by index within a
+// cell).  Candidates come from the 27 surrounding cells, or from every water when the
+// grid is too coarse (all_pairs).
 __global__ void k_neighbours(int nw, const double* __restrict__ mono, Cell cl, int3 nc, int all_pairs,
                              const unsigned* __restrict__ skey, const int* __restrict__ sidx,
                              const int* __restrict__ cstart, const int* __restrict__ cend, int cap2, int cap3,
@@ -100,11 +91,11 @@ __global__ void k_neighbours(int nw, const double* __restrict__ mono, Cell cl, i
         if (j == i) return;
         const double r2 = dist2_img(cl, oi, mono + 9 * (size_t)j);
         if (j > i && dimer_in(r2)) {
-            if (c2 < cap2) sorted_insert(my2, c2, j);
+            if (c2 < cap2) my2[c2] = j;
             ++c2;
         }
         if (tri_edge(r2)) {
-            if (c3 < cap3) sorted_insert(my3, c3, j);
+            if (c3 < cap3) my3[c3] = j;
             ++c3;
         }
     };

@@ -587,7 +587,7 @@ static int blocks(int n) { return (n + kThreads - 1) / kThreads; }
 cudaError_t launch_2b(const MbpolArgs& a, const int2* pairs, int n, int precision, const MixedPass& mp,
                       cudaStream_t s) {
     if (n <= 0) return cudaSuccess;
-    if (precision == 0) {
+    if (precision == 0 || !(mp.limit2 > 0.f)) {
         k_mbpol_2b<double><<<blocks(n), kThreads, 0, s>>>(a, pairs, n, nullptr, HardList{nullptr, nullptr, 0.f});
     } else {
         k_mbpol_2b<float><<<blocks(n), kThreads, 0, s>>>(a, pairs, n, nullptr,
@@ -601,8 +601,11 @@ cudaError_t launch_2b(const MbpolArgs& a, const int2* pairs, int n, int precisio
 cudaError_t launch_3b(const MbpolArgs& a, const int4* trip, int n, int precision, const MixedPass& mp,
                       cudaStream_t s) {
     if (n <= 0) return cudaSuccess;
-    if (precision == 0) {
+    if (precision == 0 || !(mp.limit3 > 0.f)) {
         k_mbpol_3b<double><<<blocks(n), kThreads, 0, s>>>(a, trip, n, nullptr, HardList{nullptr, nullptr, 0.f});
+    } else if (!(mp.limit3 < 3.0e38f)) {
+        // no hand-off requested: every trimer in FP32
+        k_mbpol_3b<float><<<blocks(n), kThreads, 0, s>>>(a, trip, n, nullptr, HardList{nullptr, nullptr, 0.f});
     } else {
         k_mbpol_3b<float><<<blocks(n), kThreads, 0, s>>>(a, trip, n, nullptr,
                                                          HardList{mp.hard3, mp.count + 1, mp.limit3});

@@ -59,7 +59,9 @@ int mbx_last_timings(mbx_context* ctx, double* ms, long* counts);
 
 /* Mixed path: a dimer (trimer) is evaluated in FP32 only while every polynomial
  * variable is within limit2b (limit3b) of its shift centre; the others go to the
- * FP64 kernels in the same call.  Defaults 1.0 and 2.0; 0 sends everything to FP64. */
+ * FP64 kernels in the same call.  0 sends every cluster of that body to FP64; a
+ * limit >= 3.4e38 keeps every cluster in FP32.  Defaults: 0 (2B in FP64) and
+ * 3.4e38 (3B in FP32). */
 int mbx_set_mixed_limits(mbx_context* ctx, double limit2b, double limit3b);
 
 /*
