@@ -217,13 +217,15 @@ def run_ours(args, rank, world):
     _, phase64, _ = timed(capi.FP64, 2, 0, profile=True)
 
     # e2e through the host-array C ABI from pinned host buffers
-    pin = dict(dtype=torch.float64, pin_memory=True)
-    hx = [torch.tensor(np.ascontiguousarray(box.xyz[:, k]), **pin) for k in range(3)]
-    hv = [torch.tensor(np.ascontiguousarray(box.vel[:, k]), **pin) for k in range(3)]
-    hm = torch.tensor(box.mass, **pin)
-    hf = torch.zeros((3, n), **pin)
-    hae = torch.zeros(n, **pin)
-    hl = torch.tensor(box.listttm2(), dtype=torch.int32, pin_memory=True)
+    def pinned(a):
+        return torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
+
+    hx = [pinned(box.xyz[:, k]) for k in range(3)]
+    hv = [pinned(box.vel[:, k]) for k in range(3)]
+    hm = pinned(box.mass)
+    hf = pinned(np.zeros((3, n)))
+    hae = pinned(np.zeros(n))
+    hl = pinned(box.listttm2().astype(np.int32))
     import ctypes as C
     D = C.POINTER(C.c_double)
 
