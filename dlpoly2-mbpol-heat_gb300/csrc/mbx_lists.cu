@@ -72,51 +72,92 @@ __global__ void k_cell_bounds(int nw, int ncell, const unsigned* __restrict__ sk
     if (i == nw - 1 || skey[i + 1] != c) end[c] = i + 1;
 }
 
-// Per water i: dimer partners j > i (2B test) and 3B neighbours j != i (3B edge test),
-// in candidate order (deterministic: cells in a fixed order, waters by index within a
-// cell).  Candidates come from the 27 surrounding cells, or from every water when the
-// grid is too coarse (all_pairs).
+// Per water i (one warp): dimer partners j > i (2B test) and 3B neighbours j != i
+// (3B edge test).  Lanes test candidates in parallel and append the hits in candidate
+// order through a warp ballot, so the lists are deterministic.  Candidates come from
+// the 27 surrounding cells (in a fixed order, waters by index within a cell), or from
+// every water when the grid is too coarse (all_pairs).
 __global__ void k_neighbours(int nw, const double* __restrict__ mono, Cell cl, int3 nc, int all_pairs,
                              const unsigned* __restrict__ skey, const int* __restrict__ sidx,
                              const int* __restrict__ cstart, const int* __restrict__ cend, int cap2, int cap3,
                              int* __restrict__ n2, int* __restrict__ l2, int* __restrict__ n3,
                              int* __restrict__ l3, int* __restrict__ overflow) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nw) return;
+    const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (i >= nw) return;   // warp-uniform
     const double* oi = mono + 9 * (size_t)i;
     int* my2 = l2 + (size_t)i * cap2;
     int* my3 = l3 + (size_t)i * cap3;
-    int c2 = 0, c3 = 0;
-    auto consider = [&](int j) {
-        if (j == i) return;
-        const double r2 = dist2_img(cl, oi, mono + 9 * (size_t)j);
-        if (j > i && dimer_in(r2)) {
-            if (c2 < cap2) my2[c2] = j;
-            ++c2;
-        }
-        if (tri_edge(r2)) {
-            if (c3 < cap3) my3[c3] = j;
-            ++c3;
-        }
-    };
+    // candidate ranges: lane c < 27 owns neighbour cell c
+    int cs = 0, cn = 0;
+    int total;
     if (all_pairs) {
-        for (int j = 0; j < nw; ++j) consider(j);
+        total = nw;
     } else {
-        const double* o = oi;
-        const int cx = wrap_cell(o[0] * cl.inv[0], nc.x);
-        const int cy = wrap_cell(o[1] * cl.inv[1], nc.y);
-        const int cz = wrap_cell(o[2] * cl.inv[2], nc.z);
-        for (int dz = -1; dz <= 1; ++dz)
-            for (int dy = -1; dy <= 1; ++dy)
-                for (int dx = -1; dx <= 1; ++dx) {
-                    const int x = (cx + dx + nc.x) % nc.x, y = (cy + dy + nc.y) % nc.y, z = (cz + dz + nc.z) % nc.z;
-                    const int c = (z * nc.y + y) * nc.x + x;
-                    for (int q = cstart[c]; q < cend[c]; ++q) consider(sidx[q]);
-                }
+        if (lane < 27) {
+            const int cx = wrap_cell(oi[0] * cl.inv[0], nc.x);
+            const int cy = wrap_cell(oi[1] * cl.inv[1], nc.y);
+            const int cz = wrap_cell(oi[2] * cl.inv[2], nc.z);
+            const int dx = lane % 3 - 1, dy = (lane / 3) % 3 - 1, dz = lane / 9 - 1;
+            const int x = (cx + dx + nc.x) % nc.x, y = (cy + dy + nc.y) % nc.y, z = (cz + dz + nc.z) % nc.z;
+            const int c = (z * nc.y + y) * nc.x + x;
+            cs = cstart[c];
+            cn = cend[c] - cs;
+        }
+        // inclusive prefix of the counts over lanes
+        int incl = cn;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += v;
+        }
+        total = __shfl_sync(0xffffffffu, incl, 31);
+        cn = incl;   // lane c now holds the end offset of cell c in the candidate sequence
     }
-    n2[i] = c2;
-    n3[i] = c3;
-    if (c2 > cap2 || c3 > cap3) atomicOr(overflow, 1);
+    int c2 = 0, c3 = 0;
+    for (int base = 0; base < total; base += 32) {
+        const int k = base + lane;
+        const bool valid = k < total;
+        int j = -1;
+        if (all_pairs) {
+            if (valid) j = k;
+        } else {
+            // the cell holding candidate k: the first cell whose end offset exceeds k
+            // (all lanes take part in the shuffles; total > 0 inside this loop)
+            const int kk = valid ? k : total - 1;
+            int cell = 0;
+            for (int c = 0; c < 27; ++c) {
+                const int end = __shfl_sync(0xffffffffu, cn, c);
+                if (kk >= end) cell = c + 1;
+            }
+            const int start = __shfl_sync(0xffffffffu, cs, cell);
+            const int prev_end = __shfl_sync(0xffffffffu, cn, cell > 0 ? cell - 1 : 0);
+            if (valid) j = sidx[start + (kk - (cell > 0 ? prev_end : 0))];
+        }
+        bool in2 = false, in3 = false;
+        if (j >= 0 && j != i) {
+            const double r2 = dist2_img(cl, oi, mono + 9 * (size_t)j);
+            in2 = j > i && dimer_in(r2);
+            in3 = tri_edge(r2);
+        }
+        const unsigned b2 = __ballot_sync(0xffffffffu, in2);
+        const unsigned b3 = __ballot_sync(0xffffffffu, in3);
+        const unsigned lt = (1u << lane) - 1u;
+        if (in2) {
+            const int q = c2 + __popc(b2 & lt);
+            if (q < cap2) my2[q] = j;
+        }
+        if (in3) {
+            const int q = c3 + __popc(b3 & lt);
+            if (q < cap3) my3[q] = j;
+        }
+        c2 += __popc(b2);
+        c3 += __popc(b3);
+    }
+    if (lane == 0) {
+        n2[i] = c2;
+        n3[i] = c3;
+        if (c2 > cap2 || c3 > cap3) atomicOr(overflow, 1);
+    }
 }
 
 __global__ void k_pairs_compact(int nw, int cap2, const int* __restrict__ n2, const int* __restrict__ off2,
@@ -127,16 +168,18 @@ __global__ void k_pairs_compact(int nw, int cap2, const int* __restrict__ n2, co
     for (int q = 0; q < n; ++q) pairs[o + q] = make_int2(i, l2[(size_t)i * cap2 + q]);
 }
 
-// Trimers {c, a, b} with a < b both 3B neighbours of the centre c.  A trimer is kept
-// by the reference iff some water is within the 3B cutoff of the other two
-// (istoobig1..3 in SOURCE/mbpol.f90:858-862); it is generated here by the smallest
-// such centre only, so every trimer appears exactly once.
+// Trimers {c, a, b} with a, b 3B neighbours of the centre c (one warp per centre).
+// A trimer is kept by the reference iff some water is within the 3B cutoff of the
+// other two (istoobig1..3 in SOURCE/mbpol.f90:858-862); it is generated here by the
+// smallest such centre only, so every trimer appears exactly once.  Lanes test the
+// pairs (p < q) of the neighbour list in parallel; hits are appended in pair order.
 template <bool FILL>
 __global__ void k_trimers(int nw, const double* __restrict__ mono, Cell cl, int cap3, const int* __restrict__ n3,
                           const int* __restrict__ l3, int* __restrict__ cnt, const int* __restrict__ off,
                           int4* __restrict__ trip) {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= nw) return;
+    const int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (c >= nw) return;   // warp-uniform
     const int n = min(n3[c], cap3);
     const int* nb = l3 + (size_t)c * cap3;
     int m = 0;
@@ -144,21 +187,27 @@ __global__ void k_trimers(int nw, const double* __restrict__ mono, Cell cl, int 
     for (int p = 0; p < n; ++p) {
         const int a = nb[p];
         const double* oa = mono + 9 * (size_t)a;
-        for (int q = p + 1; q < n; ++q) {
-            const int b = nb[q];
-            const bool ab = tri_edge(dist2_img(cl, oa, mono + 9 * (size_t)b));
-            if (ab && (a < c || b < c)) continue;
-            if (FILL) {
+        for (int q0 = p + 1; q0 < n; q0 += 32) {
+            const int q = q0 + lane;
+            bool keep = false;
+            int b = 0;
+            if (q < n) {
+                b = nb[q];
+                const bool ab = tri_edge(dist2_img(cl, oa, mono + 9 * (size_t)b));
+                keep = !(ab && (a < c || b < c));
+            }
+            const unsigned bal = __ballot_sync(0xffffffffu, keep);
+            if (FILL && keep) {
                 int i = c, j = a, k = b;  // sort the three indices
                 if (i > j) { int t = i; i = j; j = t; }
                 if (j > k) { int t = j; j = k; k = t; }
                 if (i > j) { int t = i; i = j; j = t; }
-                trip[base + m] = make_int4(i, j, k, 0);
+                trip[base + m + __popc(bal & ((1u << lane) - 1u))] = make_int4(i, j, k, 0);
             }
-            ++m;
+            m += __popc(bal);
         }
     }
-    if (!FILL) cnt[c] = m;
+    if (!FILL && lane == 0) cnt[c] = m;
 }
 
 // ---------------------------------------------------------------------------
@@ -262,11 +311,12 @@ cudaError_t ListBuilder::phase1(int nw, const int* list, const double* x, const 
         k_cell_bounds<<<g, kThreads, 0, s>>>(nw, ncell, skey, cstart, cend);
     }
     cudaMemsetAsync(flag, 0, sizeof(int), s);
-    k_neighbours<<<g, kThreads, 0, s>>>(nw, mono, cl, nc, all_pairs, skey, sidx, cstart, cend, cap2, cap3, n2, l2,
-                                        n3, l3, flag);
+    const int gw = (int)(((long)nw * 32 + kThreads - 1) / kThreads);   // one warp per water
+    k_neighbours<<<gw, kThreads, 0, s>>>(nw, mono, cl, nc, all_pairs, skey, sidx, cstart, cend, cap2, cap3, n2, l2,
+                                         n3, l3, flag);
     size_t a = scan_bytes;
     cub::DeviceScan::ExclusiveSum(scan_tmp, a, n2, off2, nw, s);
-    k_trimers<false><<<g, kThreads, 0, s>>>(nw, mono, cl, cap3, n3, l3, tcnt, nullptr, nullptr);
+    k_trimers<false><<<gw, kThreads, 0, s>>>(nw, mono, cl, cap3, n3, l3, tcnt, nullptr, nullptr);
     a = scan_bytes;
     cub::DeviceScan::ExclusiveSum(scan_tmp, a, tcnt, toff, nw, s);
     k_list_totals<<<1, 1, 0, s>>>(nw, n2, off2, tcnt, toff, flag, totals_dev);
@@ -277,7 +327,8 @@ cudaError_t ListBuilder::phase2(int nw, const Cell& cl, const double* mono, int2
                                 cudaStream_t s) {
     const int g = grid_for(nw);
     k_pairs_compact<<<g, kThreads, 0, s>>>(nw, cap2, n2, off2, l2, pairs);
-    k_trimers<true><<<g, kThreads, 0, s>>>(nw, mono, cl, cap3, n3, l3, nullptr, toff, trip);
+    const int gw = (int)(((long)nw * 32 + kThreads - 1) / kThreads);
+    k_trimers<true><<<gw, kThreads, 0, s>>>(nw, mono, cl, cap3, n3, l3, nullptr, toff, trip);
     launches_last += 2;
     return cudaGetLastError();
 }

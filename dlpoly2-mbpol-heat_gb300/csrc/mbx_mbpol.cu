@@ -236,11 +236,13 @@ __device__ constexpr V kV[36] = {
 };
 }  // namespace m3b
 
-// x3b_v2x_p::operator() on the 27 trimer coordinates; gradients ADDED to gt.
-// T = float: shifted variables and the FP64 hand-off, as in model_2b.
+// 3B variables (SOURCE/mbpol-3b-poly.cpp:170-206) and the factor -k e/r of their
+// gradient (g_intra/g_main, :26-87).  For T = float the variables are returned
+// shifted by kShift3B (the FP32 polynomial's expansion point); returns the largest
+// |shifted variable| (0 for double).
 template <typename T>
-__device__ __forceinline__ T model_3b(const T* t, T* gt, float limit = 0.f, bool* hard = nullptr) {
-    T x[36], fk[36];
+__device__ __forceinline__ float vars_3b(const T* t, T* x, T* fk) {
+    float dev = 0.f;
 #pragma unroll
     for (int q = 0; q < 36; ++q) {
         const m3b::V d = m3b::kV[q];
@@ -248,24 +250,19 @@ __device__ __forceinline__ T model_3b(const T* t, T* gt, float limit = 0.f, bool
         const T r = t_sqrt(dx * dx + dy * dy + dz * dz);
         const T e = t_exp(-T(d.k) * (r - T(d.r0)));
         x[q] = e;
-        fk[q] = -T(d.k) * e / r;   // g_intra/g_main factor without the polynomial gradient
-    }
-    if constexpr (sizeof(T) == 4) {
-        float dev = 0.f;
-#pragma unroll
-        for (int q = 0; q < 36; ++q) {
+        fk[q] = -T(d.k) * e / r;
+        if constexpr (sizeof(T) == 4) {
             x[q] -= kShift3B[q];
             dev = fmaxf(dev, fabsf(x[q]));
         }
-        if (hard && dev > limit) {
-            *hard = true;
-            return T(0);
-        }
     }
-    T acc[37];
-#pragma unroll
-    for (int q = 0; q < 37; ++q) acc[q] = T(0);
-    poly3b<T>(x, acc);
+    return dev;
+}
+
+// Chain rule and switching of x3b_v2x_p::operator() (SOURCE/mbpol-3b-poly.cpp:208-312)
+// given the polynomial's [E, dE/dx]; gradients ADDED to gt; returns the energy.
+template <typename T>
+__device__ __forceinline__ T finish_3b(const T* t, const T* acc, const T* fk, T* gt) {
     T retval = acc[0];
     T rab[3], rac[3], rbc[3];
     T drab = T(0), drac = T(0), drbc = T(0);
@@ -308,6 +305,23 @@ __device__ __forceinline__ T model_3b(const T* t, T* gt, float limit = 0.f, bool
         gt[m3b::Oc + n] -= gac * rac[n] + gbc * rbc[n];
     }
     return retval;
+}
+
+// x3b_v2x_p::operator() on the 27 trimer coordinates; gradients ADDED to gt.
+// T = float: shifted variables and the FP64 hand-off, as in model_2b.
+template <typename T>
+__device__ __forceinline__ T model_3b(const T* t, T* gt, float limit = 0.f, bool* hard = nullptr) {
+    T x[36], fk[36];
+    const float dev = vars_3b<T>(t, x, fk);
+    if (hard && dev > limit) {
+        *hard = true;
+        return T(0);
+    }
+    T acc[37];
+#pragma unroll
+    for (int q = 0; q < 37; ++q) acc[q] = T(0);
+    poly3b<T>(x, acc);
+    return finish_3b<T>(t, acc, fk, gt);
 }
 
 // ---------------------------------------------------------------------------
@@ -446,6 +460,100 @@ __global__ void __launch_bounds__(kThreads) k_mbpol_2b(MbpolArgs a, const int2* 
     flush_block(red, a.acc, S_E2);
 }
 
+// Gather the trimer's monomers and re-image them around the second one as do_trimer
+// does (SOURCE/mbpol.f90:867-876); w = working-frame positions (absolute for FP64,
+// shifted to the second O for FP32), p = the same in T.
+template <typename T>
+__device__ __forceinline__ void prep_3b(const MbpolArgs& a, int4 c, double* w, T* p) {
+    double w1[9], w2[9], w3[9];
+#pragma unroll
+    for (int q = 0; q < 9; ++q) {
+        w1[q] = a.mono[9 * (size_t)c.x + q];
+        w2[q] = a.mono[9 * (size_t)c.y + q];
+        w3[q] = a.mono[9 * (size_t)c.z + q];
+    }
+    double r12[3], r23[3];
+    dist2_img(a.cell, w1, w2, r12);
+    dist2_img(a.cell, w2, w3, r23);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        w1[3 + k] = dadd(dsub(w1[3 + k], w1[k]), dadd(w2[k], r12[k]));
+        w1[6 + k] = dadd(dsub(w1[6 + k], w1[k]), dadd(w2[k], r12[k]));
+        w1[k] = dadd(w2[k], r12[k]);
+        w3[3 + k] = dadd(dsub(w3[3 + k], w3[k]), dsub(w2[k], r23[k]));
+        w3[6 + k] = dadd(dsub(w3[6 + k], w3[k]), dsub(w2[k], r23[k]));
+        w3[k] = dsub(w2[k], r23[k]);
+    }
+#pragma unroll
+    for (int q = 0; q < 9; ++q) {
+        const double o = (sizeof(T) == 8) ? 0.0 : w2[q % 3];
+        w[q] = w1[q] - o;
+        w[9 + q] = w2[q] - o;
+        w[18 + q] = w3[q] - o;
+    }
+#pragma unroll
+    for (int q = 0; q < 27; ++q) p[q] = (T)w[q];
+}
+
+__device__ __forceinline__ void trimer_atoms(const MbpolArgs& a, int4 c, int* at) {
+    const int o1 = a.list[3 * c.x] - 1, o2 = a.list[3 * c.y] - 1, o3 = a.list[3 * c.z] - 1;
+    at[0] = o1; at[1] = o1 + 1; at[2] = o1 + 2;
+    at[3] = o2; at[4] = o2 + 1; at[5] = o2 + 2;
+    at[6] = o3; at[7] = o3 + 1; at[8] = o3 + 2;
+}
+
+// Mixed-path 3B: two trimers per thread, one packed (f32x2) polynomial evaluation for
+// both, so every fetched instruction does two trimers' work.  The cheap geometry is
+// recomputed after the polynomial call rather than kept live across it.
+__global__ void __launch_bounds__(kThreads) k_mbpol_3b_pair(MbpolArgs a, const int4* __restrict__ trip, int n) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    double red[14];
+#pragma unroll
+    for (int q = 0; q < 14; ++q) red[q] = 0.0;
+    const int i0 = 2 * t;
+    if (i0 < n) {
+        const int i1 = (i0 + 1 < n) ? i0 + 1 : i0;
+        float2 x2[36];
+        float2 acc2[37];
+        {
+            double w[27];
+            float p[27], x[36], fk[36];
+            prep_3b<float>(a, trip[i0], w, p);
+            vars_3b<float>(p, x, fk);
+#pragma unroll
+            for (int q = 0; q < 36; ++q) x2[q].x = x[q];
+            prep_3b<float>(a, trip[i1], w, p);
+            vars_3b<float>(p, x, fk);
+#pragma unroll
+            for (int q = 0; q < 36; ++q) x2[q].y = x[q];
+        }
+#pragma unroll
+        for (int q = 0; q < 37; ++q) acc2[q] = make_float2(0.f, 0.f);
+        poly3b_pair(x2, acc2);
+#pragma unroll 1
+        for (int h = 0; h < 2; ++h) {
+            if (h == 1 && i1 == i0) break;
+            const int4 c = trip[h ? i1 : i0];
+            double w[27];
+            float p[27], x[36], fk[36], acc[37], gt[27];
+            prep_3b<float>(a, c, w, p);
+            vars_3b<float>(p, x, fk);
+#pragma unroll
+            for (int q = 0; q < 37; ++q) acc[q] = h ? acc2[q].y : acc2[q].x;
+#pragma unroll
+            for (int q = 0; q < 27; ++q) gt[q] = 0.f;
+            const float e = finish_3b<float>(p, acc, fk, gt);
+            int at[9];
+            trimer_atoms(a, c, at);
+            double g[27];
+#pragma unroll
+            for (int q = 0; q < 27; ++q) g[q] = (double)gt[q];
+            cluster_accumulate<9>(a, at, (double)e, w, g, red);
+        }
+    }
+    flush_block(red, a.acc, S_E3);
+}
+
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_mbpol_3b(MbpolArgs a, const int4* __restrict__ trip, int n,
                                                         const int* __restrict__ n_dev, HardList hl) {
@@ -456,46 +564,18 @@ __global__ void __launch_bounds__(kThreads) k_mbpol_3b(MbpolArgs a, const int4* 
     for (int q = 0; q < 14; ++q) red[q] = 0.0;
     if (t < n) {
         const int4 c = trip[t];
-        double w1[9], w2[9], w3[9];
-#pragma unroll
-        for (int q = 0; q < 9; ++q) {
-            w1[q] = a.mono[9 * (size_t)c.x + q];
-            w2[q] = a.mono[9 * (size_t)c.y + q];
-            w3[q] = a.mono[9 * (size_t)c.z + q];
-        }
-        double r12[3], r23[3];
-        dist2_img(a.cell, w1, w2, r12);
-        dist2_img(a.cell, w2, w3, r23);
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            w1[3 + k] = dadd(dsub(w1[3 + k], w1[k]), dadd(w2[k], r12[k]));
-            w1[6 + k] = dadd(dsub(w1[6 + k], w1[k]), dadd(w2[k], r12[k]));
-            w1[k] = dadd(w2[k], r12[k]);
-            w3[3 + k] = dadd(dsub(w3[3 + k], w3[k]), dsub(w2[k], r23[k]));
-            w3[6 + k] = dadd(dsub(w3[6 + k], w3[k]), dsub(w2[k], r23[k]));
-            w3[k] = dsub(w2[k], r23[k]);
-        }
         T p[27], gt[27];
         double w[27];
+        prep_3b<T>(a, c, w, p);
 #pragma unroll
-        for (int q = 0; q < 9; ++q) {
-            const double o = (sizeof(T) == 8) ? 0.0 : w2[q % 3];
-            w[q] = w1[q] - o;
-            w[9 + q] = w2[q] - o;
-            w[18 + q] = w3[q] - o;
-        }
-#pragma unroll
-        for (int q = 0; q < 27; ++q) {
-            p[q] = (T)w[q];
-            gt[q] = T(0);
-        }
+        for (int q = 0; q < 27; ++q) gt[q] = T(0);
         bool hard = false;
         const T e = model_3b<T>(p, gt, hl.limit, hl.items ? &hard : nullptr);
         if (hard) {
             ((int4*)hl.items)[atomicAdd(hl.count, 1)] = c;
         } else {
-            const int o1 = a.list[3 * c.x] - 1, o2 = a.list[3 * c.y] - 1, o3 = a.list[3 * c.z] - 1;
-            const int at[9] = {o1, o1 + 1, o1 + 2, o2, o2 + 1, o2 + 2, o3, o3 + 1, o3 + 2};
+            int at[9];
+            trimer_atoms(a, c, at);
             double g[27];
 #pragma unroll
             for (int q = 0; q < 27; ++q) g[q] = (double)gt[q];
@@ -604,8 +684,8 @@ cudaError_t launch_3b(const MbpolArgs& a, const int4* trip, int n, int precision
     if (precision == 0 || !(mp.limit3 > 0.f)) {
         k_mbpol_3b<double><<<blocks(n), kThreads, 0, s>>>(a, trip, n, nullptr, HardList{nullptr, nullptr, 0.f});
     } else if (!(mp.limit3 < 3.0e38f)) {
-        // no hand-off requested: every trimer in FP32
-        k_mbpol_3b<float><<<blocks(n), kThreads, 0, s>>>(a, trip, n, nullptr, HardList{nullptr, nullptr, 0.f});
+        // no hand-off requested: every trimer in FP32, two per thread
+        k_mbpol_3b_pair<<<blocks((n + 1) / 2), kThreads, 0, s>>>(a, trip, n);
     } else {
         k_mbpol_3b<float><<<blocks(n), kThreads, 0, s>>>(a, trip, n, nullptr,
                                                          HardList{mp.hard3, mp.count + 1, mp.limit3});
