@@ -380,8 +380,9 @@ __device__ __forceinline__ void cluster_accumulate(const MbpolArgs& a, const int
 }
 
 // Reduce red[14] = {E, vir, stress[9], jpot[3]} of the block into acc.
-__device__ __forceinline__ void flush_block(double (&red)[14], double* acc, int eslot) {
-    __shared__ double sh[kThreads / 32][14];
+template <int NT>
+__device__ __forceinline__ void flush_block_n(double (&red)[14], double* acc, int eslot) {
+    __shared__ double sh[NT / 32][14];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
 #pragma unroll
     for (int q = 0; q < 14; ++q) {
@@ -391,11 +392,15 @@ __device__ __forceinline__ void flush_block(double (&red)[14], double* acc, int 
     __syncthreads();
     if (threadIdx.x < 14) {
         double s = 0.0;
-        for (int i = 0; i < kThreads / 32; ++i) s += sh[i][threadIdx.x];
+        for (int i = 0; i < NT / 32; ++i) s += sh[i][threadIdx.x];
         const int q = threadIdx.x;
         const int slot = q == 0 ? eslot : (q == 1 ? S_VIR : (q <= 10 ? S_STRESS + (q - 2) : S_JPOT + (q - 11)));
         if (s != 0.0) atomicAdd(acc + slot, s);
     }
+}
+
+__device__ __forceinline__ void flush_block(double (&red)[14], double* acc, int eslot) {
+    flush_block_n<kThreads>(red, acc, eslot);
 }
 
 // Mixed-precision hand-off: clusters whose FP32 variables stray beyond the limit
@@ -502,56 +507,52 @@ __device__ __forceinline__ void trimer_atoms(const MbpolArgs& a, int4 c, int* at
     at[6] = o3; at[7] = o3 + 1; at[8] = o3 + 2;
 }
 
-// Mixed-path 3B: two trimers per thread, one packed (f32x2) polynomial evaluation for
-// both, so every fetched instruction does two trimers' work.  The cheap geometry is
-// recomputed after the polynomial call rather than kept live across it.
-__global__ void __launch_bounds__(kThreads) k_mbpol_3b_pair(MbpolArgs a, const int4* __restrict__ trip, int n) {
+// Mixed-path 3B, every trimer in FP32.  The generated FP32 polynomial is ~1 MB of
+// straight-line code; its "sync" variant puts a block barrier every few hundred
+// instructions so that the eight warps of a block (one block per SM at 255
+// registers) walk the code together and share every instruction-cache line.  All
+// threads therefore call the polynomial: a thread without a trimer evaluates it at
+// the expansion point and discards the result.
+constexpr int kSyncThreads = 256;
+
+__global__ void __launch_bounds__(kSyncThreads) k_mbpol_3b_sync(MbpolArgs a, const int4* __restrict__ trip, int n) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool valid = t < n;
     double red[14];
 #pragma unroll
     for (int q = 0; q < 14; ++q) red[q] = 0.0;
-    const int i0 = 2 * t;
-    if (i0 < n) {
-        const int i1 = (i0 + 1 < n) ? i0 + 1 : i0;
-        float2 x2[36];
-        float2 acc2[37];
-        {
-            double w[27];
-            float p[27], x[36], fk[36];
-            prep_3b<float>(a, trip[i0], w, p);
+    float x[36], acc[37];
+    {
+        double w[27];
+        float p[27], fk[36];
+        if (valid) {
+            prep_3b<float>(a, trip[t], w, p);
             vars_3b<float>(p, x, fk);
+        } else {
 #pragma unroll
-            for (int q = 0; q < 36; ++q) x2[q].x = x[q];
-            prep_3b<float>(a, trip[i1], w, p);
-            vars_3b<float>(p, x, fk);
-#pragma unroll
-            for (int q = 0; q < 36; ++q) x2[q].y = x[q];
-        }
-#pragma unroll
-        for (int q = 0; q < 37; ++q) acc2[q] = make_float2(0.f, 0.f);
-        poly3b_pair(x2, acc2);
-#pragma unroll 1
-        for (int h = 0; h < 2; ++h) {
-            if (h == 1 && i1 == i0) break;
-            const int4 c = trip[h ? i1 : i0];
-            double w[27];
-            float p[27], x[36], fk[36], acc[37], gt[27];
-            prep_3b<float>(a, c, w, p);
-            vars_3b<float>(p, x, fk);
-#pragma unroll
-            for (int q = 0; q < 37; ++q) acc[q] = h ? acc2[q].y : acc2[q].x;
-#pragma unroll
-            for (int q = 0; q < 27; ++q) gt[q] = 0.f;
-            const float e = finish_3b<float>(p, acc, fk, gt);
-            int at[9];
-            trimer_atoms(a, c, at);
-            double g[27];
-#pragma unroll
-            for (int q = 0; q < 27; ++q) g[q] = (double)gt[q];
-            cluster_accumulate<9>(a, at, (double)e, w, g, red);
+            for (int q = 0; q < 36; ++q) x[q] = 0.f;
         }
     }
-    flush_block(red, a.acc, S_E3);
+#pragma unroll
+    for (int q = 0; q < 37; ++q) acc[q] = 0.f;
+    poly3b_sync(x, acc);
+    if (valid) {
+        const int4 c = trip[t];
+        double w[27];
+        float p[27], fk[36], gt[27];
+        prep_3b<float>(a, c, w, p);
+        vars_3b<float>(p, x, fk);
+#pragma unroll
+        for (int q = 0; q < 27; ++q) gt[q] = 0.f;
+        const float e = finish_3b<float>(p, acc, fk, gt);
+        int at[9];
+        trimer_atoms(a, c, at);
+        double g[27];
+#pragma unroll
+        for (int q = 0; q < 27; ++q) g[q] = (double)gt[q];
+        cluster_accumulate<9>(a, at, (double)e, w, g, red);
+    }
+    flush_block_n<kSyncThreads>(red, a.acc, S_E3);
 }
 
 template <typename T>
@@ -684,8 +685,8 @@ cudaError_t launch_3b(const MbpolArgs& a, const int4* trip, int n, int precision
     if (precision == 0 || !(mp.limit3 > 0.f)) {
         k_mbpol_3b<double><<<blocks(n), kThreads, 0, s>>>(a, trip, n, nullptr, HardList{nullptr, nullptr, 0.f});
     } else if (!(mp.limit3 < 3.0e38f)) {
-        // no hand-off requested: every trimer in FP32, two per thread
-        k_mbpol_3b_pair<<<blocks((n + 1) / 2), kThreads, 0, s>>>(a, trip, n);
+        // no hand-off requested: every trimer in FP32, block-synchronised code walk
+        k_mbpol_3b_sync<<<(n + kSyncThreads - 1) / kSyncThreads, kSyncThreads, 0, s>>>(a, trip, n);
     } else {
         k_mbpol_3b<float><<<blocks(n), kThreads, 0, s>>>(a, trip, n, nullptr,
                                                          HardList{mp.hard3, mp.count + 1, mp.limit3});

@@ -150,7 +150,7 @@ def emit_coef_module(tables, pair_tables=()):
     return "\n".join(out) + "\n"
 
 
-def emit_chunk(name, body_name, n_vars, coef, root, top_vars, f64, const_term=0.0):
+def emit_chunk(name, body_name, n_vars, coef, root, top_vars, f64, const_term=0.0, sync_every=0):
     """A device function  name(const T* x, T* acc):  acc[0] += E_chunk, acc[1+j] += dE_chunk/dx_j.
 
     FP64 chunks read their coefficients from the shared .const array (orbit
@@ -218,6 +218,14 @@ def emit_chunk(name, body_name, n_vars, coef, root, top_vars, f64, const_term=0.
     for j in sorted(used):
         out.append(" ld.%s %%x%d, [%%rd1+%d];" % (ty, j, sz * j))
         out.append(" mov.%s %%g%d, %s;" % (ty, j, zero))
+    if sync_every:
+        synced, n = [], 0
+        for l in body:
+            synced.append(l)
+            n += 1
+            if n % sync_every == 0:
+                synced.append("bar.sync 0;")
+        body = synced
     out.extend(" " + l for l in body)
     out.append(" ld.%s %%t, [%%rd2+0]; add.rn.%s %%t, %%t, %%S0; st.%s [%%rd2+0], %%t;" % (ty, ty, ty))
     for j in sorted(used):
@@ -228,77 +236,12 @@ def emit_chunk(name, body_name, n_vars, coef, root, top_vars, f64, const_term=0.
     return "\n".join(out) + "\n"
 
 
-def emit_chunk_pair(name, sym, n_vars, coef_index, n_distinct, root, top_vars, const_pair):
-    """Two clusters per thread: every register holds (cluster A, cluster B) as
-    .f32x2 and every FMA is one packed fma.rn.f32x2.  Coefficients are packed
-    (c, c) pairs in the .const array `sym` indexed through coef_index."""
-    body = []
-    used = set()
-    zero = "0x0000000000000000"
-
-    def operand(k):
-        body.append("ld.const.b64 %%c, [%s+%d];" % (sym, 8 * coef_index[k]))
-        return "%c"
-
-    def walk(node, pi, d):
-        S = "%%S%d" % d
-        if node.k is not None:
-            body.append("mov.b64 %s, %s;" % (S, operand(node.k)))
-        else:
-            body.append("mov.b64 %s, %s;" % (S, zero))
-        for j in sorted(node.ch):
-            ch = node.ch[j]
-            used.add(j)
-            if not ch.ch:
-                c = operand(ch.k)
-                body.append("fma.rn.f32x2 %s, %%x%d, %s, %s;" % (S, j, c, S))
-                body.append("fma.rn.f32x2 %%g%d, %s, %s, %%g%d;" % (j, pi, c, j))
-            else:
-                pic = "%%P%d" % (d + 1)
-                body.append("mul.rn.f32x2 %s, %s, %%x%d;" % (pic, pi, j))
-                walk(ch, pic, d + 1)
-                body.append("fma.rn.f32x2 %s, %%x%d, %%S%d, %s;" % (S, j, d + 1, S))
-                body.append("fma.rn.f32x2 %%g%d, %s, %%S%d, %%g%d;" % (j, pi, d + 1, j))
-
-    body.append("mov.b64 %%S0, 0x%016X;" % const_pair)
-    for j in top_vars:
-        ch = root.ch[j]
-        used.add(j)
-        if not ch.ch:
-            c = operand(ch.k)
-            body.append("fma.rn.f32x2 %%S0, %%x%d, %s, %%S0;" % (j, c))
-            body.append("add.rn.f32x2 %%g%d, %%g%d, %s;" % (j, j, c))
-        else:
-            walk(ch, "%%x%d" % j, 1)
-            body.append("fma.rn.f32x2 %%S0, %%x%d, %%S1, %%S0;" % j)
-            body.append("add.rn.f32x2 %%g%d, %%g%d, %%S1;" % (j, j))
-    out = ["// generated by gen_poly_ptx.py -- do not edit",
-           ".version 8.8\n.target sm_103a\n.address_size 64\n",
-           ".extern .const .align 8 .b64 %s[%d];" % (sym, n_distinct),
-           ".visible .func %s(.param .b64 px, .param .b64 pacc)\n{" % name,
-           " .reg .b64 %%x<%d>, %%g<%d>, %%S<6>, %%P<6>, %%c, %%t;" % (n_vars, n_vars),
-           " .reg .b64 %rd<3>;",
-           " ld.param.u64 %rd1, [px];",
-           " ld.param.u64 %rd2, [pacc];"]
-    for j in sorted(used):
-        out.append(" ld.b64 %%x%d, [%%rd1+%d];" % (j, 8 * j))
-        out.append(" mov.b64 %%g%d, %s;" % (j, zero))
-    out.extend(" " + l for l in body)
-    out.append(" ld.b64 %t, [%rd2+0]; add.rn.f32x2 %t, %t, %S0; st.b64 [%rd2+0], %t;")
-    for j in sorted(used):
-        off = 8 * (j + 1)
-        out.append(" ld.b64 %%t, [%%rd2+%d]; add.rn.f32x2 %%t, %%t, %%g%d; st.b64 [%%rd2+%d], %%t;" % (off, j, off))
-    out.append(" ret;\n}")
-    return "\n".join(out) + "\n"
-
-
-def _pair_hex(v):
-    h = struct.unpack("<I", struct.pack("<f", v))[0]
-    return (h << 32) | h
-
-
 # chunk counts: enough to keep every ptxas job short (they run in parallel)
-CHUNKS = {"2b": {"f64": 2, "f32": 4}, "3b": {"f64": 6, "f32": 12, "f32x2": 12}}
+CHUNKS = {"2b": {"f64": 2, "f32": 4}, "3b": {"f64": 6, "f32": 12, "f32s": 12}}
+# "f32s": FP32 chunks with a block barrier every SYNC_EVERY instructions.  The code of
+# one polynomial is ~1 MB, far larger than the instruction cache; keeping all warps
+# of a block on the same stretch of code lets them share every fetched line.
+SYNC_EVERY = 256
 
 
 def _write_if_changed(path, text):
@@ -330,27 +273,7 @@ def generate(table_dir, out_dir):
         root32 = build_trie([(i, m) for i, (m, _) in enumerate(items) if m])
         const32 = sp.get((), 0.0)
         root64 = build_trie(monos)
-        if "f32x2" in CHUNKS[body]:
-            # distinct FP32 coefficient values (the shifted polynomial keeps its orbits)
-            distinct = sorted(set(float(struct.unpack("<f", struct.pack("<f", c))[0]) for c in coef32))
-            where = {v: q for q, v in enumerate(distinct)}
-            cidx = [where[float(struct.unpack("<f", struct.pack("<f", c))[0])] for c in coef32]
-            psym = "MBX_COEF_%s_F32X2" % body.upper()
-            pair_tables.append((psym, distinct))
-            names = []
-            for c, top in enumerate(split_root(root32, CHUNKS[body]["f32x2"])):
-                name = "mbx_poly%s_f32x2_c%d" % (body, c)
-                cp = _pair_hex(const32) if c == 0 else 0
-                text = emit_chunk_pair(name, psym, n_vars, cidx, len(distinct), root32, top, cp)
-                path = os.path.join(out_dir, name + ".ptx")
-                _write_if_changed(path, text)
-                made.append(path)
-                names.append(name)
-                decls.append('extern "C" __device__ void %s(const float2* x, float2* acc);' % name)
-            disp.append("__device__ __forceinline__ void poly%s_pair(const float2* x, float2* acc) {" % body)
-            disp.extend("    %s(x, acc);" % n for n in names)
-            disp.append("}")
-        for prec in ("f64", "f32"):
+        for prec in [p for p in ("f64", "f32", "f32s") if p in CHUNKS[body]]:
             ctype = "double" if prec == "f64" else "float"
             root = root64 if prec == "f64" else root32
             cf = coef if prec == "f64" else coef32
@@ -359,14 +282,19 @@ def generate(table_dir, out_dir):
             for c, top in enumerate(chunks):
                 name = "mbx_poly%s_%s_c%d" % (body, prec, c)
                 text = emit_chunk(name, body, n_vars, cf, root, top, prec == "f64",
-                                  const_term=(const32 if (prec == "f32" and c == 0) else 0.0))
+                                  const_term=(const32 if (prec != "f64" and c == 0) else 0.0),
+                                  sync_every=SYNC_EVERY if prec == "f32s" else 0)
                 path = os.path.join(out_dir, name + ".ptx")
                 _write_if_changed(path, text)
                 made.append(path)
                 names.append(name)
                 decls.append('extern "C" __device__ void %s(const %s* x, %s* acc);' % (name, ctype, ctype))
-            disp.append("template <> __device__ __forceinline__ void poly%s<%s>(const %s* x, %s* acc) {"
-                        % (body, ctype, ctype, ctype))
+            if prec == "f32s":
+                disp.append("// every thread of the block must call this (block barriers inside)")
+                disp.append("__device__ __forceinline__ void poly%s_sync(const float* x, float* acc) {" % body)
+            else:
+                disp.append("template <> __device__ __forceinline__ void poly%s<%s>(const %s* x, %s* acc) {"
+                            % (body, ctype, ctype, ctype))
             disp.extend("    %s(x, acc);" % n for n in names)
             disp.append("}")
         decls.append("constexpr int kPoly%sVars = %d;" % (body.upper(), n_vars))
