@@ -279,7 +279,7 @@ def run_ours(args, rank, world):
     if os.path.exists(tfile):
         with open(tfile) as f:
             tj = json.load(f)
-        per = tj.get("k_mbpol_3b_float_bytes_per_trimer")
+        per = tj.get("k_mbpol_3b_bytes_per_trimer")
         if per:
             traffic = per * ntri
     value = world * args.steps / t_mixed

@@ -507,54 +507,6 @@ __device__ __forceinline__ void trimer_atoms(const MbpolArgs& a, int4 c, int* at
     at[6] = o3; at[7] = o3 + 1; at[8] = o3 + 2;
 }
 
-// Mixed-path 3B, every trimer in FP32.  The generated FP32 polynomial is ~1 MB of
-// straight-line code; its "sync" variant puts a block barrier every few hundred
-// instructions so that the eight warps of a block (one block per SM at 255
-// registers) walk the code together and share every instruction-cache line.  All
-// threads therefore call the polynomial: a thread without a trimer evaluates it at
-// the expansion point and discards the result.
-constexpr int kSyncThreads = 256;
-
-__global__ void __launch_bounds__(kSyncThreads) k_mbpol_3b_sync(MbpolArgs a, const int4* __restrict__ trip, int n) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool valid = t < n;
-    double red[14];
-#pragma unroll
-    for (int q = 0; q < 14; ++q) red[q] = 0.0;
-    float x[36], acc[37];
-    {
-        double w[27];
-        float p[27], fk[36];
-        if (valid) {
-            prep_3b<float>(a, trip[t], w, p);
-            vars_3b<float>(p, x, fk);
-        } else {
-#pragma unroll
-            for (int q = 0; q < 36; ++q) x[q] = 0.f;
-        }
-    }
-#pragma unroll
-    for (int q = 0; q < 37; ++q) acc[q] = 0.f;
-    poly3b_sync(x, acc);
-    if (valid) {
-        const int4 c = trip[t];
-        double w[27];
-        float p[27], fk[36], gt[27];
-        prep_3b<float>(a, c, w, p);
-        vars_3b<float>(p, x, fk);
-#pragma unroll
-        for (int q = 0; q < 27; ++q) gt[q] = 0.f;
-        const float e = finish_3b<float>(p, acc, fk, gt);
-        int at[9];
-        trimer_atoms(a, c, at);
-        double g[27];
-#pragma unroll
-        for (int q = 0; q < 27; ++q) g[q] = (double)gt[q];
-        cluster_accumulate<9>(a, at, (double)e, w, g, red);
-    }
-    flush_block_n<kSyncThreads>(red, a.acc, S_E3);
-}
-
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_mbpol_3b(MbpolArgs a, const int4* __restrict__ trip, int n,
                                                         const int* __restrict__ n_dev, HardList hl) {
@@ -685,8 +637,8 @@ cudaError_t launch_3b(const MbpolArgs& a, const int4* trip, int n, int precision
     if (precision == 0 || !(mp.limit3 > 0.f)) {
         k_mbpol_3b<double><<<blocks(n), kThreads, 0, s>>>(a, trip, n, nullptr, HardList{nullptr, nullptr, 0.f});
     } else if (!(mp.limit3 < 3.0e38f)) {
-        // no hand-off requested: every trimer in FP32, block-synchronised code walk
-        k_mbpol_3b_sync<<<(n + kSyncThreads - 1) / kSyncThreads, kSyncThreads, 0, s>>>(a, trip, n);
+        // no hand-off requested: every trimer in FP32
+        k_mbpol_3b<float><<<blocks(n), kThreads, 0, s>>>(a, trip, n, nullptr, HardList{nullptr, nullptr, 0.f});
     } else {
         k_mbpol_3b<float><<<blocks(n), kThreads, 0, s>>>(a, trip, n, nullptr,
                                                          HardList{mp.hard3, mp.count + 1, mp.limit3});

@@ -150,7 +150,7 @@ def emit_coef_module(tables, pair_tables=()):
     return "\n".join(out) + "\n"
 
 
-def emit_chunk(name, body_name, n_vars, coef, root, top_vars, f64, const_term=0.0, sync_every=0):
+def emit_chunk(name, body_name, n_vars, coef, root, top_vars, f64, const_term=0.0):
     """A device function  name(const T* x, T* acc):  acc[0] += E_chunk, acc[1+j] += dE_chunk/dx_j.
 
     FP64 chunks read their coefficients from the shared .const array (orbit
@@ -218,14 +218,6 @@ def emit_chunk(name, body_name, n_vars, coef, root, top_vars, f64, const_term=0.
     for j in sorted(used):
         out.append(" ld.%s %%x%d, [%%rd1+%d];" % (ty, j, sz * j))
         out.append(" mov.%s %%g%d, %s;" % (ty, j, zero))
-    if sync_every:
-        synced, n = [], 0
-        for l in body:
-            synced.append(l)
-            n += 1
-            if n % sync_every == 0:
-                synced.append("bar.sync 0;")
-        body = synced
     out.extend(" " + l for l in body)
     out.append(" ld.%s %%t, [%%rd2+0]; add.rn.%s %%t, %%t, %%S0; st.%s [%%rd2+0], %%t;" % (ty, ty, ty))
     for j in sorted(used):
@@ -237,11 +229,7 @@ def emit_chunk(name, body_name, n_vars, coef, root, top_vars, f64, const_term=0.
 
 
 # chunk counts: enough to keep every ptxas job short (they run in parallel)
-CHUNKS = {"2b": {"f64": 2, "f32": 4}, "3b": {"f64": 6, "f32": 12, "f32s": 12}}
-# "f32s": FP32 chunks with a block barrier every SYNC_EVERY instructions.  The code of
-# one polynomial is ~1 MB, far larger than the instruction cache; keeping all warps
-# of a block on the same stretch of code lets them share every fetched line.
-SYNC_EVERY = 256
+CHUNKS = {"2b": {"f64": 2, "f32": 4}, "3b": {"f64": 6, "f32": 12}}
 
 
 def _write_if_changed(path, text):
@@ -273,7 +261,7 @@ def generate(table_dir, out_dir):
         root32 = build_trie([(i, m) for i, (m, _) in enumerate(items) if m])
         const32 = sp.get((), 0.0)
         root64 = build_trie(monos)
-        for prec in [p for p in ("f64", "f32", "f32s") if p in CHUNKS[body]]:
+        for prec in ("f64", "f32"):
             ctype = "double" if prec == "f64" else "float"
             root = root64 if prec == "f64" else root32
             cf = coef if prec == "f64" else coef32
@@ -282,19 +270,14 @@ def generate(table_dir, out_dir):
             for c, top in enumerate(chunks):
                 name = "mbx_poly%s_%s_c%d" % (body, prec, c)
                 text = emit_chunk(name, body, n_vars, cf, root, top, prec == "f64",
-                                  const_term=(const32 if (prec != "f64" and c == 0) else 0.0),
-                                  sync_every=SYNC_EVERY if prec == "f32s" else 0)
+                                  const_term=(const32 if (prec != "f64" and c == 0) else 0.0))
                 path = os.path.join(out_dir, name + ".ptx")
                 _write_if_changed(path, text)
                 made.append(path)
                 names.append(name)
                 decls.append('extern "C" __device__ void %s(const %s* x, %s* acc);' % (name, ctype, ctype))
-            if prec == "f32s":
-                disp.append("// every thread of the block must call this (block barriers inside)")
-                disp.append("__device__ __forceinline__ void poly%s_sync(const float* x, float* acc) {" % body)
-            else:
-                disp.append("template <> __device__ __forceinline__ void poly%s<%s>(const %s* x, %s* acc) {"
-                            % (body, ctype, ctype, ctype))
+            disp.append("template <> __device__ __forceinline__ void poly%s<%s>(const %s* x, %s* acc) {"
+                        % (body, ctype, ctype, ctype))
             disp.extend("    %s(x, acc);" % n for n in names)
             disp.append("}")
         decls.append("constexpr int kPoly%sVars = %d;" % (body.upper(), n_vars))
