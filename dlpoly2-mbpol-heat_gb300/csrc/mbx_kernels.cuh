@@ -71,6 +71,9 @@ struct ListBuilder {
     int3 nc_last = {1, 1, 1};
     int all_pairs_last = 1;
     long launches_last = 0;  // kernels launched by the last phase1 + phase2 (CUB included)
+    // external = true: the buffers above were set by the caller (fixed capacities, no
+    // allocation, no cell sort: candidates are all waters); reserve() only checks sizes
+    bool external = false;
 
     ~ListBuilder();
     void release();

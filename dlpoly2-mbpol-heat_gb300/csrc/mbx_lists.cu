@@ -225,6 +225,7 @@ static void free_t(T*& p) {
 }
 
 void ListBuilder::release() {
+    if (external) return;
     free_t(key); free_t(skey); free_t(idx); free_t(sidx); free_t(cstart); free_t(cend);
     free_t(n2); free_t(l2); free_t(off2); free_t(n3); free_t(l3); free_t(tcnt); free_t(toff);
     free_t(flag); free_ptr(scan_tmp); free_ptr(sort_tmp);
@@ -234,6 +235,7 @@ void ListBuilder::release() {
 
 cudaError_t ListBuilder::reserve(int nw, int ncell) {
     cudaError_t e = cudaSuccess;
+    if (external) return (nw <= nw_cap && ncell <= ncell_cap) ? cudaSuccess : cudaErrorInvalidValue;
     if (nw > nw_cap || cap2 != cap2_alloc || cap3 != cap3_alloc) {
         free_t(key); free_t(skey); free_t(idx); free_t(sidx);
         free_t(n2); free_t(l2); free_t(off2); free_t(n3); free_t(l3); free_t(tcnt); free_t(toff);
@@ -281,7 +283,7 @@ cudaError_t ListBuilder::phase1(int nw, const int* list, const double* x, const 
     // grid: cells of at least the 2B cutoff; all-pairs if fewer than 3 per side or triclinic
     int3 nc = make_int3(1, 1, 1);
     int all_pairs = 1;
-    if (cl.imcon == 1 || cl.imcon == 2) {
+    if ((cl.imcon == 1 || cl.imcon == 2) && !external) {
         nc.x = (int)(cl.c[0] / kR2f);
         nc.y = (int)(cl.c[4] / kR2f);
         nc.z = (int)(cl.c[8] / kR2f);

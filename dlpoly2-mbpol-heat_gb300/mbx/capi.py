@@ -61,6 +61,8 @@ def load(path=None):
     L.mbx_set_profiling.argtypes = [C.c_void_p, C.c_int]
     L.mbx_last_timings.argtypes = [C.c_void_p, _D, _L]
     L.mbx_set_mixed_limits.argtypes = [C.c_void_p, C.c_double, C.c_double]
+    L.mbx_mbpol_forces_noalloc.argtypes = [C.c_int, C.c_int, _D, C.c_int, C.c_void_p, C.c_int] + \
+        [C.c_void_p] * 11 + [_D, C.c_void_p]
     L.mbx_last_lists.argtypes = [C.c_void_p, _I, C.c_long, _L, _I, C.c_long, _L]
     L.mbx_2b_poly_batch.argtypes = [C.c_void_p, C.c_int, C.c_long, _D, _D, _D, _D, _D]
     L.mbx_3b_poly_batch.argtypes = [C.c_void_p, C.c_int, C.c_long, _D, _D, _D, _D, _D, _D, _D]

@@ -100,6 +100,28 @@ int mbx_mbpol_forces_device(mbx_context* ctx, int precision, int imcon, const do
                             const double* vyy, const double* vzz, const double* weight, double* atomic_energy,
                             double* scalars);
 
+/*
+ * The same evaluation for callers that cannot allocate device memory at the point of
+ * the call: code running under CUDA stream capture, hosts whose device memory belongs
+ * to another allocator or pool, MD drivers that forbid allocation after start-up.  It
+ * needs no context and calls no cudaMalloc/cudaFree: every intermediate lives in one
+ * fixed-size static device array (~2.7 MB per GPU, held until the process exits).
+ * This entry point has no counterpart in the reference.
+ *   - limits: at most 512 waters (nttm2 <= 1536), 64 dimer partners and 48 3B
+ *     neighbours per water, 131072 trimers; larger systems return MBX_ERR_ARG or
+ *     MBX_ERR_CAPACITY (with a message on stderr) and compute nothing;
+ *   - arguments as mbx_mbpol_forces_device (device arrays, forces and atomic_energy
+ *     ACCUMULATED), `scalars` is a host array or NULL, `stream` a cudaStream_t or NULL;
+ *   - mixed precision uses the default split (2B FP64, 3B FP32);
+ *   - the first call on a device looks up the array's device address (make it before
+ *     any stream capture); every call shares the one array, so calls that overlap on
+ *     the GPU (other streams, other host threads) race and must be serialised.
+ */
+int mbx_mbpol_forces_noalloc(int precision, int imcon, const double* cell, int nttm2, const int* listttm2,
+                             int natms, const double* xxx, const double* yyy, const double* zzz, double* fxx,
+                             double* fyy, double* fzz, const double* vxx, const double* vyy, const double* vzz,
+                             const double* weight, double* atomic_energy, double* scalars, void* stream);
+
 /* Dimer and trimer lists of the last evaluation (0-based water indices, i<j<k), as
  * index sets; the host arrays receive up to cap entries; counts are always written. */
 int mbx_last_lists(mbx_context* ctx, int* pairs, long cap_pairs, long* npairs, int* trimers, long cap_trimers,
