@@ -407,6 +407,87 @@ extern "C" int mbx_mbpol_forces(mbx_context* ctx, int precision, int imcon, cons
     return MBX_OK;
 }
 
+extern "C" int mbx_ps_pes_forces_device(mbx_context* ctx, int imcon, const double* cell, int nang,
+                                        const int* listang, int natms, const double* xxx, const double* yyy,
+                                        const double* zzz, double* fxx, double* fyy, double* fzz, const double* vxx,
+                                        const double* vyy, const double* vzz, double* atomic_energy, double* out) {
+    if (!ctx) return MBX_ERR_ARG;
+    if (nang < 0 || (nang > 0 && !listang) || !xxx || !yyy || !zzz || !fxx || !fyy || !fzz || natms < 0)
+        return fail(ctx, MBX_ERR_ARG, "bad argument");
+    Cell cl;
+    int rc = make_cell(ctx, imcon, cell, cl);
+    if (rc) return rc;
+    CK(cudaSetDevice(ctx->device));
+    cudaStream_t s = ctx->stream;
+    const bool heat = vxx && vyy && vzz;
+    CK(cudaMemsetAsync(ctx->acc, 0, 14 * sizeof(double), s));
+    CK(launch_ps_pes(nang, listang, cl, xxx, yyy, zzz, fxx, fyy, fzz, atomic_energy, heat ? vxx : nullptr,
+                     heat ? vyy : nullptr, heat ? vzz : nullptr, ctx->acc, s));
+    CK(cudaMemcpyAsync(ctx->acc_h, ctx->acc, 14 * sizeof(double), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (out) std::memcpy(out, ctx->acc_h, 14 * sizeof(double));
+    return MBX_OK;
+}
+
+extern "C" int mbx_ps_pes_forces(mbx_context* ctx, int imcon, const double* cell, int nang, const int* listang,
+                                 int natms, const double* xxx, const double* yyy, const double* zzz, double* fxx,
+                                 double* fyy, double* fzz, double* engang, double* virang, double* stress,
+                                 const double* vxx, const double* vyy, const double* vzz, double* atomic_energy,
+                                 double* jpot) {
+    if (!ctx) return MBX_ERR_ARG;
+    if (nang < 0 || natms < 0 || !xxx || !yyy || !zzz || !fxx || !fyy || !fzz || !engang || !virang || !stress)
+        return fail(ctx, MBX_ERR_ARG, "NULL argument");
+    for (int q = 0; q < 3 * nang; ++q)
+        if (listang[q] < 1 || listang[q] > natms) return fail(ctx, MBX_ERR_ARG, "listang[%d] out of range", q);
+    CK(cudaSetDevice(ctx->device));
+    int rc = reserve_water(ctx, std::max((nang + 2) / 3, 1), std::max(natms, 1));
+    if (rc) return rc;
+    if ((long)3 * nang > 3L * ctx->nw_cap) {
+        rc = reserve_water(ctx, nang, std::max(natms, 1));
+        if (rc) return rc;
+    }
+    const bool heat = vxx && vyy && vzz;
+    cudaStream_t s = ctx->stream;
+    const size_t nb = (size_t)natms * sizeof(double);
+    double* d = ctx->atoms;
+    double *dx = d, *dy = d + natms, *dz = d + 2 * (size_t)natms;
+    double *dvx = d + 3 * (size_t)natms, *dvy = d + 4 * (size_t)natms, *dvz = d + 5 * (size_t)natms;
+    double *dfx = d + 7 * (size_t)natms, *dfy = d + 8 * (size_t)natms, *dfz = d + 9 * (size_t)natms;
+    double* dae = d + 10 * (size_t)natms;
+    if (nang) CK(cudaMemcpyAsync(ctx->list, listang, 3 * (size_t)nang * sizeof(int), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(dx, xxx, nb, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(dy, yyy, nb, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(dz, zzz, nb, cudaMemcpyHostToDevice, s));
+    if (heat) {
+        CK(cudaMemcpyAsync(dvx, vxx, nb, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(dvy, vyy, nb, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(dvz, vzz, nb, cudaMemcpyHostToDevice, s));
+    }
+    CK(cudaMemsetAsync(dfx, 0, 3 * nb, s));
+    if (atomic_energy) CK(cudaMemsetAsync(dae, 0, nb, s));
+    double out[14];
+    rc = mbx_ps_pes_forces_device(ctx, imcon, cell, nang, ctx->list, natms, dx, dy, dz, dfx, dfy, dfz,
+                                  heat ? dvx : nullptr, heat ? dvy : nullptr, heat ? dvz : nullptr,
+                                  atomic_energy ? dae : nullptr, out);
+    if (rc) return rc;
+    std::vector<double> h(4 * (size_t)natms);
+    CK(cudaMemcpyAsync(h.data(), dfx, 3 * nb, cudaMemcpyDeviceToHost, s));
+    if (atomic_energy) CK(cudaMemcpyAsync(h.data() + 3 * (size_t)natms, dae, nb, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    for (int i = 0; i < natms; ++i) {
+        fxx[i] += h[i];
+        fyy[i] += h[natms + i];
+        fzz[i] += h[2 * (size_t)natms + i];
+        if (atomic_energy) atomic_energy[i] += h[3 * (size_t)natms + i];
+    }
+    *engang += out[0];
+    *virang += out[1];
+    for (int q = 0; q < 9; ++q) stress[q] += out[2 + q];
+    if (jpot)
+        for (int q = 0; q < 3; ++q) jpot[q] += out[11 + q];
+    return MBX_OK;
+}
+
 extern "C" int mbx_last_lists(mbx_context* ctx, int* pairs, long cap_pairs, long* npairs, int* trimers,
                               long cap_trimers, long* ntrimers) {
     if (!ctx) return MBX_ERR_ARG;

@@ -53,6 +53,11 @@ cudaError_t launch_3b_direct(int n, const double* w1, const double* w2, const do
 cudaError_t launch_jkin(int nwat_atoms, const double* vx, const double* vy, const double* vz,
                         const double* mass, const double* ae, double* acc, cudaStream_t s);
 
+// 1-body PS PES over H-O-H angles (mbx_pes.cu); acc14 = {E, virial, stress[9], jpot[3]}.
+cudaError_t launch_ps_pes(int nang, const int* listang, const Cell& cl, const double* x, const double* y,
+                          const double* z, double* fx, double* fy, double* fz, double* ae, const double* vx,
+                          const double* vy, const double* vz, double* acc14, cudaStream_t s);
+
 __global__ void k_list_totals(int nw, const int* n2, const int* off2, const int* tcnt, const int* toff,
                               const int* flag, int* totals);
 

@@ -135,6 +135,35 @@ def extract(poly_cpp, model_cpp, n_vars, n_coef, out_path, title):
     return len(monos)
 
 
+def fortran_arrays(module_f90, module_name, names):
+    """Values of the initialised arrays `names` inside `module <module_name>` of a
+    Fortran source (array constructors (/ ... /), D exponents)."""
+    with open(module_f90) as f:
+        text = f.read()
+    start = text.index("module %s" % module_name)
+    end = text.index("end module %s" % module_name, start)
+    body = text[start:end]
+    out = {}
+    for name in names:
+        m = re.search(r"::\s*%s\s*\(\s*1\s*:\s*(\d+)\s*\)\s*=\s*\(/(.*?)/\)" % name, body, re.S)
+        if not m:
+            m = re.search(r"::\s*%s\s*\(\s*(\d+)\s*\)\s*=\s*\(/(.*?)/\)" % name, body, re.S)
+        n = int(m.group(1))
+        raw = m.group(2).replace("&", " ").replace("\n", " ")
+        vals = [v.strip() for v in raw.split(",") if v.strip()]
+        if len(vals) != n:
+            raise ValueError("%s: %d values, expected %d" % (name, len(vals), n))
+        out[name] = [v.replace("D", "E").replace("d", "e") for v in vals]
+    return out
+
+
+def write_arrays(path, title, arrays):
+    with open(path, "w") as f:
+        f.write("# %s\n" % title)
+        for name, vals in arrays.items():
+            f.write("%s %d %s\n" % (name, len(vals), " ".join(vals)))
+
+
 def main():
     src, out = sys.argv[1], sys.argv[2]
     os.makedirs(out, exist_ok=True)
@@ -145,6 +174,12 @@ def main():
                  36, 1163, os.path.join(out, "poly3b.tbl"),
                  "MB-pol 3B polynomial x3b_v2x (SOURCE/poly-3b-v2x.cpp, SOURCE/mbpol-3b-poly.cpp)")
     print("2B monomials %d, 3B monomials %d" % (n2, n3))
+    # 1-body Partridge-Schwenke PES (module ps_type_pes, SOURCE/module.f90:49-604)
+    pes = fortran_arrays(os.path.join(src, "module.f90"), "ps_type_pes",
+                         ["idx1", "idx2", "idx3", "c5z", "cbasis", "ccore", "crest", "cmass0",
+                          "idxm1", "idxm2", "idxm3"])
+    write_arrays(os.path.join(out, "ps_pes.tbl"),
+                 "Partridge-Schwenke 1-body PES expansion (module ps_type_pes, SOURCE/module.f90:49-604)", pes)
 
 
 if __name__ == "__main__":

@@ -1,0 +1,110 @@
+"""Generate the constant tables of the 1-body Partridge-Schwenke PES for the kernels.
+
+Input: tables/ps_pes.tbl (the raw arrays of module ps_type_pes, SOURCE/module.f90).
+The initialisation of init_ps_type_pes (SOURCE/module.f90:507-595) is applied here
+in IEEE double arithmetic with the reference's operation order (Python floats round
+every operation like the reference's x86-64 build, which has no fused multiply-add):
+mass-correction shift of `crest`, the weighted sum into c5z, the cm^-1 -> 10 J/mol
+conversion, and c5z(1) doubled.  Output: a C++ header with the final values.
+"""
+import math
+import os
+import struct
+import sys
+
+HHMASS = 1836.152697
+HDMASS = 3670.483031
+REOH = 0.958649
+B1 = 2.0
+ENGCNV = 1.19627
+F5Z = 0.99967788500000
+FBASIS = 0.15860145369897
+FCORE = -1.6351695982132
+FREST = 1.0
+PI = 3.141592653589793
+
+
+def read_arrays(path):
+    out = {}
+    with open(path) as f:
+        for line in f:
+            if line.startswith("#") or not line.strip():
+                continue
+            parts = line.split()
+            name, n = parts[0], int(parts[1])
+            vals = parts[2:]
+            assert len(vals) == n
+            out[name] = vals
+    return out
+
+
+def init_pes(a):
+    idx = [(int(a["idx1"][j]), int(a["idx2"][j]), int(a["idx3"][j])) for j in range(245)]
+    idxm = [(int(a["idxm1"][i]), int(a["idxm2"][i]), int(a["idxm3"][i])) for i in range(9)]
+    c5z = [float(v) for v in a["c5z"]]
+    cbasis = [float(v) for v in a["cbasis"]]
+    ccore = [float(v) for v in a["ccore"]]
+    crest = [float(v) for v in a["crest"]]
+    cmass = [0.0] * 9
+    for i in range(9):
+        cmass[i] = float(a["cmass0"][i]) / (1.0 / HDMASS - 1.0 / HHMASS)
+        fac = cmass[i] / HHMASS
+        if idxm[i][0] == idxm[i][1]:
+            fac = fac * 0.5
+        for j in range(245):
+            if idx[j][0] == idxm[i][0] and idx[j][1] == idxm[i][1] and idx[j][2] == idxm[i][2]:
+                crest[j] = crest[j] - fac
+                break
+        for j in range(245):
+            if idx[j][1] == idxm[i][0] and idx[j][0] == idxm[i][1] and idx[j][2] == idxm[i][2]:
+                crest[j] = crest[j] - fac
+                break
+    for i in range(245):
+        c5z[i] = F5Z * c5z[i] + FBASIS * cbasis[i] + FCORE * ccore[i] + FREST * crest[i]
+    for i in range(245):
+        c5z[i] = c5z[i] * ENGCNV
+    for i in range(9):
+        cmass[i] = cmass[i] * FREST * ENGCNV
+    thetae = 104.3475 * PI / 180.0
+    cose = math.cos(thetae)
+    c5z[0] = c5z[0] * 2.0
+    return idx, idxm, c5z, cmass, cose
+
+
+def _d(v):
+    return "__longlong_as_double(0x%016xLL)" % struct.unpack("<Q", struct.pack("<d", v))[0]
+
+
+def _hexd(v):
+    return "%s /* %.17g */" % ("0x%016xULL" % struct.unpack("<Q", struct.pack("<d", v))[0], v)
+
+
+def generate(table_dir, out_dir):
+    a = read_arrays(os.path.join(table_dir, "ps_pes.tbl"))
+    idx, idxm, c5z, cmass, cose = init_pes(a)
+    xm = 1.0 / HHMASS
+    lines = ["// generated by gen_pes.py -- do not edit", "#pragma once", "#include <stdint.h>", "",
+             "// Partridge-Schwenke 1-body PES after init_ps_type_pes (SOURCE/module.f90:507-595)",
+             "namespace mbx { namespace pes {",
+             "constexpr int kTerms = 245;",
+             "constexpr int kMass = 9;",
+             "__constant__ unsigned char kIdx[245][3] = {%s};" % ",".join("{%d,%d,%d}" % t for t in idx),
+             "__constant__ unsigned char kIdxm[9][3] = {%s};" % ",".join("{%d,%d,%d}" % t for t in idxm),
+             "__constant__ uint64_t kC5z[245] = {%s};" % ",".join(_hexd(v) for v in c5z),
+             "__constant__ uint64_t kCmass[9] = {%s};" % ",".join(_hexd(v) for v in cmass),
+             "constexpr uint64_t kCose = %s;" % _hexd(cose),
+             "constexpr uint64_t kXm = %s;" % _hexd(xm),
+             "constexpr double kReoh = %r;" % REOH,
+             "constexpr double kB1 = %r;" % B1,
+             "}}  // namespace mbx::pes", ""]
+    path = os.path.join(out_dir, "mbx_pes_gen.cuh")
+    text = "\n".join(lines)
+    old = open(path).read() if os.path.exists(path) else None
+    if old != text:
+        with open(path, "w") as f:
+            f.write(text)
+    return path
+
+
+if __name__ == "__main__":
+    print(generate(sys.argv[1], sys.argv[2]))

@@ -17,7 +17,7 @@ BUILD = os.path.join(PKG, "_build")
 CSRC = os.path.join(PKG, "csrc")
 LIB = os.path.join(BUILD, "libmbx.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CUDA_SOURCES = ["mbx_lists.cu", "mbx_mbpol.cu", "mbx_capi.cu", "mbx_noalloc.cu"]
+CUDA_SOURCES = ["mbx_lists.cu", "mbx_mbpol.cu", "mbx_capi.cu", "mbx_noalloc.cu", "mbx_pes.cu"]
 HEADERS = ["mbx_common.cuh", "mbx_kernels.cuh"]
 
 
@@ -64,6 +64,8 @@ def build_lib(verbose=False, jobs=None):
     gen_dir = os.path.join(BUILD, "gen")
     os.makedirs(gen_dir, exist_ok=True)
     ptx = gen_poly_ptx.generate(os.path.join(PKG, "tables"), gen_dir)
+    import gen_pes  # noqa: E402
+    gen_pes.generate(os.path.join(PKG, "tables"), gen_dir)
     nvcc = _nvcc()
     common = ARCH + ["-Xcompiler", "-fPIC", "-rdc=true"]
     jobs_list = []
@@ -72,6 +74,7 @@ def build_lib(verbose=False, jobs=None):
         if _newer(o, [p]):
             jobs_list.append((o, [nvcc] + common + ["-c", p, "-o", o]))
     hdr_deps = [os.path.join(CSRC, h) for h in HEADERS] + [os.path.join(gen_dir, "mbx_poly_gen.cuh"),
+                                                          os.path.join(gen_dir, "mbx_pes_gen.cuh"),
                                                           os.path.join(REPO, "include", "mbx.h")]
     cu_objs = []
     for src in CUDA_SOURCES:

@@ -63,6 +63,9 @@ def load(path=None):
     L.mbx_set_mixed_limits.argtypes = [C.c_void_p, C.c_double, C.c_double]
     L.mbx_mbpol_forces_noalloc.argtypes = [C.c_int, C.c_int, _D, C.c_int, C.c_void_p, C.c_int] + \
         [C.c_void_p] * 11 + [_D, C.c_void_p]
+    L.mbx_ps_pes_forces.argtypes = [C.c_void_p, C.c_int, _D, C.c_int, _I, C.c_int] + [_D] * 14
+    L.mbx_ps_pes_forces_device.argtypes = [C.c_void_p, C.c_int, _D, C.c_int, C.c_void_p, C.c_int] + \
+        [C.c_void_p] * 10 + [_D]
     L.mbx_last_lists.argtypes = [C.c_void_p, _I, C.c_long, _L, _I, C.c_long, _L]
     L.mbx_2b_poly_batch.argtypes = [C.c_void_p, C.c_int, C.c_long, _D, _D, _D, _D, _D]
     L.mbx_3b_poly_batch.argtypes = [C.c_void_p, C.c_int, C.c_long, _D, _D, _D, _D, _D, _D, _D]
@@ -138,6 +141,25 @@ class Context:
                    forces=f.T.copy(), atomic_energy=ae, jpot=sc[S_JPOT:S_JPOT + 3].copy(),
                    jkin=sc[S_JKIN:S_JKIN + 3].copy(), engsrp=eng.value, virsrp=vir.value, stress_acc=stress)
         return out
+
+    def ps_pes(self, box, heat=True):
+        """1-body PS PES over the box's H-O-H angles (host arrays)."""
+        n = box.natms
+        x, y, z = (_f64(box.xyz[:, k]) for k in range(3))
+        f = np.zeros((3, n))
+        eng = C.c_double(0)
+        vir = C.c_double(0)
+        stress = np.zeros(9)
+        ae = np.zeros(n)
+        jpot = np.zeros(3)
+        v = [_f64(box.vel[:, k]) for k in range(3)] if heat else [None] * 3
+        lst = np.ascontiguousarray(box.listang(), dtype=np.int32)
+        rc = self.lib.mbx_ps_pes_forces(self.h, box.imcon, _p(_f64(box.cell)), box.nw, _p(lst, _I), n, _p(x), _p(y),
+                                        _p(z), _p(f[0]), _p(f[1]), _p(f[2]), C.byref(eng), C.byref(vir), _p(stress),
+                                        _p(v[0]), _p(v[1]), _p(v[2]), _p(ae), _p(jpot))
+        self._check(rc, "mbx_ps_pes_forces")
+        return dict(engang=eng.value, virang=vir.value, stress=stress, forces=f.T.copy(), atomic_energy=ae,
+                    jpot=jpot)
 
     def mbpol_forces_device(self, precision, imcon, cell, nttm2, list_ptr, natms, xyz_ptrs, f_ptrs, v_ptrs=None,
                             mass_ptr=None, ae_ptr=None):

@@ -61,6 +61,11 @@ class WaterBox:
         """1-based atom indices of the water atoms (O,H1,H2 per molecule)."""
         return np.arange(1, 3 * self.nw + 1, dtype=np.int32)
 
+    def listang(self):
+        """1-based H-O-H angle triples (H1, O, H2), O the central atom (angfrc's ib)."""
+        o = 3 * np.arange(self.nw, dtype=np.int32) + 1
+        return np.stack([o + 1, o, o + 2], 1).astype(np.int32)
+
     def monomers(self):
         return np.ascontiguousarray(self.xyz[:3 * self.nw].reshape(self.nw, 9))
 

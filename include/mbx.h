@@ -122,6 +122,28 @@ int mbx_mbpol_forces_noalloc(int precision, int imcon, const double* cell, int n
                              double* fyy, double* fzz, const double* vxx, const double* vyy, const double* vzz,
                              const double* weight, double* atomic_energy, double* scalars, void* stream);
 
+/*
+ * 1-body MB-pol monomer term: the Partridge-Schwenke water PES with the angfrc
+ * bookkeeping.  Replaces angfrc for angle type 9 (SOURCE/angfrc.f:150-545, calling
+ * ps_type_couple, SOURCE/ps_type_couple.f90:15-274) with its HEAT_CURRENT hooks.
+ *   nang, listang[3*nang]  H-O-H angles as (ia, ib, ic), 1-based, ib the central O
+ *                          (listang(:,2:4) of the reference)
+ *   fxx..                  ACCUMULATED; engang, virang, stress[9] ACCUMULATED
+ *   vxx..                  velocities or NULL; jpot[3] ACCUMULATED (the force-matrix
+ *                          entries (ia,ib),(ib,ia),(ic,ib),(ib,ic) contracted)
+ *   atomic_energy          ACCUMULATED with pterm/3 per atom, or NULL
+ * Host arrays; the _device variant takes device arrays and returns
+ * out[14] = {engang, virang, stress[9], jpot[3]} on the host.
+ */
+int mbx_ps_pes_forces(mbx_context* ctx, int imcon, const double* cell, int nang, const int* listang, int natms,
+                      const double* xxx, const double* yyy, const double* zzz, double* fxx, double* fyy,
+                      double* fzz, double* engang, double* virang, double* stress, const double* vxx,
+                      const double* vyy, const double* vzz, double* atomic_energy, double* jpot);
+int mbx_ps_pes_forces_device(mbx_context* ctx, int imcon, const double* cell, int nang, const int* listang,
+                             int natms, const double* xxx, const double* yyy, const double* zzz, double* fxx,
+                             double* fyy, double* fzz, const double* vxx, const double* vyy, const double* vzz,
+                             double* atomic_energy, double* out);
+
 /* Dimer and trimer lists of the last evaluation (0-based water indices, i<j<k), as
  * index sets; the host arrays receive up to cap entries; counts are always written. */
 int mbx_last_lists(mbx_context* ctx, int* pairs, long cap_pairs, long* npairs, int* trimers, long cap_trimers,

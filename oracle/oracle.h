@@ -91,6 +91,16 @@ double orc_mbpol_ranks(int imcon, const double* cell, int nw, const int* listttm
                        const double* y, const double* z, int natms, int rank_begin, int rank_end, int size,
                        int nthreads);
 
+/* 1-body Partridge-Schwenke PES (SOURCE/ps_type_couple.f90, SOURCE/angfrc.f keya 9).
+ * orc_pes_load reads tables/ps_pes.tbl and applies init_ps_type_pes. */
+int orc_pes_load(const char* path);
+void orc_ps_couple(double roh1, double xoh1, double yoh1, double zoh1, double roh2, double xoh2, double yoh2,
+                   double zoh2, double theta, double* pterm, double* fdum, double* vterm);
+int orc_angfrc_ps(int imcon, const double* cell, int nang, const int* listang, const double* x, const double* y,
+                  const double* z, double* fx, double* fy, double* fz, double* engang, double* virang,
+                  double* stress, double* atomic_energy, const double* vx, const double* vy, const double* vz,
+                  double* jpot);
+
 /* image_monomers (SOURCE/mbpol.f90:1275-1301): H atoms next to their O. */
 void orc_image_monomers(int imcon, const double* cell, int nw, double* xyz);
 

@@ -47,6 +47,11 @@ class Oracle:
         L.orc_mbpol_ranks.argtypes = [C.c_int, _D, C.c_int, _I, _D, _D, _D, C.c_int, C.c_int, C.c_int, C.c_int,
                                       C.c_int]
         L.orc_mbpol_ranks.restype = C.c_double
+        L.orc_pes_load.argtypes = [C.c_char_p]
+        L.orc_ps_couple.argtypes = [C.c_double] * 9 + [_D, _D, _D]
+        L.orc_angfrc_ps.argtypes = [C.c_int, _D, C.c_int, _I] + [_D] * 14
+        if L.orc_pes_load(os.path.join(TABLES, "ps_pes.tbl").encode()):
+            raise RuntimeError("orc_pes_load failed")
         rc = L.orc_load_tables(os.path.join(TABLES, "poly2b.tbl").encode(),
                                os.path.join(TABLES, "poly3b.tbl").encode())
         if rc:
@@ -141,6 +146,24 @@ class Oracle:
         lst = np.ascontiguousarray(box.listttm2(), dtype=np.int32)
         return self.lib.orc_mbpol_ranks(box.imcon, _p(box.cell), box.nw, _p(lst, _I), _p(x), _p(y), _p(z),
                                         box.natms, rank_begin, rank_end, size, nthreads)
+
+    def angfrc_ps(self, box, velocities=True):
+        """angfrc (keya 9) over the box's H-O-H angles with the heat hooks."""
+        n = box.natms
+        x, y, z = (np.ascontiguousarray(box.xyz[:, k]) for k in range(3))
+        f = np.zeros((3, n))
+        eng = C.c_double(0)
+        vir = C.c_double(0)
+        stress = np.zeros(9)
+        ae = np.zeros(n)
+        jpot = np.zeros(3)
+        v = [np.ascontiguousarray(box.vel[:, k]) for k in range(3)] if velocities else [None] * 3
+        lst = np.ascontiguousarray(box.listang(), dtype=np.int32)
+        self.lib.orc_angfrc_ps(box.imcon, _p(box.cell), box.nw, _p(lst, _I), _p(x), _p(y), _p(z), _p(f[0]),
+                               _p(f[1]), _p(f[2]), C.byref(eng), C.byref(vir), _p(stress), _p(ae), _p(v[0]),
+                               _p(v[1]), _p(v[2]), _p(jpot))
+        return dict(engang=eng.value, virang=vir.value, stress=stress, forces=f.T.copy(), atomic_energy=ae,
+                    jpot=jpot)
 
     def image_monomers(self, box):
         m = box.monomers().copy()

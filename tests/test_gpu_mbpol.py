@@ -215,3 +215,16 @@ def test_mixed_handoff_limits(mbx_ctx, refs):
         assert hd == 0 and ht == 0
     finally:
         mbx_ctx.set_mixed_limits(0.0, 3.4e38)
+
+
+@pytest.mark.parametrize("name", ["cfg0_256", "ortho_imcon2", "shuffled_layout"])
+def test_ps_pes_fp64_matches_oracle(mbx_ctx, oracle_lib, name):
+    box = BOXES[name]
+    ref = oracle_lib.angfrc_ps(box)
+    got = mbx_ctx.ps_pes(box)
+    assert abs(got["engang"] - ref["engang"]) <= TOL64 * abs(ref["engang"])
+    assert abs(got["virang"] - ref["virang"]) <= TOL64 * abs(ref["virang"])
+    assert rel_err(got["stress"], ref["stress"]) <= TOL64
+    assert rel_err(got["forces"], ref["forces"]) <= TOL64
+    assert rel_err(got["atomic_energy"], ref["atomic_energy"]) <= TOL64
+    assert rel_err(got["jpot"], ref["jpot"]) <= TOL64
