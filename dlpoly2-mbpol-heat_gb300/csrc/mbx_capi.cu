@@ -488,6 +488,58 @@ extern "C" int mbx_ps_pes_forces(mbx_context* ctx, int imcon, const double* cell
     return MBX_OK;
 }
 
+extern "C" int mbx_msites_dms_device(mbx_context* ctx, int imcon, const double* cell, int nttm2,
+                                     const int* listttm2, int natms, double gamma, double* xxx, double* yyy,
+                                     double* zzz, double* chge, double* dqdr) {
+    if (!ctx) return MBX_ERR_ARG;
+    if (nttm2 < 0 || nttm2 % 3 || (nttm2 && !listttm2) || !xxx || !yyy || !zzz || natms < 4 * (nttm2 / 3))
+        return fail(ctx, MBX_ERR_ARG, "bad argument");
+    Cell cl;
+    int rc = make_cell(ctx, imcon, cell, cl);
+    if (rc) return rc;
+    CK(cudaSetDevice(ctx->device));
+    CK(launch_msites_dms(nttm2 / 3, listttm2, cl, xxx, yyy, zzz, gamma, chge, dqdr, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return MBX_OK;
+}
+
+extern "C" int mbx_msites_dms(mbx_context* ctx, int imcon, const double* cell, int nttm2, const int* listttm2,
+                              int natms, double gamma, double* xxx, double* yyy, double* zzz, double* chge,
+                              double* dqdr) {
+    if (!ctx) return MBX_ERR_ARG;
+    if (nttm2 < 0 || nttm2 % 3 || !xxx || !yyy || !zzz) return fail(ctx, MBX_ERR_ARG, "bad argument");
+    const int nw = nttm2 / 3;
+    if (nw == 0) return MBX_OK;
+    for (int t = 0; t < nttm2; ++t)
+        if (listttm2[t] < 1 || listttm2[t] > natms || (t % 3 && listttm2[t] != listttm2[t - t % 3] + t % 3))
+            return fail(ctx, MBX_ERR_ARG, "listttm2[%d]=%d: 1-based, O,H1,H2 consecutive", t, listttm2[t]);
+    if (listttm2[nttm2 - 1] + nw > natms) return fail(ctx, MBX_ERR_ARG, "M sites beyond natms");
+    CK(cudaSetDevice(ctx->device));
+    int rc = reserve_water(ctx, nw, natms);
+    if (rc) return rc;
+    cudaStream_t s = ctx->stream;
+    const size_t nb = (size_t)natms * sizeof(double);
+    double* d = ctx->atoms;
+    double *dx = d, *dy = d + natms, *dz = d + 2 * (size_t)natms, *dq = d + 3 * (size_t)natms;
+    double* ddp = d + 4 * (size_t)natms;   // 6*nw <= 6*natms/4 fits in the 7*natms that follow
+    CK(cudaMemcpyAsync(ctx->list, listttm2, nttm2 * sizeof(int), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(dx, xxx, nb, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(dy, yyy, nb, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(dz, zzz, nb, cudaMemcpyHostToDevice, s));
+    if (chge) CK(cudaMemcpyAsync(dq, chge, nb, cudaMemcpyHostToDevice, s));
+    Cell cl;
+    rc = make_cell(ctx, imcon, cell, cl);
+    if (rc) return rc;
+    CK(launch_msites_dms(nw, ctx->list, cl, dx, dy, dz, gamma, chge ? dq : nullptr, dqdr ? ddp : nullptr, s));
+    CK(cudaMemcpyAsync(xxx, dx, nb, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(yyy, dy, nb, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(zzz, dz, nb, cudaMemcpyDeviceToHost, s));
+    if (chge) CK(cudaMemcpyAsync(chge, dq, nb, cudaMemcpyDeviceToHost, s));
+    if (dqdr) CK(cudaMemcpyAsync(dqdr, ddp, 6 * (size_t)nw * sizeof(double), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    return MBX_OK;
+}
+
 extern "C" int mbx_last_lists(mbx_context* ctx, int* pairs, long cap_pairs, long* npairs, int* trimers,
                               long cap_trimers, long* ntrimers) {
     if (!ctx) return MBX_ERR_ARG;

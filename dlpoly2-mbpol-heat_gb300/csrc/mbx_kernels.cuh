@@ -58,6 +58,11 @@ cudaError_t launch_ps_pes(int nang, const int* listang, const Cell& cl, const do
                           const double* z, double* fx, double* fy, double* fz, double* ae, const double* vx,
                           const double* vy, const double* vz, double* acc14, cudaStream_t s);
 
+// M sites written into x/y/z at index listttm2[3nw-1] + i (0-based) and DMS charges
+// into chge (H1, H2, M) and dp[6*nw] (mbx_pes.cu); chge/dp may be null.
+cudaError_t launch_msites_dms(int nw, const int* list, const Cell& cl, double* x, double* y, double* z, double gamma,
+                              double* chge, double* dp, cudaStream_t s);
+
 __global__ void k_list_totals(int nw, const int* n2, const int* off2, const int* tcnt, const int* toff,
                               const int* flag, int* totals);
 

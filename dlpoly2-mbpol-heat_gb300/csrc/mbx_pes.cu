@@ -162,7 +162,91 @@ __global__ void __launch_bounds__(kThreads) k_ps_pes(int nang, const int* __rest
     block_sum_atomic<14>(red, acc);
 }
 
+// M-site placement (SOURCE/dlpoly_cmd.f:2041-2057) and qdetermine with the MB-pol
+// settings (ldms, new charge assignment; SOURCE/qdetermine.f90:112-285): one thread per
+// water writes r_M, q_H1, q_H2, q_M and dq/d(r1, r2, cos) (6 values) for qdforce.
+__global__ void __launch_bounds__(kThreads) k_msites_dms(int nw, const int* __restrict__ list, Cell cl, double* x,
+                                                          double* y, double* z, double gamma, double* chge,
+                                                          double* dp) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nw) return;
+    const int io = list[3 * i] - 1, h1 = list[3 * i + 1] - 1, h2 = list[3 * i + 2] - 1;
+    const int m = list[3 * nw - 1] + i;   // 0-based index of this water's M site
+    double r1x = x[h1] - x[io], r1y = y[h1] - y[io], r1z = z[h1] - z[io];
+    double r2x = x[h2] - x[io], r2y = y[h2] - y[io], r2z = z[h2] - z[io];
+    image(cl, r1x, r1y, r1z);
+    image(cl, r2x, r2y, r2z);
+    x[m] = x[io] + (r1x + r2x) * gamma / 2.0;
+    y[m] = y[io] + (r1y + r2y) * gamma / 2.0;
+    z[m] = z[io] + (r1z + r2z) * gamma / 2.0;
+    if (!chge) return;
+    const double reoh = pes::kReoh;
+    const double r1 = sqrt(r1x * r1x + r1y * r1y + r1z * r1z);
+    const double r2 = sqrt(r2x * r2x + r2y * r2y + r2z * r2z);
+    const double cost = (r1x * r2x + r1y * r2y + r1z * r2z) / (r1 * r2);
+    const double x1 = (r1 - reoh) / reoh, x2 = (r2 - reoh) / reoh;
+    const double x3 = cost - __longlong_as_double((long long)pes::kCose);
+    double fm[pes::kDmsIsump + 1][3];
+    fm[0][0] = fm[0][1] = fm[0][2] = 0.0;
+    fm[1][0] = fm[1][1] = fm[1][2] = 1.0;
+#pragma unroll
+    for (int j = 2; j <= pes::kDmsIsump; ++j) {
+        fm[j][0] = fm[j - 1][0] * x1;
+        fm[j][1] = fm[j - 1][1] * x2;
+        fm[j][2] = fm[j - 1][2] * x3;
+    }
+    double p1 = 0, p2 = 0, d11 = 0, d12 = 0, d21 = 0, d22 = 0, d1c = 0, d2c = 0;
+    for (int j = 1; j < pes::kDmsTerms; ++j) {
+        const int i1 = pes::kDmsIdx[j][0], i2 = pes::kDmsIdx[j][1], i3 = pes::kDmsIdx[j][2];
+        const double c = __longlong_as_double((long long)pes::kDmsCoef[j]);
+        p1 += c * fm[i1][0] * fm[i2][1] * fm[i3][2];
+        p2 += c * fm[i2][0] * fm[i1][1] * fm[i3][2];
+        d11 += c * (i1 - 1) * fm[i1 - 1][0] * fm[i2][1] * fm[i3][2] / reoh;
+        d12 += c * (i2 - 1) * fm[i1][0] * fm[i2 - 1][1] * fm[i3][2] / reoh;
+        d21 += c * (i2 - 1) * fm[i2 - 1][0] * fm[i1][1] * fm[i3][2] / reoh;
+        d22 += c * (i1 - 1) * fm[i2][0] * fm[i1 - 1][1] * fm[i3][2] / reoh;
+        d1c += c * (i3 - 1) * fm[i1][0] * fm[i2][1] * fm[i3 - 1][2];
+        d2c += c * (i3 - 1) * fm[i2][0] * fm[i1][1] * fm[i3 - 1][2];
+    }
+    const double bohr = 0.529177249, b1dms = 1.0, adms = 0.2999 * bohr, bdms = -0.6932;
+    const double c0 = 1.0099, c1 = -0.1801, c2 = 0.0892;
+    const double pl1 = cost, pl2 = 0.5 * (3.0 * pl1 * pl1 - 1.0);
+    const double damp = exp(-b1dms * ((r1 - reoh) * (r1 - reoh) + (r2 - reoh) * (r2 - reoh)));
+    const double dd1 = -2.0 * b1dms * (r1 - reoh) * damp, dd2 = -2.0 * b1dms * (r2 - reoh) * damp;
+    const double ang = c0 + pl1 * c1 + pl2 * c2;
+    const double q1b = pow(r1, bdms), q2b = pow(r2, bdms);
+    const double pc0 = adms * (q1b + q2b) * ang;
+    const double dpc0dr1 = adms * (bdms * pow(r1, bdms - 1)) * ang;
+    const double dpc0dr2 = adms * (bdms * pow(r2, bdms - 1)) * ang;
+    const double dpc0dcos = adms * (q1b + q2b) * (c1 + 3.0 * c2 * pl1);
+    d11 = d11 * damp + p1 * dd1 + dpc0dr1;
+    d12 = d12 * damp + p1 * dd2 + dpc0dr2;
+    d21 = d21 * damp + p2 * dd1 + dpc0dr1;
+    d22 = d22 * damp + p2 * dd2 + dpc0dr2;
+    d1c = d1c * damp + dpc0dcos;
+    d2c = d2c * damp + dpc0dcos;
+    const double c00 = __longlong_as_double((long long)pes::kDmsCoef[0]);
+    p1 = c00 + p1 * damp + pc0;
+    p2 = c00 + p2 * damp + pc0;
+    const double factor = gamma / 2.0 / (1.0 - gamma);
+    const double qh1 = p1 + factor * (p1 + p2), qh2 = p2 + factor * (p1 + p2);
+    chge[h1] = qh1;
+    chge[h2] = qh2;
+    chge[m] = -(qh1 + qh2);
+    if (dp) {
+        double* o = dp + 6 * (size_t)i;
+        o[0] = d11; o[1] = d12; o[2] = d21; o[3] = d22; o[4] = d1c; o[5] = d2c;
+    }
+}
+
 }  // namespace
+
+cudaError_t launch_msites_dms(int nw, const int* list, const Cell& cl, double* x, double* y, double* z, double gamma,
+                              double* chge, double* dp, cudaStream_t s) {
+    if (nw <= 0) return cudaSuccess;
+    k_msites_dms<<<(nw + kThreads - 1) / kThreads, kThreads, 0, s>>>(nw, list, cl, x, y, z, gamma, chge, dp);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_ps_pes(int nang, const int* listang, const Cell& cl, const double* x, const double* y,
                           const double* z, double* fx, double* fy, double* fz, double* ae, const double* vx,

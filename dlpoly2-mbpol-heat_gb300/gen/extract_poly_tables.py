@@ -180,6 +180,10 @@ def main():
                           "idxm1", "idxm2", "idxm3"])
     write_arrays(os.path.join(out, "ps_pes.tbl"),
                  "Partridge-Schwenke 1-body PES expansion (module ps_type_pes, SOURCE/module.f90:49-604)", pes)
+    # Partridge-Schwenke dipole-moment surface (module ps_type_dms, SOURCE/module.f90:745-918)
+    dms = fortran_arrays(os.path.join(src, "module.f90"), "ps_type_dms", ["idx1", "idx2", "idx3", "coef"])
+    write_arrays(os.path.join(out, "ps_dms.tbl"),
+                 "Partridge-Schwenke dipole-moment surface (module ps_type_dms, SOURCE/module.f90:745-918)", dms)
 
 
 if __name__ == "__main__":

@@ -83,6 +83,10 @@ def generate(table_dir, out_dir):
     a = read_arrays(os.path.join(table_dir, "ps_pes.tbl"))
     idx, idxm, c5z, cmass, cose = init_pes(a)
     xm = 1.0 / HHMASS
+    d = read_arrays(os.path.join(table_dir, "ps_dms.tbl"))
+    didx = [(int(d["idx1"][j]), int(d["idx2"][j]), int(d["idx3"][j])) for j in range(84)]
+    dcoef = [float(v) for v in d["coef"]]
+    isump = max(max(t) for t in didx)
     lines = ["// generated by gen_pes.py -- do not edit", "#pragma once", "#include <stdint.h>", "",
              "// Partridge-Schwenke 1-body PES after init_ps_type_pes (SOURCE/module.f90:507-595)",
              "namespace mbx { namespace pes {",
@@ -95,6 +99,11 @@ def generate(table_dir, out_dir):
              "constexpr uint64_t kCose = %s;" % _hexd(cose),
              "constexpr uint64_t kXm = %s;" % _hexd(xm),
              "constexpr double kReoh = %r;" % REOH,
+             "// Partridge-Schwenke dipole-moment surface (module ps_type_dms, SOURCE/module.f90:745-918)",
+             "constexpr int kDmsTerms = 84;",
+             "constexpr int kDmsIsump = %d;" % isump,
+             "__constant__ unsigned char kDmsIdx[84][3] = {%s};" % ",".join("{%d,%d,%d}" % t for t in didx),
+             "__constant__ uint64_t kDmsCoef[84] = {%s};" % ",".join(_hexd(v) for v in dcoef),
              "constexpr double kB1 = %r;" % B1,
              "}}  // namespace mbx::pes", ""]
     path = os.path.join(out_dir, "mbx_pes_gen.cuh")

@@ -66,6 +66,9 @@ def load(path=None):
     L.mbx_ps_pes_forces.argtypes = [C.c_void_p, C.c_int, _D, C.c_int, _I, C.c_int] + [_D] * 14
     L.mbx_ps_pes_forces_device.argtypes = [C.c_void_p, C.c_int, _D, C.c_int, C.c_void_p, C.c_int] + \
         [C.c_void_p] * 10 + [_D]
+    L.mbx_msites_dms.argtypes = [C.c_void_p, C.c_int, _D, C.c_int, _I, C.c_int, C.c_double] + [_D] * 5
+    L.mbx_msites_dms_device.argtypes = [C.c_void_p, C.c_int, _D, C.c_int, C.c_void_p, C.c_int, C.c_double] + \
+        [C.c_void_p] * 5
     L.mbx_last_lists.argtypes = [C.c_void_p, _I, C.c_long, _L, _I, C.c_long, _L]
     L.mbx_2b_poly_batch.argtypes = [C.c_void_p, C.c_int, C.c_long, _D, _D, _D, _D, _D]
     L.mbx_3b_poly_batch.argtypes = [C.c_void_p, C.c_int, C.c_long, _D, _D, _D, _D, _D, _D, _D]
@@ -160,6 +163,16 @@ class Context:
         self._check(rc, "mbx_ps_pes_forces")
         return dict(engang=eng.value, virang=vir.value, stress=stress, forces=f.T.copy(), atomic_energy=ae,
                     jpot=jpot)
+
+    def msites_dms(self, box, gamma=0.426706882):
+        """M sites and DMS charges (host arrays): (xyz with M sites, chge, dqdr[nw, 6])."""
+        x, y, z = (_f64(box.xyz[:, k]).copy() for k in range(3))
+        q = np.zeros(box.natms)
+        dp = np.zeros((box.nw, 6))
+        lst = np.ascontiguousarray(box.listttm2(), dtype=np.int32)
+        self._check(self.lib.mbx_msites_dms(self.h, box.imcon, _p(_f64(box.cell)), 3 * box.nw, _p(lst, _I),
+                                            box.natms, gamma, _p(x), _p(y), _p(z), _p(q), _p(dp)), "mbx_msites_dms")
+        return np.stack([x, y, z], 1), q, dp
 
     def mbpol_forces_device(self, precision, imcon, cell, nttm2, list_ptr, natms, xyz_ptrs, f_ptrs, v_ptrs=None,
                             mass_ptr=None, ae_ptr=None):

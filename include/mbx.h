@@ -144,6 +144,23 @@ int mbx_ps_pes_forces_device(mbx_context* ctx, int imcon, const double* cell, in
                              double* fyy, double* fzz, const double* vxx, const double* vyy, const double* vzz,
                              double* atomic_energy, double* out);
 
+/*
+ * M sites and Partridge-Schwenke dipole-moment-surface charges with MB-pol's settings
+ * (ldms, new charge assignment, gamma = 0.426706882).  Replaces the M-site placement of
+ * SOURCE/dlpoly_cmd.f:2041-2057 and qdetermine (SOURCE/qdetermine.f90:15-321).
+ *   xxx,yyy,zzz      M-site positions WRITTEN at 1-based index listttm2[nttm2-1] + i
+ *                    for water i = 1..nw (H and O read)
+ *   chge             q_H1, q_H2, q_M WRITTEN (other entries untouched), or NULL
+ *   dqdr[6*nw]       per water {dp1dr1, dp1dr2, dp2dr1, dp2dr2, dp1dcos, dp2dcos} (the
+ *                    arrays qdforce contracts), or NULL
+ * mbx_msites_dms takes host arrays; the _device variant device arrays.
+ */
+int mbx_msites_dms(mbx_context* ctx, int imcon, const double* cell, int nttm2, const int* listttm2, int natms,
+                   double gamma, double* xxx, double* yyy, double* zzz, double* chge, double* dqdr);
+int mbx_msites_dms_device(mbx_context* ctx, int imcon, const double* cell, int nttm2, const int* listttm2,
+                          int natms, double gamma, double* xxx, double* yyy, double* zzz, double* chge,
+                          double* dqdr);
+
 /* Dimer and trimer lists of the last evaluation (0-based water indices, i<j<k), as
  * index sets; the host arrays receive up to cap entries; counts are always written. */
 int mbx_last_lists(mbx_context* ctx, int* pairs, long cap_pairs, long* npairs, int* trimers, long cap_trimers,

@@ -101,6 +101,14 @@ int orc_angfrc_ps(int imcon, const double* cell, int nang, const int* listang, c
                   double* stress, double* atomic_energy, const double* vx, const double* vy, const double* vz,
                   double* jpot);
 
+/* M sites (SOURCE/dlpoly_cmd.f:2041-2057) and DMS charges (SOURCE/qdetermine.f90, MB-pol
+ * settings).  M site of water i is atom listttm2[3nw-1] + i (1-based). */
+int orc_dms_load(const char* path);
+void orc_msites(int imcon, const double* cell, int nw, const int* listttm2, double* x, double* y, double* z,
+                double gamma);
+double orc_qdetermine(int imcon, const double* cell, int nw, const int* listttm2, const double* x, const double* y,
+                      const double* z, double gamma, double* chge, double* dp);
+
 /* image_monomers (SOURCE/mbpol.f90:1275-1301): H atoms next to their O. */
 void orc_image_monomers(int imcon, const double* cell, int nw, double* xyz);
 

@@ -50,6 +50,12 @@ class Oracle:
         L.orc_pes_load.argtypes = [C.c_char_p]
         L.orc_ps_couple.argtypes = [C.c_double] * 9 + [_D, _D, _D]
         L.orc_angfrc_ps.argtypes = [C.c_int, _D, C.c_int, _I] + [_D] * 14
+        L.orc_dms_load.argtypes = [C.c_char_p]
+        L.orc_msites.argtypes = [C.c_int, _D, C.c_int, _I, _D, _D, _D, C.c_double]
+        L.orc_qdetermine.argtypes = [C.c_int, _D, C.c_int, _I, _D, _D, _D, C.c_double, _D, _D]
+        L.orc_qdetermine.restype = C.c_double
+        if L.orc_dms_load(os.path.join(TABLES, "ps_dms.tbl").encode()):
+            raise RuntimeError("orc_dms_load failed")
         if L.orc_pes_load(os.path.join(TABLES, "ps_pes.tbl").encode()):
             raise RuntimeError("orc_pes_load failed")
         rc = L.orc_load_tables(os.path.join(TABLES, "poly2b.tbl").encode(),
@@ -164,6 +170,17 @@ class Oracle:
                                _p(v[1]), _p(v[2]), _p(jpot))
         return dict(engang=eng.value, virang=vir.value, stress=stress, forces=f.T.copy(), atomic_energy=ae,
                     jpot=jpot)
+
+    def msites_dms(self, box, gamma=0.426706882):
+        """M-site positions and DMS charges; returns (xyz with M sites, chge, dp[nw,6], worst |sum q|)."""
+        x, y, z = (np.ascontiguousarray(box.xyz[:, k]).copy() for k in range(3))
+        lst = np.ascontiguousarray(box.listttm2(), dtype=np.int32)
+        self.lib.orc_msites(box.imcon, _p(box.cell), box.nw, _p(lst, _I), _p(x), _p(y), _p(z), gamma)
+        chge = np.zeros(box.natms)
+        dp = np.zeros((box.nw, 6))
+        worst = self.lib.orc_qdetermine(box.imcon, _p(box.cell), box.nw, _p(lst, _I), _p(x), _p(y), _p(z), gamma,
+                                        _p(chge), _p(dp))
+        return np.stack([x, y, z], 1), chge, dp, worst
 
     def image_monomers(self, box):
         m = box.monomers().copy()

@@ -5,6 +5,7 @@
 // TEST INFRASTRUCTURE ONLY (see oracle.h).
 #include "oracle.h"
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -333,4 +334,149 @@ extern "C" int orc_angfrc_ps(int imcon, const double* cell, int nang, const int*
     stress[3] += s2; stress[4] += s5; stress[5] += s6;
     stress[6] += s3; stress[7] += s6; stress[8] += s9;
     return 0;
+}
+
+// ---------------------------------------------------------------------------
+// M sites and the Partridge-Schwenke dipole-moment surface charges.
+namespace {
+struct Dms {
+    int idx[84][3];
+    double coef[84];
+    int isump = 0;
+    bool loaded = false;
+} g_dms;
+}  // namespace
+
+extern "C" int orc_dms_load(const char* path) {
+    FILE* fp = std::fopen(path, "r");
+    if (!fp) return 1;
+    std::map<std::string, std::vector<double>> arr;
+    char name[64];
+    int n;
+    while (std::fscanf(fp, "%63s", name) == 1) {
+        if (name[0] == '#') {
+            int c;
+            while ((c = std::fgetc(fp)) != '\n' && c != EOF) {
+            }
+            continue;
+        }
+        if (std::fscanf(fp, "%d", &n) != 1) break;
+        std::vector<double> v(n);
+        for (int i = 0; i < n; ++i)
+            if (std::fscanf(fp, "%lf", &v[i]) != 1) {
+                std::fclose(fp);
+                return 2;
+            }
+        arr[name] = v;
+    }
+    std::fclose(fp);
+    if (!arr.count("idx1") || !arr.count("coef")) return 3;
+    // init_ps_type_dms (SOURCE/module.f90:890-916)
+    g_dms.isump = 0;
+    for (int i = 0; i < 84; ++i) {
+        g_dms.idx[i][0] = (int)arr["idx1"][i];
+        g_dms.idx[i][1] = (int)arr["idx2"][i];
+        g_dms.idx[i][2] = (int)arr["idx3"][i];
+        g_dms.coef[i] = arr["coef"][i];
+        for (int k = 0; k < 3; ++k) g_dms.isump = std::max(g_dms.isump, g_dms.idx[i][k]);
+    }
+    g_dms.loaded = true;
+    return 0;
+}
+
+// M-site coordinates, SOURCE/dlpoly_cmd.f:2041-2057: r_M = r_O + gamma/2 (r_OH1 + r_OH2).
+extern "C" void orc_msites(int imcon, const double* cell, int nw, const int* listttm2, double* x, double* y, double* z,
+                           double gamma) {
+    if (nw <= 0) return;
+    int mttm2 = listttm2[3 * nw - 1];  // 1-based
+    for (int i = 0; i < nw; ++i) {
+        mttm2 = mttm2 + 1;
+        const int io = listttm2[3 * i] - 1, h1 = listttm2[3 * i + 1] - 1, h2 = listttm2[3 * i + 2] - 1;
+        double x1 = x[h1] - x[io], y1 = y[h1] - y[io], z1 = z[h1] - z[io];
+        double x2 = x[h2] - x[io], y2 = y[h2] - y[io], z2 = z[h2] - z[io];
+        images1(imcon, cell, x1, y1, z1);
+        images1(imcon, cell, x2, y2, z2);
+        x[mttm2 - 1] = x[io] + (x1 + x2) * gamma / 2.0;
+        y[mttm2 - 1] = y[io] + (y1 + y2) * gamma / 2.0;
+        z[mttm2 - 1] = z[io] + (z1 + z2) * gamma / 2.0;
+    }
+}
+
+// qdetermine with ldms, .not. lttm3, .not. lttmfold (the MB-pol settings of
+// SOURCE/simdef_cmd.f:1040-1060): H and M charges and dq/d(r1, r2, cos) into
+// dp[6*nw] = {dp1dr1, dp1dr2, dp2dr1, dp2dr2, dp1dcos, dp2dcos} per water
+// (SOURCE/qdetermine.f90:112-285).  Returns the largest |sum of water charges|.
+extern "C" double orc_qdetermine(int imcon, const double* cell, int nw, const int* listttm2, const double* x,
+                                 const double* y, const double* z, double gamma, double* chge, double* dp) {
+    if (!g_dms.loaded || !g_pes.loaded) {
+        std::fprintf(stderr, "oracle: DMS/PES tables not loaded\n");
+        std::abort();
+    }
+    const double bohr = 0.529177249;
+    const double b1dms = 1.0, adms = 0.2999 * bohr, bdms = -0.6932;
+    const double c0 = 1.0099, c1 = -0.1801, c2 = 0.0892;
+    const Dms& D = g_dms;
+    double worst = 0.0;
+    int mttm2 = nw > 0 ? listttm2[3 * nw - 1] : 0;
+    for (int i = 0; i < nw; ++i) {
+        mttm2 = mttm2 + 1;
+        const int io = listttm2[3 * i] - 1, h1 = listttm2[3 * i + 1] - 1, h2 = listttm2[3 * i + 2] - 1;
+        double r1x = x[h1] - x[io], r1y = y[h1] - y[io], r1z = z[h1] - z[io];
+        images1(imcon, cell, r1x, r1y, r1z);
+        const double r1 = std::sqrt(r1x * r1x + r1y * r1y + r1z * r1z);
+        double r2x = x[h2] - x[io], r2y = y[h2] - y[io], r2z = z[h2] - z[io];
+        images1(imcon, cell, r2x, r2y, r2z);
+        const double r2 = std::sqrt(r2x * r2x + r2y * r2y + r2z * r2z);
+        const double cost = (r1x * r2x + r1y * r2y + r1z * r2z) / (r1 * r2);
+        const double x1 = (r1 - reoh) / reoh, x2 = (r2 - reoh) / reoh, x3 = cost - g_pes.cose;
+        double fmat[11][3];
+        std::memset(fmat, 0, sizeof fmat);
+        fmat[1][0] = fmat[1][1] = fmat[1][2] = 1.0;
+        for (int j = 2; j <= D.isump; ++j) {
+            fmat[j][0] = fmat[j - 1][0] * x1;
+            fmat[j][1] = fmat[j - 1][1] * x2;
+            fmat[j][2] = fmat[j - 1][2] * x3;
+        }
+        double p1 = 0.0, p2 = 0.0, d11 = 0, d12 = 0, d21 = 0, d22 = 0, d1c = 0, d2c = 0;
+        for (int j = 1; j < 84; ++j) {
+            const int i1 = D.idx[j][0], i2 = D.idx[j][1], i3 = D.idx[j][2];
+            const double c = D.coef[j];
+            p1 = p1 + c * fmat[i1][0] * fmat[i2][1] * fmat[i3][2];
+            p2 = p2 + c * fmat[i2][0] * fmat[i1][1] * fmat[i3][2];
+            d11 = d11 + c * (i1 - 1) * fmat[i1 - 1][0] * fmat[i2][1] * fmat[i3][2] / reoh;
+            d12 = d12 + c * (i2 - 1) * fmat[i1][0] * fmat[i2 - 1][1] * fmat[i3][2] / reoh;
+            d21 = d21 + c * (i2 - 1) * fmat[i2 - 1][0] * fmat[i1][1] * fmat[i3][2] / reoh;
+            d22 = d22 + c * (i1 - 1) * fmat[i2][0] * fmat[i1 - 1][1] * fmat[i3][2] / reoh;
+            d1c = d1c + c * (i3 - 1) * fmat[i1][0] * fmat[i2][1] * fmat[i3 - 1][2];
+            d2c = d2c + c * (i3 - 1) * fmat[i2][0] * fmat[i1][1] * fmat[i3 - 1][2];
+        }
+        const double pl1 = cost;
+        const double pl2 = 0.5 * (3.0 * pl1 * pl1 - 1.0);
+        const double damp = std::exp(-b1dms * ((r1 - reoh) * (r1 - reoh) + (r2 - reoh) * (r2 - reoh)));
+        const double ddampdr1 = -2.0 * b1dms * (r1 - reoh) * damp;
+        const double ddampdr2 = -2.0 * b1dms * (r2 - reoh) * damp;
+        const double ang = c0 + pl1 * c1 + pl2 * c2;
+        const double pc0 = adms * (std::pow(r1, bdms) + std::pow(r2, bdms)) * ang;
+        const double dpc0dr1 = adms * (bdms * std::pow(r1, bdms - 1)) * ang;
+        const double dpc0dr2 = adms * (bdms * std::pow(r2, bdms - 1)) * ang;
+        const double dpc0dcos = adms * (std::pow(r1, bdms) + std::pow(r2, bdms)) * (c1 + 3.0 * c2 * pl1);
+        d11 = d11 * damp + p1 * ddampdr1 + dpc0dr1;
+        d12 = d12 * damp + p1 * ddampdr2 + dpc0dr2;
+        d21 = d21 * damp + p2 * ddampdr1 + dpc0dr1;
+        d22 = d22 * damp + p2 * ddampdr2 + dpc0dr2;
+        d1c = d1c * damp + dpc0dcos;
+        d2c = d2c * damp + dpc0dcos;
+        p1 = D.coef[0] + p1 * damp + pc0;
+        p2 = D.coef[0] + p2 * damp + pc0;
+        const double factor = gamma / 2.0 / (1.0 - gamma);
+        chge[h1] = p1 + factor * (p1 + p2);
+        chge[h2] = p2 + factor * (p1 + p2);
+        chge[mttm2 - 1] = -(chge[h1] + chge[h2]);
+        if (dp) {
+            double* o = dp + 6 * (size_t)i;
+            o[0] = d11; o[1] = d12; o[2] = d21; o[3] = d22; o[4] = d1c; o[5] = d2c;
+        }
+        worst = std::max(worst, std::fabs(chge[mttm2 - 1] + chge[h1] + chge[h2] + chge[io]));
+    }
+    return worst;
 }

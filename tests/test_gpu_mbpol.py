@@ -228,3 +228,14 @@ def test_ps_pes_fp64_matches_oracle(mbx_ctx, oracle_lib, name):
     assert rel_err(got["forces"], ref["forces"]) <= TOL64
     assert rel_err(got["atomic_energy"], ref["atomic_energy"]) <= TOL64
     assert rel_err(got["jpot"], ref["jpot"]) <= TOL64
+
+
+@pytest.mark.parametrize("name", ["cfg0_256", "ortho_imcon2", "shuffled_layout"])
+def test_msites_dms_match_oracle(mbx_ctx, oracle_lib, name):
+    box = BOXES[name]
+    rx, rq, rdp, _ = oracle_lib.msites_dms(box)
+    gx, gq, gdp = mbx_ctx.msites_dms(box)
+    nw = box.nw
+    assert np.max(np.abs(gx[3 * nw:] - rx[3 * nw:])) <= 1e-12 * max(box.L, 1.0)
+    assert rel_err(gq, rq) <= TOL64
+    assert rel_err(gdp, rdp) <= TOL64
