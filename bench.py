@@ -35,10 +35,11 @@ for _p in (PKG, os.path.join(REPO, "oracle")):
         sys.path.insert(0, _p)
 
 METRIC = "MB-pol steps/s at 4096 H2O, mixed vs FP64 on 1 GB300; served p50/p99 ms"
-WORKLOAD = "MB-pol 2B+3B forces + per-atom energies + heat current (jpot, jkin), 4096 H2O (12288 atoms + 4096 M sites), L=49.70 A"
+WORKLOAD = ("MB-pol 1B (Partridge-Schwenke coupling) + 2B + 3B forces, energy, virial, stress, per-atom energies and "
+            "heat current (jpot, jkin), 4096 H2O (12288 atoms + 4096 M sites), L=49.70 A")
 DATA = "synthetic: seeded 4096-H2O box, jittered 16^3 lattice, random orientations, 0.02 A noise, 298 K velocities"
-NOT_IN_STEP = ["TTM4-F polarizable electrostatics (induced dipoles, Ewald/SPME)", "DMS charges",
-               "1-body PS PES", "TT dispersion"]
+NOT_IN_STEP = ["TTM4-F polarizable electrostatics (induced dipoles, Ewald/SPME) and the DMS charge forces",
+               "TT dispersion", "FIELD-file bond terms of the monomer PES"]
 
 
 def _peaks():
@@ -158,14 +159,21 @@ def run_ours(args, rank, world):
     F = torch.zeros((3, n), **f64)
     AE = torch.zeros(n, **f64)
     LST = torch.tensor(box.listttm2(), dtype=torch.int32, device=dev)
+    ANG = torch.tensor(box.listang().ravel(), dtype=torch.int32, device=dev)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)   # > 129 MB L2
 
     def step(precision):
         F.zero_()
         AE.zero_()
-        return ctx.mbpol_forces_device(precision, box.imcon, box.cell, 3 * box.nw, LST.data_ptr(), n,
-                                       [x.data_ptr() for x in X], [F[k].data_ptr() for k in range(3)],
-                                       [v.data_ptr() for v in V], M.data_ptr(), AE.data_ptr())
+        xp = [x.data_ptr() for x in X]
+        fp = [F[k].data_ptr() for k in range(3)]
+        vp = [v.data_ptr() for v in V]
+        one = ctx.ps_pes_device(box.imcon, box.cell, box.nw, ANG.data_ptr(), n, xp, fp, vp, AE.data_ptr())
+        sc = ctx.mbpol_forces_device(precision, box.imcon, box.cell, 3 * box.nw, LST.data_ptr(), n, xp, fp, vp,
+                                     M.data_ptr(), AE.data_ptr())
+        sc = sc.copy()
+        sc[12:15] += one[11:14]          # jpot of the 1-body term
+        return sc
 
     def timed(precision, steps, warmup, profile=False):
         ctx.set_profiling(profile)
@@ -185,7 +193,7 @@ def run_ours(args, rank, world):
             if profile:
                 ms, cnt = ctx.last_timings()
                 phase += ms
-            launches += ctx.last_timings()[1][2] + 2   # + the two zero_ fills of the step
+            launches += ctx.last_timings()[1][2] + 3   # + the 1-body kernel and the two zero_ fills
         torch.cuda.synchronize()
         tot = sum(a.elapsed_time(b) for a, b in ev) / 1e3
         if world > 1:
@@ -237,7 +245,19 @@ def run_ours(args, rank, world):
     stress = np.zeros(9)
     sc = np.zeros(capi.NSCALARS)
 
+    hang = pinned(box.listang().ravel().astype(np.int32))
+    jp = np.zeros(3)
+    eang = C.c_double(0)
+    vang = C.c_double(0)
+
     def e2e_step():
+        rc = ctx.lib.mbx_ps_pes_forces(ctx.h, box.imcon, box.cell.ctypes.data_as(D), box.nw,
+                                       C.cast(C.c_void_p(hang.data_ptr()), C.POINTER(C.c_int)), n, hp(hx[0]),
+                                       hp(hx[1]), hp(hx[2]), hp(hf[0]), hp(hf[1]), hp(hf[2]), C.byref(eang),
+                                       C.byref(vang), stress.ctypes.data_as(D), hp(hv[0]), hp(hv[1]), hp(hv[2]),
+                                       hp(hae), jp.ctypes.data_as(D))
+        if rc:
+            raise RuntimeError("mbx_ps_pes_forces failed: %d" % rc)
         rc = ctx.lib.mbx_mbpol_forces(ctx.h, capi.MIXED, box.imcon, box.cell.ctypes.data_as(D), 3 * box.nw,
                                       C.cast(C.c_void_p(hl.data_ptr()), C.POINTER(C.c_int)), n, hp(hx[0]),
                                       hp(hx[1]), hp(hx[2]), hp(hf[0]), hp(hf[1]), hp(hf[2]), C.byref(eng),
@@ -262,8 +282,9 @@ def run_ours(args, rank, world):
         t = torch.tensor([t_e2e], device=dev)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         t_e2e = float(t.item())
-    h2d = 7 * n * 8 + 3 * box.nw * 4
-    d2h = 4 * n * 8 + capi.NSCALARS * 8
+    # two host calls per step (1-body, then 2B/3B); each copies its inputs in and results out
+    h2d = (6 * n * 8 + 3 * box.nw * 4) + (7 * n * 8 + 3 * box.nw * 4)
+    d2h = (4 * n * 8 + 14 * 8) + (4 * n * 8 + capi.NSCALARS * 8)
     ctx.close()
 
     if rank != 0:

@@ -174,6 +174,15 @@ class Context:
                                             box.natms, gamma, _p(x), _p(y), _p(z), _p(q), _p(dp)), "mbx_msites_dms")
         return np.stack([x, y, z], 1), q, dp
 
+    def ps_pes_device(self, imcon, cell, nang, listang_ptr, natms, xyz_ptrs, f_ptrs, v_ptrs=None, ae_ptr=None):
+        """Device-pointer 1-body PES; returns {engang, virang, stress[9], jpot[3]} as an array of 14."""
+        out = np.zeros(14)
+        v_ptrs = v_ptrs or (None, None, None)
+        rc = self.lib.mbx_ps_pes_forces_device(self.h, imcon, _p(_f64(cell)), nang, listang_ptr, natms, *xyz_ptrs,
+                                               *f_ptrs, *v_ptrs, ae_ptr, _p(out))
+        self._check(rc, "mbx_ps_pes_forces_device")
+        return out
+
     def mbpol_forces_device(self, precision, imcon, cell, nttm2, list_ptr, natms, xyz_ptrs, f_ptrs, v_ptrs=None,
                             mass_ptr=None, ae_ptr=None):
         """Device-pointer entry point (pointers as ints); returns the scalars."""
