@@ -349,15 +349,19 @@ def run_case(args):
     F = torch.zeros((3, n), **f64)
     AE = torch.zeros(n, **f64)
     LST = torch.tensor(box.listttm2(), dtype=torch.int32, device="cuda")
+    ANG = torch.tensor(box.listang().ravel(), dtype=torch.int32, device="cuda")
     prec = capi.MIXED if args.case == "mixed" else capi.FP64
     torch.cuda.synchronize()
     for _ in range(args.warmup + args.steps):
         F.zero_()
         AE.zero_()
         torch.cuda.synchronize()
-        ctx.mbpol_forces_device(prec, box.imcon, box.cell, 3 * box.nw, LST.data_ptr(), n,
-                                [x.data_ptr() for x in X], [F[k].data_ptr() for k in range(3)],
-                                [v.data_ptr() for v in V], M.data_ptr(), AE.data_ptr())
+        xp = [x.data_ptr() for x in X]
+        fp = [F[k].data_ptr() for k in range(3)]
+        vp = [v.data_ptr() for v in V]
+        ctx.ps_pes_device(box.imcon, box.cell, box.nw, ANG.data_ptr(), n, xp, fp, vp, AE.data_ptr())
+        ctx.mbpol_forces_device(prec, box.imcon, box.cell, 3 * box.nw, LST.data_ptr(), n, xp, fp, vp,
+                                M.data_ptr(), AE.data_ptr())
     ctx.close()
     print(json.dumps({"case": args.case, "steps": args.steps, "warmup": args.warmup}))
 
