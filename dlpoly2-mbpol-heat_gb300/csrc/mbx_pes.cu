@@ -1,6 +1,6 @@
 // 1-body Partridge-Schwenke water PES (the MB-pol monomer term) with the angfrc
 // bookkeeping: ps_type_couple (SOURCE/ps_type_couple.f90:15-274) called from angfrc
-// for keya = 9 (SOURCE/angfrc.f:150-212, :344-545).  One thread per H-O-H angle, FP64.
+// for keya = 9 (SOURCE/angfrc.f:150-212, :344-545).  One warp per H-O-H angle, FP64.
 #include "mbx_kernels.cuh"
 #include "mbx_pes_gen.cuh"
 
@@ -11,16 +11,20 @@ namespace {
 __device__ __forceinline__ double c5z(int j) { return __longlong_as_double((long long)pes::kC5z[j]); }
 __device__ __forceinline__ double cmass(int j) { return __longlong_as_double((long long)pes::kCmass[j]); }
 
-// ps_type_couple: potential, the forces on the two H (fa, fc) and the virial term.
-__device__ void ps_couple(double roh1, double xoh1, double yoh1, double zoh1, double roh2, double xoh2,
-                          double yoh2, double zoh2, double theta, double& pterm_out, double* f,
-                          double& vterm_out) {
-    const double reoh = pes::kReoh;
+// ps_type_couple, one warp per angle: lanes share the 244 expansion terms and the
+// partial sums are reduced with shuffles; lane 0 adds the mass-correction terms and the
+// exponential prefactor.  Outputs (valid on lane 0): potential, the forces on the two
+// H atoms (fa = f[0..2], fc = f[3..5]) and the virial term.
+__device__ void ps_couple_warp(int lane, double roh1, double xoh1, double yoh1, double zoh1, double roh2,
+                               double xoh2, double yoh2, double zoh2, double theta, double& pterm_out, double* f,
+                               double& vterm_out) {
+    const double reoh = pes::kReoh, ireoh = 1.0 / pes::kReoh;
     const double cose = __longlong_as_double((long long)pes::kCose);
     const double cost = cos(theta);
     const double x1 = (roh1 - reoh) / reoh;
     const double x2 = (roh2 - reoh) / reoh;
     const double x3 = cost - cose;
+    const double ir1 = 1.0 / roh1, ir2 = 1.0 / roh2;
     double fm[16][3];
     fm[0][0] = fm[0][1] = fm[0][2] = 0.0;
     fm[1][0] = fm[1][1] = fm[1][2] = 1.0;
@@ -30,69 +34,73 @@ __device__ void ps_couple(double roh1, double xoh1, double yoh1, double zoh1, do
         fm[j][1] = fm[j - 1][1] * x2;
         fm[j][2] = fm[j - 1][2] * x3;
     }
-    const double e1x = xoh2 - cost * xoh1, e1y = yoh2 - cost * yoh1, e1z = zoh2 - cost * zoh1;
-    const double e2x = xoh1 - cost * xoh2, e2y = yoh1 - cost * yoh2, e2z = zoh1 - cost * zoh2;
-    double pterm = 0.0, vterm = 0.0, fa[3] = {0, 0, 0}, fc[3] = {0, 0, 0};
-    for (int j = 1; j < pes::kTerms; ++j) {
+    // per term: potential; the x-y-z components of the H forces factor into a radial
+    // part (along the unit bond vector) and an angular part (along e1 / e2)
+    double pterm = 0.0, vterm = 0.0, ra = 0.0, aa = 0.0, rc = 0.0, ac = 0.0;
+    for (int j = 1 + lane; j < pes::kTerms; j += 32) {
         const int i1 = pes::kIdx[j][0], i2 = pes::kIdx[j][1], i3 = pes::kIdx[j][2];
         const double c = c5z(j);
         const double dum = fm[i1][0] * fm[i2][1] + fm[i2][0] * fm[i1][1];
         pterm += c * dum * fm[i3][2];
-        // H1 (atom a)
-        const double a1 = (i1 - 1) * fm[i1 - 1][0] / reoh;
-        const double a2 = (i2 - 1) * fm[i2 - 1][0] / reoh;
-        const double a3 = (i3 - 1) * fm[i3 - 1][2] / roh1;
-        const double pa = a1 * fm[i2][1] * fm[i3][2] + a2 * fm[i1][1] * fm[i3][2];
-        fa[0] -= c * (pa * xoh1 + dum * a3 * e1x);
-        fa[1] -= c * (pa * yoh1 + dum * a3 * e1y);
-        fa[2] -= c * (pa * zoh1 + dum * a3 * e1z);
-        // H2 (atom c)
-        const double b1 = (i2 - 1) * fm[i2 - 1][1] / reoh;
-        const double b2 = (i1 - 1) * fm[i1 - 1][1] / reoh;
-        const double b3 = (i3 - 1) * fm[i3 - 1][2] / roh2;
-        const double pc = fm[i1][0] * b1 * fm[i3][2] + fm[i2][0] * b2 * fm[i3][2];
-        fc[0] -= c * (pc * xoh2 + dum * b3 * e2x);
-        fc[1] -= c * (pc * yoh2 + dum * b3 * e2y);
-        fc[2] -= c * (pc * zoh2 + dum * b3 * e2z);
-        vterm += c *
-                 (roh1 * fm[i2][1] * (i1 - 1) * fm[i1 - 1][0] / reoh + roh2 * fm[i1][0] * (i2 - 1) * fm[i2 - 1][1] / reoh +
-                  roh1 * fm[i1][1] * (i2 - 1) * fm[i2 - 1][0] / reoh + roh2 * fm[i2][0] * (i1 - 1) * fm[i1 - 1][1] / reoh) *
-                 fm[i3][2];
+        const double a1 = (i1 - 1) * fm[i1 - 1][0] * ireoh;
+        const double a2 = (i2 - 1) * fm[i2 - 1][0] * ireoh;
+        const double a3 = (i3 - 1) * fm[i3 - 1][2];
+        ra += c * (a1 * fm[i2][1] + a2 * fm[i1][1]) * fm[i3][2];
+        aa += c * dum * a3;
+        const double b1 = (i2 - 1) * fm[i2 - 1][1] * ireoh;
+        const double b2 = (i1 - 1) * fm[i1 - 1][1] * ireoh;
+        rc += c * (fm[i1][0] * b1 + fm[i2][0] * b2) * fm[i3][2];
+        vterm += c * (roh1 * fm[i2][1] * (i1 - 1) * fm[i1 - 1][0] + roh2 * fm[i1][0] * (i2 - 1) * fm[i2 - 1][1] +
+                      roh1 * fm[i1][1] * (i2 - 1) * fm[i2 - 1][0] + roh2 * fm[i2][0] * (i1 - 1) * fm[i1 - 1][1]) *
+                 ireoh * fm[i3][2];
     }
-    // mass-correction terms
-    const double xm = __longlong_as_double((long long)pes::kXm);
-    double v1 = 0.0, v2 = 0.0;
-    for (int j = 0; j < pes::kMass; ++j) {
-        const int m1 = pes::kIdxm[j][0], m2 = pes::kIdxm[j][1], m3 = pes::kIdxm[j][2];
-        const double c = cmass(j);
-        v1 += c * fm[m1][0] * fm[m2][1] * fm[m3][2];
-        v2 += c * fm[m2][0] * fm[m1][1] * fm[m3][2];
-        const double d1 = (m1 - 1) * fm[m1 - 1][0] / reoh;
-        const double d2 = (m2 - 1) * fm[m2 - 1][0] / reoh;
-        const double d3 = (m3 - 1) * fm[m3 - 1][2] / roh1;
-        const double pa = xm * d1 * fm[m2][1] * fm[m3][2];
-        const double pb = xm * d2 * fm[m1][1] * fm[m3][2];
-        const double q3 = xm * (fm[m1][0] * fm[m2][1] + fm[m2][0] * fm[m1][1]) * d3;
-        fa[0] -= c * ((pa + pb) * xoh1 + q3 * e1x);
-        fa[1] -= c * ((pa + pb) * yoh1 + q3 * e1y);
-        fa[2] -= c * ((pa + pb) * zoh1 + q3 * e1z);
-        const double h1 = (m2 - 1) * fm[m2 - 1][1] / reoh;
-        const double h2 = (m1 - 1) * fm[m1 - 1][1] / reoh;
-        const double h3 = (m3 - 1) * fm[m3 - 1][2] / roh2;
-        const double qa = xm * fm[m1][0] * h1 * fm[m3][2];
-        const double qb = xm * fm[m2][0] * h2 * fm[m3][2];
-        const double q4 = xm * (fm[m1][0] * fm[m2][1] + fm[m2][0] * fm[m1][1]) * h3;
-        fc[0] -= c * ((qa + qb) * xoh2 + q4 * e2x);
-        fc[1] -= c * ((qa + qb) * yoh2 + q4 * e2y);
-        fc[2] -= c * ((qa + qb) * zoh2 + q4 * e2z);
-        vterm += c *
-                 (xm * roh1 * fm[m2][1] * (m1 - 1) * fm[m1 - 1][0] / reoh +
-                  xm * roh2 * fm[m1][0] * (m2 - 1) * fm[m2 - 1][1] / reoh +
-                  xm * roh1 * fm[m1][1] * (m2 - 1) * fm[m2 - 1][0] / reoh +
-                  xm * roh2 * fm[m2][0] * (m1 - 1) * fm[m1 - 1][1] / reoh) *
-                 fm[m3][2];
+    pterm = warp_sum(pterm);
+    vterm = warp_sum(vterm);
+    ra = warp_sum(ra);
+    aa = warp_sum(aa);
+    rc = warp_sum(rc);
+    if (lane != 0) return;
+    double fa[3], fc[3];
+    {
+        const double e1x = xoh2 - cost * xoh1, e1y = yoh2 - cost * yoh1, e1z = zoh2 - cost * zoh1;
+        const double e2x = xoh1 - cost * xoh2, e2y = yoh1 - cost * yoh2, e2z = zoh1 - cost * zoh2;
+        fa[0] = -(ra * xoh1 + aa * ir1 * e1x);
+        fa[1] = -(ra * yoh1 + aa * ir1 * e1y);
+        fa[2] = -(ra * zoh1 + aa * ir1 * e1z);
+        fc[0] = -(rc * xoh2 + aa * ir2 * e2x);
+        fc[1] = -(rc * yoh2 + aa * ir2 * e2y);
+        fc[2] = -(rc * zoh2 + aa * ir2 * e2z);
+        // mass-correction terms
+        const double xm = __longlong_as_double((long long)pes::kXm);
+        double v1 = 0.0, v2 = 0.0;
+        for (int j = 0; j < pes::kMass; ++j) {
+            const int m1 = pes::kIdxm[j][0], m2 = pes::kIdxm[j][1], m3 = pes::kIdxm[j][2];
+            const double c = cmass(j);
+            v1 += c * fm[m1][0] * fm[m2][1] * fm[m3][2];
+            v2 += c * fm[m2][0] * fm[m1][1] * fm[m3][2];
+            const double d1 = (m1 - 1) * fm[m1 - 1][0] * ireoh;
+            const double d2 = (m2 - 1) * fm[m2 - 1][0] * ireoh;
+            const double d3 = (m3 - 1) * fm[m3 - 1][2] * ir1;
+            const double pa = xm * (d1 * fm[m2][1] + d2 * fm[m1][1]) * fm[m3][2];
+            const double q3 = xm * (fm[m1][0] * fm[m2][1] + fm[m2][0] * fm[m1][1]) * d3;
+            fa[0] -= c * (pa * xoh1 + q3 * e1x);
+            fa[1] -= c * (pa * yoh1 + q3 * e1y);
+            fa[2] -= c * (pa * zoh1 + q3 * e1z);
+            const double h1 = (m2 - 1) * fm[m2 - 1][1] * ireoh;
+            const double h2 = (m1 - 1) * fm[m1 - 1][1] * ireoh;
+            const double h3 = (m3 - 1) * fm[m3 - 1][2] * ir2;
+            const double qa = xm * (fm[m1][0] * h1 + fm[m2][0] * h2) * fm[m3][2];
+            const double q4 = xm * (fm[m1][0] * fm[m2][1] + fm[m2][0] * fm[m1][1]) * h3;
+            fc[0] -= c * (qa * xoh2 + q4 * e2x);
+            fc[1] -= c * (qa * yoh2 + q4 * e2y);
+            fc[2] -= c * (qa * zoh2 + q4 * e2z);
+            vterm += c *
+                     (xm * roh1 * fm[m2][1] * (m1 - 1) * fm[m1 - 1][0] + xm * roh2 * fm[m1][0] * (m2 - 1) * fm[m2 - 1][1] +
+                      xm * roh1 * fm[m1][1] * (m2 - 1) * fm[m2 - 1][0] + xm * roh2 * fm[m2][0] * (m1 - 1) * fm[m1 - 1][1]) *
+                     ireoh * fm[m3][2];
+        }
+        pterm = pterm + xm * v1 + xm * v2;
     }
-    pterm = pterm + xm * v1 + xm * v2;
     const double b1 = pes::kB1;
     const double efac = exp(-b1 * ((roh1 - reoh) * (roh1 - reoh) + (roh2 - reoh) * (roh2 - reoh)));
     const double term = pterm;
@@ -110,18 +118,20 @@ __device__ void ps_couple(double roh1, double xoh1, double yoh1, double zoh1, do
     vterm_out = vterm;
 }
 
+// One warp per angle; lane 0 of each warp accumulates.
 __global__ void __launch_bounds__(kThreads) k_ps_pes(int nang, const int* __restrict__ listang, Cell cl,
                                                       const double* __restrict__ x, const double* __restrict__ y,
                                                       const double* __restrict__ z, double* fx, double* fy,
                                                       double* fz, double* ae, const double* __restrict__ vx,
                                                       const double* __restrict__ vy, const double* __restrict__ vz,
                                                       double* acc) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    // red = {E, virial, stress[9], jpot[3]}
+    const int t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    // red = {E, virial, stress[9], jpot[3]} (lane 0 of each warp)
     double red[14];
 #pragma unroll
     for (int q = 0; q < 14; ++q) red[q] = 0.0;
-    if (t < nang) {
+    if (t < nang) {   // warp-uniform
         const int ia = listang[3 * t] - 1, ib = listang[3 * t + 1] - 1, ic = listang[3 * t + 2] - 1;
         double xab = x[ia] - x[ib], yab = y[ia] - y[ib], zab = z[ia] - z[ib];
         double xbc = x[ic] - x[ib], ybc = y[ic] - y[ib], zbc = z[ic] - z[ib];
@@ -129,34 +139,37 @@ __global__ void __launch_bounds__(kThreads) k_ps_pes(int nang, const int* __rest
         image(cl, xbc, ybc, zbc);
         const double rab = sqrt(xab * xab + yab * yab + zab * zab);
         const double rbc = sqrt(xbc * xbc + ybc * ybc + zbc * zbc);
-        xab /= rab; yab /= rab; zab /= rab;
-        xbc /= rbc; ybc /= rbc; zbc /= rbc;
+        const double rrab = 1.0 / rab, rrbc = 1.0 / rbc;
+        xab *= rrab; yab *= rrab; zab *= rrab;
+        xbc *= rrbc; ybc *= rrbc; zbc *= rrbc;
         const double cost = xab * xbc + yab * ybc + zab * zbc;
-        double pterm, vterm, f[6];
-        ps_couple(rab, xab, yab, zab, rbc, xbc, ybc, zbc, acos(cost), pterm, f, vterm);
-        red[0] = pterm;
-        red[1] = vterm;
-        const double s1 = rab * xab * f[0] + rbc * xbc * f[3], s2 = rab * xab * f[1] + rbc * xbc * f[4];
-        const double s3 = rab * xab * f[2] + rbc * xbc * f[5], s5 = rab * yab * f[1] + rbc * ybc * f[4];
-        const double s6 = rab * yab * f[2] + rbc * ybc * f[5], s9 = rab * zab * f[2] + rbc * zbc * f[5];
-        red[2] = s1; red[3] = s2; red[4] = s3;
-        red[5] = s2; red[6] = s5; red[7] = s6;
-        red[8] = s3; red[9] = s6; red[10] = s9;
-        atomicAdd(fx + ia, f[0]); atomicAdd(fy + ia, f[1]); atomicAdd(fz + ia, f[2]);
-        atomicAdd(fx + ib, -f[0] - f[3]); atomicAdd(fy + ib, -f[1] - f[4]); atomicAdd(fz + ib, -f[2] - f[5]);
-        atomicAdd(fx + ic, f[3]); atomicAdd(fy + ic, f[4]); atomicAdd(fz + ic, f[5]);
-        if (ae) {
-            atomicAdd(ae + ia, pterm / 3);
-            atomicAdd(ae + ib, pterm / 3);
-            atomicAdd(ae + ic, pterm / 3);
-        }
-        if (vx) {
-            // force-matrix entries (ia,ib),(ib,ia),(ic,ib),(ib,ic) contracted (raw coordinates)
-            const double fva = f[0] * (vx[ia] + vx[ib]) + f[1] * (vy[ia] + vy[ib]) + f[2] * (vz[ia] + vz[ib]);
-            const double fvc = f[3] * (vx[ic] + vx[ib]) + f[4] * (vy[ic] + vy[ib]) + f[5] * (vz[ic] + vz[ib]);
-            red[11] = (x[ia] - x[ib]) * fva + (x[ic] - x[ib]) * fvc;
-            red[12] = (y[ia] - y[ib]) * fva + (y[ic] - y[ib]) * fvc;
-            red[13] = (z[ia] - z[ib]) * fva + (z[ic] - z[ib]) * fvc;
+        double pterm = 0, vterm = 0, f[6];
+        ps_couple_warp(lane, rab, xab, yab, zab, rbc, xbc, ybc, zbc, acos(cost), pterm, f, vterm);
+        if (lane == 0) {
+            red[0] = pterm;
+            red[1] = vterm;
+            const double s1 = rab * xab * f[0] + rbc * xbc * f[3], s2 = rab * xab * f[1] + rbc * xbc * f[4];
+            const double s3 = rab * xab * f[2] + rbc * xbc * f[5], s5 = rab * yab * f[1] + rbc * ybc * f[4];
+            const double s6 = rab * yab * f[2] + rbc * ybc * f[5], s9 = rab * zab * f[2] + rbc * zbc * f[5];
+            red[2] = s1; red[3] = s2; red[4] = s3;
+            red[5] = s2; red[6] = s5; red[7] = s6;
+            red[8] = s3; red[9] = s6; red[10] = s9;
+            atomicAdd(fx + ia, f[0]); atomicAdd(fy + ia, f[1]); atomicAdd(fz + ia, f[2]);
+            atomicAdd(fx + ib, -f[0] - f[3]); atomicAdd(fy + ib, -f[1] - f[4]); atomicAdd(fz + ib, -f[2] - f[5]);
+            atomicAdd(fx + ic, f[3]); atomicAdd(fy + ic, f[4]); atomicAdd(fz + ic, f[5]);
+            if (ae) {
+                atomicAdd(ae + ia, pterm / 3);
+                atomicAdd(ae + ib, pterm / 3);
+                atomicAdd(ae + ic, pterm / 3);
+            }
+            if (vx) {
+                // force-matrix entries (ia,ib),(ib,ia),(ic,ib),(ib,ic) contracted (raw coordinates)
+                const double fva = f[0] * (vx[ia] + vx[ib]) + f[1] * (vy[ia] + vy[ib]) + f[2] * (vz[ia] + vz[ib]);
+                const double fvc = f[3] * (vx[ic] + vx[ib]) + f[4] * (vy[ic] + vy[ib]) + f[5] * (vz[ic] + vz[ib]);
+                red[11] = (x[ia] - x[ib]) * fva + (x[ic] - x[ib]) * fvc;
+                red[12] = (y[ia] - y[ib]) * fva + (y[ic] - y[ib]) * fvc;
+                red[13] = (z[ia] - z[ib]) * fva + (z[ic] - z[ib]) * fvc;
+            }
         }
     }
     block_sum_atomic<14>(red, acc);
@@ -252,8 +265,8 @@ cudaError_t launch_ps_pes(int nang, const int* listang, const Cell& cl, const do
                           const double* z, double* fx, double* fy, double* fz, double* ae, const double* vx,
                           const double* vy, const double* vz, double* acc14, cudaStream_t s) {
     if (nang <= 0) return cudaSuccess;
-    k_ps_pes<<<(nang + kThreads - 1) / kThreads, kThreads, 0, s>>>(nang, listang, cl, x, y, z, fx, fy, fz, ae, vx,
-                                                                    vy, vz, acc14);
+    const int blocks = (int)(((long)nang * 32 + kThreads - 1) / kThreads);   // one warp per angle
+    k_ps_pes<<<blocks, kThreads, 0, s>>>(nang, listang, cl, x, y, z, fx, fy, fz, ae, vx, vy, vz, acc14);
     return cudaGetLastError();
 }
 
