@@ -328,8 +328,10 @@ def run_ours(args, rank, world):
         "clocks": clk,
         "gpu_launches": int(launches),
     }
+    if args.serve_requests > 0:
+        out["serving"] = serve(n_requests=args.serve_requests)
     if not args.no_cpu_baseline:
-        sps, info = cpu_reference(box)
+        sps, info = cpu_reference(box, target_core_s=40.0)
         out["cpu_baseline"] = {"value": sps, "unit": "steps/s", "cores": info["cores"], "kind": "port",
                                "sample": info["sample"]}
     return out
@@ -366,6 +368,56 @@ def run_case(args):
     print(json.dumps({"case": args.case, "steps": args.steps, "warmup": args.warmup}))
 
 
+def serve(n_requests=2000, rate=2000.0, lo=64, hi=8192, slots=8, precision=None, seed=4242):
+    """Poisson stream of force requests through the continuous-batching server.
+
+    Request sizes are log-uniform in [lo, hi] H2O; each box is generated like the
+    config-0 box from its own seed (0.997 g/cm^3, 298 K).  Returns latency percentiles
+    (submit -> results ready) and the served request rate."""
+    from mbx import capi, systems
+    precision = capi.MIXED if precision is None else precision
+    rng = np.random.default_rng(seed)
+    sizes = np.exp(rng.uniform(np.log(lo), np.log(hi), n_requests)).astype(int)
+    gaps = rng.exponential(1.0 / rate, n_requests)
+    boxes = [systems.box_for(int(n), seed=seed + 1 + k) for k, n in enumerate(sizes)]
+    srv = capi.Server(slots=slots, budget_bytes=64e9)
+    try:
+        # warm every slot's context with the largest size first
+        warm = [srv.submit(b, precision) for b in sorted(boxes[:slots * 2], key=lambda b: -b.nw)]
+        for w in warm:
+            srv.wait(w)
+        ids = [None] * n_requests
+        results = [None] * n_requests
+
+        def waiter():
+            for k in range(n_requests):
+                while ids[k] is None:
+                    time.sleep(0.0002)
+                results[k] = srv.wait(ids[k])
+
+        th = threading.Thread(target=waiter)
+        th.start()
+        t0 = time.perf_counter()
+        t_next = t0
+        for k in range(n_requests):
+            t_next += gaps[k]
+            dt = t_next - time.perf_counter()
+            if dt > 0:
+                time.sleep(dt)
+            ids[k] = srv.submit(boxes[k], precision)
+        th.join()
+        t_end = time.perf_counter()
+    finally:
+        srv.close()
+    lat = np.array([r["latency_s"] for r in results]) * 1e3
+    run = np.array([r["run_s"] for r in results]) * 1e3
+    return {"requests": int(n_requests), "arrival_rate_per_s": rate, "sizes_h2o": [int(lo), int(hi)],
+            "slots": slots, "precision": "mixed" if precision == capi.MIXED else "fp64",
+            "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+            "mean_on_slot_ms": float(run.mean()), "served_per_s": n_requests / (t_end - t0),
+            "waters_per_s": float(sizes.sum()) / (t_end - t0)}
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return None
@@ -395,6 +447,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--serve-requests", type=int, default=2000,
+                    help="requests of the Poisson serving run reported under 'serving' (0: skip)")
     ap.add_argument("--ref-core-s", type=float, default=10.0)
     ap.add_argument("--case", choices=["mixed", "fp64"], default=None,
                     help="profiling case: only warmup + K device-resident steps of one precision")

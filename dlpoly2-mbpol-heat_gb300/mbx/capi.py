@@ -69,6 +69,14 @@ def load(path=None):
     L.mbx_msites_dms.argtypes = [C.c_void_p, C.c_int, _D, C.c_int, _I, C.c_int, C.c_double] + [_D] * 5
     L.mbx_msites_dms_device.argtypes = [C.c_void_p, C.c_int, _D, C.c_int, C.c_void_p, C.c_int, C.c_double] + \
         [C.c_void_p] * 5
+    L.mbx_server_create.argtypes = [C.POINTER(C.c_void_p), C.c_int, C.c_int, C.c_double]
+    L.mbx_server_destroy.argtypes = [C.c_void_p]
+    L.mbx_server_destroy.restype = None
+    L.mbx_server_submit.argtypes = [C.c_void_p, C.c_int, C.c_int, _D, C.c_int, C.c_int] + [_D] * 7
+    L.mbx_server_submit.restype = C.c_long
+    L.mbx_server_wait.argtypes = [C.c_void_p, C.c_long] + [_D] * 6
+    L.mbx_server_error.argtypes = [C.c_void_p]
+    L.mbx_server_error.restype = C.c_char_p
     L.mbx_last_lists.argtypes = [C.c_void_p, _I, C.c_long, _L, _I, C.c_long, _L]
     L.mbx_2b_poly_batch.argtypes = [C.c_void_p, C.c_int, C.c_long, _D, _D, _D, _D, _D]
     L.mbx_3b_poly_batch.argtypes = [C.c_void_p, C.c_int, C.c_long, _D, _D, _D, _D, _D, _D, _D]
@@ -236,3 +244,49 @@ class Context:
         self._check(self.lib.mbx_3b_poly_batch(self.h, precision, n, *(_p(w) for w in W), _p(E),
                                                *(_p(a) for a in gs)), "mbx_3b_poly_batch")
         return (E, *gs)
+
+
+class Server:
+    """Continuous-batching force server (mbx_server_*): concurrent independent boxes."""
+
+    def __init__(self, device=0, slots=4, budget_bytes=32e9):
+        self.lib = load()
+        h = C.c_void_p()
+        rc = self.lib.mbx_server_create(C.byref(h), device, slots, float(budget_bytes))
+        if rc:
+            raise MbxError("mbx_server_create failed with status %d" % rc)
+        self.h = h
+        self._boxes = {}
+
+    def close(self):
+        if self.h:
+            self.lib.mbx_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def submit(self, box, precision=MIXED, heat=True):
+        x, y, z = (_f64(box.xyz[:, k]) for k in range(3))
+        v = [_f64(box.vel[:, k]) for k in range(3)] if heat else [None] * 3
+        m = _f64(box.mass) if heat else None
+        rid = self.lib.mbx_server_submit(self.h, precision, box.imcon, _p(_f64(box.cell)), box.nw, box.natms,
+                                         _p(x), _p(y), _p(z), _p(v[0]), _p(v[1]), _p(v[2]), _p(m))
+        if rid <= 0:
+            raise MbxError("mbx_server_submit failed with status %d" % -rid)
+        self._boxes[rid] = box.natms
+        return rid
+
+    def wait(self, rid):
+        n = self._boxes.pop(rid)
+        f = np.zeros((3, n))
+        ae = np.zeros(n)
+        sc = np.zeros(NSCALARS + 14)
+        t = np.zeros(3)
+        rc = self.lib.mbx_server_wait(self.h, rid, _p(f[0]), _p(f[1]), _p(f[2]), _p(ae), _p(sc), _p(t))
+        if rc:
+            raise MbxError("request %d failed with status %d" % (rid, rc))
+        return dict(forces=f.T.copy(), atomic_energy=ae, scalars=sc, queue_s=t[0], run_s=t[1], latency_s=t[2])

@@ -161,6 +161,32 @@ int mbx_msites_dms_device(mbx_context* ctx, int imcon, const double* cell, int n
                           int natms, double gamma, double* xxx, double* yyy, double* zzz, double* chge,
                           double* dqdr);
 
+/*
+ * Continuous-batching force server.  `slots` worker slots, each with its own context and
+ * CUDA stream on `device`, evaluate independent water boxes concurrently; a FIFO queue
+ * admits the next request as soon as a slot is free and its estimated device-memory
+ * footprint fits `budget_bytes` (a request larger than the budget runs alone).  Every
+ * request runs the 1-body term and the MB-pol 2B/3B terms with the heat current
+ * (standard layout: waters 1..3*nw as O,H1,H2, M sites after them, natms >= 4*nw).
+ * No counterpart in the reference (its i-PI client serves one request at a time,
+ * SOURCE/ipi.f90:33-198).
+ *   mbx_server_submit  copies the host inputs and returns a request id > 0, or -status
+ *   mbx_server_wait    blocks until the request is done, copies forces (natms each),
+ *                      per-atom energies, scalars[MBX_NSCALARS + 14] (the MB-pol block,
+ *                      then engang, virang, stress[9], jpot[3] of the 1-body term) and
+ *                      times[3] = {queueing, on a slot, total latency} in seconds; any
+ *                      output pointer may be NULL.  Returns the request's status.
+ */
+typedef struct mbx_server mbx_server;
+int mbx_server_create(mbx_server** server, int device, int slots, double budget_bytes);
+void mbx_server_destroy(mbx_server* server);
+long mbx_server_submit(mbx_server* server, int precision, int imcon, const double* cell, int nw, int natms,
+                       const double* xxx, const double* yyy, const double* zzz, const double* vxx, const double* vyy,
+                       const double* vzz, const double* weight);
+int mbx_server_wait(mbx_server* server, long id, double* fxx, double* fyy, double* fzz, double* atomic_energy,
+                    double* scalars, double* times);
+const char* mbx_server_error(const mbx_server* server);
+
 /* Dimer and trimer lists of the last evaluation (0-based water indices, i<j<k), as
  * index sets; the host arrays receive up to cap entries; counts are always written. */
 int mbx_last_lists(mbx_context* ctx, int* pairs, long cap_pairs, long* npairs, int* trimers, long cap_trimers,
