@@ -46,6 +46,21 @@ struct mbx_context {
     cudaEvent_t ev[8] = {nullptr};
     float phase_ms[4] = {0, 0, 0, 0};  // lists, 2B, 3B, heat/jkin
     long launches = 0;                 // kernel launches issued by the last evaluation
+    // many boxes in one evaluation (mbx_mbpol_multi*): buffers, and the step captured as
+    // a CUDA graph that is replayed while its key (arrays, layout, precision) is unchanged
+    MultiBoxes multi;
+    int use_graphs = 1;
+    cudaGraphExec_t mexec = nullptr;
+    const void* mkey[15] = {nullptr};
+    long mkey_gen = -1;
+    int mkey_prec = -1;
+    float mkey_lim[2] = {0, 0};
+    cudaStream_t mkey_stream = nullptr;
+    Cell* cells_h = nullptr;           // pinned, one per box
+    double* mout_h = nullptr;          // pinned: per-box MB-pol and 1-body scalars
+    int* mint_h = nullptr;             // pinned: totals[2], flag, hand-off counts[2]
+    int mbox_cap = 0;
+    long graph_replays = 0;
     char err[512] = {0};
 };
 
@@ -219,6 +234,139 @@ int run_mbpol(mbx_context* ctx, int precision, const Cell& cl, int nw, const int
     return MBX_OK;
 }
 
+// One multi-box step on device arrays: the cell copy, every kernel and the copies of the
+// per-box scalars back to pinned host memory are enqueued (or replayed as one graph),
+// then the host waits once.  A list that outgrew its capacity makes the step a no-op on
+// the device; the host then grows the lists and repeats it.
+int run_multi(mbx_context* ctx, int precision, int nbox, const int* nw_box, const double* x, const double* y,
+              const double* z, double* fx, double* fy, double* fz, const double* vx, const double* vy,
+              const double* vz, const double* mass, double* ae, double* scalars) {
+    cudaStream_t s = ctx->stream;
+    MultiBoxes& m = ctx->multi;
+    const bool need_hard =
+        precision == MBX_MIXED && (ctx->limit2 > 0.f || (ctx->limit3 > 0.f && ctx->limit3 < 3.0e38f));
+    const bool heat = vx && vy && vz;
+    MixedPass lim{nullptr, nullptr, nullptr, ctx->limit2, ctx->limit3};
+    if (ctx->profiling) CK(cudaEventRecord(ctx->ev[0], s));
+    for (int attempt = 0;; ++attempt) {
+        CK(m.setup(nbox, nw_box, need_hard, s));
+        auto enqueue_all = [&]() -> cudaError_t {
+            cudaError_t e;
+            if ((e = cudaMemcpyAsync(m.cells, ctx->cells_h, nbox * sizeof(Cell), cudaMemcpyHostToDevice, s)))
+                return e;
+            if ((e = m.enqueue(precision, lim, x, y, z, fx, fy, fz, heat ? vx : nullptr, heat ? vy : nullptr,
+                               heat ? vz : nullptr, heat ? mass : nullptr, ae, s)))
+                return e;
+            if ((e = cudaMemcpyAsync(ctx->mout_h, m.acc_box, (size_t)nbox * S_NSLOTS * sizeof(double),
+                                     cudaMemcpyDeviceToHost, s)))
+                return e;
+            if ((e = cudaMemcpyAsync(ctx->mout_h + (size_t)nbox * S_NSLOTS, m.pes_box, (size_t)nbox * 14 * sizeof(double),
+                                     cudaMemcpyDeviceToHost, s)))
+                return e;
+            if ((e = cudaMemcpyAsync(ctx->mint_h, m.totals, 2 * sizeof(int), cudaMemcpyDeviceToHost, s))) return e;
+            if ((e = cudaMemcpyAsync(ctx->mint_h + 2, m.flag, sizeof(int), cudaMemcpyDeviceToHost, s))) return e;
+            return cudaMemcpyAsync(ctx->mint_h + 3, m.hard_count, 2 * sizeof(int), cudaMemcpyDeviceToHost, s);
+        };
+        const void* key[15] = {x, y, z, fx, fy, fz, heat ? vx : nullptr, heat ? vy : nullptr, heat ? vz : nullptr,
+                               heat ? mass : nullptr, ae, (const void*)(long)nbox, ctx->cells_h, ctx->mout_h,
+                               ctx->mint_h};
+        bool launched = false;
+        if (ctx->use_graphs) {
+            const bool same = ctx->mexec && m.gen == ctx->mkey_gen && precision == ctx->mkey_prec &&
+                              ctx->mkey_lim[0] == ctx->limit2 && ctx->mkey_lim[1] == ctx->limit3 &&
+                              ctx->mkey_stream == s && std::memcmp(key, ctx->mkey, sizeof key) == 0;
+            if (!same) {
+                if (ctx->mexec) cudaGraphExecDestroy(ctx->mexec);
+                ctx->mexec = nullptr;
+                cudaGraph_t g = nullptr;
+                if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+                    const cudaError_t e1 = enqueue_all();
+                    const cudaError_t e2 = cudaStreamEndCapture(s, &g);
+                    if (e1 == cudaSuccess && e2 == cudaSuccess && g &&
+                        cudaGraphInstantiate(&ctx->mexec, g, 0) == cudaSuccess) {
+                        std::memcpy(ctx->mkey, key, sizeof key);
+                        ctx->mkey_gen = m.gen;
+                        ctx->mkey_prec = precision;
+                        ctx->mkey_lim[0] = ctx->limit2;
+                        ctx->mkey_lim[1] = ctx->limit3;
+                        ctx->mkey_stream = s;
+                    } else {
+                        ctx->mexec = nullptr;
+                    }
+                    if (g) cudaGraphDestroy(g);
+                }
+                cudaGetLastError();   // a failed capture leaves no sticky error; run uncaptured below
+            }
+            if (ctx->mexec) {
+                CK(cudaGraphLaunch(ctx->mexec, s));
+                ++ctx->graph_replays;
+                launched = true;
+            }
+        }
+        if (!launched) CK(enqueue_all());
+        CK(cudaStreamSynchronize(s));
+        if (!ctx->mint_h[2]) break;
+        if (attempt >= 6 || m.cap2 > 4096) return fail(ctx, MBX_ERR_CAPACITY, "multi-box list capacity exceeded");
+        // grow what overflowed and repeat the step (nothing was accumulated)
+        if (ctx->mint_h[2] & 1) {
+            m.cap2 *= 2;
+            m.cap3 *= 2;
+        }
+        if (ctx->mint_h[2] & 2) m.trip_per_water *= 2;
+        m.release();
+    }
+    if (ctx->profiling) {
+        CK(cudaEventRecord(ctx->ev[1], s));
+        CK(cudaEventSynchronize(ctx->ev[1]));
+        CK(cudaEventElapsedTime(&ctx->phase_ms[0], ctx->ev[0], ctx->ev[1]));
+        ctx->phase_ms[1] = ctx->phase_ms[2] = ctx->phase_ms[3] = 0.f;
+    }
+    ctx->npairs = ctx->mint_h[0];
+    ctx->ntrip = ctx->mint_h[1];
+    ctx->launches = m.launches;
+    ctx->hard_last[0] = need_hard ? ctx->mint_h[3] : 0;
+    ctx->hard_last[1] = need_hard ? ctx->mint_h[4] : 0;
+    if (scalars)
+        for (int b = 0; b < nbox; ++b) {
+            std::memcpy(scalars + (size_t)b * MBX_NBOXSCALARS, ctx->mout_h + (size_t)b * S_NSLOTS,
+                        S_NSLOTS * sizeof(double));
+            std::memcpy(scalars + (size_t)b * MBX_NBOXSCALARS + MBX_NSCALARS,
+                        ctx->mout_h + (size_t)nbox * S_NSLOTS + (size_t)b * 14, 14 * sizeof(double));
+        }
+    return MBX_OK;
+}
+
+// Validate the box layout and stage the cells (pinned) for run_multi.
+int prepare_multi(mbx_context* ctx, int precision, int imcon, int nbox, const int* nw_box, const double* cells,
+                  long* natms_out) {
+    if (precision != MBX_FP64 && precision != MBX_MIXED)
+        return fail(ctx, MBX_ERR_ARG, "precision must be MBX_FP64 or MBX_MIXED");
+    if (nbox < 1 || !nw_box || !cells) return fail(ctx, MBX_ERR_ARG, "nbox must be >= 1 with nw_box and cells");
+    long nw = 0;
+    for (int b = 0; b < nbox; ++b) {
+        if (nw_box[b] < 0) return fail(ctx, MBX_ERR_ARG, "nw_box[%d] = %d", b, nw_box[b]);
+        nw += nw_box[b];
+    }
+    if (nw > (1L << 26)) return fail(ctx, MBX_ERR_ARG, "too many waters (%ld)", nw);
+    CK(cudaSetDevice(ctx->device));
+    if (nbox > ctx->mbox_cap) {
+        if (ctx->cells_h) cudaFreeHost(ctx->cells_h);
+        if (ctx->mout_h) cudaFreeHost(ctx->mout_h);
+        ctx->cells_h = nullptr;
+        ctx->mout_h = nullptr;
+        CK(cudaMallocHost(&ctx->cells_h, nbox * sizeof(Cell)));
+        CK(cudaMallocHost(&ctx->mout_h, (size_t)nbox * (S_NSLOTS + 14) * sizeof(double)));
+        ctx->mbox_cap = nbox;
+    }
+    if (!ctx->mint_h) CK(cudaMallocHost(&ctx->mint_h, 8 * sizeof(int)));
+    for (int b = 0; b < nbox; ++b) {
+        const int rc = make_cell(ctx, imcon, cells + 9 * (size_t)b, ctx->cells_h[b]);
+        if (rc) return rc;
+    }
+    *natms_out = 4 * nw;
+    return MBX_OK;
+}
+
 int check_device(mbx_context* ctx, int device) {
     int n = 0;
     if (cudaGetDeviceCount(&n) != cudaSuccess || n <= device || device < 0)
@@ -280,6 +428,11 @@ extern "C" void mbx_destroy(mbx_context* ctx) {
         if (p) cudaFree(p);
     if (ctx->totals_h) cudaFreeHost(ctx->totals_h);
     if (ctx->acc_h) cudaFreeHost(ctx->acc_h);
+    if (ctx->mexec) cudaGraphExecDestroy(ctx->mexec);
+    if (ctx->cells_h) cudaFreeHost(ctx->cells_h);
+    if (ctx->mout_h) cudaFreeHost(ctx->mout_h);
+    if (ctx->mint_h) cudaFreeHost(ctx->mint_h);
+    ctx->multi.release();
     ctx->lb.release();
     for (cudaEvent_t e : ctx->ev)
         if (e) cudaEventDestroy(e);
@@ -404,6 +557,82 @@ extern "C" int mbx_mbpol_forces(mbx_context* ctx, int precision, int imcon, cons
     *virsrp += sc[MBX_S_VIR];
     for (int q = 0; q < 9; ++q) stress[q] += sc[MBX_S_STRESS + q];
     if (scalars) std::memcpy(scalars, sc, sizeof sc);
+    return MBX_OK;
+}
+
+extern "C" int mbx_set_graphs(mbx_context* ctx, int on) {
+    if (!ctx) return MBX_ERR_ARG;
+    ctx->use_graphs = on ? 1 : 0;
+    return MBX_OK;
+}
+
+extern "C" long mbx_graph_launches(const mbx_context* ctx) { return ctx ? ctx->graph_replays : -1; }
+
+extern "C" int mbx_mbpol_multi_device(mbx_context* ctx, int precision, int imcon, int nbox, const int* nw_box,
+                                      const double* cells, const double* xxx, const double* yyy, const double* zzz,
+                                      double* fxx, double* fyy, double* fzz, const double* vxx, const double* vyy,
+                                      const double* vzz, const double* weight, double* atomic_energy,
+                                      double* scalars) {
+    if (!ctx) return MBX_ERR_ARG;
+    long natms = 0;
+    int rc = prepare_multi(ctx, precision, imcon, nbox, nw_box, cells, &natms);
+    if (rc) return rc;
+    if (natms > 0 && (!xxx || !yyy || !zzz || !fxx || !fyy || !fzz))
+        return fail(ctx, MBX_ERR_ARG, "NULL position/force array");
+    const bool heat = vxx && vyy && vzz && weight;
+    return run_multi(ctx, precision, nbox, nw_box, xxx, yyy, zzz, fxx, fyy, fzz, heat ? vxx : nullptr,
+                     heat ? vyy : nullptr, heat ? vzz : nullptr, heat ? weight : nullptr, atomic_energy, scalars);
+}
+
+extern "C" int mbx_mbpol_multi(mbx_context* ctx, int precision, int imcon, int nbox, const int* nw_box,
+                               const double* cells, const double* xxx, const double* yyy, const double* zzz,
+                               double* fxx, double* fyy, double* fzz, const double* vxx, const double* vyy,
+                               const double* vzz, const double* weight, double* atomic_energy, double* scalars) {
+    if (!ctx) return MBX_ERR_ARG;
+    long natms_l = 0;
+    int rc = prepare_multi(ctx, precision, imcon, nbox, nw_box, cells, &natms_l);
+    if (rc) return rc;
+    const int natms = (int)natms_l;
+    if (natms > 0 && (!xxx || !yyy || !zzz || !fxx || !fyy || !fzz))
+        return fail(ctx, MBX_ERR_ARG, "NULL position/force array");
+    rc = reserve_water(ctx, std::max(natms / 4, 1), std::max(natms, 1));
+    if (rc) return rc;
+    const bool heat = vxx && vyy && vzz && weight;
+    cudaStream_t s = ctx->stream;
+    const size_t nb = (size_t)natms * sizeof(double);
+    double* d = ctx->atoms;
+    double *dx = d, *dy = d + natms, *dz = d + 2 * (size_t)natms;
+    double *dvx = d + 3 * (size_t)natms, *dvy = d + 4 * (size_t)natms, *dvz = d + 5 * (size_t)natms;
+    double* dm = d + 6 * (size_t)natms;
+    double *dfx = d + 7 * (size_t)natms, *dfy = d + 8 * (size_t)natms, *dfz = d + 9 * (size_t)natms;
+    double* dae = d + 10 * (size_t)natms;
+    if (natms) {
+        CK(cudaMemcpyAsync(dx, xxx, nb, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(dy, yyy, nb, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(dz, zzz, nb, cudaMemcpyHostToDevice, s));
+        if (heat) {
+            CK(cudaMemcpyAsync(dvx, vxx, nb, cudaMemcpyHostToDevice, s));
+            CK(cudaMemcpyAsync(dvy, vyy, nb, cudaMemcpyHostToDevice, s));
+            CK(cudaMemcpyAsync(dvz, vzz, nb, cudaMemcpyHostToDevice, s));
+            CK(cudaMemcpyAsync(dm, weight, nb, cudaMemcpyHostToDevice, s));
+        }
+        CK(cudaMemsetAsync(dfx, 0, 3 * nb, s));
+        if (atomic_energy) CK(cudaMemsetAsync(dae, 0, nb, s));
+    }
+    rc = run_multi(ctx, precision, nbox, nw_box, dx, dy, dz, dfx, dfy, dfz, heat ? dvx : nullptr,
+                   heat ? dvy : nullptr, heat ? dvz : nullptr, heat ? dm : nullptr, atomic_energy ? dae : nullptr,
+                   scalars);
+    if (rc || !natms) return rc;
+    std::vector<double> h(4 * (size_t)natms);
+    CK(cudaMemcpyAsync(h.data(), dfx, 3 * nb, cudaMemcpyDeviceToHost, s));
+    if (atomic_energy) CK(cudaMemcpyAsync(h.data() + 3 * (size_t)natms, dae, nb, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    for (int i = 0; i < natms; ++i) {
+        fxx[i] += h[i];
+        fyy[i] += h[natms + i];
+        fzz[i] += h[2 * (size_t)natms + i];
+        if (atomic_energy) atomic_energy[i] += h[3 * (size_t)natms + i];
+    }
     return MBX_OK;
 }
 

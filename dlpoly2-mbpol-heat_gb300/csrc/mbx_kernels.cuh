@@ -3,6 +3,8 @@
 
 #include "mbx_common.cuh"
 
+#include <vector>
+
 namespace mbx {
 
 // Accumulator slots of the per-evaluation scalar buffer (double, device).
@@ -27,6 +29,11 @@ struct MbpolArgs {
     double *fx, *fy, *fz;            // forces, accumulated
     double* ae;                      // per-atom energy, accumulated (may be null)
     double* acc;                     // S_NSLOTS scalars, accumulated
+    // several boxes in one launch (null for one box): cell of box b, box of water i,
+    // and per-box accumulators acc_box[b * S_NSLOTS + slot]
+    const Cell* cells = nullptr;
+    const int* wbox = nullptr;
+    double* acc_box = nullptr;
 };
 
 // Mixed-precision pass: FP32 kernels hand ill-conditioned clusters (a shifted
@@ -44,6 +51,12 @@ cudaError_t launch_2b(const MbpolArgs& a, const int2* pairs, int npairs, int pre
                       cudaStream_t s);
 cudaError_t launch_3b(const MbpolArgs& a, const int4* trip, int ntrip, int precision, const MixedPass& mp,
                       cudaStream_t s);
+// The same with the cluster count on the device (`n_dev`) and the grid sized for `cap`
+// clusters: no host synchronisation between list building and evaluation.
+cudaError_t launch_2b_dev(const MbpolArgs& a, const int2* pairs, long cap, const int* n_dev, int precision,
+                          const MixedPass& mp, cudaStream_t s);
+cudaError_t launch_3b_dev(const MbpolArgs& a, const int4* trip, long cap, const int* n_dev, int precision,
+                          const MixedPass& mp, cudaStream_t s);
 // Isolated polynomial + model evaluation for explicit clusters (the per-call ABI).
 cudaError_t launch_2b_direct(int n, const double* w1, const double* w2, double* E, double* g1, double* g2,
                              int precision, cudaStream_t s);
@@ -58,10 +71,21 @@ cudaError_t launch_ps_pes(int nang, const int* listang, const Cell& cl, const do
                           const double* z, double* fx, double* fy, double* fz, double* ae, const double* vx,
                           const double* vy, const double* vz, double* acc14, cudaStream_t s);
 
+// The same over the waters of many boxes: angle t belongs to box abox[t], with cell
+// cells[box] and accumulators acc14_box[14 * box ..]; nothing is done when *skip != 0.
+cudaError_t launch_ps_pes_boxes(int nang, const int* listang, const Cell* cells, const int* abox, const double* x,
+                                const double* y, const double* z, double* fx, double* fy, double* fz, double* ae,
+                                const double* vx, const double* vy, const double* vz, double* acc14_box,
+                                const int* skip, cudaStream_t s);
+
 // M sites written into x/y/z at index listttm2[3nw-1] + i (0-based) and DMS charges
 // into chge (H1, H2, M) and dp[6*nw] (mbx_pes.cu); chge/dp may be null.
 cudaError_t launch_msites_dms(int nw, const int* list, const Cell& cl, double* x, double* y, double* z, double gamma,
                               double* chge, double* dp, cudaStream_t s);
+
+// Dimer list from the per-water partner lists: pairs[off2[i] + q] = (i, l2[i*cap2 + q]).
+void launch_pairs_compact(int nw, int cap2, const int* n2, const int* off2, const int* l2, int2* pairs,
+                          cudaStream_t s);
 
 __global__ void k_list_totals(int nw, const int* n2, const int* off2, const int* tcnt, const int* toff,
                               const int* flag, int* totals);
@@ -92,6 +116,48 @@ struct ListBuilder {
     cudaError_t phase1(int nw, const int* list, const double* x, const double* y, const double* z, const Cell& cl,
                        double* mono, int* totals_dev, cudaStream_t s);
     cudaError_t phase2(int nw, const Cell& cl, const double* mono, int2* pairs, int4* trip, cudaStream_t s);
+};
+
+// Many independent water boxes evaluated by one set of launches (mbx_multi.cu).
+// Box b holds nw_b waters in the standard layout (3*nw_b water atoms, O H1 H2, then
+// nw_b M sites) at atom offset 4 * sum_{b'<b} nw_b'.  Every size is fixed by setup(),
+// list lengths stay on the device, so enqueue() issues no host synchronisation and can
+// be captured as a CUDA graph.
+struct MultiBoxes {
+    int cap2 = 64, cap3 = 48;     // partners / 3B neighbours per water
+    int trip_per_water = 160;     // trimer capacity per water (a 4096-water liquid box has ~98)
+    int nbox = 0, nw = 0, natms = 0;
+    std::vector<int> nw_of_box;
+    int *list = nullptr, *listang = nullptr, *wbox = nullptr, *abox = nullptr;
+    unsigned char* is_water = nullptr;
+    Cell* cells = nullptr;
+    int *bstart = nullptr, *bcount = nullptr;
+    double* mono = nullptr;
+    int *n2 = nullptr, *l2 = nullptr, *off2 = nullptr, *n3 = nullptr, *l3 = nullptr, *tcnt = nullptr,
+        *toff = nullptr;
+    int2* pairs = nullptr;
+    int4* trip = nullptr;
+    long pair_cap = 0, trip_cap = 0;
+    int2* hard2 = nullptr;         // mixed-path hand-off lists (allocated when a limit asks)
+    int4* hard3 = nullptr;
+    int* hard_count = nullptr;
+    void* scan_tmp = nullptr;
+    size_t scan_bytes = 0;
+    double* acc_box = nullptr;     // S_NSLOTS per box
+    double* pes_box = nullptr;     // 14 per box (1-body term)
+    double* ae_scratch = nullptr;  // per-atom energy for the heat current when the caller passes none
+    int* totals = nullptr;         // [0] dimers, [1] trimers
+    int* flag = nullptr;           // bit 0: neighbour capacity, bit 1: trimer capacity
+    long launches = 0;             // kernels issued by one enqueue (CUB included)
+    long gen = 0;                  // bumped whenever setup() (re)allocates
+
+    ~MultiBoxes();
+    void release();
+    // (re)allocate for this box layout; a no-op when the layout is unchanged
+    cudaError_t setup(int nbox, const int* nw_box, bool need_hard, cudaStream_t s);
+    cudaError_t enqueue(int precision, const MixedPass& limits, const double* x, const double* y, const double* z,
+                        double* fx, double* fy, double* fz, const double* vx, const double* vy, const double* vz,
+                        const double* mass, double* ae, cudaStream_t s);
 };
 
 }  // namespace mbx

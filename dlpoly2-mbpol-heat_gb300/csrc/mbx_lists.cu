@@ -335,6 +335,12 @@ cudaError_t ListBuilder::phase2(int nw, const Cell& cl, const double* mono, int2
     return cudaGetLastError();
 }
 
+void launch_pairs_compact(int nw, int cap2, const int* n2, const int* off2, const int* l2, int2* pairs,
+                          cudaStream_t s) {
+    if (nw <= 0) return;
+    k_pairs_compact<<<grid_for(nw), kThreads, 0, s>>>(nw, cap2, n2, off2, l2, pairs);
+}
+
 __global__ void k_list_totals(int nw, const int* n2, const int* off2, const int* tcnt, const int* toff,
                               const int* flag, int* totals) {
     totals[0] = nw > 0 ? off2[nw - 1] + min(n2[nw - 1], 0x7fffffff) : 0;

@@ -403,6 +403,33 @@ __device__ __forceinline__ void flush_block(double (&red)[14], double* acc, int 
     flush_block_n<kThreads>(red, acc, eslot);
 }
 
+__device__ __forceinline__ int red_slot(int q, int eslot) {
+    return q == 0 ? eslot : (q == 1 ? S_VIR : (q <= 10 ? S_STRESS + (q - 2) : S_JPOT + (q - 11)));
+}
+
+// Several boxes in one launch: clusters are grouped by box, so a warp almost always
+// holds one box -- reduce it with shuffles; a warp straddling boxes adds per lane.
+// box < 0: this thread holds no cluster.
+__device__ __forceinline__ void flush_boxes(double (&red)[14], double* acc_box, int box, int eslot) {
+    int lo = box < 0 ? 0x7fffffff : box, hi = box;
+    for (int o = 16; o > 0; o >>= 1) {
+        lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+        hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+    }
+    if (hi < 0) return;
+    if (lo == hi) {
+#pragma unroll
+        for (int q = 0; q < 14; ++q) {
+            const double v = warp_sum(red[q]);
+            if ((threadIdx.x & 31) == 0 && v != 0.0) atomicAdd(acc_box + (size_t)hi * S_NSLOTS + red_slot(q, eslot), v);
+        }
+    } else if (box >= 0) {
+#pragma unroll
+        for (int q = 0; q < 14; ++q)
+            if (red[q] != 0.0) atomicAdd(acc_box + (size_t)box * S_NSLOTS + red_slot(q, eslot), red[q]);
+    }
+}
+
 // Mixed-precision hand-off: clusters whose FP32 variables stray beyond the limit
 // are appended to `hard` and evaluated by the FP64 kernel afterwards.
 struct HardList {
@@ -419,8 +446,11 @@ __global__ void __launch_bounds__(kThreads) k_mbpol_2b(MbpolArgs a, const int2* 
     double red[14];
 #pragma unroll
     for (int q = 0; q < 14; ++q) red[q] = 0.0;
+    int box = -1;
     if (t < n) {
         const int i = pairs[t].x, j = pairs[t].y;
+        if (a.cells) box = a.wbox[i];
+        const Cell& cl = a.cells ? a.cells[box] : a.cell;
         double w1[9], w2[9];
 #pragma unroll
         for (int q = 0; q < 9; ++q) {
@@ -428,7 +458,7 @@ __global__ void __launch_bounds__(kThreads) k_mbpol_2b(MbpolArgs a, const int2* 
             w2[q] = a.mono[9 * (size_t)j + q];
         }
         double r12[3];
-        dist2_img(a.cell, w1, w2, r12);
+        dist2_img(cl, w1, w2, r12);
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
             w1[3 + k] = dadd(dsub(w1[3 + k], w1[k]), dadd(w2[k], r12[k]));
@@ -462,7 +492,8 @@ __global__ void __launch_bounds__(kThreads) k_mbpol_2b(MbpolArgs a, const int2* 
             cluster_accumulate<6>(a, at, (double)e, w, g, red);
         }
     }
-    flush_block(red, a.acc, S_E2);
+    if (a.acc_box) flush_boxes(red, a.acc_box, box, S_E2);
+    else flush_block(red, a.acc, S_E2);
 }
 
 // Gather the trimer's monomers and re-image them around the second one as do_trimer
@@ -478,8 +509,9 @@ __device__ __forceinline__ void prep_3b(const MbpolArgs& a, int4 c, double* w, T
         w3[q] = a.mono[9 * (size_t)c.z + q];
     }
     double r12[3], r23[3];
-    dist2_img(a.cell, w1, w2, r12);
-    dist2_img(a.cell, w2, w3, r23);
+    const Cell& cl = a.cells ? a.cells[a.wbox[c.x]] : a.cell;
+    dist2_img(cl, w1, w2, r12);
+    dist2_img(cl, w2, w3, r23);
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
         w1[3 + k] = dadd(dsub(w1[3 + k], w1[k]), dadd(w2[k], r12[k]));
@@ -515,8 +547,10 @@ __global__ void __launch_bounds__(kThreads) k_mbpol_3b(MbpolArgs a, const int4* 
     double red[14];
 #pragma unroll
     for (int q = 0; q < 14; ++q) red[q] = 0.0;
+    int box = -1;
     if (t < n) {
         const int4 c = trip[t];
+        if (a.cells) box = a.wbox[c.x];
         T p[27], gt[27];
         double w[27];
         prep_3b<T>(a, c, w, p);
@@ -535,7 +569,8 @@ __global__ void __launch_bounds__(kThreads) k_mbpol_3b(MbpolArgs a, const int4* 
             cluster_accumulate<9>(a, at, (double)e, w, g, red);
         }
     }
-    flush_block(red, a.acc, S_E3);
+    if (a.acc_box) flush_boxes(red, a.acc_box, box, S_E3);
+    else flush_block(red, a.acc, S_E3);
 }
 
 // Per-call model evaluation (drop-in for mbpol_2b_poly_/mbpol_3b_poly_ over many clusters).
@@ -644,6 +679,36 @@ cudaError_t launch_3b(const MbpolArgs& a, const int4* trip, int n, int precision
                                                          HardList{mp.hard3, mp.count + 1, mp.limit3});
         k_mbpol_3b<double><<<blocks(n), kThreads, 0, s>>>(a, mp.hard3, n, mp.count + 1,
                                                           HardList{nullptr, nullptr, 0.f});
+    }
+    return cudaGetLastError();
+}
+
+static int blocks_l(long n) { return (int)((n + kThreads - 1) / kThreads); }
+
+cudaError_t launch_2b_dev(const MbpolArgs& a, const int2* pairs, long cap, const int* n_dev, int precision,
+                          const MixedPass& mp, cudaStream_t s) {
+    if (cap <= 0) return cudaSuccess;
+    const int g = blocks_l(cap);
+    if (precision == 0 || !(mp.limit2 > 0.f)) {
+        k_mbpol_2b<double><<<g, kThreads, 0, s>>>(a, pairs, 0, n_dev, HardList{nullptr, nullptr, 0.f});
+    } else {
+        k_mbpol_2b<float><<<g, kThreads, 0, s>>>(a, pairs, 0, n_dev, HardList{mp.hard2, mp.count + 0, mp.limit2});
+        k_mbpol_2b<double><<<g, kThreads, 0, s>>>(a, mp.hard2, 0, mp.count + 0, HardList{nullptr, nullptr, 0.f});
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_3b_dev(const MbpolArgs& a, const int4* trip, long cap, const int* n_dev, int precision,
+                          const MixedPass& mp, cudaStream_t s) {
+    if (cap <= 0) return cudaSuccess;
+    const int g = blocks_l(cap);
+    if (precision == 0 || !(mp.limit3 > 0.f)) {
+        k_mbpol_3b<double><<<g, kThreads, 0, s>>>(a, trip, 0, n_dev, HardList{nullptr, nullptr, 0.f});
+    } else if (!(mp.limit3 < 3.0e38f)) {
+        k_mbpol_3b<float><<<g, kThreads, 0, s>>>(a, trip, 0, n_dev, HardList{nullptr, nullptr, 0.f});
+    } else {
+        k_mbpol_3b<float><<<g, kThreads, 0, s>>>(a, trip, 0, n_dev, HardList{mp.hard3, mp.count + 1, mp.limit3});
+        k_mbpol_3b<double><<<g, kThreads, 0, s>>>(a, mp.hard3, 0, mp.count + 1, HardList{nullptr, nullptr, 0.f});
     }
     return cudaGetLastError();
 }

@@ -124,7 +124,10 @@ __global__ void __launch_bounds__(kThreads) k_ps_pes(int nang, const int* __rest
                                                       const double* __restrict__ z, double* fx, double* fy,
                                                       double* fz, double* ae, const double* __restrict__ vx,
                                                       const double* __restrict__ vy, const double* __restrict__ vz,
-                                                      double* acc) {
+                                                      double* acc, const Cell* __restrict__ cells,
+                                                      const int* __restrict__ abox, double* acc_box,
+                                                      const int* __restrict__ skip) {
+    if (skip && *skip) return;   // block-uniform
     const int t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     // red = {E, virial, stress[9], jpot[3]} (lane 0 of each warp)
@@ -135,8 +138,13 @@ __global__ void __launch_bounds__(kThreads) k_ps_pes(int nang, const int* __rest
         const int ia = listang[3 * t] - 1, ib = listang[3 * t + 1] - 1, ic = listang[3 * t + 2] - 1;
         double xab = x[ia] - x[ib], yab = y[ia] - y[ib], zab = z[ia] - z[ib];
         double xbc = x[ic] - x[ib], ybc = y[ic] - y[ib], zbc = z[ic] - z[ib];
-        image(cl, xab, yab, zab);
-        image(cl, xbc, ybc, zbc);
+        if (cells) {
+            image(cells[abox[t]], xab, yab, zab);
+            image(cells[abox[t]], xbc, ybc, zbc);
+        } else {
+            image(cl, xab, yab, zab);
+            image(cl, xbc, ybc, zbc);
+        }
         const double rab = sqrt(xab * xab + yab * yab + zab * zab);
         const double rbc = sqrt(xbc * xbc + ybc * ybc + zbc * zbc);
         const double rrab = 1.0 / rab, rrbc = 1.0 / rbc;
@@ -172,7 +180,33 @@ __global__ void __launch_bounds__(kThreads) k_ps_pes(int nang, const int* __rest
             }
         }
     }
-    block_sum_atomic<14>(red, acc);
+    if (!acc_box) {
+        block_sum_atomic<14>(red, acc);
+        return;
+    }
+    // several boxes: one block sum when the block's angles share a box (the usual case,
+    // boxes are contiguous), otherwise lane 0 of each warp adds its own angle
+    __shared__ int span[2];
+    if (threadIdx.x == 0) {
+        span[0] = 0x7fffffff;
+        span[1] = -1;
+    }
+    __syncthreads();
+    const int box = t < nang ? abox[t] : -1;
+    if (lane == 0 && box >= 0) {
+        atomicMin(&span[0], box);
+        atomicMax(&span[1], box);
+    }
+    __syncthreads();
+    const int lo = span[0], hi = span[1];
+    if (hi < 0) return;   // block-uniform
+    if (lo == hi) {
+        block_sum_atomic<14>(red, acc_box + 14 * (size_t)hi);
+    } else if (lane == 0 && box >= 0) {
+#pragma unroll
+        for (int q = 0; q < 14; ++q)
+            if (red[q] != 0.0) atomicAdd(acc_box + 14 * (size_t)box + q, red[q]);
+    }
 }
 
 // M-site placement (SOURCE/dlpoly_cmd.f:2041-2057) and qdetermine with the MB-pol
@@ -266,7 +300,19 @@ cudaError_t launch_ps_pes(int nang, const int* listang, const Cell& cl, const do
                           const double* vy, const double* vz, double* acc14, cudaStream_t s) {
     if (nang <= 0) return cudaSuccess;
     const int blocks = (int)(((long)nang * 32 + kThreads - 1) / kThreads);   // one warp per angle
-    k_ps_pes<<<blocks, kThreads, 0, s>>>(nang, listang, cl, x, y, z, fx, fy, fz, ae, vx, vy, vz, acc14);
+    k_ps_pes<<<blocks, kThreads, 0, s>>>(nang, listang, cl, x, y, z, fx, fy, fz, ae, vx, vy, vz, acc14, nullptr,
+                                         nullptr, nullptr, nullptr);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_ps_pes_boxes(int nang, const int* listang, const Cell* cells, const int* abox, const double* x,
+                                const double* y, const double* z, double* fx, double* fy, double* fz, double* ae,
+                                const double* vx, const double* vy, const double* vz, double* acc14_box,
+                                const int* skip, cudaStream_t s) {
+    if (nang <= 0) return cudaSuccess;
+    const int blocks = (int)(((long)nang * 32 + kThreads - 1) / kThreads);
+    k_ps_pes<<<blocks, kThreads, 0, s>>>(nang, listang, Cell{}, x, y, z, fx, fy, fz, ae, vx, vy, vz, nullptr, cells,
+                                         abox, acc14_box, skip);
     return cudaGetLastError();
 }
 

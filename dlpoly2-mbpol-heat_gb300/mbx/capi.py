@@ -18,6 +18,7 @@ HEADER = os.path.join(REPO, "include", "mbx.h")
 FP64 = 0
 MIXED = 1
 NSCALARS = 18
+NBOXSCALARS = NSCALARS + 14
 S_ENG2, S_ENG3, S_VIR, S_STRESS, S_JPOT, S_JKIN = 0, 1, 2, 3, 12, 15
 
 _D = C.POINTER(C.c_double)
@@ -35,7 +36,7 @@ def header_functions():
     with open(HEADER) as f:
         text = f.read()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-    return re.findall(r"^\s*(?:int|void|const char\*)\s+\**\s*(\w+)\s*\(", text, flags=re.M)
+    return re.findall(r"^\s*(?:int|long|void|const char\*)\s+\**\s*(\w+)\s*\(", text, flags=re.M)
 
 
 def load(path=None):
@@ -77,6 +78,11 @@ def load(path=None):
     L.mbx_server_wait.argtypes = [C.c_void_p, C.c_long] + [_D] * 6
     L.mbx_server_error.argtypes = [C.c_void_p]
     L.mbx_server_error.restype = C.c_char_p
+    L.mbx_mbpol_multi.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, _I, _D] + [_D] * 12
+    L.mbx_mbpol_multi_device.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, _I, _D] + [C.c_void_p] * 11 + [_D]
+    L.mbx_set_graphs.argtypes = [C.c_void_p, C.c_int]
+    L.mbx_graph_launches.argtypes = [C.c_void_p]
+    L.mbx_graph_launches.restype = C.c_long
     L.mbx_last_lists.argtypes = [C.c_void_p, _I, C.c_long, _L, _I, C.c_long, _L]
     L.mbx_2b_poly_batch.argtypes = [C.c_void_p, C.c_int, C.c_long, _D, _D, _D, _D, _D]
     L.mbx_3b_poly_batch.argtypes = [C.c_void_p, C.c_int, C.c_long, _D, _D, _D, _D, _D, _D, _D]
@@ -200,6 +206,42 @@ class Context:
                                               *xyz_ptrs, *f_ptrs, *v_ptrs, mass_ptr, ae_ptr, _p(sc))
         self._check(rc, "mbx_mbpol_forces_device")
         return sc
+
+    def mbpol_multi(self, boxset, precision=FP64, heat=True, atomic_energy=True):
+        """Every box of a BoxSet in one evaluation (host arrays).  Returns the packed
+        forces/energies and scalars[nbox, NBOXSCALARS] (MB-pol block, then the 1-body
+        engang, virang, stress[9], jpot[3])."""
+        n = boxset.natms
+        x, y, z = (_f64(boxset.xyz[:, k]) for k in range(3))
+        f = np.zeros((3, n))
+        ae = np.zeros(n) if atomic_energy else None
+        sc = np.zeros((boxset.nbox, NBOXSCALARS))
+        v = [_f64(boxset.vel[:, k]) for k in range(3)] if heat else [None] * 3
+        m = _f64(boxset.mass) if heat else None
+        nwb = np.ascontiguousarray(boxset.nw_box, dtype=np.int32)
+        rc = self.lib.mbx_mbpol_multi(self.h, precision, boxset.imcon, boxset.nbox, _p(nwb, _I), _p(boxset.cells),
+                                      _p(x), _p(y), _p(z), _p(f[0]), _p(f[1]), _p(f[2]), _p(v[0]), _p(v[1]),
+                                      _p(v[2]), _p(m), _p(ae), _p(sc))
+        self._check(rc, "mbx_mbpol_multi")
+        return dict(forces=f.T.copy(), atomic_energy=ae, scalars=sc)
+
+    def mbpol_multi_device(self, precision, boxset, xyz_ptrs, f_ptrs, v_ptrs=None, mass_ptr=None, ae_ptr=None,
+                           cells=None):
+        """Device-pointer multi-box entry point; returns scalars[nbox, NBOXSCALARS]."""
+        sc = np.zeros((boxset.nbox, NBOXSCALARS))
+        v_ptrs = v_ptrs or (None, None, None)
+        nwb = np.ascontiguousarray(boxset.nw_box, dtype=np.int32)
+        cells = boxset.cells if cells is None else _f64(cells)
+        rc = self.lib.mbx_mbpol_multi_device(self.h, precision, boxset.imcon, boxset.nbox, _p(nwb, _I), _p(cells),
+                                             *xyz_ptrs, *f_ptrs, *v_ptrs, mass_ptr, ae_ptr, _p(sc))
+        self._check(rc, "mbx_mbpol_multi_device")
+        return sc
+
+    def set_graphs(self, on=True):
+        self._check(self.lib.mbx_set_graphs(self.h, 1 if on else 0), "mbx_set_graphs")
+
+    def graph_launches(self):
+        return int(self.lib.mbx_graph_launches(self.h))
 
     def set_profiling(self, on=True):
         self._check(self.lib.mbx_set_profiling(self.h, 1 if on else 0), "mbx_set_profiling")

@@ -125,3 +125,47 @@ def beads_from(box, nbeads, sigma, seed):
         xyz[:3 * box.nw] += rng.normal(scale=sigma, size=(3 * box.nw, 3))
         out.append(WaterBox(box.nw, box.L, xyz, box.vel.copy(), (box.seed, b)))
     return out
+
+
+def config2(seed=20242):
+    """32 path-integral beads of the 256-water box, each with sigma 0.05 A noise."""
+    return beads_from(config0(), 32, 0.05, seed)
+
+
+def config3(seed=20243, nbox=64, sizes=(64, 128, 256, 512, 1024)):
+    """Uneven independent boxes: sizes drawn uniformly from ``sizes``, each box seeded
+    like the 256-water box at 0.997 g/cm^3 and 298 K."""
+    rng = np.random.default_rng(seed)
+    nws = rng.choice(np.asarray(sizes), size=nbox)
+    return [box_for(int(n), (seed, b)) for b, n in enumerate(nws)]
+
+
+class BoxSet:
+    """Several boxes packed in the multi-box layout: box b's 4*nw_b sites (waters then
+    M sites) follow the sites of boxes 0..b-1."""
+
+    def __init__(self, boxes):
+        self.boxes = list(boxes)
+        self.nw_box = np.array([b.nw for b in self.boxes], dtype=np.int32)
+        self.cells = np.ascontiguousarray(np.concatenate([b.cell for b in self.boxes]), dtype=np.float64)
+        self.imcon = 1
+        self.offsets = np.concatenate([[0], np.cumsum(4 * self.nw_box)]).astype(np.int64)
+        self.xyz = np.concatenate([b.xyz for b in self.boxes])
+        self.vel = np.concatenate([b.vel for b in self.boxes])
+        self.mass = np.concatenate([b.mass for b in self.boxes])
+
+    @property
+    def nbox(self):
+        return len(self.boxes)
+
+    @property
+    def natms(self):
+        return int(self.offsets[-1])
+
+    @property
+    def nw(self):
+        return int(self.nw_box.sum())
+
+    def split(self, a):
+        """Per-box views of a per-atom array."""
+        return [a[self.offsets[b]:self.offsets[b + 1]] for b in range(self.nbox)]

@@ -187,6 +187,47 @@ int mbx_server_wait(mbx_server* server, long id, double* fxx, double* fyy, doubl
                     double* scalars, double* times);
 const char* mbx_server_error(const mbx_server* server);
 
+/*
+ * Many independent water boxes (path-integral beads, separate simulations) in ONE
+ * evaluation: the 1-body term and the MB-pol 2B/3B terms with the heat current of every
+ * box, with one set of kernel launches over all boxes and per-box scalars.  Replaces the
+ * reference's bead parallelism, where MPI ranks are split into one group per bead
+ * (SOURCE/multibead.f90:25-80) and every group runs the force routines on its own
+ * replica (SOURCE/dlpoly_cmd.f:483-511); a single call over all beads has no
+ * counterpart there.
+ *   nbox, nw_box[nbox]      waters per box; box b occupies atoms [4*W_b, 4*W_b + 4*nw_b)
+ *                           with W_b = sum of nw_box[b'] for b' < b: 3*nw_b water atoms
+ *                           (O, H1, H2) then nw_b M sites (not read), natms = 4 * sum nw_box
+ *   imcon, cells[9*nbox]    boundary key for all boxes and each box's cell (host array)
+ *   xxx.. fxx.. vxx.. weight, atomic_energy   per-atom arrays of length natms; forces and
+ *                           energies ACCUMULATED; velocities+weight NULL for no heat current
+ *   scalars[nbox * MBX_NBOXSCALARS] (host, or NULL): per box the MB-pol block
+ *                           (MBX_S_*), then engang, virang, stress[9], jpot[3] of the
+ *                           1-body term (as mbx_ps_pes_forces)
+ * Dimer and trimer candidates are the waters of the same box (O(nw_b^2) tests per box,
+ * meant for boxes of up to a few thousand waters), with the reference's O-O criteria.
+ * The lists stay on the device: the step is enqueued without host synchronisation and,
+ * with graphs on (mbx_set_graphs, default on), captured once as a CUDA graph and
+ * replayed while the arrays, box layout, precision and limits are unchanged.  The call
+ * returns after the step and the per-box scalars are done.  Mixed precision follows
+ * mbx_set_mixed_limits.  mbx_last_timings: ms[0] the whole step, counts as usual.
+ *   mbx_mbpol_multi_device  all per-atom arrays on the device
+ *   mbx_mbpol_multi         host arrays, copied in and out inside the call
+ */
+#define MBX_NBOXSCALARS (MBX_NSCALARS + 14)
+int mbx_mbpol_multi_device(mbx_context* ctx, int precision, int imcon, int nbox, const int* nw_box,
+                           const double* cells, const double* xxx, const double* yyy, const double* zzz,
+                           double* fxx, double* fyy, double* fzz, const double* vxx, const double* vyy,
+                           const double* vzz, const double* weight, double* atomic_energy, double* scalars);
+int mbx_mbpol_multi(mbx_context* ctx, int precision, int imcon, int nbox, const int* nw_box, const double* cells,
+                    const double* xxx, const double* yyy, const double* zzz, double* fxx, double* fyy, double* fzz,
+                    const double* vxx, const double* vyy, const double* vzz, const double* weight,
+                    double* atomic_energy, double* scalars);
+/* Capture and replay the multi-box step as a CUDA graph (1, default) or launch it
+ * directly (0); mbx_graph_launches counts the graph replays of the context. */
+int mbx_set_graphs(mbx_context* ctx, int on);
+long mbx_graph_launches(const mbx_context* ctx);
+
 /* Dimer and trimer lists of the last evaluation (0-based water indices, i<j<k), as
  * index sets; the host arrays receive up to cap entries; counts are always written. */
 int mbx_last_lists(mbx_context* ctx, int* pairs, long cap_pairs, long* npairs, int* trimers, long cap_trimers,

@@ -53,6 +53,7 @@ def _with_context(torch, box, d, precision):
     try:
         f = torch.zeros((3, n), dtype=torch.float64, device="cuda")
         ae = torch.zeros(n, dtype=torch.float64, device="cuda")
+        torch.cuda.synchronize()   # the context works on its own stream
         sc = ctx.mbpol_forces_device(precision, box.imcon, box.cell, 3 * box.nw, d["lst"].data_ptr(), n,
                                      [t.data_ptr() for t in d["x"]], [f[k].data_ptr() for k in range(3)],
                                      [t.data_ptr() for t in d["v"]], d["m"].data_ptr(), ae.data_ptr())
