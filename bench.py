@@ -328,12 +328,111 @@ def run_ours(args, rank, world):
         "clocks": clk,
         "gpu_launches": int(launches),
     }
+    if not args.no_batched:
+        out["batched"] = batched()
     if args.serve_requests > 0:
         out["serving"] = serve(n_requests=args.serve_requests)
     if not args.no_cpu_baseline:
         sps, info = cpu_reference(box, target_core_s=40.0)
         out["cpu_baseline"] = {"value": sps, "unit": "steps/s", "cores": info["cores"], "kind": "port",
                                "sample": info["sample"]}
+    return out
+
+
+def batched(steps=10, warmup=3):
+    """Many boxes per evaluation through mbx_mbpol_multi_device (CUDA-graph replay):
+    32 path-integral beads of the 256-water box (0.05 A bead noise) and 64 uneven boxes
+    of 64..1024 waters.  Each step evaluates every box (1-body + 2B + 3B, per-box
+    energy, virial, stress and heat current); device-resident inputs, L2 flushed
+    between steps, CUDA events on the context's stream."""
+    import torch
+    from mbx import capi, systems
+    dev = torch.device("cuda", torch.cuda.current_device())
+    stream = torch.cuda.current_stream(dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    out = {}
+    for name, boxes in (("beads_32x256", systems.config2()), ("uneven_64_boxes", systems.config3())):
+        bs = systems.BoxSet(boxes)
+        n = bs.natms
+        f64 = dict(dtype=torch.float64, device=dev)
+        X = [torch.tensor(np.ascontiguousarray(bs.xyz[:, k]), **f64) for k in range(3)]
+        V = [torch.tensor(np.ascontiguousarray(bs.vel[:, k]), **f64) for k in range(3)]
+        M = torch.tensor(bs.mass, **f64)
+        F = torch.zeros((3, n), **f64)
+        AE = torch.zeros(n, **f64)
+        ctx = capi.Context(dev.index)
+        ctx.set_stream(stream.cuda_stream)
+        xp = [x.data_ptr() for x in X]
+        fp = [F[k].data_ptr() for k in range(3)]
+        vp = [v.data_ptr() for v in V]
+        res = {"boxes": bs.nbox, "waters": bs.nw}
+        forces = {}
+        for prec, key in ((capi.FP64, "fp64"), (capi.MIXED, "mixed")):
+            def step():
+                F.zero_()
+                AE.zero_()
+                return ctx.mbpol_multi_device(prec, bs, xp, fp, vp, M.data_ptr(), AE.data_ptr())
+
+            sc = step()
+            forces[key] = (F.cpu().numpy().copy(), sc.copy())
+            for _ in range(warmup):
+                step()
+            g0 = ctx.graph_launches()
+            ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+            torch.cuda.synchronize()
+            for k in range(steps):
+                flush.zero_()
+                ev[k][0].record(stream)
+                step()
+                ev[k][1].record(stream)
+            torch.cuda.synchronize()
+            t = sum(a.elapsed_time(b) for a, b in ev) / 1e3
+            _, cnt = ctx.last_timings()
+            res[key] = {"steps_per_s": steps / t, "boxes_per_s": steps * bs.nbox / t,
+                        "waters_per_s": steps * bs.nw / t, "ms_per_step": 1e3 * t / steps,
+                        "graph_replays": ctx.graph_launches() - g0, "kernels_per_step": int(cnt[2]),
+                        "dimers": int(cnt[0]), "trimers": int(cnt[1])}
+        f64_, sc64 = forces["fp64"]
+        fm, scm = forces["mixed"]
+        j64 = sc64[:, capi.S_JPOT:capi.S_JPOT + 6].reshape(-1, 2, 3).sum(1)
+        jm = scm[:, capi.S_JPOT:capi.S_JPOT + 6].reshape(-1, 2, 3).sum(1)
+        res["mixed_error_vs_fp64"] = {
+            "force_rms_rel": float(np.sqrt(np.mean((fm - f64_) ** 2) / np.mean(f64_ ** 2))),
+            "heat_current_rel_worst_box": float(np.max(np.linalg.norm(jm - j64, axis=1) /
+                                                       np.linalg.norm(j64, axis=1)))}
+        res["mixed_over_fp64"] = res["mixed"]["steps_per_s"] / res["fp64"]["steps_per_s"]
+        if name.startswith("beads"):
+            # the same boxes one at a time through the single-box device entry points
+            nw0 = boxes[0].nw
+            LST = torch.tensor(boxes[0].listttm2(), dtype=torch.int32, device=dev)
+            ANG = torch.tensor(boxes[0].listang().ravel(), dtype=torch.int32, device=dev)
+            offs = [int(o) * 8 for o in bs.offsets[:-1]]
+
+            def loop_step():
+                F.zero_()
+                AE.zero_()
+                for b, o in enumerate(offs):
+                    xb = [p + o for p in xp]
+                    fb = [p + o for p in fp]
+                    vb = [p + o for p in vp]
+                    ctx.ps_pes_device(1, bs.cells[9 * b:9 * b + 9], nw0, ANG.data_ptr(), 4 * nw0, xb, fb, vb,
+                                      AE.data_ptr() + o)
+                    ctx.mbpol_forces_device(capi.MIXED, 1, bs.cells[9 * b:9 * b + 9], 3 * nw0, LST.data_ptr(),
+                                            4 * nw0, xb, fb, vb, M.data_ptr() + o, AE.data_ptr() + o)
+
+            for _ in range(warmup):
+                loop_step()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(steps):
+                loop_step()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            t = e0.elapsed_time(e1) / 1e3
+            res["mixed_one_box_per_call"] = {"steps_per_s": steps / t, "ms_per_step": 1e3 * t / steps}
+        ctx.close()
+        out[name] = res
     return out
 
 
@@ -450,6 +549,7 @@ def main():
     ap.add_argument("--serve-requests", type=int, default=2000,
                     help="requests of the Poisson serving run reported under 'serving' (0: skip)")
     ap.add_argument("--ref-core-s", type=float, default=10.0)
+    ap.add_argument("--no-batched", action="store_true", help="skip the multi-box section ('batched')")
     ap.add_argument("--case", choices=["mixed", "fp64"], default=None,
                     help="profiling case: only warmup + K device-resident steps of one precision")
     args = ap.parse_args()
