@@ -36,6 +36,10 @@ struct mbx_context {
     // mixed-path defaults: the 2B term in FP64 (its FP32 gradient is a small difference of
     // large partials), the 3B term entirely in shifted FP32
     float limit2 = 0.0f, limit3 = 3.4e38f;
+    // 2B and 3B in one persistent launch (launch_23) where it applies; 0 = separate kernels
+    int fused = 1;
+    int nsm = 0;                    // SMs of the device (the persistent grid)
+    int* fuse_ctr = nullptr;        // device [2]: work counters of the persistent kernel
     long hard_last[2] = {0, 0};
     long npairs = 0, ntrip = 0;
     // batch-API staging
@@ -206,14 +210,24 @@ int run_mbpol(mbx_context* ctx, int precision, const Cell& cl, int nw, const int
         a.ae = ae_use;
         a.acc = ctx->acc;
         MixedPass mp{ctx->hard2, ctx->hard3, ctx->hard_count, ctx->limit2, ctx->limit3};
-        if (precision == MBX_MIXED) CK(cudaMemsetAsync(ctx->hard_count, 0, 2 * sizeof(int), s));
-        CK(launch_2b(a, ctx->pairs, (int)np, precision, mp, s));
-        if (ctx->profiling) CK(cudaEventRecord(ctx->ev[2], s));
-        CK(launch_3b(a, ctx->trip, (int)nt, precision, mp, s));
-        if (ctx->profiling) CK(cudaEventRecord(ctx->ev[3], s));
-        const int p2 = (precision == MBX_MIXED && ctx->limit2 > 0.f) ? 2 : 1;
-        const int p3 = (precision == MBX_MIXED && ctx->limit3 > 0.f && ctx->limit3 < 3.0e38f) ? 2 : 1;
-        ctx->launches += p2 * (np > 0) + p3 * (nt > 0);
+        if (ctx->fused && fused_applies(precision, mp)) {
+            CK(launch_23(a, ctx->pairs, (int)np, nullptr, ctx->trip, (int)nt, nullptr, precision, ctx->fuse_ctr,
+                         ctx->nsm, s));
+            if (ctx->profiling) {
+                CK(cudaEventRecord(ctx->ev[2], s));
+                CK(cudaEventRecord(ctx->ev[3], s));
+            }
+            ctx->launches += 1;
+        } else {
+            if (precision == MBX_MIXED) CK(cudaMemsetAsync(ctx->hard_count, 0, 2 * sizeof(int), s));
+            CK(launch_2b(a, ctx->pairs, (int)np, precision, mp, s));
+            if (ctx->profiling) CK(cudaEventRecord(ctx->ev[2], s));
+            CK(launch_3b(a, ctx->trip, (int)nt, precision, mp, s));
+            if (ctx->profiling) CK(cudaEventRecord(ctx->ev[3], s));
+            const int p2 = (precision == MBX_MIXED && ctx->limit2 > 0.f) ? 2 : 1;
+            const int p3 = (precision == MBX_MIXED && ctx->limit3 > 0.f && ctx->limit3 < 3.0e38f) ? 2 : 1;
+            ctx->launches += p2 * (np > 0) + p3 * (nt > 0);
+        }
     } else if (ctx->profiling) {
         for (int q = 1; q < 4; ++q) CK(cudaEventRecord(ctx->ev[q], s));
     }
@@ -254,8 +268,8 @@ int run_multi(mbx_context* ctx, int precision, int nbox, const int* nw_box, cons
             cudaError_t e;
             if ((e = cudaMemcpyAsync(m.cells, ctx->cells_h, nbox * sizeof(Cell), cudaMemcpyHostToDevice, s)))
                 return e;
-            if ((e = m.enqueue(precision, lim, x, y, z, fx, fy, fz, heat ? vx : nullptr, heat ? vy : nullptr,
-                               heat ? vz : nullptr, heat ? mass : nullptr, ae, s)))
+            if ((e = m.enqueue(precision, lim, ctx->fused != 0, x, y, z, fx, fy, fz, heat ? vx : nullptr,
+                               heat ? vy : nullptr, heat ? vz : nullptr, heat ? mass : nullptr, ae, s)))
                 return e;
             if ((e = cudaMemcpyAsync(ctx->mout_h, m.acc_box, (size_t)nbox * S_NSLOTS * sizeof(double),
                                      cudaMemcpyDeviceToHost, s)))
@@ -272,7 +286,7 @@ int run_multi(mbx_context* ctx, int precision, int nbox, const int* nw_box, cons
                                ctx->mint_h};
         bool launched = false;
         if (ctx->use_graphs) {
-            const bool same = ctx->mexec && m.gen == ctx->mkey_gen && precision == ctx->mkey_prec &&
+            const bool same = ctx->mexec && m.gen == ctx->mkey_gen && precision + 2 * ctx->fused == ctx->mkey_prec &&
                               ctx->mkey_lim[0] == ctx->limit2 && ctx->mkey_lim[1] == ctx->limit3 &&
                               ctx->mkey_stream == s && std::memcmp(key, ctx->mkey, sizeof key) == 0;
             if (!same) {
@@ -286,7 +300,7 @@ int run_multi(mbx_context* ctx, int precision, int nbox, const int* nw_box, cons
                         cudaGraphInstantiate(&ctx->mexec, g, 0) == cudaSuccess) {
                         std::memcpy(ctx->mkey, key, sizeof key);
                         ctx->mkey_gen = m.gen;
-                        ctx->mkey_prec = precision;
+                        ctx->mkey_prec = precision + 2 * ctx->fused;
                         ctx->mkey_lim[0] = ctx->limit2;
                         ctx->mkey_lim[1] = ctx->limit3;
                         ctx->mkey_stream = s;
@@ -404,6 +418,8 @@ extern "C" int mbx_create(mbx_context** out, int device) {
         CK(cudaMalloc(&ctx->acc, MBX_NSCALARS * sizeof(double)));
         CK(cudaMalloc(&ctx->totals, 4 * sizeof(int)));
         CK(cudaMalloc(&ctx->hard_count, 2 * sizeof(int)));
+        CK(cudaMalloc(&ctx->fuse_ctr, 2 * sizeof(int)));
+        CK(cudaDeviceGetAttribute(&ctx->nsm, cudaDevAttrMultiProcessorCount, device));
         CK(cudaMallocHost(&ctx->totals_h, 8 * sizeof(int)));
         CK(cudaMallocHost(&ctx->acc_h, MBX_NSCALARS * sizeof(double)));
         return MBX_OK;
@@ -423,7 +439,7 @@ extern "C" void mbx_destroy(mbx_context* ctx) {
     cudaSetDevice(ctx->device);
     if (ctx->own_stream) cudaStreamSynchronize(ctx->own_stream);
     void* dev[] = {ctx->mono, ctx->list, ctx->atoms, ctx->ae_scratch, ctx->acc, ctx->totals, ctx->pairs, ctx->trip,
-                   ctx->batch, ctx->hard2, ctx->hard3, ctx->hard_count};
+                   ctx->batch, ctx->hard2, ctx->hard3, ctx->hard_count, ctx->fuse_ctr};
     for (void* p : dev)
         if (p) cudaFree(p);
     if (ctx->totals_h) cudaFreeHost(ctx->totals_h);
@@ -557,6 +573,12 @@ extern "C" int mbx_mbpol_forces(mbx_context* ctx, int precision, int imcon, cons
     *virsrp += sc[MBX_S_VIR];
     for (int q = 0; q < 9; ++q) stress[q] += sc[MBX_S_STRESS + q];
     if (scalars) std::memcpy(scalars, sc, sizeof sc);
+    return MBX_OK;
+}
+
+extern "C" int mbx_set_fused(mbx_context* ctx, int on) {
+    if (!ctx) return MBX_ERR_ARG;
+    ctx->fused = on ? 1 : 0;
     return MBX_OK;
 }
 

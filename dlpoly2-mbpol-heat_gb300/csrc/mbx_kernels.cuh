@@ -57,6 +57,13 @@ cudaError_t launch_2b_dev(const MbpolArgs& a, const int2* pairs, long cap, const
                           const MixedPass& mp, cudaStream_t s);
 cudaError_t launch_3b_dev(const MbpolArgs& a, const int4* trip, long cap, const int* n_dev, int precision,
                           const MixedPass& mp, cudaStream_t s);
+// Both bodies of the mixed method in one persistent launch of `nsm` blocks (one per
+// SM): the dimers and trimers are claimed in chunks through ctr[2] (device ints, zeroed
+// here).  Counts are n2/n3, or read from n2_dev/n3_dev when those are not null.
+// Applies to the default mixed split only (fused_applies); otherwise launch_2b/3b.
+bool fused_applies(int precision, const MixedPass& mp);
+cudaError_t launch_23(const MbpolArgs& a, const int2* pairs, int n2, const int* n2_dev, const int4* trip, int n3,
+                      const int* n3_dev, int precision, int* ctr, int nsm, cudaStream_t s);
 // Isolated polynomial + model evaluation for explicit clusters (the per-call ABI).
 cudaError_t launch_2b_direct(int n, const double* w1, const double* w2, double* E, double* g1, double* g2,
                              int precision, cudaStream_t s);
@@ -155,7 +162,10 @@ struct MultiBoxes {
     void release();
     // (re)allocate for this box layout; a no-op when the layout is unchanged
     cudaError_t setup(int nbox, const int* nw_box, bool need_hard, cudaStream_t s);
-    cudaError_t enqueue(int precision, const MixedPass& limits, const double* x, const double* y, const double* z,
+    int* ctr = nullptr;            // work counters of the persistent 2B+3B kernel
+    int nsm = 0;
+    cudaError_t enqueue(int precision, const MixedPass& limits, bool fused, const double* x, const double* y,
+                        const double* z,
                         double* fx, double* fy, double* fz, const double* vx, const double* vy, const double* vz,
                         const double* mass, double* ae, cudaStream_t s);
 };

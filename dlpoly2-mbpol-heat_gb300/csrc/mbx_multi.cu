@@ -190,11 +190,11 @@ MultiBoxes::~MultiBoxes() { release(); }
 void MultiBoxes::release() {
     void* ptrs[] = {list,  listang, wbox,  abox,     is_water, cells,   bstart,     bcount, mono,   n2,
                     l2,    off2,    n3,    l3,       tcnt,     toff,    pairs,      trip,   hard2,  hard3,
-                    hard_count, scan_tmp, acc_box, pes_box, ae_scratch, totals, flag};
+                    hard_count, scan_tmp, acc_box, pes_box, ae_scratch, totals, flag, ctr};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     list = listang = wbox = abox = bstart = bcount = n2 = l2 = off2 = n3 = l3 = tcnt = toff = nullptr;
-    hard_count = totals = flag = nullptr;
+    hard_count = totals = flag = ctr = nullptr;
     is_water = nullptr;
     cells = nullptr;
     mono = acc_box = pes_box = ae_scratch = nullptr;
@@ -283,6 +283,10 @@ cudaError_t MultiBoxes::setup(int nbox_, const int* nw_box, bool need_hard, cuda
     if ((e = cudaMalloc(&ae_scratch, ((size_t)natms + 1) * sizeof(double)))) return e;
     if ((e = cudaMalloc(&totals, 4 * sizeof(int)))) return e;
     if ((e = cudaMalloc(&flag, 4 * sizeof(int)))) return e;
+    if ((e = cudaMalloc(&ctr, 2 * sizeof(int)))) return e;
+    int dev = 0;
+    if ((e = cudaGetDevice(&dev))) return e;
+    if ((e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev))) return e;
     // pageable sources: each copy has read them before it returns
     if ((e = cudaMemcpyAsync(list, hl.data(), hl.size() * sizeof(int), cudaMemcpyHostToDevice, s))) return e;
     if ((e = cudaMemcpyAsync(listang, ha.data(), ha.size() * sizeof(int), cudaMemcpyHostToDevice, s))) return e;
@@ -295,8 +299,8 @@ cudaError_t MultiBoxes::setup(int nbox_, const int* nw_box, bool need_hard, cuda
 }
 
 // The whole multi-box step, asynchronous on `s` (no host synchronisation, no allocation).
-cudaError_t MultiBoxes::enqueue(int precision, const MixedPass& limits, const double* x, const double* y,
-                                const double* z, double* fx, double* fy, double* fz, const double* vx,
+cudaError_t MultiBoxes::enqueue(int precision, const MixedPass& limits, bool fused, const double* x,
+                                const double* y, const double* z, double* fx, double* fy, double* fz, const double* vx,
                                 const double* vy, const double* vz, const double* mass, double* ae,
                                 cudaStream_t s) {
     cudaError_t e;
@@ -361,10 +365,15 @@ cudaError_t MultiBoxes::enqueue(int precision, const MixedPass& limits, const do
         mp.limit2 = 0.f;
         mp.limit3 = 3.4e38f;
     }
-    if ((e = launch_2b_dev(args, pairs, pair_cap, totals + 0, precision, mp, s))) return e;
-    if ((e = launch_3b_dev(args, trip, trip_cap, totals + 1, precision, mp, s))) return e;
-    launches += (precision == 1 && mp.limit2 > 0.f) ? 2 : 1;
-    launches += (precision == 1 && mp.limit3 > 0.f && mp.limit3 < 3.0e38f) ? 2 : 1;
+    if (fused && fused_applies(precision, mp)) {
+        if ((e = launch_23(args, pairs, 0, totals + 0, trip, 0, totals + 1, precision, ctr, nsm, s))) return e;
+        launches += 1;
+    } else {
+        if ((e = launch_2b_dev(args, pairs, pair_cap, totals + 0, precision, mp, s))) return e;
+        if ((e = launch_3b_dev(args, trip, trip_cap, totals + 1, precision, mp, s))) return e;
+        launches += (precision == 1 && mp.limit2 > 0.f) ? 2 : 1;
+        launches += (precision == 1 && mp.limit3 > 0.f && mp.limit3 < 3.0e38f) ? 2 : 1;
+    }
     if (heat && mass) {
         k_multi_jkin<<<blocks_for(natms), kThreads, 0, s>>>(natms, abox, is_water, vx, vy, vz, mass, ae_use,
                                                             acc_box, flag);

@@ -39,7 +39,8 @@ constexpr size_t oMono = 0;
 constexpr size_t oAcc = align256(oMono + 9 * sizeof(double) * kN);
 constexpr size_t oTotals = align256(oAcc + MBX_NSCALARS * sizeof(double));
 constexpr size_t oFlag = align256(oTotals + 4 * sizeof(int));
-constexpr size_t oN2 = align256(oFlag + 4 * sizeof(int));
+constexpr size_t oCtr = align256(oFlag + 4 * sizeof(int));
+constexpr size_t oN2 = align256(oCtr + 4 * sizeof(int));
 constexpr size_t oOff2 = align256(oN2 + kN * sizeof(int));
 constexpr size_t oN3 = align256(oOff2 + kN * sizeof(int));
 constexpr size_t oTcnt = align256(oN3 + kN * sizeof(int));
@@ -198,10 +199,17 @@ extern "C" int mbx_mbpol_forces_noalloc(int precision, int imcon, const double* 
         a.fx = fxx; a.fy = fyy; a.fz = fzz;
         a.ae = atomic_energy;
         a.acc = acc;
-        // default mixed split: 2B in FP64, 3B in FP32 (no hand-off lists needed)
+        // default mixed split (2B in FP64, 3B in FP32, no hand-off lists): one persistent
+        // launch, its work counters in the scratch (zeroed by launch_23); FP64: two kernels
         MixedPass mp{nullptr, nullptr, nullptr, 0.0f, 3.4e38f};
-        NA_CK(launch_2b(a, pairs, np, precision, mp, s));
-        NA_CK(launch_3b(a, trip, nt, precision, mp, s));
+        if (fused_applies(precision, mp)) {
+            int nsm = 0;
+            NA_CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+            NA_CK(launch_23(a, pairs, np, nullptr, trip, nt, nullptr, precision, (int*)(base + oCtr), nsm, s));
+        } else {
+            NA_CK(launch_2b(a, pairs, np, precision, mp, s));
+            NA_CK(launch_3b(a, trip, nt, precision, mp, s));
+        }
     }
     if (heat && weight) NA_CK(launch_jkin(3 * nw, vxx, vyy, vzz, weight, atomic_energy, acc, s));
     double h[MBX_NSCALARS];

@@ -43,6 +43,23 @@ def _run(cmd):
     return r.stdout
 
 
+def _stale(target, deps, cmd):
+    """Rebuild when a dependency is newer or the command line changed."""
+    rec = target + ".cmd"
+    line = " ".join(cmd)
+    if _newer(target, deps) or not os.path.exists(rec):
+        return True
+    with open(rec) as f:
+        return f.read() != line
+
+
+def _compile(cmd, target):
+    out = _run(cmd)
+    with open(target + ".cmd", "w") as f:
+        f.write(" ".join(cmd))
+    return out
+
+
 def _check_stamp():
     """Objects from another machine (x86 here, aarch64 on the GPU hosts) are discarded."""
     import platform
@@ -55,6 +72,21 @@ def _check_stamp():
     os.makedirs(BUILD, exist_ok=True)
     with open(stamp, "w") as f:
         f.write(me)
+
+
+# Register budget of the generated polynomial functions.  The fused mixed-precision
+# kernel (12 warps per SM: 4 on FP64 dimers, 8 on FP32 trimers) runs at 168 registers,
+# so every function it calls -- the FP64 2B and the FP32 chunks -- is compiled within
+# that budget.  The FP64 3B chunks serve only the separate FP64 3B kernel and keep the
+# full register file.
+FUSED_MAXRREG = 168
+
+
+def _poly_reg_flags(ptx_path):
+    name = os.path.basename(ptx_path)
+    if "poly3b_f64" in name or "coef" in name:
+        return []
+    return ["-maxrregcount=%d" % FUSED_MAXRREG]
 
 
 def build_lib(verbose=False, jobs=None):
@@ -72,8 +104,9 @@ def build_lib(verbose=False, jobs=None):
     jobs_list = []
     for p in ptx:
         o = p[:-4] + ".o"
-        if _newer(o, [p]):
-            jobs_list.append((o, [nvcc] + common + ["-c", p, "-o", o]))
+        cmd = [nvcc] + common + _poly_reg_flags(p) + ["-c", p, "-o", o]
+        if _stale(o, [p], cmd):
+            jobs_list.append((o, cmd))
     hdr_deps = [os.path.join(CSRC, h) for h in HEADERS] + [os.path.join(gen_dir, "mbx_poly_gen.cuh"),
                                                           os.path.join(gen_dir, "mbx_pes_gen.cuh"),
                                                           os.path.join(REPO, "include", "mbx.h")]
@@ -82,12 +115,13 @@ def build_lib(verbose=False, jobs=None):
         s = os.path.join(CSRC, src)
         o = os.path.join(BUILD, src.replace(".cu", ".o"))
         cu_objs.append(o)
-        if _newer(o, [s] + hdr_deps):
-            jobs_list.append((o, [nvcc] + common + ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr",
-                                                    "-I", CSRC, "-I", gen_dir, "-c", s, "-o", o]))
+        cmd = [nvcc] + common + ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr", "-I", CSRC, "-I",
+                                 gen_dir, "-c", s, "-o", o]
+        if _stale(o, [s] + hdr_deps, cmd):
+            jobs_list.append((o, cmd))
     jobs = jobs or max(2, os.cpu_count() or 2)
     with ThreadPoolExecutor(max_workers=jobs) as ex:
-        outs = list(ex.map(lambda j: _run(j[1]), jobs_list))
+        outs = list(ex.map(lambda j: _compile(j[1], j[0]), jobs_list))
     if verbose:
         for o in outs:
             if o.strip():

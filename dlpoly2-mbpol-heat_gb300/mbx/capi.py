@@ -81,6 +81,7 @@ def load(path=None):
     L.mbx_mbpol_multi.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, _I, _D] + [_D] * 12
     L.mbx_mbpol_multi_device.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, _I, _D] + [C.c_void_p] * 11 + [_D]
     L.mbx_set_graphs.argtypes = [C.c_void_p, C.c_int]
+    L.mbx_set_fused.argtypes = [C.c_void_p, C.c_int]
     L.mbx_graph_launches.argtypes = [C.c_void_p]
     L.mbx_graph_launches.restype = C.c_long
     L.mbx_last_lists.argtypes = [C.c_void_p, _I, C.c_long, _L, _I, C.c_long, _L]
@@ -236,6 +237,9 @@ class Context:
                                              *xyz_ptrs, *f_ptrs, *v_ptrs, mass_ptr, ae_ptr, _p(sc))
         self._check(rc, "mbx_mbpol_multi_device")
         return sc
+
+    def set_fused(self, on=True):
+        self._check(self.lib.mbx_set_fused(self.h, 1 if on else 0), "mbx_set_fused")
 
     def set_graphs(self, on=True):
         self._check(self.lib.mbx_set_graphs(self.h, 1 if on else 0), "mbx_set_graphs")

@@ -51,8 +51,9 @@ int mbx_set_stream(mbx_context* ctx, void* stream);
 
 /* Time each phase of later evaluations with CUDA events on the context's stream. */
 int mbx_set_profiling(mbx_context* ctx, int on);
-/* Phase times of the last evaluation in ms: [0] lists, [1] 2B kernels, [2] 3B kernels,
- * [3] heat-current jkin (or -1 when profiling is off); counts[5]: [0] dimers, [1] trimers,
+/* Phase times of the last evaluation in ms: [0] lists, [1] 2B kernels (the fused 2B+3B
+ * kernel when it runs), [2] 3B kernels (0 when fused), [3] heat-current jkin (or -1 when
+ * profiling is off); counts[5]: [0] dimers, [1] trimers,
  * [2] kernel launches issued, [3]/[4] dimers/trimers the mixed path handed to FP64.
  * Either pointer may be NULL. */
 int mbx_last_timings(mbx_context* ctx, double* ms, long* counts);
@@ -63,6 +64,14 @@ int mbx_last_timings(mbx_context* ctx, double* ms, long* counts);
  * limit >= 3.4e38 keeps every cluster in FP32.  Defaults: 0 (2B in FP64) and
  * 3.4e38 (3B in FP32). */
 int mbx_set_mixed_limits(mbx_context* ctx, double limit2b, double limit3b);
+
+/* Mixed method: evaluate the 2B and 3B terms in one persistent launch (1, default) or
+ * in separate kernels (0).  Fused, each SM runs FP64 dimer warps and FP32 trimer warps
+ * side by side, so the two bodies overlap on their own pipes.  It applies to the
+ * default mixed split; hand-off limits and MBX_FP64 use the separate kernels.  The two
+ * forms agree to FP32 rounding (the compiler may contract the FP32 model code
+ * differently in the two kernels). */
+int mbx_set_fused(mbx_context* ctx, int on);
 
 /*
  * MB-pol 2B + 3B forces with the heat-current bookkeeping.

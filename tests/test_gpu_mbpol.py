@@ -239,3 +239,24 @@ def test_msites_dms_match_oracle(mbx_ctx, oracle_lib, name):
     assert np.max(np.abs(gx[3 * nw:] - rx[3 * nw:])) <= 1e-12 * max(box.L, 1.0)
     assert rel_err(gq, rq) <= TOL64
     assert rel_err(gdp, rdp) <= TOL64
+
+
+@pytest.mark.parametrize("precision", [capi.FP64, capi.MIXED])
+def test_fused_kernel_matches_separate_kernels(precision):
+    """The persistent 2B+3B kernel and the two separate kernels run the same
+    per-cluster arithmetic.  FP64 (unfused operations) agrees to the order of the FP64
+    sums; the FP32 model code is compiled into two different kernels, where the compiler
+    may contract different FP32 multiply-adds, so mixed results agree to FP32 rounding."""
+    tol = 1e-11 if precision == capi.FP64 else 1e-6
+    box = systems.config0()
+    ctx = capi.Context(0)
+    try:
+        fused = ctx.mbpol_forces(box, precision=precision)
+        ctx.set_fused(False)
+        sep = ctx.mbpol_forces(box, precision=precision)
+    finally:
+        ctx.close()
+    for k in ("eng2", "eng3", "vir"):
+        assert abs(fused[k] - sep[k]) <= tol * abs(sep[k]), k
+    for k in ("forces", "atomic_energy", "stress", "jpot", "jkin"):
+        assert rel_err(fused[k], sep[k]) <= tol, k

@@ -198,3 +198,22 @@ def test_multi_rejects_bad_arguments():
             ctx.mbpol_multi(bs, precision=7)
     finally:
         ctx.close()
+
+
+@pytest.mark.parametrize("precision", [capi.FP64, capi.MIXED])
+def test_multi_fused_matches_separate_kernels(precision):
+    # FP64: summation order only; mixed: FP32 rounding (the FP32 model code is compiled
+    # into two kernels, whose multiply-add contraction may differ)
+    tol = TOL_SAME if precision == capi.FP64 else 1e-6
+    bs = systems.BoxSet(systems.config3(seed=9, nbox=6))
+    ctx = capi.Context(0)
+    try:
+        a = ctx.mbpol_multi(bs, precision=precision)
+        ctx.set_fused(False)
+        b = ctx.mbpol_multi(bs, precision=precision)
+    finally:
+        ctx.close()
+    assert rel_err(a["forces"], b["forces"]) <= tol
+    assert rel_err(a["atomic_energy"], b["atomic_energy"]) <= tol
+    for k in range(bs.nbox):
+        assert rel_err(a["scalars"][k], b["scalars"][k]) <= tol
