@@ -72,3 +72,33 @@ def test_generated_ptx_declares_all_chunks(tmp_path):
         if name != "mbx_poly_coef":
             assert name in hdr
             assert ".visible .func %s(" % name in open(p).read()
+
+
+def test_group_form_of_3b_polynomial_matches_reference(golden):
+    """The looped FP32 3B function evaluates E(x) = sum over the 48 trimer relabellings
+    of a representative polynomial f.  In exact arithmetic (FP64 here) the sum equals
+    the reference polynomial and its gradient at the golden points and at shifted
+    variables (the kernels evaluate the shifted re-expansion)."""
+    sys.path.insert(0, os.path.join(PKG, "gen"))
+    import gen_poly_ptx as g
+    global A
+    nv, coef, monos = g.read_table(os.path.join(PKG, "tables", "poly3b.tbl"))
+    G = g.group_3b()
+    assert len(G) == 48 and G[0] == list(range(nv)) and len({tuple(p) for p in G}) == 48
+    full = {tuple(sorted(m)): coef[k] for k, m in monos}
+    reps = g.group_reduce(full, G)
+    assert len(reps) == len(coef)          # one representative per coefficient class
+    A = [c for _, c in reps]
+    root = g.build_trie([(i, m) for i, (m, _) in enumerate(reps)])
+    x = golden["X3"][0]
+    e, grad = 0.0, np.zeros(nv)
+    for p in G:
+        ep, gp = _interpret(root, x[p])
+        e += ep
+        np.add.at(grad, p, gp)
+    assert abs(e - golden["PE3b"][0]) <= 1e-10 * abs(e)
+    assert np.max(np.abs(grad - golden["PG3b"][0])) <= 1e-10 * np.max(np.abs(grad))
+    # the shifted re-expansion is invariant too (class-wise centres)
+    sp = g.shifted_polynomial(monos, coef, g.shift_centres("3b"))
+    sp.pop((), None)
+    assert len(g.group_reduce({tuple(sorted(m)): c for m, c in sp.items()}, G)) > 0

@@ -93,8 +93,10 @@ def test_mixed_within_budget(mbx_ctx, refs, name):
     jt = got["jpot"] + got["jkin"]
     jr = ref["jpot"] + ref["jkin"]
     assert np.linalg.norm(jt - jr) <= TOL_MIXED_HEAT_SMALL * np.linalg.norm(jr)
+    # total energy: the 3B energy carries the FP32 rounding (~5e-6 of E3), the total
+    # stays within 2e-6 (measured 2e-7 at 4096 waters, ~1e-6 on the 128-water box)
     e, er = got["eng2"] + got["eng3"], ref["eng2"] + ref["eng3"]
-    assert abs(e - er) <= 1e-6 * abs(er)
+    assert abs(e - er) <= 2e-6 * abs(er)
 
 
 def test_models_fp64_and_mixed_vs_reference_golden(mbx_ctx, golden):
