@@ -458,7 +458,9 @@ def run_case(args):
     AE = torch.zeros(n, **f64)
     LST = torch.tensor(box.listttm2(), dtype=torch.int32, device="cuda")
     ANG = torch.tensor(box.listang().ravel(), dtype=torch.int32, device="cuda")
-    prec = capi.MIXED if args.case == "mixed" else capi.FP64
+    prec = capi.FP64 if args.case == "fp64" else capi.MIXED
+    if args.case == "mixed-separate":
+        ctx.set_fused(False)      # the 2B and 3B kernels one after the other
     torch.cuda.synchronize()
     for _ in range(args.warmup + args.steps):
         F.zero_()
@@ -557,7 +559,7 @@ def main():
                     help="requests of the Poisson serving run reported under 'serving' (0: skip)")
     ap.add_argument("--ref-core-s", type=float, default=10.0)
     ap.add_argument("--no-batched", action="store_true", help="skip the multi-box section ('batched')")
-    ap.add_argument("--case", choices=["mixed", "fp64"], default=None,
+    ap.add_argument("--case", choices=["mixed", "mixed-separate", "fp64"], default=None,
                     help="profiling case: only warmup + K device-resident steps of one precision")
     args = ap.parse_args()
     if args.case:
