@@ -1,6 +1,6 @@
 // 1-body Partridge-Schwenke water PES (the MB-pol monomer term) with the angfrc
 // bookkeeping: ps_type_couple (SOURCE/ps_type_couple.f90:15-274) called from angfrc
-// for keya = 9 (SOURCE/angfrc.f:150-212, :344-545).  One warp per H-O-H angle, FP64.
+// for keya = 9 (SOURCE/angfrc.f:150-212, :344-545).  Eight lanes per H-O-H angle, FP64.
 #include "mbx_kernels.cuh"
 #include "mbx_pes_gen.cuh"
 
@@ -11,13 +11,28 @@ namespace {
 __device__ __forceinline__ double c5z(int j) { return __longlong_as_double((long long)pes::kC5z[j]); }
 __device__ __forceinline__ double cmass(int j) { return __longlong_as_double((long long)pes::kCmass[j]); }
 
-// ps_type_couple, one warp per angle: lanes share the 244 expansion terms and the
-// partial sums are reduced with shuffles; lane 0 adds the mass-correction terms and the
-// exponential prefactor.  Outputs (valid on lane 0): potential, the forces on the two
-// H atoms (fa = f[0..2], fc = f[3..5]) and the virial term.
-__device__ void ps_couple_warp(int lane, double roh1, double xoh1, double yoh1, double zoh1, double roh2,
-                               double xoh2, double yoh2, double zoh2, double theta, double& pterm_out, double* f,
-                               double& vterm_out) {
+// Lanes per angle: a group of kGroup lanes shares one angle's expansion terms.  The
+// FP64 pipe of this part takes one warp instruction per 64 cycles however many lanes are
+// active, so work that one lane does for an angle (the geometry, the exponential
+// prefactor) is best done for several angles at once: four angles per warp.
+constexpr int kGroup = 8;
+
+__device__ __forceinline__ double group_sum(double v) {
+#pragma unroll
+    for (int o = kGroup / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// ps_type_couple for one angle on the kGroup lanes of a group (sub-lane s): the lanes
+// share the 244 expansion terms and the 9 mass-correction terms, partial sums are
+// reduced within the group.  Outputs (valid on every lane of the group): potential,
+// the forces on the two H atoms (fa = f[0..2], fc = f[3..5]) and the virial term.
+// Per term the derivative factors (i-1) x^(i-2) / reoh come from per-angle tables, and
+// the virial term is assembled from the radial sums (vterm = roh1 * ra + roh2 * rc term
+// by term, the same sum the reference accumulates separately).
+__device__ void ps_couple_group(int s, double roh1, double xoh1, double yoh1, double zoh1, double roh2,
+                                double xoh2, double yoh2, double zoh2, double theta, double& pterm_out, double* f,
+                                double& vterm_out) {
     const double reoh = pes::kReoh, ireoh = 1.0 / pes::kReoh;
     const double cose = __longlong_as_double((long long)pes::kCose);
     const double cost = cos(theta);
@@ -25,82 +40,64 @@ __device__ void ps_couple_warp(int lane, double roh1, double xoh1, double yoh1, 
     const double x2 = (roh2 - reoh) / reoh;
     const double x3 = cost - cose;
     const double ir1 = 1.0 / roh1, ir2 = 1.0 / roh2;
-    double fm[16][3];
+    // fm[j][k] = x_k^(j-1); dm[j][k] = (j-1) x_k^(j-2) (/ reoh for the bond variables)
+    double fm[16][3], dm[16][3];
     fm[0][0] = fm[0][1] = fm[0][2] = 0.0;
     fm[1][0] = fm[1][1] = fm[1][2] = 1.0;
+    dm[0][0] = dm[0][1] = dm[0][2] = 0.0;
+    dm[1][0] = dm[1][1] = dm[1][2] = 0.0;
 #pragma unroll
     for (int j = 2; j <= 15; ++j) {
         fm[j][0] = fm[j - 1][0] * x1;
         fm[j][1] = fm[j - 1][1] * x2;
         fm[j][2] = fm[j - 1][2] * x3;
+        dm[j][0] = (j - 1) * fm[j - 1][0] * ireoh;
+        dm[j][1] = (j - 1) * fm[j - 1][1] * ireoh;
+        dm[j][2] = (j - 1) * fm[j - 1][2];
     }
-    // per term: potential; the x-y-z components of the H forces factor into a radial
-    // part (along the unit bond vector) and an angular part (along e1 / e2)
-    double pterm = 0.0, vterm = 0.0, ra = 0.0, aa = 0.0, rc = 0.0, ac = 0.0;
-    for (int j = 1 + lane; j < pes::kTerms; j += 32) {
+    double pterm = 0.0, ra = 0.0, aa = 0.0, rc = 0.0;
+    for (int j = 1 + s; j < pes::kTerms; j += kGroup) {
         const int i1 = pes::kIdx[j][0], i2 = pes::kIdx[j][1], i3 = pes::kIdx[j][2];
         const double c = c5z(j);
+        const double cz = c * fm[i3][2];
         const double dum = fm[i1][0] * fm[i2][1] + fm[i2][0] * fm[i1][1];
-        pterm += c * dum * fm[i3][2];
-        const double a1 = (i1 - 1) * fm[i1 - 1][0] * ireoh;
-        const double a2 = (i2 - 1) * fm[i2 - 1][0] * ireoh;
-        const double a3 = (i3 - 1) * fm[i3 - 1][2];
-        ra += c * (a1 * fm[i2][1] + a2 * fm[i1][1]) * fm[i3][2];
-        aa += c * dum * a3;
-        const double b1 = (i2 - 1) * fm[i2 - 1][1] * ireoh;
-        const double b2 = (i1 - 1) * fm[i1 - 1][1] * ireoh;
-        rc += c * (fm[i1][0] * b1 + fm[i2][0] * b2) * fm[i3][2];
-        vterm += c * (roh1 * fm[i2][1] * (i1 - 1) * fm[i1 - 1][0] + roh2 * fm[i1][0] * (i2 - 1) * fm[i2 - 1][1] +
-                      roh1 * fm[i1][1] * (i2 - 1) * fm[i2 - 1][0] + roh2 * fm[i2][0] * (i1 - 1) * fm[i1 - 1][1]) *
-                 ireoh * fm[i3][2];
+        pterm += cz * dum;
+        ra += cz * (dm[i1][0] * fm[i2][1] + dm[i2][0] * fm[i1][1]);
+        aa += c * dum * dm[i3][2];
+        rc += cz * (fm[i1][0] * dm[i2][1] + fm[i2][0] * dm[i1][1]);
     }
-    pterm = warp_sum(pterm);
-    vterm = warp_sum(vterm);
-    ra = warp_sum(ra);
-    aa = warp_sum(aa);
-    rc = warp_sum(rc);
-    if (lane != 0) return;
+    // mass-correction terms, one per lane (lane 0 also takes the ninth)
+    const double xm = __longlong_as_double((long long)pes::kXm);
+    const double e1x = xoh2 - cost * xoh1, e1y = yoh2 - cost * yoh1, e1z = zoh2 - cost * zoh1;
+    const double e2x = xoh1 - cost * xoh2, e2y = yoh1 - cost * yoh2, e2z = zoh1 - cost * zoh2;
+    double v12 = 0.0, pa = 0.0, q3 = 0.0, qa = 0.0, q4 = 0.0;
+    for (int j = s; j < pes::kMass; j += kGroup) {
+        const int m1 = pes::kIdxm[j][0], m2 = pes::kIdxm[j][1], m3 = pes::kIdxm[j][2];
+        const double c = cmass(j);
+        v12 += c * (fm[m1][0] * fm[m2][1] + fm[m2][0] * fm[m1][1]) * fm[m3][2];
+        pa += c * xm * (dm[m1][0] * fm[m2][1] + dm[m2][0] * fm[m1][1]) * fm[m3][2];
+        q3 += c * xm * (fm[m1][0] * fm[m2][1] + fm[m2][0] * fm[m1][1]) * dm[m3][2] * ir1;
+        qa += c * xm * (fm[m1][0] * dm[m2][1] + fm[m2][0] * dm[m1][1]) * fm[m3][2];
+        q4 += c * xm * (fm[m1][0] * fm[m2][1] + fm[m2][0] * fm[m1][1]) * dm[m3][2] * ir2;
+    }
+    pterm = group_sum(pterm);
+    ra = group_sum(ra);
+    aa = group_sum(aa);
+    rc = group_sum(rc);
+    v12 = group_sum(v12);
+    pa = group_sum(pa);
+    q3 = group_sum(q3);
+    qa = group_sum(qa);
+    q4 = group_sum(q4);
     double fa[3], fc[3];
-    {
-        const double e1x = xoh2 - cost * xoh1, e1y = yoh2 - cost * yoh1, e1z = zoh2 - cost * zoh1;
-        const double e2x = xoh1 - cost * xoh2, e2y = yoh1 - cost * yoh2, e2z = zoh1 - cost * zoh2;
-        fa[0] = -(ra * xoh1 + aa * ir1 * e1x);
-        fa[1] = -(ra * yoh1 + aa * ir1 * e1y);
-        fa[2] = -(ra * zoh1 + aa * ir1 * e1z);
-        fc[0] = -(rc * xoh2 + aa * ir2 * e2x);
-        fc[1] = -(rc * yoh2 + aa * ir2 * e2y);
-        fc[2] = -(rc * zoh2 + aa * ir2 * e2z);
-        // mass-correction terms
-        const double xm = __longlong_as_double((long long)pes::kXm);
-        double v1 = 0.0, v2 = 0.0;
-        for (int j = 0; j < pes::kMass; ++j) {
-            const int m1 = pes::kIdxm[j][0], m2 = pes::kIdxm[j][1], m3 = pes::kIdxm[j][2];
-            const double c = cmass(j);
-            v1 += c * fm[m1][0] * fm[m2][1] * fm[m3][2];
-            v2 += c * fm[m2][0] * fm[m1][1] * fm[m3][2];
-            const double d1 = (m1 - 1) * fm[m1 - 1][0] * ireoh;
-            const double d2 = (m2 - 1) * fm[m2 - 1][0] * ireoh;
-            const double d3 = (m3 - 1) * fm[m3 - 1][2] * ir1;
-            const double pa = xm * (d1 * fm[m2][1] + d2 * fm[m1][1]) * fm[m3][2];
-            const double q3 = xm * (fm[m1][0] * fm[m2][1] + fm[m2][0] * fm[m1][1]) * d3;
-            fa[0] -= c * (pa * xoh1 + q3 * e1x);
-            fa[1] -= c * (pa * yoh1 + q3 * e1y);
-            fa[2] -= c * (pa * zoh1 + q3 * e1z);
-            const double h1 = (m2 - 1) * fm[m2 - 1][1] * ireoh;
-            const double h2 = (m1 - 1) * fm[m1 - 1][1] * ireoh;
-            const double h3 = (m3 - 1) * fm[m3 - 1][2] * ir2;
-            const double qa = xm * (fm[m1][0] * h1 + fm[m2][0] * h2) * fm[m3][2];
-            const double q4 = xm * (fm[m1][0] * fm[m2][1] + fm[m2][0] * fm[m1][1]) * h3;
-            fc[0] -= c * (qa * xoh2 + q4 * e2x);
-            fc[1] -= c * (qa * yoh2 + q4 * e2y);
-            fc[2] -= c * (qa * zoh2 + q4 * e2z);
-            vterm += c *
-                     (xm * roh1 * fm[m2][1] * (m1 - 1) * fm[m1 - 1][0] + xm * roh2 * fm[m1][0] * (m2 - 1) * fm[m2 - 1][1] +
-                      xm * roh1 * fm[m1][1] * (m2 - 1) * fm[m2 - 1][0] + xm * roh2 * fm[m2][0] * (m1 - 1) * fm[m1 - 1][1]) *
-                     ireoh * fm[m3][2];
-        }
-        pterm = pterm + xm * v1 + xm * v2;
-    }
+    fa[0] = -(ra * xoh1 + aa * ir1 * e1x) - (pa * xoh1 + q3 * e1x);
+    fa[1] = -(ra * yoh1 + aa * ir1 * e1y) - (pa * yoh1 + q3 * e1y);
+    fa[2] = -(ra * zoh1 + aa * ir1 * e1z) - (pa * zoh1 + q3 * e1z);
+    fc[0] = -(rc * xoh2 + aa * ir2 * e2x) - (qa * xoh2 + q4 * e2x);
+    fc[1] = -(rc * yoh2 + aa * ir2 * e2y) - (qa * yoh2 + q4 * e2y);
+    fc[2] = -(rc * zoh2 + aa * ir2 * e2z) - (qa * zoh2 + q4 * e2z);
+    double vterm = roh1 * ra + roh2 * rc + roh1 * pa + roh2 * qa;
+    pterm = pterm + xm * v12;
     const double b1 = pes::kB1;
     const double efac = exp(-b1 * ((roh1 - reoh) * (roh1 - reoh) + (roh2 - reoh) * (roh2 - reoh)));
     const double term = pterm;
@@ -118,7 +115,7 @@ __device__ void ps_couple_warp(int lane, double roh1, double xoh1, double yoh1, 
     vterm_out = vterm;
 }
 
-// One warp per angle; lane 0 of each warp accumulates.
+// Four angles per warp (kGroup lanes each); the first lane of each group accumulates.
 __global__ void __launch_bounds__(kThreads) k_ps_pes(int nang, const int* __restrict__ listang, Cell cl,
                                                       const double* __restrict__ x, const double* __restrict__ y,
                                                       const double* __restrict__ z, double* fx, double* fy,
@@ -128,19 +125,23 @@ __global__ void __launch_bounds__(kThreads) k_ps_pes(int nang, const int* __rest
                                                       const int* __restrict__ abox, double* acc_box,
                                                       const int* __restrict__ skip) {
     if (skip && *skip) return;   // block-uniform
-    const int t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
-    // red = {E, virial, stress[9], jpot[3]} (lane 0 of each warp)
+    const int sub = lane % kGroup;
+    const int t = (blockIdx.x * blockDim.x + threadIdx.x) / kGroup;
+    const bool lead = sub == 0 && t < nang;
+    // red = {E, virial, stress[9], jpot[3]} (the leading lane of each group)
     double red[14];
 #pragma unroll
     for (int q = 0; q < 14; ++q) red[q] = 0.0;
-    if (t < nang) {   // warp-uniform
-        const int ia = listang[3 * t] - 1, ib = listang[3 * t + 1] - 1, ic = listang[3 * t + 2] - 1;
+    const int warp_first = (blockIdx.x * blockDim.x + (threadIdx.x & ~31)) / kGroup;
+    if (warp_first < nang) {   // warp-uniform: every lane takes part in the group sums
+        const int ta = min(t, nang - 1);   // groups past the end repeat the last angle, unused
+        const int ia = listang[3 * ta] - 1, ib = listang[3 * ta + 1] - 1, ic = listang[3 * ta + 2] - 1;
         double xab = x[ia] - x[ib], yab = y[ia] - y[ib], zab = z[ia] - z[ib];
         double xbc = x[ic] - x[ib], ybc = y[ic] - y[ib], zbc = z[ic] - z[ib];
         if (cells) {
-            image(cells[abox[t]], xab, yab, zab);
-            image(cells[abox[t]], xbc, ybc, zbc);
+            image(cells[abox[ta]], xab, yab, zab);
+            image(cells[abox[ta]], xbc, ybc, zbc);
         } else {
             image(cl, xab, yab, zab);
             image(cl, xbc, ybc, zbc);
@@ -152,8 +153,8 @@ __global__ void __launch_bounds__(kThreads) k_ps_pes(int nang, const int* __rest
         xbc *= rrbc; ybc *= rrbc; zbc *= rrbc;
         const double cost = xab * xbc + yab * ybc + zab * zbc;
         double pterm = 0, vterm = 0, f[6];
-        ps_couple_warp(lane, rab, xab, yab, zab, rbc, xbc, ybc, zbc, acos(cost), pterm, f, vterm);
-        if (lane == 0) {
+        ps_couple_group(sub, rab, xab, yab, zab, rbc, xbc, ybc, zbc, acos(cost), pterm, f, vterm);
+        if (lead) {
             red[0] = pterm;
             red[1] = vterm;
             const double s1 = rab * xab * f[0] + rbc * xbc * f[3], s2 = rab * xab * f[1] + rbc * xbc * f[4];
@@ -192,8 +193,8 @@ __global__ void __launch_bounds__(kThreads) k_ps_pes(int nang, const int* __rest
         span[1] = -1;
     }
     __syncthreads();
-    const int box = t < nang ? abox[t] : -1;
-    if (lane == 0 && box >= 0) {
+    const int box = lead ? abox[t] : -1;
+    if (box >= 0) {
         atomicMin(&span[0], box);
         atomicMax(&span[1], box);
     }
@@ -202,7 +203,7 @@ __global__ void __launch_bounds__(kThreads) k_ps_pes(int nang, const int* __rest
     if (hi < 0) return;   // block-uniform
     if (lo == hi) {
         block_sum_atomic<14>(red, acc_box + 14 * (size_t)hi);
-    } else if (lane == 0 && box >= 0) {
+    } else if (box >= 0) {
 #pragma unroll
         for (int q = 0; q < 14; ++q)
             if (red[q] != 0.0) atomicAdd(acc_box + 14 * (size_t)box + q, red[q]);
@@ -299,7 +300,7 @@ cudaError_t launch_ps_pes(int nang, const int* listang, const Cell& cl, const do
                           const double* z, double* fx, double* fy, double* fz, double* ae, const double* vx,
                           const double* vy, const double* vz, double* acc14, cudaStream_t s) {
     if (nang <= 0) return cudaSuccess;
-    const int blocks = (int)(((long)nang * 32 + kThreads - 1) / kThreads);   // one warp per angle
+    const int blocks = (int)(((long)nang * kGroup + kThreads - 1) / kThreads);   // kGroup lanes per angle
     k_ps_pes<<<blocks, kThreads, 0, s>>>(nang, listang, cl, x, y, z, fx, fy, fz, ae, vx, vy, vz, acc14, nullptr,
                                          nullptr, nullptr, nullptr);
     return cudaGetLastError();
@@ -310,7 +311,7 @@ cudaError_t launch_ps_pes_boxes(int nang, const int* listang, const Cell* cells,
                                 const double* vx, const double* vy, const double* vz, double* acc14_box,
                                 const int* skip, cudaStream_t s) {
     if (nang <= 0) return cudaSuccess;
-    const int blocks = (int)(((long)nang * 32 + kThreads - 1) / kThreads);
+    const int blocks = (int)(((long)nang * kGroup + kThreads - 1) / kThreads);
     k_ps_pes<<<blocks, kThreads, 0, s>>>(nang, listang, Cell{}, x, y, z, fx, fy, fz, ae, vx, vy, vz, nullptr, cells,
                                          abox, acc14_box, skip);
     return cudaGetLastError();
