@@ -92,4 +92,16 @@ __device__ __forceinline__ void block_sum_atomic(double (&v)[NV], double* out) {
     }
 }
 
+// Pair k (0 <= k < n(n-1)/2) of the pairs (p, q), p < q < n, in lexicographic order.
+__device__ __forceinline__ void pair_of_index(int n, int k, int& p, int& q) {
+    const double b = 2.0 * n - 1.0;
+    int pp = (int)((b - sqrt(b * b - 8.0 * k)) * 0.5);
+    auto off = [n](int r) { return r * (2 * n - r - 1) / 2; };
+    if (pp < 0) pp = 0;
+    while (pp > 0 && off(pp) > k) --pp;
+    while (off(pp + 1) <= k) ++pp;
+    p = pp;
+    q = k - off(pp) + pp + 1;
+}
+
 }  // namespace mbx

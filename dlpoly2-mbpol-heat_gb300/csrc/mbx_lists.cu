@@ -172,7 +172,8 @@ __global__ void k_pairs_compact(int nw, int cap2, const int* __restrict__ n2, co
 // A trimer is kept by the reference iff some water is within the 3B cutoff of the
 // other two (istoobig1..3 in SOURCE/mbpol.f90:858-862); it is generated here by the
 // smallest such centre only, so every trimer appears exactly once.  Lanes test the
-// pairs (p < q) of the neighbour list in parallel; hits are appended in pair order.
+// pairs (p < q) of the neighbour list in parallel, 32 pairs per step in lexicographic
+// order (the FP64 distance tests keep every lane busy); hits are appended in pair order.
 template <bool FILL>
 __global__ void k_trimers(int nw, const double* __restrict__ mono, Cell cl, int cap3, const int* __restrict__ n3,
                           const int* __restrict__ l3, int* __restrict__ cnt, const int* __restrict__ off,
@@ -182,30 +183,30 @@ __global__ void k_trimers(int nw, const double* __restrict__ mono, Cell cl, int 
     if (c >= nw) return;   // warp-uniform
     const int n = min(n3[c], cap3);
     const int* nb = l3 + (size_t)c * cap3;
+    const int npair = n * (n - 1) / 2;
     int m = 0;
     const int base = FILL ? off[c] : 0;
-    for (int p = 0; p < n; ++p) {
-        const int a = nb[p];
-        const double* oa = mono + 9 * (size_t)a;
-        for (int q0 = p + 1; q0 < n; q0 += 32) {
-            const int q = q0 + lane;
-            bool keep = false;
-            int b = 0;
-            if (q < n) {
-                b = nb[q];
-                const bool ab = tri_edge(dist2_img(cl, oa, mono + 9 * (size_t)b));
-                keep = !(ab && (a < c || b < c));
-            }
-            const unsigned bal = __ballot_sync(0xffffffffu, keep);
-            if (FILL && keep) {
-                int i = c, j = a, k = b;  // sort the three indices
-                if (i > j) { int t = i; i = j; j = t; }
-                if (j > k) { int t = j; j = k; k = t; }
-                if (i > j) { int t = i; i = j; j = t; }
-                trip[base + m + __popc(bal & ((1u << lane) - 1u))] = make_int4(i, j, k, 0);
-            }
-            m += __popc(bal);
+    for (int k0 = 0; k0 < npair; k0 += 32) {
+        const int k = k0 + lane;
+        bool keep = false;
+        int a = 0, b = 0;
+        if (k < npair) {
+            int p, q;
+            pair_of_index(n, k, p, q);
+            a = nb[p];
+            b = nb[q];
+            const bool ab = tri_edge(dist2_img(cl, mono + 9 * (size_t)a, mono + 9 * (size_t)b));
+            keep = !(ab && (a < c || b < c));
         }
+        const unsigned bal = __ballot_sync(0xffffffffu, keep);
+        if (FILL && keep) {
+            int i = c, j = a, kk = b;  // sort the three indices
+            if (i > j) { int t = i; i = j; j = t; }
+            if (j > kk) { int t = j; j = kk; kk = t; }
+            if (i > j) { int t = i; i = j; j = t; }
+            trip[base + m + __popc(bal & ((1u << lane) - 1u))] = make_int4(i, j, kk, 0);
+        }
+        m += __popc(bal);
     }
     if (!FILL && lane == 0) cnt[c] = m;
 }

@@ -100,32 +100,32 @@ __global__ void k_multi_trimers(int nw, const double* __restrict__ mono, const i
     const Cell& cl = cells[wbox[c]];
     const int n = n3[c];
     const int* nb = l3 + (size_t)c * cap3;
+    const int npair = n * (n - 1) / 2;
     int m = 0;
     const long base = FILL ? off[c] : 0;
-    for (int p = 0; p < n; ++p) {
-        const int a = nb[p];
-        const double* oa = mono + 9 * (size_t)a;
-        for (int q0 = p + 1; q0 < n; q0 += 32) {
-            const int q = q0 + lane;
-            bool keep = false;
-            int b = 0;
-            if (q < n) {
-                b = nb[q];
-                const bool ab = tri_edge(dist2_img(cl, oa, mono + 9 * (size_t)b));
-                keep = !(ab && (a < c || b < c));
-            }
-            const unsigned bal = __ballot_sync(0xffffffffu, keep);
-            if (FILL && keep) {
-                int i = c, j = a, k = b;
-                if (i > j) { int t = i; i = j; j = t; }
-                if (j > k) { int t = j; j = k; k = t; }
-                if (i > j) { int t = i; i = j; j = t; }
-                const long slot = base + m + __popc(bal & ((1u << lane) - 1u));
-                if (slot < cap) trip[slot] = make_int4(i, j, k, 0);
-                else atomicOr(overflow, 2);
-            }
-            m += __popc(bal);
+    for (int k0 = 0; k0 < npair; k0 += 32) {
+        const int k = k0 + lane;
+        bool keep = false;
+        int a = 0, b = 0;
+        if (k < npair) {
+            int p, q;
+            pair_of_index(n, k, p, q);
+            a = nb[p];
+            b = nb[q];
+            const bool ab = tri_edge(dist2_img(cl, mono + 9 * (size_t)a, mono + 9 * (size_t)b));
+            keep = !(ab && (a < c || b < c));
         }
+        const unsigned bal = __ballot_sync(0xffffffffu, keep);
+        if (FILL && keep) {
+            int i = c, j = a, kk = b;
+            if (i > j) { int t = i; i = j; j = t; }
+            if (j > kk) { int t = j; j = kk; kk = t; }
+            if (i > j) { int t = i; i = j; j = t; }
+            const long slot = base + m + __popc(bal & ((1u << lane) - 1u));
+            if (slot < cap) trip[slot] = make_int4(i, j, kk, 0);
+            else atomicOr(overflow, 2);
+        }
+        m += __popc(bal);
     }
     if (!FILL && lane == 0) cnt[c] = m;
 }
