@@ -140,6 +140,16 @@ def cpu_reference(box, target_core_s=20.0, threads=None):
                           "step_seconds": step_s}
 
 
+def max_over_ranks(value, world, device):
+    """The slowest rank's time (replicas: every rank evaluates its own box)."""
+    if world <= 1:
+        return value
+    import torch
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
 def run_ours(args, rank, world):
     import torch
     from mbx import capi, systems
@@ -193,14 +203,10 @@ def run_ours(args, rank, world):
             if profile:
                 ms, cnt = ctx.last_timings()
                 phase += ms
-            launches += ctx.last_timings()[1][2] + 3   # + the 1-body kernel and the two zero_ fills
+            launches += ctx.last_timings()[1][2] + 1   # libmbx kernels of the step + the 1-body kernel
         torch.cuda.synchronize()
         tot = sum(a.elapsed_time(b) for a, b in ev) / 1e3
-        if world > 1:
-            t = torch.tensor([tot], device=dev)
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            tot = float(t.item())
-        return tot, phase / steps, launches
+        return max_over_ranks(tot, world, dev), phase / steps, launches
 
     # numerics of the mixed path against the FP64 path on this machine
     sc64 = step(capi.FP64)
@@ -278,10 +284,7 @@ def run_ours(args, rank, world):
         torch.cuda.synchronize()
         e2e_step()
     t_e2e = time.perf_counter() - t0
-    if world > 1:
-        t = torch.tensor([t_e2e], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        t_e2e = float(t.item())
+    t_e2e = max_over_ranks(t_e2e, world, dev)
     # two host calls per step (1-body, then 2B/3B); each copies its inputs in and results out
     h2d = (6 * n * 8 + 3 * box.nw * 4) + (7 * n * 8 + 3 * box.nw * 4)
     d2h = (4 * n * 8 + 14 * 8) + (4 * n * 8 + capi.NSCALARS * 8)
