@@ -40,6 +40,8 @@ struct mbx_context {
     int fused = 1;
     int nsm = 0;                    // SMs of the device (the persistent grid)
     int* fuse_ctr = nullptr;        // device [2]: work counters of the persistent kernel
+    double* part2 = nullptr;        // split FP64 dimers: per-chunk partial sums (pairs_cap dimers)
+    int* done2 = nullptr;
     long hard_last[2] = {0, 0};
     long npairs = 0, ntrip = 0;
     // batch-API staging
@@ -175,11 +177,17 @@ int run_mbpol(mbx_context* ctx, int precision, const Cell& cl, int nw, const int
         if (np > ctx->pairs_cap) {
             if (ctx->pairs) cudaFree(ctx->pairs);
             if (ctx->hard2) cudaFree(ctx->hard2);
+            if (ctx->part2) cudaFree(ctx->part2);
+            if (ctx->done2) cudaFree(ctx->done2);
             ctx->pairs = nullptr;
             ctx->hard2 = nullptr;
+            ctx->part2 = nullptr;
+            ctx->done2 = nullptr;
             const long cap = np + np / 4 + 64;
             CK(cudaMalloc(&ctx->pairs, cap * sizeof(int2)));
             CK(cudaMalloc(&ctx->hard2, cap * sizeof(int2)));
+            CK(cudaMalloc(&ctx->part2, cap * dimer_parts() * 32 * sizeof(double)));
+            CK(cudaMalloc(&ctx->done2, cap * sizeof(int)));
             ctx->pairs_cap = cap;
         }
         if (nt > ctx->trip_cap) {
@@ -212,7 +220,7 @@ int run_mbpol(mbx_context* ctx, int precision, const Cell& cl, int nw, const int
         MixedPass mp{ctx->hard2, ctx->hard3, ctx->hard_count, ctx->limit2, ctx->limit3};
         if (ctx->fused && fused_applies(precision, mp)) {
             CK(launch_23(a, ctx->pairs, (int)np, nullptr, ctx->trip, (int)nt, nullptr, precision, ctx->fuse_ctr,
-                         ctx->nsm, s));
+                         ctx->nsm, s, ctx->part2, ctx->done2, ctx->pairs_cap));
             if (ctx->profiling) {
                 CK(cudaEventRecord(ctx->ev[2], s));
                 CK(cudaEventRecord(ctx->ev[3], s));
@@ -439,7 +447,7 @@ extern "C" void mbx_destroy(mbx_context* ctx) {
     cudaSetDevice(ctx->device);
     if (ctx->own_stream) cudaStreamSynchronize(ctx->own_stream);
     void* dev[] = {ctx->mono, ctx->list, ctx->atoms, ctx->ae_scratch, ctx->acc, ctx->totals, ctx->pairs, ctx->trip,
-                   ctx->batch, ctx->hard2, ctx->hard3, ctx->hard_count, ctx->fuse_ctr};
+                   ctx->batch, ctx->hard2, ctx->hard3, ctx->hard_count, ctx->fuse_ctr, ctx->part2, ctx->done2};
     for (void* p : dev)
         if (p) cudaFree(p);
     if (ctx->totals_h) cudaFreeHost(ctx->totals_h);

@@ -61,9 +61,15 @@ cudaError_t launch_3b_dev(const MbpolArgs& a, const int4* trip, long cap, const 
 // SM): the dimers and trimers are claimed in chunks through ctr[2] (device ints, zeroed
 // here).  Counts are n2/n3, or read from n2_dev/n3_dev when those are not null.
 // Applies to the default mixed split only (fused_applies); otherwise launch_2b/3b.
+// With `partial` (dimer_parts() * 32 doubles per dimer) and `done` (one int per dimer),
+// both for part_cap dimers (done is zeroed here), every FP64 dimer is split into
+// dimer_parts() tasks, one polynomial chunk each, so the FP64 work is claimed in finer
+// pieces; with more dimers than part_cap, or null buffers, one task per dimer.
 bool fused_applies(int precision, const MixedPass& mp);
+int dimer_parts();
 cudaError_t launch_23(const MbpolArgs& a, const int2* pairs, int n2, const int* n2_dev, const int4* trip, int n3,
-                      const int* n3_dev, int precision, int* ctr, int nsm, cudaStream_t s);
+                      const int* n3_dev, int precision, int* ctr, int nsm, cudaStream_t s,
+                      double* partial = nullptr, int* done = nullptr, long part_cap = 0);
 // Isolated polynomial + model evaluation for explicit clusters (the per-call ABI).
 cudaError_t launch_2b_direct(int n, const double* w1, const double* w2, double* E, double* g1, double* g2,
                              int precision, cudaStream_t s);
@@ -163,6 +169,9 @@ struct MultiBoxes {
     // (re)allocate for this box layout; a no-op when the layout is unchanged
     cudaError_t setup(int nbox, const int* nw_box, bool need_hard, cudaStream_t s);
     int* ctr = nullptr;            // work counters of the persistent 2B+3B kernel
+    double* partial = nullptr;     // split FP64 dimers: per-chunk [E, dE/dx] (launch_23)
+    int* done = nullptr;
+    long part_cap = 0;
     int nsm = 0;
     cudaError_t enqueue(int precision, const MixedPass& limits, bool fused, const double* x, const double* y,
                         const double* z,

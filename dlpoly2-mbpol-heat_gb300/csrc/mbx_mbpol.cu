@@ -117,13 +117,27 @@ __device__ __forceinline__ T f_switch(T r, T ri, T rf, T& g) {
     return T(1);
 }
 
+// One FP64 dimer evaluated as kPoly2BF64Parts tasks, one polynomial chunk each: every
+// task computes the variables and its chunk, publishes the chunk's [E, dE/dx] (32
+// doubles) in partial[(t * parts + p) * 32], and the task that completes the count in
+// done[t] sums the chunks in chunk order -- the same sums as one thread calling the
+// chunks in turn -- and finishes the dimer.
+struct Part2B {
+    int t, p;
+    double* partial;
+    int* done;
+};
+
 // x2b_v6x_p::operator() on coordinates already in the working frame.
 // Returns E (kcal/mol); g1/g2 assigned.  For T = float the polynomial is evaluated
 // in the shifted variables x - kShift2B; if any of them lies further than `limit`
 // from its centre the cluster is left to the FP64 pass (*hard = true, nothing set).
+// With `part` (T = double) only that polynomial chunk is evaluated here; unless this
+// task completes the dimer, *deferred is set and nothing else is.
 template <typename T>
 __device__ __forceinline__ T model_2b(const T* w1, const T* w2, T* g1, T* g2, float limit = 0.f,
-                                      bool* hard = nullptr) {
+                                      bool* hard = nullptr, const Part2B* part = nullptr,
+                                      bool* deferred = nullptr) {
     const T dOO[3] = {w1[0] - w2[0], w1[1] - w2[1], w1[2] - w2[2]};
     const T rOO = t_sqrt(dOO[0] * dOO[0] + dOO[1] * dOO[1] + dOO[2] * dOO[2]);
     if (rOO > T(kR2f)) {
@@ -171,7 +185,30 @@ __device__ __forceinline__ T model_2b(const T* w1, const T* w2, T* g1, T* g2, fl
     T acc[32];
 #pragma unroll
     for (int q = 0; q < 32; ++q) acc[q] = T(0);
-    poly2b<T>(v, acc);
+    if constexpr (sizeof(T) == 8) {
+        if (part) {
+            poly2b_f64_part(part->p, v, acc);
+            double* slot = part->partial + (size_t)part->t * (kPoly2BF64Parts * 32);
+#pragma unroll
+            for (int q = 0; q < 32; ++q) __stcg(slot + part->p * 32 + q, acc[q]);
+            __threadfence();
+            if (atomicAdd(part->done + part->t, 1) != kPoly2BF64Parts - 1) {
+                *deferred = true;
+                return T(0);
+            }
+            __threadfence();
+#pragma unroll
+            for (int q = 0; q < 32; ++q) acc[q] = T(0);
+            for (int pp = 0; pp < kPoly2BF64Parts; ++pp) {
+#pragma unroll
+                for (int q = 0; q < 32; ++q) acc[q] = acc[q] + __ldcg(slot + pp * 32 + q);
+            }
+        } else {
+            poly2b<T>(v, acc);
+        }
+    } else {
+        poly2b<T>(v, acc);
+    }
     const T E_poly = acc[0];
     T xgrd[30];
 #pragma unroll
@@ -447,7 +484,8 @@ struct HardList {
 // One dimer: image, model, then forces/energy/virial/stress/heat into red (or the
 // hand-off list when the FP32 variables stray beyond the limit).
 template <typename T>
-__device__ __forceinline__ void eval_dimer(const MbpolArgs& a, int2 p, double* red, int eidx, const HardList& hl) {
+__device__ __forceinline__ void eval_dimer(const MbpolArgs& a, int2 p, double* red, int eidx, const HardList& hl,
+                                           const Part2B* part = nullptr) {
     const int i = p.x, j = p.y;
     const Cell& cl = a.cells ? a.cells[a.wbox[i]] : a.cell;
     double w1[9], w2[9];
@@ -475,8 +513,9 @@ __device__ __forceinline__ void eval_dimer(const MbpolArgs& a, int2 p, double* r
         p1[q] = (T)w[q];
         p2[q] = (T)w[9 + q];
     }
-    bool hard = false;
-    const T e = model_2b<T>(p1, p2, g1, g2, hl.limit, hl.items ? &hard : nullptr);
+    bool hard = false, deferred = false;
+    const T e = model_2b<T>(p1, p2, g1, g2, hl.limit, hl.items ? &hard : nullptr, part, &deferred);
+    if (deferred) return;
     if (hard) {
         ((int2*)hl.items)[atomicAdd(hl.count, 1)] = p;
         return;
@@ -594,12 +633,15 @@ __global__ void __launch_bounds__(kThreads) k_mbpol_3b(MbpolArgs a, const int4* 
 
 // Both bodies of the mixed method in one persistent launch: one 384-thread block per
 // SM (12 warps at <= 168 registers).  Warps 0-3 (one per SM sub-partition) take FP64
-// dimers first and keep the FP64 pipe busy; warps 4-11 take FP32 trimers, whose
-// straight-line polynomial code is limited by instruction fetch and gains from the
-// extra warps; a warp whose queue runs dry moves to the other one.  The two bodies so
-// overlap on their own pipes instead of following each other (measured on the 4096-
-// water box: 4.9 ms fused against 7.1 ms for the two kernels in sequence; 4+4 warps
-// at 255 registers gave 5.2 ms).  Work is claimed 32 clusters at a time from ctr[0]
+// dimers first and keep the FP64 pipe busy; warps 4-11 take FP32 trimers; a warp whose
+// queue runs dry moves to the other one.  The two bodies so overlap on their own pipes
+// instead of following each other.  The FP64 pipe takes one warp instruction per 64
+// cycles whatever the number of active lanes, so a 32-dimer chunk is the unit of FP64
+// work (~1 ms); with a partial buffer each dimer chunk is split into one task per FP64
+// polynomial chunk, all part-0 tasks first, which halves the unit and the last round's
+// tail while the dimer warps of an SM still walk the same code.  Measured on the
+// 4096-water box: 4.67 ms (two kernels in sequence: 6.7 ms; unsplit dimers 4.85 ms;
+// 4+4 warps at 255 registers 5.2 ms).  Work is claimed 32 tasks at a time from ctr[0]
 // (dimers) and ctr[1] (trimers), which start at zero.
 constexpr int kFusedThreads = 384;
 constexpr int kFusedDimerWarps = 4;
@@ -607,9 +649,15 @@ constexpr int kFusedDimerWarps = 4;
 template <typename T2, typename T3>
 __global__ void __launch_bounds__(kFusedThreads, 1)
     k_mbpol_23(MbpolArgs a, const int2* __restrict__ pairs, int n2, const int* __restrict__ n2_dev,
-               const int4* __restrict__ trip, int n3, const int* __restrict__ n3_dev, int* ctr) {
+               const int4* __restrict__ trip, int n3, const int* __restrict__ n3_dev, int* ctr,
+               double* partial, int* done, long part_cap) {
     if (n2_dev) n2 = *n2_dev;
     if (n3_dev) n3 = *n3_dev;
+    // dimer tasks: 32-dimer chunks, each split into `parts` polynomial chunks (chunk c,
+    // part p at task block c * parts + p) when the partial buffer holds every dimer
+    if (n2 > part_cap) partial = nullptr;
+    const int parts = partial ? kPoly2BF64Parts : 1;
+    const int ntask2 = ((n2 + 31) / 32) * 32 * parts;
     const int lane = threadIdx.x & 31;
     int role = (threadIdx.x >> 5) < kFusedDimerWarps ? 0 : 1;
     bool switched = false;
@@ -621,7 +669,7 @@ __global__ void __launch_bounds__(kFusedThreads, 1)
         int base = 0;
         if (lane == 0) base = atomicAdd(ctr + role, 32);
         base = __shfl_sync(0xffffffffu, base, 0);
-        if (base >= (role ? n3 : n2)) {
+        if (base >= (role ? n3 : ntask2)) {
             if (switched) break;
             switched = true;
             role ^= 1;
@@ -630,10 +678,20 @@ __global__ void __launch_bounds__(kFusedThreads, 1)
         const int t = base + lane;
         int box = -1;
         if (role == 0) {
-            if (t < n2) {
-                const int2 p = pairs[t];
+            const int blk = base >> 5;
+            const int nchunk = (n2 + 31) / 32;
+            // all chunks of polynomial part 0 first, then part 1, ...: the dimer warps of an
+            // SM walk the same part's code at the same time
+            const int td = (blk % nchunk) * 32 + lane;
+            if (td < n2) {
+                const int2 p = pairs[td];
                 if (a.cells) box = a.wbox[p.x];
-                eval_dimer<T2>(a, p, red, 14, none);
+                if (partial) {
+                    const Part2B part{td, blk / nchunk, partial, done};
+                    eval_dimer<T2>(a, p, red, 14, none, &part);
+                } else {
+                    eval_dimer<T2>(a, p, red, 14, none);
+                }
             }
         } else if (t < n3) {
             const int4 c = trip[t];
@@ -796,12 +854,18 @@ bool fused_applies(int precision, const MixedPass& mp) {
     return precision != 0 && !(mp.limit2 > 0.f) && !(mp.limit3 < 3.0e38f);
 }
 
+int dimer_parts() { return kPoly2BF64Parts; }
+
 cudaError_t launch_23(const MbpolArgs& a, const int2* pairs, int n2, const int* n2_dev, const int4* trip, int n3,
-                      const int* n3_dev, int precision, int* ctr, int nsm, cudaStream_t s) {
+                      const int* n3_dev, int precision, int* ctr, int nsm, cudaStream_t s, double* partial,
+                      int* done, long part_cap) {
     cudaError_t e = cudaMemsetAsync(ctr, 0, 2 * sizeof(int), s);
     if (e) return e;
     if (precision == 0) return cudaErrorInvalidValue;   // see fused_applies
-    k_mbpol_23<double, float><<<nsm, kFusedThreads, 0, s>>>(a, pairs, n2, n2_dev, trip, n3, n3_dev, ctr);
+    if (!partial || !done) part_cap = 0;
+    if (part_cap > 0 && (e = cudaMemsetAsync(done, 0, (size_t)part_cap * sizeof(int), s))) return e;
+    k_mbpol_23<double, float><<<nsm, kFusedThreads, 0, s>>>(a, pairs, n2, n2_dev, trip, n3, n3_dev, ctr, partial,
+                                                             done, part_cap);
     return cudaGetLastError();
 }
 

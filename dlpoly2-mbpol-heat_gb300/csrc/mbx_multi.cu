@@ -190,11 +190,13 @@ MultiBoxes::~MultiBoxes() { release(); }
 void MultiBoxes::release() {
     void* ptrs[] = {list,  listang, wbox,  abox,     is_water, cells,   bstart,     bcount, mono,   n2,
                     l2,    off2,    n3,    l3,       tcnt,     toff,    pairs,      trip,   hard2,  hard3,
-                    hard_count, scan_tmp, acc_box, pes_box, ae_scratch, totals, flag, ctr};
+                    hard_count, scan_tmp, acc_box, pes_box, ae_scratch, totals, flag, ctr, partial, done};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     list = listang = wbox = abox = bstart = bcount = n2 = l2 = off2 = n3 = l3 = tcnt = toff = nullptr;
-    hard_count = totals = flag = ctr = nullptr;
+    hard_count = totals = flag = ctr = done = nullptr;
+    partial = nullptr;
+    part_cap = 0;
     is_water = nullptr;
     cells = nullptr;
     mono = acc_box = pes_box = ae_scratch = nullptr;
@@ -284,6 +286,11 @@ cudaError_t MultiBoxes::setup(int nbox_, const int* nw_box, bool need_hard, cuda
     if ((e = cudaMalloc(&totals, 4 * sizeof(int)))) return e;
     if ((e = cudaMalloc(&flag, 4 * sizeof(int)))) return e;
     if ((e = cudaMalloc(&ctr, 2 * sizeof(int)))) return e;
+    // split FP64 dimers for up to 32 dimers per water (liquid water has ~20-25 within
+    // the 2B cutoff); more dimers fall back to one task per dimer
+    part_cap = 32L * nw + 32;
+    if ((e = cudaMalloc(&partial, (size_t)part_cap * dimer_parts() * 32 * sizeof(double)))) return e;
+    if ((e = cudaMalloc(&done, (size_t)part_cap * sizeof(int)))) return e;
     int dev = 0;
     if ((e = cudaGetDevice(&dev))) return e;
     if ((e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev))) return e;
@@ -366,7 +373,9 @@ cudaError_t MultiBoxes::enqueue(int precision, const MixedPass& limits, bool fus
         mp.limit3 = 3.4e38f;
     }
     if (fused && fused_applies(precision, mp)) {
-        if ((e = launch_23(args, pairs, 0, totals + 0, trip, 0, totals + 1, precision, ctr, nsm, s))) return e;
+        if ((e = launch_23(args, pairs, 0, totals + 0, trip, 0, totals + 1, precision, ctr, nsm, s, partial, done,
+                           part_cap)))
+            return e;
         launches += 1;
     } else {
         if ((e = launch_2b_dev(args, pairs, pair_cap, totals + 0, precision, mp, s))) return e;

@@ -435,6 +435,15 @@ def generate(table_dir, out_dir):
                         % (body, ctype, ctype, ctype))
             disp.extend("    %s(x, acc);" % n for n in names)
             disp.append("}")
+            # one chunk at a time (the chunks' contributions add up to the whole polynomial)
+            disp.append("constexpr int kPoly%s%sParts = %d;" % (body.upper(), prec.upper(), len(names)))
+            disp.append("__device__ __forceinline__ void poly%s_%s_part(int p, const %s* x, %s* acc) {"
+                        % (body, prec, ctype, ctype))
+            disp.append("    switch (p) {")
+            disp.extend("    case %d: %s(x, acc); break;" % (c, n) for c, n in enumerate(names))
+            disp.append("    default: break;")
+            disp.append("    }")
+            disp.append("}")
         decls.append("constexpr int kPoly%sVars = %d;" % (body.upper(), n_vars))
         decls.append("// FP32 polynomial variables are x - kShift%s[v]" % body.upper())
         decls.append("__device__ constexpr float kShift%s[%d] = {%s};"
