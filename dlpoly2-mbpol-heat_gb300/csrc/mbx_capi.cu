@@ -67,6 +67,8 @@ struct mbx_context {
     int* mint_h = nullptr;             // pinned: totals[2], flag, hand-off counts[2]
     int mbox_cap = 0;
     long graph_replays = 0;
+    DispState disp;                    // dispersion tables and Verlet list
+    std::vector<int> disp_types_h, disp_mol_h;   // inputs of the host entry point's list
     char err[512] = {0};
 };
 
@@ -457,6 +459,7 @@ extern "C" void mbx_destroy(mbx_context* ctx) {
     if (ctx->mout_h) cudaFreeHost(ctx->mout_h);
     if (ctx->mint_h) cudaFreeHost(ctx->mint_h);
     ctx->multi.release();
+    ctx->disp.release();
     ctx->lb.release();
     for (cudaEvent_t e : ctx->ev)
         if (e) cudaEventDestroy(e);
@@ -583,6 +586,124 @@ extern "C" int mbx_mbpol_forces(mbx_context* ctx, int precision, int imcon, cons
     if (scalars) std::memcpy(scalars, sc, sizeof sc);
     return MBX_OK;
 }
+
+extern "C" int mbx_disp_setup(mbx_context* ctx, int ntypes, const double* prm, double rcut, double delr,
+                              int mxgrid) {
+    if (!ctx) return MBX_ERR_ARG;
+    if (ntypes < 1 || ntypes > 15 || !prm || !(rcut > 0.0) || !(delr >= 0.0) || (mxgrid != 0 && mxgrid < 8))
+        return fail(ctx, MBX_ERR_ARG, "bad dispersion parameters (ntypes 1..15, rcut > 0, delr >= 0)");
+    CK(cudaSetDevice(ctx->device));
+    CK(ctx->disp.setup(ntypes, prm, rcut, delr, mxgrid));
+    ctx->disp_types_h.clear();
+    return MBX_OK;
+}
+
+extern "C" int mbx_disp_forces_device(mbx_context* ctx, int imcon, const double* cell, int natms, const int* ltype,
+                                      const int* molecule, const double* xxx, const double* yyy, const double* zzz,
+                                      double* fxx, double* fyy, double* fzz, const double* vxx, const double* vyy,
+                                      const double* vzz, double* atomic_energy, double* out) {
+    if (!ctx) return MBX_ERR_ARG;
+    if (!ctx->disp.vvv) return fail(ctx, MBX_ERR_ARG, "mbx_disp_setup has not been called");
+    if (natms < 0 || (natms > 0 && (!ltype || !molecule || !xxx || !yyy || !zzz || !fxx || !fyy || !fzz)))
+        return fail(ctx, MBX_ERR_ARG, "bad argument");
+    Cell cl;
+    int rc = make_cell(ctx, imcon, cell, cl);
+    if (rc) return rc;
+    CK(cudaSetDevice(ctx->device));
+    cudaStream_t s = ctx->stream;
+    const bool heat = vxx && vyy && vzz;
+    CK(cudaMemsetAsync(ctx->acc, 0, 14 * sizeof(double), s));
+    bool rebuilt = false;
+    if (natms > 0) {
+        const cudaError_t e = ctx->disp.forces(cl, natms, ltype, molecule, xxx, yyy, zzz, fxx, fyy, fzz,
+                                               heat ? vxx : nullptr, heat ? vyy : nullptr, heat ? vzz : nullptr,
+                                               atomic_energy, ctx->acc, ctx->totals_h, s, &rebuilt);
+        if (e == cudaErrorInvalidValue) return fail(ctx, MBX_ERR_CAPACITY, "dispersion list capacity exceeded");
+        CK(e);
+    }
+    CK(cudaMemcpyAsync(ctx->acc_h, ctx->acc, 14 * sizeof(double), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (out) std::memcpy(out, ctx->acc_h, 14 * sizeof(double));
+    return MBX_OK;
+}
+
+extern "C" int mbx_disp_forces(mbx_context* ctx, int imcon, const double* cell, int natms, const int* ltype,
+                               const int* molecule, const double* xxx, const double* yyy, const double* zzz,
+                               double* fxx, double* fyy, double* fzz, double* engsrp, double* virsrp,
+                               double* stress, const double* vxx, const double* vyy, const double* vzz,
+                               double* atomic_energy, double* jpot) {
+    if (!ctx) return MBX_ERR_ARG;
+    if (natms < 0 || !ltype || !molecule || !xxx || !yyy || !zzz || !fxx || !fyy || !fzz || !engsrp || !virsrp ||
+        !stress)
+        return fail(ctx, MBX_ERR_ARG, "NULL argument");
+    CK(cudaSetDevice(ctx->device));
+    int rc = reserve_water(ctx, std::max(natms / 3, 1), std::max(natms, 1));
+    if (rc) return rc;
+    const bool heat = vxx && vyy && vzz;
+    cudaStream_t s = ctx->stream;
+    const size_t nb = (size_t)natms * sizeof(double);
+    double* d = ctx->atoms;
+    double *dx = d, *dy = d + natms, *dz = d + 2 * (size_t)natms;
+    double *dvx = d + 3 * (size_t)natms, *dvy = d + 4 * (size_t)natms, *dvz = d + 5 * (size_t)natms;
+    int* dint = (int*)(d + 6 * (size_t)natms);   // ltype then molecule (2 * natms ints in natms doubles)
+    double *dfx = d + 7 * (size_t)natms, *dfy = d + 8 * (size_t)natms, *dfz = d + 9 * (size_t)natms;
+    double* dae = d + 10 * (size_t)natms;
+    if (natms) {
+        CK(cudaMemcpyAsync(dx, xxx, nb, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(dy, yyy, nb, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(dz, zzz, nb, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(dint, ltype, natms * sizeof(int), cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(dint + natms, molecule, natms * sizeof(int), cudaMemcpyHostToDevice, s));
+        if (heat) {
+            CK(cudaMemcpyAsync(dvx, vxx, nb, cudaMemcpyHostToDevice, s));
+            CK(cudaMemcpyAsync(dvy, vyy, nb, cudaMemcpyHostToDevice, s));
+            CK(cudaMemcpyAsync(dvz, vzz, nb, cudaMemcpyHostToDevice, s));
+        }
+        CK(cudaMemsetAsync(dfx, 0, 3 * nb, s));
+        if (atomic_energy) CK(cudaMemsetAsync(dae, 0, nb, s));
+    }
+    // the staging arrays are rewritten every call: keep the list only while the types
+    // and molecules are those it was built for (positions are checked against the skin)
+    if (ctx->disp_types_h.size() != (size_t)natms ||
+        !std::equal(ltype, ltype + natms, ctx->disp_types_h.begin()) ||
+        !std::equal(molecule, molecule + natms, ctx->disp_mol_h.begin())) {
+        ctx->disp.valid = false;
+        ctx->disp_types_h.assign(ltype, ltype + natms);
+        ctx->disp_mol_h.assign(molecule, molecule + natms);
+    }
+    double out[14];
+    rc = mbx_disp_forces_device(ctx, imcon, cell, natms, dint, dint + natms, dx, dy, dz, dfx, dfy, dfz,
+                                heat ? dvx : nullptr, heat ? dvy : nullptr, heat ? dvz : nullptr,
+                                atomic_energy ? dae : nullptr, out);
+    if (rc) return rc;
+    std::vector<double> h(4 * (size_t)natms);
+    if (natms) {
+        CK(cudaMemcpyAsync(h.data(), dfx, 3 * nb, cudaMemcpyDeviceToHost, s));
+        if (atomic_energy) CK(cudaMemcpyAsync(h.data() + 3 * (size_t)natms, dae, nb, cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+    }
+    for (int i = 0; i < natms; ++i) {
+        fxx[i] += h[i];
+        fyy[i] += h[natms + i];
+        fzz[i] += h[2 * (size_t)natms + i];
+        if (atomic_energy) atomic_energy[i] += h[3 * (size_t)natms + i];
+    }
+    *engsrp += out[0];
+    *virsrp += out[1];
+    for (int q = 0; q < 9; ++q) stress[q] += out[2 + q];
+    if (jpot)
+        for (int q = 0; q < 3; ++q) jpot[q] += out[11 + q];
+    return MBX_OK;
+}
+
+extern "C" int mbx_disp_lrc(int ntypes, const double* prm, const int* numtyp, double rcut, double volm,
+                            double* elrc, double* virlrc) {
+    if (ntypes < 1 || !prm || !numtyp || !(rcut > 0.0) || !(volm > 0.0) || !elrc || !virlrc) return MBX_ERR_ARG;
+    disp_lrc(ntypes, prm, numtyp, rcut, volm, elrc, virlrc);
+    return MBX_OK;
+}
+
+extern "C" long mbx_disp_list_builds(const mbx_context* ctx) { return ctx ? ctx->disp.builds : -1; }
 
 extern "C" int mbx_set_fused(mbx_context* ctx, int on) {
     if (!ctx) return MBX_ERR_ARG;

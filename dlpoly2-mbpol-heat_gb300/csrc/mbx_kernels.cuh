@@ -131,6 +131,42 @@ struct ListBuilder {
     cudaError_t phase2(int nw, const Cell& cl, const double* mono, int2* pairs, int4* trip, cudaStream_t s);
 };
 
+// Short-range dispersion, DL_POLY vdw type 12 (mbx_disp.cu): tables, Verlet list with
+// skin, forces.  Types are 1-based (0: none), prm holds {C6, a6, C8, a8} per pair type
+// (pair i >= j at i(i-1)/2 + j - 1); atoms of the same molecule do not interact.
+struct DispState {
+    int ntypes = 0, mxgrid = 0;
+    double rcut = 0.0, delr = 0.0;
+    std::vector<double> prm;
+    double *vvv = nullptr, *ggg = nullptr;       // tables [pair][mxgrid]
+    unsigned vdw_types = 0;
+    unsigned long long vdw_pairs[3] = {0, 0, 0};
+    int cap = 512, cap_alloc = 0;                // list partners j > i per atom
+    int *nn = nullptr, *nbr = nullptr, *flag = nullptr;
+    double* xref = nullptr;                      // positions at the last build (x, y, z blocks)
+    unsigned *key = nullptr, *skey = nullptr;
+    int *idx = nullptr, *sidx = nullptr, *cstart = nullptr, *cend = nullptr;
+    void* sort_tmp = nullptr;
+    size_t sort_bytes = 0;
+    int natms_cap = 0, ncell_cap = 0;
+    bool valid = false;                          // the list matches the inputs below
+    int natms_last = 0, imcon_last = 0;
+    const int *ltype_last = nullptr, *mol_last = nullptr;
+    double cell_last[9] = {0};
+    long builds = 0, launches = 0;
+
+    ~DispState();
+    void release();
+    cudaError_t setup(int ntypes, const double* prm, double rcut, double delr, int mxgrid);
+    cudaError_t forces(const Cell& cl, int natms, const int* ltype, const int* mol, const double* x,
+                       const double* y, const double* z, double* fx, double* fy, double* fz, const double* vx,
+                       const double* vy, const double* vz, double* ae, double* out14, int* flag_host,
+                       cudaStream_t s, bool* rebuilt);
+};
+// lrcorrect for vdw type 12 (host): elrc and virlrc for numtyp[t] atoms of type t + 1.
+void disp_lrc(int ntypes, const double* prm, const int* numtyp, double rcut, double volm, double* elrc,
+              double* virlrc);
+
 // Many independent water boxes evaluated by one set of launches (mbx_multi.cu).
 // Box b holds nw_b waters in the standard layout (3*nw_b water atoms, O H1 H2, then
 // nw_b M sites) at atom offset 4 * sum_{b'<b} nw_b'.  Every size is fixed by setup(),

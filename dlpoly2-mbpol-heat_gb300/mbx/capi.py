@@ -80,6 +80,12 @@ def load(path=None):
     L.mbx_server_error.restype = C.c_char_p
     L.mbx_mbpol_multi.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, _I, _D] + [_D] * 12
     L.mbx_mbpol_multi_device.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, _I, _D] + [C.c_void_p] * 11 + [_D]
+    L.mbx_disp_setup.argtypes = [C.c_void_p, C.c_int, _D, C.c_double, C.c_double, C.c_int]
+    L.mbx_disp_forces.argtypes = [C.c_void_p, C.c_int, _D, C.c_int, _I, _I] + [_D] * 14
+    L.mbx_disp_forces_device.argtypes = [C.c_void_p, C.c_int, _D, C.c_int] + [C.c_void_p] * 12 + [_D]
+    L.mbx_disp_lrc.argtypes = [C.c_int, _D, _I, C.c_double, C.c_double, _D, _D]
+    L.mbx_disp_list_builds.argtypes = [C.c_void_p]
+    L.mbx_disp_list_builds.restype = C.c_long
     L.mbx_set_graphs.argtypes = [C.c_void_p, C.c_int]
     L.mbx_set_fused.argtypes = [C.c_void_p, C.c_int]
     L.mbx_graph_launches.argtypes = [C.c_void_p]
@@ -237,6 +243,34 @@ class Context:
                                              *xyz_ptrs, *f_ptrs, *v_ptrs, mass_ptr, ae_ptr, _p(sc))
         self._check(rc, "mbx_mbpol_multi_device")
         return sc
+
+    def disp_setup(self, prm, rcut=9.0, delr=1.0, mxgrid=0, ntypes=None):
+        prm = _f64(prm).reshape(-1, 4)
+        nt = ntypes or int(round((np.sqrt(8 * prm.shape[0] + 1) - 1) / 2))
+        self._check(self.lib.mbx_disp_setup(self.h, nt, _p(prm.ravel().copy()), rcut, delr, mxgrid),
+                    "mbx_disp_setup")
+
+    def dispersion(self, box, ltype, mol, heat=True):
+        """Dispersion forces on a box (host arrays); ltype/mol per atom."""
+        n = box.natms
+        x, y, z = (_f64(box.xyz[:, k]) for k in range(3))
+        f = np.zeros((3, n))
+        eng = C.c_double(0)
+        vir = C.c_double(0)
+        stress = np.zeros(9)
+        ae = np.zeros(n)
+        jpot = np.zeros(3)
+        v = [_f64(box.vel[:, k]) for k in range(3)] if heat else [None] * 3
+        lt = np.ascontiguousarray(ltype, dtype=np.int32)
+        mo = np.ascontiguousarray(mol, dtype=np.int32)
+        rc = self.lib.mbx_disp_forces(self.h, box.imcon, _p(_f64(box.cell)), n, _p(lt, _I), _p(mo, _I), _p(x),
+                                      _p(y), _p(z), _p(f[0]), _p(f[1]), _p(f[2]), C.byref(eng), C.byref(vir),
+                                      _p(stress), _p(v[0]), _p(v[1]), _p(v[2]), _p(ae), _p(jpot))
+        self._check(rc, "mbx_disp_forces")
+        return dict(eng=eng.value, vir=vir.value, stress=stress, forces=f.T.copy(), atomic_energy=ae, jpot=jpot)
+
+    def disp_list_builds(self):
+        return int(self.lib.mbx_disp_list_builds(self.h))
 
     def set_fused(self, on=True):
         self._check(self.lib.mbx_set_fused(self.h, 1 if on else 0), "mbx_set_fused")

@@ -169,3 +169,30 @@ class BoxSet:
     def split(self, a):
         """Per-box views of a per-atom array."""
         return [a[self.offsets[b]:self.offsets[b + 1]] for b in range(self.nbox)]
+
+
+# Dispersion inputs of a water box: types O = 1, H = 2, M site = 3 (no dispersion) and
+# one molecule per water (its M site included).
+def water_types(box):
+    nw = box.nw
+    ltype = np.zeros(box.natms, dtype=np.int32)
+    ltype[0:3 * nw:3] = 1
+    ltype[1:3 * nw:3] = 2
+    ltype[2:3 * nw:3] = 2
+    ltype[3 * nw:4 * nw] = 3
+    mol = np.concatenate([np.repeat(np.arange(nw), 3), np.arange(nw)]).astype(np.int32)
+    return ltype, mol
+
+
+# Tang-Toennies C6 parameters {C6, a6, C8, a8} per pair type (O-O, H-O, H-H, then the
+# M-site pairs, which do not interact), in DL_POLY internal units (10 J/mol, Angstrom).
+# The reference reads MB-pol's values from its FIELD file, which it does not ship; these
+# are values of the same form and magnitude chosen for the synthetic benchmark and tests.
+DISP_PARAMS_SYNTHETIC = np.array([
+    [600.0 * 418.4, 3.2, 0.0, 0.0],    # O-O
+    [200.0 * 418.4, 3.6, 0.0, 0.0],    # H-O
+    [60.0 * 418.4, 3.9, 0.0, 0.0],     # H-H
+    [0.0, 0.0, 0.0, 0.0],              # M-O
+    [0.0, 0.0, 0.0, 0.0],              # M-H
+    [0.0, 0.0, 0.0, 0.0],              # M-M
+])

@@ -237,6 +237,46 @@ int mbx_mbpol_multi(mbx_context* ctx, int precision, int imcon, int nbox, const 
 int mbx_set_graphs(mbx_context* ctx, int on);
 long mbx_graph_launches(const mbx_context* ctx);
 
+/*
+ * Short-range dispersion: DL_POLY van der Waals type 12, Tang-Toennies damped
+ * -C6 f6(a6 r)/r^6 - C8 f8(a8 r)/r^8.  Replaces forgen's type-12 tables
+ * (SOURCE/forgen.f:97, :262-270, :337-357), the Verlet list of parlst with the
+ * intramolecular exclusions (SOURCE/parlst.f, SOURCE/exclude_ttm.f) and srfrce2
+ * (SOURCE/srfrce2.f:80-270) with its HEAT_CURRENT hooks (update_energy_srf,
+ * update_forces), and lrcorrect for type 12 (SOURCE/lrcorrect.f:112-223).
+ *   mbx_disp_setup   ntypes atom types (1-based, <= 15); prm[4 * ntypes(ntypes+1)/2] =
+ *                    {C6, a6, C8, a8} per pair type, pair (i >= j) at index
+ *                    i(i-1)/2 + j - 1 (lstvdw order), internal energy units and Angstrom;
+ *                    a pair type whose parameters are all 0 does not interact; rcut and
+ *                    the Verlet skin delr in Angstrom; mxgrid table points, 0 = the
+ *                    reference's default max(1000, rcut / 1e-4 + 4).  The reference reads
+ *                    these parameters from its FIELD file.
+ *   mbx_disp_forces  ltype[natms] (0 = no dispersion, e.g. M sites), molecule[natms]
+ *                    (atoms of one molecule do not interact); forces, engsrp, virsrp,
+ *                    stress ACCUMULATED; per-atom energies get half of each pair energy;
+ *                    velocities (or NULL) give jpot[3] ACCUMULATED.  Host arrays.
+ *   _device          device arrays; out[14] = {engsrp, virsrp, stress[9], jpot[3]} on
+ *                    the host.  The Verlet list (pairs within rcut + delr) is kept between
+ *                    calls and rebuilt when an atom has moved more than delr / 2, or natms,
+ *                    the cell or the ltype/molecule arrays change (mbx_disp_setup also
+ *                    drops it); mbx_disp_list_builds counts the builds.
+ *   mbx_disp_lrc     elrc and virlrc for numtyp[t] atoms of type t + 1 in volume volm
+ *                    (host only, no GPU), with the reference's factorial in
+ *                    tang_toennies_lr (it multiplies by its argument at every step).
+ */
+int mbx_disp_setup(mbx_context* ctx, int ntypes, const double* prm, double rcut, double delr, int mxgrid);
+int mbx_disp_forces(mbx_context* ctx, int imcon, const double* cell, int natms, const int* ltype, const int* molecule,
+                    const double* xxx, const double* yyy, const double* zzz, double* fxx, double* fyy, double* fzz,
+                    double* engsrp, double* virsrp, double* stress, const double* vxx, const double* vyy,
+                    const double* vzz, double* atomic_energy, double* jpot);
+int mbx_disp_forces_device(mbx_context* ctx, int imcon, const double* cell, int natms, const int* ltype,
+                           const int* molecule, const double* xxx, const double* yyy, const double* zzz, double* fxx,
+                           double* fyy, double* fzz, const double* vxx, const double* vyy, const double* vzz,
+                           double* atomic_energy, double* out);
+int mbx_disp_lrc(int ntypes, const double* prm, const int* numtyp, double rcut, double volm, double* elrc,
+                 double* virlrc);
+long mbx_disp_list_builds(const mbx_context* ctx);
+
 /* Dimer and trimer lists of the last evaluation (0-based water indices, i<j<k), as
  * index sets; the host arrays receive up to cap entries; counts are always written. */
 int mbx_last_lists(mbx_context* ctx, int* pairs, long cap_pairs, long* npairs, int* trimers, long cap_trimers,

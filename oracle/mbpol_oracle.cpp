@@ -599,6 +599,11 @@ extern "C" double orc_3b(const double* w1, const double* w2, const double* w3, d
     return retval;
 }
 
+// image_vectors for the other restatements in this library (images.f's imcon 1-3)
+extern "C" void orc_image_vectors(int imcon, const double* cell, int n, double* dx) {
+    image_vectors(imcon, cell, n, dx);
+}
+
 extern "C" void orc_image_monomers(int imcon, const double* cell, int nw, double* xyz) {
     for (int i = 0; i < nw; ++i) {
         double* w = xyz + 9 * (size_t)i;

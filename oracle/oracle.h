@@ -112,6 +112,21 @@ double orc_qdetermine(int imcon, const double* cell, int nw, const int* listttm2
 /* image_monomers (SOURCE/mbpol.f90:1275-1301): H atoms next to their O. */
 void orc_image_monomers(int imcon, const double* cell, int nw, double* xyz);
 
+/* Short-range dispersion, DL_POLY vdw type 12 (Tang-Toennies damped C6/C8):
+ * SOURCE/tang-toennies.f90, SOURCE/forgen.f (tables), SOURCE/srfrce2.f (forces),
+ * SOURCE/lrcorrect.f (long-range correction).  Types are 1-based (0: none); prm holds
+ * {C6, a6, C8, a8} per pair type, pair (i >= j) at index i(i-1)/2 + j - 1.  Pairs of the
+ * same molecule are excluded.  All outputs ACCUMULATED; returns the pair count. */
+double orc_tang_toennies(int n, double x);
+double orc_tang_toennies_lr(int n, double x);
+void orc_disp_tables(int npair, const double* prm, int mxgrid, double dlrpot, double* vvv, double* ggg);
+long orc_dispersion(int imcon, const double* cell, int natms, const int* ltype, const int* mol, int ntypes,
+                    const double* prm, double rcut, int mxgrid, const double* x, const double* y, const double* z,
+                    double* fx, double* fy, double* fz, double* eng, double* vir, double* stress,
+                    double* atomic_energy, const double* vx, const double* vy, const double* vz, double* jpot);
+void orc_disp_lrc(int ntypes, const double* prm, const int* numtyp, double rcut, double volm, double* elrc,
+                  double* virlrc);
+
 #ifdef __cplusplus
 }
 #endif

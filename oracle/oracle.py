@@ -54,6 +54,14 @@ class Oracle:
         L.orc_msites.argtypes = [C.c_int, _D, C.c_int, _I, _D, _D, _D, C.c_double]
         L.orc_qdetermine.argtypes = [C.c_int, _D, C.c_int, _I, _D, _D, _D, C.c_double, _D, _D]
         L.orc_qdetermine.restype = C.c_double
+        L.orc_tang_toennies.argtypes = [C.c_int, C.c_double]
+        L.orc_tang_toennies.restype = C.c_double
+        L.orc_tang_toennies_lr.argtypes = [C.c_int, C.c_double]
+        L.orc_tang_toennies_lr.restype = C.c_double
+        L.orc_disp_tables.argtypes = [C.c_int, _D, C.c_int, C.c_double, _D, _D]
+        L.orc_dispersion.argtypes = [C.c_int, _D, C.c_int, _I, _I, C.c_int, _D, C.c_double, C.c_int] + [_D] * 14
+        L.orc_dispersion.restype = C.c_long
+        L.orc_disp_lrc.argtypes = [C.c_int, _D, _I, C.c_double, C.c_double, _D, _D]
         if L.orc_dms_load(os.path.join(TABLES, "ps_dms.tbl").encode()):
             raise RuntimeError("orc_dms_load failed")
         if L.orc_pes_load(os.path.join(TABLES, "ps_pes.tbl").encode()):
@@ -181,6 +189,38 @@ class Oracle:
         worst = self.lib.orc_qdetermine(box.imcon, _p(box.cell), box.nw, _p(lst, _I), _p(x), _p(y), _p(z), gamma,
                                         _p(chge), _p(dp))
         return np.stack([x, y, z], 1), chge, dp, worst
+
+    def dispersion(self, box, ltype, mol, prm, rcut=9.0, mxgrid=0, velocities=True):
+        """srfrce2 with type-12 tables over every intermolecular pair within rcut."""
+        n = box.natms
+        x, y, z = (np.ascontiguousarray(box.xyz[:, k]) for k in range(3))
+        f = np.zeros((3, n))
+        eng = C.c_double(0)
+        vir = C.c_double(0)
+        stress = np.zeros(9)
+        ae = np.zeros(n)
+        jpot = np.zeros(3)
+        v = [np.ascontiguousarray(box.vel[:, k]) for k in range(3)] if velocities else [None] * 3
+        prm = np.ascontiguousarray(prm, dtype=np.float64).reshape(-1, 4)
+        nt = int(round((np.sqrt(8 * prm.shape[0] + 1) - 1) / 2))
+        mxgrid = mxgrid or max(1000, int(rcut / 0.0001 + 0.5) + 4)
+        lt = np.ascontiguousarray(ltype, dtype=np.int32)
+        mo = np.ascontiguousarray(mol, dtype=np.int32)
+        npairs = self.lib.orc_dispersion(box.imcon, _p(box.cell), n, _p(lt, _I), _p(mo, _I), nt, _p(prm.ravel().copy()),
+                                         rcut, mxgrid, _p(x), _p(y), _p(z), _p(f[0]), _p(f[1]), _p(f[2]),
+                                         C.byref(eng), C.byref(vir), _p(stress), _p(ae), _p(v[0]), _p(v[1]),
+                                         _p(v[2]), _p(jpot))
+        return dict(eng=eng.value, vir=vir.value, stress=stress, forces=f.T.copy(), atomic_energy=ae, jpot=jpot,
+                    npairs=npairs)
+
+    def disp_lrc(self, prm, numtyp, rcut, volm):
+        prm = np.ascontiguousarray(prm, dtype=np.float64).reshape(-1, 4)
+        nt = int(round((np.sqrt(8 * prm.shape[0] + 1) - 1) / 2))
+        e = C.c_double(0)
+        v = C.c_double(0)
+        self.lib.orc_disp_lrc(nt, _p(prm.ravel().copy()), _p(np.ascontiguousarray(numtyp, dtype=np.int32), _I), rcut,
+                              volm, C.byref(e), C.byref(v))
+        return e.value, v.value
 
     def image_monomers(self, box):
         m = box.monomers().copy()
