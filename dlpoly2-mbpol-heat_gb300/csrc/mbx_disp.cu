@@ -136,18 +136,50 @@ __device__ __forceinline__ double sep2(const Cell& cl, double dx, double dy, dou
     return dadd(dadd(dmul(dx, dx), dmul(dy, dy)), dmul(dz, dz));
 }
 
+// |image(d)|^2 in FP32, for the list build only (the forces cut at rcut in FP64).
+__device__ __forceinline__ float sep2f(const Cell& cl, float dx, float dy, float dz) {
+    if (cl.imcon == 1 || cl.imcon == 2) {
+        dx -= (float)cl.c[0] * rintf(dx * (float)cl.inv[0]);
+        dy -= (float)cl.c[4] * rintf(dy * (float)cl.inv[1]);
+        dz -= (float)cl.c[8] * rintf(dz * (float)cl.inv[2]);
+    } else {
+        const double* r = cl.rc;
+        const double* c = cl.c;
+        float sx = (float)r[0] * dx + (float)r[3] * dy + (float)r[6] * dz;
+        float sy = (float)r[1] * dx + (float)r[4] * dy + (float)r[7] * dz;
+        float sz = (float)r[2] * dx + (float)r[5] * dy + (float)r[8] * dz;
+        sx -= rintf(sx);
+        sy -= rintf(sy);
+        sz -= rintf(sz);
+        dx = (float)c[0] * sx + (float)c[3] * sy + (float)c[6] * sz;
+        dy = (float)c[1] * sx + (float)c[4] * sy + (float)c[7] * sz;
+        dz = (float)c[2] * sx + (float)c[5] * sy + (float)c[8] * sz;
+    }
+    return dx * dx + dy * dy + dz * dz;
+}
+
+__global__ void k_disp_f32(int natms, const double* __restrict__ x, const double* __restrict__ y,
+                           const double* __restrict__ z, float4* __restrict__ xf) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < natms) xf[i] = make_float4((float)x[i], (float)y[i], (float)z[i], 0.f);
+}
+
 // Verlet list: partners j > i of different molecules within rlist; warp per atom,
 // candidates from the 27 cells around the atom's cell (or every atom), appended in
-// candidate order.
+// candidate order.  The distance test runs in FP32 against rlist plus a margin far above
+// FP32 rounding (rlist2f), so the list holds every pair within rlist; the force kernel
+// applies the exact FP64 cut at rcut.
 __global__ void k_disp_build(DispArgs a, int3 nc, int all_pairs, const int* __restrict__ sidx,
-                             const int* __restrict__ cstart, const int* __restrict__ cend, double rlist2, int cap,
-                             int* __restrict__ nn, int* __restrict__ nbr, int* __restrict__ flag) {
+                             const int* __restrict__ cstart, const int* __restrict__ cend,
+                             const float4* __restrict__ xf, float rlist2f, int cap, int* __restrict__ nn,
+                             int* __restrict__ nbr, int* __restrict__ flag) {
     const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (i >= a.natms) return;   // warp-uniform
     int cnt = 0;
     if (vdw_atom(a, i)) {
         const double xi = a.x[i], yi = a.y[i], zi = a.z[i];
+        const float4 pi = xf[i];
         const int mi = a.mol[i];
         int* my = nbr + (size_t)i * cap;
         const int ncand_cells = all_pairs ? 1 : 27;
@@ -168,8 +200,10 @@ __global__ void k_disp_build(DispArgs a, int3 nc, int all_pairs, const int* __re
                 int j = 0;
                 if (q < end) {
                     j = all_pairs ? q : sidx[q];
-                    if (j > i && vdw_atom(a, j) && a.mol[j] != mi)
-                        hit = sep2(a.cl, dsub(xi, a.x[j]), dsub(yi, a.y[j]), dsub(zi, a.z[j])) < rlist2;
+                    if (j > i && vdw_atom(a, j) && a.mol[j] != mi) {
+                        const float4 pj = xf[j];
+                        hit = sep2f(a.cl, pi.x - pj.x, pi.y - pj.y, pi.z - pj.z) < rlist2f;
+                    }
                 }
                 const unsigned bal = __ballot_sync(0xffffffffu, hit);
                 if (hit) {
@@ -421,10 +455,16 @@ cudaError_t DispState::forces(const Cell& cl, int natms, const int* ltype, const
             launches += 3;
         }
         if ((e = cudaMemsetAsync(flag, 0, sizeof(int), s))) return e;
-        k_disp_build<<<grid(32L * natms), kThreads, 0, s>>>(a, nc, all_pairs, sidx, cstart, cend, rlist * rlist, cap,
+        // FP32 copies of the positions for the distance tests live in xref until the
+        // build is done (the reference positions are written into it afterwards)
+        float4* xf = (float4*)xref;
+        k_disp_f32<<<grid(natms), kThreads, 0, s>>>(natms, x, y, z, xf);
+        const double margin = 1.0e-3;   // Angstrom, >> FP32 rounding of coordinates below ~1e3 A
+        const float rlist2f = (float)((rlist + margin) * (rlist + margin));
+        k_disp_build<<<grid(32L * natms), kThreads, 0, s>>>(a, nc, all_pairs, sidx, cstart, cend, xf, rlist2f, cap,
                                                             nn, nbr, flag);
         k_disp_ref<<<grid(natms), kThreads, 0, s>>>(natms, x, y, z, xref);
-        launches += 2;
+        launches += 3;
         if ((e = cudaMemcpyAsync(flag_host, flag, sizeof(int), cudaMemcpyDeviceToHost, s))) return e;
         if ((e = cudaStreamSynchronize(s))) return e;
         if (!(*flag_host & 1)) {
