@@ -31,9 +31,20 @@ def _check(got, ref):
     assert rel_err(got["jpot"], ref["jpot"]) <= TOL64
 
 
-@pytest.mark.parametrize("name", ["cfg0_256", "cfg1_4096", "ortho_imcon2"])
+def _triclinic():
+    b = systems.water_box(216, 19.5, seed=13, lattice=6)
+    L = b.L
+    H = np.array([[L, 0.1 * L, 0.05 * L], [0.0, L, 0.08 * L], [0.0, 0.0, L]])
+    b.xyz = (b.xyz / L) @ H.T
+    b.cell = np.ascontiguousarray(H.T.ravel())
+    b.imcon = 3
+    return b
+
+
+@pytest.mark.parametrize("name", ["cfg0_256", "cfg1_4096", "ortho_imcon2", "triclinic_imcon3"])
 def test_dispersion_matches_oracle(oracle_lib, name):
-    box = {"cfg0_256": systems.config0, "cfg1_4096": systems.config1, "ortho_imcon2": _ortho}[name]()
+    box = {"cfg0_256": systems.config0, "cfg1_4096": systems.config1, "ortho_imcon2": _ortho,
+           "triclinic_imcon3": _triclinic}[name]()
     lt, mol = systems.water_types(box)
     ctx = capi.Context(0)
     try:

@@ -28,7 +28,20 @@ def _boxes():
         "small_64_allpairs": systems.box_for(64, seed=5),
         "ortho_imcon2": _ortho(),
         "shuffled_layout": _shuffled(),
+        "triclinic_imcon3": _triclinic(),
     }
+
+
+def _triclinic():
+    """The 216-water box sheared into a parallelepiped (imcon 3): r = H s."""
+    b = systems.water_box(216, 19.5, seed=13, lattice=6)
+    L = b.L
+    H = np.array([[L, 0.1 * L, 0.05 * L], [0.0, L, 0.08 * L], [0.0, 0.0, L]])   # columns = cell vectors
+    s = b.xyz / L
+    b.xyz = s @ H.T
+    b.cell = np.ascontiguousarray(H.T.ravel())   # cell(1:3) = a, cell(4:6) = b, cell(7:9) = c
+    b.imcon = 3
+    return b
 
 
 def _ortho():
@@ -219,7 +232,7 @@ def test_mixed_handoff_limits(mbx_ctx, refs):
         mbx_ctx.set_mixed_limits(0.0, 3.4e38)
 
 
-@pytest.mark.parametrize("name", ["cfg0_256", "ortho_imcon2", "shuffled_layout"])
+@pytest.mark.parametrize("name", ["cfg0_256", "ortho_imcon2", "shuffled_layout", "triclinic_imcon3"])
 def test_ps_pes_fp64_matches_oracle(mbx_ctx, oracle_lib, name):
     box = BOXES[name]
     ref = oracle_lib.angfrc_ps(box)
@@ -232,7 +245,7 @@ def test_ps_pes_fp64_matches_oracle(mbx_ctx, oracle_lib, name):
     assert rel_err(got["jpot"], ref["jpot"]) <= TOL64
 
 
-@pytest.mark.parametrize("name", ["cfg0_256", "ortho_imcon2", "shuffled_layout"])
+@pytest.mark.parametrize("name", ["cfg0_256", "ortho_imcon2", "shuffled_layout", "triclinic_imcon3"])
 def test_msites_dms_match_oracle(mbx_ctx, oracle_lib, name):
     box = BOXES[name]
     rx, rq, rdp, _ = oracle_lib.msites_dms(box)
