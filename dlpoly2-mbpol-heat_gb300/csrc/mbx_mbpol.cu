@@ -585,6 +585,99 @@ __device__ __forceinline__ void prep_3b(const MbpolArgs& a, int4 c, double* w, T
     for (int q = 0; q < 27; ++q) p[q] = (T)w[q];
 }
 
+// The FP32 working frame of a trimer directly: positions relative to the second O, with
+// the monomers re-imaged around it as do_trimer does (SOURCE/mbpol.f90:867-876).  The
+// same frame as prep_3b<float> up to the FP64 rounding before the cast, in fewer FP64
+// operations (the FP64 pipe is the mixed kernel's bound).
+__device__ __forceinline__ void prep_3b_shifted(const MbpolArgs& a, int4 c, float* p) {
+    double w1[9], w2[9], w3[9];
+#pragma unroll
+    for (int q = 0; q < 9; ++q) {
+        w1[q] = a.mono[9 * (size_t)c.x + q];
+        w2[q] = a.mono[9 * (size_t)c.y + q];
+        w3[q] = a.mono[9 * (size_t)c.z + q];
+    }
+    double r12[3], r23[3];
+    const Cell& cl = a.cells ? a.cells[a.wbox[c.x]] : a.cell;
+    dist2_img(cl, w1, w2, r12);   // image(O1 - O2)
+    dist2_img(cl, w2, w3, r23);   // image(O2 - O3)
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        p[k] = (float)r12[k];
+        p[3 + k] = (float)dadd(dsub(w1[3 + k], w1[k]), r12[k]);
+        p[6 + k] = (float)dadd(dsub(w1[6 + k], w1[k]), r12[k]);
+        p[9 + k] = 0.f;
+        p[12 + k] = (float)dsub(w2[3 + k], w2[k]);
+        p[15 + k] = (float)dsub(w2[6 + k], w2[k]);
+        p[18 + k] = (float)(-r23[k]);
+        p[21 + k] = (float)dsub(dsub(w3[3 + k], w3[k]), r23[k]);
+        p[24 + k] = (float)dsub(dsub(w3[6 + k], w3[k]), r23[k]);
+    }
+}
+
+// cluster_accumulate for an FP32 trimer: the same quantities with the per-cluster
+// virial and stress products in FP32 on the shifted frame (a cluster's gradient sums to
+// zero, so the shift does not change them) and FP64 for the energy, the force and
+// per-atom energy atomics and the heat current (raw coordinates, FP64).
+__device__ __forceinline__ void trimer_accumulate_f32(const MbpolArgs& a, const int* at, float e_kcal,
+                                                      const float* p, const float* gt, double* red) {
+    const double e = (double)e_kcal * kEngUnit;
+    red[0] += e;
+    if (a.ae) {
+        const double ea = (1.0 / 9) * (double)e_kcal * kEngUnit;
+#pragma unroll
+        for (int q = 0; q < 9; ++q) atomicAdd(a.ae + at[q], ea);
+    }
+    double gd[27];
+#pragma unroll
+    for (int q = 0; q < 27; ++q) gd[q] = (double)(gt[q] * (float)kEngUnit);
+#pragma unroll
+    for (int q = 0; q < 9; ++q) {
+        atomicAdd(a.fx + at[q], -gd[3 * q + 0]);
+        atomicAdd(a.fy + at[q], -gd[3 * q + 1]);
+        atomicAdd(a.fz + at[q], -gd[3 * q + 2]);
+    }
+    float sv[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+    for (int q = 0; q < 9; ++q) {
+        const float w0 = p[3 * q], w1 = p[3 * q + 1], w2 = p[3 * q + 2];
+        const float g0 = gt[3 * q], g1 = gt[3 * q + 1], g2 = gt[3 * q + 2];
+        sv[0] += w0 * g0;
+        sv[1] += w0 * g1;
+        sv[2] += w0 * g2;
+        sv[3] += w1 * g1;
+        sv[4] += w1 * g2;
+        sv[5] += w2 * g2;
+    }
+    double s[6];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) s[k] = (double)sv[k] * kEngUnit;
+    red[1] += (s[0] + s[3]) + s[5];
+    red[2] -= s[0]; red[3] -= s[1]; red[4] -= s[2];
+    red[5] -= s[1]; red[6] -= s[3]; red[7] -= s[4];
+    red[8] -= s[2]; red[9] -= s[4]; red[10] -= s[5];
+    if (a.vx) {
+        // sum_q (F_q . v_q)(9 r_q - sum_j r_j) = 9 sum_q fv_q r_q - (sum_j r_j) sum_q fv_q
+        double rs[3] = {0.0, 0.0, 0.0}, A[3] = {0.0, 0.0, 0.0}, B = 0.0;
+#pragma unroll
+        for (int q = 0; q < 9; ++q) {
+            const int i = at[q];
+            const double xi = a.x[i], yi = a.y[i], zi = a.z[i];
+            const double fv = -(1.0 / 9) * (gd[3 * q] * a.vx[i] + gd[3 * q + 1] * a.vy[i] + gd[3 * q + 2] * a.vz[i]);
+            rs[0] += xi;
+            rs[1] += yi;
+            rs[2] += zi;
+            A[0] += fv * xi;
+            A[1] += fv * yi;
+            A[2] += fv * zi;
+            B += fv;
+        }
+        red[11] += 9.0 * A[0] - rs[0] * B;
+        red[12] += 9.0 * A[1] - rs[1] * B;
+        red[13] += 9.0 * A[2] - rs[2] * B;
+    }
+}
+
 __device__ __forceinline__ void trimer_atoms(const MbpolArgs& a, int4 c, int* at) {
     const int o1 = a.list[3 * c.x] - 1, o2 = a.list[3 * c.y] - 1, o3 = a.list[3 * c.z] - 1;
     at[0] = o1; at[1] = o1 + 1; at[2] = o1 + 2;
@@ -594,6 +687,22 @@ __device__ __forceinline__ void trimer_atoms(const MbpolArgs& a, int4 c, int* at
 
 template <typename T>
 __device__ __forceinline__ void eval_trimer(const MbpolArgs& a, int4 c, double* red, const HardList& hl) {
+    if constexpr (sizeof(T) == 4) {
+        float p[27], gt[27];
+        prep_3b_shifted(a, c, p);
+#pragma unroll
+        for (int q = 0; q < 27; ++q) gt[q] = 0.f;
+        bool hard = false;
+        const float e = model_3b<float>(p, gt, hl.limit, hl.items ? &hard : nullptr);
+        if (hard) {
+            ((int4*)hl.items)[atomicAdd(hl.count, 1)] = c;
+            return;
+        }
+        int at[9];
+        trimer_atoms(a, c, at);
+        trimer_accumulate_f32(a, at, e, p, gt, red);
+        return;
+    }
     T p[27], gt[27];
     double w[27];
     prep_3b<T>(a, c, w, p);
