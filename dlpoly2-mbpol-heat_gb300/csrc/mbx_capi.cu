@@ -67,6 +67,8 @@ struct mbx_context {
     int* mint_h = nullptr;             // pinned: totals[2], flag, hand-off counts[2]
     int mbox_cap = 0;
     long graph_replays = 0;
+    int* ints = nullptr;               // mbx_water_forces staging: listttm2, listang, ltype, molecule
+    size_t ints_cap = 0;
     DispState disp;                    // dispersion tables and Verlet list
     std::vector<int> disp_types_h, disp_mol_h;   // inputs of the host entry point's list
     char err[512] = {0};
@@ -449,7 +451,8 @@ extern "C" void mbx_destroy(mbx_context* ctx) {
     cudaSetDevice(ctx->device);
     if (ctx->own_stream) cudaStreamSynchronize(ctx->own_stream);
     void* dev[] = {ctx->mono, ctx->list, ctx->atoms, ctx->ae_scratch, ctx->acc, ctx->totals, ctx->pairs, ctx->trip,
-                   ctx->batch, ctx->hard2, ctx->hard3, ctx->hard_count, ctx->fuse_ctr, ctx->part2, ctx->done2};
+                   ctx->batch, ctx->hard2, ctx->hard3, ctx->hard_count, ctx->fuse_ctr, ctx->part2, ctx->done2,
+                   ctx->ints};
     for (void* p : dev)
         if (p) cudaFree(p);
     if (ctx->totals_h) cudaFreeHost(ctx->totals_h);
@@ -693,6 +696,110 @@ extern "C" int mbx_disp_forces(mbx_context* ctx, int imcon, const double* cell, 
     for (int q = 0; q < 9; ++q) stress[q] += out[2 + q];
     if (jpot)
         for (int q = 0; q < 3; ++q) jpot[q] += out[11 + q];
+    return MBX_OK;
+}
+
+extern "C" int mbx_water_forces(mbx_context* ctx, int precision, int imcon, const double* cell, int nttm2,
+                                const int* listttm2, int nang, const int* listang, const int* ltype,
+                                const int* molecule, int natms, const double* xxx, const double* yyy,
+                                const double* zzz, double* fxx, double* fyy, double* fzz, const double* vxx,
+                                const double* vyy, const double* vzz, const double* weight, double* atomic_energy,
+                                double* scalars) {
+    if (!ctx) return MBX_ERR_ARG;
+    if (nttm2 < 0 || nttm2 % 3 || nang < 0 || natms < nttm2 || (nttm2 && !listttm2) || (nang && !listang) || !xxx ||
+        !yyy || !zzz || !fxx || !fyy || !fzz)
+        return fail(ctx, MBX_ERR_ARG, "bad argument");
+    for (int t = 0; t < nttm2; ++t)
+        if (listttm2[t] < 1 || listttm2[t] > natms || (t % 3 && listttm2[t] != listttm2[t - t % 3] + t % 3))
+            return fail(ctx, MBX_ERR_ARG, "listttm2[%d]=%d: water atoms must be 1-based, O,H1,H2 consecutive", t,
+                        listttm2[t]);
+    for (int q = 0; q < 3 * nang; ++q)
+        if (listang[q] < 1 || listang[q] > natms) return fail(ctx, MBX_ERR_ARG, "listang[%d] out of range", q);
+    const bool disp = ltype && molecule;
+    if (disp && !ctx->disp.vvv) return fail(ctx, MBX_ERR_ARG, "dispersion asked for before mbx_disp_setup");
+    CK(cudaSetDevice(ctx->device));
+    const int nw = nttm2 / 3;
+    int rc = reserve_water(ctx, std::max(nw, 1), std::max(natms, 1));
+    if (rc) return rc;
+    const size_t nint = (size_t)nttm2 + 3 * (size_t)nang + 2 * (size_t)natms + 1;
+    if (nint > ctx->ints_cap) {
+        if (ctx->ints) cudaFree(ctx->ints);
+        ctx->ints = nullptr;
+        CK(cudaMalloc(&ctx->ints, nint * sizeof(int)));
+        ctx->ints_cap = nint;
+    }
+    int* d_lst = ctx->ints;
+    int* d_ang = d_lst + nttm2;
+    int* d_typ = d_ang + 3 * (size_t)nang;
+    int* d_mol = d_typ + natms;
+    const bool heat = vxx && vyy && vzz && weight;
+    cudaStream_t s = ctx->stream;
+    const size_t nb = (size_t)natms * sizeof(double);
+    double* d = ctx->atoms;
+    double *dx = d, *dy = d + natms, *dz = d + 2 * (size_t)natms;
+    double *dvx = d + 3 * (size_t)natms, *dvy = d + 4 * (size_t)natms, *dvz = d + 5 * (size_t)natms;
+    double* dm = d + 6 * (size_t)natms;
+    double *dfx = d + 7 * (size_t)natms, *dfy = d + 8 * (size_t)natms, *dfz = d + 9 * (size_t)natms;
+    double* dae = d + 10 * (size_t)natms;
+    // one copy of every input, one zeroing of the outputs
+    if (nttm2) CK(cudaMemcpyAsync(d_lst, listttm2, nttm2 * sizeof(int), cudaMemcpyHostToDevice, s));
+    if (nang) CK(cudaMemcpyAsync(d_ang, listang, 3 * (size_t)nang * sizeof(int), cudaMemcpyHostToDevice, s));
+    if (disp) {
+        CK(cudaMemcpyAsync(d_typ, ltype, natms * sizeof(int), cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(d_mol, molecule, natms * sizeof(int), cudaMemcpyHostToDevice, s));
+    }
+    CK(cudaMemcpyAsync(dx, xxx, nb, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(dy, yyy, nb, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(dz, zzz, nb, cudaMemcpyHostToDevice, s));
+    if (heat) {
+        CK(cudaMemcpyAsync(dvx, vxx, nb, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(dvy, vyy, nb, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(dvz, vzz, nb, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(dm, weight, nb, cudaMemcpyHostToDevice, s));
+    }
+    CK(cudaMemsetAsync(dfx, 0, 3 * nb, s));
+    // per-atom energies are needed on the device for jkin even when the caller passes none
+    CK(cudaMemsetAsync(dae, 0, nb, s));
+    double sc[MBX_NWATERSCALARS];
+    std::memset(sc, 0, sizeof sc);
+    // 1-body, then dispersion, then MB-pol: jkin (at the end of the MB-pol evaluation)
+    // sees every term's per-atom energy
+    if (nang) {
+        rc = mbx_ps_pes_forces_device(ctx, imcon, cell, nang, d_ang, natms, dx, dy, dz, dfx, dfy, dfz,
+                                      heat ? dvx : nullptr, heat ? dvy : nullptr, heat ? dvz : nullptr, dae,
+                                      sc + MBX_NSCALARS);
+        if (rc) return rc;
+    }
+    if (disp && natms) {
+        if (ctx->disp_types_h.size() != (size_t)natms || !std::equal(ltype, ltype + natms, ctx->disp_types_h.begin()) ||
+            !std::equal(molecule, molecule + natms, ctx->disp_mol_h.begin())) {
+            ctx->disp.valid = false;
+            ctx->disp_types_h.assign(ltype, ltype + natms);
+            ctx->disp_mol_h.assign(molecule, molecule + natms);
+        }
+        rc = mbx_disp_forces_device(ctx, imcon, cell, natms, d_typ, d_mol, dx, dy, dz, dfx, dfy, dfz,
+                                    heat ? dvx : nullptr, heat ? dvy : nullptr, heat ? dvz : nullptr, dae,
+                                    sc + MBX_NSCALARS + 14);
+        if (rc) return rc;
+    }
+    Cell cl;
+    rc = make_cell(ctx, imcon, cell, cl);
+    if (rc) return rc;
+    rc = run_mbpol(ctx, precision, cl, nw, d_lst, natms, dx, dy, dz, dfx, dfy, dfz, heat ? dvx : nullptr,
+                   heat ? dvy : nullptr, heat ? dvz : nullptr, heat ? dm : nullptr, dae, sc);
+    if (rc) return rc;
+    std::vector<double> h(4 * (size_t)natms);
+    if (natms) {
+        CK(cudaMemcpyAsync(h.data(), dfx, (atomic_energy ? 4 : 3) * nb, cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+    }
+    for (int i = 0; i < natms; ++i) {
+        fxx[i] += h[i];
+        fyy[i] += h[natms + i];
+        fzz[i] += h[2 * (size_t)natms + i];
+        if (atomic_energy) atomic_energy[i] += h[3 * (size_t)natms + i];
+    }
+    if (scalars) std::memcpy(scalars, sc, sizeof sc);
     return MBX_OK;
 }
 

@@ -19,6 +19,7 @@ FP64 = 0
 MIXED = 1
 NSCALARS = 18
 NBOXSCALARS = NSCALARS + 14
+NWATERSCALARS = NSCALARS + 28
 S_ENG2, S_ENG3, S_VIR, S_STRESS, S_JPOT, S_JKIN = 0, 1, 2, 3, 12, 15
 
 _D = C.POINTER(C.c_double)
@@ -80,6 +81,8 @@ def load(path=None):
     L.mbx_server_error.restype = C.c_char_p
     L.mbx_mbpol_multi.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, _I, _D] + [_D] * 12
     L.mbx_mbpol_multi_device.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, _I, _D] + [C.c_void_p] * 11 + [_D]
+    L.mbx_water_forces.argtypes = [C.c_void_p, C.c_int, C.c_int, _D, C.c_int, _I, C.c_int, _I, _I, _I, C.c_int] + \
+        [_D] * 12
     L.mbx_disp_setup.argtypes = [C.c_void_p, C.c_int, _D, C.c_double, C.c_double, C.c_int]
     L.mbx_disp_forces.argtypes = [C.c_void_p, C.c_int, _D, C.c_int, _I, _I] + [_D] * 14
     L.mbx_disp_forces_device.argtypes = [C.c_void_p, C.c_int, _D, C.c_int] + [C.c_void_p] * 12 + [_D]
@@ -243,6 +246,28 @@ class Context:
                                              *xyz_ptrs, *f_ptrs, *v_ptrs, mass_ptr, ae_ptr, _p(sc))
         self._check(rc, "mbx_mbpol_multi_device")
         return sc
+
+    def water_forces(self, box, precision=FP64, heat=True, dispersion=False):
+        """1-body + (dispersion) + MB-pol of one box in one call (host arrays)."""
+        n = box.natms
+        x, y, z = (_f64(box.xyz[:, k]) for k in range(3))
+        f = np.zeros((3, n))
+        ae = np.zeros(n)
+        sc = np.zeros(NWATERSCALARS)
+        v = [_f64(box.vel[:, k]) for k in range(3)] if heat else [None] * 3
+        m = _f64(box.mass) if heat else None
+        lst = np.ascontiguousarray(box.listttm2(), dtype=np.int32)
+        ang = np.ascontiguousarray(box.listang(), dtype=np.int32)
+        lt = mo = None
+        if dispersion:
+            from mbx import systems
+            lt, mo = systems.water_types(box)
+        rc = self.lib.mbx_water_forces(self.h, precision, box.imcon, _p(_f64(box.cell)), 3 * box.nw, _p(lst, _I),
+                                       box.nw, _p(ang, _I), _p(lt, _I), _p(mo, _I), n, _p(x), _p(y), _p(z),
+                                       _p(f[0]), _p(f[1]), _p(f[2]), _p(v[0]), _p(v[1]), _p(v[2]), _p(m), _p(ae),
+                                       _p(sc))
+        self._check(rc, "mbx_water_forces")
+        return dict(forces=f.T.copy(), atomic_energy=ae, scalars=sc)
 
     def disp_setup(self, prm, rcut=9.0, delr=1.0, mxgrid=0, ntypes=None):
         prm = _f64(prm).reshape(-1, 4)

@@ -238,6 +238,26 @@ int mbx_set_graphs(mbx_context* ctx, int on);
 long mbx_graph_launches(const mbx_context* ctx);
 
 /*
+ * The water force field of one MD step in one call: the 1-body term (as
+ * mbx_ps_pes_forces), the dispersion term when ltype and molecule are given (as
+ * mbx_disp_forces, after mbx_disp_setup), then the MB-pol 2B/3B terms (as
+ * mbx_mbpol_forces), with the heat current.  Replaces the angfrc (keya 9), srfrce2 and
+ * mbpol_forces calls of one force evaluation (SOURCE/dlpoly_cmd.f:2430, SOURCE/forces.f:552,
+ * SOURCE/dlpoly_cmd.f:2504); every input is copied to the device once and the forces and
+ * per-atom energies come back once.  Host arrays; forces and atomic_energy ACCUMULATED.
+ * jkin (scalars[MBX_S_JKIN..]) uses the per-atom energies of every term in the call.
+ *   scalars[MBX_NWATERSCALARS] (or NULL): the MB-pol block (MBX_S_*), then engang,
+ *   virang, stress[9], jpot[3] of the 1-body term, then engsrp, virsrp, stress[9],
+ *   jpot[3] of the dispersion term (zeros without it).
+ */
+#define MBX_NWATERSCALARS (MBX_NSCALARS + 28)
+int mbx_water_forces(mbx_context* ctx, int precision, int imcon, const double* cell, int nttm2, const int* listttm2,
+                     int nang, const int* listang, const int* ltype, const int* molecule, int natms,
+                     const double* xxx, const double* yyy, const double* zzz, double* fxx, double* fyy, double* fzz,
+                     const double* vxx, const double* vyy, const double* vzz, const double* weight,
+                     double* atomic_energy, double* scalars);
+
+/*
  * Short-range dispersion: DL_POLY van der Waals type 12, Tang-Toennies damped
  * -C6 f6(a6 r)/r^6 - C8 f8(a8 r)/r^8.  Replaces forgen's type-12 tables
  * (SOURCE/forgen.f:97, :262-270, :337-357), the Verlet list of parlst with the

@@ -275,3 +275,34 @@ def test_fused_kernel_matches_separate_kernels(precision):
         assert abs(fused[k] - sep[k]) <= tol * abs(sep[k]), k
     for k in ("forces", "atomic_energy", "stress", "jpot", "jkin"):
         assert rel_err(fused[k], sep[k]) <= tol, k
+
+
+@pytest.mark.parametrize("precision", [capi.FP64, capi.MIXED])
+def test_water_forces_one_call_matches_the_separate_calls(precision):
+    """mbx_water_forces = 1-body + dispersion + MB-pol through the separate entry points;
+    jkin sees every term's per-atom energy."""
+    box = systems.config0()
+    lt, mol = systems.water_types(box)
+    ctx = capi.Context(0)
+    try:
+        ctx.disp_setup(systems.DISP_PARAMS_SYNTHETIC, rcut=9.0, delr=1.0)
+        one = ctx.water_forces(box, precision=precision, dispersion=True)
+        pes = ctx.ps_pes(box)
+        disp = ctx.dispersion(box, lt, mol)
+        mb = ctx.mbpol_forces(box, precision=precision)
+    finally:
+        ctx.close()
+    tol = 1e-11
+    ref_f = pes["forces"] + disp["forces"] + mb["forces"]
+    assert rel_err(one["forces"], ref_f) <= tol
+    ref_ae = pes["atomic_energy"] + disp["atomic_energy"] + mb["atomic_energy"]
+    assert rel_err(one["atomic_energy"], ref_ae) <= tol
+    sc = one["scalars"]
+    assert abs(sc[capi.S_ENG3] - mb["eng3"]) <= tol * abs(mb["eng3"])
+    assert abs(sc[capi.NSCALARS] - pes["engang"]) <= tol * abs(pes["engang"])
+    assert abs(sc[capi.NSCALARS + 14] - disp["eng"]) <= tol * abs(disp["eng"])
+    assert rel_err(sc[capi.NSCALARS + 25:capi.NSCALARS + 28], disp["jpot"]) <= tol
+    nw3 = 3 * box.nw
+    m, v = box.mass[:nw3], box.vel[:nw3]
+    eng = 0.5 * m * (v * v).sum(1) + ref_ae[:nw3]
+    assert rel_err(sc[capi.S_JKIN:capi.S_JKIN + 3], (eng[:, None] * v).sum(0)) <= tol
