@@ -120,23 +120,14 @@ struct mbx_server {
             ang[3 * i + 1] = 3 * i + 1;
             ang[3 * i + 2] = 3 * i + 3;
         }
-        double eng = 0, vir = 0, stress[9] = {0}, eang = 0, vang = 0, sang[9] = {0}, jp[3] = {0};
-        const double* vx = r.heat ? r.vx.data() : nullptr;
-        const double* vy = r.heat ? r.vy.data() : nullptr;
-        const double* vz = r.heat ? r.vz.data() : nullptr;
-        int rc = mbx_ps_pes_forces(ctx, r.imcon, r.cell, nw, ang.data(), n, r.x.data(), r.y.data(), r.z.data(),
-                                   r.fx.data(), r.fy.data(), r.fz.data(), &eang, &vang, sang, vx, vy, vz, r.ae.data(),
-                                   jp);
-        if (rc == MBX_OK)
-            rc = mbx_mbpol_forces(ctx, r.precision, r.imcon, r.cell, 3 * nw, lst.data(), n, r.x.data(), r.y.data(),
-                                  r.z.data(), r.fx.data(), r.fy.data(), r.fz.data(), &eng, &vir, stress, vx, vy, vz,
-                                  r.heat ? r.mass.data() : nullptr, r.ae.data(), r.scalars);
-        r.status = rc;
-        // scalars: the MB-pol block, then {engang, virang, stress[9], jpot[3]} of the 1-body term
-        r.scalars[MBX_NSCALARS + 0] = eang;
-        r.scalars[MBX_NSCALARS + 1] = vang;
-        for (int q = 0; q < 9; ++q) r.scalars[MBX_NSCALARS + 2 + q] = sang[q];
-        for (int q = 0; q < 3; ++q) r.scalars[MBX_NSCALARS + 11 + q] = jp[q];
+        // 1-body + MB-pol in one call; scalars: the MB-pol block, then the 1-body block
+        double sc[MBX_NWATERSCALARS];
+        r.status = mbx_water_forces(ctx, r.precision, r.imcon, r.cell, 3 * nw, lst.data(), nw, ang.data(), nullptr,
+                                    nullptr, n, r.x.data(), r.y.data(), r.z.data(), r.fx.data(), r.fy.data(),
+                                    r.fz.data(), r.heat ? r.vx.data() : nullptr, r.heat ? r.vy.data() : nullptr,
+                                    r.heat ? r.vz.data() : nullptr, r.heat ? r.mass.data() : nullptr, r.ae.data(),
+                                    sc);
+        std::memcpy(r.scalars, sc, sizeof r.scalars);
     }
 };
 
