@@ -68,6 +68,49 @@ __device__ __forceinline__ bool dimer_in(double r2) { return !(r2 > kR2f * kR2f)
 // 3B pair test of do_trimer (SOURCE/mbpol.f90:839-862): the distance itself is compared.
 __device__ __forceinline__ bool tri_edge(double r2) { return !(__dsqrt_rn(r2) > kR3f); }
 
+// FP32 |image(a - b)|^2 of two O positions, for list pre-tests only.
+__device__ __forceinline__ float dist2_img_f(const Cell& cl, float4 a, float4 b) {
+    float dx = a.x - b.x, dy = a.y - b.y, dz = a.z - b.z;
+    if (cl.imcon == 1 || cl.imcon == 2) {
+        dx -= (float)cl.c[0] * rintf(dx * (float)cl.inv[0]);
+        dy -= (float)cl.c[4] * rintf(dy * (float)cl.inv[1]);
+        dz -= (float)cl.c[8] * rintf(dz * (float)cl.inv[2]);
+    } else {
+        const double* r = cl.rc;
+        const double* c = cl.c;
+        float sx = (float)r[0] * dx + (float)r[3] * dy + (float)r[6] * dz;
+        float sy = (float)r[1] * dx + (float)r[4] * dy + (float)r[7] * dz;
+        float sz = (float)r[2] * dx + (float)r[5] * dy + (float)r[8] * dz;
+        sx -= rintf(sx);
+        sy -= rintf(sy);
+        sz -= rintf(sz);
+        dx = (float)c[0] * sx + (float)c[3] * sy + (float)c[6] * sz;
+        dy = (float)c[1] * sx + (float)c[4] * sy + (float)c[7] * sz;
+        dz = (float)c[2] * sx + (float)c[5] * sy + (float)c[8] * sz;
+    }
+    return dx * dx + dy * dy + dz * dz;
+}
+
+// The two list tests of a water pair: the dimer test of do_dimer (r^2 <= 6.5^2) and the
+// 3B edge test of do_trimer (r <= 4.5).  They are decided in FP32 (from the FP32 copies
+// `of` of the O positions) when r^2 is more than 0.05 A^2 from both cutoffs -- far above
+// FP32 rounding, which also covers an image chosen differently at half a box length,
+// where both images have the same length -- and with the reference's FP64 arithmetic
+// otherwise, so the lists are the reference's.
+__device__ __forceinline__ void pair_tests(const Cell& cl, const float4* of, const double* mono, int i, int j,
+                                           bool& in2, bool& in3) {
+    const float r2f = dist2_img_f(cl, of[i], of[j]);
+    const float c2 = (float)(kR2f * kR2f), c3 = (float)(kR3f * kR3f);
+    if (fabsf(r2f - c2) < 0.05f || fabsf(r2f - c3) < 0.05f) {
+        const double r2 = dist2_img(cl, mono + 9 * (size_t)i, mono + 9 * (size_t)j);
+        in2 = dimer_in(r2);
+        in3 = tri_edge(r2);
+    } else {
+        in2 = r2f < c2;
+        in3 = r2f < c3;
+    }
+}
+
 template <typename T>
 __device__ __forceinline__ T warp_sum(T v) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);

@@ -113,6 +113,7 @@ struct ListBuilder {
     int *idx = nullptr, *sidx = nullptr, *cstart = nullptr, *cend = nullptr;
     int *n2 = nullptr, *l2 = nullptr, *off2 = nullptr, *n3 = nullptr, *l3 = nullptr;
     int *tcnt = nullptr, *toff = nullptr, *flag = nullptr;
+    float4* of = nullptr;   // FP32 copies of the imaged O positions (list pre-tests)
     void *scan_tmp = nullptr, *sort_tmp = nullptr;
     size_t scan_bytes = 0, sort_bytes = 0;
     int3 nc_last = {1, 1, 1};
@@ -182,6 +183,7 @@ struct MultiBoxes {
     Cell* cells = nullptr;
     int *bstart = nullptr, *bcount = nullptr;
     double* mono = nullptr;
+    float4* of = nullptr;          // FP32 copies of the imaged O positions (list pre-tests)
     int *n2 = nullptr, *l2 = nullptr, *off2 = nullptr, *n3 = nullptr, *l3 = nullptr, *tcnt = nullptr,
         *toff = nullptr;
     int2* pairs = nullptr;

@@ -22,7 +22,7 @@ namespace mbx {
 // mbpol_forces (SOURCE/mbpol.f90:194-200): listttm2 is 1-based.
 __global__ void k_image_monomers(int nw, const int* __restrict__ list, const double* __restrict__ x,
                                  const double* __restrict__ y, const double* __restrict__ z, Cell cl,
-                                 double* __restrict__ mono) {
+                                 double* __restrict__ mono, float4* __restrict__ of) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nw) return;
     double w[9];
@@ -43,6 +43,7 @@ __global__ void k_image_monomers(int nw, const int* __restrict__ list, const dou
     }
 #pragma unroll
     for (int q = 0; q < 9; ++q) mono[9 * (size_t)i + q] = w[q];
+    of[i] = make_float4((float)w[0], (float)w[1], (float)w[2], 0.f);
 }
 
 __device__ __forceinline__ int wrap_cell(double s, int nc) {
@@ -77,7 +78,8 @@ __global__ void k_cell_bounds(int nw, int ncell, const unsigned* __restrict__ sk
 // order through a warp ballot, so the lists are deterministic.  Candidates come from
 // the 27 surrounding cells (in a fixed order, waters by index within a cell), or from
 // every water when the grid is too coarse (all_pairs).
-__global__ void k_neighbours(int nw, const double* __restrict__ mono, Cell cl, int3 nc, int all_pairs,
+__global__ void k_neighbours(int nw, const double* __restrict__ mono, const float4* __restrict__ of, Cell cl,
+                             int3 nc, int all_pairs,
                              const unsigned* __restrict__ skey, const int* __restrict__ sidx,
                              const int* __restrict__ cstart, const int* __restrict__ cend, int cap2, int cap3,
                              int* __restrict__ n2, int* __restrict__ l2, int* __restrict__ n3,
@@ -135,9 +137,8 @@ __global__ void k_neighbours(int nw, const double* __restrict__ mono, Cell cl, i
         }
         bool in2 = false, in3 = false;
         if (j >= 0 && j != i) {
-            const double r2 = dist2_img(cl, oi, mono + 9 * (size_t)j);
-            in2 = j > i && dimer_in(r2);
-            in3 = tri_edge(r2);
+            pair_tests(cl, of, mono, i, j, in2, in3);
+            in2 = in2 && j > i;
         }
         const unsigned b2 = __ballot_sync(0xffffffffu, in2);
         const unsigned b3 = __ballot_sync(0xffffffffu, in3);
@@ -175,7 +176,8 @@ __global__ void k_pairs_compact(int nw, int cap2, const int* __restrict__ n2, co
 // pairs (p < q) of the neighbour list in parallel, 32 pairs per step in lexicographic
 // order (the FP64 distance tests keep every lane busy); hits are appended in pair order.
 template <bool FILL>
-__global__ void k_trimers(int nw, const double* __restrict__ mono, Cell cl, int cap3, const int* __restrict__ n3,
+__global__ void k_trimers(int nw, const double* __restrict__ mono, const float4* __restrict__ of, Cell cl, int cap3,
+                          const int* __restrict__ n3,
                           const int* __restrict__ l3, int* __restrict__ cnt, const int* __restrict__ off,
                           int4* __restrict__ trip) {
     const int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -195,7 +197,8 @@ __global__ void k_trimers(int nw, const double* __restrict__ mono, Cell cl, int 
             pair_of_index(n, k, p, q);
             a = nb[p];
             b = nb[q];
-            const bool ab = tri_edge(dist2_img(cl, mono + 9 * (size_t)a, mono + 9 * (size_t)b));
+            bool in2, ab;
+            pair_tests(cl, of, mono, a, b, in2, ab);
             keep = !(ab && (a < c || b < c));
         }
         const unsigned bal = __ballot_sync(0xffffffffu, keep);
@@ -229,7 +232,7 @@ void ListBuilder::release() {
     if (external) return;
     free_t(key); free_t(skey); free_t(idx); free_t(sidx); free_t(cstart); free_t(cend);
     free_t(n2); free_t(l2); free_t(off2); free_t(n3); free_t(l3); free_t(tcnt); free_t(toff);
-    free_t(flag); free_ptr(scan_tmp); free_ptr(sort_tmp);
+    free_t(flag); free_t(of); free_ptr(scan_tmp); free_ptr(sort_tmp);
     nw_cap = ncell_cap = 0;
     cap2_alloc = cap3_alloc = 0;
 }
@@ -239,7 +242,7 @@ cudaError_t ListBuilder::reserve(int nw, int ncell) {
     if (external) return (nw <= nw_cap && ncell <= ncell_cap) ? cudaSuccess : cudaErrorInvalidValue;
     if (nw > nw_cap || cap2 != cap2_alloc || cap3 != cap3_alloc) {
         free_t(key); free_t(skey); free_t(idx); free_t(sidx);
-        free_t(n2); free_t(l2); free_t(off2); free_t(n3); free_t(l3); free_t(tcnt); free_t(toff);
+        free_t(n2); free_t(l2); free_t(off2); free_t(n3); free_t(l3); free_t(tcnt); free_t(toff); free_t(of);
         free_ptr(scan_tmp); free_ptr(sort_tmp);
         const int n = std::max(nw, nw_cap) + 1;
         if ((e = cudaMalloc(&key, n * sizeof(unsigned)))) return e;
@@ -253,6 +256,7 @@ cudaError_t ListBuilder::reserve(int nw, int ncell) {
         if ((e = cudaMalloc(&toff, n * sizeof(int)))) return e;
         if ((e = cudaMalloc(&l2, (size_t)n * cap2 * sizeof(int)))) return e;
         if ((e = cudaMalloc(&l3, (size_t)n * cap3 * sizeof(int)))) return e;
+        if ((e = cudaMalloc(&of, (size_t)n * sizeof(float4)))) return e;
         size_t a = 0, b = 0;
         if ((e = cub::DeviceScan::ExclusiveSum(nullptr, a, n2, off2, n))) return e;
         if ((e = cub::DeviceRadixSort::SortPairs(nullptr, b, key, skey, idx, sidx, n))) return e;
@@ -301,7 +305,7 @@ cudaError_t ListBuilder::phase1(int nw, const int* list, const double* x, const 
     // is a histogram, an exclusive-sum and one pass per 8-bit digit.
     launches_last = 1 + 1 + 2 + 1 + 2 + 1;
     const int g = grid_for(nw);
-    k_image_monomers<<<g, kThreads, 0, s>>>(nw, list, x, y, z, cl, mono);
+    k_image_monomers<<<g, kThreads, 0, s>>>(nw, list, x, y, z, cl, mono, of);
     if (!all_pairs) {
         cudaMemsetAsync(cstart, 0, ncell * sizeof(int), s);
         cudaMemsetAsync(cend, 0, ncell * sizeof(int), s);
@@ -315,11 +319,11 @@ cudaError_t ListBuilder::phase1(int nw, const int* list, const double* x, const 
     }
     cudaMemsetAsync(flag, 0, sizeof(int), s);
     const int gw = (int)(((long)nw * 32 + kThreads - 1) / kThreads);   // one warp per water
-    k_neighbours<<<gw, kThreads, 0, s>>>(nw, mono, cl, nc, all_pairs, skey, sidx, cstart, cend, cap2, cap3, n2, l2,
+    k_neighbours<<<gw, kThreads, 0, s>>>(nw, mono, of, cl, nc, all_pairs, skey, sidx, cstart, cend, cap2, cap3, n2, l2,
                                          n3, l3, flag);
     size_t a = scan_bytes;
     cub::DeviceScan::ExclusiveSum(scan_tmp, a, n2, off2, nw, s);
-    k_trimers<false><<<gw, kThreads, 0, s>>>(nw, mono, cl, cap3, n3, l3, tcnt, nullptr, nullptr);
+    k_trimers<false><<<gw, kThreads, 0, s>>>(nw, mono, of, cl, cap3, n3, l3, tcnt, nullptr, nullptr);
     a = scan_bytes;
     cub::DeviceScan::ExclusiveSum(scan_tmp, a, tcnt, toff, nw, s);
     k_list_totals<<<1, 1, 0, s>>>(nw, n2, off2, tcnt, toff, flag, totals_dev);
@@ -331,7 +335,7 @@ cudaError_t ListBuilder::phase2(int nw, const Cell& cl, const double* mono, int2
     const int g = grid_for(nw);
     k_pairs_compact<<<g, kThreads, 0, s>>>(nw, cap2, n2, off2, l2, pairs);
     const int gw = (int)(((long)nw * 32 + kThreads - 1) / kThreads);
-    k_trimers<true><<<gw, kThreads, 0, s>>>(nw, mono, cl, cap3, n3, l3, nullptr, toff, trip);
+    k_trimers<true><<<gw, kThreads, 0, s>>>(nw, mono, of, cl, cap3, n3, l3, nullptr, toff, trip);
     launches_last += 2;
     return cudaGetLastError();
 }

@@ -17,7 +17,8 @@ namespace {
 
 __global__ void k_multi_mono(int nw, const int* __restrict__ list, const int* __restrict__ wbox,
                              const Cell* __restrict__ cells, const double* __restrict__ x,
-                             const double* __restrict__ y, const double* __restrict__ z, double* __restrict__ mono) {
+                             const double* __restrict__ y, const double* __restrict__ z, double* __restrict__ mono,
+                             float4* __restrict__ of) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nw) return;
     const Cell& cl = cells[wbox[i]];
@@ -39,10 +40,12 @@ __global__ void k_multi_mono(int nw, const int* __restrict__ list, const int* __
     }
 #pragma unroll
     for (int q = 0; q < 9; ++q) mono[9 * (size_t)i + q] = w[q];
+    of[i] = make_float4((float)w[0], (float)w[1], (float)w[2], 0.f);
 }
 
 // One warp per water: dimer partners j > i and 3B neighbours among the waters of its box.
-__global__ void k_multi_neighbours(int nw, const double* __restrict__ mono, const int* __restrict__ wbox,
+__global__ void k_multi_neighbours(int nw, const double* __restrict__ mono, const float4* __restrict__ of,
+                                   const int* __restrict__ wbox,
                                    const Cell* __restrict__ cells, const int* __restrict__ bstart,
                                    const int* __restrict__ bcount, int cap2, int cap3, int* __restrict__ n2,
                                    int* __restrict__ l2, int* __restrict__ n3, int* __restrict__ l3,
@@ -53,7 +56,6 @@ __global__ void k_multi_neighbours(int nw, const double* __restrict__ mono, cons
     const int b = wbox[i];
     const Cell& cl = cells[b];
     const int j0 = bstart[b], nb = bcount[b];
-    const double* oi = mono + 9 * (size_t)i;
     int* my2 = l2 + (size_t)i * cap2;
     int* my3 = l3 + (size_t)i * cap3;
     int c2 = 0, c3 = 0;
@@ -62,9 +64,8 @@ __global__ void k_multi_neighbours(int nw, const double* __restrict__ mono, cons
         const int j = j0 + k;
         bool in2 = false, in3 = false;
         if (k < nb && j != i) {
-            const double r2 = dist2_img(cl, oi, mono + 9 * (size_t)j);
-            in2 = j > i && dimer_in(r2);
-            in3 = tri_edge(r2);
+            pair_tests(cl, of, mono, i, j, in2, in3);
+            in2 = in2 && j > i;
         }
         const unsigned b2 = __ballot_sync(0xffffffffu, in2);
         const unsigned b3 = __ballot_sync(0xffffffffu, in3);
@@ -90,7 +91,8 @@ __global__ void k_multi_neighbours(int nw, const double* __restrict__ mono, cons
 // Trimers of each centre (one warp per centre), as the single-box k_trimers, with the
 // centre's box cell; writes beyond `cap` are dropped and flagged.
 template <bool FILL>
-__global__ void k_multi_trimers(int nw, const double* __restrict__ mono, const int* __restrict__ wbox,
+__global__ void k_multi_trimers(int nw, const double* __restrict__ mono, const float4* __restrict__ of,
+                                const int* __restrict__ wbox,
                                 const Cell* __restrict__ cells, int cap3, const int* __restrict__ n3,
                                 const int* __restrict__ l3, int* __restrict__ cnt, const int* __restrict__ off,
                                 int4* __restrict__ trip, long cap, int* __restrict__ overflow) {
@@ -112,7 +114,8 @@ __global__ void k_multi_trimers(int nw, const double* __restrict__ mono, const i
             pair_of_index(n, k, p, q);
             a = nb[p];
             b = nb[q];
-            const bool ab = tri_edge(dist2_img(cl, mono + 9 * (size_t)a, mono + 9 * (size_t)b));
+            bool in2, ab;
+            pair_tests(cl, of, mono, a, b, in2, ab);
             keep = !(ab && (a < c || b < c));
         }
         const unsigned bal = __ballot_sync(0xffffffffu, keep);
@@ -190,7 +193,7 @@ MultiBoxes::~MultiBoxes() { release(); }
 void MultiBoxes::release() {
     void* ptrs[] = {list,  listang, wbox,  abox,     is_water, cells,   bstart,     bcount, mono,   n2,
                     l2,    off2,    n3,    l3,       tcnt,     toff,    pairs,      trip,   hard2,  hard3,
-                    hard_count, scan_tmp, acc_box, pes_box, ae_scratch, totals, flag, ctr, partial, done};
+                    hard_count, scan_tmp, acc_box, pes_box, ae_scratch, totals, flag, ctr, partial, done, of};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     list = listang = wbox = abox = bstart = bcount = n2 = l2 = off2 = n3 = l3 = tcnt = toff = nullptr;
@@ -200,6 +203,7 @@ void MultiBoxes::release() {
     is_water = nullptr;
     cells = nullptr;
     mono = acc_box = pes_box = ae_scratch = nullptr;
+    of = nullptr;
     pairs = hard2 = nullptr;
     trip = hard3 = nullptr;
     scan_tmp = nullptr;
@@ -260,6 +264,7 @@ cudaError_t MultiBoxes::setup(int nbox_, const int* nw_box, bool need_hard, cuda
     if ((e = cudaMalloc(&bstart, (size_t)nbox * sizeof(int)))) return e;
     if ((e = cudaMalloc(&bcount, (size_t)nbox * sizeof(int)))) return e;
     if ((e = cudaMalloc(&mono, 9 * n * sizeof(double)))) return e;
+    if ((e = cudaMalloc(&of, n * sizeof(float4)))) return e;
     if ((e = cudaMalloc(&n2, n * sizeof(int)))) return e;
     if ((e = cudaMalloc(&off2, n * sizeof(int)))) return e;
     if ((e = cudaMalloc(&n3, n * sizeof(int)))) return e;
@@ -324,17 +329,17 @@ cudaError_t MultiBoxes::enqueue(int precision, const MixedPass& limits, bool fus
     if ((e = cudaMemsetAsync(hard_count, 0, 2 * sizeof(int), s))) return e;
     if (nw == 0) return cudaSuccess;
     // cluster lists
-    k_multi_mono<<<blocks_for(nw), kThreads, 0, s>>>(nw, list, wbox, cells, x, y, z, mono);
-    k_multi_neighbours<<<blocks_for(32L * nw), kThreads, 0, s>>>(nw, mono, wbox, cells, bstart, bcount, cap2, cap3,
+    k_multi_mono<<<blocks_for(nw), kThreads, 0, s>>>(nw, list, wbox, cells, x, y, z, mono, of);
+    k_multi_neighbours<<<blocks_for(32L * nw), kThreads, 0, s>>>(nw, mono, of, wbox, cells, bstart, bcount, cap2, cap3,
                                                                   n2, l2, n3, l3, flag);
     size_t a = scan_bytes;
     if ((e = cub::DeviceScan::ExclusiveSum(scan_tmp, a, n2, off2, nw, s))) return e;
     launch_pairs_compact(nw, cap2, n2, off2, l2, pairs, s);
-    k_multi_trimers<false><<<blocks_for(32L * nw), kThreads, 0, s>>>(nw, mono, wbox, cells, cap3, n3, l3, tcnt,
+    k_multi_trimers<false><<<blocks_for(32L * nw), kThreads, 0, s>>>(nw, mono, of, wbox, cells, cap3, n3, l3, tcnt,
                                                                       nullptr, nullptr, 0, flag);
     a = scan_bytes;
     if ((e = cub::DeviceScan::ExclusiveSum(scan_tmp, a, tcnt, toff, nw, s))) return e;
-    k_multi_trimers<true><<<blocks_for(32L * nw), kThreads, 0, s>>>(nw, mono, wbox, cells, cap3, n3, l3, nullptr,
+    k_multi_trimers<true><<<blocks_for(32L * nw), kThreads, 0, s>>>(nw, mono, of, wbox, cells, cap3, n3, l3, nullptr,
                                                                      toff, trip, trip_cap, flag);
     k_multi_totals<<<1, 1, 0, s>>>(nw, n2, off2, tcnt, toff, pair_cap, trip_cap, totals, flag);
     launches += 6 + 2 * 2;   // own kernels + two CUB scans (two kernels each)

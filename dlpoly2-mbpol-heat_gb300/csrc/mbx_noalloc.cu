@@ -39,7 +39,8 @@ constexpr size_t oMono = 0;
 constexpr size_t oAcc = align256(oMono + 9 * sizeof(double) * kN);
 constexpr size_t oTotals = align256(oAcc + MBX_NSCALARS * sizeof(double));
 constexpr size_t oFlag = align256(oTotals + 4 * sizeof(int));
-constexpr size_t oCtr = align256(oFlag + 4 * sizeof(int));
+constexpr size_t oOf = align256(oFlag + 4 * sizeof(int));
+constexpr size_t oCtr = align256(oOf + kN * sizeof(float4));
 constexpr size_t oN2 = align256(oCtr + 4 * sizeof(int));
 constexpr size_t oOff2 = align256(oN2 + kN * sizeof(int));
 constexpr size_t oN3 = align256(oOff2 + kN * sizeof(int));
@@ -170,6 +171,7 @@ extern "C" int mbx_mbpol_forces_noalloc(int precision, int imcon, const double* 
         lb.l2 = (int*)(base + oL2);
         lb.l3 = (int*)(base + oL3);
         lb.flag = (int*)(base + oFlag);
+        lb.of = (float4*)(base + oOf);
         lb.scan_tmp = base + oScan;
         size_t need = 0;
         NA_CK(cub::DeviceScan::ExclusiveSum(nullptr, need, lb.n2, lb.off2, nw));   // size query only
