@@ -67,6 +67,8 @@ struct mbx_context {
     int* mint_h = nullptr;             // pinned: totals[2], flag, hand-off counts[2]
     int mbox_cap = 0;
     long graph_replays = 0;
+    double* hstage = nullptr;          // pinned host staging of per-atom results (4 * natms)
+    size_t hstage_cap = 0;
     int* ints = nullptr;               // mbx_water_forces staging: listttm2, listang, ltype, molecule
     size_t ints_cap = 0;
     DispState disp;                    // dispersion tables and Verlet list
@@ -141,6 +143,18 @@ int reserve_water(mbx_context* ctx, int nw, int natms) {
         ctx->natms_cap = natms;
     }
     return MBX_OK;
+}
+
+// Pinned host staging for copying per-atom results back (grown as needed).
+double* host_stage(mbx_context* ctx, size_t n) {
+    if (n > ctx->hstage_cap) {
+        if (ctx->hstage) cudaFreeHost(ctx->hstage);
+        ctx->hstage = nullptr;
+        ctx->hstage_cap = 0;
+        if (cudaMallocHost(&ctx->hstage, n * sizeof(double)) != cudaSuccess) return nullptr;
+        ctx->hstage_cap = n;
+    }
+    return ctx->hstage;
 }
 
 // The whole MB-pol evaluation on device arrays.
@@ -461,6 +475,7 @@ extern "C" void mbx_destroy(mbx_context* ctx) {
     if (ctx->cells_h) cudaFreeHost(ctx->cells_h);
     if (ctx->mout_h) cudaFreeHost(ctx->mout_h);
     if (ctx->mint_h) cudaFreeHost(ctx->mint_h);
+    if (ctx->hstage) cudaFreeHost(ctx->hstage);
     ctx->multi.release();
     ctx->disp.release();
     ctx->lb.release();
@@ -573,9 +588,10 @@ extern "C" int mbx_mbpol_forces(mbx_context* ctx, int precision, int imcon, cons
                    sc);
     if (rc) return rc;
     // bring the per-atom results back and accumulate into the caller's arrays
-    std::vector<double> h(4 * (size_t)natms);
-    CK(cudaMemcpyAsync(h.data(), dfx, 3 * nb, cudaMemcpyDeviceToHost, s));
-    if (atomic_energy) CK(cudaMemcpyAsync(h.data() + 3 * (size_t)natms, dae, nb, cudaMemcpyDeviceToHost, s));
+    double* h = host_stage(ctx, 4 * (size_t)natms + 1);
+    if (!h) return fail(ctx, MBX_ERR_CUDA, "pinned host staging allocation failed");
+    CK(cudaMemcpyAsync(h, dfx, 3 * nb, cudaMemcpyDeviceToHost, s));
+    if (atomic_energy) CK(cudaMemcpyAsync(h + 3 * (size_t)natms, dae, nb, cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     for (int i = 0; i < natms; ++i) {
         fxx[i] += h[i];
@@ -679,10 +695,11 @@ extern "C" int mbx_disp_forces(mbx_context* ctx, int imcon, const double* cell, 
                                 heat ? dvx : nullptr, heat ? dvy : nullptr, heat ? dvz : nullptr,
                                 atomic_energy ? dae : nullptr, out);
     if (rc) return rc;
-    std::vector<double> h(4 * (size_t)natms);
+    double* h = host_stage(ctx, 4 * (size_t)natms + 1);
+    if (!h) return fail(ctx, MBX_ERR_CUDA, "pinned host staging allocation failed");
     if (natms) {
-        CK(cudaMemcpyAsync(h.data(), dfx, 3 * nb, cudaMemcpyDeviceToHost, s));
-        if (atomic_energy) CK(cudaMemcpyAsync(h.data() + 3 * (size_t)natms, dae, nb, cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(h, dfx, 3 * nb, cudaMemcpyDeviceToHost, s));
+        if (atomic_energy) CK(cudaMemcpyAsync(h + 3 * (size_t)natms, dae, nb, cudaMemcpyDeviceToHost, s));
         CK(cudaStreamSynchronize(s));
     }
     for (int i = 0; i < natms; ++i) {
@@ -788,9 +805,10 @@ extern "C" int mbx_water_forces(mbx_context* ctx, int precision, int imcon, cons
     rc = run_mbpol(ctx, precision, cl, nw, d_lst, natms, dx, dy, dz, dfx, dfy, dfz, heat ? dvx : nullptr,
                    heat ? dvy : nullptr, heat ? dvz : nullptr, heat ? dm : nullptr, dae, sc);
     if (rc) return rc;
-    std::vector<double> h(4 * (size_t)natms);
+    double* h = host_stage(ctx, 4 * (size_t)natms + 1);
+    if (!h) return fail(ctx, MBX_ERR_CUDA, "pinned host staging allocation failed");
     if (natms) {
-        CK(cudaMemcpyAsync(h.data(), dfx, (atomic_energy ? 4 : 3) * nb, cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(h, dfx, (atomic_energy ? 4 : 3) * nb, cudaMemcpyDeviceToHost, s));
         CK(cudaStreamSynchronize(s));
     }
     for (int i = 0; i < natms; ++i) {
@@ -881,9 +899,10 @@ extern "C" int mbx_mbpol_multi(mbx_context* ctx, int precision, int imcon, int n
                    heat ? dvy : nullptr, heat ? dvz : nullptr, heat ? dm : nullptr, atomic_energy ? dae : nullptr,
                    scalars);
     if (rc || !natms) return rc;
-    std::vector<double> h(4 * (size_t)natms);
-    CK(cudaMemcpyAsync(h.data(), dfx, 3 * nb, cudaMemcpyDeviceToHost, s));
-    if (atomic_energy) CK(cudaMemcpyAsync(h.data() + 3 * (size_t)natms, dae, nb, cudaMemcpyDeviceToHost, s));
+    double* h = host_stage(ctx, 4 * (size_t)natms + 1);
+    if (!h) return fail(ctx, MBX_ERR_CUDA, "pinned host staging allocation failed");
+    CK(cudaMemcpyAsync(h, dfx, 3 * nb, cudaMemcpyDeviceToHost, s));
+    if (atomic_energy) CK(cudaMemcpyAsync(h + 3 * (size_t)natms, dae, nb, cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     for (int i = 0; i < natms; ++i) {
         fxx[i] += h[i];
@@ -957,9 +976,10 @@ extern "C" int mbx_ps_pes_forces(mbx_context* ctx, int imcon, const double* cell
                                   heat ? dvx : nullptr, heat ? dvy : nullptr, heat ? dvz : nullptr,
                                   atomic_energy ? dae : nullptr, out);
     if (rc) return rc;
-    std::vector<double> h(4 * (size_t)natms);
-    CK(cudaMemcpyAsync(h.data(), dfx, 3 * nb, cudaMemcpyDeviceToHost, s));
-    if (atomic_energy) CK(cudaMemcpyAsync(h.data() + 3 * (size_t)natms, dae, nb, cudaMemcpyDeviceToHost, s));
+    double* h = host_stage(ctx, 4 * (size_t)natms + 1);
+    if (!h) return fail(ctx, MBX_ERR_CUDA, "pinned host staging allocation failed");
+    CK(cudaMemcpyAsync(h, dfx, 3 * nb, cudaMemcpyDeviceToHost, s));
+    if (atomic_energy) CK(cudaMemcpyAsync(h + 3 * (size_t)natms, dae, nb, cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     for (int i = 0; i < natms; ++i) {
         fxx[i] += h[i];
