@@ -196,3 +196,42 @@ DISP_PARAMS_SYNTHETIC = np.array([
     [0.0, 0.0, 0.0, 0.0],              # M-H
     [0.0, 0.0, 0.0, 0.0],              # M-M
 ])
+
+
+# TTM4-F electrostatics settings of the reference's `vmbpol` keyword
+# (SOURCE/simdef_cmd.f:1040-1060): Thole exp-4 damping with athole 0.055 (intermolecular
+# and H-H), 0.626 (O-H); charge-charge and charge-dipole smearing 0.4; M-site gamma.
+EATD = 4.803239   # Debye per e*Angstrom (SOURCE/module.f90:38)
+POLAR_NPRM = 15
+
+
+def polar_params(alpha=0.3, kmax=(8, 8, 8), rcut=9.0, toler_debye=1e-8, omega=0.3, maxit=22581,
+                 athole=0.055, athole12=0.626, athole13=0.055, ascc=0.4, ascd=0.4, gamma=0.426706882, epsq=1.0):
+    """Parameter vector of the polar Ewald path: {alpha, rcut, epsq, toler (e A), sor_omega,
+    athole, athole12, athole13, ascc, ascd, gamma, kmax1, kmax2, kmax3, maxit}.  toler is the
+    CONTROL `iter` value in Debye (SOURCE/simdef_cmd.f:728-740, default 1e-8); omega the SOR
+    weight of the old dipole (SOURCE/iter.f:50-51, default 0.3)."""
+    k = tuple(int(v) for v in kmax)
+    return np.array([alpha, rcut, epsq, toler_debye / EATD, omega, athole, athole12, athole13, ascc, ascd, gamma,
+                     k[0], k[1], k[2], maxit], dtype=np.float64)
+
+
+def kmax_scaled(L, kmax0=8, L0=19.73):
+    """kmax that keeps the k-space cutoff 2*pi*kmax/L of the 256-water box (kmax 8 at 19.73 A)."""
+    return int(math.ceil(kmax0 * L / L0 - 1e-9))
+
+
+def polarizabilities(nw):
+    """Per-site (polr, polr2): Thole widths and polarizabilities in A^3.  The reference reads
+    both from FIELD (`polar`, `polar2` per site, SOURCE/sysdef_cmd.f:466-469), which it does
+    not ship; these are MB-pol's published values (O 1.310, H 0.294).  The M site carries no
+    dipole (polr2 0) and O's width for the Thole smearing of its charge."""
+    polr = np.empty(4 * nw)
+    polr2 = np.empty(4 * nw)
+    polr[0:3 * nw:3] = 1.310
+    polr[1:3 * nw:3] = 0.294
+    polr[2:3 * nw:3] = 0.294
+    polr[3 * nw:] = 1.310
+    polr2[:3 * nw] = polr[:3 * nw]
+    polr2[3 * nw:] = 0.0
+    return polr, polr2

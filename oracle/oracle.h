@@ -127,6 +127,32 @@ long orc_dispersion(int imcon, const double* cell, int natms, const int* ltype, 
 void orc_disp_lrc(int ntypes, const double* prm, const int* numtyp, double rcut, double volm, double* elrc,
                   double* virlrc);
 
+/* TTM4-F polarizable electrostatics of MB-pol water (SOURCE/forces.f polar Ewald branch:
+ * rfield, ewald1p, iter, coulomb_polar, ewald2p, ewald3p, qdforce) with the heat-current
+ * bookkeeping and the M-site redistribution of compute_heat_flux2.  Standard layout, 4*nw
+ * sites (water w: O, H1, H2 at 3w..3w+2, M at 3nw + w).
+ *   prm[15]   {alpha, rcut, epsq, toler (e A), sor_omega, athole, athole12, athole13, ascc,
+ *              ascd, gamma, kmax1, kmax2, kmax3, maxit}
+ *   chge, dp  DMS charges and dp[6*nw] from orc_qdetermine; polr (Thole widths), polr2
+ *             (polarizabilities) per site
+ *   dip*      in: starting dipoles, out: converged dipoles
+ *   f*        ACCUMULATED site forces (M sites not redistributed)
+ *   out[16]   {engcpe, vircpe, stress[9], iterations, deltadip, eng_polar, eng_kspace,
+ *              eng_realspace}
+ *   atomic_energy (per site, not redistributed), jpot[3], jkin[3] (the redistributed
+ *   electrostatic per-atom energies times the velocities) ACCUMULATED; jpot/jkin need v*.
+ *   dense     1: contract a dense N x N force matrix as compute_heat_flux2 does; 0: entry by
+ *             entry (same value in exact arithmetic).
+ * Returns 0, or 1 when the dipoles did not converge within maxit iterations. */
+int orc_polar(const double* prm, int imcon, const double* cell, int nw, const double* x, const double* y,
+              const double* z, const double* chge, const double* dp, const double* polr, const double* polr2,
+              double* dipx, double* dipy, double* dipz, double* fx, double* fy, double* fz, double* out,
+              double* atomic_energy, const double* vx, const double* vy, const double* vz, double* jpot,
+              double* jkin, int dense);
+double orc_erfcc(double x);
+double orc_gammq(double a, double x);
+double orc_gammln(double x);
+
 #ifdef __cplusplus
 }
 #endif

@@ -62,6 +62,12 @@ class Oracle:
         L.orc_dispersion.argtypes = [C.c_int, _D, C.c_int, _I, _I, C.c_int, _D, C.c_double, C.c_int] + [_D] * 14
         L.orc_dispersion.restype = C.c_long
         L.orc_disp_lrc.argtypes = [C.c_int, _D, _I, C.c_double, C.c_double, _D, _D]
+        L.orc_polar.argtypes = [_D, C.c_int, _D, C.c_int] + [_D] * 20 + [C.c_int]
+        for f in ("orc_erfcc", "orc_gammln"):
+            getattr(L, f).argtypes = [C.c_double]
+            getattr(L, f).restype = C.c_double
+        L.orc_gammq.argtypes = [C.c_double, C.c_double]
+        L.orc_gammq.restype = C.c_double
         if L.orc_dms_load(os.path.join(TABLES, "ps_dms.tbl").encode()):
             raise RuntimeError("orc_dms_load failed")
         if L.orc_pes_load(os.path.join(TABLES, "ps_pes.tbl").encode()):
@@ -221,6 +227,28 @@ class Oracle:
         self.lib.orc_disp_lrc(nt, _p(prm.ravel().copy()), _p(np.ascontiguousarray(numtyp, dtype=np.int32), _I), rcut,
                               volm, C.byref(e), C.byref(v))
         return e.value, v.value
+
+    def polar(self, sites, cell, imcon, nw, chge, dp, polr, polr2, prm, dip0=None, vel=None, dense=False):
+        """TTM4-F electrostatics (orc_polar) on 4*nw sites.  Returns a dict with site forces,
+        energies, virial, stress, dipoles, per-site energies, jpot/jkin and the iteration count."""
+        n = 4 * nw
+        x, y, z = (np.ascontiguousarray(sites[:, k], dtype=np.float64) for k in range(3))
+        dip = np.zeros((3, n)) if dip0 is None else np.ascontiguousarray(np.asarray(dip0, np.float64).T).copy()
+        f = np.zeros((3, n))
+        out = np.zeros(16)
+        ae = np.zeros(n)
+        jpot = np.zeros(3)
+        jkin = np.zeros(3)
+        v = [np.ascontiguousarray(vel[:, k], dtype=np.float64) for k in range(3)] if vel is not None else [None] * 3
+        rc = self.lib.orc_polar(_p(np.ascontiguousarray(prm, np.float64)), imcon, _p(np.ascontiguousarray(cell, np.float64)),
+                                nw, _p(x), _p(y), _p(z), _p(np.ascontiguousarray(chge, np.float64)),
+                                _p(np.ascontiguousarray(dp, np.float64)), _p(np.ascontiguousarray(polr, np.float64)),
+                                _p(np.ascontiguousarray(polr2, np.float64)), _p(dip[0]), _p(dip[1]), _p(dip[2]),
+                                _p(f[0]), _p(f[1]), _p(f[2]), _p(out), _p(ae), _p(v[0]), _p(v[1]), _p(v[2]),
+                                _p(jpot), _p(jkin), int(dense))
+        return dict(status=rc, forces=f.T.copy(), engcpe=out[0], vircpe=out[1], stress=out[2:11].copy(),
+                    iterations=int(out[11]), deltadip=out[12], eng_polar=out[13], eng_kspace=out[14],
+                    eng_real=out[15], dipoles=dip.T.copy(), atomic_energy=ae, jpot=jpot, jkin=jkin)
 
     def image_monomers(self, box):
         m = box.monomers().copy()

@@ -1,0 +1,117 @@
+"""Self-consistency pins of the TTM4-F electrostatics oracle (CPU, no GPU).
+
+The reference ships no test, input or output for its polar Ewald path, so the oracle is
+pinned by: its special functions against independent implementations, forces against a
+central finite difference of the total electrostatic energy (M sites and DMS charges
+recomputed at every displaced geometry), the entry-by-entry heat-current contraction
+against the reference's dense force-matrix layout, momentum conservation and the
+independence of the converged result from the starting dipoles.
+"""
+import copy
+import math
+
+import numpy as np
+import pytest
+
+from mbx import systems
+
+GAMMA = 0.426706882
+
+
+@pytest.fixture(scope="module")
+def small():
+    box = systems.box_for(32, seed=5)
+    polr, polr2 = systems.polarizabilities(box.nw)
+    # 32 waters in a 9.87 A box: rcut below L/2, alpha raised to match
+    prm = systems.polar_params(alpha=0.6, rcut=4.5, kmax=(8, 8, 8), toler_debye=1e-13)
+    return box, polr, polr2, prm
+
+
+def _run(orc, box, polr, polr2, prm, **kw):
+    sites, q, dp, _ = orc.msites_dms(box)
+    return orc.polar(sites, box.cell, box.imcon, box.nw, q, dp, polr, polr2, prm, **kw)
+
+
+def _redistribute(f, nw):
+    fa = f[:3 * nw].copy()
+    m = f[3 * nw:]
+    fa[0::3] += (1 - GAMMA) * m
+    fa[1::3] += 0.5 * GAMMA * m
+    fa[2::3] += 0.5 * GAMMA * m
+    return fa
+
+
+def test_erfcc_is_the_published_fit(oracle_lib):
+    orc = oracle_lib
+    # Numerical Recipes' erfcc: fractional error below 1.2e-7 everywhere
+    for x in np.linspace(0.0, 6.0, 301):
+        ref = math.erfc(x)
+        assert abs(orc.lib.orc_erfcc(x) - ref) <= 1.3e-7 * ref + 1e-300
+    assert abs(orc.lib.orc_erfcc(-0.7) - math.erfc(-0.7)) <= 1.3e-7 * 2
+
+
+def test_gammq_and_gammln(oracle_lib):
+    orc = oracle_lib
+    sp = pytest.importorskip("scipy.special")
+    for x in [1e-3, 0.1, 0.5, 1.0, 1.74, 1.76, 3.0, 8.0, 20.0, 40.0]:
+        ref = sp.gammaincc(0.75, x)
+        got = orc.lib.orc_gammq(0.75, x)
+        assert abs(got - ref) <= 1e-6 * ref, (x, got, ref)
+    for x in [0.75, 1.5, 3.3, 10.0]:
+        assert abs(orc.lib.orc_gammln(x) - math.lgamma(x)) <= 1e-10
+
+
+def test_forces_are_minus_the_energy_gradient(oracle_lib, small):
+    orc = oracle_lib
+    box, polr, polr2, prm = small
+    r0 = _run(orc, box, polr, polr2, prm)
+    assert r0["status"] == 0
+    fa = _redistribute(r0["forces"], box.nw)
+    fmax = np.abs(fa).max()
+    h = 1e-5
+    for a, c in [(0, 1), (1, 0), (2, 2), (40, 1), (77, 0), (95, 2)]:
+        e = []
+        for s in (+h, -h):
+            b = copy.deepcopy(box)
+            b.xyz = box.xyz.copy()
+            b.xyz[a, c] += s
+            e.append(_run(orc, b, polr, polr2, prm, dip0=r0["dipoles"])["engcpe"])
+        fd = -(e[0] - e[1]) / (2 * h)
+        # the reference's real-space B functions pair an erfc fit (1.2e-7) with exact
+        # Gaussian derivatives, so energy and forces agree to a few 1e-6 of the largest force
+        assert abs(fd - fa[a, c]) <= 2e-5 * fmax, (a, c, fd, fa[a, c])
+
+
+def test_momentum_and_starting_dipoles(oracle_lib, small):
+    orc = oracle_lib
+    box, polr, polr2, prm = small
+    r0 = _run(orc, box, polr, polr2, prm)
+    f = r0["forces"]
+    assert np.abs(f.sum(0)).max() <= 1e-9 * np.abs(f).max()
+    rng = np.random.default_rng(3)
+    dip0 = rng.normal(0, 0.05, size=(4 * box.nw, 3))
+    dip0[3 * box.nw:] = 0.0
+    r1 = _run(orc, box, polr, polr2, prm, dip0=dip0)
+    assert abs(r1["engcpe"] - r0["engcpe"]) <= 1e-9 * abs(r0["engcpe"])
+    assert np.abs(r1["forces"] - f).max() <= 1e-8 * np.abs(f).max()
+    assert r0["deltadip"] <= prm[3]
+
+
+def test_dense_force_matrix_matches_entry_contraction(oracle_lib, small):
+    orc = oracle_lib
+    box, polr, polr2, prm = small
+    a = _run(orc, box, polr, polr2, prm, vel=box.vel)
+    b = _run(orc, box, polr, polr2, prm, vel=box.vel, dense=True)
+    assert np.abs(a["jpot"] - b["jpot"]).max() <= 1e-12 * np.abs(b["jpot"]).max()
+    np.testing.assert_array_equal(a["jkin"], b["jkin"])
+    # per-site energies add up to the total
+    assert abs(a["atomic_energy"].sum() - a["engcpe"]) <= 1e-10 * abs(a["engcpe"])
+
+
+def test_iteration_cap(oracle_lib, small):
+    orc = oracle_lib
+    box, polr, polr2, prm = small
+    p = prm.copy()
+    p[14] = 3
+    r = _run(orc, box, polr, polr2, p)
+    assert r["status"] == 1 and r["iterations"] == 3
