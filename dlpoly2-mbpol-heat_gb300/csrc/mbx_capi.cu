@@ -72,6 +72,9 @@ struct mbx_context {
     int* ints = nullptr;               // mbx_water_forces staging: listttm2, listang, ltype, molecule
     size_t ints_cap = 0;
     DispState disp;                    // dispersion tables and Verlet list
+    PolarState polar;                  // TTM4-F electrostatics
+    double* polar_stage = nullptr;     // host entry point staging (24 * sites)
+    size_t polar_stage_cap = 0;
     std::vector<int> disp_types_h, disp_mol_h;   // inputs of the host entry point's list
     char err[512] = {0};
 };
@@ -466,7 +469,7 @@ extern "C" void mbx_destroy(mbx_context* ctx) {
     if (ctx->own_stream) cudaStreamSynchronize(ctx->own_stream);
     void* dev[] = {ctx->mono, ctx->list, ctx->atoms, ctx->ae_scratch, ctx->acc, ctx->totals, ctx->pairs, ctx->trip,
                    ctx->batch, ctx->hard2, ctx->hard3, ctx->hard_count, ctx->fuse_ctr, ctx->part2, ctx->done2,
-                   ctx->ints};
+                   ctx->ints, ctx->polar_stage};
     for (void* p : dev)
         if (p) cudaFree(p);
     if (ctx->totals_h) cudaFreeHost(ctx->totals_h);
@@ -478,6 +481,7 @@ extern "C" void mbx_destroy(mbx_context* ctx) {
     if (ctx->hstage) cudaFreeHost(ctx->hstage);
     ctx->multi.release();
     ctx->disp.release();
+    ctx->polar.release();
     ctx->lb.release();
     for (cudaEvent_t e : ctx->ev)
         if (e) cudaEventDestroy(e);
@@ -829,6 +833,133 @@ extern "C" int mbx_disp_lrc(int ntypes, const double* prm, const int* numtyp, do
 }
 
 extern "C" long mbx_disp_list_builds(const mbx_context* ctx) { return ctx ? ctx->disp.builds : -1; }
+
+namespace {
+bool polar_prm_ok(const double* prm) {
+    return prm && prm[0] > 1e-6 && prm[1] > 0.0 && prm[2] > 0.0 && prm[3] > 0.0 && prm[4] >= 0.0 && prm[4] < 1.0 &&
+           prm[11] >= 0 && prm[12] >= 0 && prm[13] >= 0 && prm[11] <= 512 && prm[12] <= 512 && prm[13] <= 512 &&
+           prm[14] >= 1;
+}
+}  // namespace
+
+extern "C" int mbx_polar_forces_device(mbx_context* ctx, const double* prm, int imcon, const double* cell, int nw,
+                                       const double* xxx, const double* yyy, const double* zzz, const double* chge,
+                                       const double* dqdr, const double* polr, const double* polr2, double* dipx,
+                                       double* dipy, double* dipz, double* fxx, double* fyy, double* fzz,
+                                       double* out16, double* atomic_energy, const double* vxx, const double* vyy,
+                                       const double* vzz, double* jpot, double* jkin) {
+    if (!ctx) return MBX_ERR_ARG;
+    if (nw < 0 || !polar_prm_ok(prm) || !out16 || (nw && (!xxx || !yyy || !zzz || !chge || !dqdr || !polr || !polr2 ||
+                                                            !dipx || !dipy || !dipz || !fxx || !fyy || !fzz)))
+        return fail(ctx, MBX_ERR_ARG, "mbx_polar_forces: bad argument");
+    const bool heat = vxx && vyy && vzz;
+    if (heat && (!jpot || !jkin)) return fail(ctx, MBX_ERR_ARG, "mbx_polar_forces: jpot/jkin needed with velocities");
+    Cell cl;
+    int rc = make_cell(ctx, imcon, cell, cl);
+    if (rc) return rc;
+    CK(cudaSetDevice(ctx->device));
+    double jp[3] = {0, 0, 0}, jk[3] = {0, 0, 0};
+    CK(ctx->polar.run(cl, prm, nw, xxx, yyy, zzz, chge, dqdr, polr, polr2, dipx, dipy, dipz, fxx, fyy, fzz,
+                      atomic_energy, heat ? vxx : nullptr, heat ? vyy : nullptr, heat ? vzz : nullptr, out16, jp, jk,
+                      ctx->stream));
+    ctx->launches = ctx->polar.launches;
+    if (heat)
+        for (int c = 0; c < 3; ++c) {
+            jpot[c] += jp[c];
+            jkin[c] += jk[c];
+        }
+    if (!ctx->polar.converged)
+        return fail(ctx, MBX_ERR_CONVERGE, "mbx_polar_forces: dipoles not converged after %d iterations (rms change %g)",
+                    ctx->polar.iterations, out16[12]);
+    return MBX_OK;
+}
+
+extern "C" int mbx_polar_forces(mbx_context* ctx, const double* prm, int imcon, const double* cell, int nw,
+                                const double* xxx, const double* yyy, const double* zzz, const double* chge,
+                                const double* dqdr, const double* polr, const double* polr2, double* dipx, double* dipy,
+                                double* dipz, double* fxx, double* fyy, double* fzz, double* out16,
+                                double* atomic_energy, const double* vxx, const double* vyy, const double* vzz,
+                                double* jpot, double* jkin) {
+    if (!ctx) return MBX_ERR_ARG;
+    if (nw < 0 || !polar_prm_ok(prm) || !out16 || (nw && (!xxx || !yyy || !zzz || !chge || !dqdr || !polr || !polr2 ||
+                                                            !dipx || !dipy || !dipz || !fxx || !fyy || !fzz)))
+        return fail(ctx, MBX_ERR_ARG, "mbx_polar_forces: bad argument");
+    const bool heat = vxx && vyy && vzz;
+    if (heat && (!jpot || !jkin)) return fail(ctx, MBX_ERR_ARG, "mbx_polar_forces: jpot/jkin needed with velocities");
+    CK(cudaSetDevice(ctx->device));
+    const size_t n = 4 * (size_t)nw, na = 3 * (size_t)nw;
+    // x y z q polr polr2 dip(3) f(3) ae (13 n) + dp (6 nw) + v (3 na)
+    const size_t need = 13 * n + 6 * (size_t)nw + 3 * na + 1;
+    if (need > ctx->polar_stage_cap) {
+        if (ctx->polar_stage) cudaFree(ctx->polar_stage);
+        ctx->polar_stage = nullptr;
+        ctx->polar_stage_cap = 0;
+        CK(cudaMalloc(&ctx->polar_stage, need * sizeof(double)));
+        ctx->polar_stage_cap = need;
+    }
+    cudaStream_t s = ctx->stream;
+    double* d = ctx->polar_stage;
+    double *dx = d, *dy = d + n, *dz = d + 2 * n, *dq = d + 3 * n, *dpr = d + 4 * n, *dpr2 = d + 5 * n;
+    double *dmx = d + 6 * n, *dmy = d + 7 * n, *dmz = d + 8 * n, *dfx = d + 9 * n, *dfy = d + 10 * n,
+           *dfz = d + 11 * n, *dae = d + 12 * n, *ddp = d + 13 * n, *dv = d + 13 * n + 6 * (size_t)nw;
+    const size_t nb = n * sizeof(double);
+    if (n) {
+        CK(cudaMemcpyAsync(dx, xxx, nb, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(dy, yyy, nb, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(dz, zzz, nb, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(dq, chge, nb, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(dpr, polr, nb, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(dpr2, polr2, nb, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(dmx, dipx, nb, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(dmy, dipy, nb, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(dmz, dipz, nb, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(ddp, dqdr, 6 * (size_t)nw * sizeof(double), cudaMemcpyHostToDevice, s));
+        if (heat) {
+            CK(cudaMemcpyAsync(dv, vxx, na * sizeof(double), cudaMemcpyHostToDevice, s));
+            CK(cudaMemcpyAsync(dv + na, vyy, na * sizeof(double), cudaMemcpyHostToDevice, s));
+            CK(cudaMemcpyAsync(dv + 2 * na, vzz, na * sizeof(double), cudaMemcpyHostToDevice, s));
+        }
+        CK(cudaMemsetAsync(dfx, 0, 4 * nb, s));   // forces and per-site energies
+    }
+    const int rc = mbx_polar_forces_device(ctx, prm, imcon, cell, nw, dx, dy, dz, dq, ddp, dpr, dpr2, dmx, dmy, dmz,
+                                           dfx, dfy, dfz, out16, atomic_energy ? dae : nullptr,
+                                           heat ? dv : nullptr, heat ? dv + na : nullptr, heat ? dv + 2 * na : nullptr,
+                                           jpot, jkin);
+    if (rc && rc != MBX_ERR_CONVERGE) return rc;
+    double* h = host_stage(ctx, 7 * n + 1);
+    if (!h) return fail(ctx, MBX_ERR_CUDA, "pinned host staging allocation failed");
+    if (n) {
+        CK(cudaMemcpyAsync(h, dfx, 4 * nb, cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(h + 4 * n, dmx, 3 * nb, cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+    }
+    for (size_t i = 0; i < n; ++i) {
+        fxx[i] += h[i];
+        fyy[i] += h[n + i];
+        fzz[i] += h[2 * n + i];
+        if (atomic_energy) atomic_energy[i] += h[3 * n + i];
+        dipx[i] = h[4 * n + i];
+        dipy[i] = h[5 * n + i];
+        dipz[i] = h[6 * n + i];
+    }
+    return rc;
+}
+
+extern "C" int mbx_polar_iterations(const mbx_context* ctx) { return ctx ? ctx->polar.iterations : -1; }
+
+extern "C" int mbx_msite_redistribute(int nw, double gamma, double* fxx, double* fyy, double* fzz) {
+    if (nw < 0 || (nw && (!fxx || !fyy || !fzz))) return MBX_ERR_ARG;
+    for (int i = 0; i < nw; ++i) {   // SOURCE/dlpoly_cmd.f:2585-2601 (standard layout)
+        const int m = 3 * nw + i, o = 3 * i;
+        double* f[3] = {fxx, fyy, fzz};
+        for (int c = 0; c < 3; ++c) {
+            f[c][o] = f[c][o] + (1.0 - gamma) * f[c][m];
+            f[c][o + 1] = f[c][o + 1] + f[c][m] * gamma / 2.0;
+            f[c][o + 2] = f[c][o + 2] + f[c][m] * gamma / 2.0;
+        }
+    }
+    return MBX_OK;
+}
 
 extern "C" int mbx_set_fused(mbx_context* ctx, int on) {
     if (!ctx) return MBX_ERR_ARG;

@@ -164,6 +164,48 @@ struct DispState {
                        const double* vy, const double* vz, double* ae, double* out14, int* flag_host,
                        cudaStream_t s, bool* rebuilt);
 };
+// TTM4-F polarizable electrostatics of MB-pol water (mbx_polar.cu): the reference's polar
+// Ewald branch (rfield, ewald1p, iter, coulomb_polar, ewald2p, ewald3p, qdforce) with its
+// heat-current terms, on 4 * nw sites in the standard layout.
+struct PolarState {
+    int cap = 512, cap_alloc = 0;          // list partners per site
+    int n_cap = 0, nw_cap = 0, k_cap = 0;
+    size_t eik_cap = 0;
+    int mxegrd = 0;
+    double drewd = 0.0, tab_alpha = -1.0, tab_rcut = -1.0;
+    double4* ercp = nullptr;               // erfcgenp table, rows 0..mxegrd
+    int *nn = nullptr, *nbr = nullptr, *flag = nullptr;
+    float4* xf = nullptr;
+    double* tens = nullptr;                // dipole tensors of the list pairs (6 blocks)
+    double* intra = nullptr;               // intramolecular O/H dipole tensors (18 per water)
+    double* fld = nullptr;                 // efk, efc, emu, efm (3 blocks of n each)
+    double *vesp = nullptr, *ae = nullptr;
+    double2* eik = nullptr;                // exp(ik.r) [k][site]
+    double4* kv = nullptr;                 // kx, ky, kz, akk
+    double2* kx2 = nullptr;                // rksq, akv2
+    int4* lmn = nullptr;
+    double *sf = nullptr, *kterm = nullptr, *acc = nullptr, *acc_h = nullptr;
+    std::vector<double4> hk;
+    std::vector<double2> hk2;
+    std::vector<int4> hlmn;
+    bool converged = false;
+    int iterations = 0;
+    long launches = 0;
+
+    ~PolarState();
+    void release();
+    cudaError_t table(double alpha, double rcut);
+    cudaError_t reserve(int nw, int K);
+    // One evaluation on device arrays.  prm[15] as mbx_polar_forces; forces, per-site
+    // energies (ae_out, may be null), jpot and jkin are ACCUMULATED; the dipoles are
+    // updated in place; out16 as mbx_polar_forces.  `converged` tells whether the dipole
+    // iteration reached toler within maxit iterations.
+    cudaError_t run(const Cell& cl, const double* prm, int nw, const double* x, const double* y, const double* z,
+                    const double* q, const double* dp, const double* polr, const double* polr2, double* mx,
+                    double* my, double* mz, double* fx, double* fy, double* fz, double* ae_out, const double* vx,
+                    const double* vy, const double* vz, double* out16, double* jpot, double* jkin, cudaStream_t s);
+};
+
 // lrcorrect for vdw type 12 (host): elrc and virlrc for numtyp[t] atoms of type t + 1.
 void disp_lrc(int ntypes, const double* prm, const int* numtyp, double rcut, double volm, double* elrc,
               double* virlrc);

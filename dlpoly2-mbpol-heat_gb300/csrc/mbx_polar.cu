@@ -1,0 +1,1337 @@
+// TTM4-F polarizable electrostatics of MB-pol water (the reference's polar Ewald branch
+// with the vmbpol settings, SOURCE/simdef_cmd.f:1040-1060) with its heat-current terms.
+//
+//   list      site pairs of different waters within rcut (the Verlet pairs of SOURCE/parlst.f
+//             with the TTM exclusions of SOURCE/exclude_ttm.f); directed, one row per site
+//   static    rfield's first pass (SOURCE/rfield.f:59-201, :330-421): charge field of the
+//             Verlet pairs (table B functions, Thole exp-4 smearing) and of the excluded
+//             intramolecular pairs (analytic B functions); the dipole tensors of every pair
+//             are stored for the iterations
+//   k space   ewald1p (SOURCE/ewald1p.f): exp(ik.r) per k vector and site is tabulated once
+//             per call; each pass is a structure-factor reduction over sites (block per k)
+//             and a field / force gather over k vectors (thread per site)
+//   iterate   rfield's dipole field + ewald1p's dipole field + iter (SOURCE/iter.f:43-100)
+//             until the RMS dipole change is <= toler (SOURCE/forces.f:271-366)
+//   final     coulomb_polar, ewald1p iflag 1 (forces, energy, virial, stress, DMS potentials,
+//             HEAT_CURRENT per-atom stress and energy), ewald2p over the Verlet pairs,
+//             ewald3p over the excluded pairs, qdforce (SOURCE/qdforce.f90) with the summed
+//             DMS potentials
+//   heat      update_forces entries, the M-site row redistribution and compute_heat_flux2's
+//             contraction applied entry by entry (SOURCE/heatcurrent.f90:529-559, :703-728)
+//
+// Standard layout: 4*nw sites, water w has O, H1, H2 at 3w..3w+2 and its M site at 3nw+w.
+// FP64 throughout; erfcc and gammq are the reference's published approximations
+// (Numerical Recipes' erfc fit with single-precision constants; the incomplete gamma
+// series / continued fraction with EPS 3e-7).
+#include "mbx_kernels.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+namespace mbx {
+
+namespace {
+
+constexpr double kR4pie0 = 138935.4835;   // SOURCE/dl_params.inc:60
+constexpr double kSqrpi = 1.7724538509055159;
+constexpr double kPi = 3.141592653589793;
+constexpr int kSfThreads = 256;
+constexpr int kKTile = 64;
+
+// --- special functions (host and device) --------------------------------------------
+__host__ __device__ inline double erfcc(double x) {
+    const double z = fabs(x);
+    const double t = 1.0 / (1.0 + 0.5 * z);
+    const double p = (double)1.00002368f +
+                     t * ((double)0.37409196f +
+                          t * ((double)0.09678418f +
+                               t * (-(double)0.18628806f +
+                                    t * ((double)0.27886807f +
+                                         t * (-(double)1.13520398f +
+                                              t * ((double)1.48851587f +
+                                                   t * (-(double)0.82215223f + t * (double)0.17087277f)))))));
+    double e = -(z * z) - (double)1.26551223f;
+    e = e + t * p;
+    double r = t * exp(e);
+    if (x < 0.0) r = 2.0 - r;
+    return r;
+}
+
+__host__ __device__ inline double gammln(double xx) {
+    const double cof[6] = {76.18009172947146, -86.50532032941677, 24.01409824083091,
+                           -1.231739572450155, .1208650973866179e-2, -.5395239384953e-5};
+    double x = xx, y = x;
+    double tmp = x + 5.5;
+    tmp = (x + 0.5) * log(tmp) - tmp;
+    double ser = 1.000000000190015;
+    for (int j = 0; j < 6; ++j) {
+        y = y + 1.0;
+        ser = ser + cof[j] / y;
+    }
+    return tmp + log(2.5066282746310005 * ser / x);
+}
+
+__device__ inline double gammq(double a, double x) {
+    const double eps = (double)3.e-7f, fpmin = (double)1.e-30f;
+    const double gln = gammln(a);
+    if (x < a + 1.0) {
+        if (x <= 0.0) return 1.0;
+        double ap = a, sum = 1.0 / a, del = sum;
+        for (int n = 1; n <= 800; ++n) {
+            ap = ap + 1.0;
+            del = del * x / ap;
+            sum = sum + del;
+            if (fabs(del) < fabs(sum) * eps) break;
+        }
+        return 1.0 - sum * exp(-x + a * log(x) - gln);
+    }
+    double b = x + 1.0 - a, c = 1.0 / fpmin, d = 1.0 / b, h = d;
+    for (int i = 1; i <= 100; ++i) {
+        const double an = -i * (i - a);
+        b = b + 2.0;
+        d = an * d + b;
+        if (fabs(d) < fpmin) d = fpmin;
+        c = b + an / c;
+        if (fabs(c) < fpmin) c = fpmin;
+        d = 1.0 / d;
+        const double del = d * c;
+        h = h * del;
+        if (fabs(del - 1.0) < eps) break;
+    }
+    return exp(-x + a * log(x) - gln) * h;
+}
+
+// B_0..B_3 of the real-space sum from erfcc (rfield / ewald3p intramolecular form)
+__device__ inline void bfun_exact(double alpha, double rr, double rri, double rsqi, double bbb[4]) {
+    const double a = alpha * rr;
+    bbb[0] = (erfcc(a) - 1.0) * rri;
+    const double exp2a = exp(-a * a);
+    const double a2 = 2.0 * (alpha * alpha);
+    double pw = 1.0;
+    for (int m = 1; m <= 3; ++m) {
+        pw = m == 1 ? a2 : (m == 2 ? a2 * a2 : pow(a2, 3.0));
+        bbb[m] = rsqi * ((2.0 * m - 1.0) * bbb[m - 1] + pw * exp2a / alpha / kSqrpi);
+    }
+}
+
+struct PolArgs {
+    Cell cl;
+    int nw, n, cap;
+    const double *x, *y, *z, *q, *polr, *polr2, *dp;
+    double *mx, *my, *mz;
+    const double *vx, *vy, *vz;
+    double *fx, *fy, *fz;
+    double gamma, alpha, rcut, rcsq, eps, athole, athole12, athole13, ascc, ascd, toler, omega;
+    const double4* ercp;
+    double drewd;
+    const int *nn, *nbr;
+    double* tens;   // 6 blocks of n * cap
+    double* intra;  // 18 per water
+    double *efk, *efc, *emu, *efm;   // 3 blocks of n each
+    double *vesp, *ae;
+    double* acc;
+};
+
+__device__ __forceinline__ int site_mol(const PolArgs& a, int i) { return i < 3 * a.nw ? i / 3 : i - 3 * a.nw; }
+
+__device__ __forceinline__ void sep(const PolArgs& a, int i, int j, double& dx, double& dy, double& dz) {
+    dx = dsub(a.x[i], a.x[j]);
+    dy = dsub(a.y[i], a.y[j]);
+    dz = dsub(a.z[i], a.z[j]);
+    image(a.cl, dx, dy, dz);
+}
+
+__device__ __forceinline__ double norm2(double dx, double dy, double dz) {
+    return dadd(dadd(dmul(dx, dx), dmul(dy, dy)), dmul(dz, dz));
+}
+
+__device__ __forceinline__ void interp(const PolArgs& a, double rr, double bbb[4]) {
+    const int ll = (int)(rr / a.drewd);
+    const double ppp = rr / a.drewd - double(ll);
+    const double4 v0 = a.ercp[ll], v1 = a.ercp[ll + 1], v2 = a.ercp[ll + 2];
+    const double vk[4] = {v0.x, v0.y, v0.z, v0.w}, vk1[4] = {v1.x, v1.y, v1.z, v1.w}, vk2[4] = {v2.x, v2.y, v2.z, v2.w};
+#pragma unroll
+    for (int n = 0; n < 4; ++n) {
+        const double t1 = vk[n] + (vk1[n] - vk[n]) * ppp;
+        const double t2 = vk1[n] + (vk2[n] - vk1[n]) * (ppp - 1.0);
+        bbb[n] = t1 + (t2 - t1) * ppp * 0.5;
+    }
+}
+
+__device__ __forceinline__ double pow4(double t) {
+    const double t2 = t * t;
+    return t2 * t2;
+}
+
+// Heat-current contribution of the force-matrix entry (row a, column b, F) after the
+// M-site row redistribution (columns of M sites are never read).
+__device__ __forceinline__ void heat_entry(const PolArgs& a, int row, int col, double Fx, double Fy, double Fz,
+                                           double jp[3]) {
+    const int na = 3 * a.nw;
+    if (col >= na) return;
+    int c[3];
+    double w[3];
+    int m = 1;
+    if (row < na) {
+        c[0] = row;
+        w[0] = 1.0;
+    } else {
+        const int wt = row - na;
+        c[0] = 3 * wt; c[1] = 3 * wt + 1; c[2] = 3 * wt + 2;
+        w[0] = 1.0 - a.gamma; w[1] = 0.5 * a.gamma; w[2] = 0.5 * a.gamma;
+        m = 3;
+    }
+    for (int k = 0; k < m; ++k) {
+        if (c[k] == col) continue;
+        const double fv = w[k] * (Fx * a.vx[c[k]] + Fy * a.vy[c[k]] + Fz * a.vz[c[k]]);
+        jp[0] += (a.x[c[k]] - a.x[col]) * fv;
+        jp[1] += (a.y[c[k]] - a.y[col]) * fv;
+        jp[2] += (a.z[c[k]] - a.z[col]) * fv;
+    }
+}
+
+// Velocity a per-site quantity is carried with after the redistribution
+__device__ __forceinline__ void vhat(const PolArgs& a, int j, double v[3]) {
+    const int na = 3 * a.nw;
+    if (j < na) {
+        v[0] = a.vx[j]; v[1] = a.vy[j]; v[2] = a.vz[j];
+        return;
+    }
+    const int o = 3 * (j - na);
+    const double g1 = 1.0 - a.gamma, g2 = 0.5 * a.gamma;
+    v[0] = g1 * a.vx[o] + g2 * a.vx[o + 1] + g2 * a.vx[o + 2];
+    v[1] = g1 * a.vy[o] + g2 * a.vy[o + 1] + g2 * a.vy[o + 2];
+    v[2] = g1 * a.vz[o] + g2 * a.vz[o + 1] + g2 * a.vz[o + 2];
+}
+
+// --- list -----------------------------------------------------------------------------
+__global__ void k_pol_f32(int n, const double* __restrict__ x, const double* __restrict__ y,
+                          const double* __restrict__ z, float4* __restrict__ xf) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) xf[i] = make_float4((float)x[i], (float)y[i], (float)z[i], 0.f);
+}
+
+// Partners of site i: every site of another water whose imaged separation passes the
+// reference's cut (rcut > r in rfield, rcut^2 > r^2 in ewald2p), in increasing index.
+// An FP32 test with a margin far above its rounding screens the candidates first.
+__global__ void k_pol_list(PolArgs a, int* __restrict__ nn, int* __restrict__ nbr, const float4* __restrict__ xf,
+                           float r2f, int* __restrict__ flag) {
+    const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (i >= a.n) return;
+    const int mi = site_mol(a, i);
+    const float4 pi = xf[i];
+    int* my = nbr + (size_t)i * a.cap;
+    int cnt = 0;
+    for (int b = 0; b < a.n; b += 32) {
+        const int j = b + lane;
+        bool hit = false;
+        if (j < a.n && j != i && site_mol(a, j) != mi && dist2_img_f(a.cl, pi, xf[j]) < r2f) {
+            double dx, dy, dz;
+            sep(a, i, j, dx, dy, dz);
+            const double r2 = norm2(dx, dy, dz);
+            hit = a.rcut > __dsqrt_rn(r2) || a.rcsq > r2;
+        }
+        const unsigned bal = __ballot_sync(0xffffffffu, hit);
+        if (hit) {
+            const int slot = cnt + __popc(bal & ((1u << lane) - 1u));
+            if (slot < a.cap) my[slot] = j;
+        }
+        cnt += __popc(bal);
+    }
+    if (lane == 0) {
+        nn[i] = min(cnt, a.cap);
+        if (cnt > a.cap) atomicOr(flag, 1);
+    }
+}
+
+// --- static real-space field and dipole tensors ---------------------------------------
+__global__ void k_pol_static(PolArgs a) {
+    const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (i >= a.n) return;
+    const int nn = a.nn[i];
+    const size_t row = (size_t)i * a.cap, blk = (size_t)a.n * a.cap;
+    const double qi = a.q[i], pi = a.polr[i];
+    const bool poli = a.polr2[i] > 1e-6;
+    double e[3] = {0, 0, 0};
+    for (int k = lane; k < nn; k += 32) {
+        const int j = a.nbr[row + k];
+        double d[3];
+        sep(a, i, j, d[0], d[1], d[2]);
+        const double r2 = norm2(d[0], d[1], d[2]);
+        const double rr = __dsqrt_rn(r2);
+        double t[6] = {0, 0, 0, 0, 0, 0};
+        if (a.rcut > rr) {
+            double bbb[4];
+            interp(a, rr, bbb);
+            const double rsqi = 1.0 / r2, r3i = 1.0 / (rr * rr * rr), r5i = r3i * rsqi;
+            const double bb = pow(pi * a.polr[j], 1.0 / 6.0);
+            const double qj = a.q[j];
+            double eki = kR4pie0 * qj * (bbb[1] + r3i);
+            const double dum1 = exp(-(a.ascd * pow4(rr / bb)));
+            eki = eki - kR4pie0 * qj * dum1 * r3i;
+            e[0] += eki * d[0];
+            e[1] += eki * d[1];
+            e[2] += eki * d[2];
+            if (poli && a.polr2[j] > 1e-6) {
+                const double arob4 = a.athole * pow4(rr / bb);
+                const double h1 = exp(-arob4);
+                const double h2 = (1.0 + (4.0 / 3.0) * arob4) * h1;
+                const int ia[6] = {0, 0, 0, 1, 1, 2}, ib[6] = {0, 1, 2, 1, 2, 2};
+#pragma unroll
+                for (int p = 0; p < 6; ++p) {
+                    const double rirj = d[ia[p]] * d[ib[p]];
+                    if (ia[p] == ib[p]) {
+                        t[p] = kR4pie0 * ((3.0 * rirj * r5i - r3i) + rirj * bbb[2] - bbb[1]);
+                        t[p] = t[p] - (3.0 * rirj * r5i * h2 - h1 * r3i) * kR4pie0;
+                    } else {
+                        t[p] = kR4pie0 * ((3.0 * rirj * r5i) + rirj * bbb[2]);
+                        t[p] = t[p] - 3.0 * rirj * r5i * h2 * kR4pie0;
+                    }
+                }
+            }
+        }
+#pragma unroll
+        for (int p = 0; p < 6; ++p) a.tens[p * blk + row + k] = t[p];
+    }
+    for (int c = 0; c < 3; ++c) e[c] = warp_sum(e[c]);
+    if (lane == 0) {
+        a.efk[i] = e[0];
+        a.efk[a.n + i] = e[1];
+        a.efk[2 * a.n + i] = e[2];
+    }
+}
+
+// Intramolecular (excluded) pairs: static charge field and the three O/H dipole tensors.
+__global__ void k_pol_intra_static(PolArgs a) {
+    const int w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= a.nw) return;
+    const int o = 3 * w, m = 3 * a.nw + w;
+    const int pr[6][2] = {{o, o + 1}, {o, o + 2}, {o + 1, o + 2}, {o, m}, {o + 1, m}, {o + 2, m}};
+    double* T = a.intra + 18 * (size_t)w;
+    for (int p = 0; p < 6; ++p) {
+        const int i = pr[p][0], j = pr[p][1];
+        double d[3];
+        sep(a, i, j, d[0], d[1], d[2]);
+        const double r2 = norm2(d[0], d[1], d[2]);
+        const double rr = __dsqrt_rn(r2);
+        const double rri = 1.0 / rr, rsqi = 1.0 / r2, r3i = 1.0 / (rr * r2), r5i = r3i * rsqi;
+        double bbb[4];
+        bfun_exact(a.alpha, rr, rri, rsqi, bbb);
+        const double eki = kR4pie0 * a.q[j] * bbb[1] / a.eps, ekj = kR4pie0 * a.q[i] * bbb[1] / a.eps;
+        for (int c = 0; c < 3; ++c) {
+            a.efk[c * a.n + i] += eki * d[c];
+            a.efk[c * a.n + j] -= ekj * d[c];
+        }
+        if (p < 3) {
+            double t[6] = {0, 0, 0, 0, 0, 0};
+            if (a.polr2[i] > 1e-6 && a.polr2[j] > 1e-6) {
+                const double bb = pow(a.polr[i] * a.polr[j], 1.0 / 6.0);
+                const double ath = (i % 3 == 0 || j % 3 == 0) ? a.athole12 : a.athole13;
+                const double arob4 = ath * pow4(rr / bb);
+                const double h1 = exp(-arob4);
+                const double h2 = (1.0 + (4.0 / 3.0) * arob4) * h1;
+                const int ia[6] = {0, 0, 0, 1, 1, 2}, ib[6] = {0, 1, 2, 1, 2, 2};
+                for (int q = 0; q < 6; ++q) {
+                    const double rirj = d[ia[q]] * d[ib[q]];
+                    const bool dg = ia[q] == ib[q];
+                    double v = dg ? rirj * bbb[2] - bbb[1] : rirj * bbb[2];
+                    v = dg ? v + 3.0 * rirj * r5i - r3i : v + 3.0 * rirj * r5i;
+                    v = dg ? v - 3.0 * rirj * r5i * h2 + h1 * r3i : v - 3.0 * rirj * r5i * h2;
+                    t[q] = v * (kR4pie0 / a.eps);
+                }
+            }
+            for (int q = 0; q < 6; ++q) T[6 * p + q] = t[q];
+        }
+    }
+}
+
+// --- dipole field of the real-space pairs ------------------------------------------------
+__global__ void k_pol_dd(PolArgs a) {
+    const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (i >= a.n) return;
+    double e[3] = {0, 0, 0};
+    if (a.polr2[i] > 1e-6) {
+        const int nn = a.nn[i];
+        const size_t row = (size_t)i * a.cap, blk = (size_t)a.n * a.cap;
+        for (int k = lane; k < nn; k += 32) {
+            const int j = a.nbr[row + k];
+            const double mj[3] = {a.mx[j], a.my[j], a.mz[j]};
+            double t[6];
+#pragma unroll
+            for (int p = 0; p < 6; ++p) t[p] = a.tens[p * blk + row + k];
+            e[0] += t[0] * mj[0] + t[1] * mj[1] + t[2] * mj[2];
+            e[1] += t[1] * mj[0] + t[3] * mj[1] + t[4] * mj[2];
+            e[2] += t[2] * mj[0] + t[4] * mj[1] + t[5] * mj[2];
+        }
+        for (int c = 0; c < 3; ++c) e[c] = warp_sum(e[c]);
+        if (lane == 0 && i < 3 * a.nw) {
+            const int w = i / 3, s = i % 3;
+            // pairs 0 (O,H1), 1 (O,H2), 2 (H1,H2)
+            const int pj[3][2] = {{1, 2}, {0, 2}, {0, 1}};   // partner sites of s
+            const int pp[3][2] = {{0, 1}, {0, 2}, {1, 2}};   // their pair index
+            const double* T = a.intra + 18 * (size_t)w;
+            for (int u = 0; u < 2; ++u) {
+                const int j = 3 * w + pj[s][u];
+                const double* t = T + 6 * pp[s][u];
+                const double mj[3] = {a.mx[j], a.my[j], a.mz[j]};
+                e[0] += t[0] * mj[0] + t[1] * mj[1] + t[2] * mj[2];
+                e[1] += t[1] * mj[0] + t[3] * mj[1] + t[4] * mj[2];
+                e[2] += t[2] * mj[0] + t[4] * mj[1] + t[5] * mj[2];
+            }
+        }
+    }
+    if (lane == 0) {
+        a.emu[i] = e[0];
+        a.emu[a.n + i] = e[1];
+        a.emu[2 * a.n + i] = e[2];
+    }
+}
+
+// --- k space ------------------------------------------------------------------------------
+struct KArgs {
+    int K, n;
+    const double4* kv;     // kx, ky, kz, akk
+    const double2* kx2;    // rksq, akv2
+    const int4* lmn;
+    const double2* eik;    // [k * n + j] = (cos, sin)
+    double* sf;            // 8 per k: ckcs, ckss, Mc(3), Ms(3)
+    double* kterm;         // 8 per k (final pass): engc, engdum, omg 1 5 9 2 3 6
+    double rc[9];
+    double scale, ralph;
+};
+
+__global__ void k_pol_phase(KArgs k, const double* __restrict__ x, const double* __restrict__ y,
+                            const double* __restrict__ z) {
+    const int j = blockIdx.y * blockDim.x + threadIdx.x;
+    const int kk = blockIdx.x;
+    if (j >= k.n) return;
+    const double sx = k.rc[0] * x[j] + k.rc[3] * y[j] + k.rc[6] * z[j];
+    const double sy = k.rc[1] * x[j] + k.rc[4] * y[j] + k.rc[7] * z[j];
+    const double sz = k.rc[2] * x[j] + k.rc[5] * y[j] + k.rc[8] * z[j];
+    const int4 v = k.lmn[kk];
+    // exp(2 pi i (l sx + m sy + n sz)) with each product reduced mod 1 first
+    double ph = (double)v.x * sx - rint((double)v.x * sx);
+    ph += (double)v.y * sy - rint((double)v.y * sy);
+    ph += (double)v.z * sz - rint((double)v.z * sz);
+    double s, c;
+    sincospi(2.0 * ph, &s, &c);
+    ((double2*)k.eik)[(size_t)kk * k.n + j] = make_double2(c, s);
+}
+
+template <int NV>
+__device__ __forceinline__ void block_reduce_store(double (&v)[NV], double* out) {
+    __shared__ double red[kSfThreads / 32][NV];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int q = 0; q < NV; ++q) {
+        const double s = warp_sum(v[q]);
+        if (lane == 0) red[w][q] = s;
+    }
+    __syncthreads();
+    if (threadIdx.x < NV) {
+        double s = 0.0;
+        for (int i = 0; i < kSfThreads / 32; ++i) s += red[i][threadIdx.x];
+        out[threadIdx.x] = s;
+    }
+}
+
+// Structure factors of one k vector: charges and (polarizable) dipoles.  In the final
+// pass thread 0 also forms the k vector's energy and virial terms (SOURCE/ewald1p.f:695-733).
+__global__ void __launch_bounds__(kSfThreads) k_pol_sf(KArgs k, PolArgs a, int final_pass) {
+    const int kk = blockIdx.x;
+    const double2* e = k.eik + (size_t)kk * k.n;
+    double v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (int j = threadIdx.x; j < k.n; j += kSfThreads) {
+        const double2 cs = e[j];
+        const double qj = a.q[j];
+        v[0] += qj * cs.x;
+        v[1] += qj * cs.y;
+        if (a.polr2[j] > 1e-6) {
+            const double m[3] = {a.mx[j], a.my[j], a.mz[j]};
+            v[2] += cs.x * m[0]; v[3] += cs.x * m[1]; v[4] += cs.x * m[2];
+            v[5] += cs.y * m[0]; v[6] += cs.y * m[1]; v[7] += cs.y * m[2];
+        }
+    }
+    __shared__ double tot[8];
+    block_reduce_store<8>(v, tot);
+    __syncthreads();
+    if (threadIdx.x < 8) k.sf[8 * (size_t)kk + threadIdx.x] = tot[threadIdx.x];
+    if (final_pass && threadIdx.x == 0) {
+        const double4 kv = k.kv[kk];
+        const double2 k2 = k.kx2[kk];
+        const double ckcs = tot[0], ckss = tot[1];
+        const double mc[3] = {tot[2], tot[3], tot[4]}, ms[3] = {tot[5], tot[6], tot[7]};
+        const double skc = kv.x * mc[0] + kv.y * mc[1] + kv.z * mc[2];
+        const double sks = kv.x * ms[0] + kv.y * ms[1] + kv.z * ms[2];
+        const double summu1 = ckcs - sks, summu2 = ckss + skc;
+        const double akk = kv.w, akv = 2.0 * akk * (1.0 / k2.x - k.ralph);
+        const double s2 = summu1 * summu1 + summu2 * summu2;
+        const double virprs = akv * s2;
+        const double k3[3] = {kv.x, kv.y, kv.z};
+        const int oa[6] = {0, 1, 2, 0, 0, 1}, ob[6] = {0, 1, 2, 1, 2, 2};
+        double* t = k.kterm + 8 * (size_t)kk;
+        t[0] = akk * (ckcs * ckcs + ckss * ckss);
+        t[1] = akk * s2;
+        for (int q = 0; q < 6; ++q)
+            t[2 + q] = -virprs * k3[oa[q]] * k3[ob[q]] - 2.0 * akk * k3[oa[q]] * ms[ob[q]] * summu1 +
+                       2.0 * akk * k3[oa[q]] * mc[ob[q]] * summu2;
+    }
+}
+
+// k-space fields per site (iflag 0): the dipole field and, in the first pass, the static
+// charge field; thread per site, k vectors staged through shared memory.
+__global__ void __launch_bounds__(kThreads) k_pol_kfield(KArgs k, PolArgs a, int first) {
+    __shared__ double sh[kKTile][8];
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool pol = j < k.n && a.polr2[j] > 1e-6;
+    double em[3] = {0, 0, 0}, ec[3] = {0, 0, 0};
+    for (int t0 = 0; t0 < k.K; t0 += kKTile) {
+        const int nt = min(kKTile, k.K - t0);
+        __syncthreads();
+        for (int u = threadIdx.x; u < nt; u += blockDim.x) {
+            const double4 kv = k.kv[t0 + u];
+            const double* s = k.sf + 8 * (size_t)(t0 + u);
+            sh[u][0] = kv.x; sh[u][1] = kv.y; sh[u][2] = kv.z; sh[u][3] = kv.w;
+            sh[u][4] = s[0]; sh[u][5] = s[1];
+            sh[u][6] = kv.x * s[2] + kv.y * s[3] + kv.z * s[4];   // k . Mc
+            sh[u][7] = kv.x * s[5] + kv.y * s[6] + kv.z * s[7];   // k . Ms
+        }
+        __syncthreads();
+        if (j < k.n) {
+            for (int u = 0; u < nt; ++u) {
+                const double2 cs = k.eik[(size_t)(t0 + u) * k.n + j];
+                const double akk = sh[u][3];
+                if (first) {
+                    const double tt = -cs.y * sh[u][4] + cs.x * sh[u][5];
+                    ec[0] -= sh[u][0] * akk * tt;
+                    ec[1] -= sh[u][1] * akk * tt;
+                    ec[2] -= sh[u][2] * akk * tt;
+                }
+                if (pol) {
+                    const double vv = cs.y * sh[u][7] + cs.x * sh[u][6];
+                    em[0] -= sh[u][0] * akk * vv;
+                    em[1] -= sh[u][1] * akk * vv;
+                    em[2] -= sh[u][2] * akk * vv;
+                }
+            }
+        }
+    }
+    if (j >= k.n) return;
+    const double dum = 4.0 * kR4pie0 * (a.alpha * a.alpha * a.alpha) / kSqrpi / 3.0;
+    const double m[3] = {a.mx[j], a.my[j], a.mz[j]};
+    for (int c = 0; c < 3; ++c) {
+        if (first) a.efc[c * k.n + j] = k.scale * ec[c];
+        a.efm[c * k.n + j] = k.scale * em[c] + dum * m[c];
+    }
+}
+
+// iter (SOURCE/iter.f): SOR update of the dipoles; sum of squared changes and count.
+__global__ void __launch_bounds__(kThreads) k_pol_iter(PolArgs a) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double v[2] = {0, 0};
+    if (i < a.n && a.polr2[i] > a.toler) {
+        const double oldfac = a.omega, fac = 1.0 - oldfac;
+        double* m[3] = {a.mx + i, a.my + i, a.mz + i};
+        double dd = 0.0;
+        for (int c = 0; c < 3; ++c) {
+            const double o = *m[c];
+            const double f = a.efk[c * a.n + i] + a.emu[c * a.n + i] + a.efm[c * a.n + i] + a.efc[c * a.n + i] + 0.0;
+            const double nv = oldfac * o + fac * a.polr2[i] * f / kR4pie0;
+            *m[c] = nv;
+            dd += (nv - o) * (nv - o);
+        }
+        v[0] = dd;
+        v[1] = 1.0;
+    }
+    block_sum_atomic<2>(v, a.acc + 27);
+}
+
+// Final k-space pass (ewald1p iflag 1) per site, fused with coulomb_polar and the
+// self terms: forces, DMS potentials, per-site energies, the ew1p heat-current stress.
+__global__ void __launch_bounds__(kThreads) k_pol_kforce(KArgs k, PolArgs a, int heat) {
+    __shared__ double sh[kKTile][18];
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool in = j < k.n;
+    const double qj = in ? a.q[j] : 0.0;
+    const bool pol = in && a.polr2[j] > 1e-6;
+    const double dv[3] = {in ? a.mx[j] : 0.0, in ? a.my[j] : 0.0, in ? a.mz[j] : 0.0};
+    double vh[3] = {0, 0, 0};
+    if (in && heat) vhat(a, j, vh);
+    double fk[3] = {0, 0, 0}, vk = 0, vdk = 0, aek = 0, jp[3] = {0, 0, 0};
+    const double scalefactor = 0.5 * k.scale;   // 2 rvolm r4pie0 / epsq
+    for (int t0 = 0; t0 < k.K; t0 += kKTile) {
+        const int nt = min(kKTile, k.K - t0);
+        __syncthreads();
+        for (int u = threadIdx.x; u < nt; u += blockDim.x) {
+            const double4 kv = k.kv[t0 + u];
+            const double2 k2 = k.kx2[t0 + u];
+            const double* s = k.sf + 8 * (size_t)(t0 + u);
+            const double skc = kv.x * s[2] + kv.y * s[3] + kv.z * s[4];
+            const double sks = kv.x * s[5] + kv.y * s[6] + kv.z * s[7];
+            double* r = sh[u];
+            r[0] = kv.x; r[1] = kv.y; r[2] = kv.z; r[3] = kv.w;
+            r[4] = s[0]; r[5] = s[1]; r[6] = skc; r[7] = sks;
+            r[8] = s[0] - sks; r[9] = s[1] + skc;   // summu1, summu2
+            r[10] = k2.y;                            // akv2
+            for (int c = 0; c < 6; ++c) r[11 + c] = s[2 + c];
+        }
+        __syncthreads();
+        if (!in) continue;
+        for (int u = 0; u < nt; ++u) {
+            const double* r = sh[u];
+            const double2 cs = k.eik[(size_t)(t0 + u) * k.n + j];
+            const double c = cs.x, s = cs.y;
+            const double akk = r[3];
+            const double djmuk = pol ? dv[0] * r[0] + dv[1] * r[1] + dv[2] * r[2] : 0.0;
+            const double ssmu = r[8] * (-s * qj - c * djmuk) + r[9] * (-s * djmuk + c * qj);
+            fk[0] -= r[0] * akk * ssmu;
+            fk[1] -= r[1] * akk * ssmu;
+            fk[2] -= r[2] * akk * ssmu;
+            vk += akk * (c * r[4] + s * r[5]);
+            vdk += akk * (s * r[6] - c * r[7]);
+            const double Cqi = qj * c, Sqi = qj * s;
+            aek += scalefactor * akk * (Cqi * r[4] + Sqi * r[5]);
+            if (heat) {
+                const double kvec[3] = {r[0], r[1], r[2]};
+                const double* Mc = r + 11;
+                const double* Ms = r + 14;
+                const double CMi[3] = {dv[0] * c, dv[1] * c, dv[2] * c};
+                const double SMi[3] = {dv[0] * s, dv[1] * s, dv[2] * s};
+                const double dpkCMi = kvec[0] * CMi[0] + kvec[1] * CMi[1] + kvec[2] * CMi[2];
+                const double dpkSMi = kvec[0] * SMi[0] + kvec[1] * SMi[1] + kvec[2] * SMi[2];
+                const double dpkMc = r[6], dpkMs = r[7];
+                const double X = (Cqi * r[4] + Sqi * r[5]) + (Sqi * dpkMc - Cqi * dpkMs - dpkSMi * r[4] + dpkCMi * r[5]) +
+                                 (dpkCMi * dpkMc + dpkSMi * dpkMs);
+                double Y[3];
+                for (int b = 0; b < 3; ++b)
+                    Y[b] = (Sqi * Mc[b] - Cqi * Ms[b] - SMi[b] * r[4] + CMi[b] * r[5]) +
+                           (CMi[b] * dpkMc + SMi[b] * dpkMs + dpkCMi * Mc[b] + dpkSMi * Ms[b]);
+                const double f = scalefactor * akk;
+                double S[6];   // upper triangle 11 12 13 22 23 33
+                const int ia[6] = {0, 0, 0, 1, 1, 2}, ib[6] = {0, 1, 2, 1, 2, 2};
+#pragma unroll
+                for (int p = 0; p < 6; ++p)
+                    S[p] = f * (((ia[p] == ib[p] ? 1.0 : 0.0) - r[10] * kvec[ia[p]] * kvec[ib[p]]) * X + kvec[ia[p]] * Y[ib[p]]);
+                jp[0] += S[0] * vh[0] + S[1] * vh[1] + S[2] * vh[2];
+                jp[1] += S[1] * vh[0] + S[3] * vh[1] + S[4] * vh[2];
+                jp[2] += S[2] * vh[0] + S[4] * vh[1] + S[5] * vh[2];
+            }
+        }
+    }
+    double red[6] = {0, 0, 0, 0, 0, 0};   // engsic, eng_polar, jpot(3), unused
+    if (in) {
+        a.fx[j] += k.scale * fk[0];
+        a.fy[j] += k.scale * fk[1];
+        a.fz[j] += k.scale * fk[2];
+        a.vesp[j] = k.scale * vk + k.scale * vdk - 2.0 * kR4pie0 * qj * a.alpha / kSqrpi / a.eps;
+        const double self = -kR4pie0 / a.eps * a.alpha * qj * qj / kSqrpi;
+        double ae = self + aek;
+        red[0] = self;
+        if (pol) {   // coulomb_polar
+            double e = 0.0;
+            for (int c = 0; c < 3; ++c)
+                e += dv[c] * (a.efk[c * k.n + j] + a.efc[c * k.n + j] + 0.5 * (a.emu[c * k.n + j] + a.efm[c * k.n + j]) + 0.0);
+            e = -e;
+            const double edum = dv[0] * dv[0] + dv[1] * dv[1] + dv[2] * dv[2];
+            const double sp = kR4pie0 * edum / a.polr2[j] / 2.0;
+            ae += e + sp;
+            red[1] = e + sp;
+        }
+        a.ae[j] = ae;
+        red[2] = jp[0]; red[3] = jp[1]; red[4] = jp[2];
+    }
+    block_sum_atomic<6>(red, a.acc + 40);
+}
+
+// --- final real-space terms ----------------------------------------------------------------
+// ewald2p for the directed pair (i, j): force on i, its per-atom energy half, its DMS
+// potential; pair scalars only from i < j.
+__global__ void __launch_bounds__(kThreads) k_pol_ewald2p(PolArgs a, double g34, int heat) {
+    const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    double red[11] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};   // eng, vir, stress(6), jpot(3)
+    if (i < a.n) {
+        const int nn = a.nn[i];
+        const size_t row = (size_t)i * a.cap;
+        const double qi = a.q[i];
+        const double mi[3] = {a.mx[i], a.my[i], a.mz[i]};
+        const bool poli = a.polr2[i] > 1e-6;
+        double f[3] = {0, 0, 0}, aei = 0, vsp = 0;
+        for (int k = lane; k < nn; k += 32) {
+            const int j = a.nbr[row + k];
+            double d[3];
+            sep(a, i, j, d[0], d[1], d[2]);
+            const double rsq = norm2(d[0], d[1], d[2]);
+            if (!(a.rcsq > rsq)) continue;
+            const double rrr = __dsqrt_rn(rsq);
+            double bbb[4];
+            interp(a, rrr, bbb);
+            const double rri = 1.0 / rrr, rsqi = 1.0 / rsq, r3i = 1.0 / (rrr * rrr * rrr), r5i = r3i * rsqi;
+            const double qj = a.q[j];
+            const double cicj = qi * qj;
+            const double edum = cicj * (bbb[0] + 1.0 / rrr) * kR4pie0;
+            double eng = edum;
+            aei += 0.5 * edum;
+            double espdum = (bbb[0] + 1.0 / rrr) * kR4pie0;
+            double ffac = cicj * (r3i + bbb[1]) * kR4pie0;
+            const double bb = pow(a.polr[i] * a.polr[j], 1.0 / 6.0);
+            {
+                const double arob4 = a.ascc * pow4(rrr / bb);
+                const double dum1 = exp(-arob4);
+                // beyond exp's range both terms vanish (the reference adds zeros there)
+                const double gq = arob4 < 700.0 ? gammq(0.75, arob4) : 0.0;
+                const double sm = (dum1 - pow(arob4, 0.25) * g34 * gq) / rrr * kR4pie0;
+                eng -= cicj * sm;
+                aei += -cicj * 0.5 * (dum1 - pow(arob4, 0.25) * g34 * gq) / rrr * kR4pie0;
+                espdum -= sm;
+                ffac = ffac - cicj * r3i * dum1 * kR4pie0;
+            }
+            const double mj[3] = {a.mx[j], a.my[j], a.mz[j]};
+            const double rdmui = mi[0] * d[0] + mi[1] * d[1] + mi[2] * d[2];
+            const double rdmuj = mj[0] * d[0] + mj[1] * d[1] + mj[2] * d[2];
+            const double facmu0 = (qj * rdmui - qi * rdmuj) * (-3.0) * r5i * kR4pie0;
+            const double facmui0 = r3i * qj * kR4pie0;
+            const double facmuj0 = -r3i * qi * kR4pie0;
+            double facmu = facmu0 - (qj * rdmui - qi * rdmuj) * bbb[2] * kR4pie0;
+            double dfi = facmui0 + bbb[1] * qj * kR4pie0;
+            double dfj = facmuj0 - bbb[1] * qi * kR4pie0;
+            double espdc = (bbb[1] + r3i) * kR4pie0;
+            {
+                const double arob4 = a.ascd * pow4(rrr / bb);
+                const double dum1 = exp(-arob4);
+                const double dum2 = (1.0 + (4.0 / 3.0) * arob4) * dum1;
+                facmu = facmu - facmu0 * dum2;
+                dfi = dfi - facmui0 * dum1;
+                dfj = dfj - facmuj0 * dum1;
+                espdc = espdc - r3i * dum1 * kR4pie0;
+            }
+            if (poli && a.polr2[j] > 1e-6) {
+                const double dpidpj = mi[0] * mj[0] + mi[1] * mj[1] + mi[2] * mj[2];
+                facmu = facmu + ((dpidpj * 3.0 + rdmui * rdmuj * rsqi * (-15.0)) * r5i + bbb[2] * dpidpj -
+                                 bbb[3] * rdmui * rdmuj) * kR4pie0;
+                dfi = dfi + (3.0 * r5i + bbb[2]) * rdmuj * kR4pie0;
+                dfj = dfj + (3.0 * r5i + bbb[2]) * rdmui * kR4pie0;
+                const double facmu1 = -15.0 * rdmui * rdmuj * rsqi * r5i * kR4pie0;
+                const double facmu2 = 3.0 * dpidpj * r5i * kR4pie0;
+                const double dfi1 = 3.0 * rdmuj * r5i * kR4pie0;
+                const double dfj1 = 3.0 * rdmui * r5i * kR4pie0;
+                const double bb4 = pow4(bb);
+                const double arob4 = a.athole * pow4(rrr / bb);
+                const double dum1 = exp(-arob4);
+                const double dum2 = (1.0 + (4.0 / 3.0) * arob4) * dum1;
+                const double dum3 = 4.0 * a.athole * (4.0 * arob4 - 1.0) * dum1 * rsqi / bb4;
+                const double dum4 = 4.0 * a.athole * dum1 * rrr / bb4;
+                facmu = facmu - facmu1 * dum2 - facmu2 * dum1 + rdmui * rdmuj * dum3 * rri * kR4pie0 -
+                        dpidpj * rsqi * dum4 * kR4pie0;
+                dfi = dfi - dfi1 * dum2;
+                dfj = dfj - dfj1 * dum2;
+            }
+            const double dfx = dfi * mi[0] + dfj * mj[0];
+            const double dfy = dfi * mi[1] + dfj * mj[1];
+            const double dfz = dfi * mi[2] + dfj * mj[2];
+            ffac = ffac + facmu;
+            const double fx = ffac * d[0] + dfx, fy = ffac * d[1] + dfy, fz = ffac * d[2] + dfz;
+            f[0] += fx; f[1] += fy; f[2] += fz;
+            vsp += qj * espdum + rdmuj * espdc;
+            if (heat) heat_entry(a, i, j, fx, fy, fz, red + 8);
+            if (j > i) {
+                const double virdum = dfx * d[0] + dfy * d[1] + dfz * d[2];
+                red[0] += eng;
+                red[1] += -ffac * rsq - virdum;
+                red[2] += d[0] * fx; red[3] += d[0] * fy; red[4] += d[0] * fz;
+                red[5] += d[1] * fy; red[6] += d[1] * fz; red[7] += d[2] * fz;
+            }
+        }
+        for (int c = 0; c < 3; ++c) f[c] = warp_sum(f[c]);
+        aei = warp_sum(aei);
+        vsp = warp_sum(vsp);
+        if (lane == 0) {
+            a.fx[i] += f[0];
+            a.fy[i] += f[1];
+            a.fz[i] += f[2];
+            a.ae[i] += aei;
+            a.vesp[i] += vsp;
+        }
+    }
+    block_sum_atomic<11>(red, a.acc + 0);
+}
+
+// ewald3p over the six excluded pairs of one water (thread per water).
+__global__ void __launch_bounds__(kThreads) k_pol_ewald3p(PolArgs a, int heat) {
+    const int w = blockIdx.x * blockDim.x + threadIdx.x;
+    double red[11] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    if (w < a.nw) {
+        const int o = 3 * w, m = 3 * a.nw + w;
+        const int pr[6][2] = {{o, o + 1}, {o, o + 2}, {o + 1, o + 2}, {o, m}, {o + 1, m}, {o + 2, m}};
+        const double r4e = kR4pie0 / a.eps;
+        for (int p = 0; p < 6; ++p) {
+            const int ia = pr[p][0], ja = pr[p][1];
+            double d[3];
+            sep(a, ia, ja, d[0], d[1], d[2]);
+            const double rsq = norm2(d[0], d[1], d[2]);
+            const double rrr = __dsqrt_rn(rsq);
+            const double rri = 1.0 / rrr, rsqi = 1.0 / rsq, r3i = 1.0 / (rrr * rrr * rrr), r5i = r3i * rsqi;
+            double bbb[4];
+            bfun_exact(a.alpha, rrr, rri, rsqi, bbb);
+            const double qi = a.q[ia], qj = a.q[ja];
+            const double cicj = qi * qj;
+            red[0] += cicj * bbb[0] * r4e;
+            a.ae[ia] += 0.5 * cicj * bbb[0] * r4e;
+            a.ae[ja] += 0.5 * cicj * bbb[0] * r4e;
+            const double espdum = bbb[0] * r4e, espdc = bbb[1] * r4e;
+            double ffac = cicj * bbb[1] * r4e;
+            const double mi[3] = {a.mx[ia], a.my[ia], a.mz[ia]}, mj[3] = {a.mx[ja], a.my[ja], a.mz[ja]};
+            const double rdmui = mi[0] * d[0] + mi[1] * d[1] + mi[2] * d[2];
+            const double rdmuj = mj[0] * d[0] + mj[1] * d[1] + mj[2] * d[2];
+            double facmu = (qj * rdmui - qi * rdmuj) * (-bbb[2]) * r4e;
+            double dfi = bbb[1] * qj * r4e;
+            double dfj = -bbb[1] * qi * r4e;
+            if (a.polr2[ia] > 1e-6 && a.polr2[ja] > 1e-6) {
+                const double dpidpj = mi[0] * mj[0] + mi[1] * mj[1] + mi[2] * mj[2];
+                facmu = facmu + (bbb[2] * dpidpj - bbb[3] * rdmui * rdmuj) * r4e;
+                dfi = dfi + bbb[2] * rdmuj * r4e;
+                dfj = dfj + bbb[2] * rdmui * r4e;
+                const double facmu1 = -15.0 * rdmui * rdmuj * rsqi * r5i * r4e;
+                const double facmu2 = 3.0 * dpidpj * r5i * r4e;
+                facmu = facmu + facmu1 + facmu2;
+                const double dfidd = 3.0 * rdmuj * r5i * r4e, dfjdd = 3.0 * rdmui * r5i * r4e;
+                dfi = dfi + dfidd;
+                dfj = dfj + dfjdd;
+                const double bb = pow(a.polr[ia] * a.polr[ja], 1.0 / 6.0);
+                const double bb4 = pow4(bb);
+                const double ath = (ia % 3 == 0 || ja % 3 == 0) ? a.athole12 : a.athole13;
+                const double arob4 = ath * pow4(rrr / bb);
+                const double dum1 = exp(-arob4);
+                const double dum2 = (1.0 + (4.0 / 3.0) * arob4) * dum1;
+                const double dum3 = 4.0 * ath * (4.0 * arob4 - 1.0) * dum1 * rsqi / bb4;
+                const double dum4 = 4.0 * ath * dum1 * rrr / bb4;
+                facmu = facmu - facmu1 * dum2 - facmu2 * dum1 + rdmui * rdmuj * dum3 * rri * r4e - dpidpj * rsqi * dum4 * r4e;
+                dfi = dfi - dfidd * dum2;
+                dfj = dfj - dfjdd * dum2;
+            }
+            const double dfx = dfi * mi[0] + dfj * mj[0];
+            const double dfy = dfi * mi[1] + dfj * mj[1];
+            const double dfz = dfi * mi[2] + dfj * mj[2];
+            ffac = ffac + facmu;
+            const double fx = ffac * d[0] + dfx, fy = ffac * d[1] + dfy, fz = ffac * d[2] + dfz;
+            a.fx[ia] += fx; a.fy[ia] += fy; a.fz[ia] += fz;
+            a.fx[ja] -= fx; a.fy[ja] -= fy; a.fz[ja] -= fz;
+            if (heat) {
+                heat_entry(a, ia, ja, fx, fy, fz, red + 8);
+                heat_entry(a, ja, ia, -fx, -fy, -fz, red + 8);
+            }
+            const double virdum = dfx * d[0] + dfy * d[1] + dfz * d[2];
+            red[1] += -ffac * rsq - virdum;
+            a.vesp[ia] += qj * espdum + rdmuj * espdc;
+            a.vesp[ja] += qi * espdum - rdmui * espdc;
+            red[2] += d[0] * fx; red[3] += d[0] * fy; red[4] += d[0] * fz;
+            red[5] += d[1] * fy; red[6] += d[1] * fz; red[7] += d[2] * fz;
+        }
+    }
+    block_sum_atomic<11>(red, a.acc + 0);
+}
+
+// qdforce (new charge assignment) per water, with the summed DMS potentials.
+__global__ void __launch_bounds__(kThreads) k_pol_qdforce(PolArgs a, int heat) {
+    const int w = blockIdx.x * blockDim.x + threadIdx.x;
+    double red[11] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};   // -, vir, stress(6), jpot(3)
+    if (w < a.nw) {
+        const int io = 3 * w, h1 = io + 1, h2 = io + 2, mt = 3 * a.nw + w;
+        const double* D = a.dp + 6 * (size_t)w;
+        const double dp1dr1 = D[0], dp1dr2 = D[1], dp2dr1 = D[2], dp2dr2 = D[3], dp1dcos = D[4], dp2dcos = D[5];
+        double r1v[3], r2v[3];
+        sep(a, h1, io, r1v[0], r1v[1], r1v[2]);
+        sep(a, h2, io, r2v[0], r2v[1], r2v[2]);
+        const double r1 = sqrt(r1v[0] * r1v[0] + r1v[1] * r1v[1] + r1v[2] * r1v[2]);
+        const double r2 = sqrt(r2v[0] * r2v[0] + r2v[1] * r2v[1] + r2v[2] * r2v[2]);
+        const double rdot = r1v[0] * r2v[0] + r1v[1] * r2v[1] + r1v[2] * r2v[2];
+        const double cost = rdot / (r1 * r2);
+        const double r3 = sqrt(r1 * r1 + r2 * r2 - 2.0 * r1 * r2 * cost);
+        const double sint = sqrt(1.0 - cost * cost);
+        const double cott = cost / sint;
+        const double r1sqr = r1 * r1, r2sqr = r2 * r2;
+        double dr[3][4][3];
+        for (int s = 0; s < 4; ++s)
+            for (int c = 0; c < 3; ++c) dr[0][s][c] = dr[1][s][c] = dr[2][s][c] = 0.0;
+        for (int c = 0; c < 3; ++c) {
+            dr[0][1][c] = r1v[c] / r1;
+            dr[0][0][c] = -dr[0][1][c];
+            dr[1][2][c] = r2v[c] / r2;
+            dr[1][0][c] = -dr[1][2][c];
+            dr[2][1][c] = cott * (r1v[c] / r1sqr - r2v[c] / rdot);
+            dr[2][2][c] = cott * (r2v[c] / r2sqr - r1v[c] / rdot);
+            dr[2][0][c] = -dr[2][1][c] - dr[2][2][c];
+        }
+        const double g = a.gamma;
+        const double tmp = g / 2.0 / (1.0 - g);
+        double dqdr12[4] = {0, 0, 0, 0}, dqdr13[4] = {0, 0, 0, 0}, dqdcos[4] = {0, 0, 0, 0};
+        dqdr12[1] = dp1dr1 + (dp1dr1 + dp2dr1) * tmp;
+        dqdr13[1] = dp1dr2 + (dp1dr2 + dp2dr2) * tmp;
+        dqdcos[1] = dp1dcos + (dp1dcos + dp2dcos) * tmp;
+        dqdr12[2] = dp2dr1 + (dp1dr1 + dp2dr1) * tmp;
+        dqdr13[2] = dp2dr2 + (dp1dr2 + dp2dr2) * tmp;
+        dqdcos[2] = dp2dcos + (dp1dcos + dp2dcos) * tmp;
+        dqdr12[3] = -(dp1dr1 + dp2dr1) / (1.0 - g);
+        dqdr13[3] = -(dp1dr2 + dp2dr2) / (1.0 - g);
+        dqdcos[3] = -(dp1dcos + dp2dcos) / (1.0 - g);
+        const double dcosdr12 = (r1 - r2 * cost) / r1 / r2;
+        const double dcosdr13 = (r2 - r1 * cost) / r1 / r2;
+        const double dcosdr23 = -r3 / r1 / r2;
+        const int site[4] = {io, h1, h2, mt};
+        double vt[4];
+        for (int s = 0; s < 4; ++s) vt[s] = a.vesp[site[s]];
+        double fs[4][3];
+        for (int s = 0; s < 4; ++s) fs[s][0] = fs[s][1] = fs[s][2] = 0.0;
+        for (int s = 0; s < 4; ++s) {   // site whose position moves the charges
+            double dp1[3], dp2[3];
+            for (int c = 0; c < 3; ++c) {
+                dp1[c] = dp1dr1 * dr[0][s][c] + dp1dr2 * dr[1][s][c] - sint * dp1dcos * dr[2][s][c];
+                dp2[c] = dp2dr1 * dr[0][s][c] + dp2dr2 * dr[1][s][c] - sint * dp2dcos * dr[2][s][c];
+            }
+            double dq[4][3];
+            const double factor = g / 2.0 / (1.0 - g);
+            for (int c = 0; c < 3; ++c) {
+                dq[0][c] = 0.0;
+                dq[1][c] = dp1[c] * (factor + 1.0) + dp2[c] * factor;
+                dq[2][c] = dp2[c] * (factor + 1.0) + dp1[c] * factor;
+                dq[3][c] = -(dq[1][c] + dq[2][c]);
+            }
+            for (int j = 0; j < 4; ++j) {   // charge j, in the reference's loop order
+                const double F[3] = {-dq[j][0] * vt[j], -dq[j][1] * vt[j], -dq[j][2] * vt[j]};
+                for (int c = 0; c < 3; ++c) fs[s][c] += F[c];
+                if (heat) heat_entry(a, site[s], j == 3 ? a.nw + w : 3 * w + j, F[0], F[1], F[2], red + 8);
+            }
+        }
+        a.fx[io] += fs[0][0]; a.fy[io] += fs[0][1]; a.fz[io] += fs[0][2];
+        a.fx[h1] += fs[1][0]; a.fy[h1] += fs[1][1]; a.fz[h1] += fs[1][2];
+        a.fx[h2] += fs[2][0]; a.fy[h2] += fs[2][1]; a.fz[h2] += fs[2][2];
+        a.fx[mt] += fs[3][0]; a.fy[mt] += fs[3][1]; a.fz[mt] += fs[3][2];
+        double sq[6] = {0, 0, 0, 0, 0, 0}, virq = 0.0;
+        const int ta[6] = {0, 0, 0, 1, 1, 2}, tb[6] = {0, 1, 2, 1, 2, 2};
+        for (int s = 0; s < 4; ++s) {
+            const double v = vt[s];
+            for (int lab = 1; lab <= 2; ++lab) {
+                const double dqdr_tmp = lab == 1 ? dqdr12[s] : dqdr13[s];
+                const int hh = lab == 1 ? h1 : h2;
+                double r[3];
+                sep(a, io, hh, r[0], r[1], r[2]);
+                const double rjk = sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
+                for (int q = 0; q < 6; ++q) sq[q] = sq[q] - v * dqdr_tmp * r[ta[q]] * r[tb[q]] / rjk;
+                virq = virq + v * rjk * dqdr_tmp;
+            }
+            double a1[3], a2[3], a3[3];
+            sep(a, io, h1, a1[0], a1[1], a1[2]);
+            sep(a, io, h2, a2[0], a2[1], a2[2]);
+            sep(a, h1, h2, a3[0], a3[1], a3[2]);
+            const double q1 = sqrt(a1[0] * a1[0] + a1[1] * a1[1] + a1[2] * a1[2]);
+            const double q2 = sqrt(a2[0] * a2[0] + a2[1] * a2[1] + a2[2] * a2[2]);
+            const double q3 = sqrt(a3[0] * a3[0] + a3[1] * a3[1] + a3[2] * a3[2]);
+            double dc[6];
+            for (int q = 0; q < 6; ++q)
+                dc[q] = dcosdr12 * a1[ta[q]] * a1[tb[q]] / q1 + dcosdr13 * a2[ta[q]] * a2[tb[q]] / q2 +
+                        dcosdr23 * a3[ta[q]] * a3[tb[q]] / q3;
+            for (int q = 0; q < 6; ++q) sq[q] = sq[q] - v * dqdcos[s] * dc[q];
+            virq = virq + v * (dc[0] + dc[3] + dc[5]) * dqdcos[s];
+        }
+        red[1] = virq;
+        for (int q = 0; q < 6; ++q) red[2 + q] = sq[q];
+    }
+    block_sum_atomic<11>(red, a.acc + 0);
+}
+
+// jkin's electrostatic part: redistributed per-site energies times velocities; the
+// per-site energies are added to the caller's array.
+__global__ void __launch_bounds__(kThreads) k_pol_jkin(PolArgs a, double* __restrict__ ae_out, int heat) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    double red[3] = {0, 0, 0};
+    if (j < a.n) {
+        const double e = a.ae[j];
+        if (ae_out) ae_out[j] += e;
+        if (heat) {
+            double v[3];
+            vhat(a, j, v);
+            red[0] = e * v[0]; red[1] = e * v[1]; red[2] = e * v[2];
+        }
+    }
+    block_sum_atomic<3>(red, a.acc + 24);
+}
+
+__global__ void k_pol_kreduce(int K, const double* __restrict__ kterm, double* __restrict__ out) {
+    // one block: out[q] = sum over k of kterm[8k + q]
+    double v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (int k = threadIdx.x; k < K; k += blockDim.x)
+        for (int q = 0; q < 8; ++q) v[q] += kterm[8 * (size_t)k + q];
+    __shared__ double red[kSfThreads / 32][8];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int q = 0; q < 8; ++q) {
+        const double s = warp_sum(v[q]);
+        if (lane == 0) red[w][q] = s;
+    }
+    __syncthreads();
+    if (threadIdx.x < 8) {
+        double s = 0.0;
+        for (int i = 0; i < kSfThreads / 32; ++i) s += red[i][threadIdx.x];
+        out[threadIdx.x] = s;
+    }
+}
+
+inline unsigned blocks(long n, int t) { return (unsigned)((n + t - 1) / t); }
+
+}  // namespace
+
+// --- host -------------------------------------------------------------------------------
+void PolarState::release() {
+    void* p[] = {ercp, nn, nbr, flag, xf, tens, intra, fld, vesp, ae, eik, kv, kx2, lmn, sf, kterm, acc};
+    for (void* q : p)
+        if (q) cudaFree(q);
+    if (acc_h) cudaFreeHost(acc_h);
+    ercp = nullptr;
+    nn = nbr = flag = nullptr;
+    xf = nullptr;
+    tens = intra = fld = vesp = ae = sf = kterm = acc = nullptr;
+    eik = nullptr;
+    kv = nullptr;
+    kx2 = nullptr;
+    lmn = nullptr;
+    acc_h = nullptr;
+    n_cap = nw_cap = k_cap = 0;
+    eik_cap = 0;
+    tab_alpha = tab_rcut = -1.0;
+}
+
+PolarState::~PolarState() { release(); }
+
+cudaError_t PolarState::table(double alpha, double rcut) {
+    if (ercp && alpha == tab_alpha && rcut == tab_rcut) return cudaSuccess;
+    if (ercp) cudaFree(ercp);
+    ercp = nullptr;
+    mxegrd = std::max(1000, (int)(rcut / 0.0001 + 0.5) + 4);
+    drewd = rcut / double(mxegrd - 4);
+    std::vector<double4> h((size_t)mxegrd + 1, make_double4(0, 0, 0, 0));
+    for (int i = 1; i <= mxegrd; ++i) {   // erfcgenp (SOURCE/erfcgenp.f:26-46)
+        const double rrr = double(i) * drewd;
+        const double rsqi = 1.0 / rrr / rrr;
+        const double a = alpha * rrr;
+        double c[4];
+        c[0] = (erfcc(a) - 1.0) / rrr;
+        const double exp2a = std::exp(-a * a);
+        for (int n = 1; n <= 3; ++n) {
+            const double fn = n;
+            c[n] = rsqi * ((2.0 * fn - 1.0) * c[n - 1] + std::pow(2.0 * (alpha * alpha), fn) * exp2a / alpha / kSqrpi);
+        }
+        h[i] = make_double4(c[0], c[1], c[2], c[3]);
+    }
+    cudaError_t e;
+    if ((e = cudaMalloc(&ercp, h.size() * sizeof(double4)))) return e;
+    if ((e = cudaMemcpy(ercp, h.data(), h.size() * sizeof(double4), cudaMemcpyHostToDevice))) return e;
+    tab_alpha = alpha;
+    tab_rcut = rcut;
+    return cudaSuccess;
+}
+
+cudaError_t PolarState::reserve(int nw, int K) {
+    cudaError_t e;
+    const int n = 4 * nw;
+    if (!acc && (e = cudaMalloc(&acc, 64 * sizeof(double)))) return e;
+    if (!acc_h && (e = cudaMallocHost(&acc_h, 64 * sizeof(double)))) return e;
+    if (!flag && (e = cudaMalloc(&flag, 4 * sizeof(int)))) return e;
+    if (n > n_cap || cap != cap_alloc) {
+        void* p[] = {nn, nbr, xf, tens, fld, vesp, ae};
+        for (void* q : p)
+            if (q) cudaFree(q);
+        nn = nbr = nullptr;
+        xf = nullptr;
+        tens = fld = vesp = ae = nullptr;
+        const size_t m = (size_t)std::max(n, 1);
+        if ((e = cudaMalloc(&nn, m * sizeof(int)))) return e;
+        if ((e = cudaMalloc(&nbr, m * cap * sizeof(int)))) return e;
+        if ((e = cudaMalloc(&xf, m * sizeof(float4)))) return e;
+        if ((e = cudaMalloc(&tens, 6 * m * cap * sizeof(double)))) return e;
+        if ((e = cudaMalloc(&fld, 12 * m * sizeof(double)))) return e;
+        if ((e = cudaMalloc(&vesp, m * sizeof(double)))) return e;
+        if ((e = cudaMalloc(&ae, m * sizeof(double)))) return e;
+        n_cap = n;
+        cap_alloc = cap;
+    }
+    if (nw > nw_cap) {
+        if (intra) cudaFree(intra);
+        intra = nullptr;
+        if ((e = cudaMalloc(&intra, 18 * (size_t)std::max(nw, 1) * sizeof(double)))) return e;
+        nw_cap = nw;
+    }
+    if (K > k_cap) {
+        void* p[] = {kv, kx2, lmn, sf, kterm};
+        for (void* q : p)
+            if (q) cudaFree(q);
+        kv = nullptr;
+        kx2 = nullptr;
+        lmn = nullptr;
+        sf = kterm = nullptr;
+        if ((e = cudaMalloc(&kv, K * sizeof(double4)))) return e;
+        if ((e = cudaMalloc(&kx2, K * sizeof(double2)))) return e;
+        if ((e = cudaMalloc(&lmn, K * sizeof(int4)))) return e;
+        if ((e = cudaMalloc(&sf, 8 * (size_t)K * sizeof(double)))) return e;
+        if ((e = cudaMalloc(&kterm, 8 * (size_t)K * sizeof(double)))) return e;
+        k_cap = K;
+    }
+    const size_t need = (size_t)K * n;
+    if (need > eik_cap) {
+        if (eik) cudaFree(eik);
+        eik = nullptr;
+        if ((e = cudaMalloc(&eik, std::max(need, (size_t)1) * sizeof(double2)))) return e;
+        eik_cap = need;
+    }
+    return cudaSuccess;
+}
+
+cudaError_t PolarState::run(const Cell& cl, const double* prm, int nw, const double* x, const double* y,
+                            const double* z, const double* q, const double* dp, const double* polr,
+                            const double* polr2, double* mx, double* my, double* mz, double* fx, double* fy,
+                            double* fz, double* ae_out, const double* vx, const double* vy, const double* vz,
+                            double* out16, double* jpot, double* jkin, cudaStream_t s) {
+    cudaError_t e;
+    converged = false;
+    iterations = 0;
+    launches = 0;
+    const int n = 4 * nw;
+    const double alpha = prm[0], rcut = prm[1], epsq = prm[2];
+    const int kmax[3] = {(int)prm[11], (int)prm[12], (int)prm[13]};
+    const int maxit = (int)prm[14];
+    if ((e = table(alpha, rcut))) return e;
+
+    // k vectors in ewald1p's order (SOURCE/ewald1p.f:159-172, :279-348)
+    double rc[9];
+    {
+        const double* a = cl.c;
+        double b[9];
+        b[0] = a[4] * a[8] - a[5] * a[7];
+        b[1] = a[2] * a[7] - a[1] * a[8];
+        b[2] = a[1] * a[5] - a[2] * a[4];
+        b[3] = a[5] * a[6] - a[3] * a[8];
+        b[4] = a[0] * a[8] - a[2] * a[6];
+        b[5] = a[2] * a[3] - a[0] * a[5];
+        b[6] = a[3] * a[7] - a[4] * a[6];
+        b[7] = a[1] * a[6] - a[0] * a[7];
+        b[8] = a[0] * a[4] - a[1] * a[3];
+        const double d = a[0] * b[0] + a[3] * b[1] + a[6] * b[2];
+        const double r = std::fabs(d) > 0.0 ? 1.0 / d : 0.0;
+        for (int k = 0; k < 9; ++k) rc[k] = r * b[k];
+    }
+    auto widths = [](const double* aa, double* w3, double* vol) {
+        const double axb1 = aa[1] * aa[5] - aa[2] * aa[4], axb2 = aa[2] * aa[3] - aa[0] * aa[5],
+                     axb3 = aa[0] * aa[4] - aa[1] * aa[3];
+        const double bxc1 = aa[4] * aa[8] - aa[5] * aa[7], bxc2 = aa[5] * aa[6] - aa[3] * aa[8],
+                     bxc3 = aa[3] * aa[7] - aa[4] * aa[6];
+        const double cxa1 = aa[7] * aa[2] - aa[1] * aa[8], cxa2 = aa[0] * aa[8] - aa[2] * aa[6],
+                     cxa3 = aa[1] * aa[6] - aa[0] * aa[7];
+        const double v = std::fabs(aa[0] * bxc1 + aa[1] * bxc2 + aa[2] * bxc3);
+        w3[0] = v / std::sqrt(bxc1 * bxc1 + bxc2 * bxc2 + bxc3 * bxc3);
+        w3[1] = v / std::sqrt(cxa1 * cxa1 + cxa2 * cxa2 + cxa3 * cxa3);
+        w3[2] = v / std::sqrt(axb1 * axb1 + axb2 * axb2 + axb3 * axb3);
+        *vol = v;
+    };
+    double wc[3], wr[3], volm, vr;
+    widths(cl.c, wc, &volm);
+    widths(rc, wr, &vr);
+    const double twopi = 2.0 * kPi;
+    const double rvolm = twopi / volm, ralph = -0.25 / (alpha * alpha);
+    double rcpcut = std::min(std::min(double(kmax[0]) * wr[0], double(kmax[1]) * wr[1]), double(kmax[2]) * wr[2]);
+    rcpcut = rcpcut * 1.05 * twopi;
+    const double rcpct2 = rcpcut * rcpcut;
+    hk.clear();
+    hk2.clear();
+    hlmn.clear();
+    {
+        int mmin = 0, nmin = 1;
+        for (int ll = 0; ll <= kmax[0]; ++ll) {
+            const double t0 = twopi * double(ll);
+            const double rkx1 = t0 * rc[0], rky1 = t0 * rc[3], rkz1 = t0 * rc[6];
+            for (int mm = mmin; mm <= kmax[1]; ++mm) {
+                const double t1 = twopi * double(mm);
+                const double rkx2 = rkx1 + t1 * rc[1], rky2 = rky1 + t1 * rc[4], rkz2 = rkz1 + t1 * rc[7];
+                for (int nn_ = nmin; nn_ <= kmax[2]; ++nn_) {
+                    const double t2 = twopi * double(nn_);
+                    const double rkx3 = rkx2 + t2 * rc[2], rky3 = rky2 + t2 * rc[5], rkz3 = rkz2 + t2 * rc[8];
+                    const double rksq = rkx3 * rkx3 + rky3 * rky3 + rkz3 * rkz3;
+                    if (rksq <= rcpct2) {
+                        const double rrksq = 1.0 / rksq;
+                        hk.push_back(make_double4(rkx3, rky3, rkz3, std::exp(ralph * rksq) * rrksq));
+                        hk2.push_back(make_double2(rksq, 2.0 * (rrksq - ralph)));
+                        hlmn.push_back(make_int4(ll, mm, nn_, 0));
+                    }
+                }
+                nmin = -kmax[2];
+            }
+            mmin = -kmax[1];
+        }
+    }
+    const int K = (int)hk.size();
+    if (n > 65535L * kThreads) return cudaErrorInvalidValue;
+    if ((e = reserve(nw, K))) return e;
+    if (K) {
+        if ((e = cudaMemcpyAsync(kv, hk.data(), K * sizeof(double4), cudaMemcpyHostToDevice, s))) return e;
+        if ((e = cudaMemcpyAsync(kx2, hk2.data(), K * sizeof(double2), cudaMemcpyHostToDevice, s))) return e;
+        if ((e = cudaMemcpyAsync(lmn, hlmn.data(), K * sizeof(int4), cudaMemcpyHostToDevice, s))) return e;
+    }
+    const bool heat = vx && vy && vz;
+
+    PolArgs a;
+    auto bind = [&](PolArgs& b) {
+        b.cap = cap;
+        b.ercp = ercp;
+        b.drewd = drewd;
+        b.nn = nn;
+        b.nbr = nbr;
+        b.tens = tens;
+        b.intra = intra;
+        b.efk = fld;
+        b.efc = fld + 3 * (size_t)n;
+        b.emu = fld + 6 * (size_t)n;
+        b.efm = fld + 9 * (size_t)n;
+        b.vesp = vesp;
+        b.ae = ae;
+        b.acc = acc;
+    };
+    a.cl = cl;
+    a.nw = nw;
+    a.n = n;
+    a.x = x; a.y = y; a.z = z; a.q = q; a.polr = polr; a.polr2 = polr2; a.dp = dp;
+    a.mx = mx; a.my = my; a.mz = mz;
+    a.vx = vx; a.vy = vy; a.vz = vz;
+    a.fx = fx; a.fy = fy; a.fz = fz;
+    a.gamma = prm[10];
+    a.alpha = alpha;
+    a.rcut = rcut;
+    a.rcsq = rcut * rcut;
+    a.eps = epsq;
+    a.athole = prm[5]; a.athole12 = prm[6]; a.athole13 = prm[7]; a.ascc = prm[8]; a.ascd = prm[9];
+    a.toler = prm[3];
+    a.omega = prm[4];
+    bind(a);
+
+    KArgs k;
+    k.K = K;
+    k.n = n;
+    k.kv = kv;
+    k.kx2 = kx2;
+    k.lmn = lmn;
+    k.eik = eik;
+    k.sf = sf;
+    k.kterm = kterm;
+    for (int c = 0; c < 9; ++c) k.rc[c] = rc[c];
+    k.scale = 4.0 * rvolm * kR4pie0 / epsq;
+    k.ralph = ralph;
+
+    if ((e = cudaMemsetAsync(acc, 0, 64 * sizeof(double), s))) return e;
+    if (n == 0) {
+        for (int c = 0; c < 16; ++c) out16[c] = 0.0;
+        converged = true;
+        return cudaSuccess;
+    }
+    // list (grows until every row fits)
+    const float r2f = (float)((rcut + 0.01) * (rcut + 0.01));
+    for (;;) {
+        bind(a);
+        k_pol_f32<<<blocks(n, kThreads), kThreads, 0, s>>>(n, x, y, z, xf);
+        if ((e = cudaMemsetAsync(flag, 0, sizeof(int), s))) return e;
+        k_pol_list<<<blocks(32L * n, kThreads), kThreads, 0, s>>>(a, nn, nbr, xf, r2f, flag);
+        launches += 2;
+        int fh = 0;
+        if ((e = cudaMemcpyAsync(acc_h, flag, sizeof(int), cudaMemcpyDeviceToHost, s))) return e;
+        if ((e = cudaStreamSynchronize(s))) return e;
+        std::memcpy(&fh, acc_h, sizeof(int));
+        if (!fh) break;
+        cap = std::min(2 * cap, std::max(n, 32));   // a row holds at most n - 1 sites
+        if ((e = reserve(nw, K))) return e;
+    }
+    k_pol_static<<<blocks(32L * n, kThreads), kThreads, 0, s>>>(a);
+    k_pol_intra_static<<<blocks(nw, kThreads), kThreads, 0, s>>>(a);
+    launches += 2;
+    if (K) {
+        dim3 g(K, blocks(n, kThreads));   // sites per k vector along y (n < 65535 * 128)
+        k_pol_phase<<<g, kThreads, 0, s>>>(k, x, y, z);
+        ++launches;
+    }
+    double deltadip = 0.0;
+    int status_it = 0;
+    for (int it = 1;; ++it) {
+        k_pol_dd<<<blocks(32L * n, kThreads), kThreads, 0, s>>>(a);
+        if (K) k_pol_sf<<<K, kSfThreads, 0, s>>>(k, a, 0);
+        k_pol_kfield<<<blocks(n, kThreads), kThreads, 0, s>>>(k, a, it == 1);
+        if ((e = cudaMemsetAsync(acc + 27, 0, 2 * sizeof(double), s))) return e;
+        k_pol_iter<<<blocks(n, kThreads), kThreads, 0, s>>>(a);
+        launches += K ? 4 : 3;
+        if ((e = cudaMemcpyAsync(acc_h + 27, acc + 27, 2 * sizeof(double), cudaMemcpyDeviceToHost, s))) return e;
+        if ((e = cudaStreamSynchronize(s))) return e;
+        const double ndip = acc_h[28] > 0.0 ? acc_h[28] : 1.0;
+        deltadip = std::sqrt(acc_h[27] / ndip);
+        iterations = it;
+        if (deltadip <= prm[3]) {
+            converged = true;
+            break;
+        }
+        if (it >= maxit) {
+            status_it = 1;
+            break;
+        }
+    }
+    (void)status_it;
+    // final pass
+    const double g34 = std::exp(gammln(3.0 / 4.0));
+    if (K) k_pol_sf<<<K, kSfThreads, 0, s>>>(k, a, 1);
+    k_pol_kforce<<<blocks(n, kThreads), kThreads, 0, s>>>(k, a, heat);
+    k_pol_ewald2p<<<blocks(32L * n, kThreads), kThreads, 0, s>>>(a, g34, heat);
+    k_pol_ewald3p<<<blocks(nw, kThreads), kThreads, 0, s>>>(a, heat);
+    k_pol_qdforce<<<blocks(nw, kThreads), kThreads, 0, s>>>(a, heat);
+    k_pol_jkin<<<blocks(n, kThreads), kThreads, 0, s>>>(a, ae_out, heat);
+    launches += 5;
+    if (K) {
+        k_pol_kreduce<<<1, kSfThreads, 0, s>>>(K, kterm, acc + 48);
+        launches += 2;
+    }
+    if ((e = cudaGetLastError())) return e;
+    if ((e = cudaMemcpyAsync(acc_h, acc, 64 * sizeof(double), cudaMemcpyDeviceToHost, s))) return e;
+    if ((e = cudaStreamSynchronize(s))) return e;
+    const double* h = acc_h;
+    // acc: 0 eng_real, 1 vir, 2..7 stress (11 12 13 22 23 33), 8..10 jpot (real + qd),
+    //      24..26 jkin, 40 engsic, 41 eng_polar, 42..44 jpot (k space),
+    //      48 engc, 49 engdum, 50..55 omg (11 22 33 12 13 23)
+    const double scal1 = 2.0 * rvolm * kR4pie0 / epsq;
+    const double engc = K ? h[48] : 0.0, eng1 = K ? h[49] : 0.0;
+    const double omg11 = K ? h[50] : 0.0, omg22 = K ? h[51] : 0.0, omg33 = K ? h[52] : 0.0;
+    const double omg12 = K ? h[53] : 0.0, omg13 = K ? h[54] : 0.0, omg23 = K ? h[55] : 0.0;
+    const double engk = 2.0 * rvolm * kR4pie0 * engc / epsq + h[40];
+    const double virk = -scal1 * (omg11 + omg22 + omg33 + 3.0 * eng1);
+    double st[9];
+    st[0] = h[2] + scal1 * (omg11 + eng1);
+    st[1] = h[3] + scal1 * omg12;
+    st[2] = h[4] + scal1 * omg13;
+    st[3] = st[1];
+    st[4] = h[5] + scal1 * (omg22 + eng1);
+    st[5] = h[6] + scal1 * omg23;
+    st[6] = st[2];
+    st[7] = st[5];
+    st[8] = h[7] + scal1 * (omg33 + eng1);
+    out16[0] = engk + h[0] + h[41];
+    out16[1] = h[1] + virk;
+    for (int c = 0; c < 9; ++c) out16[2 + c] = st[c];
+    out16[11] = iterations;
+    out16[12] = deltadip;
+    out16[13] = h[41];
+    out16[14] = engk;
+    out16[15] = h[0];
+    if (heat) {
+        for (int c = 0; c < 3; ++c) {
+            jpot[c] += h[8 + c] + h[42 + c];
+            jkin[c] += h[24 + c];
+        }
+    }
+    return cudaSuccess;
+}
+
+}  // namespace mbx

@@ -17,6 +17,7 @@ HEADER = os.path.join(REPO, "include", "mbx.h")
 
 FP64 = 0
 MIXED = 1
+ERR_CONVERGE = 5
 NSCALARS = 18
 NBOXSCALARS = NSCALARS + 14
 NWATERSCALARS = NSCALARS + 28
@@ -87,6 +88,11 @@ def load(path=None):
     L.mbx_disp_forces.argtypes = [C.c_void_p, C.c_int, _D, C.c_int, _I, _I] + [_D] * 14
     L.mbx_disp_forces_device.argtypes = [C.c_void_p, C.c_int, _D, C.c_int] + [C.c_void_p] * 12 + [_D]
     L.mbx_disp_lrc.argtypes = [C.c_int, _D, _I, C.c_double, C.c_double, _D, _D]
+    L.mbx_polar_forces.argtypes = [C.c_void_p, _D, C.c_int, _D, C.c_int] + [_D] * 20
+    L.mbx_polar_forces_device.argtypes = [C.c_void_p, _D, C.c_int, _D, C.c_int] + [C.c_void_p] * 14 + [_D] + \
+        [C.c_void_p] * 4 + [_D, _D]
+    L.mbx_polar_iterations.argtypes = [C.c_void_p]
+    L.mbx_msite_redistribute.argtypes = [C.c_int, C.c_double, _D, _D, _D]
     L.mbx_disp_list_builds.argtypes = [C.c_void_p]
     L.mbx_disp_list_builds.restype = C.c_long
     L.mbx_set_graphs.argtypes = [C.c_void_p, C.c_int]
@@ -293,6 +299,32 @@ class Context:
                                       _p(stress), _p(v[0]), _p(v[1]), _p(v[2]), _p(ae), _p(jpot))
         self._check(rc, "mbx_disp_forces")
         return dict(eng=eng.value, vir=vir.value, stress=stress, forces=f.T.copy(), atomic_energy=ae, jpot=jpot)
+
+    def polar(self, sites, cell, imcon, nw, chge, dp, polr, polr2, prm, dip0=None, vel=None, atomic_energy=True,
+              check=True):
+        """TTM4-F electrostatics (mbx_polar_forces, host arrays) on 4*nw sites; returns a
+        dict shaped like the oracle's."""
+        n = 4 * nw
+        x, y, z = (_f64(sites[:, k]) for k in range(3))
+        dip = np.zeros((3, n)) if dip0 is None else np.ascontiguousarray(np.asarray(dip0, np.float64).T).copy()
+        f = np.zeros((3, n))
+        out = np.zeros(16)
+        ae = np.zeros(n) if atomic_energy else None
+        jpot = np.zeros(3)
+        jkin = np.zeros(3)
+        v = [_f64(vel[:3 * nw, k]) for k in range(3)] if vel is not None else [None] * 3
+        rc = self.lib.mbx_polar_forces(self.h, _p(_f64(prm)), imcon, _p(_f64(cell)), nw, _p(x), _p(y), _p(z),
+                                       _p(_f64(chge)), _p(_f64(dp)), _p(_f64(polr)), _p(_f64(polr2)), _p(dip[0]),
+                                       _p(dip[1]), _p(dip[2]), _p(f[0]), _p(f[1]), _p(f[2]), _p(out), _p(ae),
+                                       _p(v[0]), _p(v[1]), _p(v[2]), _p(jpot), _p(jkin))
+        if check:
+            self._check(rc, "mbx_polar_forces")
+        return dict(status=rc, forces=f.T.copy(), engcpe=out[0], vircpe=out[1], stress=out[2:11].copy(),
+                    iterations=int(out[11]), deltadip=out[12], eng_polar=out[13], eng_kspace=out[14],
+                    eng_real=out[15], dipoles=dip.T.copy(), atomic_energy=ae, jpot=jpot, jkin=jkin)
+
+    def polar_iterations(self):
+        return int(self.lib.mbx_polar_iterations(self.h))
 
     def disp_list_builds(self):
         return int(self.lib.mbx_disp_list_builds(self.h))

@@ -29,6 +29,7 @@ extern "C" {
 #define MBX_ERR_CUDA 2          /* a CUDA call failed; see mbx_error() */
 #define MBX_ERR_CAPACITY 3      /* a list outgrew the largest capacity the context allows */
 #define MBX_ERR_NO_DEVICE 4     /* no CUDA device, or the device is not an sm_103 part */
+#define MBX_ERR_CONVERGE 5      /* the induced dipoles did not converge within maxit iterations */
 
 /* Scalar outputs of one evaluation (indices into the `scalars` array). */
 #define MBX_S_ENG2 0            /* MB-pol 2B energy (internal units) */
@@ -169,6 +170,53 @@ int mbx_msites_dms(mbx_context* ctx, int imcon, const double* cell, int nttm2, c
 int mbx_msites_dms_device(mbx_context* ctx, int imcon, const double* cell, int nttm2, const int* listttm2,
                           int natms, double gamma, double* xxx, double* yyy, double* zzz, double* chge,
                           double* dqdr);
+
+/*
+ * TTM4-F polarizable electrostatics of MB-pol water: the polar Ewald branch of the
+ * reference's forces (SOURCE/forces.f:271-366 and :518-805) with the vmbpol settings
+ * (SOURCE/simdef_cmd.f:1040-1060) -- rfield (SOURCE/rfield.f), ewald1p (SOURCE/ewald1p.f),
+ * iter (SOURCE/iter.f), coulomb_polar (SOURCE/coulomb_polar.f), ewald2p (SOURCE/ewald2p.f),
+ * ewald3p (SOURCE/ewald3p.f), qdforce (SOURCE/qdforce.f90) -- and their HEAT_CURRENT terms.
+ * Replaces that branch of `forces` for a water-only system; ewald4p has no pairs there.
+ *   prm[15]   {alpha, rcut, epsq, toler (e*Angstrom, the CONTROL `iter` value / 4.803239),
+ *              sor_omega, athole, athole12, athole13, ascc, ascd, gamma, kmax1, kmax2,
+ *              kmax3, maxit}
+ *   sites     4*nw in the standard layout: water w has O, H1, H2 at 3w..3w+2 and its M site
+ *             at 3nw+w (0-based), M sites placed (mbx_msites_dms)
+ *   chge      DMS charges, dqdr[6*nw] from mbx_msites_dms; polr (Thole widths) and polr2
+ *             (polarizabilities, 0 = no dipole) per site, the FIELD `polar`/`polar2` values
+ *   dip*      in: starting dipoles (0 on non-polarizable sites), out: converged dipoles
+ *   f*        ACCUMULATED site forces; M-site forces are not redistributed (see
+ *             mbx_msite_redistribute)
+ *   out16     {engcpe, vircpe, stress[9], iterations, rms dipole change, polarization energy
+ *              (coulomb_polar), k-space energy (with the self term), real-space energy}
+ *             written; stress is this term's contribution
+ *   atomic_energy  per-site electrostatic energy ACCUMULATED (update_energy_ew1p/ew2p/ew3p
+ *             and _polar), not redistributed; may be NULL
+ *   v*        velocities of the 3*nw water atoms, or NULL; then jpot[3] is ACCUMULATED with
+ *             the electrostatic force-matrix and ew1p-stress terms of compute_heat_flux2
+ *             after the M-site redistribution, and jkin[3] with the redistributed per-site
+ *             energies times the velocities
+ * Returns MBX_ERR_CONVERGE (results of the last iteration written) when the dipoles did
+ * not reach toler within maxit iterations (the reference stops at 22581).
+ */
+int mbx_polar_forces(mbx_context* ctx, const double* prm, int imcon, const double* cell, int nw, const double* xxx,
+                     const double* yyy, const double* zzz, const double* chge, const double* dqdr, const double* polr,
+                     const double* polr2, double* dipx, double* dipy, double* dipz, double* fxx, double* fyy,
+                     double* fzz, double* out16, double* atomic_energy, const double* vxx, const double* vyy,
+                     const double* vzz, double* jpot, double* jkin);
+int mbx_polar_forces_device(mbx_context* ctx, const double* prm, int imcon, const double* cell, int nw,
+                            const double* xxx, const double* yyy, const double* zzz, const double* chge,
+                            const double* dqdr, const double* polr, const double* polr2, double* dipx, double* dipy,
+                            double* dipz, double* fxx, double* fyy, double* fzz, double* out16,
+                            double* atomic_energy, const double* vxx, const double* vyy, const double* vzz,
+                            double* jpot, double* jkin);
+/* Dipole iterations of the last mbx_polar_forces call. */
+int mbx_polar_iterations(const mbx_context* ctx);
+/* M-site force redistribution of the reference's MD step (SOURCE/dlpoly_cmd.f:2585-2601):
+ * F_O += (1 - gamma) F_M, F_H1 += F_M gamma / 2, F_H2 += F_M gamma / 2 (standard layout,
+ * host arrays of 4*nw sites; the M-site entries are left as they are). */
+int mbx_msite_redistribute(int nw, double gamma, double* fxx, double* fyy, double* fzz);
 
 /*
  * Continuous-batching force server.  `slots` worker slots, each with its own context and

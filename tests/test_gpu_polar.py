@@ -1,0 +1,105 @@
+"""GPU parity of the TTM4-F electrostatics (mbx_polar_forces) against the oracle.
+
+FP64 path: energies, virial, stress, site forces, converged dipoles, per-site energies and
+the heat-current terms within 1e-10 relative (vectors relative to their largest entry),
+the same number of dipole iterations.
+"""
+import numpy as np
+import pytest
+
+from mbx import capi, systems
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-10
+
+
+def _case(orc, box, prm):
+    sites, q, dp, _ = orc.msites_dms(box)
+    polr, polr2 = systems.polarizabilities(box.nw)
+    return sites, q, dp, polr, polr2, prm
+
+
+def _compare(got, ref):
+    assert got["iterations"] == ref["iterations"], (got["iterations"], ref["iterations"])
+    for key in ("engcpe", "vircpe", "eng_polar", "eng_kspace", "eng_real"):
+        assert abs(got[key] - ref[key]) <= TOL * abs(ref[key]), (key, got[key], ref[key])
+    smax = np.abs(ref["stress"]).max()
+    assert np.abs(got["stress"] - ref["stress"]).max() <= TOL * smax
+    for key in ("forces", "dipoles", "atomic_energy", "jpot", "jkin"):
+        r = ref[key]
+        assert np.abs(got[key] - r).max() <= TOL * np.abs(r).max(), (key, np.abs(got[key] - r).max(), np.abs(r).max())
+
+
+@pytest.mark.parametrize("which", ["small", "config0", "triclinic"])
+def test_polar_matches_oracle(mbx_ctx, oracle_lib, which):
+    if which == "small":
+        box = systems.box_for(32, seed=5)
+        prm = systems.polar_params(alpha=0.6, rcut=4.5, kmax=(8, 8, 8), toler_debye=1e-12)
+    elif which == "config0":
+        box = systems.config0()
+        prm = systems.polar_params(alpha=0.3, rcut=9.0, kmax=(8, 8, 8), toler_debye=1e-12)
+    else:
+        box = systems.box_for(64, seed=9)
+        L = box.L
+        # a sheared cell (imcon 3) of the same volume: the box's waters imaged into it
+        box.cell = np.array([L, 0, 0, 0.2 * L, L, 0, 0.1 * L, -0.15 * L, L], dtype=np.float64)
+        box.imcon = 3
+        prm = systems.polar_params(alpha=0.55, rcut=5.0, kmax=(7, 7, 7), toler_debye=1e-11)
+    sites, q, dp, polr, polr2, prm = _case(oracle_lib, box, prm)
+    ref = oracle_lib.polar(sites, box.cell, box.imcon, box.nw, q, dp, polr, polr2, prm, vel=box.vel)
+    assert ref["status"] == 0
+    got = mbx_ctx.polar(sites, box.cell, box.imcon, box.nw, q, dp, polr, polr2, prm, vel=box.vel)
+    _compare(got, ref)
+
+
+def test_polar_warm_start_and_no_heat(mbx_ctx, oracle_lib):
+    box = systems.box_for(32, seed=6)
+    prm = systems.polar_params(alpha=0.6, rcut=4.5, kmax=(6, 6, 6), toler_debye=1e-12)
+    sites, q, dp, polr, polr2, prm = _case(oracle_lib, box, prm)
+    first = mbx_ctx.polar(sites, box.cell, box.imcon, box.nw, q, dp, polr, polr2, prm)
+    rng = np.random.default_rng(1)
+    dip0 = first["dipoles"] + rng.normal(0, 1e-4, size=first["dipoles"].shape)
+    dip0[3 * box.nw:] = 0.0
+    ref = oracle_lib.polar(sites, box.cell, box.imcon, box.nw, q, dp, polr, polr2, prm, dip0=dip0)
+    got = mbx_ctx.polar(sites, box.cell, box.imcon, box.nw, q, dp, polr, polr2, prm, dip0=dip0)
+    assert got["iterations"] < first["iterations"]
+    assert not got["jpot"].any() and not got["jkin"].any()
+    ref["jpot"] = got["jpot"]
+    ref["jkin"] = got["jkin"]
+    _compare(got, ref)
+
+
+def test_polar_not_converged_status(mbx_ctx, oracle_lib):
+    box = systems.box_for(32, seed=5)
+    prm = systems.polar_params(alpha=0.6, rcut=4.5, kmax=(6, 6, 6), toler_debye=1e-12, maxit=3)
+    sites, q, dp, polr, polr2, prm = _case(oracle_lib, box, prm)
+    got = mbx_ctx.polar(sites, box.cell, box.imcon, box.nw, q, dp, polr, polr2, prm, check=False)
+    assert got["status"] == capi.ERR_CONVERGE and got["iterations"] == 3
+    ref = oracle_lib.polar(sites, box.cell, box.imcon, box.nw, q, dp, polr, polr2, prm)
+    assert ref["status"] == 1
+    np.testing.assert_allclose(got["dipoles"], ref["dipoles"], rtol=0, atol=1e-12)
+    # bad parameters are refused before any work
+    bad = prm.copy()
+    bad[4] = 1.5
+    with pytest.raises(capi.MbxError):
+        mbx_ctx.polar(sites, box.cell, box.imcon, box.nw, q, dp, polr, polr2, bad)
+
+
+def test_msite_redistribute(mbx_ctx):
+    import ctypes as C
+    nw = 5
+    rng = np.random.default_rng(2)
+    f = rng.normal(size=(3, 4 * nw))
+    g = 0.426706882
+    want = f.copy()
+    for w in range(nw):
+        m = want[:, 3 * nw + w].copy()
+        want[:, 3 * w] += (1 - g) * m
+        want[:, 3 * w + 1] += m * g / 2
+        want[:, 3 * w + 2] += m * g / 2
+    P = C.POINTER(C.c_double)
+    assert mbx_ctx.lib.mbx_msite_redistribute(nw, g, f[0].ctypes.data_as(P), f[1].ctypes.data_as(P),
+                                              f[2].ctypes.data_as(P)) == 0
+    # the host compiler may contract f + w * m into one FMA (aarch64): 1 ulp
+    np.testing.assert_allclose(f, want, rtol=1e-15, atol=1e-15)
