@@ -842,15 +842,16 @@ bool polar_prm_ok(const double* prm) {
 }
 }  // namespace
 
-extern "C" int mbx_polar_forces_device(mbx_context* ctx, const double* prm, int imcon, const double* cell, int nw,
+extern "C" int mbx_polar_forces_device(mbx_context* ctx, int precision, const double* prm, int imcon, const double* cell, int nw,
                                        const double* xxx, const double* yyy, const double* zzz, const double* chge,
                                        const double* dqdr, const double* polr, const double* polr2, double* dipx,
                                        double* dipy, double* dipz, double* fxx, double* fyy, double* fzz,
                                        double* out16, double* atomic_energy, const double* vxx, const double* vyy,
                                        const double* vzz, double* jpot, double* jkin) {
     if (!ctx) return MBX_ERR_ARG;
-    if (nw < 0 || !polar_prm_ok(prm) || !out16 || (nw && (!xxx || !yyy || !zzz || !chge || !dqdr || !polr || !polr2 ||
-                                                            !dipx || !dipy || !dipz || !fxx || !fyy || !fzz)))
+    if ((precision != MBX_FP64 && precision != MBX_MIXED) || nw < 0 || !polar_prm_ok(prm) || !out16 ||
+        (nw && (!xxx || !yyy || !zzz || !chge || !dqdr || !polr || !polr2 || !dipx || !dipy || !dipz || !fxx ||
+                !fyy || !fzz)))
         return fail(ctx, MBX_ERR_ARG, "mbx_polar_forces: bad argument");
     const bool heat = vxx && vyy && vzz;
     if (heat && (!jpot || !jkin)) return fail(ctx, MBX_ERR_ARG, "mbx_polar_forces: jpot/jkin needed with velocities");
@@ -859,7 +860,8 @@ extern "C" int mbx_polar_forces_device(mbx_context* ctx, const double* prm, int 
     if (rc) return rc;
     CK(cudaSetDevice(ctx->device));
     double jp[3] = {0, 0, 0}, jk[3] = {0, 0, 0};
-    CK(ctx->polar.run(cl, prm, nw, xxx, yyy, zzz, chge, dqdr, polr, polr2, dipx, dipy, dipz, fxx, fyy, fzz,
+    if (ctx->nsm > 0) ctx->polar.nsm = ctx->nsm;
+    CK(ctx->polar.run(precision, cl, prm, nw, xxx, yyy, zzz, chge, dqdr, polr, polr2, dipx, dipy, dipz, fxx, fyy, fzz,
                       atomic_energy, heat ? vxx : nullptr, heat ? vyy : nullptr, heat ? vzz : nullptr, out16, jp, jk,
                       ctx->stream));
     ctx->launches = ctx->polar.launches;
@@ -874,15 +876,16 @@ extern "C" int mbx_polar_forces_device(mbx_context* ctx, const double* prm, int 
     return MBX_OK;
 }
 
-extern "C" int mbx_polar_forces(mbx_context* ctx, const double* prm, int imcon, const double* cell, int nw,
+extern "C" int mbx_polar_forces(mbx_context* ctx, int precision, const double* prm, int imcon, const double* cell, int nw,
                                 const double* xxx, const double* yyy, const double* zzz, const double* chge,
                                 const double* dqdr, const double* polr, const double* polr2, double* dipx, double* dipy,
                                 double* dipz, double* fxx, double* fyy, double* fzz, double* out16,
                                 double* atomic_energy, const double* vxx, const double* vyy, const double* vzz,
                                 double* jpot, double* jkin) {
     if (!ctx) return MBX_ERR_ARG;
-    if (nw < 0 || !polar_prm_ok(prm) || !out16 || (nw && (!xxx || !yyy || !zzz || !chge || !dqdr || !polr || !polr2 ||
-                                                            !dipx || !dipy || !dipz || !fxx || !fyy || !fzz)))
+    if ((precision != MBX_FP64 && precision != MBX_MIXED) || nw < 0 || !polar_prm_ok(prm) || !out16 ||
+        (nw && (!xxx || !yyy || !zzz || !chge || !dqdr || !polr || !polr2 || !dipx || !dipy || !dipz || !fxx ||
+                !fyy || !fzz)))
         return fail(ctx, MBX_ERR_ARG, "mbx_polar_forces: bad argument");
     const bool heat = vxx && vyy && vzz;
     if (heat && (!jpot || !jkin)) return fail(ctx, MBX_ERR_ARG, "mbx_polar_forces: jpot/jkin needed with velocities");
@@ -921,7 +924,7 @@ extern "C" int mbx_polar_forces(mbx_context* ctx, const double* prm, int imcon, 
         }
         CK(cudaMemsetAsync(dfx, 0, 4 * nb, s));   // forces and per-site energies
     }
-    const int rc = mbx_polar_forces_device(ctx, prm, imcon, cell, nw, dx, dy, dz, dq, ddp, dpr, dpr2, dmx, dmy, dmz,
+    const int rc = mbx_polar_forces_device(ctx, precision, prm, imcon, cell, nw, dx, dy, dz, dq, ddp, dpr, dpr2, dmx, dmy, dmz,
                                            dfx, dfy, dfz, out16, atomic_energy ? dae : nullptr,
                                            heat ? dv : nullptr, heat ? dv + na : nullptr, heat ? dv + 2 * na : nullptr,
                                            jpot, jkin);
@@ -946,6 +949,8 @@ extern "C" int mbx_polar_forces(mbx_context* ctx, const double* prm, int imcon, 
 }
 
 extern "C" int mbx_polar_iterations(const mbx_context* ctx) { return ctx ? ctx->polar.iterations : -1; }
+
+extern "C" long mbx_polar_inner_sweeps(const mbx_context* ctx) { return ctx ? ctx->polar.inner_sweeps : -1; }
 
 extern "C" int mbx_msite_redistribute(int nw, double gamma, double* fxx, double* fyy, double* fzz) {
     if (nw < 0 || (nw && (!fxx || !fyy || !fzz))) return MBX_ERR_ARG;

@@ -181,6 +181,23 @@ struct PolarState {
     double* fld = nullptr;                 // efk, efc, emu, efm (3 blocks of n each)
     double *vesp = nullptr, *ae = nullptr;
     double2* eik = nullptr;                // exp(ik.r) [k][site]
+    double2* fac = nullptr;                // per-site phase factors per axis and index
+    size_t fac_cap = 0;
+    double4* md = nullptr;                 // dipoles of the polarizable sites
+    double* vh = nullptr;                  // velocities the per-site terms are carried with
+    double* kco = nullptr;                 // per-k coefficients of the gathers
+    // mixed precision: FP32 tensors, phase table and correction solve
+    float* tens32 = nullptr;
+    float2* eik32 = nullptr;
+    float* kco32 = nullptr;
+    float4 *r32 = nullptr, *d32 = nullptr;
+    float* e32 = nullptr;
+    int cap32 = 0, n32 = 0, k32 = 0;
+    size_t eik32_cap = 0;
+    long inner_sweeps = 0;
+    double* kpart = nullptr;               // per-chunk partial sums of the k-space gathers
+    size_t part_cap = 0;
+    int nsm = 152;                         // SMs of the device (grid sizing)
     double4* kv = nullptr;                 // kx, ky, kz, akk
     double2* kx2 = nullptr;                // rksq, akv2
     int4* lmn = nullptr;
@@ -195,12 +212,17 @@ struct PolarState {
     ~PolarState();
     void release();
     cudaError_t table(double alpha, double rcut);
-    cudaError_t reserve(int nw, int K);
-    // One evaluation on device arrays.  prm[15] as mbx_polar_forces; forces, per-site
+    cudaError_t reserve(int nw, int K, size_t nfac);
+    cudaError_t reserve_mixed(int n, int K);
+    cudaError_t reserve_part(size_t ndouble);
+    // One evaluation on device arrays (precision MBX_FP64 or MBX_MIXED: the dipole
+    // equations solved by FP32 corrections under FP64 refinement).  prm[15] as
+    // mbx_polar_forces; forces, per-site
     // energies (ae_out, may be null), jpot and jkin are ACCUMULATED; the dipoles are
     // updated in place; out16 as mbx_polar_forces.  `converged` tells whether the dipole
     // iteration reached toler within maxit iterations.
-    cudaError_t run(const Cell& cl, const double* prm, int nw, const double* x, const double* y, const double* z,
+    cudaError_t run(int precision, const Cell& cl, const double* prm, int nw, const double* x, const double* y,
+                    const double* z,
                     const double* q, const double* dp, const double* polr, const double* polr2, double* mx,
                     double* my, double* mz, double* fx, double* fy, double* fz, double* ae_out, const double* vx,
                     const double* vy, const double* vz, double* out16, double* jpot, double* jkin, cudaStream_t s);

@@ -128,6 +128,7 @@ struct PolArgs {
     double drewd;
     const int *nn, *nbr;
     double* tens;   // 6 blocks of n * cap
+    float* tens32;  // the same in FP32 (mixed precision), or null
     double* intra;  // 18 per water
     double *efk, *efc, *emu, *efm;   // 3 blocks of n each
     double *vesp, *ae;
@@ -296,6 +297,8 @@ __global__ void k_pol_static(PolArgs a) {
         }
 #pragma unroll
         for (int p = 0; p < 6; ++p) a.tens[p * blk + row + k] = t[p];
+        if (a.tens32)
+            for (int p = 0; p < 6; ++p) a.tens32[p * blk + row + k] = (float)t[p];
     }
     for (int c = 0; c < 3; ++c) e[c] = warp_sum(e[c]);
     if (lane == 0) {
@@ -394,33 +397,61 @@ __global__ void k_pol_dd(PolArgs a) {
 
 // --- k space ------------------------------------------------------------------------------
 struct KArgs {
-    int K, n;
+    int K, n, kmax[3];
     const double4* kv;     // kx, ky, kz, akk
     const double2* kx2;    // rksq, akv2
     const int4* lmn;
-    const double2* eik;    // [k * n + j] = (cos, sin)
+    double2* fac;          // per-site phase factors exp(2 pi i l s): x (l = 0..kmax1), y, z (-kmax..kmax)
+    double2* eik;          // exp(ik.r) [k * n + j] = (cos, sin)
+    float2* eik32;         // the same in FP32 (mixed precision), or null
+    float* kco32;          // 8 per k: kx, ky, kz, akk k.Ds, akk k.Dc of the FP32 correction
     double* sf;            // 8 per k: ckcs, ckss, Mc(3), Ms(3)
-    double* kterm;         // 8 per k (final pass): engc, engdum, omg 1 5 9 2 3 6
+    double* kco;           // 16 per k: coefficients of the gathers
+    double* kterm;         // 16 per k (final pass): engc, engdum, omg 11 22 33 12 13 23, jpot(3)
+    const double4* md;     // dipoles of the polarizable sites (0 elsewhere)
+    const double* q;       // site charges
+    const double* vh;      // velocities each site's quantities are carried with (3 blocks of n)
     double rc[9];
-    double scale, ralph;
+    double scale, ralph, sfac;   // 4 rvolm r4pie0 / epsq, -1 / (4 alpha^2), 2 rvolm r4pie0 / epsq
 };
 
-__global__ void k_pol_phase(KArgs k, const double* __restrict__ x, const double* __restrict__ y,
-                            const double* __restrict__ z) {
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
+    return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+
+// exp(2 pi i l s) for the fractional coordinates of each site and every l of each axis
+__global__ void k_pol_factors(KArgs k, const double* __restrict__ x, const double* __restrict__ y,
+                              const double* __restrict__ z) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= k.n) return;
+    const double s3[3] = {k.rc[0] * x[j] + k.rc[3] * y[j] + k.rc[6] * z[j],
+                          k.rc[1] * x[j] + k.rc[4] * y[j] + k.rc[7] * z[j],
+                          k.rc[2] * x[j] + k.rc[5] * y[j] + k.rc[8] * z[j]};
+    int off = 0;
+    for (int ax = 0; ax < 3; ++ax) {
+        const int lo = ax == 0 ? 0 : -k.kmax[ax];
+        for (int l = lo; l <= k.kmax[ax]; ++l) {
+            const double t = (double)l * s3[ax];
+            double sn, cs;
+            sincospi(2.0 * (t - rint(t)), &sn, &cs);
+            k.fac[(size_t)(off + l - lo) * k.n + j] = make_double2(cs, sn);
+        }
+        off += k.kmax[ax] - lo + 1;
+    }
+}
+
+__global__ void k_pol_phase(KArgs k) {
     const int j = blockIdx.y * blockDim.x + threadIdx.x;
     const int kk = blockIdx.x;
     if (j >= k.n) return;
-    const double sx = k.rc[0] * x[j] + k.rc[3] * y[j] + k.rc[6] * z[j];
-    const double sy = k.rc[1] * x[j] + k.rc[4] * y[j] + k.rc[7] * z[j];
-    const double sz = k.rc[2] * x[j] + k.rc[5] * y[j] + k.rc[8] * z[j];
     const int4 v = k.lmn[kk];
-    // exp(2 pi i (l sx + m sy + n sz)) with each product reduced mod 1 first
-    double ph = (double)v.x * sx - rint((double)v.x * sx);
-    ph += (double)v.y * sy - rint((double)v.y * sy);
-    ph += (double)v.z * sz - rint((double)v.z * sz);
-    double s, c;
-    sincospi(2.0 * ph, &s, &c);
-    ((double2*)k.eik)[(size_t)kk * k.n + j] = make_double2(c, s);
+    const int oy = k.kmax[0] + 1, oz = oy + 2 * k.kmax[1] + 1;
+    const double2 fx = k.fac[(size_t)v.x * k.n + j];
+    const double2 fy = k.fac[(size_t)(oy + v.y + k.kmax[1]) * k.n + j];
+    const double2 fz = k.fac[(size_t)(oz + v.z + k.kmax[2]) * k.n + j];
+    const double2 e = cmul(cmul(fx, fy), fz);
+    k.eik[(size_t)kk * k.n + j] = e;
+    if (k.eik32) k.eik32[(size_t)kk * k.n + j] = make_float2((float)e.x, (float)e.y);
 }
 
 template <int NV>
@@ -440,199 +471,494 @@ __device__ __forceinline__ void block_reduce_store(double (&v)[NV], double* out)
     }
 }
 
-// Structure factors of one k vector: charges and (polarizable) dipoles.  In the final
-// pass thread 0 also forms the k vector's energy and virial terms (SOURCE/ewald1p.f:695-733).
-__global__ void __launch_bounds__(kSfThreads) k_pol_sf(KArgs k, PolArgs a, int final_pass) {
+__global__ void k_pol_mask(PolArgs a, double4* __restrict__ md) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= a.n) return;
+    md[j] = a.polr2[j] > 1e-6 ? make_double4(a.mx[j], a.my[j], a.mz[j], 0.0) : make_double4(0, 0, 0, 0);
+}
+
+// Charge structure factors (fixed for the call): ckcs, ckss per k vector.
+__global__ void __launch_bounds__(kSfThreads) k_pol_sfq(KArgs k, const double* __restrict__ q) {
     const int kk = blockIdx.x;
     const double2* e = k.eik + (size_t)kk * k.n;
-    double v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    double v[2] = {0, 0};
     for (int j = threadIdx.x; j < k.n; j += kSfThreads) {
         const double2 cs = e[j];
-        const double qj = a.q[j];
-        v[0] += qj * cs.x;
-        v[1] += qj * cs.y;
-        if (a.polr2[j] > 1e-6) {
-            const double m[3] = {a.mx[j], a.my[j], a.mz[j]};
-            v[2] += cs.x * m[0]; v[3] += cs.x * m[1]; v[4] += cs.x * m[2];
-            v[5] += cs.y * m[0]; v[6] += cs.y * m[1]; v[7] += cs.y * m[2];
-        }
+        v[0] += q[j] * cs.x;
+        v[1] += q[j] * cs.y;
     }
-    __shared__ double tot[8];
-    block_reduce_store<8>(v, tot);
+    __shared__ double tot[2];
+    block_reduce_store<2>(v, tot);
     __syncthreads();
-    if (threadIdx.x < 8) k.sf[8 * (size_t)kk + threadIdx.x] = tot[threadIdx.x];
-    if (final_pass && threadIdx.x == 0) {
+    if (threadIdx.x < 2) k.sf[8 * (size_t)kk + threadIdx.x] = tot[threadIdx.x];
+}
+
+// Dipole structure factors of one k vector and the coefficients of the field gather.
+__global__ void __launch_bounds__(kSfThreads) k_pol_sfd(KArgs k) {
+    const int kk = blockIdx.x;
+    const double2* e = k.eik + (size_t)kk * k.n;
+    double v[6] = {0, 0, 0, 0, 0, 0};
+    for (int j = threadIdx.x; j < k.n; j += kSfThreads) {
+        const double2 cs = e[j];
+        const double4 m = k.md[j];
+        v[0] += cs.x * m.x; v[1] += cs.x * m.y; v[2] += cs.x * m.z;
+        v[3] += cs.y * m.x; v[4] += cs.y * m.y; v[5] += cs.y * m.z;
+    }
+    __shared__ double tot[6];
+    block_reduce_store<6>(v, tot);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double* sf = k.sf + 8 * (size_t)kk;
+        for (int c = 0; c < 6; ++c) sf[2 + c] = tot[c];
         const double4 kv = k.kv[kk];
-        const double2 k2 = k.kx2[kk];
-        const double ckcs = tot[0], ckss = tot[1];
-        const double mc[3] = {tot[2], tot[3], tot[4]}, ms[3] = {tot[5], tot[6], tot[7]};
-        const double skc = kv.x * mc[0] + kv.y * mc[1] + kv.z * mc[2];
-        const double sks = kv.x * ms[0] + kv.y * ms[1] + kv.z * ms[2];
-        const double summu1 = ckcs - sks, summu2 = ckss + skc;
-        const double akk = kv.w, akv = 2.0 * akk * (1.0 / k2.x - k.ralph);
-        const double s2 = summu1 * summu1 + summu2 * summu2;
-        const double virprs = akv * s2;
-        const double k3[3] = {kv.x, kv.y, kv.z};
-        const int oa[6] = {0, 1, 2, 0, 0, 1}, ob[6] = {0, 1, 2, 1, 2, 2};
-        double* t = k.kterm + 8 * (size_t)kk;
-        t[0] = akk * (ckcs * ckcs + ckss * ckss);
-        t[1] = akk * s2;
-        for (int q = 0; q < 6; ++q)
-            t[2 + q] = -virprs * k3[oa[q]] * k3[ob[q]] - 2.0 * akk * k3[oa[q]] * ms[ob[q]] * summu1 +
-                       2.0 * akk * k3[oa[q]] * mc[ob[q]] * summu2;
+        const double skc = kv.x * tot[0] + kv.y * tot[1] + kv.z * tot[2];
+        const double sks = kv.x * tot[3] + kv.y * tot[4] + kv.z * tot[5];
+        double* c = k.kco + 16 * (size_t)kk;
+        c[0] = kv.x; c[1] = kv.y; c[2] = kv.z;
+        c[3] = kv.w * sks;      // dipole field: -k akk (s k.Ms + c k.Mc)
+        c[4] = kv.w * skc;
+        c[5] = kv.w * sf[0];    // static field: -k akk (-s ckcs + c ckss)
+        c[6] = kv.w * sf[1];
     }
 }
 
-// k-space fields per site (iflag 0): the dipole field and, in the first pass, the static
-// charge field; thread per site, k vectors staged through shared memory.
-__global__ void __launch_bounds__(kThreads) k_pol_kfield(KArgs k, PolArgs a, int first) {
-    __shared__ double sh[kKTile][8];
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool pol = j < k.n && a.polr2[j] > 1e-6;
-    double em[3] = {0, 0, 0}, ec[3] = {0, 0, 0};
-    for (int t0 = 0; t0 < k.K; t0 += kKTile) {
-        const int nt = min(kKTile, k.K - t0);
-        __syncthreads();
-        for (int u = threadIdx.x; u < nt; u += blockDim.x) {
-            const double4 kv = k.kv[t0 + u];
-            const double* s = k.sf + 8 * (size_t)(t0 + u);
-            sh[u][0] = kv.x; sh[u][1] = kv.y; sh[u][2] = kv.z; sh[u][3] = kv.w;
-            sh[u][4] = s[0]; sh[u][5] = s[1];
-            sh[u][6] = kv.x * s[2] + kv.y * s[3] + kv.z * s[4];   // k . Mc
-            sh[u][7] = kv.x * s[5] + kv.y * s[6] + kv.z * s[7];   // k . Ms
-        }
-        __syncthreads();
-        if (j < k.n) {
-            for (int u = 0; u < nt; ++u) {
-                const double2 cs = k.eik[(size_t)(t0 + u) * k.n + j];
-                const double akk = sh[u][3];
-                if (first) {
-                    const double tt = -cs.y * sh[u][4] + cs.x * sh[u][5];
-                    ec[0] -= sh[u][0] * akk * tt;
-                    ec[1] -= sh[u][1] * akk * tt;
-                    ec[2] -= sh[u][2] * akk * tt;
-                }
-                if (pol) {
-                    const double vv = cs.y * sh[u][7] + cs.x * sh[u][6];
-                    em[0] -= sh[u][0] * akk * vv;
-                    em[1] -= sh[u][1] * akk * vv;
-                    em[2] -= sh[u][2] * akk * vv;
+// Final structure factors (dipoles, and with velocities the 24 sums of the ew1p
+// per-atom stress contraction), the k vector's energy, virial and heat-current terms
+// (SOURCE/ewald1p.f:575-733) and the coefficients of the force gather.
+template <int HEAT>
+__global__ void __launch_bounds__(kSfThreads) k_pol_sf_final(KArgs k) {
+    constexpr int NV = HEAT ? 30 : 6;
+    const int kk = blockIdx.x;
+    const double2* e = k.eik + (size_t)kk * k.n;
+    double v[NV];
+#pragma unroll
+    for (int q = 0; q < NV; ++q) v[q] = 0.0;
+    for (int j = threadIdx.x; j < k.n; j += kSfThreads) {
+        const double2 cs = e[j];
+        const double4 m = k.md[j];
+        v[0] += cs.x * m.x; v[1] += cs.x * m.y; v[2] += cs.x * m.z;
+        v[3] += cs.y * m.x; v[4] += cs.y * m.y; v[5] += cs.y * m.z;
+        if (HEAT) {
+            const double vb[3] = {k.vh[j], k.vh[k.n + j], k.vh[2 * (size_t)k.n + j]};
+            const double q = k.q[j];
+            const double mu[3] = {m.x, m.y, m.z};
+#pragma unroll
+            for (int b = 0; b < 3; ++b) {
+                v[6 + b] += cs.x * q * vb[b];    // V1
+                v[9 + b] += cs.y * q * vb[b];    // V2
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    v[12 + 3 * c + b] += cs.x * mu[c] * vb[b];   // W1[c][b]
+                    v[21 + 3 * c + b] += cs.y * mu[c] * vb[b];   // W2[c][b]
                 }
             }
         }
     }
-    if (j >= k.n) return;
-    const double dum = 4.0 * kR4pie0 * (a.alpha * a.alpha * a.alpha) / kSqrpi / 3.0;
-    const double m[3] = {a.mx[j], a.my[j], a.mz[j]};
+    __shared__ double tot[NV];
+    block_reduce_store<NV>(v, tot);
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    double* sf = k.sf + 8 * (size_t)kk;
+    for (int c = 0; c < 6; ++c) sf[2 + c] = tot[c];
+    const double4 kv = k.kv[kk];
+    const double2 k2 = k.kx2[kk];
+    const double kx[3] = {kv.x, kv.y, kv.z};
+    const double ckcs = sf[0], ckss = sf[1];
+    const double Mc[3] = {tot[0], tot[1], tot[2]}, Ms[3] = {tot[3], tot[4], tot[5]};
+    const double skc = kx[0] * Mc[0] + kx[1] * Mc[1] + kx[2] * Mc[2];
+    const double sks = kx[0] * Ms[0] + kx[1] * Ms[1] + kx[2] * Ms[2];
+    const double s1 = ckcs - sks, s2 = ckss + skc;
+    const double akk = kv.w, akv = 2.0 * akk * (1.0 / k2.x - k.ralph), akv2 = k2.y;
+    const double s12 = s1 * s1 + s2 * s2;
+    const double virprs = akv * s12;
+    double* t = k.kterm + 16 * (size_t)kk;
+    t[0] = akk * (ckcs * ckcs + ckss * ckss);
+    t[1] = akk * s12;
+    const int oa[6] = {0, 1, 2, 0, 0, 1}, ob[6] = {0, 1, 2, 1, 2, 2};
+    for (int q = 0; q < 6; ++q)
+        t[2 + q] = -virprs * kx[oa[q]] * kx[ob[q]] - 2.0 * akk * kx[oa[q]] * Ms[ob[q]] * s1 +
+                   2.0 * akk * kx[oa[q]] * Mc[ob[q]] * s2;
+    t[8] = t[9] = t[10] = 0.0;
+    if (HEAT) {
+        const double* V1 = tot + 6;
+        const double* V2 = tot + 9;
+        const double* W1 = tot + 12;
+        const double* W2 = tot + 21;
+        double kW1[3], kW2[3], P[3];
+        for (int b = 0; b < 3; ++b) {
+            kW1[b] = kx[0] * W1[b] + kx[1] * W1[3 + b] + kx[2] * W1[6 + b];
+            kW2[b] = kx[0] * W2[b] + kx[1] * W2[3 + b] + kx[2] * W2[6 + b];
+            P[b] = s1 * V1[b] + s2 * kW1[b] + s2 * V2[b] - s1 * kW2[b];
+        }
+        const double kp = kx[0] * P[0] + kx[1] * P[1] + kx[2] * P[2];
+        double Q[3][3];   // Q[b'][b] = sum_j Y_jb' v_jb
+        for (int bp = 0; bp < 3; ++bp)
+            for (int b = 0; b < 3; ++b)
+                Q[bp][b] = -Ms[bp] * V1[b] + s2 * W1[3 * bp + b] + Mc[bp] * kW1[b] + Mc[bp] * V2[b] -
+                           s1 * W2[3 * bp + b] + Ms[bp] * kW2[b];
+        const double f = k.sfac * akk;
+        for (int aa = 0; aa < 3; ++aa) {
+            double y = 0.0;
+            for (int b = 0; b < 3; ++b) {
+                const int lo = aa < b ? aa : b, hi = aa < b ? b : aa;
+                y += kx[lo] * Q[hi][b];
+            }
+            t[8 + aa] = f * (P[aa] - akv2 * kx[aa] * kp + y);
+        }
+    }
+    double* c = k.kco + 16 * (size_t)kk;
+    c[0] = kx[0]; c[1] = kx[1]; c[2] = kx[2]; c[3] = akk;
+    c[4] = s1; c[5] = s2; c[6] = ckcs; c[7] = ckss; c[8] = skc; c[9] = sks;
+}
+
+// k-space fields per site (iflag 0): the dipole field and, in the first pass, the static
+// charge field.  Blocks split the sites (two per thread) and the k vectors (blockIdx.y
+// chunks of kchunk); each writes its partial sums, which k_pol_kfield_sum adds in order.
+__global__ void __launch_bounds__(kThreads) k_pol_kfield(KArgs k, int first, int kchunk, double* __restrict__ part) {
+    __shared__ double sh[kKTile][8];
+    const int j0 = blockIdx.x * 2 * blockDim.x + threadIdx.x, j1 = j0 + blockDim.x;
+    const bool in0 = j0 < k.n, in1 = j1 < k.n;
+    const int kb = blockIdx.y * kchunk, ke = min(k.K, kb + kchunk);
+    double em0[3] = {0, 0, 0}, ec0[3] = {0, 0, 0}, em1[3] = {0, 0, 0}, ec1[3] = {0, 0, 0};
+    for (int t0 = kb; t0 < ke; t0 += kKTile) {
+        const int nt = min(kKTile, ke - t0);
+        __syncthreads();
+        for (int u = threadIdx.x; u < nt * 8; u += blockDim.x) sh[u >> 3][u & 7] = k.kco[16 * (size_t)(t0 + (u >> 3)) + (u & 7)];
+        __syncthreads();
+        const double2* e = k.eik + (size_t)t0 * k.n;
+        for (int u = 0; u < nt; ++u, e += k.n) {
+            const double* c = sh[u];
+            if (in0) {
+                const double2 cs = e[j0];
+                const double vv = cs.y * c[3] + cs.x * c[4];
+                em0[0] -= c[0] * vv; em0[1] -= c[1] * vv; em0[2] -= c[2] * vv;
+                if (first) {
+                    const double tt = -cs.y * c[5] + cs.x * c[6];
+                    ec0[0] -= c[0] * tt; ec0[1] -= c[1] * tt; ec0[2] -= c[2] * tt;
+                }
+            }
+            if (in1) {
+                const double2 cs = e[j1];
+                const double vv = cs.y * c[3] + cs.x * c[4];
+                em1[0] -= c[0] * vv; em1[1] -= c[1] * vv; em1[2] -= c[2] * vv;
+                if (first) {
+                    const double tt = -cs.y * c[5] + cs.x * c[6];
+                    ec1[0] -= c[0] * tt; ec1[1] -= c[1] * tt; ec1[2] -= c[2] * tt;
+                }
+            }
+        }
+    }
+    double* p = part + (size_t)blockIdx.y * 6 * k.n;
     for (int c = 0; c < 3; ++c) {
-        if (first) a.efc[c * k.n + j] = k.scale * ec[c];
-        a.efm[c * k.n + j] = k.scale * em[c] + dum * m[c];
+        if (in0) {
+            p[c * (size_t)k.n + j0] = em0[c];
+            p[(3 + c) * (size_t)k.n + j0] = ec0[c];
+        }
+        if (in1) {
+            p[c * (size_t)k.n + j1] = em1[c];
+            p[(3 + c) * (size_t)k.n + j1] = ec1[c];
+        }
     }
 }
 
-// iter (SOURCE/iter.f): SOR update of the dipoles; sum of squared changes and count.
-__global__ void __launch_bounds__(kThreads) k_pol_iter(PolArgs a) {
+__global__ void __launch_bounds__(kThreads) k_pol_kfield_sum(KArgs k, PolArgs a, int first, int nchunk,
+                                                             const double* __restrict__ part) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= k.n) return;
+    double em[3] = {0, 0, 0}, ec[3] = {0, 0, 0};
+    for (int q = 0; q < nchunk; ++q) {
+        const double* p = part + (size_t)q * 6 * k.n;
+        for (int c = 0; c < 3; ++c) {
+            em[c] += p[c * (size_t)k.n + j];
+            if (first) ec[c] += p[(3 + c) * (size_t)k.n + j];
+        }
+    }
+    const double dum = 4.0 * kR4pie0 * (a.alpha * a.alpha * a.alpha) / kSqrpi / 3.0;
+    const bool pol = a.polr2[j] > 1e-6;
+    const double m[3] = {a.mx[j], a.my[j], a.mz[j]};
+    for (int c = 0; c < 3; ++c) {
+        if (first) a.efc[c * k.n + j] = k.scale * ec[c];
+        a.efm[c * k.n + j] = (pol ? k.scale * em[c] : 0.0) + dum * m[c];
+    }
+}
+
+// iter (SOURCE/iter.f): SOR update of the dipoles; sum of squared changes and count;
+// refreshes the masked dipoles of the structure factors.
+__global__ void __launch_bounds__(kThreads) k_pol_iter(PolArgs a, double4* __restrict__ md) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     double v[2] = {0, 0};
     if (i < a.n && a.polr2[i] > a.toler) {
         const double oldfac = a.omega, fac = 1.0 - oldfac;
         double* m[3] = {a.mx + i, a.my + i, a.mz + i};
-        double dd = 0.0;
+        double dd = 0.0, nm[3];
         for (int c = 0; c < 3; ++c) {
             const double o = *m[c];
             const double f = a.efk[c * a.n + i] + a.emu[c * a.n + i] + a.efm[c * a.n + i] + a.efc[c * a.n + i] + 0.0;
             const double nv = oldfac * o + fac * a.polr2[i] * f / kR4pie0;
             *m[c] = nv;
+            nm[c] = nv;
             dd += (nv - o) * (nv - o);
         }
+        if (a.polr2[i] > 1e-6) md[i] = make_double4(nm[0], nm[1], nm[2], 0.0);
         v[0] = dd;
         v[1] = 1.0;
     }
     block_sum_atomic<2>(v, a.acc + 27);
 }
 
-// Final k-space pass (ewald1p iflag 1) per site, fused with coulomb_polar and the
-// self terms: forces, DMS potentials, per-site energies, the ew1p heat-current stress.
-__global__ void __launch_bounds__(kThreads) k_pol_kforce(KArgs k, PolArgs a, int heat) {
-    __shared__ double sh[kKTile][18];
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool in = j < k.n;
-    const double qj = in ? a.q[j] : 0.0;
-    const bool pol = in && a.polr2[j] > 1e-6;
-    const double dv[3] = {in ? a.mx[j] : 0.0, in ? a.my[j] : 0.0, in ? a.mz[j] : 0.0};
-    double vh[3] = {0, 0, 0};
-    if (in && heat) vhat(a, j, vh);
-    double fk[3] = {0, 0, 0}, vk = 0, vdk = 0, aek = 0, jp[3] = {0, 0, 0};
-    const double scalefactor = 0.5 * k.scale;   // 2 rvolm r4pie0 / epsq
-    for (int t0 = 0; t0 < k.K; t0 += kKTile) {
-        const int nt = min(kKTile, k.K - t0);
-        __syncthreads();
-        for (int u = threadIdx.x; u < nt; u += blockDim.x) {
-            const double4 kv = k.kv[t0 + u];
-            const double2 k2 = k.kx2[t0 + u];
-            const double* s = k.sf + 8 * (size_t)(t0 + u);
-            const double skc = kv.x * s[2] + kv.y * s[3] + kv.z * s[4];
-            const double sks = kv.x * s[5] + kv.y * s[6] + kv.z * s[7];
-            double* r = sh[u];
-            r[0] = kv.x; r[1] = kv.y; r[2] = kv.z; r[3] = kv.w;
-            r[4] = s[0]; r[5] = s[1]; r[6] = skc; r[7] = sks;
-            r[8] = s[0] - sks; r[9] = s[1] + skc;   // summu1, summu2
-            r[10] = k2.y;                            // akv2
-            for (int c = 0; c < 6; ++c) r[11 + c] = s[2 + c];
+// --- mixed precision: FP32 correction solves under FP64 refinement -----------------------
+struct MixArgs {
+    float4* r32;      // FP64 residual, rounded (polarizable sites; 0 elsewhere)
+    float4* d32;      // correction dipoles
+    float* e32;       // FP32 field of the correction: real space (3 blocks of n), then k space (3 blocks)
+};
+
+// FP64 residual of the dipole equations at the current dipoles: r = polr2 E / r4pie0 - mu
+// with E the four fields of the last FP64 evaluation; rounds it for the FP32 solve and
+// clears the correction.  Sums |r|^2 and the count into acc[29..30].
+__global__ void __launch_bounds__(kThreads) k_pol_resid(PolArgs a, MixArgs m) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double v[2] = {0, 0};
+    if (i < a.n) {
+        float4 r = make_float4(0, 0, 0, 0);
+        if (a.polr2[i] > a.toler) {
+            double rr[3];
+            const double mu[3] = {a.mx[i], a.my[i], a.mz[i]};
+            for (int c = 0; c < 3; ++c) {
+                const double f = a.efk[c * a.n + i] + a.emu[c * a.n + i] + a.efm[c * a.n + i] + a.efc[c * a.n + i] + 0.0;
+                rr[c] = a.polr2[i] * f / kR4pie0 - mu[c];
+            }
+            v[0] = rr[0] * rr[0] + rr[1] * rr[1] + rr[2] * rr[2];
+            v[1] = 1.0;
+            r = make_float4((float)rr[0], (float)rr[1], (float)rr[2], 0.f);
         }
-        __syncthreads();
-        if (!in) continue;
-        for (int u = 0; u < nt; ++u) {
-            const double* r = sh[u];
-            const double2 cs = k.eik[(size_t)(t0 + u) * k.n + j];
-            const double c = cs.x, s = cs.y;
-            const double akk = r[3];
-            const double djmuk = pol ? dv[0] * r[0] + dv[1] * r[1] + dv[2] * r[2] : 0.0;
-            const double ssmu = r[8] * (-s * qj - c * djmuk) + r[9] * (-s * djmuk + c * qj);
-            fk[0] -= r[0] * akk * ssmu;
-            fk[1] -= r[1] * akk * ssmu;
-            fk[2] -= r[2] * akk * ssmu;
-            vk += akk * (c * r[4] + s * r[5]);
-            vdk += akk * (s * r[6] - c * r[7]);
-            const double Cqi = qj * c, Sqi = qj * s;
-            aek += scalefactor * akk * (Cqi * r[4] + Sqi * r[5]);
-            if (heat) {
-                const double kvec[3] = {r[0], r[1], r[2]};
-                const double* Mc = r + 11;
-                const double* Ms = r + 14;
-                const double CMi[3] = {dv[0] * c, dv[1] * c, dv[2] * c};
-                const double SMi[3] = {dv[0] * s, dv[1] * s, dv[2] * s};
-                const double dpkCMi = kvec[0] * CMi[0] + kvec[1] * CMi[1] + kvec[2] * CMi[2];
-                const double dpkSMi = kvec[0] * SMi[0] + kvec[1] * SMi[1] + kvec[2] * SMi[2];
-                const double dpkMc = r[6], dpkMs = r[7];
-                const double X = (Cqi * r[4] + Sqi * r[5]) + (Sqi * dpkMc - Cqi * dpkMs - dpkSMi * r[4] + dpkCMi * r[5]) +
-                                 (dpkCMi * dpkMc + dpkSMi * dpkMs);
-                double Y[3];
-                for (int b = 0; b < 3; ++b)
-                    Y[b] = (Sqi * Mc[b] - Cqi * Ms[b] - SMi[b] * r[4] + CMi[b] * r[5]) +
-                           (CMi[b] * dpkMc + SMi[b] * dpkMs + dpkCMi * Mc[b] + dpkSMi * Ms[b]);
-                const double f = scalefactor * akk;
-                double S[6];   // upper triangle 11 12 13 22 23 33
-                const int ia[6] = {0, 0, 0, 1, 1, 2}, ib[6] = {0, 1, 2, 1, 2, 2};
+        m.r32[i] = r;
+        m.d32[i] = make_float4(0, 0, 0, 0);
+    }
+    block_sum_atomic<2>(v, a.acc + 29);
+}
+
+// FP32 real-space dipole field of the correction (warp per site).
+__global__ void k_pol_dd32(PolArgs a, MixArgs m) {
+    const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (i >= a.n) return;
+    float e[3] = {0, 0, 0};
+    if (a.polr2[i] > 1e-6) {
+        const int nn = a.nn[i];
+        const size_t row = (size_t)i * a.cap, blk = (size_t)a.n * a.cap;
+        for (int k = lane; k < nn; k += 32) {
+            const float4 d = m.d32[a.nbr[row + k]];
+            float t[6];
 #pragma unroll
-                for (int p = 0; p < 6; ++p)
-                    S[p] = f * (((ia[p] == ib[p] ? 1.0 : 0.0) - r[10] * kvec[ia[p]] * kvec[ib[p]]) * X + kvec[ia[p]] * Y[ib[p]]);
-                jp[0] += S[0] * vh[0] + S[1] * vh[1] + S[2] * vh[2];
-                jp[1] += S[1] * vh[0] + S[3] * vh[1] + S[4] * vh[2];
-                jp[2] += S[2] * vh[0] + S[4] * vh[1] + S[5] * vh[2];
+            for (int p = 0; p < 6; ++p) t[p] = a.tens32[p * blk + row + k];
+            e[0] += t[0] * d.x + t[1] * d.y + t[2] * d.z;
+            e[1] += t[1] * d.x + t[3] * d.y + t[4] * d.z;
+            e[2] += t[2] * d.x + t[4] * d.y + t[5] * d.z;
+        }
+        for (int c = 0; c < 3; ++c) e[c] = warp_sum(e[c]);
+        if (lane == 0 && i < 3 * a.nw) {
+            const int w = i / 3, s = i % 3;
+            const int pj[3][2] = {{1, 2}, {0, 2}, {0, 1}};
+            const int pp[3][2] = {{0, 1}, {0, 2}, {1, 2}};
+            const double* T = a.intra + 18 * (size_t)w;
+            for (int u = 0; u < 2; ++u) {
+                const float4 d = m.d32[3 * w + pj[s][u]];
+                const double* t = T + 6 * pp[s][u];
+                e[0] += (float)t[0] * d.x + (float)t[1] * d.y + (float)t[2] * d.z;
+                e[1] += (float)t[1] * d.x + (float)t[3] * d.y + (float)t[4] * d.z;
+                e[2] += (float)t[2] * d.x + (float)t[4] * d.y + (float)t[5] * d.z;
             }
         }
     }
-    double red[6] = {0, 0, 0, 0, 0, 0};   // engsic, eng_polar, jpot(3), unused
-    if (in) {
-        a.fx[j] += k.scale * fk[0];
-        a.fy[j] += k.scale * fk[1];
-        a.fz[j] += k.scale * fk[2];
-        a.vesp[j] = k.scale * vk + k.scale * vdk - 2.0 * kR4pie0 * qj * a.alpha / kSqrpi / a.eps;
+    if (lane == 0)
+        for (int c = 0; c < 3; ++c) m.e32[c * a.n + i] = e[c];
+}
+
+// FP32 dipole structure factors of the correction and the coefficients of its gather.
+__global__ void __launch_bounds__(kSfThreads) k_pol_sfd32(KArgs k, MixArgs m) {
+    const int kk = blockIdx.x;
+    const float2* e = k.eik32 + (size_t)kk * k.n;
+    float v[6] = {0, 0, 0, 0, 0, 0};
+    for (int j = threadIdx.x; j < k.n; j += kSfThreads) {
+        const float2 cs = e[j];
+        const float4 d = m.d32[j];
+        v[0] += cs.x * d.x; v[1] += cs.x * d.y; v[2] += cs.x * d.z;
+        v[3] += cs.y * d.x; v[4] += cs.y * d.y; v[5] += cs.y * d.z;
+    }
+    __shared__ float red[kSfThreads / 32][6];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int q = 0; q < 6; ++q) {
+        const float sq = warp_sum(v[q]);
+        if (lane == 0) red[w][q] = sq;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t[6] = {0, 0, 0, 0, 0, 0};
+        for (int i = 0; i < kSfThreads / 32; ++i)
+            for (int q = 0; q < 6; ++q) t[q] += red[i][q];
+        const double4 kv = k.kv[kk];
+        float* c = k.kco32 + 8 * (size_t)kk;
+        c[0] = (float)kv.x; c[1] = (float)kv.y; c[2] = (float)kv.z;
+        c[3] = (float)(kv.w * (kv.x * t[3] + kv.y * t[4] + kv.z * t[5]));
+        c[4] = (float)(kv.w * (kv.x * t[0] + kv.y * t[1] + kv.z * t[2]));
+    }
+}
+
+// FP32 k-space field of the correction: two sites per thread, k vectors split over
+// blockIdx.y; partial sums added in order by k_pol_kfield32_sum.
+__global__ void __launch_bounds__(kThreads) k_pol_kfield32(KArgs k, int kchunk, float* __restrict__ part) {
+    __shared__ float sh[kKTile][8];
+    const int j0 = blockIdx.x * 2 * blockDim.x + threadIdx.x, j1 = j0 + blockDim.x;
+    const int kb = blockIdx.y * kchunk, ke = min(k.K, kb + kchunk);
+    float e0[3] = {0, 0, 0}, e1[3] = {0, 0, 0};
+    for (int t0 = kb; t0 < ke; t0 += kKTile) {
+        const int nt = min(kKTile, ke - t0);
+        __syncthreads();
+        for (int u = threadIdx.x; u < nt * 8; u += blockDim.x) sh[u >> 3][u & 7] = k.kco32[8 * (size_t)(t0 + (u >> 3)) + (u & 7)];
+        __syncthreads();
+        const float2* e = k.eik32 + (size_t)t0 * k.n;
+        if (j1 < k.n) {
+#pragma unroll 4
+            for (int u = 0; u < nt; ++u) {
+                const float* c = sh[u];
+                const float2 a0 = e[(size_t)u * k.n + j0], a1 = e[(size_t)u * k.n + j1];
+                const float v0 = a0.y * c[3] + a0.x * c[4], v1 = a1.y * c[3] + a1.x * c[4];
+                e0[0] -= c[0] * v0; e0[1] -= c[1] * v0; e0[2] -= c[2] * v0;
+                e1[0] -= c[0] * v1; e1[1] -= c[1] * v1; e1[2] -= c[2] * v1;
+            }
+        } else if (j0 < k.n) {
+            for (int u = 0; u < nt; ++u) {
+                const float* c = sh[u];
+                const float2 a0 = e[(size_t)u * k.n + j0];
+                const float v0 = a0.y * c[3] + a0.x * c[4];
+                e0[0] -= c[0] * v0; e0[1] -= c[1] * v0; e0[2] -= c[2] * v0;
+            }
+        }
+    }
+    float* p = part + (size_t)blockIdx.y * 3 * k.n;
+    for (int c = 0; c < 3; ++c) {
+        if (j0 < k.n) p[c * (size_t)k.n + j0] = e0[c];
+        if (j1 < k.n) p[c * (size_t)k.n + j1] = e1[c];
+    }
+}
+
+__global__ void __launch_bounds__(kThreads) k_pol_kfield32_sum(KArgs k, PolArgs a, MixArgs m, int nchunk,
+                                                               const float* __restrict__ part) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= k.n) return;
+    float ev[3] = {0, 0, 0};
+    for (int q = 0; q < nchunk; ++q)
+        for (int c = 0; c < 3; ++c) ev[c] += part[((size_t)q * 3 + c) * k.n + j];
+    const float dum = (float)(4.0 * kR4pie0 * (a.alpha * a.alpha * a.alpha) / kSqrpi / 3.0);
+    const float sc = (float)k.scale;
+    const bool pol = a.polr2[j] > 1e-6;
+    const float4 d = m.d32[j];
+    const float dd[3] = {d.x, d.y, d.z};
+    for (int c = 0; c < 3; ++c) m.e32[(3 + c) * (size_t)k.n + j] = (pol ? sc * ev[c] : 0.f) + dum * dd[c];
+}
+
+// One SOR sweep of the correction: d <- omega d + (1 - omega)(r + polr2 E(d) / r4pie0);
+// sums |change|^2 into acc[31] (count in acc[32]).
+__global__ void __launch_bounds__(kThreads) k_pol_inner(PolArgs a, MixArgs m, int nk) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double v[2] = {0, 0};
+    if (i < a.n && a.polr2[i] > a.toler) {
+        const float om = (float)a.omega, fc = 1.f - om;
+        const float p = (float)(a.polr2[i] / kR4pie0);
+        const float4 r = m.r32[i];
+        float4 d = m.d32[i];
+        const float rv[3] = {r.x, r.y, r.z};
+        float dv[3] = {d.x, d.y, d.z};
+        float ch = 0.f;
+        for (int c = 0; c < 3; ++c) {
+            const float f = m.e32[c * (size_t)a.n + i] + (nk ? m.e32[(3 + c) * (size_t)a.n + i] : 0.f);
+            const float nv = om * dv[c] + fc * (rv[c] + p * f);
+            ch += (nv - dv[c]) * (nv - dv[c]);
+            dv[c] = nv;
+        }
+        m.d32[i] = make_float4(dv[0], dv[1], dv[2], 0.f);
+        v[0] = ch;
+        v[1] = 1.0;
+    }
+    block_sum_atomic<2>(v, a.acc + 31);
+}
+
+// mu += d in FP64; refreshes the masked dipoles.
+__global__ void k_pol_apply(PolArgs a, MixArgs m, double4* __restrict__ md) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n || !(a.polr2[i] > a.toler)) return;
+    const float4 d = m.d32[i];
+    a.mx[i] += (double)d.x;
+    a.my[i] += (double)d.y;
+    a.mz[i] += (double)d.z;
+    if (a.polr2[i] > 1e-6) md[i] = make_double4(a.mx[i], a.my[i], a.mz[i], 0.0);
+}
+
+// Final k-space pass (ewald1p iflag 1): per site and chunk of k vectors, the force, the
+// two DMS potentials and the k-space charge energy (6 partial sums per site).
+__global__ void __launch_bounds__(kThreads) k_pol_kforce(KArgs k, PolArgs a, int kchunk, double* __restrict__ part) {
+    __shared__ double sh[kKTile][10];
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool in = j < k.n;
+    const int kb = blockIdx.y * kchunk, ke = min(k.K, kb + kchunk);
+    const double qj = in ? a.q[j] : 0.0;
+    const bool pol = in && a.polr2[j] > 1e-6;
+    const double dv[3] = {in ? a.mx[j] : 0.0, in ? a.my[j] : 0.0, in ? a.mz[j] : 0.0};
+    double fk[3] = {0, 0, 0}, vk = 0, vdk = 0, aek = 0;
+    for (int t0 = kb; t0 < ke; t0 += kKTile) {
+        const int nt = min(kKTile, ke - t0);
+        __syncthreads();
+        for (int u = threadIdx.x; u < nt * 10; u += blockDim.x)
+            sh[u / 10][u % 10] = k.kco[16 * (size_t)(t0 + u / 10) + u % 10];
+        __syncthreads();
+        if (!in) continue;
+        const double2* e = k.eik + (size_t)t0 * k.n + j;
+        for (int u = 0; u < nt; ++u, e += k.n) {
+            const double* r = sh[u];
+            const double2 cs = *e;
+            const double c = cs.x, s = cs.y;
+            const double akk = r[3];
+            const double djmuk = pol ? dv[0] * r[0] + dv[1] * r[1] + dv[2] * r[2] : 0.0;
+            const double ssmu = r[4] * (-s * qj - c * djmuk) + r[5] * (-s * djmuk + c * qj);
+            fk[0] -= r[0] * akk * ssmu;
+            fk[1] -= r[1] * akk * ssmu;
+            fk[2] -= r[2] * akk * ssmu;
+            vk += akk * (c * r[6] + s * r[7]);
+            vdk += akk * (s * r[8] - c * r[9]);
+            aek += akk * (qj * c * r[6] + qj * s * r[7]);
+        }
+    }
+    if (!in) return;
+    double* p = part + (size_t)blockIdx.y * 6 * k.n;
+    p[j] = fk[0];
+    p[k.n + j] = fk[1];
+    p[2 * (size_t)k.n + j] = fk[2];
+    p[3 * (size_t)k.n + j] = vk;
+    p[4 * (size_t)k.n + j] = vdk;
+    p[5 * (size_t)k.n + j] = aek;
+}
+
+// Per site: the k-space sums of all chunks, the self terms and coulomb_polar.
+__global__ void __launch_bounds__(kThreads) k_pol_kforce_sum(KArgs k, PolArgs a, int nchunk,
+                                                             const double* __restrict__ part) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    double red[2] = {0, 0};   // engsic, eng_polar
+    if (j < k.n) {
+        double v[6] = {0, 0, 0, 0, 0, 0};
+        for (int q = 0; q < nchunk; ++q)
+            for (int c = 0; c < 6; ++c) v[c] += part[((size_t)q * 6 + c) * k.n + j];
+        const double qj = a.q[j];
+        const double dv[3] = {a.mx[j], a.my[j], a.mz[j]};
+        a.fx[j] += k.scale * v[0];
+        a.fy[j] += k.scale * v[1];
+        a.fz[j] += k.scale * v[2];
+        a.vesp[j] = k.scale * v[3] + k.scale * v[4] - 2.0 * kR4pie0 * qj * a.alpha / kSqrpi / a.eps;
         const double self = -kR4pie0 / a.eps * a.alpha * qj * qj / kSqrpi;
-        double ae = self + aek;
+        double ae = self + k.sfac * v[5];
         red[0] = self;
-        if (pol) {   // coulomb_polar
+        if (a.polr2[j] > 1e-6) {   // coulomb_polar
             double e = 0.0;
             for (int c = 0; c < 3; ++c)
                 e += dv[c] * (a.efk[c * k.n + j] + a.efc[c * k.n + j] + 0.5 * (a.emu[c * k.n + j] + a.efm[c * k.n + j]) + 0.0);
@@ -643,11 +969,11 @@ __global__ void __launch_bounds__(kThreads) k_pol_kforce(KArgs k, PolArgs a, int
             red[1] = e + sp;
         }
         a.ae[j] = ae;
-        red[2] = jp[0]; red[3] = jp[1]; red[4] = jp[2];
     }
-    block_sum_atomic<6>(red, a.acc + 40);
+    block_sum_atomic<2>(red, a.acc + 40);
 }
 
+// ---------------------------------------------------------------------------------------
 // --- final real-space terms ----------------------------------------------------------------
 // ewald2p for the directed pair (i, j): force on i, its per-atom energy half, its DMS
 // potential; pair scalars only from i < j.
@@ -962,22 +1288,34 @@ __global__ void __launch_bounds__(kThreads) k_pol_jkin(PolArgs a, double* __rest
 }
 
 __global__ void k_pol_kreduce(int K, const double* __restrict__ kterm, double* __restrict__ out) {
-    // one block: out[q] = sum over k of kterm[8k + q]
-    double v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    // one block: out[q] = sum over k of kterm[16k + q], q < 11
+    constexpr int NV = 11;
+    double v[NV];
+    for (int q = 0; q < NV; ++q) v[q] = 0.0;
     for (int k = threadIdx.x; k < K; k += blockDim.x)
-        for (int q = 0; q < 8; ++q) v[q] += kterm[8 * (size_t)k + q];
-    __shared__ double red[kSfThreads / 32][8];
+        for (int q = 0; q < NV; ++q) v[q] += kterm[16 * (size_t)k + q];
+    __shared__ double red[kSfThreads / 32][NV];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    for (int q = 0; q < 8; ++q) {
+    for (int q = 0; q < NV; ++q) {
         const double s = warp_sum(v[q]);
         if (lane == 0) red[w][q] = s;
     }
     __syncthreads();
-    if (threadIdx.x < 8) {
+    if (threadIdx.x < NV) {
         double s = 0.0;
         for (int i = 0; i < kSfThreads / 32; ++i) s += red[i][threadIdx.x];
         out[threadIdx.x] = s;
     }
+}
+
+__global__ void k_pol_vhat(PolArgs a, double* __restrict__ vh) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= a.n) return;
+    double v[3];
+    vhat(a, j, v);
+    vh[j] = v[0];
+    vh[a.n + j] = v[1];
+    vh[2 * (size_t)a.n + j] = v[2];
 }
 
 inline unsigned blocks(long n, int t) { return (unsigned)((n + t - 1) / t); }
@@ -986,15 +1324,25 @@ inline unsigned blocks(long n, int t) { return (unsigned)((n + t - 1) / t); }
 
 // --- host -------------------------------------------------------------------------------
 void PolarState::release() {
-    void* p[] = {ercp, nn, nbr, flag, xf, tens, intra, fld, vesp, ae, eik, kv, kx2, lmn, sf, kterm, acc};
+    void* p[] = {ercp, nn, nbr, flag, xf, tens, intra, fld, vesp, ae, eik, kv, kx2, lmn, sf, kterm, acc, kco, fac, md, vh,
+                 tens32, r32, d32, e32, kco32, eik32, kpart};
     for (void* q : p)
         if (q) cudaFree(q);
     if (acc_h) cudaFreeHost(acc_h);
     ercp = nullptr;
     nn = nbr = flag = nullptr;
     xf = nullptr;
-    tens = intra = fld = vesp = ae = sf = kterm = acc = nullptr;
-    eik = nullptr;
+    tens = intra = fld = vesp = ae = sf = kterm = acc = kco = vh = nullptr;
+    eik = fac = nullptr;
+    md = nullptr;
+    fac_cap = 0;
+    tens32 = e32 = kco32 = nullptr;
+    r32 = d32 = nullptr;
+    eik32 = nullptr;
+    cap32 = n32 = k32 = 0;
+    eik32_cap = 0;
+    kpart = nullptr;
+    part_cap = 0;
     kv = nullptr;
     kx2 = nullptr;
     lmn = nullptr;
@@ -1034,19 +1382,62 @@ cudaError_t PolarState::table(double alpha, double rcut) {
     return cudaSuccess;
 }
 
-cudaError_t PolarState::reserve(int nw, int K) {
+cudaError_t PolarState::reserve_part(size_t nd) {
+    if (nd <= part_cap) return cudaSuccess;
+    if (kpart) cudaFree(kpart);
+    kpart = nullptr;
+    part_cap = 0;
+    cudaError_t e = cudaMalloc(&kpart, std::max(nd, (size_t)1) * sizeof(double));
+    if (!e) part_cap = nd;
+    return e;
+}
+
+cudaError_t PolarState::reserve_mixed(int n, int K) {
+    cudaError_t e;
+    if (!tens32 || cap32 != cap || n > n32) {
+        void* p[] = {tens32, r32, d32, e32};
+        for (void* q : p)
+            if (q) cudaFree(q);
+        tens32 = e32 = nullptr;
+        r32 = d32 = nullptr;
+        const size_t m = (size_t)std::max(n, 1);
+        if ((e = cudaMalloc(&tens32, 6 * m * cap * sizeof(float)))) return e;
+        if ((e = cudaMalloc(&r32, m * sizeof(float4)))) return e;
+        if ((e = cudaMalloc(&d32, m * sizeof(float4)))) return e;
+        if ((e = cudaMalloc(&e32, 6 * m * sizeof(float)))) return e;
+        cap32 = cap;
+        n32 = n;
+    }
+    if (K > k32) {
+        if (kco32) cudaFree(kco32);
+        kco32 = nullptr;
+        if ((e = cudaMalloc(&kco32, 8 * (size_t)std::max(K, 1) * sizeof(float)))) return e;
+        k32 = K;
+    }
+    const size_t need = (size_t)K * n;
+    if (need > eik32_cap) {
+        if (eik32) cudaFree(eik32);
+        eik32 = nullptr;
+        if ((e = cudaMalloc(&eik32, std::max(need, (size_t)1) * sizeof(float2)))) return e;
+        eik32_cap = need;
+    }
+    return cudaSuccess;
+}
+
+cudaError_t PolarState::reserve(int nw, int K, size_t nfac) {
     cudaError_t e;
     const int n = 4 * nw;
     if (!acc && (e = cudaMalloc(&acc, 64 * sizeof(double)))) return e;
     if (!acc_h && (e = cudaMallocHost(&acc_h, 64 * sizeof(double)))) return e;
     if (!flag && (e = cudaMalloc(&flag, 4 * sizeof(int)))) return e;
     if (n > n_cap || cap != cap_alloc) {
-        void* p[] = {nn, nbr, xf, tens, fld, vesp, ae};
+        void* p[] = {nn, nbr, xf, tens, fld, vesp, ae, md, vh};
         for (void* q : p)
             if (q) cudaFree(q);
         nn = nbr = nullptr;
         xf = nullptr;
-        tens = fld = vesp = ae = nullptr;
+        tens = fld = vesp = ae = vh = nullptr;
+        md = nullptr;
         const size_t m = (size_t)std::max(n, 1);
         if ((e = cudaMalloc(&nn, m * sizeof(int)))) return e;
         if ((e = cudaMalloc(&nbr, m * cap * sizeof(int)))) return e;
@@ -1055,6 +1446,8 @@ cudaError_t PolarState::reserve(int nw, int K) {
         if ((e = cudaMalloc(&fld, 12 * m * sizeof(double)))) return e;
         if ((e = cudaMalloc(&vesp, m * sizeof(double)))) return e;
         if ((e = cudaMalloc(&ae, m * sizeof(double)))) return e;
+        if ((e = cudaMalloc(&md, m * sizeof(double4)))) return e;
+        if ((e = cudaMalloc(&vh, 3 * m * sizeof(double)))) return e;
         n_cap = n;
         cap_alloc = cap;
     }
@@ -1065,18 +1458,19 @@ cudaError_t PolarState::reserve(int nw, int K) {
         nw_cap = nw;
     }
     if (K > k_cap) {
-        void* p[] = {kv, kx2, lmn, sf, kterm};
+        void* p[] = {kv, kx2, lmn, sf, kterm, kco};
         for (void* q : p)
             if (q) cudaFree(q);
         kv = nullptr;
         kx2 = nullptr;
         lmn = nullptr;
-        sf = kterm = nullptr;
+        sf = kterm = kco = nullptr;
         if ((e = cudaMalloc(&kv, K * sizeof(double4)))) return e;
         if ((e = cudaMalloc(&kx2, K * sizeof(double2)))) return e;
         if ((e = cudaMalloc(&lmn, K * sizeof(int4)))) return e;
         if ((e = cudaMalloc(&sf, 8 * (size_t)K * sizeof(double)))) return e;
-        if ((e = cudaMalloc(&kterm, 8 * (size_t)K * sizeof(double)))) return e;
+        if ((e = cudaMalloc(&kterm, 16 * (size_t)K * sizeof(double)))) return e;
+        if ((e = cudaMalloc(&kco, 16 * (size_t)K * sizeof(double)))) return e;
         k_cap = K;
     }
     const size_t need = (size_t)K * n;
@@ -1086,10 +1480,16 @@ cudaError_t PolarState::reserve(int nw, int K) {
         if ((e = cudaMalloc(&eik, std::max(need, (size_t)1) * sizeof(double2)))) return e;
         eik_cap = need;
     }
+    if (nfac * n > fac_cap) {
+        if (fac) cudaFree(fac);
+        fac = nullptr;
+        if ((e = cudaMalloc(&fac, std::max(nfac * n, (size_t)1) * sizeof(double2)))) return e;
+        fac_cap = nfac * n;
+    }
     return cudaSuccess;
 }
 
-cudaError_t PolarState::run(const Cell& cl, const double* prm, int nw, const double* x, const double* y,
+cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, int nw, const double* x, const double* y,
                             const double* z, const double* q, const double* dp, const double* polr,
                             const double* polr2, double* mx, double* my, double* mz, double* fx, double* fy,
                             double* fz, double* ae_out, const double* vx, const double* vy, const double* vz,
@@ -1172,13 +1572,17 @@ cudaError_t PolarState::run(const Cell& cl, const double* prm, int nw, const dou
     }
     const int K = (int)hk.size();
     if (n > 65535L * kThreads) return cudaErrorInvalidValue;
-    if ((e = reserve(nw, K))) return e;
+    const size_t nfac = (size_t)(kmax[0] + 1) + (2 * kmax[1] + 1) + (2 * kmax[2] + 1);
+    if ((e = reserve(nw, K, nfac))) return e;
+    if (precision == 1 && (e = reserve_mixed(n, K))) return e;
     if (K) {
         if ((e = cudaMemcpyAsync(kv, hk.data(), K * sizeof(double4), cudaMemcpyHostToDevice, s))) return e;
         if ((e = cudaMemcpyAsync(kx2, hk2.data(), K * sizeof(double2), cudaMemcpyHostToDevice, s))) return e;
         if ((e = cudaMemcpyAsync(lmn, hlmn.data(), K * sizeof(int4), cudaMemcpyHostToDevice, s))) return e;
     }
     const bool heat = vx && vy && vz;
+    const bool mixed = precision == 1;
+    inner_sweeps = 0;
 
     PolArgs a;
     auto bind = [&](PolArgs& b) {
@@ -1188,6 +1592,7 @@ cudaError_t PolarState::run(const Cell& cl, const double* prm, int nw, const dou
         b.nn = nn;
         b.nbr = nbr;
         b.tens = tens;
+        b.tens32 = mixed ? tens32 : nullptr;
         b.intra = intra;
         b.efk = fld;
         b.efc = fld + 3 * (size_t)n;
@@ -1217,15 +1622,24 @@ cudaError_t PolarState::run(const Cell& cl, const double* prm, int nw, const dou
     KArgs k;
     k.K = K;
     k.n = n;
+    for (int c = 0; c < 3; ++c) k.kmax[c] = kmax[c];
     k.kv = kv;
     k.kx2 = kx2;
     k.lmn = lmn;
+    k.fac = fac;
     k.eik = eik;
+    k.eik32 = mixed ? eik32 : nullptr;
+    k.kco32 = kco32;
     k.sf = sf;
+    k.kco = kco;
     k.kterm = kterm;
+    k.md = md;
+    k.q = q;
+    k.vh = vh;
     for (int c = 0; c < 9; ++c) k.rc[c] = rc[c];
     k.scale = 4.0 * rvolm * kR4pie0 / epsq;
     k.ralph = ralph;
+    k.sfac = 2.0 * rvolm * kR4pie0 / epsq;
 
     if ((e = cudaMemsetAsync(acc, 0, 64 * sizeof(double), s))) return e;
     if (n == 0) {
@@ -1247,44 +1661,126 @@ cudaError_t PolarState::run(const Cell& cl, const double* prm, int nw, const dou
         std::memcpy(&fh, acc_h, sizeof(int));
         if (!fh) break;
         cap = std::min(2 * cap, std::max(n, 32));   // a row holds at most n - 1 sites
-        if ((e = reserve(nw, K))) return e;
+        if ((e = reserve(nw, K, nfac))) return e;
+        if (mixed && (e = reserve_mixed(n, K))) return e;
     }
+    bind(a);
+    k.eik32 = mixed ? eik32 : nullptr;
+    k.kco32 = kco32;
     k_pol_static<<<blocks(32L * n, kThreads), kThreads, 0, s>>>(a);
     k_pol_intra_static<<<blocks(nw, kThreads), kThreads, 0, s>>>(a);
     launches += 2;
+    k_pol_mask<<<blocks(n, kThreads), kThreads, 0, s>>>(a, md);
+    ++launches;
     if (K) {
+        k_pol_factors<<<blocks(n, kThreads), kThreads, 0, s>>>(k, x, y, z);
         dim3 g(K, blocks(n, kThreads));   // sites per k vector along y (n < 65535 * 128)
-        k_pol_phase<<<g, kThreads, 0, s>>>(k, x, y, z);
-        ++launches;
+        k_pol_phase<<<g, kThreads, 0, s>>>(k);
+        k_pol_sfq<<<K, kSfThreads, 0, s>>>(k, q);
+        launches += 3;
     }
     double deltadip = 0.0;
-    int status_it = 0;
-    for (int it = 1;; ++it) {
+    // k vectors per chunk of the field / force gathers: about four blocks per SM in all
+    const int sblk2 = (int)blocks(n, 2 * kThreads), sblk1 = (int)blocks(n, kThreads);
+    auto chunking = [&](int sblk, int& kchunk, int& nchunk) {
+        const int want = std::max(1, (4 * nsm + sblk - 1) / sblk);
+        kchunk = std::max(kKTile, (int)(((K + want - 1) / want + kKTile - 1) / kKTile) * kKTile);
+        nchunk = K ? (K + kchunk - 1) / kchunk : 0;
+    };
+    int kc2, nc2, kc1, nc1;
+    chunking(sblk2, kc2, nc2);
+    chunking(sblk1, kc1, nc1);
+    if ((e = reserve_part((size_t)6 * std::max(nc1, nc2) * n))) return e;
+    auto fields64 = [&](bool first) {
         k_pol_dd<<<blocks(32L * n, kThreads), kThreads, 0, s>>>(a);
-        if (K) k_pol_sf<<<K, kSfThreads, 0, s>>>(k, a, 0);
-        k_pol_kfield<<<blocks(n, kThreads), kThreads, 0, s>>>(k, a, it == 1);
-        if ((e = cudaMemsetAsync(acc + 27, 0, 2 * sizeof(double), s))) return e;
-        k_pol_iter<<<blocks(n, kThreads), kThreads, 0, s>>>(a);
-        launches += K ? 4 : 3;
-        if ((e = cudaMemcpyAsync(acc_h + 27, acc + 27, 2 * sizeof(double), cudaMemcpyDeviceToHost, s))) return e;
-        if ((e = cudaStreamSynchronize(s))) return e;
-        const double ndip = acc_h[28] > 0.0 ? acc_h[28] : 1.0;
-        deltadip = std::sqrt(acc_h[27] / ndip);
-        iterations = it;
-        if (deltadip <= prm[3]) {
-            converged = true;
-            break;
+        if (K) {
+            k_pol_sfd<<<K, kSfThreads, 0, s>>>(k);
+            k_pol_kfield<<<dim3(sblk2, nc2), kThreads, 0, s>>>(k, first, kc2, kpart);
         }
-        if (it >= maxit) {
-            status_it = 1;
-            break;
+        k_pol_kfield_sum<<<sblk1, kThreads, 0, s>>>(k, a, first, nc2, kpart);
+        launches += K ? 4 : 2;
+    };
+    auto sor64 = [&]() -> cudaError_t {   // iter, then read the rms change
+        cudaError_t err;
+        if ((err = cudaMemsetAsync(acc + 27, 0, 2 * sizeof(double), s))) return err;
+        k_pol_iter<<<blocks(n, kThreads), kThreads, 0, s>>>(a, md);
+        ++launches;
+        if ((err = cudaMemcpyAsync(acc_h + 27, acc + 27, 2 * sizeof(double), cudaMemcpyDeviceToHost, s))) return err;
+        if ((err = cudaStreamSynchronize(s))) return err;
+        deltadip = std::sqrt(acc_h[27] / (acc_h[28] > 0.0 ? acc_h[28] : 1.0));
+        return cudaSuccess;
+    };
+    if (!mixed) {
+        for (int it = 1;; ++it) {
+            fields64(it == 1);
+            if ((e = sor64())) return e;
+            iterations = it;
+            if (deltadip <= prm[3]) {
+                converged = true;
+                break;
+            }
+            if (it >= maxit) break;
+        }
+    } else {
+        // FP64 refinement: the residual of the FP64 fields decides; the correction is solved
+        // with FP32 fields; the last step is the FP64 SOR update of the reference.
+        MixArgs m;
+        m.r32 = r32;
+        m.d32 = d32;
+        m.e32 = e32;
+        const double fac = 1.0 - prm[4];
+        for (int it = 1;; ++it) {
+            fields64(it == 1);
+            if ((e = cudaMemsetAsync(acc + 29, 0, 2 * sizeof(double), s))) return e;
+            k_pol_resid<<<blocks(n, kThreads), kThreads, 0, s>>>(a, m);
+            ++launches;
+            if ((e = cudaMemcpyAsync(acc_h + 29, acc + 29, 2 * sizeof(double), cudaMemcpyDeviceToHost, s))) return e;
+            if ((e = cudaStreamSynchronize(s))) return e;
+            const double rms = std::sqrt(acc_h[29] / (acc_h[30] > 0.0 ? acc_h[30] : 1.0));
+            iterations = it;
+            if (fac * rms <= prm[3] || it >= maxit) {
+                if ((e = sor64())) return e;
+                converged = deltadip <= prm[3];
+                break;
+            }
+            const double target = std::max(1e-6 * rms, 0.05 * prm[3]);
+            for (int sweep = 0; sweep < 200; ++sweep) {
+                k_pol_dd32<<<blocks(32L * n, kThreads), kThreads, 0, s>>>(a, m);
+                if (K) {
+                    k_pol_sfd32<<<K, kSfThreads, 0, s>>>(k, m);
+                    k_pol_kfield32<<<dim3(sblk2, nc2), kThreads, 0, s>>>(k, kc2, (float*)kpart);
+                    k_pol_kfield32_sum<<<sblk1, kThreads, 0, s>>>(k, a, m, nc2, (const float*)kpart);
+                    ++launches;
+                }
+                if ((e = cudaMemsetAsync(acc + 31, 0, 2 * sizeof(double), s))) return e;
+                k_pol_inner<<<blocks(n, kThreads), kThreads, 0, s>>>(a, m, K ? 1 : 0);
+                launches += K ? 4 : 2;
+                ++inner_sweeps;
+                if ((e = cudaMemcpyAsync(acc_h + 31, acc + 31, 2 * sizeof(double), cudaMemcpyDeviceToHost, s))) return e;
+                if ((e = cudaStreamSynchronize(s))) return e;
+                const double ch = std::sqrt(acc_h[31] / (acc_h[32] > 0.0 ? acc_h[32] : 1.0));
+                if (ch <= target) break;
+            }
+            k_pol_apply<<<blocks(n, kThreads), kThreads, 0, s>>>(a, m, md);
+            ++launches;
         }
     }
-    (void)status_it;
     // final pass
     const double g34 = std::exp(gammln(3.0 / 4.0));
-    if (K) k_pol_sf<<<K, kSfThreads, 0, s>>>(k, a, 1);
-    k_pol_kforce<<<blocks(n, kThreads), kThreads, 0, s>>>(k, a, heat);
+    if (heat) {
+        k_pol_vhat<<<blocks(n, kThreads), kThreads, 0, s>>>(a, vh);
+        ++launches;
+    }
+    if (K) {
+        if (heat) k_pol_sf_final<1><<<K, kSfThreads, 0, s>>>(k);
+        else k_pol_sf_final<0><<<K, kSfThreads, 0, s>>>(k);
+        ++launches;
+    }
+    if (K) {
+        k_pol_kforce<<<dim3(sblk1, nc1), kThreads, 0, s>>>(k, a, kc1, kpart);
+        ++launches;
+    }
+    k_pol_kforce_sum<<<sblk1, kThreads, 0, s>>>(k, a, nc1, kpart);
     k_pol_ewald2p<<<blocks(32L * n, kThreads), kThreads, 0, s>>>(a, g34, heat);
     k_pol_ewald3p<<<blocks(nw, kThreads), kThreads, 0, s>>>(a, heat);
     k_pol_qdforce<<<blocks(nw, kThreads), kThreads, 0, s>>>(a, heat);
@@ -1292,15 +1788,15 @@ cudaError_t PolarState::run(const Cell& cl, const double* prm, int nw, const dou
     launches += 5;
     if (K) {
         k_pol_kreduce<<<1, kSfThreads, 0, s>>>(K, kterm, acc + 48);
-        launches += 2;
+        ++launches;
     }
     if ((e = cudaGetLastError())) return e;
     if ((e = cudaMemcpyAsync(acc_h, acc, 64 * sizeof(double), cudaMemcpyDeviceToHost, s))) return e;
     if ((e = cudaStreamSynchronize(s))) return e;
     const double* h = acc_h;
     // acc: 0 eng_real, 1 vir, 2..7 stress (11 12 13 22 23 33), 8..10 jpot (real + qd),
-    //      24..26 jkin, 40 engsic, 41 eng_polar, 42..44 jpot (k space),
-    //      48 engc, 49 engdum, 50..55 omg (11 22 33 12 13 23)
+    //      24..26 jkin, 27..28 iteration sums, 40 engsic, 41 eng_polar,
+    //      48 engc, 49 engdum, 50..55 omg (11 22 33 12 13 23), 56..58 jpot (k space)
     const double scal1 = 2.0 * rvolm * kR4pie0 / epsq;
     const double engc = K ? h[48] : 0.0, eng1 = K ? h[49] : 0.0;
     const double omg11 = K ? h[50] : 0.0, omg22 = K ? h[51] : 0.0, omg33 = K ? h[52] : 0.0;
@@ -1327,7 +1823,7 @@ cudaError_t PolarState::run(const Cell& cl, const double* prm, int nw, const dou
     out16[15] = h[0];
     if (heat) {
         for (int c = 0; c < 3; ++c) {
-            jpot[c] += h[8 + c] + h[42 + c];
+            jpot[c] += h[8 + c] + (K ? h[56 + c] : 0.0);
             jkin[c] += h[24 + c];
         }
     }

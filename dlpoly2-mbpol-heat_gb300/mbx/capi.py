@@ -88,10 +88,12 @@ def load(path=None):
     L.mbx_disp_forces.argtypes = [C.c_void_p, C.c_int, _D, C.c_int, _I, _I] + [_D] * 14
     L.mbx_disp_forces_device.argtypes = [C.c_void_p, C.c_int, _D, C.c_int] + [C.c_void_p] * 12 + [_D]
     L.mbx_disp_lrc.argtypes = [C.c_int, _D, _I, C.c_double, C.c_double, _D, _D]
-    L.mbx_polar_forces.argtypes = [C.c_void_p, _D, C.c_int, _D, C.c_int] + [_D] * 20
-    L.mbx_polar_forces_device.argtypes = [C.c_void_p, _D, C.c_int, _D, C.c_int] + [C.c_void_p] * 14 + [_D] + \
-        [C.c_void_p] * 4 + [_D, _D]
+    L.mbx_polar_forces.argtypes = [C.c_void_p, C.c_int, _D, C.c_int, _D, C.c_int] + [_D] * 20
+    L.mbx_polar_forces_device.argtypes = [C.c_void_p, C.c_int, _D, C.c_int, _D, C.c_int] + [C.c_void_p] * 14 + \
+        [_D] + [C.c_void_p] * 4 + [_D, _D]
     L.mbx_polar_iterations.argtypes = [C.c_void_p]
+    L.mbx_polar_inner_sweeps.argtypes = [C.c_void_p]
+    L.mbx_polar_inner_sweeps.restype = C.c_long
     L.mbx_msite_redistribute.argtypes = [C.c_int, C.c_double, _D, _D, _D]
     L.mbx_disp_list_builds.argtypes = [C.c_void_p]
     L.mbx_disp_list_builds.restype = C.c_long
@@ -301,7 +303,7 @@ class Context:
         return dict(eng=eng.value, vir=vir.value, stress=stress, forces=f.T.copy(), atomic_energy=ae, jpot=jpot)
 
     def polar(self, sites, cell, imcon, nw, chge, dp, polr, polr2, prm, dip0=None, vel=None, atomic_energy=True,
-              check=True):
+              check=True, precision=FP64):
         """TTM4-F electrostatics (mbx_polar_forces, host arrays) on 4*nw sites; returns a
         dict shaped like the oracle's."""
         n = 4 * nw
@@ -313,7 +315,7 @@ class Context:
         jpot = np.zeros(3)
         jkin = np.zeros(3)
         v = [_f64(vel[:3 * nw, k]) for k in range(3)] if vel is not None else [None] * 3
-        rc = self.lib.mbx_polar_forces(self.h, _p(_f64(prm)), imcon, _p(_f64(cell)), nw, _p(x), _p(y), _p(z),
+        rc = self.lib.mbx_polar_forces(self.h, precision, _p(_f64(prm)), imcon, _p(_f64(cell)), nw, _p(x), _p(y), _p(z),
                                        _p(_f64(chge)), _p(_f64(dp)), _p(_f64(polr)), _p(_f64(polr2)), _p(dip[0]),
                                        _p(dip[1]), _p(dip[2]), _p(f[0]), _p(f[1]), _p(f[2]), _p(out), _p(ae),
                                        _p(v[0]), _p(v[1]), _p(v[2]), _p(jpot), _p(jkin))
@@ -325,6 +327,9 @@ class Context:
 
     def polar_iterations(self):
         return int(self.lib.mbx_polar_iterations(self.h))
+
+    def polar_inner_sweeps(self):
+        return int(self.lib.mbx_polar_inner_sweeps(self.h))
 
     def disp_list_builds(self):
         return int(self.lib.mbx_disp_list_builds(self.h))

@@ -178,6 +178,11 @@ int mbx_msites_dms_device(mbx_context* ctx, int imcon, const double* cell, int n
  * iter (SOURCE/iter.f), coulomb_polar (SOURCE/coulomb_polar.f), ewald2p (SOURCE/ewald2p.f),
  * ewald3p (SOURCE/ewald3p.f), qdforce (SOURCE/qdforce.f90) -- and their HEAT_CURRENT terms.
  * Replaces that branch of `forces` for a water-only system; ewald4p has no pairs there.
+ *   precision MBX_FP64: the reference's SOR iteration (iter) in FP64.  MBX_MIXED: the same
+ *             fixed point by FP64 iterative refinement -- the FP64 residual of the dipole
+ *             equations, an FP32 SOR solve of the correction (FP32 dipole tensors and
+ *             exp(ik.r) table), repeated until (1 - sor_omega) * rms(residual) <= toler,
+ *             then the reference's FP64 SOR step; everything after the dipoles in FP64.
  *   prm[15]   {alpha, rcut, epsq, toler (e*Angstrom, the CONTROL `iter` value / 4.803239),
  *              sor_omega, athole, athole12, athole13, ascc, ascd, gamma, kmax1, kmax2,
  *              kmax3, maxit}
@@ -200,19 +205,21 @@ int mbx_msites_dms_device(mbx_context* ctx, int imcon, const double* cell, int n
  * Returns MBX_ERR_CONVERGE (results of the last iteration written) when the dipoles did
  * not reach toler within maxit iterations (the reference stops at 22581).
  */
-int mbx_polar_forces(mbx_context* ctx, const double* prm, int imcon, const double* cell, int nw, const double* xxx,
-                     const double* yyy, const double* zzz, const double* chge, const double* dqdr, const double* polr,
-                     const double* polr2, double* dipx, double* dipy, double* dipz, double* fxx, double* fyy,
-                     double* fzz, double* out16, double* atomic_energy, const double* vxx, const double* vyy,
-                     const double* vzz, double* jpot, double* jkin);
-int mbx_polar_forces_device(mbx_context* ctx, const double* prm, int imcon, const double* cell, int nw,
+int mbx_polar_forces(mbx_context* ctx, int precision, const double* prm, int imcon, const double* cell, int nw,
+                     const double* xxx, const double* yyy, const double* zzz, const double* chge, const double* dqdr,
+                     const double* polr, const double* polr2, double* dipx, double* dipy, double* dipz, double* fxx,
+                     double* fyy, double* fzz, double* out16, double* atomic_energy, const double* vxx,
+                     const double* vyy, const double* vzz, double* jpot, double* jkin);
+int mbx_polar_forces_device(mbx_context* ctx, int precision, const double* prm, int imcon, const double* cell, int nw,
                             const double* xxx, const double* yyy, const double* zzz, const double* chge,
                             const double* dqdr, const double* polr, const double* polr2, double* dipx, double* dipy,
                             double* dipz, double* fxx, double* fyy, double* fzz, double* out16,
                             double* atomic_energy, const double* vxx, const double* vyy, const double* vzz,
                             double* jpot, double* jkin);
-/* Dipole iterations of the last mbx_polar_forces call. */
+/* Dipole iterations of the last mbx_polar_forces call (MBX_MIXED: FP64 field evaluations),
+ * and the FP32 correction sweeps of the last MBX_MIXED call. */
 int mbx_polar_iterations(const mbx_context* ctx);
+long mbx_polar_inner_sweeps(const mbx_context* ctx);
 /* M-site force redistribution of the reference's MD step (SOURCE/dlpoly_cmd.f:2585-2601):
  * F_O += (1 - gamma) F_M, F_H1 += F_M gamma / 2, F_H2 += F_M gamma / 2 (standard layout,
  * host arrays of 4*nw sites; the M-site entries are left as they are). */

@@ -103,3 +103,26 @@ def test_msite_redistribute(mbx_ctx):
                                               f[2].ctypes.data_as(P)) == 0
     # the host compiler may contract f + w * m into one FMA (aarch64): 1 ulp
     np.testing.assert_allclose(f, want, rtol=1e-15, atol=1e-15)
+
+
+@pytest.mark.parametrize("which", ["small", "config0"])
+def test_polar_mixed_refinement(mbx_ctx, oracle_lib, which):
+    """MBX_MIXED solves the same dipole equations (FP32 corrections under FP64 refinement):
+    its results are those of the FP64 oracle within the dipole tolerance."""
+    if which == "small":
+        box = systems.box_for(32, seed=5)
+        prm = systems.polar_params(alpha=0.6, rcut=4.5, kmax=(8, 8, 8), toler_debye=1e-12)
+    else:
+        box = systems.config0()
+        prm = systems.polar_params(alpha=0.3, rcut=9.0, kmax=(8, 8, 8), toler_debye=1e-8)
+    sites, q, dp, polr, polr2, prm = _case(oracle_lib, box, prm)
+    ref = oracle_lib.polar(sites, box.cell, box.imcon, box.nw, q, dp, polr, polr2, prm, vel=box.vel)
+    got = mbx_ctx.polar(sites, box.cell, box.imcon, box.nw, q, dp, polr, polr2, prm, vel=box.vel,
+                        precision=capi.MIXED)
+    assert got["deltadip"] <= prm[3]
+    assert mbx_ctx.polar_inner_sweeps() > 0 and got["iterations"] < ref["iterations"]
+    assert abs(got["engcpe"] - ref["engcpe"]) <= 1e-8 * abs(ref["engcpe"])
+    f, fr = got["forces"], ref["forces"]
+    assert np.sqrt(np.mean((f - fr) ** 2)) <= 1e-6 * np.sqrt(np.mean(fr ** 2))
+    for key in ("jpot", "jkin"):
+        assert np.linalg.norm(got[key] - ref[key]) <= 1e-7 * np.linalg.norm(ref[key]), key
