@@ -190,11 +190,11 @@ struct PolarState {
     float* tens32 = nullptr;
     float2* eik32 = nullptr;
     float* kco32 = nullptr;
-    float4 *r32 = nullptr, *d32 = nullptr;
+    float4 *r32 = nullptr, *d32 = nullptr, *cg_x = nullptr, *cg_r = nullptr, *cg_q = nullptr;
     float* e32 = nullptr;
     int cap32 = 0, n32 = 0, k32 = 0;
     size_t eik32_cap = 0;
-    long inner_sweeps = 0;
+    long inner_sweeps = 0;                 // FP32 conjugate-gradient iterations of the last call
     double* kpart = nullptr;               // per-chunk partial sums of the k-space gathers
     size_t part_cap = 0;
     int nsm = 152;                         // SMs of the device (grid sizing)

@@ -709,8 +709,9 @@ __global__ void __launch_bounds__(kThreads) k_pol_iter(PolArgs a, double4* __res
 // --- mixed precision: FP32 correction solves under FP64 refinement -----------------------
 struct MixArgs {
     float4* r32;      // FP64 residual, rounded (polarizable sites; 0 elsewhere)
-    float4* d32;      // correction dipoles
-    float* e32;       // FP32 field of the correction: real space (3 blocks of n), then k space (3 blocks)
+    float4* d32;      // vector the FP32 field is evaluated for (the CG direction)
+    float* e32;       // FP32 field of d32: real space (3 blocks of n), then k space (3 blocks)
+    float4 *x, *rho, *q;   // CG: solution, residual, A d32
 };
 
 // FP64 residual of the dipole equations at the current dipoles: r = polr2 E / r4pie0 - mu
@@ -859,37 +860,80 @@ __global__ void __launch_bounds__(kThreads) k_pol_kfield32_sum(KArgs k, PolArgs 
     for (int c = 0; c < 3; ++c) m.e32[(3 + c) * (size_t)k.n + j] = (pol ? sc * ev[c] : 0.f) + dum * dd[c];
 }
 
-// One SOR sweep of the correction: d <- omega d + (1 - omega)(r + polr2 E(d) / r4pie0);
-// sums |change|^2 into acc[31] (count in acc[32]).
-__global__ void __launch_bounds__(kThreads) k_pol_inner(PolArgs a, MixArgs m, int nk) {
+// Conjugate gradients for the correction: A x = b with A = r4pie0 / polr2 - T (T the
+// dipole field operator: real-space tensors, k-space sum, self term; symmetric) and
+// b = r4pie0 / polr2 * r, preconditioned by the diagonal r4pie0 / polr2.  Scalars live in
+// acc: 33 rho.z, 34 d.Ad, 35 new rho.z, 36 |z|^2, 37 count.
+__global__ void __launch_bounds__(kThreads) k_pcg_init(PolArgs a, MixArgs m) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    double v[2] = {0, 0};
-    if (i < a.n && a.polr2[i] > a.toler) {
-        const float om = (float)a.omega, fc = 1.f - om;
-        const float p = (float)(a.polr2[i] / kR4pie0);
+    double v[1] = {0};
+    if (i < a.n) {
         const float4 r = m.r32[i];
-        float4 d = m.d32[i];
-        const float rv[3] = {r.x, r.y, r.z};
-        float dv[3] = {d.x, d.y, d.z};
-        float ch = 0.f;
-        for (int c = 0; c < 3; ++c) {
-            const float f = m.e32[c * (size_t)a.n + i] + (nk ? m.e32[(3 + c) * (size_t)a.n + i] : 0.f);
-            const float nv = om * dv[c] + fc * (rv[c] + p * f);
-            ch += (nv - dv[c]) * (nv - dv[c]);
-            dv[c] = nv;
-        }
-        m.d32[i] = make_float4(dv[0], dv[1], dv[2], 0.f);
-        v[0] = ch;
-        v[1] = 1.0;
+        const float w = a.polr2[i] > a.toler ? (float)(kR4pie0 / a.polr2[i]) : 0.f;
+        m.x[i] = make_float4(0, 0, 0, 0);
+        m.rho[i] = make_float4(w * r.x, w * r.y, w * r.z, 0.f);
+        m.d32[i] = r;   // z = M^-1 rho = r
+        v[0] = (double)w * ((double)r.x * r.x + (double)r.y * r.y + (double)r.z * r.z);
     }
-    block_sum_atomic<2>(v, a.acc + 31);
+    block_sum_atomic<1>(v, a.acc + 33);
+}
+
+__global__ void __launch_bounds__(kThreads) k_pcg_ad(PolArgs a, MixArgs m, int nk) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double v[1] = {0};
+    if (i < a.n) {
+        float4 q = make_float4(0, 0, 0, 0);
+        if (a.polr2[i] > a.toler) {
+            const float w = (float)(kR4pie0 / a.polr2[i]);
+            const float4 d = m.d32[i];
+            const float dv[3] = {d.x, d.y, d.z};
+            float qv[3];
+            for (int c = 0; c < 3; ++c)
+                qv[c] = w * dv[c] - (m.e32[c * (size_t)a.n + i] + (nk ? m.e32[(3 + c) * (size_t)a.n + i] : 0.f));
+            q = make_float4(qv[0], qv[1], qv[2], 0.f);
+            v[0] = (double)dv[0] * qv[0] + (double)dv[1] * qv[1] + (double)dv[2] * qv[2];
+        }
+        m.q[i] = q;
+    }
+    block_sum_atomic<1>(v, a.acc + 34);
+}
+
+__global__ void __launch_bounds__(kThreads) k_pcg_step(PolArgs a, MixArgs m) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double v[3] = {0, 0, 0};
+    const double pq = a.acc[34];
+    const float g = pq != 0.0 ? (float)(a.acc[33] / pq) : 0.f;
+    if (i < a.n && a.polr2[i] > a.toler) {
+        const float w = (float)(a.polr2[i] / kR4pie0);
+        const float4 d = m.d32[i], q = m.q[i];
+        float4 x = m.x[i], r = m.rho[i];
+        x.x += g * d.x; x.y += g * d.y; x.z += g * d.z;
+        r.x -= g * q.x; r.y -= g * q.y; r.z -= g * q.z;
+        m.x[i] = x;
+        m.rho[i] = r;
+        const double z[3] = {(double)w * r.x, (double)w * r.y, (double)w * r.z};
+        v[0] = z[0] * r.x + z[1] * r.y + z[2] * r.z;
+        v[1] = z[0] * z[0] + z[1] * z[1] + z[2] * z[2];
+        v[2] = 1.0;
+    }
+    block_sum_atomic<3>(v, a.acc + 35);
+}
+
+__global__ void __launch_bounds__(kThreads) k_pcg_dir(PolArgs a, MixArgs m) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n || !(a.polr2[i] > a.toler)) return;
+    const double rz = a.acc[33];
+    const float b = rz != 0.0 ? (float)(a.acc[35] / rz) : 0.f;
+    const float w = (float)(a.polr2[i] / kR4pie0);
+    const float4 r = m.rho[i], d = m.d32[i];
+    m.d32[i] = make_float4(w * r.x + b * d.x, w * r.y + b * d.y, w * r.z + b * d.z, 0.f);
 }
 
 // mu += d in FP64; refreshes the masked dipoles.
 __global__ void k_pol_apply(PolArgs a, MixArgs m, double4* __restrict__ md) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n || !(a.polr2[i] > a.toler)) return;
-    const float4 d = m.d32[i];
+    const float4 d = m.x[i];
     a.mx[i] += (double)d.x;
     a.my[i] += (double)d.y;
     a.mz[i] += (double)d.z;
@@ -1325,7 +1369,7 @@ inline unsigned blocks(long n, int t) { return (unsigned)((n + t - 1) / t); }
 // --- host -------------------------------------------------------------------------------
 void PolarState::release() {
     void* p[] = {ercp, nn, nbr, flag, xf, tens, intra, fld, vesp, ae, eik, kv, kx2, lmn, sf, kterm, acc, kco, fac, md, vh,
-                 tens32, r32, d32, e32, kco32, eik32, kpart};
+                 tens32, r32, d32, e32, kco32, eik32, kpart, cg_x, cg_r, cg_q};
     for (void* q : p)
         if (q) cudaFree(q);
     if (acc_h) cudaFreeHost(acc_h);
@@ -1337,7 +1381,7 @@ void PolarState::release() {
     md = nullptr;
     fac_cap = 0;
     tens32 = e32 = kco32 = nullptr;
-    r32 = d32 = nullptr;
+    r32 = d32 = cg_x = cg_r = cg_q = nullptr;
     eik32 = nullptr;
     cap32 = n32 = k32 = 0;
     eik32_cap = 0;
@@ -1395,16 +1439,19 @@ cudaError_t PolarState::reserve_part(size_t nd) {
 cudaError_t PolarState::reserve_mixed(int n, int K) {
     cudaError_t e;
     if (!tens32 || cap32 != cap || n > n32) {
-        void* p[] = {tens32, r32, d32, e32};
+        void* p[] = {tens32, r32, d32, e32, cg_x, cg_r, cg_q};
         for (void* q : p)
             if (q) cudaFree(q);
         tens32 = e32 = nullptr;
-        r32 = d32 = nullptr;
+        r32 = d32 = cg_x = cg_r = cg_q = nullptr;
         const size_t m = (size_t)std::max(n, 1);
         if ((e = cudaMalloc(&tens32, 6 * m * cap * sizeof(float)))) return e;
         if ((e = cudaMalloc(&r32, m * sizeof(float4)))) return e;
         if ((e = cudaMalloc(&d32, m * sizeof(float4)))) return e;
         if ((e = cudaMalloc(&e32, 6 * m * sizeof(float)))) return e;
+        if ((e = cudaMalloc(&cg_x, m * sizeof(float4)))) return e;
+        if ((e = cudaMalloc(&cg_r, m * sizeof(float4)))) return e;
+        if ((e = cudaMalloc(&cg_q, m * sizeof(float4)))) return e;
         cap32 = cap;
         n32 = n;
     }
@@ -1723,11 +1770,14 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
         }
     } else {
         // FP64 refinement: the residual of the FP64 fields decides; the correction is solved
-        // with FP32 fields; the last step is the FP64 SOR update of the reference.
+        // by FP32 conjugate gradients; the last step is the FP64 SOR update of the reference.
         MixArgs m;
         m.r32 = r32;
         m.d32 = d32;
         m.e32 = e32;
+        m.x = cg_x;
+        m.rho = cg_r;
+        m.q = cg_q;
         const double fac = 1.0 - prm[4];
         for (int it = 1;; ++it) {
             fields64(it == 1);
@@ -1743,23 +1793,32 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
                 converged = deltadip <= prm[3];
                 break;
             }
+            // |z| (the preconditioned residual of the correction, a dipole) down to
+            // 1e-6 of the FP64 residual or well below toler
             const double target = std::max(1e-6 * rms, 0.05 * prm[3]);
-            for (int sweep = 0; sweep < 200; ++sweep) {
+            if ((e = cudaMemsetAsync(acc + 33, 0, 5 * sizeof(double), s))) return e;
+            k_pcg_init<<<blocks(n, kThreads), kThreads, 0, s>>>(a, m);
+            ++launches;
+            for (int sweep = 0; sweep < 100; ++sweep) {
                 k_pol_dd32<<<blocks(32L * n, kThreads), kThreads, 0, s>>>(a, m);
                 if (K) {
                     k_pol_sfd32<<<K, kSfThreads, 0, s>>>(k, m);
                     k_pol_kfield32<<<dim3(sblk2, nc2), kThreads, 0, s>>>(k, kc2, (float*)kpart);
                     k_pol_kfield32_sum<<<sblk1, kThreads, 0, s>>>(k, a, m, nc2, (const float*)kpart);
-                    ++launches;
+                    launches += 3;
                 }
-                if ((e = cudaMemsetAsync(acc + 31, 0, 2 * sizeof(double), s))) return e;
-                k_pol_inner<<<blocks(n, kThreads), kThreads, 0, s>>>(a, m, K ? 1 : 0);
-                launches += K ? 4 : 2;
+                k_pcg_ad<<<blocks(n, kThreads), kThreads, 0, s>>>(a, m, K ? 1 : 0);
+                k_pcg_step<<<blocks(n, kThreads), kThreads, 0, s>>>(a, m);
+                k_pcg_dir<<<blocks(n, kThreads), kThreads, 0, s>>>(a, m);
+                launches += 4;
                 ++inner_sweeps;
-                if ((e = cudaMemcpyAsync(acc_h + 31, acc + 31, 2 * sizeof(double), cudaMemcpyDeviceToHost, s))) return e;
+                if ((e = cudaMemcpyAsync(acc_h + 35, acc + 35, 3 * sizeof(double), cudaMemcpyDeviceToHost, s))) return e;
+                // next iteration: rho.z <- new rho.z; clear the sums
+                if ((e = cudaMemcpyAsync(acc + 33, acc + 35, sizeof(double), cudaMemcpyDeviceToDevice, s))) return e;
+                if ((e = cudaMemsetAsync(acc + 34, 0, 4 * sizeof(double), s))) return e;
                 if ((e = cudaStreamSynchronize(s))) return e;
-                const double ch = std::sqrt(acc_h[31] / (acc_h[32] > 0.0 ? acc_h[32] : 1.0));
-                if (ch <= target) break;
+                const double zr = std::sqrt(acc_h[36] / (acc_h[37] > 0.0 ? acc_h[37] : 1.0));
+                if (zr <= target) break;
             }
             k_pol_apply<<<blocks(n, kThreads), kThreads, 0, s>>>(a, m, md);
             ++launches;

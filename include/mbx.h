@@ -180,8 +180,8 @@ int mbx_msites_dms_device(mbx_context* ctx, int imcon, const double* cell, int n
  * Replaces that branch of `forces` for a water-only system; ewald4p has no pairs there.
  *   precision MBX_FP64: the reference's SOR iteration (iter) in FP64.  MBX_MIXED: the same
  *             fixed point by FP64 iterative refinement -- the FP64 residual of the dipole
- *             equations, an FP32 SOR solve of the correction (FP32 dipole tensors and
- *             exp(ik.r) table), repeated until (1 - sor_omega) * rms(residual) <= toler,
+ *             equations, an FP32 conjugate-gradient solve of the correction (FP32 dipole
+ *             tensors and exp(ik.r) table), repeated until (1 - sor_omega) * rms(residual) <= toler,
  *             then the reference's FP64 SOR step; everything after the dipoles in FP64.
  *   prm[15]   {alpha, rcut, epsq, toler (e*Angstrom, the CONTROL `iter` value / 4.803239),
  *              sor_omega, athole, athole12, athole13, ascc, ascd, gamma, kmax1, kmax2,
@@ -217,7 +217,7 @@ int mbx_polar_forces_device(mbx_context* ctx, int precision, const double* prm, 
                             double* atomic_energy, const double* vxx, const double* vyy, const double* vzz,
                             double* jpot, double* jkin);
 /* Dipole iterations of the last mbx_polar_forces call (MBX_MIXED: FP64 field evaluations),
- * and the FP32 correction sweeps of the last MBX_MIXED call. */
+ * and the FP32 conjugate-gradient iterations of the last MBX_MIXED call. */
 int mbx_polar_iterations(const mbx_context* ctx);
 long mbx_polar_inner_sweeps(const mbx_context* ctx);
 /* M-site force redistribution of the reference's MD step (SOURCE/dlpoly_cmd.f:2585-2601):
