@@ -35,12 +35,16 @@ for _p in (PKG, os.path.join(REPO, "oracle")):
         sys.path.insert(0, _p)
 
 METRIC = "MB-pol steps/s at 4096 H2O, mixed vs FP64 on 1 GB300; served p50/p99 ms"
-WORKLOAD = ("MB-pol 1B (Partridge-Schwenke coupling) + 2B + 3B forces, energy, virial, stress, per-atom energies and "
-            "heat current (jpot, jkin), 4096 H2O (12288 atoms + 4096 M sites), L=49.70 A")
+WORKLOAD = ("one MB-pol MD force evaluation of 4096 H2O (12288 atoms + 4096 M sites, L=49.70 A): M sites and DMS "
+            "charges, TTM4-F polarizable electrostatics (Ewald alpha 0.3/A, kmax 21, rcut 9 A, induced dipoles to "
+            "1e-8 D warm-started from the previous step), Tang-Toennies dispersion, 1B (Partridge-Schwenke "
+            "coupling), 2B and 3B polynomials, M-site force redistribution; forces, energies, virial, stress, "
+            "per-atom energies and heat current (jpot, jkin); positions advance by v dt (dt 0.2 fs) between steps")
 DATA = "synthetic: seeded 4096-H2O box, jittered 16^3 lattice, random orientations, 0.02 A noise, 298 K velocities"
-NOT_IN_STEP = ["TTM4-F polarizable electrostatics (induced dipoles, Ewald/SPME) and the DMS charge forces",
-               "TT dispersion (built, timed separately under 'dispersion': its parameters come from a FIELD file "
-               "the reference does not ship)", "FIELD-file bond terms of the monomer PES"]
+NOT_IN_STEP = ["FIELD-file bond terms of the monomer PES (none for MB-pol water)",
+               "dispersion parameters are synthetic Tang-Toennies values of MB-pol's form (the reference reads them "
+               "from a FIELD file it does not ship)"]
+DT_PS = 0.0002       # 0.2 fs in DL_POLY time units (ps); velocities are in A/ps
 
 
 def _peaks():
@@ -152,141 +156,288 @@ def max_over_ranks(value, world, device):
     return float(t.item())
 
 
+def cpu_polar_reference(kmax1, iterations=None, nw1=4096, threads=None):
+    """CPU time of the electrostatics of one 4096-H2O step, from the oracle restatement of
+    the reference's polar Ewald branch timed on the 256-water box and scaled by operation
+    counts: real-space work with the number of sites, k-space work with sites x k vectors;
+    fixed costs (lists, static fields, final forces) and per-iteration costs separately;
+    the serial oracle time divided by the host cores (the reference runs replicated-data
+    MPI over them)."""
+    import oracle
+    from mbx import systems
+    o = oracle.load()
+    T = threads or os.cpu_count() or 1
+    box = systems.config0()
+    sites, q, dp, _ = o.msites_dms(box)
+    polr, polr2 = systems.polarizabilities(box.nw)
+
+    def run(km, maxit):
+        prm = systems.polar_params(alpha=0.3, rcut=9.0, kmax=(km, km, km), toler_debye=1e-30, maxit=maxit)
+        t0 = time.perf_counter()
+        o.polar(sites, box.cell, box.imcon, box.nw, q, dp, polr, polr2, prm, vel=box.vel)
+        return time.perf_counter() - t0
+
+    t8 = {m: run(8, m) for m in (2, 6)}
+    t0_ = {m: run(0, m) for m in (2, 6)}
+    ir = max(0.0, (t0_[6] - t0_[2]) / 4)            # real-space seconds per iteration
+    ik = max(0.0, (t8[6] - t8[2]) / 4 - ir)         # k-space seconds per iteration
+    fr = max(0.0, t0_[2] - 2 * ir)
+    fk = max(0.0, t8[2] - 2 * (ir + ik) - fr)
+
+    def nk(km):   # ewald1p's half space of k vectors for a cubic cell
+        c = 0
+        for l in range(km + 1):
+            for m in range(-km, km + 1):
+                for n_ in range(-km, km + 1):
+                    if l == 0 and (m < 0 or (m == 0 and n_ < 1)):
+                        continue
+                    c += l * l + m * m + n_ * n_ <= (1.05 * km) ** 2
+        return c
+
+    if iterations is None:
+        # SOR iterations of an MD step: converge on the 256-water box, advance the positions
+        # by v dt, start from the converged dipoles
+        prm = systems.polar_params(alpha=0.3, rcut=9.0, kmax=(8, 8, 8), toler_debye=1e-8)
+        first = o.polar(sites, box.cell, box.imcon, box.nw, q, dp, polr, polr2, prm)
+        moved = systems.config0()
+        moved.xyz = box.xyz + DT_PS * box.vel
+        s2, q2, dp2, _ = o.msites_dms(moved)
+        iterations = o.polar(s2, box.cell, box.imcon, box.nw, q2, dp2, polr, polr2, prm,
+                             dip0=first["dipoles"])["iterations"]
+
+    rs = nw1 / box.nw
+    ks = rs * nk(kmax1) / nk(8)
+    serial = rs * fr + ks * fk + iterations * (rs * ir + ks * ik)
+    return serial / T, {"cores": T, "sample": "oracle electrostatics on the 256-water box (kmax 8 and 0, 2 and 6 "
+                        "iterations: %.2f/%.2f/%.2f/%.2f s serial) scaled to 4096 H2O by sites (x%.0f) and sites x k "
+                        "vectors (x%.0f) for %d iterations, divided by %d cores" %
+                        (t8[2], t8[6], t0_[2], t0_[6], rs, ks, iterations, T)}
+
+
 def run_ours(args, rank, world):
     import torch
+    import ctypes as C
     from mbx import capi, systems
 
     dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
     torch.cuda.set_device(dev)
     box = systems.config1(seed=20241 + rank)
-    n = box.natms
+    n, nw = box.natms, box.nw
     ctx = capi.Context(dev.index)
     stream = torch.cuda.current_stream(dev)
     ctx.set_stream(stream.cuda_stream)
+    km = systems.kmax_scaled(box.L)
+    PRM = systems.polar_params(alpha=0.3, rcut=9.0, kmax=(km, km, km), toler_debye=1e-8)
+    polr, polr2 = systems.polarizabilities(nw)
+    lt, mol = systems.water_types(box)
+    ctx.disp_setup(systems.DISP_PARAMS_SYNTHETIC, rcut=9.0, delr=1.0)
 
     f64 = dict(dtype=torch.float64, device=dev)
-    X = [torch.tensor(np.ascontiguousarray(box.xyz[:, k]), **f64) for k in range(3)]
-    V = [torch.tensor(np.ascontiguousarray(box.vel[:, k]), **f64) for k in range(3)]
+    X0 = torch.tensor(np.ascontiguousarray(box.xyz.T), **f64)      # (3, n) sites
+    X = X0.clone()
+    V = torch.tensor(np.ascontiguousarray(box.vel.T), **f64)
+    VA = V.clone()
+    VA[:, 3 * nw:] = 0.0                                          # M sites are placed, not moved
     M = torch.tensor(box.mass, **f64)
     F = torch.zeros((3, n), **f64)
     AE = torch.zeros(n, **f64)
+    Q = torch.zeros(n, **f64)
+    DIP = torch.zeros((3, n), **f64)
+    PR = torch.tensor(polr, **f64)
+    PR2 = torch.tensor(polr2, **f64)
+    LT = torch.tensor(lt, dtype=torch.int32, device=dev)
+    MOL = torch.tensor(mol, dtype=torch.int32, device=dev)
     LST = torch.tensor(box.listttm2(), dtype=torch.int32, device=dev)
     ANG = torch.tensor(box.listang().ravel(), dtype=torch.int32, device=dev)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)   # > 129 MB L2
+    D = C.POINTER(C.c_double)
+    sc = np.zeros(capi.NSTEPSCALARS)
 
     def step(precision):
         F.zero_()
         AE.zero_()
-        xp = [x.data_ptr() for x in X]
-        fp = [F[k].data_ptr() for k in range(3)]
-        vp = [v.data_ptr() for v in V]
-        one = ctx.ps_pes_device(box.imcon, box.cell, box.nw, ANG.data_ptr(), n, xp, fp, vp, AE.data_ptr())
-        sc = ctx.mbpol_forces_device(precision, box.imcon, box.cell, 3 * box.nw, LST.data_ptr(), n, xp, fp, vp,
-                                     M.data_ptr(), AE.data_ptr())
-        sc = sc.copy()
-        sc[12:15] += one[11:14]          # jpot of the 1-body term
-        return sc
+        rc = ctx.lib.mbx_water_step_device(
+            ctx.h, precision, box.imcon, box.cell.ctypes.data_as(D), nw, n, PRM.ctypes.data_as(D), PR.data_ptr(),
+            PR2.data_ptr(), LT.data_ptr(), MOL.data_ptr(), X[0].data_ptr(), X[1].data_ptr(), X[2].data_ptr(),
+            DIP[0].data_ptr(), DIP[1].data_ptr(), DIP[2].data_ptr(), F[0].data_ptr(), F[1].data_ptr(),
+            F[2].data_ptr(), V[0].data_ptr(), V[1].data_ptr(), V[2].data_ptr(), M.data_ptr(), AE.data_ptr(),
+            Q.data_ptr(), sc.ctypes.data_as(D))
+        if rc:
+            raise RuntimeError("mbx_water_step_device: %d %s" % (rc, ctx.lib.mbx_error(ctx.h).decode()))
+        return sc.copy()
 
-    def timed(precision, steps, warmup, profile=False):
-        ctx.set_profiling(profile)
+    def reset():
+        X.copy_(X0)
+        DIP.zero_()
+
+    def drift():
+        X.add_(VA, alpha=DT_PS)
+
+    def timed(precision, steps, warmup):
+        """warm-up MD steps from the reset state, then `steps` timed force evaluations, the
+        positions advancing by v dt and the dipoles carried over between them"""
+        reset()
         for _ in range(warmup):
             step(precision)
+            drift()
         ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
-        phase = np.zeros(4)
-        launches = 0
+        launches, iters, inner = 0, [], 0
         if world > 1:
             torch.distributed.barrier()
         torch.cuda.synchronize()
-        for s in range(steps):
+        for s_ in range(steps):
             flush.zero_()
-            ev[s][0].record(stream)
+            ev[s_][0].record(stream)
             step(precision)
-            ev[s][1].record(stream)
-            if profile:
-                ms, cnt = ctx.last_timings()
-                phase += ms
-            launches += ctx.last_timings()[1][2] + 1   # libmbx kernels of the step + the 1-body kernel
+            ev[s_][1].record(stream)
+            drift()
+            launches += ctx.last_timings()[1][2]
+            iters.append(ctx.polar_iterations())
+            inner += ctx.polar_inner_sweeps() if precision == capi.MIXED else 0
         torch.cuda.synchronize()
         tot = sum(a.elapsed_time(b) for a, b in ev) / 1e3
-        return max_over_ranks(tot, world, dev), phase / steps, launches
+        return max_over_ranks(tot, world, dev), launches, float(np.mean(iters)), inner / max(1, steps)
 
-    # numerics of the mixed path against the FP64 path on this machine
+    # numerics of the mixed step against the FP64 step on the same state (cold dipoles)
+    reset()
     sc64 = step(capi.FP64)
     F64 = F.cpu().numpy().copy()
+    reset()
     scm = step(capi.MIXED)
     Fm = F.cpu().numpy()
     err_f = float(np.sqrt(np.mean((Fm - F64) ** 2) / np.mean(F64 ** 2)))
-    j64 = sc64[12:15] + sc64[15:18]
-    jm = scm[12:15] + scm[15:18]
-    err_j = float(np.linalg.norm(jm - j64) / np.linalg.norm(j64))
-    e64 = sc64[0] + sc64[1]
-    err_e = float(abs(scm[0] + scm[1] - e64) / abs(e64))
+    nws = capi.NWATERSCALARS
+
+    def jtot(v):
+        j = v[12:15] + v[15:18] + v[capi.NSCALARS + 11:capi.NSCALARS + 14] + v[capi.NSCALARS + 25:capi.NSCALARS + 28]
+        return j + v[nws + 16:nws + 19] + v[nws + 19:nws + 22]
+
+    def etot(v):
+        return v[0] + v[1] + v[capi.NSCALARS] + v[capi.NSCALARS + 14] + v[nws]
+
+    err_j = float(np.linalg.norm(jtot(scm) - jtot(sc64)) / np.linalg.norm(jtot(sc64)))
+    err_e = float(abs(etot(scm) - etot(sc64)) / abs(etot(sc64)))
     _, (ndim, ntri, _, hard2, hard3) = ctx.last_timings()
 
     clocks = ClockSampler(dev.index)
     clocks.start()
-    t_mixed, phase_mixed, launches = timed(capi.MIXED, args.steps, args.warmup)
+    t_mixed, launches, it_mixed, inner_mixed = timed(capi.MIXED, args.steps, args.warmup)
     clk = clocks.stop()
-    _, phase_prof, _ = timed(capi.MIXED, max(3, args.steps // 4), 1, profile=True)
-    k64 = max(2, args.steps // 8)
-    t_fp64, _, _ = timed(capi.FP64, k64, 1)
-    _, phase64, _ = timed(capi.FP64, 2, 0, profile=True)
+    k64 = max(3, args.steps // 4)
+    t_fp64, _, it_fp64, _ = timed(capi.FP64, k64, min(args.warmup, 3))
 
-    # e2e through the host-array C ABI from pinned host buffers
+    # the MB-pol 1B + 2B + 3B terms alone (the polynomial path), device resident
+    def step_poly(precision):
+        F.zero_()
+        AE.zero_()
+        xp = [X[k].data_ptr() for k in range(3)]
+        fp = [F[k].data_ptr() for k in range(3)]
+        vp = [V[k].data_ptr() for k in range(3)]
+        ctx.ps_pes_device(box.imcon, box.cell, nw, ANG.data_ptr(), n, xp, fp, vp, AE.data_ptr())
+        ctx.mbpol_forces_device(precision, box.imcon, box.cell, 3 * nw, LST.data_ptr(), n, xp, fp, vp,
+                                M.data_ptr(), AE.data_ptr())
+
+    def timed_poly(precision, steps, warmup, profile=False):
+        reset()
+        ctx.set_profiling(profile)
+        for _ in range(warmup):
+            step_poly(precision)
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        phase = np.zeros(4)
+        torch.cuda.synchronize()
+        for s_ in range(steps):
+            flush.zero_()
+            ev[s_][0].record(stream)
+            step_poly(precision)
+            ev[s_][1].record(stream)
+            if profile:
+                phase += ctx.last_timings()[0]
+        torch.cuda.synchronize()
+        ctx.set_profiling(False)
+        return sum(a.elapsed_time(b) for a, b in ev) / 1e3, phase / steps
+
+    t_poly, _ = timed_poly(capi.MIXED, args.steps, args.warmup)
+    _, phase_prof = timed_poly(capi.MIXED, max(3, args.steps // 4), 1, profile=True)
+    t_poly64, phase64 = timed_poly(capi.FP64, max(2, args.steps // 8), 1, profile=True)
+    # the electrostatics alone on the same states
+    reset()
+    sites_h = np.ascontiguousarray(X.cpu().numpy().T)
+    hs, hq, hdp = ctx.msites_dms(box)
+    t_pol = {}
+    for prec in (capi.MIXED, capi.FP64):
+        for rep in range(2):
+            t0 = time.perf_counter()
+            ctx.polar(hs, box.cell, box.imcon, nw, hq, hdp, polr, polr2, PRM, vel=box.vel, precision=prec)
+            t_pol[prec] = time.perf_counter() - t0
+
+    # e2e: the host-array entry point mbx_water_step from pinned host buffers, the same MD steps
     def pinned(a):
         return torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
 
     hx = [pinned(box.xyz[:, k]) for k in range(3)]
+    hx0 = [t.clone() for t in hx]
     hv = [pinned(box.vel[:, k]) for k in range(3)]
+    hva = [t.clone() for t in hv]
+    for t in hva:
+        t[3 * nw:] = 0.0
     hm = pinned(box.mass)
-    hf = pinned(np.zeros((3, n)))
+    hpr, hpr2 = pinned(polr), pinned(polr2)
+    hdip = [pinned(np.zeros(n)) for _ in range(3)]
+    hf = [pinned(np.zeros(n)) for _ in range(3)]
     hae = pinned(np.zeros(n))
-    hl = pinned(box.listttm2().astype(np.int32))
-    import ctypes as C
-    D = C.POINTER(C.c_double)
+    hq2 = pinned(np.zeros(n))
+    hlt = pinned(lt.astype(np.int32))
+    hmol = pinned(mol.astype(np.int32))
+    hsc = np.zeros(capi.NSTEPSCALARS)
 
     def hp(t):
         return C.cast(C.c_void_p(t.data_ptr()), D)
 
-    hang = pinned(box.listang().ravel().astype(np.int32))
-    nsc = np.zeros(capi.NWATERSCALARS)
+    def hi(t):
+        return C.cast(C.c_void_p(t.data_ptr()), C.POINTER(C.c_int))
 
     def e2e_step():
-        # one host call: 1-body + 2B + 3B with the heat current; inputs copied in once,
-        # forces and per-atom energies copied out once
-        rc = ctx.lib.mbx_water_forces(ctx.h, capi.MIXED, box.imcon, box.cell.ctypes.data_as(D), 3 * box.nw,
-                                      C.cast(C.c_void_p(hl.data_ptr()), C.POINTER(C.c_int)), box.nw,
-                                      C.cast(C.c_void_p(hang.data_ptr()), C.POINTER(C.c_int)), None, None, n,
-                                      hp(hx[0]), hp(hx[1]), hp(hx[2]), hp(hf[0]), hp(hf[1]), hp(hf[2]), hp(hv[0]),
-                                      hp(hv[1]), hp(hv[2]), hp(hm), hp(hae), nsc.ctypes.data_as(D))
+        rc = ctx.lib.mbx_water_step(ctx.h, capi.MIXED, box.imcon, box.cell.ctypes.data_as(D), nw, n,
+                                    PRM.ctypes.data_as(D), hp(hpr), hp(hpr2), hi(hlt), hi(hmol), hp(hx[0]), hp(hx[1]),
+                                    hp(hx[2]), hp(hdip[0]), hp(hdip[1]), hp(hdip[2]), hp(hf[0]), hp(hf[1]),
+                                    hp(hf[2]), hp(hv[0]), hp(hv[1]), hp(hv[2]), hp(hm), hp(hae), hp(hq2),
+                                    hsc.ctypes.data_as(D))
         if rc:
-            raise RuntimeError("mbx_water_forces failed: %d" % rc)
+            raise RuntimeError("mbx_water_step failed: %d" % rc)
 
-    ctx.set_profiling(False)
+    def e2e_drift():
+        for k in range(3):
+            hx[k].add_(hva[k], alpha=DT_PS)
+
+    for k in range(3):
+        hx[k].copy_(hx0[k])
+        hdip[k].zero_()
     for _ in range(args.warmup):
         e2e_step()
+        e2e_drift()
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
-    t0 = time.perf_counter()
+    t_e2e = 0.0
     for _ in range(args.steps):
         flush.zero_()
         torch.cuda.synchronize()
+        t0 = time.perf_counter()
         e2e_step()
-    t_e2e = time.perf_counter() - t0
+        t_e2e += time.perf_counter() - t0
+        e2e_drift()
     t_e2e = max_over_ranks(t_e2e, world, dev)
-    # one host call per step: positions, velocities, masses and both atom lists in;
-    # forces, per-atom energies and the scalars out
-    h2d = 7 * n * 8 + 3 * box.nw * 4 + 3 * box.nw * 4
-    d2h = 4 * n * 8 + capi.NWATERSCALARS * 8
+    # per step: positions, Thole widths, polarizabilities, dipoles, velocities, masses (12 arrays
+    # of natms doubles) and the dispersion types and molecules in; forces, both per-atom
+    # energy parts, dipoles, positions and charges (12 arrays) out
+    h2d = 12 * n * 8 + 2 * n * 4
+    d2h = 12 * n * 8
     ctx.close()
 
     if rank != 0:
         return None
     peaks = _peaks()
     fl = poly_flops()
-    # the mixed step's dominant kernel: k_mbpol_23<double,float>, the persistent launch
-    # holding every dimer (FP64) and trimer (FP32); its time is the profiled "2b" phase
     t23 = phase_prof[1] / 1e3
     sm_max = peaks.get("sm_max_mhz", 2070.0)
     fp32_peak = 152 * 128 * 2 * sm_max * 1e6 / 1e12   # TFLOP/s at the maximum SM clock
@@ -298,24 +449,37 @@ def run_ours(args, rank, world):
     if os.path.exists(tfile):
         with open(tfile) as f:
             tj = json.load(f)
-        per = tj.get("k_mbpol_23_bytes_per_launch")
-        if per:
-            traffic = per
+        traffic = tj.get("k_mbpol_23_bytes_per_launch")
     value = world * args.steps / t_mixed
     out = {
         "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * t_mixed / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32 per cluster, f64 accumulation",
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64 with f32 polynomial clusters and f32 dipole corrections, f64 accumulation",
         "data": DATA,
         "config": {"workload": WORKLOAD, "precision": "mixed", "parallelism": "replicas" if world > 1 else "single",
                    "l2": "flushed between steps (256 MiB write)", "dimers": int(ndim), "trimers": int(ntri),
                    "mixed_fp64_handoff": {"dimers": int(hard2), "trimers": int(hard3)},
-                   "not_yet_in_step": NOT_IN_STEP},
-        "fp64": {"value": world * k64 / t_fp64, "unit": "steps/s", "ms_per_step": 1e3 * t_fp64 / k64,
-                 "phase_ms": {"lists": phase64[0], "2b": phase64[1], "3b": phase64[2], "jkin": phase64[3]}},
+                   "electrostatics": {"method": "Ewald (the reference's polar path; its SPME has no dipoles)",
+                                      "alpha": 0.3, "kmax": km, "rcut": 9.0, "toler_debye": 1e-8,
+                                      "fp64_field_evaluations_per_step_mixed": it_mixed,
+                                      "fp32_cg_iterations_per_step_mixed": inner_mixed,
+                                      "sor_iterations_per_step_fp64": it_fp64},
+                   "not_in_step": NOT_IN_STEP},
+        "fp64": {"value": world * k64 / t_fp64, "unit": "steps/s", "ms_per_step": 1e3 * t_fp64 / k64},
         "mixed_over_fp64": (args.steps / t_mixed) / (k64 / t_fp64),
-        "mixed_error_vs_fp64": {"force_rms_rel": err_f, "heat_current_rel": err_j, "energy_rel": err_e},
-        "phase_ms": {"lists": phase_prof[0], "2b+3b (fused kernel)": phase_prof[1], "jkin": phase_prof[3]},
+        "mixed_error_vs_fp64": {"force_rms_rel": err_f, "heat_current_rel": err_j, "energy_rel": err_e,
+                                "state": "the same configuration, dipoles from zero"},
+        "components_ms": {"electrostatics_cold_start_mixed": 1e3 * t_pol[capi.MIXED],
+                          "electrostatics_cold_start_fp64": 1e3 * t_pol[capi.FP64],
+                          "mbpol_1b_2b_3b_mixed": 1e3 * t_poly / args.steps,
+                          "mbpol_1b_2b_3b_fp64": 1e3 * t_poly64 / max(2, args.steps // 8)},
+        "mbpol_1b_2b_3b_only": {"value": args.steps / t_poly, "unit": "steps/s",
+                                "fp64_value": max(2, args.steps // 8) / t_poly64,
+                                "phase_ms": {"lists": phase_prof[0], "2b+3b (fused kernel)": phase_prof[1],
+                                             "jkin": phase_prof[3]},
+                                "fp64_phase_ms": {"lists": phase64[0], "2b": phase64[1], "3b": phase64[2],
+                                                  "jkin": phase64[3]}},
         "e2e": {"value": world * args.steps / t_e2e, "unit": "steps/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
         "roofline": {"kernel": "k_mbpol_23<double,float>", "bound": "fp64",
@@ -333,16 +497,16 @@ def run_ours(args, rank, world):
         out["batched"] = batched()
         out["dispersion"] = dispersion()
     if args.serve_requests > 0:
-        # the configured stream (2000 requests/s of 64-8192 H2O) offers several times
-        # what one GPU computes, so its queue grows through the run; the same sizes at
-        # 70 % of the served rate give the latency of a loaded but stable server
         out["serving"] = serve(n_requests=args.serve_requests)
         sustainable = 0.7 * out["serving"]["served_per_s"]
         out["serving_at_70pct_capacity"] = serve(n_requests=max(200, args.serve_requests // 2), rate=sustainable)
     if not args.no_cpu_baseline:
         sps, info = cpu_reference(box, target_core_s=40.0)
-        out["cpu_baseline"] = {"value": sps, "unit": "steps/s", "cores": info["cores"], "kind": "port",
-                               "sample": info["sample"]}
+        pol_s, pinfo = cpu_polar_reference(km)
+        step_s = 1.0 / sps + pol_s
+        out["cpu_baseline"] = {"value": 1.0 / step_s, "unit": "steps/s", "cores": info["cores"], "kind": "port",
+                               "sample": "MB-pol 2B/3B: " + info["sample"] + "; electrostatics: " + pinfo["sample"],
+                               "mbpol_seconds": 1.0 / sps, "electrostatics_seconds": pol_s}
     return out
 
 
@@ -588,10 +752,11 @@ def run_reference(args, rank, world):
     box = systems.config1()
     vals = []
     info = None
+    pol_s, pinfo = cpu_polar_reference(systems.kmax_scaled(box.L))
     for s in range(args.warmup + args.steps):
         sps, info = cpu_reference(box, target_core_s=args.ref_core_s)
         if s >= args.warmup:
-            vals.append(1.0 / sps)
+            vals.append(1.0 / sps + pol_s)
     step_s = float(np.mean(vals))
     v = 1.0 / step_s
     return {"metric": METRIC, "value": v, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
@@ -599,7 +764,8 @@ def run_reference(args, rank, world):
             "vs_baseline": None, "dtype": "f64", "data": DATA, "impl": "reference",
             "config": {"workload": WORKLOAD, "precision": "fp64", "parallelism": "host threads"},
             "cpu_baseline": {"value": v, "unit": "steps/s", "cores": info["cores"], "kind": "port",
-                             "sample": info["sample"]},
+                             "sample": "MB-pol 2B/3B: " + info["sample"] + "; electrostatics (once, %.1f s per "
+                             "step): " % pol_s + pinfo["sample"]},
             "e2e": {"value": v, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 

@@ -75,6 +75,10 @@ struct mbx_context {
     PolarState polar;                  // TTM4-F electrostatics
     double* polar_stage = nullptr;     // host entry point staging (24 * sites)
     size_t polar_stage_cap = 0;
+    double* step_stage = nullptr;      // mbx_water_step staging
+    size_t step_stage_cap = 0;
+    int* step_ints = nullptr;          // standard-layout water and angle lists
+    int step_nw = -1;
     std::vector<int> disp_types_h, disp_mol_h;   // inputs of the host entry point's list
     char err[512] = {0};
 };
@@ -469,7 +473,7 @@ extern "C" void mbx_destroy(mbx_context* ctx) {
     if (ctx->own_stream) cudaStreamSynchronize(ctx->own_stream);
     void* dev[] = {ctx->mono, ctx->list, ctx->atoms, ctx->ae_scratch, ctx->acc, ctx->totals, ctx->pairs, ctx->trip,
                    ctx->batch, ctx->hard2, ctx->hard3, ctx->hard_count, ctx->fuse_ctr, ctx->part2, ctx->done2,
-                   ctx->ints, ctx->polar_stage};
+                   ctx->ints, ctx->polar_stage, ctx->step_stage, ctx->step_ints};
     for (void* p : dev)
         if (p) cudaFree(p);
     if (ctx->totals_h) cudaFreeHost(ctx->totals_h);
@@ -946,6 +950,230 @@ extern "C" int mbx_polar_forces(mbx_context* ctx, int precision, const double* p
         dipz[i] = h[6 * n + i];
     }
     return rc;
+}
+
+namespace {
+// Standard-layout water and angle lists on the device (1-based atoms; angles H1, O, H2),
+// followed by room for per-atom types and molecules.
+int step_lists(mbx_context* ctx, int nw, int natms) {
+    if (ctx->step_nw == nw) return MBX_OK;
+    if (ctx->step_ints) cudaFree(ctx->step_ints);
+    ctx->step_ints = nullptr;
+    ctx->step_nw = -1;
+    const size_t na = 3 * (size_t)nw;
+    std::vector<int> h(na + 3 * (size_t)nw + 2 * (size_t)natms);
+    for (size_t t = 0; t < na; ++t) h[t] = (int)t + 1;
+    for (int w = 0; w < nw; ++w) {
+        h[na + 3 * w] = 3 * w + 2;
+        h[na + 3 * w + 1] = 3 * w + 1;
+        h[na + 3 * w + 2] = 3 * w + 3;
+    }
+    CK(cudaMalloc(&ctx->step_ints, h.size() * sizeof(int)));
+    CK(cudaMemcpy(ctx->step_ints, h.data(), h.size() * sizeof(int), cudaMemcpyHostToDevice));
+    ctx->step_nw = nw;
+    return MBX_OK;
+}
+
+// q, aep (per-site electrostatic energies) and dqdr device workspace of the step
+int step_stage(mbx_context* ctx, size_t n, int nw, size_t extra) {
+    const size_t need = 2 * n + 6 * (size_t)nw + extra + 1;
+    if (need <= ctx->step_stage_cap) return MBX_OK;
+    if (ctx->step_stage) cudaFree(ctx->step_stage);
+    ctx->step_stage = nullptr;
+    ctx->step_stage_cap = 0;
+    CK(cudaMalloc(&ctx->step_stage, need * sizeof(double)));
+    ctx->step_stage_cap = need;
+    return MBX_OK;
+}
+
+// The step on device arrays: M sites + DMS charges, electrostatics, 1-body, dispersion,
+// MB-pol, M-site redistribution.  dq, ddq, daep are workspace; dae must be valid.
+int water_step_core(mbx_context* ctx, int precision, int imcon, const double* cell, const Cell& cl, int nw,
+                    int natms, const double* prm, const double* dpr, const double* dpr2, const int* d_typ,
+                    const int* d_mol, double* dx, double* dy, double* dz, double* dmx, double* dmy, double* dmz,
+                    double* dfx, double* dfy, double* dfz, const double* dvx, const double* dvy, const double* dvz,
+                    const double* dm, double* dae, double* dq, double* ddq, double* daep, double* sc) {
+    cudaStream_t s = ctx->stream;
+    const int* d_lst = ctx->step_ints;
+    const int* d_ang = d_lst + 3 * (size_t)nw;
+    const bool heat = dvx && dvy && dvz && dm;
+    const double gamma = prm[10];
+    CK(cudaMemsetAsync(dq, 0, natms * sizeof(double), s));   // O carries no charge
+    CK(cudaMemsetAsync(daep, 0, natms * sizeof(double), s));
+    CK(launch_msites_dms(nw, d_lst, cl, dx, dy, dz, gamma, dq, ddq, s));
+    double* sp = sc + MBX_NWATERSCALARS;
+    double jp[3] = {0, 0, 0}, jk[3] = {0, 0, 0};
+    if (ctx->nsm > 0) ctx->polar.nsm = ctx->nsm;
+    // the electrostatic per-site energies stay apart: their jkin carries them with the
+    // M-site redistribution
+    CK(ctx->polar.run(precision, cl, prm, nw, dx, dy, dz, dq, ddq, dpr, dpr2, dmx, dmy, dmz, dfx, dfy, dfz, daep,
+                      heat ? dvx : nullptr, heat ? dvy : nullptr, heat ? dvz : nullptr, sp, jp, jk, s));
+    for (int c = 0; c < 3; ++c) {
+        sp[16 + c] = jp[c];
+        sp[19 + c] = jk[c];
+    }
+    const long polar_launches = ctx->polar.launches + 1;
+    int rc = mbx_ps_pes_forces_device(ctx, imcon, cell, nw, d_ang, natms, dx, dy, dz, dfx, dfy, dfz,
+                                      heat ? dvx : nullptr, heat ? dvy : nullptr, heat ? dvz : nullptr, dae,
+                                      sc + MBX_NSCALARS);
+    if (rc) return rc;
+    if (d_typ && d_mol) {
+        rc = mbx_disp_forces_device(ctx, imcon, cell, natms, d_typ, d_mol, dx, dy, dz, dfx, dfy, dfz,
+                                    heat ? dvx : nullptr, heat ? dvy : nullptr, heat ? dvz : nullptr, dae,
+                                    sc + MBX_NSCALARS + 14);
+        if (rc) return rc;
+    }
+    rc = run_mbpol(ctx, precision, cl, nw, d_lst, natms, dx, dy, dz, dfx, dfy, dfz, heat ? dvx : nullptr,
+                   heat ? dvy : nullptr, heat ? dvz : nullptr, heat ? dm : nullptr, dae, sc);
+    if (rc) return rc;
+    CK(launch_msite_redistribute(nw, gamma, dfx, dfy, dfz, s));
+    // device atomic energies: the electrostatic part joins the others for the caller
+    ctx->launches += polar_launches + 3;   // + 1-body + M sites + redistribution
+    return MBX_OK;
+}
+}  // namespace
+
+extern "C" int mbx_water_step_device(mbx_context* ctx, int precision, int imcon, const double* cell, int nw,
+                                     int natms, const double* polar_prm, const double* polr, const double* polr2,
+                                     const int* ltype, const int* molecule, double* xxx, double* yyy, double* zzz,
+                                     double* dipx, double* dipy, double* dipz, double* fxx, double* fyy,
+                                     double* fzz, const double* vxx, const double* vyy, const double* vzz,
+                                     const double* weight, double* atomic_energy, double* chge, double* scalars) {
+    if (!ctx) return MBX_ERR_ARG;
+    if ((precision != MBX_FP64 && precision != MBX_MIXED) || nw < 0 || natms != 4 * nw ||
+        !polar_prm_ok(polar_prm) || (nw && (!polr || !polr2 || !xxx || !yyy || !zzz || !dipx || !dipy || !dipz ||
+                                            !fxx || !fyy || !fzz || !chge)))
+        return fail(ctx, MBX_ERR_ARG, "mbx_water_step_device: bad argument");
+    const bool disp = ltype && molecule;
+    if (disp && !ctx->disp.vvv) return fail(ctx, MBX_ERR_ARG, "dispersion asked for before mbx_disp_setup");
+    Cell cl;
+    int rc = make_cell(ctx, imcon, cell, cl);
+    if (rc) return rc;
+    CK(cudaSetDevice(ctx->device));
+    double sc[MBX_NSTEPSCALARS];
+    std::memset(sc, 0, sizeof sc);
+    if (nw > 0) {
+        if ((rc = reserve_water(ctx, nw, natms)) || (rc = step_lists(ctx, nw, natms)) ||
+            (rc = step_stage(ctx, natms, nw, atomic_energy ? 0 : (size_t)natms)))
+            return rc;
+        const size_t n = (size_t)natms;
+        double* g = ctx->step_stage;
+        double *daep = g, *ddq = g + n, *dae = atomic_energy ? atomic_energy : g + n + 6 * (size_t)nw;
+        if (!atomic_energy) CK(cudaMemsetAsync(dae, 0, n * sizeof(double), ctx->stream));
+        ctx->launches = 0;
+        rc = water_step_core(ctx, precision, imcon, cell, cl, nw, natms, polar_prm, polr, polr2, ltype, molecule,
+                             xxx, yyy, zzz, dipx, dipy, dipz, fxx, fyy, fzz, vxx, vyy, vzz, weight, dae, chge, ddq,
+                             daep, sc);
+        if (rc) return rc;
+        if (atomic_energy) CK(launch_add(natms, daep, atomic_energy, ctx->stream));
+    }
+    if (scalars) std::memcpy(scalars, sc, sizeof sc);
+    if (nw > 0 && !ctx->polar.converged)
+        return fail(ctx, MBX_ERR_CONVERGE, "mbx_water_step: dipoles not converged after %d iterations",
+                    ctx->polar.iterations);
+    return MBX_OK;
+}
+
+extern "C" int mbx_water_step(mbx_context* ctx, int precision, int imcon, const double* cell, int nw, int natms,
+                              const double* polar_prm, const double* polr, const double* polr2, const int* ltype,
+                              const int* molecule, double* xxx, double* yyy, double* zzz, double* dipx,
+                              double* dipy, double* dipz, double* fxx, double* fyy, double* fzz, const double* vxx,
+                              const double* vyy, const double* vzz, const double* weight, double* atomic_energy,
+                              double* chge, double* scalars) {
+    if (!ctx) return MBX_ERR_ARG;
+    if ((precision != MBX_FP64 && precision != MBX_MIXED) || nw < 0 || natms != 4 * nw ||
+        !polar_prm_ok(polar_prm) || (nw && (!polr || !polr2 || !xxx || !yyy || !zzz || !dipx || !dipy || !dipz ||
+                                            !fxx || !fyy || !fzz)))
+        return fail(ctx, MBX_ERR_ARG, "mbx_water_step: bad argument");
+    const bool disp = ltype && molecule;
+    if (disp && !ctx->disp.vvv) return fail(ctx, MBX_ERR_ARG, "dispersion asked for before mbx_disp_setup");
+    Cell cl;
+    int rc = make_cell(ctx, imcon, cell, cl);
+    if (rc) return rc;
+    CK(cudaSetDevice(ctx->device));
+    double sc[MBX_NSTEPSCALARS];
+    std::memset(sc, 0, sizeof sc);
+    if (nw == 0) {
+        if (scalars) std::memcpy(scalars, sc, sizeof sc);
+        return MBX_OK;
+    }
+    const size_t n = (size_t)natms, na = 3 * (size_t)nw;
+    // x y z vx vy vz m f(3) ae in ctx->atoms; polr polr2 dip(3) q in the step workspace
+    if ((rc = reserve_water(ctx, nw, natms)) || (rc = step_lists(ctx, nw, natms)) ||
+        (rc = step_stage(ctx, n, nw, 6 * n)))
+        return rc;
+    cudaStream_t s = ctx->stream;
+    int* d_typ = ctx->step_ints + na + 3 * (size_t)nw;
+    int* d_mol = d_typ + n;
+    const bool heat = vxx && vyy && vzz && weight;
+    const size_t nb = n * sizeof(double);
+    double* d = ctx->atoms;
+    double *dx = d, *dy = d + n, *dz = d + 2 * n, *dvx = d + 3 * n, *dvy = d + 4 * n, *dvz = d + 5 * n, *dm = d + 6 * n;
+    double *dfx = d + 7 * n, *dfy = d + 8 * n, *dfz = d + 9 * n, *dae = d + 10 * n;
+    double* g = ctx->step_stage;
+    double *daep = g, *ddq = g + n, *dpr = g + n + 6 * (size_t)nw, *dpr2 = dpr + n, *dmx = dpr2 + n, *dmy = dmx + n,
+           *dmz = dmy + n, *dq = dmz + n;
+    CK(cudaMemcpyAsync(dx, xxx, nb, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(dy, yyy, nb, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(dz, zzz, nb, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(dpr, polr, nb, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(dpr2, polr2, nb, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(dmx, dipx, nb, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(dmy, dipy, nb, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(dmz, dipz, nb, cudaMemcpyHostToDevice, s));
+    if (heat) {
+        CK(cudaMemcpyAsync(dvx, vxx, nb, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(dvy, vyy, nb, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(dvz, vzz, nb, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(dm, weight, nb, cudaMemcpyHostToDevice, s));
+    }
+    if (disp) {
+        CK(cudaMemcpyAsync(d_typ, ltype, n * sizeof(int), cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(d_mol, molecule, n * sizeof(int), cudaMemcpyHostToDevice, s));
+        if (ctx->disp_types_h.size() != n || !std::equal(ltype, ltype + n, ctx->disp_types_h.begin()) ||
+            !std::equal(molecule, molecule + n, ctx->disp_mol_h.begin())) {
+            ctx->disp.valid = false;
+            ctx->disp_types_h.assign(ltype, ltype + n);
+            ctx->disp_mol_h.assign(molecule, molecule + n);
+        }
+    }
+    CK(cudaMemsetAsync(dfx, 0, 4 * nb, s));   // forces and per-atom energies
+    ctx->launches = 0;
+    rc = water_step_core(ctx, precision, imcon, cell, cl, nw, natms, polar_prm, dpr, dpr2, disp ? d_typ : nullptr,
+                         disp ? d_mol : nullptr, dx, dy, dz, dmx, dmy, dmz, dfx, dfy, dfz, heat ? dvx : nullptr,
+                         heat ? dvy : nullptr, heat ? dvz : nullptr, heat ? dm : nullptr, dae, dq, ddq, daep, sc);
+    if (rc) return rc;
+    // forces, per-atom energies, dipoles, M-site positions, charges back through one staging area
+    double* h = host_stage(ctx, 12 * n + 1);
+    if (!h) return fail(ctx, MBX_ERR_CUDA, "pinned host staging allocation failed");
+    CK(cudaMemcpyAsync(h, dfx, 4 * nb, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(h + 4 * n, daep, nb, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(h + 5 * n, dmx, 3 * nb, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(h + 8 * n, dx, nb, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(h + 9 * n, dy, nb, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(h + 10 * n, dz, nb, cudaMemcpyDeviceToHost, s));
+    if (chge) CK(cudaMemcpyAsync(h + 11 * n, dq, nb, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    for (size_t i = 0; i < n; ++i) {
+        fxx[i] += h[i];
+        fyy[i] += h[n + i];
+        fzz[i] += h[2 * n + i];
+        if (atomic_energy) atomic_energy[i] += h[3 * n + i] + h[4 * n + i];
+        dipx[i] = h[5 * n + i];
+        dipy[i] = h[6 * n + i];
+        dipz[i] = h[7 * n + i];
+        if (chge) chge[i] = h[11 * n + i];
+    }
+    for (size_t i = na; i < n; ++i) {
+        xxx[i] = h[8 * n + i];
+        yyy[i] = h[9 * n + i];
+        zzz[i] = h[10 * n + i];
+    }
+    if (scalars) std::memcpy(scalars, sc, sizeof sc);
+    if (!ctx->polar.converged)
+        return fail(ctx, MBX_ERR_CONVERGE, "mbx_water_step: dipoles not converged after %d iterations",
+                    ctx->polar.iterations);
+    return MBX_OK;
 }
 
 extern "C" int mbx_polar_iterations(const mbx_context* ctx) { return ctx ? ctx->polar.iterations : -1; }

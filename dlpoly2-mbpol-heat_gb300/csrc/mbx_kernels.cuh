@@ -228,6 +228,11 @@ struct PolarState {
                     const double* vy, const double* vz, double* out16, double* jpot, double* jkin, cudaStream_t s);
 };
 
+// M-site force redistribution onto O, H1, H2 (standard layout, device arrays).
+cudaError_t launch_msite_redistribute(int nw, double gamma, double* fx, double* fy, double* fz, cudaStream_t s);
+// y += x on the device
+cudaError_t launch_add(int n, const double* x, double* y, cudaStream_t s);
+
 // lrcorrect for vdw type 12 (host): elrc and virlrc for numtyp[t] atoms of type t + 1.
 void disp_lrc(int ntypes, const double* prm, const int* numtyp, double rcut, double volm, double* elrc,
               double* virlrc);

@@ -1366,7 +1366,38 @@ inline unsigned blocks(long n, int t) { return (unsigned)((n + t - 1) / t); }
 
 }  // namespace
 
+// M-site force redistribution (SOURCE/dlpoly_cmd.f:2585-2601), standard layout.
+__global__ void k_msite_redistribute(int nw, double gamma, double* __restrict__ fx, double* __restrict__ fy,
+                                     double* __restrict__ fz) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nw) return;
+    const int m = 3 * nw + i, o = 3 * i;
+    double* f[3] = {fx, fy, fz};
+    for (int c = 0; c < 3; ++c) {
+        f[c][o] = f[c][o] + (1.0 - gamma) * f[c][m];
+        f[c][o + 1] = f[c][o + 1] + f[c][m] * gamma / 2.0;
+        f[c][o + 2] = f[c][o + 2] + f[c][m] * gamma / 2.0;
+    }
+}
+
+__global__ void k_add(int n, const double* __restrict__ x, double* __restrict__ y) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) y[i] += x[i];
+}
+
 // --- host -------------------------------------------------------------------------------
+cudaError_t launch_add(int n, const double* x, double* y, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    k_add<<<blocks(n, kThreads), kThreads, 0, s>>>(n, x, y);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_msite_redistribute(int nw, double gamma, double* fx, double* fy, double* fz, cudaStream_t s) {
+    if (nw <= 0) return cudaSuccess;
+    k_msite_redistribute<<<blocks(nw, kThreads), kThreads, 0, s>>>(nw, gamma, fx, fy, fz);
+    return cudaGetLastError();
+}
+
 void PolarState::release() {
     void* p[] = {ercp, nn, nbr, flag, xf, tens, intra, fld, vesp, ae, eik, kv, kx2, lmn, sf, kterm, acc, kco, fac, md, vh,
                  tens32, r32, d32, e32, kco32, eik32, kpart, cg_x, cg_r, cg_q};
@@ -1667,22 +1698,27 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
     bind(a);
 
     KArgs k;
+    // every buffer pointer of the k-space kernels; bound again whenever a reserve may have
+    // reallocated them (the list growth below)
+    auto bindk = [&](KArgs& b) {
+        b.kv = kv;
+        b.kx2 = kx2;
+        b.lmn = lmn;
+        b.fac = fac;
+        b.eik = eik;
+        b.eik32 = mixed ? eik32 : nullptr;
+        b.kco32 = kco32;
+        b.sf = sf;
+        b.kco = kco;
+        b.kterm = kterm;
+        b.md = md;
+        b.vh = vh;
+    };
     k.K = K;
     k.n = n;
     for (int c = 0; c < 3; ++c) k.kmax[c] = kmax[c];
-    k.kv = kv;
-    k.kx2 = kx2;
-    k.lmn = lmn;
-    k.fac = fac;
-    k.eik = eik;
-    k.eik32 = mixed ? eik32 : nullptr;
-    k.kco32 = kco32;
-    k.sf = sf;
-    k.kco = kco;
-    k.kterm = kterm;
-    k.md = md;
     k.q = q;
-    k.vh = vh;
+    bindk(k);
     for (int c = 0; c < 9; ++c) k.rc[c] = rc[c];
     k.scale = 4.0 * rvolm * kR4pie0 / epsq;
     k.ralph = ralph;
@@ -1712,8 +1748,7 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
         if (mixed && (e = reserve_mixed(n, K))) return e;
     }
     bind(a);
-    k.eik32 = mixed ? eik32 : nullptr;
-    k.kco32 = kco32;
+    bindk(k);
     k_pol_static<<<blocks(32L * n, kThreads), kThreads, 0, s>>>(a);
     k_pol_intra_static<<<blocks(nw, kThreads), kThreads, 0, s>>>(a);
     launches += 2;

@@ -21,6 +21,7 @@ ERR_CONVERGE = 5
 NSCALARS = 18
 NBOXSCALARS = NSCALARS + 14
 NWATERSCALARS = NSCALARS + 28
+NSTEPSCALARS = NWATERSCALARS + 22
 S_ENG2, S_ENG3, S_VIR, S_STRESS, S_JPOT, S_JKIN = 0, 1, 2, 3, 12, 15
 
 _D = C.POINTER(C.c_double)
@@ -95,6 +96,9 @@ def load(path=None):
     L.mbx_polar_inner_sweeps.argtypes = [C.c_void_p]
     L.mbx_polar_inner_sweeps.restype = C.c_long
     L.mbx_msite_redistribute.argtypes = [C.c_int, C.c_double, _D, _D, _D]
+    L.mbx_water_step.argtypes = [C.c_void_p, C.c_int, C.c_int, _D, C.c_int, C.c_int, _D, _D, _D, _I, _I] + [_D] * 16
+    L.mbx_water_step_device.argtypes = [C.c_void_p, C.c_int, C.c_int, _D, C.c_int, C.c_int, _D] + \
+        [C.c_void_p] * 19 + [_D]
     L.mbx_disp_list_builds.argtypes = [C.c_void_p]
     L.mbx_disp_list_builds.restype = C.c_long
     L.mbx_set_graphs.argtypes = [C.c_void_p, C.c_int]
@@ -119,6 +123,11 @@ def load(path=None):
 
 def _p(a, t=_D):
     return None if a is None else a.ctypes.data_as(t)
+
+
+def systems_polarizabilities(nw):
+    from . import systems
+    return systems.polarizabilities(nw)
 
 
 def _f64(a):
@@ -324,6 +333,30 @@ class Context:
         return dict(status=rc, forces=f.T.copy(), engcpe=out[0], vircpe=out[1], stress=out[2:11].copy(),
                     iterations=int(out[11]), deltadip=out[12], eng_polar=out[13], eng_kspace=out[14],
                     eng_real=out[15], dipoles=dip.T.copy(), atomic_energy=ae, jpot=jpot, jkin=jkin)
+
+    def water_step(self, box, polar_prm, precision=MIXED, dip0=None, disp=None, heat=True, check=True):
+        """mbx_water_step on a WaterBox (standard layout): the whole force evaluation of one
+        MD step.  disp = (ltype, mol) after disp_setup, or None.  Returns a dict."""
+        n = box.natms
+        x, y, z = (_f64(box.xyz[:, k]).copy() for k in range(3))
+        dip = np.zeros((3, n)) if dip0 is None else np.ascontiguousarray(np.asarray(dip0, np.float64).T).copy()
+        f = np.zeros((3, n))
+        ae = np.zeros(n)
+        q = np.zeros(n)
+        sc = np.zeros(NSTEPSCALARS)
+        polr, polr2 = systems_polarizabilities(box.nw)
+        v = [_f64(box.vel[:, k]) for k in range(3)] if heat else [None] * 3
+        m = _f64(box.mass) if heat else None
+        lt, mo = (None, None) if disp is None else (np.ascontiguousarray(disp[0], np.int32),
+                                                    np.ascontiguousarray(disp[1], np.int32))
+        rc = self.lib.mbx_water_step(self.h, precision, box.imcon, _p(_f64(box.cell)), box.nw, n,
+                                     _p(_f64(polar_prm)), _p(polr), _p(polr2), _p(lt, _I), _p(mo, _I), _p(x), _p(y),
+                                     _p(z), _p(dip[0]), _p(dip[1]), _p(dip[2]), _p(f[0]), _p(f[1]), _p(f[2]),
+                                     _p(v[0]), _p(v[1]), _p(v[2]), _p(m), _p(ae), _p(q), _p(sc))
+        if check:
+            self._check(rc, "mbx_water_step")
+        return dict(status=rc, forces=f.T.copy(), atomic_energy=ae, chge=q, scalars=sc, dipoles=dip.T.copy(),
+                    sites=np.stack([x, y, z], 1))
 
     def polar_iterations(self):
         return int(self.lib.mbx_polar_iterations(self.h))

@@ -226,6 +226,45 @@ long mbx_polar_inner_sweeps(const mbx_context* ctx);
 int mbx_msite_redistribute(int nw, double gamma, double* fxx, double* fyy, double* fzz);
 
 /*
+ * The whole force evaluation of one MD step of MB-pol water, as the reference's MD loop
+ * runs it (SOURCE/dlpoly_cmd.f:2041-2057 M sites, qdetermine, forces with the polar Ewald
+ * branch and srfrce2, angfrc keya 9, mbpol_forces at :2504, the M-site redistribution at
+ * :2585-2606, and their HEAT_CURRENT terms), in one host call.  Standard layout only:
+ * natms = 4*nw, water w has O, H1, H2 at 3w..3w+2 and its M site at 3nw+w; the 1-body
+ * term runs over the (H1, O, H2) angle of every water.
+ *   precision   MBX_FP64 or MBX_MIXED (applies to the MB-pol polynomials and the dipole solve)
+ *   polar_prm, polr, polr2   as mbx_polar_forces (gamma is polar_prm[10])
+ *   ltype, molecule          per-atom dispersion types and molecules (1-based types, 0 none)
+ *                            as mbx_disp_forces, after mbx_disp_setup; NULL: no dispersion
+ *   xxx..       water atom positions in; the M-site positions are written (natms entries)
+ *   dip*        in: starting dipoles (the previous step's, or 0), out: converged dipoles
+ *   f*          ACCUMULATED; M-site forces redistributed onto O, H1, H2 (the M entries keep
+ *               their value, as the reference leaves them)
+ *   v*, weight  velocities and masses (NULL: no heat current)
+ *   atomic_energy  per-site energy of every term ACCUMULATED (not redistributed), or NULL
+ *   chge        site charges written, or NULL
+ *   scalars[MBX_NSTEPSCALARS]  written: the mbx_water_forces block (MB-pol, 1-body,
+ *               dispersion), then mbx_polar_forces' out16, then the electrostatic jpot[3]
+ *               and jkin[3].  The total heat current is the sum of the jpot and jkin
+ *               entries of all blocks.
+ * Returns MBX_ERR_CONVERGE (everything written) when the dipoles did not converge.
+ */
+#define MBX_NSTEPSCALARS (MBX_NWATERSCALARS + 22)
+int mbx_water_step(mbx_context* ctx, int precision, int imcon, const double* cell, int nw, int natms,
+                   const double* polar_prm, const double* polr, const double* polr2, const int* ltype,
+                   const int* molecule, double* xxx, double* yyy, double* zzz, double* dipx, double* dipy,
+                   double* dipz, double* fxx, double* fyy, double* fzz, const double* vxx, const double* vyy,
+                   const double* vzz, const double* weight, double* atomic_energy, double* chge, double* scalars);
+/* The same on device arrays (ltype/molecule, polr/polr2 and every per-site array device
+ * pointers; chge is required, it is the charge workspace); scalars is a host array. */
+int mbx_water_step_device(mbx_context* ctx, int precision, int imcon, const double* cell, int nw, int natms,
+                          const double* polar_prm, const double* polr, const double* polr2, const int* ltype,
+                          const int* molecule, double* xxx, double* yyy, double* zzz, double* dipx, double* dipy,
+                          double* dipz, double* fxx, double* fyy, double* fzz, const double* vxx, const double* vyy,
+                          const double* vzz, const double* weight, double* atomic_energy, double* chge,
+                          double* scalars);
+
+/*
  * Continuous-batching force server.  `slots` worker slots, each with its own context and
  * CUDA stream on `device`, evaluate independent water boxes concurrently; a FIFO queue
  * admits the next request as soon as a slot is free and its estimated device-memory

@@ -126,3 +126,43 @@ def test_polar_mixed_refinement(mbx_ctx, oracle_lib, which):
     assert np.sqrt(np.mean((f - fr) ** 2)) <= 1e-6 * np.sqrt(np.mean(fr ** 2))
     for key in ("jpot", "jkin"):
         assert np.linalg.norm(got[key] - ref[key]) <= 1e-7 * np.linalg.norm(ref[key]), key
+
+
+@pytest.mark.parametrize("precision", [capi.FP64, capi.MIXED])
+def test_water_step_is_the_sum_of_its_terms(oracle_lib, precision):
+    """mbx_water_step = M sites/DMS + electrostatics + 1-body + dispersion + MB-pol, then the
+    M-site redistribution, in one host call; the same results as the separate entry points."""
+    box = systems.config0()
+    prm = systems.polar_params(alpha=0.3, rcut=9.0, kmax=(8, 8, 8), toler_debye=1e-10)
+    lt, mol = systems.water_types(box)
+    polr, polr2 = systems.polarizabilities(box.nw)
+    ctx = capi.Context(0)
+    try:
+        ctx.disp_setup(systems.DISP_PARAMS_SYNTHETIC, rcut=9.0, delr=1.0)
+        step = ctx.water_step(box, prm, precision=precision, disp=(lt, mol))
+        parts = ctx.water_forces(box, precision=precision, dispersion=True)
+        sites, q, dp = ctx.msites_dms(box)
+        pol = ctx.polar(sites, box.cell, box.imcon, box.nw, q, dp, polr, polr2, prm, vel=box.vel,
+                        precision=precision)
+    finally:
+        ctx.close()
+    tol = 1e-11 if precision == capi.FP64 else 1e-8
+    nw = box.nw
+    f = parts["forces"] + pol["forces"]
+    g = prm[10]
+    fm = f[3 * nw:].copy()
+    f[0:3 * nw:3] += (1 - g) * fm
+    f[1:3 * nw:3] += 0.5 * g * fm
+    f[2:3 * nw:3] += 0.5 * g * fm
+    assert np.abs(step["forces"] - f).max() <= tol * np.abs(f).max()
+    ae = parts["atomic_energy"] + pol["atomic_energy"]
+    assert np.abs(step["atomic_energy"] - ae).max() <= tol * np.abs(ae).max()
+    np.testing.assert_allclose(step["sites"][3 * nw:], sites[3 * nw:], rtol=0, atol=1e-12)
+    np.testing.assert_allclose(step["chge"], q, rtol=0, atol=1e-14)
+    assert np.abs(step["dipoles"] - pol["dipoles"]).max() <= tol * np.abs(pol["dipoles"]).max()
+    sc = step["scalars"]
+    nws = capi.NWATERSCALARS
+    assert np.abs(sc[:nws] - parts["scalars"]).max() <= tol * np.abs(parts["scalars"]).max()
+    assert abs(sc[nws] - pol["engcpe"]) <= tol * abs(pol["engcpe"])
+    assert np.abs(sc[nws + 16:nws + 19] - pol["jpot"]).max() <= tol * np.abs(pol["jpot"]).max()
+    assert np.abs(sc[nws + 19:nws + 22] - pol["jkin"]).max() <= tol * np.abs(pol["jkin"]).max()
