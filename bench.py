@@ -677,7 +677,43 @@ def run_case(args):
     AE = torch.zeros(n, **f64)
     LST = torch.tensor(box.listttm2(), dtype=torch.int32, device="cuda")
     ANG = torch.tensor(box.listang().ravel(), dtype=torch.int32, device="cuda")
-    prec = capi.FP64 if args.case == "fp64" else capi.MIXED
+    prec = capi.FP64 if args.case in ("fp64", "step-fp64") else capi.MIXED
+    if args.case.startswith("step"):
+        # the whole MD force evaluation, positions advancing by v dt, dipoles carried over
+        import ctypes as C
+        km = systems.kmax_scaled(box.L)
+        prm = systems.polar_params(alpha=0.3, rcut=9.0, kmax=(km, km, km), toler_debye=1e-8)
+        polr, polr2 = systems.polarizabilities(box.nw)
+        lt, mol = systems.water_types(box)
+        ctx.disp_setup(systems.DISP_PARAMS_SYNTHETIC, rcut=9.0, delr=1.0)
+        X = torch.tensor(np.ascontiguousarray(box.xyz.T), **f64)
+        VV = torch.tensor(np.ascontiguousarray(box.vel.T), **f64)
+        VA = VV.clone()
+        VA[:, 3 * box.nw:] = 0.0
+        DIP = torch.zeros((3, n), **f64)
+        Q = torch.zeros(n, **f64)
+        PR, PR2 = torch.tensor(polr, **f64), torch.tensor(polr2, **f64)
+        LT = torch.tensor(lt, dtype=torch.int32, device="cuda")
+        MOL = torch.tensor(mol, dtype=torch.int32, device="cuda")
+        D = C.POINTER(C.c_double)
+        sc = np.zeros(capi.NSTEPSCALARS)
+        for _ in range(args.warmup + args.steps):
+            F.zero_()
+            AE.zero_()
+            torch.cuda.synchronize()
+            rc = ctx.lib.mbx_water_step_device(
+                ctx.h, prec, box.imcon, box.cell.ctypes.data_as(D), box.nw, n, prm.ctypes.data_as(D), PR.data_ptr(),
+                PR2.data_ptr(), LT.data_ptr(), MOL.data_ptr(), X[0].data_ptr(), X[1].data_ptr(), X[2].data_ptr(),
+                DIP[0].data_ptr(), DIP[1].data_ptr(), DIP[2].data_ptr(), F[0].data_ptr(), F[1].data_ptr(),
+                F[2].data_ptr(), VV[0].data_ptr(), VV[1].data_ptr(), VV[2].data_ptr(), M.data_ptr(), AE.data_ptr(),
+                Q.data_ptr(), sc.ctypes.data_as(D))
+            if rc:
+                raise RuntimeError("mbx_water_step_device: %d" % rc)
+            X.add_(VA, alpha=DT_PS)
+        torch.cuda.synchronize()
+        ctx.close()
+        print(json.dumps({"case": args.case, "steps": args.steps, "warmup": args.warmup}))
+        return
     if args.case == "mixed-separate":
         ctx.set_fused(False)      # the 2B and 3B kernels one after the other
     torch.cuda.synchronize()
@@ -780,7 +816,7 @@ def main():
                     help="requests of the Poisson serving run reported under 'serving' (0: skip)")
     ap.add_argument("--ref-core-s", type=float, default=10.0)
     ap.add_argument("--no-batched", action="store_true", help="skip the multi-box section ('batched')")
-    ap.add_argument("--case", choices=["mixed", "mixed-separate", "fp64"], default=None,
+    ap.add_argument("--case", choices=["mixed", "mixed-separate", "fp64", "step-mixed", "step-fp64"], default=None,
                     help="profiling case: only warmup + K device-resident steps of one precision")
     args = ap.parse_args()
     if args.case:

@@ -38,6 +38,10 @@ constexpr double kR4pie0 = 138935.4835;   // SOURCE/dl_params.inc:60
 constexpr double kSqrpi = 1.7724538509055159;
 constexpr double kPi = 3.141592653589793;
 constexpr int kSfThreads = 256;
+// Beyond a Thole / smearing argument of 40 every damping factor is below exp(-40) = 4e-18
+// of the undamped term it multiplies (and gammq's term likewise): the exponentials are not
+// evaluated there, which changes no result beyond 1e-16 relative.
+constexpr double kDampCut = 40.0;
 constexpr int kKTile = 64;
 
 // --- special functions (host and device) --------------------------------------------
@@ -272,14 +276,15 @@ __global__ void k_pol_static(PolArgs a) {
             const double bb = pow(pi * a.polr[j], 1.0 / 6.0);
             const double qj = a.q[j];
             double eki = kR4pie0 * qj * (bbb[1] + r3i);
-            const double dum1 = exp(-(a.ascd * pow4(rr / bb)));
+            const double arq = a.ascd * pow4(rr / bb);
+            const double dum1 = arq < kDampCut ? exp(-arq) : 0.0;
             eki = eki - kR4pie0 * qj * dum1 * r3i;
             e[0] += eki * d[0];
             e[1] += eki * d[1];
             e[2] += eki * d[2];
             if (poli && a.polr2[j] > 1e-6) {
                 const double arob4 = a.athole * pow4(rr / bb);
-                const double h1 = exp(-arob4);
+                const double h1 = arob4 < kDampCut ? exp(-arob4) : 0.0;
                 const double h2 = (1.0 + (4.0 / 3.0) * arob4) * h1;
                 const int ia[6] = {0, 0, 0, 1, 1, 2}, ib[6] = {0, 1, 2, 1, 2, 2};
 #pragma unroll
@@ -404,7 +409,7 @@ struct KArgs {
     double2* fac;          // per-site phase factors exp(2 pi i l s): x (l = 0..kmax1), y, z (-kmax..kmax)
     double2* eik;          // exp(ik.r) [k * n + j] = (cos, sin)
     float2* eik32;         // the same in FP32 (mixed precision), or null
-    float* kco32;          // 8 per k: kx, ky, kz, akk k.Ds, akk k.Dc of the FP32 correction
+    float* kco32;          // 16 per k: the CG gather's kx, ky, kz, akk k.Ds, akk k.Dc, then the FP32 force gather's
     double* sf;            // 8 per k: ckcs, ckss, Mc(3), Ms(3)
     double* kco;           // 16 per k: coefficients of the gathers
     double* kterm;         // 16 per k (final pass): engc, engdum, omg 11 22 33 12 13 23, jpot(3)
@@ -606,9 +611,15 @@ __global__ void __launch_bounds__(kSfThreads) k_pol_sf_final(KArgs k) {
             t[8 + aa] = f * (P[aa] - akv2 * kx[aa] * kp + y);
         }
     }
+    // coefficients of the force gather: k, akk summu1, akk summu2, akk ckcs, akk ckss,
+    // akk k.Mc, akk k.Ms
     double* c = k.kco + 16 * (size_t)kk;
-    c[0] = kx[0]; c[1] = kx[1]; c[2] = kx[2]; c[3] = akk;
-    c[4] = s1; c[5] = s2; c[6] = ckcs; c[7] = ckss; c[8] = skc; c[9] = sks;
+    c[0] = kx[0]; c[1] = kx[1]; c[2] = kx[2];
+    c[3] = akk * s1; c[4] = akk * s2; c[5] = akk * ckcs; c[6] = akk * ckss; c[7] = akk * skc; c[8] = akk * sks;
+    if (k.kco32) {
+        float* f = k.kco32 + 16 * (size_t)kk;
+        for (int q = 0; q < 9; ++q) f[q] = (float)c[q];
+    }
 }
 
 // k-space fields per site (iflag 0): the dipole field and, in the first pass, the static
@@ -800,7 +811,7 @@ __global__ void __launch_bounds__(kSfThreads) k_pol_sfd32(KArgs k, MixArgs m) {
         for (int i = 0; i < kSfThreads / 32; ++i)
             for (int q = 0; q < 6; ++q) t[q] += red[i][q];
         const double4 kv = k.kv[kk];
-        float* c = k.kco32 + 8 * (size_t)kk;
+        float* c = k.kco32 + 16 * (size_t)kk;
         c[0] = (float)kv.x; c[1] = (float)kv.y; c[2] = (float)kv.z;
         c[3] = (float)(kv.w * (kv.x * t[3] + kv.y * t[4] + kv.z * t[5]));
         c[4] = (float)(kv.w * (kv.x * t[0] + kv.y * t[1] + kv.z * t[2]));
@@ -817,7 +828,7 @@ __global__ void __launch_bounds__(kThreads) k_pol_kfield32(KArgs k, int kchunk, 
     for (int t0 = kb; t0 < ke; t0 += kKTile) {
         const int nt = min(kKTile, ke - t0);
         __syncthreads();
-        for (int u = threadIdx.x; u < nt * 8; u += blockDim.x) sh[u >> 3][u & 7] = k.kco32[8 * (size_t)(t0 + (u >> 3)) + (u & 7)];
+        for (int u = threadIdx.x; u < nt * 8; u += blockDim.x) sh[u >> 3][u & 7] = k.kco32[16 * (size_t)(t0 + (u >> 3)) + (u & 7)];
         __syncthreads();
         const float2* e = k.eik32 + (size_t)t0 * k.n;
         if (j1 < k.n) {
@@ -940,48 +951,86 @@ __global__ void k_pol_apply(PolArgs a, MixArgs m, double4* __restrict__ md) {
     if (a.polr2[i] > 1e-6) md[i] = make_double4(a.mx[i], a.my[i], a.mz[i], 0.0);
 }
 
-// Final k-space pass (ewald1p iflag 1): per site and chunk of k vectors, the force, the
-// two DMS potentials and the k-space charge energy (6 partial sums per site).
+// Final k-space pass (ewald1p iflag 1): per site and chunk of k vectors, the force and the
+// two DMS potentials (5 partial sums per site; the k-space charge energy of a site is its
+// charge times the first potential).  Two sites per thread.
+//   akk ssmu = q (c akk s2 - s akk s1) - (k.mu) (c akk s1 + s akk s2)
+template <typename R, typename V2>
+__device__ __forceinline__ void kforce_site(const R* r, V2 cs, R qj, const R* dv, bool pol, R* acc) {
+    const R c = cs.x, s = cs.y;
+    const R kap = pol ? dv[0] * r[0] + dv[1] * r[1] + dv[2] * r[2] : R(0);
+    const R t1 = c * r[4] - s * r[3], t2 = c * r[3] + s * r[4];
+    const R fv = qj * t1 - kap * t2;
+    acc[0] -= r[0] * fv;
+    acc[1] -= r[1] * fv;
+    acc[2] -= r[2] * fv;
+    acc[3] += c * r[5] + s * r[6];
+    acc[4] += s * r[7] - c * r[8];
+}
+
 __global__ void __launch_bounds__(kThreads) k_pol_kforce(KArgs k, PolArgs a, int kchunk, double* __restrict__ part) {
-    __shared__ double sh[kKTile][10];
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool in = j < k.n;
+    __shared__ double sh[kKTile][9];
+    const int j0 = blockIdx.x * 2 * blockDim.x + threadIdx.x, j1 = j0 + blockDim.x;
     const int kb = blockIdx.y * kchunk, ke = min(k.K, kb + kchunk);
-    const double qj = in ? a.q[j] : 0.0;
-    const bool pol = in && a.polr2[j] > 1e-6;
-    const double dv[3] = {in ? a.mx[j] : 0.0, in ? a.my[j] : 0.0, in ? a.mz[j] : 0.0};
-    double fk[3] = {0, 0, 0}, vk = 0, vdk = 0, aek = 0;
+    const bool in0 = j0 < k.n, in1 = j1 < k.n;
+    const double q0 = in0 ? a.q[j0] : 0.0, q1 = in1 ? a.q[j1] : 0.0;
+    const bool p0 = in0 && a.polr2[j0] > 1e-6, p1 = in1 && a.polr2[j1] > 1e-6;
+    const double d0[3] = {in0 ? a.mx[j0] : 0.0, in0 ? a.my[j0] : 0.0, in0 ? a.mz[j0] : 0.0};
+    const double d1[3] = {in1 ? a.mx[j1] : 0.0, in1 ? a.my[j1] : 0.0, in1 ? a.mz[j1] : 0.0};
+    double acc0[5] = {0, 0, 0, 0, 0}, acc1[5] = {0, 0, 0, 0, 0};
     for (int t0 = kb; t0 < ke; t0 += kKTile) {
         const int nt = min(kKTile, ke - t0);
         __syncthreads();
-        for (int u = threadIdx.x; u < nt * 10; u += blockDim.x)
-            sh[u / 10][u % 10] = k.kco[16 * (size_t)(t0 + u / 10) + u % 10];
+        for (int u = threadIdx.x; u < nt * 9; u += blockDim.x)
+            sh[u / 9][u % 9] = k.kco[16 * (size_t)(t0 + u / 9) + u % 9];
         __syncthreads();
-        if (!in) continue;
-        const double2* e = k.eik + (size_t)t0 * k.n + j;
+        const double2* e = k.eik + (size_t)t0 * k.n;
         for (int u = 0; u < nt; ++u, e += k.n) {
-            const double* r = sh[u];
-            const double2 cs = *e;
-            const double c = cs.x, s = cs.y;
-            const double akk = r[3];
-            const double djmuk = pol ? dv[0] * r[0] + dv[1] * r[1] + dv[2] * r[2] : 0.0;
-            const double ssmu = r[4] * (-s * qj - c * djmuk) + r[5] * (-s * djmuk + c * qj);
-            fk[0] -= r[0] * akk * ssmu;
-            fk[1] -= r[1] * akk * ssmu;
-            fk[2] -= r[2] * akk * ssmu;
-            vk += akk * (c * r[6] + s * r[7]);
-            vdk += akk * (s * r[8] - c * r[9]);
-            aek += akk * (qj * c * r[6] + qj * s * r[7]);
+            if (in0) kforce_site<double, double2>(sh[u], e[j0], q0, d0, p0, acc0);
+            if (in1) kforce_site<double, double2>(sh[u], e[j1], q1, d1, p1, acc1);
         }
     }
-    if (!in) return;
-    double* p = part + (size_t)blockIdx.y * 6 * k.n;
-    p[j] = fk[0];
-    p[k.n + j] = fk[1];
-    p[2 * (size_t)k.n + j] = fk[2];
-    p[3 * (size_t)k.n + j] = vk;
-    p[4 * (size_t)k.n + j] = vdk;
-    p[5 * (size_t)k.n + j] = aek;
+    double* p = part + (size_t)blockIdx.y * 5 * k.n;
+    for (int c = 0; c < 5; ++c) {
+        if (in0) p[c * (size_t)k.n + j0] = acc0[c];
+        if (in1) p[c * (size_t)k.n + j1] = acc1[c];
+    }
+}
+
+// The same in FP32 (mixed precision): FP32 phases and coefficients, each tile of kKTile k
+// vectors summed in FP32 and the tiles added in FP64.
+__global__ void __launch_bounds__(kThreads) k_pol_kforce32(KArgs k, PolArgs a, int kchunk, double* __restrict__ part) {
+    __shared__ float sh[kKTile][9];
+    const int j0 = blockIdx.x * 2 * blockDim.x + threadIdx.x, j1 = j0 + blockDim.x;
+    const int kb = blockIdx.y * kchunk, ke = min(k.K, kb + kchunk);
+    const bool in0 = j0 < k.n, in1 = j1 < k.n;
+    const float q0 = in0 ? (float)a.q[j0] : 0.f, q1 = in1 ? (float)a.q[j1] : 0.f;
+    const bool p0 = in0 && a.polr2[j0] > 1e-6, p1 = in1 && a.polr2[j1] > 1e-6;
+    const float d0[3] = {in0 ? (float)a.mx[j0] : 0.f, in0 ? (float)a.my[j0] : 0.f, in0 ? (float)a.mz[j0] : 0.f};
+    const float d1[3] = {in1 ? (float)a.mx[j1] : 0.f, in1 ? (float)a.my[j1] : 0.f, in1 ? (float)a.mz[j1] : 0.f};
+    double acc0[5] = {0, 0, 0, 0, 0}, acc1[5] = {0, 0, 0, 0, 0};
+    for (int t0 = kb; t0 < ke; t0 += kKTile) {
+        const int nt = min(kKTile, ke - t0);
+        __syncthreads();
+        for (int u = threadIdx.x; u < nt * 9; u += blockDim.x)
+            sh[u / 9][u % 9] = k.kco32[16 * (size_t)(t0 + u / 9) + u % 9];
+        __syncthreads();
+        float f0[5] = {0, 0, 0, 0, 0}, f1[5] = {0, 0, 0, 0, 0};
+        const float2* e = k.eik32 + (size_t)t0 * k.n;
+        for (int u = 0; u < nt; ++u, e += k.n) {
+            if (in0) kforce_site<float, float2>(sh[u], e[j0], q0, d0, p0, f0);
+            if (in1) kforce_site<float, float2>(sh[u], e[j1], q1, d1, p1, f1);
+        }
+        for (int c = 0; c < 5; ++c) {
+            acc0[c] += (double)f0[c];
+            acc1[c] += (double)f1[c];
+        }
+    }
+    double* p = part + (size_t)blockIdx.y * 5 * k.n;
+    for (int c = 0; c < 5; ++c) {
+        if (in0) p[c * (size_t)k.n + j0] = acc0[c];
+        if (in1) p[c * (size_t)k.n + j1] = acc1[c];
+    }
 }
 
 // Per site: the k-space sums of all chunks, the self terms and coulomb_polar.
@@ -992,8 +1041,9 @@ __global__ void __launch_bounds__(kThreads) k_pol_kforce_sum(KArgs k, PolArgs a,
     if (j < k.n) {
         double v[6] = {0, 0, 0, 0, 0, 0};
         for (int q = 0; q < nchunk; ++q)
-            for (int c = 0; c < 6; ++c) v[c] += part[((size_t)q * 6 + c) * k.n + j];
+            for (int c = 0; c < 5; ++c) v[c] += part[((size_t)q * 5 + c) * k.n + j];
         const double qj = a.q[j];
+        v[5] = qj * v[3];   // k-space charge energy of the site (update_energy_ew1p)
         const double dv[3] = {a.mx[j], a.my[j], a.mz[j]};
         a.fx[j] += k.scale * v[0];
         a.fy[j] += k.scale * v[1];
@@ -1052,14 +1102,15 @@ __global__ void __launch_bounds__(kThreads) k_pol_ewald2p(PolArgs a, double g34,
             const double bb = pow(a.polr[i] * a.polr[j], 1.0 / 6.0);
             {
                 const double arob4 = a.ascc * pow4(rrr / bb);
-                const double dum1 = exp(-arob4);
-                // beyond exp's range both terms vanish (the reference adds zeros there)
-                const double gq = arob4 < 700.0 ? gammq(0.75, arob4) : 0.0;
-                const double sm = (dum1 - pow(arob4, 0.25) * g34 * gq) / rrr * kR4pie0;
-                eng -= cicj * sm;
-                aei += -cicj * 0.5 * (dum1 - pow(arob4, 0.25) * g34 * gq) / rrr * kR4pie0;
-                espdum -= sm;
-                ffac = ffac - cicj * r3i * dum1 * kR4pie0;
+                if (arob4 < kDampCut) {
+                    const double dum1 = exp(-arob4);
+                    const double gq = gammq(0.75, arob4);
+                    const double sm = (dum1 - pow(arob4, 0.25) * g34 * gq) / rrr * kR4pie0;
+                    eng -= cicj * sm;
+                    aei += -cicj * 0.5 * (dum1 - pow(arob4, 0.25) * g34 * gq) / rrr * kR4pie0;
+                    espdum -= sm;
+                    ffac = ffac - cicj * r3i * dum1 * kR4pie0;
+                }
             }
             const double mj[3] = {a.mx[j], a.my[j], a.mz[j]};
             const double rdmui = mi[0] * d[0] + mi[1] * d[1] + mi[2] * d[2];
@@ -1073,7 +1124,7 @@ __global__ void __launch_bounds__(kThreads) k_pol_ewald2p(PolArgs a, double g34,
             double espdc = (bbb[1] + r3i) * kR4pie0;
             {
                 const double arob4 = a.ascd * pow4(rrr / bb);
-                const double dum1 = exp(-arob4);
+                const double dum1 = arob4 < kDampCut ? exp(-arob4) : 0.0;
                 const double dum2 = (1.0 + (4.0 / 3.0) * arob4) * dum1;
                 facmu = facmu - facmu0 * dum2;
                 dfi = dfi - facmui0 * dum1;
@@ -1092,7 +1143,7 @@ __global__ void __launch_bounds__(kThreads) k_pol_ewald2p(PolArgs a, double g34,
                 const double dfj1 = 3.0 * rdmui * r5i * kR4pie0;
                 const double bb4 = pow4(bb);
                 const double arob4 = a.athole * pow4(rrr / bb);
-                const double dum1 = exp(-arob4);
+                const double dum1 = arob4 < kDampCut ? exp(-arob4) : 0.0;
                 const double dum2 = (1.0 + (4.0 / 3.0) * arob4) * dum1;
                 const double dum3 = 4.0 * a.athole * (4.0 * arob4 - 1.0) * dum1 * rsqi / bb4;
                 const double dum4 = 4.0 * a.athole * dum1 * rrr / bb4;
@@ -1489,7 +1540,7 @@ cudaError_t PolarState::reserve_mixed(int n, int K) {
     if (K > k32) {
         if (kco32) cudaFree(kco32);
         kco32 = nullptr;
-        if ((e = cudaMalloc(&kco32, 8 * (size_t)std::max(K, 1) * sizeof(float)))) return e;
+        if ((e = cudaMalloc(&kco32, 16 * (size_t)std::max(K, 1) * sizeof(float)))) return e;
         k32 = K;
     }
     const size_t need = (size_t)K * n;
@@ -1707,7 +1758,7 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
         b.fac = fac;
         b.eik = eik;
         b.eik32 = mixed ? eik32 : nullptr;
-        b.kco32 = kco32;
+        b.kco32 = mixed ? kco32 : nullptr;
         b.sf = sf;
         b.kco = kco;
         b.kterm = kterm;
@@ -1829,8 +1880,8 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
                 break;
             }
             // |z| (the preconditioned residual of the correction, a dipole) down to
-            // 1e-6 of the FP64 residual or well below toler
-            const double target = std::max(1e-6 * rms, 0.05 * prm[3]);
+            // 1e-6 of the FP64 residual or 5x below toler
+            const double target = std::max(1e-6 * rms, 0.2 * prm[3]);
             if ((e = cudaMemsetAsync(acc + 33, 0, 5 * sizeof(double), s))) return e;
             k_pcg_init<<<blocks(n, kThreads), kThreads, 0, s>>>(a, m);
             ++launches;
@@ -1871,10 +1922,11 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
         ++launches;
     }
     if (K) {
-        k_pol_kforce<<<dim3(sblk1, nc1), kThreads, 0, s>>>(k, a, kc1, kpart);
+        if (mixed) k_pol_kforce32<<<dim3(sblk2, nc2), kThreads, 0, s>>>(k, a, kc2, kpart);
+        else k_pol_kforce<<<dim3(sblk2, nc2), kThreads, 0, s>>>(k, a, kc2, kpart);
         ++launches;
     }
-    k_pol_kforce_sum<<<sblk1, kThreads, 0, s>>>(k, a, nc1, kpart);
+    k_pol_kforce_sum<<<sblk1, kThreads, 0, s>>>(k, a, nc2, kpart);
     k_pol_ewald2p<<<blocks(32L * n, kThreads), kThreads, 0, s>>>(a, g34, heat);
     k_pol_ewald3p<<<blocks(nw, kThreads), kThreads, 0, s>>>(a, heat);
     k_pol_qdforce<<<blocks(nw, kThreads), kThreads, 0, s>>>(a, heat);

@@ -124,8 +124,10 @@ def test_polar_mixed_refinement(mbx_ctx, oracle_lib, which):
     assert abs(got["engcpe"] - ref["engcpe"]) <= 1e-8 * abs(ref["engcpe"])
     f, fr = got["forces"], ref["forces"]
     assert np.sqrt(np.mean((f - fr) ** 2)) <= 1e-6 * np.sqrt(np.mean(fr ** 2))
+    # the heat-current budget of the mixed path: 1e-6 relative (its k-space force and
+    # per-site energy gathers run in FP32 with FP64 tile sums)
     for key in ("jpot", "jkin"):
-        assert np.linalg.norm(got[key] - ref[key]) <= 1e-7 * np.linalg.norm(ref[key]), key
+        assert np.linalg.norm(got[key] - ref[key]) <= 1e-6 * np.linalg.norm(ref[key]), key
 
 
 @pytest.mark.parametrize("precision", [capi.FP64, capi.MIXED])
