@@ -325,6 +325,19 @@ def run_ours(args, rank, world):
     clk = clocks.stop()
     k64 = max(3, args.steps // 4)
     t_fp64, _, it_fp64, _ = timed(capi.FP64, k64, min(args.warmup, 3))
+    # phase times of the electrostatics in the mixed step (CUDA events on the launching stream)
+    ctx.set_profiling(True)
+    reset()
+    pol_phase = np.zeros(4)
+    nprof = 3
+    for i_ in range(2 + nprof):
+        step(capi.MIXED)
+        drift()
+        if i_ >= 2:
+            ms, kvec = ctx.polar_timings()
+            pol_phase += ms
+    pol_phase /= nprof
+    ctx.set_profiling(False)
 
     # the MB-pol 1B + 2B + 3B terms alone (the polynomial path), device resident
     def step_poly(precision):
@@ -444,12 +457,19 @@ def run_ours(args, rank, world):
     fp64_peak = 152 * 4 * sm_max * 1e6 / 1e12         # 2 DFMA per clock per SM
     fp64_achieved = fl["2b"] * ndim / t23 / 1e12 if t23 > 0 else None
     fp32_achieved = fl["3b"] * ntri / t23 / 1e12 if t23 > 0 else None
-    traffic = None
+    traffic = traffic_sf = None
     tfile = os.path.join(REPO, "profiles", "traffic.json")
     if os.path.exists(tfile):
         with open(tfile) as f:
             tj = json.load(f)
         traffic = tj.get("k_mbpol_23_bytes_per_launch")
+        per = tj.get("k_pol_sf_final_bytes_per_k_site")
+        traffic_sf = per * kvec * n if per else None
+    # the step's largest kernel: the final structure factors with the heat sums, FP64-bound;
+    # per (k vector, site): 30 fused multiply-adds and 8 multiplies (68 flops)
+    t_sf = pol_phase[2] / 1e3
+    sf_flops = 68.0 * kvec * n
+    sf_achieved = sf_flops / t_sf / 1e12 if t_sf > 0 else None
     value = world * args.steps / t_mixed
     out = {
         "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
@@ -482,7 +502,17 @@ def run_ours(args, rank, world):
                                                   "jkin": phase64[3]}},
         "e2e": {"value": world * args.steps / t_e2e, "unit": "steps/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
-        "roofline": {"kernel": "k_mbpol_23<double,float>", "bound": "fp64",
+        "roofline": {"kernel": "k_pol_sf_final<1>", "bound": "fp64", "achieved": sf_achieved, "peak": fp64_peak,
+                     "unit": "TFLOP/s", "frac": (sf_achieved / fp64_peak) if sf_achieved else None,
+                     "traffic": traffic_sf, "kernel_ms": 1e3 * t_sf, "flops_per_k_site": 68, "k_vectors": kvec,
+                     "sites": n, "algorithmic_bytes": 16.0 * kvec * n,
+                     "peak_source": "computed at sm_max_mhz %.0f: 152 SMs x 4 FP64 flop/clk (MEASURED_PEAKS.json "
+                                    "holds HBM and bf16 figures only)" % sm_max},
+        "electrostatics_phase_ms_mixed": {"setup (list, static fields, exp(ik.r) table)": pol_phase[0],
+                                          "dipole solve": pol_phase[1],
+                                          "final structure factors + heat sums": pol_phase[2],
+                                          "final forces, real-space terms, qdforce": pol_phase[3]},
+        "roofline_mbpol_23": {"kernel": "k_mbpol_23<double,float>", "bound": "fp64",
                      "achieved": fp64_achieved, "peak": fp64_peak, "unit": "TFLOP/s",
                      "frac": (fp64_achieved / fp64_peak) if fp64_achieved else None, "traffic": traffic,
                      "kernel_ms": 1e3 * t23, "flops_per_dimer_fp64": fl["2b"], "flops_per_trimer_fp32": fl["3b"],
@@ -666,7 +696,7 @@ def run_case(args):
     """Warmup + K device-resident steps of one precision (for profilers)."""
     import torch
     from mbx import capi, systems
-    box = systems.config1()
+    box = systems.box_for(args.nw, seed=20241) if args.nw else systems.config1()
     n = box.natms
     ctx = capi.Context(0)
     f64 = dict(dtype=torch.float64, device="cuda")
@@ -816,6 +846,7 @@ def main():
                     help="requests of the Poisson serving run reported under 'serving' (0: skip)")
     ap.add_argument("--ref-core-s", type=float, default=10.0)
     ap.add_argument("--no-batched", action="store_true", help="skip the multi-box section ('batched')")
+    ap.add_argument("--nw", type=int, default=0, help="profiling case: waters of the box (default 4096)")
     ap.add_argument("--case", choices=["mixed", "mixed-separate", "fp64", "step-mixed", "step-fp64"], default=None,
                     help="profiling case: only warmup + K device-resident steps of one precision")
     args = ap.parse_args()

@@ -865,6 +865,7 @@ extern "C" int mbx_polar_forces_device(mbx_context* ctx, int precision, const do
     CK(cudaSetDevice(ctx->device));
     double jp[3] = {0, 0, 0}, jk[3] = {0, 0, 0};
     if (ctx->nsm > 0) ctx->polar.nsm = ctx->nsm;
+    ctx->polar.profiling = ctx->profiling != 0;
     CK(ctx->polar.run(precision, cl, prm, nw, xxx, yyy, zzz, chge, dqdr, polr, polr2, dipx, dipy, dipz, fxx, fyy, fzz,
                       atomic_energy, heat ? vxx : nullptr, heat ? vyy : nullptr, heat ? vzz : nullptr, out16, jp, jk,
                       ctx->stream));
@@ -1006,6 +1007,7 @@ int water_step_core(mbx_context* ctx, int precision, int imcon, const double* ce
     if (ctx->nsm > 0) ctx->polar.nsm = ctx->nsm;
     // the electrostatic per-site energies stay apart: their jkin carries them with the
     // M-site redistribution
+    ctx->polar.profiling = ctx->profiling != 0;
     CK(ctx->polar.run(precision, cl, prm, nw, dx, dy, dz, dq, ddq, dpr, dpr2, dmx, dmy, dmz, dfx, dfy, dfz, daep,
                       heat ? dvx : nullptr, heat ? dvy : nullptr, heat ? dvz : nullptr, sp, jp, jk, s));
     for (int c = 0; c < 3; ++c) {
@@ -1179,6 +1181,13 @@ extern "C" int mbx_water_step(mbx_context* ctx, int precision, int imcon, const 
 extern "C" int mbx_polar_iterations(const mbx_context* ctx) { return ctx ? ctx->polar.iterations : -1; }
 
 extern "C" long mbx_polar_inner_sweeps(const mbx_context* ctx) { return ctx ? ctx->polar.inner_sweeps : -1; }
+
+extern "C" int mbx_polar_timings(const mbx_context* ctx, float* ms4, long* kvectors) {
+    if (!ctx || !ms4) return MBX_ERR_ARG;
+    for (int q = 0; q < 4; ++q) ms4[q] = ctx->polar.phase_ms[q];
+    if (kvectors) *kvectors = ctx->polar.K_last;
+    return MBX_OK;
+}
 
 extern "C" int mbx_msite_redistribute(int nw, double gamma, double* fxx, double* fyy, double* fzz) {
     if (nw < 0 || (nw && (!fxx || !fyy || !fzz))) return MBX_ERR_ARG;

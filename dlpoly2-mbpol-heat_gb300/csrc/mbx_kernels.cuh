@@ -198,6 +198,11 @@ struct PolarState {
     double* kpart = nullptr;               // per-chunk partial sums of the k-space gathers
     size_t part_cap = 0;
     int nsm = 152;                         // SMs of the device (grid sizing)
+    bool profiling = false;                // record the phase times below
+    cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    float phase_ms[4] = {0, 0, 0, 0};      // setup (lists, static fields, phases), dipole solve,
+                                           // final structure factors, rest of the final pass
+    long K_last = 0;                       // k vectors of the last call
     double4* kv = nullptr;                 // kx, ky, kz, akk
     double2* kx2 = nullptr;                // rksq, akv2
     int4* lmn = nullptr;

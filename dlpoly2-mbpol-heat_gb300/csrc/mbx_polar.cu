@@ -1455,6 +1455,11 @@ void PolarState::release() {
     for (void* q : p)
         if (q) cudaFree(q);
     if (acc_h) cudaFreeHost(acc_h);
+    for (auto& v : ev)
+        if (v) {
+            cudaEventDestroy(v);
+            v = nullptr;
+        }
     ercp = nullptr;
     nn = nbr = flag = nullptr;
     xf = nullptr;
@@ -1776,6 +1781,12 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
     k.sfac = 2.0 * rvolm * kR4pie0 / epsq;
 
     if ((e = cudaMemsetAsync(acc, 0, 64 * sizeof(double), s))) return e;
+    K_last = K;
+    if (profiling) {
+        for (auto& v : ev)
+            if (!v && (e = cudaEventCreate(&v))) return e;
+        if ((e = cudaEventRecord(ev[0], s))) return e;
+    }
     if (n == 0) {
         for (int c = 0; c < 16; ++c) out16[c] = 0.0;
         converged = true;
@@ -1916,11 +1927,13 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
         k_pol_vhat<<<blocks(n, kThreads), kThreads, 0, s>>>(a, vh);
         ++launches;
     }
+    if (profiling && (e = cudaEventRecord(ev[2], s))) return e;
     if (K) {
         if (heat) k_pol_sf_final<1><<<K, kSfThreads, 0, s>>>(k);
         else k_pol_sf_final<0><<<K, kSfThreads, 0, s>>>(k);
         ++launches;
     }
+    if (profiling && (e = cudaEventRecord(ev[3], s))) return e;
     if (K) {
         if (mixed) k_pol_kforce32<<<dim3(sblk2, nc2), kThreads, 0, s>>>(k, a, kc2, kpart);
         else k_pol_kforce<<<dim3(sblk2, nc2), kThreads, 0, s>>>(k, a, kc2, kpart);
@@ -1937,8 +1950,12 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
         ++launches;
     }
     if ((e = cudaGetLastError())) return e;
+    if (profiling && (e = cudaEventRecord(ev[4], s))) return e;
     if ((e = cudaMemcpyAsync(acc_h, acc, 64 * sizeof(double), cudaMemcpyDeviceToHost, s))) return e;
     if ((e = cudaStreamSynchronize(s))) return e;
+    if (profiling)
+        for (int q = 0; q < 4; ++q)
+            if ((e = cudaEventElapsedTime(&phase_ms[q], ev[q], ev[q + 1]))) return e;
     const double* h = acc_h;
     // acc: 0 eng_real, 1 vir, 2..7 stress (11 12 13 22 23 33), 8..10 jpot (real + qd),
     //      24..26 jkin, 27..28 iteration sums, 40 engsic, 41 eng_polar,

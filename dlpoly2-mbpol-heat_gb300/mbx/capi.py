@@ -95,6 +95,7 @@ def load(path=None):
     L.mbx_polar_iterations.argtypes = [C.c_void_p]
     L.mbx_polar_inner_sweeps.argtypes = [C.c_void_p]
     L.mbx_polar_inner_sweeps.restype = C.c_long
+    L.mbx_polar_timings.argtypes = [C.c_void_p, C.POINTER(C.c_float), _L]
     L.mbx_msite_redistribute.argtypes = [C.c_int, C.c_double, _D, _D, _D]
     L.mbx_water_step.argtypes = [C.c_void_p, C.c_int, C.c_int, _D, C.c_int, C.c_int, _D, _D, _D, _I, _I] + [_D] * 16
     L.mbx_water_step_device.argtypes = [C.c_void_p, C.c_int, C.c_int, _D, C.c_int, C.c_int, _D] + \
@@ -360,6 +361,13 @@ class Context:
 
     def polar_iterations(self):
         return int(self.lib.mbx_polar_iterations(self.h))
+
+    def polar_timings(self):
+        """(ms[4]: setup, dipole solve, final structure factors, rest of the final pass; K)"""
+        ms = (C.c_float * 4)()
+        kv = C.c_long(0)
+        self._check(self.lib.mbx_polar_timings(self.h, ms, C.byref(kv)), "mbx_polar_timings")
+        return np.array(list(ms)), int(kv.value)
 
     def polar_inner_sweeps(self):
         return int(self.lib.mbx_polar_inner_sweeps(self.h))

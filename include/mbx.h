@@ -220,6 +220,10 @@ int mbx_polar_forces_device(mbx_context* ctx, int precision, const double* prm, 
  * and the FP32 conjugate-gradient iterations of the last MBX_MIXED call. */
 int mbx_polar_iterations(const mbx_context* ctx);
 long mbx_polar_inner_sweeps(const mbx_context* ctx);
+/* With mbx_set_profiling on: the last electrostatics call's phase times in ms[4] (lists,
+ * static fields and exp(ik.r) table; dipole solve; final structure factors with the heat
+ * sums; rest of the final pass) and its number of k vectors. */
+int mbx_polar_timings(const mbx_context* ctx, float* ms4, long* kvectors);
 /* M-site force redistribution of the reference's MD step (SOURCE/dlpoly_cmd.f:2585-2601):
  * F_O += (1 - gamma) F_M, F_H1 += F_M gamma / 2, F_H2 += F_M gamma / 2 (standard layout,
  * host arrays of 4*nw sites; the M-site entries are left as they are). */
