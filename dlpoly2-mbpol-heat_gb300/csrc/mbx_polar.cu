@@ -1823,6 +1823,7 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
         k_pol_sfq<<<K, kSfThreads, 0, s>>>(k, q);
         launches += 3;
     }
+    if (profiling && (e = cudaEventRecord(ev[1], s))) return e;
     double deltadip = 0.0;
     // k vectors per chunk of the field / force gathers: about four blocks per SM in all
     const int sblk2 = (int)blocks(n, 2 * kThreads), sblk1 = (int)blocks(n, kThreads);

@@ -168,3 +168,17 @@ def test_water_step_is_the_sum_of_its_terms(oracle_lib, precision):
     assert abs(sc[nws] - pol["engcpe"]) <= tol * abs(pol["engcpe"])
     assert np.abs(sc[nws + 16:nws + 19] - pol["jpot"]).max() <= tol * np.abs(pol["jpot"]).max()
     assert np.abs(sc[nws + 19:nws + 22] - pol["jkin"]).max() <= tol * np.abs(pol["jkin"]).max()
+
+
+def test_polar_phase_timings(mbx_ctx, oracle_lib):
+    box = systems.box_for(32, seed=5)
+    prm = systems.polar_params(alpha=0.6, rcut=4.5, kmax=(6, 6, 6), toler_debye=1e-10)
+    sites, q, dp, polr, polr2, prm = _case(oracle_lib, box, prm)
+    mbx_ctx.set_profiling(True)
+    try:
+        for prec in (capi.FP64, capi.MIXED):
+            mbx_ctx.polar(sites, box.cell, box.imcon, box.nw, q, dp, polr, polr2, prm, vel=box.vel, precision=prec)
+            ms, kv = mbx_ctx.polar_timings()
+            assert kv > 0 and (ms >= 0).all() and ms.sum() > 0
+    finally:
+        mbx_ctx.set_profiling(False)
