@@ -466,9 +466,10 @@ def run_ours(args, rank, world):
         per = tj.get("k_pol_sf_final_bytes_per_k_site")
         traffic_sf = per * kvec * n if per else None
     # the step's largest kernel: the final structure factors with the heat sums, FP64-bound;
-    # per (k vector, site): 30 fused multiply-adds and 8 multiplies (68 flops)
+    # per (k vector, site) 30 multiply-adds (60 flops): 6 of the dipole structure factors and
+    # 24 of the heat sums over the per-site products q v and mu v
     t_sf = pol_phase[2] / 1e3
-    sf_flops = 68.0 * kvec * n
+    sf_flops = 60.0 * kvec * n
     sf_achieved = sf_flops / t_sf / 1e12 if t_sf > 0 else None
     value = world * args.steps / t_mixed
     out = {
@@ -504,7 +505,7 @@ def run_ours(args, rank, world):
                 "d2h_bytes_per_step": d2h},
         "roofline": {"kernel": "k_pol_sf_final<1>", "bound": "fp64", "achieved": sf_achieved, "peak": fp64_peak,
                      "unit": "TFLOP/s", "frac": (sf_achieved / fp64_peak) if sf_achieved else None,
-                     "traffic": traffic_sf, "kernel_ms": 1e3 * t_sf, "flops_per_k_site": 68, "k_vectors": kvec,
+                     "traffic": traffic_sf, "kernel_ms": 1e3 * t_sf, "flops_per_k_site": 60, "k_vectors": kvec,
                      "sites": n, "algorithmic_bytes": 16.0 * kvec * n,
                      "peak_source": "computed at sm_max_mhz %.0f: 152 SMs x 4 FP64 flop/clk (MEASURED_PEAKS.json "
                                     "holds HBM and bf16 figures only)" % sm_max},

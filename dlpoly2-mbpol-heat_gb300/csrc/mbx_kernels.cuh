@@ -184,7 +184,7 @@ struct PolarState {
     double2* fac = nullptr;                // per-site phase factors per axis and index
     size_t fac_cap = 0;
     double4* md = nullptr;                 // dipoles of the polarizable sites
-    double* vh = nullptr;                  // velocities the per-site terms are carried with
+    double* vh = nullptr;                  // per-site products of the ew1p heat sums (12 per site)
     double* kco = nullptr;                 // per-k coefficients of the gathers
     // mixed precision: FP32 tensors, phase table and correction solve
     float* tens32 = nullptr;

@@ -415,7 +415,7 @@ struct KArgs {
     double* kterm;         // 16 per k (final pass): engc, engdum, omg 11 22 33 12 13 23, jpot(3)
     const double4* md;     // dipoles of the polarizable sites (0 elsewhere)
     const double* q;       // site charges
-    const double* vh;      // velocities each site's quantities are carried with (3 blocks of n)
+    const double* vh;      // per-site products of the heat sums: q v (3 blocks of n), mu_c v_b (9 blocks)
     double rc[9];
     double scale, ralph, sfac;   // 4 rvolm r4pie0 / epsq, -1 / (4 alpha^2), 2 rvolm r4pie0 / epsq
 };
@@ -544,18 +544,18 @@ __global__ void __launch_bounds__(kSfThreads) k_pol_sf_final(KArgs k) {
         v[0] += cs.x * m.x; v[1] += cs.x * m.y; v[2] += cs.x * m.z;
         v[3] += cs.y * m.x; v[4] += cs.y * m.y; v[5] += cs.y * m.z;
         if (HEAT) {
-            const double vb[3] = {k.vh[j], k.vh[k.n + j], k.vh[2 * (size_t)k.n + j]};
-            const double q = k.q[j];
-            const double mu[3] = {m.x, m.y, m.z};
+            // per-site products q v (3) and mu_c v_b (9), rows of k.vh
 #pragma unroll
             for (int b = 0; b < 3; ++b) {
-                v[6 + b] += cs.x * q * vb[b];    // V1
-                v[9 + b] += cs.y * q * vb[b];    // V2
+                const double qv = k.vh[(size_t)b * k.n + j];
+                v[6 + b] += cs.x * qv;    // V1
+                v[9 + b] += cs.y * qv;    // V2
+            }
 #pragma unroll
-                for (int c = 0; c < 3; ++c) {
-                    v[12 + 3 * c + b] += cs.x * mu[c] * vb[b];   // W1[c][b]
-                    v[21 + 3 * c + b] += cs.y * mu[c] * vb[b];   // W2[c][b]
-                }
+            for (int cb = 0; cb < 9; ++cb) {
+                const double mv = k.vh[(size_t)(3 + cb) * k.n + j];
+                v[12 + cb] += cs.x * mv;   // W1[c][b]
+                v[21 + cb] += cs.y * mv;   // W2[c][b]
             }
         }
     }
@@ -1403,14 +1403,19 @@ __global__ void k_pol_kreduce(int K, const double* __restrict__ kterm, double* _
     }
 }
 
-__global__ void k_pol_vhat(PolArgs a, double* __restrict__ vh) {
+// Per-site products of the ew1p heat sums, with v the velocity each site's terms are
+// carried with: q v (3 rows), then mu_c v_b (9 rows, c major), mu the masked dipole.
+__global__ void k_pol_vhat(PolArgs a, const double4* __restrict__ md, double* __restrict__ vh) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= a.n) return;
     double v[3];
     vhat(a, j, v);
-    vh[j] = v[0];
-    vh[a.n + j] = v[1];
-    vh[2 * (size_t)a.n + j] = v[2];
+    const double q = a.q[j];
+    const double4 m = md[j];
+    const double mu[3] = {m.x, m.y, m.z};
+    for (int b = 0; b < 3; ++b) vh[(size_t)b * a.n + j] = q * v[b];
+    for (int c = 0; c < 3; ++c)
+        for (int b = 0; b < 3; ++b) vh[(size_t)(3 + 3 * c + b) * a.n + j] = mu[c] * v[b];
 }
 
 inline unsigned blocks(long n, int t) { return (unsigned)((n + t - 1) / t); }
@@ -1581,7 +1586,7 @@ cudaError_t PolarState::reserve(int nw, int K, size_t nfac) {
         if ((e = cudaMalloc(&vesp, m * sizeof(double)))) return e;
         if ((e = cudaMalloc(&ae, m * sizeof(double)))) return e;
         if ((e = cudaMalloc(&md, m * sizeof(double4)))) return e;
-        if ((e = cudaMalloc(&vh, 3 * m * sizeof(double)))) return e;
+        if ((e = cudaMalloc(&vh, 12 * m * sizeof(double)))) return e;
         n_cap = n;
         cap_alloc = cap;
     }
@@ -1925,7 +1930,7 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
     // final pass
     const double g34 = std::exp(gammln(3.0 / 4.0));
     if (heat) {
-        k_pol_vhat<<<blocks(n, kThreads), kThreads, 0, s>>>(a, vh);
+        k_pol_vhat<<<blocks(n, kThreads), kThreads, 0, s>>>(a, md, vh);
         ++launches;
     }
     if (profiling && (e = cudaEventRecord(ev[2], s))) return e;
