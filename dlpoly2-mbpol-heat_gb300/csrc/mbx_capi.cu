@@ -132,7 +132,10 @@ int make_cell(mbx_context* ctx, int imcon, const double* cell, Cell& cl) {
 }
 
 int reserve_water(mbx_context* ctx, int nw, int natms) {
+    // a capacity is zeroed before its buffers are replaced, so a failed allocation can
+    // never leave a capacity that promises memory which is not there
     if (nw > ctx->nw_cap) {
+        ctx->nw_cap = 0;
         if (ctx->mono) cudaFree(ctx->mono);
         if (ctx->list) cudaFree(ctx->list);
         ctx->mono = nullptr;
@@ -142,6 +145,7 @@ int reserve_water(mbx_context* ctx, int nw, int natms) {
         ctx->nw_cap = nw;
     }
     if (natms > ctx->natms_cap) {
+        ctx->natms_cap = 0;
         if (ctx->atoms) cudaFree(ctx->atoms);
         if (ctx->ae_scratch) cudaFree(ctx->ae_scratch);
         ctx->atoms = ctx->ae_scratch = nullptr;
@@ -204,6 +208,7 @@ int run_mbpol(mbx_context* ctx, int precision, const Cell& cl, int nw, const int
             if (ctx->hard2) cudaFree(ctx->hard2);
             if (ctx->part2) cudaFree(ctx->part2);
             if (ctx->done2) cudaFree(ctx->done2);
+            ctx->pairs_cap = 0;
             ctx->pairs = nullptr;
             ctx->hard2 = nullptr;
             ctx->part2 = nullptr;
@@ -218,6 +223,7 @@ int run_mbpol(mbx_context* ctx, int precision, const Cell& cl, int nw, const int
         if (nt > ctx->trip_cap) {
             if (ctx->trip) cudaFree(ctx->trip);
             if (ctx->hard3) cudaFree(ctx->hard3);
+            ctx->trip_cap = 0;
             ctx->trip = nullptr;
             ctx->hard3 = nullptr;
             const long cap = nt + nt / 4 + 64;
@@ -399,6 +405,7 @@ int prepare_multi(mbx_context* ctx, int precision, int imcon, int nbox, const in
     if (nbox > ctx->mbox_cap) {
         if (ctx->cells_h) cudaFreeHost(ctx->cells_h);
         if (ctx->mout_h) cudaFreeHost(ctx->mout_h);
+        ctx->mbox_cap = 0;
         ctx->cells_h = nullptr;
         ctx->mout_h = nullptr;
         CK(cudaMallocHost(&ctx->cells_h, nbox * sizeof(Cell)));
@@ -749,6 +756,7 @@ extern "C" int mbx_water_forces(mbx_context* ctx, int precision, int imcon, cons
     const size_t nint = (size_t)nttm2 + 3 * (size_t)nang + 2 * (size_t)natms + 1;
     if (nint > ctx->ints_cap) {
         if (ctx->ints) cudaFree(ctx->ints);
+        ctx->ints_cap = 0;
         ctx->ints = nullptr;
         CK(cudaMalloc(&ctx->ints, nint * sizeof(int)));
         ctx->ints_cap = nint;
@@ -839,6 +847,14 @@ extern "C" int mbx_disp_lrc(int ntypes, const double* prm, const int* numtyp, do
 extern "C" long mbx_disp_list_builds(const mbx_context* ctx) { return ctx ? ctx->disp.builds : -1; }
 
 namespace {
+// An electrostatics call that failed part way leaves no half-built state behind: the next
+// call allocates everything again.
+int polar_failed(mbx_context* ctx, cudaError_t e) {
+    cudaStreamSynchronize(ctx->stream);
+    ctx->polar.release();
+    return fail(ctx, MBX_ERR_CUDA, "electrostatics: %s", cudaGetErrorString(e));
+}
+
 bool polar_prm_ok(const double* prm) {
     return prm && prm[0] > 1e-6 && prm[1] > 0.0 && prm[2] > 0.0 && prm[3] > 0.0 && prm[4] >= 0.0 && prm[4] < 1.0 &&
            prm[11] >= 0 && prm[12] >= 0 && prm[13] >= 0 && prm[11] <= 512 && prm[12] <= 512 && prm[13] <= 512 &&
@@ -866,9 +882,10 @@ extern "C" int mbx_polar_forces_device(mbx_context* ctx, int precision, const do
     double jp[3] = {0, 0, 0}, jk[3] = {0, 0, 0};
     if (ctx->nsm > 0) ctx->polar.nsm = ctx->nsm;
     ctx->polar.profiling = ctx->profiling != 0;
-    CK(ctx->polar.run(precision, cl, prm, nw, xxx, yyy, zzz, chge, dqdr, polr, polr2, dipx, dipy, dipz, fxx, fyy, fzz,
-                      atomic_energy, heat ? vxx : nullptr, heat ? vyy : nullptr, heat ? vzz : nullptr, out16, jp, jk,
-                      ctx->stream));
+    const cudaError_t pe = ctx->polar.run(precision, cl, prm, nw, xxx, yyy, zzz, chge, dqdr, polr, polr2, dipx, dipy,
+                                          dipz, fxx, fyy, fzz, atomic_energy, heat ? vxx : nullptr,
+                                          heat ? vyy : nullptr, heat ? vzz : nullptr, out16, jp, jk, ctx->stream);
+    if (pe != cudaSuccess) return polar_failed(ctx, pe);
     ctx->launches = ctx->polar.launches;
     if (heat)
         for (int c = 0; c < 3; ++c) {
@@ -1008,8 +1025,10 @@ int water_step_core(mbx_context* ctx, int precision, int imcon, const double* ce
     // the electrostatic per-site energies stay apart: their jkin carries them with the
     // M-site redistribution
     ctx->polar.profiling = ctx->profiling != 0;
-    CK(ctx->polar.run(precision, cl, prm, nw, dx, dy, dz, dq, ddq, dpr, dpr2, dmx, dmy, dmz, dfx, dfy, dfz, daep,
-                      heat ? dvx : nullptr, heat ? dvy : nullptr, heat ? dvz : nullptr, sp, jp, jk, s));
+    const cudaError_t pe = ctx->polar.run(precision, cl, prm, nw, dx, dy, dz, dq, ddq, dpr, dpr2, dmx, dmy, dmz, dfx,
+                                          dfy, dfz, daep, heat ? dvx : nullptr, heat ? dvy : nullptr,
+                                          heat ? dvz : nullptr, sp, jp, jk, s);
+    if (pe != cudaSuccess) return polar_failed(ctx, pe);
     for (int c = 0; c < 3; ++c) {
         sp[16 + c] = jp[c];
         sp[19 + c] = jk[c];
@@ -1176,6 +1195,18 @@ extern "C" int mbx_water_step(mbx_context* ctx, int precision, int imcon, const 
         return fail(ctx, MBX_ERR_CONVERGE, "mbx_water_step: dipoles not converged after %d iterations",
                     ctx->polar.iterations);
     return MBX_OK;
+}
+
+extern "C" double mbx_trim(mbx_context* ctx, double keep_bytes) {
+    if (!ctx) return -1.0;
+    const double held = (double)ctx->polar.held_bytes();
+    if (held > keep_bytes) {
+        cudaSetDevice(ctx->device);
+        cudaStreamSynchronize(ctx->stream);
+        ctx->polar.release();
+        return held;
+    }
+    return 0.0;
 }
 
 extern "C" int mbx_polar_iterations(const mbx_context* ctx) { return ctx ? ctx->polar.iterations : -1; }

@@ -399,6 +399,8 @@ cudaError_t DispState::forces(const Cell& cl, int natms, const int* ltype, const
         xref = nullptr;
         key = skey = nullptr;
         sort_tmp = nullptr;
+        natms_cap = 0;   // until every buffer below exists
+        cap_alloc = 0;
         const size_t n = (size_t)natms + 1;
         if ((e = cudaMalloc(&nn, n * sizeof(int)))) return e;
         if ((e = cudaMalloc(&nbr, n * cap * sizeof(int)))) return e;
@@ -441,6 +443,7 @@ cudaError_t DispState::forces(const Cell& cl, int natms, const int* ltype, const
             if (cstart) cudaFree(cstart);
             if (cend) cudaFree(cend);
             cstart = cend = nullptr;
+            ncell_cap = 0;
             if ((e = cudaMalloc(&cstart, ncell * sizeof(int)))) return e;
             if ((e = cudaMalloc(&cend, ncell * sizeof(int)))) return e;
             ncell_cap = ncell;
@@ -483,7 +486,10 @@ cudaError_t DispState::forces(const Cell& cl, int natms, const int* ltype, const
         cap = std::min(2 * cap, natms + 32);
         if (nbr) cudaFree(nbr);
         nbr = nullptr;
-        if ((e = cudaMalloc(&nbr, ((size_t)natms_cap + 1) * cap * sizeof(int)))) return e;
+        const int keep = natms_cap;
+        natms_cap = 0;   // the rows are gone until the new ones exist
+        if ((e = cudaMalloc(&nbr, ((size_t)keep + 1) * cap * sizeof(int)))) return e;
+        natms_cap = keep;
         cap_alloc = cap;
     }
     k_disp_forces<<<grid(32L * natms), kThreads, 0, s>>>(a, nn, nbr, cap);

@@ -216,6 +216,12 @@ struct PolarState {
 
     ~PolarState();
     void release();
+    // device bytes held by the large buffers (phase tables, pair tensors)
+    size_t held_bytes() const {
+        return eik_cap * sizeof(double2) + eik32_cap * sizeof(float2) + fac_cap * sizeof(double2) +
+               (size_t)n_cap * cap_alloc * (6 * sizeof(double) + sizeof(int)) + (size_t)n32 * cap32 * 6 * sizeof(float) +
+               part_cap * sizeof(double);
+    }
     cudaError_t table(double alpha, double rcut);
     cudaError_t reserve(int nw, int K, size_t nfac);
     cudaError_t reserve_mixed(int n, int K);

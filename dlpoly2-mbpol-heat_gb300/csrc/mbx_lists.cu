@@ -245,6 +245,8 @@ cudaError_t ListBuilder::reserve(int nw, int ncell) {
         free_t(n2); free_t(l2); free_t(off2); free_t(n3); free_t(l3); free_t(tcnt); free_t(toff); free_t(of);
         free_ptr(scan_tmp); free_ptr(sort_tmp);
         const int n = std::max(nw, nw_cap) + 1;
+        nw_cap = 0;   // until every buffer below exists
+        cap2_alloc = cap3_alloc = 0;
         if ((e = cudaMalloc(&key, n * sizeof(unsigned)))) return e;
         if ((e = cudaMalloc(&skey, n * sizeof(unsigned)))) return e;
         if ((e = cudaMalloc(&idx, n * sizeof(int)))) return e;
@@ -271,6 +273,7 @@ cudaError_t ListBuilder::reserve(int nw, int ncell) {
     if (ncell > ncell_cap) {
         free_t(cstart);
         free_t(cend);
+        ncell_cap = 0;
         if ((e = cudaMalloc(&cstart, ncell * sizeof(int)))) return e;
         if ((e = cudaMalloc(&cend, ncell * sizeof(int)))) return e;
         ncell_cap = ncell;

@@ -1536,6 +1536,7 @@ cudaError_t PolarState::reserve_mixed(int n, int K) {
             if (q) cudaFree(q);
         tens32 = e32 = nullptr;
         r32 = d32 = cg_x = cg_r = cg_q = nullptr;
+        cap32 = n32 = 0;
         const size_t m = (size_t)std::max(n, 1);
         if ((e = cudaMalloc(&tens32, 6 * m * cap * sizeof(float)))) return e;
         if ((e = cudaMalloc(&r32, m * sizeof(float4)))) return e;
@@ -1550,6 +1551,7 @@ cudaError_t PolarState::reserve_mixed(int n, int K) {
     if (K > k32) {
         if (kco32) cudaFree(kco32);
         kco32 = nullptr;
+        k32 = 0;
         if ((e = cudaMalloc(&kco32, 16 * (size_t)std::max(K, 1) * sizeof(float)))) return e;
         k32 = K;
     }
@@ -1557,6 +1559,7 @@ cudaError_t PolarState::reserve_mixed(int n, int K) {
     if (need > eik32_cap) {
         if (eik32) cudaFree(eik32);
         eik32 = nullptr;
+        eik32_cap = 0;
         if ((e = cudaMalloc(&eik32, std::max(need, (size_t)1) * sizeof(float2)))) return e;
         eik32_cap = need;
     }
@@ -1569,10 +1572,14 @@ cudaError_t PolarState::reserve(int nw, int K, size_t nfac) {
     if (!acc && (e = cudaMalloc(&acc, 64 * sizeof(double)))) return e;
     if (!acc_h && (e = cudaMallocHost(&acc_h, 64 * sizeof(double)))) return e;
     if (!flag && (e = cudaMalloc(&flag, 4 * sizeof(int)))) return e;
+    // a capacity is zeroed before its buffers are replaced, so a failed allocation leaves
+    // nothing that a later call would take for allocated
     if (n > n_cap || cap != cap_alloc) {
         void* p[] = {nn, nbr, xf, tens, fld, vesp, ae, md, vh};
         for (void* q : p)
             if (q) cudaFree(q);
+        n_cap = 0;
+        cap_alloc = 0;
         nn = nbr = nullptr;
         xf = nullptr;
         tens = fld = vesp = ae = vh = nullptr;
@@ -1593,6 +1600,7 @@ cudaError_t PolarState::reserve(int nw, int K, size_t nfac) {
     if (nw > nw_cap) {
         if (intra) cudaFree(intra);
         intra = nullptr;
+        nw_cap = 0;
         if ((e = cudaMalloc(&intra, 18 * (size_t)std::max(nw, 1) * sizeof(double)))) return e;
         nw_cap = nw;
     }
@@ -1604,6 +1612,7 @@ cudaError_t PolarState::reserve(int nw, int K, size_t nfac) {
         kx2 = nullptr;
         lmn = nullptr;
         sf = kterm = kco = nullptr;
+        k_cap = 0;
         if ((e = cudaMalloc(&kv, K * sizeof(double4)))) return e;
         if ((e = cudaMalloc(&kx2, K * sizeof(double2)))) return e;
         if ((e = cudaMalloc(&lmn, K * sizeof(int4)))) return e;
@@ -1616,12 +1625,14 @@ cudaError_t PolarState::reserve(int nw, int K, size_t nfac) {
     if (need > eik_cap) {
         if (eik) cudaFree(eik);
         eik = nullptr;
+        eik_cap = 0;
         if ((e = cudaMalloc(&eik, std::max(need, (size_t)1) * sizeof(double2)))) return e;
         eik_cap = need;
     }
     if (nfac * n > fac_cap) {
         if (fac) cudaFree(fac);
         fac = nullptr;
+        fac_cap = 0;
         if ((e = cudaMalloc(&fac, std::max(nfac * n, (size_t)1) * sizeof(double2)))) return e;
         fac_cap = nfac * n;
     }

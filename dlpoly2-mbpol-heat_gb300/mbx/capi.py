@@ -79,6 +79,9 @@ def load(path=None):
     L.mbx_server_submit.argtypes = [C.c_void_p, C.c_int, C.c_int, _D, C.c_int, C.c_int] + [_D] * 7
     L.mbx_server_submit.restype = C.c_long
     L.mbx_server_wait.argtypes = [C.c_void_p, C.c_long] + [_D] * 6
+    L.mbx_server_submit_step.argtypes = [C.c_void_p, C.c_int, C.c_long, C.c_int, _D, C.c_int] + [_D] * 7
+    L.mbx_server_submit_step.restype = C.c_long
+    L.mbx_server_wait_step.argtypes = [C.c_void_p, C.c_long] + [_D] * 7
     L.mbx_server_error.argtypes = [C.c_void_p]
     L.mbx_server_error.restype = C.c_char_p
     L.mbx_mbpol_multi.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, _I, _D] + [_D] * 12
@@ -95,6 +98,8 @@ def load(path=None):
     L.mbx_polar_iterations.argtypes = [C.c_void_p]
     L.mbx_polar_inner_sweeps.argtypes = [C.c_void_p]
     L.mbx_polar_inner_sweeps.restype = C.c_long
+    L.mbx_trim.argtypes = [C.c_void_p, C.c_double]
+    L.mbx_trim.restype = C.c_double
     L.mbx_polar_timings.argtypes = [C.c_void_p, C.POINTER(C.c_float), _L]
     L.mbx_msite_redistribute.argtypes = [C.c_int, C.c_double, _D, _D, _D]
     L.mbx_water_step.argtypes = [C.c_void_p, C.c_int, C.c_int, _D, C.c_int, C.c_int, _D, _D, _D, _I, _I] + [_D] * 16
@@ -473,3 +478,30 @@ class Server:
         if rc:
             raise MbxError("request %d failed with status %d" % (rid, rc))
         return dict(forces=f.T.copy(), atomic_energy=ae, scalars=sc, queue_s=t[0], run_s=t[1], latency_s=t[2])
+
+    def submit_step(self, box, client, precision=MIXED, heat=True):
+        """The whole force evaluation with the electrostatics; dipoles warm-started from the
+        client's previous request."""
+        x, y, z = (_f64(box.xyz[:, k]) for k in range(3))
+        v = [_f64(box.vel[:, k]) for k in range(3)] if heat else [None] * 3
+        m = _f64(box.mass) if heat else None
+        rid = self.lib.mbx_server_submit_step(self.h, precision, int(client), box.imcon, _p(_f64(box.cell)), box.nw,
+                                              _p(x), _p(y), _p(z), _p(v[0]), _p(v[1]), _p(v[2]), _p(m))
+        if rid <= 0:
+            raise MbxError("mbx_server_submit_step failed with status %d" % -rid)
+        self._boxes[rid] = box.natms
+        return rid
+
+    def wait_step(self, rid):
+        n = self._boxes.pop(rid)
+        f = np.zeros((3, n))
+        ae = np.zeros(n)
+        dip = np.zeros((3, n))
+        sc = np.zeros(NSTEPSCALARS)
+        t = np.zeros(3)
+        rc = self.lib.mbx_server_wait_step(self.h, rid, _p(f[0]), _p(f[1]), _p(f[2]), _p(ae), _p(dip.reshape(-1)),
+                                           _p(sc), _p(t))
+        if rc:
+            raise MbxError("request %d failed with status %d: %s" % (rid, rc, self.lib.mbx_server_error(self.h).decode()))
+        return dict(forces=f.T.copy(), atomic_energy=ae, dipoles=dip.T.copy(), scalars=sc, queue_s=t[0],
+                    run_s=t[1], latency_s=t[2])

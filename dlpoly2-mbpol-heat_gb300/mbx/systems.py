@@ -235,3 +235,18 @@ def polarizabilities(nw):
     polr2[:3 * nw] = polr[:3 * nw]
     polr2[3 * nw:] = 0.0
     return polr, polr2
+
+
+def polar_params_for(cell, maxit=22581):
+    """The server's Ewald settings for a cell (mbx_server_submit_step): rcut = min(9, 0.49 x
+    the narrowest width), alpha = 2.7 / rcut, kmax per axis ceil(8 alpha w / (0.3 x 19.73))."""
+    a = np.asarray(cell, dtype=np.float64)
+    bxc = np.array([a[4] * a[8] - a[5] * a[7], a[5] * a[6] - a[3] * a[8], a[3] * a[7] - a[4] * a[6]])
+    cxa = np.array([a[7] * a[2] - a[1] * a[8], a[0] * a[8] - a[2] * a[6], a[1] * a[6] - a[0] * a[7]])
+    axb = np.array([a[1] * a[5] - a[2] * a[4], a[2] * a[3] - a[0] * a[5], a[0] * a[4] - a[1] * a[3]])
+    v = abs(a[0] * bxc[0] + a[1] * bxc[1] + a[2] * bxc[2])
+    w = [v / np.sqrt(bxc @ bxc), v / np.sqrt(cxa @ cxa), v / np.sqrt(axb @ axb)]
+    rcut = min(9.0, 0.49 * min(w))
+    alpha = 2.7 / rcut
+    km = tuple(max(1, int(math.ceil(8.0 * alpha * wi / (0.3 * 19.73) - 1e-9))) for wi in w)
+    return polar_params(alpha=alpha, kmax=km, rcut=rcut, toler_debye=1e-8, maxit=maxit)

@@ -224,6 +224,10 @@ long mbx_polar_inner_sweeps(const mbx_context* ctx);
  * static fields and exp(ik.r) table; dipole solve; final structure factors with the heat
  * sums; rest of the final pass) and its number of k vectors. */
 int mbx_polar_timings(const mbx_context* ctx, float* ms4, long* kvectors);
+/* Frees the electrostatics' device buffers (phase tables, pair tensors) of a context when
+ * they hold more than keep_bytes; returns the bytes freed (0: kept).  The next call
+ * allocates them again. */
+double mbx_trim(mbx_context* ctx, double keep_bytes);
 /* M-site force redistribution of the reference's MD step (SOURCE/dlpoly_cmd.f:2585-2601):
  * F_O += (1 - gamma) F_M, F_H1 += F_M gamma / 2, F_H2 += F_M gamma / 2 (standard layout,
  * host arrays of 4*nw sites; the M-site entries are left as they are). */
@@ -292,6 +296,24 @@ long mbx_server_submit(mbx_server* server, int precision, int imcon, const doubl
                        const double* vzz, const double* weight);
 int mbx_server_wait(mbx_server* server, long id, double* fxx, double* fyy, double* fzz, double* atomic_energy,
                     double* scalars, double* times);
+/*
+ * The whole force evaluation per request (mbx_water_step: M sites, DMS charges, TTM4-F
+ * electrostatics, 1-body, 2B, 3B, M-site redistribution, heat current); natms = 4*nw in
+ * the standard layout.  The Ewald settings follow the cell: rcut = min(9, 0.49 x the
+ * narrowest width), alpha = 2.7 / rcut, kmax per axis keeping 2 pi kmax / (alpha L) of
+ * the 256-water box (kmax 8 at alpha 0.3, L 19.73); the vmbpol Thole settings, MB-pol's
+ * polarizabilities, dipoles to 1e-8 D.  The induced dipoles start from the last converged
+ * ones of the same `client` (zero for its first request or after a size change); a
+ * client's requests run one at a time in submission order.  Admission counts the
+ * electrostatics' phase tables and pair tensors in the footprint.
+ *   mbx_server_wait_step  as mbx_server_wait, plus the converged dipoles (3 * natms, x
+ *                         block then y then z) and scalars[MBX_NSTEPSCALARS].
+ */
+long mbx_server_submit_step(mbx_server* server, int precision, long client, int imcon, const double* cell, int nw,
+                            const double* xxx, const double* yyy, const double* zzz, const double* vxx,
+                            const double* vyy, const double* vzz, const double* weight);
+int mbx_server_wait_step(mbx_server* server, long id, double* fxx, double* fyy, double* fzz, double* atomic_energy,
+                         double* dipoles, double* scalars, double* times);
 const char* mbx_server_error(const mbx_server* server);
 
 /*
