@@ -987,7 +987,10 @@ int step_lists(mbx_context* ctx, int nw, int natms) {
         h[na + 3 * w + 2] = 3 * w + 3;
     }
     CK(cudaMalloc(&ctx->step_ints, h.size() * sizeof(int)));
-    CK(cudaMemcpy(ctx->step_ints, h.data(), h.size() * sizeof(int), cudaMemcpyHostToDevice));
+    // on the context's stream and complete before returning: a plain cudaMemcpy from pageable
+    // memory may return before its DMA lands, unordered with the (non-blocking) stream
+    CK(cudaMemcpyAsync(ctx->step_ints, h.data(), h.size() * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
     ctx->step_nw = nw;
     return MBX_OK;
 }
@@ -1457,6 +1460,7 @@ extern "C" int mbx_last_lists(mbx_context* ctx, int* pairs, long cap_pairs, long
     if (npairs) *npairs = ctx->npairs;
     if (ntrimers) *ntrimers = ctx->ntrip;
     CK(cudaSetDevice(ctx->device));
+    CK(cudaStreamSynchronize(ctx->stream));   // the lists come from the context's stream
     if (pairs && ctx->npairs) {
         const long n = std::min(cap_pairs, ctx->npairs);
         CK(cudaMemcpy(pairs, ctx->pairs, n * sizeof(int2), cudaMemcpyDeviceToHost));

@@ -360,6 +360,9 @@ cudaError_t DispState::setup(int ntypes_, const double* prm_, double rcut_, doub
     if ((e = cudaMalloc(&ggg, hg.size() * sizeof(double)))) return e;
     if ((e = cudaMemcpy(vvv, hv.data(), hv.size() * sizeof(double), cudaMemcpyHostToDevice))) return e;
     if ((e = cudaMemcpy(ggg, hg.data(), hg.size() * sizeof(double), cudaMemcpyHostToDevice))) return e;
+    // a copy from pageable memory may return before its DMA lands; the tables are read by
+    // kernels on non-blocking streams, so wait for the copies here
+    if ((e = cudaStreamSynchronize(cudaStreamLegacy))) return e;
     valid = false;
     return cudaSuccess;
 }

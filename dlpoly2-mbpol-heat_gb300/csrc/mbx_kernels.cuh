@@ -222,7 +222,7 @@ struct PolarState {
                (size_t)n_cap * cap_alloc * (6 * sizeof(double) + sizeof(int)) + (size_t)n32 * cap32 * 6 * sizeof(float) +
                part_cap * sizeof(double);
     }
-    cudaError_t table(double alpha, double rcut);
+    cudaError_t table(double alpha, double rcut, cudaStream_t s);
     cudaError_t reserve(int nw, int K, size_t nfac);
     cudaError_t reserve_mixed(int n, int K);
     cudaError_t reserve_part(size_t ndouble);

@@ -1490,7 +1490,7 @@ void PolarState::release() {
 
 PolarState::~PolarState() { release(); }
 
-cudaError_t PolarState::table(double alpha, double rcut) {
+cudaError_t PolarState::table(double alpha, double rcut, cudaStream_t s) {
     if (ercp && alpha == tab_alpha && rcut == tab_rcut) return cudaSuccess;
     if (ercp) cudaFree(ercp);
     ercp = nullptr;
@@ -1512,7 +1512,10 @@ cudaError_t PolarState::table(double alpha, double rcut) {
     }
     cudaError_t e;
     if ((e = cudaMalloc(&ercp, h.size() * sizeof(double4)))) return e;
-    if ((e = cudaMemcpy(ercp, h.data(), h.size() * sizeof(double4), cudaMemcpyHostToDevice))) return e;
+    // stream-ordered and complete before the host vector goes (a plain cudaMemcpy from
+    // pageable memory may return before its DMA lands, unordered with non-blocking streams)
+    if ((e = cudaMemcpyAsync(ercp, h.data(), h.size() * sizeof(double4), cudaMemcpyHostToDevice, s))) return e;
+    if ((e = cudaStreamSynchronize(s))) return e;
     tab_alpha = alpha;
     tab_rcut = rcut;
     return cudaSuccess;
@@ -1652,7 +1655,7 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
     const double alpha = prm[0], rcut = prm[1], epsq = prm[2];
     const int kmax[3] = {(int)prm[11], (int)prm[12], (int)prm[13]};
     const int maxit = (int)prm[14];
-    if ((e = table(alpha, rcut))) return e;
+    if ((e = table(alpha, rcut, s))) return e;
 
     // k vectors in ewald1p's order (SOURCE/ewald1p.f:159-172, :279-348)
     double rc[9];
