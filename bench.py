@@ -526,6 +526,7 @@ def run_ours(args, rank, world):
     }
     if not args.no_batched:
         out["batched"] = batched()
+        out["batched_whole_evaluation"] = batched_whole()
         out["dispersion"] = dispersion()
     if args.serve_requests > 0:
         out["serving"] = serve(n_requests=args.serve_requests)
@@ -690,6 +691,115 @@ def batched(steps=10, warmup=3):
             torch.cuda.synchronize()
             t = e0.elapsed_time(e1) / 1e3
             res["mixed_one_box_per_call"] = {"steps_per_s": steps / t, "ms_per_step": 1e3 * t / steps}
+        ctx.close()
+        out[name] = res
+    return out
+
+
+def batched_whole(steps=4, warmup=2, lanes=8):
+    """Whole force evaluations (M sites, DMS charges, TTM4-F electrostatics with the dipole
+    solve, dispersion, 1-body, 2B + 3B, heat current) of many boxes per call through
+    mbx_water_step_multi: 32 beads of the 256-water box (Ewald alpha 0.3, kmax 8, rcut 9)
+    and 64 uneven boxes (alpha L fixed: the server's settings per cell).  Host buffers
+    (the call copies in and out), positions advanced by v dt and dipoles carried over
+    between steps as in MD; wall-clock per call.  The beads also run one box per call on
+    one context for comparison."""
+    import ctypes as C
+    from mbx import capi, systems
+    D, I = C.POINTER(C.c_double), C.POINTER(C.c_int)
+
+    def p(a, t=D):
+        return None if a is None else a.ctypes.data_as(t)
+
+    out = {}
+    for name, boxes in (("beads_32x256", systems.config2()), ("uneven_64_boxes", systems.config3())):
+        nb = len(boxes)
+        if name.startswith("beads"):
+            prms = [systems.polar_params(alpha=0.3, rcut=9.0, kmax=(8, 8, 8), toler_debye=1e-8) for _ in boxes]
+        else:
+            prms = [systems.polar_params_for(b.cell) for b in boxes]
+            for q in prms:
+                q[3] = systems.polar_params(toler_debye=1e-8)[3]
+        nws = np.array([b.nw for b in boxes], np.int32)
+        imc = np.array([b.imcon for b in boxes], np.int32)
+        cells = np.concatenate([np.asarray(b.cell, np.float64) for b in boxes])
+        prm = np.concatenate(prms)
+        xyz0 = np.concatenate([b.xyz for b in boxes])
+        vel = np.concatenate([b.vel for b in boxes])
+        n = xyz0.shape[0]
+        v = [np.ascontiguousarray(vel[:, k]) for k in range(3)]
+        mass = np.ascontiguousarray(np.concatenate([b.mass for b in boxes]), np.float64)
+        pol = [systems.polarizabilities(b.nw) for b in boxes]
+        polr = np.concatenate([a for a, _ in pol])
+        polr2 = np.concatenate([b_ for _, b_ in pol])
+        lt, mol = (np.ascontiguousarray(np.concatenate(a), np.int32)
+                   for a in zip(*(systems.water_types(b) for b in boxes)))
+        atom = np.zeros(n, bool)
+        o = 0
+        for b in boxes:
+            atom[o:o + 3 * b.nw] = True
+            o += b.natms
+        res = {"boxes": nb, "waters": int(nws.sum()), "lanes": lanes}
+        ctx = capi.Context(0)
+        ctx.set_lanes(lanes)
+        ctx.disp_setup(systems.DISP_PARAMS_SYNTHETIC, rcut=min(9.0, 0.45 * min(b.L for b in boxes)), delr=0.5)
+        sc = np.zeros((nb, capi.NSTEPSCALARS))
+        st = np.zeros(nb, np.int32)
+        for prec, key in ((capi.MIXED, "mixed"), (capi.FP64, "fp64")):
+            x, y, z = (np.ascontiguousarray(xyz0[:, k]).copy() for k in range(3))
+            dip = [np.zeros(n) for _ in range(3)]
+            f = [np.zeros(n) for _ in range(3)]
+            ae = np.zeros(n)
+            ts, its = [], []
+            for s_ in range(warmup + steps):
+                for a in f:
+                    a[:] = 0.0
+                ae[:] = 0.0
+                t0 = time.perf_counter()
+                rc = ctx.lib.mbx_water_step_multi(
+                    ctx.h, prec, nb, p(imc, I), p(cells), p(nws, I), p(prm), p(polr), p(polr2), p(lt, I),
+                    p(mol, I), p(x), p(y), p(z), p(dip[0]), p(dip[1]), p(dip[2]), p(f[0]), p(f[1]), p(f[2]),
+                    p(v[0]), p(v[1]), p(v[2]), p(mass), p(ae), None, p(sc), p(st, I))
+                t1 = time.perf_counter()
+                if rc:
+                    raise RuntimeError("mbx_water_step_multi: %d %s" % (rc, ctx.lib.mbx_error(ctx.h)))
+                if s_ >= warmup:
+                    ts.append(t1 - t0)
+                for k, a in enumerate((x, y, z)):
+                    a[atom] += DT_PS * v[k][atom]
+            t = float(np.mean(ts))
+            res[key] = {"steps_per_s": 1.0 / t, "ms_per_step": 1e3 * t, "boxes_per_s": nb / t,
+                        "waters_per_s": float(nws.sum()) / t}
+        if name.startswith("beads"):
+            # the same whole evaluations one box per call on one context (mixed)
+            x, y, z = (np.ascontiguousarray(xyz0[:, k]).copy() for k in range(3))
+            dip = [np.zeros(n) for _ in range(3)]
+            f = [np.zeros(n) for _ in range(3)]
+            ae = np.zeros(n)
+            s1 = np.zeros(capi.NSTEPSCALARS)
+            ts = []
+            for s_ in range(warmup + steps):
+                t0 = time.perf_counter()
+                o = 0
+                for b, box in enumerate(boxes):
+                    m = box.natms
+                    sl = lambda a: a[o:].ctypes.data_as(D)
+                    rc = ctx.lib.mbx_water_step(
+                        ctx.h, capi.MIXED, box.imcon, p(np.asarray(box.cell, np.float64)), box.nw, m,
+                        p(prms[b]), sl(polr), sl(polr2), lt[o:].ctypes.data_as(I), mol[o:].ctypes.data_as(I),
+                        sl(x), sl(y), sl(z), sl(dip[0]), sl(dip[1]), sl(dip[2]), sl(f[0]), sl(f[1]), sl(f[2]),
+                        sl(v[0]), sl(v[1]), sl(v[2]), sl(mass), sl(ae), None, p(s1))
+                    if rc:
+                        raise RuntimeError("mbx_water_step: %d" % rc)
+                    o += m
+                t1 = time.perf_counter()
+                if s_ >= warmup:
+                    ts.append(t1 - t0)
+                for k, a in enumerate((x, y, z)):
+                    a[atom] += DT_PS * v[k][atom]
+            t = float(np.mean(ts))
+            res["mixed_one_box_per_call"] = {"steps_per_s": 1.0 / t, "ms_per_step": 1e3 * t}
+        res["mixed_over_fp64"] = res["mixed"]["steps_per_s"] / res["fp64"]["steps_per_s"]
         ctx.close()
         out[name] = res
     return out

@@ -7,7 +7,10 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <atomic>
 #include <mutex>
+#include <numeric>
+#include <thread>
 #include <vector>
 
 using namespace mbx;
@@ -80,6 +83,15 @@ struct mbx_context {
     int* step_ints = nullptr;          // standard-layout water and angle lists
     int step_nw = -1;
     std::vector<int> disp_types_h, disp_mol_h;   // inputs of the host entry point's list
+    // mbx_water_step_multi: worker lanes (child contexts, each with its own stream and
+    // buffers, driven by one host thread per call) and the dispersion setup they replay
+    std::vector<mbx_context*> lane;
+    int nlanes = 8;
+    std::vector<double> disp_prm_h;
+    int disp_ntypes = 0, disp_mxgrid = 0;
+    double disp_rcut = 0.0, disp_delr = 0.0;
+    long disp_gen = 0;       // setups made on this context
+    long disp_gen_seen = -1; // (on a lane) the parent's setup it holds
     char err[512] = {0};
 };
 
@@ -476,6 +488,8 @@ extern "C" int mbx_create(mbx_context** out, int device) {
 
 extern "C" void mbx_destroy(mbx_context* ctx) {
     if (!ctx) return;
+    for (mbx_context* c : ctx->lane) mbx_destroy(c);
+    ctx->lane.clear();
     cudaSetDevice(ctx->device);
     if (ctx->own_stream) cudaStreamSynchronize(ctx->own_stream);
     void* dev[] = {ctx->mono, ctx->list, ctx->atoms, ctx->ae_scratch, ctx->acc, ctx->totals, ctx->pairs, ctx->trip,
@@ -629,6 +643,12 @@ extern "C" int mbx_disp_setup(mbx_context* ctx, int ntypes, const double* prm, d
     CK(cudaSetDevice(ctx->device));
     CK(ctx->disp.setup(ntypes, prm, rcut, delr, mxgrid));
     ctx->disp_types_h.clear();
+    ctx->disp_prm_h.assign(prm, prm + 4 * (size_t)(ntypes * (ntypes + 1) / 2));   // replayed on the lanes
+    ctx->disp_ntypes = ntypes;
+    ctx->disp_rcut = rcut;
+    ctx->disp_delr = delr;
+    ctx->disp_mxgrid = mxgrid;
+    ++ctx->disp_gen;
     return MBX_OK;
 }
 
@@ -1197,6 +1217,104 @@ extern "C" int mbx_water_step(mbx_context* ctx, int precision, int imcon, const 
     if (!ctx->polar.converged)
         return fail(ctx, MBX_ERR_CONVERGE, "mbx_water_step: dipoles not converged after %d iterations",
                     ctx->polar.iterations);
+    return MBX_OK;
+}
+
+// Many boxes, one call: box b runs mbx_water_step on its slice of the arrays on one of the
+// context's worker lanes.  A lane is a child context (its own stream and device buffers,
+// kept between calls) driven by its own host thread for the call, so the boxes' kernels
+// and host round trips overlap; boxes are taken largest first from a shared counter.
+extern "C" int mbx_set_lanes(mbx_context* ctx, int lanes) {
+    if (!ctx) return MBX_ERR_ARG;
+    if (lanes < 1 || lanes > 64) return fail(ctx, MBX_ERR_ARG, "lanes must be 1..64");
+    ctx->nlanes = lanes;
+    return MBX_OK;
+}
+
+extern "C" int mbx_water_step_multi(mbx_context* ctx, int precision, int nbox, const int* imcon, const double* cell,
+                                    const int* nw, const double* polar_prm, const double* polr, const double* polr2,
+                                    const int* ltype, const int* molecule, double* xxx, double* yyy, double* zzz,
+                                    double* dipx, double* dipy, double* dipz, double* fxx, double* fyy, double* fzz,
+                                    const double* vxx, const double* vyy, const double* vzz, const double* weight,
+                                    double* atomic_energy, double* chge, double* scalars, int* status) {
+    if (!ctx) return MBX_ERR_ARG;
+    if ((precision != MBX_FP64 && precision != MBX_MIXED) || nbox < 0 || (nbox && (!imcon || !cell || !nw ||
+                                                                                     !polar_prm)))
+        return fail(ctx, MBX_ERR_ARG, "mbx_water_step_multi: bad argument");
+    std::vector<size_t> off(nbox + 1, 0);
+    for (int b = 0; b < nbox; ++b) {
+        if (nw[b] < 0) return fail(ctx, MBX_ERR_ARG, "mbx_water_step_multi: box %d has %d waters", b, nw[b]);
+        if (!polar_prm_ok(polar_prm + 15 * (size_t)b))
+            return fail(ctx, MBX_ERR_ARG, "mbx_water_step_multi: bad electrostatics parameters of box %d", b);
+        off[b + 1] = off[b] + 4 * (size_t)nw[b];
+    }
+    if (off[nbox] && (!polr || !polr2 || !xxx || !yyy || !zzz || !dipx || !dipy || !dipz || !fxx || !fyy || !fzz))
+        return fail(ctx, MBX_ERR_ARG, "mbx_water_step_multi: bad argument");
+    const bool disp = ltype && molecule;
+    if (disp && ctx->disp_gen == 0) return fail(ctx, MBX_ERR_ARG, "dispersion asked for before mbx_disp_setup");
+    const bool heat = vxx && vyy && vzz && weight;
+    const int nl = std::min(ctx->nlanes, std::max(nbox, 1));
+    while ((int)ctx->lane.size() < nl) {
+        mbx_context* c = nullptr;
+        const int rc = mbx_create(&c, ctx->device);
+        if (rc) return fail(ctx, rc, "mbx_water_step_multi: creating a lane failed");
+        ctx->lane.push_back(c);
+    }
+    for (int l = 0; l < nl; ++l) {   // the parent's settings and dispersion tables
+        mbx_context* c = ctx->lane[l];
+        c->limit2 = ctx->limit2;
+        c->limit3 = ctx->limit3;
+        c->fused = ctx->fused;
+        if (disp && c->disp_gen_seen != ctx->disp_gen) {
+            const int rc = mbx_disp_setup(c, ctx->disp_ntypes, ctx->disp_prm_h.data(), ctx->disp_rcut, ctx->disp_delr,
+                                          ctx->disp_mxgrid);
+            if (rc) return fail(ctx, rc, "mbx_water_step_multi: lane %d: %s", l, c->err);
+            c->disp_gen_seen = ctx->disp_gen;
+        }
+    }
+    std::vector<int> order(nbox), st(nbox, MBX_OK);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return nw[a] > nw[b]; });
+    std::atomic<int> next{0};
+    std::mutex err_mu;   // the first lane error goes to the parent context
+    std::vector<long> launches(nl, 0);
+    auto work = [&](int l) {
+        mbx_context* c = ctx->lane[l];
+        for (int t; (t = next.fetch_add(1)) < nbox;) {
+            const int b = order[t];
+            const size_t o = off[b];
+            double sc[MBX_NSTEPSCALARS];
+            st[b] = mbx_water_step(c, precision, imcon[b], cell + 9 * (size_t)b, nw[b], 4 * nw[b],
+                                   polar_prm + 15 * (size_t)b, polr + o, polr2 + o, disp ? ltype + o : nullptr,
+                                   disp ? molecule + o : nullptr, xxx + o, yyy + o, zzz + o, dipx + o, dipy + o,
+                                   dipz + o, fxx + o, fyy + o, fzz + o, heat ? vxx + o : nullptr,
+                                   heat ? vyy + o : nullptr, heat ? vzz + o : nullptr, heat ? weight + o : nullptr,
+                                   atomic_energy ? atomic_energy + o : nullptr, chge ? chge + o : nullptr, sc);
+            if (scalars) std::memcpy(scalars + MBX_NSTEPSCALARS * (size_t)b, sc, sizeof sc);
+            launches[l] += c->launches;
+            if (st[b] != MBX_OK && st[b] != MBX_ERR_CONVERGE) {
+                std::lock_guard<std::mutex> lk(err_mu);
+                if (!ctx->err[0]) std::snprintf(ctx->err, sizeof ctx->err, "box %d: %s", b, c->err);
+            }
+        }
+    };
+    ctx->err[0] = 0;
+    if (nl == 1) {
+        work(0);
+    } else {
+        std::vector<std::thread> th;
+        for (int l = 0; l < nl; ++l) th.emplace_back(work, l);
+        for (auto& t : th) t.join();
+    }
+    ctx->launches = std::accumulate(launches.begin(), launches.end(), 0L);
+    if (status) std::copy(st.begin(), st.end(), status);
+    int rc = MBX_OK;
+    for (int b = 0; b < nbox && rc == MBX_OK; ++b)
+        if (st[b] != MBX_OK && st[b] != MBX_ERR_CONVERGE) rc = st[b];
+    if (rc) return rc;
+    for (int b = 0; b < nbox; ++b)
+        if (st[b] == MBX_ERR_CONVERGE)
+            return fail(ctx, MBX_ERR_CONVERGE, "mbx_water_step_multi: dipoles of box %d not converged", b);
     return MBX_OK;
 }
 

@@ -103,6 +103,9 @@ def load(path=None):
     L.mbx_polar_timings.argtypes = [C.c_void_p, C.POINTER(C.c_float), _L]
     L.mbx_msite_redistribute.argtypes = [C.c_int, C.c_double, _D, _D, _D]
     L.mbx_water_step.argtypes = [C.c_void_p, C.c_int, C.c_int, _D, C.c_int, C.c_int, _D, _D, _D, _I, _I] + [_D] * 16
+    L.mbx_set_lanes.argtypes = [C.c_void_p, C.c_int]
+    L.mbx_water_step_multi.argtypes = ([C.c_void_p, C.c_int, C.c_int, _I, _D, _I, _D, _D, _D, _I, _I] + [_D] * 16 +
+                                       [_I])
     L.mbx_water_step_device.argtypes = [C.c_void_p, C.c_int, C.c_int, _D, C.c_int, C.c_int, _D] + \
         [C.c_void_p] * 19 + [_D]
     L.mbx_disp_list_builds.argtypes = [C.c_void_p]
@@ -363,6 +366,47 @@ class Context:
             self._check(rc, "mbx_water_step")
         return dict(status=rc, forces=f.T.copy(), atomic_energy=ae, chge=q, scalars=sc, dipoles=dip.T.copy(),
                     sites=np.stack([x, y, z], 1))
+
+    def set_lanes(self, lanes):
+        self._check(self.lib.mbx_set_lanes(self.h, int(lanes)), "mbx_set_lanes")
+
+    def water_step_multi(self, boxes, polar_prms, precision=MIXED, dip0=None, disp=None, heat=True, check=True):
+        """mbx_water_step_multi on a list of WaterBoxes (standard layout), polar_prms one
+        15-vector per box; dip0 (sites x 3, all boxes concatenated) or None; disp = (ltype,
+        mol) concatenated, after disp_setup.  Returns a dict with per-box scalars and status."""
+        nb = len(boxes)
+        nws = np.array([b.nw for b in boxes], np.int32)
+        imc = np.array([b.imcon for b in boxes], np.int32)
+        cells = np.concatenate([_f64(b.cell) for b in boxes]) if nb else np.zeros(9)
+        prm = np.ascontiguousarray(np.concatenate([_f64(p) for p in polar_prms]) if nb else np.zeros(15))
+        xyz = np.concatenate([b.xyz for b in boxes]) if nb else np.zeros((0, 3))
+        n = xyz.shape[0]
+        x, y, z = (np.ascontiguousarray(xyz[:, k], np.float64).copy() for k in range(3))
+        dip = np.zeros((3, n)) if dip0 is None else np.ascontiguousarray(np.asarray(dip0, np.float64).T).copy()
+        f = np.zeros((3, n))
+        ae = np.zeros(n)
+        q = np.zeros(n)
+        sc = np.zeros((max(nb, 1), NSTEPSCALARS))
+        st = np.zeros(max(nb, 1), np.int32)
+        pol = [systems_polarizabilities(b.nw) for b in boxes]
+        polr = np.concatenate([p[0] for p in pol]) if nb else np.zeros(1)
+        polr2 = np.concatenate([p[1] for p in pol]) if nb else np.zeros(1)
+        if heat and nb:
+            vel = np.concatenate([b.vel for b in boxes])
+            v = [np.ascontiguousarray(vel[:, k], np.float64) for k in range(3)]
+            m = np.ascontiguousarray(np.concatenate([b.mass for b in boxes]), np.float64)
+        else:
+            v, m = [None] * 3, None
+        lt, mo = (None, None) if disp is None or not nb else (np.ascontiguousarray(disp[0], np.int32),
+                                                              np.ascontiguousarray(disp[1], np.int32))
+        rc = self.lib.mbx_water_step_multi(self.h, precision, nb, _p(imc, _I), _p(cells), _p(nws, _I), _p(prm),
+                                           _p(polr), _p(polr2), _p(lt, _I), _p(mo, _I), _p(x), _p(y), _p(z),
+                                           _p(dip[0]), _p(dip[1]), _p(dip[2]), _p(f[0]), _p(f[1]), _p(f[2]),
+                                           _p(v[0]), _p(v[1]), _p(v[2]), _p(m), _p(ae), _p(q), _p(sc), _p(st, _I))
+        if check:
+            self._check(rc, "mbx_water_step_multi")
+        return dict(status=rc, box_status=st[:nb].copy(), forces=f.T.copy(), atomic_energy=ae, chge=q,
+                    scalars=sc[:nb].copy(), dipoles=dip.T.copy(), sites=np.stack([x, y, z], 1))
 
     def polar_iterations(self):
         return int(self.lib.mbx_polar_iterations(self.h))

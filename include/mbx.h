@@ -273,6 +273,33 @@ int mbx_water_step_device(mbx_context* ctx, int precision, int imcon, const doub
                           double* scalars);
 
 /*
+ * Whole force evaluations (as mbx_water_step) of many independent boxes in one host call:
+ * path-integral beads, or separate simulations of any sizes.  The boxes run concurrently
+ * on the context's worker lanes (mbx_set_lanes, default 8): each lane is a child context
+ * with its own CUDA stream and device buffers, kept between calls, and one host thread
+ * for the call; boxes are handed out largest first.  Box b's results are those of
+ * mbx_water_step on its slice.  The reference gives each bead its own MPI group
+ * (SOURCE/multibead.f90:75-84), which runs one force evaluation per step
+ * (SOURCE/dlpoly_cmd.f:2287, :2504).
+ *   nbox; imcon[nbox], cell[9*nbox], nw[nbox]; box b has 4*nw[b] sites (standard layout)
+ *        stored from offset sum_{c<b} 4*nw[c] in every per-site array below
+ *   polar_prm[15*nbox]  per box (kmax follows the box size)
+ *   polr, polr2, ltype, molecule, xxx.., dip*, f*, v*, weight, atomic_energy, chge
+ *        as mbx_water_step, concatenated over the boxes (ltype/molecule NULL: no
+ *        dispersion; its setup is the one of mbx_disp_setup on this context)
+ *   scalars[MBX_NSTEPSCALARS*nbox]  per box; status[nbox] per box, or NULL
+ * Returns the first failing box's error, else MBX_ERR_CONVERGE when a box's dipoles did
+ * not converge (everything written), else MBX_OK.
+ */
+int mbx_set_lanes(mbx_context* ctx, int lanes);
+int mbx_water_step_multi(mbx_context* ctx, int precision, int nbox, const int* imcon, const double* cell,
+                         const int* nw, const double* polar_prm, const double* polr, const double* polr2,
+                         const int* ltype, const int* molecule, double* xxx, double* yyy, double* zzz, double* dipx,
+                         double* dipy, double* dipz, double* fxx, double* fyy, double* fzz, const double* vxx,
+                         const double* vyy, const double* vzz, const double* weight, double* atomic_energy,
+                         double* chge, double* scalars, int* status);
+
+/*
  * Continuous-batching force server.  `slots` worker slots, each with its own context and
  * CUDA stream on `device`, evaluate independent water boxes concurrently; a FIFO queue
  * admits the next request as soon as a slot is free and its estimated device-memory
