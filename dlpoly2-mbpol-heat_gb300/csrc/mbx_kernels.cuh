@@ -186,14 +186,18 @@ struct PolarState {
     double4* md = nullptr;                 // dipoles of the polarizable sites
     double* vh = nullptr;                  // per-site products of the ew1p heat sums (12 per site)
     double* kco = nullptr;                 // per-k coefficients of the gathers
-    // mixed precision: FP32 tensors, phase table and correction solve
+    // mixed precision: FP32 tensors, axis factors and correction solve
     float* tens32 = nullptr;
-    float2* eik32 = nullptr;
+    float2* fac32 = nullptr;               // FP32 copy of fac (the FP32 k-space passes form their phases)
+    int4* ktile = nullptr;                 // per 256 k vectors: first l, x rows, first m, y rows
+    std::vector<int4> hktile;
+    int ktile_cap = 0;
     float* kco32 = nullptr;
     float4 *r32 = nullptr, *d32 = nullptr, *cg_x = nullptr, *cg_r = nullptr, *cg_q = nullptr;
+    float4* vh32 = nullptr;                // FP32 heat weights of the final pass (3 per site)
     float* e32 = nullptr;
     int cap32 = 0, n32 = 0, k32 = 0;
-    size_t eik32_cap = 0;
+    size_t fac32_cap = 0;
     long inner_sweeps = 0;                 // FP32 conjugate-gradient iterations of the last call
     double* kpart = nullptr;               // per-chunk partial sums of the k-space gathers
     size_t part_cap = 0;
@@ -218,13 +222,13 @@ struct PolarState {
     void release();
     // device bytes held by the large buffers (phase tables, pair tensors)
     size_t held_bytes() const {
-        return eik_cap * sizeof(double2) + eik32_cap * sizeof(float2) + fac_cap * sizeof(double2) +
+        return eik_cap * sizeof(double2) + fac32_cap * sizeof(float2) + fac_cap * sizeof(double2) +
                (size_t)n_cap * cap_alloc * (6 * sizeof(double) + sizeof(int)) + (size_t)n32 * cap32 * 6 * sizeof(float) +
                part_cap * sizeof(double);
     }
     cudaError_t table(double alpha, double rcut, cudaStream_t s);
     cudaError_t reserve(int nw, int K, size_t nfac);
-    cudaError_t reserve_mixed(int n, int K);
+    cudaError_t reserve_mixed(int n, int K, size_t nfac);
     cudaError_t reserve_part(size_t ndouble);
     // One evaluation on device arrays (precision MBX_FP64 or MBX_MIXED: the dipole
     // equations solved by FP32 corrections under FP64 refinement).  prm[15] as

@@ -28,6 +28,8 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <mutex>
+#include <set>
 #include <vector>
 
 namespace mbx {
@@ -408,7 +410,8 @@ struct KArgs {
     const int4* lmn;
     double2* fac;          // per-site phase factors exp(2 pi i l s): x (l = 0..kmax1), y, z (-kmax..kmax)
     double2* eik;          // exp(ik.r) [k * n + j] = (cos, sin)
-    float2* eik32;         // the same in FP32 (mixed precision), or null
+    float2* fac32;         // the per-site axis factors in FP32 (mixed precision), or null
+    const int4* ktile;     // per kSfThreads k vectors: first l, x rows, first m, y rows (FP32 structure factors)
     float* kco32;          // 16 per k: the CG gather's kx, ky, kz, akk k.Ds, akk k.Dc, then the FP32 force gather's
     double* sf;            // 8 per k: ckcs, ckss, Mc(3), Ms(3)
     double* kco;           // 16 per k: coefficients of the gathers
@@ -440,6 +443,7 @@ __global__ void k_pol_factors(KArgs k, const double* __restrict__ x, const doubl
             double sn, cs;
             sincospi(2.0 * (t - rint(t)), &sn, &cs);
             k.fac[(size_t)(off + l - lo) * k.n + j] = make_double2(cs, sn);
+            if (k.fac32) k.fac32[(size_t)(off + l - lo) * k.n + j] = make_float2((float)cs, (float)sn);
         }
         off += k.kmax[ax] - lo + 1;
     }
@@ -456,7 +460,6 @@ __global__ void k_pol_phase(KArgs k) {
     const double2 fz = k.fac[(size_t)(oz + v.z + k.kmax[2]) * k.n + j];
     const double2 e = cmul(cmul(fx, fy), fz);
     k.eik[(size_t)kk * k.n + j] = e;
-    if (k.eik32) k.eik32[(size_t)kk * k.n + j] = make_float2((float)e.x, (float)e.y);
 }
 
 template <int NV>
@@ -527,42 +530,11 @@ __global__ void __launch_bounds__(kSfThreads) k_pol_sfd(KArgs k) {
     }
 }
 
-// Final structure factors (dipoles, and with velocities the 24 sums of the ew1p
-// per-atom stress contraction), the k vector's energy, virial and heat-current terms
+// Per k vector, from its 6 (NV = 6) or 30 (NV = 30, with velocities) structure-factor sums:
+// the final dipole structure factors, the k vector's energy, virial and heat-current terms
 // (SOURCE/ewald1p.f:575-733) and the coefficients of the force gather.
 template <int HEAT>
-__global__ void __launch_bounds__(kSfThreads) k_pol_sf_final(KArgs k) {
-    constexpr int NV = HEAT ? 30 : 6;
-    const int kk = blockIdx.x;
-    const double2* e = k.eik + (size_t)kk * k.n;
-    double v[NV];
-#pragma unroll
-    for (int q = 0; q < NV; ++q) v[q] = 0.0;
-    for (int j = threadIdx.x; j < k.n; j += kSfThreads) {
-        const double2 cs = e[j];
-        const double4 m = k.md[j];
-        v[0] += cs.x * m.x; v[1] += cs.x * m.y; v[2] += cs.x * m.z;
-        v[3] += cs.y * m.x; v[4] += cs.y * m.y; v[5] += cs.y * m.z;
-        if (HEAT) {
-            // per-site products q v (3) and mu_c v_b (9), rows of k.vh
-#pragma unroll
-            for (int b = 0; b < 3; ++b) {
-                const double qv = k.vh[(size_t)b * k.n + j];
-                v[6 + b] += cs.x * qv;    // V1
-                v[9 + b] += cs.y * qv;    // V2
-            }
-#pragma unroll
-            for (int cb = 0; cb < 9; ++cb) {
-                const double mv = k.vh[(size_t)(3 + cb) * k.n + j];
-                v[12 + cb] += cs.x * mv;   // W1[c][b]
-                v[21 + cb] += cs.y * mv;   // W2[c][b]
-            }
-        }
-    }
-    __shared__ double tot[NV];
-    block_reduce_store<NV>(v, tot);
-    __syncthreads();
-    if (threadIdx.x != 0) return;
+__device__ __forceinline__ void final_k(const KArgs& k, int kk, const double* tot) {
     double* sf = k.sf + 8 * (size_t)kk;
     for (int c = 0; c < 6; ++c) sf[2 + c] = tot[c];
     const double4 kv = k.kv[kk];
@@ -620,6 +592,44 @@ __global__ void __launch_bounds__(kSfThreads) k_pol_sf_final(KArgs k) {
         float* f = k.kco32 + 16 * (size_t)kk;
         for (int q = 0; q < 9; ++q) f[q] = (float)c[q];
     }
+}
+
+// Final structure factors (dipoles, and with velocities the 24 sums of the ew1p
+// per-atom stress contraction), the k vector's energy, virial and heat-current terms
+// (SOURCE/ewald1p.f:575-733) and the coefficients of the force gather.
+template <int HEAT>
+__global__ void __launch_bounds__(kSfThreads) k_pol_sf_final(KArgs k) {
+    constexpr int NV = HEAT ? 30 : 6;
+    const int kk = blockIdx.x;
+    const double2* e = k.eik + (size_t)kk * k.n;
+    double v[NV];
+#pragma unroll
+    for (int q = 0; q < NV; ++q) v[q] = 0.0;
+    for (int j = threadIdx.x; j < k.n; j += kSfThreads) {
+        const double2 cs = e[j];
+        const double4 m = k.md[j];
+        v[0] += cs.x * m.x; v[1] += cs.x * m.y; v[2] += cs.x * m.z;
+        v[3] += cs.y * m.x; v[4] += cs.y * m.y; v[5] += cs.y * m.z;
+        if (HEAT) {
+            // per-site products q v (3) and mu_c v_b (9), rows of k.vh
+#pragma unroll
+            for (int b = 0; b < 3; ++b) {
+                const double qv = k.vh[(size_t)b * k.n + j];
+                v[6 + b] += cs.x * qv;    // V1
+                v[9 + b] += cs.y * qv;    // V2
+            }
+#pragma unroll
+            for (int cb = 0; cb < 9; ++cb) {
+                const double mv = k.vh[(size_t)(3 + cb) * k.n + j];
+                v[12 + cb] += cs.x * mv;   // W1[c][b]
+                v[21 + cb] += cs.y * mv;   // W2[c][b]
+            }
+        }
+    }
+    __shared__ double tot[NV];
+    block_reduce_store<NV>(v, tot);
+    __syncthreads();
+    if (threadIdx.x == 0) final_k<HEAT>(k, kk, tot);
 }
 
 // k-space fields per site (iflag 0): the dipole field and, in the first pass, the static
@@ -695,9 +705,11 @@ __global__ void __launch_bounds__(kThreads) k_pol_kfield_sum(KArgs k, PolArgs a,
 
 // iter (SOURCE/iter.f): SOR update of the dipoles; sum of squared changes and count;
 // refreshes the masked dipoles of the structure factors.
-__global__ void __launch_bounds__(kThreads) k_pol_iter(PolArgs a, double4* __restrict__ md) {
+// With dlt (mixed precision) the update of the masked dipoles is also written in FP32.
+__global__ void __launch_bounds__(kThreads) k_pol_iter(PolArgs a, double4* __restrict__ md, float4* __restrict__ dlt) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     double v[2] = {0, 0};
+    if (dlt && i < a.n) dlt[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     if (i < a.n && a.polr2[i] > a.toler) {
         const double oldfac = a.omega, fac = 1.0 - oldfac;
         double* m[3] = {a.mx + i, a.my + i, a.mz + i};
@@ -710,7 +722,13 @@ __global__ void __launch_bounds__(kThreads) k_pol_iter(PolArgs a, double4* __res
             nm[c] = nv;
             dd += (nv - o) * (nv - o);
         }
-        if (a.polr2[i] > 1e-6) md[i] = make_double4(nm[0], nm[1], nm[2], 0.0);
+        if (a.polr2[i] > 1e-6) {
+            if (dlt) {
+                const double4 o = md[i];
+                dlt[i] = make_float4((float)(nm[0] - o.x), (float)(nm[1] - o.y), (float)(nm[2] - o.z), 0.f);
+            }
+            md[i] = make_double4(nm[0], nm[1], nm[2], 0.0);
+        }
         v[0] = dd;
         v[1] = 1.0;
     }
@@ -787,72 +805,266 @@ __global__ void k_pol_dd32(PolArgs a, MixArgs m) {
         for (int c = 0; c < 3; ++c) m.e32[c * a.n + i] = e[c];
 }
 
-// FP32 dipole structure factors of the correction and the coefficients of its gather.
-__global__ void __launch_bounds__(kSfThreads) k_pol_sfd32(KArgs k, MixArgs m) {
-    const int kk = blockIdx.x;
-    const float2* e = k.eik32 + (size_t)kk * k.n;
-    float v[6] = {0, 0, 0, 0, 0, 0};
-    for (int j = threadIdx.x; j < k.n; j += kSfThreads) {
-        const float2 cs = e[j];
-        const float4 d = m.d32[j];
-        v[0] += cs.x * d.x; v[1] += cs.x * d.y; v[2] += cs.x * d.z;
-        v[3] += cs.y * d.x; v[4] += cs.y * d.y; v[5] += cs.y * d.z;
-    }
-    __shared__ float red[kSfThreads / 32][6];
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-#pragma unroll
-    for (int q = 0; q < 6; ++q) {
-        const float sq = warp_sum(v[q]);
-        if (lane == 0) red[w][q] = sq;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double t[6] = {0, 0, 0, 0, 0, 0};
-        for (int i = 0; i < kSfThreads / 32; ++i)
-            for (int q = 0; q < 6; ++q) t[q] += red[i][q];
-        const double4 kv = k.kv[kk];
-        float* c = k.kco32 + 16 * (size_t)kk;
-        c[0] = (float)kv.x; c[1] = (float)kv.y; c[2] = (float)kv.z;
-        c[3] = (float)(kv.w * (kv.x * t[3] + kv.y * t[4] + kv.z * t[5]));
-        c[4] = (float)(kv.w * (kv.x * t[0] + kv.y * t[1] + kv.z * t[2]));
+__device__ __forceinline__ float2 cmulf(float2 a, float2 b) {
+    return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+
+// Rows of the per-site axis factors: x rows l = 0..kmax1, then y rows m = -kmax2..kmax2,
+// then z rows n = -kmax3..kmax3 (each row n sites).
+__device__ __forceinline__ int row_y(const KArgs& k, int m) { return k.kmax[0] + 1 + k.kmax[1] + m; }
+__device__ __forceinline__ int row_z(const KArgs& k, int n) { return k.kmax[0] + 2 * k.kmax[1] + 2 + k.kmax[2] + n; }
+
+// FP32 dipole structure factors of the correction, phases formed on the fly:
+// exp(ik.r_j) = fx_l(j) fy_m(j) fz_n(j) from the FP32 axis factors.  One k vector per
+// thread (blockIdx.x: kSfThreads consecutive vectors), sites split over blockIdx.y.  The
+// block stages tiles of kSfTile sites in shared memory: the x and y rows its vectors use
+// (ktile), every z row, and d32.  Per k and site chunk: sum_j e_j (k.d_j), summed in FP32
+// within a tile and in FP64 across tiles; k_pol_sfd32_sum adds the chunks in order.
+constexpr int kSfTile = 64;
+constexpr int kMaxRows = 448;   // factor rows a tile of k vectors may use (kmax up to ~100)
+constexpr size_t kMaxDynSmem = 200 * 1024;   // dynamic shared memory of the FP32 k-space kernels
+
+// The factor rows used by the tile of k vectors `tl` (first l, x rows, first m, y rows,
+// then every z row): global row of each shared-memory row.
+__device__ __forceinline__ int tile_rows(const KArgs& k, int4 tl, int* grow) {
+    const int nz = 2 * k.kmax[2] + 1, nrow = tl.y + tl.w + nz;
+    for (int r = threadIdx.x; r < nrow; r += blockDim.x)
+        grow[r] = r < tl.y ? tl.x + r : (r < tl.y + tl.w ? row_y(k, tl.z + r - tl.y) : row_z(k, r - tl.y - tl.w - k.kmax[2]));
+    return nrow;
+}
+
+// kSfTile sites (from s0, ns of them real) of the rows grow[0..nrow), transposed:
+// fs[t * rowp + r] (rowp odd spreads the stores over the banks).
+__device__ __forceinline__ void stage_rows(const KArgs& k, const int* grow, int nrow, int rowp, int s0, int ns,
+                                           float2* fs) {
+    for (int idx = threadIdx.x; idx < nrow * kSfTile; idx += blockDim.x) {
+        const int r = idx / kSfTile, t = idx % kSfTile;
+        fs[t * rowp + r] = t < ns ? k.fac32[(size_t)grow[r] * k.n + s0 + t] : make_float2(0.f, 0.f);
     }
 }
 
-// FP32 k-space field of the correction: two sites per thread, k vectors split over
-// blockIdx.y; partial sums added in order by k_pol_kfield32_sum.
+__global__ void __launch_bounds__(kSfThreads) k_pol_sfd32(KArgs k, MixArgs m, int schunk, int rowp,
+                                                          double* __restrict__ part) {
+    extern __shared__ float4 sfd_smem[];
+    float4* ds = sfd_smem;                                   // [kSfTile]
+    float2* fs = reinterpret_cast<float2*>(sfd_smem + kSfTile);   // [kSfTile][rowp]
+    __shared__ int grow[kMaxRows];
+    const int kk = blockIdx.x * kSfThreads + threadIdx.x;
+    const int4 tl = k.ktile[blockIdx.x];                     // l0, x rows, m0, y rows
+    const int nrow = tile_rows(k, tl, grow);
+    int rl = 0, rm = 0, rn = 0;
+    float kx = 0.f, ky = 0.f, kz = 0.f;
+    if (kk < k.K) {
+        const int4 v = k.lmn[kk];
+        rl = v.x - tl.x;
+        rm = tl.y + v.y - tl.z;
+        rn = tl.y + tl.w + v.z + k.kmax[2];
+        const double4 kv = k.kv[kk];
+        kx = (float)kv.x;
+        ky = (float)kv.y;
+        kz = (float)kv.z;
+    }
+    const int sb = blockIdx.y * schunk, se = min(k.n, sb + schunk);
+    double ac = 0.0, as = 0.0;
+    for (int s0 = sb; s0 < se; s0 += kSfTile) {
+        const int ns = min(kSfTile, se - s0);
+        __syncthreads();
+        stage_rows(k, grow, nrow, rowp, s0, ns, fs);
+        for (int t = threadIdx.x; t < kSfTile; t += kSfThreads)
+            ds[t] = t < ns ? m.d32[s0 + t] : make_float4(0.f, 0.f, 0.f, 0.f);
+        __syncthreads();
+        float c = 0.f, sn = 0.f;
+#pragma unroll 8
+        for (int t = 0; t < kSfTile; ++t) {
+            const float2* f = fs + t * rowp;
+            const float2 e = cmulf(cmulf(f[rl], f[rm]), f[rn]);
+            const float4 d = ds[t];
+            const float pk = kx * d.x + ky * d.y + kz * d.z;
+            c += e.x * pk;
+            sn += e.y * pk;
+        }
+        ac += (double)c;
+        as += (double)sn;
+    }
+    if (kk < k.K) {
+        double* p = part + 2 * ((size_t)blockIdx.y * k.K + kk);
+        p[0] = ac;
+        p[1] = as;
+    }
+}
+
+// The site chunks of k_pol_sfd32 added in order; the coefficients of the FP32 gather.
+__global__ void __launch_bounds__(kThreads) k_pol_sfd32_sum(KArgs k, int nchunk, const double* __restrict__ part) {
+    const int kk = blockIdx.x * blockDim.x + threadIdx.x;
+    if (kk >= k.K) return;
+    double skc = 0.0, sks = 0.0;
+    for (int q = 0; q < nchunk; ++q) {
+        const double* p = part + 2 * ((size_t)q * k.K + kk);
+        skc += p[0];
+        sks += p[1];
+    }
+    const double4 kv = k.kv[kk];
+    float* c = k.kco32 + 16 * (size_t)kk;
+    c[0] = (float)kv.x; c[1] = (float)kv.y; c[2] = (float)kv.z;
+    c[3] = (float)(kv.w * sks);
+    c[4] = (float)(kv.w * skc);
+}
+
+// Mixed precision, final pass: the final dipoles differ from those of the last FP64
+// structure factors (k.sf) only by the last SOR update `dlt` (at the dipole tolerance), so
+// the final dipole structure factors are k.sf plus the FP32 structure factors of dlt.
+// With velocities the 24 sums of the ew1p per-atom stress contraction (weights q v_b and
+// mu_c v_b, FP32, 12 per site in vh32) come from the same pass.  One k vector per thread,
+// phases formed on the fly as in k_pol_sfd32; FP32 within a site tile, FP64 across tiles;
+// per site chunk NV sums, added in order by k_pol_sfx32_fin.
+template <int HEAT>
+__global__ void __launch_bounds__(kSfThreads, 2) k_pol_sfx32(KArgs k, const float4* __restrict__ dlt,
+                                                             const float4* __restrict__ vh32, int schunk, int rowp,
+                                                             double* __restrict__ part) {
+    constexpr int NV = HEAT ? 30 : 6;
+    constexpr int NW = HEAT ? 4 : 1;   // float4 per site: dlt, then the 12 heat weights
+    extern __shared__ float4 sfx_smem[];
+    __shared__ int grow[kMaxRows];
+    float4* ws = sfx_smem;                                       // [kSfTile][NW]
+    float2* fs = reinterpret_cast<float2*>(sfx_smem + kSfTile * NW);   // [kSfTile][rowp]
+    const int kk = blockIdx.x * kSfThreads + threadIdx.x;
+    const int4 tl = k.ktile[blockIdx.x];
+    const int nrow = tile_rows(k, tl, grow);
+    int rl = 0, rm = 0, rn = 0;
+    if (kk < k.K) {
+        const int4 v = k.lmn[kk];
+        rl = v.x - tl.x;
+        rm = tl.y + v.y - tl.z;
+        rn = tl.y + tl.w + v.z + k.kmax[2];
+    }
+    const int sb = blockIdx.y * schunk, se = min(k.n, sb + schunk);
+    double acc[NV];
+#pragma unroll
+    for (int q = 0; q < NV; ++q) acc[q] = 0.0;
+    for (int s0 = sb; s0 < se; s0 += kSfTile) {
+        const int ns = min(kSfTile, se - s0);
+        __syncthreads();
+        stage_rows(k, grow, nrow, rowp, s0, ns, fs);
+        for (int t = threadIdx.x; t < kSfTile * NW; t += kSfThreads) {
+            const int site = t / NW, w = t % NW;
+            float4 val = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (site < ns) val = w == 0 ? dlt[s0 + site] : vh32[3 * (size_t)(s0 + site) + w - 1];
+            ws[t] = val;
+        }
+        __syncthreads();
+        float v[NV];
+#pragma unroll
+        for (int q = 0; q < NV; ++q) v[q] = 0.f;
+#pragma unroll 2
+        for (int t = 0; t < kSfTile; ++t) {
+            const float2* f = fs + t * rowp;
+            const float2 e = cmulf(cmulf(f[rl], f[rm]), f[rn]);
+            const float4 d = ws[t * NW];
+            v[0] += e.x * d.x; v[1] += e.x * d.y; v[2] += e.x * d.z;
+            v[3] += e.y * d.x; v[4] += e.y * d.y; v[5] += e.y * d.z;
+            if (HEAT) {
+                const float4 w0 = ws[t * NW + 1], w1 = ws[t * NW + 2], w2 = ws[t * NW + 3];
+                const float w[12] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w, w2.x, w2.y, w2.z, w2.w};
+#pragma unroll
+                for (int b = 0; b < 3; ++b) {
+                    v[6 + b] += e.x * w[b];    // V1
+                    v[9 + b] += e.y * w[b];    // V2
+                }
+#pragma unroll
+                for (int cb = 0; cb < 9; ++cb) {
+                    v[12 + cb] += e.x * w[3 + cb];   // W1[c][b]
+                    v[21 + cb] += e.y * w[3 + cb];   // W2[c][b]
+                }
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < NV; ++q) acc[q] += (double)v[q];
+    }
+    if (kk < k.K) {
+        double* p = part + NV * ((size_t)blockIdx.y * k.K + kk);
+#pragma unroll
+        for (int q = 0; q < NV; ++q) p[q] = acc[q];
+    }
+}
+
+template <int HEAT>
+__global__ void __launch_bounds__(kThreads) k_pol_sfx32_fin(KArgs k, int nchunk, const double* __restrict__ part) {
+    constexpr int NV = HEAT ? 30 : 6;
+    const int kk = blockIdx.x * blockDim.x + threadIdx.x;
+    if (kk >= k.K) return;
+    double tot[NV];
+    for (int q = 0; q < NV; ++q) tot[q] = 0.0;
+    for (int c = 0; c < nchunk; ++c) {
+        const double* p = part + NV * ((size_t)c * k.K + kk);
+        for (int q = 0; q < NV; ++q) tot[q] += p[q];
+    }
+    const double* sf = k.sf + 8 * (size_t)kk;
+    for (int q = 0; q < 6; ++q) tot[q] = sf[2 + q] + tot[q];
+    final_k<HEAT>(k, kk, tot);
+}
+
+// Shared-memory bytes of the FP32 gathers: the z rows of the block's sites.
+inline size_t gather_smem(const int* kmax) { return (size_t)(2 * kmax[2] + 1) * kThreads * sizeof(float2); }
+
+// The per-site part of the FP32 gathers: the block's sites keep their z-row factors in
+// shared memory; fx fy are read (from L2) when the (l, m) column changes, which in
+// ewald1p's order happens every few dozen k vectors.
+struct GatherPhase {
+    const float2* fz;   // this thread's column of the staged z rows
+    const float2* fac32;
+    int n, j, cl = -1, cm = 0;
+    float2 fxy = make_float2(0.f, 0.f);
+    __device__ GatherPhase(const KArgs& k, float2* smem, int j_, bool in) : fac32(k.fac32), n(k.n), j(j_) {
+        const int nz = 2 * k.kmax[2] + 1;
+        for (int r = 0; r < nz; ++r)
+            smem[r * kThreads + threadIdx.x] = in ? k.fac32[(size_t)row_z(k, r - k.kmax[2]) * k.n + j] : make_float2(0.f, 0.f);
+        fz = smem + threadIdx.x + (size_t)k.kmax[2] * kThreads;
+    }
+    // exp(ik.r_j) for k = (l, m, nn); ry = row of fy_m
+    __device__ __forceinline__ float2 operator()(int l, int ry, int m, int nn, bool in) {
+        if (l != cl || m != cm) {   // uniform across the block
+            cl = l;
+            cm = m;
+            fxy = in ? cmulf(fac32[(size_t)l * n + j], fac32[(size_t)ry * n + j]) : make_float2(0.f, 0.f);
+        }
+        return cmulf(fxy, fz[nn * kThreads]);
+    }
+};
+
+// FP32 k-space field of the correction: one site per thread, k vectors split over
+// blockIdx.y; each tile of kKTile vectors summed in FP32, the tiles in FP64; the partial
+// sums of the chunks added in order by k_pol_kfield32_sum.
 __global__ void __launch_bounds__(kThreads) k_pol_kfield32(KArgs k, int kchunk, float* __restrict__ part) {
-    __shared__ float sh[kKTile][8];
-    const int j0 = blockIdx.x * 2 * blockDim.x + threadIdx.x, j1 = j0 + blockDim.x;
+    extern __shared__ float2 gat_smem[];
+    __shared__ float sh[kKTile][5];
+    __shared__ int4 sl[kKTile];   // l, row of fy_m, m, n
+    const int j = blockIdx.x * kThreads + threadIdx.x;
+    const bool in = j < k.n;
+    GatherPhase ph(k, gat_smem, j, in);
     const int kb = blockIdx.y * kchunk, ke = min(k.K, kb + kchunk);
-    float e0[3] = {0, 0, 0}, e1[3] = {0, 0, 0};
+    double ed[3] = {0, 0, 0};
     for (int t0 = kb; t0 < ke; t0 += kKTile) {
         const int nt = min(kKTile, ke - t0);
         __syncthreads();
-        for (int u = threadIdx.x; u < nt * 8; u += blockDim.x) sh[u >> 3][u & 7] = k.kco32[16 * (size_t)(t0 + (u >> 3)) + (u & 7)];
-        __syncthreads();
-        const float2* e = k.eik32 + (size_t)t0 * k.n;
-        if (j1 < k.n) {
-#pragma unroll 4
-            for (int u = 0; u < nt; ++u) {
-                const float* c = sh[u];
-                const float2 a0 = e[(size_t)u * k.n + j0], a1 = e[(size_t)u * k.n + j1];
-                const float v0 = a0.y * c[3] + a0.x * c[4], v1 = a1.y * c[3] + a1.x * c[4];
-                e0[0] -= c[0] * v0; e0[1] -= c[1] * v0; e0[2] -= c[2] * v0;
-                e1[0] -= c[0] * v1; e1[1] -= c[1] * v1; e1[2] -= c[2] * v1;
-            }
-        } else if (j0 < k.n) {
-            for (int u = 0; u < nt; ++u) {
-                const float* c = sh[u];
-                const float2 a0 = e[(size_t)u * k.n + j0];
-                const float v0 = a0.y * c[3] + a0.x * c[4];
-                e0[0] -= c[0] * v0; e0[1] -= c[1] * v0; e0[2] -= c[2] * v0;
-            }
+        for (int u = threadIdx.x; u < nt * 5; u += blockDim.x) sh[u / 5][u % 5] = k.kco32[16 * (size_t)(t0 + u / 5) + u % 5];
+        for (int u = threadIdx.x; u < nt; u += blockDim.x) {
+            const int4 v = k.lmn[t0 + u];
+            sl[u] = make_int4(v.x, row_y(k, v.y), v.y, v.z);
         }
+        __syncthreads();
+        float e[3] = {0, 0, 0};
+        for (int u = 0; u < nt; ++u) {
+            const float* c = sh[u];
+            const int4 v = sl[u];
+            const float2 a = ph(v.x, v.y, v.z, v.w, in);
+            const float w = a.y * c[3] + a.x * c[4];
+            e[0] -= c[0] * w; e[1] -= c[1] * w; e[2] -= c[2] * w;
+        }
+        for (int c = 0; c < 3; ++c) ed[c] += (double)e[c];
     }
-    float* p = part + (size_t)blockIdx.y * 3 * k.n;
-    for (int c = 0; c < 3; ++c) {
-        if (j0 < k.n) p[c * (size_t)k.n + j0] = e0[c];
-        if (j1 < k.n) p[c * (size_t)k.n + j1] = e1[c];
+    if (in) {
+        float* p = part + (size_t)blockIdx.y * 3 * k.n;
+        for (int c = 0; c < 3; ++c) p[c * (size_t)k.n + j] = (float)ed[c];
     }
 }
 
@@ -997,39 +1209,41 @@ __global__ void __launch_bounds__(kThreads) k_pol_kforce(KArgs k, PolArgs a, int
     }
 }
 
-// The same in FP32 (mixed precision): FP32 phases and coefficients, each tile of kKTile k
-// vectors summed in FP32 and the tiles added in FP64.
+// The same in FP32 (mixed precision): FP32 coefficients and phases formed on the fly from
+// the FP32 axis factors (one site per thread), each tile of kKTile k vectors summed in FP32
+// and the tiles added in FP64.
 __global__ void __launch_bounds__(kThreads) k_pol_kforce32(KArgs k, PolArgs a, int kchunk, double* __restrict__ part) {
+    extern __shared__ float2 gat_smem[];
     __shared__ float sh[kKTile][9];
-    const int j0 = blockIdx.x * 2 * blockDim.x + threadIdx.x, j1 = j0 + blockDim.x;
+    __shared__ int4 sl[kKTile];
+    const int j = blockIdx.x * kThreads + threadIdx.x;
+    const bool in = j < k.n;
+    GatherPhase ph(k, gat_smem, j, in);
     const int kb = blockIdx.y * kchunk, ke = min(k.K, kb + kchunk);
-    const bool in0 = j0 < k.n, in1 = j1 < k.n;
-    const float q0 = in0 ? (float)a.q[j0] : 0.f, q1 = in1 ? (float)a.q[j1] : 0.f;
-    const bool p0 = in0 && a.polr2[j0] > 1e-6, p1 = in1 && a.polr2[j1] > 1e-6;
-    const float d0[3] = {in0 ? (float)a.mx[j0] : 0.f, in0 ? (float)a.my[j0] : 0.f, in0 ? (float)a.mz[j0] : 0.f};
-    const float d1[3] = {in1 ? (float)a.mx[j1] : 0.f, in1 ? (float)a.my[j1] : 0.f, in1 ? (float)a.mz[j1] : 0.f};
-    double acc0[5] = {0, 0, 0, 0, 0}, acc1[5] = {0, 0, 0, 0, 0};
+    const float qj = in ? (float)a.q[j] : 0.f;
+    const bool pj = in && a.polr2[j] > 1e-6;
+    const float dj[3] = {in ? (float)a.mx[j] : 0.f, in ? (float)a.my[j] : 0.f, in ? (float)a.mz[j] : 0.f};
+    double acc[5] = {0, 0, 0, 0, 0};
     for (int t0 = kb; t0 < ke; t0 += kKTile) {
         const int nt = min(kKTile, ke - t0);
         __syncthreads();
         for (int u = threadIdx.x; u < nt * 9; u += blockDim.x)
             sh[u / 9][u % 9] = k.kco32[16 * (size_t)(t0 + u / 9) + u % 9];
+        for (int u = threadIdx.x; u < nt; u += blockDim.x) {
+            const int4 v = k.lmn[t0 + u];
+            sl[u] = make_int4(v.x, row_y(k, v.y), v.y, v.z);
+        }
         __syncthreads();
-        float f0[5] = {0, 0, 0, 0, 0}, f1[5] = {0, 0, 0, 0, 0};
-        const float2* e = k.eik32 + (size_t)t0 * k.n;
-        for (int u = 0; u < nt; ++u, e += k.n) {
-            if (in0) kforce_site<float, float2>(sh[u], e[j0], q0, d0, p0, f0);
-            if (in1) kforce_site<float, float2>(sh[u], e[j1], q1, d1, p1, f1);
+        float f[5] = {0, 0, 0, 0, 0};
+        for (int u = 0; u < nt; ++u) {
+            const int4 v = sl[u];
+            kforce_site<float, float2>(sh[u], ph(v.x, v.y, v.z, v.w, in), qj, dj, pj, f);
         }
-        for (int c = 0; c < 5; ++c) {
-            acc0[c] += (double)f0[c];
-            acc1[c] += (double)f1[c];
-        }
+        for (int c = 0; c < 5; ++c) acc[c] += (double)f[c];
     }
-    double* p = part + (size_t)blockIdx.y * 5 * k.n;
-    for (int c = 0; c < 5; ++c) {
-        if (in0) p[c * (size_t)k.n + j0] = acc0[c];
-        if (in1) p[c * (size_t)k.n + j1] = acc1[c];
+    if (in) {
+        double* p = part + (size_t)blockIdx.y * 5 * k.n;
+        for (int c = 0; c < 5; ++c) p[c * (size_t)k.n + j] = acc[c];
     }
 }
 
@@ -1405,7 +1619,9 @@ __global__ void k_pol_kreduce(int K, const double* __restrict__ kterm, double* _
 
 // Per-site products of the ew1p heat sums, with v the velocity each site's terms are
 // carried with: q v (3 rows), then mu_c v_b (9 rows, c major), mu the masked dipole.
-__global__ void k_pol_vhat(PolArgs a, const double4* __restrict__ md, double* __restrict__ vh) {
+// vh (FP64, 12 blocks of n) or vh32 (FP32, 12 per site as 3 float4): q v_b, mu_c v_b.
+__global__ void k_pol_vhat(PolArgs a, const double4* __restrict__ md, double* __restrict__ vh,
+                           float4* __restrict__ vh32) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= a.n) return;
     double v[3];
@@ -1413,9 +1629,15 @@ __global__ void k_pol_vhat(PolArgs a, const double4* __restrict__ md, double* __
     const double q = a.q[j];
     const double4 m = md[j];
     const double mu[3] = {m.x, m.y, m.z};
-    for (int b = 0; b < 3; ++b) vh[(size_t)b * a.n + j] = q * v[b];
+    double w[12];
+    for (int b = 0; b < 3; ++b) w[b] = q * v[b];
     for (int c = 0; c < 3; ++c)
-        for (int b = 0; b < 3; ++b) vh[(size_t)(3 + 3 * c + b) * a.n + j] = mu[c] * v[b];
+        for (int b = 0; b < 3; ++b) w[3 + 3 * c + b] = mu[c] * v[b];
+    if (vh)
+        for (int q_ = 0; q_ < 12; ++q_) vh[(size_t)q_ * a.n + j] = w[q_];
+    if (vh32)
+        for (int u = 0; u < 3; ++u)
+            vh32[3 * (size_t)j + u] = make_float4((float)w[4 * u], (float)w[4 * u + 1], (float)w[4 * u + 2], (float)w[4 * u + 3]);
 }
 
 inline unsigned blocks(long n, int t) { return (unsigned)((n + t - 1) / t); }
@@ -1456,7 +1678,7 @@ cudaError_t launch_msite_redistribute(int nw, double gamma, double* fx, double* 
 
 void PolarState::release() {
     void* p[] = {ercp, nn, nbr, flag, xf, tens, intra, fld, vesp, ae, eik, kv, kx2, lmn, sf, kterm, acc, kco, fac, md, vh,
-                 tens32, r32, d32, e32, kco32, eik32, kpart, cg_x, cg_r, cg_q};
+                 tens32, r32, d32, e32, kco32, fac32, ktile, kpart, cg_x, cg_r, cg_q, vh32};
     for (void* q : p)
         if (q) cudaFree(q);
     if (acc_h) cudaFreeHost(acc_h);
@@ -1473,10 +1695,12 @@ void PolarState::release() {
     md = nullptr;
     fac_cap = 0;
     tens32 = e32 = kco32 = nullptr;
-    r32 = d32 = cg_x = cg_r = cg_q = nullptr;
-    eik32 = nullptr;
+    r32 = d32 = cg_x = cg_r = cg_q = vh32 = nullptr;
+    fac32 = nullptr;
+    ktile = nullptr;
+    ktile_cap = 0;
     cap32 = n32 = k32 = 0;
-    eik32_cap = 0;
+    fac32_cap = 0;
     kpart = nullptr;
     part_cap = 0;
     kv = nullptr;
@@ -1531,14 +1755,14 @@ cudaError_t PolarState::reserve_part(size_t nd) {
     return e;
 }
 
-cudaError_t PolarState::reserve_mixed(int n, int K) {
+cudaError_t PolarState::reserve_mixed(int n, int K, size_t nfac) {
     cudaError_t e;
     if (!tens32 || cap32 != cap || n > n32) {
-        void* p[] = {tens32, r32, d32, e32, cg_x, cg_r, cg_q};
+        void* p[] = {tens32, r32, d32, e32, cg_x, cg_r, cg_q, vh32};
         for (void* q : p)
             if (q) cudaFree(q);
         tens32 = e32 = nullptr;
-        r32 = d32 = cg_x = cg_r = cg_q = nullptr;
+        r32 = d32 = cg_x = cg_r = cg_q = vh32 = nullptr;
         cap32 = n32 = 0;
         const size_t m = (size_t)std::max(n, 1);
         if ((e = cudaMalloc(&tens32, 6 * m * cap * sizeof(float)))) return e;
@@ -1548,6 +1772,7 @@ cudaError_t PolarState::reserve_mixed(int n, int K) {
         if ((e = cudaMalloc(&cg_x, m * sizeof(float4)))) return e;
         if ((e = cudaMalloc(&cg_r, m * sizeof(float4)))) return e;
         if ((e = cudaMalloc(&cg_q, m * sizeof(float4)))) return e;
+        if ((e = cudaMalloc(&vh32, 3 * m * sizeof(float4)))) return e;
         cap32 = cap;
         n32 = n;
     }
@@ -1558,13 +1783,21 @@ cudaError_t PolarState::reserve_mixed(int n, int K) {
         if ((e = cudaMalloc(&kco32, 16 * (size_t)std::max(K, 1) * sizeof(float)))) return e;
         k32 = K;
     }
-    const size_t need = (size_t)K * n;
-    if (need > eik32_cap) {
-        if (eik32) cudaFree(eik32);
-        eik32 = nullptr;
-        eik32_cap = 0;
-        if ((e = cudaMalloc(&eik32, std::max(need, (size_t)1) * sizeof(float2)))) return e;
-        eik32_cap = need;
+    const size_t need = nfac * n;
+    if (need > fac32_cap) {
+        if (fac32) cudaFree(fac32);
+        fac32 = nullptr;
+        fac32_cap = 0;
+        if ((e = cudaMalloc(&fac32, std::max(need, (size_t)1) * sizeof(float2)))) return e;
+        fac32_cap = need;
+    }
+    const int nt = (K + kSfThreads - 1) / kSfThreads;
+    if (nt > ktile_cap) {
+        if (ktile) cudaFree(ktile);
+        ktile = nullptr;
+        ktile_cap = 0;
+        if ((e = cudaMalloc(&ktile, std::max(nt, 1) * sizeof(int4)))) return e;
+        ktile_cap = nt;
     }
     return cudaSuccess;
 }
@@ -1639,6 +1872,25 @@ cudaError_t PolarState::reserve(int nw, int K, size_t nfac) {
         if ((e = cudaMalloc(&fac, std::max(nfac * n, (size_t)1) * sizeof(double2)))) return e;
         fac_cap = nfac * n;
     }
+    return cudaSuccess;
+}
+
+// The dynamic shared-memory cap of the FP32 k-space kernels.  The attribute is process-wide
+// (per device), so it is raised once to a fixed bound rather than per call: contexts on other
+// threads launch the same kernels with their own sizes.
+static cudaError_t allow_dynamic_smem() {
+    static std::mutex mu;
+    static std::set<int> done;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e) return e;
+    std::lock_guard<std::mutex> lk(mu);
+    if (done.count(dev)) return cudaSuccess;
+    const void* f[] = {(const void*)k_pol_sfd32, (const void*)k_pol_sfx32<0>, (const void*)k_pol_sfx32<1>,
+                       (const void*)k_pol_kfield32, (const void*)k_pol_kforce32};
+    for (const void* q : f)
+        if ((e = cudaFuncSetAttribute(q, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxDynSmem))) return e;
+    done.insert(dev);
     return cudaSuccess;
 }
 
@@ -1727,7 +1979,7 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
     if (n > 65535L * kThreads) return cudaErrorInvalidValue;
     const size_t nfac = (size_t)(kmax[0] + 1) + (2 * kmax[1] + 1) + (2 * kmax[2] + 1);
     if ((e = reserve(nw, K, nfac))) return e;
-    if (precision == 1 && (e = reserve_mixed(n, K))) return e;
+    if (precision == 1 && (e = reserve_mixed(n, K, nfac))) return e;
     if (K) {
         if ((e = cudaMemcpyAsync(kv, hk.data(), K * sizeof(double4), cudaMemcpyHostToDevice, s))) return e;
         if ((e = cudaMemcpyAsync(kx2, hk2.data(), K * sizeof(double2), cudaMemcpyHostToDevice, s))) return e;
@@ -1736,6 +1988,34 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
     const bool heat = vx && vy && vz;
     const bool mixed = precision == 1;
     inner_sweeps = 0;
+    // FP32 structure factors: per tile of kSfThreads k vectors the x and y factor rows it
+    // uses (k vectors come l-major, so a tile spans few l); the widest tile sizes the
+    // shared-memory rows (odd, so the transposed stores spread over the banks)
+    int rowp = 1;
+    const int nkt = (K + kSfThreads - 1) / kSfThreads;
+    if (mixed && K) {
+        hktile.resize(nkt);
+        for (int t = 0; t < nkt; ++t) {
+            const int b = t * kSfThreads, e_ = std::min(K, b + kSfThreads);
+            int m0 = hlmn[b].y, m1 = m0;
+            for (int q = b; q < e_; ++q) {
+                m0 = std::min(m0, hlmn[q].y);
+                m1 = std::max(m1, hlmn[q].y);
+            }
+            hktile[t] = make_int4(hlmn[b].x, hlmn[e_ - 1].x - hlmn[b].x + 1, m0, m1 - m0 + 1);
+            rowp = std::max(rowp, hktile[t].y + hktile[t].w + 2 * kmax[2] + 1);
+        }
+        rowp |= 1;
+        if ((e = cudaMemcpyAsync(ktile, hktile.data(), nkt * sizeof(int4), cudaMemcpyHostToDevice, s))) return e;
+    }
+    const size_t sfd_smem = kSfTile * (sizeof(float4) + (size_t)rowp * sizeof(float2));
+    const size_t sfx_smem0 = sfd_smem, sfx_smem1 = kSfTile * (4 * sizeof(float4) + (size_t)rowp * sizeof(float2));
+    const size_t gat_smem = gather_smem(kmax);
+    if (mixed && K) {
+        // the FP32 k-space passes keep their factor rows in shared memory (kmax up to ~100)
+        if (rowp > kMaxRows || sfx_smem1 > kMaxDynSmem || gat_smem > kMaxDynSmem) return cudaErrorInvalidValue;
+        if ((e = allow_dynamic_smem())) return e;
+    }
 
     PolArgs a;
     auto bind = [&](PolArgs& b) {
@@ -1781,7 +2061,8 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
         b.lmn = lmn;
         b.fac = fac;
         b.eik = eik;
-        b.eik32 = mixed ? eik32 : nullptr;
+        b.fac32 = mixed ? fac32 : nullptr;
+        b.ktile = mixed ? ktile : nullptr;
         b.kco32 = mixed ? kco32 : nullptr;
         b.sf = sf;
         b.kco = kco;
@@ -1826,7 +2107,7 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
         if (!fh) break;
         cap = std::min(2 * cap, std::max(n, 32));   // a row holds at most n - 1 sites
         if ((e = reserve(nw, K, nfac))) return e;
-        if (mixed && (e = reserve_mixed(n, K))) return e;
+        if (mixed && (e = reserve_mixed(n, K, nfac))) return e;
     }
     bind(a);
     bindk(k);
@@ -1854,7 +2135,11 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
     int kc2, nc2, kc1, nc1;
     chunking(sblk2, kc2, nc2);
     chunking(sblk1, kc1, nc1);
-    if ((e = reserve_part((size_t)6 * std::max(nc1, nc2) * n))) return e;
+    // FP32 structure factors: site chunks so that the grid holds about four blocks per SM
+    const int nsc = nkt ? std::max(1, std::min((n + kSfTile - 1) / kSfTile, (4 * nsm + nkt - 1) / nkt)) : 1;
+    const int schunk = ((n + nsc - 1) / nsc + kSfTile - 1) / kSfTile * kSfTile;
+    const int nsc_used = (n + schunk - 1) / schunk;
+    if ((e = reserve_part(std::max((size_t)6 * std::max(nc1, nc2) * n, (size_t)30 * nsc_used * K)))) return e;
     auto fields64 = [&](bool first) {
         k_pol_dd<<<blocks(32L * n, kThreads), kThreads, 0, s>>>(a);
         if (K) {
@@ -1867,7 +2152,7 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
     auto sor64 = [&]() -> cudaError_t {   // iter, then read the rms change
         cudaError_t err;
         if ((err = cudaMemsetAsync(acc + 27, 0, 2 * sizeof(double), s))) return err;
-        k_pol_iter<<<blocks(n, kThreads), kThreads, 0, s>>>(a, md);
+        k_pol_iter<<<blocks(n, kThreads), kThreads, 0, s>>>(a, md, mixed ? d32 : nullptr);
         ++launches;
         if ((err = cudaMemcpyAsync(acc_h + 27, acc + 27, 2 * sizeof(double), cudaMemcpyDeviceToHost, s))) return err;
         if ((err = cudaStreamSynchronize(s))) return err;
@@ -1919,10 +2204,11 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
             for (int sweep = 0; sweep < 100; ++sweep) {
                 k_pol_dd32<<<blocks(32L * n, kThreads), kThreads, 0, s>>>(a, m);
                 if (K) {
-                    k_pol_sfd32<<<K, kSfThreads, 0, s>>>(k, m);
-                    k_pol_kfield32<<<dim3(sblk2, nc2), kThreads, 0, s>>>(k, kc2, (float*)kpart);
-                    k_pol_kfield32_sum<<<sblk1, kThreads, 0, s>>>(k, a, m, nc2, (const float*)kpart);
-                    launches += 3;
+                    k_pol_sfd32<<<dim3(nkt, nsc_used), kSfThreads, sfd_smem, s>>>(k, m, schunk, rowp, kpart);
+                    k_pol_sfd32_sum<<<blocks(K, kThreads), kThreads, 0, s>>>(k, nsc_used, kpart);
+                    k_pol_kfield32<<<dim3(sblk1, nc1), kThreads, gat_smem, s>>>(k, kc1, (float*)kpart);
+                    k_pol_kfield32_sum<<<sblk1, kThreads, 0, s>>>(k, a, m, nc1, (const float*)kpart);
+                    launches += 4;
                 }
                 k_pcg_ad<<<blocks(n, kThreads), kThreads, 0, s>>>(a, m, K ? 1 : 0);
                 k_pcg_step<<<blocks(n, kThreads), kThreads, 0, s>>>(a, m);
@@ -1944,22 +2230,34 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
     // final pass
     const double g34 = std::exp(gammln(3.0 / 4.0));
     if (heat) {
-        k_pol_vhat<<<blocks(n, kThreads), kThreads, 0, s>>>(a, md, vh);
+        k_pol_vhat<<<blocks(n, kThreads), kThreads, 0, s>>>(a, md, mixed ? nullptr : vh, mixed ? vh32 : nullptr);
         ++launches;
     }
     if (profiling && (e = cudaEventRecord(ev[2], s))) return e;
     if (K) {
-        if (heat) k_pol_sf_final<1><<<K, kSfThreads, 0, s>>>(k);
-        else k_pol_sf_final<0><<<K, kSfThreads, 0, s>>>(k);
-        ++launches;
+        if (mixed) {   // the last FP64 structure factors plus FP32 ones of the last update
+            const dim3 g(nkt, nsc_used);
+            if (heat) {
+                k_pol_sfx32<1><<<g, kSfThreads, sfx_smem1, s>>>(k, d32, vh32, schunk, rowp, kpart);
+                k_pol_sfx32_fin<1><<<blocks(K, kThreads), kThreads, 0, s>>>(k, nsc_used, kpart);
+            } else {
+                k_pol_sfx32<0><<<g, kSfThreads, sfx_smem0, s>>>(k, d32, vh32, schunk, rowp, kpart);
+                k_pol_sfx32_fin<0><<<blocks(K, kThreads), kThreads, 0, s>>>(k, nsc_used, kpart);
+            }
+            launches += 2;
+        } else {
+            if (heat) k_pol_sf_final<1><<<K, kSfThreads, 0, s>>>(k);
+            else k_pol_sf_final<0><<<K, kSfThreads, 0, s>>>(k);
+            ++launches;
+        }
     }
     if (profiling && (e = cudaEventRecord(ev[3], s))) return e;
     if (K) {
-        if (mixed) k_pol_kforce32<<<dim3(sblk2, nc2), kThreads, 0, s>>>(k, a, kc2, kpart);
+        if (mixed) k_pol_kforce32<<<dim3(sblk1, nc1), kThreads, gat_smem, s>>>(k, a, kc1, kpart);
         else k_pol_kforce<<<dim3(sblk2, nc2), kThreads, 0, s>>>(k, a, kc2, kpart);
         ++launches;
     }
-    k_pol_kforce_sum<<<sblk1, kThreads, 0, s>>>(k, a, nc2, kpart);
+    k_pol_kforce_sum<<<sblk1, kThreads, 0, s>>>(k, a, mixed ? nc1 : nc2, kpart);
     k_pol_ewald2p<<<blocks(32L * n, kThreads), kThreads, 0, s>>>(a, g34, heat);
     k_pol_ewald3p<<<blocks(nw, kThreads), kThreads, 0, s>>>(a, heat);
     k_pol_qdforce<<<blocks(nw, kThreads), kThreads, 0, s>>>(a, heat);
