@@ -1224,6 +1224,14 @@ extern "C" int mbx_water_step(mbx_context* ctx, int precision, int imcon, const 
 // context's worker lanes.  A lane is a child context (its own stream and device buffers,
 // kept between calls) driven by its own host thread for the call, so the boxes' kernels
 // and host round trips overlap; boxes are taken largest first from a shared counter.
+extern "C" int mbx_set_precond_sweeps(mbx_context* ctx, int sweeps) {
+    if (!ctx) return MBX_ERR_ARG;
+    if (sweeps < 1 || sweeps > 9 || sweeps % 2 == 0)
+        return fail(ctx, MBX_ERR_ARG, "preconditioner sweeps must be odd, 1..9");
+    ctx->polar.precond_sweeps = sweeps;
+    return MBX_OK;
+}
+
 extern "C" int mbx_set_lanes(mbx_context* ctx, int lanes) {
     if (!ctx) return MBX_ERR_ARG;
     if (lanes < 1 || lanes > 64) return fail(ctx, MBX_ERR_ARG, "lanes must be 1..64");
@@ -1265,6 +1273,7 @@ extern "C" int mbx_water_step_multi(mbx_context* ctx, int precision, int nbox, c
         c->limit2 = ctx->limit2;
         c->limit3 = ctx->limit3;
         c->fused = ctx->fused;
+        c->polar.precond_sweeps = ctx->polar.precond_sweeps;
         if (disp && c->disp_gen_seen != ctx->disp_gen) {
             const int rc = mbx_disp_setup(c, ctx->disp_ntypes, ctx->disp_prm_h.data(), ctx->disp_rcut, ctx->disp_delr,
                                           ctx->disp_mxgrid);

@@ -195,6 +195,8 @@ struct PolarState {
     float* kco32 = nullptr;
     float4 *r32 = nullptr, *d32 = nullptr, *cg_x = nullptr, *cg_r = nullptr, *cg_q = nullptr;
     float4* vh32 = nullptr;                // FP32 heat weights of the final pass (3 per site)
+    float4* cg_z = nullptr;                // preconditioned residual of the correction solve
+    int precond_sweeps = 3;                // Jacobi sweeps of the CG preconditioner (odd; 1: diagonal only)
     float* e32 = nullptr;
     int cap32 = 0, n32 = 0, k32 = 0;
     size_t fac32_cap = 0;

@@ -768,8 +768,8 @@ __global__ void __launch_bounds__(kThreads) k_pol_resid(PolArgs a, MixArgs m) {
     block_sum_atomic<2>(v, a.acc + 29);
 }
 
-// FP32 real-space dipole field of the correction (warp per site).
-__global__ void k_pol_dd32(PolArgs a, MixArgs m) {
+// FP32 real-space dipole field (warp per site) of `in`, written to `out` (3 blocks of n).
+__global__ void k_pol_dd32(PolArgs a, const float4* __restrict__ in, float* __restrict__ out) {
     const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (i >= a.n) return;
@@ -778,7 +778,7 @@ __global__ void k_pol_dd32(PolArgs a, MixArgs m) {
         const int nn = a.nn[i];
         const size_t row = (size_t)i * a.cap, blk = (size_t)a.n * a.cap;
         for (int k = lane; k < nn; k += 32) {
-            const float4 d = m.d32[a.nbr[row + k]];
+            const float4 d = in[a.nbr[row + k]];
             float t[6];
 #pragma unroll
             for (int p = 0; p < 6; ++p) t[p] = a.tens32[p * blk + row + k];
@@ -793,7 +793,7 @@ __global__ void k_pol_dd32(PolArgs a, MixArgs m) {
             const int pp[3][2] = {{0, 1}, {0, 2}, {1, 2}};
             const double* T = a.intra + 18 * (size_t)w;
             for (int u = 0; u < 2; ++u) {
-                const float4 d = m.d32[3 * w + pj[s][u]];
+                const float4 d = in[3 * w + pj[s][u]];
                 const double* t = T + 6 * pp[s][u];
                 e[0] += (float)t[0] * d.x + (float)t[1] * d.y + (float)t[2] * d.z;
                 e[1] += (float)t[1] * d.x + (float)t[3] * d.y + (float)t[4] * d.z;
@@ -802,7 +802,7 @@ __global__ void k_pol_dd32(PolArgs a, MixArgs m) {
         }
     }
     if (lane == 0)
-        for (int c = 0; c < 3; ++c) m.e32[c * a.n + i] = e[c];
+        for (int c = 0; c < 3; ++c) out[c * a.n + i] = e[c];
 }
 
 __device__ __forceinline__ float2 cmulf(float2 a, float2 b) {
@@ -1142,14 +1142,53 @@ __global__ void __launch_bounds__(kThreads) k_pcg_step(PolArgs a, MixArgs m) {
     block_sum_atomic<3>(v, a.acc + 35);
 }
 
-__global__ void __launch_bounds__(kThreads) k_pcg_dir(PolArgs a, MixArgs m) {
+// d = z + beta d, z = M^-1 rho: the diagonal (z null) or the polynomial preconditioner's z.
+__global__ void __launch_bounds__(kThreads) k_pcg_dir(PolArgs a, MixArgs m, const float4* __restrict__ z) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n || !(a.polr2[i] > a.toler)) return;
     const double rz = a.acc[33];
     const float b = rz != 0.0 ? (float)(a.acc[35] / rz) : 0.f;
-    const float w = (float)(a.polr2[i] / kR4pie0);
-    const float4 r = m.rho[i], d = m.d32[i];
-    m.d32[i] = make_float4(w * r.x + b * d.x, w * r.y + b * d.y, w * r.z + b * d.z, 0.f);
+    const float4 d = m.d32[i];
+    float4 zz;
+    if (z) {
+        zz = z[i];
+    } else {
+        const float w = (float)(a.polr2[i] / kR4pie0);
+        const float4 r = m.rho[i];
+        zz = make_float4(w * r.x, w * r.y, w * r.z, 0.f);
+    }
+    m.d32[i] = make_float4(zz.x + b * d.x, zz.y + b * d.y, zz.z + b * d.z, 0.f);
+}
+
+// Polynomial preconditioner: p Jacobi sweeps on the real-space part of the system,
+// (D - T_real) z = rho with D = r4pie0 / polr2, from z = 0:
+//   z <- D^-1 (rho + T_real z)   (t = T_real z; t null: the first sweep, z = D^-1 rho),
+// i.e. z = sum_{i<p} (D^-1 T_real)^i D^-1 rho, symmetric; positive definite for even p.
+__global__ void __launch_bounds__(kThreads) k_pcg_jacobi(PolArgs a, MixArgs m, const float* __restrict__ t,
+                                                         float4* __restrict__ z) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (a.polr2[i] > a.toler) {
+        const float w = (float)(a.polr2[i] / kR4pie0);
+        const float4 r = m.rho[i];
+        v = t ? make_float4(w * (r.x + t[i]), w * (r.y + t[(size_t)a.n + i]), w * (r.z + t[2 * (size_t)a.n + i]), 0.f)
+              : make_float4(w * r.x, w * r.y, w * r.z, 0.f);
+    }
+    z[i] = v;
+}
+
+// rho.z into acc[slot]; with `dir`, also d32 = z (the first direction).
+__global__ void __launch_bounds__(kThreads) k_pcg_rz(PolArgs a, MixArgs m, const float4* __restrict__ z, int slot,
+                                                     int dir) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double v[1] = {0};
+    if (i < a.n) {
+        const float4 r = m.rho[i], zz = z[i];
+        v[0] = (double)r.x * zz.x + (double)r.y * zz.y + (double)r.z * zz.z;
+        if (dir) m.d32[i] = zz;
+    }
+    block_sum_atomic<1>(v, a.acc + slot);
 }
 
 // mu += d in FP64; refreshes the masked dipoles.
@@ -1678,7 +1717,7 @@ cudaError_t launch_msite_redistribute(int nw, double gamma, double* fx, double* 
 
 void PolarState::release() {
     void* p[] = {ercp, nn, nbr, flag, xf, tens, intra, fld, vesp, ae, eik, kv, kx2, lmn, sf, kterm, acc, kco, fac, md, vh,
-                 tens32, r32, d32, e32, kco32, fac32, ktile, kpart, cg_x, cg_r, cg_q, vh32};
+                 tens32, r32, d32, e32, kco32, fac32, ktile, kpart, cg_x, cg_r, cg_q, cg_z, vh32};
     for (void* q : p)
         if (q) cudaFree(q);
     if (acc_h) cudaFreeHost(acc_h);
@@ -1695,7 +1734,7 @@ void PolarState::release() {
     md = nullptr;
     fac_cap = 0;
     tens32 = e32 = kco32 = nullptr;
-    r32 = d32 = cg_x = cg_r = cg_q = vh32 = nullptr;
+    r32 = d32 = cg_x = cg_r = cg_q = cg_z = vh32 = nullptr;
     fac32 = nullptr;
     ktile = nullptr;
     ktile_cap = 0;
@@ -1758,11 +1797,11 @@ cudaError_t PolarState::reserve_part(size_t nd) {
 cudaError_t PolarState::reserve_mixed(int n, int K, size_t nfac) {
     cudaError_t e;
     if (!tens32 || cap32 != cap || n > n32) {
-        void* p[] = {tens32, r32, d32, e32, cg_x, cg_r, cg_q, vh32};
+        void* p[] = {tens32, r32, d32, e32, cg_x, cg_r, cg_q, cg_z, vh32};
         for (void* q : p)
             if (q) cudaFree(q);
         tens32 = e32 = nullptr;
-        r32 = d32 = cg_x = cg_r = cg_q = vh32 = nullptr;
+        r32 = d32 = cg_x = cg_r = cg_q = cg_z = vh32 = nullptr;
         cap32 = n32 = 0;
         const size_t m = (size_t)std::max(n, 1);
         if ((e = cudaMalloc(&tens32, 6 * m * cap * sizeof(float)))) return e;
@@ -1773,6 +1812,7 @@ cudaError_t PolarState::reserve_mixed(int n, int K, size_t nfac) {
         if ((e = cudaMalloc(&cg_r, m * sizeof(float4)))) return e;
         if ((e = cudaMalloc(&cg_q, m * sizeof(float4)))) return e;
         if ((e = cudaMalloc(&vh32, 3 * m * sizeof(float4)))) return e;
+        if ((e = cudaMalloc(&cg_z, m * sizeof(float4)))) return e;
         cap32 = cap;
         n32 = n;
     }
@@ -2181,6 +2221,24 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
         m.rho = cg_r;
         m.q = cg_q;
         const double fac = 1.0 - prm[4];
+        // z = M^-1 rho into cg_z, rho.z into acc[slot] (and the first direction); `pre`
+        // Jacobi sweeps (odd: the polynomial is positive definite for every eigenvalue of
+        // D^-1 T_real below 1, which the dipole equations guarantee)
+        int pre = precond_sweeps | 1;
+        auto precondition = [&](int slot, int dir) -> cudaError_t {
+            k_pcg_jacobi<<<blocks(n, kThreads), kThreads, 0, s>>>(a, m, nullptr, cg_z);
+            for (int q = 1; q < pre; ++q) {
+                k_pol_dd32<<<blocks(32L * n, kThreads), kThreads, 0, s>>>(a, cg_z, e32 + 3 * (size_t)n);
+                k_pcg_jacobi<<<blocks(n, kThreads), kThreads, 0, s>>>(a, m, e32 + 3 * (size_t)n, cg_z);
+                launches += 2;
+            }
+            cudaError_t err;
+            if ((err = cudaMemsetAsync(acc + slot, 0, sizeof(double), s))) return err;
+            k_pcg_rz<<<blocks(n, kThreads), kThreads, 0, s>>>(a, m, cg_z, slot, dir);
+            launches += 2;
+            return cudaSuccess;
+        };
+        double rms_prev = HUGE_VAL;
         for (int it = 1;; ++it) {
             fields64(it == 1);
             if ((e = cudaMemsetAsync(acc + 29, 0, 2 * sizeof(double), s))) return e;
@@ -2195,36 +2253,65 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
                 converged = deltadip <= prm[3];
                 break;
             }
+            // an outer step that did not halve the FP64 residual: the diagonal preconditioner
+            // from here on
+            if (pre > 1 && !(rms <= 0.5 * rms_prev)) pre = 1;
+            rms_prev = rms;
             // |z| (the preconditioned residual of the correction, a dipole) down to
             // 1e-6 of the FP64 residual or 5x below toler
             const double target = std::max(1e-6 * rms, 0.2 * prm[3]);
-            if ((e = cudaMemsetAsync(acc + 33, 0, 5 * sizeof(double), s))) return e;
-            k_pcg_init<<<blocks(n, kThreads), kThreads, 0, s>>>(a, m);
-            ++launches;
-            for (int sweep = 0; sweep < 100; ++sweep) {
-                k_pol_dd32<<<blocks(32L * n, kThreads), kThreads, 0, s>>>(a, m);
-                if (K) {
-                    k_pol_sfd32<<<dim3(nkt, nsc_used), kSfThreads, sfd_smem, s>>>(k, m, schunk, rowp, kpart);
-                    k_pol_sfd32_sum<<<blocks(K, kThreads), kThreads, 0, s>>>(k, nsc_used, kpart);
-                    k_pol_kfield32<<<dim3(sblk1, nc1), kThreads, gat_smem, s>>>(k, kc1, (float*)kpart);
-                    k_pol_kfield32_sum<<<sblk1, kThreads, 0, s>>>(k, a, m, nc1, (const float*)kpart);
+            bool broke = false;
+            for (bool restart = true; restart;) {
+                restart = false;
+                broke = false;
+                if ((e = cudaMemsetAsync(acc + 33, 0, 5 * sizeof(double), s))) return e;
+                k_pcg_init<<<blocks(n, kThreads), kThreads, 0, s>>>(a, m);
+                ++launches;
+                const bool poly = pre > 1;
+                if (poly && (e = precondition(33, 1))) return e;
+                for (int sweep = 0; sweep < 100; ++sweep) {
+                    k_pol_dd32<<<blocks(32L * n, kThreads), kThreads, 0, s>>>(a, d32, e32);
+                    if (K) {
+                        k_pol_sfd32<<<dim3(nkt, nsc_used), kSfThreads, sfd_smem, s>>>(k, m, schunk, rowp, kpart);
+                        k_pol_sfd32_sum<<<blocks(K, kThreads), kThreads, 0, s>>>(k, nsc_used, kpart);
+                        k_pol_kfield32<<<dim3(sblk1, nc1), kThreads, gat_smem, s>>>(k, kc1, (float*)kpart);
+                        k_pol_kfield32_sum<<<sblk1, kThreads, 0, s>>>(k, a, m, nc1, (const float*)kpart);
+                        launches += 4;
+                    }
+                    k_pcg_ad<<<blocks(n, kThreads), kThreads, 0, s>>>(a, m, K ? 1 : 0);
+                    k_pcg_step<<<blocks(n, kThreads), kThreads, 0, s>>>(a, m);
+                    if (poly && (e = precondition(35, 0))) return e;
+                    k_pcg_dir<<<blocks(n, kThreads), kThreads, 0, s>>>(a, m, poly ? cg_z : nullptr);
                     launches += 4;
+                    ++inner_sweeps;
+                    if ((e = cudaMemcpyAsync(acc_h + 34, acc + 34, 4 * sizeof(double), cudaMemcpyDeviceToHost, s)))
+                        return e;
+                    // next iteration: rho.z <- new rho.z; clear the sums
+                    if ((e = cudaMemcpyAsync(acc + 33, acc + 35, sizeof(double), cudaMemcpyDeviceToDevice, s))) return e;
+                    if ((e = cudaMemsetAsync(acc + 34, 0, 4 * sizeof(double), s))) return e;
+                    if ((e = cudaStreamSynchronize(s))) return e;
+                    // d.Ad <= 0 (or a non-finite sum): the preconditioned operator is not
+                    // positive definite in FP32 here; the diagonal preconditioner takes over,
+                    // and with it an FP64 SOR step replaces this correction
+                    if (!(acc_h[34] > 0.0) || !std::isfinite(acc_h[35]) || !std::isfinite(acc_h[36])) {
+                        if (pre > 1) {
+                            pre = 1;
+                            restart = true;
+                        } else {
+                            broke = true;
+                        }
+                        break;
+                    }
+                    const double zr = std::sqrt(acc_h[36] / (acc_h[37] > 0.0 ? acc_h[37] : 1.0));
+                    if (zr <= target) break;
                 }
-                k_pcg_ad<<<blocks(n, kThreads), kThreads, 0, s>>>(a, m, K ? 1 : 0);
-                k_pcg_step<<<blocks(n, kThreads), kThreads, 0, s>>>(a, m);
-                k_pcg_dir<<<blocks(n, kThreads), kThreads, 0, s>>>(a, m);
-                launches += 4;
-                ++inner_sweeps;
-                if ((e = cudaMemcpyAsync(acc_h + 35, acc + 35, 3 * sizeof(double), cudaMemcpyDeviceToHost, s))) return e;
-                // next iteration: rho.z <- new rho.z; clear the sums
-                if ((e = cudaMemcpyAsync(acc + 33, acc + 35, sizeof(double), cudaMemcpyDeviceToDevice, s))) return e;
-                if ((e = cudaMemsetAsync(acc + 34, 0, 4 * sizeof(double), s))) return e;
-                if ((e = cudaStreamSynchronize(s))) return e;
-                const double zr = std::sqrt(acc_h[36] / (acc_h[37] > 0.0 ? acc_h[37] : 1.0));
-                if (zr <= target) break;
             }
-            k_pol_apply<<<blocks(n, kThreads), kThreads, 0, s>>>(a, m, md);
-            ++launches;
+            if (broke) {
+                if ((e = sor64())) return e;
+            } else {
+                k_pol_apply<<<blocks(n, kThreads), kThreads, 0, s>>>(a, m, md);
+                ++launches;
+            }
         }
     }
     // final pass

@@ -104,6 +104,7 @@ def load(path=None):
     L.mbx_msite_redistribute.argtypes = [C.c_int, C.c_double, _D, _D, _D]
     L.mbx_water_step.argtypes = [C.c_void_p, C.c_int, C.c_int, _D, C.c_int, C.c_int, _D, _D, _D, _I, _I] + [_D] * 16
     L.mbx_set_lanes.argtypes = [C.c_void_p, C.c_int]
+    L.mbx_set_precond_sweeps.argtypes = [C.c_void_p, C.c_int]
     L.mbx_water_step_multi.argtypes = ([C.c_void_p, C.c_int, C.c_int, _I, _D, _I, _D, _D, _D, _I, _I] + [_D] * 16 +
                                        [_I])
     L.mbx_water_step_device.argtypes = [C.c_void_p, C.c_int, C.c_int, _D, C.c_int, C.c_int, _D] + \
@@ -366,6 +367,9 @@ class Context:
             self._check(rc, "mbx_water_step")
         return dict(status=rc, forces=f.T.copy(), atomic_energy=ae, chge=q, scalars=sc, dipoles=dip.T.copy(),
                     sites=np.stack([x, y, z], 1))
+
+    def set_precond_sweeps(self, sweeps):
+        self._check(self.lib.mbx_set_precond_sweeps(self.h, int(sweeps)), "mbx_set_precond_sweeps")
 
     def set_lanes(self, lanes):
         self._check(self.lib.mbx_set_lanes(self.h, int(lanes)), "mbx_set_lanes")

@@ -292,6 +292,12 @@ int mbx_water_step_device(mbx_context* ctx, int precision, int imcon, const doub
  * not converge (everything written), else MBX_OK.
  */
 int mbx_set_lanes(mbx_context* ctx, int lanes);
+/* MBX_MIXED dipole solve: Jacobi sweeps of the conjugate-gradient preconditioner on the
+ * real-space part of the dipole equations, odd 1..9 (1: the diagonal alone; default 3).
+ * An odd count keeps the preconditioner positive definite; a breakdown or an outer step
+ * that does not halve the residual falls back to the diagonal.  Changes the iteration
+ * count, not the converged dipoles beyond the dipole tolerance. */
+int mbx_set_precond_sweeps(mbx_context* ctx, int sweeps);
 int mbx_water_step_multi(mbx_context* ctx, int precision, int nbox, const int* imcon, const double* cell,
                          const int* nw, const double* polar_prm, const double* polr, const double* polr2,
                          const int* ltype, const int* molecule, double* xxx, double* yyy, double* zzz, double* dipx,
