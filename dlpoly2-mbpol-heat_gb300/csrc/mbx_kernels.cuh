@@ -189,8 +189,11 @@ struct PolarState {
     // mixed precision: FP32 tensors, axis factors and correction solve
     float* tens32 = nullptr;
     float2* fac32 = nullptr;               // FP32 copy of fac (the FP32 k-space passes form their phases)
-    int4* ktile = nullptr;                 // per 256 k vectors: first l, x rows, first m, y rows
-    std::vector<int4> hktile;
+    int4* ktile = nullptr;                 // per 256 k vectors: first (l, m) column, columns
+    int4* kaux = nullptr;                  // per k: column in its tile, next column, column, z offset
+    int* kcol = nullptr;                   // per (l, m) column: l << 16 | y row
+    std::vector<int4> hktile, hkaux;
+    std::vector<int> hkcol;
     int ktile_cap = 0;
     float* kco32 = nullptr;
     float4 *r32 = nullptr, *d32 = nullptr, *cg_x = nullptr, *cg_r = nullptr, *cg_q = nullptr;

@@ -411,7 +411,9 @@ struct KArgs {
     double2* fac;          // per-site phase factors exp(2 pi i l s): x (l = 0..kmax1), y, z (-kmax..kmax)
     double2* eik;          // exp(ik.r) [k * n + j] = (cos, sin)
     float2* fac32;         // the per-site axis factors in FP32 (mixed precision), or null
-    const int4* ktile;     // per kSfThreads k vectors: first l, x rows, first m, y rows (FP32 structure factors)
+    const int4* ktile;     // per kSfThreads k vectors: first (l, m) column, columns (FP32 structure factors)
+    const int4* kaux;      // per k: column within its tile, next column (l << 16 | y row), column, z offset
+    const int* kcol;       // per (l, m) column: l << 16 | y row
     float* kco32;          // 16 per k: the CG gather's kx, ky, kz, akk k.Ds, akk k.Dc, then the FP32 force gather's
     double* sf;            // 8 per k: ckcs, ckss, Mc(3), Ms(3)
     double* kco;           // 16 per k: coefficients of the gathers
@@ -824,22 +826,24 @@ constexpr int kSfTile = 64;
 constexpr int kMaxRows = 448;   // factor rows a tile of k vectors may use (kmax up to ~100)
 constexpr size_t kMaxDynSmem = 200 * 1024;   // dynamic shared memory of the FP32 k-space kernels
 
-// The factor rows used by the tile of k vectors `tl` (first l, x rows, first m, y rows,
-// then every z row): global row of each shared-memory row.
-__device__ __forceinline__ int tile_rows(const KArgs& k, int4 tl, int* grow) {
-    const int nz = 2 * k.kmax[2] + 1, nrow = tl.y + tl.w + nz;
-    for (int r = threadIdx.x; r < nrow; r += blockDim.x)
-        grow[r] = r < tl.y ? tl.x + r : (r < tl.y + tl.w ? row_y(k, tl.z + r - tl.y) : row_z(k, r - tl.y - tl.w - k.kmax[2]));
-    return nrow;
-}
-
-// kSfTile sites (from s0, ns of them real) of the rows grow[0..nrow), transposed:
-// fs[t * rowp + r] (rowp odd spreads the stores over the banks).
-__device__ __forceinline__ void stage_rows(const KArgs& k, const int* grow, int nrow, int rowp, int s0, int ns,
-                                           float2* fs) {
+// kSfTile sites (from s0, ns of them real) of the tile's factor rows, transposed
+// (fs[t * rowp + r]; rowp odd spreads the stores over the banks): rows 0..ncol-1 the
+// products fx_l fy_m of the tile's (l, m) columns, then the z rows n = -kmax3..kmax3.
+__device__ __forceinline__ void stage_tile(const KArgs& k, int4 tl, int rowp, int s0, int ns, float2* fs) {
+    const int nrow = tl.y + 2 * k.kmax[2] + 1;
     for (int idx = threadIdx.x; idx < nrow * kSfTile; idx += blockDim.x) {
         const int r = idx / kSfTile, t = idx % kSfTile;
-        fs[t * rowp + r] = t < ns ? k.fac32[(size_t)grow[r] * k.n + s0 + t] : make_float2(0.f, 0.f);
+        float2 v = make_float2(0.f, 0.f);
+        if (t < ns) {
+            const size_t j = (size_t)s0 + t;
+            if (r < tl.y) {
+                const int c = k.kcol[tl.x + r];
+                v = cmulf(k.fac32[(size_t)(c >> 16) * k.n + j], k.fac32[(size_t)(c & 0xffff) * k.n + j]);
+            } else {
+                v = k.fac32[(size_t)row_z(k, r - tl.y - k.kmax[2]) * k.n + j];
+            }
+        }
+        fs[t * rowp + r] = v;
     }
 }
 
@@ -848,17 +852,13 @@ __global__ void __launch_bounds__(kSfThreads) k_pol_sfd32(KArgs k, MixArgs m, in
     extern __shared__ float4 sfd_smem[];
     float4* ds = sfd_smem;                                   // [kSfTile]
     float2* fs = reinterpret_cast<float2*>(sfd_smem + kSfTile);   // [kSfTile][rowp]
-    __shared__ int grow[kMaxRows];
     const int kk = blockIdx.x * kSfThreads + threadIdx.x;
-    const int4 tl = k.ktile[blockIdx.x];                     // l0, x rows, m0, y rows
-    const int nrow = tile_rows(k, tl, grow);
-    int rl = 0, rm = 0, rn = 0;
+    const int4 tl = k.ktile[blockIdx.x];                     // first column, columns
+    int rc = 0, rn = 0;
     float kx = 0.f, ky = 0.f, kz = 0.f;
     if (kk < k.K) {
-        const int4 v = k.lmn[kk];
-        rl = v.x - tl.x;
-        rm = tl.y + v.y - tl.z;
-        rn = tl.y + tl.w + v.z + k.kmax[2];
+        rc = k.kaux[kk].x;
+        rn = tl.y + k.lmn[kk].z + k.kmax[2];
         const double4 kv = k.kv[kk];
         kx = (float)kv.x;
         ky = (float)kv.y;
@@ -869,7 +869,7 @@ __global__ void __launch_bounds__(kSfThreads) k_pol_sfd32(KArgs k, MixArgs m, in
     for (int s0 = sb; s0 < se; s0 += kSfTile) {
         const int ns = min(kSfTile, se - s0);
         __syncthreads();
-        stage_rows(k, grow, nrow, rowp, s0, ns, fs);
+        stage_tile(k, tl, rowp, s0, ns, fs);
         for (int t = threadIdx.x; t < kSfTile; t += kSfThreads)
             ds[t] = t < ns ? m.d32[s0 + t] : make_float4(0.f, 0.f, 0.f, 0.f);
         __syncthreads();
@@ -877,7 +877,7 @@ __global__ void __launch_bounds__(kSfThreads) k_pol_sfd32(KArgs k, MixArgs m, in
 #pragma unroll 8
         for (int t = 0; t < kSfTile; ++t) {
             const float2* f = fs + t * rowp;
-            const float2 e = cmulf(cmulf(f[rl], f[rm]), f[rn]);
+            const float2 e = cmulf(f[rc], f[rn]);
             const float4 d = ds[t];
             const float pk = kx * d.x + ky * d.y + kz * d.z;
             c += e.x * pk;
@@ -924,18 +924,14 @@ __global__ void __launch_bounds__(kSfThreads, 2) k_pol_sfx32(KArgs k, const floa
     constexpr int NV = HEAT ? 30 : 6;
     constexpr int NW = HEAT ? 4 : 1;   // float4 per site: dlt, then the 12 heat weights
     extern __shared__ float4 sfx_smem[];
-    __shared__ int grow[kMaxRows];
     float4* ws = sfx_smem;                                       // [kSfTile][NW]
     float2* fs = reinterpret_cast<float2*>(sfx_smem + kSfTile * NW);   // [kSfTile][rowp]
     const int kk = blockIdx.x * kSfThreads + threadIdx.x;
     const int4 tl = k.ktile[blockIdx.x];
-    const int nrow = tile_rows(k, tl, grow);
-    int rl = 0, rm = 0, rn = 0;
+    int rc = 0, rn = 0;
     if (kk < k.K) {
-        const int4 v = k.lmn[kk];
-        rl = v.x - tl.x;
-        rm = tl.y + v.y - tl.z;
-        rn = tl.y + tl.w + v.z + k.kmax[2];
+        rc = k.kaux[kk].x;
+        rn = tl.y + k.lmn[kk].z + k.kmax[2];
     }
     const int sb = blockIdx.y * schunk, se = min(k.n, sb + schunk);
     double acc[NV];
@@ -944,7 +940,7 @@ __global__ void __launch_bounds__(kSfThreads, 2) k_pol_sfx32(KArgs k, const floa
     for (int s0 = sb; s0 < se; s0 += kSfTile) {
         const int ns = min(kSfTile, se - s0);
         __syncthreads();
-        stage_rows(k, grow, nrow, rowp, s0, ns, fs);
+        stage_tile(k, tl, rowp, s0, ns, fs);
         for (int t = threadIdx.x; t < kSfTile * NW; t += kSfThreads) {
             const int site = t / NW, w = t % NW;
             float4 val = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -958,7 +954,7 @@ __global__ void __launch_bounds__(kSfThreads, 2) k_pol_sfx32(KArgs k, const floa
 #pragma unroll 2
         for (int t = 0; t < kSfTile; ++t) {
             const float2* f = fs + t * rowp;
-            const float2 e = cmulf(cmulf(f[rl], f[rm]), f[rn]);
+            const float2 e = cmulf(f[rc], f[rn]);
             const float4 d = ws[t * NW];
             v[0] += e.x * d.x; v[1] += e.x * d.y; v[2] += e.x * d.z;
             v[3] += e.y * d.x; v[4] += e.y * d.y; v[5] += e.y * d.z;
@@ -1006,28 +1002,32 @@ __global__ void __launch_bounds__(kThreads) k_pol_sfx32_fin(KArgs k, int nchunk,
 // Shared-memory bytes of the FP32 gathers: the z rows of the block's sites.
 inline size_t gather_smem(const int* kmax) { return (size_t)(2 * kmax[2] + 1) * kThreads * sizeof(float2); }
 
-// The per-site part of the FP32 gathers: the block's sites keep their z-row factors in
-// shared memory; fx fy are read (from L2) when the (l, m) column changes, which in
-// ewald1p's order happens every few dozen k vectors.
+// The FP32 gathers (one site per thread, k vectors in ewald1p's order): the block's sites
+// keep their z-row factors in shared memory ([row][kThreads]); the product fx_l fy_m of the
+// current (l, m) column stays in registers, and the next column's factors are loaded (from
+// L2) when a column starts, so they have arrived when it ends.  Out-of-range threads work
+// on the last site and store nothing.
 struct GatherPhase {
-    const float2* fz;   // this thread's column of the staged z rows
     const float2* fac32;
-    int n, j, cl = -1, cm = 0;
-    float2 fxy = make_float2(0.f, 0.f);
-    __device__ GatherPhase(const KArgs& k, float2* smem, int j_, bool in) : fac32(k.fac32), n(k.n), j(j_) {
+    size_t n, jc;
+    int col = -1;
+    float2 fxy = make_float2(0.f, 0.f), px, py;
+    __device__ GatherPhase(const KArgs& k, float2* smem, int jc_, int kfirst) : fac32(k.fac32), n(k.n), jc(jc_) {
         const int nz = 2 * k.kmax[2] + 1;
-        for (int r = 0; r < nz; ++r)
-            smem[r * kThreads + threadIdx.x] = in ? k.fac32[(size_t)row_z(k, r - k.kmax[2]) * k.n + j] : make_float2(0.f, 0.f);
-        fz = smem + threadIdx.x + (size_t)k.kmax[2] * kThreads;
+        for (int r = 0; r < nz; ++r) smem[r * kThreads + threadIdx.x] = fac32[(size_t)row_z(k, r - k.kmax[2]) * n + jc];
+        const int c = k.kcol[k.kaux[kfirst].z];
+        px = fac32[(size_t)(c >> 16) * n + jc];
+        py = fac32[(size_t)(c & 0xffff) * n + jc];
     }
-    // exp(ik.r_j) for k = (l, m, nn); ry = row of fy_m
-    __device__ __forceinline__ float2 operator()(int l, int ry, int m, int nn, bool in) {
-        if (l != cl || m != cm) {   // uniform across the block
-            cl = l;
-            cm = m;
-            fxy = in ? cmulf(fac32[(size_t)l * n + j], fac32[(size_t)ry * n + j]) : make_float2(0.f, 0.f);
+    // exp(ik.r_j) for the k vector with auxiliary record x (column, z offset)
+    __device__ __forceinline__ float2 operator()(int4 x, const float2* smem) {
+        if (x.z != col) {   // uniform across the block
+            col = x.z;
+            fxy = cmulf(px, py);
+            px = fac32[(size_t)(x.y >> 16) * n + jc];
+            py = fac32[(size_t)(x.y & 0xffff) * n + jc];
         }
-        return cmulf(fxy, fz[nn * kThreads]);
+        return cmulf(fxy, smem[x.w + threadIdx.x]);
     }
 };
 
@@ -1036,33 +1036,31 @@ struct GatherPhase {
 // sums of the chunks added in order by k_pol_kfield32_sum.
 __global__ void __launch_bounds__(kThreads) k_pol_kfield32(KArgs k, int kchunk, float* __restrict__ part) {
     extern __shared__ float2 gat_smem[];
-    __shared__ float sh[kKTile][5];
-    __shared__ int4 sl[kKTile];   // l, row of fy_m, m, n
+    __shared__ float4 cf[kKTile][2];   // kx ky kz c3, c4 ...
+    __shared__ int4 ax[kKTile];
     const int j = blockIdx.x * kThreads + threadIdx.x;
-    const bool in = j < k.n;
-    GatherPhase ph(k, gat_smem, j, in);
     const int kb = blockIdx.y * kchunk, ke = min(k.K, kb + kchunk);
+    GatherPhase ph(k, gat_smem, min(j, k.n - 1), kb);
     double ed[3] = {0, 0, 0};
     for (int t0 = kb; t0 < ke; t0 += kKTile) {
         const int nt = min(kKTile, ke - t0);
         __syncthreads();
-        for (int u = threadIdx.x; u < nt * 5; u += blockDim.x) sh[u / 5][u % 5] = k.kco32[16 * (size_t)(t0 + u / 5) + u % 5];
-        for (int u = threadIdx.x; u < nt; u += blockDim.x) {
-            const int4 v = k.lmn[t0 + u];
-            sl[u] = make_int4(v.x, row_y(k, v.y), v.y, v.z);
-        }
+        for (int u = threadIdx.x; u < 2 * nt; u += kThreads)
+            cf[u >> 1][u & 1] = reinterpret_cast<const float4*>(k.kco32)[4 * (size_t)(t0 + (u >> 1)) + (u & 1)];
+        for (int u = threadIdx.x; u < nt; u += kThreads) ax[u] = k.kaux[t0 + u];
         __syncthreads();
         float e[3] = {0, 0, 0};
+#pragma unroll 4
         for (int u = 0; u < nt; ++u) {
-            const float* c = sh[u];
-            const int4 v = sl[u];
-            const float2 a = ph(v.x, v.y, v.z, v.w, in);
-            const float w = a.y * c[3] + a.x * c[4];
-            e[0] -= c[0] * w; e[1] -= c[1] * w; e[2] -= c[2] * w;
+            const float4 c0 = cf[u][0];
+            const float c4 = cf[u][1].x;
+            const float2 a = ph(ax[u], gat_smem);
+            const float w = a.y * c0.w + a.x * c4;
+            e[0] -= c0.x * w; e[1] -= c0.y * w; e[2] -= c0.z * w;
         }
         for (int c = 0; c < 3; ++c) ed[c] += (double)e[c];
     }
-    if (in) {
+    if (j < k.n) {
         float* p = part + (size_t)blockIdx.y * 3 * k.n;
         for (int c = 0; c < 3; ++c) p[c * (size_t)k.n + j] = (float)ed[c];
     }
@@ -1253,30 +1251,29 @@ __global__ void __launch_bounds__(kThreads) k_pol_kforce(KArgs k, PolArgs a, int
 // and the tiles added in FP64.
 __global__ void __launch_bounds__(kThreads) k_pol_kforce32(KArgs k, PolArgs a, int kchunk, double* __restrict__ part) {
     extern __shared__ float2 gat_smem[];
-    __shared__ float sh[kKTile][9];
-    __shared__ int4 sl[kKTile];
+    __shared__ float4 cf[kKTile][3];   // the 9 coefficients
+    __shared__ int4 ax[kKTile];
     const int j = blockIdx.x * kThreads + threadIdx.x;
     const bool in = j < k.n;
-    GatherPhase ph(k, gat_smem, j, in);
+    const int jc = min(j, k.n - 1);
     const int kb = blockIdx.y * kchunk, ke = min(k.K, kb + kchunk);
-    const float qj = in ? (float)a.q[j] : 0.f;
-    const bool pj = in && a.polr2[j] > 1e-6;
-    const float dj[3] = {in ? (float)a.mx[j] : 0.f, in ? (float)a.my[j] : 0.f, in ? (float)a.mz[j] : 0.f};
+    GatherPhase ph(k, gat_smem, jc, kb);
+    const float qj = (float)a.q[jc];
+    const bool pj = a.polr2[jc] > 1e-6;
+    const float dj[3] = {(float)a.mx[jc], (float)a.my[jc], (float)a.mz[jc]};
     double acc[5] = {0, 0, 0, 0, 0};
     for (int t0 = kb; t0 < ke; t0 += kKTile) {
         const int nt = min(kKTile, ke - t0);
         __syncthreads();
-        for (int u = threadIdx.x; u < nt * 9; u += blockDim.x)
-            sh[u / 9][u % 9] = k.kco32[16 * (size_t)(t0 + u / 9) + u % 9];
-        for (int u = threadIdx.x; u < nt; u += blockDim.x) {
-            const int4 v = k.lmn[t0 + u];
-            sl[u] = make_int4(v.x, row_y(k, v.y), v.y, v.z);
-        }
+        for (int u = threadIdx.x; u < 3 * nt; u += kThreads)
+            cf[u / 3][u % 3] = reinterpret_cast<const float4*>(k.kco32)[4 * (size_t)(t0 + u / 3) + u % 3];
+        for (int u = threadIdx.x; u < nt; u += kThreads) ax[u] = k.kaux[t0 + u];
         __syncthreads();
         float f[5] = {0, 0, 0, 0, 0};
         for (int u = 0; u < nt; ++u) {
-            const int4 v = sl[u];
-            kforce_site<float, float2>(sh[u], ph(v.x, v.y, v.z, v.w, in), qj, dj, pj, f);
+            const float4 c0 = cf[u][0], c1 = cf[u][1], c2 = cf[u][2];
+            const float r[9] = {c0.x, c0.y, c0.z, c0.w, c1.x, c1.y, c1.z, c1.w, c2.x};
+            kforce_site<float, float2>(r, ph(ax[u], gat_smem), qj, dj, pj, f);
         }
         for (int c = 0; c < 5; ++c) acc[c] += (double)f[c];
     }
@@ -1717,7 +1714,7 @@ cudaError_t launch_msite_redistribute(int nw, double gamma, double* fx, double* 
 
 void PolarState::release() {
     void* p[] = {ercp, nn, nbr, flag, xf, tens, intra, fld, vesp, ae, eik, kv, kx2, lmn, sf, kterm, acc, kco, fac, md, vh,
-                 tens32, r32, d32, e32, kco32, fac32, ktile, kpart, cg_x, cg_r, cg_q, cg_z, vh32};
+                 tens32, r32, d32, e32, kco32, fac32, ktile, kaux, kcol, kpart, cg_x, cg_r, cg_q, cg_z, vh32};
     for (void* q : p)
         if (q) cudaFree(q);
     if (acc_h) cudaFreeHost(acc_h);
@@ -1737,6 +1734,8 @@ void PolarState::release() {
     r32 = d32 = cg_x = cg_r = cg_q = cg_z = vh32 = nullptr;
     fac32 = nullptr;
     ktile = nullptr;
+    kaux = nullptr;
+    kcol = nullptr;
     ktile_cap = 0;
     cap32 = n32 = k32 = 0;
     fac32_cap = 0;
@@ -1817,10 +1816,17 @@ cudaError_t PolarState::reserve_mixed(int n, int K, size_t nfac) {
         n32 = n;
     }
     if (K > k32) {
-        if (kco32) cudaFree(kco32);
+        void* p[] = {kco32, kaux, kcol};
+        for (void* q : p)
+            if (q) cudaFree(q);
         kco32 = nullptr;
+        kaux = nullptr;
+        kcol = nullptr;
         k32 = 0;
-        if ((e = cudaMalloc(&kco32, 16 * (size_t)std::max(K, 1) * sizeof(float)))) return e;
+        const size_t kk = (size_t)std::max(K, 1);
+        if ((e = cudaMalloc(&kco32, 16 * kk * sizeof(float)))) return e;
+        if ((e = cudaMalloc(&kaux, kk * sizeof(int4)))) return e;
+        if ((e = cudaMalloc(&kcol, kk * sizeof(int)))) return e;
         k32 = K;
     }
     const size_t need = nfac * n;
@@ -2034,19 +2040,31 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
     int rowp = 1;
     const int nkt = (K + kSfThreads - 1) / kSfThreads;
     if (mixed && K) {
+        // the (l, m) columns of the k vectors (runs of n), each tile's first column and
+        // count, and per k its column within the tile, the next column, its column and
+        // the offset of its z row in the gathers' shared memory
+        hkcol.clear();
+        std::vector<int> col(K);
+        for (int q = 0; q < K; ++q) {
+            if (q == 0 || hlmn[q].x != hlmn[q - 1].x || hlmn[q].y != hlmn[q - 1].y)
+                hkcol.push_back((hlmn[q].x << 16) | (kmax[0] + 1 + kmax[1] + hlmn[q].y));
+            col[q] = (int)hkcol.size() - 1;
+        }
+        const int ncols = (int)hkcol.size();
         hktile.resize(nkt);
+        hkaux.resize(K);
         for (int t = 0; t < nkt; ++t) {
             const int b = t * kSfThreads, e_ = std::min(K, b + kSfThreads);
-            int m0 = hlmn[b].y, m1 = m0;
-            for (int q = b; q < e_; ++q) {
-                m0 = std::min(m0, hlmn[q].y);
-                m1 = std::max(m1, hlmn[q].y);
-            }
-            hktile[t] = make_int4(hlmn[b].x, hlmn[e_ - 1].x - hlmn[b].x + 1, m0, m1 - m0 + 1);
-            rowp = std::max(rowp, hktile[t].y + hktile[t].w + 2 * kmax[2] + 1);
+            hktile[t] = make_int4(col[b], col[e_ - 1] - col[b] + 1, 0, 0);
+            rowp = std::max(rowp, hktile[t].y + 2 * kmax[2] + 1);
+            for (int q = b; q < e_; ++q)
+                hkaux[q] = make_int4(col[q] - col[b], hkcol[std::min(col[q] + 1, ncols - 1)], col[q],
+                                     (hlmn[q].z + kmax[2]) * kThreads);
         }
         rowp |= 1;
         if ((e = cudaMemcpyAsync(ktile, hktile.data(), nkt * sizeof(int4), cudaMemcpyHostToDevice, s))) return e;
+        if ((e = cudaMemcpyAsync(kaux, hkaux.data(), K * sizeof(int4), cudaMemcpyHostToDevice, s))) return e;
+        if ((e = cudaMemcpyAsync(kcol, hkcol.data(), ncols * sizeof(int), cudaMemcpyHostToDevice, s))) return e;
     }
     const size_t sfd_smem = kSfTile * (sizeof(float4) + (size_t)rowp * sizeof(float2));
     const size_t sfx_smem0 = sfd_smem, sfx_smem1 = kSfTile * (4 * sizeof(float4) + (size_t)rowp * sizeof(float2));
@@ -2103,6 +2121,8 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
         b.eik = eik;
         b.fac32 = mixed ? fac32 : nullptr;
         b.ktile = mixed ? ktile : nullptr;
+        b.kaux = mixed ? kaux : nullptr;
+        b.kcol = mixed ? kcol : nullptr;
         b.kco32 = mixed ? kco32 : nullptr;
         b.sf = sf;
         b.kco = kco;
