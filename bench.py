@@ -1,18 +1,21 @@
-"""Benchmark: MB-pol force + heat-current steps/s at 4096 H2O on one GB300.
+"""Benchmark: MB-pol MD force evaluations per second at 4096 H2O on one GB300.
 
-One step = one evaluation of the MB-pol 2B + 3B forces with the heat-current
-bookkeeping (dimer/trimer lists rebuilt on the device, forces, energy, virial,
-stress, per-atom energies, jpot and jkin) on the seeded 4096-water box
-(jittered 16^3 lattice, L = 49.70 A, 298 K).
+One step = the whole force evaluation of one MD step of MB-pol water on the seeded
+4096-water box (jittered 16^3 lattice, L = 49.70 A, 298 K): M sites and DMS charges,
+TTM4-F polarizable electrostatics (Ewald) with the induced-dipole solve warm-started
+from the previous step, dispersion, the 1-body PES, the 2B + 3B polynomials, the M-site
+force redistribution, per-atom energies and the heat current; positions advance by
+v dt between steps.
 
     python bench.py [--gpus N --steps K --warmup W] [--impl reference]
 
 Our arm prints one JSON line: `value` is mixed-precision steps/s with inputs
 resident in HBM (L2 flushed between steps); `fp64` the plain FP64 path; `e2e` the
 same metric through the host-array C ABI (host<->device copies timed); `roofline`
-the dominant kernel (the 3B cluster kernel) against the FP32 pipe; `cpu_baseline`
-the reference algorithm (the oracle's restatement of the Fortran loops) timed on a
-bounded share of the same step on this host's cores.
+the mixed step's largest kernel (the FP64 k-space field gather) against the FP64
+pipe; `cpu_baseline` the reference algorithm (the oracle's restatement) timed on a
+bounded share of the same step on this host's cores; `batched*` many boxes per call;
+`serving*` a Poisson stream of whole evaluations through the continuous-batching server.
 
 --impl reference times that CPU implementation alone (all host threads).
 Under torchrun each rank evaluates its own independent box (replicas, weak
@@ -329,6 +332,8 @@ def run_ours(args, rank, world):
     ctx.set_profiling(True)
     reset()
     pol_phase = np.zeros(4)
+    kf_ms = kf_flops = 0.0
+    kf_n = 0
     nprof = 3
     for i_ in range(2 + nprof):
         step(capi.MIXED)
@@ -336,6 +341,10 @@ def run_ours(args, rank, world):
         if i_ >= 2:
             ms, kvec = ctx.polar_timings()
             pol_phase += ms
+            a_, b_, c_ = ctx.polar_field_timing()
+            kf_ms += a_
+            kf_flops += b_
+            kf_n += c_
     pol_phase /= nprof
     ctx.set_profiling(False)
 
@@ -457,20 +466,18 @@ def run_ours(args, rank, world):
     fp64_peak = 152 * 4 * sm_max * 1e6 / 1e12         # 2 DFMA per clock per SM
     fp64_achieved = fl["2b"] * ndim / t23 / 1e12 if t23 > 0 else None
     fp32_achieved = fl["3b"] * ntri / t23 / 1e12 if t23 > 0 else None
-    traffic = traffic_sf = None
+    traffic = traffic_kf = None
     tfile = os.path.join(REPO, "profiles", "traffic.json")
     if os.path.exists(tfile):
         with open(tfile) as f:
             tj = json.load(f)
         traffic = tj.get("k_mbpol_23_bytes_per_launch")
-        per = tj.get("k_pol_sf_final_bytes_per_k_site")
-        traffic_sf = per * kvec * n if per else None
-    # the step's largest kernel: the final structure factors with the heat sums, FP64-bound;
-    # per (k vector, site) 30 multiply-adds (60 flops): 6 of the dipole structure factors and
-    # 24 of the heat sums over the per-site products q v and mu v
-    t_sf = pol_phase[2] / 1e3
-    sf_flops = 60.0 * kvec * n
-    sf_achieved = sf_flops / t_sf / 1e12 if t_sf > 0 else None
+        per = tj.get("k_pol_kfield_bytes_per_k_site")
+        traffic_kf = per * kvec * n if per else None
+    # the mixed step's largest kernel: the FP64 k-space field gather of the dipole solve's
+    # FP64 field evaluations (k_pol_kfield), FP64-bound; per (k vector, site) 9 flops, 18 in
+    # the first evaluation (the static charge field); CUDA events around each launch
+    kf_achieved = kf_flops / (kf_ms / 1e3) / 1e12 if kf_ms > 0 else None
     value = world * args.steps / t_mixed
     out = {
         "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
@@ -503,9 +510,10 @@ def run_ours(args, rank, world):
                                                   "jkin": phase64[3]}},
         "e2e": {"value": world * args.steps / t_e2e, "unit": "steps/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
-        "roofline": {"kernel": "k_pol_sf_final<1>", "bound": "fp64", "achieved": sf_achieved, "peak": fp64_peak,
-                     "unit": "TFLOP/s", "frac": (sf_achieved / fp64_peak) if sf_achieved else None,
-                     "traffic": traffic_sf, "kernel_ms": 1e3 * t_sf, "flops_per_k_site": 60, "k_vectors": kvec,
+        "roofline": {"kernel": "k_pol_kfield", "bound": "fp64", "achieved": kf_achieved, "peak": fp64_peak,
+                     "unit": "TFLOP/s", "frac": (kf_achieved / fp64_peak) if kf_achieved else None,
+                     "traffic": traffic_kf, "kernel_ms": kf_ms / max(1, kf_n), "launches_timed": kf_n,
+                     "flops_per_k_site": "9 (18 in the first evaluation)", "k_vectors": kvec,
                      "sites": n, "algorithmic_bytes": 16.0 * kvec * n,
                      "peak_source": "computed at sm_max_mhz %.0f: 152 SMs x 4 FP64 flop/clk (MEASURED_PEAKS.json "
                                     "holds HBM and bf16 figures only)" % sm_max},

@@ -1350,6 +1350,14 @@ extern "C" int mbx_polar_timings(const mbx_context* ctx, float* ms4, long* kvect
     return MBX_OK;
 }
 
+extern "C" int mbx_polar_field_timing(const mbx_context* ctx, double* ms, double* flops, long* launches) {
+    if (!ctx) return MBX_ERR_ARG;
+    if (ms) *ms = ctx->polar.kf_ms;
+    if (flops) *flops = ctx->polar.kf_flops;
+    if (launches) *launches = ctx->polar.kf_launches;
+    return MBX_OK;
+}
+
 extern "C" int mbx_msite_redistribute(int nw, double gamma, double* fxx, double* fyy, double* fzz) {
     if (nw < 0 || (nw && (!fxx || !fyy || !fzz))) return MBX_ERR_ARG;
     for (int i = 0; i < nw; ++i) {   // SOURCE/dlpoly_cmd.f:2585-2601 (standard layout)

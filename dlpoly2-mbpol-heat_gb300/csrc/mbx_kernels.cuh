@@ -212,6 +212,11 @@ struct PolarState {
     float phase_ms[4] = {0, 0, 0, 0};      // setup (lists, static fields, phases), dipole solve,
                                            // final structure factors, rest of the final pass
     long K_last = 0;                       // k vectors of the last call
+    static constexpr int kKfEvents = 16;
+    cudaEvent_t kfev[kKfEvents][2] = {};   // profiling: around the FP64 field gathers (k_pol_kfield)
+    float kf_ms = 0.f;                     // their device time, algorithmic flops and launches
+    double kf_flops = 0.0;
+    long kf_launches = 0;
     double4* kv = nullptr;                 // kx, ky, kz, akk
     double2* kx2 = nullptr;                // rksq, akv2
     int4* lmn = nullptr;

@@ -1190,14 +1190,61 @@ __global__ void __launch_bounds__(kThreads) k_pcg_rz(PolArgs a, MixArgs m, const
 }
 
 // mu += d in FP64; refreshes the masked dipoles.
+// Also writes the update of the masked dipoles (the structure factors' dipoles) to d32,
+// for the next field evaluation's k-space part (k_pol_kfield32_dsum).
 __global__ void k_pol_apply(PolArgs a, MixArgs m, double4* __restrict__ md) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= a.n || !(a.polr2[i] > a.toler)) return;
-    const float4 d = m.x[i];
-    a.mx[i] += (double)d.x;
-    a.my[i] += (double)d.y;
-    a.mz[i] += (double)d.z;
-    if (a.polr2[i] > 1e-6) md[i] = make_double4(a.mx[i], a.my[i], a.mz[i], 0.0);
+    if (i >= a.n) return;
+    float4 dm = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (a.polr2[i] > a.toler) {
+        const float4 d = m.x[i];
+        a.mx[i] += (double)d.x;
+        a.my[i] += (double)d.y;
+        a.mz[i] += (double)d.z;
+        if (a.polr2[i] > 1e-6) {
+            md[i] = make_double4(a.mx[i], a.my[i], a.mz[i], 0.0);
+            dm = make_float4(d.x, d.y, d.z, 0.f);
+        }
+    }
+    m.d32[i] = dm;
+}
+
+// Mixed precision, FP64 field evaluations after a correction: the k-space dipole field is
+// linear in the dipoles, so it is the previous one (efm, FP64) plus the field of the
+// correction (FP32 phases and sums, on a quantity at the size of the residual).  Per k:
+// the chunks of k_pol_sfx32<0> over the correction added in order; the dipole structure
+// factors k.sf updated in FP64; the coefficients of the FP32 gather of the correction.
+__global__ void __launch_bounds__(kThreads) k_pol_sfd_dfin(KArgs k, int nchunk, const double* __restrict__ part) {
+    const int kk = blockIdx.x * blockDim.x + threadIdx.x;
+    if (kk >= k.K) return;
+    double t[6] = {0, 0, 0, 0, 0, 0};
+    for (int c = 0; c < nchunk; ++c) {
+        const double* p = part + 6 * ((size_t)c * k.K + kk);
+        for (int q = 0; q < 6; ++q) t[q] += p[q];
+    }
+    double* sf = k.sf + 8 * (size_t)kk;
+    for (int q = 0; q < 6; ++q) sf[2 + q] += t[q];
+    const double4 kv = k.kv[kk];
+    float* c = k.kco32 + 16 * (size_t)kk;
+    c[0] = (float)kv.x; c[1] = (float)kv.y; c[2] = (float)kv.z;
+    c[3] = (float)(kv.w * (kv.x * t[3] + kv.y * t[4] + kv.z * t[5]));
+    c[4] = (float)(kv.w * (kv.x * t[0] + kv.y * t[1] + kv.z * t[2]));
+}
+
+// efm += scale * (k-space field of the correction) + self term of the dipole change.
+__global__ void __launch_bounds__(kThreads) k_pol_kfield32_dsum(KArgs k, PolArgs a, MixArgs m, int nchunk,
+                                                                const float* __restrict__ part) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= k.n) return;
+    double em[3] = {0, 0, 0};
+    for (int q = 0; q < nchunk; ++q)
+        for (int c = 0; c < 3; ++c) em[c] += (double)part[((size_t)q * 3 + c) * k.n + j];
+    const double dum = 4.0 * kR4pie0 * (a.alpha * a.alpha * a.alpha) / kSqrpi / 3.0;
+    const bool pol = a.polr2[j] > 1e-6;
+    float4 x = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (a.polr2[j] > a.toler) x = m.x[j];   // the dipole change of k_pol_apply
+    const double dx[3] = {(double)x.x, (double)x.y, (double)x.z};
+    for (int c = 0; c < 3; ++c) a.efm[c * k.n + j] += (pol ? k.scale * em[c] : 0.0) + dum * dx[c];
 }
 
 // Final k-space pass (ewald1p iflag 1): per site and chunk of k vectors, the force and the
@@ -1723,6 +1770,12 @@ void PolarState::release() {
             cudaEventDestroy(v);
             v = nullptr;
         }
+    for (auto& pr : kfev)
+        for (auto& v : pr)
+            if (v) {
+                cudaEventDestroy(v);
+                v = nullptr;
+            }
     ercp = nullptr;
     nn = nbr = flag = nullptr;
     xf = nullptr;
@@ -2200,11 +2253,25 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
     const int schunk = ((n + nsc - 1) / nsc + kSfTile - 1) / kSfTile * kSfTile;
     const int nsc_used = (n + schunk - 1) / schunk;
     if ((e = reserve_part(std::max((size_t)6 * std::max(nc1, nc2) * n, (size_t)30 * nsc_used * K)))) return e;
+    int kf_calls = 0;          // profiling: k_pol_kfield launches of this call with events
+    double kf_call_flops = 0.0;
     auto fields64 = [&](bool first) {
         k_pol_dd<<<blocks(32L * n, kThreads), kThreads, 0, s>>>(a);
         if (K) {
             k_pol_sfd<<<K, kSfThreads, 0, s>>>(k);
+            const bool timed = profiling && kf_calls < kKfEvents;
+            if (timed) {
+                for (auto& v : kfev[kf_calls])
+                    if (!v) cudaEventCreate(&v);
+                cudaEventRecord(kfev[kf_calls][0], s);
+            }
             k_pol_kfield<<<dim3(sblk2, nc2), kThreads, 0, s>>>(k, first, kc2, kpart);
+            if (timed) {
+                cudaEventRecord(kfev[kf_calls][1], s);
+                // algorithmic flops per (k vector, site): 9, and 9 more for the static field
+                kf_call_flops += (first ? 18.0 : 9.0) * K * (double)n;
+                ++kf_calls;
+            }
         }
         k_pol_kfield_sum<<<sblk1, kThreads, 0, s>>>(k, a, first, nc2, kpart);
         launches += K ? 4 : 2;
@@ -2259,8 +2326,24 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
             return cudaSuccess;
         };
         double rms_prev = HUGE_VAL;
+        bool corrected = false;   // the dipoles changed by k_pol_apply since the last evaluation
+        // the field evaluation after a correction: FP64 real space; k space the previous
+        // FP64 fields plus the FP32 ones of the correction
+        auto fields_delta = [&]() {
+            k_pol_dd<<<blocks(32L * n, kThreads), kThreads, 0, s>>>(a);
+            if (K) {
+                k_pol_sfx32<0><<<dim3(nkt, nsc_used), kSfThreads, sfx_smem0, s>>>(k, d32, vh32, schunk, rowp, kpart);
+                k_pol_sfd_dfin<<<blocks(K, kThreads), kThreads, 0, s>>>(k, nsc_used, kpart);
+                k_pol_kfield32<<<dim3(sblk1, nc1), kThreads, gat_smem, s>>>(k, kc1, (float*)kpart);
+                launches += 3;
+            }
+            k_pol_kfield32_dsum<<<sblk1, kThreads, 0, s>>>(k, a, m, K ? nc1 : 0, (const float*)kpart);
+            launches += 2;
+        };
         for (int it = 1;; ++it) {
-            fields64(it == 1);
+            if (corrected) fields_delta();
+            else fields64(it == 1);
+            corrected = false;
             if ((e = cudaMemsetAsync(acc + 29, 0, 2 * sizeof(double), s))) return e;
             k_pol_resid<<<blocks(n, kThreads), kThreads, 0, s>>>(a, m);
             ++launches;
@@ -2331,6 +2414,7 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
             } else {
                 k_pol_apply<<<blocks(n, kThreads), kThreads, 0, s>>>(a, m, md);
                 ++launches;
+                corrected = true;
             }
         }
     }
@@ -2378,9 +2462,18 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
     if (profiling && (e = cudaEventRecord(ev[4], s))) return e;
     if ((e = cudaMemcpyAsync(acc_h, acc, 64 * sizeof(double), cudaMemcpyDeviceToHost, s))) return e;
     if ((e = cudaStreamSynchronize(s))) return e;
-    if (profiling)
+    if (profiling) {
         for (int q = 0; q < 4; ++q)
             if ((e = cudaEventElapsedTime(&phase_ms[q], ev[q], ev[q + 1]))) return e;
+        kf_ms = 0.f;
+        for (int q = 0; q < kf_calls; ++q) {
+            float t = 0.f;
+            if ((e = cudaEventElapsedTime(&t, kfev[q][0], kfev[q][1]))) return e;
+            kf_ms += t;
+        }
+        kf_launches = kf_calls;
+        kf_flops = kf_call_flops;
+    }
     const double* h = acc_h;
     // acc: 0 eng_real, 1 vir, 2..7 stress (11 12 13 22 23 33), 8..10 jpot (real + qd),
     //      24..26 jkin, 27..28 iteration sums, 40 engsic, 41 eng_polar,

@@ -105,6 +105,7 @@ def load(path=None):
     L.mbx_water_step.argtypes = [C.c_void_p, C.c_int, C.c_int, _D, C.c_int, C.c_int, _D, _D, _D, _I, _I] + [_D] * 16
     L.mbx_set_lanes.argtypes = [C.c_void_p, C.c_int]
     L.mbx_set_precond_sweeps.argtypes = [C.c_void_p, C.c_int]
+    L.mbx_polar_field_timing.argtypes = [C.c_void_p, _D, _D, C.POINTER(C.c_long)]
     L.mbx_water_step_multi.argtypes = ([C.c_void_p, C.c_int, C.c_int, _I, _D, _I, _D, _D, _D, _I, _I] + [_D] * 16 +
                                        [_I])
     L.mbx_water_step_device.argtypes = [C.c_void_p, C.c_int, C.c_int, _D, C.c_int, C.c_int, _D] + \
@@ -421,6 +422,14 @@ class Context:
         kv = C.c_long(0)
         self._check(self.lib.mbx_polar_timings(self.h, ms, C.byref(kv)), "mbx_polar_timings")
         return np.array(list(ms)), int(kv.value)
+
+    def polar_field_timing(self):
+        """(ms, algorithmic flops, launches) of the last call's FP64 k-space field gathers"""
+        ms = np.zeros(1)
+        fl = np.zeros(1)
+        n = C.c_long(0)
+        self._check(self.lib.mbx_polar_field_timing(self.h, _p(ms), _p(fl), C.byref(n)), "mbx_polar_field_timing")
+        return float(ms[0]), float(fl[0]), int(n.value)
 
     def polar_inner_sweeps(self):
         return int(self.lib.mbx_polar_inner_sweeps(self.h))

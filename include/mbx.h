@@ -224,6 +224,10 @@ long mbx_polar_inner_sweeps(const mbx_context* ctx);
  * static fields and exp(ik.r) table; dipole solve; final structure factors with the heat
  * sums; rest of the final pass) and its number of k vectors. */
 int mbx_polar_timings(const mbx_context* ctx, float* ms4, long* kvectors);
+/* With mbx_set_profiling on: the FP64 k-space field gathers of the last call (the
+ * iteration's largest FP64 kernel): device ms, algorithmic flops (9 per k vector and site,
+ * 18 in the first evaluation, which adds the static charge field) and launches timed. */
+int mbx_polar_field_timing(const mbx_context* ctx, double* ms, double* flops, long* launches);
 /* Frees the electrostatics' device buffers (phase tables, pair tensors) of a context when
  * they hold more than keep_bytes; returns the bytes freed (0: kept).  The next call
  * allocates them again. */
