@@ -192,6 +192,8 @@ struct PolarState {
     int4* ktile = nullptr;                 // per 256 k vectors: first (l, m) column, columns
     int4* kaux = nullptr;                  // per k: column in its tile, next column, column, z offset
     int* kcol = nullptr;                   // per (l, m) column: l << 16 | y row
+    int2* colk = nullptr;                  // per (l, m) column: first k vector, count
+    std::vector<int2> hcolk;
     std::vector<int4> hktile, hkaux;
     std::vector<int> hkcol;
     int ktile_cap = 0;

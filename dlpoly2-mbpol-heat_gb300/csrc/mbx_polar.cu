@@ -414,6 +414,7 @@ struct KArgs {
     const int4* ktile;     // per kSfThreads k vectors: first (l, m) column, columns (FP32 structure factors)
     const int4* kaux;      // per k: column within its tile, next column (l << 16 | y row), column, z offset
     const int* kcol;       // per (l, m) column: l << 16 | y row
+    const int2* colk;      // per (l, m) column: first k vector, count
     float* kco32;          // 16 per k: the CG gather's kx, ky, kz, akk k.Ds, akk k.Dc, then the FP32 force gather's
     double* sf;            // 8 per k: ckcs, ckss, Mc(3), Ms(3)
     double* kco;           // 16 per k: coefficients of the gathers
@@ -451,17 +452,20 @@ __global__ void k_pol_factors(KArgs k, const double* __restrict__ x, const doubl
     }
 }
 
+// exp(ik.r_j) = (fx_l fy_m) fz_n per (l, m) column (blockIdx.x) and site: the product
+// fx_l fy_m once per column and site, then one complex product per k vector.
 __global__ void k_pol_phase(KArgs k) {
     const int j = blockIdx.y * blockDim.x + threadIdx.x;
-    const int kk = blockIdx.x;
     if (j >= k.n) return;
-    const int4 v = k.lmn[kk];
-    const int oy = k.kmax[0] + 1, oz = oy + 2 * k.kmax[1] + 1;
-    const double2 fx = k.fac[(size_t)v.x * k.n + j];
-    const double2 fy = k.fac[(size_t)(oy + v.y + k.kmax[1]) * k.n + j];
-    const double2 fz = k.fac[(size_t)(oz + v.z + k.kmax[2]) * k.n + j];
-    const double2 e = cmul(cmul(fx, fy), fz);
-    k.eik[(size_t)kk * k.n + j] = e;
+    const int2 ck = k.colk[blockIdx.x];   // first k vector, count
+    const int c = k.kcol[blockIdx.x];
+    const int oz = k.kmax[0] + 2 * k.kmax[1] + 2 + k.kmax[2];
+    const double2 fxy = cmul(k.fac[(size_t)(c >> 16) * k.n + j], k.fac[(size_t)(c & 0xffff) * k.n + j]);
+    for (int q = 0; q < ck.y; ++q) {
+        const int kk = ck.x + q;
+        const double2 fz = k.fac[(size_t)(oz + k.lmn[kk].z) * k.n + j];
+        k.eik[(size_t)kk * k.n + j] = cmul(fxy, fz);
+    }
 }
 
 template <int NV>
@@ -1761,7 +1765,7 @@ cudaError_t launch_msite_redistribute(int nw, double gamma, double* fx, double* 
 
 void PolarState::release() {
     void* p[] = {ercp, nn, nbr, flag, xf, tens, intra, fld, vesp, ae, eik, kv, kx2, lmn, sf, kterm, acc, kco, fac, md, vh,
-                 tens32, r32, d32, e32, kco32, fac32, ktile, kaux, kcol, kpart, cg_x, cg_r, cg_q, cg_z, vh32};
+                 tens32, r32, d32, e32, kco32, fac32, ktile, kaux, kcol, colk, kpart, cg_x, cg_r, cg_q, cg_z, vh32};
     for (void* q : p)
         if (q) cudaFree(q);
     if (acc_h) cudaFreeHost(acc_h);
@@ -1789,6 +1793,7 @@ void PolarState::release() {
     ktile = nullptr;
     kaux = nullptr;
     kcol = nullptr;
+    colk = nullptr;
     ktile_cap = 0;
     cap32 = n32 = k32 = 0;
     fac32_cap = 0;
@@ -1869,17 +1874,15 @@ cudaError_t PolarState::reserve_mixed(int n, int K, size_t nfac) {
         n32 = n;
     }
     if (K > k32) {
-        void* p[] = {kco32, kaux, kcol};
+        void* p[] = {kco32, kaux};
         for (void* q : p)
             if (q) cudaFree(q);
         kco32 = nullptr;
         kaux = nullptr;
-        kcol = nullptr;
         k32 = 0;
         const size_t kk = (size_t)std::max(K, 1);
         if ((e = cudaMalloc(&kco32, 16 * kk * sizeof(float)))) return e;
         if ((e = cudaMalloc(&kaux, kk * sizeof(int4)))) return e;
-        if ((e = cudaMalloc(&kcol, kk * sizeof(int)))) return e;
         k32 = K;
     }
     const size_t need = nfac * n;
@@ -1940,13 +1943,15 @@ cudaError_t PolarState::reserve(int nw, int K, size_t nfac) {
         nw_cap = nw;
     }
     if (K > k_cap) {
-        void* p[] = {kv, kx2, lmn, sf, kterm, kco};
+        void* p[] = {kv, kx2, lmn, sf, kterm, kco, kcol, colk};
         for (void* q : p)
             if (q) cudaFree(q);
         kv = nullptr;
         kx2 = nullptr;
         lmn = nullptr;
         sf = kterm = kco = nullptr;
+        kcol = nullptr;
+        colk = nullptr;
         k_cap = 0;
         if ((e = cudaMalloc(&kv, K * sizeof(double4)))) return e;
         if ((e = cudaMalloc(&kx2, K * sizeof(double2)))) return e;
@@ -1954,6 +1959,8 @@ cudaError_t PolarState::reserve(int nw, int K, size_t nfac) {
         if ((e = cudaMalloc(&sf, 8 * (size_t)K * sizeof(double)))) return e;
         if ((e = cudaMalloc(&kterm, 16 * (size_t)K * sizeof(double)))) return e;
         if ((e = cudaMalloc(&kco, 16 * (size_t)K * sizeof(double)))) return e;
+        if ((e = cudaMalloc(&kcol, K * sizeof(int)))) return e;
+        if ((e = cudaMalloc(&colk, K * sizeof(int2)))) return e;
         k_cap = K;
     }
     const size_t need = (size_t)K * n;
@@ -2092,18 +2099,26 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
     // shared-memory rows (odd, so the transposed stores spread over the banks)
     int rowp = 1;
     const int nkt = (K + kSfThreads - 1) / kSfThreads;
-    if (mixed && K) {
-        // the (l, m) columns of the k vectors (runs of n), each tile's first column and
-        // count, and per k its column within the tile, the next column, its column and
-        // the offset of its z row in the gathers' shared memory
-        hkcol.clear();
-        std::vector<int> col(K);
-        for (int q = 0; q < K; ++q) {
-            if (q == 0 || hlmn[q].x != hlmn[q - 1].x || hlmn[q].y != hlmn[q - 1].y)
-                hkcol.push_back((hlmn[q].x << 16) | (kmax[0] + 1 + kmax[1] + hlmn[q].y));
-            col[q] = (int)hkcol.size() - 1;
+    // the (l, m) columns of the k vectors (runs of n): l << 16 | y row, first k and count
+    hkcol.clear();
+    hcolk.clear();
+    std::vector<int> col(K);
+    for (int q = 0; q < K; ++q) {
+        if (q == 0 || hlmn[q].x != hlmn[q - 1].x || hlmn[q].y != hlmn[q - 1].y) {
+            hkcol.push_back((hlmn[q].x << 16) | (kmax[0] + 1 + kmax[1] + hlmn[q].y));
+            hcolk.push_back(make_int2(q, 0));
         }
-        const int ncols = (int)hkcol.size();
+        col[q] = (int)hkcol.size() - 1;
+        ++hcolk.back().y;
+    }
+    const int ncols = (int)hkcol.size();
+    if (K) {
+        if ((e = cudaMemcpyAsync(kcol, hkcol.data(), ncols * sizeof(int), cudaMemcpyHostToDevice, s))) return e;
+        if ((e = cudaMemcpyAsync(colk, hcolk.data(), ncols * sizeof(int2), cudaMemcpyHostToDevice, s))) return e;
+    }
+    if (mixed && K) {
+        // each tile's first column and count, and per k its column within the tile, the
+        // next column, its column and the offset of its z row in the gathers' shared memory
         hktile.resize(nkt);
         hkaux.resize(K);
         for (int t = 0; t < nkt; ++t) {
@@ -2117,7 +2132,6 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
         rowp |= 1;
         if ((e = cudaMemcpyAsync(ktile, hktile.data(), nkt * sizeof(int4), cudaMemcpyHostToDevice, s))) return e;
         if ((e = cudaMemcpyAsync(kaux, hkaux.data(), K * sizeof(int4), cudaMemcpyHostToDevice, s))) return e;
-        if ((e = cudaMemcpyAsync(kcol, hkcol.data(), ncols * sizeof(int), cudaMemcpyHostToDevice, s))) return e;
     }
     const size_t sfd_smem = kSfTile * (sizeof(float4) + (size_t)rowp * sizeof(float2));
     const size_t sfx_smem0 = sfd_smem, sfx_smem1 = kSfTile * (4 * sizeof(float4) + (size_t)rowp * sizeof(float2));
@@ -2175,7 +2189,8 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
         b.fac32 = mixed ? fac32 : nullptr;
         b.ktile = mixed ? ktile : nullptr;
         b.kaux = mixed ? kaux : nullptr;
-        b.kcol = mixed ? kcol : nullptr;
+        b.kcol = kcol;
+        b.colk = colk;
         b.kco32 = mixed ? kco32 : nullptr;
         b.sf = sf;
         b.kco = kco;
@@ -2231,7 +2246,7 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
     ++launches;
     if (K) {
         k_pol_factors<<<blocks(n, kThreads), kThreads, 0, s>>>(k, x, y, z);
-        dim3 g(K, blocks(n, kThreads));   // sites per k vector along y (n < 65535 * 128)
+        dim3 g(ncols, blocks(n, kThreads));   // sites per column along y (n < 65535 * 128)
         k_pol_phase<<<g, kThreads, 0, s>>>(k);
         k_pol_sfq<<<K, kSfThreads, 0, s>>>(k, q);
         launches += 3;
