@@ -180,6 +180,13 @@ struct PolarState {
     double* intra = nullptr;               // intramolecular O/H dipole tensors (18 per water)
     double* fld = nullptr;                 // efk, efc, emu, efm (3 blocks of n each)
     double *vesp = nullptr, *ae = nullptr;
+    double* polr6 = nullptr;               // polr^(1/6) per site
+    // cell list of the pair-list build: sort keys and indices, radix-sort scratch, bounds
+    unsigned *ckey = nullptr, *cskey = nullptr;
+    int *cidx = nullptr, *csidx = nullptr, *cstart = nullptr, *cend = nullptr;
+    void* csort = nullptr;
+    size_t csort_bytes = 0;
+    int cell_n_cap = 0, ncell_cap = 0;
     double2* eik = nullptr;                // exp(ik.r) [k][site]
     double2* fac = nullptr;                // per-site phase factors per axis and index
     size_t fac_cap = 0;
@@ -242,6 +249,7 @@ struct PolarState {
     cudaError_t reserve(int nw, int K, size_t nfac);
     cudaError_t reserve_mixed(int n, int K, size_t nfac);
     cudaError_t reserve_part(size_t ndouble);
+    cudaError_t reserve_cells(int n, int ncell);
     // One evaluation on device arrays (precision MBX_FP64 or MBX_MIXED: the dipole
     // equations solved by FP32 corrections under FP64 refinement).  prm[15] as
     // mbx_polar_forces; forces, per-site

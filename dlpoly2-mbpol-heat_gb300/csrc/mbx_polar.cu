@@ -25,6 +25,8 @@
 // series / continued fraction with EPS 3e-7).
 #include "mbx_kernels.cuh"
 
+#include <cub/device/device_radix_sort.cuh>
+
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -126,6 +128,7 @@ struct PolArgs {
     Cell cl;
     int nw, n, cap;
     const double *x, *y, *z, *q, *polr, *polr2, *dp;
+    const double* polr6;   // polr^(1/6) per site: the Thole width of a pair is polr6_i polr6_j
     double *mx, *my, *mz;
     const double *vx, *vy, *vz;
     double *fx, *fy, *fz;
@@ -223,8 +226,40 @@ __global__ void k_pol_f32(int n, const double* __restrict__ x, const double* __r
 // Partners of site i: every site of another water whose imaged separation passes the
 // reference's cut (rcut > r in rfield, rcut^2 > r^2 in ewald2p), in increasing index.
 // An FP32 test with a margin far above its rounding screens the candidates first.
+// Cell of a site along one axis (orthorhombic cells, positions wrapped into the box).
+__device__ __forceinline__ int pol_wrap(double s, int nc) {
+    s = s - floor(s);
+    const int c = (int)(s * nc);
+    return c >= nc ? nc - 1 : (c < 0 ? 0 : c);
+}
+
+__global__ void k_pol_keys(int n, const double* __restrict__ x, const double* __restrict__ y,
+                           const double* __restrict__ z, Cell cl, int3 nc, unsigned* __restrict__ key,
+                           int* __restrict__ idx) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    key[i] = (unsigned)((pol_wrap(z[i] * cl.inv[2], nc.z) * nc.y + pol_wrap(y[i] * cl.inv[1], nc.y)) * nc.x +
+                        pol_wrap(x[i] * cl.inv[0], nc.x));
+    idx[i] = i;
+}
+
+__global__ void k_pol_bounds(int n, const unsigned* __restrict__ skey, int* __restrict__ start,
+                             int* __restrict__ end) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const unsigned c = skey[i];
+    if (i == 0 || skey[i - 1] != c) start[c] = i;
+    if (i == n - 1 || skey[i + 1] != c) end[c] = i + 1;
+}
+
+// The site pair list (the reference's Verlet pairs with exclude_ttm's exclusions: every
+// site of another water within rcut), one directed row per site, warp per site.
+// Candidates: the sites of the 27 cells around the site's cell (orthorhombic boxes with
+// at least 3 cells of width >= rcut + 0.02 A per side), else every site.  An FP32
+// prefilter with a 0.01 A margin, then the reference's FP64 test.
 __global__ void k_pol_list(PolArgs a, int* __restrict__ nn, int* __restrict__ nbr, const float4* __restrict__ xf,
-                           float r2f, int* __restrict__ flag) {
+                           float r2f, int* __restrict__ flag, int3 nc, int cells, const int* __restrict__ sidx,
+                           const int* __restrict__ cstart, const int* __restrict__ cend) {
     const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (i >= a.n) return;
@@ -232,26 +267,48 @@ __global__ void k_pol_list(PolArgs a, int* __restrict__ nn, int* __restrict__ nb
     const float4 pi = xf[i];
     int* my = nbr + (size_t)i * a.cap;
     int cnt = 0;
-    for (int b = 0; b < a.n; b += 32) {
-        const int j = b + lane;
-        bool hit = false;
-        if (j < a.n && j != i && site_mol(a, j) != mi && dist2_img_f(a.cl, pi, xf[j]) < r2f) {
-            double dx, dy, dz;
-            sep(a, i, j, dx, dy, dz);
-            const double r2 = norm2(dx, dy, dz);
-            hit = a.rcut > __dsqrt_rn(r2) || a.rcsq > r2;
+    const int ncand = cells ? 27 : 1;
+    for (int c = 0; c < ncand; ++c) {
+        int beg = 0, end = a.n;
+        if (cells) {
+            const int cx = pol_wrap(a.x[i] * a.cl.inv[0], nc.x), cy = pol_wrap(a.y[i] * a.cl.inv[1], nc.y),
+                      cz = pol_wrap(a.z[i] * a.cl.inv[2], nc.z);
+            const int ox = c % 3 - 1, oy = (c / 3) % 3 - 1, oz = c / 9 - 1;
+            const int cc = (((cz + oz + nc.z) % nc.z) * nc.y + (cy + oy + nc.y) % nc.y) * nc.x + (cx + ox + nc.x) % nc.x;
+            beg = cstart[cc];
+            end = cend[cc];
         }
-        const unsigned bal = __ballot_sync(0xffffffffu, hit);
-        if (hit) {
-            const int slot = cnt + __popc(bal & ((1u << lane) - 1u));
-            if (slot < a.cap) my[slot] = j;
+        for (int b = beg; b < end; b += 32) {
+            const int q = b + lane;
+            bool hit = false;
+            int j = 0;
+            if (q < end) {
+                j = cells ? sidx[q] : q;
+                if (j != i && site_mol(a, j) != mi && dist2_img_f(a.cl, pi, xf[j]) < r2f) {
+                    double dx, dy, dz;
+                    sep(a, i, j, dx, dy, dz);
+                    const double r2 = norm2(dx, dy, dz);
+                    hit = a.rcut > __dsqrt_rn(r2) || a.rcsq > r2;
+                }
+            }
+            const unsigned bal = __ballot_sync(0xffffffffu, hit);
+            if (hit) {
+                const int slot = cnt + __popc(bal & ((1u << lane) - 1u));
+                if (slot < a.cap) my[slot] = j;
+            }
+            cnt += __popc(bal);
         }
-        cnt += __popc(bal);
     }
     if (lane == 0) {
         nn[i] = min(cnt, a.cap);
         if (cnt > a.cap) atomicOr(flag, 1);
     }
+}
+
+// polr^(1/6) per site, once per call (the pair kernels multiply two of them).
+__global__ void k_pol_polr6(PolArgs a, double* __restrict__ out) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < a.n) out[j] = pow(a.polr[j], 1.0 / 6.0);
 }
 
 // --- static real-space field and dipole tensors ---------------------------------------
@@ -261,7 +318,6 @@ __global__ void k_pol_static(PolArgs a) {
     if (i >= a.n) return;
     const int nn = a.nn[i];
     const size_t row = (size_t)i * a.cap, blk = (size_t)a.n * a.cap;
-    const double qi = a.q[i], pi = a.polr[i];
     const bool poli = a.polr2[i] > 1e-6;
     double e[3] = {0, 0, 0};
     for (int k = lane; k < nn; k += 32) {
@@ -275,7 +331,7 @@ __global__ void k_pol_static(PolArgs a) {
             double bbb[4];
             interp(a, rr, bbb);
             const double rsqi = 1.0 / r2, r3i = 1.0 / (rr * rr * rr), r5i = r3i * rsqi;
-            const double bb = pow(pi * a.polr[j], 1.0 / 6.0);
+            const double bb = a.polr6[i] * a.polr6[j];
             const double qj = a.q[j];
             double eki = kR4pie0 * qj * (bbb[1] + r3i);
             const double arq = a.ascd * pow4(rr / bb);
@@ -817,7 +873,6 @@ __device__ __forceinline__ float2 cmulf(float2 a, float2 b) {
 
 // Rows of the per-site axis factors: x rows l = 0..kmax1, then y rows m = -kmax2..kmax2,
 // then z rows n = -kmax3..kmax3 (each row n sites).
-__device__ __forceinline__ int row_y(const KArgs& k, int m) { return k.kmax[0] + 1 + k.kmax[1] + m; }
 __device__ __forceinline__ int row_z(const KArgs& k, int n) { return k.kmax[0] + 2 * k.kmax[1] + 2 + k.kmax[2] + n; }
 
 // FP32 dipole structure factors of the correction, phases formed on the fly:
@@ -1400,7 +1455,7 @@ __global__ void __launch_bounds__(kThreads) k_pol_ewald2p(PolArgs a, double g34,
             aei += 0.5 * edum;
             double espdum = (bbb[0] + 1.0 / rrr) * kR4pie0;
             double ffac = cicj * (r3i + bbb[1]) * kR4pie0;
-            const double bb = pow(a.polr[i] * a.polr[j], 1.0 / 6.0);
+            const double bb = a.polr6[i] * a.polr6[j];
             {
                 const double arob4 = a.ascc * pow4(rrr / bb);
                 if (arob4 < kDampCut) {
@@ -1764,7 +1819,8 @@ cudaError_t launch_msite_redistribute(int nw, double gamma, double* fx, double* 
 }
 
 void PolarState::release() {
-    void* p[] = {ercp, nn, nbr, flag, xf, tens, intra, fld, vesp, ae, eik, kv, kx2, lmn, sf, kterm, acc, kco, fac, md, vh,
+    void* p[] = {ercp, nn, nbr, flag, xf, tens, intra, fld, vesp, ae, eik, kv, kx2, lmn, sf, kterm, acc, kco, fac, md, vh, polr6,
+                 ckey, cskey, cidx, csidx, csort, cstart, cend,
                  tens32, r32, d32, e32, kco32, fac32, ktile, kaux, kcol, colk, kpart, cg_x, cg_r, cg_q, cg_z, vh32};
     for (void* q : p)
         if (q) cudaFree(q);
@@ -1783,7 +1839,12 @@ void PolarState::release() {
     ercp = nullptr;
     nn = nbr = flag = nullptr;
     xf = nullptr;
-    tens = intra = fld = vesp = ae = sf = kterm = acc = kco = vh = nullptr;
+    tens = intra = fld = vesp = ae = sf = kterm = acc = kco = vh = polr6 = nullptr;
+    ckey = cskey = nullptr;
+    cidx = csidx = cstart = cend = nullptr;
+    csort = nullptr;
+    cell_n_cap = ncell_cap = 0;
+    csort_bytes = 0;
     eik = fac = nullptr;
     md = nullptr;
     fac_cap = 0;
@@ -1838,6 +1899,40 @@ cudaError_t PolarState::table(double alpha, double rcut, cudaStream_t s) {
     if ((e = cudaStreamSynchronize(s))) return e;
     tab_alpha = alpha;
     tab_rcut = rcut;
+    return cudaSuccess;
+}
+
+// Cell-list buffers of the pair-list build: sort keys and indices (n) and cell bounds.
+cudaError_t PolarState::reserve_cells(int n, int ncell) {
+    cudaError_t e;
+    if (n > cell_n_cap) {
+        void* p[] = {ckey, cskey, cidx, csidx, csort};
+        for (void* q : p)
+            if (q) cudaFree(q);
+        ckey = cskey = nullptr;
+        cidx = csidx = nullptr;
+        csort = nullptr;
+        cell_n_cap = 0;
+        const size_t m = (size_t)std::max(n, 1);
+        if ((e = cudaMalloc(&ckey, m * sizeof(unsigned)))) return e;
+        if ((e = cudaMalloc(&cskey, m * sizeof(unsigned)))) return e;
+        if ((e = cudaMalloc(&cidx, m * sizeof(int)))) return e;
+        if ((e = cudaMalloc(&csidx, m * sizeof(int)))) return e;
+        size_t b = 0;
+        if ((e = cub::DeviceRadixSort::SortPairs(nullptr, b, ckey, cskey, cidx, csidx, (int)m))) return e;
+        if ((e = cudaMalloc(&csort, std::max(b, (size_t)1)))) return e;
+        csort_bytes = b;
+        cell_n_cap = n;
+    }
+    if (ncell > ncell_cap) {
+        if (cstart) cudaFree(cstart);
+        if (cend) cudaFree(cend);
+        cstart = cend = nullptr;
+        ncell_cap = 0;
+        if ((e = cudaMalloc(&cstart, ncell * sizeof(int)))) return e;
+        if ((e = cudaMalloc(&cend, ncell * sizeof(int)))) return e;
+        ncell_cap = ncell;
+    }
     return cudaSuccess;
 }
 
@@ -1913,14 +2008,14 @@ cudaError_t PolarState::reserve(int nw, int K, size_t nfac) {
     // a capacity is zeroed before its buffers are replaced, so a failed allocation leaves
     // nothing that a later call would take for allocated
     if (n > n_cap || cap != cap_alloc) {
-        void* p[] = {nn, nbr, xf, tens, fld, vesp, ae, md, vh};
+        void* p[] = {nn, nbr, xf, tens, fld, vesp, ae, md, vh, polr6};
         for (void* q : p)
             if (q) cudaFree(q);
         n_cap = 0;
         cap_alloc = 0;
         nn = nbr = nullptr;
         xf = nullptr;
-        tens = fld = vesp = ae = vh = nullptr;
+        tens = fld = vesp = ae = vh = polr6 = nullptr;
         md = nullptr;
         const size_t m = (size_t)std::max(n, 1);
         if ((e = cudaMalloc(&nn, m * sizeof(int)))) return e;
@@ -1932,6 +2027,7 @@ cudaError_t PolarState::reserve(int nw, int K, size_t nfac) {
         if ((e = cudaMalloc(&ae, m * sizeof(double)))) return e;
         if ((e = cudaMalloc(&md, m * sizeof(double4)))) return e;
         if ((e = cudaMalloc(&vh, 12 * m * sizeof(double)))) return e;
+        if ((e = cudaMalloc(&polr6, m * sizeof(double)))) return e;
         n_cap = n;
         cap_alloc = cap;
     }
@@ -2158,6 +2254,7 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
         b.efm = fld + 9 * (size_t)n;
         b.vesp = vesp;
         b.ae = ae;
+        b.polr6 = polr6;
         b.acc = acc;
     };
     a.cl = cl;
@@ -2220,13 +2317,32 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
         converged = true;
         return cudaSuccess;
     }
-    // list (grows until every row fits)
+    // list (grows until every row fits); cell-sorted candidates where the box allows
     const float r2f = (float)((rcut + 0.01) * (rcut + 0.01));
+    int3 nc = make_int3(1, 1, 1);
+    int cells = 0;
+    if (cl.imcon == 1 || cl.imcon == 2) {
+        const double wcell = rcut + 0.02;
+        nc = make_int3((int)(cl.c[0] / wcell), (int)(cl.c[4] / wcell), (int)(cl.c[8] / wcell));
+        cells = nc.x >= 3 && nc.y >= 3 && nc.z >= 3 && (long)nc.x * nc.y * nc.z < (1L << 24);
+        if (!cells) nc = make_int3(1, 1, 1);
+    }
+    if (cells) {
+        if ((e = reserve_cells(n, nc.x * nc.y * nc.z))) return e;
+        k_pol_keys<<<blocks(n, kThreads), kThreads, 0, s>>>(n, x, y, z, cl, nc, ckey, cidx);
+        size_t b = csort_bytes;
+        if ((e = cub::DeviceRadixSort::SortPairs(csort, b, ckey, cskey, cidx, csidx, n, 0, 32, s))) return e;
+        if ((e = cudaMemsetAsync(cstart, 0, (size_t)nc.x * nc.y * nc.z * sizeof(int), s))) return e;
+        if ((e = cudaMemsetAsync(cend, 0, (size_t)nc.x * nc.y * nc.z * sizeof(int), s))) return e;
+        k_pol_bounds<<<blocks(n, kThreads), kThreads, 0, s>>>(n, cskey, cstart, cend);
+        launches += 3;
+    }
     for (;;) {
         bind(a);
         k_pol_f32<<<blocks(n, kThreads), kThreads, 0, s>>>(n, x, y, z, xf);
         if ((e = cudaMemsetAsync(flag, 0, sizeof(int), s))) return e;
-        k_pol_list<<<blocks(32L * n, kThreads), kThreads, 0, s>>>(a, nn, nbr, xf, r2f, flag);
+        k_pol_list<<<blocks(32L * n, kThreads), kThreads, 0, s>>>(a, nn, nbr, xf, r2f, flag, nc, cells, csidx, cstart,
+                                                                   cend);
         launches += 2;
         int fh = 0;
         if ((e = cudaMemcpyAsync(acc_h, flag, sizeof(int), cudaMemcpyDeviceToHost, s))) return e;
@@ -2239,9 +2355,10 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
     }
     bind(a);
     bindk(k);
+    k_pol_polr6<<<blocks(n, kThreads), kThreads, 0, s>>>(a, polr6);
     k_pol_static<<<blocks(32L * n, kThreads), kThreads, 0, s>>>(a);
     k_pol_intra_static<<<blocks(nw, kThreads), kThreads, 0, s>>>(a);
-    launches += 2;
+    launches += 3;
     k_pol_mask<<<blocks(n, kThreads), kThreads, 0, s>>>(a, md);
     ++launches;
     if (K) {
