@@ -906,25 +906,34 @@ __device__ __forceinline__ void stage_tile(const KArgs& k, int4 tl, int rowp, in
     }
 }
 
+// Two k vectors per thread: the block takes two consecutive tiles of kSfThreads vectors
+// (their columns are contiguous), so each staged site tile serves 512 vectors.
 __global__ void __launch_bounds__(kSfThreads) k_pol_sfd32(KArgs k, MixArgs m, int schunk, int rowp,
                                                           double* __restrict__ part) {
     extern __shared__ float4 sfd_smem[];
     float4* ds = sfd_smem;                                   // [kSfTile]
     float2* fs = reinterpret_cast<float2*>(sfd_smem + kSfTile);   // [kSfTile][rowp]
-    const int kk = blockIdx.x * kSfThreads + threadIdx.x;
-    const int4 tl = k.ktile[blockIdx.x];                     // first column, columns
-    int rc = 0, rn = 0;
-    float kx = 0.f, ky = 0.f, kz = 0.f;
-    if (kk < k.K) {
-        rc = k.kaux[kk].x;
-        rn = tl.y + k.lmn[kk].z + k.kmax[2];
-        const double4 kv = k.kv[kk];
-        kx = (float)kv.x;
-        ky = (float)kv.y;
-        kz = (float)kv.z;
+    const int nkt = (k.K + kSfThreads - 1) / kSfThreads;
+    const int4 ta = k.ktile[2 * blockIdx.x];
+    const int4 tb = 2 * blockIdx.x + 1 < nkt ? k.ktile[2 * blockIdx.x + 1] : ta;
+    const int4 tl = make_int4(ta.x, max(ta.x + ta.y, tb.x + tb.y) - ta.x, 0, 0);   // first column, columns
+    int rc[2] = {0, 0}, rn[2] = {0, 0};
+    float kx[2] = {0.f, 0.f}, ky[2] = {0.f, 0.f}, kz[2] = {0.f, 0.f};
+    const int kk0 = 2 * blockIdx.x * kSfThreads + threadIdx.x;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const int kk = kk0 + h * kSfThreads;
+        if (kk < k.K) {
+            rc[h] = k.kaux[kk].z - tl.x;
+            rn[h] = tl.y + k.lmn[kk].z + k.kmax[2];
+            const double4 kv = k.kv[kk];
+            kx[h] = (float)kv.x;
+            ky[h] = (float)kv.y;
+            kz[h] = (float)kv.z;
+        }
     }
     const int sb = blockIdx.y * schunk, se = min(k.n, sb + schunk);
-    double ac = 0.0, as = 0.0;
+    double ac[2] = {0.0, 0.0}, as[2] = {0.0, 0.0};
     for (int s0 = sb; s0 < se; s0 += kSfTile) {
         const int ns = min(kSfTile, se - s0);
         __syncthreads();
@@ -932,23 +941,33 @@ __global__ void __launch_bounds__(kSfThreads) k_pol_sfd32(KArgs k, MixArgs m, in
         for (int t = threadIdx.x; t < kSfTile; t += kSfThreads)
             ds[t] = t < ns ? m.d32[s0 + t] : make_float4(0.f, 0.f, 0.f, 0.f);
         __syncthreads();
-        float c = 0.f, sn = 0.f;
-#pragma unroll 8
+        float c0 = 0.f, s0_ = 0.f, c1 = 0.f, s1 = 0.f;
+#pragma unroll 4
         for (int t = 0; t < kSfTile; ++t) {
             const float2* f = fs + t * rowp;
-            const float2 e = cmulf(f[rc], f[rn]);
             const float4 d = ds[t];
-            const float pk = kx * d.x + ky * d.y + kz * d.z;
-            c += e.x * pk;
-            sn += e.y * pk;
+            const float2 e0 = cmulf(f[rc[0]], f[rn[0]]);
+            const float2 e1 = cmulf(f[rc[1]], f[rn[1]]);
+            const float p0 = kx[0] * d.x + ky[0] * d.y + kz[0] * d.z;
+            const float p1 = kx[1] * d.x + ky[1] * d.y + kz[1] * d.z;
+            c0 += e0.x * p0;
+            s0_ += e0.y * p0;
+            c1 += e1.x * p1;
+            s1 += e1.y * p1;
         }
-        ac += (double)c;
-        as += (double)sn;
+        ac[0] += (double)c0;
+        as[0] += (double)s0_;
+        ac[1] += (double)c1;
+        as[1] += (double)s1;
     }
-    if (kk < k.K) {
-        double* p = part + 2 * ((size_t)blockIdx.y * k.K + kk);
-        p[0] = ac;
-        p[1] = as;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const int kk = kk0 + h * kSfThreads;
+        if (kk < k.K) {
+            double* p = part + 2 * ((size_t)blockIdx.y * k.K + kk);
+            p[0] = ac[h];
+            p[1] = as[h];
+        }
     }
 }
 
@@ -2193,8 +2212,8 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
     // FP32 structure factors: per tile of kSfThreads k vectors the x and y factor rows it
     // uses (k vectors come l-major, so a tile spans few l); the widest tile sizes the
     // shared-memory rows (odd, so the transposed stores spread over the banks)
-    int rowp = 1;
-    const int nkt = (K + kSfThreads - 1) / kSfThreads;
+    int rowp = 1, rowp2 = 1;
+    const int nkt = (K + kSfThreads - 1) / kSfThreads, nkt2 = (nkt + 1) / 2;
     // the (l, m) columns of the k vectors (runs of n): l << 16 | y row, first k and count
     hkcol.clear();
     hcolk.clear();
@@ -2226,15 +2245,23 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
                                      (hlmn[q].z + kmax[2]) * kThreads);
         }
         rowp |= 1;
+        // k_pol_sfd32 takes two tiles per block: the rows of both
+        for (int t = 0; t < nkt; t += 2) {
+            const int4 ta = hktile[t], tb = t + 1 < nkt ? hktile[t + 1] : ta;
+            rowp2 = std::max(rowp2, std::max(ta.x + ta.y, tb.x + tb.y) - ta.x + 2 * kmax[2] + 1);
+        }
+        rowp2 |= 1;
         if ((e = cudaMemcpyAsync(ktile, hktile.data(), nkt * sizeof(int4), cudaMemcpyHostToDevice, s))) return e;
         if ((e = cudaMemcpyAsync(kaux, hkaux.data(), K * sizeof(int4), cudaMemcpyHostToDevice, s))) return e;
     }
-    const size_t sfd_smem = kSfTile * (sizeof(float4) + (size_t)rowp * sizeof(float2));
-    const size_t sfx_smem0 = sfd_smem, sfx_smem1 = kSfTile * (4 * sizeof(float4) + (size_t)rowp * sizeof(float2));
+    const size_t sfd_smem = kSfTile * (sizeof(float4) + (size_t)rowp2 * sizeof(float2));
+    const size_t sfx_smem0 = kSfTile * (sizeof(float4) + (size_t)rowp * sizeof(float2)),
+                 sfx_smem1 = kSfTile * (4 * sizeof(float4) + (size_t)rowp * sizeof(float2));
     const size_t gat_smem = gather_smem(kmax);
     if (mixed && K) {
         // the FP32 k-space passes keep their factor rows in shared memory (kmax up to ~100)
-        if (rowp > kMaxRows || sfx_smem1 > kMaxDynSmem || gat_smem > kMaxDynSmem) return cudaErrorInvalidValue;
+        if (rowp > kMaxRows || sfx_smem1 > kMaxDynSmem || sfd_smem > kMaxDynSmem || gat_smem > kMaxDynSmem)
+            return cudaErrorInvalidValue;
         if ((e = allow_dynamic_smem())) return e;
     }
 
@@ -2384,7 +2411,13 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
     const int nsc = nkt ? std::max(1, std::min((n + kSfTile - 1) / kSfTile, (4 * nsm + nkt - 1) / nkt)) : 1;
     const int schunk = ((n + nsc - 1) / nsc + kSfTile - 1) / kSfTile * kSfTile;
     const int nsc_used = (n + schunk - 1) / schunk;
-    if ((e = reserve_part(std::max((size_t)6 * std::max(nc1, nc2) * n, (size_t)30 * nsc_used * K)))) return e;
+    // k_pol_sfd32 (two tiles per block): its own site chunks for about four blocks per SM
+    const int nsc2 = nkt2 ? std::max(1, std::min((n + kSfTile - 1) / kSfTile, (4 * nsm + nkt2 - 1) / nkt2)) : 1;
+    const int schunk2 = ((n + nsc2 - 1) / nsc2 + kSfTile - 1) / kSfTile * kSfTile;
+    const int nsc2_used = (n + schunk2 - 1) / schunk2;
+    if ((e = reserve_part(std::max(std::max((size_t)6 * std::max(nc1, nc2) * n, (size_t)30 * nsc_used * K),
+                                   (size_t)2 * nsc2_used * K))))
+        return e;
     int kf_calls = 0;          // profiling: k_pol_kfield launches of this call with events
     double kf_call_flops = 0.0;
     auto fields64 = [&](bool first) {
@@ -2507,8 +2540,8 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
                 for (int sweep = 0; sweep < 100; ++sweep) {
                     k_pol_dd32<<<blocks(32L * n, kThreads), kThreads, 0, s>>>(a, d32, e32);
                     if (K) {
-                        k_pol_sfd32<<<dim3(nkt, nsc_used), kSfThreads, sfd_smem, s>>>(k, m, schunk, rowp, kpart);
-                        k_pol_sfd32_sum<<<blocks(K, kThreads), kThreads, 0, s>>>(k, nsc_used, kpart);
+                        k_pol_sfd32<<<dim3(nkt2, nsc2_used), kSfThreads, sfd_smem, s>>>(k, m, schunk2, rowp2, kpart);
+                        k_pol_sfd32_sum<<<blocks(K, kThreads), kThreads, 0, s>>>(k, nsc2_used, kpart);
                         k_pol_kfield32<<<dim3(sblk1, nc1), kThreads, gat_smem, s>>>(k, kc1, (float*)kpart);
                         k_pol_kfield32_sum<<<sblk1, kThreads, 0, s>>>(k, a, m, nc1, (const float*)kpart);
                         launches += 4;
