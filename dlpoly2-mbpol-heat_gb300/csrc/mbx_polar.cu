@@ -288,7 +288,7 @@ __global__ void k_pol_list(PolArgs a, int* __restrict__ nn, int* __restrict__ nb
                     double dx, dy, dz;
                     sep(a, i, j, dx, dy, dz);
                     const double r2 = norm2(dx, dy, dz);
-                    hit = a.rcut > __dsqrt_rn(r2) || a.rcsq > r2;
+                    hit = a.rcsq > r2 || a.rcut > __dsqrt_rn(r2);   // the root only near the cut
                 }
             }
             const unsigned bal = __ballot_sync(0xffffffffu, hit);
