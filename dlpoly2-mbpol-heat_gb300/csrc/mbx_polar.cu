@@ -268,6 +268,9 @@ __global__ void k_pol_list(PolArgs a, int* __restrict__ nn, int* __restrict__ nb
     int* my = nbr + (size_t)i * a.cap;
     int cnt = 0;
     const int ncand = cells ? 27 : 1;
+    // FP32 box constants once (converting them per candidate occupies the FP64 pipe)
+    const float bx = (float)a.cl.c[0], by = (float)a.cl.c[4], bz = (float)a.cl.c[8];
+    const float ibx = (float)a.cl.inv[0], iby = (float)a.cl.inv[1], ibz = (float)a.cl.inv[2];
     for (int c = 0; c < ncand; ++c) {
         int beg = 0, end = a.n;
         if (cells) {
@@ -284,7 +287,20 @@ __global__ void k_pol_list(PolArgs a, int* __restrict__ nn, int* __restrict__ nb
             int j = 0;
             if (q < end) {
                 j = cells ? sidx[q] : q;
-                if (j != i && site_mol(a, j) != mi && dist2_img_f(a.cl, pi, xf[j]) < r2f) {
+                bool near = false;
+                if (j != i && site_mol(a, j) != mi) {
+                    const float4 pj = xf[j];
+                    if (cells) {   // orthorhombic
+                        float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+                        dx -= bx * rintf(dx * ibx);
+                        dy -= by * rintf(dy * iby);
+                        dz -= bz * rintf(dz * ibz);
+                        near = dx * dx + dy * dy + dz * dz < r2f;
+                    } else {
+                        near = dist2_img_f(a.cl, pi, pj) < r2f;
+                    }
+                }
+                if (near) {
                     double dx, dy, dz;
                     sep(a, i, j, dx, dy, dz);
                     const double r2 = norm2(dx, dy, dz);
