@@ -1224,6 +1224,10 @@ extern "C" int mbx_water_step(mbx_context* ctx, int precision, int imcon, const 
 // context's worker lanes.  A lane is a child context (its own stream and device buffers,
 // kept between calls) driven by its own host thread for the call, so the boxes' kernels
 // and host round trips overlap; boxes are taken largest first from a shared counter.
+void mbx_set_error_text(mbx_context* ctx, const char* msg) {
+    if (ctx && msg) std::snprintf(ctx->err, sizeof ctx->err, "%s", msg);
+}
+
 extern "C" int mbx_set_precond_sweeps(mbx_context* ctx, int sweeps) {
     if (!ctx) return MBX_ERR_ARG;
     if (sweeps < 1 || sweeps > 9 || sweeps % 2 == 0)

@@ -322,3 +322,7 @@ struct MultiBoxes {
 };
 
 }  // namespace mbx
+
+// The context's last error text (host code outside mbx_capi.cu: the i-PI driver).
+struct mbx_context;
+void mbx_set_error_text(mbx_context* ctx, const char* msg);

@@ -103,6 +103,11 @@ size_t step_footprint_bytes(int nw, int K) {
 
 }  // namespace
 
+extern "C" void mbx_polar_params_for_cell(const double* cell, double* prm) {
+    int K = 0;
+    step_params(cell, prm, &K);
+}
+
 struct mbx_server {
     int device = 0;
     size_t budget = 0;

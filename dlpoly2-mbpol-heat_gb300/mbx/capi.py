@@ -17,6 +17,7 @@ HEADER = os.path.join(REPO, "include", "mbx.h")
 
 FP64 = 0
 MIXED = 1
+ERR_ARG = 1
 ERR_CONVERGE = 5
 NSCALARS = 18
 NBOXSCALARS = NSCALARS + 14
@@ -32,6 +33,45 @@ _lib = None
 
 class MbxError(RuntimeError):
     pass
+
+
+# mbx_ipi_force_fn: (user, replica, natoms, cell[9], xyz[3n], energy*, forces[3n], stress[9], moldip[n])
+IPI_FORCE_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                           C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double),
+                           C.POINTER(C.c_double))
+
+
+def polar_params_for_cell(cell):
+    """mbx_polar_params_for_cell: the server's Ewald and dipole settings for a cell"""
+    prm = np.zeros(15)
+    load().mbx_polar_params_for_cell(_p(_f64(cell)), _p(prm))
+    return prm
+
+
+def ipi_run_callback(address, fn, max_steps=0):
+    """mbx_ipi_run_callback with a Python force function
+    fn(replica, cell[9], xyz[n, 3]) -> (energy, forces[n, 3], stress[9], moldip[n/3, 3]) in DL_POLY
+    units; returns (status, steps, error text)."""
+    lib = load()
+
+    def cb(user, replica, nat, cell, xyz, energy, forces, stress, moldip):
+        try:
+            c = np.ctypeslib.as_array(cell, (9,)).copy()
+            x = np.ctypeslib.as_array(xyz, (3 * nat,)).reshape(nat, 3).copy()
+            e, f, st, md = fn(replica, c, x)
+            energy[0] = float(e)
+            np.ctypeslib.as_array(forces, (3 * nat,))[:] = np.asarray(f, np.float64).ravel()
+            np.ctypeslib.as_array(stress, (9,))[:] = np.asarray(st, np.float64).ravel()
+            np.ctypeslib.as_array(moldip, (3 * (nat // 3),))[:] = np.asarray(md, np.float64).ravel()
+            return 0
+        except Exception:   # reported to the caller as a failed evaluation
+            return ERR_ARG
+
+    cfn = IPI_FORCE_FN(cb)
+    steps = C.c_long(0)
+    err = C.create_string_buffer(256)
+    rc = lib.mbx_ipi_run_callback(address.encode(), cfn, None, int(max_steps), C.byref(steps), err, 256)
+    return rc, int(steps.value), err.value.decode()
 
 
 def header_functions():
@@ -106,6 +146,11 @@ def load(path=None):
     L.mbx_set_lanes.argtypes = [C.c_void_p, C.c_int]
     L.mbx_set_precond_sweeps.argtypes = [C.c_void_p, C.c_int]
     L.mbx_polar_field_timing.argtypes = [C.c_void_p, _D, _D, C.POINTER(C.c_long)]
+    L.mbx_polar_params_for_cell.argtypes = [_D, _D]
+    L.mbx_polar_params_for_cell.restype = None
+    L.mbx_ipi_run_callback.argtypes = [C.c_char_p, IPI_FORCE_FN, C.c_void_p, C.c_long, C.POINTER(C.c_long),
+                                       C.c_char_p, C.c_int]
+    L.mbx_ipi_run.argtypes = [C.c_void_p, C.c_char_p, C.c_int, _D, C.c_int, C.c_long, C.POINTER(C.c_long)]
     L.mbx_water_step_multi.argtypes = ([C.c_void_p, C.c_int, C.c_int, _I, _D, _I, _D, _D, _D, _I, _I] + [_D] * 16 +
                                        [_I])
     L.mbx_water_step_device.argtypes = [C.c_void_p, C.c_int, C.c_int, _D, C.c_int, C.c_int, _D] + \
@@ -368,6 +413,15 @@ class Context:
             self._check(rc, "mbx_water_step")
         return dict(status=rc, forces=f.T.copy(), atomic_energy=ae, chge=q, scalars=sc, dipoles=dip.T.copy(),
                     sites=np.stack([x, y, z], 1))
+
+    def ipi_run(self, address, precision=MIXED, polar_prm=None, dispersion=False, max_steps=0):
+        """mbx_ipi_run: i-PI driver mode on this context; returns the force replies sent"""
+        steps = C.c_long(0)
+        prm = None if polar_prm is None else _f64(polar_prm)
+        rc = self.lib.mbx_ipi_run(self.h, address.encode(), precision, _p(prm), 1 if dispersion else 0,
+                                  int(max_steps), C.byref(steps))
+        self._check(rc, "mbx_ipi_run")
+        return int(steps.value)
 
     def set_precond_sweeps(self, sweeps):
         self._check(self.lib.mbx_set_precond_sweeps(self.h, int(sweeps)), "mbx_set_precond_sweeps")

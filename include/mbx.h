@@ -310,6 +310,46 @@ int mbx_water_step_multi(mbx_context* ctx, int precision, int nbox, const int* i
                          double* chge, double* scalars, int* status);
 
 /*
+ * The Ewald and dipole settings the server uses for a cell (cell[9], Angstrom): rcut =
+ * min(9, 0.49 x the narrowest width), alpha = 2.7 / rcut, kmax per axis scaled from the
+ * 256-water box's alpha 0.3 / kmax 8, the vmbpol Thole and smearing constants, toler
+ * 1e-8 D, SOR weight 0.3, maxit 22581; written to prm[15] in mbx_polar_forces' layout.
+ */
+void mbx_polar_params_for_cell(const double* cell, double* prm);
+
+/*
+ * i-PI driver mode: the reference's IPI_INIT / IPI_STEP (SOURCE/ipi.f90:33-198) with its
+ * socket wrapper (SOURCE/sockets.c).  The client connects to an i-PI server at `address`:
+ * "inet:host:port", "unix:name:port" (the socket /tmp/ipi_<name>), or "host:port".  It
+ * answers STATUS (HAVEDATA / READY / NEEDINIT), INIT (replica index and parameter string),
+ * POSDATA (cell, inverse, atoms, positions in bohr: the configuration is evaluated) and
+ * GETFORCE (FORCEREADY, energy, atoms, forces, virial in atomic units, then the water
+ * dipoles as text), until EXIT or max_steps force replies (0: no limit).  Unit factors are
+ * the reference's single-precision constants (SOURCE/ipi.f90:72-77); the cell and the
+ * virial are transposed as there.
+ *   mbx_ipi_run           evaluates each configuration of nat = 3 nw atoms (O, H, H per
+ *                         water) with mbx_water_step on ctx: polar_prm[15], or NULL for
+ *                         mbx_polar_params_for_cell of each cell; dispersion != 0 uses the
+ *                         mbx_disp_setup of ctx with types 1 (O), 2 (H), 3 (M).  Each
+ *                         replica's dipoles are the warm start of its next configuration.
+ *                         The energy sent is the sum of the evaluated terms (the dispersion
+ *                         long-range correction, a constant of the volume, is not included).
+ *   mbx_ipi_run_callback  the protocol with a caller's force function: it gets the replica,
+ *                         atoms, cell[9] and interleaved positions in Angstrom and returns
+ *                         the energy, interleaved forces and stress[9] in DL_POLY units
+ *                         (10 J/mol, Angstrom) and 3 values per water for the dipole text;
+ *                         it returns MBX_OK (or MBX_ERR_CONVERGE) to continue.  err[errlen]
+ *                         receives the reason of a failure.
+ * Both return MBX_OK after EXIT or max_steps, else the failure's status.
+ */
+typedef int (*mbx_ipi_force_fn)(void* user, int replica, int natoms, const double* cell, const double* xyz,
+                                double* energy, double* forces, double* stress, double* moldip);
+int mbx_ipi_run_callback(const char* address, mbx_ipi_force_fn fn, void* user, long max_steps, long* steps_done,
+                         char* err, int errlen);
+int mbx_ipi_run(mbx_context* ctx, const char* address, int precision, const double* polar_prm, int dispersion,
+                long max_steps, long* steps_done);
+
+/*
  * Continuous-batching force server.  `slots` worker slots, each with its own context and
  * CUDA stream on `device`, evaluate independent water boxes concurrently; a FIFO queue
  * admits the next request as soon as a slot is free and its estimated device-memory
