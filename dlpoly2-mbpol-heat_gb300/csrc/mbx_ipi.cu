@@ -204,7 +204,7 @@ extern "C" int mbx_ipi_run_callback(const char* address, mbx_ipi_force_fn fn, vo
             ok = send_header(fd, hasdata ? "HAVEDATA" : (imginit ? "READY" : "NEEDINIT"));
         } else if (t == "INIT") {
             int32_t rid = 0, len = 0;
-            ok = read_all(fd, &rid, 4) && read_all(fd, &len, 4) && len >= 0;
+            ok = read_all(fd, &rid, 4) && read_all(fd, &len, 4) && len >= 0 && len <= (1 << 24);
             std::vector<char> par(ok ? (size_t)len : 0);
             ok = ok && (len == 0 || read_all(fd, par.data(), (size_t)len));
             replica = rid;
@@ -212,7 +212,8 @@ extern "C" int mbx_ipi_run_callback(const char* address, mbx_ipi_force_fn fn, vo
         } else if (t == "POSDATA") {
             double hb[9], hi[9];
             int32_t n = 0;
-            if (!(read_all(fd, hb, sizeof hb) && read_all(fd, hi, sizeof hi) && read_all(fd, &n, 4) && n > 0)) {
+            if (!(read_all(fd, hb, sizeof hb) && read_all(fd, hi, sizeof hi) && read_all(fd, &n, 4) && n > 0 &&
+                  n <= 100000000)) {
                 rc = fail(MBX_ERR_ARG, "i-PI POSDATA: bad cell or atom count");
                 break;
             }

@@ -84,3 +84,12 @@ def test_ipi_max_steps_and_errors(lib):
     assert rc == capi.ERR_ARG and steps == 0 and "connect" in err
     rc, _, err = capi.ipi_run_callback("nonsense", force)
     assert rc == capi.ERR_ARG and "address" in err
+
+
+def test_polar_params_for_cell_matches_systems(lib):
+    for cell in ([19.73, 0, 0, 0, 19.73, 0, 0, 0, 19.73], [49.7, 0, 0, 0, 49.7, 0, 0, 0, 49.7],
+                 [12.4, 0, 0, 2.0, 12.0, 0, 1.0, -1.5, 13.0]):
+        got = capi.polar_params_for_cell(cell)
+        from mbx import systems
+        want = systems.polar_params_for(np.array(cell, np.float64))
+        np.testing.assert_allclose(got, want, rtol=1e-14, atol=0)
