@@ -182,3 +182,29 @@ def test_polar_phase_timings(mbx_ctx, oracle_lib):
             assert kv > 0 and (ms >= 0).all() and ms.sum() > 0
     finally:
         mbx_ctx.set_profiling(False)
+
+
+def test_polar_mixed_preconditioner_settings(mbx_ctx, oracle_lib):
+    """The mixed solve's preconditioner (mbx_set_precond_sweeps: 1 diagonal, 3 default, 5)
+    changes the iteration count, not the converged results beyond the mixed budgets; even
+    counts (not positive definite in general) are refused."""
+    box = systems.config0()
+    prm = systems.polar_params(alpha=0.3, rcut=9.0, kmax=(8, 8, 8), toler_debye=1e-8)
+    sites, q, dp, polr, polr2, prm = _case(oracle_lib, box, prm)
+    ref = oracle_lib.polar(sites, box.cell, box.imcon, box.nw, q, dp, polr, polr2, prm, vel=box.vel)
+    with pytest.raises(capi.MbxError):
+        mbx_ctx.set_precond_sweeps(2)
+    sweeps = {}
+    try:
+        for p in (1, 3, 5):
+            mbx_ctx.set_precond_sweeps(p)
+            got = mbx_ctx.polar(sites, box.cell, box.imcon, box.nw, q, dp, polr, polr2, prm, vel=box.vel,
+                                precision=capi.MIXED)
+            sweeps[p] = mbx_ctx.polar_inner_sweeps()
+            assert got["deltadip"] <= prm[3]
+            assert abs(got["engcpe"] - ref["engcpe"]) <= 1e-8 * abs(ref["engcpe"])
+            f, fr = got["forces"], ref["forces"]
+            assert np.sqrt(np.mean((f - fr) ** 2)) <= 1e-6 * np.sqrt(np.mean(fr ** 2))
+    finally:
+        mbx_ctx.set_precond_sweeps(3)
+    assert min(sweeps.values()) > 0
