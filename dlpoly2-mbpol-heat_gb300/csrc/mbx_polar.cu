@@ -2415,8 +2415,17 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
     double deltadip = 0.0;
     // k vectors per chunk of the field / force gathers: about four blocks per SM in all
     const int sblk2 = (int)blocks(n, 2 * kThreads), sblk1 = (int)blocks(n, kThreads);
+    // A grid that is not a multiple of the SM count leaves some SMs one block (or a last
+    // short wave) longer than the rest: take the smallest chunk count from the four-per-SM
+    // target up to four times it that makes sites x chunks a multiple of the SMs, when
+    // there is one.
     auto chunking = [&](int sblk, int& kchunk, int& nchunk) {
-        const int want = std::max(1, (4 * nsm + sblk - 1) / sblk);
+        int want = std::max(1, (4 * nsm + sblk - 1) / sblk);
+        for (int c = want; c <= 4 * want; ++c)
+            if (((long)sblk * c) % nsm == 0) {
+                want = c;
+                break;
+            }
         kchunk = std::max(kKTile, (int)(((K + want - 1) / want + kKTile - 1) / kKTile) * kKTile);
         nchunk = K ? (K + kchunk - 1) / kchunk : 0;
     };
