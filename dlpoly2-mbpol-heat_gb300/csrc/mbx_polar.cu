@@ -257,9 +257,13 @@ __global__ void k_pol_bounds(int n, const unsigned* __restrict__ skey, int* __re
 // Candidates: the sites of the 27 cells around the site's cell (orthorhombic boxes with
 // at least 3 cells of width >= rcut + 0.02 A per side), else every site.  An FP32
 // prefilter with a 0.01 A margin, then the reference's FP64 test.
+// A pair whose FP32 distance is inside rcut - 0.01 A (r2in) is inside rcut in FP64 too (the
+// FP32 error of r^2 is below 1e-3 A^2 for coordinates under 1e3 A), so only the thin shell
+// between r2in and r2f takes the reference's FP64 test.
 __global__ void k_pol_list(PolArgs a, int* __restrict__ nn, int* __restrict__ nbr, const float4* __restrict__ xf,
-                           float r2f, int* __restrict__ flag, int3 nc, int cells, const int* __restrict__ sidx,
-                           const int* __restrict__ cstart, const int* __restrict__ cend) {
+                           float r2f, float r2in, int* __restrict__ flag, int3 nc, int cells,
+                           const int* __restrict__ sidx, const int* __restrict__ cstart,
+                           const int* __restrict__ cend) {
     const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (i >= a.n) return;
@@ -287,20 +291,25 @@ __global__ void k_pol_list(PolArgs a, int* __restrict__ nn, int* __restrict__ nb
             int j = 0;
             if (q < end) {
                 j = cells ? sidx[q] : q;
-                bool near = false;
+                bool near = false, inside = false;
                 if (j != i && site_mol(a, j) != mi) {
                     const float4 pj = xf[j];
+                    float d2;
                     if (cells) {   // orthorhombic
                         float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
                         dx -= bx * rintf(dx * ibx);
                         dy -= by * rintf(dy * iby);
                         dz -= bz * rintf(dz * ibz);
-                        near = dx * dx + dy * dy + dz * dz < r2f;
+                        d2 = dx * dx + dy * dy + dz * dz;
                     } else {
-                        near = dist2_img_f(a.cl, pi, pj) < r2f;
+                        d2 = dist2_img_f(a.cl, pi, pj);
                     }
+                    near = d2 < r2f;
+                    inside = d2 < r2in;
                 }
-                if (near) {
+                if (inside) {
+                    hit = true;
+                } else if (near) {
                     double dx, dy, dz;
                     sep(a, i, j, dx, dy, dz);
                     const double r2 = norm2(dx, dy, dz);
@@ -2362,6 +2371,7 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
     }
     // list (grows until every row fits); cell-sorted candidates where the box allows
     const float r2f = (float)((rcut + 0.01) * (rcut + 0.01));
+    const float r2in = rcut > 0.02 ? (float)((rcut - 0.01) * (rcut - 0.01)) : 0.f;
     int3 nc = make_int3(1, 1, 1);
     int cells = 0;
     if (cl.imcon == 1 || cl.imcon == 2) {
@@ -2384,8 +2394,8 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
         bind(a);
         k_pol_f32<<<blocks(n, kThreads), kThreads, 0, s>>>(n, x, y, z, xf);
         if ((e = cudaMemsetAsync(flag, 0, sizeof(int), s))) return e;
-        k_pol_list<<<blocks(32L * n, kThreads), kThreads, 0, s>>>(a, nn, nbr, xf, r2f, flag, nc, cells, csidx, cstart,
-                                                                   cend);
+        k_pol_list<<<blocks(32L * n, kThreads), kThreads, 0, s>>>(a, nn, nbr, xf, r2f, r2in, flag, nc, cells, csidx,
+                                                                   cstart, cend);
         launches += 2;
         int fh = 0;
         if ((e = cudaMemcpyAsync(acc_h, flag, sizeof(int), cudaMemcpyDeviceToHost, s))) return e;
