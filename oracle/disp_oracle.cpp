@@ -1,6 +1,9 @@
 // Oracle for the short-range dispersion term: DL_POLY van der Waals type 12
 // (Tang-Toennies damped C6/r^6 + C8/r^8) as the reference tabulates and applies it.
 //
+// Parity unpinned: restated from the reference's Fortran, which cannot be compiled in
+// this image; checked against the tabulated formula, finite differences, momentum and
+// the virial sum, not against a reference run.
 // TEST INFRASTRUCTURE ONLY (see oracle.h).  Restates, operation by operation:
 //   - tang_toennies / tang_toennies_lr (SOURCE/tang-toennies.f90:6-74), including the
 //     reference's factorial, which multiplies by its argument at every step (z^z);

@@ -1,5 +1,9 @@
 // Oracle restatement of the MB-pol 2B/3B models and of the mbpol_forces driver
 // with its heat-current bookkeeping.  TEST INFRASTRUCTURE ONLY (see oracle.h).
+// The 2B/3B models are pinned against the reference's own C++ (golden vectors); the
+// mbpol_forces driver is restated from Fortran that cannot be compiled in this image
+// (parity unpinned for the driver: checked by finite differences, the dense
+// force-matrix heat form and bit-exact list sets).
 //
 // Floating-point expressions keep the reference's association order so that the
 // oracle agrees with the reference to rounding; the file is compiled with

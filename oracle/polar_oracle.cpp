@@ -2,6 +2,11 @@
 // polar Ewald branch computes it (keyword vmbpol: Thole exp-4 damping, all charges and
 // dipoles smeared, DMS charges; SOURCE/simdef_cmd.f:1040-1060).
 //
+// Parity unpinned: the reference's Fortran cannot be compiled in this image and the
+// reference ships no input or output files, so this restatement is checked by
+// self-consistency (forces against finite differences of the energy, momentum, the
+// dense-matrix heat form, the published erfcc and gammq methods), not against a
+// reference run.
 // TEST INFRASTRUCTURE ONLY (see oracle.h).  Restates, operation by operation:
 //   - erfcc (SOURCE/erfcc.f; its literals are default REAL, i.e. single precision)
 //     and the table ercp(i, 0:3) of erfcgenp (SOURCE/erfcgenp.f:26-46);

@@ -3,6 +3,8 @@
 // (SOURCE/ps_type_couple.f90:15-274) and its caller angfrc with keya = 9
 // (SOURCE/angfrc.f:150-212, :344-410, :533-543) including the HEAT_CURRENT hooks.
 // TEST INFRASTRUCTURE ONLY (see oracle.h).
+// Parity unpinned: restated from the reference's Fortran, which cannot be compiled in
+// this image; checked by finite differences, not against a reference run.
 #include "oracle.h"
 
 #include <algorithm>
