@@ -3,6 +3,7 @@
 #include "mbx_kernels.cuh"
 
 #include <algorithm>
+#include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstdlib>
@@ -1236,6 +1237,150 @@ extern "C" int mbx_set_precond_sweeps(mbx_context* ctx, int sweeps) {
     return MBX_OK;
 }
 
+extern "C" int mbx_set_spme(mbx_context* ctx, int order, double spacing, const int* grid) {
+    if (!ctx) return MBX_ERR_ARG;
+    if (order != 0 && (order < 4 || order > 8)) return fail(ctx, MBX_ERR_ARG, "SPME order must be 0 or 4..8");
+    if (order && grid && grid[0] > 0) {
+        for (int a = 0; a < 3; ++a)
+            if (grid[a] < order || grid[a] > 1024 || grid[a] % 2 || spme_smooth_even(grid[a]) != grid[a])
+                return fail(ctx, MBX_ERR_ARG, "SPME grid must be even, 2-3-5 smooth, order..1024 per axis");
+    } else if (order && !(spacing > 0.05 && spacing < 100.0)) {
+        return fail(ctx, MBX_ERR_ARG, "SPME spacing out of range");
+    }
+    ctx->polar.spme_order = order;
+    ctx->polar.spme_spacing = spacing;
+    for (int a = 0; a < 3; ++a) ctx->polar.spme_grid[a] = (order && grid && grid[0] > 0) ? grid[a] : 0;
+    return MBX_OK;
+}
+
+extern "C" int mbx_spme_last_grid(const mbx_context* ctx, int* grid) {
+    if (!ctx || !grid) return MBX_ERR_ARG;
+    for (int a = 0; a < 3; ++a) grid[a] = ctx->polar.spme_order ? ctx->polar.spme_K_last[a] : 0;
+    return MBX_OK;
+}
+
+extern "C" int mbx_spme_grid_for_cell(const double* cell, double spacing, int* grid) {
+    if (!cell || !grid || !(spacing > 0.0)) return MBX_ERR_ARG;
+    const double* a = cell;   // perpendicular widths of the cell
+    const double axb[3] = {a[1] * a[5] - a[2] * a[4], a[2] * a[3] - a[0] * a[5], a[0] * a[4] - a[1] * a[3]};
+    const double bxc[3] = {a[4] * a[8] - a[5] * a[7], a[5] * a[6] - a[3] * a[8], a[3] * a[7] - a[4] * a[6]};
+    const double cxa[3] = {a[7] * a[2] - a[1] * a[8], a[0] * a[8] - a[2] * a[6], a[1] * a[6] - a[0] * a[7]};
+    const double v = std::fabs(a[0] * bxc[0] + a[1] * bxc[1] + a[2] * bxc[2]);
+    auto nrm = [](const double* u) { return std::sqrt(u[0] * u[0] + u[1] * u[1] + u[2] * u[2]); };
+    const double w[3] = {v / nrm(bxc), v / nrm(cxa), v / nrm(axb)};
+    for (int c = 0; c < 3; ++c) grid[c] = spme_smooth_even(w[c] / spacing);
+    return MBX_OK;
+}
+
+extern "C" int mbx_fft3d(mbx_context* ctx, int n1, int n2, int n3, int count, int sign, double* data) {
+    if (!ctx) return MBX_ERR_ARG;
+    if (n1 < 1 || n2 < 1 || n3 < 1 || n1 > 1024 || n2 > 1024 || n3 > 1024 || count < 1 || !data ||
+        (sign != 1 && sign != -1))
+        return fail(ctx, MBX_ERR_ARG, "mbx_fft3d: bad argument");
+    for (int n : {n1, n2, n3}) {
+        int m = n;
+        for (int p : {2, 3, 5})
+            while (m % p == 0) m /= p;
+        if (m != 1) return fail(ctx, MBX_ERR_ARG, "mbx_fft3d: sizes must have no prime factor above 5");
+    }
+    CK(cudaSetDevice(ctx->device));
+    SpmeState st;
+    const double cell[9] = {(double)n1, 0, 0, 0, (double)n2, 0, 0, 0, (double)n3};
+    const int K[3] = {n1, n2, n3};
+    // the FFT tables need no B-spline order beyond the grid: the smallest order that fits
+    const int order = std::max(4, std::min(8, std::min(n1, std::min(n2, n3))));
+    if (std::min(n1, std::min(n2, n3)) < 4) return fail(ctx, MBX_ERR_ARG, "mbx_fft3d: sizes must be >= 4");
+    CK(st.prepare(cell, 1.0, order, K, false, 1, ctx->stream));
+    const size_t ng = (size_t)n1 * n2 * n3 * count;
+    double2* d = nullptr;
+    CK(cudaMalloc(&d, ng * sizeof(double2)));
+    cudaError_t e = cudaMemcpyAsync(d, data, ng * sizeof(double2), cudaMemcpyHostToDevice, ctx->stream);
+    if (!e) e = st.fft64(d, count, sign, ctx->stream);
+    if (!e) e = cudaMemcpyAsync(data, d, ng * sizeof(double2), cudaMemcpyDeviceToHost, ctx->stream);
+    if (!e) e = cudaStreamSynchronize(ctx->stream);
+    cudaFree(d);
+    CK(e);
+    return MBX_OK;
+}
+
+extern "C" int mbx_spme_kspace(mbx_context* ctx, const double* prm, int order, const int* grid, int imcon,
+                               const double* cell, int n, const double* xxx, const double* yyy, const double* zzz,
+                               const double* chge, const double* dip, const double* vel, double* forces, double* field,
+                               double* pot, double* out) {
+    if (!ctx) return MBX_ERR_ARG;
+    if (!prm || !grid || !out || n < 0 || (n && (!xxx || !yyy || !zzz || !chge || !forces)) || !(prm[0] > 0.0) ||
+        !(prm[1] > 0.0) || order < 4 || order > 8)
+        return fail(ctx, MBX_ERR_ARG, "mbx_spme_kspace: bad argument");
+    for (int a = 0; a < 3; ++a)
+        if (grid[a] < order || grid[a] > 1024 || grid[a] % 2 || spme_smooth_even(grid[a]) != grid[a])
+            return fail(ctx, MBX_ERR_ARG, "mbx_spme_kspace: grid must be even, 2-3-5 smooth, order..1024 per axis");
+    Cell cl;
+    int rc = make_cell(ctx, imcon, cell, cl);
+    if (rc) return rc;
+    CK(cudaSetDevice(ctx->device));
+    cudaStream_t s = ctx->stream;
+    SpmeState& st = ctx->polar.spme;
+    const bool heat = vel != nullptr;
+    CK(st.prepare(cell, prm[0], order, grid, false, heat ? 9 : 1, s));
+    const size_t m = (size_t)std::max(n, 1);
+    // device staging: x y z q (4 n), md (n double4), vh (12 n), part5 (5 n), field (3 n), acc (64)
+    std::vector<double> h(4 * m + 4 * m + 12 * m, 0.0);
+    for (int j = 0; j < n; ++j) {
+        h[j] = xxx[j];
+        h[m + j] = yyy[j];
+        h[2 * m + j] = zzz[j];
+        h[3 * m + j] = chge[j];
+        const double mu[3] = {dip ? dip[j] : 0.0, dip ? dip[(size_t)n + j] : 0.0, dip ? dip[2 * (size_t)n + j] : 0.0};
+        for (int c = 0; c < 3; ++c) h[4 * m + 4 * j + c] = mu[c];
+        if (heat) {
+            const double v[3] = {vel[j], vel[(size_t)n + j], vel[2 * (size_t)n + j]};
+            for (int b = 0; b < 3; ++b) h[8 * m + (size_t)b * m + j] = chge[j] * v[b];
+            for (int c = 0; c < 3; ++c)
+                for (int b = 0; b < 3; ++b) h[8 * m + (size_t)(3 + 3 * c + b) * m + j] = mu[c] * v[b];
+        }
+    }
+    double* d = nullptr;
+    const size_t nd = h.size() + 8 * m + 64;
+    CK(cudaMalloc(&d, nd * sizeof(double)));
+    double* part5 = d + h.size();
+    double* dfield = part5 + 5 * m;
+    double* acc = dfield + 3 * m;
+    std::vector<double> hp(8 * m + 64);
+    double sc = 0.0;
+    cudaError_t e = cudaMemcpyAsync(d, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice, s);
+    if (!e) e = cudaMemsetAsync(acc, 0, 64 * sizeof(double), s);
+    if (!e) {
+        const double* a = cell;
+        const double vol = std::fabs(a[0] * (a[4] * a[8] - a[5] * a[7]) + a[1] * (a[5] * a[6] - a[3] * a[8]) +
+                                     a[2] * (a[3] * a[7] - a[4] * a[6]));
+        sc = 2.0 * (2.0 * 3.141592653589793 / vol) * 138935.4835 / prm[1];   // sfac
+        e = st.final(n, d, d + m, d + 2 * m, d + 3 * m, reinterpret_cast<const double4*>(d + 4 * m),
+                     heat ? d + 8 * m : nullptr, sc, part5, acc, dfield, s);
+    }
+    if (!e) e = cudaMemcpyAsync(hp.data(), part5, hp.size() * sizeof(double), cudaMemcpyDeviceToHost, s);
+    if (!e) e = cudaStreamSynchronize(s);
+    cudaFree(d);
+    CK(e);
+    const double* p5 = hp.data();
+    const double* hf = p5 + 5 * m;
+    const double* ha = hf + 3 * m;
+    for (int j = 0; j < n; ++j) {
+        for (int c = 0; c < 3; ++c) {
+            forces[(size_t)c * n + j] = 2.0 * sc * p5[(size_t)c * m + j];
+            if (field) field[(size_t)c * n + j] = hf[(size_t)c * m + j];
+        }
+        if (pot) pot[j] = 2.0 * sc * (p5[3 * m + j] + p5[4 * m + j]);
+    }
+    const double engc = ha[48], eng1 = ha[49];
+    out[0] = sc * engc;
+    out[1] = sc * eng1;
+    const double* o = ha + 50;   // omg 11 22 33 12 13 23
+    const double st9[9] = {o[0] + eng1, o[3], o[4], o[3], o[1] + eng1, o[5], o[4], o[5], o[2] + eng1};
+    for (int c = 0; c < 9; ++c) out[2 + c] = sc * st9[c];
+    for (int c = 0; c < 3; ++c) out[11 + c] = heat ? ha[56 + c] : 0.0;
+    return MBX_OK;
+}
+
 extern "C" int mbx_set_lanes(mbx_context* ctx, int lanes) {
     if (!ctx) return MBX_ERR_ARG;
     if (lanes < 1 || lanes > 64) return fail(ctx, MBX_ERR_ARG, "lanes must be 1..64");
@@ -1278,6 +1423,9 @@ extern "C" int mbx_water_step_multi(mbx_context* ctx, int precision, int nbox, c
         c->limit3 = ctx->limit3;
         c->fused = ctx->fused;
         c->polar.precond_sweeps = ctx->polar.precond_sweeps;
+        c->polar.spme_order = ctx->polar.spme_order;
+        c->polar.spme_spacing = ctx->polar.spme_spacing;
+        for (int a = 0; a < 3; ++a) c->polar.spme_grid[a] = ctx->polar.spme_grid[a];
         if (disp && c->disp_gen_seen != ctx->disp_gen) {
             const int rc = mbx_disp_setup(c, ctx->disp_ntypes, ctx->disp_prm_h.data(), ctx->disp_rcut, ctx->disp_delr,
                                           ctx->disp_mxgrid);

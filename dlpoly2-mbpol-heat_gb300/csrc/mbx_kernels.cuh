@@ -2,6 +2,7 @@
 #pragma once
 
 #include "mbx_common.cuh"
+#include "mbx_spme.cuh"
 
 #include <vector>
 
@@ -236,6 +237,17 @@ struct PolarState {
     bool converged = false;
     int iterations = 0;
     long launches = 0;
+    // k space: the explicit Ewald sum of the reference (spme_order 0), or SPME of order
+    // spme_order on spme_grid (or, with spme_grid[0] == 0, the smallest even 2-3-5 grid
+    // with spacing <= spme_spacing along each cell width)
+    int spme_order = 0;
+    int spme_grid[3] = {0, 0, 0};
+    double spme_spacing = 0.8;
+    int spme_K_last[3] = {0, 0, 0};
+    SpmeState spme;
+    float spme_ms = 0.f;                   // profiling: device time of the SPME passes of the last call
+    long spme_calls = 0;
+    cudaEvent_t spev[2] = {nullptr, nullptr};
 
     ~PolarState();
     void release();

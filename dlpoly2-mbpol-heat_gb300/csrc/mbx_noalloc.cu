@@ -1,12 +1,15 @@
 // mbx_mbpol_forces_noalloc: the MB-pol evaluation without any device allocation.
 //
-// Some callers cannot call cudaMalloc at the point where they need forces: code
-// running inside a CUDA stream capture (allocation is not a capturable operation),
-// hosts whose device memory is owned by another allocator or pool and must not be
-// fragmented, and real-time MD drivers that forbid allocation after start-up.  For
-// them this entry point keeps every intermediate (imaged monomers, neighbour and
-// cluster lists, scan workspace, accumulators) in one file-scope __device__ array of
-// fixed size, and the caller passes only its inputs and outputs.
+// Some callers cannot call cudaMalloc at the point where they need forces: hosts whose
+// device memory is owned by another allocator or pool and must not be fragmented or
+// raced by a second allocator, and real-time MD drivers that forbid allocation after
+// start-up (an allocation can synchronise the device and take milliseconds).  For them
+// this entry point keeps every intermediate (imaged monomers, neighbour and cluster
+// lists, scan workspace, accumulators) in one file-scope __device__ array of fixed
+// size, and the caller passes only its inputs and outputs.
+//
+// The call synchronises the caller's stream twice: once to read the list totals (they
+// size the cluster launches) and once at the end to read the scalars.
 //
 // Limits: at most kMaxWaters waters, at most kCap2 dimer partners and kCap3 3B
 // neighbours per water, at most kMaxTrimers trimers; beyond them the call returns
@@ -70,7 +73,9 @@ int report(int code, const char* msg) {
 
 // Device address of the scratch on the current device, looked up once per device.
 // In host code g_mbx_noalloc_scratch is only a host-side stand-in for the symbol, so
-// the address must come from cudaGetSymbolAddress with that device current.
+// the address must come from cudaGetSymbolAddress with that device current.  The
+// address is cached for the life of the process: do not use this entry point across a
+// cudaDeviceReset of the device (the module, and with it the array, may move).
 unsigned char* scratch_for_current_device(int* dev_out) {
     int dev = -1;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;

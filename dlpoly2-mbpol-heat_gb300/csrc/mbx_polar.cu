@@ -2197,7 +2197,8 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
     hk.clear();
     hk2.clear();
     hlmn.clear();
-    {
+    const bool spme_on = spme_order > 0;
+    if (!spme_on) {
         int mmin = 0, nmin = 1;
         for (int ll = 0; ll <= kmax[0]; ++ll) {
             const double t0 = twopi * double(ll);
@@ -2414,6 +2415,13 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
     launches += 3;
     k_pol_mask<<<blocks(n, kThreads), kThreads, 0, s>>>(a, md);
     ++launches;
+    if (spme_on) {
+        int Kg[3];
+        for (int c = 0; c < 3; ++c)
+            Kg[c] = spme_grid[0] > 0 ? spme_grid[c] : spme_smooth_even(wc[c] / spme_spacing);
+        for (int c = 0; c < 3; ++c) spme_K_last[c] = Kg[c];
+        if ((e = spme.prepare(cl.c, alpha, spme_order, Kg, mixed, heat ? 9 : 1, s))) return e;
+    }
     if (K) {
         k_pol_factors<<<blocks(n, kThreads), kThreads, 0, s>>>(k, x, y, z);
         dim3 g(ncols, blocks(n, kThreads));   // sites per column along y (n < 65535 * 128)
@@ -2450,13 +2458,24 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
     const int nsc2 = nkt2 ? std::max(1, std::min((n + kSfTile - 1) / kSfTile, (4 * nsm + nkt2 - 1) / nkt2)) : 1;
     const int schunk2 = ((n + nsc2 - 1) / nsc2 + kSfTile - 1) / kSfTile * kSfTile;
     const int nsc2_used = (n + schunk2 - 1) / schunk2;
-    if ((e = reserve_part(std::max(std::max((size_t)6 * std::max(nc1, nc2) * n, (size_t)30 * nsc_used * K),
-                                   (size_t)2 * nsc2_used * K))))
+    if ((e = reserve_part(std::max(std::max(std::max((size_t)6 * std::max(nc1, nc2) * n, (size_t)30 * nsc_used * K),
+                                            (size_t)2 * nsc2_used * K),
+                                   spme_on ? (size_t)5 * n : (size_t)0))))
         return e;
+    // self term of the k-space dipole field (SOURCE/ewald1p.f), added with every field
+    const double dum_self = 4.0 * kR4pie0 * (alpha * alpha * alpha) / kSqrpi / 3.0;
+    cudaError_t field_err = cudaSuccess;   // a failed SPME field evaluation (checked after each)
     int kf_calls = 0;          // profiling: k_pol_kfield launches of this call with events
     double kf_call_flops = 0.0;
     auto fields64 = [&](bool first) {
         k_pol_dd<<<blocks(32L * n, kThreads), kThreads, 0, s>>>(a);
+        if (spme_on) {
+            const cudaError_t fe =
+                spme.field64(n, x, y, z, first ? q : nullptr, md, polr2, mx, my, mz, k.sfac, dum_self, a.efm, a.efc, s);
+            if (fe && !field_err) field_err = fe;
+            launches += 1 + spme.launches;
+            return;
+        }
         if (K) {
             k_pol_sfd<<<K, kSfThreads, 0, s>>>(k);
             const bool timed = profiling && kf_calls < kKfEvents;
@@ -2478,6 +2497,7 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
     };
     auto sor64 = [&]() -> cudaError_t {   // iter, then read the rms change
         cudaError_t err;
+        if (field_err) return field_err;
         if ((err = cudaMemsetAsync(acc + 27, 0, 2 * sizeof(double), s))) return err;
         k_pol_iter<<<blocks(n, kThreads), kThreads, 0, s>>>(a, md, mixed ? d32 : nullptr);
         ++launches;
@@ -2530,6 +2550,10 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
         // the field evaluation after a correction: FP64 real space; k space the previous
         // FP64 fields plus the FP32 ones of the correction
         auto fields_delta = [&]() {
+            if (spme_on) {   // the SPME field is cheap: a full FP64 evaluation
+                fields64(false);
+                return;
+            }
             k_pol_dd<<<blocks(32L * n, kThreads), kThreads, 0, s>>>(a);
             if (K) {
                 k_pol_sfx32<0><<<dim3(nkt, nsc_used), kSfThreads, sfx_smem0, s>>>(k, d32, vh32, schunk, rowp, kpart);
@@ -2544,6 +2568,7 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
             if (corrected) fields_delta();
             else fields64(it == 1);
             corrected = false;
+            if (field_err) return field_err;
             if ((e = cudaMemsetAsync(acc + 29, 0, 2 * sizeof(double), s))) return e;
             k_pol_resid<<<blocks(n, kThreads), kThreads, 0, s>>>(a, m);
             ++launches;
@@ -2574,14 +2599,18 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
                 if (poly && (e = precondition(33, 1))) return e;
                 for (int sweep = 0; sweep < 100; ++sweep) {
                     k_pol_dd32<<<blocks(32L * n, kThreads), kThreads, 0, s>>>(a, d32, e32);
-                    if (K) {
+                    if (spme_on) {
+                        if ((e = spme.field32(n, x, y, z, d32, polr2, k.sfac, dum_self, e32 + 3 * (size_t)n, s)))
+                            return e;
+                        launches += spme.launches;
+                    } else if (K) {
                         k_pol_sfd32<<<dim3(nkt2, nsc2_used), kSfThreads, sfd_smem, s>>>(k, m, schunk2, rowp2, kpart);
                         k_pol_sfd32_sum<<<blocks(K, kThreads), kThreads, 0, s>>>(k, nsc2_used, kpart);
                         k_pol_kfield32<<<dim3(sblk1, nc1), kThreads, gat_smem, s>>>(k, kc1, (float*)kpart);
                         k_pol_kfield32_sum<<<sblk1, kThreads, 0, s>>>(k, a, m, nc1, (const float*)kpart);
                         launches += 4;
                     }
-                    k_pcg_ad<<<blocks(n, kThreads), kThreads, 0, s>>>(a, m, K ? 1 : 0);
+                    k_pcg_ad<<<blocks(n, kThreads), kThreads, 0, s>>>(a, m, (K || spme_on) ? 1 : 0);
                     k_pcg_step<<<blocks(n, kThreads), kThreads, 0, s>>>(a, m);
                     if (poly && (e = precondition(35, 0))) return e;
                     k_pcg_dir<<<blocks(n, kThreads), kThreads, 0, s>>>(a, m, poly ? cg_z : nullptr);
@@ -2621,7 +2650,8 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
     // final pass
     const double g34 = std::exp(gammln(3.0 / 4.0));
     if (heat) {
-        k_pol_vhat<<<blocks(n, kThreads), kThreads, 0, s>>>(a, md, mixed ? nullptr : vh, mixed ? vh32 : nullptr);
+        const bool w32 = mixed && !spme_on;   // the FP32 Ewald heat sums take FP32 weights
+        k_pol_vhat<<<blocks(n, kThreads), kThreads, 0, s>>>(a, md, w32 ? nullptr : vh, w32 ? vh32 : nullptr);
         ++launches;
     }
     if (profiling && (e = cudaEventRecord(ev[2], s))) return e;
@@ -2642,13 +2672,17 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
             ++launches;
         }
     }
+    if (spme_on) {
+        if ((e = spme.final(n, x, y, z, q, md, heat ? vh : nullptr, k.sfac, kpart, acc, nullptr, s))) return e;
+        launches += spme.launches;
+    }
     if (profiling && (e = cudaEventRecord(ev[3], s))) return e;
     if (K) {
         if (mixed) k_pol_kforce32<<<dim3(sblk1, nc1), kThreads, gat_smem, s>>>(k, a, kc1, kpart);
         else k_pol_kforce<<<dim3(sblk2, nc2), kThreads, 0, s>>>(k, a, kc2, kpart);
         ++launches;
     }
-    k_pol_kforce_sum<<<sblk1, kThreads, 0, s>>>(k, a, mixed ? nc1 : nc2, kpart);
+    k_pol_kforce_sum<<<sblk1, kThreads, 0, s>>>(k, a, spme_on ? 1 : (mixed ? nc1 : nc2), kpart);
     k_pol_ewald2p<<<blocks(32L * n, kThreads), kThreads, 0, s>>>(a, g34, heat);
     k_pol_ewald3p<<<blocks(nw, kThreads), kThreads, 0, s>>>(a, heat);
     k_pol_qdforce<<<blocks(nw, kThreads), kThreads, 0, s>>>(a, heat);
@@ -2679,9 +2713,10 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
     //      24..26 jkin, 27..28 iteration sums, 40 engsic, 41 eng_polar,
     //      48 engc, 49 engdum, 50..55 omg (11 22 33 12 13 23), 56..58 jpot (k space)
     const double scal1 = 2.0 * rvolm * kR4pie0 / epsq;
-    const double engc = K ? h[48] : 0.0, eng1 = K ? h[49] : 0.0;
-    const double omg11 = K ? h[50] : 0.0, omg22 = K ? h[51] : 0.0, omg33 = K ? h[52] : 0.0;
-    const double omg12 = K ? h[53] : 0.0, omg13 = K ? h[54] : 0.0, omg23 = K ? h[55] : 0.0;
+    const bool kon = K || spme_on;
+    const double engc = kon ? h[48] : 0.0, eng1 = kon ? h[49] : 0.0;
+    const double omg11 = kon ? h[50] : 0.0, omg22 = kon ? h[51] : 0.0, omg33 = kon ? h[52] : 0.0;
+    const double omg12 = kon ? h[53] : 0.0, omg13 = kon ? h[54] : 0.0, omg23 = kon ? h[55] : 0.0;
     const double engk = 2.0 * rvolm * kR4pie0 * engc / epsq + h[40];
     const double virk = -scal1 * (omg11 + omg22 + omg33 + 3.0 * eng1);
     double st[9];
@@ -2704,7 +2739,7 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
     out16[15] = h[0];
     if (heat) {
         for (int c = 0; c < 3; ++c) {
-            jpot[c] += h[8 + c] + (K ? h[56 + c] : 0.0);
+            jpot[c] += h[8 + c] + (kon ? h[56 + c] : 0.0);
             jkin[c] += h[24 + c];
         }
     }

@@ -18,8 +18,8 @@ CSRC = os.path.join(PKG, "csrc")
 LIB = os.path.join(BUILD, "libmbx.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUDA_SOURCES = ["mbx_lists.cu", "mbx_mbpol.cu", "mbx_capi.cu", "mbx_noalloc.cu", "mbx_pes.cu", "mbx_server.cu",
-                "mbx_multi.cu", "mbx_disp.cu", "mbx_polar.cu", "mbx_ipi.cu"]
-HEADERS = ["mbx_common.cuh", "mbx_kernels.cuh"]
+                "mbx_multi.cu", "mbx_disp.cu", "mbx_polar.cu", "mbx_ipi.cu", "mbx_spme.cu"]
+HEADERS = ["mbx_common.cuh", "mbx_kernels.cuh", "mbx_spme.cuh"]
 
 
 def _nvcc():
@@ -132,14 +132,14 @@ def build_lib(verbose=False, jobs=None):
     return LIB
 
 
-def build_oracle(with_reference=None):
-    """Compile the oracle (and, when the reference tree exists, its C++ polynomials)."""
+def build_oracle(reference_source=None):
+    """Compile the oracle, and the reference's own C++ polynomials when the path of the
+    reference's SOURCE directory is given (argument, else the environment variable
+    MBX_REFERENCE_SOURCE); without one only the oracle is built."""
     odir = os.path.join(REPO, "oracle")
     _run(["make", "-s", "-B", "-C", odir, "liboracle.so"])
-    ref = "/root/reference/SOURCE"
-    if with_reference is None:
-        with_reference = os.path.isdir(ref)
-    if with_reference:
+    ref = reference_source or os.environ.get("MBX_REFERENCE_SOURCE")
+    if ref and os.path.isdir(ref):
         _run(["make", "-s", "-C", odir, "ref", "REFSRC=" + ref])
     return os.path.join(odir, "liboracle.so")
 

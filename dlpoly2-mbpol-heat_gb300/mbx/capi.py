@@ -146,6 +146,11 @@ def load(path=None):
     L.mbx_set_lanes.argtypes = [C.c_void_p, C.c_int]
     L.mbx_set_precond_sweeps.argtypes = [C.c_void_p, C.c_int]
     L.mbx_polar_field_timing.argtypes = [C.c_void_p, _D, _D, C.POINTER(C.c_long)]
+    L.mbx_set_spme.argtypes = [C.c_void_p, C.c_int, C.c_double, _I]
+    L.mbx_spme_last_grid.argtypes = [C.c_void_p, _I]
+    L.mbx_spme_grid_for_cell.argtypes = [_D, C.c_double, _I]
+    L.mbx_spme_kspace.argtypes = [C.c_void_p, _D, C.c_int, _I, C.c_int, _D, C.c_int] + [_D] * 10
+    L.mbx_fft3d.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _D]
     L.mbx_polar_params_for_cell.argtypes = [_D, _D]
     L.mbx_polar_params_for_cell.restype = None
     L.mbx_ipi_run_callback.argtypes = [C.c_char_p, IPI_FORCE_FN, C.c_void_p, C.c_long, C.POINTER(C.c_long),
@@ -425,6 +430,48 @@ class Context:
 
     def set_precond_sweeps(self, sweeps):
         self._check(self.lib.mbx_set_precond_sweeps(self.h, int(sweeps)), "mbx_set_precond_sweeps")
+
+    def set_spme(self, order=6, spacing=0.8, grid=None):
+        """k space of later electrostatics calls: SPME of `order` (0: the Ewald sum) on
+        `grid` (3 ints) or the grid of `spacing`."""
+        g = None if grid is None else np.ascontiguousarray(grid, np.int32)
+        self._check(self.lib.mbx_set_spme(self.h, int(order), float(spacing), _p(g, _I)), "mbx_set_spme")
+
+    def spme_last_grid(self):
+        g = np.zeros(3, np.int32)
+        self._check(self.lib.mbx_spme_last_grid(self.h, _p(g, _I)), "mbx_spme_last_grid")
+        return tuple(int(v) for v in g)
+
+    def spme_kspace(self, sites, cell, imcon, chge, alpha, grid, order=6, dip=None, vel=None, epsq=1.0):
+        """mbx_spme_kspace on host arrays: sites (n x 3), chge (n), dip / vel (n x 3) or None.
+        Returns dict(engc, eng, stress (9), jpot (3), forces, field, pot)."""
+        sites = np.asarray(sites, np.float64)
+        n = sites.shape[0]
+        x, y, z = (_f64(sites[:, k]) for k in range(3))
+        d = None if dip is None else np.ascontiguousarray(np.asarray(dip, np.float64).T).reshape(-1)
+        v = None if vel is None else np.ascontiguousarray(np.asarray(vel, np.float64).T).reshape(-1)
+        f = np.zeros(3 * n)
+        fld = np.zeros(3 * n)
+        pot = np.zeros(n)
+        out = np.zeros(14)
+        prm = np.array([alpha, epsq], np.float64)
+        g = np.ascontiguousarray(grid, np.int32)
+        rc = self.lib.mbx_spme_kspace(self.h, _p(prm), int(order), _p(g, _I), int(imcon), _p(_f64(cell)), n, _p(x),
+                                      _p(y), _p(z), _p(_f64(chge)), _p(d), _p(v), _p(f), _p(fld), _p(pot), _p(out))
+        self._check(rc, "mbx_spme_kspace")
+        return dict(engc=out[0], eng=out[1], stress=out[2:11].copy(), jpot=out[11:14].copy(),
+                    forces=f.reshape(3, n).T.copy(), field=fld.reshape(3, n).T.copy(), pot=pot)
+
+    def fft3d(self, data, sign=1):
+        """mbx_fft3d on a complex array of shape (count, n3, n2, n1) or (n3, n2, n1) (x fastest)."""
+        a = np.ascontiguousarray(data, np.complex128)
+        shp = a.shape
+        if a.ndim == 3:
+            a = a[None]
+        cnt, n3, n2, n1 = a.shape
+        buf = np.ascontiguousarray(a).view(np.float64).reshape(-1).copy()
+        self._check(self.lib.mbx_fft3d(self.h, n1, n2, n3, cnt, int(sign), _p(buf)), "mbx_fft3d")
+        return buf.view(np.complex128).reshape(shp)
 
     def set_lanes(self, lanes):
         self._check(self.lib.mbx_set_lanes(self.h, int(lanes)), "mbx_set_lanes")

@@ -112,10 +112,11 @@ int mbx_mbpol_forces_device(mbx_context* ctx, int precision, int imcon, const do
 
 /*
  * The same evaluation for callers that cannot allocate device memory at the point of
- * the call: code running under CUDA stream capture, hosts whose device memory belongs
- * to another allocator or pool, MD drivers that forbid allocation after start-up.  It
- * needs no context and calls no cudaMalloc/cudaFree: every intermediate lives in one
- * fixed-size static device array (~2.7 MB per GPU, held until the process exits).
+ * the call: hosts whose device memory belongs to another allocator or pool, and MD
+ * drivers that forbid allocation after start-up.  It needs no context and calls no
+ * cudaMalloc/cudaFree: every intermediate lives in one fixed-size static device array
+ * (~2.7 MB per GPU, held until the process exits).  The call synchronises `stream`
+ * twice (after the list totals, and at the end for the scalars).
  * This entry point has no counterpart in the reference.
  *   - limits: at most 512 waters (nttm2 <= 1536), 64 dimer partners and 48 3B
  *     neighbours per water, 131072 trimers; larger systems return MBX_ERR_ARG or
@@ -124,8 +125,9 @@ int mbx_mbpol_forces_device(mbx_context* ctx, int precision, int imcon, const do
  *     ACCUMULATED), `scalars` is a host array or NULL, `stream` a cudaStream_t or NULL;
  *   - mixed precision uses the default split (2B FP64, 3B FP32);
  *   - the first call on a device looks up the array's device address (make it before
- *     any stream capture); every call shares the one array, so calls that overlap on
- *     the GPU (other streams, other host threads) race and must be serialised.
+ *     any stream capture) and caches it for the process: do not call it across a
+ *     cudaDeviceReset; every call shares the one array, so calls that overlap on the
+ *     GPU (other streams, other host threads) race and must be serialised.
  */
 int mbx_mbpol_forces_noalloc(int precision, int imcon, const double* cell, int nttm2, const int* listttm2,
                              int natms, const double* xxx, const double* yyy, const double* zzz, double* fxx,
@@ -232,6 +234,50 @@ int mbx_polar_field_timing(const mbx_context* ctx, double* ms, double* flops, lo
  * they hold more than keep_bytes; returns the bytes freed (0: kept).  The next call
  * allocates them again. */
 double mbx_trim(mbx_context* ctx, double keep_bytes);
+/*
+ * k space of the electrostatics: the reference's explicit Ewald sum (order 0, the default;
+ * kmax from prm[11..13]) or smooth particle-mesh Ewald (order 4..8) for later
+ * mbx_polar_forces / mbx_water_step calls of the context (and its worker lanes).  SPME
+ * spreads charges and induced dipoles (mu . grad of the B-splines) on a K1 x K2 x K3 grid:
+ * grid[3] (even, no prime factor above 5), or grid NULL / grid[0] == 0 for the smallest
+ * such grid whose spacing along each cell width is <= `spacing` Angstrom.  The charge part
+ * follows the reference's ewald_spme (SOURCE/ewald_spme.f:1-362, SOURCE/bspgen.f,
+ * SOURCE/bspcoe.f, SOURCE/spme_for.f: fractional coordinates shifted by half a cell, the
+ * Euler-spline moduli, the spherical k cut at 1.05 x half the grid, the mean k-space force
+ * removed); the reference evaluates induced dipoles with the explicit Ewald sum only
+ * (SOURCE/ewald1p.f), so the dipole part has no counterpart there.  alpha and rcut still
+ * come from prm; the real-space terms are unchanged.  mbx_spme_last_grid gives the grid
+ * of the last electrostatics call (zeros with the Ewald sum).
+ */
+int mbx_set_spme(mbx_context* ctx, int order, double spacing, const int* grid);
+int mbx_spme_last_grid(const mbx_context* ctx, int* grid);
+/* The grid mbx_set_spme picks for a cell at a spacing (grid[3] written). */
+int mbx_spme_grid_for_cell(const double* cell, double spacing, int* grid);
+/*
+ * SPME k space of point charges and point dipoles, one call on host arrays (the
+ * reference's ewald_spme for the charges, SOURCE/ewald_spme.f:1-362, with the dipole
+ * extension above):
+ *   prm[2] = {alpha, epsq}; order 4..8; grid[3] as mbx_set_spme; imcon, cell[9]
+ *   n sites: xxx, yyy, zzz, chge; dip (3 blocks of n: x, y, z) or NULL
+ *   vel (3 blocks of n) or NULL: the velocity each site's heat terms are carried with
+ *   forces[3n]  WRITTEN: -dE/dr of the k-space energy, the mean over the sites removed
+ *   field[3n]   WRITTEN or NULL: the k-space field -dE/dmu (no self term)
+ *   pot[n]      WRITTEN or NULL: dE/dq
+ *   out[14]     WRITTEN: {E of the charges alone, E of charges and dipoles, stress[9] (with
+ *               the dipoles' strain term), jpot[3] (ewald1p's HEAT_CURRENT per-atom stress
+ *               contracted with vel, SOURCE/ewald1p.f:575-690; 0 without vel)}
+ * E excludes the self terms; units as mbx_polar_forces.
+ */
+int mbx_spme_kspace(mbx_context* ctx, const double* prm, int order, const int* grid, int imcon, const double* cell,
+                    int n, const double* xxx, const double* yyy, const double* zzz, const double* chge,
+                    const double* dip, const double* vel, double* forces, double* field, double* pot, double* out);
+/*
+ * The hand-written 3D FFT of the SPME path on `count` complex grids (host array, interleaved
+ * re/im, x fastest, n1 x n2 x n3 each, sizes 4..1024 with no prime factor above 5), in
+ * place and unnormalised: sign +1 sums data * exp(+2 pi i m.g / n), sign -1 with the
+ * opposite exponent.  The counterpart of the reference's dlpfft3 (SOURCE/dlpfft3.f:1-401).
+ */
+int mbx_fft3d(mbx_context* ctx, int n1, int n2, int n3, int count, int sign, double* data);
 /* M-site force redistribution of the reference's MD step (SOURCE/dlpoly_cmd.f:2585-2601):
  * F_O += (1 - gamma) F_M, F_H1 += F_M gamma / 2, F_H2 += F_M gamma / 2 (standard layout,
  * host arrays of 4*nw sites; the M-site entries are left as they are). */

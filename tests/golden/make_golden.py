@@ -2,7 +2,9 @@
 
 The reference's polynomial sources (SOURCE/mbpol-2b-poly.cpp, poly-2b-v6x.cpp,
 mbpol-3b-poly.cpp, poly-3b-v2x.cpp) are compiled from the reference tree by
-``make -C oracle ref`` into oracle/_ref/libmbpol_ref.so; this script calls their
+``make -C oracle ref REFSRC=<the reference SOURCE directory>`` (the build recipe
+``__graft_entry__.build()`` does this when the reference tree is mounted) into
+oracle/_ref/libmbpol_ref.so; this script calls their
 exported C entry points ``mbpol_2b_poly_`` / ``mbpol_3b_poly_``
 (SOURCE/mbpol-2b-poly.cpp:1888, SOURCE/mbpol-3b-poly.cpp:1526) on seeded water
 dimers and trimers and stores inputs and outputs in ``mbpol_models.npz``.

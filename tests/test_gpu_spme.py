@@ -1,0 +1,111 @@
+"""SPME k space on the GPU (mbx_spme.cu).
+
+* The hand-written 3D FFT against numpy (FP64, both signs, mixed radices 2/3/4/5).
+* mbx_spme_kspace (charges + induced point dipoles: energies, stress, heat term, forces,
+  fields, potentials) against the numpy restatement (oracle/spme_oracle.py) to 1e-9; that
+  restatement's charge part equals the reference's ewald_spme (tests/test_oracle_spme.py).
+* Whole electrostatics solves with SPME against the explicit Ewald sum at the same alpha
+  and converged kmax (the reference's method): the difference is the SPME discretisation
+  error, bounded per quantity below; mixed SPME against FP64 SPME within the mixed budget.
+"""
+import numpy as np
+import pytest
+
+import spme_oracle as so
+from mbx import capi, systems
+
+pytestmark = pytest.mark.gpu
+
+
+def _rel(a, b):
+    a = np.asarray(a)
+    b = np.asarray(b)
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+
+@pytest.mark.parametrize("shape", [(64, 64, 64), (20, 24, 30), (10, 12, 8), (50, 6, 4)])
+def test_fft3d_matches_numpy(mbx_ctx, shape):
+    n3, n2, n1 = shape
+    rng = np.random.default_rng(sum(shape))
+    a = rng.normal(size=(2, n3, n2, n1)) + 1j * rng.normal(size=(2, n3, n2, n1))
+    fwd = mbx_ctx.fft3d(a, sign=1)
+    bwd = mbx_ctx.fft3d(a, sign=-1)
+    N = n1 * n2 * n3
+    ref_f = np.fft.ifftn(a, axes=(1, 2, 3)) * N   # sum_g a(g) exp(+2 pi i m.g / n)
+    ref_b = np.fft.fftn(a, axes=(1, 2, 3))
+    assert _rel(fwd, ref_f) <= 1e-13
+    assert _rel(bwd, ref_b) <= 1e-13
+
+
+def _sites_case(orc, box, seed):
+    sites, q, _, _ = orc.msites_dms(box)
+    n = sites.shape[0]
+    rng = np.random.default_rng(seed)
+    dip = rng.normal(0.0, 0.05, size=(n, 3))
+    dip[3 * box.nw:] = 0.0
+    vel = np.array(box.vel[:n], np.float64)
+    vel[3 * box.nw:] = rng.normal(0.0, 0.01, size=(box.nw, 3))
+    return sites, q, dip, vel
+
+
+@pytest.mark.parametrize("which", ["config0", "triclinic"])
+def test_spme_kspace_matches_oracle(mbx_ctx, oracle_lib, which):
+    if which == "config0":
+        box = systems.config0()
+        grid, order, alpha = (24, 24, 24), 6, 0.35
+    else:
+        box = systems.box_for(64, seed=9)
+        L = box.L
+        box.cell = np.array([L, 0, 0, 0.2 * L, L, 0, 0.1 * L, -0.15 * L, L], dtype=np.float64)
+        box.imcon = 3
+        grid, order, alpha = (20, 24, 30), 5, 0.5
+    sites, q, dip, vel = _sites_case(oracle_lib, box, 3)
+    got = mbx_ctx.spme_kspace(sites, box.cell, box.imcon, q, alpha, grid, order=order, dip=dip, vel=vel)
+    ref = so.spme_kspace(sites, q, box.cell, alpha, grid, order, dip=dip, vel=vel)
+    for key in ("engc", "eng"):
+        assert abs(got[key] - ref[key]) <= 1e-10 * abs(ref[key]), (key, got[key], ref[key])
+    for key in ("stress", "jpot", "forces", "field", "pot"):
+        assert _rel(got[key], ref[key]) <= 1e-9, (key, _rel(got[key], ref[key]))
+
+
+def _polar_case(orc, box, alpha, kmax, toler=1e-10):
+    sites, q, dp, _ = orc.msites_dms(box)
+    polr, polr2 = systems.polarizabilities(box.nw)
+    prm = systems.polar_params(alpha=alpha, rcut=9.0, kmax=kmax, toler_debye=toler)
+    return sites, q, dp, polr, polr2, prm
+
+
+# SPME (order 6, ~0.8 A spacing, alpha 0.35) against the converged Ewald sum: measured
+# differences on the 256-water box are ~1e-6 of the total energy and a few 1e-6 of the
+# largest force; the bounds leave a factor of ~10
+SPME_TOL = {"engcpe": 2e-5, "forces": 5e-5, "dipoles": 5e-5, "atomic_energy": 5e-5, "jpot": 2e-4, "jkin": 5e-5,
+            "stress": 5e-5}
+
+
+def test_spme_solve_matches_ewald(oracle_lib):
+    box = systems.config0()
+    sites, q, dp, polr, polr2, prm = _polar_case(oracle_lib, box, 0.35, (13, 13, 13))
+    ctx = capi.Context(0)
+    try:
+        ew = ctx.polar(sites, box.cell, box.imcon, box.nw, q, dp, polr, polr2, prm, vel=box.vel)
+        ctx.set_spme(6, grid=(24, 24, 24))
+        sp = ctx.polar(sites, box.cell, box.imcon, box.nw, q, dp, polr, polr2, prm, vel=box.vel)
+        assert ctx.spme_last_grid() == (24, 24, 24)
+        mixed = ctx.polar(sites, box.cell, box.imcon, box.nw, q, dp, polr, polr2, prm, vel=box.vel,
+                          precision=capi.MIXED)
+    finally:
+        ctx.close()
+    errs = {"engcpe": abs(sp["engcpe"] - ew["engcpe"]) / abs(ew["engcpe"])}
+    for key in ("forces", "dipoles", "atomic_energy", "jpot", "jkin", "stress"):
+        errs[key] = _rel(sp[key], ew[key])
+    print("SPME vs Ewald:", {k: "%.2e" % v for k, v in errs.items()})
+    for key, tol in SPME_TOL.items():
+        assert errs[key] <= tol, (key, errs[key])
+    # mixed SPME against FP64 SPME: the mixed path's budget
+    frms = np.sqrt(np.mean((mixed["forces"] - sp["forces"]) ** 2)) / np.sqrt(np.mean(sp["forces"] ** 2))
+    print("mixed vs FP64 SPME: force rms %.2e, jpot %.2e, energy %.2e" %
+          (frms, _rel(mixed["jpot"], sp["jpot"]), abs(mixed["engcpe"] - sp["engcpe"]) / abs(sp["engcpe"])))
+    assert frms <= 1e-6
+    assert _rel(mixed["jpot"], sp["jpot"]) <= 1e-6
+    assert _rel(mixed["jkin"], sp["jkin"]) <= 1e-6
+    assert abs(mixed["engcpe"] - sp["engcpe"]) <= 1e-8 * abs(sp["engcpe"])
