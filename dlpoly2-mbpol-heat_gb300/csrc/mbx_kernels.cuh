@@ -175,6 +175,8 @@ struct PolarState {
     int mxegrd = 0;
     double drewd = 0.0, tab_alpha = -1.0, tab_rcut = -1.0;
     double4* ercp = nullptr;               // erfcgenp table, rows 0..mxegrd
+    float4* ercp32 = nullptr;              // its screened functions C_n in FP32 (mixed-path ewald2p)
+    bool ewald2p_fp64 = false;             // mixed path: keep ewald2p's pair terms in FP64
     int *nn = nullptr, *nbr = nullptr, *flag = nullptr;
     float4* xf = nullptr;
     double* tens = nullptr;                // dipole tensors of the list pairs (6 blocks)

@@ -134,6 +134,7 @@ struct PolArgs {
     double *fx, *fy, *fz;
     double gamma, alpha, rcut, rcsq, eps, athole, athole12, athole13, ascc, ascd, toler, omega;
     const double4* ercp;
+    const float4* ercp32;   // C_n = B_n + (2n-1)!! / r^(2n+1) per table row, FP32 (mixed path), or null
     double drewd;
     const int *nn, *nbr;
     double* tens;   // 6 blocks of n * cap
@@ -1582,6 +1583,168 @@ __global__ void __launch_bounds__(kThreads) k_pol_ewald2p(PolArgs a, double g34,
     block_sum_atomic<11>(red, a.acc + 0);
 }
 
+// The mixed path's ewald2p: the same terms as k_pol_ewald2p.  The pair energies stay FP64
+// (the screened 1/r interpolated from the FP64 table, the smeared charge-charge term with
+// the FP64 gammq: the per-site energies feed jkin, whose budget FP32 pair energies would
+// exceed); the forces, the potentials and the dipole terms are FP32 per pair (the B
+// functions from the FP32 table of C_n = B_n + (2n-1)!!/r^(2n+1), free of the cancellation
+// between B_n and the bare 1/r^(2n+1)); separation, cut test and heat entries FP64; every
+// sum FP64.
+__global__ void __launch_bounds__(kThreads) k_pol_ewald2p32(PolArgs a, double g34d, int heat) {
+    const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    double red[11] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};   // eng, vir, stress(6), jpot(3)
+    if (i < a.n) {
+        const int nn = a.nn[i];
+        const size_t row = (size_t)i * a.cap;
+        const float r4 = (float)kR4pie0;
+        const double qid = a.q[i];
+        const float qi = (float)qid;
+        const float mi[3] = {(float)a.mx[i], (float)a.my[i], (float)a.mz[i]};
+        const bool poli = a.polr2[i] > 1e-6;
+        const float p6i = (float)a.polr6[i];
+        const float ascc = (float)a.ascc, ascd = (float)a.ascd, athole = (float)a.athole;
+        const float rdw = (float)(1.0 / a.drewd);
+        double f[3] = {0, 0, 0}, aei = 0, vsp = 0;
+        for (int k = lane; k < nn; k += 32) {
+            const int j = a.nbr[row + k];
+            double dd[3];
+            sep(a, i, j, dd[0], dd[1], dd[2]);
+            const double rsqd = norm2(dd[0], dd[1], dd[2]);
+            if (!(a.rcsq > rsqd)) continue;
+            const float d[3] = {(float)dd[0], (float)dd[1], (float)dd[2]};
+            const float rsq = (float)rsqd;
+            const float rrr = sqrtf(rsq);
+            // 3-point interpolation of the C_n table (erfcgenp's grid)
+            float bbb[4];
+            {
+                const float u = rrr * rdw;
+                const int ll = (int)u;
+                const float ppp = u - (float)ll;
+                const float4 v0 = a.ercp32[ll], v1 = a.ercp32[ll + 1], v2 = a.ercp32[ll + 2];
+                const float vk[4] = {v0.x, v0.y, v0.z, v0.w}, vk1[4] = {v1.x, v1.y, v1.z, v1.w},
+                            vk2[4] = {v2.x, v2.y, v2.z, v2.w};
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const float t1 = vk[q] + (vk1[q] - vk[q]) * ppp;
+                    const float t2 = vk1[q] + (vk2[q] - vk1[q]) * (ppp - 1.f);
+                    bbb[q] = t1 + (t2 - t1) * ppp * 0.5f;
+                }
+            }
+            const float rri = 1.f / rrr, rsqi = 1.f / rsq, r3i = rri * rsqi, r5i = r3i * rsqi;
+            const double qjd = a.q[j];
+            const float qj = (float)qjd;
+            const float cicj = qi * qj;
+            // FP64 energy: the screened 1/r (bbb[0] + 1/r of the FP64 table) and the smeared term
+            const double rrd = __dsqrt_rn(rsqd);
+            double c0;
+            {
+                const double u = rrd / a.drewd;
+                const int ll = (int)u;
+                const double ppp = u - double(ll);
+                const double v0 = a.ercp[ll].x, v1 = a.ercp[ll + 1].x, v2 = a.ercp[ll + 2].x;
+                const double t1 = v0 + (v1 - v0) * ppp;
+                const double t2 = v1 + (v2 - v1) * (ppp - 1.0);
+                c0 = t1 + (t2 - t1) * ppp * 0.5 + 1.0 / rrd;
+            }
+            const double cicjd = qid * qjd;
+            const double edum = cicjd * c0 * kR4pie0;
+            double eng = edum;
+            double aeh = 0.5 * edum;
+            // bbb[1] = the screened 1/r^3 (C_1), bbb[2] = C_2, bbb[3] = C_3
+            float espdum = bbb[0] * r4;
+            float ffac = cicj * bbb[1] * r4;
+            const float bb = p6i * (float)a.polr6[j];
+            const float rb = rrr / bb, rb2 = rb * rb, rb4 = rb2 * rb2;
+            {
+                const float arob4 = ascc * rb4;
+                if (arob4 < (float)kDampCut) {
+                    const float dum1 = expf(-arob4);
+                    const double bbd = a.polr6[i] * a.polr6[j];
+                    const double arob4d = a.ascc * pow4(rrd / bbd);
+                    const double dum1d = exp(-arob4d);
+                    const double gq = gammq(0.75, arob4d);
+                    const double sm = (dum1d - pow(arob4d, 0.25) * g34d * gq) / rrd * kR4pie0;
+                    eng -= cicjd * sm;
+                    aeh -= cicjd * 0.5 * (dum1d - pow(arob4d, 0.25) * g34d * gq) / rrd * kR4pie0;
+                    espdum -= (float)sm;
+                    ffac = ffac - cicj * r3i * dum1 * r4;
+                }
+            }
+            const float mj[3] = {(float)a.mx[j], (float)a.my[j], (float)a.mz[j]};
+            const float rdmui = mi[0] * d[0] + mi[1] * d[1] + mi[2] * d[2];
+            const float rdmuj = mj[0] * d[0] + mj[1] * d[1] + mj[2] * d[2];
+            const float x0 = qj * rdmui - qi * rdmuj;
+            const float facmu0 = x0 * (-3.f) * r5i * r4;
+            const float facmui0 = r3i * qj * r4;
+            const float facmuj0 = -r3i * qi * r4;
+            // facmu0 - x0 B_2 = -x0 C_2; facmui0 + B_1 qj = C_1 qj
+            float facmu = -x0 * bbb[2] * r4;
+            float dfi = bbb[1] * qj * r4;
+            float dfj = -bbb[1] * qi * r4;
+            float espdc = bbb[1] * r4;
+            {
+                const float arob4 = ascd * rb4;
+                const float dum1 = arob4 < (float)kDampCut ? expf(-arob4) : 0.f;
+                const float dum2 = (1.f + (4.f / 3.f) * arob4) * dum1;
+                facmu = facmu - facmu0 * dum2;
+                dfi = dfi - facmui0 * dum1;
+                dfj = dfj - facmuj0 * dum1;
+                espdc = espdc - r3i * dum1 * r4;
+            }
+            if (poli && a.polr2[j] > 1e-6) {
+                const float dpidpj = mi[0] * mj[0] + mi[1] * mj[1] + mi[2] * mj[2];
+                // (3 dpidpj - 15 rdmui rdmuj / r^2) r5i + B_2 dpidpj - B_3 rdmui rdmuj = C_2 dpidpj - C_3 rdmui rdmuj
+                facmu = facmu + (bbb[2] * dpidpj - bbb[3] * rdmui * rdmuj) * r4;
+                dfi = dfi + bbb[2] * rdmuj * r4;
+                dfj = dfj + bbb[2] * rdmui * r4;
+                const float facmu1 = -15.f * rdmui * rdmuj * rsqi * r5i * r4;
+                const float facmu2 = 3.f * dpidpj * r5i * r4;
+                const float dfi1 = 3.f * rdmuj * r5i * r4;
+                const float dfj1 = 3.f * rdmui * r5i * r4;
+                const float bb2 = bb * bb, bb4 = bb2 * bb2;
+                const float arob4 = athole * rb4;
+                const float dum1 = arob4 < (float)kDampCut ? expf(-arob4) : 0.f;
+                const float dum2 = (1.f + (4.f / 3.f) * arob4) * dum1;
+                const float dum3 = 4.f * athole * (4.f * arob4 - 1.f) * dum1 * rsqi / bb4;
+                const float dum4 = 4.f * athole * dum1 * rrr / bb4;
+                facmu = facmu - facmu1 * dum2 - facmu2 * dum1 + rdmui * rdmuj * dum3 * rri * r4 -
+                        dpidpj * rsqi * dum4 * r4;
+                dfi = dfi - dfi1 * dum2;
+                dfj = dfj - dfj1 * dum2;
+            }
+            const float dfx = dfi * mi[0] + dfj * mj[0];
+            const float dfy = dfi * mi[1] + dfj * mj[1];
+            const float dfz = dfi * mi[2] + dfj * mj[2];
+            ffac = ffac + facmu;
+            const double fx = (double)(ffac * d[0] + dfx), fy = (double)(ffac * d[1] + dfy),
+                         fz = (double)(ffac * d[2] + dfz);
+            f[0] += fx; f[1] += fy; f[2] += fz;
+            aei += aeh;
+            vsp += (double)(qj * espdum + rdmuj * espdc);
+            if (heat) heat_entry(a, i, j, fx, fy, fz, red + 8);
+            if (j > i) {
+                const double virdum = (double)(dfx * d[0] + dfy * d[1] + dfz * d[2]);
+                red[0] += eng;
+                red[1] += -(double)ffac * rsqd - virdum;
+                red[2] += dd[0] * fx; red[3] += dd[0] * fy; red[4] += dd[0] * fz;
+                red[5] += dd[1] * fy; red[6] += dd[1] * fz; red[7] += dd[2] * fz;
+            }
+        }
+        for (int c = 0; c < 3; ++c) f[c] = warp_sum(f[c]);
+        aei = warp_sum(aei);
+        vsp = warp_sum(vsp);
+        if (lane == 0) {
+            a.fx[i] += f[0];
+            a.fy[i] += f[1];
+            a.fz[i] += f[2];
+            a.ae[i] += aei;
+            a.vesp[i] += vsp;
+        }
+    }
+    block_sum_atomic<11>(red, a.acc + 0);
+}
+
 // ewald3p over the six excluded pairs of one water (thread per water).
 __global__ void __launch_bounds__(kThreads) k_pol_ewald3p(PolArgs a, int heat) {
     const int w = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1863,7 +2026,7 @@ cudaError_t launch_msite_redistribute(int nw, double gamma, double* fx, double* 
 }
 
 void PolarState::release() {
-    void* p[] = {ercp, nn, nbr, flag, xf, tens, intra, fld, vesp, ae, eik, kv, kx2, lmn, sf, kterm, acc, kco, fac, md, vh, polr6,
+    void* p[] = {ercp, ercp32, nn, nbr, flag, xf, tens, intra, fld, vesp, ae, eik, kv, kx2, lmn, sf, kterm, acc, kco, fac, md, vh, polr6,
                  ckey, cskey, cidx, csidx, csort, cstart, cend,
                  tens32, r32, d32, e32, kco32, fac32, ktile, kaux, kcol, colk, kpart, cg_x, cg_r, cg_q, cg_z, vh32};
     for (void* q : p)
@@ -1881,6 +2044,7 @@ void PolarState::release() {
                 v = nullptr;
             }
     ercp = nullptr;
+    ercp32 = nullptr;
     nn = nbr = flag = nullptr;
     xf = nullptr;
     tens = intra = fld = vesp = ae = sf = kterm = acc = kco = vh = polr6 = nullptr;
@@ -1918,7 +2082,9 @@ PolarState::~PolarState() { release(); }
 cudaError_t PolarState::table(double alpha, double rcut, cudaStream_t s) {
     if (ercp && alpha == tab_alpha && rcut == tab_rcut) return cudaSuccess;
     if (ercp) cudaFree(ercp);
+    if (ercp32) cudaFree(ercp32);
     ercp = nullptr;
+    ercp32 = nullptr;
     mxegrd = std::max(1000, (int)(rcut / 0.0001 + 0.5) + 4);
     drewd = rcut / double(mxegrd - 4);
     std::vector<double4> h((size_t)mxegrd + 1, make_double4(0, 0, 0, 0));
@@ -1935,11 +2101,22 @@ cudaError_t PolarState::table(double alpha, double rcut, cudaStream_t s) {
         }
         h[i] = make_double4(c[0], c[1], c[2], c[3]);
     }
+    // the mixed path's FP32 table: C_n = B_n + (2n-1)!!/r^(2n+1), the screened functions
+    // themselves (row 0, r = 0, is never read: sites of different waters are not that close)
+    std::vector<float4> h32(h.size(), make_float4(0.f, 0.f, 0.f, 0.f));
+    for (int i = 1; i <= mxegrd; ++i) {
+        const double r = double(i) * drewd, ri = 1.0 / r, r2i = ri * ri;
+        const double c0 = h[i].x + ri, c1 = h[i].y + ri * r2i, c2 = h[i].z + 3.0 * ri * r2i * r2i,
+                     c3 = h[i].w + 15.0 * ri * r2i * r2i * r2i;
+        h32[i] = make_float4((float)c0, (float)c1, (float)c2, (float)c3);
+    }
     cudaError_t e;
     if ((e = cudaMalloc(&ercp, h.size() * sizeof(double4)))) return e;
+    if ((e = cudaMalloc(&ercp32, h32.size() * sizeof(float4)))) return e;
     // stream-ordered and complete before the host vector goes (a plain cudaMemcpy from
     // pageable memory may return before its DMA lands, unordered with non-blocking streams)
     if ((e = cudaMemcpyAsync(ercp, h.data(), h.size() * sizeof(double4), cudaMemcpyHostToDevice, s))) return e;
+    if ((e = cudaMemcpyAsync(ercp32, h32.data(), h32.size() * sizeof(float4), cudaMemcpyHostToDevice, s))) return e;
     if ((e = cudaStreamSynchronize(s))) return e;
     tab_alpha = alpha;
     tab_rcut = rcut;
@@ -2295,6 +2472,7 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
     auto bind = [&](PolArgs& b) {
         b.cap = cap;
         b.ercp = ercp;
+        b.ercp32 = ercp32;
         b.drewd = drewd;
         b.nn = nn;
         b.nbr = nbr;
@@ -2683,7 +2861,10 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
         ++launches;
     }
     k_pol_kforce_sum<<<sblk1, kThreads, 0, s>>>(k, a, spme_on ? 1 : (mixed ? nc1 : nc2), kpart);
-    k_pol_ewald2p<<<blocks(32L * n, kThreads), kThreads, 0, s>>>(a, g34, heat);
+    if (mixed && !ewald2p_fp64)
+        k_pol_ewald2p32<<<blocks(32L * n, kThreads), kThreads, 0, s>>>(a, g34, heat);
+    else
+        k_pol_ewald2p<<<blocks(32L * n, kThreads), kThreads, 0, s>>>(a, g34, heat);
     k_pol_ewald3p<<<blocks(nw, kThreads), kThreads, 0, s>>>(a, heat);
     k_pol_qdforce<<<blocks(nw, kThreads), kThreads, 0, s>>>(a, heat);
     k_pol_jkin<<<blocks(n, kThreads), kThreads, 0, s>>>(a, ae_out, heat);

@@ -49,6 +49,8 @@ struct Request {
     int status = MBX_OK;
     bool done = false;
     size_t footprint = 0;
+    int spme_order = 0;       // step requests: k space (0: Ewald; else SPME of this order)
+    double spme_spacing = 0.8;
     Clock::time_point t_submit, t_start, t_done;
 };
 
@@ -101,6 +103,15 @@ size_t step_footprint_bytes(int nw, int K) {
     return (size_t)K * n * 24 + n * 1024 * (4 + 48 + 24) + n * 300 * 8 + (size_t)K * 256 + (8u << 20);
 }
 
+// The SPME grids of a step request instead of the phase tables: nine FP64 and one FP32
+// complex grids plus the influence functions, at the grid the spacing gives the cell.
+size_t spme_grid_bytes(const double* cell, double spacing) {
+    int g[3] = {0, 0, 0};
+    if (mbx_spme_grid_for_cell(cell, spacing, g)) return 0;
+    const size_t ng = (size_t)g[0] * g[1] * g[2];
+    return ng * (9 * 16 + 8 + 12);
+}
+
 }  // namespace
 
 extern "C" void mbx_polar_params_for_cell(const double* cell, double* prm) {
@@ -120,6 +131,8 @@ struct mbx_server {
     std::map<long, std::shared_ptr<Request>> live;
     std::vector<std::thread> workers;
     std::map<long, std::vector<double>> client_dip;   // last converged dipoles per client
+    int spme_order = 0;                                // k space of step requests (0: Ewald)
+    double spme_spacing = 0.8;
     std::set<long> busy;                               // clients with a request on a slot
     long completed = 0;
     char err[256] = {0};
@@ -160,6 +173,7 @@ struct mbx_server {
                 }
             }
             r->t_start = Clock::now();
+            if (r->step) mbx_set_spme(ctx, r->spme_order, r->spme_spacing, nullptr);
             run(ctx, *r);
             r->t_done = Clock::now();
             {
@@ -237,6 +251,15 @@ extern "C" int mbx_server_create(mbx_server** out, int device, int slots, double
     return MBX_OK;
 }
 
+extern "C" int mbx_server_set_spme(mbx_server* s, int order, double spacing) {
+    if (!s || (order != 0 && (order < 4 || order > 8)) || (order && !(spacing > 0.05 && spacing < 100.0)))
+        return MBX_ERR_ARG;
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->spme_order = order;
+    s->spme_spacing = spacing;
+    return MBX_OK;
+}
+
 extern "C" void mbx_server_destroy(mbx_server* s) {
     if (!s) return;
     {
@@ -309,7 +332,13 @@ extern "C" long mbx_server_submit_step(mbx_server* s, int precision, long client
     double prm[15];
     int K = 0;
     step_params(cell, prm, &K);
-    r->footprint = footprint_bytes(nw) + step_footprint_bytes(nw, K);
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        r->spme_order = s->spme_order;
+        r->spme_spacing = s->spme_spacing;
+    }
+    r->footprint = footprint_bytes(nw) + (r->spme_order ? step_footprint_bytes(nw, 0) + spme_grid_bytes(cell, r->spme_spacing)
+                                                        : step_footprint_bytes(nw, K));
     r->t_submit = Clock::now();
     {
         std::lock_guard<std::mutex> lk(s->mu);

@@ -114,6 +114,7 @@ def load(path=None):
     L.mbx_msites_dms_device.argtypes = [C.c_void_p, C.c_int, _D, C.c_int, C.c_void_p, C.c_int, C.c_double] + \
         [C.c_void_p] * 5
     L.mbx_server_create.argtypes = [C.POINTER(C.c_void_p), C.c_int, C.c_int, C.c_double]
+    L.mbx_server_set_spme.argtypes = [C.c_void_p, C.c_int, C.c_double]
     L.mbx_server_destroy.argtypes = [C.c_void_p]
     L.mbx_server_destroy.restype = None
     L.mbx_server_submit.argtypes = [C.c_void_p, C.c_int, C.c_int, _D, C.c_int, C.c_int] + [_D] * 7
@@ -603,6 +604,12 @@ class Server:
             raise MbxError("mbx_server_create failed with status %d" % rc)
         self.h = h
         self._boxes = {}
+
+    def set_spme(self, order=6, spacing=0.8):
+        """k space of later step requests: SPME (order 4..8) or the Ewald sum (order 0)."""
+        rc = self.lib.mbx_server_set_spme(self.h, int(order), float(spacing))
+        if rc:
+            raise MbxError("mbx_server_set_spme failed with status %d" % rc)
 
     def close(self):
         if self.h:

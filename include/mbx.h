@@ -438,6 +438,10 @@ long mbx_server_submit_step(mbx_server* server, int precision, long client, int 
 int mbx_server_wait_step(mbx_server* server, long id, double* fxx, double* fyy, double* fzz, double* atomic_energy,
                          double* dipoles, double* scalars, double* times);
 const char* mbx_server_error(const mbx_server* server);
+/* k space of later step requests: SPME of `order` (4..8) on the grid of `spacing` per cell
+ * (as mbx_set_spme with grid NULL), or order 0 for the explicit Ewald sum (the default).
+ * With SPME the admission footprint holds the grids instead of the exp(ik.r) tables. */
+int mbx_server_set_spme(mbx_server* server, int order, double spacing);
 
 /*
  * Many independent water boxes (path-integral beads, separate simulations) in ONE

@@ -109,3 +109,40 @@ def test_spme_solve_matches_ewald(oracle_lib):
     assert _rel(mixed["jpot"], sp["jpot"]) <= 1e-6
     assert _rel(mixed["jkin"], sp["jkin"]) <= 1e-6
     assert abs(mixed["engcpe"] - sp["engcpe"]) <= 1e-8 * abs(sp["engcpe"])
+
+
+def test_water_step_spme_4096():
+    """Config 1's box and k space (4096 H2O, SPME 64^3, order 6, alpha 0.35): the whole FP64
+    force evaluation against the same evaluation with the converged Ewald sum (kmax 27,
+    exp(-k^2 / 4 alpha^2) < 1e-13 beyond it), and mixed SPME against FP64 SPME."""
+    box = systems.config1()
+    prm = systems.polar_params(alpha=0.35, rcut=9.0, kmax=(27, 27, 27), toler_debye=1e-10)
+    ctx = capi.Context(0)
+    try:
+        ew = ctx.water_step(box, prm, precision=capi.FP64)
+        ctx.set_spme(6, spacing=49.70 / 64)
+        sp = ctx.water_step(box, prm, precision=capi.FP64)
+        assert ctx.spme_last_grid() == (64, 64, 64)
+        mixed = ctx.water_step(box, prm, precision=capi.MIXED)
+    finally:
+        ctx.close()
+    nws = capi.NWATERSCALARS
+
+    def heat(r):
+        v = r["scalars"]
+        j = v[12:15] + v[15:18] + v[capi.NSCALARS + 11:capi.NSCALARS + 14] + v[capi.NSCALARS + 25:capi.NSCALARS + 28]
+        return j + v[nws + 16:nws + 19] + v[nws + 19:nws + 22]
+
+    errs = {"engcpe": abs(sp["scalars"][nws] - ew["scalars"][nws]) / abs(ew["scalars"][nws]),
+            "forces": _rel(sp["forces"], ew["forces"]), "dipoles": _rel(sp["dipoles"], ew["dipoles"]),
+            "atomic_energy": _rel(sp["atomic_energy"], ew["atomic_energy"]),
+            "heat": float(np.linalg.norm(heat(sp) - heat(ew)) / np.linalg.norm(heat(ew)))}
+    print("4096 H2O, SPME 64^3 vs Ewald:", {k: "%.2e" % v for k, v in errs.items()})
+    for key, tol in (("engcpe", 2e-5), ("forces", 5e-5), ("dipoles", 5e-5), ("atomic_energy", 5e-5),
+                     ("heat", 5e-5)):
+        assert errs[key] <= tol, (key, errs[key])
+    frms = np.sqrt(np.mean((mixed["forces"] - sp["forces"]) ** 2)) / np.sqrt(np.mean(sp["forces"] ** 2))
+    herr = float(np.linalg.norm(heat(mixed) - heat(sp)) / np.linalg.norm(heat(sp)))
+    print("4096 H2O mixed vs FP64 (SPME): force rms %.2e, heat %.2e" % (frms, herr))
+    assert frms <= 1e-5
+    assert herr <= 1e-6
