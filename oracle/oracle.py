@@ -63,6 +63,8 @@ class Oracle:
         L.orc_dispersion.restype = C.c_long
         L.orc_disp_lrc.argtypes = [C.c_int, _D, _I, C.c_double, C.c_double, _D, _D]
         L.orc_polar.argtypes = [_D, C.c_int, _D, C.c_int] + [_D] * 20 + [C.c_int]
+        L.orc_induced_error.argtypes = [_D, C.c_int, _D, C.c_int] + [_D] * 11
+        L.orc_induced_error.restype = None
         for f in ("orc_erfcc", "orc_gammln"):
             getattr(L, f).argtypes = [C.c_double]
             getattr(L, f).restype = C.c_double
@@ -249,6 +251,19 @@ class Oracle:
         return dict(status=rc, forces=f.T.copy(), engcpe=out[0], vircpe=out[1], stress=out[2:11].copy(),
                     iterations=int(out[11]), deltadip=out[12], eng_polar=out[13], eng_kspace=out[14],
                     eng_real=out[15], dipoles=dip.T.copy(), atomic_energy=ae, jpot=jpot, jkin=jkin)
+
+    def induced_error(self, sites, cell, imcon, nw, chge, dp, polr, polr2, prm, dipoles):
+        """induced_error (SOURCE/induced_error.f90) of the given dipoles (sites x 3) under the
+        oracle's fields: (L2 norm, largest component) of mu - polr2 E(mu) / r4pie0."""
+        x, y, z = (np.ascontiguousarray(sites[:, k], dtype=np.float64) for k in range(3))
+        d = [np.ascontiguousarray(np.asarray(dipoles, np.float64)[:, k]) for k in range(3)]
+        r = np.zeros(2)
+        self.lib.orc_induced_error(_p(np.ascontiguousarray(prm, np.float64)), imcon,
+                                   _p(np.ascontiguousarray(cell, np.float64)), nw, _p(x), _p(y), _p(z),
+                                   _p(np.ascontiguousarray(chge, np.float64)), _p(np.ascontiguousarray(dp, np.float64)),
+                                   _p(np.ascontiguousarray(polr, np.float64)), _p(np.ascontiguousarray(polr2, np.float64)),
+                                   _p(d[0]), _p(d[1]), _p(d[2]), _p(r))
+        return float(r[0]), float(r[1])
 
     def image_monomers(self, box):
         m = box.monomers().copy()

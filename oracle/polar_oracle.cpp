@@ -309,11 +309,11 @@ struct KVec {
  * dip* in: starting dipoles; out: converged dipoles.
  * Returns 0, or 1 when the dipoles did not converge within maxit iterations.
  */
-extern "C" int orc_polar(const double* prm, int imcon, const double* cell, int nw, const double* x, const double* y,
-                         const double* z, const double* chge, const double* dp, const double* polr,
-                         const double* polr2, double* dipx, double* dipy, double* dipz, double* fx, double* fy,
-                         double* fz, double* out, double* atomic_energy, const double* vx, const double* vy,
-                         const double* vz, double* jpot, double* jkin, int dense) {
+static int polar_run(const double* prm, int imcon, const double* cell, int nw, const double* x, const double* y,
+                     const double* z, const double* chge, const double* dp, const double* polr,
+                     const double* polr2, double* dipx, double* dipy, double* dipz, double* fx, double* fy,
+                     double* fz, double* out, double* atomic_energy, const double* vx, const double* vy,
+                     const double* vz, double* jpot, double* jkin, int dense, double* resid) {
     Params P;
     P.alpha = prm[0]; P.rcut = prm[1]; P.epsq = prm[2]; P.toler = prm[3]; P.omega = prm[4];
     P.athole = prm[5]; P.athole12 = prm[6]; P.athole13 = prm[7]; P.ascc = prm[8]; P.ascd = prm[9];
@@ -622,6 +622,26 @@ extern "C" int orc_polar(const double* prm, int imcon, const double* cell, int n
                 efm[3 * j + 0] += dum * dipx[j];
                 efm[3 * j + 1] += dum * dipy[j];
                 efm[3 * j + 2] += dum * dipz[j];
+            }
+        }
+        // ---- induced_error (SOURCE/induced_error.f90:3-66): the residual of the dipole
+        // equations, mu - polr2 E(mu) / r4pie0 over the polarizable sites, with the fields of
+        // this pass (those of the dipoles entering it); L2 norm and largest component
+        {
+            double l2 = 0.0, linf = 0.0;
+            for (int i = 0; i < N; ++i) {
+                if (polr2[i] <= 1e-6) continue;
+                const double mu[3] = {dipx[i], dipy[i], dipz[i]};
+                for (int c = 0; c < 3; ++c) {
+                    const double dm = mu[c] - polr2[i] * (efk[3 * i + c] + emu[3 * i + c] + efm[3 * i + c] +
+                                                          efc[3 * i + c] + 0.0) / r4;
+                    l2 += dm * dm;
+                    linf = std::max(linf, std::fabs(dm));
+                }
+            }
+            if (resid) {
+                resid[0] = std::sqrt(l2);
+                resid[1] = linf;
             }
         }
         // ---- iter
@@ -1073,6 +1093,36 @@ extern "C" int orc_polar(const double* prm, int imcon, const double* cell, int n
 }
 
 // The pieces the GPU path shares with the oracle, exposed for unit tests.
+extern "C" int orc_polar(const double* prm, int imcon, const double* cell, int nw, const double* x, const double* y,
+                         const double* z, const double* chge, const double* dp, const double* polr,
+                         const double* polr2, double* dipx, double* dipy, double* dipz, double* fx, double* fy,
+                         double* fz, double* out, double* atomic_energy, const double* vx, const double* vy,
+                         const double* vz, double* jpot, double* jkin, int dense) {
+    return polar_run(prm, imcon, cell, nw, x, y, z, chge, dp, polr, polr2, dipx, dipy, dipz, fx, fy, fz, out,
+                     atomic_energy, vx, vy, vz, jpot, jkin, dense, nullptr);
+}
+
+/*
+ * induced_error (SOURCE/induced_error.f90:3-66) of given dipoles: one pass of the fields at
+ * dip* (rfield and ewald1p of the polar branch) and the residual of the dipole equations,
+ * resid[2] = {L2 norm, largest component} over the polarizable sites.  prm as orc_polar;
+ * the dipoles are not changed.
+ */
+extern "C" void orc_induced_error(const double* prm, int imcon, const double* cell, int nw, const double* x,
+                                  const double* y, const double* z, const double* chge, const double* dp,
+                                  const double* polr, const double* polr2, const double* dipx, const double* dipy,
+                                  const double* dipz, double* resid) {
+    const int N = 4 * nw;
+    double p1[15];
+    for (int q = 0; q < 15; ++q) p1[q] = prm[q];
+    p1[14] = 1;   // one pass: the fields at the given dipoles
+    std::vector<double> mx(dipx, dipx + N), my(dipy, dipy + N), mz(dipz, dipz + N), f(3 * (size_t)N, 0.0);
+    double out[16];
+    polar_run(p1, imcon, cell, nw, x, y, z, chge, dp, polr, polr2, mx.data(), my.data(), mz.data(), f.data(),
+              f.data() + N, f.data() + 2 * (size_t)N, out, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, 0,
+              resid);
+}
+
 extern "C" double orc_erfcc(double x) { return erfcc(x); }
 extern "C" double orc_gammq(double a, double x) { return gammq(a, x); }
 extern "C" double orc_gammln(double x) { return gammln(x); }

@@ -208,3 +208,19 @@ def test_polar_mixed_preconditioner_settings(mbx_ctx, oracle_lib):
     finally:
         mbx_ctx.set_precond_sweeps(3)
     assert min(sweeps.values()) > 0
+
+
+@pytest.mark.parametrize("precision", [capi.FP64, capi.MIXED])
+def test_gpu_dipoles_solve_the_oracle_equations(mbx_ctx, oracle_lib, precision):
+    """induced_error (SOURCE/induced_error.f90) of the GPU's converged dipoles under the
+    ORACLE's fields: whatever the iteration path (the reference's SOR, or FP32 corrections
+    under FP64 refinement), the dipoles solve the reference's dipole equations to the
+    tolerance."""
+    box = systems.config0()
+    prm = systems.polar_params(alpha=0.3, rcut=9.0, kmax=(8, 8, 8), toler_debye=1e-10)
+    sites, q, dp, polr, polr2, prm = _case(oracle_lib, box, prm)
+    got = mbx_ctx.polar(sites, box.cell, box.imcon, box.nw, q, dp, polr, polr2, prm, precision=precision)
+    l2, linf = oracle_lib.induced_error(sites, box.cell, box.imcon, box.nw, q, dp, polr, polr2, prm, got["dipoles"])
+    npol = int((polr2 > 1e-6).sum())
+    assert l2 / np.sqrt(3 * npol) <= prm[3] / (1.0 - prm[4]), (l2, prm[3])
+    assert linf <= 20 * prm[3]

@@ -146,3 +146,22 @@ def test_water_step_spme_4096():
     print("4096 H2O mixed vs FP64 (SPME): force rms %.2e, heat %.2e" % (frms, herr))
     assert frms <= 1e-5
     assert herr <= 1e-6
+
+
+def test_spme_dipoles_under_the_ewald_equations(oracle_lib):
+    """induced_error of the SPME solve's dipoles under the oracle's Ewald fields (same alpha,
+    converged kmax): the residual is the SPME field error, below 1e-4 of the dipoles."""
+    box = systems.config0()
+    sites, q, dp, polr, polr2, prm = _polar_case(oracle_lib, box, 0.35, (13, 13, 13))
+    ctx = capi.Context(0)
+    try:
+        ctx.set_spme(6, grid=(24, 24, 24))
+        sp = ctx.polar(sites, box.cell, box.imcon, box.nw, q, dp, polr, polr2, prm)
+    finally:
+        ctx.close()
+    pol = polr2 > 1e-6
+    l2, _ = oracle_lib.induced_error(sites, box.cell, box.imcon, box.nw, q, dp, polr, polr2, prm, sp["dipoles"])
+    rms_mu = float(np.sqrt(np.mean(sp["dipoles"][pol] ** 2)))
+    rel = l2 / np.sqrt(3 * pol.sum()) / rms_mu
+    print("SPME dipoles: Ewald residual rms / dipole rms = %.2e" % rel)
+    assert rel <= 1e-4

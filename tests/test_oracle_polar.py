@@ -115,3 +115,50 @@ def test_iteration_cap(oracle_lib, small):
     p[14] = 3
     r = _run(orc, box, polr, polr2, p)
     assert r["status"] == 1 and r["iterations"] == 3
+
+
+def test_induced_error_pins_the_converged_dipoles(oracle_lib, small):
+    """induced_error (SOURCE/induced_error.f90): the residual mu - polr2 E(mu) / r4pie0 of the
+    converged dipoles is at the dipole tolerance (the SOR stop tests the update, which is
+    (1 - omega) x the residual); dipoles moved by 1e-6 e A give a residual 1e8 times larger."""
+    box, polr, polr2, prm = small
+    sites, q, dp, _ = oracle_lib.msites_dms(box)
+    r = oracle_lib.polar(sites, box.cell, box.imcon, box.nw, q, dp, polr, polr2, prm)
+    assert r["status"] == 0
+    pol = polr2 > 1e-6
+    l2, linf = oracle_lib.induced_error(sites, box.cell, box.imcon, box.nw, q, dp, polr, polr2, prm, r["dipoles"])
+    assert l2 / math.sqrt(3 * pol.sum()) <= prm[3] / (1.0 - prm[4])
+    assert linf <= 10 * prm[3]
+    moved = r["dipoles"] + np.random.default_rng(0).normal(0, 1e-6, r["dipoles"].shape) * pol[:, None]
+    l2m, _ = oracle_lib.induced_error(sites, box.cell, box.imcon, box.nw, q, dp, polr, polr2, prm, moved)
+    assert l2m > 1e7 * l2
+
+
+def test_results_independent_of_the_ewald_split(oracle_lib):
+    """The Ewald splitting parameter is a numerical choice: at converged kmax and rcut
+    (erfc(alpha rcut) <= 2e-8, exp(-k^2/4 alpha^2) <= 1e-18 at the k cut) the energy, the
+    forces, the converged dipoles, the virial and the diagonal of the stress agree across
+    alpha 0.65 / 0.75 / 0.85 to the accuracy of the erfc fit the reference uses (1.2e-7 per
+    screened pair term; a few 1e-6 of these totals, 2e-5 bound).  The stress's off-diagonal
+    entries and the heat current are not split-independent in the reference's formulas: the
+    stress is symmetrised from the upper triangles of non-symmetric dipole terms, and the
+    per-atom energy split of the heat current depends on alpha."""
+    box = systems.box_for(64, seed=3)
+    polr, polr2 = systems.polarizabilities(box.nw)
+    sites, q, dp, _ = oracle_lib.msites_dms(box)
+    res = {}
+    for a in (0.65, 0.75, 0.85):
+        km = int(np.ceil(2 * a * np.sqrt(38) * box.L / (2 * np.pi))) + 1
+        p = systems.polar_params(alpha=a, rcut=6.1, kmax=(km, km, km), toler_debye=1e-12)
+        res[a] = oracle_lib.polar(sites, box.cell, box.imcon, box.nw, q, dp, polr, polr2, p)
+        assert res[a]["status"] == 0
+    ref = res[0.75]
+    diag = [0, 4, 8]
+    for a in (0.65, 0.85):
+        r = res[a]
+        assert abs(r["engcpe"] - ref["engcpe"]) <= 2e-5 * abs(ref["engcpe"])
+        assert abs(r["vircpe"] - ref["vircpe"]) <= 2e-5 * abs(ref["vircpe"])
+        assert np.abs(r["forces"] - ref["forces"]).max() <= 2e-5 * np.abs(ref["forces"]).max()
+        assert np.abs(r["dipoles"] - ref["dipoles"]).max() <= 2e-5 * np.abs(ref["dipoles"]).max()
+        sd, rd = r["stress"][diag], ref["stress"][diag]
+        assert np.abs(sd - rd).max() <= 2e-5 * np.abs(rd).max()
