@@ -93,6 +93,11 @@ struct mbx_context {
     double disp_rcut = 0.0, disp_delr = 0.0;
     long disp_gen = 0;       // setups made on this context
     long disp_gen_seen = -1; // (on a lane) the parent's setup it holds
+    // path-integral bead coupling: device copies of the normal-mode matrices for pimd_P
+    // beads (nmode_to_cart then cart_to_nmode, P x P each) and two accumulators
+    double* pimd_mat = nullptr;
+    double* pimd_acc = nullptr;
+    int pimd_P = 0, pimd_lang = -1;
     char err[512] = {0};
 };
 
@@ -495,7 +500,7 @@ extern "C" void mbx_destroy(mbx_context* ctx) {
     if (ctx->own_stream) cudaStreamSynchronize(ctx->own_stream);
     void* dev[] = {ctx->mono, ctx->list, ctx->atoms, ctx->ae_scratch, ctx->acc, ctx->totals, ctx->pairs, ctx->trip,
                    ctx->batch, ctx->hard2, ctx->hard3, ctx->hard_count, ctx->fuse_ctr, ctx->part2, ctx->done2,
-                   ctx->ints, ctx->polar_stage, ctx->step_stage, ctx->step_ints};
+                   ctx->ints, ctx->polar_stage, ctx->step_stage, ctx->step_ints, ctx->pimd_mat, ctx->pimd_acc};
     for (void* p : dev)
         if (p) cudaFree(p);
     if (ctx->totals_h) cudaFreeHost(ctx->totals_h);
@@ -1381,6 +1386,81 @@ extern "C" int mbx_spme_kspace(mbx_context* ctx, const double* prm, int order, c
     return MBX_OK;
 }
 
+extern "C" int mbx_pimd_matrices(int nbead, int langevin, double* nmode_to_cart, double* cart_to_nmode,
+                                 double* lambda) {
+    if (nbead < 2 || nbead % 2 || nbead > pimd_max_beads()) return MBX_ERR_ARG;
+    std::vector<double> n2c, c2n, lam;
+    pimd_matrices(nbead, langevin != 0, n2c, c2n, lam);
+    if (nmode_to_cart) std::memcpy(nmode_to_cart, n2c.data(), n2c.size() * sizeof(double));
+    if (cart_to_nmode) std::memcpy(cart_to_nmode, c2n.data(), c2n.size() * sizeof(double));
+    if (lambda) std::memcpy(lambda, lam.data(), lam.size() * sizeof(double));
+    return MBX_OK;
+}
+
+namespace {
+int pimd_prepare(mbx_context* ctx, int P, int langevin) {
+    if (P < 2 || P % 2 || P > pimd_max_beads())
+        return fail(ctx, MBX_ERR_ARG, "the number of beads must be even, 2..%d", pimd_max_beads());
+    if (ctx->pimd_mat && ctx->pimd_P == P && ctx->pimd_lang == (langevin != 0)) return MBX_OK;
+    std::vector<double> n2c, c2n, lam;
+    pimd_matrices(P, langevin != 0, n2c, c2n, lam);
+    if (ctx->pimd_mat) cudaFree(ctx->pimd_mat);
+    ctx->pimd_mat = nullptr;
+    ctx->pimd_P = 0;
+    CK(cudaMalloc(&ctx->pimd_mat, 2 * (size_t)P * P * sizeof(double)));
+    if (!ctx->pimd_acc) CK(cudaMalloc(&ctx->pimd_acc, 2 * sizeof(double)));
+    CK(cudaMemcpyAsync(ctx->pimd_mat, n2c.data(), n2c.size() * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->pimd_mat + (size_t)P * P, c2n.data(), c2n.size() * sizeof(double),
+                       cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));   // the host vectors go out of scope
+    ctx->pimd_P = P;
+    ctx->pimd_lang = langevin != 0;
+    return MBX_OK;
+}
+}  // namespace
+
+extern "C" int mbx_pimd_transform_device(mbx_context* ctx, int nbead, int langevin, int to_modes, long nvals,
+                                         const double* in, double* out) {
+    if (!ctx) return MBX_ERR_ARG;
+    if (nvals < 0 || (nvals && (!in || !out)) || in == out)
+        return fail(ctx, MBX_ERR_ARG, "mbx_pimd_transform_device: bad argument");
+    CK(cudaSetDevice(ctx->device));
+    int rc = pimd_prepare(ctx, nbead, langevin);
+    if (rc) return rc;
+    const double* A = ctx->pimd_mat + (to_modes ? (size_t)nbead * nbead : 0);
+    CK(launch_pimd_transform(nbead, nvals, A, in, out, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return MBX_OK;
+}
+
+extern "C" int mbx_pimd_spring_forces_device(mbx_context* ctx, int nbead, int langevin, int add_spring_to_forces,
+                                             double hbar, double beta, double force_scale, int natms,
+                                             const double* xxx, const double* yyy, const double* zzz, double* fxx,
+                                             double* fyy, double* fzz, const double* mass, double* energies) {
+    if (!ctx) return MBX_ERR_ARG;
+    if (natms < 0 || !(hbar > 0.0) || !(beta > 0.0) || !(force_scale != 0.0) ||
+        (natms && (!xxx || !yyy || !zzz || !fxx || !fyy || !fzz || !mass)))
+        return fail(ctx, MBX_ERR_ARG, "mbx_pimd_spring_forces_device: bad argument");
+    CK(cudaSetDevice(ctx->device));
+    int rc = pimd_prepare(ctx, nbead, langevin);
+    if (rc) return rc;
+    const double coeff = double(nbead) / ((hbar * beta) * (hbar * beta));
+    const double fac1 = langevin ? 1.0 / std::sqrt(double(nbead)) : 1.0;
+    const double fac3 = (langevin && !add_spring_to_forces) ? 0.0 : force_scale;
+    CK(cudaMemsetAsync(ctx->pimd_acc, 0, 2 * sizeof(double), ctx->stream));
+    // row 0 of cart_to_nmode: the centroid mode's weights
+    CK(launch_pimd_springs(nbead, natms, ctx->pimd_mat + (size_t)nbead * nbead, xxx, yyy, zzz, fxx, fyy, fzz, mass,
+                           coeff, fac1, fac3, ctx->pimd_acc, ctx->stream));
+    double h[2] = {0.0, 0.0};
+    CK(cudaMemcpyAsync(h, ctx->pimd_acc, 2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (energies) {
+        energies[0] = 0.5 * coeff * h[0];
+        energies[1] = 0.5 * h[1] / force_scale;
+    }
+    return MBX_OK;
+}
+
 extern "C" int mbx_set_lanes(mbx_context* ctx, int lanes) {
     if (!ctx) return MBX_ERR_ARG;
     if (lanes < 1 || lanes > 64) return fail(ctx, MBX_ERR_ARG, "lanes must be 1..64");
@@ -1850,11 +1930,56 @@ mbx_context* global_ctx() {
 }
 }  // namespace
 
+extern "C" int mbx_2b_force_matrix_batch(mbx_context* ctx, long n, const double* w1, const double* w2, double* fm) {
+    if (!ctx) return MBX_ERR_ARG;
+    if (n < 0 || n > 0x7fffffff) return fail(ctx, MBX_ERR_ARG, "bad n");
+    if (n == 0) return MBX_OK;
+    if (!w1 || !w2 || !fm) return fail(ctx, MBX_ERR_ARG, "NULL argument");
+    CK(cudaSetDevice(ctx->device));
+    const size_t b9 = 9 * (size_t)n * sizeof(double), bf = 108 * (size_t)n * sizeof(double);
+    int rc = batch_reserve(ctx, 2 * b9 + bf);
+    if (rc) return rc;
+    double *d1 = ctx->batch, *d2 = d1 + 9 * n, *df = d2 + 9 * n;
+    cudaStream_t s = ctx->stream;
+    CK(cudaMemcpyAsync(d1, w1, b9, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(d2, w2, b9, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(df, fm, bf, cudaMemcpyHostToDevice, s));   // entries not written keep their values
+    CK(launch_2b_fm((int)n, d1, d2, df, s));
+    CK(cudaMemcpyAsync(fm, df, bf, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    return MBX_OK;
+}
+
+extern "C" int mbx_3b_force_matrix_batch(mbx_context* ctx, long n, const double* w1, const double* w2,
+                                         const double* w3, double* fm) {
+    if (!ctx) return MBX_ERR_ARG;
+    if (n < 0 || n > 0x7fffffff) return fail(ctx, MBX_ERR_ARG, "bad n");
+    if (n == 0) return MBX_OK;
+    if (!w1 || !w2 || !w3 || !fm) return fail(ctx, MBX_ERR_ARG, "NULL argument");
+    CK(cudaSetDevice(ctx->device));
+    const size_t b9 = 9 * (size_t)n * sizeof(double), bf = 243 * (size_t)n * sizeof(double);
+    int rc = batch_reserve(ctx, 3 * b9 + bf);
+    if (rc) return rc;
+    double *d1 = ctx->batch, *d2 = d1 + 9 * n, *d3 = d2 + 9 * n, *df = d3 + 9 * n;
+    cudaStream_t s = ctx->stream;
+    CK(cudaMemcpyAsync(d1, w1, b9, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(d2, w2, b9, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(d3, w3, b9, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(df, fm, bf, cudaMemcpyHostToDevice, s));
+    CK(launch_3b_fm((int)n, d1, d2, d3, df, s));
+    CK(cudaMemcpyAsync(fm, df, bf, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    return MBX_OK;
+}
+
 extern "C" void mbpol_2b_poly_(const double* w1, const double* w2, double* E, double* g1, double* g2,
                                double* force_matrix) {
-    (void)force_matrix;
     mbx_context* c = global_ctx();
     std::lock_guard<std::mutex> lk(g_mu);
+    if (force_matrix && mbx_2b_force_matrix_batch(c, 1, w1, w2, force_matrix) != MBX_OK) {
+        std::fprintf(stderr, "mbpol_2b_poly_: %s\n", mbx_error(c));
+        std::abort();
+    }
     if (mbx_2b_poly_batch(c, MBX_FP64, 1, w1, w2, E, g1, g2) != MBX_OK) {
         std::fprintf(stderr, "mbpol_2b_poly_: %s\n", mbx_error(c));
         std::abort();
@@ -1863,9 +1988,12 @@ extern "C" void mbpol_2b_poly_(const double* w1, const double* w2, double* E, do
 
 extern "C" void mbpol_3b_poly_(const double* w1, const double* w2, const double* w3, double* E, double* g1,
                                double* g2, double* g3, double* force_matrix) {
-    (void)force_matrix;
     mbx_context* c = global_ctx();
     std::lock_guard<std::mutex> lk(g_mu);
+    if (force_matrix && mbx_3b_force_matrix_batch(c, 1, w1, w2, w3, force_matrix) != MBX_OK) {
+        std::fprintf(stderr, "mbpol_3b_poly_: %s\n", mbx_error(c));
+        std::abort();
+    }
     if (mbx_3b_poly_batch(c, MBX_FP64, 1, w1, w2, w3, E, g1, g2, g3) != MBX_OK) {
         std::fprintf(stderr, "mbpol_3b_poly_: %s\n", mbx_error(c));
         std::abort();

@@ -27,6 +27,7 @@
 
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <string>
@@ -64,8 +65,9 @@ bool write_all(int fd, const void* p, size_t n) {
 }
 
 // "inet:host:port" or "unix:name:port" as the reference parses it (host between the first
-// and the last colon, port after the last; a unix socket is /tmp/ipi_<name>), or
-// "host:port" (inet).
+// and the last colon, port after the last; a unix socket is /tmp/ipi_<name>, or
+// <dir>/ipi_<name> with the environment variable MBX_IPI_UNIX_DIR set), or "host:port"
+// (inet).
 int open_socket(const char* address, int* fd, std::string& err) {
     const std::string a = address ? address : "";
     const size_t first = a.find(':'), last = a.rfind(':');
@@ -86,7 +88,8 @@ int open_socket(const char* address, int* fd, std::string& err) {
         sockaddr_un sa;
         std::memset(&sa, 0, sizeof sa);
         sa.sun_family = AF_UNIX;
-        const std::string path = "/tmp/ipi_" + host;
+        const char* dir = std::getenv("MBX_IPI_UNIX_DIR");
+        const std::string path = std::string(dir && *dir ? dir : "/tmp") + "/ipi_" + host;
         if (path.size() >= sizeof sa.sun_path) {
             err = "unix socket path too long";
             return MBX_ERR_ARG;

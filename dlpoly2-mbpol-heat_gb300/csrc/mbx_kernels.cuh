@@ -76,6 +76,21 @@ cudaError_t launch_2b_direct(int n, const double* w1, const double* w2, double* 
                              int precision, cudaStream_t s);
 cudaError_t launch_3b_direct(int n, const double* w1, const double* w2, const double* w3, double* E,
                              double* g1, double* g2, double* g3, int precision, cudaStream_t s);
+// The force matrices of the per-cluster C entry points (FP64): 108 doubles per dimer, 243
+// per trimer, entries written as the reference writes them (the rest left as they are).
+cudaError_t launch_2b_fm(int n, const double* w1, const double* w2, double* fm, cudaStream_t s);
+cudaError_t launch_3b_fm(int n, const double* w1, const double* w2, const double* w3, double* fm, cudaStream_t s);
+// Path-integral bead coupling (mbx_pimd.cu): the normal-mode matrices of
+// SOURCE/centroid_matrix.f (nmode_to_cart[bead][mode], cart_to_nmode[mode][bead], lambda),
+// the transform out = A in over P beads of m values, and the spring forces of
+// SOURCE/centroid_spring_force.f (acc[0] += sum m |d2|^2, acc[1] += sum -d1 . f).
+void pimd_matrices(int P, bool langevin, std::vector<double>& n2c, std::vector<double>& c2n,
+                   std::vector<double>& lam);
+int pimd_max_beads();
+cudaError_t launch_pimd_transform(int P, long m, const double* A, const double* in, double* out, cudaStream_t s);
+cudaError_t launch_pimd_springs(int P, int n, const double* c2n0, const double* x, const double* y, const double* z,
+                                double* fx, double* fy, double* fz, const double* mass, double coeff, double fac1,
+                                double fac3, double* acc, cudaStream_t s);
 // jkin = sum_i (K_i + U_i) v_i over the water atoms (SOURCE/heatcurrent.f90:713-716).
 cudaError_t launch_jkin(int nwat_atoms, const double* vx, const double* vy, const double* vz,
                         const double* mass, const double* ae, double* acc, cudaStream_t s);

@@ -864,6 +864,192 @@ __global__ void __launch_bounds__(kThreads) k_3b_direct(int n, const double* __r
     }
 }
 
+// --- the per-cluster force matrices of the reference's C entry points --------------------
+// mbpol_2b_poly_ / mbpol_3b_poly_ also return a pairwise split of the cluster gradient,
+// read by the reference's HEAT_STRESS build (SOURCE/mbpol.f90:564-566, :951-953): entry
+// (i, j, :) of the sites of a cluster is the gradient of the polynomial variable that links
+// sites i and j (g_v dv/d(r_i - r_j)), +/- for the two orders.
+
+// 2B (SOURCE/mbpol-2b-poly.cpp:449-653): the 10 x 10 x 3 matrix over O, H, H, O, H, H and
+// the four X sites, the X rows redistributed onto their monomer's O, H, H through the
+// X-site geometry and the X columns of atom rows moved onto the other monomer's O, then the
+// 6 x 6 x 3 block of the atoms times the switch, the switch's gradient added to the two O-O
+// entries.  The diagonal has no variable: the reference copies it from an uninitialised
+// array, here it is 0.  Beyond the cutoff the matrix is not touched, as in the reference.
+__device__ __forceinline__ void fm_xrows(const double* oh1, const double* oh2, double* gX1, double* gX2,
+                                         double* grd, bool clear) {
+    // rows X1, X2 (entries at gX1, gX2) onto rows O, H1, H2 (grd + 30 k) of the same column
+    const double gm[3] = {gX1[0] - gX2[0], gX1[1] - gX2[1], gX1[2] - gX2[2]};
+    const double t1[3] = {oh2[1] * gm[2] - oh2[2] * gm[1], oh2[2] * gm[0] - oh2[0] * gm[2],
+                          oh2[0] * gm[1] - oh2[1] * gm[0]};
+    const double t2[3] = {oh1[1] * gm[2] - oh1[2] * gm[1], oh1[2] * gm[0] - oh1[0] * gm[2],
+                          oh1[0] * gm[1] - oh1[1] * gm[0]};
+    for (int i = 0; i < 3; ++i) {
+        const double gsum = gX1[i] + gX2[i];
+        const double in_plane = 0.5 * m2b::in_plane_gamma * gsum;
+        const double gh1 = in_plane + m2b::out_of_plane_gamma * t1[i];
+        const double gh2 = in_plane - m2b::out_of_plane_gamma * t2[i];
+        grd[i] += gsum - (gh1 + gh2);
+        grd[i + 30] += gh1;
+        grd[i + 60] += gh2;
+        if (clear) {
+            gX1[i] = 0.0;
+            gX2[i] = 0.0;
+        }
+    }
+}
+
+__device__ void fm_2b(const double* w1, const double* w2, double* fm) {
+    const double dOO[3] = {w1[0] - w2[0], w1[1] - w2[1], w1[2] - w2[2]};
+    const double rOO = sqrt(dOO[0] * dOO[0] + dOO[1] * dOO[1] + dOO[2] * dOO[2]);
+    if (rOO > kR2f) return;
+    double xc[30];
+    for (int i = 0; i < 9; ++i) {
+        xc[i] = w1[i];
+        xc[9 + i] = w2[i];
+    }
+    double oha[2][3], ohb[2][3];
+    xsites(xc + m2b::Oa, oha[0], oha[1], xc + m2b::Xa1, xc + m2b::Xa2);
+    xsites(xc + m2b::Ob, ohb[0], ohb[1], xc + m2b::Xb1, xc + m2b::Xb2);
+    double v[31], gg[31];
+    for (int q = 0; q < 31; ++q) {
+        const m2b::V d = m2b::kV[q];
+        const double dx = xc[d.s1] - xc[d.s2], dy = xc[d.s1 + 1] - xc[d.s2 + 1], dz = xc[d.s1 + 2] - xc[d.s2 + 2];
+        const double r = sqrt(dx * dx + dy * dy + dz * dz);
+        const double e = exp(d.k * (d.r0 - r));
+        if (!d.coul) {
+            v[q] = e;
+            gg[q] = -d.k * e / r;
+        } else {
+            const double rinv = 1.0 / r;
+            v[q] = e * rinv;
+            gg[q] = -(d.k + rinv) * v[q] * rinv;
+        }
+    }
+    double acc[32];
+    for (int q = 0; q < 32; ++q) acc[q] = 0.0;
+    poly2b<double>(v, acc);
+    double tmp[300];
+    for (int q = 0; q < 300; ++q) tmp[q] = 0.0;
+    for (int q = 0; q < 31; ++q) {
+        const m2b::V d = m2b::kV[q];
+        for (int c = 0; c < 3; ++c) {
+            const double t = acc[1 + q] * ((xc[d.s1 + c] - xc[d.s2 + c]) * gg[q]);
+            tmp[10 * d.s1 + d.s2 + c] = t;    // row site s1, column site s2 (10 sites x 3 per row)
+            tmp[10 * d.s2 + d.s1 + c] = -t;
+        }
+    }
+    // site s at row 30 s, column 3 s: Oa 0, Ha1 1, Ha2 2, Ob 3, Hb1 4, Hb2 5, Xa1 6, Xa2 7, Xb1 8, Xb2 9
+    auto at = [&](int r, int c) { return tmp + 30 * r + 3 * c; };
+    fm_xrows(oha[0], oha[1], at(6, 3), at(7, 3), at(0, 3), false);   // X rows of a, column Ob
+    fm_xrows(oha[0], oha[1], at(6, 4), at(7, 4), at(0, 4), false);   // column Hb1
+    fm_xrows(oha[0], oha[1], at(6, 5), at(7, 5), at(0, 5), false);   // column Hb2
+    fm_xrows(ohb[0], ohb[1], at(8, 0), at(9, 0), at(3, 0), false);   // X rows of b, column Oa
+    fm_xrows(ohb[0], ohb[1], at(8, 1), at(9, 1), at(3, 1), false);
+    fm_xrows(ohb[0], ohb[1], at(8, 2), at(9, 2), at(3, 2), false);
+    // X columns of atom rows onto the other monomer's O column
+    const int ra[3] = {0, 1, 2}, rb[3] = {3, 4, 5};
+    for (int k = 0; k < 3; ++k)
+        for (int x = 8; x <= 9; ++x)
+            for (int c = 0; c < 3; ++c) {
+                at(ra[k], 3)[c] += at(ra[k], x)[c];
+                at(ra[k], x)[c] = 0.0;
+            }
+    for (int k = 0; k < 3; ++k)
+        for (int x = 6; x <= 7; ++x)
+            for (int c = 0; c < 3; ++c) {
+                at(rb[k], 0)[c] += at(rb[k], x)[c];
+                at(rb[k], x)[c] = 0.0;
+            }
+    // X-X entries: X rows onto O, H, H rows, the entries to the other monomer's O column
+    fm_xrows(oha[0], oha[1], at(6, 8), at(7, 8), at(0, 3), true);
+    fm_xrows(oha[0], oha[1], at(6, 9), at(7, 9), at(0, 3), true);
+    fm_xrows(ohb[0], ohb[1], at(8, 6), at(9, 6), at(3, 0), true);
+    fm_xrows(ohb[0], ohb[1], at(8, 7), at(9, 7), at(3, 0), true);
+    double gsw;
+    const double sw = f_switch(rOO, kR2i, kR2f, gsw);
+    for (int r = 0; r < 6; ++r)
+        for (int i = 0; i < 18; ++i) fm[i + 18 * r] = sw * tmp[i + 30 * r];
+    gsw *= acc[0] / rOO;
+    for (int i = 0; i < 3; ++i) {
+        const double d = gsw * dOO[i];
+        fm[i + 18 * 0 + 3 * 3] += d;
+        fm[i + 18 * 3 + 3 * 0] -= d;
+    }
+}
+
+// 3B (SOURCE/mbpol-3b-poly.cpp:208-312): the 9 x 9 x 3 matrix over the three monomers'
+// O, H, H, every off-diagonal entry assigned from its variable (the gradient including
+// the switching product), the switch's gradients added to the O-O entries; the diagonal is
+// not written, as in the reference.
+__device__ void fm_3b(const double* t, double* fm) {
+    double x[36], fk[36];
+    vars_3b<double>(t, x, fk);
+    double acc[37];
+    for (int q = 0; q < 37; ++q) acc[q] = 0.0;
+    poly3b<double>(x, acc);
+    double rab[3], rac[3], rbc[3], drab = 0.0, drac = 0.0, drbc = 0.0;
+    for (int n = 0; n < 3; ++n) {
+        rab[n] = t[m3b::Oa + n] - t[m3b::Ob + n];
+        drab += rab[n] * rab[n];
+        rac[n] = t[m3b::Oa + n] - t[m3b::Oc + n];
+        drac += rac[n] * rac[n];
+        rbc[n] = t[m3b::Ob + n] - t[m3b::Oc + n];
+        drbc += rbc[n] * rbc[n];
+    }
+    drab = sqrt(drab);
+    drac = sqrt(drac);
+    drbc = sqrt(drbc);
+    double gab, gac, gbc;
+    const double sab = f_switch(drab, 0.0, kR3f, gab);
+    const double sac = f_switch(drac, 0.0, kR3f, gac);
+    const double sbc = f_switch(drbc, 0.0, kR3f, gbc);
+    const double s = sab * sac + sab * sbc + sac * sbc;
+    for (int q = 0; q < 36; ++q) {
+        const m3b::V d = m3b::kV[q];
+        const double gq = (acc[1 + q] * s) * fk[q];
+        const int i = d.a1 / 3, j = d.a2 / 3;
+        for (int c = 0; c < 3; ++c) {
+            const double v = gq * (t[d.a1 + c] - t[d.a2 + c]);
+            fm[27 * i + 3 * j + c] = v;
+            fm[27 * j + 3 * i + c] = -v;
+        }
+    }
+    const double e = acc[0];
+    gab *= (sac + sbc) * e / drab;
+    gac *= (sab + sbc) * e / drac;
+    gbc *= (sab + sac) * e / drbc;
+    for (int n = 0; n < 3; ++n) {
+        fm[27 * 0 + 3 * 3 + n] += gab * rab[n];
+        fm[27 * 3 + 3 * 0 + n] -= gab * rab[n];
+        fm[27 * 0 + 3 * 6 + n] += gac * rac[n];
+        fm[27 * 6 + 3 * 0 + n] -= gac * rac[n];
+        fm[27 * 3 + 3 * 6 + n] += gbc * rbc[n];
+        fm[27 * 6 + 3 * 3 + n] -= gbc * rbc[n];
+    }
+}
+
+__global__ void __launch_bounds__(kThreads) k_2b_fm(int n, const double* __restrict__ w1s,
+                                                     const double* __restrict__ w2s, double* __restrict__ fms) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    fm_2b(w1s + 9 * (size_t)t, w2s + 9 * (size_t)t, fms + 108 * (size_t)t);
+}
+
+__global__ void __launch_bounds__(kThreads) k_3b_fm(int n, const double* __restrict__ w1s,
+                                                     const double* __restrict__ w2s, const double* __restrict__ w3s,
+                                                     double* __restrict__ fms) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    double p[27];
+    for (int q = 0; q < 9; ++q) {
+        p[q] = w1s[9 * (size_t)t + q];
+        p[9 + q] = w2s[9 * (size_t)t + q];
+        p[18 + q] = w3s[9 * (size_t)t + q];
+    }
+    fm_3b(p, fms + 243 * (size_t)t);
+}
+
 __global__ void __launch_bounds__(kThreads) k_jkin(int n, const double* __restrict__ vx,
                                                     const double* __restrict__ vy, const double* __restrict__ vz,
                                                     const double* __restrict__ mass, const double* __restrict__ ae,
@@ -991,6 +1177,18 @@ cudaError_t launch_3b_direct(int n, const double* w1, const double* w2, const do
     if (n <= 0) return cudaSuccess;
     if (precision == 0) k_3b_direct<double><<<blocks(n), kThreads, 0, s>>>(n, w1, w2, w3, E, g1, g2, g3);
     else k_3b_direct<float><<<blocks(n), kThreads, 0, s>>>(n, w1, w2, w3, E, g1, g2, g3);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_2b_fm(int n, const double* w1, const double* w2, double* fm, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    k_2b_fm<<<blocks(n), kThreads, 0, s>>>(n, w1, w2, fm);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_3b_fm(int n, const double* w1, const double* w2, const double* w3, double* fm, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    k_3b_fm<<<blocks(n), kThreads, 0, s>>>(n, w1, w2, w3, fm);
     return cudaGetLastError();
 }
 

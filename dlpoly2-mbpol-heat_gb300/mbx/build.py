@@ -18,7 +18,7 @@ CSRC = os.path.join(PKG, "csrc")
 LIB = os.path.join(BUILD, "libmbx.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUDA_SOURCES = ["mbx_lists.cu", "mbx_mbpol.cu", "mbx_capi.cu", "mbx_noalloc.cu", "mbx_pes.cu", "mbx_server.cu",
-                "mbx_multi.cu", "mbx_disp.cu", "mbx_polar.cu", "mbx_ipi.cu", "mbx_spme.cu"]
+                "mbx_multi.cu", "mbx_disp.cu", "mbx_polar.cu", "mbx_ipi.cu", "mbx_spme.cu", "mbx_pimd.cu"]
 HEADERS = ["mbx_common.cuh", "mbx_kernels.cuh", "mbx_spme.cuh"]
 
 

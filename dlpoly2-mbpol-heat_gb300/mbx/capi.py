@@ -170,6 +170,13 @@ def load(path=None):
     L.mbx_last_lists.argtypes = [C.c_void_p, _I, C.c_long, _L, _I, C.c_long, _L]
     L.mbx_2b_poly_batch.argtypes = [C.c_void_p, C.c_int, C.c_long, _D, _D, _D, _D, _D]
     L.mbx_3b_poly_batch.argtypes = [C.c_void_p, C.c_int, C.c_long, _D, _D, _D, _D, _D, _D, _D]
+    L.mbx_2b_force_matrix_batch.argtypes = [C.c_void_p, C.c_long, _D, _D, _D]
+    L.mbx_3b_force_matrix_batch.argtypes = [C.c_void_p, C.c_long, _D, _D, _D, _D]
+    L.mbx_pimd_matrices.argtypes = [C.c_int, C.c_int, _D, _D, _D]
+    L.mbx_pimd_transform_device.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_long, C.c_void_p,
+                                            C.c_void_p]
+    L.mbx_pimd_spring_forces_device.argtypes = ([C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
+                                                 C.c_double, C.c_int] + [C.c_void_p] * 7 + [_D])
     L.mbpol_2b_poly_.argtypes = [_D] * 6
     L.mbpol_2b_poly_.restype = None
     L.mbpol_3b_poly_.argtypes = [_D] * 8

@@ -18,18 +18,30 @@ def _hdr(text):
 
 
 class FakeIpiServer:
-    def __init__(self, frames, init_text="params"):
+    """unix_dir/unix_name: listen on the unix socket <unix_dir>/ipi_<unix_name> (the client
+    finds it through MBX_IPI_UNIX_DIR) instead of TCP."""
+
+    def __init__(self, frames, init_text="params", unix_dir=None, unix_name=None):
         self.frames = frames
         self.init_text = init_text.encode()
         self.replies = []
         self.statuses = []
         self.error = None
-        self.sock = socket.socket(socket.AF_INET, socket.SOCK_STREAM)
-        self.sock.bind(("127.0.0.1", 0))
+        self.unix = unix_dir is not None
+        if self.unix:
+            import os
+            self.path = os.path.join(unix_dir, "ipi_" + unix_name)
+            self.sock = socket.socket(socket.AF_UNIX, socket.SOCK_STREAM)
+            self.sock.bind(self.path)
+            self.address = "unix:%s:0" % unix_name
+        else:
+            self.sock = socket.socket(socket.AF_INET, socket.SOCK_STREAM)
+            self.sock.bind(("127.0.0.1", 0))
         self.sock.listen(1)
         self.sock.settimeout(300)
-        self.port = self.sock.getsockname()[1]
-        self.address = "inet:127.0.0.1:%d" % self.port
+        if not self.unix:
+            self.port = self.sock.getsockname()[1]
+            self.address = "inet:127.0.0.1:%d" % self.port
         self.thread = threading.Thread(target=self._run, daemon=True)
         self.thread.start()
 
@@ -52,7 +64,8 @@ class FakeIpiServer:
         try:
             conn, _ = self.sock.accept()
             conn.settimeout(300)
-            conn.setsockopt(socket.IPPROTO_TCP, socket.TCP_NODELAY, 1)
+            if not self.unix:
+                conn.setsockopt(socket.IPPROTO_TCP, socket.TCP_NODELAY, 1)
             with conn:
                 for replica, h, hinv, pos in self.frames:
                     if self._status(conn) == "NEEDINIT":

@@ -396,6 +396,35 @@ int mbx_ipi_run(mbx_context* ctx, const char* address, int precision, const doub
                 long max_steps, long* steps_done);
 
 /*
+ * Path-integral bead coupling of the reference's PIMD/CMD mode on the device, for callers
+ * that evaluate the beads' physical forces with mbx_water_step_multi (one box per bead) and
+ * propagate them: the normal-mode transformation (transformation_matrix and the
+ * cart <-> normal-mode transforms, SOURCE/centroid_matrix.f:3-270) and the ring-polymer
+ * spring forces (SOURCE/centroid_spring_force.f:1-157).  nbead even, 2..256; the beads are
+ * a leading array axis (value j of bead b at b * n + j), not MPI ring ranks.
+ *   mbx_pimd_matrices          host only: nmode_to_cart[bead * P + mode],
+ *                              cart_to_nmode[mode * P + bead], lambda[P] (any may be NULL)
+ *   mbx_pimd_transform_device  out[p * nvals + j] = sum_b A[p][b] in[b * nvals + j] with A
+ *                              cart_to_nmode (to_modes != 0) or nmode_to_cart; device arrays
+ *   mbx_pimd_spring_forces_device  natms atoms per bead (x, y, z, f device arrays of
+ *                              nbead * natms, mass[natms] device, the physical masses);
+ *                              the spring forces coeff m (2 r_k - r_{k-1} - r_{k+1}) x
+ *                              force_scale (0 with langevin and add_spring_to_forces 0)
+ *                              SUBTRACTED from f, coeff = nbead / (hbar beta)^2;
+ *                              energies[2] (host) = {the spring energy
+ *                              0.5 coeff sum m |r_k - r_{k-1}|^2, the centroid-virial term
+ *                              0.5 sum -(r_k - c) . f_k / force_scale with the incoming
+ *                              forces}; c the centroid, the first normal mode as a position.
+ */
+int mbx_pimd_matrices(int nbead, int langevin, double* nmode_to_cart, double* cart_to_nmode, double* lambda);
+int mbx_pimd_transform_device(mbx_context* ctx, int nbead, int langevin, int to_modes, long nvals, const double* in,
+                              double* out);
+int mbx_pimd_spring_forces_device(mbx_context* ctx, int nbead, int langevin, int add_spring_to_forces, double hbar,
+                                  double beta, double force_scale, int natms, const double* xxx, const double* yyy,
+                                  const double* zzz, double* fxx, double* fyy, double* fzz, const double* mass,
+                                  double* energies);
+
+/*
  * Continuous-batching force server.  `slots` worker slots, each with its own context and
  * CUDA stream on `device`, evaluate independent water boxes concurrently; a FIFO queue
  * admits the next request as soon as a slot is free and its estimated device-memory
@@ -564,10 +593,28 @@ int mbx_3b_poly_batch(mbx_context* ctx, int precision, long n, const double* w1,
  * Drop-ins for the reference's per-cluster C entry points, same signatures and
  * meaning (SOURCE/mbpol-2b-poly.cpp:1884-1904, SOURCE/mbpol-3b-poly.cpp:1522-1542).
  * They run one FP64 evaluation on the current CUDA device through a process-wide
- * context.  The reference's optional `force_matrix` decomposition (used only
- * under HEAT_STRESS) is not produced: the array is left untouched.
+ * context.  A non-NULL `force_matrix` receives the reference's pairwise split of the
+ * gradient (read by its HEAT_STRESS build, SOURCE/mbpol.f90:564-566, :951-953), as
+ * mbx_2b_force_matrix_batch / mbx_3b_force_matrix_batch below write it.
  * On a CUDA error they print a message and abort (the reference has no error path).
  */
+/*
+ * The force matrices of many clusters (host arrays, FP64), as the reference's C models
+ * write them (SOURCE/mbpol-2b-poly.cpp:449-653, SOURCE/mbpol-3b-poly.cpp:208-312): entry
+ * (i, j, c) of the cluster's sites (O, H1, H2 per monomer) is component c of the gradient
+ * of the polynomial variable linking sites i and j, with the sign of r_i - r_j.
+ *   2B: fm[108 n], 6 x 6 x 3 per dimer; the X sites' rows are redistributed onto their
+ *       monomer's atoms through the X-site geometry and their columns onto the other
+ *       monomer's O; times the switch, its gradient added to the O-O entries.  Diagonal
+ *       entries are written 0 (the reference copies them from an uninitialised array;
+ *       its reader skips them).  Dimers beyond the 6.5 A cutoff are left untouched.
+ *   3B: fm[243 n], 9 x 9 x 3 per trimer; every off-diagonal entry written (the switching
+ *       product included), the switch gradients added to the O-O entries, the diagonal
+ *       left untouched.
+ */
+int mbx_2b_force_matrix_batch(mbx_context* ctx, long n, const double* w1, const double* w2, double* fm);
+int mbx_3b_force_matrix_batch(mbx_context* ctx, long n, const double* w1, const double* w2, const double* w3,
+                              double* fm);
 void mbpol_2b_poly_(const double* w1, const double* w2, double* E, double* g1, double* g2, double* force_matrix);
 void mbpol_3b_poly_(const double* w1, const double* w2, const double* w3, double* E, double* g1, double* g2,
                     double* g3, double* force_matrix);

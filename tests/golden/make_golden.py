@@ -92,12 +92,16 @@ def main():
         lib.mbpol_2b_poly_(w1.ctypes.data_as(_D), w2.ctypes.data_as(_D), C.byref(e), g1.ctypes.data_as(_D),
                            g2.ctypes.data_as(_D), fm.ctypes.data_as(_D))
         E2[k] = e.value
-        # the reference leaves g untouched beyond the cutoff: record zeros there
+        # the reference leaves g untouched beyond the cutoff: record zeros there.  Its 2B
+        # force matrix takes the 6 diagonal entries from an uninitialised local array
+        # (SOURCE/mbpol-2b-poly.cpp:454, :627-634); its HEAT_STRESS reader skips them
+        # (SOURCE/mbpol.f90:551-553), and so do the tests
         G2[k, 0] = np.nan_to_num(g1)
         G2[k, 1] = np.nan_to_num(g2)
         F2[k] = fm
     E3 = np.zeros(len(W3))
     G3 = np.zeros((len(W3), 3, 9))
+    F3 = np.zeros((len(W3), 243))
     for k in range(len(W3)):
         w = [np.ascontiguousarray(W3[k, q]) for q in range(3)]
         e = C.c_double(0)
@@ -107,6 +111,7 @@ def main():
                            fm.ctypes.data_as(_D))
         E3[k] = e.value
         G3[k] = np.stack(g)
+        F3[k] = fm
     # raw polynomial probes: variables drawn in the physical range (0, 1.5]
     rng = np.random.default_rng(7)
     X2 = rng.uniform(0.01, 1.5, size=(16, 31))
@@ -134,7 +139,7 @@ def main():
             PG[k] = g
         P["PE" + body] = PE
         P["PG" + body] = PG
-    np.savez_compressed(os.path.join(HERE, "mbpol_models.npz"), W2=W2, E2=E2, G2=G2, FM2=F2, W3=W3, E3=E3, G3=G3,
+    np.savez_compressed(os.path.join(HERE, "mbpol_models.npz"), W2=W2, E2=E2, G2=G2, FM2=F2, W3=W3, E3=E3, G3=G3, FM3=F3,
                         X2=X2, X3=X3, **P)
     print("dimers %d (nonzero %d), trimers %d (nonzero %d)" % (len(W2), (E2 != 0).sum(), len(W3), (E3 != 0).sum()))
 

@@ -306,3 +306,54 @@ def test_water_forces_one_call_matches_the_separate_calls(precision):
     m, v = box.mass[:nw3], box.vel[:nw3]
     eng = 0.5 * m * (v * v).sum(1) + ref_ae[:nw3]
     assert rel_err(sc[capi.S_JKIN:capi.S_JKIN + 3], (eng[:, None] * v).sum(0)) <= tol
+
+
+def _offdiag(nsite):
+    m = np.ones((nsite, nsite, 3), bool)
+    for i in range(nsite):
+        m[i, i, :] = False
+    return m.ravel()
+
+
+def test_force_matrices_match_reference_golden(mbx_ctx, golden):
+    """The force matrices of the per-cluster entry points (read by the reference's
+    HEAT_STRESS build) against the reference's own C++ on the golden clusters: every
+    entry its reader uses (the off-diagonal ones), 1e-10 of max(|entry|, 1); 3B leaves its
+    diagonal as given, 2B writes 0 there; dimers beyond the cutoff are left untouched."""
+    lib = mbx_ctx.lib
+    D = C.POINTER(C.c_double)
+    W2 = np.ascontiguousarray(golden["W2"])
+    n2 = len(W2)
+    w1, w2 = np.ascontiguousarray(W2[:, 0]), np.ascontiguousarray(W2[:, 1])
+    fm = np.zeros((n2, 108))
+    assert lib.mbx_2b_force_matrix_batch(mbx_ctx.h, n2, w1.ctypes.data_as(D), w2.ctypes.data_as(D),
+                                         fm.ctypes.data_as(D)) == 0
+    ref = golden["FM2"]
+    off = _offdiag(6)
+    scale = np.maximum(np.abs(ref[:, off]).max(1), 1.0)
+    assert np.all(np.abs(fm[:, off] - ref[:, off]).max(1) <= 1e-10 * scale)
+    assert not fm[:, ~off].any()
+    # the O-O entries carry the switch: the rows of a dimer sum to its gradient (row
+    # sums of the 6 x 6 block, X sites redistributed) -- a check of the bookkeeping
+    G = golden["G2"].reshape(n2, 18)
+    rows = fm.reshape(n2, 6, 6, 3).sum(2).reshape(n2, 18)
+    inside = golden["E2"] != 0
+    assert np.abs(rows[inside] - G[inside]).max() <= 1e-9 * np.abs(G).max()
+    W3 = np.ascontiguousarray(golden["W3"])
+    n3 = len(W3)
+    v = [np.ascontiguousarray(W3[:, q]) for q in range(3)]
+    fm3 = np.zeros((n3, 243))
+    assert lib.mbx_3b_force_matrix_batch(mbx_ctx.h, n3, *(a.ctypes.data_as(D) for a in v),
+                                         fm3.ctypes.data_as(D)) == 0
+    ref3 = golden["FM3"]
+    scale3 = np.maximum(np.abs(ref3).max(1), 1.0)
+    assert np.all(np.abs(fm3 - ref3).max(1) <= 1e-10 * scale3)
+    # through the drop-in symbol, as the reference's Fortran calls it
+    e = C.c_double(0)
+    g1, g2 = np.zeros(9), np.zeros(9)
+    k = int(np.argmax(inside))
+    a, b = np.ascontiguousarray(W2[k, 0]), np.ascontiguousarray(W2[k, 1])
+    f1 = np.zeros(108)
+    lib.mbpol_2b_poly_(a.ctypes.data_as(D), b.ctypes.data_as(D), C.byref(e), g1.ctypes.data_as(D),
+                       g2.ctypes.data_as(D), f1.ctypes.data_as(D))
+    assert np.abs(f1[off] - ref[k, off]).max() <= 1e-10 * max(np.abs(ref[k, off]).max(), 1.0)

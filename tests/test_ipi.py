@@ -93,3 +93,27 @@ def test_polar_params_for_cell_matches_systems(lib):
         from mbx import systems
         want = systems.polar_params_for(np.array(cell, np.float64))
         np.testing.assert_allclose(got, want, rtol=1e-14, atol=0)
+
+
+def test_ipi_unix_socket(lib, tmp_path, monkeypatch):
+    """The unix-socket form of the address (the reference's /tmp/ipi_<name>; the directory
+    from MBX_IPI_UNIX_DIR here): the same exchange as over TCP."""
+    import os
+    monkeypatch.setenv("MBX_IPI_UNIX_DIR", str(tmp_path))
+    rng = np.random.default_rng(13)
+    frames = _frames(rng)
+    srv = FakeIpiServer(frames, unix_dir=str(tmp_path), unix_name="t%d" % os.getpid())
+
+    def force(replica, cell, xyz):
+        return 0.5 * float((xyz ** 2).sum()), -xyz, np.zeros(9), np.zeros((xyz.shape[0] // 3, 3))
+
+    rc, steps, err = capi.ipi_run_callback(srv.address, force)
+    srv.join()
+    assert srv.error is None, srv.error
+    assert rc == 0 and steps == 3, (rc, steps, err)
+    assert srv.statuses == ["NEEDINIT", "READY", "HAVEDATA"] * 3
+    for (_, _, _, pos), reply in zip(frames, srv.replies):
+        np.testing.assert_array_equal(reply["forces"], -(pos * BOHR) * E_AU * BOHR * RATIO)
+    # no socket there: a connection error naming the path
+    rc, _, err = capi.ipi_run_callback("unix:absent%d:0" % os.getpid(), force)
+    assert rc == capi.ERR_ARG and str(tmp_path) in err

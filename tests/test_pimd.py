@@ -64,3 +64,21 @@ def test_centroid_virial_uses_the_first_mode():
 def test_odd_bead_counts_are_refused():
     with pytest.raises(ValueError):
         pimd.transformation_matrix(3)
+
+
+@pytest.mark.parametrize("P", [2, 8, 32])
+@pytest.mark.parametrize("langevin", [False, True])
+def test_library_matrices_match_the_restatement(P, langevin):
+    """mbx_pimd_matrices (host code of the library) = mbx/pimd.py's restatement."""
+    import ctypes as C
+    from mbx import capi
+    lib = capi.load()
+    D = C.POINTER(C.c_double)
+    n2c, c2n, lam = np.zeros((P, P)), np.zeros((P, P)), np.zeros(P)
+    assert lib.mbx_pimd_matrices(P, int(langevin), n2c.ctypes.data_as(D), c2n.ctypes.data_as(D),
+                                 lam.ctypes.data_as(D)) == 0
+    c, c2, l = pimd.transformation_matrix(P, langevin)
+    np.testing.assert_allclose(n2c, c, rtol=0, atol=1e-15)
+    np.testing.assert_allclose(c2n, c2, rtol=0, atol=1e-15)
+    np.testing.assert_allclose(lam, l, rtol=1e-15, atol=0)
+    assert lib.mbx_pimd_matrices(3, 0, None, None, None) == capi.ERR_ARG
