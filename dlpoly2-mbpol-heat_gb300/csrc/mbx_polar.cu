@@ -833,10 +833,10 @@ struct MixArgs {
 
 // FP64 residual of the dipole equations at the current dipoles: r = polr2 E / r4pie0 - mu
 // with E the four fields of the last FP64 evaluation; rounds it for the FP32 solve and
-// clears the correction.  Sums |r|^2 and the count into acc[29..30].
+// clears the correction.  Sums |r|^2, the count and |mu|^2 into acc[29..31].
 __global__ void __launch_bounds__(kThreads) k_pol_resid(PolArgs a, MixArgs m) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    double v[2] = {0, 0};
+    double v[3] = {0, 0, 0};
     if (i < a.n) {
         float4 r = make_float4(0, 0, 0, 0);
         if (a.polr2[i] > a.toler) {
@@ -848,12 +848,13 @@ __global__ void __launch_bounds__(kThreads) k_pol_resid(PolArgs a, MixArgs m) {
             }
             v[0] = rr[0] * rr[0] + rr[1] * rr[1] + rr[2] * rr[2];
             v[1] = 1.0;
+            v[2] = mu[0] * mu[0] + mu[1] * mu[1] + mu[2] * mu[2];
             r = make_float4((float)rr[0], (float)rr[1], (float)rr[2], 0.f);
         }
         m.r32[i] = r;
         m.d32[i] = make_float4(0, 0, 0, 0);
     }
-    block_sum_atomic<2>(v, a.acc + 29);
+    block_sum_atomic<3>(v, a.acc + 29);
 }
 
 // FP32 real-space dipole field (warp per site) of `in`, written to `out` (3 blocks of n).
@@ -2747,12 +2748,13 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
             else fields64(it == 1);
             corrected = false;
             if (field_err) return field_err;
-            if ((e = cudaMemsetAsync(acc + 29, 0, 2 * sizeof(double), s))) return e;
+            if ((e = cudaMemsetAsync(acc + 29, 0, 3 * sizeof(double), s))) return e;
             k_pol_resid<<<blocks(n, kThreads), kThreads, 0, s>>>(a, m);
             ++launches;
-            if ((e = cudaMemcpyAsync(acc_h + 29, acc + 29, 2 * sizeof(double), cudaMemcpyDeviceToHost, s))) return e;
+            if ((e = cudaMemcpyAsync(acc_h + 29, acc + 29, 3 * sizeof(double), cudaMemcpyDeviceToHost, s))) return e;
             if ((e = cudaStreamSynchronize(s))) return e;
             const double rms = std::sqrt(acc_h[29] / (acc_h[30] > 0.0 ? acc_h[30] : 1.0));
+            const double rms_mu = std::sqrt(acc_h[31] / (acc_h[30] > 0.0 ? acc_h[30] : 1.0));
             iterations = it;
             if (fac * rms <= prm[3] || it >= maxit) {
                 if ((e = sor64())) return e;
@@ -2821,7 +2823,11 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
             } else {
                 k_pol_apply<<<blocks(n, kThreads), kThreads, 0, s>>>(a, m, md);
                 ++launches;
-                corrected = true;
+                // the next FP64 evaluation adds the FP32 k-space field of this correction to the
+                // previous one; its FP32 rounding (1e-7 of the correction's field) stays in the
+                // fields of every later residual, so a correction that is not small against
+                // the dipoles (a cold start's first) is followed by a full FP64 evaluation
+                corrected = rms <= 1e-4 * rms_mu;
             }
         }
     }
