@@ -162,3 +162,98 @@ def test_results_independent_of_the_ewald_split(oracle_lib):
         assert np.abs(r["dipoles"] - ref["dipoles"]).max() <= 2e-5 * np.abs(ref["dipoles"]).max()
         sd, rd = r["stress"][diag], ref["stress"][diag]
         assert np.abs(sd - rd).max() <= 2e-5 * np.abs(rd).max()
+
+
+def _two_waters_apart(L=14.0):
+    """Two waters in a cubic cell, every intermolecular distance (images included) above
+    10 A, so the Thole damping and charge smearing between molecules vanish (< 1e-16)."""
+    box = copy.deepcopy(systems.box_for(2, seed=1))
+    box.L = L
+    box.cell = np.array([L, 0, 0, 0, L, 0, 0, 0, L], np.float64)
+    xyz = np.array(box.xyz, np.float64)
+    for w, c in ((0, (2.0, 2.5, 1.5)), (1, (9.0, 8.5, 9.5))):
+        xyz[3 * w:3 * w + 3] += np.array(c) - xyz[3 * w]
+    box.xyz = xyz
+    return box
+
+
+def _lattice_sum(sites, q, mol, L, R):
+    """Direct sum over the image cells within R of a cubic lattice, the cells weighted by a
+    smooth radial taper (1 inside R/2, exp(-1/x) blend to 0 at R): the charges' energy and
+    field at every site, the home cell's intramolecular pairs left out, with the spherical
+    shape terms removed (a sphere in vacuum against the Ewald sum's conducting boundary:
+    E_ewald = E_sphere - 2 pi |M|^2 / 3V, field_ewald = field_sphere + 4 pi M / 3V)."""
+    nmax = int(np.ceil(R / L)) + 1
+    g = np.arange(-nmax, nmax + 1)
+    n = np.array(np.meshgrid(g, g, g, indexing="ij")).reshape(3, -1).T * L
+    s = np.linalg.norm(n, axis=1) / R
+    n, s = n[s < 1], s[s < 1]
+    t = np.clip(2 * s - 1, 0, 1)
+    h = lambda x: np.where(x > 0, np.exp(-1 / np.maximum(x, 1e-300)), 0.0)
+    w = h(1 - t) / (h(1 - t) + h(t))
+    home = np.all(n == 0, axis=1)
+    e = 0.0
+    f = np.zeros((len(q), 3))
+    for i in range(len(q)):
+        for j in range(len(q)):
+            d = sites[i] - sites[j] + n
+            r = np.linalg.norm(d, axis=1)
+            ok = ~home | (mol[i] != mol[j])
+            e += 0.5 * q[i] * q[j] * np.sum(w[ok] / r[ok])
+            f[i] += q[j] * np.sum((w[ok] / r[ok] ** 3)[:, None] * d[ok], axis=0)
+    V = L ** 3
+    M = (q[:, None] * sites).sum(0)
+    return e - 2 * np.pi / (3 * V) * M.dot(M), f + 4 * np.pi / (3 * V) * M
+
+
+def test_lattice_sum_pins_the_ewald_energy(oracle_lib):
+    """The Ewald energy of the charges and the charge-dipole energy against a direct lattice
+    sum (two waters 12 A apart in a 14 A cell; alpha 0.73, rcut 6.9, kmax 20: every
+    truncation below 1e-11).
+    * The exact-erfc Ewald sum (spme_oracle.ewald_kspace's k space, self and excluded-pair
+      terms with scipy's erfc) equals the lattice sum to 1e-9.
+    * The oracle's k space (with the self term) equals the exact one to 1e-11; its total
+      differs only through the reference's erfc fit (SOURCE/erfcc.f: fractional error below
+      1.2e-7) in the excluded pairs' erf(alpha r) / r: |dE| <= 1.2e-7 sum |q_i q_j|
+      erfc(alpha r) / r over those pairs (measured: a tenth of the bound).
+    * With the induced dipoles, the energy is E_qq - mu . E_q / 2 at the oracle's converged
+      dipoles (the stationarity identity of the linear dipole equations), with E_q the lattice
+      sum's charge field; the field's fit error adds at most 1.2e-7 sum |mu_i| |q_j|
+      erfc(alpha r) / r^2 / 2 over the excluded pairs."""
+    from scipy.special import erf, erfc
+
+    import spme_oracle as so
+
+    box = _two_waters_apart()
+    sites, q, dp, _ = oracle_lib.msites_dms(box)
+    polr, polr2 = systems.polarizabilities(2)
+    alpha, rcut, L = 0.73, 6.9, box.L
+    prm = systems.polar_params(alpha=alpha, rcut=rcut, kmax=(20, 20, 20), toler_debye=1e-13)
+    charges = oracle_lib.polar(sites, box.cell, box.imcon, 2, q, dp, polr, np.zeros_like(polr2), prm)
+    full = oracle_lib.polar(sites, box.cell, box.imcon, 2, q, dp, polr, polr2, prm)
+    assert charges["status"] == 0 and full["status"] == 0
+    mol = np.array([0, 0, 0, 1, 1, 1, 0, 1])
+    e_lat, f_lat = _lattice_sum(sites, q, mol, L, 32 * L)
+    e_lat *= so.R4PIE0
+    f_lat *= so.R4PIE0
+    # the exact Ewald sum: k space, self term and the excluded pairs (no real-space pair of
+    # different waters lies within rcut)
+    ek = so.ewald_kspace(sites, q, box.cell, alpha, (20, 20, 20))["eng"]
+    self_term = -alpha / np.sqrt(np.pi) * np.sum(q ** 2) * so.R4PIE0
+    excl = [(i, j) for i in range(8) for j in range(i + 1, 8) if mol[i] == mol[j]]
+    rij = {p: np.linalg.norm(sites[p[0]] - sites[p[1]]) for p in excl}
+    e_excl = -sum(q[i] * q[j] * erf(alpha * rij[(i, j)]) / rij[(i, j)] for i, j in excl) * so.R4PIE0
+    e_exact = ek + self_term + e_excl
+    assert abs(e_exact - e_lat) <= 1e-9 * abs(e_lat)
+    assert abs(charges["eng_kspace"] - (ek + self_term)) <= 1e-11 * abs(ek + self_term)
+    fit = 1.2e-7 * so.R4PIE0 * sum(abs(q[i] * q[j]) * erfc(alpha * rij[(i, j)]) / rij[(i, j)] for i, j in excl)
+    assert abs(charges["engcpe"] - e_lat) <= fit
+    mu = full["dipoles"]
+    e_pol = -0.5 * np.sum(mu * f_lat)
+    fit_f = 0.5 * 1.2e-7 * so.R4PIE0 * sum(
+        np.linalg.norm(mu[a]) * abs(q[b]) * erfc(alpha * rij[(i, j)]) / rij[(i, j)] ** 2
+        for i, j in excl for a, b in ((i, j), (j, i)))
+    # the excluded pairs' energy error is the same in both runs: the difference is the
+    # dipoles' energy alone
+    assert abs((full["engcpe"] - charges["engcpe"]) - e_pol) <= fit_f
+    assert abs(e_pol) > 100 * fit_f
