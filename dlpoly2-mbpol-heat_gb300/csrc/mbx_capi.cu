@@ -1258,6 +1258,43 @@ extern "C" int mbx_set_spme(mbx_context* ctx, int order, double spacing, const i
     return MBX_OK;
 }
 
+extern "C" int mbx_set_polar_skin(mbx_context* ctx, double delr) {
+    if (!ctx) return MBX_ERR_ARG;
+    if (!(delr >= 0.0 && delr < 10.0)) return fail(ctx, MBX_ERR_ARG, "skin must be in [0, 10) Angstrom");
+    ctx->polar.list_skin = delr;
+    ctx->polar.skin_ok = false;
+    return MBX_OK;
+}
+
+extern "C" long mbx_polar_list_builds(const mbx_context* ctx) { return ctx ? ctx->polar.list_builds : -1; }
+
+extern "C" int mbx_polar_last_pairs(mbx_context* ctx, int* pairs, long cap, long* npairs) {
+    if (!ctx || !npairs || cap < 0 || (cap && !pairs)) return MBX_ERR_ARG;
+    PolarState& P = ctx->polar;
+    *npairs = 0;
+    if (!P.nn || P.n_cap == 0) return MBX_OK;
+    const int n = P.last_n;
+    if (n <= 0) return MBX_OK;
+    CK(cudaSetDevice(ctx->device));
+    std::vector<int> nn(n), nbr((size_t)n * P.cap);
+    CK(cudaMemcpyAsync(nn.data(), P.nn, n * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaMemcpyAsync(nbr.data(), P.nbr, nbr.size() * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    long c = 0;
+    for (int i = 0; i < n; ++i)
+        for (int k = 0; k < nn[i]; ++k) {
+            const int j = nbr[(size_t)i * P.cap + k];
+            if (j <= i) continue;
+            if (c < cap) {
+                pairs[2 * c] = i;
+                pairs[2 * c + 1] = j;
+            }
+            ++c;
+        }
+    *npairs = c;
+    return MBX_OK;
+}
+
 extern "C" int mbx_spme_last_grid(const mbx_context* ctx, int* grid) {
     if (!ctx || !grid) return MBX_ERR_ARG;
     for (int a = 0; a < 3; ++a) grid[a] = ctx->polar.spme_order ? ctx->polar.spme_K_last[a] : 0;
@@ -1503,6 +1540,7 @@ extern "C" int mbx_water_step_multi(mbx_context* ctx, int precision, int nbox, c
         c->limit3 = ctx->limit3;
         c->fused = ctx->fused;
         c->polar.precond_sweeps = ctx->polar.precond_sweeps;
+        c->polar.list_skin = ctx->polar.list_skin;
         c->polar.spme_order = ctx->polar.spme_order;
         c->polar.spme_spacing = ctx->polar.spme_spacing;
         for (int a = 0; a < 3; ++a) c->polar.spme_grid[a] = ctx->polar.spme_grid[a];

@@ -192,6 +192,17 @@ struct PolarState {
     double4* ercp = nullptr;               // erfcgenp table, rows 0..mxegrd
     float4* ercp32 = nullptr;              // its screened functions C_n in FP32 (mixed-path ewald2p)
     bool ewald2p_fp64 = false;             // mixed path: keep ewald2p's pair terms in FP64
+    // Verlet skin of the site pair list (0: the list is rebuilt at every call): the pairs
+    // within rcut + list_skin, kept until a site moved more than list_skin / 2
+    double list_skin = 1.0;
+    int *nn_s = nullptr, *nbr_s = nullptr;
+    int cap_s = 768, cap_s_alloc = 0, ns_cap = 0;
+    double* xref = nullptr;                // positions at the skin list's build (x, y, z blocks)
+    bool skin_ok = false;
+    int skin_n = 0, skin_imcon = 0;
+    double skin_rcut = 0.0, skin_delr = 0.0, skin_cell[9] = {};
+    long list_builds = 0;
+    int last_n = 0;                        // sites of the last call (the pair list's rows)
     int *nn = nullptr, *nbr = nullptr, *flag = nullptr;
     float4* xf = nullptr;
     double* tens = nullptr;                // dipole tensors of the list pairs (6 blocks)
@@ -231,6 +242,7 @@ struct PolarState {
     int cap32 = 0, n32 = 0, k32 = 0;
     size_t fac32_cap = 0;
     long inner_sweeps = 0;                 // FP32 conjugate-gradient iterations of the last call
+    int cg_hint = 8;                       // sweeps the last correction solve took (first batch size)
     double* kpart = nullptr;               // per-chunk partial sums of the k-space gathers
     size_t part_cap = 0;
     int nsm = 152;                         // SMs of the device (grid sizing)
@@ -278,6 +290,7 @@ struct PolarState {
     cudaError_t reserve(int nw, int K, size_t nfac);
     cudaError_t reserve_mixed(int n, int K, size_t nfac);
     cudaError_t reserve_part(size_t ndouble);
+    cudaError_t reserve_skin(int n);
     cudaError_t reserve_cells(int n, int ncell);
     // One evaluation on device arrays (precision MBX_FP64 or MBX_MIXED: the dipole
     // equations solved by FP32 corrections under FP64 refinement).  prm[15] as

@@ -261,17 +261,18 @@ __global__ void k_pol_bounds(int n, const unsigned* __restrict__ skey, int* __re
 // A pair whose FP32 distance is inside rcut - 0.01 A (r2in) is inside rcut in FP64 too (the
 // FP32 error of r^2 is below 1e-3 A^2 for coordinates under 1e3 A), so only the thin shell
 // between r2in and r2f takes the reference's FP64 test.
-__global__ void k_pol_list(PolArgs a, int* __restrict__ nn, int* __restrict__ nbr, const float4* __restrict__ xf,
-                           float r2f, float r2in, int* __restrict__ flag, int3 nc, int cells,
-                           const int* __restrict__ sidx, const int* __restrict__ cstart,
+__global__ void k_pol_list(PolArgs a, int* __restrict__ nn, int* __restrict__ nbr, int rowcap, double lc,
+                           const float4* __restrict__ xf, float r2f, float r2in, int* __restrict__ flag, int3 nc,
+                           int cells, const int* __restrict__ sidx, const int* __restrict__ cstart,
                            const int* __restrict__ cend) {
     const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (i >= a.n) return;
     const int mi = site_mol(a, i);
     const float4 pi = xf[i];
-    int* my = nbr + (size_t)i * a.cap;
+    int* my = nbr + (size_t)i * rowcap;
     int cnt = 0;
+    const double lc2 = lc * lc;
     const int ncand = cells ? 27 : 1;
     // FP32 box constants once (converting them per candidate occupies the FP64 pipe)
     const float bx = (float)a.cl.c[0], by = (float)a.cl.c[4], bz = (float)a.cl.c[8];
@@ -314,16 +315,94 @@ __global__ void k_pol_list(PolArgs a, int* __restrict__ nn, int* __restrict__ nb
                     double dx, dy, dz;
                     sep(a, i, j, dx, dy, dz);
                     const double r2 = norm2(dx, dy, dz);
-                    hit = a.rcsq > r2 || a.rcut > __dsqrt_rn(r2);   // the root only near the cut
+                    hit = lc2 > r2 || lc > __dsqrt_rn(r2);   // the root only near the cut
                 }
             }
             const unsigned bal = __ballot_sync(0xffffffffu, hit);
             if (hit) {
                 const int slot = cnt + __popc(bal & ((1u << lane) - 1u));
-                if (slot < a.cap) my[slot] = j;
+                if (slot < rowcap) my[slot] = j;
             }
             cnt += __popc(bal);
         }
+    }
+    if (lane == 0) {
+        nn[i] = min(cnt, rowcap);
+        if (cnt > rowcap) atomicOr(flag, 1);
+    }
+}
+
+// Verlet list with a skin (SOURCE/parlst.f with the rebuild test of SOURCE/centroid_vertest.f):
+// the pairs within rcut + delr are kept between calls and the list is rebuilt once a site
+// has moved more than delr / 2 since the build (flag set).
+__global__ void k_pol_moved(int n, const double* __restrict__ x, const double* __restrict__ y,
+                            const double* __restrict__ z, const double* __restrict__ xref, Cell cl, double half2,
+                            int* __restrict__ flag) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double dx = x[i] - xref[i], dy = y[i] - xref[n + i], dz = z[i] - xref[2 * (size_t)n + i];
+    image(cl, dx, dy, dz);
+    if (dx * dx + dy * dy + dz * dz > half2) atomicOr(flag, 1);
+}
+
+__global__ void k_pol_ref(int n, const double* __restrict__ x, const double* __restrict__ y,
+                          const double* __restrict__ z, double* __restrict__ xref) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    xref[i] = x[i];
+    xref[n + i] = y[i];
+    xref[2 * (size_t)n + i] = z[i];
+}
+
+// The exact list from the skin list: each row's pairs within rcut, tested as k_pol_list does
+// (FP32 with margins, the reference's FP64 test in the shell around the cut), in the skin
+// list's order.
+__global__ void k_pol_filter(PolArgs a, const int* __restrict__ nn_s, const int* __restrict__ nbr_s, int cap_s,
+                             int* __restrict__ nn, int* __restrict__ nbr, const float4* __restrict__ xf, float r2f,
+                             float r2in, int* __restrict__ flag) {
+    const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (i >= a.n) return;
+    const float4 pi = xf[i];
+    const int m = nn_s[i];
+    const int* src = nbr_s + (size_t)i * cap_s;
+    int* my = nbr + (size_t)i * a.cap;
+    const bool ortho = a.cl.imcon == 1 || a.cl.imcon == 2;
+    const float bx = (float)a.cl.c[0], by = (float)a.cl.c[4], bz = (float)a.cl.c[8];
+    const float ibx = (float)a.cl.inv[0], iby = (float)a.cl.inv[1], ibz = (float)a.cl.inv[2];
+    int cnt = 0;
+    for (int b = 0; b < m; b += 32) {
+        const int q = b + lane;
+        bool hit = false;
+        int j = 0;
+        if (q < m) {
+            j = src[q];
+            const float4 pj = xf[j];
+            float d2;
+            if (ortho) {
+                float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+                dx -= bx * rintf(dx * ibx);
+                dy -= by * rintf(dy * iby);
+                dz -= bz * rintf(dz * ibz);
+                d2 = dx * dx + dy * dy + dz * dz;
+            } else {
+                d2 = dist2_img_f(a.cl, pi, pj);
+            }
+            if (d2 < r2in) {
+                hit = true;
+            } else if (d2 < r2f) {
+                double dx, dy, dz;
+                sep(a, i, j, dx, dy, dz);
+                const double r2 = norm2(dx, dy, dz);
+                hit = a.rcsq > r2 || a.rcut > __dsqrt_rn(r2);
+            }
+        }
+        const unsigned bal = __ballot_sync(0xffffffffu, hit);
+        if (hit) {
+            const int slot = cnt + __popc(bal & ((1u << lane) - 1u));
+            if (slot < a.cap) my[slot] = j;
+        }
+        cnt += __popc(bal);
     }
     if (lane == 0) {
         nn[i] = min(cnt, a.cap);
@@ -506,6 +585,7 @@ struct KArgs {
     const double* vh;      // per-site products of the heat sums: q v (3 blocks of n), mu_c v_b (9 blocks)
     double rc[9];
     double scale, ralph, sfac;   // 4 rvolm r4pie0 / epsq, -1 / (4 alpha^2), 2 rvolm r4pie0 / epsq
+    const int* stop = nullptr;   // the CG sweeps' FP32 kernels: nonzero state = return at once
 };
 
 __device__ __forceinline__ double2 cmul(double2 a, double2 b) {
@@ -829,6 +909,7 @@ struct MixArgs {
     float4* d32;      // vector the FP32 field is evaluated for (the CG direction)
     float* e32;       // FP32 field of d32: real space (3 blocks of n), then k space (3 blocks)
     float4 *x, *rho, *q;   // CG: solution, residual, A d32
+    const int* stop = nullptr;   // CG state on the device (nonzero: the sweep kernels return at once)
 };
 
 // FP64 residual of the dipole equations at the current dipoles: r = polr2 E / r4pie0 - mu
@@ -858,7 +939,9 @@ __global__ void __launch_bounds__(kThreads) k_pol_resid(PolArgs a, MixArgs m) {
 }
 
 // FP32 real-space dipole field (warp per site) of `in`, written to `out` (3 blocks of n).
-__global__ void k_pol_dd32(PolArgs a, const float4* __restrict__ in, float* __restrict__ out) {
+__global__ void k_pol_dd32(PolArgs a, const float4* __restrict__ in, float* __restrict__ out,
+                           const int* __restrict__ stop = nullptr) {
+    if (stop && *stop) return;
     const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (i >= a.n) return;
@@ -937,6 +1020,7 @@ __device__ __forceinline__ void stage_tile(const KArgs& k, int4 tl, int rowp, in
 // (their columns are contiguous), so each staged site tile serves 512 vectors.
 __global__ void __launch_bounds__(kSfThreads) k_pol_sfd32(KArgs k, MixArgs m, int schunk, int rowp,
                                                           double* __restrict__ part) {
+    if (k.stop && *k.stop) return;
     extern __shared__ float4 sfd_smem[];
     float4* ds = sfd_smem;                                   // [kSfTile]
     float2* fs = reinterpret_cast<float2*>(sfd_smem + kSfTile);   // [kSfTile][rowp]
@@ -1000,6 +1084,7 @@ __global__ void __launch_bounds__(kSfThreads) k_pol_sfd32(KArgs k, MixArgs m, in
 
 // The site chunks of k_pol_sfd32 added in order; the coefficients of the FP32 gather.
 __global__ void __launch_bounds__(kThreads) k_pol_sfd32_sum(KArgs k, int nchunk, const double* __restrict__ part) {
+    if (k.stop && *k.stop) return;
     const int kk = blockIdx.x * blockDim.x + threadIdx.x;
     if (kk >= k.K) return;
     double skc = 0.0, sks = 0.0;
@@ -1140,6 +1225,7 @@ struct GatherPhase {
 // blockIdx.y; each tile of kKTile vectors summed in FP32, the tiles in FP64; the partial
 // sums of the chunks added in order by k_pol_kfield32_sum.
 __global__ void __launch_bounds__(kThreads) k_pol_kfield32(KArgs k, int kchunk, float* __restrict__ part) {
+    if (k.stop && *k.stop) return;
     extern __shared__ float2 gat_smem[];
     __shared__ float4 cf[kKTile][2];   // kx ky kz c3, c4 ...
     __shared__ int4 ax[kKTile];
@@ -1173,6 +1259,7 @@ __global__ void __launch_bounds__(kThreads) k_pol_kfield32(KArgs k, int kchunk, 
 
 __global__ void __launch_bounds__(kThreads) k_pol_kfield32_sum(KArgs k, PolArgs a, MixArgs m, int nchunk,
                                                                const float* __restrict__ part) {
+    if (k.stop && *k.stop) return;
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= k.n) return;
     float ev[3] = {0, 0, 0};
@@ -1205,6 +1292,7 @@ __global__ void __launch_bounds__(kThreads) k_pcg_init(PolArgs a, MixArgs m) {
 }
 
 __global__ void __launch_bounds__(kThreads) k_pcg_ad(PolArgs a, MixArgs m, int nk) {
+    if (m.stop && *m.stop) return;   // the CG solve has stopped (uniform per launch)
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     double v[1] = {0};
     if (i < a.n) {
@@ -1225,6 +1313,7 @@ __global__ void __launch_bounds__(kThreads) k_pcg_ad(PolArgs a, MixArgs m, int n
 }
 
 __global__ void __launch_bounds__(kThreads) k_pcg_step(PolArgs a, MixArgs m) {
+    if (m.stop && *m.stop) return;   // the CG solve has stopped (uniform per launch)
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     double v[3] = {0, 0, 0};
     const double pq = a.acc[34];
@@ -1247,6 +1336,7 @@ __global__ void __launch_bounds__(kThreads) k_pcg_step(PolArgs a, MixArgs m) {
 
 // d = z + beta d, z = M^-1 rho: the diagonal (z null) or the polynomial preconditioner's z.
 __global__ void __launch_bounds__(kThreads) k_pcg_dir(PolArgs a, MixArgs m, const float4* __restrict__ z) {
+    if (m.stop && *m.stop) return;   // the CG solve has stopped (uniform per launch)
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n || !(a.polr2[i] > a.toler)) return;
     const double rz = a.acc[33];
@@ -1269,6 +1359,7 @@ __global__ void __launch_bounds__(kThreads) k_pcg_dir(PolArgs a, MixArgs m, cons
 // i.e. z = sum_{i<p} (D^-1 T_real)^i D^-1 rho, symmetric; positive definite for even p.
 __global__ void __launch_bounds__(kThreads) k_pcg_jacobi(PolArgs a, MixArgs m, const float* __restrict__ t,
                                                          float4* __restrict__ z) {
+    if (m.stop && *m.stop) return;   // the CG solve has stopped (uniform per launch)
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
     float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -1284,6 +1375,7 @@ __global__ void __launch_bounds__(kThreads) k_pcg_jacobi(PolArgs a, MixArgs m, c
 // rho.z into acc[slot]; with `dir`, also d32 = z (the first direction).
 __global__ void __launch_bounds__(kThreads) k_pcg_rz(PolArgs a, MixArgs m, const float4* __restrict__ z, int slot,
                                                      int dir) {
+    if (m.stop && *m.stop) return;   // the CG solve has stopped (uniform per launch)
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     double v[1] = {0};
     if (i < a.n) {
@@ -1292,6 +1384,29 @@ __global__ void __launch_bounds__(kThreads) k_pcg_rz(PolArgs a, MixArgs m, const
         if (dir) m.d32[i] = zz;
     }
     block_sum_atomic<1>(v, a.acc + slot);
+}
+
+// End of a CG sweep, on the device: the stopping test of the correction solve (|z| <= target
+// with z the diagonally preconditioned residual; a breakdown when d.Ad <= 0 or a sum is not
+// finite), then rho.z <- new rho.z and the sums cleared for the next sweep.
+// st[0]: 0 running, 1 converged, 2 breakdown; st[1]: sweeps run; acc[42..45] the sums of the
+// sweep that stopped it.
+__global__ void k_pcg_next(double* __restrict__ acc, int* __restrict__ st, double target) {
+    if (threadIdx.x != 0 || blockIdx.x != 0 || st[0] != 0) return;
+    st[1] += 1;
+    const double dad = acc[34], rz = acc[35], zz = acc[36], cnt = acc[37];
+    int state = 0;
+    if (!(dad > 0.0) || !isfinite(rz) || !isfinite(zz)) state = 2;
+    else if (sqrt(zz / (cnt > 0.0 ? cnt : 1.0)) <= target) state = 1;
+    if (state) {
+        acc[42] = dad;
+        acc[43] = rz;
+        acc[44] = zz;
+        acc[45] = cnt;
+        st[0] = state;
+    }
+    acc[33] = rz;
+    acc[34] = acc[35] = acc[36] = acc[37] = 0.0;
 }
 
 // mu += d in FP64; refreshes the masked dipoles.
@@ -2027,7 +2142,7 @@ cudaError_t launch_msite_redistribute(int nw, double gamma, double* fx, double* 
 }
 
 void PolarState::release() {
-    void* p[] = {ercp, ercp32, nn, nbr, flag, xf, tens, intra, fld, vesp, ae, eik, kv, kx2, lmn, sf, kterm, acc, kco, fac, md, vh, polr6,
+    void* p[] = {ercp, ercp32, nn_s, nbr_s, xref, nn, nbr, flag, xf, tens, intra, fld, vesp, ae, eik, kv, kx2, lmn, sf, kterm, acc, kco, fac, md, vh, polr6,
                  ckey, cskey, cidx, csidx, csort, cstart, cend,
                  tens32, r32, d32, e32, kco32, fac32, ktile, kaux, kcol, colk, kpart, cg_x, cg_r, cg_q, cg_z, vh32};
     for (void* q : p)
@@ -2046,6 +2161,10 @@ void PolarState::release() {
             }
     ercp = nullptr;
     ercp32 = nullptr;
+    nn_s = nbr_s = nullptr;
+    xref = nullptr;
+    ns_cap = cap_s_alloc = 0;
+    skin_ok = false;
     nn = nbr = flag = nullptr;
     xf = nullptr;
     tens = intra = fld = vesp = ae = sf = kterm = acc = kco = vh = polr6 = nullptr;
@@ -2154,6 +2273,27 @@ cudaError_t PolarState::reserve_cells(int n, int ncell) {
         if ((e = cudaMalloc(&cstart, ncell * sizeof(int)))) return e;
         if ((e = cudaMalloc(&cend, ncell * sizeof(int)))) return e;
         ncell_cap = ncell;
+    }
+    return cudaSuccess;
+}
+
+// The skin list (cap_s partners per site) and the positions of its build.
+cudaError_t PolarState::reserve_skin(int n) {
+    cudaError_t e;
+    if (n > ns_cap || cap_s != cap_s_alloc) {
+        void* p[] = {nn_s, nbr_s, xref};
+        for (void* q : p)
+            if (q) cudaFree(q);
+        nn_s = nbr_s = nullptr;
+        xref = nullptr;
+        ns_cap = cap_s_alloc = 0;
+        skin_ok = false;
+        const size_t m = (size_t)std::max(n, 1);
+        if ((e = cudaMalloc(&nn_s, m * sizeof(int)))) return e;
+        if ((e = cudaMalloc(&nbr_s, m * cap_s * sizeof(int)))) return e;
+        if ((e = cudaMalloc(&xref, 3 * m * sizeof(double)))) return e;
+        ns_cap = n;
+        cap_s_alloc = cap_s;
     }
     return cudaSuccess;
 }
@@ -2549,42 +2689,119 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
         converged = true;
         return cudaSuccess;
     }
-    // list (grows until every row fits); cell-sorted candidates where the box allows
+    // list (grows until every row fits); cell-sorted candidates where the box allows.  With a
+    // skin the pairs within rcut + skin are kept between calls (rebuilt when a site moved more
+    // than skin / 2) and the exact list is filtered from them each call.
+    const double skin = list_skin > 0.0 ? list_skin : 0.0;
+    last_n = n;
     const float r2f = (float)((rcut + 0.01) * (rcut + 0.01));
     const float r2in = rcut > 0.02 ? (float)((rcut - 0.01) * (rcut - 0.01)) : 0.f;
-    int3 nc = make_int3(1, 1, 1);
-    int cells = 0;
-    if (cl.imcon == 1 || cl.imcon == 2) {
-        const double wcell = rcut + 0.02;
-        nc = make_int3((int)(cl.c[0] / wcell), (int)(cl.c[4] / wcell), (int)(cl.c[8] / wcell));
-        cells = nc.x >= 3 && nc.y >= 3 && nc.z >= 3 && (long)nc.x * nc.y * nc.z < (1L << 24);
-        if (!cells) nc = make_int3(1, 1, 1);
-    }
-    if (cells) {
-        if ((e = reserve_cells(n, nc.x * nc.y * nc.z))) return e;
-        k_pol_keys<<<blocks(n, kThreads), kThreads, 0, s>>>(n, x, y, z, cl, nc, ckey, cidx);
-        size_t b = csort_bytes;
-        if ((e = cub::DeviceRadixSort::SortPairs(csort, b, ckey, cskey, cidx, csidx, n, 0, 32, s))) return e;
-        if ((e = cudaMemsetAsync(cstart, 0, (size_t)nc.x * nc.y * nc.z * sizeof(int), s))) return e;
-        if ((e = cudaMemsetAsync(cend, 0, (size_t)nc.x * nc.y * nc.z * sizeof(int), s))) return e;
-        k_pol_bounds<<<blocks(n, kThreads), kThreads, 0, s>>>(n, cskey, cstart, cend);
-        launches += 3;
-    }
-    for (;;) {
-        bind(a);
-        k_pol_f32<<<blocks(n, kThreads), kThreads, 0, s>>>(n, x, y, z, xf);
-        if ((e = cudaMemsetAsync(flag, 0, sizeof(int), s))) return e;
-        k_pol_list<<<blocks(32L * n, kThreads), kThreads, 0, s>>>(a, nn, nbr, xf, r2f, r2in, flag, nc, cells, csidx,
-                                                                   cstart, cend);
-        launches += 2;
-        int fh = 0;
-        if ((e = cudaMemcpyAsync(acc_h, flag, sizeof(int), cudaMemcpyDeviceToHost, s))) return e;
-        if ((e = cudaStreamSynchronize(s))) return e;
-        std::memcpy(&fh, acc_h, sizeof(int));
-        if (!fh) break;
-        cap = std::min(2 * cap, std::max(n, 32));   // a row holds at most n - 1 sites
-        if ((e = reserve(nw, K, nfac))) return e;
-        if (mixed && (e = reserve_mixed(n, K, nfac))) return e;
+    auto build = [&](int* lnn, int* lnbr, int rowcap, double lcut) -> cudaError_t {
+        // one pass of k_pol_list at cut lcut into (lnn, lnbr); the overflow flag is read by the caller
+        cudaError_t err;
+        int3 nc = make_int3(1, 1, 1);
+        int cells = 0;
+        if (cl.imcon == 1 || cl.imcon == 2) {
+            const double wcell = lcut + 0.02;
+            nc = make_int3((int)(cl.c[0] / wcell), (int)(cl.c[4] / wcell), (int)(cl.c[8] / wcell));
+            cells = nc.x >= 3 && nc.y >= 3 && nc.z >= 3 && (long)nc.x * nc.y * nc.z < (1L << 24);
+            if (!cells) nc = make_int3(1, 1, 1);
+        }
+        if (cells) {
+            if ((err = reserve_cells(n, nc.x * nc.y * nc.z))) return err;
+            k_pol_keys<<<blocks(n, kThreads), kThreads, 0, s>>>(n, x, y, z, cl, nc, ckey, cidx);
+            size_t b = csort_bytes;
+            if ((err = cub::DeviceRadixSort::SortPairs(csort, b, ckey, cskey, cidx, csidx, n, 0, 32, s))) return err;
+            if ((err = cudaMemsetAsync(cstart, 0, (size_t)nc.x * nc.y * nc.z * sizeof(int), s))) return err;
+            if ((err = cudaMemsetAsync(cend, 0, (size_t)nc.x * nc.y * nc.z * sizeof(int), s))) return err;
+            k_pol_bounds<<<blocks(n, kThreads), kThreads, 0, s>>>(n, cskey, cstart, cend);
+            launches += 3;
+        }
+        const float lf = (float)((lcut + 0.01) * (lcut + 0.01));
+        const float li = lcut > 0.02 ? (float)((lcut - 0.01) * (lcut - 0.01)) : 0.f;
+        k_pol_list<<<blocks(32L * n, kThreads), kThreads, 0, s>>>(a, lnn, lnbr, rowcap, lcut, xf, lf, li, flag, nc,
+                                                                   cells, csidx, cstart, cend);
+        ++launches;
+        return cudaGetLastError();
+    };
+    auto read_flags = [&](int* h2) -> cudaError_t {
+        cudaError_t err;
+        if ((err = cudaMemcpyAsync(acc_h, flag, 2 * sizeof(int), cudaMemcpyDeviceToHost, s))) return err;
+        if ((err = cudaStreamSynchronize(s))) return err;
+        std::memcpy(h2, acc_h, 2 * sizeof(int));
+        return cudaSuccess;
+    };
+    bind(a);
+    k_pol_f32<<<blocks(n, kThreads), kThreads, 0, s>>>(n, x, y, z, xf);
+    ++launches;
+    if (skin > 0.0) {
+        if ((e = reserve_skin(n))) return e;
+        bool same = skin_ok && skin_n == n && skin_rcut == rcut && skin_delr == skin && skin_imcon == cl.imcon &&
+                    std::equal(cl.c, cl.c + 9, skin_cell);
+        for (;;) {
+            if (same) {
+                // the movement test and the filter of the kept list, one host read for both
+                bind(a);
+                if ((e = cudaMemsetAsync(flag, 0, 2 * sizeof(int), s))) return e;
+                k_pol_moved<<<blocks(n, kThreads), kThreads, 0, s>>>(n, x, y, z, xref, cl, 0.25 * skin * skin,
+                                                                     flag + 1);
+                k_pol_filter<<<blocks(32L * n, kThreads), kThreads, 0, s>>>(a, nn_s, nbr_s, cap_s, nn, nbr, xf, r2f,
+                                                                            r2in, flag);
+                launches += 2;
+                int fh[2];
+                if ((e = read_flags(fh))) return e;
+                if (fh[1]) {
+                    same = false;
+                } else if (fh[0]) {
+                    cap = std::min(2 * cap, std::max(n, 32));
+                    if ((e = reserve(nw, K, nfac))) return e;
+                    if (mixed && (e = reserve_mixed(n, K, nfac))) return e;
+                    // reserve() reallocates the FP32 positions with the rows
+                    k_pol_f32<<<blocks(n, kThreads), kThreads, 0, s>>>(n, x, y, z, xf);
+                    ++launches;
+                    continue;
+                } else {
+                    break;
+                }
+            }
+            // (re)build the skin list at rcut + skin until every row fits
+            for (;;) {
+                if ((e = cudaMemsetAsync(flag, 0, 2 * sizeof(int), s))) return e;
+                bind(a);
+                if ((e = build(nn_s, nbr_s, cap_s, rcut + skin))) return e;
+                int fh[2];
+                if ((e = read_flags(fh))) return e;
+                if (!fh[0]) break;
+                cap_s = std::min(2 * cap_s, std::max(n, 32));
+                if ((e = reserve_skin(n))) return e;
+            }
+            k_pol_ref<<<blocks(n, kThreads), kThreads, 0, s>>>(n, x, y, z, xref);
+            ++launches;
+            ++list_builds;
+            skin_ok = true;
+            skin_n = n;
+            skin_rcut = rcut;
+            skin_delr = skin;
+            skin_imcon = cl.imcon;
+            std::copy(cl.c, cl.c + 9, skin_cell);
+            same = true;
+        }
+    } else {
+        skin_ok = false;
+        for (;;) {
+            bind(a);
+            if ((e = cudaMemsetAsync(flag, 0, 2 * sizeof(int), s))) return e;
+            if ((e = build(nn, nbr, cap, rcut))) return e;
+            int fh[2];
+            if ((e = read_flags(fh))) return e;
+            if (!fh[0]) break;
+            cap = std::min(2 * cap, std::max(n, 32));   // a row holds at most n - 1 sites
+            if ((e = reserve(nw, K, nfac))) return e;
+            if (mixed && (e = reserve_mixed(n, K, nfac))) return e;
+            k_pol_f32<<<blocks(n, kThreads), kThreads, 0, s>>>(n, x, y, z, xf);
+            ++launches;
+        }
+        ++list_builds;
     }
     bind(a);
     bindk(k);
@@ -2769,53 +2986,80 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
             // 1e-6 of the FP64 residual or 5x below toler
             const double target = std::max(1e-6 * rms, 0.2 * prm[3]);
             bool broke = false;
+            // The sweeps are enqueued in batches without host round trips: the stopping test
+            // runs on the device (k_pcg_next), and once it has stopped the solve, the rest of
+            // the batch returns at once.  The host reads the state after each batch; the first
+            // batch is as long as the previous solve took.
+            int* cgs = flag + 2;
+            MixArgs ms = m;
+            ms.stop = cgs;
+            KArgs ks = k;
+            ks.stop = cgs;
             for (bool restart = true; restart;) {
                 restart = false;
                 broke = false;
                 if ((e = cudaMemsetAsync(acc + 33, 0, 5 * sizeof(double), s))) return e;
+                if ((e = cudaMemsetAsync(cgs, 0, 2 * sizeof(int), s))) return e;
                 k_pcg_init<<<blocks(n, kThreads), kThreads, 0, s>>>(a, m);
                 ++launches;
                 const bool poly = pre > 1;
                 if (poly && (e = precondition(33, 1))) return e;
-                for (int sweep = 0; sweep < 100; ++sweep) {
-                    k_pol_dd32<<<blocks(32L * n, kThreads), kThreads, 0, s>>>(a, d32, e32);
-                    if (spme_on) {
-                        if ((e = spme.field32(n, x, y, z, d32, polr2, k.sfac, dum_self, e32 + 3 * (size_t)n, s)))
-                            return e;
-                        launches += spme.launches;
-                    } else if (K) {
-                        k_pol_sfd32<<<dim3(nkt2, nsc2_used), kSfThreads, sfd_smem, s>>>(k, m, schunk2, rowp2, kpart);
-                        k_pol_sfd32_sum<<<blocks(K, kThreads), kThreads, 0, s>>>(k, nsc2_used, kpart);
-                        k_pol_kfield32<<<dim3(sblk1, nc1), kThreads, gat_smem, s>>>(k, kc1, (float*)kpart);
-                        k_pol_kfield32_sum<<<sblk1, kThreads, 0, s>>>(k, a, m, nc1, (const float*)kpart);
-                        launches += 4;
-                    }
-                    k_pcg_ad<<<blocks(n, kThreads), kThreads, 0, s>>>(a, m, (K || spme_on) ? 1 : 0);
-                    k_pcg_step<<<blocks(n, kThreads), kThreads, 0, s>>>(a, m);
-                    if (poly && (e = precondition(35, 0))) return e;
-                    k_pcg_dir<<<blocks(n, kThreads), kThreads, 0, s>>>(a, m, poly ? cg_z : nullptr);
-                    launches += 4;
-                    ++inner_sweeps;
-                    if ((e = cudaMemcpyAsync(acc_h + 34, acc + 34, 4 * sizeof(double), cudaMemcpyDeviceToHost, s)))
-                        return e;
-                    // next iteration: rho.z <- new rho.z; clear the sums
-                    if ((e = cudaMemcpyAsync(acc + 33, acc + 35, sizeof(double), cudaMemcpyDeviceToDevice, s))) return e;
-                    if ((e = cudaMemsetAsync(acc + 34, 0, 4 * sizeof(double), s))) return e;
-                    if ((e = cudaStreamSynchronize(s))) return e;
-                    // d.Ad <= 0 (or a non-finite sum): the preconditioned operator is not
-                    // positive definite in FP32 here; the diagonal preconditioner takes over,
-                    // and with it an FP64 SOR step replaces this correction
-                    if (!(acc_h[34] > 0.0) || !std::isfinite(acc_h[35]) || !std::isfinite(acc_h[36])) {
-                        if (pre > 1) {
-                            pre = 1;
-                            restart = true;
-                        } else {
-                            broke = true;
+                int queued = 0, batch = std::max(2, std::min(cg_hint, 40));
+                int st[2] = {0, 0};
+                while (queued < 100) {
+                    for (int b = 0; b < batch && queued < 100; ++b, ++queued) {
+                        k_pol_dd32<<<blocks(32L * n, kThreads), kThreads, 0, s>>>(a, d32, e32, cgs);
+                        if (spme_on) {
+                            if ((e = spme.field32(n, x, y, z, d32, polr2, k.sfac, dum_self, e32 + 3 * (size_t)n, s,
+                                                  cgs)))
+                                return e;
+                            launches += spme.launches;
+                        } else if (K) {
+                            k_pol_sfd32<<<dim3(nkt2, nsc2_used), kSfThreads, sfd_smem, s>>>(ks, ms, schunk2, rowp2,
+                                                                                            kpart);
+                            k_pol_sfd32_sum<<<blocks(K, kThreads), kThreads, 0, s>>>(ks, nsc2_used, kpart);
+                            k_pol_kfield32<<<dim3(sblk1, nc1), kThreads, gat_smem, s>>>(ks, kc1, (float*)kpart);
+                            k_pol_kfield32_sum<<<sblk1, kThreads, 0, s>>>(ks, a, ms, nc1, (const float*)kpart);
+                            launches += 4;
                         }
-                        break;
+                        k_pcg_ad<<<blocks(n, kThreads), kThreads, 0, s>>>(a, ms, (K || spme_on) ? 1 : 0);
+                        k_pcg_step<<<blocks(n, kThreads), kThreads, 0, s>>>(a, ms);
+                        if (poly) {
+                            k_pcg_jacobi<<<blocks(n, kThreads), kThreads, 0, s>>>(a, ms, nullptr, cg_z);
+                            for (int qq = 1; qq < pre; ++qq) {
+                                k_pol_dd32<<<blocks(32L * n, kThreads), kThreads, 0, s>>>(a, cg_z, e32 + 3 * (size_t)n,
+                                                                                           cgs);
+                                k_pcg_jacobi<<<blocks(n, kThreads), kThreads, 0, s>>>(a, ms, e32 + 3 * (size_t)n,
+                                                                                     cg_z);
+                                launches += 2;
+                            }
+                            // rho.z of the polynomial z replaces k_pcg_step's diagonal one
+                            if ((e = cudaMemsetAsync(acc + 35, 0, sizeof(double), s))) return e;
+                            k_pcg_rz<<<blocks(n, kThreads), kThreads, 0, s>>>(a, ms, cg_z, 35, 0);
+                            launches += 2;
+                        }
+                        k_pcg_dir<<<blocks(n, kThreads), kThreads, 0, s>>>(a, ms, poly ? cg_z : nullptr);
+                        k_pcg_next<<<1, 32, 0, s>>>(acc, cgs, target);
+                        launches += 5;
                     }
-                    const double zr = std::sqrt(acc_h[36] / (acc_h[37] > 0.0 ? acc_h[37] : 1.0));
-                    if (zr <= target) break;
+                    if ((e = cudaMemcpyAsync(acc_h + 60, cgs, 2 * sizeof(int), cudaMemcpyDeviceToHost, s))) return e;
+                    if ((e = cudaStreamSynchronize(s))) return e;
+                    std::memcpy(st, acc_h + 60, 2 * sizeof(int));
+                    if (st[0] != 0) break;
+                    batch = 2;
+                }
+                inner_sweeps += st[1];
+                cg_hint = std::max(2, st[1]);
+                // d.Ad <= 0 (or a non-finite sum): the preconditioned operator is not
+                // positive definite in FP32 here; the diagonal preconditioner takes over,
+                // and with it an FP64 SOR step replaces this correction
+                if (st[0] == 2) {
+                    if (pre > 1) {
+                        pre = 1;
+                        restart = true;
+                    } else {
+                        broke = true;
+                    }
                 }
             }
             if (broke) {

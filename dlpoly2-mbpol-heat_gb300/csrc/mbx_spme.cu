@@ -3,13 +3,13 @@
 // conventions; the reference's charge-only SPME is SOURCE/ewald_spme.f (B-splines
 // SOURCE/bspgen.f, moduli SOURCE/bspcoe.f, forces SOURCE/spme_for.f, FFT SOURCE/dlpfft3.f).
 //
-//   spread    thread per site: p^3 grid points of its B-spline support, FP64 (FP32 for the
-//             correction solve) atomic adds into the complex grid
+//   spread    8 lanes per site, one z plane of its p^3-point B-spline support each, FP64
+//             (FP32 for the correction solve) atomic adds into the complex grid
 //   fft       one axis per launch: a block loads nl lines into shared memory ([element][line],
 //             line pitch nl + 1), runs the Stockham radix-2/3/4/5 stages there and stores
 //             them back; the z pass of a convolution does forward FFT, influence function
 //             and backward FFT of its lines in one launch
-//   gather    thread per site over its p^3 points, summed per x row first
+//   gather    8 lanes per site, one z plane each, summed per x row, then over the lanes
 //   k terms   thread per grid point: energies, virial and heat-current terms of every k
 //             vector, block partial sums added in order by one block
 #include "mbx_kernels.cuh"
@@ -184,8 +184,10 @@ struct GridDims {
 template <typename T, int MODE>
 __global__ void __launch_bounds__(kFftThreads) k_fft_axis(typename Cx<T>::t* data, size_t gstride, int axis,
                                                           FftAxis ax, GridDims d, int nl, int ntile,
-                                                          const typename Cx<T>::t* tw, const T* G) {
+                                                          const typename Cx<T>::t* tw, const T* G,
+                                                          const int* __restrict__ stop) {
     typedef typename Cx<T>::t C;
+    if (stop && *stop) return;   // the CG solve that queued this pass has stopped
     extern __shared__ __align__(16) unsigned char fft_smem[];
     const int n = ax.n, P = nl + 1;
     C* s0 = reinterpret_cast<C*>(fft_smem);
@@ -264,6 +266,7 @@ struct SpArgs {
     int n, K1, K2, K3;
     double rc[9];    // s_a = rc[a] x + rc[a + 3] y + rc[a + 6] z
     double jac[9];   // dt_a / dr_c = K_a rc[a + 3c] at [3a + c]
+    const int* stop; // FP32 CG sweeps: nonzero = the solve has stopped, return at once
 };
 
 // M_p(w + j), j = 0..p-1, for w in [0, 1) (bspgen's values bspx(i, j + 1)), and with
@@ -339,6 +342,30 @@ __device__ __forceinline__ void dip_of(const DV* d, int j, double& x, double& y,
     z = v.z;
 }
 
+// The spread and gather kernels give each site a group of kLanes (8) consecutive lanes, lane
+// jz of the group handling the z plane jz of the site's support (lanes jz >= p idle): eight
+// times the threads of a thread-per-site form, which left the SMs latency-bound.
+constexpr int kLanes = 8;
+
+// a[jz] with jz a run-time lane index, by unrolled selects (a dynamic index would move the
+// spline arrays to local memory)
+template <typename T, int P>
+__device__ __forceinline__ T pick(const T (&a)[P], int jz) {
+    T v = a[0];
+#pragma unroll
+    for (int k = 1; k < P; ++k) v = jz == k ? a[k] : v;
+    return v;
+}
+
+// Sum of v over the site's lane group (width kLanes, the group's own mask).
+template <typename T>
+__device__ __forceinline__ T group_sum(T v) {
+    const unsigned gm = 0xffu << (threadIdx.x & 24);
+#pragma unroll
+    for (int o = kLanes / 2; o > 0; o >>= 1) v += __shfl_xor_sync(gm, v, o, kLanes);
+    return v;
+}
+
 // Spread one density (or two: real and imaginary part) onto the grid.
 //   MODE 0: re += mu . grad M                      (dipole field evaluations)
 //   MODE 1: re += mu . grad M, im += q M           (the first evaluation: dipoles and charges)
@@ -352,8 +379,10 @@ __global__ void __launch_bounds__(kSpThreads) k_spme_spread(SpArgs s, const doub
                                                             const double* __restrict__ polr2,
                                                             typename Cx<T>::t* __restrict__ grid) {
     typedef typename Cx<T>::t C;
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= s.n) return;
+    if (s.stop && *s.stop) return;
+    const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    const int j = (int)(t / kLanes), jz = (int)(t % kLanes);
+    if (j >= s.n || jz >= P) return;
     int gi[3][P];
     T th[3][P], d1[3][P], d2[3][P];
     site_splines<T, P, 1>(s, x[j], y[j], z[j], gi, th, d1, d2);
@@ -363,22 +392,21 @@ __global__ void __launch_bounds__(kSpThreads) k_spme_spread(SpArgs s, const doub
     to_t<T>(s, mxd, myd, mzd, mt);
     const T qj = MODE >= 1 ? (T)q[j] : T(0);
     const size_t K12 = (size_t)s.K1 * s.K2;
-#pragma unroll 1
-    for (int jz = 0; jz < P; ++jz) {
-#pragma unroll 1
-        for (int jy = 0; jy < P; ++jy) {
-            const T tyz = th[1][jy] * th[2][jz];
-            // w = dx (mt_x ty tz) + tx (mt_y dy tz + mt_z ty dz) (+ q tx ty tz)
-            const T r1 = mt[0] * tyz;
-            T r2 = mt[1] * d1[1][jy] * th[2][jz] + mt[2] * th[1][jy] * d1[2][jz];
-            if (MODE == 2) r2 += qj * tyz;
-            C* row = grid + gi[2][jz] * K12 + (size_t)gi[1][jy] * s.K1;
+    const T tz = pick(th[2], jz), dz = pick(d1[2], jz);
+    C* plane = grid + pick(gi[2], jz) * K12;
 #pragma unroll
-            for (int jx = 0; jx < P; ++jx) {
-                const T w = d1[0][jx] * r1 + th[0][jx] * r2;
-                atomic_add_re(row + gi[0][jx], w);
-                if (MODE >= 1) atomic_add_im(row + gi[0][jx], qj * th[0][jx] * tyz);
-            }
+    for (int jy = 0; jy < P; ++jy) {
+        const T tyz = th[1][jy] * tz;
+        // w = dx (mt_x ty tz) + tx (mt_y dy tz + mt_z ty dz) (+ q tx ty tz)
+        const T r1 = mt[0] * tyz;
+        T r2 = mt[1] * d1[1][jy] * tz + mt[2] * th[1][jy] * dz;
+        if (MODE == 2) r2 += qj * tyz;
+        C* row = plane + (size_t)gi[1][jy] * s.K1;
+#pragma unroll
+        for (int jx = 0; jx < P; ++jx) {
+            const T w = d1[0][jx] * r1 + th[0][jx] * r2;
+            atomic_add_re(row + gi[0][jx], w);
+            if (MODE >= 1) atomic_add_im(row + gi[0][jx], qj * th[0][jx] * tyz);
         }
     }
 }
@@ -392,8 +420,9 @@ __global__ void __launch_bounds__(kSpThreads) k_spme_spread_heat(SpArgs s, const
                                                                  const double4* __restrict__ md,
                                                                  const double* __restrict__ vh,
                                                                  double2* __restrict__ grid, size_t gstride) {
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= s.n) return;
+    const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    const int j = (int)(t / kLanes), jz = (int)(t % kLanes);
+    if (j >= s.n || jz >= P) return;
     int gi[3][P];
     double th[3][P], d1[3][P], d2[3][P];
     site_splines<double, P, 0>(s, x[j], y[j], z[j], gi, th, d1, d2);
@@ -406,21 +435,20 @@ __global__ void __launch_bounds__(kSpThreads) k_spme_spread_heat(SpArgs s, const
     for (int r = 0; r < 12; ++r) w[3 + r] = vh[(size_t)r * s.n + j];
     w[15] = 0.0;
     const size_t K12 = (size_t)s.K1 * s.K2;
-#pragma unroll 1
-    for (int jz = 0; jz < P; ++jz) {
-#pragma unroll 1
-        for (int jy = 0; jy < P; ++jy) {
-            const double tyz = th[1][jy] * th[2][jz];
-            const size_t row = gi[2][jz] * K12 + (size_t)gi[1][jy] * s.K1;
-#pragma unroll 1
-            for (int jx = 0; jx < P; ++jx) {
-                const double t = th[0][jx] * tyz;
-                const size_t g = row + gi[0][jx];
+    const double tz = pick(th[2], jz);
+    const size_t plane = pick(gi[2], jz) * K12;
 #pragma unroll
-                for (int h = 0; h < 8; ++h) {
-                    if (w[2 * h] != 0.0) atomicAdd(&grid[h * gstride + g].x, w[2 * h] * t);
-                    if (w[2 * h + 1] != 0.0) atomicAdd(&grid[h * gstride + g].y, w[2 * h + 1] * t);
-                }
+    for (int jy = 0; jy < P; ++jy) {
+        const double tyz = th[1][jy] * tz;
+        const size_t row = plane + (size_t)gi[1][jy] * s.K1;
+#pragma unroll
+        for (int jx = 0; jx < P; ++jx) {
+            const double tt = th[0][jx] * tyz;
+            const size_t g = row + gi[0][jx];
+#pragma unroll
+            for (int h = 0; h < 8; ++h) {
+                if (w[2 * h] != 0.0) atomicAdd(&grid[h * gstride + g].x, w[2 * h] * tt);
+                if (w[2 * h + 1] != 0.0) atomicAdd(&grid[h * gstride + g].y, w[2 * h + 1] * tt);
             }
         }
     }
@@ -440,18 +468,21 @@ __global__ void __launch_bounds__(kSpThreads) k_spme_field(SpArgs s, const doubl
                                                            double* __restrict__ efc, const float4* __restrict__ d32,
                                                            float* __restrict__ e32k) {
     typedef typename Cx<T>::t C;
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= s.n) return;
-    int gi[3][P];
-    T th[3][P], d1[3][P], d2[3][P];
-    site_splines<T, P, 1>(s, x[j], y[j], z[j], gi, th, d1, d2);
+    if (s.stop && *s.stop) return;
+    const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    const int j = (int)(t / kLanes), jz = (int)(t % kLanes);
+    if (j >= s.n) return;   // whole lane groups leave together
     T D[3] = {0, 0, 0}, Dq[3] = {0, 0, 0};
-    const size_t K12 = (size_t)s.K1 * s.K2;
-#pragma unroll 1
-    for (int jz = 0; jz < P; ++jz) {
-#pragma unroll 1
+    if (jz < P) {
+        int gi[3][P];
+        T th[3][P], d1[3][P], d2[3][P];
+        site_splines<T, P, 1>(s, x[j], y[j], z[j], gi, th, d1, d2);
+        const size_t K12 = (size_t)s.K1 * s.K2;
+        const C* plane = grid + pick(gi[2], jz) * K12;
+        const T tz = pick(th[2], jz), dz = pick(d1[2], jz);
+#pragma unroll
         for (int jy = 0; jy < P; ++jy) {
-            const C* row = grid + gi[2][jz] * K12 + (size_t)gi[1][jy] * s.K1;
+            const C* row = plane + (size_t)gi[1][jy] * s.K1;
             T s0 = 0, s1 = 0, q0 = 0, q1 = 0;
 #pragma unroll
             for (int jx = 0; jx < P; ++jx) {
@@ -463,7 +494,7 @@ __global__ void __launch_bounds__(kSpThreads) k_spme_field(SpArgs s, const doubl
                     q1 += p.y * d1[0][jx];
                 }
             }
-            const T a = th[1][jy] * th[2][jz], b = d1[1][jy] * th[2][jz], c = th[1][jy] * d1[2][jz];
+            const T a = th[1][jy] * tz, b = d1[1][jy] * tz, c = th[1][jy] * dz;
             D[0] += a * s1;
             D[1] += b * s0;
             D[2] += c * s0;
@@ -474,6 +505,12 @@ __global__ void __launch_bounds__(kSpThreads) k_spme_field(SpArgs s, const doubl
             }
         }
     }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        D[c] = group_sum(D[c]);
+        if (FIRST) Dq[c] = group_sum(Dq[c]);
+    }
+    if (jz != 0) return;
     const bool pol = polr2[j] > 1e-6;
     const int n = s.n;
     for (int c = 0; c < 3; ++c) {
@@ -506,22 +543,24 @@ __global__ void __launch_bounds__(kSpThreads) k_spme_final_gather(SpArgs s, cons
                                                                   const double4* __restrict__ md, double sfac,
                                                                   double* __restrict__ part5, double* __restrict__ acc,
                                                                   double* __restrict__ field) {
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    const int j = (int)(t / kLanes), jz = (int)(t % kLanes);
     double red[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-    if (j < s.n) {
-        int gi[3][P];
-        double th[3][P], d1[3][P], d2[3][P];
-        site_splines<double, P, 2>(s, x[j], y[j], z[j], gi, th, d1, d2);
-        const double4 m = md[j];
-        double mt[3];
-        to_t<double>(s, m.x, m.y, m.z, mt);
+    if (j < s.n) {   // whole lane groups in or out: the group sums below see all 8 lanes
         double Pt = 0, Pq = 0, D[3] = {0, 0, 0}, W[3] = {0, 0, 0};
-        const size_t K12 = (size_t)s.K1 * s.K2;
-#pragma unroll 1
-        for (int jz = 0; jz < P; ++jz) {
-#pragma unroll 1
+        const double4 m = md[j];
+        if (jz < P) {
+            int gi[3][P];
+            double th[3][P], d1[3][P], d2[3][P];
+            site_splines<double, P, 2>(s, x[j], y[j], z[j], gi, th, d1, d2);
+            double mt[3];
+            to_t<double>(s, m.x, m.y, m.z, mt);
+            const size_t K12 = (size_t)s.K1 * s.K2;
+            const double2* plane = grid + pick(gi[2], jz) * K12;
+            const double tz = pick(th[2], jz), dz = pick(d1[2], jz), ddz = pick(d2[2], jz);
+#pragma unroll
             for (int jy = 0; jy < P; ++jy) {
-                const double2* row = grid + gi[2][jz] * K12 + (size_t)gi[1][jy] * s.K1;
+                const double2* row = plane + (size_t)gi[1][jy] * s.K1;
                 double s0 = 0, s1 = 0, s2 = 0, q0 = 0;
 #pragma unroll
                 for (int jx = 0; jx < P; ++jx) {
@@ -532,7 +571,6 @@ __global__ void __launch_bounds__(kSpThreads) k_spme_final_gather(SpArgs s, cons
                     q0 += p.y * th[0][jx];
                 }
                 const double ty = th[1][jy], dy = d1[1][jy], ddy = d2[1][jy];
-                const double tz = th[2][jz], dz = d1[2][jz], ddz = d2[2][jz];
                 const double a = ty * tz, b = dy * tz, c = ty * dz;
                 Pt += a * s0;
                 Pq += a * q0;
@@ -546,28 +584,36 @@ __global__ void __launch_bounds__(kSpThreads) k_spme_final_gather(SpArgs s, cons
                 W[2] += mt[0] * c * s1 + (mt[1] * f + mt[2] * h) * s0;
             }
         }
-        const double qj = q[j];
-        double Dr[3], Wr[3];
+        Pt = group_sum(Pt);
+        Pq = group_sum(Pq);
         for (int c = 0; c < 3; ++c) {
-            Dr[c] = s.jac[c] * D[0] + s.jac[3 + c] * D[1] + s.jac[6 + c] * D[2];
-            Wr[c] = s.jac[c] * W[0] + s.jac[3 + c] * W[1] + s.jac[6 + c] * W[2];
+            D[c] = group_sum(D[c]);
+            W[c] = group_sum(W[c]);
         }
-        const int n = s.n;
-        for (int c = 0; c < 3; ++c) {
-            const double v = -0.5 * (qj * Dr[c] + Wr[c]);
-            part5[(size_t)c * n + j] = v;
-            red[6 + c] = v;
-            if (field) field[(size_t)c * n + j] = -sfac * Dr[c];
+        if (jz == 0) {
+            const double qj = q[j];
+            double Dr[3], Wr[3];
+            for (int c = 0; c < 3; ++c) {
+                Dr[c] = s.jac[c] * D[0] + s.jac[3 + c] * D[1] + s.jac[6 + c] * D[2];
+                Wr[c] = s.jac[c] * W[0] + s.jac[3 + c] * W[1] + s.jac[6 + c] * W[2];
+            }
+            const int n = s.n;
+            for (int c = 0; c < 3; ++c) {
+                const double v = -0.5 * (qj * Dr[c] + Wr[c]);
+                part5[(size_t)c * n + j] = v;
+                red[6 + c] = v;
+                if (field) field[(size_t)c * n + j] = -sfac * Dr[c];
+            }
+            part5[3 * (size_t)n + j] = 0.5 * Pq;
+            part5[4 * (size_t)n + j] = 0.5 * (Pt - Pq);
+            const double mu[3] = {m.x, m.y, m.z};
+            red[0] = mu[0] * Dr[0];
+            red[1] = mu[1] * Dr[1];
+            red[2] = mu[2] * Dr[2];
+            red[3] = mu[1] * Dr[0];
+            red[4] = mu[2] * Dr[0];
+            red[5] = mu[2] * Dr[1];
         }
-        part5[3 * (size_t)n + j] = 0.5 * Pq;
-        part5[4 * (size_t)n + j] = 0.5 * (Pt - Pq);
-        const double mu[3] = {m.x, m.y, m.z};
-        red[0] = mu[0] * Dr[0];
-        red[1] = mu[1] * Dr[1];
-        red[2] = mu[2] * Dr[2];
-        red[3] = mu[1] * Dr[0];
-        red[4] = mu[2] * Dr[0];
-        red[5] = mu[2] * Dr[1];
     }
     block_sum_atomic<9>(red, acc + 11);
 }
@@ -741,7 +787,8 @@ cudaError_t allow_fft_smem() {
 // One axis pass over `count` grids.
 template <typename T>
 cudaError_t fft_pass(int mode, typename Cx<T>::t* data, size_t gstride, int count, int axis, const FftAxis& ax,
-                     const int* K, const typename Cx<T>::t* tw, const T* G, cudaStream_t s) {
+                     const int* K, const typename Cx<T>::t* tw, const T* G, cudaStream_t s,
+                     const int* stop = nullptr) {
     const int n = ax.n;
     const int nl = lines_per_block(n);
     const GridDims d{K[0], K[1], K[2]};
@@ -757,10 +804,10 @@ cudaError_t fft_pass(int mode, typename Cx<T>::t* data, size_t gstride, int coun
     if (sm > (size_t)kMaxFftSmem) return cudaErrorInvalidValue;
     const dim3 g(nb, count);
     switch (mode) {
-        case 0: k_fft_axis<T, 0><<<g, kFftThreads, sm, s>>>(data, gstride, axis, ax, d, nl, ntile, tw, G); break;
-        case 1: k_fft_axis<T, 1><<<g, kFftThreads, sm, s>>>(data, gstride, axis, ax, d, nl, ntile, tw, G); break;
-        case 2: k_fft_axis<T, 2><<<g, kFftThreads, sm, s>>>(data, gstride, axis, ax, d, nl, ntile, tw, G); break;
-        default: k_fft_axis<T, 3><<<g, kFftThreads, sm, s>>>(data, gstride, axis, ax, d, nl, ntile, tw, G); break;
+        case 0: k_fft_axis<T, 0><<<g, kFftThreads, sm, s>>>(data, gstride, axis, ax, d, nl, ntile, tw, G, stop); break;
+        case 1: k_fft_axis<T, 1><<<g, kFftThreads, sm, s>>>(data, gstride, axis, ax, d, nl, ntile, tw, G, stop); break;
+        case 2: k_fft_axis<T, 2><<<g, kFftThreads, sm, s>>>(data, gstride, axis, ax, d, nl, ntile, tw, G, stop); break;
+        default: k_fft_axis<T, 3><<<g, kFftThreads, sm, s>>>(data, gstride, axis, ax, d, nl, ntile, tw, G, stop); break;
     }
     return cudaGetLastError();
 }
@@ -769,13 +816,13 @@ cudaError_t fft_pass(int mode, typename Cx<T>::t* data, size_t gstride, int coun
 // backward z), backward y, backward x.
 template <typename T>
 cudaError_t convolve(typename Cx<T>::t* data, const FftAxis* ax, const int* K, const typename Cx<T>::t* tw, const T* G,
-                     cudaStream_t s, long& launches) {
+                     cudaStream_t s, long& launches, const int* stop = nullptr) {
     cudaError_t e;
-    if ((e = fft_pass<T>(0, data, 0, 1, 0, ax[0], K, tw, G, s))) return e;
-    if ((e = fft_pass<T>(0, data, 0, 1, 1, ax[1], K, tw, G, s))) return e;
-    if ((e = fft_pass<T>(2, data, 0, 1, 2, ax[2], K, tw, G, s))) return e;
-    if ((e = fft_pass<T>(1, data, 0, 1, 1, ax[1], K, tw, G, s))) return e;
-    if ((e = fft_pass<T>(1, data, 0, 1, 0, ax[0], K, tw, G, s))) return e;
+    if ((e = fft_pass<T>(0, data, 0, 1, 0, ax[0], K, tw, G, s, stop))) return e;
+    if ((e = fft_pass<T>(0, data, 0, 1, 1, ax[1], K, tw, G, s, stop))) return e;
+    if ((e = fft_pass<T>(2, data, 0, 1, 2, ax[2], K, tw, G, s, stop))) return e;
+    if ((e = fft_pass<T>(1, data, 0, 1, 1, ax[1], K, tw, G, s, stop))) return e;
+    if ((e = fft_pass<T>(1, data, 0, 1, 0, ax[0], K, tw, G, s, stop))) return e;
     launches += 5;
     return cudaSuccess;
 }
@@ -786,6 +833,7 @@ SpArgs sp_args(const SpmeState& st, int n) {
     a.K1 = st.K[0];
     a.K2 = st.K[1];
     a.K3 = st.K[2];
+    a.stop = nullptr;
     for (int i = 0; i < 9; ++i) {
         a.rc[i] = st.rc[i];
         a.jac[i] = st.jac[i];
@@ -1009,7 +1057,7 @@ cudaError_t SpmeState::field64(int n, const double* x, const double* y, const do
     launches = 0;
     if ((e = cudaMemsetAsync(grid, 0, ng * sizeof(double2), s))) return e;
     const SpArgs sa = sp_args(*this, n);
-    const unsigned nb = nblocks(n, kSpThreads);
+    const unsigned nb = nblocks((long)kLanes * n, kSpThreads);
     if (n > 0) {
         if (q) {
             SPME_ORDER_SWITCH(order, (k_spme_spread<double, P_, 1, double4><<<nb, kSpThreads, 0, s>>>(
@@ -1035,18 +1083,20 @@ cudaError_t SpmeState::field64(int n, const double* x, const double* y, const do
 }
 
 cudaError_t SpmeState::field32(int n, const double* x, const double* y, const double* z, const float4* d,
-                               const double* polr2, double sfac, double dum, float* e32k, cudaStream_t s) {
+                               const double* polr2, double sfac, double dum, float* e32k, cudaStream_t s,
+                               const int* stop) {
     cudaError_t e;
     launches = 0;
     if (!have32) return cudaErrorInvalidValue;
     if ((e = cudaMemsetAsync(grid32, 0, ng * sizeof(float2), s))) return e;
-    const SpArgs sa = sp_args(*this, n);
-    const unsigned nb = nblocks(n, kSpThreads);
+    SpArgs sa = sp_args(*this, n);
+    sa.stop = stop;
+    const unsigned nb = nblocks((long)kLanes * n, kSpThreads);
     if (n > 0)
         SPME_ORDER_SWITCH(order, (k_spme_spread<float, P_, 0, float4><<<nb, kSpThreads, 0, s>>>(
                                      sa, x, y, z, nullptr, d, polr2, grid32)));
     if ((e = cudaGetLastError())) return e;
-    if ((e = convolve<float>(grid32, ax, K, tw32, G32, s, launches))) return e;
+    if ((e = convolve<float>(grid32, ax, K, tw32, G32, s, launches, stop))) return e;
     if (n > 0)
         SPME_ORDER_SWITCH(order, (k_spme_field<float, P_, false><<<nb, kSpThreads, 0, s>>>(
                                      sa, x, y, z, grid32, polr2, sfac, dum, nullptr, nullptr, nullptr, nullptr,
@@ -1067,7 +1117,7 @@ cudaError_t SpmeState::final(int n, const double* x, const double* y, const doub
     if ((e = cudaMemsetAsync(grid, 0, (size_t)ngr * gs * sizeof(double2), s))) return e;
     if ((e = cudaMemsetAsync(acc + 11, 0, 9 * sizeof(double), s))) return e;
     const SpArgs sa = sp_args(*this, n);
-    const unsigned nb = nblocks(n, kSpThreads);
+    const unsigned nb = nblocks((long)kLanes * n, kSpThreads);
     if (n > 0) {
         SPME_ORDER_SWITCH(order, (k_spme_spread<double, P_, 2, double4><<<nb, kSpThreads, 0, s>>>(
                                      sa, x, y, z, q, md, nullptr, grid)));
@@ -1088,7 +1138,7 @@ cudaError_t SpmeState::final(int n, const double* x, const double* y, const doub
     if (n > 0) {
         SPME_ORDER_SWITCH(order, (k_spme_final_gather<P_><<<nb, kSpThreads, 0, s>>>(sa, x, y, z, grid, q, md, sfac,
                                                                                    part5, acc, field)));
-        k_spme_drift<<<nb, kSpThreads, 0, s>>>(n, acc, part5);
+        k_spme_drift<<<nblocks(n, kSpThreads), kSpThreads, 0, s>>>(n, acc, part5);
     }
     k_spme_kreduce<<<1, 1024, 0, s>>>(nblk, part, acc);
     launches += (heat ? 2 : 1) + 3 + 1 + 3 + (n > 0 ? 2 : 0) + 1;

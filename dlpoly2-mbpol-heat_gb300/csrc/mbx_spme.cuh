@@ -99,8 +99,11 @@ struct SpmeState {
                         const double4* md, const double* polr2, const double* mx, const double* my,
                         const double* mz, double sfac, double dum, double* efm, double* efc, cudaStream_t s);
     // The same in FP32 for the correction solve: e32k = (polr2 > 1e-6 ? field(d) : 0) + dum d.
+    // stop (device, or null): when nonzero the kernels return at once (a CG solve that has
+    // stopped while further sweeps were queued).
     cudaError_t field32(int n, const double* x, const double* y, const double* z, const float4* d,
-                        const double* polr2, double sfac, double dum, float* e32k, cudaStream_t s);
+                        const double* polr2, double sfac, double dum, float* e32k, cudaStream_t s,
+                        const int* stop = nullptr);
     // Final pass at the converged dipoles.  part5 (5 blocks of n): per site the k-space
     // force / scale (mean removed), half the charges' potential, half the dipoles'
     // potential (the layout of the Ewald force gather, scale = 2 sfac); acc[48..58] =

@@ -148,6 +148,10 @@ def load(path=None):
     L.mbx_set_precond_sweeps.argtypes = [C.c_void_p, C.c_int]
     L.mbx_polar_field_timing.argtypes = [C.c_void_p, _D, _D, C.POINTER(C.c_long)]
     L.mbx_set_spme.argtypes = [C.c_void_p, C.c_int, C.c_double, _I]
+    L.mbx_set_polar_skin.argtypes = [C.c_void_p, C.c_double]
+    L.mbx_polar_list_builds.argtypes = [C.c_void_p]
+    L.mbx_polar_list_builds.restype = C.c_long
+    L.mbx_polar_last_pairs.argtypes = [C.c_void_p, _I, C.c_long, _L]
     L.mbx_spme_last_grid.argtypes = [C.c_void_p, _I]
     L.mbx_spme_grid_for_cell.argtypes = [_D, C.c_double, _I]
     L.mbx_spme_kspace.argtypes = [C.c_void_p, _D, C.c_int, _I, C.c_int, _D, C.c_int] + [_D] * 10
@@ -444,6 +448,20 @@ class Context:
         `grid` (3 ints) or the grid of `spacing`."""
         g = None if grid is None else np.ascontiguousarray(grid, np.int32)
         self._check(self.lib.mbx_set_spme(self.h, int(order), float(spacing), _p(g, _I)), "mbx_set_spme")
+
+    def set_polar_skin(self, delr):
+        self._check(self.lib.mbx_set_polar_skin(self.h, float(delr)), "mbx_set_polar_skin")
+
+    def polar_list_builds(self):
+        return int(self.lib.mbx_polar_list_builds(self.h))
+
+    def polar_last_pairs(self):
+        """(npairs x 2) site pairs i < j within rcut of the last electrostatics call"""
+        n = C.c_long(0)
+        self._check(self.lib.mbx_polar_last_pairs(self.h, None, 0, C.byref(n)), "mbx_polar_last_pairs")
+        out = np.zeros((max(n.value, 1), 2), np.int32)
+        self._check(self.lib.mbx_polar_last_pairs(self.h, _p(out, _I), n.value, C.byref(n)), "mbx_polar_last_pairs")
+        return out[:n.value]
 
     def spme_last_grid(self):
         g = np.zeros(3, np.int32)

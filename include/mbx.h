@@ -250,6 +250,19 @@ double mbx_trim(mbx_context* ctx, double keep_bytes);
  * of the last electrostatics call (zeros with the Ewald sum).
  */
 int mbx_set_spme(mbx_context* ctx, int order, double spacing, const int* grid);
+/*
+ * The electrostatics' site pair list as the reference's Verlet list (SOURCE/parlst.f with
+ * the rebuild test of SOURCE/centroid_vertest.f:53-88): the pairs within rcut + delr are kept
+ * between calls of the context and rebuilt once a site has moved more than delr / 2 since
+ * the build (or the cell, rcut or size changed); every call filters the pairs within rcut
+ * from them with the reference's cut test, so results do not depend on delr.  delr 0
+ * rebuilds the list at every call; the default is 1 Angstrom.  mbx_polar_list_builds
+ * counts the builds; mbx_polar_last_pairs gives the last call's pairs within rcut (i < j,
+ * 0-based sites), up to cap of them in pairs[2 * cap], their count in *npairs.
+ */
+int mbx_set_polar_skin(mbx_context* ctx, double delr);
+long mbx_polar_list_builds(const mbx_context* ctx);
+int mbx_polar_last_pairs(mbx_context* ctx, int* pairs, long cap, long* npairs);
 int mbx_spme_last_grid(const mbx_context* ctx, int* grid);
 /* The grid mbx_set_spme picks for a cell at a spacing (grid[3] written). */
 int mbx_spme_grid_for_cell(const double* cell, double spacing, int* grid);

@@ -224,3 +224,76 @@ def test_gpu_dipoles_solve_the_oracle_equations(mbx_ctx, oracle_lib, precision):
     npol = int((polr2 > 1e-6).sum())
     assert l2 / np.sqrt(3 * npol) <= prm[3] / (1.0 - prm[4]), (l2, prm[3])
     assert linf <= 20 * prm[3]
+
+
+def _brute_pairs(sites, cell, nw, rcut):
+    """Site pairs i < j of different waters within rcut (the Verlet pairs of SOURCE/parlst.f
+    with exclude_ttm's intramolecular exclusions), by brute force with the nearest image."""
+    n = sites.shape[0]
+    mol = np.concatenate([np.arange(3 * nw) // 3, np.arange(nw)])
+    h = np.asarray(cell, np.float64).reshape(3, 3)        # rows: the cell vectors
+    hinv = np.linalg.inv(h)
+    out = []
+    for i in range(n - 1):
+        d = sites[i] - sites[i + 1:]
+        s = d @ hinv
+        s -= np.round(s)
+        r2 = np.sum((s @ h) ** 2, 1)
+        j = np.nonzero((r2 < rcut * rcut) & (mol[i + 1:] != mol[i]))[0] + i + 1
+        out.extend((i, int(k)) for k in j)
+    return set(out)
+
+
+@pytest.mark.parametrize("which", ["config0", "triclinic"])
+def test_pair_list_is_the_verlet_set(oracle_lib, which):
+    """The electrostatics' site pair list (kept with a skin) is exactly the set of site pairs
+    of different waters within rcut."""
+    if which == "config0":
+        box = systems.config0()
+        prm = systems.polar_params(alpha=0.3, rcut=9.0, kmax=(8, 8, 8), toler_debye=1e-8)
+    else:
+        box = systems.box_for(64, seed=9)
+        L = box.L
+        box.cell = np.array([L, 0, 0, 0.2 * L, L, 0, 0.1 * L, -0.15 * L, L], dtype=np.float64)
+        box.imcon = 3
+        prm = systems.polar_params(alpha=0.55, rcut=5.0, kmax=(7, 7, 7), toler_debye=1e-8)
+    sites, q, dp, polr, polr2, prm = _case(oracle_lib, box, prm)
+    ctx = capi.Context(0)
+    try:
+        ctx.polar(sites, box.cell, box.imcon, box.nw, q, dp, polr, polr2, prm)
+        got = set(map(tuple, ctx.polar_last_pairs().tolist()))
+    finally:
+        ctx.close()
+    want = _brute_pairs(sites, box.cell, box.nw, prm[1])
+    assert got == want, (len(got), len(want), len(got ^ want))
+
+
+def test_skin_list_reuse_matches_rebuilding(oracle_lib):
+    """Along a trajectory (atoms moved by v dt, the fastest 0.06 A per step, so that a skin
+    of 0.3 A runs out after a few steps) the electrostatics with the kept skin list equal those with the
+    list rebuilt at every call (the same pairs, summed in another order), and the list is
+    rebuilt only when a site moved more than half the skin."""
+    box = systems.config0()
+    prm = systems.polar_params(alpha=0.3, rcut=9.0, kmax=(8, 8, 8), toler_debye=1e-10)
+    polr, polr2 = systems.polarizabilities(box.nw)
+    kept, fresh = capi.Context(0), capi.Context(0)
+    try:
+        kept.set_polar_skin(0.3)
+        fresh.set_polar_skin(0.0)
+        x0 = box.xyz.copy()
+        steps = 8
+        dt = 0.06 / np.abs(box.vel).max()                # the fastest atom moves 0.06 A per step
+        for k in range(steps):
+            box.xyz = x0 + k * dt * box.vel
+            sites, q, dp, _ = oracle_lib.msites_dms(box)
+            a = kept.polar(sites, box.cell, box.imcon, box.nw, q, dp, polr, polr2, prm, vel=box.vel)
+            b = fresh.polar(sites, box.cell, box.imcon, box.nw, q, dp, polr, polr2, prm, vel=box.vel)
+            assert a["iterations"] == b["iterations"]
+            assert abs(a["engcpe"] - b["engcpe"]) <= 1e-12 * abs(b["engcpe"])
+            for key in ("forces", "dipoles", "atomic_energy", "jpot", "jkin"):
+                assert np.abs(a[key] - b[key]).max() <= 1e-11 * np.abs(b[key]).max(), key
+        assert fresh.polar_list_builds() == steps
+        assert 1 < kept.polar_list_builds() < steps
+    finally:
+        kept.close()
+        fresh.close()
