@@ -195,7 +195,7 @@ struct PolarState {
     // Verlet skin of the site pair list (0: the list is rebuilt at every call): the pairs
     // within rcut + list_skin, kept until a site moved more than list_skin / 2
     double list_skin = 1.0;
-    int *nn_s = nullptr, *nbr_s = nullptr;
+    int *nn_s = nullptr, *nbr_s = nullptr, *npol_s = nullptr;
     int cap_s = 768, cap_s_alloc = 0, ns_cap = 0;
     double* xref = nullptr;                // positions at the skin list's build (x, y, z blocks)
     bool skin_ok = false;
@@ -204,6 +204,7 @@ struct PolarState {
     long list_builds = 0;
     int last_n = 0;                        // sites of the last call (the pair list's rows)
     int *nn = nullptr, *nbr = nullptr, *flag = nullptr;
+    int* npol = nullptr;                   // per row: the polarizable partners, first in the row
     float4* xf = nullptr;
     double* tens = nullptr;                // dipole tensors of the list pairs (6 blocks)
     double* intra = nullptr;               // intramolecular O/H dipole tensors (18 per water)

@@ -81,9 +81,9 @@ __host__ __device__ inline double gammln(double xx) {
     return tmp + log(2.5066282746310005 * ser / x);
 }
 
-__device__ inline double gammq(double a, double x) {
+// gammq(a, x) with gln = gammln(a) given (a per-call constant of the smeared-charge term)
+__device__ inline double gammq_g(double a, double x, double gln) {
     const double eps = (double)3.e-7f, fpmin = (double)1.e-30f;
-    const double gln = gammln(a);
     if (x < a + 1.0) {
         if (x <= 0.0) return 1.0;
         double ap = a, sum = 1.0 / a, del = sum;
@@ -111,6 +111,8 @@ __device__ inline double gammq(double a, double x) {
     return exp(-x + a * log(x) - gln) * h;
 }
 
+__device__ inline double gammq(double a, double x) { return gammq_g(a, x, gammln(a)); }
+
 // B_0..B_3 of the real-space sum from erfcc (rfield / ewald3p intramolecular form)
 __device__ inline void bfun_exact(double alpha, double rr, double rri, double rsqi, double bbb[4]) {
     const double a = alpha * rr;
@@ -129,17 +131,20 @@ struct PolArgs {
     int nw, n, cap;
     const double *x, *y, *z, *q, *polr, *polr2, *dp;
     const double* polr6;   // polr^(1/6) per site: the Thole width of a pair is polr6_i polr6_j
+    const double* rpolr6;  // 1 / polr6 per site
     double *mx, *my, *mz;
     const double *vx, *vy, *vz;
     double *fx, *fy, *fz;
     double gamma, alpha, rcut, rcsq, eps, athole, athole12, athole13, ascc, ascd, toler, omega;
     const double4* ercp;
     const float4* ercp32;   // C_n = B_n + (2n-1)!! / r^(2n+1) per table row, FP32 (mixed path), or null
-    double drewd;
+    double drewd, rdrewd;   // the erfcgenp grid step and its reciprocal
     const int *nn, *nbr;
-    double* tens;   // 6 blocks of n * cap
+    const int* npol;   // per row: its first npol partners are the polarizable ones (polr2 > 1e-6)
+    double* tens;   // 6 blocks of n * cap: the first npol entries of the polarizable rows
     float* tens32;  // the same in FP32 (mixed precision), or null
     double* intra;  // 18 per water
+    float* intra32; // the same in FP32 (the FP32 real-space field)
     double *efk, *efc, *emu, *efm;   // 3 blocks of n each
     double *vesp, *ae;
     double* acc;
@@ -158,6 +163,22 @@ __device__ __forceinline__ double norm2(double dx, double dy, double dz) {
     return dadd(dadd(dmul(dx, dx), dmul(dy, dy)), dmul(dz, dz));
 }
 
+// interp with the grid index from r / drewd as a product with the reciprocal step (the
+// index and fraction agree with the quotient's to rounding)
+__device__ __forceinline__ void interp_r(const PolArgs& a, double rr, double bbb[4]) {
+    const double u = rr * a.rdrewd;
+    const int ll = (int)u;
+    const double ppp = u - double(ll);
+    const double4 v0 = a.ercp[ll], v1 = a.ercp[ll + 1], v2 = a.ercp[ll + 2];
+    const double vk[4] = {v0.x, v0.y, v0.z, v0.w}, vk1[4] = {v1.x, v1.y, v1.z, v1.w}, vk2[4] = {v2.x, v2.y, v2.z, v2.w};
+#pragma unroll
+    for (int n = 0; n < 4; ++n) {
+        const double t1 = vk[n] + (vk1[n] - vk[n]) * ppp;
+        const double t2 = vk1[n] + (vk2[n] - vk1[n]) * (ppp - 1.0);
+        bbb[n] = t1 + (t2 - t1) * ppp * 0.5;
+    }
+}
+
 __device__ __forceinline__ void interp(const PolArgs& a, double rr, double bbb[4]) {
     const int ll = (int)(rr / a.drewd);
     const double ppp = rr / a.drewd - double(ll);
@@ -174,6 +195,16 @@ __device__ __forceinline__ void interp(const PolArgs& a, double rr, double bbb[4
 __device__ __forceinline__ double pow4(double t) {
     const double t2 = t * t;
     return t2 * t2;
+}
+
+// 1 / sqrt(x) for x > 0 (a squared pair distance): the FP32 estimate refined by two
+// Newton-Raphson steps y <- y (3 - x y^2) / 2, each squaring the relative error (~1e-7 ->
+// ~1e-14 -> rounding level).  Eight FP64-pipe operations where a correctly rounded root
+// and a division take about twice that; results agree with them to a few ulp.
+__device__ __forceinline__ double rsqrt_nr(double x) {
+    double y = (double)rsqrtf((float)x);
+    y = y * (1.5 - 0.5 * x * y * y);
+    return y * (1.5 - 0.5 * x * y * y);
 }
 
 // Heat-current contribution of the force-matrix entry (row a, column b, F) after the
@@ -261,10 +292,10 @@ __global__ void k_pol_bounds(int n, const unsigned* __restrict__ skey, int* __re
 // A pair whose FP32 distance is inside rcut - 0.01 A (r2in) is inside rcut in FP64 too (the
 // FP32 error of r^2 is below 1e-3 A^2 for coordinates under 1e3 A), so only the thin shell
 // between r2in and r2f takes the reference's FP64 test.
-__global__ void k_pol_list(PolArgs a, int* __restrict__ nn, int* __restrict__ nbr, int rowcap, double lc,
-                           const float4* __restrict__ xf, float r2f, float r2in, int* __restrict__ flag, int3 nc,
-                           int cells, const int* __restrict__ sidx, const int* __restrict__ cstart,
-                           const int* __restrict__ cend) {
+__global__ void k_pol_list(PolArgs a, int* __restrict__ nn, int* __restrict__ nbr, int* __restrict__ npol,
+                           int rowcap, double lc, const float4* __restrict__ xf, float r2f, float r2in,
+                           int* __restrict__ flag, int3 nc, int cells, const int* __restrict__ sidx,
+                           const int* __restrict__ cstart, const int* __restrict__ cend) {
     const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (i >= a.n) return;
@@ -277,53 +308,58 @@ __global__ void k_pol_list(PolArgs a, int* __restrict__ nn, int* __restrict__ nb
     // FP32 box constants once (converting them per candidate occupies the FP64 pipe)
     const float bx = (float)a.cl.c[0], by = (float)a.cl.c[4], bz = (float)a.cl.c[8];
     const float ibx = (float)a.cl.inv[0], iby = (float)a.cl.inv[1], ibz = (float)a.cl.inv[2];
-    for (int c = 0; c < ncand; ++c) {
-        int beg = 0, end = a.n;
-        if (cells) {
-            const int cx = pol_wrap(a.x[i] * a.cl.inv[0], nc.x), cy = pol_wrap(a.y[i] * a.cl.inv[1], nc.y),
-                      cz = pol_wrap(a.z[i] * a.cl.inv[2], nc.z);
-            const int ox = c % 3 - 1, oy = (c / 3) % 3 - 1, oz = c / 9 - 1;
-            const int cc = (((cz + oz + nc.z) % nc.z) * nc.y + (cy + oy + nc.y) % nc.y) * nc.x + (cx + ox + nc.x) % nc.x;
-            beg = cstart[cc];
-            end = cend[cc];
-        }
-        for (int b = beg; b < end; b += 32) {
-            const int q = b + lane;
-            bool hit = false;
-            int j = 0;
-            if (q < end) {
-                j = cells ? sidx[q] : q;
-                bool near = false, inside = false;
-                if (j != i && site_mol(a, j) != mi) {
-                    const float4 pj = xf[j];
-                    float d2;
-                    if (cells) {   // orthorhombic
-                        float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
-                        dx -= bx * rintf(dx * ibx);
-                        dy -= by * rintf(dy * iby);
-                        dz -= bz * rintf(dz * ibz);
-                        d2 = dx * dx + dy * dy + dz * dz;
-                    } else {
-                        d2 = dist2_img_f(a.cl, pi, pj);
+    // two passes: the polarizable partners first (the dipole tensors are kept for them only)
+    for (int pass = 0; pass < 2; ++pass) {
+        if (pass == 1 && lane == 0) npol[i] = min(cnt, rowcap);
+        for (int c = 0; c < ncand; ++c) {
+            int beg = 0, end = a.n;
+            if (cells) {
+                const int cx = pol_wrap(a.x[i] * a.cl.inv[0], nc.x), cy = pol_wrap(a.y[i] * a.cl.inv[1], nc.y),
+                          cz = pol_wrap(a.z[i] * a.cl.inv[2], nc.z);
+                const int ox = c % 3 - 1, oy = (c / 3) % 3 - 1, oz = c / 9 - 1;
+                const int cc = (((cz + oz + nc.z) % nc.z) * nc.y + (cy + oy + nc.y) % nc.y) * nc.x + (cx + ox + nc.x) % nc.x;
+                beg = cstart[cc];
+                end = cend[cc];
+            }
+            for (int b = beg; b < end; b += 32) {
+                const int q = b + lane;
+                bool hit = false;
+                int j = 0;
+                if (q < end) {
+                    j = cells ? sidx[q] : q;
+                    bool near = false, inside = false;
+                    if (j != i && site_mol(a, j) != mi && (a.polr2[j] > 1e-6) == (pass == 0)) {
+                        const float4 pj = xf[j];
+                        float d2;
+                        if (cells) {   // orthorhombic
+                            float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+                            dx -= bx * rintf(dx * ibx);
+                            dy -= by * rintf(dy * iby);
+                            dz -= bz * rintf(dz * ibz);
+                            d2 = dx * dx + dy * dy + dz * dz;
+                        } else {
+                            d2 = dist2_img_f(a.cl, pi, pj);
+                        }
+                        near = d2 < r2f;
+                        inside = d2 < r2in;
                     }
-                    near = d2 < r2f;
-                    inside = d2 < r2in;
+                    if (inside) {
+                        hit = true;
+                    } else if (near) {
+                        double dx, dy, dz;
+                        sep(a, i, j, dx, dy, dz);
+                        const double r2 = norm2(dx, dy, dz);
+                        // the reference's test; the root only where rounding could decide it
+                        hit = lc2 > r2 || (r2 < lc2 * (1.0 + 1e-14) && lc > __dsqrt_rn(r2));
+                    }
                 }
-                if (inside) {
-                    hit = true;
-                } else if (near) {
-                    double dx, dy, dz;
-                    sep(a, i, j, dx, dy, dz);
-                    const double r2 = norm2(dx, dy, dz);
-                    hit = lc2 > r2 || lc > __dsqrt_rn(r2);   // the root only near the cut
+                const unsigned bal = __ballot_sync(0xffffffffu, hit);
+                if (hit) {
+                    const int slot = cnt + __popc(bal & ((1u << lane) - 1u));
+                    if (slot < rowcap) my[slot] = j;
                 }
+                cnt += __popc(bal);
             }
-            const unsigned bal = __ballot_sync(0xffffffffu, hit);
-            if (hit) {
-                const int slot = cnt + __popc(bal & ((1u << lane) - 1u));
-                if (slot < rowcap) my[slot] = j;
-            }
-            cnt += __popc(bal);
         }
     }
     if (lane == 0) {
@@ -357,14 +393,16 @@ __global__ void k_pol_ref(int n, const double* __restrict__ x, const double* __r
 // The exact list from the skin list: each row's pairs within rcut, tested as k_pol_list does
 // (FP32 with margins, the reference's FP64 test in the shell around the cut), in the skin
 // list's order.
-__global__ void k_pol_filter(PolArgs a, const int* __restrict__ nn_s, const int* __restrict__ nbr_s, int cap_s,
-                             int* __restrict__ nn, int* __restrict__ nbr, const float4* __restrict__ xf, float r2f,
-                             float r2in, int* __restrict__ flag) {
+__global__ void k_pol_filter(PolArgs a, const int* __restrict__ nn_s, const int* __restrict__ nbr_s,
+                             const int* __restrict__ npol_s, int cap_s, int* __restrict__ nn, int* __restrict__ nbr,
+                             int* __restrict__ npol, const float4* __restrict__ xf, float r2f, float r2in,
+                             int* __restrict__ flag) {
     const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (i >= a.n) return;
     const float4 pi = xf[i];
-    const int m = nn_s[i];
+    const int m = nn_s[i], mp = npol_s[i];   // the skin row's polarizable partners come first
+    int cntp = 0;
     const int* src = nbr_s + (size_t)i * cap_s;
     int* my = nbr + (size_t)i * a.cap;
     const bool ortho = a.cl.imcon == 1 || a.cl.imcon == 2;
@@ -394,7 +432,7 @@ __global__ void k_pol_filter(PolArgs a, const int* __restrict__ nn_s, const int*
                 double dx, dy, dz;
                 sep(a, i, j, dx, dy, dz);
                 const double r2 = norm2(dx, dy, dz);
-                hit = a.rcsq > r2 || a.rcut > __dsqrt_rn(r2);
+                hit = a.rcsq > r2 || (r2 < a.rcsq * (1.0 + 1e-14) && a.rcut > __dsqrt_rn(r2));
             }
         }
         const unsigned bal = __ballot_sync(0xffffffffu, hit);
@@ -403,17 +441,26 @@ __global__ void k_pol_filter(PolArgs a, const int* __restrict__ nn_s, const int*
             if (slot < a.cap) my[slot] = j;
         }
         cnt += __popc(bal);
+        // hits among the skin row's first mp entries: the polarizable ones
+        const int lp = min(32, max(0, mp - b));
+        cntp += __popc(bal & (lp == 32 ? 0xffffffffu : ((1u << lp) - 1u)));
     }
     if (lane == 0) {
         nn[i] = min(cnt, a.cap);
+        npol[i] = min(cntp, a.cap);
         if (cnt > a.cap) atomicOr(flag, 1);
     }
 }
 
-// polr^(1/6) per site, once per call (the pair kernels multiply two of them).
+// polr^(1/6) per site and its reciprocal (n further), once per call (the pair kernels
+// multiply two of them).
 __global__ void k_pol_polr6(PolArgs a, double* __restrict__ out) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j < a.n) out[j] = pow(a.polr[j], 1.0 / 6.0);
+    if (j < a.n) {
+        const double p6 = pow(a.polr[j], 1.0 / 6.0);
+        out[j] = p6;
+        out[a.n + j] = 1.0 / p6;
+    }
 }
 
 // --- static real-space field and dipole tensors ---------------------------------------
@@ -424,29 +471,34 @@ __global__ void k_pol_static(PolArgs a) {
     const int nn = a.nn[i];
     const size_t row = (size_t)i * a.cap, blk = (size_t)a.n * a.cap;
     const bool poli = a.polr2[i] > 1e-6;
+    const int np = poli ? a.npol[i] : 0;   // tensors of the polarizable partners (the row's first np)
     double e[3] = {0, 0, 0};
     for (int k = lane; k < nn; k += 32) {
         const int j = a.nbr[row + k];
         double d[3];
         sep(a, i, j, d[0], d[1], d[2]);
         const double r2 = norm2(d[0], d[1], d[2]);
-        const double rr = __dsqrt_rn(r2);
+        // one reciprocal root gives r, 1/r^2, 1/r^3 and 1/r^5; the table index and the Thole
+        // arguments multiply by reciprocals (FP64 divisions are the costliest FP64-pipe
+        // operations of this kernel)
+        const double rri = rsqrt_nr(r2);
+        const double rr = r2 * rri;
         double t[6] = {0, 0, 0, 0, 0, 0};
         if (a.rcut > rr) {
             double bbb[4];
-            interp(a, rr, bbb);
-            const double rsqi = 1.0 / r2, r3i = 1.0 / (rr * rr * rr), r5i = r3i * rsqi;
-            const double bb = a.polr6[i] * a.polr6[j];
+            interp_r(a, rr, bbb);
+            const double rsqi = rri * rri, r3i = rsqi * rri, r5i = r3i * rsqi;
+            const double rob = rr * (a.rpolr6[i] * a.rpolr6[j]);   // r / bb
             const double qj = a.q[j];
             double eki = kR4pie0 * qj * (bbb[1] + r3i);
-            const double arq = a.ascd * pow4(rr / bb);
+            const double arq = a.ascd * pow4(rob);
             const double dum1 = arq < kDampCut ? exp(-arq) : 0.0;
             eki = eki - kR4pie0 * qj * dum1 * r3i;
             e[0] += eki * d[0];
             e[1] += eki * d[1];
             e[2] += eki * d[2];
-            if (poli && a.polr2[j] > 1e-6) {
-                const double arob4 = a.athole * pow4(rr / bb);
+            if (k < np) {
+                const double arob4 = a.athole * pow4(rob);
                 const double h1 = arob4 < kDampCut ? exp(-arob4) : 0.0;
                 const double h2 = (1.0 + (4.0 / 3.0) * arob4) * h1;
                 const int ia[6] = {0, 0, 0, 1, 1, 2}, ib[6] = {0, 1, 2, 1, 2, 2};
@@ -463,10 +515,12 @@ __global__ void k_pol_static(PolArgs a) {
                 }
             }
         }
+        if (k < np) {
 #pragma unroll
-        for (int p = 0; p < 6; ++p) a.tens[p * blk + row + k] = t[p];
-        if (a.tens32)
-            for (int p = 0; p < 6; ++p) a.tens32[p * blk + row + k] = (float)t[p];
+            for (int p = 0; p < 6; ++p) a.tens[p * blk + row + k] = t[p];
+            if (a.tens32)
+                for (int p = 0; p < 6; ++p) a.tens32[p * blk + row + k] = (float)t[p];
+        }
     }
     for (int c = 0; c < 3; ++c) e[c] = warp_sum(e[c]);
     if (lane == 0) {
@@ -516,6 +570,7 @@ __global__ void k_pol_intra_static(PolArgs a) {
                 }
             }
             for (int q = 0; q < 6; ++q) T[6 * p + q] = t[q];
+            for (int q = 0; q < 6; ++q) a.intra32[18 * (size_t)w + 6 * p + q] = (float)t[q];
         }
     }
 }
@@ -527,7 +582,7 @@ __global__ void k_pol_dd(PolArgs a) {
     if (i >= a.n) return;
     double e[3] = {0, 0, 0};
     if (a.polr2[i] > 1e-6) {
-        const int nn = a.nn[i];
+        const int nn = a.npol[i];   // the other partners carry no dipole
         const size_t row = (size_t)i * a.cap, blk = (size_t)a.n * a.cap;
         for (int k = lane; k < nn; k += 32) {
             const int j = a.nbr[row + k];
@@ -947,7 +1002,7 @@ __global__ void k_pol_dd32(PolArgs a, const float4* __restrict__ in, float* __re
     if (i >= a.n) return;
     float e[3] = {0, 0, 0};
     if (a.polr2[i] > 1e-6) {
-        const int nn = a.nn[i];
+        const int nn = a.npol[i];   // the other partners carry no dipole
         const size_t row = (size_t)i * a.cap, blk = (size_t)a.n * a.cap;
         for (int k = lane; k < nn; k += 32) {
             const float4 d = in[a.nbr[row + k]];
@@ -963,13 +1018,14 @@ __global__ void k_pol_dd32(PolArgs a, const float4* __restrict__ in, float* __re
             const int w = i / 3, s = i % 3;
             const int pj[3][2] = {{1, 2}, {0, 2}, {0, 1}};
             const int pp[3][2] = {{0, 1}, {0, 2}, {1, 2}};
-            const double* T = a.intra + 18 * (size_t)w;
+            // the FP32 copy: FP64 loads and conversions would occupy the FP64 pipe (1/64 rate)
+            const float* T = a.intra32 + 18 * (size_t)w;
             for (int u = 0; u < 2; ++u) {
                 const float4 d = in[3 * w + pj[s][u]];
-                const double* t = T + 6 * pp[s][u];
-                e[0] += (float)t[0] * d.x + (float)t[1] * d.y + (float)t[2] * d.z;
-                e[1] += (float)t[1] * d.x + (float)t[3] * d.y + (float)t[4] * d.z;
-                e[2] += (float)t[2] * d.x + (float)t[4] * d.y + (float)t[5] * d.z;
+                const float* t = T + 6 * pp[s][u];
+                e[0] += t[0] * d.x + t[1] * d.y + t[2] * d.z;
+                e[1] += t[1] * d.x + t[3] * d.y + t[4] * d.z;
+                e[2] += t[2] * d.x + t[4] * d.y + t[5] * d.z;
             }
         }
     }
@@ -1706,11 +1762,49 @@ __global__ void __launch_bounds__(kThreads) k_pol_ewald2p(PolArgs a, double g34,
 // functions from the FP32 table of C_n = B_n + (2n-1)!!/r^(2n+1), free of the cancellation
 // between B_n and the bare 1/r^(2n+1)); separation, cut test and heat entries FP64; every
 // sum FP64.
-__global__ void __launch_bounds__(kThreads) k_pol_ewald2p32(PolArgs a, double g34d, int heat) {
+// The pairs of a row whose smeared charge-charge term is not negligible (ascc (r/bb)^4 below
+// kDampCut: about 1 in 20 listed pairs, within ~3.5 A) need an FP64 gammq, pow and exp,
+// several hundred FP64-pipe instructions.  Taken in the pair loop, a warp ran them for
+// whichever of its lanes had such a pair, and most warp steps had one.  They are queued
+// instead (32 per warp) and evaluated with every lane active when the queue fills and at
+// the end of the row.
+struct SmearQueue {
+    int j[32];
+    double r[32];
+};
+
+__device__ __forceinline__ void smear_flush(const PolArgs& a, int i, const SmearQueue& q, int cnt, int lane,
+                                            double gln, double g34d, double qid, double& eng, double& aei,
+                                            double& vsp) {
+    if (lane >= cnt) return;
+    const int j = q.j[lane];
+    const double rrd = q.r[lane];
+    const double arob4d = a.ascc * pow4(rrd * (a.rpolr6[i] * a.rpolr6[j]));
+    const double dum1d = exp(-arob4d);
+    const double gq = gammq_g(0.75, arob4d, gln);
+    const double sm = (dum1d - pow(arob4d, 0.25) * g34d * gq) / rrd * kR4pie0;
+    const double qjd = a.q[j];
+    const double cicjd = qid * qjd;
+    if (j > i) eng -= cicjd * sm;
+    aei -= cicjd * 0.5 * sm;
+    vsp -= qjd * sm;
+}
+
+// The mixed path's ewald2p: the same terms as k_pol_ewald2p.  The pair energies stay FP64
+// (the screened 1/r interpolated from the FP64 table, the smeared charge-charge term with
+// the FP64 gammq: the per-site energies feed jkin, whose budget FP32 pair energies would
+// exceed); the forces, the potentials and the dipole terms are FP32 per pair (the B
+// functions from the FP32 table of C_n = B_n + (2n-1)!!/r^(2n+1), free of the cancellation
+// between B_n and the bare 1/r^(2n+1)); separation, cut test and heat entries FP64; every
+// sum FP64.
+__global__ void __launch_bounds__(kThreads) k_pol_ewald2p32(PolArgs a, double g34d, double gln, int heat) {
+    __shared__ SmearQueue sq[kThreads / 32];
     const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     double red[11] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};   // eng, vir, stress(6), jpot(3)
     if (i < a.n) {
+        SmearQueue& q = sq[threadIdx.x >> 5];
+        int qn = 0;   // queued pairs (warp-uniform)
         const int nn = a.nn[i];
         const size_t row = (size_t)i * a.cap;
         const float r4 = (float)kR4pie0;
@@ -1721,132 +1815,152 @@ __global__ void __launch_bounds__(kThreads) k_pol_ewald2p32(PolArgs a, double g3
         const float p6i = (float)a.polr6[i];
         const float ascc = (float)a.ascc, ascd = (float)a.ascd, athole = (float)a.athole;
         const float rdw = (float)(1.0 / a.drewd);
-        double f[3] = {0, 0, 0}, aei = 0, vsp = 0;
-        for (int k = lane; k < nn; k += 32) {
-            const int j = a.nbr[row + k];
-            double dd[3];
-            sep(a, i, j, dd[0], dd[1], dd[2]);
-            const double rsqd = norm2(dd[0], dd[1], dd[2]);
-            if (!(a.rcsq > rsqd)) continue;
-            const float d[3] = {(float)dd[0], (float)dd[1], (float)dd[2]};
-            const float rsq = (float)rsqd;
-            const float rrr = sqrtf(rsq);
-            // 3-point interpolation of the C_n table (erfcgenp's grid)
-            float bbb[4];
-            {
-                const float u = rrr * rdw;
-                const int ll = (int)u;
-                const float ppp = u - (float)ll;
-                const float4 v0 = a.ercp32[ll], v1 = a.ercp32[ll + 1], v2 = a.ercp32[ll + 2];
-                const float vk[4] = {v0.x, v0.y, v0.z, v0.w}, vk1[4] = {v1.x, v1.y, v1.z, v1.w},
-                            vk2[4] = {v2.x, v2.y, v2.z, v2.w};
+        const double rdwd = a.rdrewd;
+        double f[3] = {0, 0, 0}, aei = 0, vsp = 0, engq = 0;
+        for (int b = 0; b < nn; b += 32) {
+            const int k = b + lane;
+            bool smear = false;
+            int j = 0;
+            double rrd = 0.0;
+            if (k < nn) {
+                j = a.nbr[row + k];
+                double dd[3];
+                sep(a, i, j, dd[0], dd[1], dd[2]);
+                const double rsqd = norm2(dd[0], dd[1], dd[2]);
+                if (a.rcsq > rsqd) {
+                    const float d[3] = {(float)dd[0], (float)dd[1], (float)dd[2]};
+                    const float rsq = (float)rsqd;
+                    const float rrr = sqrtf(rsq);
+                    // 3-point interpolation of the C_n table (erfcgenp's grid)
+                    float bbb[4];
+                    {
+                        const float u = rrr * rdw;
+                        const int ll = (int)u;
+                        const float ppp = u - (float)ll;
+                        const float4 v0 = a.ercp32[ll], v1 = a.ercp32[ll + 1], v2 = a.ercp32[ll + 2];
+                        const float vk[4] = {v0.x, v0.y, v0.z, v0.w}, vk1[4] = {v1.x, v1.y, v1.z, v1.w},
+                                    vk2[4] = {v2.x, v2.y, v2.z, v2.w};
 #pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    const float t1 = vk[q] + (vk1[q] - vk[q]) * ppp;
-                    const float t2 = vk1[q] + (vk2[q] - vk1[q]) * (ppp - 1.f);
-                    bbb[q] = t1 + (t2 - t1) * ppp * 0.5f;
+                        for (int qq = 0; qq < 4; ++qq) {
+                            const float t1 = vk[qq] + (vk1[qq] - vk[qq]) * ppp;
+                            const float t2 = vk1[qq] + (vk2[qq] - vk1[qq]) * (ppp - 1.f);
+                            bbb[qq] = t1 + (t2 - t1) * ppp * 0.5f;
+                        }
+                    }
+                    const float rri = 1.f / rrr, rsqi = 1.f / rsq, r3i = rri * rsqi, r5i = r3i * rsqi;
+                    const double qjd = a.q[j];
+                    const float qj = (float)qjd;
+                    const float cicj = qi * qj;
+                    // FP64 energy: the screened 1/r (bbb[0] + 1/r of the FP64 table); the
+                    // smeared term is queued
+                    const double rrid = rsqrt_nr(rsqd);
+                    rrd = rsqd * rrid;
+                    double c0;
+                    {
+                        const double u = rrd * rdwd;
+                        const int ll = (int)u;
+                        const double ppp = u - double(ll);
+                        const double v0 = a.ercp[ll].x, v1 = a.ercp[ll + 1].x, v2 = a.ercp[ll + 2].x;
+                        const double t1 = v0 + (v1 - v0) * ppp;
+                        const double t2 = v1 + (v2 - v1) * (ppp - 1.0);
+                        c0 = t1 + (t2 - t1) * ppp * 0.5 + rrid;
+                    }
+                    const double cicjd = qid * qjd;
+                    const double edum = cicjd * c0 * kR4pie0;
+                    // bbb[1] = the screened 1/r^3 (C_1), bbb[2] = C_2, bbb[3] = C_3
+                    const float espdum = bbb[0] * r4;
+                    float ffac = cicj * bbb[1] * r4;
+                    const float bb = p6i * (float)a.polr6[j];
+                    const float rb = rrr / bb, rb2 = rb * rb, rb4 = rb2 * rb2;
+                    {
+                        const float arob4 = ascc * rb4;
+                        if (arob4 < (float)kDampCut) {
+                            smear = true;
+                            ffac = ffac - cicj * r3i * expf(-arob4) * r4;
+                        }
+                    }
+                    const float mj[3] = {(float)a.mx[j], (float)a.my[j], (float)a.mz[j]};
+                    const float rdmui = mi[0] * d[0] + mi[1] * d[1] + mi[2] * d[2];
+                    const float rdmuj = mj[0] * d[0] + mj[1] * d[1] + mj[2] * d[2];
+                    const float x0 = qj * rdmui - qi * rdmuj;
+                    const float facmu0 = x0 * (-3.f) * r5i * r4;
+                    const float facmui0 = r3i * qj * r4;
+                    const float facmuj0 = -r3i * qi * r4;
+                    // facmu0 - x0 B_2 = -x0 C_2; facmui0 + B_1 qj = C_1 qj
+                    float facmu = -x0 * bbb[2] * r4;
+                    float dfi = bbb[1] * qj * r4;
+                    float dfj = -bbb[1] * qi * r4;
+                    float espdc = bbb[1] * r4;
+                    {
+                        const float arob4 = ascd * rb4;
+                        const float dum1 = arob4 < (float)kDampCut ? expf(-arob4) : 0.f;
+                        const float dum2 = (1.f + (4.f / 3.f) * arob4) * dum1;
+                        facmu = facmu - facmu0 * dum2;
+                        dfi = dfi - facmui0 * dum1;
+                        dfj = dfj - facmuj0 * dum1;
+                        espdc = espdc - r3i * dum1 * r4;
+                    }
+                    if (poli && a.polr2[j] > 1e-6) {
+                        const float dpidpj = mi[0] * mj[0] + mi[1] * mj[1] + mi[2] * mj[2];
+                        // (3 dpidpj - 15 rdmui rdmuj / r^2) r5i + B_2 dpidpj - B_3 rdmui rdmuj = C_2 dpidpj - C_3 rdmui rdmuj
+                        facmu = facmu + (bbb[2] * dpidpj - bbb[3] * rdmui * rdmuj) * r4;
+                        dfi = dfi + bbb[2] * rdmuj * r4;
+                        dfj = dfj + bbb[2] * rdmui * r4;
+                        const float facmu1 = -15.f * rdmui * rdmuj * rsqi * r5i * r4;
+                        const float facmu2 = 3.f * dpidpj * r5i * r4;
+                        const float dfi1 = 3.f * rdmuj * r5i * r4;
+                        const float dfj1 = 3.f * rdmui * r5i * r4;
+                        const float bb2 = bb * bb, bb4 = bb2 * bb2;
+                        const float arob4 = athole * rb4;
+                        const float dum1 = arob4 < (float)kDampCut ? expf(-arob4) : 0.f;
+                        const float dum2 = (1.f + (4.f / 3.f) * arob4) * dum1;
+                        const float dum3 = 4.f * athole * (4.f * arob4 - 1.f) * dum1 * rsqi / bb4;
+                        const float dum4 = 4.f * athole * dum1 * rrr / bb4;
+                        facmu = facmu - facmu1 * dum2 - facmu2 * dum1 + rdmui * rdmuj * dum3 * rri * r4 -
+                                dpidpj * rsqi * dum4 * r4;
+                        dfi = dfi - dfi1 * dum2;
+                        dfj = dfj - dfj1 * dum2;
+                    }
+                    const float dfx = dfi * mi[0] + dfj * mj[0];
+                    const float dfy = dfi * mi[1] + dfj * mj[1];
+                    const float dfz = dfi * mi[2] + dfj * mj[2];
+                    ffac = ffac + facmu;
+                    const double fx = (double)(ffac * d[0] + dfx), fy = (double)(ffac * d[1] + dfy),
+                                 fz = (double)(ffac * d[2] + dfz);
+                    f[0] += fx; f[1] += fy; f[2] += fz;
+                    aei += 0.5 * edum;
+                    vsp += (double)(qj * espdum + rdmuj * espdc);
+                    if (heat) heat_entry(a, i, j, fx, fy, fz, red + 8);
+                    if (j > i) {
+                        const double virdum = (double)(dfx * d[0] + dfy * d[1] + dfz * d[2]);
+                        red[0] += edum;
+                        red[1] += -(double)ffac * rsqd - virdum;
+                        red[2] += dd[0] * fx; red[3] += dd[0] * fy; red[4] += dd[0] * fz;
+                        red[5] += dd[1] * fy; red[6] += dd[1] * fz; red[7] += dd[2] * fz;
+                    }
                 }
             }
-            const float rri = 1.f / rrr, rsqi = 1.f / rsq, r3i = rri * rsqi, r5i = r3i * rsqi;
-            const double qjd = a.q[j];
-            const float qj = (float)qjd;
-            const float cicj = qi * qj;
-            // FP64 energy: the screened 1/r (bbb[0] + 1/r of the FP64 table) and the smeared term
-            const double rrd = __dsqrt_rn(rsqd);
-            double c0;
-            {
-                const double u = rrd / a.drewd;
-                const int ll = (int)u;
-                const double ppp = u - double(ll);
-                const double v0 = a.ercp[ll].x, v1 = a.ercp[ll + 1].x, v2 = a.ercp[ll + 2].x;
-                const double t1 = v0 + (v1 - v0) * ppp;
-                const double t2 = v1 + (v2 - v1) * (ppp - 1.0);
-                c0 = t1 + (t2 - t1) * ppp * 0.5 + 1.0 / rrd;
-            }
-            const double cicjd = qid * qjd;
-            const double edum = cicjd * c0 * kR4pie0;
-            double eng = edum;
-            double aeh = 0.5 * edum;
-            // bbb[1] = the screened 1/r^3 (C_1), bbb[2] = C_2, bbb[3] = C_3
-            float espdum = bbb[0] * r4;
-            float ffac = cicj * bbb[1] * r4;
-            const float bb = p6i * (float)a.polr6[j];
-            const float rb = rrr / bb, rb2 = rb * rb, rb4 = rb2 * rb2;
-            {
-                const float arob4 = ascc * rb4;
-                if (arob4 < (float)kDampCut) {
-                    const float dum1 = expf(-arob4);
-                    const double bbd = a.polr6[i] * a.polr6[j];
-                    const double arob4d = a.ascc * pow4(rrd / bbd);
-                    const double dum1d = exp(-arob4d);
-                    const double gq = gammq(0.75, arob4d);
-                    const double sm = (dum1d - pow(arob4d, 0.25) * g34d * gq) / rrd * kR4pie0;
-                    eng -= cicjd * sm;
-                    aeh -= cicjd * 0.5 * (dum1d - pow(arob4d, 0.25) * g34d * gq) / rrd * kR4pie0;
-                    espdum -= (float)sm;
-                    ffac = ffac - cicj * r3i * dum1 * r4;
+            // queue this step's smeared pairs; flush a full queue first
+            const unsigned sb = __ballot_sync(0xffffffffu, smear);
+            if (sb) {
+                const int cnt = __popc(sb);
+                if (qn + cnt > 32) {
+                    __syncwarp();
+                    smear_flush(a, i, q, qn, lane, gln, g34d, qid, engq, aei, vsp);
+                    qn = 0;
+                    __syncwarp();
                 }
-            }
-            const float mj[3] = {(float)a.mx[j], (float)a.my[j], (float)a.mz[j]};
-            const float rdmui = mi[0] * d[0] + mi[1] * d[1] + mi[2] * d[2];
-            const float rdmuj = mj[0] * d[0] + mj[1] * d[1] + mj[2] * d[2];
-            const float x0 = qj * rdmui - qi * rdmuj;
-            const float facmu0 = x0 * (-3.f) * r5i * r4;
-            const float facmui0 = r3i * qj * r4;
-            const float facmuj0 = -r3i * qi * r4;
-            // facmu0 - x0 B_2 = -x0 C_2; facmui0 + B_1 qj = C_1 qj
-            float facmu = -x0 * bbb[2] * r4;
-            float dfi = bbb[1] * qj * r4;
-            float dfj = -bbb[1] * qi * r4;
-            float espdc = bbb[1] * r4;
-            {
-                const float arob4 = ascd * rb4;
-                const float dum1 = arob4 < (float)kDampCut ? expf(-arob4) : 0.f;
-                const float dum2 = (1.f + (4.f / 3.f) * arob4) * dum1;
-                facmu = facmu - facmu0 * dum2;
-                dfi = dfi - facmui0 * dum1;
-                dfj = dfj - facmuj0 * dum1;
-                espdc = espdc - r3i * dum1 * r4;
-            }
-            if (poli && a.polr2[j] > 1e-6) {
-                const float dpidpj = mi[0] * mj[0] + mi[1] * mj[1] + mi[2] * mj[2];
-                // (3 dpidpj - 15 rdmui rdmuj / r^2) r5i + B_2 dpidpj - B_3 rdmui rdmuj = C_2 dpidpj - C_3 rdmui rdmuj
-                facmu = facmu + (bbb[2] * dpidpj - bbb[3] * rdmui * rdmuj) * r4;
-                dfi = dfi + bbb[2] * rdmuj * r4;
-                dfj = dfj + bbb[2] * rdmui * r4;
-                const float facmu1 = -15.f * rdmui * rdmuj * rsqi * r5i * r4;
-                const float facmu2 = 3.f * dpidpj * r5i * r4;
-                const float dfi1 = 3.f * rdmuj * r5i * r4;
-                const float dfj1 = 3.f * rdmui * r5i * r4;
-                const float bb2 = bb * bb, bb4 = bb2 * bb2;
-                const float arob4 = athole * rb4;
-                const float dum1 = arob4 < (float)kDampCut ? expf(-arob4) : 0.f;
-                const float dum2 = (1.f + (4.f / 3.f) * arob4) * dum1;
-                const float dum3 = 4.f * athole * (4.f * arob4 - 1.f) * dum1 * rsqi / bb4;
-                const float dum4 = 4.f * athole * dum1 * rrr / bb4;
-                facmu = facmu - facmu1 * dum2 - facmu2 * dum1 + rdmui * rdmuj * dum3 * rri * r4 -
-                        dpidpj * rsqi * dum4 * r4;
-                dfi = dfi - dfi1 * dum2;
-                dfj = dfj - dfj1 * dum2;
-            }
-            const float dfx = dfi * mi[0] + dfj * mj[0];
-            const float dfy = dfi * mi[1] + dfj * mj[1];
-            const float dfz = dfi * mi[2] + dfj * mj[2];
-            ffac = ffac + facmu;
-            const double fx = (double)(ffac * d[0] + dfx), fy = (double)(ffac * d[1] + dfy),
-                         fz = (double)(ffac * d[2] + dfz);
-            f[0] += fx; f[1] += fy; f[2] += fz;
-            aei += aeh;
-            vsp += (double)(qj * espdum + rdmuj * espdc);
-            if (heat) heat_entry(a, i, j, fx, fy, fz, red + 8);
-            if (j > i) {
-                const double virdum = (double)(dfx * d[0] + dfy * d[1] + dfz * d[2]);
-                red[0] += eng;
-                red[1] += -(double)ffac * rsqd - virdum;
-                red[2] += dd[0] * fx; red[3] += dd[0] * fy; red[4] += dd[0] * fz;
-                red[5] += dd[1] * fy; red[6] += dd[1] * fz; red[7] += dd[2] * fz;
+                if (smear) {
+                    const int slot = qn + __popc(sb & ((1u << lane) - 1u));
+                    q.j[slot] = j;
+                    q.r[slot] = rrd;
+                }
+                qn += cnt;
             }
         }
+        __syncwarp();
+        if (qn) smear_flush(a, i, q, qn, lane, gln, g34d, qid, engq, aei, vsp);
+        red[0] += engq;
         for (int c = 0; c < 3; ++c) f[c] = warp_sum(f[c]);
         aei = warp_sum(aei);
         vsp = warp_sum(vsp);
@@ -2142,7 +2256,7 @@ cudaError_t launch_msite_redistribute(int nw, double gamma, double* fx, double* 
 }
 
 void PolarState::release() {
-    void* p[] = {ercp, ercp32, nn_s, nbr_s, xref, nn, nbr, flag, xf, tens, intra, fld, vesp, ae, eik, kv, kx2, lmn, sf, kterm, acc, kco, fac, md, vh, polr6,
+    void* p[] = {ercp, ercp32, nn_s, nbr_s, npol_s, xref, nn, nbr, npol, flag, xf, tens, intra, fld, vesp, ae, eik, kv, kx2, lmn, sf, kterm, acc, kco, fac, md, vh, polr6,
                  ckey, cskey, cidx, csidx, csort, cstart, cend,
                  tens32, r32, d32, e32, kco32, fac32, ktile, kaux, kcol, colk, kpart, cg_x, cg_r, cg_q, cg_z, vh32};
     for (void* q : p)
@@ -2161,11 +2275,11 @@ void PolarState::release() {
             }
     ercp = nullptr;
     ercp32 = nullptr;
-    nn_s = nbr_s = nullptr;
+    nn_s = nbr_s = npol_s = nullptr;
     xref = nullptr;
     ns_cap = cap_s_alloc = 0;
     skin_ok = false;
-    nn = nbr = flag = nullptr;
+    nn = nbr = flag = npol = nullptr;
     xf = nullptr;
     tens = intra = fld = vesp = ae = sf = kterm = acc = kco = vh = polr6 = nullptr;
     ckey = cskey = nullptr;
@@ -2281,15 +2395,16 @@ cudaError_t PolarState::reserve_cells(int n, int ncell) {
 cudaError_t PolarState::reserve_skin(int n) {
     cudaError_t e;
     if (n > ns_cap || cap_s != cap_s_alloc) {
-        void* p[] = {nn_s, nbr_s, xref};
+        void* p[] = {nn_s, nbr_s, npol_s, xref};
         for (void* q : p)
             if (q) cudaFree(q);
-        nn_s = nbr_s = nullptr;
+        nn_s = nbr_s = npol_s = nullptr;
         xref = nullptr;
         ns_cap = cap_s_alloc = 0;
         skin_ok = false;
         const size_t m = (size_t)std::max(n, 1);
         if ((e = cudaMalloc(&nn_s, m * sizeof(int)))) return e;
+        if ((e = cudaMalloc(&npol_s, m * sizeof(int)))) return e;
         if ((e = cudaMalloc(&nbr_s, m * cap_s * sizeof(int)))) return e;
         if ((e = cudaMalloc(&xref, 3 * m * sizeof(double)))) return e;
         ns_cap = n;
@@ -2370,17 +2485,18 @@ cudaError_t PolarState::reserve(int nw, int K, size_t nfac) {
     // a capacity is zeroed before its buffers are replaced, so a failed allocation leaves
     // nothing that a later call would take for allocated
     if (n > n_cap || cap != cap_alloc) {
-        void* p[] = {nn, nbr, xf, tens, fld, vesp, ae, md, vh, polr6};
+        void* p[] = {nn, nbr, npol, xf, tens, fld, vesp, ae, md, vh, polr6};
         for (void* q : p)
             if (q) cudaFree(q);
         n_cap = 0;
         cap_alloc = 0;
-        nn = nbr = nullptr;
+        nn = nbr = npol = nullptr;
         xf = nullptr;
         tens = fld = vesp = ae = vh = polr6 = nullptr;
         md = nullptr;
         const size_t m = (size_t)std::max(n, 1);
         if ((e = cudaMalloc(&nn, m * sizeof(int)))) return e;
+        if ((e = cudaMalloc(&npol, m * sizeof(int)))) return e;
         if ((e = cudaMalloc(&nbr, m * cap * sizeof(int)))) return e;
         if ((e = cudaMalloc(&xf, m * sizeof(float4)))) return e;
         if ((e = cudaMalloc(&tens, 6 * m * cap * sizeof(double)))) return e;
@@ -2389,7 +2505,7 @@ cudaError_t PolarState::reserve(int nw, int K, size_t nfac) {
         if ((e = cudaMalloc(&ae, m * sizeof(double)))) return e;
         if ((e = cudaMalloc(&md, m * sizeof(double4)))) return e;
         if ((e = cudaMalloc(&vh, 12 * m * sizeof(double)))) return e;
-        if ((e = cudaMalloc(&polr6, m * sizeof(double)))) return e;
+        if ((e = cudaMalloc(&polr6, 2 * m * sizeof(double)))) return e;
         n_cap = n;
         cap_alloc = cap;
     }
@@ -2397,7 +2513,8 @@ cudaError_t PolarState::reserve(int nw, int K, size_t nfac) {
         if (intra) cudaFree(intra);
         intra = nullptr;
         nw_cap = 0;
-        if ((e = cudaMalloc(&intra, 18 * (size_t)std::max(nw, 1) * sizeof(double)))) return e;
+        // FP64 tensors, then their FP32 copy
+        if ((e = cudaMalloc(&intra, 18 * (size_t)std::max(nw, 1) * (sizeof(double) + sizeof(float))))) return e;
         nw_cap = nw;
     }
     if (K > k_cap) {
@@ -2615,11 +2732,14 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
         b.ercp = ercp;
         b.ercp32 = ercp32;
         b.drewd = drewd;
+        b.rdrewd = 1.0 / drewd;
         b.nn = nn;
         b.nbr = nbr;
+        b.npol = npol;
         b.tens = tens;
         b.tens32 = mixed ? tens32 : nullptr;
         b.intra = intra;
+        b.intra32 = reinterpret_cast<float*>(intra + 18 * (size_t)std::max(nw, 1));
         b.efk = fld;
         b.efc = fld + 3 * (size_t)n;
         b.emu = fld + 6 * (size_t)n;
@@ -2627,6 +2747,7 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
         b.vesp = vesp;
         b.ae = ae;
         b.polr6 = polr6;
+        b.rpolr6 = polr6 + n;
         b.acc = acc;
     };
     a.cl = cl;
@@ -2696,7 +2817,7 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
     last_n = n;
     const float r2f = (float)((rcut + 0.01) * (rcut + 0.01));
     const float r2in = rcut > 0.02 ? (float)((rcut - 0.01) * (rcut - 0.01)) : 0.f;
-    auto build = [&](int* lnn, int* lnbr, int rowcap, double lcut) -> cudaError_t {
+    auto build = [&](int* lnn, int* lnbr, int* lnpol, int rowcap, double lcut) -> cudaError_t {
         // one pass of k_pol_list at cut lcut into (lnn, lnbr); the overflow flag is read by the caller
         cudaError_t err;
         int3 nc = make_int3(1, 1, 1);
@@ -2719,8 +2840,8 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
         }
         const float lf = (float)((lcut + 0.01) * (lcut + 0.01));
         const float li = lcut > 0.02 ? (float)((lcut - 0.01) * (lcut - 0.01)) : 0.f;
-        k_pol_list<<<blocks(32L * n, kThreads), kThreads, 0, s>>>(a, lnn, lnbr, rowcap, lcut, xf, lf, li, flag, nc,
-                                                                   cells, csidx, cstart, cend);
+        k_pol_list<<<blocks(32L * n, kThreads), kThreads, 0, s>>>(a, lnn, lnbr, lnpol, rowcap, lcut, xf, lf, li,
+                                                                   flag, nc, cells, csidx, cstart, cend);
         ++launches;
         return cudaGetLastError();
     };
@@ -2745,8 +2866,8 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
                 if ((e = cudaMemsetAsync(flag, 0, 2 * sizeof(int), s))) return e;
                 k_pol_moved<<<blocks(n, kThreads), kThreads, 0, s>>>(n, x, y, z, xref, cl, 0.25 * skin * skin,
                                                                      flag + 1);
-                k_pol_filter<<<blocks(32L * n, kThreads), kThreads, 0, s>>>(a, nn_s, nbr_s, cap_s, nn, nbr, xf, r2f,
-                                                                            r2in, flag);
+                k_pol_filter<<<blocks(32L * n, kThreads), kThreads, 0, s>>>(a, nn_s, nbr_s, npol_s, cap_s, nn, nbr,
+                                                                            npol, xf, r2f, r2in, flag);
                 launches += 2;
                 int fh[2];
                 if ((e = read_flags(fh))) return e;
@@ -2768,7 +2889,7 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
             for (;;) {
                 if ((e = cudaMemsetAsync(flag, 0, 2 * sizeof(int), s))) return e;
                 bind(a);
-                if ((e = build(nn_s, nbr_s, cap_s, rcut + skin))) return e;
+                if ((e = build(nn_s, nbr_s, npol_s, cap_s, rcut + skin))) return e;
                 int fh[2];
                 if ((e = read_flags(fh))) return e;
                 if (!fh[0]) break;
@@ -2791,7 +2912,7 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
         for (;;) {
             bind(a);
             if ((e = cudaMemsetAsync(flag, 0, 2 * sizeof(int), s))) return e;
-            if ((e = build(nn, nbr, cap, rcut))) return e;
+            if ((e = build(nn, nbr, npol, cap, rcut))) return e;
             int fh[2];
             if ((e = read_flags(fh))) return e;
             if (!fh[0]) break;
@@ -2817,6 +2938,10 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
             Kg[c] = spme_grid[0] > 0 ? spme_grid[c] : spme_smooth_even(wc[c] / spme_spacing);
         for (int c = 0; c < 3; ++c) spme_K_last[c] = Kg[c];
         if ((e = spme.prepare(cl.c, alpha, spme_order, Kg, mixed, heat ? 9 : 1, s))) return e;
+        if (mixed) {   // the FP32 passes' site frame for this call's positions
+            if ((e = spme.frame32(n, x, y, z, s))) return e;
+            ++launches;
+        }
     }
     if (K) {
         k_pol_factors<<<blocks(n, kThreads), kThreads, 0, s>>>(k, x, y, z);
@@ -3112,7 +3237,7 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
     }
     k_pol_kforce_sum<<<sblk1, kThreads, 0, s>>>(k, a, spme_on ? 1 : (mixed ? nc1 : nc2), kpart);
     if (mixed && !ewald2p_fp64)
-        k_pol_ewald2p32<<<blocks(32L * n, kThreads), kThreads, 0, s>>>(a, g34, heat);
+        k_pol_ewald2p32<<<blocks(32L * n, kThreads), kThreads, 0, s>>>(a, g34, gammln(0.75), heat);
     else
         k_pol_ewald2p<<<blocks(32L * n, kThreads), kThreads, 0, s>>>(a, g34, heat);
     k_pol_ewald3p<<<blocks(nw, kThreads), kThreads, 0, s>>>(a, heat);

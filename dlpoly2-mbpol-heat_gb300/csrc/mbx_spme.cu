@@ -28,6 +28,7 @@ namespace {
 
 constexpr double kPiS = 3.141592653589793;
 constexpr int kFftThreads = 256;
+constexpr int kFftPlaneThreads = 512;
 constexpr int kSpThreads = 128;
 constexpr int kKtThreads = 256;
 constexpr int kMaxGrid = 1024;     // points per axis
@@ -267,6 +268,11 @@ struct SpArgs {
     double rc[9];    // s_a = rc[a] x + rc[a + 3] y + rc[a + 6] z
     double jac[9];   // dt_a / dr_c = K_a rc[a + 3c] at [3a + c]
     const int* stop; // FP32 CG sweeps: nonzero = the solve has stopped, return at once
+    // FP32 kernels: the per-call site frame (base grid index and fractional part per axis,
+    // from the FP64 positions once per call) and the Jacobian in FP32
+    const int4* sib;
+    const float4* sw;
+    float jac32[9];
 };
 
 // M_p(w + j), j = 0..p-1, for w in [0, 1) (bspgen's values bspx(i, j + 1)), and with
@@ -319,6 +325,47 @@ __device__ __forceinline__ void site_splines(const SpArgs& s, double x, double y
             gi[a][j] = g < 0 ? g + Ka[a] : g;
         }
         bspline<T, P, ND>((T)(t - fl), th[a], d1[a], d2[a]);
+    }
+}
+
+// The site frame of the FP32 passes, once per call: floor(t_a) mod K_a and t_a - floor(t_a)
+// (FP64, rounded to FP32: 6e-8 absolute in the fraction) for every site.
+__global__ void k_spme_frame(SpArgs s, const double* __restrict__ x, const double* __restrict__ y,
+                             const double* __restrict__ z, int4* __restrict__ sib, float4* __restrict__ sw) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= s.n) return;
+    const int Ka[3] = {s.K1, s.K2, s.K3};
+    int ib[3];
+    float w[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const double t = (double)Ka[a] * (s.rc[a] * x[j] + s.rc[a + 3] * y[j] + s.rc[a + 6] * z[j] + 0.5);
+        const double fl = floor(t);
+        long long b = (long long)fl % Ka[a];
+        if (b < 0) b += Ka[a];
+        ib[a] = (int)b;
+        w[a] = (float)(t - fl);
+    }
+    sib[j] = make_int4(ib[0], ib[1], ib[2], 0);
+    sw[j] = make_float4(w[0], w[1], w[2], 0.f);
+}
+
+// site_splines of the FP32 passes from the site frame (no FP64 arithmetic per lane)
+template <int P, int ND>
+__device__ __forceinline__ void site_splines32(const SpArgs& s, int j, int (&gi)[3][P], float (&th)[3][P],
+                                               float (&d1)[3][P], float (&d2)[3][P]) {
+    const int4 ib = s.sib[j];
+    const float4 w = s.sw[j];
+    const int Ka[3] = {s.K1, s.K2, s.K3}, b[3] = {ib.x, ib.y, ib.z};
+    const float wa[3] = {w.x, w.y, w.z};
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+#pragma unroll
+        for (int q = 0; q < P; ++q) {
+            const int g = b[a] - q;
+            gi[a][q] = g < 0 ? g + Ka[a] : g;
+        }
+        bspline<float, P, ND>(wa[a], th[a], d1[a], d2[a]);
     }
 }
 
@@ -383,13 +430,22 @@ __global__ void __launch_bounds__(kSpThreads) k_spme_spread(SpArgs s, const doub
     const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
     const int j = (int)(t / kLanes), jz = (int)(t % kLanes);
     if (j >= s.n || jz >= P) return;
+    // MODE 0 spreads dipoles alone: a masked site (the M sites) adds nothing
+    if (MODE == 0 && polr2 && !(polr2[j] > 1e-6)) return;
     int gi[3][P];
     T th[3][P], d1[3][P], d2[3][P];
-    site_splines<T, P, 1>(s, x[j], y[j], z[j], gi, th, d1, d2);
-    double mxd = 0, myd = 0, mzd = 0;
-    if (!polr2 || polr2[j] > 1e-6) dip_of(dv, j, mxd, myd, mzd);
     T mt[3];
-    to_t<T>(s, mxd, myd, mzd, mt);
+    if constexpr (sizeof(T) == 4 && MODE == 0) {   // the CG sweeps: site frame, FP32 dipoles
+        site_splines32<P, 1>(s, j, gi, th, d1, d2);
+        const DV d = dv[j];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) mt[a] = s.jac32[3 * a] * d.x + s.jac32[3 * a + 1] * d.y + s.jac32[3 * a + 2] * d.z;
+    } else {
+        site_splines<T, P, 1>(s, x[j], y[j], z[j], gi, th, d1, d2);
+        double mxd = 0, myd = 0, mzd = 0;
+        if (!polr2 || polr2[j] > 1e-6) dip_of(dv, j, mxd, myd, mzd);
+        to_t<T>(s, mxd, myd, mzd, mt);
+    }
     const T qj = MODE >= 1 ? (T)q[j] : T(0);
     const size_t K12 = (size_t)s.K1 * s.K2;
     const T tz = pick(th[2], jz), dz = pick(d1[2], jz);
@@ -472,11 +528,14 @@ __global__ void __launch_bounds__(kSpThreads) k_spme_field(SpArgs s, const doubl
     const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
     const int j = (int)(t / kLanes), jz = (int)(t % kLanes);
     if (j >= s.n) return;   // whole lane groups leave together
+    const bool pol = polr2[j] > 1e-6;
     T D[3] = {0, 0, 0}, Dq[3] = {0, 0, 0};
-    if (jz < P) {
+    // without the charges' field a masked site needs no gather (its field is not used)
+    if (jz < P && (FIRST || pol)) {
         int gi[3][P];
         T th[3][P], d1[3][P], d2[3][P];
-        site_splines<T, P, 1>(s, x[j], y[j], z[j], gi, th, d1, d2);
+        if constexpr (sizeof(T) == 4) site_splines32<P, 1>(s, j, gi, th, d1, d2);
+        else site_splines<T, P, 1>(s, x[j], y[j], z[j], gi, th, d1, d2);
         const size_t K12 = (size_t)s.K1 * s.K2;
         const C* plane = grid + pick(gi[2], jz) * K12;
         const T tz = pick(th[2], jz), dz = pick(d1[2], jz);
@@ -511,11 +570,10 @@ __global__ void __launch_bounds__(kSpThreads) k_spme_field(SpArgs s, const doubl
         if (FIRST) Dq[c] = group_sum(Dq[c]);
     }
     if (jz != 0) return;
-    const bool pol = polr2[j] > 1e-6;
     const int n = s.n;
     for (int c = 0; c < 3; ++c) {
-        const double Dr = s.jac[c] * (double)D[0] + s.jac[3 + c] * (double)D[1] + s.jac[6 + c] * (double)D[2];
         if (efm) {
+            const double Dr = s.jac[c] * (double)D[0] + s.jac[3 + c] * (double)D[1] + s.jac[6 + c] * (double)D[2];
             const double mu = c == 0 ? mx[j] : (c == 1 ? my[j] : mz[j]);
             efm[(size_t)c * n + j] = (pol ? -sfac * Dr : 0.0) + dum * mu;
             if (FIRST)
@@ -524,7 +582,8 @@ __global__ void __launch_bounds__(kSpThreads) k_spme_field(SpArgs s, const doubl
         } else {
             const float4 dd = d32[j];
             const float dc = c == 0 ? dd.x : (c == 1 ? dd.y : dd.z);
-            e32k[(size_t)c * n + j] = (pol ? (float)(-sfac * Dr) : 0.f) + (float)dum * dc;
+            const float Drf = s.jac32[c] * (float)D[0] + s.jac32[3 + c] * (float)D[1] + s.jac32[6 + c] * (float)D[2];
+            e32k[(size_t)c * n + j] = (pol ? (float)(-sfac) * Drf : 0.f) + (float)dum * dc;
         }
     }
 }
@@ -761,6 +820,51 @@ bool factor(int n, FftAxis& a) {
     return m == 1;
 }
 
+// The x and y axes of the 3D FFT in one pass: one block per z plane (blockIdx.x) of grid
+// blockIdx.y.  The plane is loaded once (coalesced), transformed along x ([x][y] layout,
+// pitch K2 + 1), transposed in shared memory and transformed along y ([y][x], pitch K1 + 1),
+// then stored once: two passes over the grid and two launches fewer than one pass per axis.
+// sg +1 forward, -1 backward.
+template <typename T>
+__global__ void __launch_bounds__(kFftPlaneThreads) k_fft_plane(typename Cx<T>::t* data, size_t gstride, FftAxis ax,
+                                                                FftAxis ay, int sg, const typename Cx<T>::t* tw,
+                                                                const int* __restrict__ stop) {
+    typedef typename Cx<T>::t C;
+    if (stop && *stop) return;   // the CG solve that queued this pass has stopped
+    extern __shared__ __align__(16) unsigned char fft_smem[];
+    const int K1 = ax.n, K2 = ay.n, P1 = K2 + 1, P2 = K1 + 1;
+    const int words = max(K1 * P1, K2 * P2);
+    C* s0 = reinterpret_cast<C*>(fft_smem);
+    C* s1 = s0 + words;
+    C* twx = s1 + words;
+    C* twy = twx + K1;
+    C* g = data + (size_t)blockIdx.y * gstride + (size_t)blockIdx.x * K1 * K2;
+    for (int i = threadIdx.x; i < K1; i += blockDim.x) twx[i] = tw[ax.tw_off + i];
+    for (int i = threadIdx.x; i < K2; i += blockDim.x) twy[i] = tw[ay.tw_off + i];
+    for (int i = threadIdx.x; i < K1 * K2; i += blockDim.x) {
+        const int x = i % K1, y = i / K1;
+        s0[x * P1 + y] = g[i];
+    }
+    __syncthreads();
+    C* r = fft_lines<T>(s0, s1, ax, P1, K2, twx, sg);
+    C* t = r == s0 ? s1 : s0;
+    for (int i = threadIdx.x; i < K1 * K2; i += blockDim.x) {
+        const int x = i % K1, y = i / K1;
+        t[y * P2 + x] = r[x * P1 + y];
+    }
+    __syncthreads();
+    C* u = fft_lines<T>(t, r, ay, P2, K1, twy, sg);
+    for (int i = threadIdx.x; i < K1 * K2; i += blockDim.x) {
+        const int x = i % K1, y = i / K1;
+        g[i] = u[y * P2 + x];
+    }
+}
+
+// Shared memory of the plane pass: two buffers and the x and y twiddles.
+inline size_t plane_smem_bytes(int K1, int K2, size_t csize) {
+    return (2 * (size_t)std::max(K1 * (K2 + 1), K2 * (K1 + 1)) + K1 + K2) * csize;
+}
+
 // Lines per FFT block: about 1024 complex values per block.
 inline int lines_per_block(int n) { return std::max(2, std::min(16, 1024 / n)); }
 
@@ -777,7 +881,8 @@ cudaError_t allow_fft_smem() {
     const void* f[] = {(const void*)k_fft_axis<double, 0>, (const void*)k_fft_axis<double, 1>,
                        (const void*)k_fft_axis<double, 2>, (const void*)k_fft_axis<double, 3>,
                        (const void*)k_fft_axis<float, 0>,  (const void*)k_fft_axis<float, 1>,
-                       (const void*)k_fft_axis<float, 2>,  (const void*)k_fft_axis<float, 3>};
+                       (const void*)k_fft_axis<float, 2>,  (const void*)k_fft_axis<float, 3>,
+                       (const void*)k_fft_plane<double>,   (const void*)k_fft_plane<float>};
     for (const void* q : f)
         if ((e = cudaFuncSetAttribute(q, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxFftSmem))) return e;
     done.insert(dev);
@@ -818,6 +923,19 @@ template <typename T>
 cudaError_t convolve(typename Cx<T>::t* data, const FftAxis* ax, const int* K, const typename Cx<T>::t* tw, const T* G,
                      cudaStream_t s, long& launches, const int* stop = nullptr) {
     cudaError_t e;
+    typedef typename Cx<T>::t C;
+    const size_t psm = plane_smem_bytes(K[0], K[1], sizeof(C));
+    // FP32: x and y in one pass per plane (64 x 64: 14 us against 2 x 8.8 us).  FP64 keeps the
+    // axis passes: its plane pass (one 135 KB block per plane, 64 of the 152 SMs) is FP64-pipe
+    // bound and took 62 us against 2 x 18 us.
+    if (sizeof(T) == 4 && psm <= (size_t)kMaxFftSmem) {
+        k_fft_plane<T><<<dim3(K[2], 1), kFftPlaneThreads, psm, s>>>(data, 0, ax[0], ax[1], 1, tw, stop);
+        if ((e = cudaGetLastError())) return e;
+        if ((e = fft_pass<T>(2, data, 0, 1, 2, ax[2], K, tw, G, s, stop))) return e;
+        k_fft_plane<T><<<dim3(K[2], 1), kFftPlaneThreads, psm, s>>>(data, 0, ax[0], ax[1], -1, tw, stop);
+        launches += 3;
+        return cudaGetLastError();
+    }
     if ((e = fft_pass<T>(0, data, 0, 1, 0, ax[0], K, tw, G, s, stop))) return e;
     if ((e = fft_pass<T>(0, data, 0, 1, 1, ax[1], K, tw, G, s, stop))) return e;
     if ((e = fft_pass<T>(2, data, 0, 1, 2, ax[2], K, tw, G, s, stop))) return e;
@@ -834,9 +952,12 @@ SpArgs sp_args(const SpmeState& st, int n) {
     a.K2 = st.K[1];
     a.K3 = st.K[2];
     a.stop = nullptr;
+    a.sib = st.sib;
+    a.sw = st.sw;
     for (int i = 0; i < 9; ++i) {
         a.rc[i] = st.rc[i];
         a.jac[i] = st.jac[i];
+        a.jac32[i] = (float)st.jac[i];
     }
     return a;
 }
@@ -867,9 +988,12 @@ int spme_smooth_even(double x) {
 SpmeState::~SpmeState() { release(); }
 
 void SpmeState::release() {
-    void* p[] = {G, G32, tw, tw32, grid, grid32, part};
+    void* p[] = {G, G32, tw, tw32, grid, grid32, part, sib, sw};
     for (void* q : p)
         if (q) cudaFree(q);
+    sib = nullptr;
+    sw = nullptr;
+    site_cap = 0;
     G = nullptr;
     G32 = nullptr;
     tw = nullptr;
@@ -1082,6 +1206,23 @@ cudaError_t SpmeState::field64(int n, const double* x, const double* y, const do
     return cudaGetLastError();
 }
 
+cudaError_t SpmeState::frame32(int n, const double* x, const double* y, const double* z, cudaStream_t s) {
+    cudaError_t e;
+    if (!order) return cudaErrorInvalidValue;
+    if (n > site_cap) {
+        if (sib) cudaFree(sib);
+        if (sw) cudaFree(sw);
+        sib = nullptr;
+        sw = nullptr;
+        site_cap = 0;
+        if ((e = cudaMalloc(&sib, (size_t)n * sizeof(int4)))) return e;
+        if ((e = cudaMalloc(&sw, (size_t)n * sizeof(float4)))) return e;
+        site_cap = n;
+    }
+    if (n > 0) k_spme_frame<<<nblocks(n, 256), 256, 0, s>>>(sp_args(*this, n), x, y, z, sib, sw);
+    return cudaGetLastError();
+}
+
 cudaError_t SpmeState::field32(int n, const double* x, const double* y, const double* z, const float4* d,
                                const double* polr2, double sfac, double dum, float* e32k, cudaStream_t s,
                                const int* stop) {
@@ -1149,6 +1290,13 @@ cudaError_t SpmeState::fft64(double2* data, int count, int sign, cudaStream_t s)
     cudaError_t e;
     if (!order) return cudaErrorInvalidValue;
     const size_t gs = ng;
+    const size_t psm = plane_smem_bytes(K[0], K[1], sizeof(double2));
+    if (psm <= (size_t)kMaxFftSmem) {   // the FP32 convolutions' form: x and y in one plane pass
+        k_fft_plane<double><<<dim3(K[2], count), kFftPlaneThreads, psm, s>>>(data, gs, ax[0], ax[1], sign > 0 ? 1 : -1,
+                                                                            tw, nullptr);
+        if ((e = cudaGetLastError())) return e;
+        return fft_pass<double>(sign > 0 ? 0 : 1, data, gs, count, 2, ax[2], K, tw, G, s);
+    }
     for (int a = 0; a < 3; ++a)
         if ((e = fft_pass<double>(sign > 0 ? 0 : 1, data, gs, count, a, ax[a], K, tw, G, s))) return e;
     return cudaSuccess;
