@@ -341,54 +341,6 @@ def run_ours(args, rank, world):
         tot = sum(a.elapsed_time(b) for a, b in ev) / 1e3
         return max_over_ranks(tot, world, dev), launches, float(np.mean(iters)), inner / max(1, steps)
 
-    # numerics of the mixed step against the FP64 step on the same state (cold dipoles)
-    reset()
-    sc64 = step(capi.FP64)
-    F64 = F.cpu().numpy().copy()
-    reset()
-    scm = step(capi.MIXED)
-    Fm = F.cpu().numpy()
-    err_f = float(np.sqrt(np.mean((Fm - F64) ** 2) / np.mean(F64 ** 2)))
-    nws = capi.NWATERSCALARS
-
-    def jtot(v):
-        j = v[12:15] + v[15:18] + v[capi.NSCALARS + 11:capi.NSCALARS + 14] + v[capi.NSCALARS + 25:capi.NSCALARS + 28]
-        return j + v[nws + 16:nws + 19] + v[nws + 19:nws + 22]
-
-    def etot(v):
-        return v[0] + v[1] + v[capi.NSCALARS] + v[capi.NSCALARS + 14] + v[nws]
-
-    err_j = float(np.linalg.norm(jtot(scm) - jtot(sc64)) / np.linalg.norm(jtot(sc64)))
-    err_e = float(abs(etot(scm) - etot(sc64)) / abs(etot(sc64)))
-    _, (ndim, ntri, _, hard2, hard3) = ctx.last_timings()
-
-    clocks = ClockSampler(dev.index)
-    clocks.start()
-    t_mixed, launches, it_mixed, inner_mixed = timed(capi.MIXED, args.steps, args.warmup)
-    clk = clocks.stop()
-    grid = ctx.spme_last_grid()
-    k64 = max(3, args.steps // 4)
-    t_fp64, _, it_fp64, _ = timed(capi.FP64, k64, min(args.warmup, 3))
-    # phase times of the electrostatics in the mixed step (CUDA events on the launching stream)
-    ctx.set_profiling(True)
-    reset()
-    pol_phase = np.zeros(4)
-    kf_ms = kf_flops = 0.0
-    kf_n = 0
-    nprof = 3
-    for i_ in range(2 + nprof):
-        step(capi.MIXED)
-        drift()
-        if i_ >= 2:
-            ms, kvec = ctx.polar_timings()
-            pol_phase += ms
-            a_, b_, c_ = ctx.polar_field_timing()
-            kf_ms += a_
-            kf_flops += b_
-            kf_n += c_
-    pol_phase /= nprof
-    ctx.set_profiling(False)
-
     # the MB-pol 1B + 2B + 3B terms alone (the polynomial path), device resident
     def step_poly(precision):
         F.zero_()
@@ -418,6 +370,74 @@ def run_ours(args, rank, world):
         torch.cuda.synchronize()
         ctx.set_profiling(False)
         return sum(a.elapsed_time(b) for a, b in ev) / 1e3, phase / steps
+
+    # split of the fused 2B/3B kernel (dimer warps of its 12 per block): timed once per run on
+    # this box and device, the fastest kept for every measurement below
+    split_ms = {}
+    for w_ in (2, 3, 4, 5, 6, 8):
+        ctx.set_fused_split(w_)
+        _, ph_ = timed_poly(capi.MIXED, 4, 1, profile=True)
+        split_ms[w_] = float(ph_[1])
+    best_split = min(split_ms, key=split_ms.get)
+    ctx.set_fused_split(best_split)
+
+    # numerics of the mixed step against the FP64 step on the same state (cold dipoles)
+    reset()
+    sc64 = step(capi.FP64)
+    F64 = F.cpu().numpy().copy()
+    reset()
+    scm = step(capi.MIXED)
+    Fm = F.cpu().numpy()
+    err_f = float(np.sqrt(np.mean((Fm - F64) ** 2) / np.mean(F64 ** 2)))
+    nws = capi.NWATERSCALARS
+
+    def jtot(v):
+        j = v[12:15] + v[15:18] + v[capi.NSCALARS + 11:capi.NSCALARS + 14] + v[capi.NSCALARS + 25:capi.NSCALARS + 28]
+        return j + v[nws + 16:nws + 19] + v[nws + 19:nws + 22]
+
+    def etot(v):
+        return v[0] + v[1] + v[capi.NSCALARS] + v[capi.NSCALARS + 14] + v[nws]
+
+    err_j = float(np.linalg.norm(jtot(scm) - jtot(sc64)) / np.linalg.norm(jtot(sc64)))
+    err_e = float(abs(etot(scm) - etot(sc64)) / abs(etot(sc64)))
+    _, (ndim, ntri, _, hard2, hard3) = ctx.last_timings()
+
+    # the mixed solve's preconditioner (Jacobi sweeps on the real-space system, odd): timed on a
+    # few MD steps of this box, the fastest kept for the measurements below
+    pre_ms = {}
+    for p_ in (1, 3, 5):
+        ctx.set_precond_sweeps(p_)
+        t_, _, _, _ = timed(capi.MIXED, 4, 2)
+        pre_ms[p_] = 1e3 * t_ / 4
+    best_pre = min(pre_ms, key=pre_ms.get)
+    ctx.set_precond_sweeps(best_pre)
+
+    clocks = ClockSampler(dev.index)
+    clocks.start()
+    t_mixed, launches, it_mixed, inner_mixed = timed(capi.MIXED, args.steps, args.warmup)
+    clk = clocks.stop()
+    grid = ctx.spme_last_grid()
+    k64 = max(3, args.steps // 4)
+    t_fp64, _, it_fp64, _ = timed(capi.FP64, k64, min(args.warmup, 3))
+    # phase times of the electrostatics in the mixed step (CUDA events on the launching stream)
+    ctx.set_profiling(True)
+    reset()
+    pol_phase = np.zeros(4)
+    kf_ms = kf_flops = 0.0
+    kf_n = 0
+    nprof = 3
+    for i_ in range(2 + nprof):
+        step(capi.MIXED)
+        drift()
+        if i_ >= 2:
+            ms, kvec = ctx.polar_timings()
+            pol_phase += ms
+            a_, b_, c_ = ctx.polar_field_timing()
+            kf_ms += a_
+            kf_flops += b_
+            kf_n += c_
+    pol_phase /= nprof
+    ctx.set_profiling(False)
 
     t_poly, _ = timed_poly(capi.MIXED, args.steps, args.warmup)
     _, phase_prof = timed_poly(capi.MIXED, max(3, args.steps // 4), 1, profile=True)
@@ -557,6 +577,14 @@ def run_ours(args, rank, world):
                                              "jkin": phase_prof[3]},
                                 "fp64_phase_ms": {"lists": phase64[0], "2b": phase64[1], "3b": phase64[2],
                                                   "jkin": phase64[3]}},
+        "precond_tuning": {"mixed_step_ms_by_jacobi_sweeps": {str(k): v for k, v in pre_ms.items()},
+                           "chosen_sweeps": best_pre,
+                           "method": "each preconditioner timed on 4 warm-started MD steps of this box "
+                                     "(CUDA events), the fastest used for every measurement of the run"},
+        "fused_split_tuning": {"fused_kernel_ms_by_dimer_warps": {str(k): v for k, v in split_ms.items()},
+                               "chosen_dimer_warps": best_split,
+                               "method": "each split timed on 4 steps of the 1B+2B+3B path of this box "
+                                         "(CUDA events), the fastest used for every measurement of the run"},
         "e2e": {"value": world * args.steps / t_e2e, "unit": "steps/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
         # the mixed step's largest kernel: the fused 2B (FP64) + 3B (FP32) polynomial kernel,
@@ -769,7 +797,7 @@ def batched(steps=10, warmup=3):
     return out
 
 
-def batched_whole(steps=4, warmup=2, lanes=8):
+def batched_whole(steps=4, warmup=2):
     """Whole force evaluations (M sites, DMS charges, TTM4-F electrostatics with the dipole
     solve, dispersion, 1-body, 2B + 3B, heat current) of many boxes per call through
     mbx_water_step_multi: 32 beads of the 256-water box (Ewald alpha 0.3, kmax 8, rcut 9)
@@ -812,19 +840,21 @@ def batched_whole(steps=4, warmup=2, lanes=8):
         for b in boxes:
             atom[o:o + 3 * b.nw] = True
             o += b.natms
-        res = {"boxes": nb, "waters": int(nws.sum()), "lanes": lanes}
+        res = {"boxes": nb, "waters": int(nws.sum())}
         ctx = capi.Context(0)
-        ctx.set_lanes(lanes)
         ctx.disp_setup(systems.DISP_PARAMS_SYNTHETIC, rcut=min(9.0, 0.45 * min(b.L for b in boxes)), delr=0.5)
         sc = np.zeros((nb, capi.NSTEPSCALARS))
         st = np.zeros(nb, np.int32)
-        for prec, key in ((capi.MIXED, "mixed"), (capi.FP64, "fp64")):
+
+        def run(prec, nsteps, nwarm):
+            """nwarm + nsteps MD steps from the initial state; the mean wall time of the last
+            nsteps calls, and the first call's forces and per-box scalars"""
             x, y, z = (np.ascontiguousarray(xyz0[:, k]).copy() for k in range(3))
             dip = [np.zeros(n) for _ in range(3)]
             f = [np.zeros(n) for _ in range(3)]
             ae = np.zeros(n)
-            ts, its = [], []
-            for s_ in range(warmup + steps):
+            ts, first = [], None
+            for s_ in range(nwarm + nsteps):
                 for a in f:
                     a[:] = 0.0
                 ae[:] = 0.0
@@ -836,13 +866,48 @@ def batched_whole(steps=4, warmup=2, lanes=8):
                 t1 = time.perf_counter()
                 if rc:
                     raise RuntimeError("mbx_water_step_multi: %d %s" % (rc, ctx.lib.mbx_error(ctx.h)))
-                if s_ >= warmup:
+                if s_ == 0:
+                    first = (np.stack([a.copy() for a in f]), sc.copy())
+                if s_ >= nwarm:
                     ts.append(t1 - t0)
                 for k, a in enumerate((x, y, z)):
                     a[atom] += DT_PS * v[k][atom]
-            t = float(np.mean(ts))
+            return float(np.mean(ts)) if ts else 0.0, first
+
+        # worker lanes (concurrent boxes): timed per run, the fastest kept
+        lane_ms = {}
+        for L in (8, 16, 32):
+            ctx.set_lanes(L)
+            lane_ms[L] = 1e3 * run(capi.MIXED, 2, 1)[0]
+        lanes = min(lane_ms, key=lane_ms.get)
+        ctx.set_lanes(lanes)
+        res["lanes"] = lanes
+        res["lanes_tuning_ms_by_lanes"] = {str(k): v_ for k, v_ in lane_ms.items()}
+        for prec, key in ((capi.MIXED, "mixed"), (capi.FP64, "fp64")):
+            t, first = run(prec, steps, warmup)
             res[key] = {"steps_per_s": 1.0 / t, "ms_per_step": 1e3 * t, "boxes_per_s": nb / t,
                         "waters_per_s": float(nws.sum()) / t}
+            res[key + "_first_state"] = first
+        # mixed against FP64 per box on the same configuration (dipoles from zero)
+        fm, scm = res.pop("mixed_first_state")
+        fd, scd = res.pop("fp64_first_state")
+        nws_ = capi.NWATERSCALARS
+
+        def jt(v_):
+            j = (v_[12:15] + v_[15:18] + v_[capi.NSCALARS + 11:capi.NSCALARS + 14] +
+                 v_[capi.NSCALARS + 25:capi.NSCALARS + 28])
+            return j + v_[nws_ + 16:nws_ + 19] + v_[nws_ + 19:nws_ + 22]
+
+        herr, ferr, o = [], [], 0
+        for b_, box in enumerate(boxes):
+            sl = slice(o, o + 3 * box.nw)
+            o += box.natms
+            herr.append(float(np.linalg.norm(jt(scm[b_]) - jt(scd[b_])) / np.linalg.norm(jt(scd[b_]))))
+            ferr.append(float(np.sqrt(np.mean((fm[:, sl] - fd[:, sl]) ** 2) / np.mean(fd[:, sl] ** 2))))
+        res["mixed_error_vs_fp64_per_box"] = {"heat_current_rel_worst": max(herr),
+                                              "heat_current_rel_median": float(np.median(herr)),
+                                              "force_rms_rel_worst": max(ferr),
+                                              "state": "the same configuration, dipoles from zero"}
         if name.startswith("beads"):
             # the same whole evaluations one box per call on one context (mixed)
             x, y, z = (np.ascontiguousarray(xyz0[:, k]).copy() for k in range(3))

@@ -42,6 +42,7 @@ struct mbx_context {
     float limit2 = 0.0f, limit3 = 3.4e38f;
     // 2B and 3B in one persistent launch (launch_23) where it applies; 0 = separate kernels
     int fused = 1;
+    int fused_split = 0;            // dimer warps of the 12 per block (0: the default, 4)
     int nsm = 0;                    // SMs of the device (the persistent grid)
     int* fuse_ctr = nullptr;        // device [2]: work counters of the persistent kernel
     double* part2 = nullptr;        // split FP64 dimers: per-chunk partial sums (pairs_cap dimers)
@@ -269,7 +270,7 @@ int run_mbpol(mbx_context* ctx, int precision, const Cell& cl, int nw, const int
         MixedPass mp{ctx->hard2, ctx->hard3, ctx->hard_count, ctx->limit2, ctx->limit3};
         if (ctx->fused && fused_applies(precision, mp)) {
             CK(launch_23(a, ctx->pairs, (int)np, nullptr, ctx->trip, (int)nt, nullptr, precision, ctx->fuse_ctr,
-                         ctx->nsm, s, ctx->part2, ctx->done2, ctx->pairs_cap));
+                         ctx->nsm, s, ctx->part2, ctx->done2, ctx->pairs_cap, ctx->fused_split));
             if (ctx->profiling) {
                 CK(cudaEventRecord(ctx->ev[2], s));
                 CK(cudaEventRecord(ctx->ev[3], s));
@@ -1236,8 +1237,8 @@ void mbx_set_error_text(mbx_context* ctx, const char* msg) {
 
 extern "C" int mbx_set_precond_sweeps(mbx_context* ctx, int sweeps) {
     if (!ctx) return MBX_ERR_ARG;
-    if (sweeps < 1 || sweeps > 9 || sweeps % 2 == 0)
-        return fail(ctx, MBX_ERR_ARG, "preconditioner sweeps must be odd, 1..9");
+    if (sweeps != 0 && (sweeps < 1 || sweeps > 9 || sweeps % 2 == 0))
+        return fail(ctx, MBX_ERR_ARG, "preconditioner sweeps must be 0 (automatic) or odd, 1..9");
     ctx->polar.precond_sweeps = sweeps;
     return MBX_OK;
 }
@@ -1396,8 +1397,10 @@ extern "C" int mbx_spme_kspace(mbx_context* ctx, const double* prm, int order, c
         const double vol = std::fabs(a[0] * (a[4] * a[8] - a[5] * a[7]) + a[1] * (a[5] * a[6] - a[3] * a[8]) +
                                      a[2] * (a[3] * a[7] - a[4] * a[6]));
         sc = 2.0 * (2.0 * 3.141592653589793 / vol) * 138935.4835 / prm[1];   // sfac
-        e = st.final(n, d, d + m, d + 2 * m, d + 3 * m, reinterpret_cast<const double4*>(d + 4 * m),
-                     heat ? d + 8 * m : nullptr, sc, part5, acc, dfield, s);
+        e = st.frame(n, d, d + m, d + 2 * m, s);
+        if (!e)
+            e = st.final(n, d, d + m, d + 2 * m, d + 3 * m, reinterpret_cast<const double4*>(d + 4 * m),
+                         heat ? d + 8 * m : nullptr, sc, part5, acc, dfield, s);
     }
     if (!e) e = cudaMemcpyAsync(hp.data(), part5, hp.size() * sizeof(double), cudaMemcpyDeviceToHost, s);
     if (!e) e = cudaStreamSynchronize(s);
@@ -1645,6 +1648,12 @@ extern "C" int mbx_msite_redistribute(int nw, double gamma, double* fxx, double*
 extern "C" int mbx_set_fused(mbx_context* ctx, int on) {
     if (!ctx) return MBX_ERR_ARG;
     ctx->fused = on ? 1 : 0;
+    return MBX_OK;
+}
+
+extern "C" int mbx_set_fused_split(mbx_context* ctx, int dimer_warps) {
+    if (!ctx || dimer_warps < 0 || dimer_warps > 11) return MBX_ERR_ARG;
+    ctx->fused_split = dimer_warps;
     return MBX_OK;
 }
 

@@ -26,6 +26,16 @@ __device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a,
 __device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }
 __device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a, b); }
 
+// 1 / sqrt(x) for x > 0 (a squared pair distance): the FP32 estimate refined by two
+// Newton-Raphson steps y <- y (3 - x y^2) / 2, each squaring the relative error (~1e-7 ->
+// ~1e-14 -> rounding level).  Eight FP64-pipe operations where a correctly rounded root
+// and a division take about twice that; results agree with them to a few ulp.
+__device__ __forceinline__ double rsqrt_nr(double x) {
+    double y = (double)rsqrtf((float)x);
+    y = y * (1.5 - 0.5 * x * y * y);
+    return y * (1.5 - 0.5 * x * y * y);
+}
+
 // Fortran NINT on a double: round half away from zero.
 __device__ __forceinline__ double nint(double x) { return round(x); }
 
@@ -130,7 +140,8 @@ __device__ __forceinline__ void block_sum_atomic(double (&v)[NV], double* out) {
     __syncthreads();
     if (threadIdx.x < NV) {
         double s = 0.0;
-        for (int i = 0; i < kThreads / 32; ++i) s += red[i][threadIdx.x];
+        const int nwarp = ((int)blockDim.x + 31) >> 5;   // blocks of up to kThreads
+        for (int i = 0; i < nwarp; ++i) s += red[i][threadIdx.x];
         atomicAdd(out + threadIdx.x, s);
     }
 }

@@ -258,7 +258,8 @@ __global__ void __launch_bounds__(kThreads) k_disp_forces(DispArgs a, const int*
             image(a.cl, dx, dy, dz);
             const double rsq = dadd(dadd(dmul(dx, dx), dmul(dy, dy)), dmul(dz, dz));
             if (!(a.rcsq > rsq)) continue;
-            const double rrr = sqrt(rsq);
+            const double rri = rsqrt_nr(rsq);   // r and 1/r^2 without an FP64 root and division
+            const double rrr = rsq * rri;
             // l >= 1 unless two atoms are closer than one table step (the reference would
             // read before its table there); r < rcut keeps l + 2 <= mxgrid
             const int l = max((int)dmul(rrr, a.rdr), 1);
@@ -272,7 +273,7 @@ __global__ void __launch_bounds__(kThreads) k_disp_forces(DispArgs a, const int*
             const double gk = gt[0], gk1 = gt[1], gk2 = gt[2];
             t1 = dadd(gk, dmul(dsub(gk1, gk), ppp));
             t2 = dadd(gk1, dmul(dsub(gk2, gk1), dsub(ppp, 1.0)));
-            const double gamma = dadd(t1, dmul(dmul(dsub(t2, t1), ppp), 0.5)) / rsq;
+            const double gamma = dadd(t1, dmul(dmul(dsub(t2, t1), ppp), 0.5)) * (rri * rri);
             const double f0 = gamma * dx, f1 = gamma * dy, f2 = gamma * dz;
             fi[0] += f0;
             fi[1] += f1;

@@ -70,7 +70,7 @@ bool fused_applies(int precision, const MixedPass& mp);
 int dimer_parts();
 cudaError_t launch_23(const MbpolArgs& a, const int2* pairs, int n2, const int* n2_dev, const int4* trip, int n3,
                       const int* n3_dev, int precision, int* ctr, int nsm, cudaStream_t s,
-                      double* partial = nullptr, int* done = nullptr, long part_cap = 0);
+                      double* partial = nullptr, int* done = nullptr, long part_cap = 0, int dimer_warps = 0);
 // Isolated polynomial + model evaluation for explicit clusters (the per-call ABI).
 cudaError_t launch_2b_direct(int n, const double* w1, const double* w2, double* E, double* g1, double* g2,
                              int precision, cudaStream_t s);
@@ -196,6 +196,7 @@ struct PolarState {
     // within rcut + list_skin, kept until a site moved more than list_skin / 2
     double list_skin = 1.0;
     int *nn_s = nullptr, *nbr_s = nullptr, *npol_s = nullptr;
+    int2* nup_s = nullptr;
     int cap_s = 768, cap_s_alloc = 0, ns_cap = 0;
     double* xref = nullptr;                // positions at the skin list's build (x, y, z blocks)
     bool skin_ok = false;
@@ -205,6 +206,7 @@ struct PolarState {
     int last_n = 0;                        // sites of the last call (the pair list's rows)
     int *nn = nullptr, *nbr = nullptr, *flag = nullptr;
     int* npol = nullptr;                   // per row: the polarizable partners, first in the row
+    int2* nup = nullptr;                   // per row: partners j > i heading each group (pol, other)
     float4* xf = nullptr;
     double* tens = nullptr;                // dipole tensors of the list pairs (6 blocks)
     double* intra = nullptr;               // intramolecular O/H dipole tensors (18 per water)
@@ -238,7 +240,8 @@ struct PolarState {
     float4 *r32 = nullptr, *d32 = nullptr, *cg_x = nullptr, *cg_r = nullptr, *cg_q = nullptr;
     float4* vh32 = nullptr;                // FP32 heat weights of the final pass (3 per site)
     float4* cg_z = nullptr;                // preconditioned residual of the correction solve
-    int precond_sweeps = 3;                // Jacobi sweeps of the CG preconditioner (odd; 1: diagonal only)
+    int precond_sweeps = 0;                // Jacobi sweeps of the CG preconditioner (odd; 1: diagonal
+                                           // only; 0: 1 with SPME, 3 with the Ewald sum)
     float* e32 = nullptr;
     int cap32 = 0, n32 = 0, k32 = 0;
     size_t fac32_cap = 0;

@@ -753,13 +753,13 @@ __global__ void __launch_bounds__(kThreads) k_mbpol_3b(MbpolArgs a, const int4* 
 // 4+4 warps at 255 registers 5.2 ms).  Work is claimed 32 tasks at a time from ctr[0]
 // (dimers) and ctr[1] (trimers), which start at zero.
 constexpr int kFusedThreads = 384;
-constexpr int kFusedDimerWarps = 4;
+constexpr int kFusedDimerWarps = 4;   // the default split (dimer_warps 0)
 
 template <typename T2, typename T3>
 __global__ void __launch_bounds__(kFusedThreads, 1)
     k_mbpol_23(MbpolArgs a, const int2* __restrict__ pairs, int n2, const int* __restrict__ n2_dev,
                const int4* __restrict__ trip, int n3, const int* __restrict__ n3_dev, int* ctr,
-               double* partial, int* done, long part_cap) {
+               double* partial, int* done, long part_cap, int dimer_warps) {
     if (n2_dev) n2 = *n2_dev;
     if (n3_dev) n3 = *n3_dev;
     // dimer tasks: 32-dimer chunks, each split into `parts` polynomial chunks (chunk c,
@@ -768,7 +768,7 @@ __global__ void __launch_bounds__(kFusedThreads, 1)
     const int parts = partial ? kPoly2BF64Parts : 1;
     const int ntask2 = ((n2 + 31) / 32) * 32 * parts;
     const int lane = threadIdx.x & 31;
-    int role = (threadIdx.x >> 5) < kFusedDimerWarps ? 0 : 1;
+    int role = (int)(threadIdx.x >> 5) < dimer_warps ? 0 : 1;
     bool switched = false;
     const HardList none{nullptr, nullptr, 0.f};
     double red[15];
@@ -1153,14 +1153,16 @@ int dimer_parts() { return kPoly2BF64Parts; }
 
 cudaError_t launch_23(const MbpolArgs& a, const int2* pairs, int n2, const int* n2_dev, const int4* trip, int n3,
                       const int* n3_dev, int precision, int* ctr, int nsm, cudaStream_t s, double* partial,
-                      int* done, long part_cap) {
+                      int* done, long part_cap, int dimer_warps) {
+    if (dimer_warps <= 0) dimer_warps = kFusedDimerWarps;
+    if (dimer_warps >= kFusedThreads / 32) return cudaErrorInvalidValue;
     cudaError_t e = cudaMemsetAsync(ctr, 0, 2 * sizeof(int), s);
     if (e) return e;
     if (precision == 0) return cudaErrorInvalidValue;   // see fused_applies
     if (!partial || !done) part_cap = 0;
     if (part_cap > 0 && (e = cudaMemsetAsync(done, 0, (size_t)part_cap * sizeof(int), s))) return e;
     k_mbpol_23<double, float><<<nsm, kFusedThreads, 0, s>>>(a, pairs, n2, n2_dev, trip, n3, n3_dev, ctr, partial,
-                                                             done, part_cap);
+                                                             done, part_cap, dimer_warps);
     return cudaGetLastError();
 }
 

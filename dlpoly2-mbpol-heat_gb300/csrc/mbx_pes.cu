@@ -213,20 +213,29 @@ __global__ void __launch_bounds__(kThreads) k_ps_pes(int nang, const int* __rest
 // M-site placement (SOURCE/dlpoly_cmd.f:2041-2057) and qdetermine with the MB-pol
 // settings (ldms, new charge assignment; SOURCE/qdetermine.f90:112-285): one thread per
 // water writes r_M, q_H1, q_H2, q_M and dq/d(r1, r2, cos) (6 values) for qdforce.
+// Eight lanes per water: every lane places the M site's geometry, lane l takes the DMS
+// expansion terms j = l (mod 8), and the group adds its partial sums by shuffles (one
+// thread per water left 4096 waters at 128 warps: latency-bound at 0.29 ms).  The 1/reoh
+// factor of the r derivatives is applied once to the sums.
+constexpr int kDmsLanes = 8;
+
 __global__ void __launch_bounds__(kThreads) k_msites_dms(int nw, const int* __restrict__ list, Cell cl, double* x,
                                                           double* y, double* z, double gamma, double* chge,
                                                           double* dp) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nw) return;
+    const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    const int i = (int)(t / kDmsLanes), l = (int)(t % kDmsLanes);
+    if (i >= nw) return;   // whole lane groups leave together
     const int io = list[3 * i] - 1, h1 = list[3 * i + 1] - 1, h2 = list[3 * i + 2] - 1;
     const int m = list[3 * nw - 1] + i;   // 0-based index of this water's M site
     double r1x = x[h1] - x[io], r1y = y[h1] - y[io], r1z = z[h1] - z[io];
     double r2x = x[h2] - x[io], r2y = y[h2] - y[io], r2z = z[h2] - z[io];
     image(cl, r1x, r1y, r1z);
     image(cl, r2x, r2y, r2z);
-    x[m] = x[io] + (r1x + r2x) * gamma / 2.0;
-    y[m] = y[io] + (r1y + r2y) * gamma / 2.0;
-    z[m] = z[io] + (r1z + r2z) * gamma / 2.0;
+    if (l == 0) {
+        x[m] = x[io] + (r1x + r2x) * gamma / 2.0;
+        y[m] = y[io] + (r1y + r2y) * gamma / 2.0;
+        z[m] = z[io] + (r1z + r2z) * gamma / 2.0;
+    }
     if (!chge) return;
     const double reoh = pes::kReoh;
     const double r1 = sqrt(r1x * r1x + r1y * r1y + r1z * r1z);
@@ -243,19 +252,27 @@ __global__ void __launch_bounds__(kThreads) k_msites_dms(int nw, const int* __re
         fm[j][1] = fm[j - 1][1] * x2;
         fm[j][2] = fm[j - 1][2] * x3;
     }
-    double p1 = 0, p2 = 0, d11 = 0, d12 = 0, d21 = 0, d22 = 0, d1c = 0, d2c = 0;
-    for (int j = 1; j < pes::kDmsTerms; ++j) {
+    double v[8] = {0, 0, 0, 0, 0, 0, 0, 0};   // p1, p2, d11, d12, d21, d22 (times reoh), d1c, d2c
+    for (int j = 1 + l; j < pes::kDmsTerms; j += kDmsLanes) {
         const int i1 = pes::kDmsIdx[j][0], i2 = pes::kDmsIdx[j][1], i3 = pes::kDmsIdx[j][2];
         const double c = __longlong_as_double((long long)pes::kDmsCoef[j]);
-        p1 += c * fm[i1][0] * fm[i2][1] * fm[i3][2];
-        p2 += c * fm[i2][0] * fm[i1][1] * fm[i3][2];
-        d11 += c * (i1 - 1) * fm[i1 - 1][0] * fm[i2][1] * fm[i3][2] / reoh;
-        d12 += c * (i2 - 1) * fm[i1][0] * fm[i2 - 1][1] * fm[i3][2] / reoh;
-        d21 += c * (i2 - 1) * fm[i2 - 1][0] * fm[i1][1] * fm[i3][2] / reoh;
-        d22 += c * (i1 - 1) * fm[i2][0] * fm[i1 - 1][1] * fm[i3][2] / reoh;
-        d1c += c * (i3 - 1) * fm[i1][0] * fm[i2][1] * fm[i3 - 1][2];
-        d2c += c * (i3 - 1) * fm[i2][0] * fm[i1][1] * fm[i3 - 1][2];
+        v[0] += c * fm[i1][0] * fm[i2][1] * fm[i3][2];
+        v[1] += c * fm[i2][0] * fm[i1][1] * fm[i3][2];
+        v[2] += c * (i1 - 1) * fm[i1 - 1][0] * fm[i2][1] * fm[i3][2];
+        v[3] += c * (i2 - 1) * fm[i1][0] * fm[i2 - 1][1] * fm[i3][2];
+        v[4] += c * (i2 - 1) * fm[i2 - 1][0] * fm[i1][1] * fm[i3][2];
+        v[5] += c * (i1 - 1) * fm[i2][0] * fm[i1 - 1][1] * fm[i3][2];
+        v[6] += c * (i3 - 1) * fm[i1][0] * fm[i2][1] * fm[i3 - 1][2];
+        v[7] += c * (i3 - 1) * fm[i2][0] * fm[i1][1] * fm[i3 - 1][2];
     }
+    const unsigned gm = 0xffu << (threadIdx.x & 24);   // this water's lane group
+#pragma unroll
+    for (int q = 0; q < 8; ++q)
+#pragma unroll
+        for (int o = kDmsLanes / 2; o > 0; o >>= 1) v[q] += __shfl_xor_sync(gm, v[q], o, kDmsLanes);
+    if (l != 0) return;
+    double p1 = v[0], p2 = v[1];
+    double d11 = v[2] / reoh, d12 = v[3] / reoh, d21 = v[4] / reoh, d22 = v[5] / reoh, d1c = v[6], d2c = v[7];
     const double bohr = 0.529177249, b1dms = 1.0, adms = 0.2999 * bohr, bdms = -0.6932;
     const double c0 = 1.0099, c1 = -0.1801, c2 = 0.0892;
     const double pl1 = cost, pl2 = 0.5 * (3.0 * pl1 * pl1 - 1.0);
@@ -292,7 +309,9 @@ __global__ void __launch_bounds__(kThreads) k_msites_dms(int nw, const int* __re
 cudaError_t launch_msites_dms(int nw, const int* list, const Cell& cl, double* x, double* y, double* z, double gamma,
                               double* chge, double* dp, cudaStream_t s) {
     if (nw <= 0) return cudaSuccess;
-    k_msites_dms<<<(nw + kThreads - 1) / kThreads, kThreads, 0, s>>>(nw, list, cl, x, y, z, gamma, chge, dp);
+    const long threads = (long)kDmsLanes * nw;
+    k_msites_dms<<<(unsigned)((threads + kThreads - 1) / kThreads), kThreads, 0, s>>>(nw, list, cl, x, y, z, gamma,
+                                                                                       chge, dp);
     return cudaGetLastError();
 }
 

@@ -141,6 +141,7 @@ struct PolArgs {
     double drewd, rdrewd;   // the erfcgenp grid step and its reciprocal
     const int *nn, *nbr;
     const int* npol;   // per row: its first npol partners are the polarizable ones (polr2 > 1e-6)
+    const int2* nup;   // per row: partners j > i at the head of each group (x polarizable, y the others)
     double* tens;   // 6 blocks of n * cap: the first npol entries of the polarizable rows
     float* tens32;  // the same in FP32 (mixed precision), or null
     double* intra;  // 18 per water
@@ -197,15 +198,6 @@ __device__ __forceinline__ double pow4(double t) {
     return t2 * t2;
 }
 
-// 1 / sqrt(x) for x > 0 (a squared pair distance): the FP32 estimate refined by two
-// Newton-Raphson steps y <- y (3 - x y^2) / 2, each squaring the relative error (~1e-7 ->
-// ~1e-14 -> rounding level).  Eight FP64-pipe operations where a correctly rounded root
-// and a division take about twice that; results agree with them to a few ulp.
-__device__ __forceinline__ double rsqrt_nr(double x) {
-    double y = (double)rsqrtf((float)x);
-    y = y * (1.5 - 0.5 * x * y * y);
-    return y * (1.5 - 0.5 * x * y * y);
-}
 
 // Heat-current contribution of the force-matrix entry (row a, column b, F) after the
 // M-site row redistribution (columns of M sites are never read).
@@ -292,9 +284,12 @@ __global__ void k_pol_bounds(int n, const unsigned* __restrict__ skey, int* __re
 // A pair whose FP32 distance is inside rcut - 0.01 A (r2in) is inside rcut in FP64 too (the
 // FP32 error of r^2 is below 1e-3 A^2 for coordinates under 1e3 A), so only the thin shell
 // between r2in and r2f takes the reference's FP64 test.
+// Row order: the polarizable partners first (npol of them), then the others; within each
+// group the partners j > i first (nup.x and nup.y of them), so a kernel can take every pair
+// once from its lower site (k_pol_ewald2p32) while the dipole kernels read whole rows.
 __global__ void k_pol_list(PolArgs a, int* __restrict__ nn, int* __restrict__ nbr, int* __restrict__ npol,
-                           int rowcap, double lc, const float4* __restrict__ xf, float r2f, float r2in,
-                           int* __restrict__ flag, int3 nc, int cells, const int* __restrict__ sidx,
+                           int2* __restrict__ nup, int rowcap, double lc, const float4* __restrict__ xf, float r2f,
+                           float r2in, int* __restrict__ flag, int3 nc, int cells, const int* __restrict__ sidx,
                            const int* __restrict__ cstart, const int* __restrict__ cend) {
     const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
@@ -308,9 +303,14 @@ __global__ void k_pol_list(PolArgs a, int* __restrict__ nn, int* __restrict__ nb
     // FP32 box constants once (converting them per candidate occupies the FP64 pipe)
     const float bx = (float)a.cl.c[0], by = (float)a.cl.c[4], bz = (float)a.cl.c[8];
     const float ibx = (float)a.cl.inv[0], iby = (float)a.cl.inv[1], ibz = (float)a.cl.inv[2];
-    // two passes: the polarizable partners first (the dipole tensors are kept for them only)
-    for (int pass = 0; pass < 2; ++pass) {
-        if (pass == 1 && lane == 0) npol[i] = min(cnt, rowcap);
+    // four passes: polarizable j > i, polarizable j < i, the others j > i, the others j < i
+    // (the dipole tensors are kept for the polarizable partners only)
+    int c1 = 0, c2 = 0, c3 = 0;
+    for (int pass = 0; pass < 4; ++pass) {
+        if (pass == 1) c1 = cnt;
+        if (pass == 2) c2 = cnt;
+        if (pass == 3) c3 = cnt;
+        const bool polpass = pass < 2, uppass = pass % 2 == 0;
         for (int c = 0; c < ncand; ++c) {
             int beg = 0, end = a.n;
             if (cells) {
@@ -328,7 +328,7 @@ __global__ void k_pol_list(PolArgs a, int* __restrict__ nn, int* __restrict__ nb
                 if (q < end) {
                     j = cells ? sidx[q] : q;
                     bool near = false, inside = false;
-                    if (j != i && site_mol(a, j) != mi && (a.polr2[j] > 1e-6) == (pass == 0)) {
+                    if (j != i && site_mol(a, j) != mi && (a.polr2[j] > 1e-6) == polpass && (j > i) == uppass) {
                         const float4 pj = xf[j];
                         float d2;
                         if (cells) {   // orthorhombic
@@ -364,6 +364,8 @@ __global__ void k_pol_list(PolArgs a, int* __restrict__ nn, int* __restrict__ nb
     }
     if (lane == 0) {
         nn[i] = min(cnt, rowcap);
+        npol[i] = min(c2, rowcap);
+        nup[i] = make_int2(min(c1, rowcap), min(c3, rowcap) - min(c2, rowcap));
         if (cnt > rowcap) atomicOr(flag, 1);
     }
 }
@@ -394,15 +396,19 @@ __global__ void k_pol_ref(int n, const double* __restrict__ x, const double* __r
 // (FP32 with margins, the reference's FP64 test in the shell around the cut), in the skin
 // list's order.
 __global__ void k_pol_filter(PolArgs a, const int* __restrict__ nn_s, const int* __restrict__ nbr_s,
-                             const int* __restrict__ npol_s, int cap_s, int* __restrict__ nn, int* __restrict__ nbr,
-                             int* __restrict__ npol, const float4* __restrict__ xf, float r2f, float r2in,
+                             const int* __restrict__ npol_s, const int2* __restrict__ nup_s, int cap_s,
+                             int* __restrict__ nn, int* __restrict__ nbr, int* __restrict__ npol,
+                             int2* __restrict__ nup, const float4* __restrict__ xf, float r2f, float r2in,
                              int* __restrict__ flag) {
     const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (i >= a.n) return;
     const float4 pi = xf[i];
-    const int m = nn_s[i], mp = npol_s[i];   // the skin row's polarizable partners come first
-    int cntp = 0;
+    // the skin row's segments (k_pol_list): [0, up.x) polarizable j > i, [up.x, mp) polarizable
+    // j < i, [mp, mp + up.y) the others j > i, then the others j < i; kept in order
+    const int m = nn_s[i], mp = npol_s[i];
+    const int2 up = nup_s[i];
+    int cntp = 0, cntu = 0, cntn = 0;
     const int* src = nbr_s + (size_t)i * cap_s;
     int* my = nbr + (size_t)i * a.cap;
     const bool ortho = a.cl.imcon == 1 || a.cl.imcon == 2;
@@ -441,13 +447,19 @@ __global__ void k_pol_filter(PolArgs a, const int* __restrict__ nn_s, const int*
             if (slot < a.cap) my[slot] = j;
         }
         cnt += __popc(bal);
-        // hits among the skin row's first mp entries: the polarizable ones
-        const int lp = min(32, max(0, mp - b));
-        cntp += __popc(bal & (lp == 32 ? 0xffffffffu : ((1u << lp) - 1u)));
+        // hits among the first B entries of the skin row, for the segment ends B
+        auto below = [&](int B) {
+            const int l = min(32, max(0, B - b));
+            return __popc(bal & (l == 32 ? 0xffffffffu : ((1u << l) - 1u)));
+        };
+        cntu += below(up.x);
+        cntp += below(mp);
+        cntn += below(mp + up.y) - below(mp);
     }
     if (lane == 0) {
         nn[i] = min(cnt, a.cap);
         npol[i] = min(cntp, a.cap);
+        nup[i] = make_int2(min(cntu, a.cap), min(cntp + cntn, a.cap) - min(cntp, a.cap));
         if (cnt > a.cap) atomicOr(flag, 1);
     }
 }
@@ -468,6 +480,12 @@ __global__ void k_pol_static(PolArgs a) {
     const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (i >= a.n) return;
+    // the static field is read only at sites that carry a dipole (iter, the residual,
+    // coulomb_polar): the rows of the others (the M sites) are skipped
+    if (!(a.polr2[i] > a.toler) && !(a.polr2[i] > 1e-6)) {
+        if (lane < 3) a.efk[lane * (size_t)a.n + i] = 0.0;
+        return;
+    }
     const int nn = a.nn[i];
     const size_t row = (size_t)i * a.cap, blk = (size_t)a.n * a.cap;
     const bool poli = a.polr2[i] > 1e-6;
@@ -1785,9 +1803,11 @@ __device__ __forceinline__ void smear_flush(const PolArgs& a, int i, const Smear
     const double sm = (dum1d - pow(arob4d, 0.25) * g34d * gq) / rrd * kR4pie0;
     const double qjd = a.q[j];
     const double cicjd = qid * qjd;
-    if (j > i) eng -= cicjd * sm;
+    eng -= cicjd * sm;                      // every queued pair has j > i: its energy once
     aei -= cicjd * 0.5 * sm;
     vsp -= qjd * sm;
+    atomicAdd(a.ae + j, -cicjd * 0.5 * sm);   // the partner's share
+    atomicAdd(a.vesp + j, -qid * sm);
 }
 
 // The mixed path's ewald2p: the same terms as k_pol_ewald2p.  The pair energies stay FP64
@@ -1796,7 +1816,9 @@ __device__ __forceinline__ void smear_flush(const PolArgs& a, int i, const Smear
 // exceed); the forces, the potentials and the dipole terms are FP32 per pair (the B
 // functions from the FP32 table of C_n = B_n + (2n-1)!!/r^(2n+1), free of the cancellation
 // between B_n and the bare 1/r^(2n+1)); separation, cut test and heat entries FP64; every
-// sum FP64.
+// sum FP64.  Every pair is taken once, from its lower site (the rows' j > i segments): the
+// partner's force (the pair forces are antisymmetric), energy half, potential and heat
+// entry go to it by FP64 atomics, which halves the FP64-pipe work of the pair loop.
 __global__ void __launch_bounds__(kThreads) k_pol_ewald2p32(PolArgs a, double g34d, double gln, int heat) {
     __shared__ SmearQueue sq[kThreads / 32];
     const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -1817,12 +1839,16 @@ __global__ void __launch_bounds__(kThreads) k_pol_ewald2p32(PolArgs a, double g3
         const float rdw = (float)(1.0 / a.drewd);
         const double rdwd = a.rdrewd;
         double f[3] = {0, 0, 0}, aei = 0, vsp = 0, engq = 0;
-        for (int b = 0; b < nn; b += 32) {
-            const int k = b + lane;
+        // the partners j > i: [0, up.x) and [npol, npol + up.y) of the row
+        const int2 up = a.nup[i];
+        const int np = a.npol[i], nu = up.x + up.y;
+        for (int b = 0; b < nu; b += 32) {
+            const int v = b + lane;
             bool smear = false;
             int j = 0;
             double rrd = 0.0;
-            if (k < nn) {
+            if (v < nu) {
+                const int k = v < up.x ? v : np + (v - up.x);
                 j = a.nbr[row + k];
                 double dd[3];
                 sep(a, i, j, dd[0], dd[1], dd[2]);
@@ -1930,14 +1956,22 @@ __global__ void __launch_bounds__(kThreads) k_pol_ewald2p32(PolArgs a, double g3
                     f[0] += fx; f[1] += fy; f[2] += fz;
                     aei += 0.5 * edum;
                     vsp += (double)(qj * espdum + rdmuj * espdc);
-                    if (heat) heat_entry(a, i, j, fx, fy, fz, red + 8);
-                    if (j > i) {
-                        const double virdum = (double)(dfx * d[0] + dfy * d[1] + dfz * d[2]);
-                        red[0] += edum;
-                        red[1] += -(double)ffac * rsqd - virdum;
-                        red[2] += dd[0] * fx; red[3] += dd[0] * fy; red[4] += dd[0] * fz;
-                        red[5] += dd[1] * fy; red[6] += dd[1] * fz; red[7] += dd[2] * fz;
+                    // the partner: the opposite force, its energy half, its potential (r_j - r_i =
+                    // -d), its heat entry
+                    atomicAdd(a.fx + j, -fx);
+                    atomicAdd(a.fy + j, -fy);
+                    atomicAdd(a.fz + j, -fz);
+                    atomicAdd(a.ae + j, 0.5 * edum);
+                    atomicAdd(a.vesp + j, (double)(qi * espdum - rdmui * espdc));
+                    if (heat) {
+                        heat_entry(a, i, j, fx, fy, fz, red + 8);
+                        heat_entry(a, j, i, -fx, -fy, -fz, red + 8);
                     }
+                    const double virdum = (double)(dfx * d[0] + dfy * d[1] + dfz * d[2]);
+                    red[0] += edum;
+                    red[1] += -(double)ffac * rsqd - virdum;
+                    red[2] += dd[0] * fx; red[3] += dd[0] * fy; red[4] += dd[0] * fz;
+                    red[5] += dd[1] * fy; red[6] += dd[1] * fz; red[7] += dd[2] * fz;
                 }
             }
             // queue this step's smeared pairs; flush a full queue first
@@ -1964,12 +1998,12 @@ __global__ void __launch_bounds__(kThreads) k_pol_ewald2p32(PolArgs a, double g3
         for (int c = 0; c < 3; ++c) f[c] = warp_sum(f[c]);
         aei = warp_sum(aei);
         vsp = warp_sum(vsp);
-        if (lane == 0) {
-            a.fx[i] += f[0];
-            a.fy[i] += f[1];
-            a.fz[i] += f[2];
-            a.ae[i] += aei;
-            a.vesp[i] += vsp;
+        if (lane == 0) {   // atomics: other rows add their pairs with this site concurrently
+            atomicAdd(a.fx + i, f[0]);
+            atomicAdd(a.fy + i, f[1]);
+            atomicAdd(a.fz + i, f[2]);
+            atomicAdd(a.ae + i, aei);
+            atomicAdd(a.vesp + i, vsp);
         }
     }
     block_sum_atomic<11>(red, a.acc + 0);
@@ -2256,7 +2290,7 @@ cudaError_t launch_msite_redistribute(int nw, double gamma, double* fx, double* 
 }
 
 void PolarState::release() {
-    void* p[] = {ercp, ercp32, nn_s, nbr_s, npol_s, xref, nn, nbr, npol, flag, xf, tens, intra, fld, vesp, ae, eik, kv, kx2, lmn, sf, kterm, acc, kco, fac, md, vh, polr6,
+    void* p[] = {ercp, ercp32, nn_s, nbr_s, npol_s, nup_s, xref, nn, nbr, npol, nup, flag, xf, tens, intra, fld, vesp, ae, eik, kv, kx2, lmn, sf, kterm, acc, kco, fac, md, vh, polr6,
                  ckey, cskey, cidx, csidx, csort, cstart, cend,
                  tens32, r32, d32, e32, kco32, fac32, ktile, kaux, kcol, colk, kpart, cg_x, cg_r, cg_q, cg_z, vh32};
     for (void* q : p)
@@ -2276,6 +2310,7 @@ void PolarState::release() {
     ercp = nullptr;
     ercp32 = nullptr;
     nn_s = nbr_s = npol_s = nullptr;
+    nup_s = nup = nullptr;
     xref = nullptr;
     ns_cap = cap_s_alloc = 0;
     skin_ok = false;
@@ -2395,16 +2430,18 @@ cudaError_t PolarState::reserve_cells(int n, int ncell) {
 cudaError_t PolarState::reserve_skin(int n) {
     cudaError_t e;
     if (n > ns_cap || cap_s != cap_s_alloc) {
-        void* p[] = {nn_s, nbr_s, npol_s, xref};
+        void* p[] = {nn_s, nbr_s, npol_s, nup_s, xref};
         for (void* q : p)
             if (q) cudaFree(q);
         nn_s = nbr_s = npol_s = nullptr;
+        nup_s = nullptr;
         xref = nullptr;
         ns_cap = cap_s_alloc = 0;
         skin_ok = false;
         const size_t m = (size_t)std::max(n, 1);
         if ((e = cudaMalloc(&nn_s, m * sizeof(int)))) return e;
         if ((e = cudaMalloc(&npol_s, m * sizeof(int)))) return e;
+        if ((e = cudaMalloc(&nup_s, m * sizeof(int2)))) return e;
         if ((e = cudaMalloc(&nbr_s, m * cap_s * sizeof(int)))) return e;
         if ((e = cudaMalloc(&xref, 3 * m * sizeof(double)))) return e;
         ns_cap = n;
@@ -2485,18 +2522,20 @@ cudaError_t PolarState::reserve(int nw, int K, size_t nfac) {
     // a capacity is zeroed before its buffers are replaced, so a failed allocation leaves
     // nothing that a later call would take for allocated
     if (n > n_cap || cap != cap_alloc) {
-        void* p[] = {nn, nbr, npol, xf, tens, fld, vesp, ae, md, vh, polr6};
+        void* p[] = {nn, nbr, npol, nup, xf, tens, fld, vesp, ae, md, vh, polr6};
         for (void* q : p)
             if (q) cudaFree(q);
         n_cap = 0;
         cap_alloc = 0;
         nn = nbr = npol = nullptr;
+        nup = nullptr;
         xf = nullptr;
         tens = fld = vesp = ae = vh = polr6 = nullptr;
         md = nullptr;
         const size_t m = (size_t)std::max(n, 1);
         if ((e = cudaMalloc(&nn, m * sizeof(int)))) return e;
         if ((e = cudaMalloc(&npol, m * sizeof(int)))) return e;
+        if ((e = cudaMalloc(&nup, m * sizeof(int2)))) return e;
         if ((e = cudaMalloc(&nbr, m * cap * sizeof(int)))) return e;
         if ((e = cudaMalloc(&xf, m * sizeof(float4)))) return e;
         if ((e = cudaMalloc(&tens, 6 * m * cap * sizeof(double)))) return e;
@@ -2736,6 +2775,7 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
         b.nn = nn;
         b.nbr = nbr;
         b.npol = npol;
+        b.nup = nup;
         b.tens = tens;
         b.tens32 = mixed ? tens32 : nullptr;
         b.intra = intra;
@@ -2817,7 +2857,7 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
     last_n = n;
     const float r2f = (float)((rcut + 0.01) * (rcut + 0.01));
     const float r2in = rcut > 0.02 ? (float)((rcut - 0.01) * (rcut - 0.01)) : 0.f;
-    auto build = [&](int* lnn, int* lnbr, int* lnpol, int rowcap, double lcut) -> cudaError_t {
+    auto build = [&](int* lnn, int* lnbr, int* lnpol, int2* lnup, int rowcap, double lcut) -> cudaError_t {
         // one pass of k_pol_list at cut lcut into (lnn, lnbr); the overflow flag is read by the caller
         cudaError_t err;
         int3 nc = make_int3(1, 1, 1);
@@ -2840,8 +2880,8 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
         }
         const float lf = (float)((lcut + 0.01) * (lcut + 0.01));
         const float li = lcut > 0.02 ? (float)((lcut - 0.01) * (lcut - 0.01)) : 0.f;
-        k_pol_list<<<blocks(32L * n, kThreads), kThreads, 0, s>>>(a, lnn, lnbr, lnpol, rowcap, lcut, xf, lf, li,
-                                                                   flag, nc, cells, csidx, cstart, cend);
+        k_pol_list<<<blocks(32L * n, kThreads), kThreads, 0, s>>>(a, lnn, lnbr, lnpol, lnup, rowcap, lcut, xf, lf,
+                                                                   li, flag, nc, cells, csidx, cstart, cend);
         ++launches;
         return cudaGetLastError();
     };
@@ -2866,8 +2906,8 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
                 if ((e = cudaMemsetAsync(flag, 0, 2 * sizeof(int), s))) return e;
                 k_pol_moved<<<blocks(n, kThreads), kThreads, 0, s>>>(n, x, y, z, xref, cl, 0.25 * skin * skin,
                                                                      flag + 1);
-                k_pol_filter<<<blocks(32L * n, kThreads), kThreads, 0, s>>>(a, nn_s, nbr_s, npol_s, cap_s, nn, nbr,
-                                                                            npol, xf, r2f, r2in, flag);
+                k_pol_filter<<<blocks(32L * n, kThreads), kThreads, 0, s>>>(a, nn_s, nbr_s, npol_s, nup_s, cap_s, nn,
+                                                                            nbr, npol, nup, xf, r2f, r2in, flag);
                 launches += 2;
                 int fh[2];
                 if ((e = read_flags(fh))) return e;
@@ -2889,7 +2929,7 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
             for (;;) {
                 if ((e = cudaMemsetAsync(flag, 0, 2 * sizeof(int), s))) return e;
                 bind(a);
-                if ((e = build(nn_s, nbr_s, npol_s, cap_s, rcut + skin))) return e;
+                if ((e = build(nn_s, nbr_s, npol_s, nup_s, cap_s, rcut + skin))) return e;
                 int fh[2];
                 if ((e = read_flags(fh))) return e;
                 if (!fh[0]) break;
@@ -2912,7 +2952,7 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
         for (;;) {
             bind(a);
             if ((e = cudaMemsetAsync(flag, 0, 2 * sizeof(int), s))) return e;
-            if ((e = build(nn, nbr, npol, cap, rcut))) return e;
+            if ((e = build(nn, nbr, npol, nup, cap, rcut))) return e;
             int fh[2];
             if ((e = read_flags(fh))) return e;
             if (!fh[0]) break;
@@ -2928,7 +2968,7 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
     bindk(k);
     k_pol_polr6<<<blocks(n, kThreads), kThreads, 0, s>>>(a, polr6);
     k_pol_static<<<blocks(32L * n, kThreads), kThreads, 0, s>>>(a);
-    k_pol_intra_static<<<blocks(nw, kThreads), kThreads, 0, s>>>(a);
+    k_pol_intra_static<<<blocks(nw, 32), 32, 0, s>>>(a);   // one-warp blocks: every SM
     launches += 3;
     k_pol_mask<<<blocks(n, kThreads), kThreads, 0, s>>>(a, md);
     ++launches;
@@ -2938,10 +2978,9 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
             Kg[c] = spme_grid[0] > 0 ? spme_grid[c] : spme_smooth_even(wc[c] / spme_spacing);
         for (int c = 0; c < 3; ++c) spme_K_last[c] = Kg[c];
         if ((e = spme.prepare(cl.c, alpha, spme_order, Kg, mixed, heat ? 9 : 1, s))) return e;
-        if (mixed) {   // the FP32 passes' site frame for this call's positions
-            if ((e = spme.frame32(n, x, y, z, s))) return e;
-            ++launches;
-        }
+        // the site frame of this call's positions (grid indices, FP32 fractions, FP64 splines)
+        if ((e = spme.frame(n, x, y, z, s))) return e;
+        ++launches;
     }
     if (K) {
         k_pol_factors<<<blocks(n, kThreads), kThreads, 0, s>>>(k, x, y, z);
@@ -3052,7 +3091,9 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
         // z = M^-1 rho into cg_z, rho.z into acc[slot] (and the first direction); `pre`
         // Jacobi sweeps (odd: the polynomial is positive definite for every eigenvalue of
         // D^-1 T_real below 1, which the dipole equations guarantee)
-        int pre = precond_sweeps | 1;
+        // with SPME a CG sweep's k space is cheap beside two more real-space sweeps: the
+        // diagonal; with the Ewald sum the polynomial's fewer sweeps pay
+        int pre = (precond_sweeps > 0 ? precond_sweeps : (spme_on ? 1 : 3)) | 1;
         auto precondition = [&](int slot, int dir) -> cudaError_t {
             k_pcg_jacobi<<<blocks(n, kThreads), kThreads, 0, s>>>(a, m, nullptr, cg_z);
             for (int q = 1; q < pre; ++q) {
@@ -3240,8 +3281,9 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
         k_pol_ewald2p32<<<blocks(32L * n, kThreads), kThreads, 0, s>>>(a, g34, gammln(0.75), heat);
     else
         k_pol_ewald2p<<<blocks(32L * n, kThreads), kThreads, 0, s>>>(a, g34, heat);
-    k_pol_ewald3p<<<blocks(nw, kThreads), kThreads, 0, s>>>(a, heat);
-    k_pol_qdforce<<<blocks(nw, kThreads), kThreads, 0, s>>>(a, heat);
+    // thread per water, FP64-latency bound: one-warp blocks spread them over every SM
+    k_pol_ewald3p<<<blocks(nw, 32), 32, 0, s>>>(a, heat);
+    k_pol_qdforce<<<blocks(nw, 32), 32, 0, s>>>(a, heat);
     k_pol_jkin<<<blocks(n, kThreads), kThreads, 0, s>>>(a, ae_out, heat);
     launches += 5;
     if (K) {

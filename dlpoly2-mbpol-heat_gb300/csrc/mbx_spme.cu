@@ -273,7 +273,12 @@ struct SpArgs {
     const int4* sib;
     const float4* sw;
     float jac32[9];
+    // FP64 kernels: the per-call spline table, per site [axis][th, d1, d2][kSplStride]
+    const double* spl;
 };
+
+constexpr int kSplStride = 8;                    // entries per (axis, kind): orders up to 8
+constexpr int kSplSite = 3 * 3 * kSplStride;     // doubles per site
 
 // M_p(w + j), j = 0..p-1, for w in [0, 1) (bspgen's values bspx(i, j + 1)), and with
 // ND >= 1 (2) the first (second) derivatives.  Recursion over the order from M_2:
@@ -328,26 +333,53 @@ __device__ __forceinline__ void site_splines(const SpArgs& s, double x, double y
     }
 }
 
-// The site frame of the FP32 passes, once per call: floor(t_a) mod K_a and t_a - floor(t_a)
-// (FP64, rounded to FP32: 6e-8 absolute in the fraction) for every site.
+// The site frame, once per call: per site floor(t_a) mod K_a, for the FP32 passes the
+// fraction t_a - floor(t_a) (FP64, rounded to FP32: 6e-8 absolute), and for the FP64 passes
+// the B-spline values with their first and second derivatives (the table site_splines
+// would compute in every lane of every FP64 spread and gather).  Thread per (site, axis).
+template <int P>
 __global__ void k_spme_frame(SpArgs s, const double* __restrict__ x, const double* __restrict__ y,
-                             const double* __restrict__ z, int4* __restrict__ sib, float4* __restrict__ sw) {
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+                             const double* __restrict__ z, int4* __restrict__ sib, float4* __restrict__ sw,
+                             double* __restrict__ spl) {
+    const long t3 = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    const int j = (int)(t3 / 3), a = (int)(t3 % 3);
     if (j >= s.n) return;
-    const int Ka[3] = {s.K1, s.K2, s.K3};
-    int ib[3];
-    float w[3];
+    const int Ka = a == 0 ? s.K1 : (a == 1 ? s.K2 : s.K3);
+    const double t = (double)Ka * (s.rc[a] * x[j] + s.rc[a + 3] * y[j] + s.rc[a + 6] * z[j] + 0.5);
+    const double fl = floor(t);
+    long long b = (long long)fl % Ka;
+    if (b < 0) b += Ka;
+    reinterpret_cast<int*>(sib + j)[a] = (int)b;
+    reinterpret_cast<float*>(sw + j)[a] = (float)(t - fl);
+    double th[P], d1[P], d2[P];
+    bspline<double, P, 2>(t - fl, th, d1, d2);
+    double* o = spl + (size_t)j * kSplSite + a * 3 * kSplStride;
+#pragma unroll
+    for (int q = 0; q < P; ++q) {
+        o[q] = th[q];
+        o[kSplStride + q] = d1[q];
+        o[2 * kSplStride + q] = d2[q];
+    }
+}
+
+// site_splines of the FP64 passes from the per-call table (the same values)
+template <int P, int ND>
+__device__ __forceinline__ void site_splines_tab(const SpArgs& s, int j, int (&gi)[3][P], double (&th)[3][P],
+                                                 double (&d1)[3][P], double (&d2)[3][P]) {
+    const int4 ib = s.sib[j];
+    const int Ka[3] = {s.K1, s.K2, s.K3}, b[3] = {ib.x, ib.y, ib.z};
+    const double* row = s.spl + (size_t)j * kSplSite;
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-        const double t = (double)Ka[a] * (s.rc[a] * x[j] + s.rc[a + 3] * y[j] + s.rc[a + 6] * z[j] + 0.5);
-        const double fl = floor(t);
-        long long b = (long long)fl % Ka[a];
-        if (b < 0) b += Ka[a];
-        ib[a] = (int)b;
-        w[a] = (float)(t - fl);
+#pragma unroll
+        for (int q = 0; q < P; ++q) {
+            const int g = b[a] - q;
+            gi[a][q] = g < 0 ? g + Ka[a] : g;
+            th[a][q] = row[a * 3 * kSplStride + q];
+            if (ND >= 1) d1[a][q] = row[a * 3 * kSplStride + kSplStride + q];
+            if (ND >= 2) d2[a][q] = row[a * 3 * kSplStride + 2 * kSplStride + q];
+        }
     }
-    sib[j] = make_int4(ib[0], ib[1], ib[2], 0);
-    sw[j] = make_float4(w[0], w[1], w[2], 0.f);
 }
 
 // site_splines of the FP32 passes from the site frame (no FP64 arithmetic per lane)
@@ -441,7 +473,8 @@ __global__ void __launch_bounds__(kSpThreads) k_spme_spread(SpArgs s, const doub
 #pragma unroll
         for (int a = 0; a < 3; ++a) mt[a] = s.jac32[3 * a] * d.x + s.jac32[3 * a + 1] * d.y + s.jac32[3 * a + 2] * d.z;
     } else {
-        site_splines<T, P, 1>(s, x[j], y[j], z[j], gi, th, d1, d2);
+        if constexpr (sizeof(T) == 8) site_splines_tab<P, 1>(s, j, gi, th, d1, d2);
+        else site_splines<T, P, 1>(s, x[j], y[j], z[j], gi, th, d1, d2);
         double mxd = 0, myd = 0, mzd = 0;
         if (!polr2 || polr2[j] > 1e-6) dip_of(dv, j, mxd, myd, mzd);
         to_t<T>(s, mxd, myd, mzd, mt);
@@ -481,7 +514,7 @@ __global__ void __launch_bounds__(kSpThreads) k_spme_spread_heat(SpArgs s, const
     if (j >= s.n || jz >= P) return;
     int gi[3][P];
     double th[3][P], d1[3][P], d2[3][P];
-    site_splines<double, P, 0>(s, x[j], y[j], z[j], gi, th, d1, d2);
+    site_splines_tab<P, 0>(s, j, gi, th, d1, d2);
     double w[16];
     const double4 m = md[j];
     w[0] = m.x;
@@ -535,7 +568,7 @@ __global__ void __launch_bounds__(kSpThreads) k_spme_field(SpArgs s, const doubl
         int gi[3][P];
         T th[3][P], d1[3][P], d2[3][P];
         if constexpr (sizeof(T) == 4) site_splines32<P, 1>(s, j, gi, th, d1, d2);
-        else site_splines<T, P, 1>(s, x[j], y[j], z[j], gi, th, d1, d2);
+        else site_splines_tab<P, 1>(s, j, gi, th, d1, d2);
         const size_t K12 = (size_t)s.K1 * s.K2;
         const C* plane = grid + pick(gi[2], jz) * K12;
         const T tz = pick(th[2], jz), dz = pick(d1[2], jz);
@@ -611,7 +644,7 @@ __global__ void __launch_bounds__(kSpThreads) k_spme_final_gather(SpArgs s, cons
         if (jz < P) {
             int gi[3][P];
             double th[3][P], d1[3][P], d2[3][P];
-            site_splines<double, P, 2>(s, x[j], y[j], z[j], gi, th, d1, d2);
+            site_splines_tab<P, 2>(s, j, gi, th, d1, d2);
             double mt[3];
             to_t<double>(s, m.x, m.y, m.z, mt);
             const size_t K12 = (size_t)s.K1 * s.K2;
@@ -954,6 +987,7 @@ SpArgs sp_args(const SpmeState& st, int n) {
     a.stop = nullptr;
     a.sib = st.sib;
     a.sw = st.sw;
+    a.spl = st.spl;
     for (int i = 0; i < 9; ++i) {
         a.rc[i] = st.rc[i];
         a.jac[i] = st.jac[i];
@@ -988,11 +1022,12 @@ int spme_smooth_even(double x) {
 SpmeState::~SpmeState() { release(); }
 
 void SpmeState::release() {
-    void* p[] = {G, G32, tw, tw32, grid, grid32, part, sib, sw};
+    void* p[] = {G, G32, tw, tw32, grid, grid32, part, sib, sw, spl};
     for (void* q : p)
         if (q) cudaFree(q);
     sib = nullptr;
     sw = nullptr;
+    spl = nullptr;
     site_cap = 0;
     G = nullptr;
     G32 = nullptr;
@@ -1206,20 +1241,26 @@ cudaError_t SpmeState::field64(int n, const double* x, const double* y, const do
     return cudaGetLastError();
 }
 
-cudaError_t SpmeState::frame32(int n, const double* x, const double* y, const double* z, cudaStream_t s) {
+cudaError_t SpmeState::frame(int n, const double* x, const double* y, const double* z, cudaStream_t s) {
     cudaError_t e;
     if (!order) return cudaErrorInvalidValue;
     if (n > site_cap) {
         if (sib) cudaFree(sib);
         if (sw) cudaFree(sw);
+        if (spl) cudaFree(spl);
         sib = nullptr;
         sw = nullptr;
+        spl = nullptr;
         site_cap = 0;
         if ((e = cudaMalloc(&sib, (size_t)n * sizeof(int4)))) return e;
         if ((e = cudaMalloc(&sw, (size_t)n * sizeof(float4)))) return e;
+        if ((e = cudaMalloc(&spl, (size_t)n * kSplSite * sizeof(double)))) return e;
         site_cap = n;
     }
-    if (n > 0) k_spme_frame<<<nblocks(n, 256), 256, 0, s>>>(sp_args(*this, n), x, y, z, sib, sw);
+    if (n > 0) {
+        const SpArgs sa = sp_args(*this, n);
+        SPME_ORDER_SWITCH(order, (k_spme_frame<P_><<<nblocks(3L * n, 256), 256, 0, s>>>(sa, x, y, z, sib, sw, spl)));
+    }
     return cudaGetLastError();
 }
 

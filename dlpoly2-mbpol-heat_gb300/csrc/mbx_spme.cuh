@@ -78,8 +78,9 @@ struct SpmeState {
     float2* tw32 = nullptr;
     double2* grid = nullptr;       // complex grids, ngrid_cap of them
     float2* grid32 = nullptr;
-    int4* sib = nullptr;           // FP32 passes: per site floor(t_a) mod K_a (frame32)
-    float4* sw = nullptr;          //   and t_a - floor(t_a)
+    int4* sib = nullptr;           // per site floor(t_a) mod K_a (frame)
+    float4* sw = nullptr;          //   FP32 passes: t_a - floor(t_a)
+    double* spl = nullptr;         //   FP64 passes: B-spline values and derivatives per axis
     int site_cap = 0;
     double* part = nullptr;        // per-block partial sums of the k-vector terms
     size_t g_cap = 0, part_cap = 0;
@@ -101,8 +102,9 @@ struct SpmeState {
     cudaError_t field64(int n, const double* x, const double* y, const double* z, const double* q,
                         const double4* md, const double* polr2, const double* mx, const double* my,
                         const double* mz, double sfac, double dum, double* efm, double* efc, cudaStream_t s);
-    // The site frame of the FP32 passes for these positions (once per call, before field32).
-    cudaError_t frame32(int n, const double* x, const double* y, const double* z, cudaStream_t s);
+    // The site frame for these positions (once per call, after prepare and before any spread
+    // or gather): grid indices, FP32 fractions and the FP64 spline table.
+    cudaError_t frame(int n, const double* x, const double* y, const double* z, cudaStream_t s);
     // The same in FP32 for the correction solve: e32k = (polr2 > 1e-6 ? field(d) : 0) + dum d.
     // stop (device, or null): when nonzero the kernels return at once (a CG solve that has
     // stopped while further sweeps were queued).

@@ -74,6 +74,12 @@ int mbx_set_mixed_limits(mbx_context* ctx, double limit2b, double limit3b);
  * differently in the two kernels). */
 int mbx_set_fused(mbx_context* ctx, int on);
 
+/* The fused launch's split of each 384-thread block: dimer_warps of its 12 warps start on the
+ * FP64 dimers, the rest on the FP32 trimers (either queue's warps take the other's work when
+ * theirs runs dry).  0 = the default (4, one per SM sub-partition); 1..11 otherwise.  A
+ * tuning knob: the split changes timings, and results only in the order of FP64 atomics. */
+int mbx_set_fused_split(mbx_context* ctx, int dimer_warps);
+
 /*
  * MB-pol 2B + 3B forces with the heat-current bookkeeping.
  * Replaces mbpol_forces (SOURCE/mbpol.f90:98-449, called from SOURCE/dlpoly_cmd.f:2504)
@@ -356,7 +362,9 @@ int mbx_water_step_device(mbx_context* ctx, int precision, int imcon, const doub
  */
 int mbx_set_lanes(mbx_context* ctx, int lanes);
 /* MBX_MIXED dipole solve: Jacobi sweeps of the conjugate-gradient preconditioner on the
- * real-space part of the dipole equations, odd 1..9 (1: the diagonal alone; default 3).
+ * real-space part of the dipole equations, odd 1..9 (1: the diagonal alone), or 0 (the
+ * default): 1 with SPME, whose k space makes a CG sweep cheap beside two more real-space
+ * sweeps, 3 with the Ewald sum.
  * An odd count keeps the preconditioner positive definite; a breakdown or an outer step
  * that does not halve the residual falls back to the diagonal.  Changes the iteration
  * count, not the converged dipoles beyond the dipole tolerance. */

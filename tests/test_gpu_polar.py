@@ -185,8 +185,8 @@ def test_polar_phase_timings(mbx_ctx, oracle_lib):
 
 
 def test_polar_mixed_preconditioner_settings(mbx_ctx, oracle_lib):
-    """The mixed solve's preconditioner (mbx_set_precond_sweeps: 1 diagonal, 3 default, 5)
-    changes the iteration count, not the converged results beyond the mixed budgets; even
+    """The mixed solve's preconditioner (mbx_set_precond_sweeps: 0 automatic, 1 diagonal, 3,
+    5) changes the iteration count, not the converged results beyond the mixed budgets; even
     counts (not positive definite in general) are refused."""
     box = systems.config0()
     prm = systems.polar_params(alpha=0.3, rcut=9.0, kmax=(8, 8, 8), toler_debye=1e-8)
@@ -196,7 +196,7 @@ def test_polar_mixed_preconditioner_settings(mbx_ctx, oracle_lib):
         mbx_ctx.set_precond_sweeps(2)
     sweeps = {}
     try:
-        for p in (1, 3, 5):
+        for p in (0, 1, 3, 5):
             mbx_ctx.set_precond_sweeps(p)
             got = mbx_ctx.polar(sites, box.cell, box.imcon, box.nw, q, dp, polr, polr2, prm, vel=box.vel,
                                 precision=capi.MIXED)
@@ -206,8 +206,9 @@ def test_polar_mixed_preconditioner_settings(mbx_ctx, oracle_lib):
             f, fr = got["forces"], ref["forces"]
             assert np.sqrt(np.mean((f - fr) ** 2)) <= 1e-6 * np.sqrt(np.mean(fr ** 2))
     finally:
-        mbx_ctx.set_precond_sweeps(3)
+        mbx_ctx.set_precond_sweeps(0)
     assert min(sweeps.values()) > 0
+    assert sweeps[0] == sweeps[3]   # automatic with the Ewald sum: the 3-sweep polynomial
 
 
 @pytest.mark.parametrize("precision", [capi.FP64, capi.MIXED])
