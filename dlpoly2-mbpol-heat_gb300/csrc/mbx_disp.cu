@@ -245,7 +245,7 @@ __global__ void __launch_bounds__(kThreads) k_disp_forces(DispArgs a, const int*
     double red[14];
 #pragma unroll
     for (int q = 0; q < 14; ++q) red[q] = 0.0;
-    double fi[3] = {0.0, 0.0, 0.0};
+    double fi[3] = {0.0, 0.0, 0.0}, aei = 0.0;
     if (i < a.natms) {   // warp-uniform
         const int n = nn[i];
         const int ti = a.ltype[i];
@@ -282,8 +282,8 @@ __global__ void __launch_bounds__(kThreads) k_disp_forces(DispArgs a, const int*
             atomicAdd(a.fy + j, -f1);
             atomicAdd(a.fz + j, -f2);
             red[0] += e;
-            if (a.ae) {
-                atomicAdd(a.ae + i, 0.5 * e);
+            if (a.ae) {   // the row's half summed per lane, the partner's by an atomic
+                aei += 0.5 * e;
                 atomicAdd(a.ae + j, 0.5 * e);
             }
             red[1] -= gamma * rsq;
@@ -299,11 +299,13 @@ __global__ void __launch_bounds__(kThreads) k_disp_forces(DispArgs a, const int*
         }
 #pragma unroll
         for (int c = 0; c < 3; ++c) fi[c] = warp_sum(fi[c]);
+        aei = warp_sum(aei);
         if (lane == 0 && (fi[0] != 0.0 || fi[1] != 0.0 || fi[2] != 0.0)) {
             atomicAdd(a.fx + i, fi[0]);
             atomicAdd(a.fy + i, fi[1]);
             atomicAdd(a.fz + i, fi[2]);
         }
+        if (lane == 0 && a.ae && aei != 0.0) atomicAdd(a.ae + i, aei);
     }
     block_sum_atomic<14>(red, a.acc14);
 }
