@@ -411,6 +411,15 @@ def run_ours(args, rank, world):
         pre_ms[p_] = 1e3 * t_ / 4
     best_pre = min(pre_ms, key=pre_ms.get)
     ctx.set_precond_sweeps(best_pre)
+    # the MB-pol terms beside the dipole solve (mbx_set_overlap) or after it: off, or on with
+    # 3, 4 or 5 of the 8-warp fused kernel's warps on the dimers
+    ovl_ms = {}
+    for key_, on_, w_ in (("off", False, 0), ("on_3", True, 3), ("on_4", True, 4), ("on_5", True, 5)):
+        ctx.set_overlap(on_, w_)
+        t_, _, _, _ = timed(capi.MIXED, 4, 2)
+        ovl_ms[key_] = 1e3 * t_ / 4
+    best_ovl = min(ovl_ms, key=ovl_ms.get)
+    ctx.set_overlap(best_ovl != "off", 0 if best_ovl == "off" else int(best_ovl[-1]))
 
     clocks = ClockSampler(dev.index)
     clocks.start()
@@ -577,6 +586,11 @@ def run_ours(args, rank, world):
                                              "jkin": phase_prof[3]},
                                 "fp64_phase_ms": {"lists": phase64[0], "2b": phase64[1], "3b": phase64[2],
                                                   "jkin": phase64[3]}},
+        "overlap_tuning": {"mixed_step_ms": ovl_ms, "chosen": best_ovl,
+                           "method": "the MB-pol terms after the electrostatics (off) or on a second stream "
+                                     "beside the dipole solve with n of 8 warps on the dimers (on_n), each timed "
+                                     "on 4 warm-started MD steps (CUDA events), the fastest used for every "
+                                     "measurement of the run"},
         "precond_tuning": {"mixed_step_ms_by_jacobi_sweeps": {str(k): v for k, v in pre_ms.items()},
                            "chosen_sweeps": best_pre,
                            "method": "each preconditioner timed on 4 warm-started MD steps of this box "

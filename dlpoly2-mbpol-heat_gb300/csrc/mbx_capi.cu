@@ -43,6 +43,12 @@ struct mbx_context {
     // 2B and 3B in one persistent launch (launch_23) where it applies; 0 = separate kernels
     int fused = 1;
     int fused_split = 0;            // dimer warps of the 12 per block (0: the default, 4)
+    // the whole step (mbx_water_step*): the MB-pol terms on a second stream, beside the
+    // electrostatics' FP32 CG sweeps (mbx_set_overlap)
+    int overlap = 0;
+    int overlap_split = 0;          // dimer warps of the 8-warp block (0: 4)
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     int nsm = 0;                    // SMs of the device (the persistent grid)
     int* fuse_ctr = nullptr;        // device [2]: work counters of the persistent kernel
     double* part2 = nullptr;        // split FP64 dimers: per-chunk partial sums (pairs_cap dimers)
@@ -188,10 +194,16 @@ double* host_stage(mbx_context* ctx, size_t n) {
 }
 
 // The whole MB-pol evaluation on device arrays.
+int finish_mbpol(mbx_context* ctx, int precision, int nw, double* scalars);
+
+// The 1-body-free MB-pol terms on ctx->stream.  wait: read the scalars back (the stream is
+// synchronised); otherwise the work is only enqueued and finish_mbpol reads them later, and
+// jkin (which reads every term's per-atom energy) is left to the caller.  shared_sm: the
+// fused kernel in its 8-warp form, to share the SMs with other work.
 int run_mbpol(mbx_context* ctx, int precision, const Cell& cl, int nw, const int* list_dev, int natms,
               const double* x, const double* y, const double* z, double* fx, double* fy, double* fz,
               const double* vx, const double* vy, const double* vz, const double* mass, double* ae,
-              double* scalars) {
+              double* scalars, bool wait = true, bool shared_sm = false) {
     if (precision != MBX_FP64 && precision != MBX_MIXED)
         return fail(ctx, MBX_ERR_ARG, "precision must be MBX_FP64 or MBX_MIXED");
     if (nw < 0 || natms < 3 * nw) return fail(ctx, MBX_ERR_ARG, "bad sizes nw=%d natms=%d", nw, natms);
@@ -270,7 +282,8 @@ int run_mbpol(mbx_context* ctx, int precision, const Cell& cl, int nw, const int
         MixedPass mp{ctx->hard2, ctx->hard3, ctx->hard_count, ctx->limit2, ctx->limit3};
         if (ctx->fused && fused_applies(precision, mp)) {
             CK(launch_23(a, ctx->pairs, (int)np, nullptr, ctx->trip, (int)nt, nullptr, precision, ctx->fuse_ctr,
-                         ctx->nsm, s, ctx->part2, ctx->done2, ctx->pairs_cap, ctx->fused_split));
+                         ctx->nsm, s, ctx->part2, ctx->done2, ctx->pairs_cap,
+                         shared_sm ? ctx->overlap_split : ctx->fused_split, shared_sm));
             if (ctx->profiling) {
                 CK(cudaEventRecord(ctx->ev[2], s));
                 CK(cudaEventRecord(ctx->ev[3], s));
@@ -289,11 +302,18 @@ int run_mbpol(mbx_context* ctx, int precision, const Cell& cl, int nw, const int
     } else if (ctx->profiling) {
         for (int q = 1; q < 4; ++q) CK(cudaEventRecord(ctx->ev[q], s));
     }
-    if (heat && mass) {
+    if (heat && mass && wait) {
         CK(launch_jkin(3 * nw, vx, vy, vz, mass, ae_use, ctx->acc, s));
         ctx->launches += nw > 0;
     }
     if (ctx->profiling) CK(cudaEventRecord(ctx->ev[4], s));
+    if (!wait) return MBX_OK;
+    return finish_mbpol(ctx, precision, nw, scalars);
+}
+
+// The scalars of run_mbpol (its stream is the context's stream when it was enqueued).
+int finish_mbpol(mbx_context* ctx, int precision, int nw, double* scalars) {
+    cudaStream_t s = ctx->stream;
     CK(cudaMemcpyAsync(ctx->acc_h, ctx->acc, MBX_NSCALARS * sizeof(double), cudaMemcpyDeviceToHost, s));
     if (precision == MBX_MIXED && nw >= 2)
         CK(cudaMemcpyAsync(ctx->totals_h + 4, ctx->hard_count, 2 * sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -517,6 +537,12 @@ extern "C" void mbx_destroy(mbx_context* ctx) {
     ctx->lb.release();
     for (cudaEvent_t e : ctx->ev)
         if (e) cudaEventDestroy(e);
+    if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
+    if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
+    if (ctx->side) {
+        cudaStreamSynchronize(ctx->side);
+        cudaStreamDestroy(ctx->side);
+    }
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
     delete ctx;
 }
@@ -1055,10 +1081,45 @@ int water_step_core(mbx_context* ctx, int precision, int imcon, const double* ce
     // the electrostatic per-site energies stay apart: their jkin carries them with the
     // M-site redistribution
     ctx->polar.profiling = ctx->profiling != 0;
+    // overlapped form: the MB-pol 2B/3B terms (positions only) on the side stream, launched
+    // when the mixed solve starts its FP32 CG sweeps, in the 8-warp fused kernel that leaves
+    // room on every SM for the CG kernels; the final pass waits for it
+    const MixedPass mpq{ctx->hard2, ctx->hard3, ctx->hard_count, ctx->limit2, ctx->limit3};
+    const bool overlap = ctx->overlap && precision == MBX_MIXED && nw >= 2 && ctx->fused &&
+                         fused_applies(precision, mpq);
+    int mb_rc = MBX_OK;
+    if (overlap) {
+        if (!ctx->side) CK(cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking));
+        if (!ctx->ev_fork) CK(cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming));
+        if (!ctx->ev_join) CK(cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming));
+        ctx->polar.fork_hook = [&]() -> cudaError_t {
+            cudaError_t e;
+            if ((e = cudaEventRecord(ctx->ev_fork, s))) return e;
+            if ((e = cudaStreamWaitEvent(ctx->side, ctx->ev_fork, 0))) return e;
+            ctx->stream = ctx->side;
+            mb_rc = run_mbpol(ctx, precision, cl, nw, d_lst, natms, dx, dy, dz, dfx, dfy, dfz, heat ? dvx : nullptr,
+                              heat ? dvy : nullptr, heat ? dvz : nullptr, heat ? dm : nullptr, dae, sc, false, true);
+            ctx->stream = s;
+            if (mb_rc) return cudaErrorUnknown;
+            return cudaEventRecord(ctx->ev_join, ctx->side);
+        };
+        ctx->polar.join_hook = [&]() -> cudaError_t { return cudaStreamWaitEvent(s, ctx->ev_join, 0); };
+    }
     const cudaError_t pe = ctx->polar.run(precision, cl, prm, nw, dx, dy, dz, dq, ddq, dpr, dpr2, dmx, dmy, dmz, dfx,
                                           dfy, dfz, daep, heat ? dvx : nullptr, heat ? dvy : nullptr,
                                           heat ? dvz : nullptr, sp, jp, jk, s);
+    ctx->polar.fork_hook = nullptr;
+    ctx->polar.join_hook = nullptr;
+    if (mb_rc) return mb_rc;
     if (pe != cudaSuccess) return polar_failed(ctx, pe);
+    if (overlap) {   // the MB-pol scalars (the side stream has finished with the join)
+        CK(cudaStreamWaitEvent(s, ctx->ev_join, 0));
+        ctx->stream = ctx->side;
+        const int frc = finish_mbpol(ctx, precision, nw, sc);
+        ctx->stream = s;
+        if (frc) return frc;
+    }
+    const long mb_launches = overlap ? ctx->launches : 0;
     for (int c = 0; c < 3; ++c) {
         sp[16 + c] = jp[c];
         sp[19 + c] = jk[c];
@@ -1074,9 +1135,21 @@ int water_step_core(mbx_context* ctx, int precision, int imcon, const double* ce
                                     sc + MBX_NSCALARS + 14);
         if (rc) return rc;
     }
-    rc = run_mbpol(ctx, precision, cl, nw, d_lst, natms, dx, dy, dz, dfx, dfy, dfz, heat ? dvx : nullptr,
-                   heat ? dvy : nullptr, heat ? dvz : nullptr, heat ? dm : nullptr, dae, sc);
-    if (rc) return rc;
+    if (!overlap) {
+        rc = run_mbpol(ctx, precision, cl, nw, d_lst, natms, dx, dy, dz, dfx, dfy, dfz, heat ? dvx : nullptr,
+                       heat ? dvy : nullptr, heat ? dvz : nullptr, heat ? dm : nullptr, dae, sc);
+        if (rc) return rc;
+    } else {
+        ctx->launches = mb_launches;
+        if (heat) {   // jkin once every term's per-atom energy is in (the sequential form's last step)
+            CK(cudaMemsetAsync(ctx->acc, 0, MBX_NSCALARS * sizeof(double), s));
+            CK(launch_jkin(3 * nw, dvx, dvy, dvz, dm, dae, ctx->acc, s));
+            CK(cudaMemcpyAsync(ctx->acc_h, ctx->acc, MBX_NSCALARS * sizeof(double), cudaMemcpyDeviceToHost, s));
+            CK(cudaStreamSynchronize(s));
+            for (int c = 0; c < 3; ++c) sc[S_JKIN + c] += ctx->acc_h[S_JKIN + c];
+            ++ctx->launches;
+        }
+    }
     CK(launch_msite_redistribute(nw, gamma, dfx, dfy, dfz, s));
     // device atomic energies: the electrostatic part joins the others for the caller
     ctx->launches += polar_launches + 3;   // + 1-body + M sites + redistribution
@@ -1654,6 +1727,13 @@ extern "C" int mbx_set_fused(mbx_context* ctx, int on) {
 extern "C" int mbx_set_fused_split(mbx_context* ctx, int dimer_warps) {
     if (!ctx || dimer_warps < 0 || dimer_warps > 11) return MBX_ERR_ARG;
     ctx->fused_split = dimer_warps;
+    return MBX_OK;
+}
+
+extern "C" int mbx_set_overlap(mbx_context* ctx, int on, int dimer_warps) {
+    if (!ctx || dimer_warps < 0 || dimer_warps > 7) return MBX_ERR_ARG;
+    ctx->overlap = on ? 1 : 0;
+    ctx->overlap_split = dimer_warps;
     return MBX_OK;
 }
 

@@ -4,6 +4,7 @@
 #include "mbx_common.cuh"
 #include "mbx_spme.cuh"
 
+#include <functional>
 #include <vector>
 
 namespace mbx {
@@ -70,7 +71,8 @@ bool fused_applies(int precision, const MixedPass& mp);
 int dimer_parts();
 cudaError_t launch_23(const MbpolArgs& a, const int2* pairs, int n2, const int* n2_dev, const int4* trip, int n3,
                       const int* n3_dev, int precision, int* ctr, int nsm, cudaStream_t s,
-                      double* partial = nullptr, int* done = nullptr, long part_cap = 0, int dimer_warps = 0);
+                      double* partial = nullptr, int* done = nullptr, long part_cap = 0, int dimer_warps = 0,
+                      bool shared_sm = false);
 // Isolated polynomial + model evaluation for explicit clusters (the per-call ABI).
 cudaError_t launch_2b_direct(int n, const double* w1, const double* w2, double* E, double* g1, double* g2,
                              int precision, cudaStream_t s);
@@ -302,6 +304,11 @@ struct PolarState {
     // energies (ae_out, may be null), jpot and jkin are ACCUMULATED; the dipoles are
     // updated in place; out16 as mbx_polar_forces.  `converged` tells whether the dipole
     // iteration reached toler within maxit iterations.
+    // Optional hooks of the mixed solve, for work the caller runs beside it: fork_hook is
+    // called once, when the first FP32 CG solve is about to be enqueued (or before the final
+    // pass if none is), join_hook before the final pass (the caller's work must be done
+    // before it: both add to the force arrays).
+    std::function<cudaError_t()> fork_hook, join_hook;
     cudaError_t run(int precision, const Cell& cl, const double* prm, int nw, const double* x, const double* y,
                     const double* z,
                     const double* q, const double* dp, const double* polr, const double* polr2, double* mx,

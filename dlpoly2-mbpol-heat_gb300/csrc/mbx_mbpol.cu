@@ -753,10 +753,13 @@ __global__ void __launch_bounds__(kThreads) k_mbpol_3b(MbpolArgs a, const int4* 
 // 4+4 warps at 255 registers 5.2 ms).  Work is claimed 32 tasks at a time from ctr[0]
 // (dimers) and ctr[1] (trimers), which start at zero.
 constexpr int kFusedThreads = 384;
+// The block of the overlapped form (mbx_set_overlap): 8 warps at <= 168 registers, 43K of an
+// SM's 64K registers, so the electrostatics' FP32 CG kernels fit beside it on every SM.
+constexpr int kFusedThreadsShared = 256;
 constexpr int kFusedDimerWarps = 4;   // the default split (dimer_warps 0)
 
-template <typename T2, typename T3>
-__global__ void __launch_bounds__(kFusedThreads, 1)
+template <typename T2, typename T3, int NT>
+__global__ void __launch_bounds__(NT, 1)
     k_mbpol_23(MbpolArgs a, const int2* __restrict__ pairs, int n2, const int* __restrict__ n2_dev,
                const int4* __restrict__ trip, int n3, const int* __restrict__ n3_dev, int* ctr,
                double* partial, int* done, long part_cap, int dimer_warps) {
@@ -813,7 +816,7 @@ __global__ void __launch_bounds__(kFusedThreads, 1)
             for (int q = 0; q < 15; ++q) red[q] = 0.0;
         }
     }
-    if (!a.acc_box) flush_block_n<kFusedThreads, 15>(red, a.acc, S_E3);
+    if (!a.acc_box) flush_block_n<NT, 15>(red, a.acc, S_E3);
 }
 
 // Per-call model evaluation (drop-in for mbpol_2b_poly_/mbpol_3b_poly_ over many clusters).
@@ -1153,16 +1156,21 @@ int dimer_parts() { return kPoly2BF64Parts; }
 
 cudaError_t launch_23(const MbpolArgs& a, const int2* pairs, int n2, const int* n2_dev, const int4* trip, int n3,
                       const int* n3_dev, int precision, int* ctr, int nsm, cudaStream_t s, double* partial,
-                      int* done, long part_cap, int dimer_warps) {
+                      int* done, long part_cap, int dimer_warps, bool shared_sm) {
+    const int nt = shared_sm ? kFusedThreadsShared : kFusedThreads;
     if (dimer_warps <= 0) dimer_warps = kFusedDimerWarps;
-    if (dimer_warps >= kFusedThreads / 32) return cudaErrorInvalidValue;
+    if (dimer_warps >= nt / 32) return cudaErrorInvalidValue;
     cudaError_t e = cudaMemsetAsync(ctr, 0, 2 * sizeof(int), s);
     if (e) return e;
     if (precision == 0) return cudaErrorInvalidValue;   // see fused_applies
     if (!partial || !done) part_cap = 0;
     if (part_cap > 0 && (e = cudaMemsetAsync(done, 0, (size_t)part_cap * sizeof(int), s))) return e;
-    k_mbpol_23<double, float><<<nsm, kFusedThreads, 0, s>>>(a, pairs, n2, n2_dev, trip, n3, n3_dev, ctr, partial,
-                                                             done, part_cap, dimer_warps);
+    if (shared_sm)
+        k_mbpol_23<double, float, kFusedThreadsShared><<<nsm, kFusedThreadsShared, 0, s>>>(
+            a, pairs, n2, n2_dev, trip, n3, n3_dev, ctr, partial, done, part_cap, dimer_warps);
+    else
+        k_mbpol_23<double, float, kFusedThreads><<<nsm, kFusedThreads, 0, s>>>(
+            a, pairs, n2, n2_dev, trip, n3, n3_dev, ctr, partial, done, part_cap, dimer_warps);
     return cudaGetLastError();
 }
 

@@ -2621,6 +2621,7 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
                             double* out16, double* jpot, double* jkin, cudaStream_t s) {
     cudaError_t e;
     converged = false;
+    bool forked = false;   // fork_hook called (the caller's work runs beside the solve)
     iterations = 0;
     launches = 0;
     const int n = 4 * nw;
@@ -3156,6 +3157,10 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
             // runs on the device (k_pcg_next), and once it has stopped the solve, the rest of
             // the batch returns at once.  The host reads the state after each batch; the first
             // batch is as long as the previous solve took.
+            if (fork_hook && !forked) {
+                if ((e = fork_hook())) return e;
+                forked = true;
+            }
             int* cgs = flag + 2;
             MixArgs ms = m;
             ms.stop = cgs;
@@ -3241,7 +3246,13 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
             }
         }
     }
-    // final pass
+    // final pass: after the caller's work that ran beside the solve (its kernels may add to
+    // the same force arrays); with no CG solve, that work runs here, before the pass
+    if (fork_hook && !forked) {
+        if ((e = fork_hook())) return e;
+        forked = true;
+    }
+    if (forked && join_hook && (e = join_hook())) return e;
     const double g34 = std::exp(gammln(3.0 / 4.0));
     if (heat) {
         const bool w32 = mixed && !spme_on;   // the FP32 Ewald heat sums take FP32 weights

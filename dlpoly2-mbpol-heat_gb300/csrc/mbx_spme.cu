@@ -28,7 +28,7 @@ namespace {
 
 constexpr double kPiS = 3.141592653589793;
 constexpr int kFftThreads = 256;
-constexpr int kFftPlaneThreads = 512;
+constexpr int kFftPlaneThreads = 256;   // fits beside the overlapped 2B/3B kernel on an SM
 constexpr int kSpThreads = 128;
 constexpr int kKtThreads = 256;
 constexpr int kMaxGrid = 1024;     // points per axis

@@ -170,6 +170,7 @@ def load(path=None):
     L.mbx_set_graphs.argtypes = [C.c_void_p, C.c_int]
     L.mbx_set_fused.argtypes = [C.c_void_p, C.c_int]
     L.mbx_set_fused_split.argtypes = [C.c_void_p, C.c_int]
+    L.mbx_set_overlap.argtypes = [C.c_void_p, C.c_int, C.c_int]
     L.mbx_graph_launches.argtypes = [C.c_void_p]
     L.mbx_graph_launches.restype = C.c_long
     L.mbx_last_lists.argtypes = [C.c_void_p, _I, C.c_long, _L, _I, C.c_long, _L]
@@ -567,6 +568,10 @@ class Context:
 
     def set_fused(self, on=True):
         self._check(self.lib.mbx_set_fused(self.h, 1 if on else 0), "mbx_set_fused")
+
+    def set_overlap(self, on=True, dimer_warps=0):
+        """The MB-pol terms beside the electrostatics' dipole solve in mbx_water_step (mixed)."""
+        self._check(self.lib.mbx_set_overlap(self.h, 1 if on else 0, int(dimer_warps)), "mbx_set_overlap")
 
     def set_fused_split(self, dimer_warps=0):
         """Dimer warps of the fused 2B/3B kernel's 12 per block (0: the default, 4)."""

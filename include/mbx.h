@@ -80,6 +80,14 @@ int mbx_set_fused(mbx_context* ctx, int on);
  * tuning knob: the split changes timings, and results only in the order of FP64 atomics. */
 int mbx_set_fused_split(mbx_context* ctx, int dimer_warps);
 
+/* mbx_water_step / mbx_water_step_device, mixed precision: run the MB-pol 2B/3B terms (they
+ * need the positions only) on a second stream of the context while the electrostatics solve
+ * its dipoles (on = 1), in an 8-warp form of the fused kernel (dimer_warps of them on the
+ * dimers; 0 = 4) that leaves room on every SM for the FP32 CG kernels; the final pass of the
+ * electrostatics starts after it.  Results equal the sequential form's up to the order of
+ * FP64 atomic additions.  Default off. */
+int mbx_set_overlap(mbx_context* ctx, int on, int dimer_warps);
+
 /*
  * MB-pol 2B + 3B forces with the heat-current bookkeeping.
  * Replaces mbpol_forces (SOURCE/mbpol.f90:98-449, called from SOURCE/dlpoly_cmd.f:2504)
@@ -130,10 +138,10 @@ int mbx_mbpol_forces_device(mbx_context* ctx, int precision, int imcon, const do
  *   - arguments as mbx_mbpol_forces_device (device arrays, forces and atomic_energy
  *     ACCUMULATED), `scalars` is a host array or NULL, `stream` a cudaStream_t or NULL;
  *   - mixed precision uses the default split (2B FP64, 3B FP32);
- *   - the first call on a device looks up the array's device address (make it before
- *     any stream capture) and caches it for the process: do not call it across a
- *     cudaDeviceReset; every call shares the one array, so calls that overlap on the
- *     GPU (other streams, other host threads) race and must be serialised.
+ *   - the first call on a device looks up the array's device address and caches it for
+ *     the process: do not call it across a cudaDeviceReset; every call shares the one
+ *     array, so calls that overlap on the GPU (other streams, other host threads) race
+ *     and must be serialised.
  */
 int mbx_mbpol_forces_noalloc(int precision, int imcon, const double* cell, int nttm2, const int* listttm2,
                              int natms, const double* xxx, const double* yyy, const double* zzz, double* fxx,

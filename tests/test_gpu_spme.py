@@ -165,3 +165,29 @@ def test_spme_dipoles_under_the_ewald_equations(oracle_lib):
     rel = l2 / np.sqrt(3 * pol.sum()) / rms_mu
     print("SPME dipoles: Ewald residual rms / dipole rms = %.2e" % rel)
     assert rel <= 1e-4
+
+
+@pytest.mark.parametrize("spme", [True, False])
+def test_overlapped_step_matches_sequential(spme):
+    """mbx_set_overlap: the MB-pol terms on a second stream beside the dipole solve give the
+    sequential step's results up to the order of FP64 atomic additions.  That order can move
+    a CG stopping decision, and the converged dipoles then differ within the dipole
+    tolerance (measured: forces 3e-8 relative), so the bound is 2e-7; a lost or doubled
+    force update would show at 1e-3 and above."""
+    box = systems.box_for(512, seed=11)
+    prm = systems.polar_params(alpha=0.35, rcut=9.0, kmax=(12, 12, 12), toler_debye=1e-8)
+    ctx = capi.Context(0)
+    try:
+        if spme:
+            ctx.set_spme(6, spacing=0.78)
+        seq = ctx.water_step(box, prm, precision=capi.MIXED)
+        ctx.set_overlap(True)
+        ovl = ctx.water_step(box, prm, precision=capi.MIXED)
+        ctx.set_overlap(True, dimer_warps=3)
+        ov3 = ctx.water_step(box, prm, precision=capi.MIXED)
+    finally:
+        ctx.close()
+    for got in (ovl, ov3):
+        assert got["status"] == 0
+        for key in ("forces", "atomic_energy", "dipoles", "scalars"):
+            assert _rel(got[key], seq[key]) <= 2e-7, (key, _rel(got[key], seq[key]))
