@@ -3278,7 +3278,7 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
         }
     }
     if (spme_on) {
-        if ((e = spme.final(n, x, y, z, q, md, heat ? vh : nullptr, k.sfac, kpart, acc, nullptr, s))) return e;
+        if ((e = spme.final(n, x, y, z, q, md, heat ? vh : nullptr, k.sfac, kpart, acc, nullptr, s, mixed))) return e;
         launches += spme.launches;
     }
     if (profiling && (e = cudaEventRecord(ev[3], s))) return e;

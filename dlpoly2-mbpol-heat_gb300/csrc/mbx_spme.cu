@@ -543,6 +543,47 @@ __global__ void __launch_bounds__(kSpThreads) k_spme_spread_heat(SpArgs s, const
     }
 }
 
+// The same heat densities on 8 FP32 grids (the mixed path's final pass): splines from the
+// site frame, one float2 atomic per grid point and grid.
+template <int P>
+__global__ void __launch_bounds__(kSpThreads) k_spme_spread_heat32(SpArgs s, const double4* __restrict__ md,
+                                                                   const double* __restrict__ vh,
+                                                                   float2* __restrict__ grid, size_t gstride) {
+    const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    const int j = (int)(t / kLanes), jz = (int)(t % kLanes);
+    if (j >= s.n || jz >= P) return;
+    int gi[3][P];
+    float th[3][P], d1[3][P], d2[3][P];
+    site_splines32<P, 0>(s, j, gi, th, d1, d2);
+    float w[16];
+    const double4 m = md[j];
+    w[0] = (float)m.x;
+    w[1] = (float)m.y;
+    w[2] = (float)m.z;
+#pragma unroll
+    for (int r = 0; r < 12; ++r) w[3 + r] = (float)vh[(size_t)r * s.n + j];
+    w[15] = 0.f;
+    bool any[8];
+#pragma unroll
+    for (int h = 0; h < 8; ++h) any[h] = w[2 * h] != 0.f || w[2 * h + 1] != 0.f;
+    const size_t K12 = (size_t)s.K1 * s.K2;
+    const float tz = pick(th[2], jz);
+    const size_t plane = pick(gi[2], jz) * K12;
+#pragma unroll
+    for (int jy = 0; jy < P; ++jy) {
+        const float tyz = th[1][jy] * tz;
+        const size_t row = plane + (size_t)gi[1][jy] * s.K1;
+#pragma unroll
+        for (int jx = 0; jx < P; ++jx) {
+            const float tt = th[0][jx] * tyz;
+            const size_t g = row + gi[0][jx];
+#pragma unroll
+            for (int h = 0; h < 8; ++h)
+                if (any[h]) atomicAdd(&grid[h * gstride + g], make_float2(w[2 * h] * tt, w[2 * h + 1] * tt));
+        }
+    }
+}
+
 // Field gathers of the dipole iterations: D_t = sum_g phi(g) grad_t M, D = J^T D_t and the
 // field -sfac D; with FIRST the charges' field from the imaginary part as well.
 //   FP64 (T double): efm = (polr2 > 1e-6 ? -sfac D : 0) + dum mu, efc = -sfac D_q
@@ -724,10 +765,11 @@ __device__ __forceinline__ int mfreq(int i, int K) { return i < K / 2 ? i : i - 
 // term from the structure factors of grids 1..8 (mu, q v, mu v).  F(m) of a density packed
 // as the real or imaginary part of grid Z is (Z(m) + conj Z(-m)) / 2 or
 // (Z(m) - conj Z(-m)) / 2i.  Block partial sums go to part[block * 11 + q].
-template <int HEAT>
+template <int HEAT, typename HC>
 __global__ void __launch_bounds__(kKtThreads) k_spme_kterms(SpArgs s, const double2* __restrict__ grid,
-                                                            size_t gstride, const double* __restrict__ G,
-                                                            double ralph, double sfac, double* __restrict__ part) {
+                                                            const HC* __restrict__ hgrid, size_t hstride,
+                                                            const double* __restrict__ G, double ralph, double sfac,
+                                                            double* __restrict__ part) {
     double acc[11];
 #pragma unroll
     for (int q = 0; q < 11; ++q) acc[q] = 0.0;
@@ -759,7 +801,7 @@ __global__ void __launch_bounds__(kKtThreads) k_spme_kterms(SpArgs s, const doub
             double re[16], im[16];
 #pragma unroll
             for (int h = 0; h < 8; ++h) {
-                const double2 a = grid[(h + 1) * gstride + i], b = grid[(h + 1) * gstride + jm];
+                const HC a = hgrid[h * hstride + i], b = hgrid[h * hstride + jm];
                 re[2 * h] = 0.5 * (a.x + b.x);
                 im[2 * h] = 0.5 * (a.y - b.y);
                 re[2 * h + 1] = 0.5 * (a.y + b.y);
@@ -1022,9 +1064,11 @@ int spme_smooth_even(double x) {
 SpmeState::~SpmeState() { release(); }
 
 void SpmeState::release() {
-    void* p[] = {G, G32, tw, tw32, grid, grid32, part, sib, sw, spl};
+    void* p[] = {G, G32, tw, tw32, grid, grid32, hgrid32, part, sib, sw, spl};
     for (void* q : p)
         if (q) cudaFree(q);
+    hgrid32 = nullptr;
+    hgrid_cap_ng = 0;
     sib = nullptr;
     sw = nullptr;
     spl = nullptr;
@@ -1070,6 +1114,13 @@ cudaError_t SpmeState::prepare(const double* cell, double alpha_, int order_, co
         grid32_cap_ng = 0;
         if ((e = cudaMalloc(&grid32, ngn * sizeof(float2)))) return e;
         grid32_cap_ng = (int)ngn;
+    }
+    if (fp32 && ngrids > 1 && ngn > hgrid_cap_ng) {   // the mixed final pass's 8 FP32 heat grids
+        if (hgrid32) cudaFree(hgrid32);
+        hgrid32 = nullptr;
+        hgrid_cap_ng = 0;
+        if ((e = cudaMalloc(&hgrid32, 8 * ngn * sizeof(float2)))) return e;
+        hgrid_cap_ng = ngn;
     }
     if (same) return cudaSuccess;
     // tables for this cell, alpha, order and grid
@@ -1289,31 +1340,53 @@ cudaError_t SpmeState::field32(int n, const double* x, const double* y, const do
 
 cudaError_t SpmeState::final(int n, const double* x, const double* y, const double* z, const double* q,
                              const double4* md, const double* vh, double sfac, double* part5, double* acc,
-                             double* field, cudaStream_t s) {
+                             double* field, cudaStream_t s, bool heat32) {
     cudaError_t e;
     launches = 0;
     const bool heat = vh != nullptr;
-    const int ngr = heat ? 9 : 1;
+    heat32 = heat && heat32 && hgrid32;
+    const int ngr = heat && !heat32 ? 9 : 1;   // FP64 grids: the densities, and the heat ones in FP64
     if (ngr > ngrid_cap || !order) return cudaErrorInvalidValue;
     const size_t gs = grid_cap_ng;
     if ((e = cudaMemsetAsync(grid, 0, (size_t)ngr * gs * sizeof(double2), s))) return e;
+    if (heat32 && (e = cudaMemsetAsync(hgrid32, 0, 8 * ng * sizeof(float2), s))) return e;
     if ((e = cudaMemsetAsync(acc + 11, 0, 9 * sizeof(double), s))) return e;
     const SpArgs sa = sp_args(*this, n);
     const unsigned nb = nblocks((long)kLanes * n, kSpThreads);
     if (n > 0) {
         SPME_ORDER_SWITCH(order, (k_spme_spread<double, P_, 2, double4><<<nb, kSpThreads, 0, s>>>(
                                      sa, x, y, z, q, md, nullptr, grid)));
-        if (heat)
+        if (heat32) {
+            SPME_ORDER_SWITCH(order, (k_spme_spread_heat32<P_><<<nb, kSpThreads, 0, s>>>(sa, md, vh, hgrid32, ng)));
+        } else if (heat) {
             SPME_ORDER_SWITCH(order, (k_spme_spread_heat<P_><<<nb, kSpThreads, 0, s>>>(sa, x, y, z, md, vh, grid + gs,
                                                                                       gs)));
+        }
     }
     if ((e = cudaGetLastError())) return e;
     for (int a = 0; a < 3; ++a)
         if ((e = fft_pass<double>(0, grid, gs, ngr, a, ax[a], K, tw, G, s))) return e;
+    if (heat32) {   // the 8 FP32 heat grids forward: plane passes (x, y) and the z pass
+        const size_t psm = plane_smem_bytes(K[0], K[1], sizeof(float2));
+        if (psm <= (size_t)kMaxFftSmem) {
+            k_fft_plane<float><<<dim3(K[2], 8), kFftPlaneThreads, psm, s>>>(hgrid32, ng, ax[0], ax[1], 1, tw32,
+                                                                           nullptr);
+            if ((e = cudaGetLastError())) return e;
+        } else {
+            for (int a = 0; a < 2; ++a)
+                if ((e = fft_pass<float>(0, hgrid32, ng, 8, a, ax[a], K, tw32, G32, s))) return e;
+        }
+        if ((e = fft_pass<float>(0, hgrid32, ng, 8, 2, ax[2], K, tw32, G32, s))) return e;
+        launches += 2;
+    }
     const int nblk = (int)std::min<long>(nblocks((long)ng, kKtThreads), kKtBlocks);
     const double ralph = -0.25 / (alpha * alpha);
-    if (heat) k_spme_kterms<1><<<nblk, kKtThreads, 0, s>>>(sa, grid, gs, G, ralph, sfac, part);
-    else k_spme_kterms<0><<<nblk, kKtThreads, 0, s>>>(sa, grid, gs, G, ralph, sfac, part);
+    if (heat32)
+        k_spme_kterms<1, float2><<<nblk, kKtThreads, 0, s>>>(sa, grid, hgrid32, ng, G, ralph, sfac, part);
+    else if (heat)
+        k_spme_kterms<1, double2><<<nblk, kKtThreads, 0, s>>>(sa, grid, grid + gs, gs, G, ralph, sfac, part);
+    else
+        k_spme_kterms<0, double2><<<nblk, kKtThreads, 0, s>>>(sa, grid, grid, gs, G, ralph, sfac, part);
     if ((e = fft_pass<double>(3, grid, 0, 1, 2, ax[2], K, tw, G, s))) return e;
     if ((e = fft_pass<double>(1, grid, 0, 1, 1, ax[1], K, tw, G, s))) return e;
     if ((e = fft_pass<double>(1, grid, 0, 1, 0, ax[0], K, tw, G, s))) return e;

@@ -78,6 +78,8 @@ struct SpmeState {
     float2* tw32 = nullptr;
     double2* grid = nullptr;       // complex grids, ngrid_cap of them
     float2* grid32 = nullptr;
+    float2* hgrid32 = nullptr;     // the mixed final pass's 8 heat grids in FP32
+    size_t hgrid_cap_ng = 0;
     int4* sib = nullptr;           // per site floor(t_a) mod K_a (frame)
     float4* sw = nullptr;          //   FP32 passes: t_a - floor(t_a)
     double* spl = nullptr;         //   FP64 passes: B-spline values and derivatives per axis
@@ -118,9 +120,11 @@ struct SpmeState {
     // half-space convention of the Ewald sums; acc[11..19] scratch.  vh: the 12 per-site
     // heat weights (q v, mu_c v_b) or null.  field (3 blocks of n) receives the total
     // k-space field without the self term, or null.
+    // heat32 (mixed precision, with vh): the heat densities on FP32 grids (FP32 spread, FFT and
+    // products; the k sums in FP64), the charges and dipoles in FP64 as always.
     cudaError_t final(int n, const double* x, const double* y, const double* z, const double* q,
                       const double4* md, const double* vh, double sfac, double* part5, double* acc, double* field,
-                      cudaStream_t s);
+                      cudaStream_t s, bool heat32 = false);
     // Forward (sign +1) or backward (-1) unnormalised 3D FFT of `count` FP64 grids in place.
     cudaError_t fft64(double2* data, int count, int sign, cudaStream_t s);
 };
