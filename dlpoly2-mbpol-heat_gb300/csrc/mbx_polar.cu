@@ -602,15 +602,23 @@ __global__ void k_pol_dd(PolArgs a) {
     if (a.polr2[i] > 1e-6) {
         const int nn = a.npol[i];   // the other partners carry no dipole
         const size_t row = (size_t)i * a.cap, blk = (size_t)a.n * a.cap;
-        for (int k = lane; k < nn; k += 32) {
-            const int j = a.nbr[row + k];
-            const double mj[3] = {a.mx[j], a.my[j], a.mz[j]};
-            double t[6];
+        // two entries per lane and step (the loads of both in flight together), as k_pol_dd32
+        for (int k = lane; k < nn; k += 64) {
+            const bool two = k + 32 < nn;
+            const int j0 = a.nbr[row + k], j1 = two ? a.nbr[row + k + 32] : j0;
+            double t0[6], t1[6];
 #pragma unroll
-            for (int p = 0; p < 6; ++p) t[p] = a.tens[p * blk + row + k];
-            e[0] += t[0] * mj[0] + t[1] * mj[1] + t[2] * mj[2];
-            e[1] += t[1] * mj[0] + t[3] * mj[1] + t[4] * mj[2];
-            e[2] += t[2] * mj[0] + t[4] * mj[1] + t[5] * mj[2];
+            for (int p = 0; p < 6; ++p) {
+                t0[p] = a.tens[p * blk + row + k];
+                t1[p] = two ? a.tens[p * blk + row + k + 32] : 0.0;
+            }
+            const double m0[3] = {a.mx[j0], a.my[j0], a.mz[j0]}, m1[3] = {a.mx[j1], a.my[j1], a.mz[j1]};
+            e[0] += t0[0] * m0[0] + t0[1] * m0[1] + t0[2] * m0[2];
+            e[1] += t0[1] * m0[0] + t0[3] * m0[1] + t0[4] * m0[2];
+            e[2] += t0[2] * m0[0] + t0[4] * m0[1] + t0[5] * m0[2];
+            e[0] += t1[0] * m1[0] + t1[1] * m1[1] + t1[2] * m1[2];
+            e[1] += t1[1] * m1[0] + t1[3] * m1[1] + t1[4] * m1[2];
+            e[2] += t1[2] * m1[0] + t1[4] * m1[1] + t1[5] * m1[2];
         }
         for (int c = 0; c < 3; ++c) e[c] = warp_sum(e[c]);
         if (lane == 0 && i < 3 * a.nw) {
@@ -1022,14 +1030,24 @@ __global__ void k_pol_dd32(PolArgs a, const float4* __restrict__ in, float* __re
     if (a.polr2[i] > 1e-6) {
         const int nn = a.npol[i];   // the other partners carry no dipole
         const size_t row = (size_t)i * a.cap, blk = (size_t)a.n * a.cap;
-        for (int k = lane; k < nn; k += 32) {
-            const float4 d = in[a.nbr[row + k]];
-            float t[6];
+        // two entries per lane and step: both index loads, then both dipole and tensor loads,
+        // in flight together (the index -> dipole chain is two memory latencies)
+        for (int k = lane; k < nn; k += 64) {
+            const bool two = k + 32 < nn;
+            const int j0 = a.nbr[row + k], j1 = two ? a.nbr[row + k + 32] : j0;
+            float t0[6], t1[6];
 #pragma unroll
-            for (int p = 0; p < 6; ++p) t[p] = a.tens32[p * blk + row + k];
-            e[0] += t[0] * d.x + t[1] * d.y + t[2] * d.z;
-            e[1] += t[1] * d.x + t[3] * d.y + t[4] * d.z;
-            e[2] += t[2] * d.x + t[4] * d.y + t[5] * d.z;
+            for (int p = 0; p < 6; ++p) {
+                t0[p] = a.tens32[p * blk + row + k];
+                t1[p] = two ? a.tens32[p * blk + row + k + 32] : 0.f;
+            }
+            const float4 d0 = in[j0], d1 = in[j1];
+            e[0] += t0[0] * d0.x + t0[1] * d0.y + t0[2] * d0.z;
+            e[1] += t0[1] * d0.x + t0[3] * d0.y + t0[4] * d0.z;
+            e[2] += t0[2] * d0.x + t0[4] * d0.y + t0[5] * d0.z;
+            e[0] += t1[0] * d1.x + t1[1] * d1.y + t1[2] * d1.z;
+            e[1] += t1[1] * d1.x + t1[3] * d1.y + t1[4] * d1.z;
+            e[2] += t1[2] * d1.x + t1[4] * d1.y + t1[5] * d1.z;
         }
         for (int c = 0; c < 3; ++c) e[c] = warp_sum(e[c]);
         if (lane == 0 && i < 3 * a.nw) {
