@@ -428,6 +428,14 @@ def run_ours(args, rank, world):
     grid = ctx.spme_last_grid()
     k64 = max(3, args.steps // 4)
     t_fp64, _, it_fp64, _ = timed(capi.FP64, k64, min(args.warmup, 3))
+    # the reference's ASPC mode (CONTROL `aspc`: k 4, SOR weight 6/11, 6 converged steps, then
+    # the predicted dipoles and one corrector iteration per step): the same MD steps, mixed
+    omega0 = PRM[4]
+    PRM[4] = 6.0 / 11.0
+    ctx.set_aspc(4, 6)
+    t_aspc, _, it_aspc, _ = timed(capi.MIXED, args.steps, 7)
+    ctx.set_aspc(0)
+    PRM[4] = omega0
     # phase times of the electrostatics in the mixed step (CUDA events on the launching stream)
     ctx.set_profiling(True)
     reset()
@@ -574,6 +582,12 @@ def run_ours(args, rank, world):
                    "not_in_step": NOT_IN_STEP},
         "fp64": {"value": world * k64 / t_fp64, "unit": "steps/s", "ms_per_step": 1e3 * t_fp64 / k64},
         "mixed_over_fp64": (args.steps / t_mixed) / (k64 / t_fp64),
+        "aspc_md": {"value": world * args.steps / t_aspc, "unit": "steps/s",
+                    "ms_per_step": 1e3 * t_aspc / args.steps, "precision": "mixed", "k": 4, "iter_nstep": 6,
+                    "sor_omega": 6.0 / 11.0, "fp64_field_evaluations_per_step": it_aspc,
+                    "mode": "the reference's CONTROL `aspc`: after 6 converged steps each step starts from "
+                            "Kolafa's prediction over the last 6 steps' dipoles and makes one SOR iteration "
+                            "(dipoles not converged to toler, as in the reference); 7 warm-up steps"},
         "mixed_error_vs_fp64": {"force_rms_rel": err_f, "heat_current_rel": err_j, "energy_rel": err_e,
                                 "state": "the same configuration, dipoles from zero"},
         "components_ms": {"electrostatics_cold_start_mixed": 1e3 * t_pol[capi.MIXED],

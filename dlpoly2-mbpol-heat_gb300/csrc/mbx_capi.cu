@@ -1316,6 +1316,24 @@ extern "C" int mbx_set_precond_sweeps(mbx_context* ctx, int sweeps) {
     return MBX_OK;
 }
 
+extern "C" int mbx_set_aspc(mbx_context* ctx, int k, int iter_nstep) {
+    if (!ctx) return MBX_ERR_ARG;
+    // aspc_init stops on any other order (SOURCE/aspc.f90:68-71)
+    if (k != 0 && k != 2 && k != 4) return fail(ctx, MBX_ERR_ARG, "ASPC order must be 0 (off), 2 or 4");
+    if (iter_nstep < 0) return fail(ctx, MBX_ERR_ARG, "ASPC iter_nstep must be >= 0");
+    CK(cudaSetDevice(ctx->device));
+    CK(ctx->polar.aspc_reset(k, iter_nstep));
+    return MBX_OK;
+}
+
+extern "C" int mbx_aspc_restart(mbx_context* ctx) {
+    if (!ctx) return MBX_ERR_ARG;
+    ctx->polar.aspc_restart();
+    return MBX_OK;
+}
+
+extern "C" int mbx_aspc_step(mbx_context* ctx) { return ctx ? ctx->polar.aspc_step : -1; }
+
 extern "C" int mbx_set_spme(mbx_context* ctx, int order, double spacing, const int* grid) {
     if (!ctx) return MBX_ERR_ARG;
     if (order != 0 && (order < 4 || order > 8)) return fail(ctx, MBX_ERR_ARG, "SPME order must be 0 or 4..8");

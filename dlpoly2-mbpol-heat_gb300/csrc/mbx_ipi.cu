@@ -302,6 +302,7 @@ struct WaterDriver {
     const double* prm;   // 15 Ewald / dipole settings, or null: mbx_polar_params_for_cell
     int dispersion;
     std::map<int, std::vector<double>> dip;   // per replica: 3 blocks of 4 nw site dipoles
+    int last_replica = -1;
 };
 
 int water_driver_forces(void* user, int replica, int nat, const double* cell, const double* xyz, double* energy,
@@ -332,6 +333,12 @@ int water_driver_forces(void* user, int replica, int nat, const double* cell, co
             lt[i] = m ? 3 : (i % 3 == 0 ? 1 : 2);
             mol[i] = (m ? i - 3 * nw : i / 3) + 1;
         }
+    }
+    // another replica than the last frame's: the ASPC step count restarts, as the reference's
+    // imglock test does (SOURCE/dlpoly_cmd.f:1765-1768)
+    if (replica != d.last_replica) {
+        mbx_aspc_restart(d.ctx);
+        d.last_replica = replica;
     }
     std::vector<double>& dp = d.dip[replica];
     if (dp.size() != 3 * (size_t)n) dp.assign(3 * (size_t)n, 0.0);

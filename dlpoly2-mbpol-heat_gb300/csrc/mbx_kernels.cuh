@@ -283,6 +283,17 @@ struct PolarState {
     float spme_ms = 0.f;                   // profiling: device time of the SPME passes of the last call
     long spme_calls = 0;
     cudaEvent_t spev[2] = {nullptr, nullptr};
+    // ASPC (Kolafa's always stable predictor-corrector; SOURCE/aspc.f90 and forces.f:334-366):
+    // order aspc_k (2 or 4; 0: off); each call is one MD step (aspc_step, the reference's
+    // nstep_for_guess); after aspc_niter steps the dipoles start from the prediction over
+    // the last k+2 steps, and one corrector iteration replaces the converged solve
+    int aspc_k = 0, aspc_niter = 0, aspc_step = 0;
+    int aspc_n = 0, aspc_head = 0;         // sites of the history; its newest slot
+    double* aspc_hist = nullptr;           // k+2 slots of 3 x aspc_n dipoles (x, y, z blocks)
+    cudaError_t aspc_reset(int k, int niter);   // aspc_init: history zeroed, step count 0
+    void aspc_restart();                         // nstep_for_guess = 0 (an image change)
+    cudaError_t aspc_predict(int n, double* mx, double* my, double* mz, cudaStream_t s);
+    cudaError_t aspc_push(int n, const double* mx, const double* my, const double* mz, cudaStream_t s);
 
     ~PolarState();
     void release();

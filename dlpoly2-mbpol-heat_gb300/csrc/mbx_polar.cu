@@ -476,7 +476,53 @@ __global__ void k_pol_polr6(PolArgs a, double* __restrict__ out) {
 }
 
 // --- static real-space field and dipole tensors ---------------------------------------
-__global__ void k_pol_static(PolArgs a) {
+// rfield's first pass per pair (SOURCE/rfield.f:59-201): the charge field q_j (B_1 + 1/r^3
+// - exp(-a_cd (r/bb)^4) / r^3) r, and for the polarizable partners the dipole tensor
+// r r^T A - B I with A = 3/r^5 + B_2 and B = 1/r^3 + B_1, less its Thole damping (h1, h2 of
+// exp(-a_dd (r/bb)^4)).  The damping is nonzero within ~3.5 A (charge) and ~5.5 A (dipole)
+// only, a few pairs of a row of ~400, but one lane that needs the FP64 exp makes its whole
+// warp execute it: so every lane first adds its pair's undamped field and writes its
+// undamped tensor, and the damped pairs are queued per warp (their slots in the row) and
+// evaluated 32 at a time, their damping subtracted from the field sum and from the tensor
+// written before (read back and rewritten by the same warp).
+__device__ __forceinline__ void static_damp(const PolArgs& a, int i, int k, size_t row, size_t blk, int np,
+                                            double rpi, double e[3]) {
+    const int j = a.nbr[row + k];
+    double d[3];
+    sep(a, i, j, d[0], d[1], d[2]);
+    const double r2 = norm2(d[0], d[1], d[2]);
+    const double rri = rsqrt_nr(r2);
+    const double rr = r2 * rri;
+    const double r3i = rri * rri * rri, r5i = r3i * rri * rri;
+    const double u = pow4(rr * (rpi * a.rpolr6[j]));
+    const double arq = a.ascd * u;
+    if (arq < kDampCut) {
+        const double f = kR4pie0 * a.q[j] * exp(-arq) * r3i;
+        e[0] -= f * d[0];
+        e[1] -= f * d[1];
+        e[2] -= f * d[2];
+    }
+    if (k >= np) return;
+    const double arob4 = a.athole * u;
+    const bool dd = arob4 < kDampCut;
+    const double h1 = dd ? exp(-arob4) : 0.0;
+    const double h2 = (1.0 + (4.0 / 3.0) * arob4) * h1;
+    const double C = 3.0 * kR4pie0 * r5i * h2, D = kR4pie0 * h1 * r3i;
+    const int ia[6] = {0, 0, 0, 1, 1, 2}, ib[6] = {0, 1, 2, 1, 2, 2};
+#pragma unroll
+    for (int p = 0; p < 6; ++p) {
+        double t = a.tens[p * blk + row + k];
+        if (dd) {
+            const double rirj = d[ia[p]] * d[ib[p]];
+            t -= ia[p] == ib[p] ? fma(rirj, C, -D) : rirj * C;
+            a.tens[p * blk + row + k] = t;
+        }
+        if (a.tens32) a.tens32[p * blk + row + k] = (float)t;   // not written by the first pass
+    }
+}
+
+__global__ void __launch_bounds__(kThreads) k_pol_static(PolArgs a) {
+    __shared__ int dq[kThreads / 32][64];   // per warp: row slots of the damped pairs
     const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (i >= a.n) return;
@@ -490,56 +536,67 @@ __global__ void k_pol_static(PolArgs a) {
     const size_t row = (size_t)i * a.cap, blk = (size_t)a.n * a.cap;
     const bool poli = a.polr2[i] > 1e-6;
     const int np = poli ? a.npol[i] : 0;   // tensors of the polarizable partners (the row's first np)
+    const double rpi = a.rpolr6[i];
+    int* q = dq[threadIdx.x >> 5];
+    int qn = 0;                            // queued pairs (warp-uniform)
     double e[3] = {0, 0, 0};
-    for (int k = lane; k < nn; k += 32) {
-        const int j = a.nbr[row + k];
-        double d[3];
-        sep(a, i, j, d[0], d[1], d[2]);
-        const double r2 = norm2(d[0], d[1], d[2]);
-        // one reciprocal root gives r, 1/r^2, 1/r^3 and 1/r^5; the table index and the Thole
-        // arguments multiply by reciprocals (FP64 divisions are the costliest FP64-pipe
-        // operations of this kernel)
-        const double rri = rsqrt_nr(r2);
-        const double rr = r2 * rri;
-        double t[6] = {0, 0, 0, 0, 0, 0};
-        if (a.rcut > rr) {
-            double bbb[4];
-            interp_r(a, rr, bbb);
-            const double rsqi = rri * rri, r3i = rsqi * rri, r5i = r3i * rsqi;
-            const double rob = rr * (a.rpolr6[i] * a.rpolr6[j]);   // r / bb
-            const double qj = a.q[j];
-            double eki = kR4pie0 * qj * (bbb[1] + r3i);
-            const double arq = a.ascd * pow4(rob);
-            const double dum1 = arq < kDampCut ? exp(-arq) : 0.0;
-            eki = eki - kR4pie0 * qj * dum1 * r3i;
-            e[0] += eki * d[0];
-            e[1] += eki * d[1];
-            e[2] += eki * d[2];
-            if (k < np) {
-                const double arob4 = a.athole * pow4(rob);
-                const double h1 = arob4 < kDampCut ? exp(-arob4) : 0.0;
-                const double h2 = (1.0 + (4.0 / 3.0) * arob4) * h1;
-                const int ia[6] = {0, 0, 0, 1, 1, 2}, ib[6] = {0, 1, 2, 1, 2, 2};
-#pragma unroll
-                for (int p = 0; p < 6; ++p) {
-                    const double rirj = d[ia[p]] * d[ib[p]];
-                    if (ia[p] == ib[p]) {
-                        t[p] = kR4pie0 * ((3.0 * rirj * r5i - r3i) + rirj * bbb[2] - bbb[1]);
-                        t[p] = t[p] - (3.0 * rirj * r5i * h2 - h1 * r3i) * kR4pie0;
-                    } else {
-                        t[p] = kR4pie0 * ((3.0 * rirj * r5i) + rirj * bbb[2]);
-                        t[p] = t[p] - 3.0 * rirj * r5i * h2 * kR4pie0;
-                    }
+    for (int base = 0; base < nn; base += 32) {
+        const int k = base + lane;
+        bool damped = false;
+        if (k < nn) {
+            const int j = a.nbr[row + k];
+            double d[3];
+            sep(a, i, j, d[0], d[1], d[2]);
+            const double r2 = norm2(d[0], d[1], d[2]);
+            // one reciprocal root gives r, 1/r^2, 1/r^3 and 1/r^5; the table index and the
+            // Thole arguments multiply by reciprocals (FP64 divisions are the costliest
+            // FP64-pipe operations of this kernel)
+            const double rri = rsqrt_nr(r2);
+            const double rr = r2 * rri;
+            double t[6] = {0, 0, 0, 0, 0, 0};
+            if (a.rcut > rr) {
+                double bbb[4];
+                interp_r(a, rr, bbb);
+                const double rsqi = rri * rri, r3i = rsqi * rri, r5i = r3i * rsqi;
+                const double eki = kR4pie0 * a.q[j] * (bbb[1] + r3i);
+                e[0] += eki * d[0];
+                e[1] += eki * d[1];
+                e[2] += eki * d[2];
+                const double u = pow4(rr * (rpi * a.rpolr6[j]));   // (r / bb)^4
+                damped = a.ascd * u < kDampCut || (k < np && a.athole * u < kDampCut);
+                if (k < np) {
+                    const double A = kR4pie0 * (3.0 * r5i + bbb[2]), B = kR4pie0 * (r3i + bbb[1]);
+                    const double ax = A * d[0], ay = A * d[1], az = A * d[2];
+                    t[0] = fma(ax, d[0], -B);
+                    t[1] = ax * d[1];
+                    t[2] = ax * d[2];
+                    t[3] = fma(ay, d[1], -B);
+                    t[4] = ay * d[2];
+                    t[5] = fma(az, d[2], -B);
                 }
             }
-        }
-        if (k < np) {
+            if (k < np) {
 #pragma unroll
-            for (int p = 0; p < 6; ++p) a.tens[p * blk + row + k] = t[p];
-            if (a.tens32)
-                for (int p = 0; p < 6; ++p) a.tens32[p * blk + row + k] = (float)t[p];
+                for (int p = 0; p < 6; ++p) a.tens[p * blk + row + k] = t[p];
+                // a damped pair's FP32 copy is written with its damping
+                if (a.tens32 && !damped)
+                    for (int p = 0; p < 6; ++p) a.tens32[p * blk + row + k] = (float)t[p];
+            }
+        }
+        const unsigned bal = __ballot_sync(0xffffffffu, damped);
+        if (damped) q[qn + __popc(bal & ((1u << lane) - 1u))] = k;
+        qn += __popc(bal);
+        if (qn >= 32) {   // a full warp of damped pairs
+            __syncwarp();
+            static_damp(a, i, q[lane], row, blk, np, rpi, e);
+            __syncwarp();
+            if (lane < qn - 32) q[lane] = q[32 + lane];
+            qn -= 32;
+            __syncwarp();
         }
     }
+    __syncwarp();
+    if (lane < qn) static_damp(a, i, q[lane], row, blk, np, rpi, e);
     for (int c = 0; c < 3; ++c) e[c] = warp_sum(e[c]);
     if (lane == 0) {
         a.efk[i] = e[0];
@@ -2310,7 +2367,8 @@ cudaError_t launch_msite_redistribute(int nw, double gamma, double* fx, double* 
 void PolarState::release() {
     void* p[] = {ercp, ercp32, nn_s, nbr_s, npol_s, nup_s, xref, nn, nbr, npol, nup, flag, xf, tens, intra, fld, vesp, ae, eik, kv, kx2, lmn, sf, kterm, acc, kco, fac, md, vh, polr6,
                  ckey, cskey, cidx, csidx, csort, cstart, cend,
-                 tens32, r32, d32, e32, kco32, fac32, ktile, kaux, kcol, colk, kpart, cg_x, cg_r, cg_q, cg_z, vh32};
+                 tens32, r32, d32, e32, kco32, fac32, ktile, kaux, kcol, colk, kpart, cg_x, cg_r, cg_q, cg_z, vh32,
+                 aspc_hist};
     for (void* q : p)
         if (q) cudaFree(q);
     if (acc_h) cudaFreeHost(acc_h);
@@ -2362,9 +2420,92 @@ void PolarState::release() {
     n_cap = nw_cap = k_cap = 0;
     eik_cap = 0;
     tab_alpha = tab_rcut = -1.0;
+    aspc_hist = nullptr;
+    aspc_n = aspc_head = 0;
 }
 
 PolarState::~PolarState() { release(); }
+
+cudaError_t PolarState::aspc_reset(int k, int niter) {
+    aspc_k = k;
+    aspc_niter = niter;
+    aspc_step = 0;
+    aspc_head = 0;
+    if (aspc_hist) cudaFree(aspc_hist);   // reallocated (zeroed) by the next call
+    aspc_hist = nullptr;
+    aspc_n = 0;
+    return cudaSuccess;
+}
+
+void PolarState::aspc_restart() { aspc_step = 0; }
+
+// Kolafa's predictor coefficients B_1..B_{k+2} (J. Comput. Chem. 25 (2004) 335, eq. 6):
+// B_j = (-1)^(j+1) j (4k+6)/(k+3) prod_{m<j} (k+2-m)/(k+3+m), as SOURCE/aspc.f90:110-114
+// builds them (k = 2: 14/5, -14/5, 6/5, -1/5)
+struct AspcCoef {
+    double b[6];
+};
+
+static AspcCoef aspc_coefficients(int k) {
+    AspcCoef c{};
+    const double rk = k;
+    double t = 1.0 / (rk + 3.0);
+    for (int j = 1; j <= k + 2 && j <= 6; ++j) {
+        c.b[j - 1] = ((j & 1) ? 1.0 : -1.0) * double(j) * (4.0 * rk + 6.0) * t;
+        t = t * (rk + 2.0 - double(j)) / (rk + 3.0 + double(j));
+    }
+    return c;
+}
+
+// mu = sum_j B_j mu(t - j h) over the history, newest first (SOURCE/aspc.f90:143-170)
+__global__ void k_aspc_predict(int n, int m, int head, AspcCoef c, const double* __restrict__ hist,
+                               double* __restrict__ mx, double* __restrict__ my, double* __restrict__ mz) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double* out[3] = {mx, my, mz};
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        double v = 0.0;
+        for (int j = 0; j < m; ++j) {
+            const int slot = (head + j) % m;
+            v += c.b[j] * hist[((size_t)slot * 3 + d) * n + i];
+        }
+        out[d][i] = v;
+    }
+}
+
+cudaError_t PolarState::aspc_predict(int n, double* mx, double* my, double* mz, cudaStream_t s) {
+    cudaError_t e;
+    const int m = aspc_k + 2;
+    if (!aspc_hist || aspc_n != n) {   // a new history (aspc_init): zeroed, the step count restarts
+        if (aspc_hist) cudaFree(aspc_hist);
+        aspc_hist = nullptr;
+        if ((e = cudaMalloc(&aspc_hist, (size_t)m * 3 * n * sizeof(double)))) return e;
+        if ((e = cudaMemsetAsync(aspc_hist, 0, (size_t)m * 3 * n * sizeof(double), s))) return e;
+        aspc_n = n;
+        aspc_head = 0;
+        aspc_step = 0;
+    }
+    ++aspc_step;
+    if (aspc_step > aspc_niter) {   // as aspc_predict's test (its slots not yet filled are zeros)
+        k_aspc_predict<<<blocks(n, kThreads), kThreads, 0, s>>>(n, m, aspc_head, aspc_coefficients(aspc_k),
+                                                                aspc_hist, mx, my, mz);
+        ++launches;
+    }
+    return cudaSuccess;
+}
+
+cudaError_t PolarState::aspc_push(int n, const double* mx, const double* my, const double* mz, cudaStream_t s) {
+    const int m = aspc_k + 2;
+    aspc_head = (aspc_head + m - 1) % m;
+    const double* src[3] = {mx, my, mz};
+    for (int d = 0; d < 3; ++d) {
+        const cudaError_t e = cudaMemcpyAsync(aspc_hist + ((size_t)aspc_head * 3 + d) * n, src[d], n * sizeof(double),
+                                              cudaMemcpyDeviceToDevice, s);
+        if (e) return e;
+    }
+    return cudaSuccess;
+}
 
 cudaError_t PolarState::table(double alpha, double rcut, cudaStream_t s) {
     if (ercp && alpha == tab_alpha && rcut == tab_rcut) return cudaSuccess;
@@ -2824,6 +2965,15 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
     a.athole = prm[5]; a.athole12 = prm[6]; a.athole13 = prm[7]; a.ascc = prm[8]; a.ascd = prm[9];
     a.toler = prm[3];
     a.omega = prm[4];
+    // ASPC (SOURCE/forces.f:334-366): once aspc_niter steps are past, the dipoles predicted
+    // from the history (aspc_predict before forces, SOURCE/dlpoly_cmd.f:2273-2283) and one
+    // corrector iteration; SOR weight 0.3 for the first four steps
+    bool aspc_one = false;
+    if (aspc_k) {
+        if ((e = aspc_predict(n, mx, my, mz, s))) return e;
+        if (aspc_step < 5) a.omega = 0.3;
+        aspc_one = aspc_step > aspc_niter;
+    }
     bind(a);
 
     KArgs k;
@@ -3085,7 +3235,12 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
         deltadip = std::sqrt(acc_h[27] / (acc_h[28] > 0.0 ? acc_h[28] : 1.0));
         return cudaSuccess;
     };
-    if (!mixed) {
+    if (aspc_one) {   // one iteration, then marked converged (SOURCE/forces.f:361-366)
+        fields64(true);
+        if ((e = sor64())) return e;
+        iterations = 1;
+        converged = true;
+    } else if (!mixed) {
         for (int it = 1;; ++it) {
             fields64(it == 1);
             if ((e = sor64())) return e;
@@ -3106,7 +3261,7 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
         m.x = cg_x;
         m.rho = cg_r;
         m.q = cg_q;
-        const double fac = 1.0 - prm[4];
+        const double fac = 1.0 - a.omega;
         // z = M^-1 rho into cg_z, rho.z into acc[slot] (and the first direction); `pre`
         // Jacobi sweeps (odd: the polynomial is positive definite for every eigenvalue of
         // D^-1 T_real below 1, which the dipole equations guarantee)
@@ -3264,6 +3419,8 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
             }
         }
     }
+    // aspc_set (SOURCE/dlpoly_cmd.f:2318-2320): the step's dipoles join the history
+    if (aspc_k && (e = aspc_push(n, mx, my, mz, s))) return e;
     // final pass: after the caller's work that ran beside the solve (its kernels may add to
     // the same force arrays); with no CG solve, that work runs here, before the pass
     if (fork_hook && !forked) {

@@ -146,6 +146,9 @@ def load(path=None):
     L.mbx_water_step.argtypes = [C.c_void_p, C.c_int, C.c_int, _D, C.c_int, C.c_int, _D, _D, _D, _I, _I] + [_D] * 16
     L.mbx_set_lanes.argtypes = [C.c_void_p, C.c_int]
     L.mbx_set_precond_sweeps.argtypes = [C.c_void_p, C.c_int]
+    L.mbx_set_aspc.argtypes = [C.c_void_p, C.c_int, C.c_int]
+    L.mbx_aspc_step.argtypes = [C.c_void_p]
+    L.mbx_aspc_restart.argtypes = [C.c_void_p]
     L.mbx_polar_field_timing.argtypes = [C.c_void_p, _D, _D, C.POINTER(C.c_long)]
     L.mbx_set_spme.argtypes = [C.c_void_p, C.c_int, C.c_double, _I]
     L.mbx_set_polar_skin.argtypes = [C.c_void_p, C.c_double]
@@ -444,6 +447,18 @@ class Context:
 
     def set_precond_sweeps(self, sweeps):
         self._check(self.lib.mbx_set_precond_sweeps(self.h, int(sweeps)), "mbx_set_precond_sweeps")
+
+    def set_aspc(self, k, iter_nstep=None):
+        """ASPC dipole prediction of order k (2 or 4; 0: off) after iter_nstep converged
+        steps (default k+2); clears the history and the step count."""
+        n = (int(k) + 2 if k else 0) if iter_nstep is None else int(iter_nstep)
+        self._check(self.lib.mbx_set_aspc(self.h, int(k), n), "mbx_set_aspc")
+
+    def aspc_restart(self):
+        self._check(self.lib.mbx_aspc_restart(self.h), "mbx_aspc_restart")
+
+    def aspc_step(self):
+        return int(self.lib.mbx_aspc_step(self.h))
 
     def set_spme(self, order=6, spacing=0.8, grid=None):
         """k space of later electrostatics calls: SPME of `order` (0: the Ewald sum) on

@@ -9,6 +9,9 @@ reference skips what its run does not use.
     (:1213-1300);
   - `spme` is read like `ewald` (this library evaluates it with the Ewald sum);
   - `polar`, `iter toler` (Debye), `aspc_omega`, `ascc`, `ascd`;
+  - `aspc` (ASPC on, k 4, 6 converged steps, SOR weight 6/11) and `aspc_k k` (for k 2 or
+    4: weight (k+2)/(2k+3), k+2 converged steps; ASPC stays off without `aspc`), read in the
+    order the lines come (:742-788);
   - `vmbpol` (:1040-1060: Thole 0.055 / 0.626 / 0.055, smearing 0.4 / 0.4, gamma
     0.426706882);
   - `eps` (dielectric constant).
@@ -58,7 +61,8 @@ def _fields(line):
 def read_control(src):
     """CONTROL keywords of the MB-pol path -> dict"""
     c = {"rcut": None, "rvdw": None, "delr": 0.0, "ewald": None, "polar": False, "toler": None,
-         "sor_omega": 0.3, "ascc": None, "ascd": None, "vmbpol": False, "epsq": 1.0, "spme": False}
+         "sor_omega": 0.3, "ascc": None, "ascd": None, "vmbpol": False, "epsq": 1.0, "spme": False,
+         "aspc": False, "aspc_k": 4, "aspc_iter_nstep": 6}
     for raw in _lines(src):
         rec = raw.strip().lower()
         if not rec or rec.startswith("#"):
@@ -83,7 +87,24 @@ def read_control(src):
         elif rec.startswith("iter"):
             c["toler"] = nums[0] / EATD        # Debye to e Angstrom
         elif rec.startswith("aspc_omega"):
+            if not 0.0 <= nums[0] <= 1.0:
+                raise ValueError("CONTROL: aspc_omega must lie in [0, 1]")
             c["sor_omega"] = nums[0]
+        elif rec.startswith("aspc_k"):
+            # Kolafa's corrector weight and iter_nstep = k+2 for k = 2 or 4 (SOURCE/simdef_cmd.f:754-773)
+            k = int(nums[0])
+            if k < 0:
+                raise ValueError("CONTROL: aspc_k must be >= 0")
+            c["aspc_k"] = k
+            if k in (2, 4):
+                c["sor_omega"] = (k + 2.0) / (2.0 * k + 3.0)
+                c["aspc_iter_nstep"] = k + 2
+        elif rec.startswith("aspc"):
+            # ASPC on with k = 4 (SOURCE/simdef_cmd.f:775-788)
+            c["aspc"] = True
+            c["sor_omega"] = 6.0 / 11.0
+            c["aspc_k"] = 4
+            c["aspc_iter_nstep"] = 6
         elif rec.startswith("ascc"):
             c["ascc"] = nums[0]
         elif rec.startswith("ascd"):
@@ -210,7 +231,8 @@ def deck_inputs(control, field, config):
     read_config results.  Standard layout: the water molecule type(s) of 3 sites first, the
     M-site type last (one site per water).  Returns dict(nw, natms, imcon, cell, xyz, vel,
     mass, polr, polr2, polar_prm[15], disp=(ntypes, prm) or None, ltype, molecule (0-based
-    ids, one per water), rvdw, delr)."""
+    ids, one per water), rvdw, delr, aspc=(k, iter_nstep) or None: mbx_set_aspc's
+    arguments)."""
     mols = field["molecules"]
     if len(mols) < 2 or len(mols[-1][2]) != 1:
         raise ValueError("FIELD: expected the water type(s) then a one-site M-site type")
@@ -274,7 +296,8 @@ def deck_inputs(control, field, config):
     return {"nw": nw, "natms": n, "imcon": config["imcon"], "cell": cell, "xyz": config["xyz"],
             "vel": config["vel"], "mass": mass, "polr": polr, "polr2": polr2, "polar_prm": prm, "disp": disp,
             "ltype": ltype, "molecule": np.array(molecule, np.int32) - 1, "rvdw": control["rvdw"] or rcut,
-            "delr": control["delr"]}
+            "delr": control["delr"],
+            "aspc": (control["aspc_k"], control["aspc_iter_nstep"]) if control.get("aspc") else None}
 
 
 def write_deck(box, control_extra="", units="kcal", vdw=None, title="MB-pol water"):

@@ -377,6 +377,27 @@ int mbx_set_lanes(mbx_context* ctx, int lanes);
  * that does not halve the residual falls back to the diagonal.  Changes the iteration
  * count, not the converged dipoles beyond the dipole tolerance. */
 int mbx_set_precond_sweeps(mbx_context* ctx, int sweeps);
+/* ASPC dipole prediction, the CONTROL keywords `aspc` and `aspc_k` (replaces aspc_init,
+ * aspc_predict and aspc_set of SOURCE/aspc.f90:45-251 with the ASPC branch of the dipole
+ * loop, SOURCE/forces.f:334-366, as SOURCE/dlpoly_cmd.f:2273-2320 drives them).
+ *   k           2 or 4 turns it on; 0 (the default) turns it off: each call's dipoles then
+ *               start from the caller's, as set_guess_dipole(1, ...) leaves them
+ *   iter_nstep  aspc_iter_nstep: k+2 when the deck sets `aspc_k`, 6 for `aspc`
+ * Each later mbx_polar_forces / mbx_water_step(_device) call on this context is one MD
+ * step.  Steps 1..iter_nstep iterate to toler (SOR weight 0.3 for steps 1..4, then
+ * polar_prm[4]).  Every later step starts from sum_j B_j mu(t - j) over the last k+2
+ * steps' dipoles (Kolafa's coefficients) and makes ONE SOR iteration with polar_prm[4]
+ * (4/7 or 6/11 when the deck sets `aspc_k`): its dipoles are not converged, as in the
+ * reference.  The history is kept per context on the device.  Calling this again clears the
+ * history and the step count (aspc_init), as does a change of the site count.  The worker
+ * lanes of mbx_water_step_multi do not predict. */
+int mbx_set_aspc(mbx_context* ctx, int k, int iter_nstep);
+/* nstep_for_guess = 0 (SOURCE/dlpoly_cmd.f:1765-1768, an i-PI image change): the next call
+ * is ASPC step 1 again; the history is kept, as the reference keeps it.  mbx_ipi_run does
+ * this when the replica changes. */
+int mbx_aspc_restart(mbx_context* ctx);
+/* The ASPC step count of the context (nstep_for_guess); -1 without a context. */
+int mbx_aspc_step(mbx_context* ctx);
 int mbx_water_step_multi(mbx_context* ctx, int precision, int nbox, const int* imcon, const double* cell,
                          const int* nw, const double* polar_prm, const double* polr, const double* polr2,
                          const int* ltype, const int* molecule, double* xxx, double* yyy, double* zzz, double* dipx,

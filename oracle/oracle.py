@@ -271,5 +271,50 @@ class Oracle:
         return m
 
 
+def aspc_coefficients(k):
+    """Kolafa's ASPC predictor coefficients B_1..B_{k+2}, built as aspc_init builds them
+    (SOURCE/aspc.f90:106-114): B_j = (-1)^(j+1) j (4k+6)/(k+3) prod_{m<j} (k+2-m)/(k+3+m)."""
+    rk = float(k)
+    t = 1.0 / (rk + 3.0)
+    out = []
+    for j in range(1, k + 3):
+        out.append((1.0 if j % 2 else -1.0) * j * (4.0 * rk + 6.0) * t)
+        t = t * (rk + 2.0 - j) / (rk + 3.0 + j)
+    return out
+
+
+class AspcDriver:
+    """The reference's ASPC step sequence around the dipole solve: aspc_predict before
+    forces and aspc_set after it (SOURCE/dlpoly_cmd.f:2273-2320, SOURCE/aspc.f90:118-251),
+    with the loop branch of SOURCE/forces.f:334-366 (SOR weight 0.3 for steps below 5; one
+    iteration, marked converged, after iter_nstep steps)."""
+
+    def __init__(self, k, iter_nstep):
+        self.k, self.niter = int(k), int(iter_nstep)
+        self.B = aspc_coefficients(self.k)
+        self.hist = None     # k+2 dipole arrays, newest first (zeros after aspc_init)
+        self.step_count = 0  # nstep_for_guess
+
+    def step(self, orc, sites, cell, imcon, nw, chge, dp, polr, polr2, prm, dip0=None, vel=None):
+        n = 4 * nw
+        if self.hist is None:
+            self.hist = [np.zeros((n, 3)) for _ in range(self.k + 2)]
+        self.step_count += 1
+        dip = np.zeros((n, 3)) if dip0 is None else np.array(dip0, np.float64)
+        if self.step_count > self.niter:
+            dip = self.B[0] * self.hist[0]
+            for b, h in zip(self.B[1:], self.hist[1:]):
+                dip = dip + b * h
+        p = np.array(prm, np.float64).copy()
+        if self.step_count < 5:
+            p[4] = 0.3
+        if self.step_count > self.niter:
+            p[14] = 0            # one iteration; the oracle then reports status 1
+        res = orc.polar(sites, cell, imcon, nw, chge, dp, polr, polr2, p, dip0=dip, vel=vel)
+        self.hist.insert(0, res["dipoles"].copy())
+        del self.hist[self.k + 2:]
+        return res
+
+
 def load(path=None):
     return Oracle(path)

@@ -47,6 +47,26 @@ def test_units_and_control_keywords():
     np.testing.assert_array_equal(d["disp"][1][0], [100.0, 2.0, 300.0, 4.0])
 
 
+@pytest.mark.parametrize("lines, want", [
+    ("", None),
+    ("aspc", (4, 6, 6.0 / 11.0)),
+    ("aspc_k 2", None),                                   # sets k, ASPC still off
+    ("aspc\naspc_k 2", (2, 4, 4.0 / 7.0)),
+    ("aspc_k 2\naspc", (4, 6, 6.0 / 11.0)),               # `aspc` afterwards restores k 4
+    ("aspc\naspc_k 2\naspc_omega 0.5", (2, 4, 0.5)),
+    ("aspc\naspc_k 3", (3, 6, 6.0 / 11.0)),               # other k keep the weight and step count
+])
+def test_aspc_keywords(lines, want):
+    """`aspc`, `aspc_k`, `aspc_omega` in the order given, as SOURCE/simdef_cmd.f:742-788."""
+    box = systems.box_for(32, seed=3)
+    c, f, g = decks.write_deck(box, control_extra=lines)
+    d = decks.read_deck(c, f, g)
+    if want is None:
+        assert d["aspc"] is None
+    else:
+        assert d["aspc"] == want[:2] and d["polar_prm"][4] == want[2]
+
+
 def test_ewald_precision_rule():
     cell = [19.73, 0, 0, 0, 21.0, 0, 0, 0, 23.5]
     alpha, km = decks.ewald_from_precision(cell, 9.0, 1e-6)

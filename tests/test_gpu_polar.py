@@ -70,6 +70,58 @@ def test_polar_warm_start_and_no_heat(mbx_ctx, oracle_lib):
     _compare(got, ref)
 
 
+@pytest.mark.parametrize("precision", [capi.FP64, capi.MIXED])
+def test_aspc_steps_match_the_oracle(oracle_lib, precision):
+    """ASPC (mbx_set_aspc, k 2, 4 converged steps): an MD sequence of 8 steps with the
+    positions advancing by v dt, against the oracle's restatement of aspc_predict /
+    aspc_set and the loop branch of SOURCE/forces.f:334-366 (AspcDriver).  Steps 1-4 iterate
+    to toler with SOR weight 0.3; steps 5-8 start from the prediction and make one
+    iteration.  FP64: every result within 1e-10 at every step; mixed: the converged steps
+    within the dipole tolerance, the one-iteration steps' dipoles within 1e-9."""
+    import copy
+
+    import oracle
+    box0 = systems.box_for(32, seed=5)
+    prm = systems.polar_params(alpha=0.6, rcut=4.5, kmax=(8, 8, 8), toler_debye=1e-12, omega=4.0 / 7.0)
+    polr, polr2 = systems.polarizabilities(box0.nw)
+    ctx = capi.Context(0)
+    try:
+        with pytest.raises(capi.MbxError):
+            ctx.set_aspc(3)
+        ctx.set_aspc(2, 4)
+        assert ctx.aspc_step() == 0
+        drv = oracle.AspcDriver(2, 4)
+        dg = dr = None
+        for step in range(1, 9):
+            box = copy.copy(box0)
+            box.xyz = box0.xyz + (step - 1) * 0.0005 * box0.vel
+            sites, q, dp, _ = oracle_lib.msites_dms(box)
+            ref = drv.step(oracle_lib, sites, box.cell, box.imcon, box.nw, q, dp, polr, polr2, prm, dip0=dr,
+                           vel=box.vel)
+            got = ctx.polar(sites, box.cell, box.imcon, box.nw, q, dp, polr, polr2, prm, dip0=dg, vel=box.vel,
+                            precision=precision)
+            assert ctx.aspc_step() == step
+            assert ref["status"] == (0 if step <= 4 else 1)
+            if step > 4:
+                assert got["iterations"] == 1
+            if precision == capi.FP64:
+                _compare(got, ref)
+            else:
+                m = np.abs(ref["dipoles"]).max()
+                assert np.abs(got["dipoles"] - ref["dipoles"]).max() <= 1e-9 * m, step
+                f, fr = got["forces"], ref["forces"]
+                assert np.sqrt(np.mean((f - fr) ** 2)) <= 1e-6 * np.sqrt(np.mean(fr ** 2)), step
+            dg, dr = got["dipoles"], ref["dipoles"]
+        # a restart (an image change): the next step is step 1 again and iterates to toler
+        ctx.aspc_restart()
+        assert ctx.aspc_step() == 0
+        got = ctx.polar(sites, box.cell, box.imcon, box.nw, q, dp, polr, polr2, prm, dip0=dg, precision=precision)
+        assert ctx.aspc_step() == 1 and got["iterations"] > 1
+        ctx.set_aspc(0, 0)
+    finally:
+        ctx.close()
+
+
 def test_polar_not_converged_status(mbx_ctx, oracle_lib):
     box = systems.box_for(32, seed=5)
     prm = systems.polar_params(alpha=0.6, rcut=4.5, kmax=(6, 6, 6), toler_debye=1e-12, maxit=3)

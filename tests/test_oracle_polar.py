@@ -257,3 +257,18 @@ def test_lattice_sum_pins_the_ewald_energy(oracle_lib):
     # dipoles' energy alone
     assert abs((full["engcpe"] - charges["engcpe"]) - e_pol) <= fit_f
     assert abs(e_pol) > 100 * fit_f
+
+
+def test_aspc_coefficients_are_kolafas():
+    """The oracle's ASPC predictor coefficients (SOURCE/aspc.f90:106-114) are Kolafa's
+    published B_j (J. Comput. Chem. 25 (2004) 335, table 1) and sum to 1."""
+    from fractions import Fraction as F
+    import oracle
+    pub = {2: [F(14, 5), F(-14, 5), F(6, 5), F(-1, 5)],
+           4: [F(22, 7), F(-55, 14), F(55, 21), F(-22, 21), F(5, 21), F(-1, 42)]}
+    for k, b in pub.items():
+        got = oracle.aspc_coefficients(k)
+        assert len(got) == k + 2
+        for g, w in zip(got, b):
+            assert abs(g - float(w)) <= 1e-15 * abs(float(w))
+        assert abs(sum(got) - 1.0) <= 1e-14
