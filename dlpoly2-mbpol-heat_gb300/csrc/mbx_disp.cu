@@ -255,6 +255,7 @@ __global__ void __launch_bounds__(kThreads) k_disp_forces(DispArgs a, const int*
             const int k = pair_index(ti, a.ltype[j]);
             if (!((a.vdw_pairs[k >> 6] >> (k & 63)) & 1ull)) continue;
             double dx = dsub(xi, a.x[j]), dy = dsub(yi, a.y[j]), dz = dsub(zi, a.z[j]);
+            const double rx = dx, ry = dy, rz = dz;   // the raw separation (the heat term's)
             image(a.cl, dx, dy, dz);
             const double rsq = dadd(dadd(dmul(dx, dx), dmul(dy, dy)), dmul(dz, dz));
             if (!(a.rcsq > rsq)) continue;
@@ -287,14 +288,14 @@ __global__ void __launch_bounds__(kThreads) k_disp_forces(DispArgs a, const int*
                 atomicAdd(a.ae + j, 0.5 * e);
             }
             red[1] -= gamma * rsq;
+            // the stress's lower triangle (5, 8, 9) repeats 3, 4, 7: copied after the loop
             red[2] += dx * f0; red[3] += dx * f1; red[4] += dx * f2;
-            red[5] += dx * f1; red[6] += dy * f1; red[7] += dy * f2;
-            red[8] += dx * f2; red[9] += dy * f2; red[10] += dz * f2;
+            red[6] += dy * f1; red[7] += dy * f2; red[10] += dz * f2;
             if (a.vx) {
                 const double fv = f0 * (a.vx[i] + a.vx[j]) + f1 * (a.vy[i] + a.vy[j]) + f2 * (a.vz[i] + a.vz[j]);
-                red[11] += (xi - a.x[j]) * fv;
-                red[12] += (yi - a.y[j]) * fv;
-                red[13] += (zi - a.z[j]) * fv;
+                red[11] += rx * fv;
+                red[12] += ry * fv;
+                red[13] += rz * fv;
             }
         }
 #pragma unroll
@@ -307,6 +308,9 @@ __global__ void __launch_bounds__(kThreads) k_disp_forces(DispArgs a, const int*
         }
         if (lane == 0 && a.ae && aei != 0.0) atomicAdd(a.ae + i, aei);
     }
+    red[5] = red[3];
+    red[8] = red[4];
+    red[9] = red[7];
     block_sum_atomic<14>(red, a.acc14);
 }
 

@@ -1461,7 +1461,12 @@ __global__ void __launch_bounds__(kThreads) k_pcg_ad(PolArgs a, MixArgs m, int n
     block_sum_atomic<1>(v, a.acc + 34);
 }
 
-__global__ void __launch_bounds__(kThreads) k_pcg_step(PolArgs a, MixArgs m) {
+__device__ void pcg_next_body(double* acc, int* st, double target, bool keep_beta);
+
+// With `st` (the diagonal preconditioner), the last block to finish also runs the sweep's
+// stopping test (pcg_next_body, as k_pcg_next) on the complete sums; `ticket` counts the
+// finished blocks and is left at 0.
+__global__ void __launch_bounds__(kThreads) k_pcg_step(PolArgs a, MixArgs m, int* st, double target, int* ticket) {
     if (m.stop && *m.stop) return;   // the CG solve has stopped (uniform per launch)
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     double v[3] = {0, 0, 0};
@@ -1481,15 +1486,28 @@ __global__ void __launch_bounds__(kThreads) k_pcg_step(PolArgs a, MixArgs m) {
         v[2] = 1.0;
     }
     block_sum_atomic<3>(v, a.acc + 35);
+    if (!st) return;
+    __shared__ int last;
+    __threadfence();   // this block's sums (threads 0..2) before its ticket
+    __syncthreads();
+    if (threadIdx.x == 0) last = atomicAdd(ticket, 1) == (int)gridDim.x - 1;
+    __syncthreads();
+    if (!last || threadIdx.x != 0) return;
+    __threadfence();
+    *ticket = 0;
+    pcg_next_body(a.acc, st, target, true);
 }
 
 // d = z + beta d, z = M^-1 rho: the diagonal (z null) or the polynomial preconditioner's z.
-__global__ void __launch_bounds__(kThreads) k_pcg_dir(PolArgs a, MixArgs m, const float4* __restrict__ z) {
+// beta: the new rho.z over the previous one, or (fused: the stopping test has run in
+// k_pcg_step and moved the sums on) the beta it kept in acc[38].
+__global__ void __launch_bounds__(kThreads) k_pcg_dir(PolArgs a, MixArgs m, const float4* __restrict__ z,
+                                                      int fused) {
     if (m.stop && *m.stop) return;   // the CG solve has stopped (uniform per launch)
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n || !(a.polr2[i] > a.toler)) return;
     const double rz = a.acc[33];
-    const float b = rz != 0.0 ? (float)(a.acc[35] / rz) : 0.f;
+    const float b = fused ? (float)a.acc[38] : (rz != 0.0 ? (float)(a.acc[35] / rz) : 0.f);
     const float4 d = m.d32[i];
     float4 zz;
     if (z) {
@@ -1540,10 +1558,15 @@ __global__ void __launch_bounds__(kThreads) k_pcg_rz(PolArgs a, MixArgs m, const
 // finite), then rho.z <- new rho.z and the sums cleared for the next sweep.
 // st[0]: 0 running, 1 converged, 2 breakdown; st[1]: sweeps run; acc[42..45] the sums of the
 // sweep that stopped it.
-__global__ void k_pcg_next(double* __restrict__ acc, int* __restrict__ st, double target) {
-    if (threadIdx.x != 0 || blockIdx.x != 0 || st[0] != 0) return;
+__device__ void pcg_next_body(double* acc, int* st, double target, bool keep_beta) {
+    if (st[0] != 0) return;
     st[1] += 1;
-    const double dad = acc[34], rz = acc[35], zz = acc[36], cnt = acc[37];
+    // L2 reads: the sums were added by atomics of other blocks
+    const double dad = __ldcg(acc + 34), rz = __ldcg(acc + 35), zz = __ldcg(acc + 36), cnt = __ldcg(acc + 37);
+    if (keep_beta) {
+        const double rz0 = __ldcg(acc + 33);
+        acc[38] = rz0 != 0.0 ? rz / rz0 : 0.0;
+    }
     int state = 0;
     if (!(dad > 0.0) || !isfinite(rz) || !isfinite(zz)) state = 2;
     else if (sqrt(zz / (cnt > 0.0 ? cnt : 1.0)) <= target) state = 1;
@@ -1556,6 +1579,11 @@ __global__ void k_pcg_next(double* __restrict__ acc, int* __restrict__ st, doubl
     }
     acc[33] = rz;
     acc[34] = acc[35] = acc[36] = acc[37] = 0.0;
+}
+
+__global__ void k_pcg_next(double* __restrict__ acc, int* __restrict__ st, double target) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    pcg_next_body(acc, st, target, false);
 }
 
 // mu += d in FP64; refreshes the masked dipoles.
@@ -2677,7 +2705,7 @@ cudaError_t PolarState::reserve(int nw, int K, size_t nfac) {
     const int n = 4 * nw;
     if (!acc && (e = cudaMalloc(&acc, 64 * sizeof(double)))) return e;
     if (!acc_h && (e = cudaMallocHost(&acc_h, 64 * sizeof(double)))) return e;
-    if (!flag && (e = cudaMalloc(&flag, 4 * sizeof(int)))) return e;
+    if (!flag && (e = cudaMalloc(&flag, 8 * sizeof(int)))) return e;
     // a capacity is zeroed before its buffers are replaced, so a failed allocation leaves
     // nothing that a later call would take for allocated
     if (n > n_cap || cap != cap_alloc) {
@@ -3343,7 +3371,7 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
                 restart = false;
                 broke = false;
                 if ((e = cudaMemsetAsync(acc + 33, 0, 5 * sizeof(double), s))) return e;
-                if ((e = cudaMemsetAsync(cgs, 0, 2 * sizeof(int), s))) return e;
+                if ((e = cudaMemsetAsync(cgs, 0, 3 * sizeof(int), s))) return e;   // state, sweeps, ticket
                 k_pcg_init<<<blocks(n, kThreads), kThreads, 0, s>>>(a, m);
                 ++launches;
                 const bool poly = pre > 1;
@@ -3367,7 +3395,9 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
                             launches += 4;
                         }
                         k_pcg_ad<<<blocks(n, kThreads), kThreads, 0, s>>>(a, ms, (K || spme_on) ? 1 : 0);
-                        k_pcg_step<<<blocks(n, kThreads), kThreads, 0, s>>>(a, ms);
+                        // the diagonal preconditioner: the stopping test in k_pcg_step's last block
+                        k_pcg_step<<<blocks(n, kThreads), kThreads, 0, s>>>(a, ms, poly ? nullptr : cgs, target,
+                                                                            cgs + 2);
                         if (poly) {
                             k_pcg_jacobi<<<blocks(n, kThreads), kThreads, 0, s>>>(a, ms, nullptr, cg_z);
                             for (int qq = 1; qq < pre; ++qq) {
@@ -3382,9 +3412,12 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
                             k_pcg_rz<<<blocks(n, kThreads), kThreads, 0, s>>>(a, ms, cg_z, 35, 0);
                             launches += 2;
                         }
-                        k_pcg_dir<<<blocks(n, kThreads), kThreads, 0, s>>>(a, ms, poly ? cg_z : nullptr);
-                        k_pcg_next<<<1, 32, 0, s>>>(acc, cgs, target);
-                        launches += 5;
+                        k_pcg_dir<<<blocks(n, kThreads), kThreads, 0, s>>>(a, ms, poly ? cg_z : nullptr, poly ? 0 : 1);
+                        if (poly) {
+                            k_pcg_next<<<1, 32, 0, s>>>(acc, cgs, target);
+                            ++launches;
+                        }
+                        launches += 4;
                     }
                     if ((e = cudaMemcpyAsync(acc_h + 60, cgs, 2 * sizeof(int), cudaMemcpyDeviceToHost, s))) return e;
                     if ((e = cudaStreamSynchronize(s))) return e;

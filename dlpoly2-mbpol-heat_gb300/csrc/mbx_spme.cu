@@ -28,7 +28,8 @@ namespace {
 
 constexpr double kPiS = 3.141592653589793;
 constexpr int kFftThreads = 256;
-constexpr int kFftPlaneThreads = 256;   // fits beside the overlapped 2B/3B kernel on an SM
+constexpr int kFftPlaneThreads = 1024;  // one block per plane: 64 blocks of a 64^3 grid, so
+                                         // each block needs many warps to hide its latencies
 constexpr int kSpThreads = 128;
 constexpr int kKtThreads = 256;
 constexpr int kMaxGrid = 1024;     // points per axis
@@ -123,6 +124,20 @@ __device__ __forceinline__ void bfly(typename Cx<T>::t* v, int sg) {
     }
 }
 
+// a / d and a % d for d > 0: a shift and a mask when d is a power of two (the usual grid
+// sizes and line counts), the integer division otherwise (the branch is uniform).
+struct IDiv {
+    int d, sh;
+    __device__ __forceinline__ explicit IDiv(int d_) : d(d_), sh(-1) {
+        if ((d_ & (d_ - 1)) == 0) {
+            sh = 0;
+            while ((1 << sh) < d_) ++sh;
+        }
+    }
+    __device__ __forceinline__ int div(int a) const { return sh >= 0 ? a >> sh : a / d; }
+    __device__ __forceinline__ int mod(int a) const { return sh >= 0 ? a & (d - 1) : a % d; }
+};
+
 // One Stockham stage of radix R over nl lines of length n in shared memory ([e][l], pitch P):
 // sub-transforms of length Ns are combined into length Ns R; the output is in natural
 // order after the last stage.
@@ -132,9 +147,10 @@ __device__ __forceinline__ void fft_stage(const typename Cx<T>::t* src, typename
     typedef typename Cx<T>::t C;
     const int nb = n / R;
     const int step = n / (Ns * R);
+    const IDiv dl(nl), ds(Ns);
     for (int b = threadIdx.x; b < nl * nb; b += blockDim.x) {
-        const int l = b % nl, j = b / nl;
-        const int k = j % Ns;
+        const int l = dl.mod(b), j = dl.div(b);
+        const int k = ds.mod(j);
         C v[R];
 #pragma unroll
         for (int t = 0; t < R; ++t) v[t] = src[(j + t * nb) * P + l];
@@ -147,7 +163,7 @@ __device__ __forceinline__ void fft_stage(const typename Cx<T>::t* src, typename
             }
         }
         bfly<T, R>(v, sg);
-        const int o = (j / Ns) * Ns * R + k;
+        const int o = ds.div(j) * Ns * R + k;
 #pragma unroll
         for (int t = 0; t < R; ++t) dst[(o + t * Ns) * P + l] = v[t];
     }
@@ -212,51 +228,49 @@ __global__ void __launch_bounds__(kFftThreads) k_fft_axis(typename Cx<T>::t* dat
         lstride = 1;
     }
     for (int i = threadIdx.x; i < n; i += blockDim.x) tws[i] = tw[ax.tw_off + i];
-    if (axis == 0) {
-        for (int i = threadIdx.x; i < nl * n; i += blockDim.x) {
-            const int l = i / n, e = i % n;
-            C v;
-            v.x = 0;
-            v.y = 0;
-            if (l < lcount) {
-                const size_t off = base + (size_t)l * lstride + e;
-                v = g[off];
-                if (MODE == 3) v = cscale(v, G[off]);
+    // element i of the block's tile: line l and element e (axis 0: l = i / n; else l = i % nl)
+    const IDiv dn(n), dl(nl);
+    const int tot = nl * n, bs = blockDim.x;
+    constexpr int U = 4;   // loads in flight per thread
+    for (int i0 = threadIdx.x; i0 < tot; i0 += U * bs) {
+        C v[U];
+#pragma unroll
+        for (int q = 0; q < U; ++q) {
+            const int i = i0 + q * bs;
+            const int l = axis == 0 ? dn.div(i) : dl.mod(i), e = axis == 0 ? dn.mod(i) : dl.div(i);
+            v[q].x = 0;
+            v[q].y = 0;
+            if (i < tot && l < lcount) {
+                const size_t off = axis == 0 ? base + (size_t)l * lstride + e : base + (size_t)e * estride + l;
+                v[q] = g[off];
+                if (MODE == 3) v[q] = cscale(v[q], G[off]);
             }
-            s0[e * P + l] = v;
         }
-    } else {
-        for (int i = threadIdx.x; i < nl * n; i += blockDim.x) {
-            const int l = i % nl, e = i / nl;
-            C v;
-            v.x = 0;
-            v.y = 0;
-            if (l < lcount) {
-                const size_t off = base + (size_t)e * estride + l;
-                v = g[off];
-                if (MODE == 3) v = cscale(v, G[off]);
-            }
-            s0[e * P + l] = v;
+#pragma unroll
+        for (int q = 0; q < U; ++q) {
+            const int i = i0 + q * bs;
+            const int l = axis == 0 ? dn.div(i) : dl.mod(i), e = axis == 0 ? dn.mod(i) : dl.div(i);
+            if (i < tot) s0[e * P + l] = v[q];
         }
     }
     __syncthreads();
     C* r = fft_lines<T>(s0, s1, ax, P, nl, tws, (MODE == 0 || MODE == 2) ? 1 : -1);
     if (MODE == 2) {
-        for (int i = threadIdx.x; i < nl * n; i += blockDim.x) {
-            const int l = i % nl, e = i / nl;
+        for (int i = threadIdx.x; i < tot; i += bs) {
+            const int l = dl.mod(i), e = dl.div(i);
             if (l < lcount) r[e * P + l] = cscale(r[e * P + l], G[base + (size_t)e * estride + (size_t)l * lstride]);
         }
         __syncthreads();
         r = fft_lines<T>(r, r == s0 ? s1 : s0, ax, P, nl, tws, -1);
     }
     if (axis == 0) {
-        for (int i = threadIdx.x; i < lcount * n; i += blockDim.x) {
-            const int l = i / n, e = i % n;
+        for (int i = threadIdx.x; i < lcount * n; i += bs) {
+            const int l = dn.div(i), e = dn.mod(i);
             g[base + (size_t)l * lstride + e] = r[e * P + l];
         }
     } else {
-        for (int i = threadIdx.x; i < nl * n; i += blockDim.x) {
-            const int l = i % nl, e = i / nl;
+        for (int i = threadIdx.x; i < tot; i += bs) {
+            const int l = dl.mod(i), e = dl.div(i);
             if (l < lcount) g[base + (size_t)e * estride + l] = r[e * P + l];
         }
     }
@@ -916,23 +930,31 @@ __global__ void __launch_bounds__(kFftPlaneThreads) k_fft_plane(typename Cx<T>::
     C* g = data + (size_t)blockIdx.y * gstride + (size_t)blockIdx.x * K1 * K2;
     for (int i = threadIdx.x; i < K1; i += blockDim.x) twx[i] = tw[ax.tw_off + i];
     for (int i = threadIdx.x; i < K2; i += blockDim.x) twy[i] = tw[ay.tw_off + i];
-    for (int i = threadIdx.x; i < K1 * K2; i += blockDim.x) {
-        const int x = i % K1, y = i / K1;
-        s0[x * P1 + y] = g[i];
+    const IDiv dk(K1);
+    const int nxy = K1 * K2, bs = blockDim.x;
+    // the plane's loads issued U at a time per thread (all in flight before the first store)
+    constexpr int U = 4;
+    for (int i0 = threadIdx.x; i0 < nxy; i0 += U * bs) {
+        C v[U];
+#pragma unroll
+        for (int q = 0; q < U; ++q)
+            if (i0 + q * bs < nxy) v[q] = g[i0 + q * bs];
+#pragma unroll
+        for (int q = 0; q < U; ++q) {
+            const int i = i0 + q * bs;
+            if (i < nxy) s0[dk.mod(i) * P1 + dk.div(i)] = v[q];
+        }
     }
     __syncthreads();
     C* r = fft_lines<T>(s0, s1, ax, P1, K2, twx, sg);
     C* t = r == s0 ? s1 : s0;
-    for (int i = threadIdx.x; i < K1 * K2; i += blockDim.x) {
-        const int x = i % K1, y = i / K1;
+    for (int i = threadIdx.x; i < nxy; i += bs) {
+        const int x = dk.mod(i), y = dk.div(i);
         t[y * P2 + x] = r[x * P1 + y];
     }
     __syncthreads();
     C* u = fft_lines<T>(t, r, ay, P2, K1, twy, sg);
-    for (int i = threadIdx.x; i < K1 * K2; i += blockDim.x) {
-        const int x = i % K1, y = i / K1;
-        g[i] = u[y * P2 + x];
-    }
+    for (int i = threadIdx.x; i < nxy; i += bs) g[i] = u[dk.div(i) * P2 + dk.mod(i)];
 }
 
 // Shared memory of the plane pass: two buffers and the x and y twiddles.
