@@ -309,9 +309,17 @@ def run_ours(args, rank, world):
             raise RuntimeError("mbx_water_step_device: %d %s" % (rc, ctx.lib.mbx_error(ctx.h).decode()))
         return sc.copy()
 
+    guess = [0]     # extrapolated initial guess of the dipole solves (mbx_set_dipole_guess)
+    aspc = [None]   # or ASPC (k, iter_nstep) (mbx_set_aspc)
+
     def reset():
         X.copy_(X0)
         DIP.zero_()
+        # a new trajectory: the history of the guess or of ASPC cleared
+        if aspc[0]:
+            ctx.set_aspc(*aspc[0])
+        else:
+            ctx.set_dipole_guess(guess[0])
 
     def drift():
         X.add_(VA, alpha=DT_PS)
@@ -411,6 +419,17 @@ def run_ours(args, rank, world):
         pre_ms[p_] = 1e3 * t_ / 4
     best_pre = min(pre_ms, key=pre_ms.get)
     ctx.set_precond_sweeps(best_pre)
+    # the initial guess of each step's dipole solve: the last step's dipoles (0) or their
+    # extrapolation of degree 1..3 over the last steps (converged to the same toler); timed on
+    # 4 MD steps after 5 warm-up steps
+    guess_ms, guess_it = {}, {}
+    for o_ in (0, 1, 2, 3):
+        guess[0] = o_
+        t_, _, _, inner_ = timed(capi.MIXED, 4, 5)
+        guess_ms[o_] = 1e3 * t_ / 4
+        guess_it[o_] = inner_
+    best_guess = min(guess_ms, key=guess_ms.get)
+    guess[0] = best_guess
     # the MB-pol terms beside the dipole solve (mbx_set_overlap) or after it: off, or on with
     # 3, 4 or 5 of the 8-warp fused kernel's warps on the dimers
     ovl_ms = {}
@@ -432,8 +451,9 @@ def run_ours(args, rank, world):
     # the predicted dipoles and one corrector iteration per step): the same MD steps, mixed
     omega0 = PRM[4]
     PRM[4] = 6.0 / 11.0
-    ctx.set_aspc(4, 6)
+    aspc[0] = (4, 6)
     t_aspc, _, it_aspc, _ = timed(capi.MIXED, args.steps, 7)
+    aspc[0] = None
     ctx.set_aspc(0)
     PRM[4] = omega0
     # phase times of the electrostatics in the mixed step (CUDA events on the launching stream)
@@ -605,6 +625,15 @@ def run_ours(args, rank, world):
                                      "beside the dipole solve with n of 8 warps on the dimers (on_n), each timed "
                                      "on 4 warm-started MD steps (CUDA events), the fastest used for every "
                                      "measurement of the run"},
+        "guess_tuning": {"mixed_step_ms_by_order": {str(k): v for k, v in guess_ms.items()},
+                         "fp32_cg_iterations_per_step_by_order": {str(k): v for k, v in guess_it.items()},
+                         "chosen_order": best_guess,
+                         "method": "the dipole solve of each MD step starts from the last step's dipoles "
+                                   "(order 0, the reference's warm start) or from their polynomial "
+                                   "extrapolation over the last order+1 steps (mbx_set_dipole_guess), and "
+                                   "iterates to the same toler either way; each timed on 4 MD steps after 5 "
+                                   "warm-up steps (CUDA events), the fastest used for every measurement of "
+                                   "the run"},
         "precond_tuning": {"mixed_step_ms_by_jacobi_sweeps": {str(k): v for k, v in pre_ms.items()},
                            "chosen_sweeps": best_pre,
                            "method": "each preconditioner timed on 4 warm-started MD steps of this box "

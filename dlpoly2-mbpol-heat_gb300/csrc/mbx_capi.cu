@@ -1326,6 +1326,14 @@ extern "C" int mbx_set_aspc(mbx_context* ctx, int k, int iter_nstep) {
     return MBX_OK;
 }
 
+extern "C" int mbx_set_dipole_guess(mbx_context* ctx, int order) {
+    if (!ctx) return MBX_ERR_ARG;
+    if (order < 0 || order > 3) return fail(ctx, MBX_ERR_ARG, "dipole guess order must be 0..3");
+    CK(cudaSetDevice(ctx->device));
+    CK(ctx->polar.guess_reset(order));
+    return MBX_OK;
+}
+
 extern "C" int mbx_aspc_restart(mbx_context* ctx) {
     if (!ctx) return MBX_ERR_ARG;
     ctx->polar.aspc_restart();

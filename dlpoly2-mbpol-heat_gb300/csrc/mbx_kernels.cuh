@@ -292,6 +292,11 @@ struct PolarState {
     double* aspc_hist = nullptr;           // k+2 slots of 3 x aspc_n dipoles (x, y, z blocks)
     cudaError_t aspc_reset(int k, int niter);   // aspc_init: history zeroed, step count 0
     void aspc_restart();                         // nstep_for_guess = 0 (an image change)
+    // Not the reference's: the initial guess of the converged solve extrapolated from the last
+    // guess_order+1 steps' dipoles (0: off), the same history; the solve still iterates to toler
+    int guess_order = 0;
+    cudaError_t guess_reset(int order);   // history cleared, step count 0, ASPC off
+    int aspc_slots() const { return aspc_k ? aspc_k + 2 : guess_order + 1; }
     cudaError_t aspc_predict(int n, double* mx, double* my, double* mz, cudaStream_t s);
     cudaError_t aspc_push(int n, const double* mx, const double* my, const double* mz, cudaStream_t s);
 

@@ -606,13 +606,15 @@ __global__ void __launch_bounds__(kThreads) k_pol_static(PolArgs a) {
 }
 
 // Intramolecular (excluded) pairs: static charge field and the three O/H dipole tensors.
+// One thread per excluded pair (6 per water); the field sums by atomics.
 __global__ void k_pol_intra_static(PolArgs a) {
-    const int w = blockIdx.x * blockDim.x + threadIdx.x;
-    if (w >= a.nw) return;
+    const int tt = blockIdx.x * blockDim.x + threadIdx.x;
+    if (tt >= 6 * a.nw) return;
+    const int w = tt / 6, p = tt % 6;
     const int o = 3 * w, m = 3 * a.nw + w;
     const int pr[6][2] = {{o, o + 1}, {o, o + 2}, {o + 1, o + 2}, {o, m}, {o + 1, m}, {o + 2, m}};
     double* T = a.intra + 18 * (size_t)w;
-    for (int p = 0; p < 6; ++p) {
+    {
         const int i = pr[p][0], j = pr[p][1];
         double d[3];
         sep(a, i, j, d[0], d[1], d[2]);
@@ -623,8 +625,8 @@ __global__ void k_pol_intra_static(PolArgs a) {
         bfun_exact(a.alpha, rr, rri, rsqi, bbb);
         const double eki = kR4pie0 * a.q[j] * bbb[1] / a.eps, ekj = kR4pie0 * a.q[i] * bbb[1] / a.eps;
         for (int c = 0; c < 3; ++c) {
-            a.efk[c * a.n + i] += eki * d[c];
-            a.efk[c * a.n + j] -= ekj * d[c];
+            atomicAdd(a.efk + c * a.n + i, eki * d[c]);
+            atomicAdd(a.efk + c * a.n + j, -ekj * d[c]);
         }
         if (p < 3) {
             double t[6] = {0, 0, 0, 0, 0, 0};
@@ -2113,14 +2115,17 @@ __global__ void __launch_bounds__(kThreads) k_pol_ewald2p32(PolArgs a, double g3
 }
 
 // ewald3p over the six excluded pairs of one water (thread per water).
+// One thread per excluded pair (6 per water): the pairs of a water add to the same sites,
+// by atomics.
 __global__ void __launch_bounds__(kThreads) k_pol_ewald3p(PolArgs a, int heat) {
-    const int w = blockIdx.x * blockDim.x + threadIdx.x;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
     double red[11] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
-    if (w < a.nw) {
+    if (t < 6 * a.nw) {
+        const int w = t / 6, p = t % 6;
         const int o = 3 * w, m = 3 * a.nw + w;
         const int pr[6][2] = {{o, o + 1}, {o, o + 2}, {o + 1, o + 2}, {o, m}, {o + 1, m}, {o + 2, m}};
         const double r4e = kR4pie0 / a.eps;
-        for (int p = 0; p < 6; ++p) {
+        {
             const int ia = pr[p][0], ja = pr[p][1];
             double d[3];
             sep(a, ia, ja, d[0], d[1], d[2]);
@@ -2132,8 +2137,8 @@ __global__ void __launch_bounds__(kThreads) k_pol_ewald3p(PolArgs a, int heat) {
             const double qi = a.q[ia], qj = a.q[ja];
             const double cicj = qi * qj;
             red[0] += cicj * bbb[0] * r4e;
-            a.ae[ia] += 0.5 * cicj * bbb[0] * r4e;
-            a.ae[ja] += 0.5 * cicj * bbb[0] * r4e;
+            atomicAdd(a.ae + ia, 0.5 * cicj * bbb[0] * r4e);
+            atomicAdd(a.ae + ja, 0.5 * cicj * bbb[0] * r4e);
             const double espdum = bbb[0] * r4e, espdc = bbb[1] * r4e;
             double ffac = cicj * bbb[1] * r4e;
             const double mi[3] = {a.mx[ia], a.my[ia], a.mz[ia]}, mj[3] = {a.mx[ja], a.my[ja], a.mz[ja]};
@@ -2170,16 +2175,16 @@ __global__ void __launch_bounds__(kThreads) k_pol_ewald3p(PolArgs a, int heat) {
             const double dfz = dfi * mi[2] + dfj * mj[2];
             ffac = ffac + facmu;
             const double fx = ffac * d[0] + dfx, fy = ffac * d[1] + dfy, fz = ffac * d[2] + dfz;
-            a.fx[ia] += fx; a.fy[ia] += fy; a.fz[ia] += fz;
-            a.fx[ja] -= fx; a.fy[ja] -= fy; a.fz[ja] -= fz;
+            atomicAdd(a.fx + ia, fx); atomicAdd(a.fy + ia, fy); atomicAdd(a.fz + ia, fz);
+            atomicAdd(a.fx + ja, -fx); atomicAdd(a.fy + ja, -fy); atomicAdd(a.fz + ja, -fz);
             if (heat) {
                 heat_entry(a, ia, ja, fx, fy, fz, red + 8);
                 heat_entry(a, ja, ia, -fx, -fy, -fz, red + 8);
             }
             const double virdum = dfx * d[0] + dfy * d[1] + dfz * d[2];
             red[1] += -ffac * rsq - virdum;
-            a.vesp[ia] += qj * espdum + rdmuj * espdc;
-            a.vesp[ja] += qi * espdum - rdmui * espdc;
+            atomicAdd(a.vesp + ia, qj * espdum + rdmuj * espdc);
+            atomicAdd(a.vesp + ja, qi * espdum - rdmui * espdc);
             red[2] += d[0] * fx; red[3] += d[0] * fy; red[4] += d[0] * fz;
             red[5] += d[1] * fy; red[6] += d[1] * fz; red[7] += d[2] * fz;
         }
@@ -2457,6 +2462,7 @@ PolarState::~PolarState() { release(); }
 cudaError_t PolarState::aspc_reset(int k, int niter) {
     aspc_k = k;
     aspc_niter = niter;
+    if (k) guess_order = 0;
     aspc_step = 0;
     aspc_head = 0;
     if (aspc_hist) cudaFree(aspc_hist);   // reallocated (zeroed) by the next call
@@ -2466,6 +2472,12 @@ cudaError_t PolarState::aspc_reset(int k, int niter) {
 }
 
 void PolarState::aspc_restart() { aspc_step = 0; }
+
+cudaError_t PolarState::guess_reset(int order) {
+    const cudaError_t e = aspc_reset(0, 0);
+    guess_order = order;
+    return e;
+}
 
 // Kolafa's predictor coefficients B_1..B_{k+2} (J. Comput. Chem. 25 (2004) 335, eq. 6):
 // B_j = (-1)^(j+1) j (4k+6)/(k+3) prod_{m<j} (k+2-m)/(k+3+m), as SOURCE/aspc.f90:110-114
@@ -2485,12 +2497,32 @@ static AspcCoef aspc_coefficients(int k) {
     return c;
 }
 
-// mu = sum_j B_j mu(t - j h) over the history, newest first (SOURCE/aspc.f90:143-170)
+// The initial guess of a converged solve: the polynomial of degree `order` through the last
+// order+1 steps' dipoles, extrapolated one step, c_j = (-1)^(j+1) C(order+1, j) (newest first:
+// 2, -1 linear; 3, -3, 1 quadratic).
+static AspcCoef extrapolation_coefficients(int order) {
+    AspcCoef c{};
+    double b = 1.0;
+    for (int j = 1; j <= order + 1 && j <= 6; ++j) {
+        b = b * double(order + 2 - j) / double(j);   // C(order+1, j)
+        c.b[j - 1] = (j & 1) ? b : -b;
+    }
+    return c;
+}
+
+// mu = sum_j B_j mu(t - j h) over the history, newest first (SOURCE/aspc.f90:143-170).
+// With `carried` (the initial guess of a converged solve) a site keeps the caller's dipole
+// unless it is the newest history entry (the caller carried the last step's dipoles over).
 __global__ void k_aspc_predict(int n, int m, int head, AspcCoef c, const double* __restrict__ hist,
-                               double* __restrict__ mx, double* __restrict__ my, double* __restrict__ mz) {
+                               double* __restrict__ mx, double* __restrict__ my, double* __restrict__ mz,
+                               int carried) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     double* out[3] = {mx, my, mz};
+    if (carried) {
+        const double* h0 = hist + (size_t)head * 3 * n;
+        if (mx[i] != h0[i] || my[i] != h0[n + i] || mz[i] != h0[2 * (size_t)n + i]) return;
+    }
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
         double v = 0.0;
@@ -2504,7 +2536,7 @@ __global__ void k_aspc_predict(int n, int m, int head, AspcCoef c, const double*
 
 cudaError_t PolarState::aspc_predict(int n, double* mx, double* my, double* mz, cudaStream_t s) {
     cudaError_t e;
-    const int m = aspc_k + 2;
+    const int m = aspc_slots();
     if (!aspc_hist || aspc_n != n) {   // a new history (aspc_init): zeroed, the step count restarts
         if (aspc_hist) cudaFree(aspc_hist);
         aspc_hist = nullptr;
@@ -2515,16 +2547,21 @@ cudaError_t PolarState::aspc_predict(int n, double* mx, double* my, double* mz, 
         aspc_step = 0;
     }
     ++aspc_step;
-    if (aspc_step > aspc_niter) {   // as aspc_predict's test (its slots not yet filled are zeros)
+    if (aspc_k && aspc_step > aspc_niter) {   // as aspc_predict's test (slots not yet filled are zeros)
         k_aspc_predict<<<blocks(n, kThreads), kThreads, 0, s>>>(n, m, aspc_head, aspc_coefficients(aspc_k),
-                                                                aspc_hist, mx, my, mz);
+                                                                aspc_hist, mx, my, mz, 0);
+        ++launches;
+    } else if (guess_order && aspc_step > m) {   // m steps in the history
+        k_aspc_predict<<<blocks(n, kThreads), kThreads, 0, s>>>(n, m, aspc_head,
+                                                                extrapolation_coefficients(guess_order), aspc_hist,
+                                                                mx, my, mz, 1);
         ++launches;
     }
     return cudaSuccess;
 }
 
 cudaError_t PolarState::aspc_push(int n, const double* mx, const double* my, const double* mz, cudaStream_t s) {
-    const int m = aspc_k + 2;
+    const int m = aspc_slots();
     aspc_head = (aspc_head + m - 1) % m;
     const double* src[3] = {mx, my, mz};
     for (int d = 0; d < 3; ++d) {
@@ -3001,6 +3038,8 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
         if ((e = aspc_predict(n, mx, my, mz, s))) return e;
         if (aspc_step < 5) a.omega = 0.3;
         aspc_one = aspc_step > aspc_niter;
+    } else if (guess_order && (e = aspc_predict(n, mx, my, mz, s))) {   // the start of a converged solve
+        return e;
     }
     bind(a);
 
@@ -3165,7 +3204,7 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
     bindk(k);
     k_pol_polr6<<<blocks(n, kThreads), kThreads, 0, s>>>(a, polr6);
     k_pol_static<<<blocks(32L * n, kThreads), kThreads, 0, s>>>(a);
-    k_pol_intra_static<<<blocks(nw, 32), 32, 0, s>>>(a);   // one-warp blocks: every SM
+    k_pol_intra_static<<<blocks(6L * nw, 64), 64, 0, s>>>(a);   // a thread per excluded pair
     launches += 3;
     k_pol_mask<<<blocks(n, kThreads), kThreads, 0, s>>>(a, md);
     ++launches;
@@ -3453,7 +3492,7 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
         }
     }
     // aspc_set (SOURCE/dlpoly_cmd.f:2318-2320): the step's dipoles join the history
-    if (aspc_k && (e = aspc_push(n, mx, my, mz, s))) return e;
+    if ((aspc_k || guess_order) && (e = aspc_push(n, mx, my, mz, s))) return e;
     // final pass: after the caller's work that ran beside the solve (its kernels may add to
     // the same force arrays); with no CG solve, that work runs here, before the pass
     if (fork_hook && !forked) {
@@ -3501,7 +3540,7 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
     else
         k_pol_ewald2p<<<blocks(32L * n, kThreads), kThreads, 0, s>>>(a, g34, heat);
     // thread per water, FP64-latency bound: one-warp blocks spread them over every SM
-    k_pol_ewald3p<<<blocks(nw, 32), 32, 0, s>>>(a, heat);
+    k_pol_ewald3p<<<blocks(6L * nw, 64), 64, 0, s>>>(a, heat);   // a thread per excluded pair
     k_pol_qdforce<<<blocks(nw, 32), 32, 0, s>>>(a, heat);
     k_pol_jkin<<<blocks(n, kThreads), kThreads, 0, s>>>(a, ae_out, heat);
     launches += 5;

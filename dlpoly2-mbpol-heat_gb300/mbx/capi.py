@@ -149,6 +149,7 @@ def load(path=None):
     L.mbx_set_aspc.argtypes = [C.c_void_p, C.c_int, C.c_int]
     L.mbx_aspc_step.argtypes = [C.c_void_p]
     L.mbx_aspc_restart.argtypes = [C.c_void_p]
+    L.mbx_set_dipole_guess.argtypes = [C.c_void_p, C.c_int]
     L.mbx_polar_field_timing.argtypes = [C.c_void_p, _D, _D, C.POINTER(C.c_long)]
     L.mbx_set_spme.argtypes = [C.c_void_p, C.c_int, C.c_double, _I]
     L.mbx_set_polar_skin.argtypes = [C.c_void_p, C.c_double]
@@ -453,6 +454,11 @@ class Context:
         steps (default k+2); clears the history and the step count."""
         n = (int(k) + 2 if k else 0) if iter_nstep is None else int(iter_nstep)
         self._check(self.lib.mbx_set_aspc(self.h, int(k), n), "mbx_set_aspc")
+
+    def set_dipole_guess(self, order):
+        """Extrapolated initial guess of the converged dipole solves (order 1..3; 0 off);
+        clears the history."""
+        self._check(self.lib.mbx_set_dipole_guess(self.h, int(order)), "mbx_set_dipole_guess")
 
     def aspc_restart(self):
         self._check(self.lib.mbx_aspc_restart(self.h), "mbx_aspc_restart")

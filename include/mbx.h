@@ -396,6 +396,14 @@ int mbx_set_aspc(mbx_context* ctx, int k, int iter_nstep);
  * is ASPC step 1 again; the history is kept, as the reference keeps it.  mbx_ipi_run does
  * this when the replica changes. */
 int mbx_aspc_restart(mbx_context* ctx);
+/* Not a reference option: the initial guess of each converged dipole solve (ASPC off) is
+ * the polynomial of degree `order` (1..3; 0 off, the default) through the last order+1
+ * calls' converged dipoles, extrapolated one step, for sites whose input dipoles are the
+ * last call's output (the caller carried them over); other sites start from the caller's.
+ * The solve still iterates to toler: results stay within the dipole tolerance of a
+ * warm-started solve; the number of iterations changes.  The history is the ASPC one (per
+ * context; this call clears it and turns ASPC off; mbx_set_aspc turns the guess off). */
+int mbx_set_dipole_guess(mbx_context* ctx, int order);
 /* The ASPC step count of the context (nstep_for_guess); -1 without a context. */
 int mbx_aspc_step(mbx_context* ctx);
 int mbx_water_step_multi(mbx_context* ctx, int precision, int nbox, const int* imcon, const double* cell,

@@ -122,6 +122,42 @@ def test_aspc_steps_match_the_oracle(oracle_lib, precision):
         ctx.close()
 
 
+@pytest.mark.parametrize("precision", [capi.FP64, capi.MIXED])
+def test_dipole_guess_changes_iterations_not_results(oracle_lib, precision):
+    """mbx_set_dipole_guess: on an MD sequence (positions advancing by v dt, dipoles carried
+    over) the extrapolated start needs fewer iterations than the warm start, and every step's
+    results agree with the warm-started ones within the dipole tolerance."""
+    import copy
+    box0 = systems.box_for(32, seed=5)
+    prm = systems.polar_params(alpha=0.6, rcut=4.5, kmax=(8, 8, 8), toler_debye=1e-11)
+    polr, polr2 = systems.polarizabilities(box0.nw)
+    runs = {}
+    for order in (0, 2):
+        ctx = capi.Context(0)
+        try:
+            ctx.set_dipole_guess(order)
+            dip, out = None, []
+            for step in range(7):
+                box = copy.copy(box0)
+                box.xyz = box0.xyz + step * 0.0005 * box0.vel
+                sites, q, dp, _ = oracle_lib.msites_dms(box)
+                got = ctx.polar(sites, box.cell, box.imcon, box.nw, q, dp, polr, polr2, prm, dip0=dip, vel=box.vel,
+                                precision=precision)
+                inner = ctx.polar_inner_sweeps() if precision == capi.MIXED else got["iterations"]
+                out.append((got, inner))
+                dip = got["dipoles"]
+        finally:
+            ctx.close()
+        runs[order] = out
+    # the mixed path's FP32 pair forces round differently for dipoles a tolerance apart
+    ftol = 1e-8 if precision == capi.FP64 else 1e-6
+    for (g0, _), (g2, _) in zip(runs[0], runs[2]):
+        assert np.abs(g2["dipoles"] - g0["dipoles"]).max() <= 1e-8 * np.abs(g0["dipoles"]).max()
+        assert np.abs(g2["forces"] - g0["forces"]).max() <= ftol * np.abs(g0["forces"]).max()
+    # steps 4..7 start from the quadratic extrapolation
+    assert sum(i for _, i in runs[2][3:]) < sum(i for _, i in runs[0][3:])
+
+
 def test_polar_not_converged_status(mbx_ctx, oracle_lib):
     box = systems.box_for(32, seed=5)
     prm = systems.polar_params(alpha=0.6, rcut=4.5, kmax=(6, 6, 6), toler_debye=1e-12, maxit=3)
