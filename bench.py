@@ -1003,9 +1003,9 @@ def batched_whole(steps=4, warmup=2):
 def ipi_loop(frames=12, warmup=2):
     """i-PI driver mode (mbx_ipi_run) on the 4096-water box through a loopback i-PI server:
     each frame is one MD step of the same replica (positions advanced by v dt, sent in bohr),
-    answered with the whole force evaluation (mixed, dispersion on, the server's Ewald
-    settings for the cell) and the water dipoles; wall clock per frame, socket and unit
-    conversion included."""
+    answered with the whole force evaluation (mixed, dispersion on, the server's alpha and
+    rcut for the cell with its SPME k space) and the water dipoles; wall clock per frame,
+    socket and unit conversion included."""
     from mbx import capi, systems
     from mbx.ipi_loopback import FakeIpiServer
     box = systems.config1()
@@ -1016,6 +1016,7 @@ def ipi_loop(frames=12, warmup=2):
     pos = [(box.xyz[:3 * nw] + (k + 1) * DT_PS * box.vel[:3 * nw]) / bohr for k in range(warmup + frames)]
     ctx = capi.Context(0)
     ctx.disp_setup(systems.DISP_PARAMS_SYNTHETIC, rcut=9.0, delr=1.0)
+    ctx.set_spme(SPME_ORDER, spacing=0.78)   # the server's k space: SPME at its 0.78 A spacing
     try:
         srv = FakeIpiServer([(0, h, hinv, p) for p in pos[:warmup]])
         ctx.ipi_run(srv.address, precision=capi.MIXED, dispersion=True)
@@ -1028,8 +1029,9 @@ def ipi_loop(frames=12, warmup=2):
     finally:
         ctx.close()
     return {"frames": n, "steps_per_s": n / t, "ms_per_step": 1e3 * t / n, "waters": nw,
-            "work": "i-PI POSDATA -> whole force evaluation (mixed, dispersion) -> FORCEREADY with the water "
-                    "dipoles, loopback server on 127.0.0.1, dipoles warm-started within the replica"}
+            "work": "i-PI POSDATA -> whole force evaluation (mixed, dispersion; the server's alpha and rcut "
+                    "for the cell, SPME order %d at 0.78 A) -> FORCEREADY with the water dipoles, loopback server "
+                    "on 127.0.0.1, dipoles warm-started within the replica" % SPME_ORDER}
 
 
 def run_case(args):
