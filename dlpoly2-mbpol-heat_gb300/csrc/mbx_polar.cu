@@ -415,13 +415,20 @@ __global__ void k_pol_filter(PolArgs a, const int* __restrict__ nn_s, const int*
     const float bx = (float)a.cl.c[0], by = (float)a.cl.c[4], bz = (float)a.cl.c[8];
     const float ibx = (float)a.cl.inv[0], iby = (float)a.cl.inv[1], ibz = (float)a.cl.inv[2];
     int cnt = 0;
+    // two 32-entry chunks per step: both chunks' index and position loads are issued
+    // before the first test
+    int jn = lane < m ? src[lane] : 0;
+    float4 pn = lane < m ? xf[jn] : make_float4(0.f, 0.f, 0.f, 0.f);
     for (int b = 0; b < m; b += 32) {
         const int q = b + lane;
         bool hit = false;
-        int j = 0;
+        const int j = jn;
+        const float4 pj = pn;
+        if (q + 32 < m) {   // the next chunk's loads, in flight during this chunk's tests
+            jn = src[q + 32];
+            pn = xf[jn];
+        }
         if (q < m) {
-            j = src[q];
-            const float4 pj = xf[j];
             float d2;
             if (ortho) {
                 float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
@@ -1588,6 +1595,14 @@ __global__ void k_pcg_next(double* __restrict__ acc, int* __restrict__ st, doubl
     pcg_next_body(acc, st, target, false);
 }
 
+// SPME: efm += the FP32 k-space field of the correction (its self term included), the
+// k-space field being linear in the dipoles.
+__global__ void k_pol_efm_add(PolArgs a, const float* __restrict__ e32k) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    for (int c = 0; c < 3; ++c) a.efm[c * (size_t)a.n + i] += (double)e32k[c * (size_t)a.n + i];
+}
+
 // mu += d in FP64; refreshes the masked dipoles.
 // Also writes the update of the masked dipoles (the structure factors' dipoles) to d32,
 // for the next field evaluation's k-space part (k_pol_kfield32_dsum).
@@ -2192,9 +2207,12 @@ __global__ void __launch_bounds__(kThreads) k_pol_ewald3p(PolArgs a, int heat) {
     block_sum_atomic<11>(red, a.acc + 0);
 }
 
-// qdforce (new charge assignment) per water, with the summed DMS potentials.
+// qdforce (new charge assignment) with the summed DMS potentials: a thread per (water,
+// site s) - four per water, each repeating the water's geometry - takes the force on site
+// s from the four charges and site s's share of the stress.
 __global__ void __launch_bounds__(kThreads) k_pol_qdforce(PolArgs a, int heat) {
-    const int w = blockIdx.x * blockDim.x + threadIdx.x;
+    const int tq = blockIdx.x * blockDim.x + threadIdx.x;
+    const int w = tq >> 2, s = tq & 3;
     double red[11] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};   // -, vir, stress(6), jpot(3)
     if (w < a.nw) {
         const int io = 3 * w, h1 = io + 1, h2 = io + 2, mt = 3 * a.nw + w;
@@ -2212,8 +2230,8 @@ __global__ void __launch_bounds__(kThreads) k_pol_qdforce(PolArgs a, int heat) {
         const double cott = cost / sint;
         const double r1sqr = r1 * r1, r2sqr = r2 * r2;
         double dr[3][4][3];
-        for (int s = 0; s < 4; ++s)
-            for (int c = 0; c < 3; ++c) dr[0][s][c] = dr[1][s][c] = dr[2][s][c] = 0.0;
+        for (int u = 0; u < 4; ++u)
+            for (int c = 0; c < 3; ++c) dr[0][u][c] = dr[1][u][c] = dr[2][u][c] = 0.0;
         for (int c = 0; c < 3; ++c) {
             dr[0][1][c] = r1v[c] / r1;
             dr[0][0][c] = -dr[0][1][c];
@@ -2240,10 +2258,9 @@ __global__ void __launch_bounds__(kThreads) k_pol_qdforce(PolArgs a, int heat) {
         const double dcosdr23 = -r3 / r1 / r2;
         const int site[4] = {io, h1, h2, mt};
         double vt[4];
-        for (int s = 0; s < 4; ++s) vt[s] = a.vesp[site[s]];
-        double fs[4][3];
-        for (int s = 0; s < 4; ++s) fs[s][0] = fs[s][1] = fs[s][2] = 0.0;
-        for (int s = 0; s < 4; ++s) {   // site whose position moves the charges
+        for (int u = 0; u < 4; ++u) vt[u] = a.vesp[site[u]];
+        double fs[3] = {0.0, 0.0, 0.0};
+        {   // site s, whose position moves the charges
             double dp1[3], dp2[3];
             for (int c = 0; c < 3; ++c) {
                 dp1[c] = dp1dr1 * dr[0][s][c] + dp1dr2 * dr[1][s][c] - sint * dp1dcos * dr[2][s][c];
@@ -2259,17 +2276,14 @@ __global__ void __launch_bounds__(kThreads) k_pol_qdforce(PolArgs a, int heat) {
             }
             for (int j = 0; j < 4; ++j) {   // charge j, in the reference's loop order
                 const double F[3] = {-dq[j][0] * vt[j], -dq[j][1] * vt[j], -dq[j][2] * vt[j]};
-                for (int c = 0; c < 3; ++c) fs[s][c] += F[c];
+                for (int c = 0; c < 3; ++c) fs[c] += F[c];
                 if (heat) heat_entry(a, site[s], j == 3 ? a.nw + w : 3 * w + j, F[0], F[1], F[2], red + 8);
             }
         }
-        a.fx[io] += fs[0][0]; a.fy[io] += fs[0][1]; a.fz[io] += fs[0][2];
-        a.fx[h1] += fs[1][0]; a.fy[h1] += fs[1][1]; a.fz[h1] += fs[1][2];
-        a.fx[h2] += fs[2][0]; a.fy[h2] += fs[2][1]; a.fz[h2] += fs[2][2];
-        a.fx[mt] += fs[3][0]; a.fy[mt] += fs[3][1]; a.fz[mt] += fs[3][2];
+        a.fx[site[s]] += fs[0]; a.fy[site[s]] += fs[1]; a.fz[site[s]] += fs[2];
         double sq[6] = {0, 0, 0, 0, 0, 0}, virq = 0.0;
         const int ta[6] = {0, 0, 0, 1, 1, 2}, tb[6] = {0, 1, 2, 1, 2, 2};
-        for (int s = 0; s < 4; ++s) {
+        {   // the stress of charge s's potential
             const double v = vt[s];
             for (int lab = 1; lab <= 2; ++lab) {
                 const double dqdr_tmp = lab == 1 ? dqdr12[s] : dqdr13[s];
@@ -3353,8 +3367,13 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
         // the field evaluation after a correction: FP64 real space; k space the previous
         // FP64 fields plus the FP32 ones of the correction
         auto fields_delta = [&]() {
-            if (spme_on) {   // the SPME field is cheap: a full FP64 evaluation
-                fields64(false);
+            if (spme_on) {   // FP64 real space; k space the previous FP64 field + the FP32 SPME field of the correction
+                k_pol_dd<<<blocks(32L * n, kThreads), kThreads, 0, s>>>(a);
+                const cudaError_t fe =
+                    spme.field32(n, x, y, z, d32, polr2, k.sfac, dum_self, e32 + 3 * (size_t)n, s, nullptr);
+                if (fe && !field_err) field_err = fe;
+                k_pol_efm_add<<<blocks(n, kThreads), kThreads, 0, s>>>(a, e32 + 3 * (size_t)n);
+                launches += 2 + spme.launches;
                 return;
             }
             k_pol_dd<<<blocks(32L * n, kThreads), kThreads, 0, s>>>(a);
@@ -3541,7 +3560,7 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
         k_pol_ewald2p<<<blocks(32L * n, kThreads), kThreads, 0, s>>>(a, g34, heat);
     // thread per water, FP64-latency bound: one-warp blocks spread them over every SM
     k_pol_ewald3p<<<blocks(6L * nw, 64), 64, 0, s>>>(a, heat);   // a thread per excluded pair
-    k_pol_qdforce<<<blocks(nw, 32), 32, 0, s>>>(a, heat);
+    k_pol_qdforce<<<blocks(4L * nw, 64), 64, 0, s>>>(a, heat);   // a thread per (water, site)
     k_pol_jkin<<<blocks(n, kThreads), kThreads, 0, s>>>(a, ae_out, heat);
     launches += 5;
     if (K) {
