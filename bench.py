@@ -413,12 +413,14 @@ def run_ours(args, rank, world):
     # the mixed solve's preconditioner (Jacobi sweeps on the real-space system, odd): timed on a
     # few MD steps of this box, the fastest kept for the measurements below
     pre_ms = {}
-    for p_ in (1, 3, 5):
-        ctx.set_precond_sweeps(p_)
+    for p_ in (1, 3, 5, "block"):
+        ctx.set_precond_block(p_ == "block")
+        ctx.set_precond_sweeps(1 if p_ == "block" else p_)
         t_, _, _, _ = timed(capi.MIXED, 4, 2)
         pre_ms[p_] = 1e3 * t_ / 4
     best_pre = min(pre_ms, key=pre_ms.get)
-    ctx.set_precond_sweeps(best_pre)
+    ctx.set_precond_block(best_pre == "block")
+    ctx.set_precond_sweeps(1 if best_pre == "block" else best_pre)
     # the initial guess of each step's dipole solve: the last step's dipoles (0) or their
     # extrapolation of degree 1..3 over the last steps (converged to the same toler); timed on
     # 4 MD steps after 5 warm-up steps
@@ -636,7 +638,8 @@ def run_ours(args, rank, world):
                                    "the run"},
         "precond_tuning": {"mixed_step_ms_by_jacobi_sweeps": {str(k): v for k, v in pre_ms.items()},
                            "chosen_sweeps": best_pre,
-                           "method": "each preconditioner timed on 4 warm-started MD steps of this box "
+                           "method": "the diagonal (1), 3 or 5 Jacobi sweeps, or the per-water 9x9 block "
+                                     "inverse (block), each timed on 4 warm-started MD steps of this box "
                                      "(CUDA events), the fastest used for every measurement of the run"},
         "fused_split_tuning": {"fused_kernel_ms_by_dimer_warps": {str(k): v for k, v in split_ms.items()},
                                "chosen_dimer_warps": best_split,

@@ -1342,6 +1342,12 @@ extern "C" int mbx_aspc_restart(mbx_context* ctx) {
 
 extern "C" int mbx_aspc_step(mbx_context* ctx) { return ctx ? ctx->polar.aspc_step : -1; }
 
+extern "C" int mbx_set_precond_block(mbx_context* ctx, int on) {
+    if (!ctx) return MBX_ERR_ARG;
+    ctx->polar.precond_block = on != 0;
+    return MBX_OK;
+}
+
 extern "C" int mbx_set_spme(mbx_context* ctx, int order, double spacing, const int* grid) {
     if (!ctx) return MBX_ERR_ARG;
     if (order != 0 && (order < 4 || order > 8)) return fail(ctx, MBX_ERR_ARG, "SPME order must be 0 or 4..8");

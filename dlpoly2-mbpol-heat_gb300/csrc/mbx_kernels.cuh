@@ -244,6 +244,9 @@ struct PolarState {
     float4* cg_z = nullptr;                // preconditioned residual of the correction solve
     int precond_sweeps = 0;                // Jacobi sweeps of the CG preconditioner (odd; 1: diagonal
                                            // only; 0: 1 with SPME, 3 with the Ewald sum)
+    bool precond_block = true;             // the per-water block-Jacobi preconditioner instead
+    float* binv = nullptr;                 // its 9x9 inverses (81 floats per water)
+    int binv_cap = 0;
     float* e32 = nullptr;
     int cap32 = 0, n32 = 0, k32 = 0;
     size_t fac32_cap = 0;

@@ -1529,6 +1529,121 @@ __global__ void __launch_bounds__(kThreads) k_pcg_dir(PolArgs a, MixArgs m, cons
     m.d32[i] = make_float4(zz.x + b * d.x, zz.y + b * d.y, zz.z + b * d.z, 0.f);
 }
 
+// Block-Jacobi preconditioner: per water, the inverse of the 9x9 block of the CG matrix
+// A = r4pie0/polr2 - dum - T over its three sites (the diagonal, the self term and the
+// intramolecular tensors O-H1, O-H2, H1-H2; the k-space coupling inside the block left
+// out), by Cholesky in FP32, stored whole (81 floats per water).  A water whose block is not
+// positive definite, or with a site that carries no dipole, keeps the diagonal.
+__global__ void k_pcg_block_setup(PolArgs a, float dum, float* __restrict__ binv) {
+    const int w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= a.nw) return;
+    float B[9][9];
+    float d[3];
+    bool ok = true;
+    for (int s = 0; s < 3; ++s) {
+        const double p2 = a.polr2[3 * w + s];
+        ok = ok && p2 > a.toler;
+        d[s] = p2 > a.toler ? (float)(kR4pie0 / p2) : 0.f;
+    }
+#pragma unroll
+    for (int r = 0; r < 9; ++r)
+#pragma unroll
+        for (int c = 0; c < 9; ++c) B[r][c] = 0.f;
+#pragma unroll
+    for (int s = 0; s < 3; ++s)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) B[3 * s + c][3 * s + c] = d[s] - dum;
+    const int pa[3] = {0, 0, 1}, pb[3] = {1, 2, 2};
+    const int ia[6] = {0, 0, 0, 1, 1, 2}, ib[6] = {0, 1, 2, 1, 2, 2};
+    const float* T = a.intra32 + 18 * (size_t)w;
+#pragma unroll
+    for (int p = 0; p < 3; ++p)
+#pragma unroll
+        for (int q = 0; q < 6; ++q) {
+            const float t = T[6 * p + q];
+            const int r = 3 * pa[p] + ia[q], c = 3 * pb[p] + ib[q];
+            const int r2 = 3 * pa[p] + ib[q], c2 = 3 * pb[p] + ia[q];
+            B[r][c] = -t;   // the (a, b) block and its transpose
+            B[c][r] = -t;
+            B[r2][c2] = -t;
+            B[c2][r2] = -t;
+        }
+    // B = L L^T in place (lower triangle)
+#pragma unroll
+    for (int j = 0; j < 9; ++j) {
+        float v = B[j][j];
+#pragma unroll
+        for (int k = 0; k < j; ++k) v -= B[j][k] * B[j][k];
+        ok = ok && v > 0.f;
+        const float ljj = sqrtf(fmaxf(v, 1e-30f)), rl = 1.f / ljj;
+        B[j][j] = ljj;
+#pragma unroll
+        for (int i = j + 1; i < 9; ++i) {
+            float u = B[i][j];
+#pragma unroll
+            for (int k = 0; k < j; ++k) u -= B[i][k] * B[j][k];
+            B[i][j] = u * rl;
+        }
+    }
+    float* out = binv + 81 * (size_t)w;
+    if (!ok) {   // the diagonal
+        for (int r = 0; r < 9; ++r)
+            for (int c = 0; c < 9; ++c) out[9 * r + c] = (r == c && d[r / 3] > 0.f) ? 1.f / d[r / 3] : 0.f;
+        return;
+    }
+    // M = L^-1 (lower), written into the upper triangle of B transposed: Mt[k][i] = M[i][k]
+    float M[9][9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) {
+#pragma unroll
+        for (int k = 0; k < 9; ++k) M[i][k] = 0.f;
+        M[i][i] = 1.f / B[i][i];
+#pragma unroll
+        for (int k = 0; k < i; ++k) {
+            float u = 0.f;
+#pragma unroll
+            for (int q = k; q < i; ++q) u += B[i][q] * M[q][k];
+            M[i][k] = -u * M[i][i];
+        }
+    }
+    // B^-1 = M^T M
+#pragma unroll
+    for (int r = 0; r < 9; ++r)
+#pragma unroll
+        for (int c = 0; c < 9; ++c) {
+            float u = 0.f;
+#pragma unroll
+            for (int q = 0; q < 9; ++q) u += M[q][r] * M[q][c];
+            out[9 * r + c] = u;
+        }
+}
+
+// z = M^-1 rho with the block inverses: a thread per site, the three rows of its water's
+// inverse times the water's residual; the sites of no water (M sites) 0.
+__global__ void __launch_bounds__(kThreads) k_pcg_block(PolArgs a, MixArgs m, const float* __restrict__ binv,
+                                                        float4* __restrict__ z) {
+    if (m.stop && *m.stop) return;   // the CG solve has stopped (uniform per launch)
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    if (i >= 3 * a.nw) {
+        z[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        return;
+    }
+    const int w = i / 3, s = i % 3;
+    const float4 r0 = m.rho[3 * w], r1 = m.rho[3 * w + 1], r2 = m.rho[3 * w + 2];
+    const float rv[9] = {r0.x, r0.y, r0.z, r1.x, r1.y, r1.z, r2.x, r2.y, r2.z};
+    const float* B = binv + 81 * (size_t)w + 27 * s;
+    float o[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        float u = 0.f;
+#pragma unroll
+        for (int q = 0; q < 9; ++q) u += B[9 * c + q] * rv[q];
+        o[c] = u;
+    }
+    z[i] = make_float4(o[0], o[1], o[2], 0.f);
+}
+
 // Polynomial preconditioner: p Jacobi sweeps on the real-space part of the system,
 // (D - T_real) z = rho with D = r4pie0 / polr2, from z = 0:
 //   z <- D^-1 (rho + T_real z)   (t = T_real z; t null: the first sweep, z = D^-1 rho),
@@ -2415,7 +2530,7 @@ void PolarState::release() {
     void* p[] = {ercp, ercp32, nn_s, nbr_s, npol_s, nup_s, xref, nn, nbr, npol, nup, flag, xf, tens, intra, fld, vesp, ae, eik, kv, kx2, lmn, sf, kterm, acc, kco, fac, md, vh, polr6,
                  ckey, cskey, cidx, csidx, csort, cstart, cend,
                  tens32, r32, d32, e32, kco32, fac32, ktile, kaux, kcol, colk, kpart, cg_x, cg_r, cg_q, cg_z, vh32,
-                 aspc_hist};
+                 aspc_hist, binv};
     for (void* q : p)
         if (q) cudaFree(q);
     if (acc_h) cudaFreeHost(acc_h);
@@ -2469,6 +2584,8 @@ void PolarState::release() {
     tab_alpha = tab_rcut = -1.0;
     aspc_hist = nullptr;
     aspc_n = aspc_head = 0;
+    binv = nullptr;
+    binv_cap = 0;
 }
 
 PolarState::~PolarState() { release(); }
@@ -3349,12 +3466,30 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
         // with SPME a CG sweep's k space is cheap beside two more real-space sweeps: the
         // diagonal; with the Ewald sum the polynomial's fewer sweeps pay
         int pre = (precond_sweeps > 0 ? precond_sweeps : (spme_on ? 1 : 3)) | 1;
+        // the block-Jacobi preconditioner (per-water 9x9 inverses), in place of the sweeps
+        bool blk = precond_block && nw > 0;
+        if (blk) {
+            if (binv_cap < nw) {
+                if (binv) cudaFree(binv);
+                binv = nullptr;
+                binv_cap = 0;
+                if ((e = cudaMalloc(&binv, 81 * (size_t)nw * sizeof(float)))) return e;
+                binv_cap = nw;
+            }
+            k_pcg_block_setup<<<blocks(nw, 64), 64, 0, s>>>(a, (float)dum_self, binv);
+            ++launches;
+        }
         auto precondition = [&](int slot, int dir) -> cudaError_t {
-            k_pcg_jacobi<<<blocks(n, kThreads), kThreads, 0, s>>>(a, m, nullptr, cg_z);
-            for (int q = 1; q < pre; ++q) {
-                k_pol_dd32<<<blocks(32L * n, kThreads), kThreads, 0, s>>>(a, cg_z, e32 + 3 * (size_t)n);
-                k_pcg_jacobi<<<blocks(n, kThreads), kThreads, 0, s>>>(a, m, e32 + 3 * (size_t)n, cg_z);
-                launches += 2;
+            if (blk) {
+                k_pcg_block<<<blocks(n, kThreads), kThreads, 0, s>>>(a, m, binv, cg_z);
+                ++launches;
+            } else {
+                k_pcg_jacobi<<<blocks(n, kThreads), kThreads, 0, s>>>(a, m, nullptr, cg_z);
+                for (int q = 1; q < pre; ++q) {
+                    k_pol_dd32<<<blocks(32L * n, kThreads), kThreads, 0, s>>>(a, cg_z, e32 + 3 * (size_t)n);
+                    k_pcg_jacobi<<<blocks(n, kThreads), kThreads, 0, s>>>(a, m, e32 + 3 * (size_t)n, cg_z);
+                    launches += 2;
+                }
             }
             cudaError_t err;
             if ((err = cudaMemsetAsync(acc + slot, 0, sizeof(double), s))) return err;
@@ -3406,7 +3541,10 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
             }
             // an outer step that did not halve the FP64 residual: the diagonal preconditioner
             // from here on
-            if (pre > 1 && !(rms <= 0.5 * rms_prev)) pre = 1;
+            if ((pre > 1 || blk) && !(rms <= 0.5 * rms_prev)) {
+                pre = 1;
+                blk = false;
+            }
             rms_prev = rms;
             // |z| (the preconditioned residual of the correction, a dipole) down to
             // 1e-6 of the FP64 residual or 5x below toler
@@ -3432,7 +3570,7 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
                 if ((e = cudaMemsetAsync(cgs, 0, 3 * sizeof(int), s))) return e;   // state, sweeps, ticket
                 k_pcg_init<<<blocks(n, kThreads), kThreads, 0, s>>>(a, m);
                 ++launches;
-                const bool poly = pre > 1;
+                const bool poly = pre > 1 || blk;
                 if (poly && (e = precondition(33, 1))) return e;
                 int queued = 0, batch = std::max(2, std::min(cg_hint, 40));
                 int st[2] = {0, 0};
@@ -3456,7 +3594,13 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
                         // the diagonal preconditioner: the stopping test in k_pcg_step's last block
                         k_pcg_step<<<blocks(n, kThreads), kThreads, 0, s>>>(a, ms, poly ? nullptr : cgs, target,
                                                                             cgs + 2);
-                        if (poly) {
+                        if (poly && blk) {
+                            k_pcg_block<<<blocks(n, kThreads), kThreads, 0, s>>>(a, ms, binv, cg_z);
+                            // rho.z of the block z replaces k_pcg_step's diagonal one
+                            if ((e = cudaMemsetAsync(acc + 35, 0, sizeof(double), s))) return e;
+                            k_pcg_rz<<<blocks(n, kThreads), kThreads, 0, s>>>(a, ms, cg_z, 35, 0);
+                            launches += 2;
+                        } else if (poly) {
                             k_pcg_jacobi<<<blocks(n, kThreads), kThreads, 0, s>>>(a, ms, nullptr, cg_z);
                             for (int qq = 1; qq < pre; ++qq) {
                                 k_pol_dd32<<<blocks(32L * n, kThreads), kThreads, 0, s>>>(a, cg_z, e32 + 3 * (size_t)n,
@@ -3489,8 +3633,9 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
                 // positive definite in FP32 here; the diagonal preconditioner takes over,
                 // and with it an FP64 SOR step replaces this correction
                 if (st[0] == 2) {
-                    if (pre > 1) {
+                    if (pre > 1 || blk) {
                         pre = 1;
+                        blk = false;
                         restart = true;
                     } else {
                         broke = true;

@@ -146,6 +146,7 @@ def load(path=None):
     L.mbx_water_step.argtypes = [C.c_void_p, C.c_int, C.c_int, _D, C.c_int, C.c_int, _D, _D, _D, _I, _I] + [_D] * 16
     L.mbx_set_lanes.argtypes = [C.c_void_p, C.c_int]
     L.mbx_set_precond_sweeps.argtypes = [C.c_void_p, C.c_int]
+    L.mbx_set_precond_block.argtypes = [C.c_void_p, C.c_int]
     L.mbx_set_aspc.argtypes = [C.c_void_p, C.c_int, C.c_int]
     L.mbx_aspc_step.argtypes = [C.c_void_p]
     L.mbx_aspc_restart.argtypes = [C.c_void_p]
@@ -445,6 +446,11 @@ class Context:
                                   int(max_steps), C.byref(steps))
         self._check(rc, "mbx_ipi_run")
         return int(steps.value)
+
+    def set_precond_block(self, on):
+        """Per-water block-Jacobi preconditioner of the mixed dipole solve (on by default;
+        off: the sweeps of set_precond_sweeps)."""
+        self._check(self.lib.mbx_set_precond_block(self.h, int(bool(on))), "mbx_set_precond_block")
 
     def set_precond_sweeps(self, sweeps):
         self._check(self.lib.mbx_set_precond_sweeps(self.h, int(sweeps)), "mbx_set_precond_sweeps")

@@ -369,14 +369,22 @@ int mbx_water_step_device(mbx_context* ctx, int precision, int imcon, const doub
  * not converge (everything written), else MBX_OK.
  */
 int mbx_set_lanes(mbx_context* ctx, int lanes);
-/* MBX_MIXED dipole solve: Jacobi sweeps of the conjugate-gradient preconditioner on the
- * real-space part of the dipole equations, odd 1..9 (1: the diagonal alone), or 0 (the
- * default): 1 with SPME, whose k space makes a CG sweep cheap beside two more real-space
- * sweeps, 3 with the Ewald sum.
+/* MBX_MIXED dipole solve, with the block preconditioner off (mbx_set_precond_block): Jacobi
+ * sweeps of the conjugate-gradient preconditioner on the real-space part of the dipole
+ * equations, odd 1..9 (1: the diagonal alone), or 0 (the default): 1 with SPME, whose k
+ * space makes a CG sweep cheap beside two more real-space sweeps, 3 with the Ewald sum.
  * An odd count keeps the preconditioner positive definite; a breakdown or an outer step
  * that does not halve the residual falls back to the diagonal.  Changes the iteration
  * count, not the converged dipoles beyond the dipole tolerance. */
 int mbx_set_precond_sweeps(mbx_context* ctx, int sweeps);
+/* MBX_MIXED dipole solve: with on != 0 (the default) the conjugate-gradient preconditioner
+ * is the inverse of each water's 9x9 block of the system (the polarizabilities, the self
+ * term and the three intramolecular dipole tensors; Cholesky per water once per call)
+ * instead of the sweeps of mbx_set_precond_sweeps, which apply with on == 0.  A water whose
+ * block is not positive definite keeps the diagonal; a breakdown or an outer step that does
+ * not halve the residual falls back to the diagonal.  Changes the iteration count, not the
+ * converged dipoles beyond the dipole tolerance. */
+int mbx_set_precond_block(mbx_context* ctx, int on);
 /* ASPC dipole prediction, the CONTROL keywords `aspc` and `aspc_k` (replaces aspc_init,
  * aspc_predict and aspc_set of SOURCE/aspc.f90:45-251 with the ASPC branch of the dipole
  * loop, SOURCE/forces.f:334-366, as SOURCE/dlpoly_cmd.f:2273-2320 drives them).

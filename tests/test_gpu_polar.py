@@ -274,8 +274,9 @@ def test_polar_phase_timings(mbx_ctx, oracle_lib):
 
 def test_polar_mixed_preconditioner_settings(mbx_ctx, oracle_lib):
     """The mixed solve's preconditioner (mbx_set_precond_sweeps: 0 automatic, 1 diagonal, 3,
-    5) changes the iteration count, not the converged results beyond the mixed budgets; even
-    counts (not positive definite in general) are refused."""
+    5; mbx_set_precond_block: the per-water block inverse) changes the iteration count, not
+    the converged results beyond the mixed budgets; even counts (not positive definite in
+    general) are refused."""
     box = systems.config0()
     prm = systems.polar_params(alpha=0.3, rcut=9.0, kmax=(8, 8, 8), toler_debye=1e-8)
     sites, q, dp, polr, polr2, prm = _case(oracle_lib, box, prm)
@@ -284,8 +285,9 @@ def test_polar_mixed_preconditioner_settings(mbx_ctx, oracle_lib):
         mbx_ctx.set_precond_sweeps(2)
     sweeps = {}
     try:
-        for p in (0, 1, 3, 5):
-            mbx_ctx.set_precond_sweeps(p)
+        for p in (0, 1, 3, 5, "block"):
+            mbx_ctx.set_precond_block(p == "block")
+            mbx_ctx.set_precond_sweeps(1 if p == "block" else p)
             got = mbx_ctx.polar(sites, box.cell, box.imcon, box.nw, q, dp, polr, polr2, prm, vel=box.vel,
                                 precision=capi.MIXED)
             sweeps[p] = mbx_ctx.polar_inner_sweeps()
@@ -294,9 +296,12 @@ def test_polar_mixed_preconditioner_settings(mbx_ctx, oracle_lib):
             f, fr = got["forces"], ref["forces"]
             assert np.sqrt(np.mean((f - fr) ** 2)) <= 1e-6 * np.sqrt(np.mean(fr ** 2))
     finally:
+        mbx_ctx.set_precond_block(True)   # the default
         mbx_ctx.set_precond_sweeps(0)
     assert min(sweeps.values()) > 0
     assert sweeps[0] == sweeps[3]   # automatic with the Ewald sum: the 3-sweep polynomial
+    # the per-water block inverse takes fewer sweeps than the diagonal
+    assert sweeps["block"] < sweeps[1], sweeps
 
 
 @pytest.mark.parametrize("precision", [capi.FP64, capi.MIXED])
