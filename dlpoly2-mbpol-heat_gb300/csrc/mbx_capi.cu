@@ -685,10 +685,12 @@ extern "C" int mbx_disp_setup(mbx_context* ctx, int ntypes, const double* prm, d
     return MBX_OK;
 }
 
-extern "C" int mbx_disp_forces_device(mbx_context* ctx, int imcon, const double* cell, int natms, const int* ltype,
-                                      const int* molecule, const double* xxx, const double* yyy, const double* zzz,
-                                      double* fxx, double* fyy, double* fzz, const double* vxx, const double* vyy,
-                                      const double* vzz, double* atomic_energy, double* out) {
+// The dispersion on device arrays; fp32: the mixed form (k_disp_forces32), used by the
+// mixed whole evaluation.
+static int disp_forces_dev(mbx_context* ctx, int imcon, const double* cell, int natms, const int* ltype,
+                           const int* molecule, const double* xxx, const double* yyy, const double* zzz, double* fxx,
+                           double* fyy, double* fzz, const double* vxx, const double* vyy, const double* vzz,
+                           double* atomic_energy, double* out, bool fp32) {
     if (!ctx) return MBX_ERR_ARG;
     if (!ctx->disp.vvv) return fail(ctx, MBX_ERR_ARG, "mbx_disp_setup has not been called");
     if (natms < 0 || (natms > 0 && (!ltype || !molecule || !xxx || !yyy || !zzz || !fxx || !fyy || !fzz)))
@@ -704,7 +706,7 @@ extern "C" int mbx_disp_forces_device(mbx_context* ctx, int imcon, const double*
     if (natms > 0) {
         const cudaError_t e = ctx->disp.forces(cl, natms, ltype, molecule, xxx, yyy, zzz, fxx, fyy, fzz,
                                                heat ? vxx : nullptr, heat ? vyy : nullptr, heat ? vzz : nullptr,
-                                               atomic_energy, ctx->acc, ctx->totals_h, s, &rebuilt);
+                                               atomic_energy, ctx->acc, ctx->totals_h, s, &rebuilt, fp32);
         if (e == cudaErrorInvalidValue) return fail(ctx, MBX_ERR_CAPACITY, "dispersion list capacity exceeded");
         CK(e);
     }
@@ -712,6 +714,14 @@ extern "C" int mbx_disp_forces_device(mbx_context* ctx, int imcon, const double*
     CK(cudaStreamSynchronize(s));
     if (out) std::memcpy(out, ctx->acc_h, 14 * sizeof(double));
     return MBX_OK;
+}
+
+extern "C" int mbx_disp_forces_device(mbx_context* ctx, int imcon, const double* cell, int natms, const int* ltype,
+                                      const int* molecule, const double* xxx, const double* yyy, const double* zzz,
+                                      double* fxx, double* fyy, double* fzz, const double* vxx, const double* vyy,
+                                      const double* vzz, double* atomic_energy, double* out) {
+    return disp_forces_dev(ctx, imcon, cell, natms, ltype, molecule, xxx, yyy, zzz, fxx, fyy, fzz, vxx, vyy, vzz,
+                           atomic_energy, out, false);
 }
 
 extern "C" int mbx_disp_forces(mbx_context* ctx, int imcon, const double* cell, int natms, const int* ltype,
@@ -863,9 +873,9 @@ extern "C" int mbx_water_forces(mbx_context* ctx, int precision, int imcon, cons
             ctx->disp_types_h.assign(ltype, ltype + natms);
             ctx->disp_mol_h.assign(molecule, molecule + natms);
         }
-        rc = mbx_disp_forces_device(ctx, imcon, cell, natms, d_typ, d_mol, dx, dy, dz, dfx, dfy, dfz,
-                                    heat ? dvx : nullptr, heat ? dvy : nullptr, heat ? dvz : nullptr, dae,
-                                    sc + MBX_NSCALARS + 14);
+        rc = disp_forces_dev(ctx, imcon, cell, natms, d_typ, d_mol, dx, dy, dz, dfx, dfy, dfz,
+                             heat ? dvx : nullptr, heat ? dvy : nullptr, heat ? dvz : nullptr, dae,
+                             sc + MBX_NSCALARS + 14, precision == MBX_MIXED);
         if (rc) return rc;
     }
     Cell cl;
@@ -1130,9 +1140,9 @@ int water_step_core(mbx_context* ctx, int precision, int imcon, const double* ce
                                       sc + MBX_NSCALARS);
     if (rc) return rc;
     if (d_typ && d_mol) {
-        rc = mbx_disp_forces_device(ctx, imcon, cell, natms, d_typ, d_mol, dx, dy, dz, dfx, dfy, dfz,
-                                    heat ? dvx : nullptr, heat ? dvy : nullptr, heat ? dvz : nullptr, dae,
-                                    sc + MBX_NSCALARS + 14);
+        rc = disp_forces_dev(ctx, imcon, cell, natms, d_typ, d_mol, dx, dy, dz, dfx, dfy, dfz,
+                             heat ? dvx : nullptr, heat ? dvy : nullptr, heat ? dvz : nullptr, dae,
+                             sc + MBX_NSCALARS + 14, precision == MBX_MIXED);
         if (rc) return rc;
     }
     if (!overlap) {

@@ -314,6 +314,100 @@ __global__ void __launch_bounds__(kThreads) k_disp_forces(DispArgs a, const int*
     block_sum_atomic<14>(red, a.acc14);
 }
 
+// The mixed-precision form of k_disp_forces: the separation, the image and the cut test in
+// FP64 as there (the same pairs), the rest in FP32: the distance, the 3-point interpolation of
+// FP32 copies of the tables, the forces, and per-lane FP32 partial sums of the forces,
+// energies, virial, stress and heat terms, turned into FP64 for the warp and block sums
+// and for the partner atomics.
+__global__ void __launch_bounds__(kThreads) k_disp_forces32(DispArgs a, const int* __restrict__ nn,
+                                                             const int* __restrict__ nbr, int cap,
+                                                             const float* __restrict__ vvv32,
+                                                             const float* __restrict__ ggg32,
+                                                             const float4* __restrict__ vf, float rdr32) {
+    const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    float rf[14];
+#pragma unroll
+    for (int q = 0; q < 14; ++q) rf[q] = 0.f;
+    float fi[3] = {0.f, 0.f, 0.f}, aei = 0.f;
+    if (i < a.natms) {   // warp-uniform
+        const int n = nn[i];
+        const int ti = a.ltype[i];
+        const double xi = a.x[i], yi = a.y[i], zi = a.z[i];
+        const float4 vi = vf ? vf[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int m = lane; m < n; m += 32) {
+            const int j = nbr[(size_t)i * cap + m];
+            const int k = pair_index(ti, a.ltype[j]);
+            if (!((a.vdw_pairs[k >> 6] >> (k & 63)) & 1ull)) continue;
+            double dx = dsub(xi, a.x[j]), dy = dsub(yi, a.y[j]), dz = dsub(zi, a.z[j]);
+            const float rx = (float)dx, ry = (float)dy, rz = (float)dz;   // the raw separation
+            image(a.cl, dx, dy, dz);
+            const double rsq = dadd(dadd(dmul(dx, dx), dmul(dy, dy)), dmul(dz, dz));
+            if (!(a.rcsq > rsq)) continue;
+            const float d0 = (float)dx, d1 = (float)dy, d2 = (float)dz;
+            const float r2 = d0 * d0 + d1 * d1 + d2 * d2;
+            const float ri = rsqrtf(r2);
+            const float u = r2 * ri * rdr32;
+            const int l = max((int)u, 1);
+            const float ppp = u - (float)l;
+            const float* vt = vvv32 + (size_t)k * a.mxgrid + (l - 1);
+            const float* gt = ggg32 + (size_t)k * a.mxgrid + (l - 1);
+            float t1 = vt[0] + (vt[1] - vt[0]) * ppp;
+            float t2 = vt[1] + (vt[2] - vt[1]) * (ppp - 1.f);
+            const float e = t1 + (t2 - t1) * ppp * 0.5f;
+            t1 = gt[0] + (gt[1] - gt[0]) * ppp;
+            t2 = gt[1] + (gt[2] - gt[1]) * (ppp - 1.f);
+            const float gamma = (t1 + (t2 - t1) * ppp * 0.5f) * (ri * ri);
+            const float f0 = gamma * d0, f1 = gamma * d1, f2 = gamma * d2;
+            fi[0] += f0;
+            fi[1] += f1;
+            fi[2] += f2;
+            atomicAdd(a.fx + j, -(double)f0);
+            atomicAdd(a.fy + j, -(double)f1);
+            atomicAdd(a.fz + j, -(double)f2);
+            rf[0] += e;
+            if (a.ae) {
+                aei += 0.5f * e;
+                atomicAdd(a.ae + j, (double)(0.5f * e));
+            }
+            rf[1] -= gamma * r2;
+            rf[2] += d0 * f0; rf[3] += d0 * f1; rf[4] += d0 * f2;
+            rf[6] += d1 * f1; rf[7] += d1 * f2; rf[10] += d2 * f2;
+            if (vf) {
+                const float4 vj = vf[j];
+                const float fv = f0 * (vi.x + vj.x) + f1 * (vi.y + vj.y) + f2 * (vi.z + vj.z);
+                rf[11] += rx * fv;
+                rf[12] += ry * fv;
+                rf[13] += rz * fv;
+            }
+        }
+        double fd[3] = {(double)fi[0], (double)fi[1], (double)fi[2]};
+#pragma unroll
+        for (int c = 0; c < 3; ++c) fd[c] = warp_sum(fd[c]);
+        const double aed = warp_sum((double)aei);
+        if (lane == 0 && (fd[0] != 0.0 || fd[1] != 0.0 || fd[2] != 0.0)) {
+            atomicAdd(a.fx + i, fd[0]);
+            atomicAdd(a.fy + i, fd[1]);
+            atomicAdd(a.fz + i, fd[2]);
+        }
+        if (lane == 0 && a.ae && aed != 0.0) atomicAdd(a.ae + i, aed);
+    }
+    rf[5] = rf[3];
+    rf[8] = rf[4];
+    rf[9] = rf[7];
+    double red[14];
+#pragma unroll
+    for (int q = 0; q < 14; ++q) red[q] = (double)rf[q];
+    block_sum_atomic<14>(red, a.acc14);
+}
+
+// FP32 copies of the velocities (the mixed form's heat terms)
+__global__ void k_disp_vf(int natms, const double* __restrict__ vx, const double* __restrict__ vy,
+                          const double* __restrict__ vz, float4* __restrict__ vf) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < natms) vf[i] = make_float4((float)vx[i], (float)vy[i], (float)vz[i], 0.f);
+}
+
 int grid(long threads) { return (int)((threads + kThreads - 1) / kThreads); }
 
 }  // namespace
@@ -321,10 +415,13 @@ int grid(long threads) { return (int)((threads + kThreads - 1) / kThreads); }
 DispState::~DispState() { release(); }
 
 void DispState::release() {
-    void* p[] = {vvv, ggg, nn, nbr, xref, flag, key, skey, idx, sidx, cstart, cend, sort_tmp};
+    void* p[] = {vvv, ggg, nn, nbr, xref, flag, key, skey, idx, sidx, cstart, cend, sort_tmp, vvv32, vf};
     for (void* q : p)
         if (q) cudaFree(q);
     vvv = ggg = xref = nullptr;
+    vvv32 = nullptr;
+    vf = nullptr;
+    vf_cap = 0;
     nn = nbr = flag = idx = sidx = cstart = cend = nullptr;
     key = skey = nullptr;
     sort_tmp = nullptr;
@@ -337,7 +434,9 @@ cudaError_t DispState::setup(int ntypes_, const double* prm_, double rcut_, doub
     cudaError_t e;
     if (vvv) cudaFree(vvv);
     if (ggg) cudaFree(ggg);
+    if (vvv32) cudaFree(vvv32);
     vvv = ggg = nullptr;
+    vvv32 = ggg32 = nullptr;
     ntypes = ntypes_;
     rcut = rcut_;
     delr = delr_;
@@ -367,6 +466,16 @@ cudaError_t DispState::setup(int ntypes_, const double* prm_, double rcut_, doub
     if ((e = cudaMalloc(&ggg, hg.size() * sizeof(double)))) return e;
     if ((e = cudaMemcpy(vvv, hv.data(), hv.size() * sizeof(double), cudaMemcpyHostToDevice))) return e;
     if ((e = cudaMemcpy(ggg, hg.data(), hg.size() * sizeof(double), cudaMemcpyHostToDevice))) return e;
+    {   // the FP32 copies of the mixed form (vvv32 then ggg32 in one allocation)
+        std::vector<float> h32(2 * hv.size());
+        for (size_t q = 0; q < hv.size(); ++q) {
+            h32[q] = (float)hv[q];
+            h32[hv.size() + q] = (float)hg[q];
+        }
+        if ((e = cudaMalloc(&vvv32, h32.size() * sizeof(float)))) return e;
+        ggg32 = vvv32 + hv.size();
+        if ((e = cudaMemcpy(vvv32, h32.data(), h32.size() * sizeof(float), cudaMemcpyHostToDevice))) return e;
+    }
     // a copy from pageable memory may return before its DMA lands; the tables are read by
     // kernels on non-blocking streams, so wait for the copies here
     if ((e = cudaStreamSynchronize(cudaStreamLegacy))) return e;
@@ -380,7 +489,7 @@ cudaError_t DispState::setup(int ntypes_, const double* prm_, double rcut_, doub
 cudaError_t DispState::forces(const Cell& cl, int natms, const int* ltype, const int* mol, const double* x,
                               const double* y, const double* z, double* fx, double* fy, double* fz,
                               const double* vx, const double* vy, const double* vz, double* ae, double* out14,
-                              int* flag_host, cudaStream_t s, bool* rebuilt) {
+                              int* flag_host, cudaStream_t s, bool* rebuilt, bool fp32) {
     cudaError_t e;
     *rebuilt = false;
     if (!vvv) return cudaErrorInvalidValue;
@@ -502,7 +611,24 @@ cudaError_t DispState::forces(const Cell& cl, int natms, const int* ltype, const
         natms_cap = keep;
         cap_alloc = cap;
     }
-    k_disp_forces<<<grid(32L * natms), kThreads, 0, s>>>(a, nn, nbr, cap);
+    if (fp32) {
+        const float4* vfp = nullptr;
+        if (vx) {
+            if (vf_cap < natms) {
+                if (vf) cudaFree(vf);
+                vf = nullptr;
+                vf_cap = 0;
+                if ((e = cudaMalloc(&vf, (size_t)natms * sizeof(float4)))) return e;
+                vf_cap = natms;
+            }
+            k_disp_vf<<<grid(natms), kThreads, 0, s>>>(natms, vx, vy, vz, vf);
+            vfp = vf;
+            ++launches;
+        }
+        k_disp_forces32<<<grid(32L * natms), kThreads, 0, s>>>(a, nn, nbr, cap, vvv32, ggg32, vfp, (float)a.rdr);
+    } else {
+        k_disp_forces<<<grid(32L * natms), kThreads, 0, s>>>(a, nn, nbr, cap);
+    }
     ++launches;
     return cudaGetLastError();
 }

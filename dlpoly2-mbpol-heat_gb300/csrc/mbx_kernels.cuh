@@ -158,6 +158,9 @@ struct DispState {
     double rcut = 0.0, delr = 0.0;
     std::vector<double> prm;
     double *vvv = nullptr, *ggg = nullptr;       // tables [pair][mxgrid]
+    float *vvv32 = nullptr, *ggg32 = nullptr;    // their FP32 copies (one allocation at vvv32)
+    float4* vf = nullptr;                        // FP32 velocities of the mixed form
+    int vf_cap = 0;
     unsigned vdw_types = 0;
     unsigned long long vdw_pairs[3] = {0, 0, 0};
     int cap = 512, cap_alloc = 0;                // list partners j > i per atom
@@ -180,7 +183,7 @@ struct DispState {
     cudaError_t forces(const Cell& cl, int natms, const int* ltype, const int* mol, const double* x,
                        const double* y, const double* z, double* fx, double* fy, double* fz, const double* vx,
                        const double* vy, const double* vz, double* ae, double* out14, int* flag_host,
-                       cudaStream_t s, bool* rebuilt);
+                       cudaStream_t s, bool* rebuilt, bool fp32 = false);   // fp32: the mixed form
 };
 // TTM4-F polarizable electrostatics of MB-pol water (mbx_polar.cu): the reference's polar
 // Ewald branch (rfield, ewald1p, iter, coulomb_polar, ewald2p, ewald3p, qdforce) with its

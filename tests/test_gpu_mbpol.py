@@ -293,19 +293,24 @@ def test_water_forces_one_call_matches_the_separate_calls(precision):
     finally:
         ctx.close()
     tol = 1e-11
+    # the mixed whole evaluation takes the dispersion's mixed form (FP32 pair terms, FP64
+    # sums): against the FP64 entry point its forces and per-atom energies within 2e-7 of
+    # their largest entries, its energy and heat terms within 1e-6
+    tol_a = tol if precision == capi.FP64 else 2e-7
+    tol_s = tol if precision == capi.FP64 else 1e-6
     ref_f = pes["forces"] + disp["forces"] + mb["forces"]
-    assert rel_err(one["forces"], ref_f) <= tol
+    assert rel_err(one["forces"], ref_f) <= tol_a
     ref_ae = pes["atomic_energy"] + disp["atomic_energy"] + mb["atomic_energy"]
-    assert rel_err(one["atomic_energy"], ref_ae) <= tol
+    assert rel_err(one["atomic_energy"], ref_ae) <= tol_a
     sc = one["scalars"]
     assert abs(sc[capi.S_ENG3] - mb["eng3"]) <= tol * abs(mb["eng3"])
     assert abs(sc[capi.NSCALARS] - pes["engang"]) <= tol * abs(pes["engang"])
-    assert abs(sc[capi.NSCALARS + 14] - disp["eng"]) <= tol * abs(disp["eng"])
-    assert rel_err(sc[capi.NSCALARS + 25:capi.NSCALARS + 28], disp["jpot"]) <= tol
+    assert abs(sc[capi.NSCALARS + 14] - disp["eng"]) <= tol_s * abs(disp["eng"])
+    assert rel_err(sc[capi.NSCALARS + 25:capi.NSCALARS + 28], disp["jpot"]) <= tol_s
     nw3 = 3 * box.nw
     m, v = box.mass[:nw3], box.vel[:nw3]
     eng = 0.5 * m * (v * v).sum(1) + ref_ae[:nw3]
-    assert rel_err(sc[capi.S_JKIN:capi.S_JKIN + 3], (eng[:, None] * v).sum(0)) <= tol
+    assert rel_err(sc[capi.S_JKIN:capi.S_JKIN + 3], (eng[:, None] * v).sum(0)) <= tol_a
 
 
 def _offdiag(nsite):
