@@ -280,8 +280,8 @@ __global__ void k_pol_bounds(int n, const unsigned* __restrict__ skey, int* __re
 // site of another water within rcut), one directed row per site, warp per site.
 // Candidates: the sites of the 27 cells around the site's cell (orthorhombic boxes with
 // at least 3 cells of width >= rcut + 0.02 A per side), else every site.  An FP32
-// prefilter with a 0.01 A margin, then the reference's FP64 test.
-// A pair whose FP32 distance is inside rcut - 0.01 A (r2in) is inside rcut in FP64 too (the
+// prefilter with a 0.001 A margin, then the reference's FP64 test.
+// A pair whose FP32 distance is inside rcut - 0.001 A (r2in) is inside rcut in FP64 too (the
 // FP32 error of r^2 is below 1e-3 A^2 for coordinates under 1e3 A), so only the thin shell
 // between r2in and r2f takes the reference's FP64 test.
 // Row order: the polarizable partners first (npol of them), then the others; within each
@@ -3222,8 +3222,11 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
     // than skin / 2) and the exact list is filtered from them each call.
     const double skin = list_skin > 0.0 ? list_skin : 0.0;
     last_n = n;
-    const float r2f = (float)((rcut + 0.01) * (rcut + 0.01));
-    const float r2in = rcut > 0.02 ? (float)((rcut - 0.01) * (rcut - 0.01)) : 0.f;
+    // the shell of the FP64 test: +-0.001 A about rcut, 0.018 A^2 in r^2 at 9 A, 18 times the
+    // FP32 error bound of r^2 below (a warp holding one shell entry runs its FP64 test: a
+    // thinner shell is fewer such warps)
+    const float r2f = (float)((rcut + 0.001) * (rcut + 0.001));
+    const float r2in = rcut > 0.002 ? (float)((rcut - 0.001) * (rcut - 0.001)) : 0.f;
     auto build = [&](int* lnn, int* lnbr, int* lnpol, int2* lnup, int rowcap, double lcut) -> cudaError_t {
         // one pass of k_pol_list at cut lcut into (lnn, lnbr); the overflow flag is read by the caller
         cudaError_t err;
