@@ -1475,7 +1475,8 @@ __device__ void pcg_next_body(double* acc, int* st, double target, bool keep_bet
 // With `st` (the diagonal preconditioner), the last block to finish also runs the sweep's
 // stopping test (pcg_next_body, as k_pcg_next) on the complete sums; `ticket` counts the
 // finished blocks and is left at 0.
-__global__ void __launch_bounds__(kThreads) k_pcg_step(PolArgs a, MixArgs m, int* st, double target, int* ticket) {
+__global__ void __launch_bounds__(kThreads) k_pcg_step(PolArgs a, MixArgs m, int* st, double target, int* ticket,
+                                                       int skip_rz) {
     if (m.stop && *m.stop) return;   // the CG solve has stopped (uniform per launch)
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     double v[3] = {0, 0, 0};
@@ -1490,7 +1491,7 @@ __global__ void __launch_bounds__(kThreads) k_pcg_step(PolArgs a, MixArgs m, int
         m.x[i] = x;
         m.rho[i] = r;
         const double z[3] = {(double)w * r.x, (double)w * r.y, (double)w * r.z};
-        v[0] = z[0] * r.x + z[1] * r.y + z[2] * r.z;
+        v[0] = skip_rz ? 0.0 : z[0] * r.x + z[1] * r.y + z[2] * r.z;   // the block kernel's rho.z instead
         v[1] = z[0] * z[0] + z[1] * z[1] + z[2] * z[2];
         v[2] = 1.0;
     }
@@ -1528,6 +1529,8 @@ __global__ void __launch_bounds__(kThreads) k_pcg_dir(PolArgs a, MixArgs m, cons
     }
     m.d32[i] = make_float4(zz.x + b * d.x, zz.y + b * d.y, zz.z + b * d.z, 0.f);
 }
+
+__device__ void pcg_next_body(double* acc, int* st, double target, bool keep_beta);
 
 // Block-Jacobi preconditioner: per water, the inverse of the 9x9 block of the CG matrix
 // A = r4pie0/polr2 - dum - T over its three sites (the diagonal, the self term and the
@@ -1620,28 +1623,45 @@ __global__ void k_pcg_block_setup(PolArgs a, float dum, float* __restrict__ binv
 
 // z = M^-1 rho with the block inverses: a thread per site, the three rows of its water's
 // inverse times the water's residual; the sites of no water (M sites) 0.
+// With `slot` >= 0 also rho.z into acc[slot], and with `st` the sweep's stopping test in the
+// last block to finish (as k_pcg_step's; `ticket` counts the finished blocks).
 __global__ void __launch_bounds__(kThreads) k_pcg_block(PolArgs a, MixArgs m, const float* __restrict__ binv,
-                                                        float4* __restrict__ z) {
+                                                        float4* __restrict__ z, int slot, int* st, double target,
+                                                        int* ticket) {
     if (m.stop && *m.stop) return;   // the CG solve has stopped (uniform per launch)
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= a.n) return;
-    if (i >= 3 * a.nw) {
-        z[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-        return;
-    }
-    const int w = i / 3, s = i % 3;
-    const float4 r0 = m.rho[3 * w], r1 = m.rho[3 * w + 1], r2 = m.rho[3 * w + 2];
-    const float rv[9] = {r0.x, r0.y, r0.z, r1.x, r1.y, r1.z, r2.x, r2.y, r2.z};
-    const float* B = binv + 81 * (size_t)w + 27 * s;
-    float o[3];
+    double v[1] = {0.0};
+    if (i < a.n) {
+        float o[3] = {0.f, 0.f, 0.f};
+        if (i < 3 * a.nw) {
+            const int w = i / 3, s = i % 3;
+            const float4 r0 = m.rho[3 * w], r1 = m.rho[3 * w + 1], r2 = m.rho[3 * w + 2];
+            const float rv[9] = {r0.x, r0.y, r0.z, r1.x, r1.y, r1.z, r2.x, r2.y, r2.z};
+            const float* B = binv + 81 * (size_t)w + 27 * s;
 #pragma unroll
-    for (int c = 0; c < 3; ++c) {
-        float u = 0.f;
+            for (int c = 0; c < 3; ++c) {
+                float u = 0.f;
 #pragma unroll
-        for (int q = 0; q < 9; ++q) u += B[9 * c + q] * rv[q];
-        o[c] = u;
+                for (int q = 0; q < 9; ++q) u += B[9 * c + q] * rv[q];
+                o[c] = u;
+            }
+            const float* ri = rv + 3 * s;
+            v[0] = (double)ri[0] * o[0] + (double)ri[1] * o[1] + (double)ri[2] * o[2];
+        }
+        z[i] = make_float4(o[0], o[1], o[2], 0.f);
     }
-    z[i] = make_float4(o[0], o[1], o[2], 0.f);
+    if (slot < 0) return;
+    block_sum_atomic<1>(v, a.acc + slot);
+    if (!st) return;
+    __shared__ int last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = atomicAdd(ticket, 1) == (int)gridDim.x - 1;
+    __syncthreads();
+    if (!last || threadIdx.x != 0) return;
+    __threadfence();
+    *ticket = 0;
+    pcg_next_body(a.acc, st, target, true);
 }
 
 // Polynomial preconditioner: p Jacobi sweeps on the real-space part of the system,
@@ -3484,7 +3504,7 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
         }
         auto precondition = [&](int slot, int dir) -> cudaError_t {
             if (blk) {
-                k_pcg_block<<<blocks(n, kThreads), kThreads, 0, s>>>(a, m, binv, cg_z);
+                k_pcg_block<<<blocks(n, kThreads), kThreads, 0, s>>>(a, m, binv, cg_z, -1, nullptr, 0.0, nullptr);
                 ++launches;
             } else {
                 k_pcg_jacobi<<<blocks(n, kThreads), kThreads, 0, s>>>(a, m, nullptr, cg_z);
@@ -3596,13 +3616,12 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
                         k_pcg_ad<<<blocks(n, kThreads), kThreads, 0, s>>>(a, ms, (K || spme_on) ? 1 : 0);
                         // the diagonal preconditioner: the stopping test in k_pcg_step's last block
                         k_pcg_step<<<blocks(n, kThreads), kThreads, 0, s>>>(a, ms, poly ? nullptr : cgs, target,
-                                                                            cgs + 2);
+                                                                            cgs + 2, blk ? 1 : 0);
                         if (poly && blk) {
-                            k_pcg_block<<<blocks(n, kThreads), kThreads, 0, s>>>(a, ms, binv, cg_z);
-                            // rho.z of the block z replaces k_pcg_step's diagonal one
-                            if ((e = cudaMemsetAsync(acc + 35, 0, sizeof(double), s))) return e;
-                            k_pcg_rz<<<blocks(n, kThreads), kThreads, 0, s>>>(a, ms, cg_z, 35, 0);
-                            launches += 2;
+                            // z, rho.z (in place of k_pcg_step's diagonal one) and the stopping test
+                            k_pcg_block<<<blocks(n, kThreads), kThreads, 0, s>>>(a, ms, binv, cg_z, 35, cgs, target,
+                                                                                 cgs + 2);
+                            ++launches;
                         } else if (poly) {
                             k_pcg_jacobi<<<blocks(n, kThreads), kThreads, 0, s>>>(a, ms, nullptr, cg_z);
                             for (int qq = 1; qq < pre; ++qq) {
@@ -3617,8 +3636,10 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
                             k_pcg_rz<<<blocks(n, kThreads), kThreads, 0, s>>>(a, ms, cg_z, 35, 0);
                             launches += 2;
                         }
-                        k_pcg_dir<<<blocks(n, kThreads), kThreads, 0, s>>>(a, ms, poly ? cg_z : nullptr, poly ? 0 : 1);
-                        if (poly) {
+                        // fused stopping test (diagonal: in k_pcg_step; block: in k_pcg_block)
+                        const bool fused = !poly || blk;
+                        k_pcg_dir<<<blocks(n, kThreads), kThreads, 0, s>>>(a, ms, poly ? cg_z : nullptr, fused ? 1 : 0);
+                        if (!fused) {
                             k_pcg_next<<<1, 32, 0, s>>>(acc, cgs, target);
                             ++launches;
                         }
