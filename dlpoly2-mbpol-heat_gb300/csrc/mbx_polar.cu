@@ -1730,12 +1730,19 @@ __global__ void k_pcg_next(double* __restrict__ acc, int* __restrict__ st, doubl
     pcg_next_body(acc, st, target, false);
 }
 
-// SPME: efm += the FP32 k-space field of the correction (its self term included), the
-// k-space field being linear in the dipoles.
-__global__ void k_pol_efm_add(PolArgs a, const float* __restrict__ e32k) {
+// The evaluation after a correction: the fields are linear in the dipoles, so each is the
+// previous FP64 one plus the FP32 field of the correction (e32: real space in the first 3
+// blocks, SPME k space with its self term in the next 3): emu += real (with `real`), efm +=
+// k space (with `kspace`).  The correction is at the size of the residual, ~1e-4 of the
+// dipoles in an MD step, so the FP32 rounding enters ~1e-11 of the fields.
+__global__ void k_pol_field_add(PolArgs a, const float* __restrict__ e32, int real, int kspace) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
-    for (int c = 0; c < 3; ++c) a.efm[c * (size_t)a.n + i] += (double)e32k[c * (size_t)a.n + i];
+    const size_t n = a.n;
+    for (int c = 0; c < 3; ++c) {
+        if (real) a.emu[c * n + i] += (double)e32[c * n + i];
+        if (kspace) a.efm[c * n + i] += (double)e32[(3 + c) * n + i];
+    }
 }
 
 // mu += d in FP64; refreshes the masked dipoles.
@@ -3525,16 +3532,18 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
         // the field evaluation after a correction: FP64 real space; k space the previous
         // FP64 fields plus the FP32 ones of the correction
         auto fields_delta = [&]() {
-            if (spme_on) {   // FP64 real space; k space the previous FP64 field + the FP32 SPME field of the correction
-                k_pol_dd<<<blocks(32L * n, kThreads), kThreads, 0, s>>>(a);
+            // real space: the previous FP64 field + the FP32 field of the correction
+            k_pol_dd32<<<blocks(32L * n, kThreads), kThreads, 0, s>>>(a, d32, e32);
+            if (spme_on) {   // k space likewise: the FP32 SPME field of the correction
                 const cudaError_t fe =
                     spme.field32(n, x, y, z, d32, polr2, k.sfac, dum_self, e32 + 3 * (size_t)n, s, nullptr);
                 if (fe && !field_err) field_err = fe;
-                k_pol_efm_add<<<blocks(n, kThreads), kThreads, 0, s>>>(a, e32 + 3 * (size_t)n);
+                k_pol_field_add<<<blocks(n, kThreads), kThreads, 0, s>>>(a, e32, 1, 1);
                 launches += 2 + spme.launches;
                 return;
             }
-            k_pol_dd<<<blocks(32L * n, kThreads), kThreads, 0, s>>>(a);
+            k_pol_field_add<<<blocks(n, kThreads), kThreads, 0, s>>>(a, e32, 1, 0);
+            launches += 2;
             if (K) {
                 k_pol_sfx32<0><<<dim3(nkt, nsc_used), kSfThreads, sfx_smem0, s>>>(k, d32, vh32, schunk, rowp, kpart);
                 k_pol_sfd_dfin<<<blocks(K, kThreads), kThreads, 0, s>>>(k, nsc_used, kpart);
