@@ -2089,7 +2089,6 @@ __global__ void __launch_bounds__(kThreads) k_pol_ewald2p32(PolArgs a, double g3
     if (i < a.n) {
         SmearQueue& q = sq[threadIdx.x >> 5];
         int qn = 0;   // queued pairs (warp-uniform)
-        const int nn = a.nn[i];
         const size_t row = (size_t)i * a.cap;
         const float r4 = (float)kR4pie0;
         const double qid = a.q[i];
