@@ -441,6 +441,14 @@ def run_ours(args, rank, world):
         ovl_ms[key_] = 1e3 * t_ / 4
     best_ovl = min(ovl_ms, key=ovl_ms.get)
     ctx.set_overlap(best_ovl != "off", 0 if best_ovl == "off" else int(best_ovl[-1]))
+    # the 1-body and dispersion terms beside the electrostatics (mbx_set_overlap_terms) or after
+    side_ms = {}
+    for on_ in (False, True):
+        ctx.set_overlap_terms(on_)
+        t_, _, _, _ = timed(capi.MIXED, 4, 2)
+        side_ms["on" if on_ else "off"] = 1e3 * t_ / 4
+    best_side = min(side_ms, key=side_ms.get)
+    ctx.set_overlap_terms(best_side == "on")
 
     clocks = ClockSampler(dev.index)
     clocks.start()
@@ -636,6 +644,11 @@ def run_ours(args, rank, world):
                                    "iterates to the same toler either way; each timed on 4 MD steps after 5 "
                                    "warm-up steps (CUDA events), the fastest used for every measurement of "
                                    "the run"},
+        "overlap_terms_tuning": {"mixed_step_ms": side_ms, "chosen": best_side,
+                                 "method": "the 1-body and dispersion terms after the electrostatics (off) or on "
+                                           "a third stream beside its setup and solve (on), each timed on 4 "
+                                           "warm-started MD steps (CUDA events), the faster used for every "
+                                           "measurement of the run"},
         "precond_tuning": {"mixed_step_ms_by_jacobi_sweeps": {str(k): v for k, v in pre_ms.items()},
                            "chosen_sweeps": best_pre,
                            "method": "the diagonal (1), 3 or 5 Jacobi sweeps, or the per-water 9x9 block "

@@ -49,6 +49,13 @@ struct mbx_context {
     int overlap_split = 0;          // dimer warps of the 8-warp block (0: 4)
     cudaStream_t side = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    // the whole step: the 1-body and dispersion terms on a third stream beside the
+    // electrostatics' setup and solve (mbx_set_overlap_terms), their scalars in side_acc
+    int overlap_terms = 0;
+    cudaStream_t side2 = nullptr;
+    cudaEvent_t ev_fork2 = nullptr, ev_join2 = nullptr;
+    double* side_acc = nullptr;     // device [28]: 1-body 14, dispersion 14
+    double* side_acc_h = nullptr;   // pinned copy
     int nsm = 0;                    // SMs of the device (the persistent grid)
     int* fuse_ctr = nullptr;        // device [2]: work counters of the persistent kernel
     double* part2 = nullptr;        // split FP64 dimers: per-chunk partial sums (pairs_cap dimers)
@@ -543,6 +550,14 @@ extern "C" void mbx_destroy(mbx_context* ctx) {
         cudaStreamSynchronize(ctx->side);
         cudaStreamDestroy(ctx->side);
     }
+    if (ctx->side2) {
+        cudaStreamSynchronize(ctx->side2);
+        cudaStreamDestroy(ctx->side2);
+    }
+    if (ctx->ev_fork2) cudaEventDestroy(ctx->ev_fork2);
+    if (ctx->ev_join2) cudaEventDestroy(ctx->ev_join2);
+    if (ctx->side_acc) cudaFree(ctx->side_acc);
+    if (ctx->side_acc_h) cudaFreeHost(ctx->side_acc_h);
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
     delete ctx;
 }
@@ -1098,6 +1113,40 @@ int water_step_core(mbx_context* ctx, int precision, int imcon, const double* ce
     const bool overlap = ctx->overlap && precision == MBX_MIXED && nw >= 2 && ctx->fused &&
                          fused_applies(precision, mpq);
     int mb_rc = MBX_OK;
+    // the 1-body and dispersion terms (positions only) on the third stream, beside the
+    // electrostatics' setup and solve; the final pass, whose kernels add to the same force
+    // arrays, waits for them (join_hook)
+    const bool side_terms = ctx->overlap_terms && nw > 0;
+    const bool disp = d_typ && d_mol;
+    if (side_terms) {
+        if (disp && !ctx->disp.vvv) return fail(ctx, MBX_ERR_ARG, "mbx_disp_setup has not been called");
+        if (!ctx->side2) CK(cudaStreamCreateWithFlags(&ctx->side2, cudaStreamNonBlocking));
+        if (!ctx->ev_fork2) CK(cudaEventCreateWithFlags(&ctx->ev_fork2, cudaEventDisableTiming));
+        if (!ctx->ev_join2) CK(cudaEventCreateWithFlags(&ctx->ev_join2, cudaEventDisableTiming));
+        if (!ctx->side_acc) CK(cudaMalloc(&ctx->side_acc, 28 * sizeof(double)));
+        if (!ctx->side_acc_h) CK(cudaMallocHost(&ctx->side_acc_h, 28 * sizeof(double)));
+        cudaStream_t s2 = ctx->side2;
+        CK(cudaEventRecord(ctx->ev_fork2, s));   // after the M sites
+        CK(cudaStreamWaitEvent(s2, ctx->ev_fork2, 0));
+        CK(cudaMemsetAsync(ctx->side_acc, 0, 28 * sizeof(double), s2));
+        if (disp) {   // first: its skin test reads a flag back, a short wait here
+            bool rebuilt = false;
+            const cudaError_t e = ctx->disp.forces(cl, natms, d_typ, d_mol, dx, dy, dz, dfx, dfy, dfz,
+                                                   heat ? dvx : nullptr, heat ? dvy : nullptr, heat ? dvz : nullptr,
+                                                   dae, ctx->side_acc + 14, ctx->totals_h, s2, &rebuilt,
+                                                   precision == MBX_MIXED);
+            if (e == cudaErrorInvalidValue) return fail(ctx, MBX_ERR_CAPACITY, "dispersion list capacity exceeded");
+            CK(e);
+        }
+        CK(launch_ps_pes(nw, d_ang, cl, dx, dy, dz, dfx, dfy, dfz, dae, heat ? dvx : nullptr, heat ? dvy : nullptr,
+                         heat ? dvz : nullptr, ctx->side_acc, s2));
+        CK(cudaMemcpyAsync(ctx->side_acc_h, ctx->side_acc, 28 * sizeof(double), cudaMemcpyDeviceToHost, s2));
+        CK(cudaEventRecord(ctx->ev_join2, s2));
+        if (!overlap) {   // the hooks of the solve: nothing to fork, the join before the final pass
+            ctx->polar.fork_hook = []() -> cudaError_t { return cudaSuccess; };
+            ctx->polar.join_hook = [&]() -> cudaError_t { return cudaStreamWaitEvent(s, ctx->ev_join2, 0); };
+        }
+    }
     if (overlap) {
         if (!ctx->side) CK(cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking));
         if (!ctx->ev_fork) CK(cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming));
@@ -1113,13 +1162,19 @@ int water_step_core(mbx_context* ctx, int precision, int imcon, const double* ce
             if (mb_rc) return cudaErrorUnknown;
             return cudaEventRecord(ctx->ev_join, ctx->side);
         };
-        ctx->polar.join_hook = [&]() -> cudaError_t { return cudaStreamWaitEvent(s, ctx->ev_join, 0); };
+        ctx->polar.join_hook = [&]() -> cudaError_t {
+            cudaError_t e;
+            if (side_terms && (e = cudaStreamWaitEvent(s, ctx->ev_join2, 0))) return e;
+            return cudaStreamWaitEvent(s, ctx->ev_join, 0);
+        };
     }
     const cudaError_t pe = ctx->polar.run(precision, cl, prm, nw, dx, dy, dz, dq, ddq, dpr, dpr2, dmx, dmy, dmz, dfx,
                                           dfy, dfz, daep, heat ? dvx : nullptr, heat ? dvy : nullptr,
                                           heat ? dvz : nullptr, sp, jp, jk, s);
     ctx->polar.fork_hook = nullptr;
     ctx->polar.join_hook = nullptr;
+    // the side terms are done before anything else touches the force arrays, on error too
+    if (side_terms) CK(cudaStreamSynchronize(ctx->side2));
     if (mb_rc) return mb_rc;
     if (pe != cudaSuccess) return polar_failed(ctx, pe);
     if (overlap) {   // the MB-pol scalars (the side stream has finished with the join)
@@ -1135,15 +1190,22 @@ int water_step_core(mbx_context* ctx, int precision, int imcon, const double* ce
         sp[19 + c] = jk[c];
     }
     const long polar_launches = ctx->polar.launches + 1;
-    int rc = mbx_ps_pes_forces_device(ctx, imcon, cell, nw, d_ang, natms, dx, dy, dz, dfx, dfy, dfz,
+    int rc = MBX_OK;
+    if (side_terms) {   // their scalars (the final pass has waited for the stream)
+        CK(cudaEventSynchronize(ctx->ev_join2));
+        std::memcpy(sc + MBX_NSCALARS, ctx->side_acc_h, 14 * sizeof(double));
+        if (disp) std::memcpy(sc + MBX_NSCALARS + 14, ctx->side_acc_h + 14, 14 * sizeof(double));
+    } else {
+        rc = mbx_ps_pes_forces_device(ctx, imcon, cell, nw, d_ang, natms, dx, dy, dz, dfx, dfy, dfz,
                                       heat ? dvx : nullptr, heat ? dvy : nullptr, heat ? dvz : nullptr, dae,
                                       sc + MBX_NSCALARS);
-    if (rc) return rc;
-    if (d_typ && d_mol) {
-        rc = disp_forces_dev(ctx, imcon, cell, natms, d_typ, d_mol, dx, dy, dz, dfx, dfy, dfz,
-                             heat ? dvx : nullptr, heat ? dvy : nullptr, heat ? dvz : nullptr, dae,
-                             sc + MBX_NSCALARS + 14, precision == MBX_MIXED);
         if (rc) return rc;
+        if (disp) {
+            rc = disp_forces_dev(ctx, imcon, cell, natms, d_typ, d_mol, dx, dy, dz, dfx, dfy, dfz,
+                                 heat ? dvx : nullptr, heat ? dvy : nullptr, heat ? dvz : nullptr, dae,
+                                 sc + MBX_NSCALARS + 14, precision == MBX_MIXED);
+            if (rc) return rc;
+        }
     }
     if (!overlap) {
         rc = run_mbpol(ctx, precision, cl, nw, d_lst, natms, dx, dy, dz, dfx, dfy, dfz, heat ? dvx : nullptr,
@@ -1776,6 +1838,12 @@ extern "C" int mbx_set_overlap(mbx_context* ctx, int on, int dimer_warps) {
     if (!ctx || dimer_warps < 0 || dimer_warps > 7) return MBX_ERR_ARG;
     ctx->overlap = on ? 1 : 0;
     ctx->overlap_split = dimer_warps;
+    return MBX_OK;
+}
+
+extern "C" int mbx_set_overlap_terms(mbx_context* ctx, int on) {
+    if (!ctx) return MBX_ERR_ARG;
+    ctx->overlap_terms = on ? 1 : 0;
     return MBX_OK;
 }
 

@@ -176,6 +176,7 @@ def load(path=None):
     L.mbx_set_fused.argtypes = [C.c_void_p, C.c_int]
     L.mbx_set_fused_split.argtypes = [C.c_void_p, C.c_int]
     L.mbx_set_overlap.argtypes = [C.c_void_p, C.c_int, C.c_int]
+    L.mbx_set_overlap_terms.argtypes = [C.c_void_p, C.c_int]
     L.mbx_graph_launches.argtypes = [C.c_void_p]
     L.mbx_graph_launches.restype = C.c_long
     L.mbx_last_lists.argtypes = [C.c_void_p, _I, C.c_long, _L, _I, C.c_long, _L]
@@ -595,6 +596,10 @@ class Context:
 
     def set_fused(self, on=True):
         self._check(self.lib.mbx_set_fused(self.h, 1 if on else 0), "mbx_set_fused")
+
+    def set_overlap_terms(self, on):
+        """1-body and dispersion terms on a third stream beside the electrostatics (on/off)."""
+        self._check(self.lib.mbx_set_overlap_terms(self.h, int(bool(on))), "mbx_set_overlap_terms")
 
     def set_overlap(self, on=True, dimer_warps=0):
         """The MB-pol terms beside the electrostatics' dipole solve in mbx_water_step (mixed)."""

@@ -88,6 +88,13 @@ int mbx_set_fused_split(mbx_context* ctx, int dimer_warps);
  * FP64 atomic additions.  Default off. */
 int mbx_set_overlap(mbx_context* ctx, int on, int dimer_warps);
 
+/* mbx_water_step / mbx_water_step_device: run the 1-body and dispersion terms (positions
+ * only) on a third stream of the context beside the electrostatics' setup and solve (on = 1);
+ * the electrostatics' final pass, whose kernels add to the same force arrays, starts after
+ * them.  Results equal the sequential form's up to the order of FP64 atomic additions.
+ * Default off. */
+int mbx_set_overlap_terms(mbx_context* ctx, int on);
+
 /*
  * MB-pol 2B + 3B forces with the heat-current bookkeeping.
  * Replaces mbpol_forces (SOURCE/mbpol.f90:98-449, called from SOURCE/dlpoly_cmd.f:2504)

@@ -191,3 +191,32 @@ def test_overlapped_step_matches_sequential(spme):
         assert got["status"] == 0
         for key in ("forces", "atomic_energy", "dipoles", "scalars"):
             assert _rel(got[key], seq[key]) <= 2e-7, (key, _rel(got[key], seq[key]))
+
+
+@pytest.mark.parametrize("precision", [capi.FP64, capi.MIXED])
+def test_overlapped_terms_match_sequential(precision):
+    """mbx_set_overlap_terms: the 1-body and dispersion terms on a third stream beside the
+    electrostatics (and with the MB-pol overlap as well) give the sequential step's results
+    up to the order of FP64 atomic additions (FP64: 1e-11; mixed: 2e-7, the bound of the
+    MB-pol overlap, for a CG stopping decision moved by that order); a lost or doubled
+    force update would show at 1e-3 and above."""
+    box = systems.box_for(512, seed=11)
+    prm = systems.polar_params(alpha=0.35, rcut=9.0, kmax=(12, 12, 12), toler_debye=1e-8)
+    lt, mol = systems.water_types(box)
+    ctx = capi.Context(0)
+    try:
+        ctx.set_spme(6, spacing=0.78)
+        ctx.disp_setup(systems.DISP_PARAMS_SYNTHETIC, rcut=9.0, delr=1.0)
+        seq = ctx.water_step(box, prm, precision=precision, disp=(lt, mol))
+        ctx.set_overlap_terms(True)
+        got = [ctx.water_step(box, prm, precision=precision, disp=(lt, mol))]
+        if precision == capi.MIXED:
+            ctx.set_overlap(True)
+            got.append(ctx.water_step(box, prm, precision=precision, disp=(lt, mol)))
+    finally:
+        ctx.close()
+    tol = 1e-11 if precision == capi.FP64 else 2e-7
+    for g in got:
+        assert g["status"] == 0
+        for key in ("forces", "atomic_energy", "dipoles", "scalars"):
+            assert _rel(g[key], seq[key]) <= tol, (key, _rel(g[key], seq[key]))
