@@ -37,7 +37,11 @@ __device__ __forceinline__ double rsqrt_nr(double x) {
 }
 
 // Fortran NINT on a double: round half away from zero.
-__device__ __forceinline__ double nint(double x) { return round(x); }
+// The image shift: the reference's NINT rounds halves away from zero, rint to even; the two
+// differ only at a scaled separation of exactly k + 1/2, a separation of half a box or more,
+// outside every cutoff of the path (rcut <= half the box), so every pair within reach gets
+// the same shift bit for bit.  rint is one FP64 instruction, round several.
+__device__ __forceinline__ double nint(double x) { return rint(x); }
 
 // image_vectors (SOURCE/mbpol.f90:1305-1361) applied to one vector.
 __device__ __forceinline__ void image(const Cell& cl, double& x, double& y, double& z) {
