@@ -757,9 +757,13 @@ constexpr int kFusedThreads = 384;
 // SM's 64K registers, so the electrostatics' FP32 CG kernels fit beside it on every SM.
 constexpr int kFusedThreadsShared = 256;
 constexpr int kFusedDimerWarps = 4;   // the default split (dimer_warps 0)
+// Registers per thread of both blocks, the budget the polynomial functions are compiled to.
+// It is set with __maxnreg__ (launch bounds of 256 threads, one block, would let the kernel
+// body take 255 registers and the whole register file).
+constexpr int kFusedMaxRegs = 168;
 
 template <typename T2, typename T3, int NT>
-__global__ void __launch_bounds__(NT, 1)
+__global__ void __maxnreg__(kFusedMaxRegs)
     k_mbpol_23(MbpolArgs a, const int2* __restrict__ pairs, int n2, const int* __restrict__ n2_dev,
                const int4* __restrict__ trip, int n3, const int* __restrict__ n3_dev, int* ctr,
                double* partial, int* done, long part_cap, int dimer_warps) {
