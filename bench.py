@@ -956,14 +956,18 @@ def batched_whole(steps=4, warmup=2):
         ctx.set_lanes(lanes)
         res["lanes"] = lanes
         res["lanes_tuning_ms_by_lanes"] = {str(k): v_ for k, v_ in lane_ms.items()}
-        for prec, key in ((capi.MIXED, "mixed"), (capi.FP64, "fp64")):
+        # mixed, FP64, and mixed with the electrostatics' final pass in FP64 (mbx_set_final_fp64)
+        for prec, key in ((capi.MIXED, "mixed"), (capi.FP64, "fp64"), (capi.MIXED, "mixed_final_fp64")):
+            ctx.set_final_fp64(key == "mixed_final_fp64")
             t, first = run(prec, steps, warmup)
             res[key] = {"steps_per_s": 1.0 / t, "ms_per_step": 1e3 * t, "boxes_per_s": nb / t,
                         "waters_per_s": float(nws.sum()) / t}
             res[key + "_first_state"] = first
+        ctx.set_final_fp64(False)
         # mixed against FP64 per box on the same configuration (dipoles from zero)
         fm, scm = res.pop("mixed_first_state")
         fd, scd = res.pop("fp64_first_state")
+        ff, scf = res.pop("mixed_final_fp64_first_state")
         nws_ = capi.NWATERSCALARS
 
         def jt(v_):
@@ -981,6 +985,11 @@ def batched_whole(steps=4, warmup=2):
                                               "heat_current_rel_median": float(np.median(herr)),
                                               "force_rms_rel_worst": max(ferr),
                                               "state": "the same configuration, dipoles from zero"}
+        herr = [float(np.linalg.norm(jt(scf[b_]) - jt(scd[b_])) / np.linalg.norm(jt(scd[b_])))
+                for b_ in range(nb)]
+        res["mixed_final_fp64"]["error_vs_fp64_per_box"] = {
+            "heat_current_rel_worst": max(herr), "heat_current_rel_median": float(np.median(herr)),
+            "boxes_over_1e-6": int(sum(h > 1e-6 for h in herr))}
         if name.startswith("beads"):
             # the same whole evaluations one box per call on one context (mixed)
             x, y, z = (np.ascontiguousarray(xyz0[:, k]).copy() for k in range(3))

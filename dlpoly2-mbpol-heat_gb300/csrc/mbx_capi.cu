@@ -1720,6 +1720,7 @@ extern "C" int mbx_water_step_multi(mbx_context* ctx, int precision, int nbox, c
         c->limit3 = ctx->limit3;
         c->fused = ctx->fused;
         c->polar.precond_sweeps = ctx->polar.precond_sweeps;
+        c->polar.final_fp64 = ctx->polar.final_fp64;
         c->polar.list_skin = ctx->polar.list_skin;
         c->polar.spme_order = ctx->polar.spme_order;
         c->polar.spme_spacing = ctx->polar.spme_spacing;
@@ -1844,6 +1845,12 @@ extern "C" int mbx_set_overlap(mbx_context* ctx, int on, int dimer_warps) {
 extern "C" int mbx_set_overlap_terms(mbx_context* ctx, int on) {
     if (!ctx) return MBX_ERR_ARG;
     ctx->overlap_terms = on ? 1 : 0;
+    return MBX_OK;
+}
+
+extern "C" int mbx_set_final_fp64(mbx_context* ctx, int on) {
+    if (!ctx) return MBX_ERR_ARG;
+    ctx->polar.final_fp64 = on != 0;
     return MBX_OK;
 }
 

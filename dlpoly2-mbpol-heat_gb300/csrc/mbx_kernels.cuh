@@ -197,6 +197,9 @@ struct PolarState {
     double4* ercp = nullptr;               // erfcgenp table, rows 0..mxegrd
     float4* ercp32 = nullptr;              // its screened functions C_n in FP32 (mixed-path ewald2p)
     bool ewald2p_fp64 = false;             // mixed path: keep ewald2p's pair terms in FP64
+    // mixed path: the final pass (forces, energies, virial, heat current of the converged
+    // dipoles) in FP64 as in the FP64 method; the solve stays mixed
+    bool final_fp64 = false;
     // Verlet skin of the site pair list (0: the list is rebuilt at every call): the pairs
     // within rcut + list_skin, kept until a site moved more than list_skin / 2
     double list_skin = 1.0;

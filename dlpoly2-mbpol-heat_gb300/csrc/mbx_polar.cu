@@ -3697,14 +3697,15 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
     }
     if (forked && join_hook && (e = join_hook())) return e;
     const double g34 = std::exp(gammln(3.0 / 4.0));
+    const bool mfin = mixed && !final_fp64;   // the final pass's FP32 forms
     if (heat) {
-        const bool w32 = mixed && !spme_on;   // the FP32 Ewald heat sums take FP32 weights
+        const bool w32 = mfin && !spme_on;   // the FP32 Ewald heat sums take FP32 weights
         k_pol_vhat<<<blocks(n, kThreads), kThreads, 0, s>>>(a, md, w32 ? nullptr : vh, w32 ? vh32 : nullptr);
         ++launches;
     }
     if (profiling && (e = cudaEventRecord(ev[2], s))) return e;
     if (K) {
-        if (mixed) {   // the last FP64 structure factors plus FP32 ones of the last update
+        if (mfin) {   // the last FP64 structure factors plus FP32 ones of the last update
             const dim3 g(nkt, nsc_used);
             if (heat) {
                 k_pol_sfx32<1><<<g, kSfThreads, sfx_smem1, s>>>(k, d32, vh32, schunk, rowp, kpart);
@@ -3721,17 +3722,17 @@ cudaError_t PolarState::run(int precision, const Cell& cl, const double* prm, in
         }
     }
     if (spme_on) {
-        if ((e = spme.final(n, x, y, z, q, md, heat ? vh : nullptr, k.sfac, kpart, acc, nullptr, s, mixed))) return e;
+        if ((e = spme.final(n, x, y, z, q, md, heat ? vh : nullptr, k.sfac, kpart, acc, nullptr, s, mfin))) return e;
         launches += spme.launches;
     }
     if (profiling && (e = cudaEventRecord(ev[3], s))) return e;
     if (K) {
-        if (mixed) k_pol_kforce32<<<dim3(sblk1, nc1), kThreads, gat_smem, s>>>(k, a, kc1, kpart);
+        if (mfin) k_pol_kforce32<<<dim3(sblk1, nc1), kThreads, gat_smem, s>>>(k, a, kc1, kpart);
         else k_pol_kforce<<<dim3(sblk2, nc2), kThreads, 0, s>>>(k, a, kc2, kpart);
         ++launches;
     }
-    k_pol_kforce_sum<<<sblk1, kThreads, 0, s>>>(k, a, spme_on ? 1 : (mixed ? nc1 : nc2), kpart);
-    if (mixed && !ewald2p_fp64)
+    k_pol_kforce_sum<<<sblk1, kThreads, 0, s>>>(k, a, spme_on ? 1 : (mfin ? nc1 : nc2), kpart);
+    if (mfin && !ewald2p_fp64)
         k_pol_ewald2p32<<<blocks(32L * n, kThreads), kThreads, 0, s>>>(a, g34, gammln(0.75), heat);
     else
         k_pol_ewald2p<<<blocks(32L * n, kThreads), kThreads, 0, s>>>(a, g34, heat);

@@ -177,6 +177,7 @@ def load(path=None):
     L.mbx_set_fused_split.argtypes = [C.c_void_p, C.c_int]
     L.mbx_set_overlap.argtypes = [C.c_void_p, C.c_int, C.c_int]
     L.mbx_set_overlap_terms.argtypes = [C.c_void_p, C.c_int]
+    L.mbx_set_final_fp64.argtypes = [C.c_void_p, C.c_int]
     L.mbx_graph_launches.argtypes = [C.c_void_p]
     L.mbx_graph_launches.restype = C.c_long
     L.mbx_last_lists.argtypes = [C.c_void_p, _I, C.c_long, _L, _I, C.c_long, _L]
@@ -600,6 +601,10 @@ class Context:
     def set_overlap_terms(self, on):
         """1-body and dispersion terms on a third stream beside the electrostatics (on/off)."""
         self._check(self.lib.mbx_set_overlap_terms(self.h, int(bool(on))), "mbx_set_overlap_terms")
+
+    def set_final_fp64(self, on):
+        """Mixed method: the electrostatics' final pass in FP64 (on/off); the solve stays mixed."""
+        self._check(self.lib.mbx_set_final_fp64(self.h, int(bool(on))), "mbx_set_final_fp64")
 
     def set_overlap(self, on=True, dimer_warps=0):
         """The MB-pol terms beside the electrostatics' dipole solve in mbx_water_step (mixed)."""

@@ -95,6 +95,13 @@ int mbx_set_overlap(mbx_context* ctx, int on, int dimer_warps);
  * Default off. */
 int mbx_set_overlap_terms(mbx_context* ctx, int on);
 
+/* Mixed method (mbx_polar_forces, mbx_water_step, mbx_water_step_multi): evaluate the
+ * electrostatics' final pass -- forces, energies, virial, stress and heat current of the
+ * converged dipoles -- in FP64 as the FP64 method does (on = 1), instead of its FP32 pair
+ * forces, FP32 k-space heat sums and FP32 SPME heat grids.  The dipole solve stays mixed.
+ * Default off. */
+int mbx_set_final_fp64(mbx_context* ctx, int on);
+
 /*
  * MB-pol 2B + 3B forces with the heat-current bookkeeping.
  * Replaces mbpol_forces (SOURCE/mbpol.f90:98-449, called from SOURCE/dlpoly_cmd.f:2504)

@@ -220,3 +220,44 @@ def test_overlapped_terms_match_sequential(precision):
         assert g["status"] == 0
         for key in ("forces", "atomic_energy", "dipoles", "scalars"):
             assert _rel(g[key], seq[key]) <= tol, (key, _rel(g[key], seq[key]))
+
+
+def _jtotal(v):
+    """The step's total heat current: the MB-pol block's jpot + jkin, the 1-body and
+    dispersion jpot, and the electrostatics' jpot + jkin (include/mbx.h scalar layout)."""
+    ns, nw = capi.NSCALARS, capi.NWATERSCALARS
+    j = v[12:15] + v[15:18] + v[ns + 11:ns + 14] + v[ns + 25:ns + 28]
+    return j + v[nw + 16:nw + 19] + v[nw + 19:nw + 22]
+
+
+@pytest.mark.parametrize("spme", [True, False])
+def test_final_fp64_pass(spme):
+    """mbx_set_final_fp64: the mixed step with its electrostatics' final pass in FP64.  The
+    dipoles converge to the same tolerance as the FP64 method's, so the electrostatics'
+    heat current (jpot + jkin) and forces match the FP64 step's to the dipole tolerance
+    (measured on the 64 uneven boxes: 3e-9 to 1.8e-8 of the total heat current, against
+    up to 1.5e-6 with the FP32 final pass); the total heat current stays within the 1e-6
+    budget (its remaining error is the FP32 3B term's)."""
+    box = systems.box_for(256, seed=5)
+    prm = systems.polar_params(alpha=0.35, rcut=8.0, kmax=(10, 10, 10), toler_debye=1e-8)
+    ctx = capi.Context(0)
+    try:
+        if spme:
+            ctx.set_spme(6, spacing=0.78)
+        ref = ctx.water_step(box, prm, precision=capi.FP64)
+        ctx.set_final_fp64(True)
+        got = ctx.water_step(box, prm, precision=capi.MIXED)
+        ctx.set_final_fp64(False)
+        dflt = ctx.water_step(box, prm, precision=capi.MIXED)
+    finally:
+        ctx.close()
+    nw = capi.NWATERSCALARS
+    jr = _jtotal(ref["scalars"])
+    jel = lambda v: v[nw + 16:nw + 19] + v[nw + 19:nw + 22]
+    assert got["status"] == 0 and dflt["status"] == 0
+    assert np.linalg.norm(jel(got["scalars"]) - jel(ref["scalars"])) <= 1e-7 * np.linalg.norm(jr)
+    assert np.linalg.norm(_jtotal(got["scalars"]) - jr) <= 1e-6 * np.linalg.norm(jr)
+    assert _rel(got["dipoles"], ref["dipoles"]) <= 1e-6
+    # the MB-pol terms are the mixed method's in both mixed calls
+    assert _rel(got["forces"], ref["forces"]) <= 1e-5
+    assert _rel(got["forces"], dflt["forces"]) <= 1e-5
